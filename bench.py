@@ -1,0 +1,376 @@
+"""Benchmark of GOM's per-timestep core on GB300 through the C ABI.
+
+Workload: the baroclinic estuary (about 150k cells: 600 x 250 squares of 100 m plus a 4-row
+triangle strip, 20 z-layers, river 500 m3/s, ocean boundary with M2 0.6 m and S/T series,
+TVD limiter on, wind stress 0.1 Pa, dt = 60 s), generated from a fixed seed.  A step is one
+timestep of the core (main.f90:94-272).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+value          cell-layer-steps/s with the state resident in HBM: per step the host forcing
+               (a few kB) is uploaded and gom_step_all replays the captured timestep graph;
+               timed with CUDA events on the library's stream.
+e2e            the same through the public API end to end: host forcing computed per step,
+               uploaded from pinned memory, and the step's result (status, PCG iterations and
+               the FP64 volume/salt sums) read back every step.
+roofline       the dominant phase timed alone with CUDA events, algorithmic bytes / time against
+               the measured HBM copy bandwidth.
+cpu_baseline   the CPU restatement of the reference (oracle/, serial FP64) on a bounded sample.
+
+N > 1 runs independent replicas (the single-run path does not shard): value is the sum over
+ranks of cell-layer-steps divided by the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "cell-layer-steps/s; batched-ensemble p50/p99 latency vs plain FP64 on same GPU"
+UNIT = "cell-layer-steps/s"
+ORACLE_SO = ROOT / "oracle" / "_build" / "libgomoracle.so"
+
+# algorithmic bytes per active unit and phase (FP64 state read once and written once per phase,
+# integer topology counted once); the unit is stated beside each figure
+PHASE_BYTES_PER_CELL_LAYER = {
+    "advection": 100, "momentum": 208, "velocities": 120, "layers": 64, "node_velocity": 96,
+    "density": 80, "bottom_friction": 2, "boundary_velocity": 0, "swap": 0,
+}
+TRANSPORT_BYTES_PER_CELL_LAYER_SUBCYCLE = 168
+TRANSPORT_BYTES_PER_CELL_LAYER_AVERAGING = 72
+PCG_BYTES_PER_CELL_ITERATION = 120
+FS_ASSEMBLY_BYTES_PER_CELL_LAYER = 64
+
+
+def make_deck(small: bool):
+    from gom_release_gb300.deck import estuary
+    if small:
+        return estuary(nx=120, ny=50, dx=100.0, n_layers=20)
+    return estuary()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int = 0):
+        self.index = index
+        self.samples: list[list[str]] = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 8:
+                self.samples.append(parts)
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.thread.join(timeout=2)
+
+    def summary(self) -> dict:
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[4 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def kernel_launches_per_step(deck) -> int:
+    p = deck.params
+    n = 1                                   # bottom friction
+    n += 1 if deck.n_qb else 0              # river boundary velocity
+    n += (2 if p.elm_backtrace_flag == 1 else 1) if p.advection_flag else 1
+    n += 2                                  # momentum (dry-face clear + columns)
+    n += 4                                  # assembly, PCG, node eta (wet, dry)
+    n += 2                                  # face velocities, cell w
+    n += 4                                  # layers: cells, faces, nodes, check
+    n += 2                                  # face levels, node u/v/w
+    if p.transport_flag:
+        nt = max(1, p.trans_sub_iter)
+        lim = p.h_flux_limiter > 0 or p.v_flux_limiter > 0
+        per = (1 if deck.n_ob + deck.n_qb else 0) + 2 + (2 if lim else 0) + 1
+        n += 1 + nt * per + 2
+    if p.baroclinic_flag == 1:
+        n += 3 if p.ana_density == 0 else 2
+    return n
+
+
+def stream_events(core):
+    import torch
+    stream = torch.cuda.ExternalStream(core.stream_handle())
+    return torch, stream
+
+
+def time_steps(run, forcings, torch, stream) -> float:
+    """K steps (state resident, host forcing precomputed), CUDA events on the library stream."""
+    core = run.core
+    core.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for f in forcings:
+        core.set_forcing(f)
+        core.step_all()
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / 1e3
+
+
+def time_phases(deck, st_snapshot, lib, forcing, torch, reps: int = 3) -> dict:
+    """Each phase timed alone with CUDA events on the library stream, from the same snapshot."""
+    from gom_release_gb300.core import GomCore, TIME_LOOP
+    core = GomCore(deck, lib=lib)
+    core.load_state(st_snapshot)
+    stream = torch.cuda.ExternalStream(core.stream_handle())
+    out = {}
+    for ph in TIME_LOOP:
+        ts = []
+        core.load_state(st_snapshot)
+        core.set_forcing(forcing)
+        for _ in range(reps):
+            core.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            core.step(ph)
+            e1.record(stream)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1) / 1e3)
+        out[ph] = min(ts)
+    core.close()
+    return out
+
+
+def phase_bytes(deck, ncl: int, pcg_iters: float) -> dict:
+    p = deck.params
+    nt = max(1, p.trans_sub_iter)
+    b = {ph: v * ncl for ph, v in PHASE_BYTES_PER_CELL_LAYER.items()}
+    b["transport"] = ncl * (TRANSPORT_BYTES_PER_CELL_LAYER_SUBCYCLE * nt + TRANSPORT_BYTES_PER_CELL_LAYER_AVERAGING)
+    b["free_surface"] = ncl * FS_ASSEMBLY_BYTES_PER_CELL_LAYER + deck.n_cells * PCG_BYTES_PER_CELL_ITERATION * pcg_iters
+    return b
+
+
+def measured_peak() -> tuple[float, str]:
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        try:
+            return float(json.loads(f.read_text())["hbm_gbs"]), "measured"
+        except (KeyError, ValueError):
+            pass
+    return 6800.0, "fallback"
+
+
+def cpu_baseline(deck, st, ncl: int, steps: int = 2) -> dict:
+    from gom_release_gb300.core import GomCore
+    from gom_release_gb300.driver import Run
+    if not ORACLE_SO.exists():
+        subprocess.run(["make", "-s", "-C", str(ROOT / "oracle")], check=True)
+    run = Run(deck, GomCore(deck, lib_path=ORACLE_SO), st)
+    t0 = time.perf_counter()
+    run.advance(steps)
+    dt = time.perf_counter() - t0
+    return {"value": ncl * steps / dt, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{steps} timesteps of the same estuary workload on 1 host core (serial FP64 CPU restatement)",
+            "seconds": dt}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return world, rank, local
+
+
+def reduce_max(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    from gom_release_gb300.deck import active_cell_layers, initial_state
+    deck = make_deck(args.small)
+    st = initial_state(deck)
+    ncl = active_cell_layers(deck, st)
+    from gom_release_gb300.core import GomCore
+    from gom_release_gb300.driver import Run
+    if not ORACLE_SO.exists():
+        subprocess.run(["make", "-s", "-C", str(ROOT / "oracle")], check=True)
+    run = Run(deck, GomCore(deck, lib_path=ORACLE_SO), st)
+    w = min(args.warmup, 1)
+    run.advance(w)
+    k = max(1, min(args.steps, 2))
+    t0 = time.perf_counter()
+    run.advance(k)
+    dt = time.perf_counter() - t0
+    value = ncl * k / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": k,
+        "warmup": w, "ms_per_step": dt / k * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"estuary {deck.n_cells} cells x {deck.n_layers} layers, {ncl} active cell-layers",
+                   "sample": f"{k} timesteps (bounded sample)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
+                         "sample": f"{k} timesteps of the estuary workload, serial FP64 CPU restatement "
+                                   "(the reference is Fortran and no Fortran compiler exists here)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--small", action="store_true", help="a 6k-cell estuary (profiling runs)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+    if args.warmup < 3:
+        args.warmup = 3
+    import torch
+    from gom_release_gb300.core import GomCore, load_core
+    from gom_release_gb300.deck import HostForcing, active_cell_layers, initial_state
+    from gom_release_gb300.driver import Run
+
+    deck = make_deck(args.small)
+    st = initial_state(deck)
+    ncl = active_cell_layers(deck, st)
+    lib = load_core()
+    run = Run(deck, GomCore(deck, lib=lib), st)
+    torch_mod, stream = stream_events(run.core)
+    run.advance(args.warmup)
+    # ---- value: K steps, state resident in HBM, host forcing precomputed
+    hf = HostForcing(deck)
+    hf.julian_day = run.forcing.julian_day
+    hf.first = False
+    forcings = [hf.step(run.it + 1 + i) for i in range(args.steps)]
+    barrier(world)
+    with ClockSampler(local) as clocks:
+        secs = time_steps(run, forcings, torch_mod, stream)
+    run.it += args.steps
+    run.forcing = hf
+    secs = reduce_max(secs, world)
+    pcg_total = run.core.pcg_iterations_total()
+    # ---- e2e: the public API with host buffers, forcing computed and result read every step
+    ke = max(10, args.steps // 4)
+    run.core.synchronize()
+    t0 = time.perf_counter()
+    e0 = torch_mod.cuda.Event(enable_timing=True)
+    e1 = torch_mod.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    h2d = 0
+    for _ in range(ke):
+        run.it += 1
+        f = run.forcing.step(run.it)
+        h2d = sum(np.asarray(v).nbytes for v in f.values() if isinstance(v, np.ndarray)) + 32
+        run.core.set_forcing(f)
+        run.core.step_all()
+        run.core.conservation()
+    e1.record(stream)
+    e1.synchronize()
+    e2e_secs = reduce_max(e0.elapsed_time(e1) / 1e3, world)
+    wall_e2e = time.perf_counter() - t0
+    # ---- per-phase timing for the roofline
+    snap = run.core.state()
+    f = dict(run.forcing.step(run.it + 1))
+    f.update(wind_stress_normal=run.forcing.wind_normal, wind_stress_tangnt=run.forcing.wind_tangnt,
+             gamma_t=run.forcing.gamma_t)
+    pcg_mean = (pcg_total / max(1, args.warmup + args.steps))
+    phases = time_phases(deck, snap, lib, f, torch_mod)
+    pb = phase_bytes(deck, ncl, pcg_mean)
+    dom = max(phases, key=phases.get)
+    peak, peak_kind = measured_peak()
+    achieved = pb.get(dom, 0) / phases[dom] / 1e9
+    if rank != 0:
+        barrier(world)
+        return
+    value = ncl * args.steps * world / secs
+    cpu = None
+    if not args.no_cpu_baseline:
+        cpu = cpu_baseline(deck, st, ncl)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": secs / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {
+            "workload": (f"estuary: {deck.n_cells} cells ({deck.meta['nx']}x{deck.meta['ny']} squares of "
+                         f"{deck.meta['dx']:g} m + {deck.meta['tri_rows']}-row triangle strip), {deck.n_faces} faces, "
+                         f"{deck.n_nodes} nodes, {deck.n_layers} layers, {ncl} active cell-layers, dt={deck.params.dt:g} s, "
+                         f"TVD limiter, {deck.params.trans_sub_iter} transport subcycles, baroclinic"),
+            "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+            "l2": "state larger than L2 (each phase streams its arrays from HBM)",
+            "simulated_hours_per_wall_s": deck.params.dt * args.steps / secs / 3600.0,
+            "pcg_iters_mean": pcg_mean,
+        },
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+                     "phase_ms": {k: v * 1e3 for k, v in phases.items()}},
+        "cpu_baseline": cpu,
+        "e2e": {"value": ncl * ke * world / e2e_secs, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": 16 + 20, "wall_s": wall_e2e},
+        "gpu_launches": kernel_launches_per_step(deck) * args.steps,
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    barrier(world)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,313 @@
+"""ctypes binding of the C ABI in include/gom_core.h.
+
+``GomCore`` drives a context of any library that exports the ABI.  The product library is
+``libgomcore.so`` (CUDA, sm_103a); ``load_core()`` fails loudly when it is missing or when no
+GPU is visible -- there is no CPU fallback on the product path.  The CPU restatement used as
+the test checker lives under ``oracle/`` and is loaded only by the tests, ``smoke()`` and the
+CPU-baseline leg of ``bench.py`` through ``GomCore(lib_path=...)``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+ROOT = PKG.parent
+CORE_SO = PKG / "_build" / "libgomcore.so"
+
+# gom_field enum of include/gom_core.h (tests check this table against the header)
+FIELDS = [
+    "eta_cell", "eta_cell_new", "eta_node", "wetdry_node",
+    "un_face", "vn_face", "un_face_new", "vn_face_new", "un_elm", "vn_elm",
+    "wn_cell", "wn_cell_new", "u_node", "v_node", "w_node", "u_face_level", "v_face_level",
+    "dz_cell", "dz_cell_new", "dzhalf_cell", "dzhalf_cell_new",
+    "dz_face", "dz_face_new", "dzhalf_face", "dzhalf_face_new",
+    "dz_node", "dz_node_new", "dzhalf_node", "dzhalf_node_new",
+    "top_layer_cell", "top_layer_face", "top_layer_node",
+    "ainvg1", "ainvg2", "ainvdz1", "ainvdz2", "kh", "av", "kv",
+    "salt_cell", "salt_cell_new", "temp_cell", "temp_cell_new", "salt_node", "temp_node",
+    "salt_face", "temp_face", "rho_cell", "rho_node", "rho_face", "num_sub_elm",
+    "cdb", "gamma_b", "qu_boundary", "elm_foot", "elm_near_edge",
+]
+FIELD_ID = {name: i + 1 for i, name in enumerate(FIELDS)}
+
+ERR_NAMES = {0: "GOM_OK", 1: "GOM_E_ARG", 2: "GOM_E_CUDA", 3: "GOM_E_NOT_SPD", 4: "GOM_E_ZERO_PIVOT",
+             5: "GOM_E_ELM", 6: "GOM_E_DRY", 7: "GOM_E_LAYER", 8: "GOM_E_DENSITY", 9: "GOM_E_PCG_MAXIT",
+             10: "GOM_E_TIMEOUT", 11: "GOM_E_NOMEM"}
+
+_D = C.POINTER(C.c_double)
+_I = C.POINTER(C.c_int32)
+
+
+class GomDims(C.Structure):
+    _fields_ = [("n_cells", C.c_int32), ("n_faces", C.c_int32), ("n_nodes", C.c_int32),
+                ("n_layers", C.c_int32), ("max_nb", C.c_int32), ("n_ob", C.c_int32),
+                ("n_qb", C.c_int32), ("reserved", C.c_int32)]
+
+
+_PARAM_D = ["gravity", "rho_o", "msl", "dt", "theta", "adv_onoff_depth", "von_karman", "cd_const",
+            "dry_depth", "smagorinsky", "ah_0", "kh_0", "error_tolerance", "delta_z_min",
+            "denominator_min_for_matrix"]
+_PARAM_I = ["advection_flag", "elm_backtrace_flag", "elm_sub_iter", "elm_min_iter", "elm_max_iter",
+            "bf_flag", "baroclinic_flag", "ana_density", "max_iteration_pcg", "transport_flag",
+            "trans_sub_iter", "h_flux_limiter", "v_flux_limiter", "is_salt", "is_temp", "heat_option"]
+
+
+class GomParams(C.Structure):
+    _fields_ = [(n, C.c_double) for n in _PARAM_D] + [(n, C.c_int32) for n in _PARAM_I] + \
+               [("reserved", C.c_int32 * 4)]
+
+
+_GEOM = [
+    ("x_node", _D), ("y_node", _D), ("h_node", _D), ("adj_cells_at_node", _I), ("adj_cellnum_at_node", _I),
+    ("node_count_each_element", _I), ("adj_nodes_at_node", _I), ("adj_nodenum_at_node", _I),
+    ("bottom_layer_at_node", _I), ("initial_wetdry_node", _I),
+    ("x_cell", _D), ("y_cell", _D), ("h_cell", _D), ("area", _D), ("tri_or_quad", _I),
+    ("nodenum_at_cell", _I), ("facenum_at_cell", _I), ("adj_cellnum_at_cell", _I), ("sign_in_outflow", _I),
+    ("bottom_layer_at_element", _I), ("ob_element_flag", _I), ("qb_element_flag", _I),
+    ("x_face", _D), ("y_face", _D), ("h_face", _D), ("face_length", _D), ("delta_j", _D),
+    ("cos_theta", _D), ("sin_theta", _D), ("cos_theta2", _D), ("sin_theta2", _D),
+    ("adj_cellnum_at_face", _I), ("nodenum_at_face", _I), ("bottom_layer_at_face", _I),
+    ("boundary_type_of_face", _I), ("isflowside3", _I), ("coriolis_factor", _D), ("manning", _D),
+    ("bf_height", _D), ("ob_cell_id", _I), ("qb_cell", _I), ("qb_face", _I), ("z_level", _D), ("delta_z", _D),
+]
+
+
+class GomGeom(C.Structure):
+    _fields_ = _GEOM
+
+
+class GomForcing(C.Structure):
+    _fields_ = [("elapsed_time", C.c_double), ("spinup_tide", C.c_double), ("spinup_baroclinic", C.c_double),
+                ("reserved", C.c_double), ("eta_at_ob_old", _D), ("eta_at_ob_new", _D), ("q_add", _D),
+                ("wind_stress_normal", _D), ("wind_stress_tangnt", _D), ("gamma_t", _D), ("air_p", _D),
+                ("con_at_ob", _D), ("con_at_qb", _D), ("phi_sw", _D)]
+
+
+class GomStatus(C.Structure):
+    _fields_ = [("code", C.c_int32), ("site", C.c_int32), ("entity", C.c_int32), ("layer", C.c_int32),
+                ("value", C.c_double)]
+
+
+class GomError(RuntimeError):
+    def __init__(self, code: int, where: str, status: GomStatus | None = None, message: str = ""):
+        self.code = code
+        self.status = status
+        s = f"{where}: {ERR_NAMES.get(code, code)}"
+        if status is not None and status.code:
+            s += f" (site={status.site} entity={status.entity} layer={status.layer} value={status.value:g})"
+        if message:
+            s += f" [{message}]"
+        super().__init__(s)
+
+
+_STEPS = ["bottom_friction", "boundary_velocity", "advection", "momentum", "velocities", "layers",
+          "node_velocity", "transport", "density", "swap"]
+
+
+def _bind(lib: C.CDLL) -> C.CDLL:
+    vp = C.c_void_p
+    lib.gom_abi_version.restype = C.c_int
+    lib.gom_errstr.restype = C.c_char_p
+    lib.gom_errstr.argtypes = [C.c_int]
+    lib.gom_last_message.restype = C.c_char_p
+    lib.gom_last_message.argtypes = [vp]
+    lib.gom_field_info.argtypes = [C.POINTER(GomDims), C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int32)]
+    lib.gom_create.argtypes = [C.POINTER(GomDims), C.POINTER(GomParams), C.POINTER(GomGeom), C.POINTER(vp)]
+    lib.gom_destroy.argtypes = [vp]
+    lib.gom_destroy.restype = None
+    lib.gom_set_field.argtypes = [vp, C.c_int, vp, C.c_int64]
+    lib.gom_get_field.argtypes = [vp, C.c_int, vp, C.c_int64]
+    lib.gom_set_forcing.argtypes = [vp, C.POINTER(GomForcing)]
+    for s in _STEPS:
+        getattr(lib, f"gom_step_{s}").argtypes = [vp]
+    lib.gom_step_free_surface.argtypes = [vp, C.POINTER(C.c_int32)]
+    lib.gom_step_all.argtypes = [vp, C.POINTER(C.c_int32)]
+    lib.gom_conservation.argtypes = [vp, _D, _D]
+    lib.gom_get_status.argtypes = [vp, C.POINTER(GomStatus), C.c_int]
+    lib.gom_synchronize.argtypes = [vp]
+    lib.gom_pcg_iterations_total.argtypes = [vp]
+    lib.gom_pcg_iterations_total.restype = C.c_int64
+    lib.gom_stream.argtypes = [vp]
+    lib.gom_stream.restype = vp
+    return lib
+
+
+def load_library(path: str | os.PathLike) -> C.CDLL:
+    path = Path(path)
+    if not path.exists():
+        raise FileNotFoundError(f"{path} is not built")
+    lib = _bind(C.CDLL(str(path), mode=C.RTLD_LOCAL))
+    v = lib.gom_abi_version()
+    if v != 1:
+        raise RuntimeError(f"{path}: ABI version {v}, expected 1")
+    return lib
+
+
+def load_core() -> C.CDLL:
+    """The CUDA library.  Raises if it is not built or no GPU is usable."""
+    if not CORE_SO.exists():
+        raise RuntimeError(f"CUDA extension missing: {CORE_SO} (run __graft_entry__.build())")
+    return load_library(CORE_SO)
+
+
+def _ptr(a: np.ndarray | None, kind):
+    if a is None:
+        return C.cast(None, kind)
+    return a.ctypes.data_as(kind)
+
+
+def _dbl(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _int(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+class GomCore:
+    """One context of a library exporting the GOM core ABI, created from a ``Deck``."""
+
+    def __init__(self, deck, lib: C.CDLL | None = None, lib_path: str | os.PathLike | None = None):
+        if lib is None:
+            lib = load_library(lib_path) if lib_path is not None else load_core()
+        self.lib = lib
+        self.deck = deck
+        d = deck
+        p = d.params
+        self.dims = GomDims(d.n_cells, d.n_faces, d.n_nodes, d.n_layers, d.max_nb, d.n_ob, d.n_qb, 0)
+        self.params = GomParams(*[getattr(p, n) for n in _PARAM_D], *[int(getattr(p, n)) for n in _PARAM_I])
+        g = d.geo
+        keep = {}
+        for name, kind in _GEOM:
+            if name == "ob_cell_id":
+                arr = d.ob_cell_id
+            elif name in ("qb_cell", "qb_face"):
+                arr = getattr(d, name)
+            elif name == "z_level":
+                arr = d.z_level
+            elif name == "delta_z":
+                arr = d.delta_z
+            else:
+                arr = g[name]
+            keep[name] = _dbl(arr) if kind is _D else _int(arr)
+        self._geom_keep = keep
+        self.geom = GomGeom(**{n: _ptr(keep[n], k) for n, k in _GEOM})
+        ctx = C.c_void_p()
+        rc = lib.gom_create(C.byref(self.dims), C.byref(self.params), C.byref(self.geom), C.byref(ctx))
+        if rc != 0:
+            raise GomError(rc, "gom_create")
+        self.ctx = ctx
+        self._forcing_keep = {}
+
+    # ------------------------------------------------------------------ lifetime
+    def close(self):
+        if getattr(self, "ctx", None):
+            self.lib.gom_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ------------------------------------------------------------------ fields
+    def field_info(self, name: str) -> tuple[int, int]:
+        n = C.c_int64()
+        eb = C.c_int32()
+        rc = self.lib.gom_field_info(C.byref(self.dims), FIELD_ID[name], C.byref(n), C.byref(eb))
+        if rc:
+            raise GomError(rc, f"gom_field_info({name})")
+        return n.value, eb.value
+
+    def set_field(self, name: str, arr: np.ndarray):
+        n, eb = self.field_info(name)
+        a = _int(arr) if eb == 4 else _dbl(arr)
+        if a.size != n:
+            raise ValueError(f"{name}: {a.size} elements, expected {n}")
+        self._check(self.lib.gom_set_field(self.ctx, FIELD_ID[name], a.ctypes.data, n), f"set_field({name})")
+
+    def get_field(self, name: str) -> np.ndarray:
+        n, eb = self.field_info(name)
+        a = np.empty(n, dtype=np.int32 if eb == 4 else np.float64)
+        self._check(self.lib.gom_get_field(self.ctx, FIELD_ID[name], a.ctypes.data, n), f"get_field({name})")
+        return a
+
+    def load_state(self, state: dict):
+        for name, arr in state.items():
+            self.set_field(name, arr)
+
+    def state(self, names=None) -> dict:
+        return {n: self.get_field(n) for n in (names or FIELDS)}
+
+    # ------------------------------------------------------------------ forcing / steps
+    def set_forcing(self, f: dict):
+        keep = {}
+
+        def arr(name):
+            if name not in f or f[name] is None:
+                return C.cast(None, _D)
+            a = _dbl(np.asarray(f[name]).transpose(2, 1, 0).ravel()
+                     if name in ("con_at_ob", "con_at_qb") else f[name])
+            keep[name] = a
+            return a.ctypes.data_as(_D)
+
+        s = GomForcing(f.get("elapsed_time", 0.0), f.get("spinup_tide", 1.0), f.get("spinup_baroclinic", 1.0), 0.0,
+                       arr("eta_at_ob_old"), arr("eta_at_ob_new"), arr("q_add"), arr("wind_stress_normal"),
+                       arr("wind_stress_tangnt"), arr("gamma_t"), arr("air_p"), arr("con_at_ob"),
+                       arr("con_at_qb"), arr("phi_sw"))
+        self._forcing_keep = keep
+        self._check(self.lib.gom_set_forcing(self.ctx, C.byref(s)), "set_forcing")
+
+    def step(self, name: str):
+        if name == "free_surface":
+            it = C.c_int32()
+            self._check(self.lib.gom_step_free_surface(self.ctx, C.byref(it)), "step_free_surface")
+            return it.value
+        self._check(getattr(self.lib, f"gom_step_{name}")(self.ctx), f"step_{name}")
+        return None
+
+    def step_all(self) -> int:
+        it = C.c_int32()
+        self._check(self.lib.gom_step_all(self.ctx, C.byref(it)), "step_all")
+        return it.value
+
+    def synchronize(self):
+        self._check(self.lib.gom_synchronize(self.ctx), "synchronize")
+
+    def conservation(self) -> tuple[float, float]:
+        v = C.c_double()
+        s = C.c_double()
+        self._check(self.lib.gom_conservation(self.ctx, C.byref(v), C.byref(s)), "conservation")
+        return v.value, s.value
+
+    def status(self, clear: bool = False) -> GomStatus:
+        st = GomStatus()
+        self.lib.gom_get_status(self.ctx, C.byref(st), 1 if clear else 0)
+        return st
+
+    def stream_handle(self) -> int:
+        return int(self.lib.gom_stream(self.ctx) or 0)
+
+    def pcg_iterations_total(self) -> int:
+        return int(self.lib.gom_pcg_iterations_total(self.ctx))
+
+    def _check(self, rc: int, where: str):
+        if rc != 0:
+            msg = self.lib.gom_last_message(self.ctx) if getattr(self, "ctx", None) else b""
+            raise GomError(rc, where, self.status(), (msg or b"").decode(errors="replace"))
+
+
+# ------------------------------------------------------------------ time loop (main.f90:53-304)
+TIME_LOOP = ["bottom_friction", "boundary_velocity", "advection", "momentum", "free_surface",
+             "velocities", "layers", "node_velocity", "transport", "density", "swap"]
+
+
+def prepare(core: GomCore, state: dict):
+    """prepare_gom.f90: upload the cold-start state and compute the initial density."""
+    core.load_state(state)
+    core.step("density")

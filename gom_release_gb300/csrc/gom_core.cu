@@ -1,0 +1,595 @@
+// gom_core.cu -- the C ABI of include/gom_core.h on a GB300 (sm_103a).
+//
+// A context owns: the static geometry copied to HBM once, every state array of the time loop
+// resident in HBM in the reference's (k, entity) layout, the work buffers of the phases, one
+// CUDA stream, pinned staging for the per-step forcing, and a CUDA graph of the whole timestep
+// (captured on first use of gom_step_all).  Host arrays are read only during a call.
+#include <cstdio>
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "gom_launch.h"
+
+using namespace gom;
+
+namespace {
+
+struct FieldDesc {
+    void **dev;      // address of the State member
+    int lo;          // -1: 1-D entity array; else lower layer bound (0 or 1)
+    int kind;        // 0 cells, 1 faces, 2 nodes, 3 river cells
+    int is_int;
+};
+
+}  // namespace
+
+struct gom_ctx {
+    gom_dims d{};
+    gom_params hp{};
+    Launch x;
+    int device = 0;
+    std::vector<void *> allocs;
+    std::string msg;
+    FieldDesc fields[GOM_F_COUNT];
+    // forcing arrays on the device (the Forcing view points into these)
+    double *f_scal = nullptr;
+    double *f_eta_old = nullptr, *f_eta_new = nullptr, *f_q_add = nullptr, *f_wsn = nullptr, *f_wst = nullptr,
+           *f_gamma_t = nullptr, *f_air_p = nullptr, *f_con_ob = nullptr, *f_con_qb = nullptr, *f_phi_sw = nullptr;
+    // pinned host mirrors
+    gom_status *h_status = nullptr;
+    int *h_iters = nullptr;
+    double *h_cons = nullptr;
+    double *h_stage = nullptr;
+    size_t stage_len = 0;
+    long long pcg_total = 0;
+    cudaGraphExec_t graph = nullptr;
+    bool graph_failed = false;
+};
+
+namespace {
+
+int set_cuda_error(gom_ctx *c, cudaError_t e, const char *where) {
+    if (e == cudaSuccess) return GOM_OK;
+    if (c) {
+        c->msg = std::string(where) + ": " + cudaGetErrorString(e);
+        if (c->h_status && c->h_status->code == 0) c->h_status->code = GOM_E_CUDA;
+    }
+    return e == cudaErrorMemoryAllocation ? GOM_E_NOMEM : GOM_E_CUDA;
+}
+
+#define CK(call)                                                          \
+    do {                                                                  \
+        cudaError_t _e = (call);                                          \
+        if (_e != cudaSuccess) return set_cuda_error(c, _e, #call);      \
+    } while (0)
+
+template <typename T> cudaError_t dalloc(gom_ctx *c, T **p, size_t n) {
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
+    if (e == cudaSuccess) {
+        c->allocs.push_back(*p);
+        e = cudaMemset(*p, 0, n * sizeof(T));
+    }
+    return e;
+}
+
+template <typename T> cudaError_t upload(gom_ctx *c, const T **dst, const T *src, size_t n, bool required) {
+    T *p = nullptr;
+    cudaError_t e = dalloc(c, &p, n);
+    if (e != cudaSuccess) return e;
+    if (src) e = cudaMemcpy(p, src, n * sizeof(T), cudaMemcpyHostToDevice);
+    else if (required) e = cudaErrorInvalidValue;
+    *dst = p;
+    return e;
+}
+
+int64_t field_count(const gom_dims &d, const FieldDesc &f) {
+    int64_t n = f.kind == 0 ? d.n_cells : f.kind == 1 ? d.n_faces : f.kind == 2 ? d.n_nodes : d.n_qb;
+    if (f.lo < 0) return n;
+    return n * (int64_t)(d.n_layers - f.lo + 1);
+}
+
+void describe_fields(gom_ctx *c) {
+    State &s = c->x.s;
+    auto D = [&](int id, double **m, int lo, int kind) { c->fields[id] = FieldDesc{(void **)m, lo, kind, 0}; };
+    auto I = [&](int id, int **m, int lo, int kind) { c->fields[id] = FieldDesc{(void **)m, lo, kind, 1}; };
+    for (int f = 0; f < GOM_F_COUNT; ++f) c->fields[f] = FieldDesc{nullptr, -2, 0, 0};
+    D(GOM_F_ETA_CELL, &s.eta_cell, -1, 0);
+    D(GOM_F_ETA_CELL_NEW, &s.eta_cell_new, -1, 0);
+    D(GOM_F_ETA_NODE, &s.eta_node, -1, 2);
+    I(GOM_F_WETDRY_NODE, &s.wetdry_node, -1, 2);
+    D(GOM_F_UN_FACE, &s.un_face, 1, 1);
+    D(GOM_F_VN_FACE, &s.vn_face, 1, 1);
+    D(GOM_F_UN_FACE_NEW, &s.un_face_new, 1, 1);
+    D(GOM_F_VN_FACE_NEW, &s.vn_face_new, 1, 1);
+    D(GOM_F_UN_ELM, &s.un_elm, 1, 1);
+    D(GOM_F_VN_ELM, &s.vn_elm, 1, 1);
+    D(GOM_F_WN_CELL, &s.wn_cell, 0, 0);
+    D(GOM_F_WN_CELL_NEW, &s.wn_cell_new, 0, 0);
+    D(GOM_F_U_NODE, &s.u_node, 0, 2);
+    D(GOM_F_V_NODE, &s.v_node, 0, 2);
+    D(GOM_F_W_NODE, &s.w_node, 0, 2);
+    D(GOM_F_U_FACE_LEVEL, &s.u_face_level, 0, 1);
+    D(GOM_F_V_FACE_LEVEL, &s.v_face_level, 0, 1);
+    D(GOM_F_DZ_CELL, &s.dz_cell, 1, 0);
+    D(GOM_F_DZ_CELL_NEW, &s.dz_cell_new, 1, 0);
+    D(GOM_F_DZHALF_CELL, &s.dzhalf_cell, 0, 0);
+    D(GOM_F_DZHALF_CELL_NEW, &s.dzhalf_cell_new, 0, 0);
+    D(GOM_F_DZ_FACE, &s.dz_face, 1, 1);
+    D(GOM_F_DZ_FACE_NEW, &s.dz_face_new, 1, 1);
+    D(GOM_F_DZHALF_FACE, &s.dzhalf_face, 0, 1);
+    D(GOM_F_DZHALF_FACE_NEW, &s.dzhalf_face_new, 0, 1);
+    D(GOM_F_DZ_NODE, &s.dz_node, 1, 2);
+    D(GOM_F_DZ_NODE_NEW, &s.dz_node_new, 1, 2);
+    D(GOM_F_DZHALF_NODE, &s.dzhalf_node, 0, 2);
+    D(GOM_F_DZHALF_NODE_NEW, &s.dzhalf_node_new, 0, 2);
+    I(GOM_F_TOP_LAYER_CELL, &s.top_cell, -1, 0);
+    I(GOM_F_TOP_LAYER_FACE, &s.top_face, -1, 1);
+    I(GOM_F_TOP_LAYER_NODE, &s.top_node, -1, 2);
+    D(GOM_F_AINVG1, &s.ainvg1, 1, 1);
+    D(GOM_F_AINVG2, &s.ainvg2, 1, 1);
+    D(GOM_F_AINVDZ1, &s.ainvdz1, 1, 1);
+    D(GOM_F_AINVDZ2, &s.ainvdz2, 1, 1);
+    D(GOM_F_KH, &s.kh, 1, 1);
+    D(GOM_F_AV, &s.av, 0, 1);
+    D(GOM_F_KV, &s.kv, 0, 0);
+    D(GOM_F_SALT_CELL, &s.salt_cell, 1, 0);
+    D(GOM_F_SALT_CELL_NEW, &s.salt_cell_new, 1, 0);
+    D(GOM_F_TEMP_CELL, &s.temp_cell, 1, 0);
+    D(GOM_F_TEMP_CELL_NEW, &s.temp_cell_new, 1, 0);
+    D(GOM_F_SALT_NODE, &s.salt_node, 1, 2);
+    D(GOM_F_TEMP_NODE, &s.temp_node, 1, 2);
+    D(GOM_F_SALT_FACE, &s.salt_face, 1, 1);
+    D(GOM_F_TEMP_FACE, &s.temp_face, 1, 1);
+    D(GOM_F_RHO_CELL, &s.rho_cell, 1, 0);
+    D(GOM_F_RHO_NODE, &s.rho_node, 1, 2);
+    D(GOM_F_RHO_FACE, &s.rho_face, 1, 1);
+    I(GOM_F_NUM_SUB_ELM, &s.num_sub_elm, 1, 2);
+    D(GOM_F_CDB, &s.cdb, -1, 1);
+    D(GOM_F_GAMMA_B, &s.gamma_b, -1, 1);
+    D(GOM_F_QU_BOUNDARY, &s.qu_boundary, -1, 3);
+    I(GOM_F_ELM_FOOT, &s.elm_foot, 1, 1);
+    I(GOM_F_ELM_NEAR_EDGE, &s.elm_near_edge, 1, 1);
+}
+
+// state arrays that update_variables.f90:16-31 copies from *_new to the old name
+const int kSwapPairs[][2] = {{GOM_F_ETA_CELL, GOM_F_ETA_CELL_NEW},   {GOM_F_WN_CELL, GOM_F_WN_CELL_NEW},
+                             {GOM_F_DZ_CELL, GOM_F_DZ_CELL_NEW},     {GOM_F_DZHALF_CELL, GOM_F_DZHALF_CELL_NEW},
+                             {GOM_F_SALT_CELL, GOM_F_SALT_CELL_NEW}, {GOM_F_TEMP_CELL, GOM_F_TEMP_CELL_NEW},
+                             {GOM_F_UN_FACE, GOM_F_UN_FACE_NEW},     {GOM_F_VN_FACE, GOM_F_VN_FACE_NEW},
+                             {GOM_F_DZ_FACE, GOM_F_DZ_FACE_NEW},     {GOM_F_DZHALF_FACE, GOM_F_DZHALF_FACE_NEW},
+                             {GOM_F_DZ_NODE, GOM_F_DZ_NODE_NEW},     {GOM_F_DZHALF_NODE, GOM_F_DZHALF_NODE_NEW}};
+
+cudaError_t enqueue_swap(gom_ctx *c) {
+    for (auto &pr : kSwapPairs) {
+        const FieldDesc &a = c->fields[pr[0]];
+        const FieldDesc &b = c->fields[pr[1]];
+        size_t bytes = (size_t)field_count(c->d, a) * 8;
+        cudaError_t e = cudaMemcpyAsync(*a.dev, *b.dev, bytes, cudaMemcpyDeviceToDevice, c->x.stream);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+// the phases of main.f90:94-272 in order
+cudaError_t enqueue_step(gom_ctx *c) {
+    const Launch &x = c->x;
+    cudaError_t e;
+    if ((e = launch_bottom_friction(x))) return e;
+    if ((e = launch_boundary_velocity(x))) return e;
+    if ((e = launch_advection(x))) return e;
+    if ((e = launch_momentum(x))) return e;
+    if ((e = launch_free_surface(x))) return e;
+    if ((e = launch_velocities(x))) return e;
+    if ((e = launch_layers(x))) return e;
+    if ((e = launch_node_velocity(x))) return e;
+    if ((e = launch_transport(x))) return e;
+    if ((e = launch_density(x))) return e;
+    return enqueue_swap(c);
+}
+
+// copy status and PCG iterations to pinned memory, wait, translate to a return code
+int finish(gom_ctx *c, int32_t *pcg_iters, bool had_pcg) {
+    CK(cudaMemcpyAsync(c->h_status, c->x.status, sizeof(gom_status), cudaMemcpyDeviceToHost, c->x.stream));
+    if (had_pcg) CK(cudaMemcpyAsync(c->h_iters, c->x.w.pcg_iters, sizeof(int), cudaMemcpyDeviceToHost, c->x.stream));
+    CK(cudaStreamSynchronize(c->x.stream));
+    if (had_pcg) {
+        c->pcg_total += *c->h_iters;
+        if (pcg_iters) *pcg_iters = *c->h_iters;
+    }
+    return c->h_status->code;
+}
+
+int run_phase(gom_ctx *c, cudaError_t (*fn)(const Launch &)) {
+    if (!c) return GOM_E_ARG;
+    CK(fn(c->x));
+    return finish(c, nullptr, false);
+}
+
+}  // namespace
+
+extern "C" {
+
+int gom_abi_version(void) { return GOM_ABI_VERSION; }
+
+const char *gom_errstr(int code) {
+    switch (code) {
+    case GOM_OK: return "ok";
+    case GOM_E_ARG: return "bad argument";
+    case GOM_E_CUDA: return "CUDA error";
+    case GOM_E_NOT_SPD: return "free-surface matrix not positive definite";
+    case GOM_E_ZERO_PIVOT: return "tridiagonal solver zero pivot";
+    case GOM_E_ELM: return "ELM backtracking geometry failure";
+    case GOM_E_DRY: return "dry element or boundary where water is required";
+    case GOM_E_LAYER: return "impossible elevation or layer";
+    case GOM_E_DENSITY: return "density, salinity or temperature out of range";
+    case GOM_E_PCG_MAXIT: return "PCG reached max_iteration_pcg";
+    case GOM_E_TIMEOUT: return "device wait timed out";
+    case GOM_E_NOMEM: return "out of device memory";
+    default: return "unknown error";
+    }
+}
+
+const char *gom_last_message(const gom_ctx *ctx) { return ctx ? ctx->msg.c_str() : ""; }
+
+int gom_field_info(const gom_dims *dims, int field, int64_t *count, int32_t *elem_bytes) {
+    if (!dims || field <= 0 || field >= GOM_F_COUNT) return GOM_E_ARG;
+    gom_ctx tmp;
+    describe_fields(&tmp);
+    const FieldDesc &f = tmp.fields[field];
+    if (f.lo == -2) return GOM_E_ARG;
+    if (count) *count = field_count(*dims, f);
+    if (elem_bytes) *elem_bytes = f.is_int ? 4 : 8;
+    return GOM_OK;
+}
+
+int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g, gom_ctx **out) {
+    if (!dims || !params || !g || !out) return GOM_E_ARG;
+    *out = nullptr;
+    const gom_dims &d = *dims;
+    if (d.n_cells <= 0 || d.n_faces <= 0 || d.n_nodes <= 0 || d.n_layers <= 0 || d.n_layers > GOM_MAXL ||
+        d.max_nb <= 0 || d.max_nb > GOM_MAXNB || d.n_ob < 0 || d.n_qb < 0)
+        return GOM_E_ARG;
+    if (params->transport_flag && params->is_salt == 0 && params->is_temp == 1) return GOM_E_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return GOM_E_CUDA;
+    gom_ctx *c = new gom_ctx();
+    c->d = d;
+    c->hp = *params;
+    cudaGetDevice(&c->device);
+    describe_fields(c);
+    auto fail = [&](int code) {
+        gom_destroy(c);
+        return code;
+    };
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, c->device) != cudaSuccess) return fail(GOM_E_CUDA);
+    c->x.num_sms = prop.multiProcessorCount;
+    if (cudaStreamCreateWithFlags(&c->x.stream, cudaStreamNonBlocking) != cudaSuccess) return fail(GOM_E_CUDA);
+    const size_t NC = d.n_cells, NF = d.n_faces, NN = d.n_nodes, NB = d.max_nb, L = d.n_layers;
+    Geom &G = c->x.g;
+    G.NC = d.n_cells;
+    G.NF = d.n_faces;
+    G.NN = d.n_nodes;
+    G.L = d.n_layers;
+    G.NB = d.max_nb;
+    G.NOB = d.n_ob;
+    G.NQB = d.n_qb;
+    cudaError_t e = cudaSuccess;
+#define UP(dst, src, n, req) \
+    if (e == cudaSuccess) e = upload(c, &G.dst, g->src, n, req)
+    UP(x_node, x_node, NN, true);
+    UP(y_node, y_node, NN, true);
+    UP(h_node, h_node, NN, true);
+    UP(adj_cells_at_node, adj_cells_at_node, NN, true);
+    UP(adj_cellnum_at_node, adj_cellnum_at_node, NB * NN, true);
+    UP(node_count_each_element, node_count_each_element, NB * NN, true);
+    UP(adj_nodes_at_node, adj_nodes_at_node, NN, true);
+    UP(adj_nodenum_at_node, adj_nodenum_at_node, (NB + 1) * NN, true);
+    UP(bottom_node, bottom_layer_at_node, NN, true);
+    UP(initial_wetdry_node, initial_wetdry_node, NN, false);
+    UP(x_cell, x_cell, NC, true);
+    UP(y_cell, y_cell, NC, true);
+    UP(h_cell, h_cell, NC, true);
+    UP(area, area, NC, true);
+    UP(tri_or_quad, tri_or_quad, NC, true);
+    UP(nodenum_at_cell, nodenum_at_cell, 4 * NC, true);
+    UP(facenum_at_cell, facenum_at_cell, 4 * NC, true);
+    UP(adj_cellnum_at_cell, adj_cellnum_at_cell, 4 * NC, true);
+    UP(sign_in_outflow, sign_in_outflow, 4 * NC, true);
+    UP(bottom_cell, bottom_layer_at_element, NC, true);
+    UP(ob_element_flag, ob_element_flag, NC, false);
+    UP(qb_element_flag, qb_element_flag, NC, false);
+    UP(x_face, x_face, NF, true);
+    UP(y_face, y_face, NF, true);
+    UP(h_face, h_face, NF, true);
+    UP(face_length, face_length, NF, true);
+    UP(delta_j, delta_j, NF, true);
+    UP(cos_theta, cos_theta, NF, true);
+    UP(sin_theta, sin_theta, NF, true);
+    UP(cos_theta2, cos_theta2, NF, true);
+    UP(sin_theta2, sin_theta2, NF, true);
+    UP(coriolis_factor, coriolis_factor, NF, false);
+    UP(manning, manning, NF, params->bf_flag == 1);
+    UP(bf_height, bf_height, NF, params->bf_flag == 2);
+    UP(adj_cellnum_at_face, adj_cellnum_at_face, 2 * NF, true);
+    UP(nodenum_at_face, nodenum_at_face, 2 * NF, true);
+    UP(bottom_face, bottom_layer_at_face, NF, true);
+    UP(boundary_type_of_face, boundary_type_of_face, NF, true);
+    UP(isflowside3, isflowside3, NF, false);
+    UP(ob_cell_id, ob_cell_id, (size_t)d.n_ob, d.n_ob > 0);
+    UP(qb_cell, qb_cell, (size_t)d.n_qb, d.n_qb > 0);
+    UP(qb_face, qb_face, (size_t)d.n_qb, d.n_qb > 0);
+    UP(z_level, z_level, L + 1, true);
+    UP(delta_z, delta_z, L, true);
+#undef UP
+    if (e != cudaSuccess) return fail(e == cudaErrorInvalidValue ? GOM_E_ARG : GOM_E_CUDA);
+    // state
+    for (int f = 1; f < GOM_F_COUNT && e == cudaSuccess; ++f) {
+        const FieldDesc &fd = c->fields[f];
+        if (fd.lo == -2) continue;
+        size_t n = (size_t)field_count(d, fd);
+        if (fd.is_int) e = dalloc(c, (int **)fd.dev, n);
+        else e = dalloc(c, (double **)fd.dev, n);
+    }
+    // forcing
+    int nt = params->trans_sub_iter > 0 ? params->trans_sub_iter : 1;
+    if (e == cudaSuccess) e = dalloc(c, &c->f_eta_old, (size_t)d.n_ob);
+    if (e == cudaSuccess) e = dalloc(c, &c->f_eta_new, (size_t)d.n_ob);
+    if (e == cudaSuccess) e = dalloc(c, &c->f_q_add, (size_t)d.n_qb);
+    if (e == cudaSuccess) e = dalloc(c, &c->f_wsn, NF);
+    if (e == cudaSuccess) e = dalloc(c, &c->f_wst, NF);
+    if (e == cudaSuccess) e = dalloc(c, &c->f_gamma_t, NF);
+    if (e == cudaSuccess) e = dalloc(c, &c->f_air_p, NN);
+    if (e == cudaSuccess) e = dalloc(c, &c->f_con_ob, (size_t)d.n_ob * 2 * nt);
+    if (e == cudaSuccess) e = dalloc(c, &c->f_con_qb, (size_t)d.n_qb * 2 * nt);
+    if (e == cudaSuccess) e = dalloc(c, &c->f_phi_sw, NC);
+    if (e == cudaSuccess) e = dalloc(c, &c->f_scal, 4);
+    if (e == cudaSuccess) {
+        const double one[4] = {0.0, 1.0, 1.0, 0.0};
+        e = cudaMemcpy(c->f_scal, one, sizeof(one), cudaMemcpyHostToDevice);
+    }
+    Forcing &F = c->x.f;
+    F.scal = c->f_scal;
+    F.eta_at_ob_old = c->f_eta_old;
+    F.eta_at_ob_new = c->f_eta_new;
+    F.q_add = c->f_q_add;
+    F.wind_stress_normal = c->f_wsn;
+    F.wind_stress_tangnt = c->f_wst;
+    F.gamma_t = c->f_gamma_t;
+    F.air_p = c->f_air_p;
+    F.con_at_ob = c->f_con_ob;
+    F.con_at_qb = c->f_con_qb;
+    F.phi_sw = c->f_phi_sw;
+    // work
+    Work &W = c->x.w;
+    if (e == cudaSuccess) e = dalloc(c, &W.sparsem, 5 * NC);
+    if (e == cudaSuccess) e = dalloc(c, &W.rhs, NC);
+    if (e == cudaSuccess) e = dalloc(c, &W.minv, NC);
+    if (e == cudaSuccess) e = dalloc(c, &W.r, NC);
+    if (e == cudaSuccess) e = dalloc(c, &W.s, NC);
+    if (e == cudaSuccess) e = dalloc(c, &W.q, NC);
+    if (e == cudaSuccess) e = dalloc(c, &W.d0, NC);
+    if (e == cudaSuccess) e = dalloc(c, &W.d1, NC);
+    if (e == cudaSuccess) e = dalloc(c, &W.barrier, 2);
+    if (e == cudaSuccess) e = dalloc(c, &W.pcg_iters, 1);
+    if (e == cudaSuccess) e = dalloc(c, &W.con, (L + 2) * NC * 2);
+    if (e == cudaSuccess) e = dalloc(c, &W.con2, (L + 2) * NC * 2);
+    if (e == cudaSuccess) e = dalloc(c, &W.qj, L * NF);
+    if (e == cudaSuccess) e = dalloc(c, &W.dj, L * NF);
+    if (e == cudaSuccess) e = dalloc(c, &W.phij, L * NF);
+    if (e == cudaSuccess) e = dalloc(c, &W.qi, (L + 1) * NC);
+    if (e == cudaSuccess) e = dalloc(c, &W.di, (L + 1) * NC);
+    if (e == cudaSuccess) e = dalloc(c, &W.phii, (L + 1) * NC);
+    if (e == cudaSuccess) e = dalloc(c, &W.psij, L * NF * 2);
+    if (e == cudaSuccess) e = dalloc(c, &W.psii, (L + 1) * NC * 2);
+    if (e == cudaSuccess) e = dalloc(c, &W.sa1, L * NC * 2);
+    if (e == cudaSuccess) e = dalloc(c, &W.sa2, L * NC * 2);
+    if (e == cudaSuccess) e = dalloc(c, &W.obk, L * (size_t)d.n_ob * 2);
+    if (e == cudaSuccess) e = dalloc(c, &W.qbk, L * (size_t)d.n_qb * 2);
+    if (e == cudaSuccess) e = dalloc(c, &W.cons, 2 + 2 * (size_t)((NC + 255) / 256));
+    if (e == cudaSuccess) e = dalloc(c, &c->x.status, 1);
+    if (e != cudaSuccess) return fail(e == cudaErrorMemoryAllocation ? GOM_E_NOMEM : GOM_E_CUDA);
+    // parameters
+    Params &P = c->x.p;
+    P.gravity = params->gravity;
+    P.rho_o = params->rho_o;
+    P.msl = params->msl;
+    P.dt = params->dt;
+    P.theta = params->theta;
+    P.adv_onoff_depth = params->adv_onoff_depth;
+    P.von_karman = params->von_karman;
+    P.cd_const = params->cd_const;
+    P.dry_depth = params->dry_depth;
+    P.smagorinsky = params->smagorinsky;
+    P.ah_0 = params->ah_0;
+    P.kh_0 = params->kh_0;
+    P.error_tolerance = params->error_tolerance;
+    P.delta_z_min = params->delta_z_min;
+    P.denominator_min_for_matrix = params->denominator_min_for_matrix;
+    P.advection_flag = params->advection_flag;
+    P.elm_backtrace_flag = params->elm_backtrace_flag;
+    P.elm_sub_iter = params->elm_sub_iter;
+    P.elm_min_iter = params->elm_min_iter;
+    P.elm_max_iter = params->elm_max_iter;
+    P.bf_flag = params->bf_flag;
+    P.baroclinic_flag = params->baroclinic_flag;
+    P.ana_density = params->ana_density;
+    P.max_iteration_pcg = params->max_iteration_pcg;
+    P.transport_flag = params->transport_flag;
+    P.trans_sub_iter = params->trans_sub_iter;
+    P.h_flux_limiter = params->h_flux_limiter;
+    P.v_flux_limiter = params->v_flux_limiter;
+    P.is_salt = params->is_salt;
+    P.is_temp = params->is_temp;
+    P.heat_option = params->heat_option;
+    // pinned host staging
+    c->stage_len = std::max<size_t>({NF, NN, NC, (size_t)d.n_ob * 2 * nt, (size_t)d.n_qb * 2 * nt}) * 10 + 64;
+    if (cudaMallocHost((void **)&c->h_status, sizeof(gom_status)) != cudaSuccess ||
+        cudaMallocHost((void **)&c->h_iters, sizeof(int)) != cudaSuccess ||
+        cudaMallocHost((void **)&c->h_cons, 2 * sizeof(double)) != cudaSuccess ||
+        cudaMallocHost((void **)&c->h_stage, c->stage_len * sizeof(double)) != cudaSuccess)
+        return fail(GOM_E_NOMEM);
+    std::memset(c->h_status, 0, sizeof(gom_status));
+    if (pcg_configure(c->x, c->device) != cudaSuccess) return fail(GOM_E_CUDA);
+    {
+        size_t nb = (size_t)c->x.w.pcg_blocks;
+        if (dalloc(c, &W.partial_dq, nb) != cudaSuccess || dalloc(c, &W.partial_delta, nb) != cudaSuccess)
+            return fail(GOM_E_NOMEM);
+    }
+    if (cudaDeviceSynchronize() != cudaSuccess) return fail(GOM_E_CUDA);
+    *out = c;
+    return GOM_OK;
+}
+
+void gom_destroy(gom_ctx *c) {
+    if (!c) return;
+    if (c->x.stream) cudaStreamSynchronize(c->x.stream);
+    if (c->graph) cudaGraphExecDestroy(c->graph);
+    for (void *p : c->allocs) cudaFree(p);
+    if (c->h_status) cudaFreeHost(c->h_status);
+    if (c->h_iters) cudaFreeHost(c->h_iters);
+    if (c->h_cons) cudaFreeHost(c->h_cons);
+    if (c->h_stage) cudaFreeHost(c->h_stage);
+    if (c->x.stream) cudaStreamDestroy(c->x.stream);
+    delete c;
+}
+
+int gom_set_field(gom_ctx *c, int field, const void *host, int64_t count) {
+    if (!c || !host || field <= 0 || field >= GOM_F_COUNT) return GOM_E_ARG;
+    const FieldDesc &f = c->fields[field];
+    if (f.lo == -2 || count != field_count(c->d, f)) return GOM_E_ARG;
+    CK(cudaMemcpyAsync(*f.dev, host, (size_t)count * (f.is_int ? 4 : 8), cudaMemcpyHostToDevice, c->x.stream));
+    CK(cudaStreamSynchronize(c->x.stream));
+    return GOM_OK;
+}
+
+int gom_get_field(gom_ctx *c, int field, void *host, int64_t count) {
+    if (!c || !host || field <= 0 || field >= GOM_F_COUNT) return GOM_E_ARG;
+    const FieldDesc &f = c->fields[field];
+    if (f.lo == -2 || count != field_count(c->d, f)) return GOM_E_ARG;
+    CK(cudaMemcpyAsync(host, *f.dev, (size_t)count * (f.is_int ? 4 : 8), cudaMemcpyDeviceToHost, c->x.stream));
+    CK(cudaStreamSynchronize(c->x.stream));
+    return GOM_OK;
+}
+
+int gom_set_forcing(gom_ctx *c, const gom_forcing *fo) {
+    if (!c || !fo) return GOM_E_ARG;
+    const gom_dims &d = c->d;
+    const double scal[4] = {fo->elapsed_time, fo->spinup_tide, fo->spinup_baroclinic, 0.0};
+    int nt = c->hp.trans_sub_iter > 0 ? c->hp.trans_sub_iter : 1;
+    struct Item {
+        const double *src;
+        double *dst;
+        size_t n;
+    } items[] = {{scal, c->f_scal, 4},
+                 {fo->eta_at_ob_old, c->f_eta_old, (size_t)d.n_ob},
+                 {fo->eta_at_ob_new, c->f_eta_new, (size_t)d.n_ob},
+                 {fo->q_add, c->f_q_add, (size_t)d.n_qb},
+                 {fo->wind_stress_normal, c->f_wsn, (size_t)d.n_faces},
+                 {fo->wind_stress_tangnt, c->f_wst, (size_t)d.n_faces},
+                 {fo->gamma_t, c->f_gamma_t, (size_t)d.n_faces},
+                 {fo->air_p, c->f_air_p, (size_t)d.n_nodes},
+                 {fo->con_at_ob, c->f_con_ob, (size_t)d.n_ob * 2 * nt},
+                 {fo->con_at_qb, c->f_con_qb, (size_t)d.n_qb * 2 * nt},
+                 {fo->phi_sw, c->f_phi_sw, (size_t)d.n_cells}};
+    // wait for the previous upload through the staging buffer before overwriting it
+    CK(cudaStreamSynchronize(c->x.stream));
+    size_t off = 0;
+    for (auto &it : items) {
+        if (!it.src || it.n == 0) continue;
+        if (off + it.n > c->stage_len) {
+            CK(cudaMemcpyAsync(it.dst, it.src, it.n * 8, cudaMemcpyHostToDevice, c->x.stream));
+            continue;
+        }
+        std::memcpy(c->h_stage + off, it.src, it.n * 8);
+        CK(cudaMemcpyAsync(it.dst, c->h_stage + off, it.n * 8, cudaMemcpyHostToDevice, c->x.stream));
+        off += it.n;
+    }
+    return GOM_OK;
+}
+
+int gom_get_status(gom_ctx *c, gom_status *s, int clear) {
+    if (!c || !s) return GOM_E_ARG;
+    CK(cudaMemcpyAsync(c->h_status, c->x.status, sizeof(gom_status), cudaMemcpyDeviceToHost, c->x.stream));
+    CK(cudaStreamSynchronize(c->x.stream));
+    *s = *c->h_status;
+    if (clear) {
+        CK(cudaMemsetAsync(c->x.status, 0, sizeof(gom_status), c->x.stream));
+        CK(cudaStreamSynchronize(c->x.stream));
+        std::memset(c->h_status, 0, sizeof(gom_status));
+    }
+    return GOM_OK;
+}
+
+int gom_synchronize(gom_ctx *c) {
+    if (!c) return GOM_E_ARG;
+    CK(cudaStreamSynchronize(c->x.stream));
+    return GOM_OK;
+}
+
+int64_t gom_pcg_iterations_total(gom_ctx *c) { return c ? c->pcg_total : 0; }
+
+void *gom_stream(gom_ctx *c) { return c ? (void *)c->x.stream : nullptr; }
+
+int gom_step_bottom_friction(gom_ctx *c) { return run_phase(c, launch_bottom_friction); }
+int gom_step_boundary_velocity(gom_ctx *c) { return run_phase(c, launch_boundary_velocity); }
+int gom_step_advection(gom_ctx *c) { return run_phase(c, launch_advection); }
+int gom_step_momentum(gom_ctx *c) { return run_phase(c, launch_momentum); }
+int gom_step_velocities(gom_ctx *c) { return run_phase(c, launch_velocities); }
+int gom_step_layers(gom_ctx *c) { return run_phase(c, launch_layers); }
+int gom_step_node_velocity(gom_ctx *c) { return run_phase(c, launch_node_velocity); }
+int gom_step_transport(gom_ctx *c) { return run_phase(c, launch_transport); }
+int gom_step_density(gom_ctx *c) { return run_phase(c, launch_density); }
+
+int gom_step_free_surface(gom_ctx *c, int32_t *pcg_iters) {
+    if (!c) return GOM_E_ARG;
+    CK(launch_free_surface(c->x));
+    return finish(c, pcg_iters, true);
+}
+
+int gom_step_swap(gom_ctx *c) {
+    if (!c) return GOM_E_ARG;
+    CK(enqueue_swap(c));
+    return finish(c, nullptr, false);
+}
+
+int gom_step_all(gom_ctx *c, int32_t *pcg_iters) {
+    if (!c) return GOM_E_ARG;
+    // The timestep is captured once into a CUDA graph and replayed: every kernel argument is a
+    // device pointer or a constant of the context, and per-step forcing lives in device memory.
+    if (!c->graph && !c->graph_failed) {
+        cudaGraph_t gr = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(c->x.stream, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            cudaError_t e2 = enqueue_step(c);
+            e = cudaStreamEndCapture(c->x.stream, &gr);
+            if (e2 != cudaSuccess) e = e2;
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&c->graph, gr, 0);
+        if (gr) cudaGraphDestroy(gr);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            c->graph_failed = true;
+            c->graph = nullptr;
+            c->msg = std::string("graph capture unavailable: ") + cudaGetErrorString(e);
+        }
+    }
+    if (c->graph) CK(cudaGraphLaunch(c->graph, c->x.stream));
+    else CK(enqueue_step(c));
+    return finish(c, pcg_iters, true);
+}
+
+int gom_conservation(gom_ctx *c, double *volume, double *salt_mass) {
+    if (!c) return GOM_E_ARG;
+    CK(launch_conservation(c->x));
+    CK(cudaMemcpyAsync(c->h_cons, c->x.w.cons, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->x.stream));
+    CK(cudaStreamSynchronize(c->x.stream));
+    if (volume) *volume = c->h_cons[0];
+    if (salt_mass) *salt_mass = c->h_cons[1];
+    return GOM_OK;
+}
+
+}  // extern "C"

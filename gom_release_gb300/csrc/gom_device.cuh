@@ -1,0 +1,144 @@
+// gom_device.cuh -- device-side data views and helpers shared by the GOM core kernels.
+//
+// Memory layout is that of the Fortran module arrays (include/gom_core.h): every cell, face and
+// node column is contiguous over its layers, so one warp staging a batch of columns reads
+// contiguous bytes.  Entity indices stay 1-based as in the reference connectivity.
+//
+// Floating point: the library is compiled with -fmad=false and IEEE division/square root, so
+// each expression below rounds exactly like the serial FP64 restatement of the reference.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/gom_core.h"
+
+#define GOM_MAXL 64          // largest n_layers a context accepts
+#define GOM_MAXNB 16         // largest max_no_neighbor_node a context accepts
+
+namespace gom {
+
+__host__ __device__ inline double F(float x) { return (double)x; }
+
+// -------------------------------------------------------------------- static geometry (device)
+struct Geom {
+    int NC, NF, NN, L, NB, NOB, NQB;
+    // nodes
+    const double *x_node, *y_node, *h_node;
+    const int *adj_cells_at_node, *adj_cellnum_at_node, *node_count_each_element;
+    const int *adj_nodes_at_node, *adj_nodenum_at_node, *bottom_node, *initial_wetdry_node;
+    // cells
+    const double *x_cell, *y_cell, *h_cell, *area;
+    const int *tri_or_quad, *nodenum_at_cell, *facenum_at_cell, *adj_cellnum_at_cell, *sign_in_outflow;
+    const int *bottom_cell, *ob_element_flag, *qb_element_flag;
+    // faces
+    const double *x_face, *y_face, *h_face, *face_length, *delta_j, *cos_theta, *sin_theta, *cos_theta2,
+        *sin_theta2, *coriolis_factor, *manning, *bf_height;
+    const int *adj_cellnum_at_face, *nodenum_at_face, *bottom_face, *boundary_type_of_face, *isflowside3;
+    // boundaries / vertical grid
+    const int *ob_cell_id, *qb_cell, *qb_face;
+    const double *z_level, *delta_z;
+
+    // 1-based accessors of the (m, N) connectivity arrays
+    __device__ __forceinline__ int cell_node(int l, int i) const { return nodenum_at_cell[(i - 1) * 4 + l - 1]; }
+    __device__ __forceinline__ int cell_face(int l, int i) const { return facenum_at_cell[(i - 1) * 4 + l - 1]; }
+    __device__ __forceinline__ int cell_adj(int l, int i) const { return adj_cellnum_at_cell[(i - 1) * 4 + l - 1]; }
+    __device__ __forceinline__ int cell_sign(int l, int i) const { return sign_in_outflow[(i - 1) * 4 + l - 1]; }
+    __device__ __forceinline__ int face_cell(int l, int j) const { return adj_cellnum_at_face[(j - 1) * 2 + l - 1]; }
+    __device__ __forceinline__ int face_node(int l, int j) const { return nodenum_at_face[(j - 1) * 2 + l - 1]; }
+    __device__ __forceinline__ int node_cell(int l, int i) const { return adj_cellnum_at_node[(i - 1) * NB + l - 1]; }
+    __device__ __forceinline__ int node_count(int l, int i) const { return node_count_each_element[(i - 1) * NB + l - 1]; }
+    __device__ __forceinline__ int node_nb(int l, int i) const { return adj_nodenum_at_node[(i - 1) * (NB + 1) + l]; }
+};
+
+// -------------------------------------------------------------------- state (device)
+struct State {
+    double *eta_cell, *eta_cell_new, *eta_node;
+    int *wetdry_node;
+    double *un_face, *vn_face, *un_face_new, *vn_face_new, *un_elm, *vn_elm;
+    double *wn_cell, *wn_cell_new, *u_node, *v_node, *w_node, *u_face_level, *v_face_level;
+    double *dz_cell, *dz_cell_new, *dzhalf_cell, *dzhalf_cell_new;
+    double *dz_face, *dz_face_new, *dzhalf_face, *dzhalf_face_new;
+    double *dz_node, *dz_node_new, *dzhalf_node, *dzhalf_node_new;
+    int *top_cell, *top_face, *top_node;
+    double *ainvg1, *ainvg2, *ainvdz1, *ainvdz2, *kh, *av, *kv;
+    double *salt_cell, *salt_cell_new, *temp_cell, *temp_cell_new, *salt_node, *temp_node, *salt_face, *temp_face;
+    double *rho_cell, *rho_node, *rho_face;
+    int *num_sub_elm;
+    double *cdb, *gamma_b, *qu_boundary;
+    int *elm_foot, *elm_near_edge;
+};
+
+// per-step forcing (device copies)
+struct Forcing {
+    const double *scal;   // [elapsed_time, spinup_tide, spinup_baroclinic] in device memory
+    const double *eta_at_ob_old, *eta_at_ob_new, *q_add, *wind_stress_normal, *wind_stress_tangnt, *gamma_t, *air_p,
+        *con_at_ob, *con_at_qb, *phi_sw;
+};
+
+// scalar parameters
+struct Params {
+    double gravity, rho_o, msl, dt, theta, adv_onoff_depth, von_karman, cd_const, dry_depth, smagorinsky, ah_0,
+        kh_0, error_tolerance, delta_z_min, denominator_min_for_matrix;
+    int advection_flag, elm_backtrace_flag, elm_sub_iter, elm_min_iter, elm_max_iter, bf_flag, baroclinic_flag,
+        ana_density, max_iteration_pcg, transport_flag, trans_sub_iter, h_flux_limiter, v_flux_limiter, is_salt,
+        is_temp, heat_option;
+};
+
+// -------------------------------------------------------------------- layer indexing
+// (1:L, N) arrays
+__device__ __forceinline__ long ix(int k, int e, int L) { return (long)(e - 1) * L + (k - 1); }
+// (0:L, N) arrays
+__device__ __forceinline__ long ix0(int k, int e, int L) { return (long)(e - 1) * (L + 1) + k; }
+
+// -------------------------------------------------------------------- error status
+__device__ inline void record_error(gom_status *st, int code, int site, int entity, int layer, double value) {
+    if (atomicCAS(&st->code, 0, code) == 0) {
+        st->site = site;
+        st->entity = entity;
+        st->layer = layer;
+        st->value = value;
+    }
+}
+
+__device__ __forceinline__ bool failed(const gom_status *st) { return *(volatile const int *)&st->code != 0; }
+
+// -------------------------------------------------------------------- geometry helpers
+// mod_function_library.f90:49-60
+__device__ __forceinline__ double calculate_area(double x1, double x2, double x3, double y1, double y2, double y3) {
+    return fabs((x1 - x3) * (y2 - y3) - (x2 - x3) * (y1 - y3)) / 2.0;
+}
+
+// set_geometry_1.f90:48-63
+__device__ __forceinline__ int start_end_node(int k, int i, int j) {
+    int v = i + j;
+    return v > k ? v - k : v;
+}
+
+// tridiagonal_solver.f90:15-61, one right-hand side held in registers/local memory.
+// Returns false on a zero pivot.
+template <int NRHS>
+__device__ inline bool thomas(int n, const double *a, const double *b, const double *c, double (*rhs)[NRHS],
+                              double *gam) {
+    if (b[0] == 0.0) return false;
+    double den = b[0];
+#pragma unroll
+    for (int r = 0; r < NRHS; ++r) rhs[0][r] = rhs[0][r] / den;
+    for (int j = 1; j < n; ++j) {
+        gam[j] = c[j - 1] / den;
+        den = b[j] - a[j] * gam[j];
+        if (den == 0.0) return false;
+#pragma unroll
+        for (int r = 0; r < NRHS; ++r) rhs[j][r] = (rhs[j][r] - a[j] * rhs[j - 1][r]) / den;
+    }
+    for (int j = n - 2; j >= 0; --j) {
+#pragma unroll
+        for (int r = 0; r < NRHS; ++r) rhs[j][r] = rhs[j][r] - gam[j + 1] * rhs[j + 1][r];
+    }
+    return true;
+}
+
+// -------------------------------------------------------------------- launch helpers
+inline int blocks_for(long n, int threads) { return (int)((n + threads - 1) / threads); }
+
+}  // namespace gom

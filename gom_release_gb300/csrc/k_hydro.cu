@@ -1,0 +1,712 @@
+// k_hydro.cu -- bottom friction, river boundary velocity, ELM advection and the per-face momentum
+// tridiagonal solves of GOM's per-timestep core, for sm_103a.
+//
+// References (GOM_Rv1.1.0/source):
+//   calculate_bottom_friction.f90:9-73, compute_boundary_velocity.f90:60-94,
+//   solve_nonlinear_advection.f90:14-204, ELM_backtrace_v1.f90:15-200,
+//   search_straight_line.f90:15-399, check_intersection.f90:14-50,
+//   bilinear_interpolation.f90:8-121, solve_momentum_equation.f90:15-656,
+//   tridiagonal_solver.f90:15-90.
+#include "gom_launch.h"
+
+namespace gom {
+
+// ============================================================================================
+// calculate_bottom_friction.f90:21-63; bf_flag 3 is the constant-Cd extension. One thread per face.
+__global__ void k_bottom_friction(Geom g, State s, Params p) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (j > g.NF) return;
+    const int L = g.L;
+    double cdb = 0.0, gb = 0.0;
+    double hf = g.h_face[j - 1];
+    if (p.bf_flag >= 1 && p.bf_flag <= 3 && hf > p.dry_depth) {
+        int k = g.bottom_face[j - 1];
+        if (p.bf_flag == 1) {
+            double hr = fmax(1.0, hf);
+            double chezy = pow(hr, 1.0 / 6.0) / g.manning[j - 1];
+            cdb = p.gravity / (chezy * chezy);
+        } else if (p.bf_flag == 2) {
+            double lg = log(fmax(0.5, s.dzhalf_face[ix0(k - 1, j, L)]) / g.bf_height[j - 1]);
+            cdb = p.von_karman * p.von_karman / (lg * lg);
+        } else {
+            cdb = p.cd_const;
+        }
+        double u = s.un_face[ix(k, j, L)], v = s.vn_face[ix(k, j, L)];
+        gb = cdb * sqrt(u * u + v * v);
+    }
+    s.cdb[j - 1] = cdb;
+    s.gamma_b[j - 1] = gb;
+}
+
+cudaError_t launch_bottom_friction(const Launch &x) {
+    k_bottom_friction<<<blocks_for(x.g.NF, 256), 256, 0, x.stream>>>(x.g, x.s, x.p);
+    return cudaGetLastError();
+}
+
+// compute_boundary_velocity.f90:71-92. One thread per river cell.
+__global__ void k_boundary_velocity(Geom g, State s, Forcing f, Params p, gom_status *st) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (i > g.NQB) return;
+    int j = g.qb_face[i - 1];
+    int n1 = g.face_node(1, j), n2 = g.face_node(2, j);
+    double depth = g.h_face[j - 1] + (s.eta_node[n1 - 1] + s.eta_node[n2 - 1]) * 0.5;
+    if (depth < p.dry_depth) {
+        record_error(st, GOM_E_DRY, 80, i, 0, depth);
+        return;
+    }
+    s.qu_boundary[i - 1] = -f.q_add[i - 1] / (g.face_length[j - 1] * depth);
+}
+
+cudaError_t launch_boundary_velocity(const Launch &x) {
+    if (x.g.NQB == 0) return cudaSuccess;
+    k_boundary_velocity<<<blocks_for(x.g.NQB, 128), 128, 0, x.stream>>>(x.g, x.s, x.f, x.p, x.status);
+    return cudaGetLastError();
+}
+
+// ============================================================================================
+// ELM
+// check_intersection.f90:14-50
+__device__ __forceinline__ int check_intersection(double x1, double x2, double x3, double x4, double y1, double y2,
+                                                  double y3, double y4, double &xin, double &yin) {
+    double delta = (x2 - x1) * (y3 - y4) - (y2 - y1) * (x3 - x4);
+    double delta1 = (x3 - x1) * (y3 - y4) - (y3 - y1) * (x3 - x4);
+    double delta2 = (x2 - x1) * (y3 - y1) - (y2 - y1) * (x3 - x1);
+    if (delta != 0.0) {
+        double tt1 = delta1 / delta;
+        double tt2 = delta2 / delta;
+        if (tt1 >= -0.0 && tt1 <= 1.0 && tt2 >= -0.0 && tt2 <= 1.0) {
+            xin = x1 + (x2 - x1) * tt1;
+            yin = y1 + (y2 - y1) * tt1;
+            return 1;
+        }
+    }
+    return 0;
+}
+
+// bilinear_interpolation.f90:8-121: returns 0 or GOM_ELM_BILINEAR
+__device__ int bilinear_interpolation(double x1, double x2, double x3, double x4, double y1, double y2, double y3,
+                                      double y4, double x, double y, double shapef[4]) {
+    const double small3 = F(1.e-5f), small_06 = F(1.e-6f), b11 = F(1.1f);
+    double xi = 0.0, eta = 0.0;
+    double x0 = (x1 + x2 + x3 + x4) / 4.0;
+    double y0 = (y1 + y2 + y3 + y4) / 4.0;
+    double axi0 = x2 - x1 + x3 - x4, axi1 = y2 - y1 + y3 - y4;
+    double aet0 = x3 + x4 - x1 - x2, aet1 = y3 + y4 - y1 - y2;
+    double bxy0 = x1 - x2 + x3 - x4, bxy1 = y1 - y2 + y3 - y4;
+    double dxi = 2.0 * ((x3 - x4) * (y1 - y2) - (y3 - y4) * (x1 - x2));
+    double deta = 2.0 * ((x4 - x1) * (y3 - y2) - (y4 - y1) * (x3 - x2));
+    if ((fabs(bxy0) < small3 && fabs(bxy1) < small3) || (fabs(dxi) < small3 && fabs(deta) < small3)) {
+        double dd = axi0 * aet1 - axi1 * aet0;
+        if (dd == 0.0) return GOM_ELM_BILINEAR;
+        xi = 4.0 * (aet1 * (x - x0) - aet0 * (y - y0)) / dd;
+        eta = 4.0 * (axi0 * (y - y0) - axi1 * (x - x0)) / dd;
+    } else if (fabs(dxi) < small3 && fabs(deta) >= small3) {
+        eta = 4.0 * (bxy1 * (x - x0) - bxy0 * (y - y0)) / deta;
+        double t1 = axi0 + eta * bxy0, t2 = axi1 + eta * bxy1;
+        double dd = t1 * t1 + t2 * t2;
+        if (dd == 0.0) return GOM_ELM_BILINEAR;
+        xi = ((4.0 * (x - x0) - eta * aet0) * (axi0 + eta * bxy0) + (4.0 * (y - y0) - eta * aet1) * (axi1 + eta * bxy1)) / dd;
+    } else if (fabs(dxi) >= small3 && fabs(deta) < small3) {
+        xi = 4.0 * (bxy1 * (x - x0) - bxy0 * (y - y0)) / dxi;
+        double t1 = aet0 + xi * bxy0, t2 = aet1 + xi * bxy1;
+        double dd = t1 * t1 + t2 * t2;
+        if (dd == 0.0) return GOM_ELM_BILINEAR;
+        eta = ((4.0 * (x - x0) - xi * axi0) * (aet0 + xi * bxy0) + (4.0 * (y - y0) - xi * axi1) * (aet1 + xi * bxy1)) / dd;
+    } else {
+        double beta = aet1 * axi0 - aet0 * axi1 - 4 * (bxy1 * (x - x0) - bxy0 * (y - y0));
+        double gamma = 4.0 * (aet0 * (y - y0) - aet1 * (x - x0));
+        double delta = beta * beta - 4 * gamma * dxi;
+        if (delta == 0.0) {
+            xi = -beta / 2 / dxi;
+            eta = (4.0 * (bxy1 * (x - x0) - bxy0 * (y - y0)) - xi * dxi) / deta;
+        } else if (delta > 0) {
+            double sq = sqrt(delta);
+            double rx[2] = {(-beta + sq) / 2 / dxi, (-beta - sq) / 2 / dxi};
+            int icount = 0;
+            for (int i = 0; i < 2; ++i) {
+                double re = (4 * (bxy1 * (x - x0) - bxy0 * (y - y0)) - rx[i] * dxi) / deta;
+                if (fabs(rx[i]) <= b11 && fabs(re) <= b11) {
+                    xi = rx[i];
+                    eta = re;
+                    icount = icount + 1;
+                }
+            }
+            if (!(icount == 2 && fabs(rx[0] - rx[1]) < small_06) && icount != 1) return GOM_ELM_BILINEAR;
+        } else {
+            return GOM_ELM_BILINEAR;
+        }
+    }
+    if (fabs(xi) > b11 || fabs(eta) > b11) return GOM_ELM_BILINEAR;
+    xi = fmin(1.0, fmax(xi, -1.0));
+    eta = fmin(1.0, fmax(eta, -1.0));
+    shapef[0] = (1 - xi) * (1 - eta) / 4;
+    shapef[1] = (1 + xi) * (1 - eta) / 4;
+    shapef[2] = (1 + xi) * (1 + eta) / 4;
+    shapef[3] = (1 - xi) * (1 + eta) / 4;
+    return 0;
+}
+
+__device__ __forceinline__ int top_el(const State &s, int e) { return e == 0 ? 0 : s.top_cell[e - 1]; }
+
+__device__ __forceinline__ double area_sum(const Geom &g, int nel, double x, double y) {
+    int tq = g.tri_or_quad[nel - 1];
+    double a = 0.0;
+    for (int l = 1; l <= tq; ++l) {
+        int n1 = g.cell_node(l, nel), n2 = g.cell_node(start_end_node(tq, l, 1), nel);
+        a = a + fabs(calculate_area(g.x_node[n1 - 1], g.x_node[n2 - 1], x, g.y_node[n1 - 1], g.y_node[n2 - 1], y));
+    }
+    return a;
+}
+
+// search_straight_line.f90:15-399 (mode 1). Returns 0 or a GOM_ELM_* site.
+__device__ int search_straight_line(const Geom &g, const State &s, const Params &p, int &nnel, int &jlev, double time,
+                                    double x0, double y0, double z0, double &xt, double &yt, double &zt, int &nfl) {
+    const double small_06 = F(1.e-6f);
+    const double MSL = p.msl;
+    const int L = g.L;
+    if (top_el(s, nnel) == 0 || MSL - g.h_cell[nnel - 1] > MSL + s.eta_cell[nnel - 1]) return GOM_ELM_START_DRY;
+    nfl = 0;
+    double trm = time;
+    int nel = nnel;
+    double area1 = area_sum(g, nel, x0, y0);
+    double area2 = area_sum(g, nel, xt, yt);
+    double ar = g.area[nel - 1];
+    double ae = fabs(area1 - ar) / ar;
+    if (ae > small_06) return GOM_ELM_START_OUTSIDE;
+    ae = fabs(area2 - ar) / ar;
+    if (!(ae < small_06)) {
+        const double c1 = 1.0 - 1.0e-4;
+        double xcg = c1 * x0 + 1.0e-4 * g.x_cell[nel - 1];
+        double ycg = c1 * y0 + 1.0e-4 * g.y_cell[nel - 1];
+        double pathl = sqrt((xt - xcg) * (xt - xcg) + (yt - ycg) * (yt - ycg));
+        if ((xcg == xt && ycg == yt) || pathl == 0.0) return GOM_ELM_ZERO_PATH;
+        int iflag = 0, nel_j = 0;
+        double xin = 0.0, yin = 0.0;
+        int tq = g.tri_or_quad[nel - 1];
+        for (int l = 1; l <= tq; ++l) {
+            int jd1 = g.cell_node(start_end_node(tq, l, 1), nel);
+            int jd2 = g.cell_node(start_end_node(tq, l, 2), nel);
+            iflag = check_intersection(xcg, xt, g.x_node[jd1 - 1], g.x_node[jd2 - 1], ycg, yt, g.y_node[jd1 - 1],
+                                       g.y_node[jd2 - 1], xin, yin);
+            if (iflag == 1) {
+                nel_j = l;
+                break;
+            }
+        }
+        if (iflag == 0) return GOM_ELM_NO_FIRST_EDGE;
+        double zin = z0;
+        int iteration = 0;
+        for (;;) {
+            iteration = iteration + 1;
+            if (iteration > 1000) {
+                nfl = 1;
+                xt = xin;
+                yt = yin;
+                zt = zin;
+                nnel = nel;
+                break;
+            }
+            int tqn = g.tri_or_quad[nel - 1];
+            int md1 = g.cell_node(start_end_node(tqn, nel_j, 1), nel);
+            int md2 = g.cell_node(start_end_node(tqn, nel_j, 2), nel);
+            double dist = sqrt((xin - xt) * (xin - xt) + (yin - yt) * (yin - yt));
+            if (dist / pathl > 1.0 + 1.0e-4) return GOM_ELM_OVERSHOOT;
+            zin = zt - dist / pathl * (zt - zin);
+            trm = trm * dist / pathl;
+            pathl = sqrt((xin - xt) * (xin - xt) + (yin - yt) * (yin - yt));
+            if (pathl == 0.0 || trm == 0.0) return GOM_ELM_ZERO_REMAIN;
+            int adjc = g.cell_adj(nel_j, nel);
+            if (adjc == 0 || top_el(s, adjc) == 0) {
+                int isd = g.cell_face(nel_j, nel);
+                if (g.face_node(1, isd) + g.face_node(2, isd) != md1 + md2) return GOM_ELM_FACE_MISMATCH;
+                xin = c1 * xin + 1.0e-4 * g.x_cell[nel - 1];
+                yin = c1 * yin + 1.0e-4 * g.y_cell[nel - 1];
+                nfl = 1;
+                xt = xin;
+                yt = yin;
+                zt = zin;
+                nnel = nel;
+                break;
+            }
+            nel = adjc;
+            ar = g.area[nel - 1];
+            area1 = area_sum(g, nel, xt, yt);
+            ae = fabs(area1 - ar) / ar;
+            if (ae < small_06) {
+                nnel = nel;
+                break;
+            }
+            tqn = g.tri_or_quad[nel - 1];
+            bool found = false;
+            for (int l = 1; l <= tqn; ++l) {
+                int jd1 = g.cell_node(start_end_node(tqn, l, 1), nel);
+                int jd2 = g.cell_node(start_end_node(tqn, l, 2), nel);
+                if ((jd1 == md1 && jd2 == md2) || (jd2 == md1 && jd1 == md2)) continue;
+                iflag = check_intersection(xcg, xt, g.x_node[jd1 - 1], g.x_node[jd2 - 1], ycg, yt, g.y_node[jd1 - 1],
+                                           g.y_node[jd2 - 1], xin, yin);
+                if (iflag == 1) {
+                    nel_j = l;
+                    found = true;
+                    break;
+                }
+            }
+            if (found) continue;
+            if (iflag == 0) return GOM_ELM_NO_NEXT_EDGE;
+        }
+    } else {
+        nnel = nel;
+    }
+    if (top_el(s, nnel) == 0 || MSL - g.h_cell[nnel - 1] > MSL + s.eta_cell[nnel - 1]) return GOM_ELM_END_DRY;
+    zt = fmin(fmax(zt, MSL - g.h_cell[nnel - 1]), MSL + s.eta_cell[nnel - 1]);
+    if (zt <= g.z_level[0] || zt > g.z_level[L]) return GOM_ELM_Z_RANGE;
+    for (int k = 0; k <= L - 1; ++k) {
+        if (zt > g.z_level[k] && zt <= g.z_level[k + 1]) {
+            jlev = k + 1;
+            break;
+        }
+    }
+    jlev = min(max(jlev, g.bottom_cell[nnel - 1]), top_el(s, nnel));
+    return 0;
+}
+
+__device__ double edge_distance(const Geom &g, int nel, double x, double y) {
+    double dmin = 1e300;
+    int tq = g.tri_or_quad[nel - 1];
+    for (int l = 1; l <= tq; ++l) {
+        int a = g.cell_node(l, nel), b = g.cell_node(start_end_node(tq, l, 1), nel);
+        double ex = g.x_node[b - 1] - g.x_node[a - 1], ey = g.y_node[b - 1] - g.y_node[a - 1];
+        double len = sqrt(ex * ex + ey * ey);
+        double cr = fabs(ex * (y - g.y_node[a - 1]) - ey * (x - g.x_node[a - 1])) / len;
+        dmin = fmin(dmin, cr);
+    }
+    return dmin;
+}
+
+// ELM_backtrace_v1.f90:40-200 (mode 1)
+__device__ int elm_backtrace(const Geom &g, const State &s, const Params &p, int bt_step, double bt_dt, double &uu,
+                             double &vv, double &ww, double x0, double y0, double z0, int &nnel, int &jlev,
+                             int &near_edge) {
+    const double small_06 = F(1.e-6f);
+    const int L = g.L;
+    for (int idt = 1; idt <= bt_step; ++idt) {
+        double xt = x0 - bt_dt * uu;
+        double yt = y0 - bt_dt * vv;
+        double zt = z0 - bt_dt * ww;
+        int nfl = 0;
+        int e = search_straight_line(g, s, p, nnel, jlev, bt_dt, x0, y0, z0, xt, yt, zt, nfl);
+        if (e) return e;
+        int tq = g.tri_or_quad[nnel - 1];
+        double zup = (jlev == s.top_cell[nnel - 1]) ? p.msl + s.eta_cell[nnel - 1] : g.z_level[jlev];
+        if (zt > zup) return GOM_ELM_Z_ABOVE;
+        double zrat = (zup - zt) / s.dz_cell[ix(jlev, nnel, L)];
+        double vxn[4], vyn[4], vzn[4], sta[4];
+        for (int l = 1; l <= tq; ++l) {
+            int nd = g.cell_node(l, nnel);
+            long i1 = ix0(jlev - 1, nd, L), i2 = ix0(jlev, nd, L);
+            vxn[l - 1] = s.u_node[i2] * (1 - zrat) + s.u_node[i1] * zrat;
+            vyn[l - 1] = s.v_node[i2] * (1 - zrat) + s.v_node[i1] * zrat;
+            vzn[l - 1] = s.w_node[i2] * (1 - zrat) + s.w_node[i1] * zrat;
+        }
+        int n1 = g.cell_node(1, nnel), n2 = g.cell_node(2, nnel), n3 = g.cell_node(3, nnel);
+        double X1 = g.x_node[n1 - 1], X2 = g.x_node[n2 - 1], X3 = g.x_node[n3 - 1];
+        double Y1 = g.y_node[n1 - 1], Y2 = g.y_node[n2 - 1], Y3 = g.y_node[n3 - 1];
+        double ar = g.area[nnel - 1];
+        if (tq == 3) {
+            sta[0] = calculate_area(xt, X2, X3, yt, Y2, Y3) / ar;
+            sta[1] = calculate_area(X1, xt, X3, Y1, yt, Y3) / ar;
+            sta[2] = calculate_area(X1, X2, xt, Y1, Y2, yt) / ar;
+            sta[0] = fmax(0.0, fmin(1.0, sta[0]));
+            sta[1] = fmax(0.0, fmin(1.0, sta[1]));
+            if (sta[0] + sta[1] > 1) {
+                sta[2] = 0;
+                sta[1] = 1.0 - sta[0];
+            } else {
+                sta[2] = 1.0 - sta[0] - sta[1];
+            }
+        } else {
+            int n4 = g.cell_node(4, nnel);
+            double X4 = g.x_node[n4 - 1], Y4 = g.y_node[n4 - 1];
+            double aa1 = calculate_area(X1, X2, xt, Y1, Y2, yt);
+            double aa2 = calculate_area(X2, X3, xt, Y2, Y3, yt);
+            double aa3 = calculate_area(X3, X4, xt, Y3, Y4, yt);
+            double aa4 = calculate_area(X4, X1, xt, Y4, Y1, yt);
+            double aa = fabs(aa1) + fabs(aa2) + fabs(aa3) + fabs(aa4);
+            if (fabs(aa - ar) / ar > small_06) return GOM_ELM_QUAD_OUTSIDE;
+            int b = bilinear_interpolation(X1, X2, X3, X4, Y1, Y2, Y3, Y4, xt, yt, sta);
+            if (b) return b;
+        }
+        uu = 0.0;
+        vv = 0.0;
+        ww = 0.0;
+        for (int j = 0; j < tq; ++j) {
+            uu = uu + vxn[j] * sta[j];
+            vv = vv + vyn[j] * sta[j];
+            ww = ww + vzn[j] * sta[j];
+        }
+        if (edge_distance(g, nnel, xt, yt) < 1e-12) near_edge = 1;
+        if (nfl == 1) break;
+        x0 = xt;
+        y0 = yt;
+        z0 = zt;
+    }
+    return 0;
+}
+
+// solve_nonlinear_advection.f90:52-87: one thread per (node, layer)
+__global__ void k_elm_substeps(Geom g, State s, Params p) {
+    long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int L = g.L;
+    if (t >= (long)g.NN * L) return;
+    int i = (int)(t / L) + 1, k = (int)(t % L) + 1;
+    const double dt = p.dt;
+    int nadj = g.adj_cells_at_node[i - 1];
+    double xi = g.x_node[i - 1], yi = g.y_node[i - 1];
+    double ui = (s.u_node[ix0(k, i, L)] + s.u_node[ix0(k - 1, i, L)]) * 0.5;
+    double vi = (s.v_node[ix0(k, i, L)] + s.v_node[ix0(k - 1, i, L)]) * 0.5;
+    double wi = (s.w_node[ix0(k, i, L)] + s.w_node[ix0(k - 1, i, L)]) * 0.5;
+    int iw = (int)(2 * wi * dt / p.delta_z_min);
+    double summ = 0.0;
+    for (int j = 1; j <= nadj; ++j) {
+        int ie = g.node_cell(j, i), id = g.node_count(j, i);
+        int tq = g.tri_or_quad[ie - 1];
+        double devm = 0.0;
+        for (int l = 1; l <= 2; ++l) {
+            int nd = g.cell_node(l == 1 ? start_end_node(tq, id, 1) : start_end_node(tq, id, tq - 1), ie);
+            double dx = xi - g.x_node[nd - 1], dy = yi - g.y_node[nd - 1];
+            double rl = sqrt(dx * dx + dy * dy);
+            double u2 = (s.u_node[ix0(k, nd, L)] + s.u_node[ix0(k - 1, nd, L)]) * 0.5;
+            double v2 = (s.v_node[ix0(k, nd, L)] + s.v_node[ix0(k - 1, nd, L)]) * 0.5;
+            double du = ui - u2, dv = vi - v2;
+            double dev = sqrt(du * du + dv * dv) / rl * dt;
+            if (dev > devm) devm = dev;
+        }
+        int idelta = max((int)(devm / F(1.e-1f)), iw);
+        summ = summ + (double)idelta / nadj;
+    }
+    s.num_sub_elm[ix(k, i, L)] = max(p.elm_min_iter, min(p.elm_max_iter, (int)summ));
+}
+
+// solve_nonlinear_advection.f90:94-201: one thread per (face, layer)
+__global__ void k_elm_faces(Geom g, State s, Params p, gom_status *st) {
+    long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int L = g.L;
+    if (t >= (long)g.NF * L) return;
+    int j = (int)(t / L) + 1, k = (int)(t % L) + 1;
+    long o = ix(k, j, L);
+    int b = g.bottom_face[j - 1], tf = s.top_face[j - 1];
+    double unf = s.un_face[o], vnf = s.vn_face[o];
+    s.elm_foot[o] = 0;
+    s.elm_near_edge[o] = 0;
+    if (k < b || k > tf) {
+        s.un_elm[o] = 0.0;
+        s.vn_elm[o] = 0.0;
+        return;
+    }
+    int n1 = g.face_node(1, j), n2 = g.face_node(2, j);
+    if (fabs(fmax(g.h_node[n1 - 1], g.h_node[n2 - 1])) < p.adv_onoff_depth) {
+        s.un_elm[o] = unf;
+        s.vn_elm[o] = vnf;
+        return;
+    }
+    int a1 = g.face_cell(1, j), a2 = g.face_cell(2, j);
+    int ie0;
+    if (s.top_cell[a1 - 1] != 0) ie0 = a1;
+    else if (a2 != 0 && s.top_cell[a2 - 1] != 0) ie0 = a2;
+    else {
+        s.un_elm[o] = unf;
+        s.vn_elm[o] = vnf;
+        return;
+    }
+    int nnel = ie0, jlev = k;
+    double ct = g.cos_theta[j - 1], sn = g.sin_theta[j - 1];
+    double x0 = g.x_face[j - 1], y0 = g.y_face[j - 1], z0;
+    if (k == s.top_cell[nnel - 1]) z0 = p.msl + s.eta_cell[nnel - 1] - s.dz_cell[ix(k, nnel, L)] * 0.5;
+    else z0 = g.z_level[k] - s.dz_cell[ix(k, nnel, L)] * 0.5;
+    double uu = unf * ct - vnf * sn;
+    double vv = unf * sn + vnf * ct;
+    double wdown = (s.w_node[ix0(k - 1, n1, L)] + s.w_node[ix0(k - 1, n2, L)]) * 0.5;
+    double wup = (s.w_node[ix0(k, n1, L)] + s.w_node[ix0(k, n2, L)]) * 0.5;
+    double ww = (wdown + wup) * 0.5;
+    double vmag = sqrt(uu * uu + vv * vv + ww * ww);
+    if (vmag <= F(1.e-4f)) {
+        s.un_elm[o] = unf;
+        s.vn_elm[o] = vnf;
+        return;
+    }
+    int bt_step = (int)((double)(s.num_sub_elm[ix(k, n1, L)] + s.num_sub_elm[ix(k, n2, L)]) * 0.5);
+    double bt_dt = p.dt / bt_step;
+    int near = 0;
+    int e = elm_backtrace(g, s, p, bt_step, bt_dt, uu, vv, ww, x0, y0, z0, nnel, jlev, near);
+    if (e) {
+        record_error(st, GOM_E_ELM, e, j, k, 0.0);
+        return;
+    }
+    s.elm_foot[o] = nnel;
+    s.elm_near_edge[o] = near;
+    s.un_elm[o] = uu * ct + vv * sn;
+    s.vn_elm[o] = -uu * sn + vv * ct;
+}
+
+__global__ void k_copy_elm(Geom g, State s) {
+    long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    long n = (long)g.NF * g.L;
+    if (t >= n) return;
+    s.un_elm[t] = s.un_face[t];
+    s.vn_elm[t] = s.vn_face[t];
+    s.elm_foot[t] = 0;
+    s.elm_near_edge[t] = 0;
+}
+
+cudaError_t launch_advection(const Launch &x) {
+    long nfl = (long)x.g.NF * x.g.L;
+    if (x.p.advection_flag == 0) {
+        k_copy_elm<<<blocks_for(nfl, 256), 256, 0, x.stream>>>(x.g, x.s);
+        return cudaGetLastError();
+    }
+    if (x.p.elm_backtrace_flag == 1) {
+        long nnl = (long)x.g.NN * x.g.L;
+        k_elm_substeps<<<blocks_for(nnl, 256), 256, 0, x.stream>>>(x.g, x.s, x.p);
+    }
+    k_elm_faces<<<blocks_for(nfl, 128), 128, 0, x.stream>>>(x.g, x.s, x.p, x.status);
+    return cudaGetLastError();
+}
+
+// ============================================================================================
+// solve_momentum_equation.f90:15-656, one thread per face column.
+//
+// rtemp0 of the reference carries over between faces: on a boundary face whose nodes are not both
+// wet, the air-pressure term at :503-505 reuses the last rtemp0 assigned for an earlier wet face
+// (serial order).  prev_rtemp0() restates that by walking back to the nearest such face.
+__device__ double face_final_rtemp0(const Geom &g, const State &s, const Forcing &f, const Params &p, int j, bool &known) {
+    known = true;
+    int a2 = g.face_cell(2, j);
+    if (a2 != 0) {
+        double t1 = 0.0, t2 = 0.0;
+        int ie = g.face_cell(1, j);
+        int tq = g.tri_or_quad[ie - 1];
+        for (int ll = 1; ll <= tq; ++ll) t1 = t1 + f.air_p[g.cell_node(ll, ie) - 1] / tq;
+        tq = g.tri_or_quad[a2 - 1];
+        for (int ll = 1; ll <= tq; ++ll) t2 = t2 + f.air_p[g.cell_node(ll, a2) - 1] / tq;
+        return -p.dt / p.rho_o * (t2 - t1) / g.delta_j[j - 1];
+    }
+    int n1 = g.face_node(1, j), n2 = g.face_node(2, j);
+    if (s.wetdry_node[n1 - 1] == 0 && s.wetdry_node[n2 - 1] == 0)
+        return p.gravity * p.dt / g.face_length[j - 1] * (1.0 - p.theta) * (s.eta_node[n2 - 1] - s.eta_node[n1 - 1]);
+    known = false;
+    return 0.0;
+}
+
+__device__ double prev_rtemp0(const Geom &g, const State &s, const Forcing &f, const Params &p, int j) {
+    for (int jj = j - 1; jj >= 1; --jj) {
+        if (s.top_face[jj - 1] == 0) continue;
+        bool known;
+        double v = face_final_rtemp0(g, s, f, p, jj, known);
+        if (known) return v;
+    }
+    return 0.0;
+}
+
+__global__ void __launch_bounds__(128) k_momentum(Geom g, State s, Forcing f, Params p, gom_status *st) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (j > g.NF) return;
+    const int L = g.L;
+    int tj = s.top_face[j - 1];
+    if (tj == 0) return;
+    const double dt = p.dt, gravity = p.gravity, theta = p.theta;
+    int bj = g.bottom_face[j - 1];
+    int nvl = tj - bj + 1;
+    int node1 = g.face_node(1, j), node2 = g.face_node(2, j);
+    int a1 = g.face_cell(1, j), a2 = g.face_cell(2, j);
+    int btype = g.boundary_type_of_face[j - 1];
+    const double dj = g.delta_j[j - 1], fl = g.face_length[j - 1];
+    const double ct = g.cos_theta[j - 1], sn = g.sin_theta[j - 1], ct2 = g.cos_theta2[j - 1], sn2 = g.sin_theta2[j - 1];
+    const double cor = g.coriolis_factor[j - 1];
+    double a[GOM_MAXL], bd[GOM_MAXL], cu[GOM_MAXL], gam[GOM_MAXL];
+    double rhs[GOM_MAXL][3];
+    // :120-169
+    for (int k = bj + 1; k <= tj - 1; ++k) {
+        int kk = tj - k + 1;
+        a[kk - 1] = -dt * s.av[ix0(k, j, L)] / s.dzhalf_face[ix0(k, j, L)];
+        cu[kk - 1] = -dt * s.av[ix0(k - 1, j, L)] / s.dzhalf_face[ix0(k - 1, j, L)];
+        bd[kk - 1] = -a[kk - 1] + s.dz_face[ix(k, j, L)] - cu[kk - 1];
+    }
+    if (tj == bj) {
+        bd[0] = s.dz_face[ix(tj, j, L)] + s.gamma_b[j - 1] * dt;
+    } else {
+        cu[0] = -dt * s.av[ix0(tj - 1, j, L)] / s.dzhalf_face[ix0(tj - 1, j, L)];
+        bd[0] = f.gamma_t[j - 1] * dt + s.dz_face[ix(tj, j, L)] - cu[0];
+        a[nvl - 1] = -dt * s.av[ix0(bj, j, L)] / s.dzhalf_face[ix0(bj, j, L)];
+        bd[nvl - 1] = -a[nvl - 1] + s.dz_face[ix(bj, j, L)] + s.gamma_b[j - 1] * dt;
+    }
+    bool wet_nodes = s.wetdry_node[node1 - 1] == 0 && s.wetdry_node[node2 - 1] == 0;
+    double eta_n1 = s.eta_node[node1 - 1], eta_n2 = s.eta_node[node2 - 1];
+    // rtemp0 reaching the air-pressure term of a boundary face
+    double rt0_air;
+    if (a2 != 0) {
+        bool known;
+        rt0_air = face_final_rtemp0(g, s, f, p, j, known);
+    } else if (wet_nodes) {
+        rt0_air = gravity * dt / fl * (1.0 - theta) * (eta_n2 - eta_n1);
+    } else {
+        rt0_air = prev_rtemp0(g, s, f, p, j);
+    }
+    double rtemp3_air = -dt / p.rho_o * ((f.air_p[node2 - 1] - f.air_p[node1 - 1]) / fl);
+    const double c069 = F(0.69f);
+    int ibnd = g.isflowside3[j - 1];
+    double eta1 = s.eta_cell[a1 - 1];
+    double eta2 = a2 != 0 ? s.eta_cell[a2 - 1] : 0.0;
+    int ba1 = g.bottom_cell[a1 - 1], ta1 = s.top_cell[a1 - 1];
+    int ba2 = a2 != 0 ? g.bottom_cell[a2 - 1] : 0, ta2 = a2 != 0 ? s.top_cell[a2 - 1] : 0;
+    int bn1 = g.bottom_node[node1 - 1], tn1 = s.top_node[node1 - 1];
+    int bn2 = g.bottom_node[node2 - 1], tn2 = s.top_node[node2 - 1];
+    for (int k = 1; k <= nvl; ++k) {
+        int kk = tj - k + 1;
+        double dzk = s.dz_face[ix(kk, j, L)];
+        double unk = s.un_face[ix(kk, j, L)], vnk = s.vn_face[ix(kk, j, L)];
+        double G1 = dzk * (s.un_elm[ix(kk, j, L)] + cor * dt * vnk);
+        double G2 = dzk * (s.vn_elm[ix(kk, j, L)] - cor * dt * unk);
+        if (a2 != 0) {
+            // :269-344 Smagorinsky horizontal diffusion
+            double tmp[12];
+            for (int l = 1; l <= 2; ++l) {
+                int nd = g.face_node(l, j);
+                double ut = (s.u_node[ix0(kk, nd, L)] + s.u_node[ix0(kk - 1, nd, L)]) * 0.5;
+                double vt = (s.v_node[ix0(kk, nd, L)] + s.v_node[ix0(kk - 1, nd, L)]) * 0.5;
+                tmp[2 * l - 2] = ut * ct + vt * sn;
+                tmp[2 * l - 1] = -ut * sn + vt * ct;
+            }
+            for (int l = 1; l <= 2; ++l) {
+                int ie = g.face_cell(l, j);
+                int tq = g.tri_or_quad[ie - 1];
+                double ut = 0.0, vt = 0.0;
+                for (int ll = 1; ll <= tq; ++ll) {
+                    int nd = g.cell_node(ll, ie);
+                    ut = ut + (s.u_node[ix0(kk, nd, L)] + s.u_node[ix0(kk - 1, nd, L)]) * 0.5 / tq;
+                    vt = vt + (s.v_node[ix0(kk, nd, L)] + s.v_node[ix0(kk - 1, nd, L)]) * 0.5 / tq;
+                }
+                tmp[2 * l + 2] = ut * ct + vt * sn;
+                tmp[2 * l + 3] = -ut * sn + vt * ct;
+            }
+            double dudx = (tmp[6] - tmp[4]) / dj;
+            double dvdx = (tmp[7] - tmp[5]) / dj;
+            double dudy = (tmp[2] - tmp[0]) / fl;
+            double dvdy = (tmp[3] - tmp[1]) / fl;
+            double sdd = dvdx + dudy;
+            double hdiff = p.smagorinsky * sqrt(dudx * dudx + dvdy * dvdy + 0.5 * (sdd * sdd));
+            double khv = hdiff * g.area[a1 - 1];
+            hdiff = hdiff + p.ah_0;
+            s.kh[ix(k, j, L)] = khv + p.kh_0;
+            double d2udy = 4.0 * (tmp[2] + tmp[0] - 2 * unk) / (fl * fl);
+            double d2vdy = 4.0 * (tmp[3] + tmp[1] - 2 * vnk) / (fl * fl);
+            for (int l = 1; l <= 2; ++l) {
+                int ie = g.face_cell(l, j);
+                double ddx = g.x_cell[ie - 1] - g.x_face[j - 1], ddy = g.y_cell[ie - 1] - g.y_face[j - 1];
+                double rl = sqrt(ddx * ddx + ddy * ddy);
+                tmp[2 * l + 6] = (tmp[2 * l + 2] - unk) / rl;
+                tmp[2 * l + 7] = (tmp[2 * l + 3] - vnk) / rl;
+            }
+            double d2udx = 2.0 * (tmp[8] + tmp[10]) / dj;
+            double d2vdx = 2.0 * (tmp[9] + tmp[11]) / dj;
+            G1 = G1 + dzk * dt * hdiff * (d2udx + d2udy);
+            G2 = G2 + dzk * dt * hdiff * (d2vdx + d2vdy);
+        }
+        // :350-397 barotropic gradients at (1-theta)
+        double rtemp2 = 0.0;
+        if (btype == 0) {
+            double rtemp0 = gravity * dt / dj * (1.0 - theta) * (eta2 - eta1);
+            double rtemp1 = rtemp0 * ct2;
+            rtemp2 = rtemp0 * sn2;
+            G1 = G1 - dzk * rtemp1;
+        } else if (btype > 0) {
+            int ie = g.ob_element_flag[a1 - 1];
+            double rtemp1 = gravity * dt / dj * (1.0 - theta) * (f.eta_at_ob_old[ie - 1] - eta1);
+            G1 = G1 - dzk * rtemp1;
+        } else {
+            G1 = 0.0;
+        }
+        if (wet_nodes) {
+            double rtemp0 = gravity * dt / fl * (1.0 - theta) * (eta_n2 - eta_n1);
+            if (btype == 0) G2 = G2 - dzk * (rtemp0 + rtemp2);
+            else G2 = G2 - dzk * rtemp0;
+        }
+        // :400-471 baroclinic pressure gradient
+        if (p.baroclinic_flag == 1) {
+            double sum1 = 0.0, sum2 = 0.0;
+            for (int k2 = kk; k2 <= tj; ++k2) {
+                double dz2 = s.dz_face[ix(k2, j, L)];
+                if (a2 != 0 && k2 >= ba1 && k2 <= ta1 && k2 >= ba2 && k2 <= ta2) {
+                    double dr = s.rho_cell[ix(k2, a2, L)] - s.rho_cell[ix(k2, a1, L)];
+                    sum1 = sum1 + (k2 == kk ? 0.5 * dr : 1.0 * dr) * dz2;
+                }
+                if (k2 >= bn1 && k2 <= tn1 && k2 >= bn2 && k2 <= tn2) {
+                    double dr = s.rho_node[ix(k2, node2, L)] - s.rho_node[ix(k2, node1, L)];
+                    sum2 = sum2 + (k2 == kk ? 0.5 * dr : 1.0 * dr) * dz2;
+                }
+            }
+            double dzrow = s.dz_face[ix(k, j, L)];   // the reference uses the top-down row here
+            double rtemp1 = dzrow * (-gravity * dt / (p.rho_o * dj)) * sum1;
+            rtemp2 = dzrow * (-gravity * dt / (p.rho_o * fl)) * sum2;
+            double rtemp3 = rtemp1 * ct2;
+            double rtemp4 = rtemp1 * sn2;
+            const double spin = f.scal[2];
+            G1 = G1 + rtemp3 * spin;
+            G2 = G2 + (rtemp2 + rtemp4) * spin;
+        }
+        if (k == 1) {
+            G1 = G1 + dt * f.wind_stress_normal[j - 1];
+            G2 = G2 + dt * f.wind_stress_tangnt[j - 1];
+        }
+        G1 = G1 + c069 * dzk * gravity * dt * 0.0;
+        G2 = G2 + c069 * dzk * gravity * dt * 0.0;
+        // :490-509 air pressure
+        G1 = G1 + dzk * (rt0_air * ct2);
+        G2 = G2 + dzk * (rtemp3_air + rt0_air * sn2);
+        if (btype == -1) G1 = 0.0;
+        if (ibnd > 0) G1 = G1 + dzk * s.qu_boundary[ibnd - 1];
+        rhs[k - 1][0] = G1;
+        rhs[k - 1][1] = G2;
+        rhs[k - 1][2] = dzk;
+    }
+    if (!thomas<3>(nvl, a, bd, cu, rhs, gam)) {
+        record_error(st, GOM_E_ZERO_PIVOT, 587, j, 0, 0.0);
+        return;
+    }
+    bool zero_g1 = (btype == -1 && ibnd == 0);
+    bool zero_dz1 = (btype == -1);
+    for (int k = 1; k <= L; ++k) {
+        long o = ix(k, j, L);
+        if (k <= nvl) {
+            s.ainvg1[o] = zero_g1 ? 0.0 : rhs[k - 1][0];
+            s.ainvg2[o] = rhs[k - 1][1];
+            s.ainvdz1[o] = zero_dz1 ? 0.0 : rhs[k - 1][2];
+            s.ainvdz2[o] = rhs[k - 1][2];
+        } else {
+            s.ainvg1[o] = 0.0;
+            s.ainvg2[o] = 0.0;
+            s.ainvdz1[o] = 0.0;
+            s.ainvdz2[o] = 0.0;
+        }
+    }
+}
+
+__global__ void k_zero_face_columns(Geom g, State s) {
+    // faces that are dry keep zero results (the reference zeroes all four arrays first)
+    long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int L = g.L;
+    if (t >= (long)g.NF * L) return;
+    int j = (int)(t / L) + 1;
+    if (s.top_face[j - 1] != 0) return;
+    s.ainvg1[t] = 0.0;
+    s.ainvg2[t] = 0.0;
+    s.ainvdz1[t] = 0.0;
+    s.ainvdz2[t] = 0.0;
+}
+
+cudaError_t launch_momentum(const Launch &x) {
+    long nfl = (long)x.g.NF * x.g.L;
+    k_zero_face_columns<<<blocks_for(nfl, 256), 256, 0, x.stream>>>(x.g, x.s);
+    k_momentum<<<blocks_for(x.g.NF, 128), 128, 0, x.stream>>>(x.g, x.s, x.f, x.p, x.status);
+    return cudaGetLastError();
+}
+
+}  // namespace gom

@@ -1,0 +1,705 @@
+// k_surface.cu -- theta-scheme free surface (assembly + Jacobi-PCG), node elevations, velocity
+// recovery, layer/wet-dry update and node velocities, for sm_103a.
+//
+// References (GOM_Rv1.1.0/source):
+//   solve_free_surface_equation.f90:17-396, pre_conj_grad.f90:9-230, solve_velocities.f90:8-260,
+//   update_vertical_layers_1.f90:18-333, calculate_velocity_at_node.f90:10-140.
+#include "gom_launch.h"
+
+#include <cooperative_groups.h>
+
+namespace gom {
+
+// ============================================================================================
+// solve_free_surface_equation.f90:65-214: one thread per cell builds its 5-point row and RHS.
+__global__ void k_fs_assemble(Geom g, State s, Forcing f, Params p, double *sparsem, double *rhs, gom_status *st) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (i > g.NC) return;
+    const int L = g.L;
+    const double dt = p.dt, gravity = p.gravity, theta = p.theta;
+    const double gdt2th2 = gravity * (dt * dt) * (theta * theta);
+    int tq = g.tri_or_quad[i - 1];
+    double ar = g.area[i - 1];
+    double diag = ar;
+    double off[4] = {0.0, 0.0, 0.0, 0.0};
+    double r = ar * s.eta_cell[i - 1];
+    int obf = g.ob_element_flag[i - 1];
+    for (int l = 1; l <= tq; ++l) {
+        int j = g.cell_face(l, i);
+        int tj = s.top_face[j - 1];
+        if (tj == 0) continue;
+        int nvl = tj - g.bottom_face[j - 1] + 1;
+        double sdz = 0.0, c1 = 0.0, c2 = 0.0;
+        for (int k = 1; k <= nvl; ++k) {
+            int kk = tj + 1 - k;
+            double dz = s.dz_face[ix(kk, j, L)];
+            sdz = sdz + dz * s.ainvdz1[ix(k, j, L)];
+        }
+        double base = gdt2th2 * g.face_length[j - 1] / g.delta_j[j - 1] * sdz;
+        double coef = base * g.cos_theta2[j - 1];
+        if (coef < 0.0) {
+            record_error(st, GOM_E_NOT_SPD, 100, i, 0, coef);
+            return;
+        }
+        diag = diag + coef;
+        if (g.cell_adj(l, i) != 0) off[l - 1] = -coef;
+        (void)c1;
+        (void)c2;
+    }
+    // RHS (:134-151), computed in a second pass like the reference
+    for (int l = 1; l <= tq; ++l) {
+        int j = g.cell_face(l, i);
+        int tj = s.top_face[j - 1];
+        if (tj == 0) continue;
+        int nvl = tj - g.bottom_face[j - 1] + 1;
+        double c1 = 0.0, c2 = 0.0;
+        for (int k = 1; k <= nvl; ++k) {
+            int kk = tj + 1 - k;
+            double dz = s.dz_face[ix(kk, j, L)];
+            c1 = c1 + dz * s.un_face[ix(kk, j, L)];
+            c2 = c2 + dz * s.ainvg1[ix(k, j, L)];
+        }
+        double sgn = (double)g.cell_sign(l, i);
+        double fl = g.face_length[j - 1];
+        r = r - (1.0 - theta) * dt * sgn * fl * c1 - theta * dt * sgn * fl * c2;
+    }
+    // open-boundary Dirichlet term (:185-212)
+    if (obf > 0) {
+        for (int l = 1; l <= tq; ++l) {
+            int j = g.cell_face(l, i);
+            int tj = s.top_face[j - 1];
+            if (g.boundary_type_of_face[j - 1] > 0 && tj != 0) {
+                int nvl = tj - g.bottom_face[j - 1] + 1;
+                double sdz = 0.0;
+                for (int k = 1; k <= nvl; ++k) sdz = sdz + s.dz_face[ix(tj + 1 - k, j, L)] * s.ainvdz1[ix(k, j, L)];
+                double base = gdt2th2 * g.face_length[j - 1] / g.delta_j[j - 1] * sdz;
+                r = r + base * f.eta_at_ob_new[obf - 1];
+            }
+        }
+    }
+    double *row = sparsem + (long)(i - 1) * 5;
+    row[0] = diag;
+    row[1] = off[0];
+    row[2] = off[1];
+    row[3] = off[2];
+    row[4] = off[3];
+    rhs[i - 1] = r;
+}
+
+// -------------------------------------------------------------------- grid-wide barrier
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Sense-counting barrier over all blocks of a cooperative launch.  Every wait is bounded: after
+// about 2 s the block records GOM_E_TIMEOUT and the caller leaves the kernel.
+__device__ bool grid_barrier(unsigned *bar, unsigned nblocks, gom_status *st) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned *vgen = bar + 1;
+        unsigned gen = *vgen;
+        __threadfence();
+        unsigned arrived = atomicAdd(bar, 1u);
+        int good = 1;
+        if (arrived == nblocks - 1) {
+            atomicExch(bar, 0u);
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            unsigned long long t0 = globaltimer_ns();
+            while (*vgen == gen) {
+                __nanosleep(64);
+                if (globaltimer_ns() - t0 > 2000000000ull) {
+                    record_error(st, GOM_E_TIMEOUT, 1, (int)blockIdx.x, 0, 0.0);
+                    good = 0;
+                    break;
+                }
+            }
+        }
+        __threadfence();
+        ok = good;
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+// block reduction of one double; result valid in every thread
+template <int THREADS>
+__device__ __forceinline__ double block_sum(double v, double *sh) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (w == 0) {
+        t = lane < THREADS / 32 ? sh[lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+        if (lane == 0) sh[32] = t;
+    }
+    __syncthreads();
+    double r = sh[32];
+    __syncthreads();
+    return r;
+}
+
+// sum of all block partials in a fixed order (identical in every block)
+__device__ __forceinline__ double sum_partials(const double *part, int n, double *sh) {
+    int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (w == 0) {
+        double t = 0.0;
+        for (int i = lane; i < n; i += 32) t += ((volatile const double *)part)[i];
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+        if (lane == 0) sh[33] = t;
+    }
+    __syncthreads();
+    double r = sh[33];
+    __syncthreads();
+    return r;
+}
+
+struct PcgArgs {
+    Geom g;
+    const double *sp, *b;
+    double *x, *minv, *r, *s, *q, *dA, *dB, *pdq, *pdelta;
+    unsigned *bar;
+    int *iters;
+    int maxit;
+    double tol;
+    gom_status *st;
+};
+
+// pre_conj_grad.f90:46-221 as one cooperative kernel: the matrix-vector product of row i uses
+// the row's own 5 coefficients in CSR order (diagonal first) and the neighbours' values; the
+// d-update of iteration n is fused into the product of iteration n+1 (d double-buffered), so one
+// iteration needs two grid barriers.
+constexpr int PCG_THREADS = 256;
+
+__global__ void __launch_bounds__(PCG_THREADS) k_pcg(PcgArgs a) {
+    __shared__ double sh[40];
+    const Geom &g = a.g;
+    const int n = g.NC;
+    const unsigned nblocks = gridDim.x;
+    const long stride = (long)gridDim.x * blockDim.x;
+    const long t0 = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    // initial residual, Jacobi preconditioner, d = M^-1 r
+    double loc = 0.0;
+    for (long i = t0; i < n; i += stride) {
+        const double *row = a.sp + i * 5;
+        int cell = (int)i + 1;
+        double sum = 0.0;
+        sum = sum + row[0] * a.x[i];
+        int tq = g.tri_or_quad[i];
+        for (int l = 1; l <= tq; ++l) {
+            int nb = g.cell_adj(l, cell);
+            if (nb != 0) sum = sum + row[l] * a.x[nb - 1];
+        }
+        double mi = 1.0 / row[0];
+        double ri = a.b[i] - sum;
+        double di = 0.0 + mi * ri;
+        a.minv[i] = mi;
+        a.r[i] = ri;
+        a.dA[i] = di;
+        loc += ri * di;
+    }
+    double bs = block_sum<PCG_THREADS>(loc, sh);
+    if (threadIdx.x == 0) a.pdelta[blockIdx.x] = bs;
+    if (!grid_barrier(a.bar, nblocks, a.st)) return;
+    double delta_new = sum_partials(a.pdelta, nblocks, sh);
+    const double delta_0 = delta_new;
+    int iters = 0;
+    if (delta_0 != 0.0) {
+        double beta = 0.0;
+        double *dcur = a.dA, *dnext = a.dB;
+        bool first = true;
+        for (int it = 1; it <= a.maxit; ++it) {
+            if (failed(a.st)) return;
+            // q = A d with d = s + beta*d_old fused in
+            loc = 0.0;
+            for (long i = t0; i < n; i += stride) {
+                const double *row = a.sp + i * 5;
+                int cell = (int)i + 1;
+                double di = first ? dcur[i] : a.s[i] + beta * dcur[i];
+                double sum = 0.0;
+                sum = sum + row[0] * di;
+                int tq = g.tri_or_quad[i];
+                for (int l = 1; l <= tq; ++l) {
+                    int nb = g.cell_adj(l, cell);
+                    if (nb != 0) {
+                        double dn = first ? dcur[nb - 1] : a.s[nb - 1] + beta * dcur[nb - 1];
+                        sum = sum + row[l] * dn;
+                    }
+                }
+                if (!first) dnext[i] = di;
+                a.q[i] = sum;
+                loc += di * sum;
+            }
+            bs = block_sum<PCG_THREADS>(loc, sh);
+            if (threadIdx.x == 0) a.pdq[blockIdx.x] = bs;
+            if (!grid_barrier(a.bar, nblocks, a.st)) return;
+            double dq = sum_partials(a.pdq, nblocks, sh);
+            double alpha = delta_new / dq;
+            double *dv = first ? dcur : dnext;
+            loc = 0.0;
+            for (long i = t0; i < n; i += stride) {
+                double di = dv[i];
+                a.x[i] = a.x[i] + alpha * di;
+                double ri = a.r[i] - alpha * a.q[i];
+                a.r[i] = ri;
+                double si = 0.0 + a.minv[i] * ri;
+                a.s[i] = si;
+                loc += ri * si;
+            }
+            bs = block_sum<PCG_THREADS>(loc, sh);
+            if (threadIdx.x == 0) a.pdelta[blockIdx.x] = bs;
+            if (!grid_barrier(a.bar, nblocks, a.st)) return;
+            double delta_old = delta_new;
+            delta_new = sum_partials(a.pdelta, nblocks, sh);
+            beta = delta_new / delta_old;
+            if (!first) {
+                double *t = dcur;
+                dcur = dnext;
+                dnext = t;
+            }
+            first = false;
+            iters = it;
+            if (sqrt(delta_new * delta_new / (delta_0 * delta_0)) < a.tol) break;
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *a.iters = iters;
+}
+
+// :353-375 node elevation from wet cells; wetdry_node
+__global__ void k_node_eta(Geom g, State s) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (i > g.NN) return;
+    int wd = 0;
+    double sum1 = 0.0, sum0 = 0.0;
+    int na = g.adj_cells_at_node[i - 1];
+    for (int j = 1; j <= na; ++j) {
+        int ie = g.node_cell(j, i);
+        if (s.top_cell[ie - 1] == 0) wd = 1;
+        else {
+            double ar = g.area[ie - 1];
+            sum1 = sum1 + ar * s.eta_cell_new[ie - 1];
+            sum0 = sum0 + ar;
+        }
+    }
+    s.wetdry_node[i - 1] = wd;
+    if (wd == 0) s.eta_node[i - 1] = sum1 / sum0;
+}
+
+// :378-394 dry nodes take the mean of their wet neighbours
+__global__ void k_node_eta_dry(Geom g, State s) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (i > g.NN) return;
+    if (s.wetdry_node[i - 1] != 1) return;
+    double sum0 = 0.0;
+    int icount = 0;
+    int nn = g.adj_nodes_at_node[i - 1];
+    for (int j = 1; j <= nn; ++j) {
+        int nd = g.node_nb(j, i);
+        if (s.wetdry_node[nd - 1] == 0) {
+            icount = icount + 1;
+            sum0 = sum0 + s.eta_node[nd - 1];
+        }
+    }
+    if (icount != 0) s.eta_node[i - 1] = sum0 / icount;
+}
+
+cudaError_t pcg_configure(Launch &x, int device) {
+    int per_sm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg, PCG_THREADS, 0);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) per_sm = 1;
+    int coop = 0;
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device);
+    if (!coop) return cudaErrorNotSupported;
+    long need = (x.g.NC + PCG_THREADS - 1) / PCG_THREADS;
+    long maxb = (long)per_sm * x.num_sms;
+    // two resident blocks per SM at most: enough threads for one to a few rows each
+    long cap = (long)x.num_sms * (per_sm < 2 ? per_sm : 2);
+    if (cap > maxb) cap = maxb;
+    x.w.pcg_blocks = (int)(need < cap ? need : cap);
+    if (x.w.pcg_blocks < 1) x.w.pcg_blocks = 1;
+    x.w.pcg_threads = PCG_THREADS;
+    return cudaSuccess;
+}
+
+cudaError_t launch_free_surface(const Launch &x) {
+    const Geom &g = x.g;
+    k_fs_assemble<<<blocks_for(g.NC, 128), 128, 0, x.stream>>>(x.g, x.s, x.f, x.p, x.w.sparsem, x.w.rhs, x.status);
+    cudaError_t e = cudaMemsetAsync(x.w.barrier, 0, 2 * sizeof(unsigned), x.stream);
+    if (e != cudaSuccess) return e;
+    PcgArgs a;
+    a.g = g;
+    a.sp = x.w.sparsem;
+    a.b = x.w.rhs;
+    a.x = x.s.eta_cell_new;
+    a.minv = x.w.minv;
+    a.r = x.w.r;
+    a.s = x.w.s;
+    a.q = x.w.q;
+    a.dA = x.w.d0;
+    a.dB = x.w.d1;
+    a.pdq = x.w.partial_dq;
+    a.pdelta = x.w.partial_delta;
+    a.bar = x.w.barrier;
+    a.iters = x.w.pcg_iters;
+    a.maxit = x.p.max_iteration_pcg;
+    a.tol = x.p.error_tolerance;
+    a.st = x.status;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(x.w.pcg_blocks);
+    cfg.blockDim = dim3(x.w.pcg_threads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = x.stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    e = cudaLaunchKernelEx(&cfg, k_pcg, a);
+    if (e != cudaSuccess) return e;
+    k_node_eta<<<blocks_for(g.NN, 256), 256, 0, x.stream>>>(x.g, x.s);
+    k_node_eta_dry<<<blocks_for(g.NN, 256), 256, 0, x.stream>>>(x.g, x.s);
+    return cudaGetLastError();
+}
+
+// ============================================================================================
+// solve_velocities.f90:23-184: one thread per face column
+__global__ void k_face_velocity(Geom g, State s, Forcing f, Params p) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (j > g.NF) return;
+    const int L = g.L;
+    int tj = s.top_face[j - 1];
+    if (tj == 0) {
+        for (int k = 1; k <= L; ++k) {
+            s.un_face_new[ix(k, j, L)] = 0.0;
+            s.vn_face_new[ix(k, j, L)] = 0.0;
+        }
+        return;
+    }
+    const double dt = p.dt, gravity = p.gravity, theta = p.theta;
+    int bj = g.bottom_face[j - 1];
+    int n1 = g.face_node(1, j), n2 = g.face_node(2, j);
+    int btype = g.boundary_type_of_face[j - 1];
+    int a1 = g.face_cell(1, j), a2 = g.face_cell(2, j);
+    bool wet = s.wetdry_node[n1 - 1] == 0 && s.wetdry_node[n2 - 1] == 0;
+    bool init_dry = g.initial_wetdry_node[n1 - 1] == 1 || g.initial_wetdry_node[n2 - 1] == 1;
+    double dj = g.delta_j[j - 1], fl = g.face_length[j - 1];
+    double dEta = 0.0;
+    if (btype == 0) dEta = s.eta_cell_new[a2 - 1] - s.eta_cell_new[a1 - 1];
+    else if (btype > 0) dEta = f.eta_at_ob_new[g.ob_element_flag[a1 - 1] - 1] - s.eta_cell_new[a1 - 1];
+    double dEtaN = s.eta_node[n2 - 1] - s.eta_node[n1 - 1];
+    for (int k = 1; k <= tj - bj + 1; ++k) {
+        int kk = tj + 1 - k;
+        long o = ix(kk, j, L), ok = ix(k, j, L);
+        double rtemp2 = 0.0;
+        if (btype == -1) {
+            s.un_face_new[o] = 0.0;
+        } else if (btype == 0) {
+            double rtemp0 = theta * gravity * dt / dj * dEta * s.ainvdz1[ok];
+            double rtemp1 = rtemp0 * g.cos_theta2[j - 1];
+            rtemp2 = rtemp0 * g.sin_theta2[j - 1];
+            s.un_face_new[o] = s.ainvg1[ok] - rtemp1;
+        } else {
+            double rtemp0 = theta * gravity * dt / dj * dEta * s.ainvdz1[ok];
+            s.un_face_new[o] = s.ainvg1[ok] - rtemp0;
+        }
+        if (wet) {
+            double rtemp1 = theta * gravity * dt / fl * dEtaN * s.ainvdz2[ok];
+            if (btype == 0) s.vn_face_new[o] = s.ainvg2[ok] - (rtemp1 + rtemp2);
+            else s.vn_face_new[o] = s.ainvg2[ok] - rtemp1;
+        }
+        if (init_dry) s.vn_face_new[o] = fmax(-5.0, fmin(s.vn_face_new[o], 5.0));
+    }
+    int ibnd = g.isflowside3[j - 1];
+    if (ibnd > 0) {
+        double qu = s.qu_boundary[ibnd - 1];
+        for (int k = bj; k <= tj; ++k) s.un_face_new[ix(k, j, L)] = qu;
+    }
+    for (int k = 1; k <= bj - 1; ++k) {
+        s.un_face_new[ix(k, j, L)] = 0.0;
+        s.vn_face_new[ix(k, j, L)] = 0.0;
+    }
+    double ut = s.un_face_new[ix(tj, j, L)], vt = s.vn_face_new[ix(tj, j, L)];
+    for (int k = tj + 1; k <= L; ++k) {
+        s.un_face_new[ix(k, j, L)] = ut;
+        s.vn_face_new[ix(k, j, L)] = vt;
+    }
+}
+
+// solve_velocities.f90:191-258: one thread per cell column
+__global__ void k_cell_w(Geom g, State s) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (i > g.NC) return;
+    const int L = g.L;
+    int t = s.top_cell[i - 1], b = g.bottom_cell[i - 1];
+    if (t == 0) {
+        for (int k = 0; k <= L; ++k) s.wn_cell_new[ix0(k, i, L)] = 0.0;
+        return;
+    }
+    int tq = g.tri_or_quad[i - 1];
+    int fj[4], fb[4], ft[4];
+    double fsl[4];
+    for (int l = 1; l <= tq; ++l) {
+        int jt = g.cell_face(l, i);
+        fj[l - 1] = jt;
+        fb[l - 1] = g.bottom_face[jt - 1];
+        ft[l - 1] = s.top_face[jt - 1];
+        fsl[l - 1] = (double)g.cell_sign(l, i) * g.face_length[jt - 1];
+    }
+    double ar = g.area[i - 1];
+    double w = 0.0;
+    s.wn_cell_new[ix0(b - 1, i, L)] = 0.0;
+    for (int k = b; k <= t; ++k) {
+        double sum1 = 0.0;
+        for (int l = 0; l < tq; ++l) {
+            if (k >= fb[l] && k <= ft[l])
+                sum1 = sum1 + fsl[l] * s.dz_face[ix(k, fj[l], L)] * s.un_face_new[ix(k, fj[l], L)];
+        }
+        w = w - sum1 / ar;
+        s.wn_cell_new[ix0(k, i, L)] = w;
+    }
+    for (int k = 0; k <= b - 2; ++k) s.wn_cell_new[ix0(k, i, L)] = 0.0;
+    for (int k = t + 1; k <= L; ++k) s.wn_cell_new[ix0(k, i, L)] = w;
+}
+
+cudaError_t launch_velocities(const Launch &x) {
+    k_face_velocity<<<blocks_for(x.g.NF, 128), 128, 0, x.stream>>>(x.g, x.s, x.f, x.p);
+    k_cell_w<<<blocks_for(x.g.NC, 128), 128, 0, x.stream>>>(x.g, x.s);
+    return cudaGetLastError();
+}
+
+// ============================================================================================
+// update_vertical_layers_1.f90: new top layers and thicknesses for an entity column.
+// kind 0 = cell (:42-133), 1 = face (:139-198), 2 = node (:204-254)
+template <int KIND>
+__device__ __forceinline__ int new_column(const Geom &g, const Params &p, double h, double eta, int b, double *dz,
+                                          double *dzh, long base_dz, long base_dzh, bool &bad) {
+    const int L = g.L;
+    const double MSL = p.msl;
+    int tnew = 0;
+    bad = false;
+    double total = h + eta;
+    if (total <= p.dry_depth) return 0;
+    double tmp = MSL + eta;
+    for (int k = L - 1; k >= 0; --k) {
+        if (tmp > g.z_level[k] && tmp <= g.z_level[k + 1]) {
+            tnew = k + 1;
+            dz[base_dz + tnew - 1] = tmp - g.z_level[k];
+            break;
+        }
+    }
+    if (tnew < b) {
+        bad = true;
+        return tnew;
+    }
+    if (tnew == b) {
+        dz[base_dz + tnew - 1] = total;
+        if (KIND == 1) dzh[base_dzh + tnew - 1] = total;
+        dzh[base_dzh + tnew] = total;
+    } else {
+        dz[base_dz + b - 1] = g.z_level[b] - (MSL - h);
+        for (int k = b + 1; k <= tnew - 1; ++k) dz[base_dz + k - 1] = g.delta_z[k - 1];
+        for (int k = b; k <= tnew - 1; ++k) dzh[base_dzh + k] = (dz[base_dz + k] + dz[base_dz + k - 1]) * 0.5;
+        if (KIND != 2) {
+            dzh[base_dzh + tnew] = dz[base_dz + tnew - 1];
+            dzh[base_dzh + b - 1] = dz[base_dz + b - 1];
+        }
+    }
+    return tnew;
+}
+
+__global__ void k_layers_cells(Geom g, State s, Params p, gom_status *st) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (i > g.NC) return;
+    const int L = g.L;
+    bool bad;
+    int b = g.bottom_cell[i - 1];
+    int tnew = new_column<0>(g, p, g.h_cell[i - 1], s.eta_cell_new[i - 1], b, s.dz_cell_new, s.dzhalf_cell_new,
+                             (long)(i - 1) * L, (long)(i - 1) * (L + 1), bad);
+    if (bad) {
+        record_error(st, GOM_E_LAYER, 66, i, tnew, s.eta_cell_new[i - 1]);
+        return;
+    }
+    if (s.top_cell[i - 1] == 0 && tnew != 0)
+        for (int k = 0; k <= L; ++k) s.wn_cell_new[ix0(k, i, L)] = 0.0;
+    s.top_cell[i - 1] = tnew;
+}
+
+__global__ void k_layers_faces(Geom g, State s, Params p, gom_status *st) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (j > g.NF) return;
+    const int L = g.L;
+    int a1 = g.face_cell(1, j), a2 = g.face_cell(2, j);
+    double eta_max = a2 != 0 ? fmax(s.eta_cell_new[a1 - 1], s.eta_cell_new[a2 - 1]) : s.eta_cell_new[a1 - 1];
+    bool bad;
+    int b = g.bottom_face[j - 1];
+    int tnew = new_column<1>(g, p, g.h_face[j - 1], eta_max, b, s.dz_face_new, s.dzhalf_face_new, (long)(j - 1) * L,
+                             (long)(j - 1) * (L + 1), bad);
+    if (bad) {
+        record_error(st, GOM_E_LAYER, 166, j, tnew, eta_max);
+        return;
+    }
+    s.top_face[j - 1] = tnew;
+    for (int k = b; k <= tnew - 1; ++k) {
+        double v = s.dzhalf_face_new[ix0(k, j, L)];
+        if (v < p.denominator_min_for_matrix) {
+            record_error(st, GOM_E_LAYER, 301, j, k, v);
+            return;
+        }
+    }
+}
+
+__global__ void k_layers_nodes(Geom g, State s, Params p, gom_status *st) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (i > g.NN) return;
+    const int L = g.L;
+    bool bad;
+    int b = g.bottom_node[i - 1];
+    int tnew = new_column<2>(g, p, g.h_node[i - 1], s.eta_node[i - 1], b, s.dz_node_new, s.dzhalf_node_new,
+                             (long)(i - 1) * L, (long)(i - 1) * (L + 1), bad);
+    if (bad) {
+        record_error(st, GOM_E_LAYER, 224, i, tnew, s.eta_node[i - 1]);
+        return;
+    }
+    s.top_node[i - 1] = tnew;
+    for (int k = b; k <= tnew - 1; ++k) {
+        double v = s.dzhalf_node_new[ix0(k, i, L)];
+        if (v < p.denominator_min_for_matrix) {
+            record_error(st, GOM_E_LAYER, 318, i, k, v);
+            return;
+        }
+    }
+}
+
+// :260-296 an element is dry when all its nodes are dry; consistency checks
+__global__ void k_layers_check(Geom g, State s, Params p, gom_status *st) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (i > g.NC) return;
+    const int L = g.L;
+    int nsum1 = 0, nsum2 = 0;
+    int tq = g.tri_or_quad[i - 1];
+    for (int l = 1; l <= tq; ++l) {
+        nsum1 += s.top_node[g.cell_node(l, i) - 1];
+        nsum2 += s.top_face[g.cell_face(l, i) - 1];
+    }
+    int t = s.top_cell[i - 1];
+    if (nsum1 == 0) {
+        t = 0;
+        s.top_cell[i - 1] = 0;
+    }
+    if (nsum2 == 0 && t != 0) {
+        record_error(st, GOM_E_DRY, 273, i, 0, 0.0);
+        return;
+    }
+    for (int k = g.bottom_cell[i - 1]; k <= t - 1; ++k) {
+        double v = s.dzhalf_cell_new[ix0(k, i, L)];
+        if (v < p.denominator_min_for_matrix) {
+            record_error(st, GOM_E_LAYER, 284, i, k, v);
+            return;
+        }
+    }
+}
+
+cudaError_t launch_layers(const Launch &x) {
+    k_layers_cells<<<blocks_for(x.g.NC, 256), 256, 0, x.stream>>>(x.g, x.s, x.p, x.status);
+    k_layers_faces<<<blocks_for(x.g.NF, 256), 256, 0, x.stream>>>(x.g, x.s, x.p, x.status);
+    k_layers_nodes<<<blocks_for(x.g.NN, 256), 256, 0, x.stream>>>(x.g, x.s, x.p, x.status);
+    k_layers_check<<<blocks_for(x.g.NC, 256), 256, 0, x.stream>>>(x.g, x.s, x.p, x.status);
+    return cudaGetLastError();
+}
+
+// ============================================================================================
+// calculate_velocity_at_node.f90:31-60: face-level velocities, one thread per face column
+__global__ void k_face_level(Geom g, State s) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (j > g.NF) return;
+    const int L = g.L;
+    int t = s.top_face[j - 1];
+    if (t == 0) return;
+    int b = g.bottom_face[j - 1];
+    double ct = g.cos_theta[j - 1], sn = g.sin_theta[j - 1];
+    double uk = 0, vk = 0;
+    {
+        double un = s.un_face_new[ix(b, j, L)], vn = s.vn_face_new[ix(b, j, L)];
+        uk = un * ct - vn * sn;
+        vk = un * sn + vn * ct;
+    }
+    s.u_face_level[ix0(b - 1, j, L)] = uk;
+    s.v_face_level[ix0(b - 1, j, L)] = vk;
+    for (int k = b; k <= t - 1; ++k) {
+        double un = s.un_face_new[ix(k + 1, j, L)], vn = s.vn_face_new[ix(k + 1, j, L)];
+        double u1 = un * ct - vn * sn;
+        double v1 = un * sn + vn * ct;
+        double fac = s.dz_face[ix(k, j, L)] * 0.5 / s.dzhalf_face[ix0(k, j, L)];
+        s.u_face_level[ix0(k, j, L)] = uk + fac * (u1 - uk);
+        s.v_face_level[ix0(k, j, L)] = vk + fac * (v1 - vk);
+        uk = u1;
+        vk = v1;
+    }
+    s.u_face_level[ix0(t, j, L)] = uk;
+    s.v_face_level[ix0(t, j, L)] = vk;
+}
+
+// :67-138 node u, v (face-length weighted face levels) and w (area-weighted cell w):
+// one thread per (node, level)
+__global__ void k_node_uvw(Geom g, State s) {
+    long tt = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int L = g.L;
+    if (tt >= (long)g.NN * (L + 1)) return;
+    int i = (int)(tt / (L + 1)) + 1, k = (int)(tt % (L + 1));
+    double u = 0.0, v = 0.0, weight = 0.0;
+    int icount = 0;
+    int na = g.adj_cells_at_node[i - 1];
+    for (int j = 1; j <= na; ++j) {
+        int isn = g.node_cell(j, i), nc = g.node_count(j, i);
+        int tq = g.tri_or_quad[isn - 1];
+        for (int l = tq - 2; l <= tq - 1; ++l) {
+            int ifn = g.cell_face(start_end_node(tq, nc, l), isn);
+            double fw = g.face_cell(2, ifn) == 0 ? 2.0 : 1.0;
+            double fl = g.face_length[ifn - 1];
+            int tf = s.top_face[ifn - 1];
+            if (tf != 0 && k >= g.bottom_face[ifn - 1] - 1) {
+                int kvt = min(k, tf);
+                u = u + s.u_face_level[ix0(kvt, ifn, L)] / fl * fw;
+                v = v + s.v_face_level[ix0(kvt, ifn, L)] / fl * fw;
+                icount = icount + 1;
+            }
+            weight = weight + fw / fl;
+        }
+    }
+    if (icount != 0) {
+        u = u / weight;
+        v = v / weight;
+    }
+    double w = 0.0, tw = 0.0;
+    for (int j = 1; j <= na; ++j) {
+        int ite = g.node_cell(j, i);
+        int te = s.top_cell[ite - 1];
+        if (te != 0 && k >= g.bottom_cell[ite - 1] - 1) {
+            int kvt = min(k, te);
+            double ar = g.area[ite - 1];
+            tw = tw + ar;
+            w = w + s.wn_cell[ix0(kvt, ite, L)] * ar;
+        }
+    }
+    if (tw != 0.0) w = w / tw;
+    long o = ix0(k, i, L);
+    s.u_node[o] = u;
+    s.v_node[o] = v;
+    s.w_node[o] = w;
+}
+
+cudaError_t launch_node_velocity(const Launch &x) {
+    k_face_level<<<blocks_for(x.g.NF, 128), 128, 0, x.stream>>>(x.g, x.s);
+    long n = (long)x.g.NN * (x.g.L + 1);
+    k_node_uvw<<<blocks_for(n, 256), 256, 0, x.stream>>>(x.g, x.s);
+    return cudaGetLastError();
+}
+
+}  // namespace gom

@@ -1,0 +1,325 @@
+/*
+ * gom_core.h -- C ABI of the GB300 per-timestep core of the General Ocean Model (GOM).
+ *
+ * GOM's Fortran driver (GOM_Rv1.1.0/source/main.f90) calls its per-timestep subroutines
+ * without arguments; they exchange data through module globals declared in
+ * GOM_Rv1.1.0/source/mod_global_variables.f90 and allocated in allocate_variables.f90.
+ * This header replaces those calls with explicit entry points that take plain pointers
+ * and sizes.  Two libraries export exactly these symbols:
+ *
+ *   libgomcore.so    -- the product: hand-written CUDA for sm_103a, state resident in HBM;
+ *   libgomoracle.so  -- a serial FP64 CPU restatement used only as the test checker.
+ *
+ * Array conventions (identical to the Fortran module arrays, so a Fortran caller passes
+ * c_loc() of its arrays unchanged):
+ *   - column-major "(k, entity)" storage: layer index fastest, entity slowest;
+ *   - an array declared (lo:hi, N) in Fortran has (hi-lo+1)*N elements and element
+ *     (k, e) (k in lo..hi, e in 1..N) lives at offset (e-1)*(hi-lo+1) + (k-lo);
+ *   - connectivity is 1-based with 0 meaning "none";
+ *   - real(dp) is double, integer is int32_t.
+ *
+ * Error model: every call returns GOM_OK (0) or a positive gom_err code.  Conditions on
+ * which the reference executes `stop` are reported as codes; the library never aborts
+ * the process.  gom_get_status() returns the first failing site, entity and layer.
+ *
+ * Threading: a context is not re-entrant.  All device work of a context runs on one
+ * CUDA stream owned by the context.  Host arrays are only read during a call.
+ */
+#ifndef GOM_CORE_H
+#define GOM_CORE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GOM_ABI_VERSION 1
+
+typedef struct gom_ctx gom_ctx;
+
+/* ------------------------------------------------------------------ error codes */
+typedef enum gom_err {
+    GOM_OK = 0,
+    GOM_E_ARG = 1,            /* bad argument, size mismatch, unsupported option            */
+    GOM_E_CUDA = 2,           /* CUDA runtime error (message via gom_last_message)          */
+    GOM_E_NOT_SPD = 3,        /* solve_free_surface_equation.f90:100-104                    */
+    GOM_E_ZERO_PIVOT = 4,     /* tridiagonal_solver.f90:32-35,47-50                         */
+    GOM_E_ELM = 5,            /* ELM geometry failure: search_straight_line.f90,
+                                 ELM_backtrace_v1.f90, bilinear_interpolation.f90 stops     */
+    GOM_E_DRY = 6,            /* wet element with dry nodes/sides, dry river boundary       */
+    GOM_E_LAYER = 7,          /* impossible elevation/layer: update_vertical_layers_1.f90   */
+    GOM_E_DENSITY = 8,        /* calculate_density_full.f90:43-53,103-107                   */
+    GOM_E_PCG_MAXIT = 9,      /* warning: PCG hit max_iteration_pcg (the reference goes on) */
+    GOM_E_TIMEOUT = 10,       /* a bounded device-side wait gave up                         */
+    GOM_E_NOMEM = 11          /* device allocation failed                                   */
+} gom_err;
+
+/* Sub-sites recorded in gom_status.site for GOM_E_ELM, one per reference `stop`. */
+enum {
+    GOM_ELM_START_DRY = 1,        /* search_straight_line.f90:37-46   */
+    GOM_ELM_START_OUTSIDE = 2,    /* search_straight_line.f90:82-89   */
+    GOM_ELM_ZERO_PATH = 3,        /* search_straight_line.f90:129-139 */
+    GOM_ELM_NO_FIRST_EDGE = 4,    /* search_straight_line.f90:162-169 */
+    GOM_ELM_OVERSHOOT = 5,        /* search_straight_line.f90:199-207 */
+    GOM_ELM_ZERO_REMAIN = 6,      /* search_straight_line.f90:218-222 */
+    GOM_ELM_FACE_MISMATCH = 7,    /* search_straight_line.f90:237-242 */
+    GOM_ELM_NO_NEXT_EDGE = 8,     /* search_straight_line.f90:343-353 */
+    GOM_ELM_END_DRY = 9,          /* search_straight_line.f90:363-372 */
+    GOM_ELM_Z_RANGE = 10,         /* search_straight_line.f90:379-385 */
+    GOM_ELM_Z_ABOVE = 11,         /* ELM_backtrace_v1.f90:107-113     */
+    GOM_ELM_QUAD_OUTSIDE = 12,    /* ELM_backtrace_v1.f90:164-170     */
+    GOM_ELM_BILINEAR = 13         /* bilinear_interpolation.f90:41-113 */
+};
+
+typedef struct gom_status {
+    int32_t code;      /* gom_err of the first failure, 0 if none            */
+    int32_t site;      /* sub-site (GOM_ELM_*) or reference line of the stop */
+    int32_t entity;    /* 1-based face / cell / node index                   */
+    int32_t layer;     /* layer index, 0 if not applicable                    */
+    double value;      /* offending value where the reference prints one     */
+} gom_status;
+
+/* ------------------------------------------------------------------ sizes */
+typedef struct gom_dims {
+    int32_t n_cells;    /* maxele                  */
+    int32_t n_faces;    /* maxface                 */
+    int32_t n_nodes;    /* maxnod                  */
+    int32_t n_layers;   /* maxlayer                */
+    int32_t max_nb;     /* max_no_neighbor_node    */
+    int32_t n_ob;       /* num_ob_cell             */
+    int32_t n_qb;       /* num_Qb_cell             */
+    int32_t reserved;
+} gom_dims;
+
+/* ------------------------------------------------------------------ scalar configuration
+ * Card numbers refer to main.inp as parsed by read_main_inp.f90. */
+typedef struct gom_params {
+    double gravity;            /* C01 */
+    double rho_o;              /* C01 */
+    double msl;                /* C2  MSL */
+    double dt;                 /* C3  */
+    double theta;              /* C5_01 */
+    double adv_onoff_depth;    /* C5_01 */
+    double von_karman;         /* C5_02 */
+    double cd_const;           /* bf_flag == 3 only: constant drag coefficient (extension) */
+    double dry_depth;          /* C5_03 */
+    double smagorinsky;        /* C5_04 Smagorinsky_parameter */
+    double ah_0;               /* C5_04 */
+    double kh_0;               /* C5_04 */
+    double error_tolerance;    /* C6 */
+    double delta_z_min;        /* derived in read_main_inp.f90 card C2_1 */
+    double denominator_min_for_matrix; /* derived in read_main_inp.f90 card C5_03 */
+    int32_t advection_flag;    /* C5_01 */
+    int32_t elm_backtrace_flag;/* C5_01 */
+    int32_t elm_sub_iter;      /* C5_01 */
+    int32_t elm_min_iter;      /* C5_01 */
+    int32_t elm_max_iter;      /* C5_01 */
+    int32_t bf_flag;           /* C5_02: 0 none, 1 Manning, 2 log law, 3 constant Cd (extension) */
+    int32_t baroclinic_flag;   /* C5_03 */
+    int32_t ana_density;       /* C5_03: 0 full UNESCO EOS, 1 linear */
+    int32_t max_iteration_pcg; /* C6 */
+    int32_t transport_flag;    /* C7 (transport_solver must be 1, TVD) */
+    int32_t trans_sub_iter;    /* C7_1 */
+    int32_t h_flux_limiter;    /* C7_1 */
+    int32_t v_flux_limiter;    /* C7_1 */
+    int32_t is_salt;           /* C7_2 is_tran(1) */
+    int32_t is_temp;           /* C7_2 is_tran(2) */
+    int32_t heat_option;       /* C7_3 (only 2 supported when is_temp) */
+    int32_t reserved[4];
+} gom_params;
+
+/* ------------------------------------------------------------------ static geometry
+ * Produced once on the host by read_node_inp/read_cell_inp, set_geometry_1, set_geometry_2,
+ * calculate_voronoi_center and calculate_coriolis_factor.  Copied at gom_create. */
+typedef struct gom_geom {
+    /* nodes */
+    const double  *x_node, *y_node, *h_node;             /* (N_n)               */
+    const int32_t *adj_cells_at_node;                    /* (N_n)               */
+    const int32_t *adj_cellnum_at_node;                  /* (max_nb, N_n)       */
+    const int32_t *node_count_each_element;              /* (max_nb, N_n)       */
+    const int32_t *adj_nodes_at_node;                    /* (N_n)               */
+    const int32_t *adj_nodenum_at_node;                  /* (0:max_nb, N_n)     */
+    const int32_t *bottom_layer_at_node;                 /* (N_n)               */
+    const int32_t *initial_wetdry_node;                  /* (N_n)               */
+    /* cells */
+    const double  *x_cell, *y_cell, *h_cell, *area;      /* (N_c)               */
+    const int32_t *tri_or_quad;                          /* (N_c)               */
+    const int32_t *nodenum_at_cell;                      /* (4, N_c)            */
+    const int32_t *facenum_at_cell;                      /* (4, N_c)            */
+    const int32_t *adj_cellnum_at_cell;                  /* (4, N_c)            */
+    const int32_t *sign_in_outflow;                      /* (4, N_c)            */
+    const int32_t *bottom_layer_at_element;              /* (N_c)               */
+    const int32_t *ob_element_flag;                      /* (N_c)               */
+    const int32_t *qb_element_flag;                      /* (N_c) Qb_element_flag */
+    /* faces */
+    const double  *x_face, *y_face, *h_face, *face_length, *delta_j;   /* (N_f)   */
+    const double  *cos_theta, *sin_theta, *cos_theta2, *sin_theta2;    /* (N_f)   */
+    const int32_t *adj_cellnum_at_face;                  /* (2, N_f)            */
+    const int32_t *nodenum_at_face;                      /* (2, N_f)            */
+    const int32_t *bottom_layer_at_face;                 /* (N_f)               */
+    const int32_t *boundary_type_of_face;                /* (N_f) -1 land, 0 inner, >0 open bnd */
+    const int32_t *isflowside3;                          /* (N_f) river face -> Q index */
+    const double  *coriolis_factor;                      /* (N_f)               */
+    const double  *manning;                              /* (N_f) bf_flag 1, may be NULL */
+    const double  *bf_height;                            /* (N_f) bf_flag 2, may be NULL */
+    /* boundaries */
+    const int32_t *ob_cell_id;                           /* (n_ob)              */
+    const int32_t *qb_cell;                              /* (n_qb) Q_boundary(:,1) */
+    const int32_t *qb_face;                              /* (n_qb) Q_boundary(:,2) */
+    /* vertical grid */
+    const double  *z_level;                              /* (0:L)               */
+    const double  *delta_z;                              /* (L)                 */
+} gom_geom;
+
+/* ------------------------------------------------------------------ per-step forcing
+ * Computed on the host by setup_spinup, compute_boundary_eta, calculate_Q and the series
+ * interpolation at solve_transport_equation_v19.f90:229-534.  NULL array = keep the last
+ * uploaded value (all start at zero). */
+typedef struct gom_forcing {
+    double elapsed_time;               /* it*dt                                      */
+    double spinup_tide;                /* spinup_function_tide                       */
+    double spinup_baroclinic;          /* spinup_function_baroclinic                 */
+    double reserved;
+    const double *eta_at_ob_old;       /* (n_ob)                                     */
+    const double *eta_at_ob_new;       /* (n_ob)                                     */
+    const double *q_add;               /* (n_qb) river discharge Q_add [m3/s]        */
+    const double *wind_stress_normal;  /* (N_f) kinematic stress along face normal   */
+    const double *wind_stress_tangnt;  /* (N_f)                                      */
+    const double *gamma_t;             /* (N_f) surface drag Gamma_T                 */
+    const double *air_p;               /* (N_n) air_p1                               */
+    const double *con_at_ob;           /* (n_ob, 2, Nt): con_at_ob(i,i3) per subcycle */
+    const double *con_at_qb;           /* (n_qb, 2, Nt): con_at_Qb(i,i3) per subcycle */
+    const double *phi_sw;              /* (N_c) surface heat term of heat_option 2   */
+} gom_forcing;
+
+/* ------------------------------------------------------------------ state fields
+ * Shapes are those of mod_global_variables; gom_field_info() returns element count and
+ * element size so a caller can size buffers. */
+typedef enum gom_field {
+    GOM_F_ETA_CELL = 1,        /* (N_c)        */
+    GOM_F_ETA_CELL_NEW,        /* (N_c)        */
+    GOM_F_ETA_NODE,            /* (N_n)        */
+    GOM_F_WETDRY_NODE,         /* (N_n) int    */
+    GOM_F_UN_FACE,             /* (L, N_f)     */
+    GOM_F_VN_FACE,             /* (L, N_f)     */
+    GOM_F_UN_FACE_NEW,         /* (L, N_f)     */
+    GOM_F_VN_FACE_NEW,         /* (L, N_f)     */
+    GOM_F_UN_ELM,              /* (L, N_f)     */
+    GOM_F_VN_ELM,              /* (L, N_f)     */
+    GOM_F_WN_CELL,             /* (0:L, N_c)   */
+    GOM_F_WN_CELL_NEW,         /* (0:L, N_c)   */
+    GOM_F_U_NODE,              /* (0:L, N_n)   */
+    GOM_F_V_NODE,              /* (0:L, N_n)   */
+    GOM_F_W_NODE,              /* (0:L, N_n)   */
+    GOM_F_U_FACE_LEVEL,        /* (0:L, N_f)   */
+    GOM_F_V_FACE_LEVEL,        /* (0:L, N_f)   */
+    GOM_F_DZ_CELL,             /* (L, N_c)     */
+    GOM_F_DZ_CELL_NEW,         /* (L, N_c)     */
+    GOM_F_DZHALF_CELL,         /* (0:L, N_c)   */
+    GOM_F_DZHALF_CELL_NEW,     /* (0:L, N_c)   */
+    GOM_F_DZ_FACE,             /* (L, N_f)     */
+    GOM_F_DZ_FACE_NEW,         /* (L, N_f)     */
+    GOM_F_DZHALF_FACE,         /* (0:L, N_f)   */
+    GOM_F_DZHALF_FACE_NEW,     /* (0:L, N_f)   */
+    GOM_F_DZ_NODE,             /* (L, N_n)     */
+    GOM_F_DZ_NODE_NEW,         /* (L, N_n)     */
+    GOM_F_DZHALF_NODE,         /* (0:L, N_n)   */
+    GOM_F_DZHALF_NODE_NEW,     /* (0:L, N_n)   */
+    GOM_F_TOP_LAYER_CELL,      /* (N_c) int    */
+    GOM_F_TOP_LAYER_FACE,      /* (N_f) int    */
+    GOM_F_TOP_LAYER_NODE,      /* (N_n) int    */
+    GOM_F_AINVG1,              /* (L, N_f) top-down rows */
+    GOM_F_AINVG2,              /* (L, N_f)     */
+    GOM_F_AINVDZ1,             /* (L, N_f)     */
+    GOM_F_AINVDZ2,             /* (L, N_f)     */
+    GOM_F_KH,                  /* (L, N_f)     */
+    GOM_F_AV,                  /* (0:L, N_f)   */
+    GOM_F_KV,                  /* (0:L, N_c)   */
+    GOM_F_SALT_CELL,           /* (L, N_c)     */
+    GOM_F_SALT_CELL_NEW,       /* (L, N_c)     */
+    GOM_F_TEMP_CELL,           /* (L, N_c)     */
+    GOM_F_TEMP_CELL_NEW,       /* (L, N_c)     */
+    GOM_F_SALT_NODE,           /* (L, N_n)     */
+    GOM_F_TEMP_NODE,           /* (L, N_n)     */
+    GOM_F_SALT_FACE,           /* (L, N_f)     */
+    GOM_F_TEMP_FACE,           /* (L, N_f)     */
+    GOM_F_RHO_CELL,            /* (L, N_c)     */
+    GOM_F_RHO_NODE,            /* (L, N_n)     */
+    GOM_F_RHO_FACE,            /* (L, N_f)     */
+    GOM_F_NUM_SUB_ELM,         /* (L, N_n) int num_sub_elm_iteration */
+    GOM_F_CDB,                 /* (N_f)        */
+    GOM_F_GAMMA_B,             /* (N_f)        */
+    GOM_F_QU_BOUNDARY,         /* (n_qb)       */
+    GOM_F_ELM_FOOT,            /* (L, N_f) int: element holding the final ELM foot, 0 = no walk */
+    GOM_F_ELM_NEAR_EDGE,       /* (L, N_f) int: 1 if a foot landed within 1e-12 m of an edge    */
+    GOM_F_COUNT
+} gom_field;
+
+/* ------------------------------------------------------------------ entry points */
+
+/* ABI version of the loaded library; must equal GOM_ABI_VERSION. */
+int gom_abi_version(void);
+
+/* Human-readable name of an error code (static storage). */
+const char *gom_errstr(int code);
+
+/* Last diagnostic message of a context (static to the context; "" if none). */
+const char *gom_last_message(const struct gom_ctx *ctx);
+
+/* Element count and element size (8 or 4 bytes) of a field for these dims. */
+int gom_field_info(const gom_dims *dims, int field, int64_t *count, int32_t *elem_bytes);
+
+/* Create a context: validates dims/params, copies geometry to the device.
+ * Replaces the allocation part of allocate_variables.f90 for the hot-path arrays.
+ * The caller then uploads the initial state with gom_set_field (cold or hot start). */
+int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *geom,
+               struct gom_ctx **out);
+void gom_destroy(struct gom_ctx *ctx);
+
+/* Upload / download one state field (count elements, checked against the dims). */
+int gom_set_field(struct gom_ctx *ctx, int field, const void *host, int64_t count);
+int gom_get_field(struct gom_ctx *ctx, int field, void *host, int64_t count);
+
+/* Per-step host forcing (main.f90:85-161). */
+int gom_set_forcing(struct gom_ctx *ctx, const gom_forcing *forcing);
+
+/* One entry per reference subroutine of the time loop, in main.f90 order. */
+int gom_step_bottom_friction(struct gom_ctx *ctx);   /* calculate_bottom_friction.f90:9      */
+int gom_step_boundary_velocity(struct gom_ctx *ctx); /* compute_boundary_velocity.f90:8      */
+int gom_step_advection(struct gom_ctx *ctx);         /* solve_nonlinear_advection.f90:14 / main.f90:167-177 */
+int gom_step_momentum(struct gom_ctx *ctx);          /* solve_momentum_equation.f90:15      */
+int gom_step_free_surface(struct gom_ctx *ctx, int32_t *pcg_iters); /* solve_free_surface_equation.f90:17 */
+int gom_step_velocities(struct gom_ctx *ctx);        /* solve_velocities.f90:8               */
+int gom_step_layers(struct gom_ctx *ctx);            /* update_vertical_layers_1.f90:18      */
+int gom_step_node_velocity(struct gom_ctx *ctx);     /* calculate_velocity_at_node.f90:10    */
+int gom_step_transport(struct gom_ctx *ctx);         /* solve_transport_equation_v19.f90:7   */
+int gom_step_density(struct gom_ctx *ctx);           /* calculate_density_full.f90:13 / _linear.f90:10 */
+int gom_step_swap(struct gom_ctx *ctx);              /* update_variables.f90:4 (state part)  */
+
+/* The whole per-timestep core after forcing, main.f90:94-272 order.  The CUDA library
+ * replays it as a captured CUDA graph.  pcg_iters may be NULL. */
+int gom_step_all(struct gom_ctx *ctx, int32_t *pcg_iters);
+
+/* Volume and salt mass of the wet cells: sum(area*dz_cell), sum(area*dz_cell*salt_cell),
+ * accumulated in FP64 (spec: check_conservation.f90:28-57). */
+int gom_conservation(struct gom_ctx *ctx, double *volume, double *salt_mass);
+
+/* First recorded failure; clear != 0 resets it. */
+int gom_get_status(struct gom_ctx *ctx, gom_status *status, int clear);
+
+/* Wait for all device work of the context. */
+int gom_synchronize(struct gom_ctx *ctx);
+
+/* The CUDA stream (cudaStream_t) all device work of the context is ordered on, so a caller can
+ * record events or order its own work against the core.  NULL for a CPU implementation. */
+void *gom_stream(struct gom_ctx *ctx);
+
+/* Accumulated PCG iterations since creation (diagnostic). */
+int64_t gom_pcg_iterations_total(struct gom_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GOM_CORE_H */

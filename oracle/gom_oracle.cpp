@@ -1,0 +1,2161 @@
+// gom_oracle.cpp -- TEST INFRASTRUCTURE ONLY.
+//
+// A serial FP64 CPU restatement of GOM's per-timestep core (GOM_Rv1.1.0/source), used by the
+// tests, smoke() and bench.py's CPU-baseline leg as the checker of the CUDA library.  It is
+// never linked into, loaded by or called from the product path (libgomcore.so).
+//
+// It exports the C ABI of include/gom_core.h.  Every routine follows the Fortran file and lines
+// cited beside it, in the same loop order and the same floating-point operation order, with
+// these rules:
+//   * compiled with -O2 -ffp-contract=off (no fused multiply-add), like gfortran -O2 on x86-64;
+//   * default-REAL (single precision) literals of the Fortran source are written F(x) =
+//     (double)(float)x, because gfortran promotes them from single precision;
+//   * x**2 is x*x; x**3 = (x*x)*x; x**4 = (x*x)*(x*x); x**5 = ((x*x)*x)*(x*x), GCC's powi
+//     expansion for constant exponents;
+//   * loops run serially in index order, so order-dependent reference behaviour (the stale
+//     rtemp0 of solve_momentum_equation.f90:503, the last-writer r_jk of
+//     solve_transport_equation_v19.f90:789-796) is that of a single-threaded run;
+//   * entries of the reference's automatic work arrays that the reference reads without ever
+//     assigning them in the call (solve_transport_equation_v19.f90:738,809,806,1130,1136) are
+//     defined as 0 (no flux).
+//
+// Parity is unpinned: the reference has no tests or golden vectors and cannot be compiled in
+// this environment (no Fortran compiler), so this file is checked against known-answer tests
+// derived from the mathematics (tests/test_oracle_kat.py) and the CUDA library against it.
+
+#include "../include/gom_core.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+namespace {
+
+inline double F(float x) { return (double)x; }
+
+// 1-D array with 1-based index
+template <typename T> struct A1 {
+    T *p = nullptr;
+    T &operator()(long i) const { return p[i - 1]; }
+};
+// 2-D Fortran array (lo:hi, 1:N): element (k, e)
+template <typename T> struct A2 {
+    T *p = nullptr;
+    int lo = 1, n = 0;
+    T &operator()(long k, long e) const { return p[(e - 1) * (long)n + (k - lo)]; }
+};
+
+struct Err {
+    int code = 0, site = 0, entity = 0, layer = 0;
+    double value = 0;
+};
+
+}  // namespace
+
+struct gom_ctx {
+    gom_dims d{};
+    gom_params p{};
+    int L = 0, NC = 0, NF = 0, NN = 0, NB = 0, NOB = 0, NQB = 0;
+    Err err;
+    std::string msg;
+    long long pcg_total = 0;
+
+    // ---------------- geometry storage
+    std::vector<double> g_x_node, g_y_node, g_h_node, g_x_cell, g_y_cell, g_h_cell, g_area;
+    std::vector<double> g_x_face, g_y_face, g_h_face, g_face_length, g_delta_j, g_cos_theta, g_sin_theta,
+        g_cos_theta2, g_sin_theta2, g_coriolis, g_manning, g_bf_height, g_z_level, g_delta_z;
+    std::vector<int32_t> g_adj_cells_at_node, g_adj_cellnum_at_node, g_node_count_each_element,
+        g_adj_nodes_at_node, g_adj_nodenum_at_node, g_bottom_node, g_initial_wetdry_node, g_tri_or_quad,
+        g_nodenum_at_cell, g_facenum_at_cell, g_adj_cellnum_at_cell, g_sign_in_outflow, g_bottom_cell,
+        g_ob_element_flag, g_qb_element_flag, g_adj_cellnum_at_face, g_nodenum_at_face, g_bottom_face,
+        g_boundary_type_of_face, g_isflowside3, g_ob_cell_id, g_qb_cell, g_qb_face;
+
+    // ---------------- state storage, indexed by gom_field
+    std::vector<double> fd[GOM_F_COUNT];
+    std::vector<int32_t> fi[GOM_F_COUNT];
+
+    // ---------------- forcing
+    double elapsed_time = 0, spinup_tide = 1, spinup_baroclinic = 1;
+    std::vector<double> eta_at_ob_old, eta_at_ob_new, q_add, wind_stress_normal, wind_stress_tangnt, gamma_t,
+        air_p, con_at_ob, con_at_qb, phi_sw;
+
+    // ---------------- accessors (geometry)
+    A1<double> x_node, y_node, h_node, x_cell, y_cell, h_cell, area, x_face, y_face, h_face, face_length, delta_j,
+        cos_theta, sin_theta, cos_theta2, sin_theta2, coriolis_factor, manning, bf_height, delta_z;
+    A2<double> z_level;  // (0:L, 1) used as z_level(k, 1)
+    A1<int32_t> adj_cells_at_node, adj_nodes_at_node, bottom_layer_at_node, initial_wetdry_node, tri_or_quad,
+        bottom_layer_at_element, ob_element_flag, Qb_element_flag, bottom_layer_at_face, boundary_type_of_face,
+        isflowside3, ob_cell_id, qb_cell, qb_face;
+    A2<int32_t> adj_cellnum_at_node, node_count_each_element, adj_nodenum_at_node, nodenum_at_cell,
+        facenum_at_cell, adj_cellnum_at_cell, sign_in_outflow, adj_cellnum_at_face, nodenum_at_face;
+
+    double zl(int k) const { return g_z_level[k]; }
+};
+
+namespace {
+
+struct FieldShape {
+    int lo;       // lower layer bound, or -1 for a 1-D entity array
+    int kind;     // 0 cells, 1 faces, 2 nodes, 3 qb
+    int is_int;
+    int extra;    // 0: hi = L ; 1: hi = L
+};
+
+FieldShape field_shape(int f) {
+    switch (f) {
+    case GOM_F_ETA_CELL: case GOM_F_ETA_CELL_NEW: return {-1, 0, 0, 0};
+    case GOM_F_ETA_NODE: return {-1, 2, 0, 0};
+    case GOM_F_WETDRY_NODE: return {-1, 2, 1, 0};
+    case GOM_F_UN_FACE: case GOM_F_VN_FACE: case GOM_F_UN_FACE_NEW: case GOM_F_VN_FACE_NEW:
+    case GOM_F_UN_ELM: case GOM_F_VN_ELM: case GOM_F_DZ_FACE: case GOM_F_DZ_FACE_NEW:
+    case GOM_F_AINVG1: case GOM_F_AINVG2: case GOM_F_AINVDZ1: case GOM_F_AINVDZ2: case GOM_F_KH:
+    case GOM_F_SALT_FACE: case GOM_F_TEMP_FACE: case GOM_F_RHO_FACE:
+        return {1, 1, 0, 0};
+    case GOM_F_ELM_FOOT: case GOM_F_ELM_NEAR_EDGE: return {1, 1, 1, 0};
+    case GOM_F_WN_CELL: case GOM_F_WN_CELL_NEW: case GOM_F_DZHALF_CELL: case GOM_F_DZHALF_CELL_NEW:
+    case GOM_F_KV:
+        return {0, 0, 0, 0};
+    case GOM_F_U_NODE: case GOM_F_V_NODE: case GOM_F_W_NODE: case GOM_F_DZHALF_NODE: case GOM_F_DZHALF_NODE_NEW:
+        return {0, 2, 0, 0};
+    case GOM_F_U_FACE_LEVEL: case GOM_F_V_FACE_LEVEL: case GOM_F_DZHALF_FACE: case GOM_F_DZHALF_FACE_NEW:
+    case GOM_F_AV:
+        return {0, 1, 0, 0};
+    case GOM_F_DZ_CELL: case GOM_F_DZ_CELL_NEW: case GOM_F_SALT_CELL: case GOM_F_SALT_CELL_NEW:
+    case GOM_F_TEMP_CELL: case GOM_F_TEMP_CELL_NEW: case GOM_F_RHO_CELL:
+        return {1, 0, 0, 0};
+    case GOM_F_DZ_NODE: case GOM_F_DZ_NODE_NEW: case GOM_F_SALT_NODE: case GOM_F_TEMP_NODE: case GOM_F_RHO_NODE:
+        return {1, 2, 0, 0};
+    case GOM_F_NUM_SUB_ELM: return {1, 2, 1, 0};
+    case GOM_F_TOP_LAYER_CELL: return {-1, 0, 1, 0};
+    case GOM_F_TOP_LAYER_FACE: return {-1, 1, 1, 0};
+    case GOM_F_TOP_LAYER_NODE: return {-1, 2, 1, 0};
+    case GOM_F_CDB: case GOM_F_GAMMA_B: return {-1, 1, 0, 0};
+    case GOM_F_QU_BOUNDARY: return {-1, 3, 0, 0};
+    default: return {-2, 0, 0, 0};
+    }
+}
+
+int64_t field_count(const gom_dims &d, int f, int32_t *eb) {
+    FieldShape s = field_shape(f);
+    if (s.lo == -2) return -1;
+    int64_t n = s.kind == 0 ? d.n_cells : s.kind == 1 ? d.n_faces : s.kind == 2 ? d.n_nodes : d.n_qb;
+    if (eb) *eb = s.is_int ? 4 : 8;
+    if (s.lo == -1) return n;
+    return n * (int64_t)(d.n_layers - s.lo + 1);
+}
+
+void set_err(gom_ctx *c, int code, int site, int entity, int layer, double value) {
+    if (c->err.code == 0) {
+        c->err.code = code;
+        c->err.site = site;
+        c->err.entity = entity;
+        c->err.layer = layer;
+        c->err.value = value;
+    }
+}
+
+// field accessors
+A2<double> FD(gom_ctx *c, int f) {
+    FieldShape s = field_shape(f);
+    return A2<double>{c->fd[f].data(), s.lo, c->L - s.lo + 1};
+}
+A2<int32_t> FI(gom_ctx *c, int f) {
+    FieldShape s = field_shape(f);
+    return A2<int32_t>{c->fi[f].data(), s.lo, c->L - s.lo + 1};
+}
+A1<double> FD1(gom_ctx *c, int f) { return A1<double>{c->fd[f].data()}; }
+A1<int32_t> FI1(gom_ctx *c, int f) { return A1<int32_t>{c->fi[f].data()}; }
+
+template <typename T> void copy_in(std::vector<T> &dst, const T *src, size_t n) {
+    if (src) dst.assign(src, src + n);
+    else dst.assign(n, T(0));
+}
+
+// mod_function_library.f90:49-60
+inline double calculate_area(double x1, double x2, double x3, double y1, double y2, double y3) {
+    return std::fabs((x1 - x3) * (y2 - y3) - (x2 - x3) * (y1 - y3)) / 2.0;
+}
+
+// set_geometry_1.f90:48-63
+inline int start_end_node(int k, int i, int j) {
+    int v = i + j;
+    if (v > k) v -= k;
+    return v;
+}
+
+// tridiagonal_solver.f90:15-61; solution/rhs are (nmax, nc) column-major
+bool tridiagonal_solver(int nmax, int n, int nc, const double *a, const double *b, const double *cu,
+                        const double *rhs, double *sol, double *gam) {
+    if (b[0] == 0.0) return false;
+    double den = b[0];
+    for (int i = 0; i < nc; ++i) sol[i * nmax + 0] = rhs[i * nmax + 0] / den;
+    for (int j = 2; j <= n; ++j) {
+        gam[j - 1] = cu[j - 2] / den;
+        den = b[j - 1] - a[j - 1] * gam[j - 1];
+        if (den == 0.0) return false;
+        for (int i = 0; i < nc; ++i)
+            sol[i * nmax + j - 1] = (rhs[i * nmax + j - 1] - a[j - 1] * sol[i * nmax + j - 2]) / den;
+    }
+    for (int j = n - 1; j >= 1; --j)
+        for (int i = 0; i < nc; ++i) sol[i * nmax + j - 1] = sol[i * nmax + j - 1] - gam[j] * sol[i * nmax + j];
+    return true;
+}
+
+// check_intersection.f90:14-50
+inline void check_intersection(double x1, double x2, double x3, double x4, double y1, double y2, double y3,
+                               double y4, int &iflag, double &xin, double &yin) {
+    const double small2 = 0.0;
+    iflag = 0;
+    double delta = (x2 - x1) * (y3 - y4) - (y2 - y1) * (x3 - x4);
+    double delta1 = (x3 - x1) * (y3 - y4) - (y3 - y1) * (x3 - x4);
+    double delta2 = (x2 - x1) * (y3 - y1) - (y2 - y1) * (x3 - x1);
+    if (delta != 0.0) {
+        double tt1 = delta1 / delta;
+        double tt2 = delta2 / delta;
+        if (tt1 >= -small2 && tt1 <= 1 + small2 && tt2 >= -small2 && tt2 <= 1 + small2) {
+            iflag = 1;
+            xin = x1 + (x2 - x1) * tt1;
+            yin = y1 + (y2 - y1) * tt1;
+        }
+    }
+}
+
+// bilinear_interpolation.f90:8-121; returns 0 or GOM_ELM_BILINEAR
+int bilinear_interpolation(double x1, double x2, double x3, double x4, double y1, double y2, double y3,
+                           double y4, double x, double y, double &xi, double &eta, double shapef[4]) {
+    const double small3 = F(1.e-5f);
+    const double small_06 = F(1.e-6f);
+    const double b11 = F(1.1f);
+    double axi[2], aet[2], bxy[2], root_xi[2], root_et[2];
+    double x0 = (x1 + x2 + x3 + x4) / 4.0;
+    double y0 = (y1 + y2 + y3 + y4) / 4.0;
+    axi[0] = x2 - x1 + x3 - x4;
+    axi[1] = y2 - y1 + y3 - y4;
+    aet[0] = x3 + x4 - x1 - x2;
+    aet[1] = y3 + y4 - y1 - y2;
+    bxy[0] = x1 - x2 + x3 - x4;
+    bxy[1] = y1 - y2 + y3 - y4;
+    double dxi = 2.0 * ((x3 - x4) * (y1 - y2) - (y3 - y4) * (x1 - x2));
+    double deta = 2.0 * ((x4 - x1) * (y3 - y2) - (y4 - y1) * (x3 - x2));
+    if ((std::fabs(bxy[0]) < small3 && std::fabs(bxy[1]) < small3) ||
+        (std::fabs(dxi) < small3 && std::fabs(deta) < small3)) {
+        double dd = axi[0] * aet[1] - axi[1] * aet[0];
+        if (dd == 0.0) return GOM_ELM_BILINEAR;
+        xi = 4.0 * (aet[1] * (x - x0) - aet[0] * (y - y0)) / dd;
+        eta = 4.0 * (axi[0] * (y - y0) - axi[1] * (x - x0)) / dd;
+    } else if (std::fabs(dxi) < small3 && std::fabs(deta) >= small3) {
+        eta = 4.0 * (bxy[1] * (x - x0) - bxy[0] * (y - y0)) / deta;
+        double t1 = axi[0] + eta * bxy[0], t2 = axi[1] + eta * bxy[1];
+        double dd = t1 * t1 + t2 * t2;
+        if (dd == 0.0) return GOM_ELM_BILINEAR;
+        xi = ((4.0 * (x - x0) - eta * aet[0]) * (axi[0] + eta * bxy[0]) +
+              (4.0 * (y - y0) - eta * aet[1]) * (axi[1] + eta * bxy[1])) / dd;
+    } else if (std::fabs(dxi) >= small3 && std::fabs(deta) < small3) {
+        xi = 4.0 * (bxy[1] * (x - x0) - bxy[0] * (y - y0)) / dxi;
+        double t1 = aet[0] + xi * bxy[0], t2 = aet[1] + xi * bxy[1];
+        double dd = t1 * t1 + t2 * t2;
+        if (dd == 0.0) return GOM_ELM_BILINEAR;
+        eta = ((4.0 * (x - x0) - xi * axi[0]) * (aet[0] + xi * bxy[0]) +
+               (4.0 * (y - y0) - xi * axi[1]) * (aet[1] + xi * bxy[1])) / dd;
+    } else {
+        double beta = aet[1] * axi[0] - aet[0] * axi[1] - 4 * (bxy[1] * (x - x0) - bxy[0] * (y - y0));
+        double gamma = 4.0 * (aet[0] * (y - y0) - aet[1] * (x - x0));
+        double delta = beta * beta - 4 * gamma * dxi;
+        if (delta == 0.0) {
+            xi = -beta / 2 / dxi;
+            eta = (4.0 * (bxy[1] * (x - x0) - bxy[0] * (y - y0)) - xi * dxi) / deta;
+        } else if (delta > 0) {
+            root_xi[0] = (-beta + std::sqrt(delta)) / 2 / dxi;
+            root_xi[1] = (-beta - std::sqrt(delta)) / 2 / dxi;
+            int icount = 0;
+            for (int i = 0; i < 2; ++i) {
+                root_et[i] = (4 * (bxy[1] * (x - x0) - bxy[0] * (y - y0)) - root_xi[i] * dxi) / deta;
+                if (std::fabs(root_xi[i]) <= b11 && std::fabs(root_et[i]) <= b11) {
+                    xi = root_xi[i];
+                    eta = root_et[i];
+                    icount = icount + 1;
+                }
+            }
+            if (icount == 2 && std::fabs(root_xi[0] - root_xi[1]) < small_06) {
+                // two equal roots: keep the last one
+            } else if (icount != 1) {
+                return GOM_ELM_BILINEAR;
+            }
+        } else {
+            return GOM_ELM_BILINEAR;
+        }
+    }
+    if (std::fabs(xi) > b11 || std::fabs(eta) > b11) return GOM_ELM_BILINEAR;
+    xi = std::min(1.0, std::max(xi, -1.0));
+    eta = std::min(1.0, std::max(eta, -1.0));
+    shapef[0] = (1 - xi) * (1 - eta) / 4;
+    shapef[1] = (1 + xi) * (1 - eta) / 4;
+    shapef[2] = (1 + xi) * (1 + eta) / 4;
+    shapef[3] = (1 - xi) * (1 + eta) / 4;
+    return 0;
+}
+
+// distance from (x, y) to the nearest edge line of element nel (diagnostic for foot parity)
+double edge_distance(gom_ctx *c, int nel, double x, double y) {
+    double dmin = 1e300;
+    int tq = c->tri_or_quad(nel);
+    for (int l = 1; l <= tq; ++l) {
+        int a = c->nodenum_at_cell(l, nel);
+        int b = c->nodenum_at_cell(start_end_node(tq, l, 1), nel);
+        double ex = c->x_node(b) - c->x_node(a), ey = c->y_node(b) - c->y_node(a);
+        double len = std::sqrt(ex * ex + ey * ey);
+        double cr = std::fabs(ex * (y - c->y_node(a)) - ey * (x - c->x_node(a))) / len;
+        dmin = std::min(dmin, cr);
+    }
+    return dmin;
+}
+
+// ============================================================================================
+// search_straight_line.f90:15-399 (i_which_backtrack = 1).  Returns 0 or a GOM_ELM_* site.
+int search_straight_line(gom_ctx *c, int &nnel, int &jlev, double time, double x0, double y0, double z0,
+                         double &xt, double &yt, double &zt, int &nfl) {
+    const double small_06 = F(1.e-6f);
+    A1<double> eta_cell = FD1(c, GOM_F_ETA_CELL);
+    A1<int32_t> top = FI1(c, GOM_F_TOP_LAYER_CELL);
+    auto top_el = [&](int e) { return e == 0 ? 0 : top(e); };
+    const double MSL = c->p.msl;
+    int L = c->L;
+    if (top_el(nnel) == 0 || MSL - c->h_cell(nnel) > MSL + eta_cell(nnel)) return GOM_ELM_START_DRY;
+    nfl = 0;
+    double trm = time;
+    int nel = nnel;
+    double area1 = 0.0, area2 = 0.0;
+    int tq = c->tri_or_quad(nel);
+    for (int l = 1; l <= tq; ++l) {
+        int node1 = c->nodenum_at_cell(l, nel);
+        int node2 = c->nodenum_at_cell(start_end_node(tq, l, 1), nel);
+        area1 = area1 + std::fabs(calculate_area(c->x_node(node1), c->x_node(node2), x0, c->y_node(node1),
+                                                 c->y_node(node2), y0));
+        area2 = area2 + std::fabs(calculate_area(c->x_node(node1), c->x_node(node2), xt, c->y_node(node1),
+                                                 c->y_node(node2), yt));
+    }
+    double ae = std::fabs(area1 - c->area(nel)) / c->area(nel);
+    if (ae > small_06) return GOM_ELM_START_OUTSIDE;
+    ae = std::fabs(area2 - c->area(nel)) / c->area(nel);
+    if (ae < small_06) {
+        nnel = nel;
+    } else {
+        const double c1 = 1.0 - 1.0e-4;
+        double xcg = c1 * x0 + 1.0e-4 * c->x_cell(nel);
+        double ycg = c1 * y0 + 1.0e-4 * c->y_cell(nel);
+        double pathl = std::sqrt((xt - xcg) * (xt - xcg) + (yt - ycg) * (yt - ycg));
+        if ((xcg == xt && ycg == yt) || pathl == 0.0) return GOM_ELM_ZERO_PATH;
+        int iflag = 0, nel_j = 0;
+        double xin = 0, yin = 0;
+        for (int l = 1; l <= tq; ++l) {
+            int jd1 = c->nodenum_at_cell(start_end_node(tq, l, 1), nel);
+            int jd2 = c->nodenum_at_cell(start_end_node(tq, l, 2), nel);
+            check_intersection(xcg, xt, c->x_node(jd1), c->x_node(jd2), ycg, yt, c->y_node(jd1), c->y_node(jd2),
+                               iflag, xin, yin);
+            if (iflag == 1) {
+                nel_j = l;
+                break;
+            }
+        }
+        if (iflag == 0) return GOM_ELM_NO_FIRST_EDGE;
+        double zin = z0;
+        int iteration = 0;
+        for (;;) {
+            iteration = iteration + 1;
+            if (iteration > 1000) {
+                nfl = 1;
+                xt = xin;
+                yt = yin;
+                zt = zin;
+                nnel = nel;
+                break;
+            }
+            int tqn = c->tri_or_quad(nel);
+            int md1 = c->nodenum_at_cell(start_end_node(tqn, nel_j, 1), nel);
+            int md2 = c->nodenum_at_cell(start_end_node(tqn, nel_j, 2), nel);
+            double dist = std::sqrt((xin - xt) * (xin - xt) + (yin - yt) * (yin - yt));
+            if (dist / pathl > 1.0 + 1.0e-4) return GOM_ELM_OVERSHOOT;
+            zin = zt - dist / pathl * (zt - zin);
+            trm = trm * dist / pathl;
+            pathl = std::sqrt((xin - xt) * (xin - xt) + (yin - yt) * (yin - yt));
+            if (pathl == 0.0 || trm == 0.0) return GOM_ELM_ZERO_REMAIN;
+            int iter_temp = 0;
+            int adjc = c->adj_cellnum_at_cell(nel_j, nel);
+            if (adjc == 0 || top_el(adjc) == 0) {
+                iter_temp = 1;
+                int isd = c->facenum_at_cell(nel_j, nel);
+                if (c->nodenum_at_face(1, isd) + c->nodenum_at_face(2, isd) != md1 + md2) return GOM_ELM_FACE_MISMATCH;
+                xin = c1 * xin + 1.0e-4 * c->x_cell(nel);
+                yin = c1 * yin + 1.0e-4 * c->y_cell(nel);
+                nfl = 1;
+                xt = xin;
+                yt = yin;
+                zt = zin;
+                nnel = nel;
+                break;
+            }
+            if (iter_temp == 0) nel = adjc;
+            area1 = 0.0;
+            tqn = c->tri_or_quad(nel);
+            for (int l = 1; l <= tqn; ++l) {
+                int k1 = c->nodenum_at_cell(l, nel);
+                int k2 = c->nodenum_at_cell(start_end_node(tqn, l, 1), nel);
+                area1 = area1 + std::fabs(calculate_area(c->x_node(k1), c->x_node(k2), xt, c->y_node(k1),
+                                                         c->y_node(k2), yt));
+            }
+            ae = std::fabs(area1 - c->area(nel)) / c->area(nel);
+            if (ae < small_06) {
+                nnel = nel;
+                break;
+            }
+            bool found = false;
+            for (int l = 1; l <= tqn; ++l) {
+                int jd1 = c->nodenum_at_cell(start_end_node(tqn, l, 1), nel);
+                int jd2 = c->nodenum_at_cell(start_end_node(tqn, l, 2), nel);
+                if ((jd1 == md1 && jd2 == md2) || (jd2 == md1 && jd1 == md2)) continue;
+                check_intersection(xcg, xt, c->x_node(jd1), c->x_node(jd2), ycg, yt, c->y_node(jd1),
+                                   c->y_node(jd2), iflag, xin, yin);
+                if (iflag == 1) {
+                    nel_j = l;
+                    found = true;
+                    break;
+                }
+            }
+            if (found) continue;
+            if (iflag == 0) return GOM_ELM_NO_NEXT_EDGE;
+        }
+    }
+    if (top_el(nnel) == 0 || MSL - c->h_cell(nnel) > MSL + eta_cell(nnel)) return GOM_ELM_END_DRY;
+    zt = std::min(std::max(zt, MSL - c->h_cell(nnel)), MSL + eta_cell(nnel));
+    if (zt <= c->zl(0)) return GOM_ELM_Z_RANGE;
+    if (zt > c->zl(L)) return GOM_ELM_Z_RANGE;
+    for (int k = 0; k <= L - 1; ++k) {
+        if (zt > c->zl(k) && zt <= c->zl(k + 1)) {
+            jlev = k + 1;
+            break;
+        }
+    }
+    jlev = std::min(std::max(jlev, (int)c->bottom_layer_at_element(nnel)), (int)top_el(nnel));
+    return 0;
+}
+
+// ELM_backtrace_v1.f90:15-200 (i_which_backtrack = 1).  Returns 0 or a GOM_ELM_* site.
+int elm_backtrace(gom_ctx *c, int bt_step, double bt_dt, double &uuint, double &vvint, double &wwint,
+                  double &x0, double &y0, double &z0, int &nnel, int &jlev, int &near_edge) {
+    const double small_06 = F(1.e-6f);
+    A2<double> u_node = FD(c, GOM_F_U_NODE), v_node = FD(c, GOM_F_V_NODE), w_node = FD(c, GOM_F_W_NODE);
+    A2<double> dz_cell = FD(c, GOM_F_DZ_CELL);
+    A1<double> eta_cell = FD1(c, GOM_F_ETA_CELL);
+    A1<int32_t> top = FI1(c, GOM_F_TOP_LAYER_CELL);
+    double xt = 0, yt = 0, zt = 0;
+    double vxl[4][2], vyl[4][2], vzl[4][2], vxn[4], vyn[4], vzn[4], staint[4];
+    for (int idt = 1; idt <= bt_step; ++idt) {
+        xt = x0 - bt_dt * uuint;
+        yt = y0 - bt_dt * vvint;
+        zt = z0 - bt_dt * wwint;
+        int nfl = 0;
+        int e = search_straight_line(c, nnel, jlev, bt_dt, x0, y0, z0, xt, yt, zt, nfl);
+        if (e) return e;
+        int tq = c->tri_or_quad(nnel);
+        for (int l = 1; l <= tq; ++l) {
+            int nd = c->nodenum_at_cell(l, nnel);
+            for (int k2 = 1; k2 <= 2; ++k2) {
+                int lev = jlev + k2 - 2;
+                vxl[l - 1][k2 - 1] = u_node(lev, nd);
+                vyl[l - 1][k2 - 1] = v_node(lev, nd);
+                vzl[l - 1][k2 - 1] = w_node(lev, nd);
+            }
+        }
+        double zup = (jlev == top(nnel)) ? c->p.msl + eta_cell(nnel) : c->zl(jlev);
+        if (zt > zup) return GOM_ELM_Z_ABOVE;
+        double zrat = (zup - zt) / dz_cell(jlev, nnel);
+        for (int l = 1; l <= tq; ++l) {
+            vxn[l - 1] = vxl[l - 1][1] * (1 - zrat) + vxl[l - 1][0] * zrat;
+            vyn[l - 1] = vyl[l - 1][1] * (1 - zrat) + vyl[l - 1][0] * zrat;
+            vzn[l - 1] = vzl[l - 1][1] * (1 - zrat) + vzl[l - 1][0] * zrat;
+        }
+        int node1 = c->nodenum_at_cell(1, nnel), node2 = c->nodenum_at_cell(2, nnel),
+            node3 = c->nodenum_at_cell(3, nnel);
+        if (tq == 3) {
+            double ar = c->area(nnel);
+            staint[0] = calculate_area(xt, c->x_node(node2), c->x_node(node3), yt, c->y_node(node2), c->y_node(node3)) / ar;
+            staint[1] = calculate_area(c->x_node(node1), xt, c->x_node(node3), c->y_node(node1), yt, c->y_node(node3)) / ar;
+            staint[2] = calculate_area(c->x_node(node1), c->x_node(node2), xt, c->y_node(node1), c->y_node(node2), yt) / ar;
+            staint[0] = std::max(0.0, std::min(1.0, staint[0]));
+            staint[1] = std::max(0.0, std::min(1.0, staint[1]));
+            if (staint[0] + staint[1] > 1) {
+                staint[2] = 0;
+                staint[1] = 1.0 - staint[0];
+            } else {
+                staint[2] = 1.0 - staint[0] - staint[1];
+            }
+        } else {
+            int node4 = c->nodenum_at_cell(4, nnel);
+            double aa1 = calculate_area(c->x_node(node1), c->x_node(node2), xt, c->y_node(node1), c->y_node(node2), yt);
+            double aa2 = calculate_area(c->x_node(node2), c->x_node(node3), xt, c->y_node(node2), c->y_node(node3), yt);
+            double aa3 = calculate_area(c->x_node(node3), c->x_node(node4), xt, c->y_node(node3), c->y_node(node4), yt);
+            double aa4 = calculate_area(c->x_node(node4), c->x_node(node1), xt, c->y_node(node4), c->y_node(node1), yt);
+            double aa = std::fabs(aa1) + std::fabs(aa2) + std::fabs(aa3) + std::fabs(aa4);
+            if (std::fabs(aa - c->area(nnel)) / c->area(nnel) > small_06) return GOM_ELM_QUAD_OUTSIDE;
+            double csi, etta;
+            int b = bilinear_interpolation(c->x_node(node1), c->x_node(node2), c->x_node(node3), c->x_node(node4),
+                                           c->y_node(node1), c->y_node(node2), c->y_node(node3), c->y_node(node4), xt,
+                                           yt, csi, etta, staint);
+            if (b) return b;
+        }
+        uuint = 0.0;
+        vvint = 0.0;
+        wwint = 0.0;
+        for (int j = 1; j <= tq; ++j) {
+            uuint = uuint + vxn[j - 1] * staint[j - 1];
+            vvint = vvint + vyn[j - 1] * staint[j - 1];
+            wwint = wwint + vzn[j - 1] * staint[j - 1];
+        }
+        if (edge_distance(c, nnel, xt, yt) < 1e-12) near_edge = 1;
+        if (nfl == 1) break;
+        x0 = xt;
+        y0 = yt;
+        z0 = zt;
+    }
+    return 0;
+}
+
+}  // namespace
+
+// ============================================================================================
+extern "C" {
+
+int gom_abi_version(void) { return GOM_ABI_VERSION; }
+
+const char *gom_errstr(int code) {
+    switch (code) {
+    case GOM_OK: return "ok";
+    case GOM_E_ARG: return "bad argument";
+    case GOM_E_CUDA: return "CUDA error";
+    case GOM_E_NOT_SPD: return "free-surface matrix not positive definite";
+    case GOM_E_ZERO_PIVOT: return "tridiagonal solver zero pivot";
+    case GOM_E_ELM: return "ELM backtracking geometry failure";
+    case GOM_E_DRY: return "dry element or boundary where water is required";
+    case GOM_E_LAYER: return "impossible elevation or layer";
+    case GOM_E_DENSITY: return "density, salinity or temperature out of range";
+    case GOM_E_PCG_MAXIT: return "PCG reached max_iteration_pcg";
+    case GOM_E_TIMEOUT: return "device wait timed out";
+    case GOM_E_NOMEM: return "out of device memory";
+    default: return "unknown error";
+    }
+}
+
+const char *gom_last_message(const gom_ctx *ctx) { return ctx ? ctx->msg.c_str() : ""; }
+
+int gom_field_info(const gom_dims *dims, int field, int64_t *count, int32_t *elem_bytes) {
+    if (!dims) return GOM_E_ARG;
+    int32_t eb = 0;
+    int64_t n = field_count(*dims, field, &eb);
+    if (n < 0) return GOM_E_ARG;
+    if (count) *count = n;
+    if (elem_bytes) *elem_bytes = eb;
+    return GOM_OK;
+}
+
+int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g, gom_ctx **out) {
+    if (!dims || !params || !g || !out) return GOM_E_ARG;
+    const gom_dims &d = *dims;
+    if (d.n_cells <= 0 || d.n_faces <= 0 || d.n_nodes <= 0 || d.n_layers <= 0 || d.max_nb <= 0 || d.n_ob < 0 ||
+        d.n_qb < 0)
+        return GOM_E_ARG;
+    if (params->transport_flag && params->is_salt == 0 && params->is_temp == 1) return GOM_E_ARG;
+    gom_ctx *c = new gom_ctx();
+    c->d = d;
+    c->p = *params;
+    c->L = d.n_layers;
+    c->NC = d.n_cells;
+    c->NF = d.n_faces;
+    c->NN = d.n_nodes;
+    c->NB = d.max_nb;
+    c->NOB = d.n_ob;
+    c->NQB = d.n_qb;
+    size_t NC = d.n_cells, NF = d.n_faces, NN = d.n_nodes, NB = d.max_nb, L = d.n_layers;
+    copy_in(c->g_x_node, g->x_node, NN);
+    copy_in(c->g_y_node, g->y_node, NN);
+    copy_in(c->g_h_node, g->h_node, NN);
+    copy_in(c->g_adj_cells_at_node, g->adj_cells_at_node, NN);
+    copy_in(c->g_adj_cellnum_at_node, g->adj_cellnum_at_node, NB * NN);
+    copy_in(c->g_node_count_each_element, g->node_count_each_element, NB * NN);
+    copy_in(c->g_adj_nodes_at_node, g->adj_nodes_at_node, NN);
+    copy_in(c->g_adj_nodenum_at_node, g->adj_nodenum_at_node, (NB + 1) * NN);
+    copy_in(c->g_bottom_node, g->bottom_layer_at_node, NN);
+    copy_in(c->g_initial_wetdry_node, g->initial_wetdry_node, NN);
+    copy_in(c->g_x_cell, g->x_cell, NC);
+    copy_in(c->g_y_cell, g->y_cell, NC);
+    copy_in(c->g_h_cell, g->h_cell, NC);
+    copy_in(c->g_area, g->area, NC);
+    copy_in(c->g_tri_or_quad, g->tri_or_quad, NC);
+    copy_in(c->g_nodenum_at_cell, g->nodenum_at_cell, 4 * NC);
+    copy_in(c->g_facenum_at_cell, g->facenum_at_cell, 4 * NC);
+    copy_in(c->g_adj_cellnum_at_cell, g->adj_cellnum_at_cell, 4 * NC);
+    copy_in(c->g_sign_in_outflow, g->sign_in_outflow, 4 * NC);
+    copy_in(c->g_bottom_cell, g->bottom_layer_at_element, NC);
+    copy_in(c->g_ob_element_flag, g->ob_element_flag, NC);
+    copy_in(c->g_qb_element_flag, g->qb_element_flag, NC);
+    copy_in(c->g_x_face, g->x_face, NF);
+    copy_in(c->g_y_face, g->y_face, NF);
+    copy_in(c->g_h_face, g->h_face, NF);
+    copy_in(c->g_face_length, g->face_length, NF);
+    copy_in(c->g_delta_j, g->delta_j, NF);
+    copy_in(c->g_cos_theta, g->cos_theta, NF);
+    copy_in(c->g_sin_theta, g->sin_theta, NF);
+    copy_in(c->g_cos_theta2, g->cos_theta2, NF);
+    copy_in(c->g_sin_theta2, g->sin_theta2, NF);
+    copy_in(c->g_adj_cellnum_at_face, g->adj_cellnum_at_face, 2 * NF);
+    copy_in(c->g_nodenum_at_face, g->nodenum_at_face, 2 * NF);
+    copy_in(c->g_bottom_face, g->bottom_layer_at_face, NF);
+    copy_in(c->g_boundary_type_of_face, g->boundary_type_of_face, NF);
+    copy_in(c->g_isflowside3, g->isflowside3, NF);
+    copy_in(c->g_coriolis, g->coriolis_factor, NF);
+    copy_in(c->g_manning, g->manning, NF);
+    copy_in(c->g_bf_height, g->bf_height, NF);
+    copy_in(c->g_ob_cell_id, g->ob_cell_id, (size_t)d.n_ob);
+    copy_in(c->g_qb_cell, g->qb_cell, (size_t)d.n_qb);
+    copy_in(c->g_qb_face, g->qb_face, (size_t)d.n_qb);
+    copy_in(c->g_z_level, g->z_level, L + 1);
+    copy_in(c->g_delta_z, g->delta_z, L);
+
+    c->x_node.p = c->g_x_node.data();
+    c->y_node.p = c->g_y_node.data();
+    c->h_node.p = c->g_h_node.data();
+    c->x_cell.p = c->g_x_cell.data();
+    c->y_cell.p = c->g_y_cell.data();
+    c->h_cell.p = c->g_h_cell.data();
+    c->area.p = c->g_area.data();
+    c->x_face.p = c->g_x_face.data();
+    c->y_face.p = c->g_y_face.data();
+    c->h_face.p = c->g_h_face.data();
+    c->face_length.p = c->g_face_length.data();
+    c->delta_j.p = c->g_delta_j.data();
+    c->cos_theta.p = c->g_cos_theta.data();
+    c->sin_theta.p = c->g_sin_theta.data();
+    c->cos_theta2.p = c->g_cos_theta2.data();
+    c->sin_theta2.p = c->g_sin_theta2.data();
+    c->coriolis_factor.p = c->g_coriolis.data();
+    c->manning.p = c->g_manning.data();
+    c->bf_height.p = c->g_bf_height.data();
+    c->delta_z.p = c->g_delta_z.data();
+    c->adj_cells_at_node.p = c->g_adj_cells_at_node.data();
+    c->adj_nodes_at_node.p = c->g_adj_nodes_at_node.data();
+    c->bottom_layer_at_node.p = c->g_bottom_node.data();
+    c->initial_wetdry_node.p = c->g_initial_wetdry_node.data();
+    c->tri_or_quad.p = c->g_tri_or_quad.data();
+    c->bottom_layer_at_element.p = c->g_bottom_cell.data();
+    c->ob_element_flag.p = c->g_ob_element_flag.data();
+    c->Qb_element_flag.p = c->g_qb_element_flag.data();
+    c->bottom_layer_at_face.p = c->g_bottom_face.data();
+    c->boundary_type_of_face.p = c->g_boundary_type_of_face.data();
+    c->isflowside3.p = c->g_isflowside3.data();
+    c->ob_cell_id.p = c->g_ob_cell_id.data();
+    c->qb_cell.p = c->g_qb_cell.data();
+    c->qb_face.p = c->g_qb_face.data();
+    c->adj_cellnum_at_node = A2<int32_t>{c->g_adj_cellnum_at_node.data(), 1, (int)NB};
+    c->node_count_each_element = A2<int32_t>{c->g_node_count_each_element.data(), 1, (int)NB};
+    c->adj_nodenum_at_node = A2<int32_t>{c->g_adj_nodenum_at_node.data(), 0, (int)NB + 1};
+    c->nodenum_at_cell = A2<int32_t>{c->g_nodenum_at_cell.data(), 1, 4};
+    c->facenum_at_cell = A2<int32_t>{c->g_facenum_at_cell.data(), 1, 4};
+    c->adj_cellnum_at_cell = A2<int32_t>{c->g_adj_cellnum_at_cell.data(), 1, 4};
+    c->sign_in_outflow = A2<int32_t>{c->g_sign_in_outflow.data(), 1, 4};
+    c->adj_cellnum_at_face = A2<int32_t>{c->g_adj_cellnum_at_face.data(), 1, 2};
+    c->nodenum_at_face = A2<int32_t>{c->g_nodenum_at_face.data(), 1, 2};
+
+    for (int f = 1; f < GOM_F_COUNT; ++f) {
+        int32_t eb = 0;
+        int64_t n = field_count(d, f, &eb);
+        if (n < 0) continue;
+        if (eb == 4) c->fi[f].assign((size_t)n, 0);
+        else c->fd[f].assign((size_t)n, 0.0);
+    }
+    c->eta_at_ob_old.assign(d.n_ob, 0.0);
+    c->eta_at_ob_new.assign(d.n_ob, 0.0);
+    c->q_add.assign(d.n_qb, 0.0);
+    c->wind_stress_normal.assign(NF, 0.0);
+    c->wind_stress_tangnt.assign(NF, 0.0);
+    c->gamma_t.assign(NF, 0.0);
+    c->air_p.assign(NN, 0.0);
+    int nt = std::max(1, params->trans_sub_iter);
+    c->con_at_ob.assign((size_t)d.n_ob * 2 * nt, 0.0);
+    c->con_at_qb.assign((size_t)d.n_qb * 2 * nt, 0.0);
+    c->phi_sw.assign(NC, 0.0);
+    *out = c;
+    return GOM_OK;
+}
+
+void gom_destroy(gom_ctx *ctx) { delete ctx; }
+
+int gom_set_field(gom_ctx *c, int field, const void *host, int64_t count) {
+    if (!c || !host) return GOM_E_ARG;
+    int32_t eb = 0;
+    int64_t n = field_count(c->d, field, &eb);
+    if (n < 0 || n != count) return GOM_E_ARG;
+    if (eb == 4) std::memcpy(c->fi[field].data(), host, (size_t)n * 4);
+    else std::memcpy(c->fd[field].data(), host, (size_t)n * 8);
+    return GOM_OK;
+}
+
+int gom_get_field(gom_ctx *c, int field, void *host, int64_t count) {
+    if (!c || !host) return GOM_E_ARG;
+    int32_t eb = 0;
+    int64_t n = field_count(c->d, field, &eb);
+    if (n < 0 || n != count) return GOM_E_ARG;
+    if (eb == 4) std::memcpy(host, c->fi[field].data(), (size_t)n * 4);
+    else std::memcpy(host, c->fd[field].data(), (size_t)n * 8);
+    return GOM_OK;
+}
+
+int gom_set_forcing(gom_ctx *c, const gom_forcing *f) {
+    if (!c || !f) return GOM_E_ARG;
+    c->elapsed_time = f->elapsed_time;
+    c->spinup_tide = f->spinup_tide;
+    c->spinup_baroclinic = f->spinup_baroclinic;
+    int nt = std::max(1, c->p.trans_sub_iter);
+    auto up = [](std::vector<double> &v, const double *s) {
+        if (s) std::memcpy(v.data(), s, v.size() * sizeof(double));
+    };
+    up(c->eta_at_ob_old, f->eta_at_ob_old);
+    up(c->eta_at_ob_new, f->eta_at_ob_new);
+    up(c->q_add, f->q_add);
+    up(c->wind_stress_normal, f->wind_stress_normal);
+    up(c->wind_stress_tangnt, f->wind_stress_tangnt);
+    up(c->gamma_t, f->gamma_t);
+    up(c->air_p, f->air_p);
+    up(c->con_at_ob, f->con_at_ob);
+    up(c->con_at_qb, f->con_at_qb);
+    up(c->phi_sw, f->phi_sw);
+    (void)nt;
+    return GOM_OK;
+}
+
+int gom_get_status(gom_ctx *c, gom_status *s, int clear) {
+    if (!c || !s) return GOM_E_ARG;
+    s->code = c->err.code;
+    s->site = c->err.site;
+    s->entity = c->err.entity;
+    s->layer = c->err.layer;
+    s->value = c->err.value;
+    if (clear) c->err = Err();
+    return GOM_OK;
+}
+
+int gom_synchronize(gom_ctx *c) { return c ? GOM_OK : GOM_E_ARG; }
+
+int64_t gom_pcg_iterations_total(gom_ctx *c) { return c ? c->pcg_total : 0; }
+
+void *gom_stream(gom_ctx *c) {
+    (void)c;
+    return nullptr;
+}
+
+// ============================================================================================
+// calculate_bottom_friction.f90:9-73 (bf_flag 3 = constant Cd, an extension for quadratic drag)
+int gom_step_bottom_friction(gom_ctx *c) {
+    if (!c) return GOM_E_ARG;
+    A1<double> Cdb = FD1(c, GOM_F_CDB), Gamma_B = FD1(c, GOM_F_GAMMA_B);
+    A2<double> un_face = FD(c, GOM_F_UN_FACE), vn_face = FD(c, GOM_F_VN_FACE), dzhalf_face = FD(c, GOM_F_DZHALF_FACE);
+    const gom_params &p = c->p;
+    for (int j = 1; j <= c->NF; ++j) {
+        Cdb(j) = 0.0;
+        Gamma_B(j) = 0.0;
+    }
+    if (p.bf_flag == 1) {
+        double expo = 1.0 / 6.0;
+        for (int j = 1; j <= c->NF; ++j) {
+            if (c->h_face(j) > p.dry_depth) {
+                double hydraulic_radius = std::max(1.0, c->h_face(j));
+                double chezy_coef = std::pow(hydraulic_radius, expo) / c->manning(j);
+                double rtemp = p.gravity / (chezy_coef * chezy_coef);
+                Cdb(j) = rtemp;
+                int k = c->bottom_layer_at_face(j);
+                Gamma_B(j) = Cdb(j) * std::sqrt(un_face(k, j) * un_face(k, j) + vn_face(k, j) * vn_face(k, j));
+            }
+        }
+    } else if (p.bf_flag == 2) {
+        for (int j = 1; j <= c->NF; ++j) {
+            if (c->h_face(j) > p.dry_depth) {
+                int k = c->bottom_layer_at_face(j);
+                double lg = std::log(std::max(0.5, dzhalf_face(k - 1, j)) / c->bf_height(j));
+                double rtemp = p.von_karman * p.von_karman / (lg * lg);
+                Cdb(j) = rtemp;
+                Gamma_B(j) = Cdb(j) * std::sqrt(un_face(k, j) * un_face(k, j) + vn_face(k, j) * vn_face(k, j));
+            }
+        }
+    } else if (p.bf_flag == 3) {
+        for (int j = 1; j <= c->NF; ++j) {
+            if (c->h_face(j) > p.dry_depth) {
+                int k = c->bottom_layer_at_face(j);
+                Cdb(j) = p.cd_const;
+                Gamma_B(j) = Cdb(j) * std::sqrt(un_face(k, j) * un_face(k, j) + vn_face(k, j) * vn_face(k, j));
+            }
+        }
+    }
+    return GOM_OK;
+}
+
+// compute_boundary_velocity.f90:60-94 (river faces; Q_add comes from the host's calculate_Q)
+int gom_step_boundary_velocity(gom_ctx *c) {
+    if (!c) return GOM_E_ARG;
+    A1<double> Qu = FD1(c, GOM_F_QU_BOUNDARY), eta_node = FD1(c, GOM_F_ETA_NODE);
+    for (int i = 1; i <= c->NQB; ++i) {
+        int j = c->qb_face(i);
+        double channel_width = c->face_length(j);
+        int n1 = c->nodenum_at_face(1, j), n2 = c->nodenum_at_face(2, j);
+        double temp_depth = c->h_face(j) + (eta_node(n1) + eta_node(n2)) * 0.5;
+        if (temp_depth < c->p.dry_depth) {
+            set_err(c, GOM_E_DRY, 80, i, 0, temp_depth);
+            return GOM_E_DRY;
+        }
+        Qu(i) = -c->q_add[i - 1] / (channel_width * temp_depth);
+    }
+    return GOM_OK;
+}
+
+// main.f90:167-177 and solve_nonlinear_advection.f90:14-204
+int gom_step_advection(gom_ctx *c) {
+    if (!c) return GOM_E_ARG;
+    const gom_params &p = c->p;
+    int L = c->L;
+    A2<double> un_ELM = FD(c, GOM_F_UN_ELM), vn_ELM = FD(c, GOM_F_VN_ELM), un_face = FD(c, GOM_F_UN_FACE),
+               vn_face = FD(c, GOM_F_VN_FACE);
+    A2<int32_t> foot = FI(c, GOM_F_ELM_FOOT), near = FI(c, GOM_F_ELM_NEAR_EDGE);
+    std::fill(c->fi[GOM_F_ELM_FOOT].begin(), c->fi[GOM_F_ELM_FOOT].end(), 0);
+    std::fill(c->fi[GOM_F_ELM_NEAR_EDGE].begin(), c->fi[GOM_F_ELM_NEAR_EDGE].end(), 0);
+    if (p.advection_flag == 0) {
+        for (int j = 1; j <= c->NF; ++j)
+            for (int k = 1; k <= L; ++k) {
+                un_ELM(k, j) = un_face(k, j);
+                vn_ELM(k, j) = vn_face(k, j);
+            }
+        return GOM_OK;
+    }
+    A2<double> u_node = FD(c, GOM_F_U_NODE), v_node = FD(c, GOM_F_V_NODE), w_node = FD(c, GOM_F_W_NODE),
+               dz_cell = FD(c, GOM_F_DZ_CELL);
+    A2<int32_t> nsub = FI(c, GOM_F_NUM_SUB_ELM);
+    A1<double> eta_cell = FD1(c, GOM_F_ETA_CELL);
+    A1<int32_t> top_el = FI1(c, GOM_F_TOP_LAYER_CELL), top_f = FI1(c, GOM_F_TOP_LAYER_FACE);
+    std::fill(c->fd[GOM_F_UN_ELM].begin(), c->fd[GOM_F_UN_ELM].end(), 0.0);
+    std::fill(c->fd[GOM_F_VN_ELM].begin(), c->fd[GOM_F_VN_ELM].end(), 0.0);
+    // :52-87 adaptive substep count
+    if (p.elm_backtrace_flag == 1) {
+        double dt = p.dt;
+        for (int i = 1; i <= c->NN; ++i) {
+            for (int k = 1; k <= L; ++k) {
+                double summ = 0.0;
+                int nadj = c->adj_cells_at_node(i);
+                for (int j = 1; j <= nadj; ++j) {
+                    int ie = c->adj_cellnum_at_node(j, i);
+                    int id = c->node_count_each_element(j, i);
+                    double devm = 0.0;
+                    int tq = c->tri_or_quad(ie);
+                    for (int l = 1; l <= 2; ++l) {
+                        int nd = (l == 1) ? c->nodenum_at_cell(start_end_node(tq, id, 1), ie)
+                                          : c->nodenum_at_cell(start_end_node(tq, id, tq - 1), ie);
+                        double dx = c->x_node(i) - c->x_node(nd), dy = c->y_node(i) - c->y_node(nd);
+                        double rl = std::sqrt(dx * dx + dy * dy);
+                        double uvel1 = (u_node(k, i) + u_node(k - 1, i)) * 0.5;
+                        double uvel2 = (u_node(k, nd) + u_node(k - 1, nd)) * 0.5;
+                        double vvel1 = (v_node(k, i) + v_node(k - 1, i)) * 0.5;
+                        double vvel2 = (v_node(k, nd) + v_node(k - 1, nd)) * 0.5;
+                        double du = uvel1 - uvel2, dv = vvel1 - vvel2;
+                        double dev = std::sqrt(du * du + dv * dv) / rl * dt;
+                        if (dev > devm) devm = dev;
+                    }
+                    double velo_w = (w_node(k, i) + w_node(k - 1, i)) * 0.5;
+                    int iw = (int)(2 * velo_w * dt / p.delta_z_min);
+                    int idelta = std::max((int)(devm / F(1.e-1f)), iw);
+                    summ = summ + (double)idelta / nadj;
+                }
+                nsub(k, i) = std::max(p.elm_min_iter, std::min(p.elm_max_iter, (int)summ));
+            }
+        }
+    }
+    // :94-201 face loop
+    for (int j = 1; j <= c->NF; ++j) {
+        int n1 = c->nodenum_at_face(1, j), n2 = c->nodenum_at_face(2, j);
+        double adv_turn_off_depth = std::max(c->h_node(n1), c->h_node(n2));
+        int b = c->bottom_layer_at_face(j), t = top_f(j);
+        if (std::fabs(adv_turn_off_depth) < p.adv_onoff_depth) {
+            for (int k = b; k <= t; ++k) {
+                un_ELM(k, j) = un_face(k, j);
+                vn_ELM(k, j) = vn_face(k, j);
+            }
+            continue;
+        }
+        int a1 = c->adj_cellnum_at_face(1, j), a2 = c->adj_cellnum_at_face(2, j);
+        int ie0;
+        if (top_el(a1) != 0) ie0 = a1;
+        else if (a2 != 0 && top_el(a2) != 0) ie0 = a2;
+        else {
+            for (int k = b; k <= t; ++k) {
+                un_ELM(k, j) = un_face(k, j);
+                vn_ELM(k, j) = vn_face(k, j);
+            }
+            continue;
+        }
+        for (int k = b; k <= t; ++k) {
+            int nnel = ie0, jlev = k;
+            double x0 = c->x_face(j), y0 = c->y_face(j), z0;
+            if (k == top_el(nnel)) z0 = p.msl + eta_cell(nnel) - dz_cell(k, nnel) * 0.5;
+            else z0 = c->zl(k) - dz_cell(k, nnel) * 0.5;
+            double uuint = un_face(k, j) * c->cos_theta(j) - vn_face(k, j) * c->sin_theta(j);
+            double vvint = un_face(k, j) * c->sin_theta(j) + vn_face(k, j) * c->cos_theta(j);
+            double wdown = (w_node(k - 1, n1) + w_node(k - 1, n2)) * 0.5;
+            double wup = (w_node(k, n1) + w_node(k, n2)) * 0.5;
+            double wwint = (wdown + wup) * 0.5;
+            double vmag = std::sqrt(uuint * uuint + vvint * vvint + wwint * wwint);
+            if (vmag <= F(1.e-4f)) {
+                un_ELM(k, j) = un_face(k, j);
+                vn_ELM(k, j) = vn_face(k, j);
+            } else {
+                int bt_step = (int)((double)(nsub(k, n1) + nsub(k, n2)) * 0.5);
+                double bt_dt = p.dt / bt_step;
+                int ne = 0;
+                int e = elm_backtrace(c, bt_step, bt_dt, uuint, vvint, wwint, x0, y0, z0, nnel, jlev, ne);
+                if (e) {
+                    set_err(c, GOM_E_ELM, e, j, k, 0.0);
+                    return GOM_E_ELM;
+                }
+                foot(k, j) = nnel;
+                near(k, j) = ne;
+                un_ELM(k, j) = uuint * c->cos_theta(j) + vvint * c->sin_theta(j);
+                vn_ELM(k, j) = -uuint * c->sin_theta(j) + vvint * c->cos_theta(j);
+            }
+        }
+    }
+    return GOM_OK;
+}
+
+// solve_momentum_equation.f90:15-656
+int gom_step_momentum(gom_ctx *c) {
+    if (!c) return GOM_E_ARG;
+    const gom_params &p = c->p;
+    const int L = c->L;
+    const double dt = p.dt, gravity = p.gravity, theta = p.theta;
+    A2<double> AinvG1 = FD(c, GOM_F_AINVG1), AinvG2 = FD(c, GOM_F_AINVG2), AinvDZ1 = FD(c, GOM_F_AINVDZ1),
+               AinvDZ2 = FD(c, GOM_F_AINVDZ2), Kh = FD(c, GOM_F_KH);
+    A2<double> dz_face = FD(c, GOM_F_DZ_FACE), dzhalf_face = FD(c, GOM_F_DZHALF_FACE), Av = FD(c, GOM_F_AV);
+    A2<double> un_face = FD(c, GOM_F_UN_FACE), vn_face = FD(c, GOM_F_VN_FACE), un_ELM = FD(c, GOM_F_UN_ELM),
+               vn_ELM = FD(c, GOM_F_VN_ELM), u_node = FD(c, GOM_F_U_NODE), v_node = FD(c, GOM_F_V_NODE),
+               rho_cell = FD(c, GOM_F_RHO_CELL), rho_node = FD(c, GOM_F_RHO_NODE);
+    A1<double> eta_cell = FD1(c, GOM_F_ETA_CELL), eta_node = FD1(c, GOM_F_ETA_NODE), Gamma_B = FD1(c, GOM_F_GAMMA_B),
+               Qu = FD1(c, GOM_F_QU_BOUNDARY);
+    A1<int32_t> top_f = FI1(c, GOM_F_TOP_LAYER_FACE), top_el = FI1(c, GOM_F_TOP_LAYER_CELL),
+                top_n = FI1(c, GOM_F_TOP_LAYER_NODE), wetdry = FI1(c, GOM_F_WETDRY_NODE);
+    std::fill(c->fd[GOM_F_AINVG1].begin(), c->fd[GOM_F_AINVG1].end(), 0.0);
+    std::fill(c->fd[GOM_F_AINVG2].begin(), c->fd[GOM_F_AINVG2].end(), 0.0);
+    std::fill(c->fd[GOM_F_AINVDZ1].begin(), c->fd[GOM_F_AINVDZ1].end(), 0.0);
+    std::fill(c->fd[GOM_F_AINVDZ2].begin(), c->fd[GOM_F_AINVDZ2].end(), 0.0);
+    const int nmax = L + 1;
+    std::vector<double> G1(nmax, 0.0), G2(nmax, 0.0), a(nmax, 0.0), bd(nmax, 0.0), cu(nmax, 0.0), gam(nmax, 0.0);
+    std::vector<double> rhs(nmax * 3, 0.0), sol(nmax * 3, 0.0);
+    double temp[12] = {0};
+    double rtemp0 = 0.0, rtemp1 = 0.0, rtemp2 = 0.0, rtemp3 = 0.0, rtemp4 = 0.0;
+    const double c069 = F(0.69f);
+    for (int j = 1; j <= c->NF; ++j) {
+        if (top_f(j) == 0) continue;
+        int node1 = c->nodenum_at_face(1, j), node2 = c->nodenum_at_face(2, j);
+        int tj = top_f(j), bj = c->bottom_layer_at_face(j);
+        int nvl = tj - bj + 1;
+        int a1 = c->adj_cellnum_at_face(1, j), a2 = c->adj_cellnum_at_face(2, j);
+        int btype = c->boundary_type_of_face(j);
+        // :120-169 matrix
+        for (int k = bj + 1; k <= tj - 1; ++k) {
+            int kk = tj - k + 1;
+            a[kk - 1] = -dt * Av(k, j) / dzhalf_face(k, j);
+            cu[kk - 1] = -dt * Av(k - 1, j) / dzhalf_face(k - 1, j);
+            bd[kk - 1] = -a[kk - 1] + dz_face(k, j) - cu[kk - 1];
+        }
+        if (tj == bj) {
+            bd[0] = dz_face(tj, j) + Gamma_B(j) * dt;
+        } else {
+            cu[0] = -dt * Av(tj - 1, j) / dzhalf_face(tj - 1, j);
+            bd[0] = c->gamma_t[j - 1] * dt + dz_face(tj, j) - cu[0];
+            a[nvl - 1] = -dt * Av(bj, j) / dzhalf_face(bj, j);
+            bd[nvl - 1] = -a[nvl - 1] + dz_face(bj, j) + Gamma_B(j) * dt;
+        }
+        // :173-216 earth tide: not configured (no_Etide_species = 0)
+        double detp_dx = 0.0, detp_dy = 0.0;
+        for (int k = 1; k <= nvl; ++k) {
+            int kk = tj - k + 1;
+            G1[k - 1] = dz_face(kk, j) * (un_ELM(kk, j) + c->coriolis_factor(j) * dt * vn_face(kk, j));
+            G2[k - 1] = dz_face(kk, j) * (vn_ELM(kk, j) - c->coriolis_factor(j) * dt * un_face(kk, j));
+            if (a2 != 0) {
+                // :269-301
+                for (int l = 1; l <= 2; ++l) {
+                    int nd = c->nodenum_at_face(l, j);
+                    double utmp = (u_node(kk, nd) + u_node(kk - 1, nd)) * 0.5;
+                    double vtmp = (v_node(kk, nd) + v_node(kk - 1, nd)) * 0.5;
+                    temp[2 * l - 2] = utmp * c->cos_theta(j) + vtmp * c->sin_theta(j);
+                    temp[2 * l - 1] = -utmp * c->sin_theta(j) + vtmp * c->cos_theta(j);
+                }
+                for (int l = 1; l <= 2; ++l) {
+                    int ie = c->adj_cellnum_at_face(l, j);
+                    double utmp = 0.0, vtmp = 0.0;
+                    int tq = c->tri_or_quad(ie);
+                    for (int ll = 1; ll <= tq; ++ll) {
+                        int nd = c->nodenum_at_cell(ll, ie);
+                        utmp = utmp + (u_node(kk, nd) + u_node(kk - 1, nd)) * 0.5 / tq;
+                        vtmp = vtmp + (v_node(kk, nd) + v_node(kk - 1, nd)) * 0.5 / tq;
+                    }
+                    temp[2 * l + 2] = utmp * c->cos_theta(j) + vtmp * c->sin_theta(j);
+                    temp[2 * l + 3] = -utmp * c->sin_theta(j) + vtmp * c->cos_theta(j);
+                }
+                double dudx = (temp[6] - temp[4]) / c->delta_j(j);
+                double dvdx = (temp[7] - temp[5]) / c->delta_j(j);
+                double dudy = (temp[2] - temp[0]) / c->face_length(j);
+                double dvdy = (temp[3] - temp[1]) / c->face_length(j);
+                double s = dvdx + dudy;
+                double hdiff = p.smagorinsky * std::sqrt(dudx * dudx + dvdy * dvdy + 0.5 * (s * s));
+                Kh(k, j) = hdiff * c->area(a1);
+                hdiff = hdiff + p.ah_0;
+                Kh(k, j) = Kh(k, j) + p.kh_0;
+                double fl = c->face_length(j);
+                double d2udy = 4.0 * (temp[2] + temp[0] - 2 * un_face(kk, j)) / (fl * fl);
+                double d2vdy = 4.0 * (temp[3] + temp[1] - 2 * vn_face(kk, j)) / (fl * fl);
+                for (int l = 1; l <= 2; ++l) {
+                    int ie = c->adj_cellnum_at_face(l, j);
+                    double ddx = c->x_cell(ie) - c->x_face(j), ddy = c->y_cell(ie) - c->y_face(j);
+                    double rl = std::sqrt(ddx * ddx + ddy * ddy);
+                    temp[2 * l + 6] = (temp[2 * l + 2] - un_face(kk, j)) / rl;
+                    temp[2 * l + 7] = (temp[2 * l + 3] - vn_face(kk, j)) / rl;
+                }
+                double d2udx = 2.0 * (temp[8] + temp[10]) / c->delta_j(j);
+                double d2vdx = 2.0 * (temp[9] + temp[11]) / c->delta_j(j);
+                G1[k - 1] = G1[k - 1] + dz_face(kk, j) * dt * hdiff * (d2udx + d2udy);
+                G2[k - 1] = G2[k - 1] + dz_face(kk, j) * dt * hdiff * (d2vdx + d2vdy);
+            }
+            // :350-376 barotropic gradient, (1-theta) part
+            if (btype == 0) {
+                rtemp0 = gravity * dt / c->delta_j(j) * (1.0 - theta) * (eta_cell(a2) - eta_cell(a1));
+                rtemp1 = rtemp0 * c->cos_theta2(j);
+                rtemp2 = rtemp0 * c->sin_theta2(j);
+                G1[k - 1] = G1[k - 1] - dz_face(kk, j) * rtemp1;
+            } else if (btype > 0) {
+                int ie = c->ob_element_flag(a1);
+                rtemp1 = gravity * dt / c->delta_j(j) * (1.0 - theta) * (c->eta_at_ob_old[ie - 1] - eta_cell(a1));
+                G1[k - 1] = G1[k - 1] - dz_face(kk, j) * rtemp1;
+            } else if (btype == -1) {
+                G1[k - 1] = 0.0;
+            }
+            // :380-397
+            if (wetdry(node1) == 0 && wetdry(node2) == 0) {
+                rtemp0 = gravity * dt / c->face_length(j) * (1.0 - theta) * (eta_node(node2) - eta_node(node1));
+                if (btype == 0) G2[k - 1] = G2[k - 1] - dz_face(kk, j) * (rtemp0 + rtemp2);
+                else G2[k - 1] = G2[k - 1] - dz_face(kk, j) * rtemp0;
+            }
+            // :400-471 baroclinic
+            if (p.baroclinic_flag == 1) {
+                double sum1 = 0.0, sum2 = 0.0;
+                for (int k2 = kk; k2 <= tj; ++k2) {
+                    if (a2 != 0 && k2 >= c->bottom_layer_at_element(a1) && k2 <= top_el(a1) &&
+                        k2 >= c->bottom_layer_at_element(a2) && k2 <= top_el(a2)) {
+                        if (k2 == kk)
+                            sum1 = sum1 + 0.5 * (rho_cell(k2, a2) - rho_cell(k2, a1)) * dz_face(k2, j);
+                        else
+                            sum1 = sum1 + 1.0 * (rho_cell(k2, a2) - rho_cell(k2, a1)) * dz_face(k2, j);
+                    }
+                    if (k2 >= c->bottom_layer_at_node(node1) && k2 <= top_n(node1) &&
+                        k2 >= c->bottom_layer_at_node(node2) && k2 <= top_n(node2)) {
+                        if (k2 == kk) sum2 = sum2 + 0.5 * (rho_node(k2, node2) - rho_node(k2, node1)) * dz_face(k2, j);
+                        else sum2 = sum2 + 1.0 * (rho_node(k2, node2) - rho_node(k2, node1)) * dz_face(k2, j);
+                    }
+                }
+                // the reference indexes dz_face with the top-down row k here (:455-456)
+                rtemp1 = dz_face(k, j) * (-gravity * dt / (p.rho_o * c->delta_j(j))) * sum1;
+                rtemp2 = dz_face(k, j) * (-gravity * dt / (p.rho_o * c->face_length(j))) * sum2;
+                rtemp3 = rtemp1 * c->cos_theta2(j);
+                rtemp4 = rtemp1 * c->sin_theta2(j);
+                G1[k - 1] = G1[k - 1] + rtemp3 * c->spinup_baroclinic;
+                G2[k - 1] = G2[k - 1] + (rtemp2 + rtemp4) * c->spinup_baroclinic;
+            }
+            // :474-477 wind at the top row
+            if (k == 1) {
+                G1[k - 1] = G1[k - 1] + dt * c->wind_stress_normal[j - 1];
+                G2[k - 1] = G2[k - 1] + dt * c->wind_stress_tangnt[j - 1];
+            }
+            // :485-486 earth tide gradient (zero here)
+            G1[k - 1] = G1[k - 1] + c069 * dz_face(kk, j) * gravity * dt * detp_dx;
+            G2[k - 1] = G2[k - 1] + c069 * dz_face(kk, j) * gravity * dt * detp_dy;
+            // :490-509 air pressure; on boundary faces rtemp0 is the value left from before
+            if (a2 != 0) {
+                for (int l = 1; l <= 2; ++l) {
+                    temp[l - 1] = 0.0;
+                    int ie = c->adj_cellnum_at_face(l, j);
+                    int tq = c->tri_or_quad(ie);
+                    for (int ll = 1; ll <= tq; ++ll)
+                        temp[l - 1] = temp[l - 1] + c->air_p[c->nodenum_at_cell(ll, ie) - 1] / tq;
+                }
+                rtemp0 = -dt / p.rho_o * (temp[1] - temp[0]) / c->delta_j(j);
+            }
+            rtemp1 = rtemp0 * c->cos_theta2(j);
+            rtemp2 = rtemp0 * c->sin_theta2(j);
+            G1[k - 1] = G1[k - 1] + dz_face(kk, j) * rtemp1;
+            rtemp3 = -dt / p.rho_o * ((c->air_p[node2 - 1] - c->air_p[node1 - 1]) / c->face_length(j));
+            G2[k - 1] = G2[k - 1] + dz_face(kk, j) * (rtemp3 + rtemp2);
+            // :519-535 (isflowside is never set; the land branch applies)
+            if (btype == -1) G1[k - 1] = 0.0;
+            // :544-551 river
+            if (c->isflowside3(j) > 0) {
+                int ibnd = c->isflowside3(j);
+                G1[k - 1] = G1[k - 1] + dz_face(kk, j) * Qu(ibnd);
+            }
+            rhs[0 * nmax + k - 1] = G1[k - 1];
+            rhs[1 * nmax + k - 1] = G2[k - 1];
+            rhs[2 * nmax + k - 1] = dz_face(kk, j);
+        }
+        if (!tridiagonal_solver(nmax, nvl, 3, a.data(), bd.data(), cu.data(), rhs.data(), sol.data(), gam.data())) {
+            set_err(c, GOM_E_ZERO_PIVOT, 587, j, 0, 0.0);
+            return GOM_E_ZERO_PIVOT;
+        }
+        for (int k = 1; k <= nvl; ++k) {
+            AinvG1(k, j) = sol[0 * nmax + k - 1];
+            AinvG2(k, j) = sol[1 * nmax + k - 1];
+        }
+        if (btype == -1 && c->isflowside3(j) == 0)
+            for (int k = 1; k <= nvl; ++k) AinvG1(k, j) = 0.0;
+        for (int k = 1; k <= nvl; ++k) {
+            AinvDZ1(k, j) = sol[2 * nmax + k - 1];
+            AinvDZ2(k, j) = sol[2 * nmax + k - 1];
+        }
+        if (btype == -1)
+            for (int k = 1; k <= nvl; ++k) AinvDZ1(k, j) = 0.0;
+    }
+    return GOM_OK;
+}
+
+// solve_free_surface_equation.f90:17-396 with pre_conj_grad.f90:9-230 (serial, CSR order)
+int gom_step_free_surface(gom_ctx *c, int32_t *pcg_iters) {
+    if (!c) return GOM_E_ARG;
+    const gom_params &p = c->p;
+    const double dt = p.dt, gravity = p.gravity, theta = p.theta;
+    const int NC = c->NC;
+    A2<double> dz_face = FD(c, GOM_F_DZ_FACE), AinvDZ1 = FD(c, GOM_F_AINVDZ1), AinvG1 = FD(c, GOM_F_AINVG1),
+               un_face = FD(c, GOM_F_UN_FACE);
+    A1<double> eta_cell = FD1(c, GOM_F_ETA_CELL), eta_new = FD1(c, GOM_F_ETA_CELL_NEW), eta_node = FD1(c, GOM_F_ETA_NODE);
+    A1<int32_t> top_f = FI1(c, GOM_F_TOP_LAYER_FACE), top_el = FI1(c, GOM_F_TOP_LAYER_CELL),
+                wetdry = FI1(c, GOM_F_WETDRY_NODE);
+    std::vector<double> sparsem(5 * (size_t)NC, 0.0), rhs_1(NC, 0.0);
+    auto SP = [&](int l, int i) -> double & { return sparsem[(size_t)(i - 1) * 5 + l]; };
+    for (int i = 1; i <= NC; ++i) {
+        SP(0, i) = c->area(i);
+        int tq = c->tri_or_quad(i);
+        for (int l = 1; l <= tq; ++l) {
+            int ii = c->adj_cellnum_at_cell(l, i);
+            int j = c->facenum_at_cell(l, i);
+            if (top_f(j) != 0) {
+                double s = 0.0;
+                int nvl = top_f(j) - c->bottom_layer_at_face(j) + 1;
+                for (int k = 1; k <= nvl; ++k) s = s + dz_face(top_f(j) + 1 - k, j) * AinvDZ1(k, j);
+                s = gravity * (dt * dt) * (theta * theta) * c->face_length(j) / c->delta_j(j) * s;
+                s = s * c->cos_theta2(j);
+                if (s < 0.0) {
+                    set_err(c, GOM_E_NOT_SPD, 100, i, 0, s);
+                    return GOM_E_NOT_SPD;
+                }
+                SP(0, i) = SP(0, i) + s;
+                if (ii != 0) SP(l, i) = -s;
+            }
+        }
+        rhs_1[i - 1] = c->area(i) * eta_cell(i);
+        for (int l = 1; l <= tq; ++l) {
+            int j = c->facenum_at_cell(l, i);
+            if (top_f(j) != 0) {
+                double const1 = 0.0, const2 = 0.0;
+                int nvl = top_f(j) - c->bottom_layer_at_face(j) + 1;
+                for (int k = 1; k <= nvl; ++k) {
+                    int kk = top_f(j) + 1 - k;
+                    const1 = const1 + dz_face(kk, j) * un_face(kk, j);
+                    const2 = const2 + dz_face(kk, j) * AinvG1(k, j);
+                }
+                double sgn = (double)c->sign_in_outflow(l, i);
+                rhs_1[i - 1] = rhs_1[i - 1] - (1.0 - theta) * dt * sgn * c->face_length(j) * const1 -
+                               theta * dt * sgn * c->face_length(j) * const2;
+            }
+        }
+        if (c->ob_element_flag(i) > 0) {
+            for (int l = 1; l <= tq; ++l) {
+                int j = c->facenum_at_cell(l, i);
+                if (c->boundary_type_of_face(j) > 0 && top_f(j) != 0) {
+                    double s = 0.0;
+                    int nvl = top_f(j) - c->bottom_layer_at_face(j) + 1;
+                    for (int k = 1; k <= nvl; ++k) s = s + dz_face(top_f(j) + 1 - k, j) * AinvDZ1(k, j);
+                    s = gravity * (dt * dt) * (theta * theta) * c->face_length(j) / c->delta_j(j) * s;
+                    rhs_1[i - 1] = rhs_1[i - 1] + s * c->eta_at_ob_new[c->ob_element_flag(i) - 1];
+                }
+            }
+        }
+    }
+    // CSR (:233-258): diagonal first, then neighbours in local order
+    std::vector<int> ia(NC + 1), ja;
+    std::vector<double> a1;
+    ja.reserve(5 * (size_t)NC);
+    a1.reserve(5 * (size_t)NC);
+    std::vector<double> x(NC);
+    for (int i = 1; i <= NC; ++i) {
+        ia[i - 1] = (int)ja.size();
+        ja.push_back(i);
+        a1.push_back(SP(0, i));
+        x[i - 1] = eta_new(i);
+        for (int l = 1; l <= c->tri_or_quad(i); ++l) {
+            int ii = c->adj_cellnum_at_cell(l, i);
+            if (ii != 0) {
+                ja.push_back(ii);
+                a1.push_back(SP(l, i));
+            }
+        }
+    }
+    ia[NC] = (int)ja.size();
+    // pre_conj_grad.f90:46-221
+    std::vector<double> Minv(NC), r(NC), d(NC), q(NC), s(NC);
+    for (int i = 0; i < NC; ++i) {
+        double sum1 = 0.0;
+        for (int k = ia[i]; k < ia[i + 1]; ++k) {
+            if (ja[k] == i + 1) Minv[i] = 1.0 / a1[k];
+            sum1 = sum1 + a1[k] * x[ja[k] - 1];
+        }
+        r[i] = rhs_1[i] - sum1;
+    }
+    for (int i = 0; i < NC; ++i) d[i] = Minv[i] * r[i];
+    double delta_new = 0.0;
+    for (int i = 0; i < NC; ++i) delta_new = delta_new + r[i] * d[i];
+    double delta_0 = delta_new;
+    int cgit2 = 0;
+    // A zero initial residual would make the reference divide 0 by 0 (alpha = delta/dq);
+    // the restatement returns the initial guess instead.
+    if (delta_0 != 0.0) {
+        for (int cgit = 1; cgit <= p.max_iteration_pcg; ++cgit) {
+            for (int i = 0; i < NC; ++i) {
+                double sum1 = 0.0;
+                for (int k = ia[i]; k < ia[i + 1]; ++k) sum1 = sum1 + a1[k] * d[ja[k] - 1];
+                q[i] = sum1;
+            }
+            double dq = 0.0;
+            for (int i = 0; i < NC; ++i) dq = dq + d[i] * q[i];
+            double alpha = delta_new / dq;
+            for (int i = 0; i < NC; ++i) {
+                x[i] = x[i] + alpha * d[i];
+                r[i] = r[i] - alpha * q[i];
+            }
+            for (int i = 0; i < NC; ++i) s[i] = Minv[i] * r[i];
+            double delta_old = delta_new;
+            delta_new = 0.0;
+            for (int i = 0; i < NC; ++i) delta_new = delta_new + r[i] * s[i];
+            double beta = delta_new / delta_old;
+            for (int i = 0; i < NC; ++i) d[i] = s[i] + beta * d[i];
+            cgit2 = cgit;
+            if (std::sqrt(delta_new * delta_new / (delta_0 * delta_0)) < p.error_tolerance) break;
+        }
+    }
+    if (pcg_iters) *pcg_iters = cgit2;
+    c->pcg_total += cgit2;
+    for (int i = 1; i <= NC; ++i) eta_new(i) = x[i - 1];
+    // :353-396 node elevation and wet/dry nodes
+    for (int i = 1; i <= c->NN; ++i) {
+        wetdry(i) = 0;
+        double sum1 = 0.0, sum0 = 0.0;
+        for (int j = 1; j <= c->adj_cells_at_node(i); ++j) {
+            int ie = c->adj_cellnum_at_node(j, i);
+            if (top_el(ie) == 0) wetdry(i) = 1;
+            else {
+                sum1 = sum1 + c->area(ie) * eta_new(ie);
+                sum0 = sum0 + c->area(ie);
+            }
+        }
+        if (wetdry(i) == 0) eta_node(i) = sum1 / sum0;
+    }
+    for (int i = 1; i <= c->NN; ++i) {
+        if (wetdry(i) == 1) {
+            double sum0 = 0.0;
+            int icount = 0;
+            for (int j = 1; j <= c->adj_nodes_at_node(i); ++j) {
+                int nd = c->adj_nodenum_at_node(j, i);
+                if (wetdry(nd) == 0) {
+                    icount = icount + 1;
+                    sum0 = sum0 + eta_node(nd);
+                }
+            }
+            if (icount != 0) eta_node(i) = sum0 / icount;
+        }
+    }
+    return GOM_OK;
+}
+
+// solve_velocities.f90:8-260
+int gom_step_velocities(gom_ctx *c) {
+    if (!c) return GOM_E_ARG;
+    const gom_params &p = c->p;
+    const int L = c->L;
+    const double dt = p.dt, gravity = p.gravity, theta = p.theta;
+    A2<double> un_new = FD(c, GOM_F_UN_FACE_NEW), vn_new = FD(c, GOM_F_VN_FACE_NEW), AinvG1 = FD(c, GOM_F_AINVG1),
+               AinvG2 = FD(c, GOM_F_AINVG2), AinvDZ1 = FD(c, GOM_F_AINVDZ1), AinvDZ2 = FD(c, GOM_F_AINVDZ2),
+               wn_new = FD(c, GOM_F_WN_CELL_NEW), dz_face = FD(c, GOM_F_DZ_FACE);
+    A1<double> eta_new = FD1(c, GOM_F_ETA_CELL_NEW), eta_node = FD1(c, GOM_F_ETA_NODE), Qu = FD1(c, GOM_F_QU_BOUNDARY);
+    A1<int32_t> top_f = FI1(c, GOM_F_TOP_LAYER_FACE), top_el = FI1(c, GOM_F_TOP_LAYER_CELL),
+                wetdry = FI1(c, GOM_F_WETDRY_NODE);
+    for (int j = 1; j <= c->NF; ++j) {
+        int n1 = c->nodenum_at_face(1, j), n2 = c->nodenum_at_face(2, j);
+        int tj = top_f(j), bj = c->bottom_layer_at_face(j);
+        int btype = c->boundary_type_of_face(j);
+        if (tj == 0) {
+            for (int k = 1; k <= L; ++k) {
+                un_new(k, j) = 0.0;
+                vn_new(k, j) = 0.0;
+            }
+            continue;
+        }
+        double rtemp2 = 0.0;
+        for (int k = 1; k <= tj - bj + 1; ++k) {
+            int kk = tj + 1 - k;
+            if (btype == -1) {
+                un_new(kk, j) = 0.0;
+            } else if (btype == 0) {
+                int a1 = c->adj_cellnum_at_face(1, j), a2 = c->adj_cellnum_at_face(2, j);
+                double rtemp0 = theta * gravity * dt / c->delta_j(j) * (eta_new(a2) - eta_new(a1)) * AinvDZ1(k, j);
+                double rtemp1 = rtemp0 * c->cos_theta2(j);
+                rtemp2 = rtemp0 * c->sin_theta2(j);
+                un_new(kk, j) = AinvG1(k, j) - rtemp1;
+            } else {
+                int a1 = c->adj_cellnum_at_face(1, j);
+                double rtemp0 = theta * gravity * dt / c->delta_j(j) *
+                                (c->eta_at_ob_new[c->ob_element_flag(a1) - 1] - eta_new(a1)) * AinvDZ1(k, j);
+                un_new(kk, j) = AinvG1(k, j) - rtemp0;
+            }
+            if (wetdry(n1) == 0 && wetdry(n2) == 0) {
+                double rtemp1 = theta * gravity * dt / c->face_length(j) * (eta_node(n2) - eta_node(n1)) * AinvDZ2(k, j);
+                if (btype == 0) vn_new(kk, j) = AinvG2(k, j) - (rtemp1 + rtemp2);
+                else vn_new(kk, j) = AinvG2(k, j) - rtemp1;
+            }
+            if (c->initial_wetdry_node(n1) == 1 || c->initial_wetdry_node(n2) == 1)
+                vn_new(kk, j) = std::max(-5.0, std::min(vn_new(kk, j), 5.0));
+        }
+        if (c->isflowside3(j) > 0) {
+            int ibnd = c->isflowside3(j);
+            for (int k = bj; k <= tj; ++k) un_new(k, j) = Qu(ibnd);
+        }
+        for (int k = 1; k <= bj - 1; ++k) {
+            un_new(k, j) = 0.0;
+            vn_new(k, j) = 0.0;
+        }
+        for (int k = tj + 1; k <= L; ++k) {
+            un_new(k, j) = un_new(tj, j);
+            vn_new(k, j) = vn_new(tj, j);
+        }
+    }
+    for (int i = 1; i <= c->NC; ++i) {
+        int t = top_el(i), b = c->bottom_layer_at_element(i);
+        if (t == 0) {
+            for (int k = 0; k <= L; ++k) wn_new(k, i) = 0.0;
+            continue;
+        }
+        wn_new(b - 1, i) = 0.0;
+        for (int k = b; k <= t; ++k) {
+            double sum1 = 0.0;
+            for (int l = 1; l <= c->tri_or_quad(i); ++l) {
+                int jt = c->facenum_at_cell(l, i);
+                if (k >= c->bottom_layer_at_face(jt) && k <= top_f(jt))
+                    sum1 = sum1 + (double)c->sign_in_outflow(l, i) * c->face_length(jt) * dz_face(k, jt) * un_new(k, jt);
+            }
+            wn_new(k, i) = wn_new(k - 1, i) - sum1 / c->area(i);
+        }
+        for (int k = 0; k <= b - 2; ++k) wn_new(k, i) = 0.0;
+        for (int k = t + 1; k <= L; ++k) wn_new(k, i) = wn_new(t, i);
+    }
+    return GOM_OK;
+}
+
+// update_vertical_layers_1.f90:18-333
+int gom_step_layers(gom_ctx *c) {
+    if (!c) return GOM_E_ARG;
+    const gom_params &p = c->p;
+    const int L = c->L;
+    const double MSL = p.msl;
+    A2<double> dz_cn = FD(c, GOM_F_DZ_CELL_NEW), dzh_cn = FD(c, GOM_F_DZHALF_CELL_NEW), wn_new = FD(c, GOM_F_WN_CELL_NEW),
+               dz_fn = FD(c, GOM_F_DZ_FACE_NEW), dzh_fn = FD(c, GOM_F_DZHALF_FACE_NEW), dz_nn = FD(c, GOM_F_DZ_NODE_NEW),
+               dzh_nn = FD(c, GOM_F_DZHALF_NODE_NEW);
+    A1<double> eta_new = FD1(c, GOM_F_ETA_CELL_NEW), eta_node = FD1(c, GOM_F_ETA_NODE);
+    A1<int32_t> top_el = FI1(c, GOM_F_TOP_LAYER_CELL), top_f = FI1(c, GOM_F_TOP_LAYER_FACE),
+                top_n = FI1(c, GOM_F_TOP_LAYER_NODE);
+    for (int i = 1; i <= c->NC; ++i) {
+        int tnew = 0;
+        double total = c->h_cell(i) + eta_new(i);
+        int b = c->bottom_layer_at_element(i);
+        if (total > p.dry_depth) {
+            double tmp = MSL + eta_new(i);
+            for (int k = L - 1; k >= 0; --k)
+                if (tmp > c->zl(k) && tmp <= c->zl(k + 1)) {
+                    tnew = k + 1;
+                    dz_cn(tnew, i) = tmp - c->zl(k);
+                    break;
+                }
+            if (tnew < b) {
+                set_err(c, GOM_E_LAYER, 66, i, tnew, eta_new(i));
+                return GOM_E_LAYER;
+            }
+            if (tnew == b) {
+                dz_cn(tnew, i) = total;
+                dzh_cn(tnew, i) = total;
+            } else {
+                dz_cn(b, i) = c->zl(b) - (MSL - c->h_cell(i));
+                for (int k = b + 1; k <= tnew - 1; ++k) dz_cn(k, i) = c->delta_z(k);
+                for (int k = b; k <= tnew - 1; ++k) dzh_cn(k, i) = (dz_cn(k + 1, i) + dz_cn(k, i)) * 0.5;
+                dzh_cn(tnew, i) = dz_cn(tnew, i);
+                dzh_cn(b - 1, i) = dz_cn(b, i);
+            }
+        }
+        if (top_el(i) == 0 && tnew != 0)
+            for (int k = 0; k <= L; ++k) wn_new(k, i) = 0.0;
+        top_el(i) = tnew;
+    }
+    for (int j = 1; j <= c->NF; ++j) {
+        int tnew = 0;
+        int a1 = c->adj_cellnum_at_face(1, j), a2 = c->adj_cellnum_at_face(2, j);
+        double eta_max = (a2 != 0) ? std::max(eta_new(a1), eta_new(a2)) : eta_new(a1);
+        double total = c->h_face(j) + eta_max;
+        int b = c->bottom_layer_at_face(j);
+        if (total > p.dry_depth) {
+            double tmp = MSL + eta_max;
+            for (int k = L - 1; k >= 0; --k)
+                if (tmp > c->zl(k) && tmp <= c->zl(k + 1)) {
+                    tnew = k + 1;
+                    dz_fn(tnew, j) = tmp - c->zl(k);
+                    break;
+                }
+            if (tnew < b) {
+                set_err(c, GOM_E_LAYER, 166, j, tnew, eta_max);
+                return GOM_E_LAYER;
+            }
+            if (tnew == b) {
+                dz_fn(tnew, j) = total;
+                dzh_fn(tnew - 1, j) = total;
+                dzh_fn(tnew, j) = total;
+            } else {
+                dz_fn(b, j) = c->zl(b) - (MSL - c->h_face(j));
+                for (int k = b + 1; k <= tnew - 1; ++k) dz_fn(k, j) = c->delta_z(k);
+                for (int k = b; k <= tnew - 1; ++k) dzh_fn(k, j) = (dz_fn(k + 1, j) + dz_fn(k, j)) * 0.5;
+                dzh_fn(tnew, j) = dz_fn(tnew, j);
+                dzh_fn(b - 1, j) = dz_fn(b, j);
+            }
+        }
+        top_f(j) = tnew;
+    }
+    for (int i = 1; i <= c->NN; ++i) {
+        int tnew = 0;
+        double total = c->h_node(i) + eta_node(i);
+        int b = c->bottom_layer_at_node(i);
+        if (total > p.dry_depth) {
+            double tmp = MSL + eta_node(i);
+            for (int k = L - 1; k >= 0; --k)
+                if (tmp > c->zl(k) && tmp <= c->zl(k + 1)) {
+                    tnew = k + 1;
+                    dz_nn(tnew, i) = tmp - c->zl(k);
+                    break;
+                }
+            if (tnew < b) {
+                set_err(c, GOM_E_LAYER, 224, i, tnew, eta_node(i));
+                return GOM_E_LAYER;
+            }
+            if (tnew == b) {
+                dz_nn(tnew, i) = total;
+                dzh_nn(tnew, i) = total;
+            } else {
+                dz_nn(b, i) = c->zl(b) - (MSL - c->h_node(i));
+                for (int k = b + 1; k <= tnew - 1; ++k) dz_nn(k, i) = c->delta_z(k);
+                for (int k = b; k <= tnew - 1; ++k) dzh_nn(k, i) = (dz_nn(k + 1, i) + dz_nn(k, i)) * 0.5;
+            }
+        }
+        top_n(i) = tnew;
+    }
+    for (int i = 1; i <= c->NC; ++i) {
+        int nsum1 = 0, nsum2 = 0;
+        for (int l = 1; l <= c->tri_or_quad(i); ++l) {
+            nsum1 = nsum1 + top_n(c->nodenum_at_cell(l, i));
+            nsum2 = nsum2 + top_f(c->facenum_at_cell(l, i));
+        }
+        if (nsum1 == 0) top_el(i) = 0;
+        if (nsum2 == 0 && top_el(i) != 0) {
+            set_err(c, GOM_E_DRY, 273, i, 0, 0.0);
+            return GOM_E_DRY;
+        }
+    }
+    for (int i = 1; i <= c->NC; ++i)
+        for (int k = c->bottom_layer_at_element(i); k <= top_el(i) - 1; ++k)
+            if (dzh_cn(k, i) < p.denominator_min_for_matrix) {
+                set_err(c, GOM_E_LAYER, 284, i, k, dzh_cn(k, i));
+                return GOM_E_LAYER;
+            }
+    for (int j = 1; j <= c->NF; ++j)
+        for (int k = c->bottom_layer_at_face(j); k <= top_f(j) - 1; ++k)
+            if (dzh_fn(k, j) < p.denominator_min_for_matrix) {
+                set_err(c, GOM_E_LAYER, 301, j, k, dzh_fn(k, j));
+                return GOM_E_LAYER;
+            }
+    for (int i = 1; i <= c->NN; ++i)
+        for (int k = c->bottom_layer_at_node(i); k <= top_n(i) - 1; ++k)
+            if (dzh_nn(k, i) < p.denominator_min_for_matrix) {
+                set_err(c, GOM_E_LAYER, 318, i, k, dzh_nn(k, i));
+                return GOM_E_LAYER;
+            }
+    return GOM_OK;
+}
+
+// calculate_velocity_at_node.f90:10-140
+int gom_step_node_velocity(gom_ctx *c) {
+    if (!c) return GOM_E_ARG;
+    const int L = c->L;
+    A2<double> un_new = FD(c, GOM_F_UN_FACE_NEW), vn_new = FD(c, GOM_F_VN_FACE_NEW), dz_face = FD(c, GOM_F_DZ_FACE),
+               dzhalf_face = FD(c, GOM_F_DZHALF_FACE), ufl = FD(c, GOM_F_U_FACE_LEVEL), vfl = FD(c, GOM_F_V_FACE_LEVEL),
+               u_node = FD(c, GOM_F_U_NODE), v_node = FD(c, GOM_F_V_NODE), w_node = FD(c, GOM_F_W_NODE),
+               wn_cell = FD(c, GOM_F_WN_CELL);
+    A1<int32_t> top_f = FI1(c, GOM_F_TOP_LAYER_FACE), top_el = FI1(c, GOM_F_TOP_LAYER_CELL);
+    std::vector<double> uf(L + 2, 0.0), vf(L + 2, 0.0);
+    for (int j = 1; j <= c->NF; ++j) {
+        int t = top_f(j), b = c->bottom_layer_at_face(j);
+        if (t == 0) continue;
+        for (int k = b; k <= t; ++k) {
+            uf[k] = un_new(k, j) * c->cos_theta(j) - vn_new(k, j) * c->sin_theta(j);
+            vf[k] = un_new(k, j) * c->sin_theta(j) + vn_new(k, j) * c->cos_theta(j);
+        }
+        ufl(b - 1, j) = uf[b];
+        vfl(b - 1, j) = vf[b];
+        ufl(t, j) = uf[t];
+        vfl(t, j) = vf[t];
+        for (int k = b; k <= t - 1; ++k) {
+            ufl(k, j) = uf[k] + dz_face(k, j) * 0.5 / dzhalf_face(k, j) * (uf[k + 1] - uf[k]);
+            vfl(k, j) = vf[k] + dz_face(k, j) * 0.5 / dzhalf_face(k, j) * (vf[k + 1] - vf[k]);
+        }
+    }
+    for (int i = 1; i <= c->NN; ++i) {
+        for (int k = 0; k <= L; ++k) {
+            u_node(k, i) = 0.0;
+            v_node(k, i) = 0.0;
+            double weight = 0.0;
+            int icount = 0;
+            for (int j = 1; j <= c->adj_cells_at_node(i); ++j) {
+                int isn = c->adj_cellnum_at_node(j, i);
+                int nc = c->node_count_each_element(j, i);
+                int tq = c->tri_or_quad(isn);
+                for (int l = tq - 2; l <= tq - 1; ++l) {
+                    int ifn = c->facenum_at_cell(start_end_node(tq, nc, l), isn);
+                    double fw = (c->adj_cellnum_at_face(2, ifn) == 0) ? 2.0 : 1.0;
+                    if (top_f(ifn) != 0 && k >= c->bottom_layer_at_face(ifn) - 1) {
+                        int kvt = std::min(k, (int)top_f(ifn));
+                        u_node(k, i) = u_node(k, i) + ufl(kvt, ifn) / c->face_length(ifn) * fw;
+                        v_node(k, i) = v_node(k, i) + vfl(kvt, ifn) / c->face_length(ifn) * fw;
+                        icount = icount + 1;
+                    }
+                    weight = weight + fw / c->face_length(ifn);
+                }
+            }
+            if (icount != 0) {
+                u_node(k, i) = u_node(k, i) / weight;
+                v_node(k, i) = v_node(k, i) / weight;
+            }
+        }
+    }
+    for (int i = 1; i <= c->NN; ++i) {
+        for (int k = 0; k <= L; ++k) {
+            w_node(k, i) = 0.0;
+            double tw = 0.0;
+            for (int j = 1; j <= c->adj_cells_at_node(i); ++j) {
+                int ite = c->adj_cellnum_at_node(j, i);
+                if (top_el(ite) != 0 && k >= c->bottom_layer_at_element(ite) - 1) {
+                    int kvt = std::min(k, (int)top_el(ite));
+                    tw = tw + c->area(ite);
+                    w_node(k, i) = w_node(k, i) + wn_cell(kvt, ite) * c->area(ite);
+                }
+            }
+            if (tw != 0.0) w_node(k, i) = w_node(k, i) / tw;
+        }
+    }
+    return GOM_OK;
+}
+
+// solve_transport_equation_v19.f90:7-1482 (transport_solver = 1, tracers S and T)
+int gom_step_transport(gom_ctx *c) {
+    if (!c) return GOM_E_ARG;
+    const gom_params &p = c->p;
+    if (!p.transport_flag) return GOM_OK;
+    const int L = c->L, NC = c->NC, NF = c->NF, NN = c->NN;
+    const double dt = p.dt, theta = p.theta, rho_o = p.rho_o;
+    const int ntr = (p.is_salt ? 1 : 0) + (p.is_temp ? 1 : 0);
+    if (ntr == 0) return GOM_OK;
+    int tran_id[2];
+    {
+        int ii = 0;
+        if (p.is_salt) tran_id[ii++] = 1;
+        if (p.is_temp) tran_id[ii++] = 2;
+    }
+    A2<double> salt_cell = FD(c, GOM_F_SALT_CELL), temp_cell = FD(c, GOM_F_TEMP_CELL), dz_cell = FD(c, GOM_F_DZ_CELL),
+               dz_cn = FD(c, GOM_F_DZ_CELL_NEW), dzh_c = FD(c, GOM_F_DZHALF_CELL), dzh_cn = FD(c, GOM_F_DZHALF_CELL_NEW),
+               dz_face = FD(c, GOM_F_DZ_FACE), dz_fn = FD(c, GOM_F_DZ_FACE_NEW), un_face = FD(c, GOM_F_UN_FACE),
+               un_new = FD(c, GOM_F_UN_FACE_NEW), wn_cell = FD(c, GOM_F_WN_CELL), wn_new = FD(c, GOM_F_WN_CELL_NEW),
+               Kh = FD(c, GOM_F_KH), Kv = FD(c, GOM_F_KV);
+    A1<int32_t> top_el = FI1(c, GOM_F_TOP_LAYER_CELL), top_f = FI1(c, GOM_F_TOP_LAYER_FACE),
+                top_n = FI1(c, GOM_F_TOP_LAYER_NODE);
+    const int LC = L + 2;  // con_cell (0:L+1)
+    std::vector<double> con_cell((size_t)LC * NC * ntr, 0.0), con_cell_new((size_t)L * NC * ntr, 0.0),
+        con_node_new((size_t)L * NN * ntr, 0.0), con_face_new((size_t)L * NF * ntr, 0.0);
+    auto CC = [&](int k, int i, int t) -> double & { return con_cell[((size_t)(t - 1) * NC + (i - 1)) * LC + k]; };
+    auto CN = [&](int k, int i, int t) -> double & { return con_cell_new[((size_t)(t - 1) * NC + (i - 1)) * L + k - 1]; };
+    auto NDN = [&](int k, int i, int t) -> double & { return con_node_new[((size_t)(t - 1) * NN + (i - 1)) * L + k - 1]; };
+    auto FCN = [&](int k, int j, int t) -> double & { return con_face_new[((size_t)(t - 1) * NF + (j - 1)) * L + k - 1]; };
+    const double cp = 4186.0;
+    // :88-173 load tracers
+    for (int i3 = 1; i3 <= ntr; ++i3) {
+        for (int i = 1; i <= NC; ++i) {
+            for (int k = 1; k <= L; ++k) CC(k, i, i3) = tran_id[i3 - 1] == 1 ? salt_cell(k, i) : temp_cell(k, i);
+            CC(0, i, i3) = 0.0;
+            CC(L + 1, i, i3) = 0.0;
+            if (tran_id[i3 - 1] == 2 && p.heat_option == 2) {
+                // :150-159 adds dt*phi_sw/(rho_o*cp*dz_top) to all layers; dry cells are skipped
+                // (the reference would index dz_cell(0,i) there)
+                int t = top_el(i);
+                if (t > 0)
+                    for (int k = 1; k <= L; ++k)
+                        CC(k, i, i3) = CC(k, i, i3) + dt * c->phi_sw[i - 1] / (rho_o * cp * dz_cell(t, i));
+            }
+        }
+    }
+    int Nt = p.trans_sub_iter;
+    if (Nt == 0) Nt = 1;
+    const double dt2 = dt / Nt;
+    // work arrays: unassigned entries read as 0
+    std::vector<double> Q_jk((size_t)L * NF), D_jk((size_t)L * NF), d_jk((size_t)L * NF), phi_jk((size_t)L * NF);
+    std::vector<double> Q_ik((size_t)(L + 1) * NC), D_ik((size_t)(L + 1) * NC), d_ik((size_t)(L + 1) * NC),
+        phi_ik((size_t)(L + 1) * NC);
+    std::vector<double> r_jk((size_t)L * NF * ntr), r_ik((size_t)(L + 1) * NC * ntr), PSI_jk((size_t)L * NF * ntr),
+        PSI_ik((size_t)(L + 1) * NC * ntr);
+    auto QJ = [&](int k, int j) -> double & { return Q_jk[(size_t)(j - 1) * L + k - 1]; };
+    auto DJ = [&](int k, int j) -> double & { return D_jk[(size_t)(j - 1) * L + k - 1]; };
+    auto dJ = [&](int k, int j) -> double & { return d_jk[(size_t)(j - 1) * L + k - 1]; };
+    auto pJ = [&](int k, int j) -> double & { return phi_jk[(size_t)(j - 1) * L + k - 1]; };
+    auto QI = [&](int k, int i) -> double & { return Q_ik[(size_t)(i - 1) * (L + 1) + k]; };
+    auto DI = [&](int k, int i) -> double & { return D_ik[(size_t)(i - 1) * (L + 1) + k]; };
+    auto dI = [&](int k, int i) -> double & { return d_ik[(size_t)(i - 1) * (L + 1) + k]; };
+    auto pI = [&](int k, int i) -> double & { return phi_ik[(size_t)(i - 1) * (L + 1) + k]; };
+    auto RJ = [&](int k, int j, int t) -> double & { return r_jk[((size_t)(t - 1) * NF + j - 1) * L + k - 1]; };
+    auto RI = [&](int k, int i, int t) -> double & { return r_ik[((size_t)(t - 1) * NC + i - 1) * (L + 1) + k]; };
+    auto PJ = [&](int k, int j, int t) -> double & { return PSI_jk[((size_t)(t - 1) * NF + j - 1) * L + k - 1]; };
+    auto PI_ = [&](int k, int i, int t) -> double & { return PSI_ik[((size_t)(t - 1) * NC + i - 1) * (L + 1) + k]; };
+    std::vector<double> con_at_obk((size_t)L * c->NOB * ntr), con_at_qbk((size_t)L * c->NQB * ntr);
+    auto OBK = [&](int k, int i, int t) -> double & { return con_at_obk[((size_t)(t - 1) * c->NOB + i - 1) * L + k - 1]; };
+    auto QBK = [&](int k, int i, int t) -> double & { return con_at_qbk[((size_t)(t - 1) * c->NQB + i - 1) * L + k - 1]; };
+    std::vector<double> oQb((size_t)L * ntr, 0.0);
+    auto OQB = [&](int k, int t) -> double & { return oQb[(size_t)(t - 1) * L + k - 1]; };
+    std::vector<double> am(L + 1), bm(L + 1), cm(L + 1), gm(L + 1), rhs((size_t)L * ntr), sol((size_t)L * ntr);
+    // con_at_ob(i, i3) for subcycle s: host array (n_ob, 2, Nt), slot 1 = salt, 2 = temperature
+    auto con_ob = [&](int i, int i3, int s) {
+        return c->con_at_ob[((size_t)s * 2 + (tran_id[i3 - 1] - 1)) * c->NOB + (i - 1)];
+    };
+    auto con_qb = [&](int i, int i3, int s) {
+        return c->con_at_qb[((size_t)s * 2 + (tran_id[i3 - 1] - 1)) * c->NQB + (i - 1)];
+    };
+    for (int subcycle = 0; subcycle <= Nt - 1; ++subcycle) {
+        std::fill(con_at_obk.begin(), con_at_obk.end(), 0.0);
+        std::fill(con_at_qbk.begin(), con_at_qbk.end(), 0.0);
+        std::fill(r_ik.begin(), r_ik.end(), 1.0);
+        std::fill(r_jk.begin(), r_jk.end(), 1.0);
+        // :232-321 open-boundary concentrations by upwind direction
+        for (int i = 1; i <= c->NOB; ++i) {
+            int i2 = c->ob_cell_id(i);
+            int t = top_el(i2), b = c->bottom_layer_at_element(i2);
+            for (int l = 1; l <= c->tri_or_quad(i2); ++l) {
+                int j2 = c->facenum_at_cell(l, i2);
+                if (c->boundary_type_of_face(j2) > 0) {
+                    for (int k = b; k <= t; ++k) {
+                        double dz_old = (dz_face(k, j2) + (dz_fn(k, j2) - dz_face(k, j2)) * subcycle / Nt);
+                        double sg = (double)c->sign_in_outflow(l, i2);
+                        double q2 = c->face_length(j2) * dz_old *
+                                    ((1.0 - theta) * un_face(k, j2) * sg + theta * un_new(k, j2) * sg);
+                        for (int i3 = 1; i3 <= ntr; ++i3)
+                            OBK(k, i, i3) = (q2 <= 0.0) ? con_ob(i, i3, subcycle) : CC(k, i2, i3);
+                    }
+                }
+            }
+        }
+        // :327-397 river concentrations
+        for (int i = 1; i <= c->NQB; ++i) {
+            int i2 = c->qb_cell(i);
+            int t = top_el(i2), b = c->bottom_layer_at_element(i2);
+            for (int k = b; k <= t; ++k)
+                for (int i3 = 1; i3 <= ntr; ++i3) QBK(k, i, i3) = con_qb(i, i3, subcycle);
+        }
+        // :551-581 face coefficients
+        for (int j = 1; j <= NF; ++j) {
+            int b = c->bottom_layer_at_face(j), t = top_f(j);
+            for (int k = b; k <= t; ++k) {
+                double dz_old = dz_face(k, j) + (dz_fn(k, j) - dz_face(k, j)) * subcycle / Nt;
+                QJ(k, j) = c->face_length(j) * dz_old * ((1.0 - theta) * un_face(k, j) + theta * un_new(k, j));
+                DJ(k, j) = c->face_length(j) * dz_old * Kh(k, j) / c->delta_j(j);
+                dJ(k, j) = std::max(0.0, DJ(k, j) - 0.5 * std::fabs(QJ(k, j)));
+                if (QJ(k, j) == 0.0) pJ(k, j) = 1.0;
+                else pJ(k, j) = std::min(1.0, 2.0 * DJ(k, j) / std::fabs(QJ(k, j)));
+            }
+        }
+        // :585-610 vertical coefficients
+        for (int i = 1; i <= NC; ++i) {
+            int b = c->bottom_layer_at_element(i), t = top_el(i);
+            for (int k = b; k <= t - 1; ++k) {
+                QI(k, i) = c->area(i) * ((1.0 - theta) * wn_cell(k, i) + theta * wn_new(k, i));
+                double dz_old = dzh_c(k, i) + (dzh_cn(k, i) - dzh_c(k, i)) * subcycle / Nt;
+                DI(k, i) = c->area(i) * Kv(k, i) / dz_old;
+                dI(k, i) = std::max(0.0, DI(k, i) - 0.5 * std::fabs(QI(k, i)));
+                if (QI(k, i) == 0.0) pI(k, i) = 1.0;
+                else pI(k, i) = std::min(1.0, 2.0 * DI(k, i) / std::fabs(QI(k, i)));
+            }
+        }
+        auto load_oqb = [&](int i, int b, int t) {
+            int ith_ob = c->ob_element_flag(i), ith_Qb = c->Qb_element_flag(i);
+            if (ith_ob > 0)
+                for (int k = b; k <= t; ++k)
+                    for (int i3 = 1; i3 <= ntr; ++i3) OQB(k, i3) = OBK(k, ith_ob, i3);
+            if (ith_Qb > 0)
+                for (int k = b; k <= t; ++k)
+                    for (int i3 = 1; i3 <= ntr; ++i3) OQB(k, i3) = QBK(k, ith_Qb, i3);
+        };
+        auto face_open = [&](int j) {
+            return c->boundary_type_of_face(j) != -1 || c->isflowside3(j) > 0;
+        };
+        // :615-904 limiter
+        if (p.h_flux_limiter > 0 || p.v_flux_limiter > 0) {
+            double sum1[2], sum2[2], s1a[2], s2a[2], cik[2], Q2[4];
+            for (int i = 1; i <= NC; ++i) {
+                int t = top_el(i), b = c->bottom_layer_at_element(i);
+                if (t == 0) continue;
+                int nvl = t - b + 1;
+                load_oqb(i, b, t);
+                int tq = c->tri_or_quad(i);
+                for (int k = b; k <= t; ++k) {
+                    for (int i3 = 0; i3 < 2; ++i3) sum1[i3] = sum2[i3] = s1a[i3] = s2a[i3] = 0.0;
+                    if (nvl != 1) {
+                        if (k == b) {
+                            for (int i3 = 1; i3 <= ntr; ++i3) {
+                                double rt2 = std::fabs(0.5 * (QI(k, i) + std::fabs(QI(k, i))));
+                                s1a[i3 - 1] = rt2 * (CC(k, i, i3) - CC(k + 1, i, i3));
+                                s2a[i3 - 1] = rt2;
+                            }
+                        } else if (k == t) {
+                            for (int i3 = 1; i3 <= ntr; ++i3) {
+                                double rt1 = std::fabs(0.5 * (QI(k - 1, i) + std::fabs(QI(k - 1, i))));
+                                s1a[i3 - 1] = rt1 * (CC(k, i, i3) - CC(k - 1, i, i3));
+                                s2a[i3 - 1] = rt1;
+                            }
+                        } else {
+                            for (int i3 = 1; i3 <= ntr; ++i3) {
+                                double rt1 = std::fabs(0.5 * (QI(k - 1, i) + std::fabs(QI(k - 1, i))));
+                                double rt2 = std::fabs(0.5 * (QI(k, i) + std::fabs(QI(k, i))));
+                                s1a[i3 - 1] = rt1 * (CC(k, i, i3) - CC(k - 1, i, i3)) + rt2 * (CC(k, i, i3) - CC(k + 1, i, i3));
+                                s2a[i3 - 1] = rt1 + rt2;
+                            }
+                        }
+                    }
+                    for (int l = 1; l <= tq; ++l) {
+                        int j = c->facenum_at_cell(l, i);
+                        int ii = c->adj_cellnum_at_cell(l, i);
+                        if (face_open(j)) {
+                            Q2[l - 1] = QJ(k, j) * (double)c->sign_in_outflow(l, i);
+                            if (Q2[l - 1] < 0.0) {
+                                for (int i3 = 1; i3 <= ntr; ++i3) cik[i3 - 1] = ii > 0 ? CC(k, ii, i3) : OQB(k, i3);
+                                for (int i3 = 1; i3 <= ntr; ++i3) {
+                                    sum1[i3 - 1] = sum1[i3 - 1] + std::fabs(Q2[l - 1]) * (CC(k, i, i3) - cik[i3 - 1]);
+                                    sum2[i3 - 1] = sum2[i3 - 1] + std::fabs(Q2[l - 1]);
+                                }
+                            }
+                        }
+                    }
+                    for (int i3 = 1; i3 <= ntr; ++i3) {
+                        s1a[i3 - 1] = s1a[i3 - 1] + sum1[i3 - 1];
+                        s2a[i3 - 1] = s2a[i3 - 1] + sum2[i3 - 1];
+                    }
+                    for (int l = 1; l <= tq; ++l) {
+                        int j = c->facenum_at_cell(l, i);
+                        int ii = c->adj_cellnum_at_cell(l, i);
+                        if (face_open(j)) {
+                            if (Q2[l - 1] >= 0.0) {
+                                for (int i3 = 1; i3 <= ntr; ++i3) cik[i3 - 1] = ii > 0 ? CC(k, ii, i3) : OQB(k, i3);
+                                for (int i3 = 1; i3 <= ntr; ++i3) {
+                                    double rtemp = s2a[i3 - 1] * (cik[i3 - 1] - CC(k, i, i3));
+                                    if (rtemp == 0.0) RJ(k, j, i3) = F(1.0f);
+                                    else RJ(k, j, i3) = s1a[i3 - 1] / rtemp;
+                                }
+                            }
+                        }
+                    }
+                }
+                // :806-840 vertical ratios from the last layer's horizontal sums
+                if (QI(t, i) >= 0.0) {
+                    for (int k = b; k <= t - 1; ++k)
+                        for (int i3 = 1; i3 <= ntr; ++i3) {
+                            double rt1 = sum1[i3 - 1] + std::fabs(QI(k - 1, i)) * (CC(k, i, i3) - CC(k - 1, i, i3));
+                            double rt2 = sum2[i3 - 1] + std::fabs(QI(k - 1, i));
+                            double rtemp = (CC(k + 1, i, i3) - CC(k, i, i3)) * rt2;
+                            if (rtemp == 0.0) RI(k, i, i3) = 1.0;
+                            else RI(k, i, i3) = rt1 / rtemp;
+                        }
+                } else {
+                    for (int k = b + 1; k <= t; ++k)
+                        for (int i3 = 1; i3 <= ntr; ++i3) {
+                            double rt1 = sum1[i3 - 1] + std::fabs(QI(k, i)) * (CC(k, i, i3) - CC(k + 1, i, i3));
+                            double rt2 = sum2[i3 - 1] + std::fabs(QI(k, i));
+                            double rtemp = (CC(k - 1, i, i3) - CC(k, i, i3)) * rt2;
+                            if (rtemp == 0.0) RI(k - 1, i, i3) = 1.0;
+                            else RI(k - 1, i, i3) = rt1 / rtemp;
+                        }
+                }
+                for (int i3 = 1; i3 <= ntr; ++i3) {
+                    RI(t, i, i3) = 1.0;
+                    RI(b - 1, i, i3) = 1.0;
+                }
+            }
+            auto limiter = [&](double small_phi, double r) {
+                switch (p.h_flux_limiter) {
+                case 1: return std::max(small_phi, std::min(F(1.0f), r)) - small_phi;
+                case 2: return std::max(small_phi, (r + std::fabs(r)) / (F(1.0f) + std::fabs(r))) - small_phi;
+                case 3: return std::max(std::max(small_phi, std::min(F(1.0f), 2.0 * r)), std::min(2.0, r)) - small_phi;
+                default: return 0.0;
+                }
+            };
+            for (int i = 1; i <= NC; ++i) {
+                int b = c->bottom_layer_at_element(i), t = top_el(i);
+                for (int k = b; k <= t - 1; ++k)
+                    for (int i3 = 1; i3 <= ntr; ++i3) PI_(k, i, i3) = limiter(pI(k, i), RI(k, i, i3));
+            }
+            for (int j = 1; j <= NF; ++j) {
+                int b = c->bottom_layer_at_face(j), t = top_f(j);
+                for (int k = b; k <= t; ++k)
+                    for (int i3 = 1; i3 <= ntr; ++i3) PJ(k, j, i3) = limiter(pJ(k, j), RJ(k, j, i3));
+            }
+        }
+        // :921-1346 implicit vertical solve per cell
+        for (int i = 1; i <= NC; ++i) {
+            int b = c->bottom_layer_at_element(i), t = top_el(i);
+            if (t == 0) continue;
+            int nvl = t - b + 1;
+            double ar = c->area(i);
+            for (int k = b + 1; k <= t - 1; ++k) {
+                int kk = t + 1 - k;
+                am[kk - 1] = -dt2 * dI(k, i);
+                cm[kk - 1] = -dt2 * dI(k - 1, i);
+                double dz_new = dz_cell(k, i) + (dz_cn(k, i) - dz_cell(k, i)) * (subcycle + 1) / Nt;
+                bm[kk - 1] = -am[kk - 1] + ar * dz_new - cm[kk - 1];
+            }
+            if (t == b) {
+                double dz_new = dz_cell(t, i) + (dz_cn(t, i) - dz_cell(t, i)) * (subcycle + 1) / Nt;
+                bm[0] = ar * dz_new;
+            } else {
+                cm[0] = -dt2 * dI(t - 1, i);
+                double dz_new = dz_cell(t, i) + (dz_cn(t, i) - dz_cell(t, i)) * (subcycle + 1) / Nt;
+                bm[0] = ar * dz_new - cm[0];
+                am[nvl - 1] = -dt2 * dI(b, i);
+                dz_new = dz_cell(b, i) + (dz_cn(b, i) - dz_cell(b, i)) * (subcycle + 1) / Nt;
+                bm[nvl - 1] = -am[nvl - 1] + ar * dz_new;
+            }
+            load_oqb(i, b, t);
+            int tq = c->tri_or_quad(i);
+            for (int k = b; k <= t; ++k) {
+                int kk = t + 1 - k;
+                double sQi[2] = {0, 0}, sQii[2] = {0, 0}, shd[2] = {0, 0}, shl[2] = {0, 0}, cik[2];
+                for (int l = 1; l <= tq; ++l) {
+                    int j = c->facenum_at_cell(l, i);
+                    int ii = c->adj_cellnum_at_cell(l, i);
+                    for (int i3 = 1; i3 <= ntr; ++i3) cik[i3 - 1] = ii > 0 ? CC(k, ii, i3) : OQB(k, i3);
+                    if (face_open(j)) {
+                        double q2 = QJ(k, j) * (double)c->sign_in_outflow(l, i);
+                        if (q2 > 0.0) {
+                            for (int i3 = 1; i3 <= ntr; ++i3) sQi[i3 - 1] = sQi[i3 - 1] + std::fabs(q2) * CC(k, i, i3);
+                        } else if (q2 < 0.0) {
+                            for (int i3 = 1; i3 <= ntr; ++i3) sQii[i3 - 1] = sQii[i3 - 1] + std::fabs(q2) * cik[i3 - 1];
+                        }
+                        for (int i3 = 1; i3 <= ntr; ++i3) shd[i3 - 1] = shd[i3 - 1] + dJ(k, j) * (cik[i3 - 1] - CC(k, i, i3));
+                        for (int i3 = 1; i3 <= ntr; ++i3)
+                            shl[i3 - 1] = shl[i3 - 1] + PJ(k, j, i3) * std::fabs(q2) * (CC(k, i, i3) - cik[i3 - 1]);
+                    }
+                }
+                for (int i3 = 1; i3 <= ntr; ++i3) {
+                    double h_adv = dt2 * (sQii[i3 - 1] - sQi[i3 - 1]);
+                    double h_diff = dt2 * shd[i3 - 1];
+                    double h_flux = 0.5 * dt2 * shl[i3 - 1];
+                    double dz_old = dz_cell(k, i) + (dz_cn(k, i) - dz_cell(k, i)) * subcycle / Nt;
+                    double v = ar * dz_old * CC(k, i, i3) + h_adv + h_diff;
+                    if (p.h_flux_limiter > 0) v = v + h_flux;
+                    rhs[(size_t)(i3 - 1) * L + kk - 1] = v;
+                }
+            }
+            if (nvl != 1) {
+                for (int k = b; k <= t; ++k) {
+                    int kk = t + 1 - k;
+                    for (int i3 = 1; i3 <= ntr; ++i3) {
+                        double &R = rhs[(size_t)(i3 - 1) * L + kk - 1];
+                        double v_adv, v_flux = 0.0;
+                        if (k == b) {
+                            double qp = std::fabs(0.5 * (QI(k, i) + std::fabs(QI(k, i))));
+                            double qm = std::fabs(0.5 * (QI(k, i) - std::fabs(QI(k, i))));
+                            v_adv = dt2 * (-qp * CC(k, i, i3) + qm * CC(k + 1, i, i3));
+                            R = R + v_adv;
+                            if (p.v_flux_limiter > 0) {
+                                v_flux = 0.5 * dt2 * (-PI_(k, i, i3) * qp * (CC(k + 1, i, i3) - CC(k, i, i3)) +
+                                                      PI_(k, i, i3) * qm * (CC(k, i, i3) - CC(k + 1, i, i3)));
+                                R = R + v_flux;
+                            }
+                        } else if (k == t) {
+                            double qp = std::fabs(0.5 * (QI(k - 1, i) + std::fabs(QI(k - 1, i))));
+                            double qm = std::fabs(0.5 * (QI(k - 1, i) - std::fabs(QI(k - 1, i))));
+                            v_adv = dt2 * (qp * CC(k - 1, i, i3) - qm * CC(k, i, i3));
+                            R = R + v_adv;
+                            if (p.v_flux_limiter > 0) {
+                                v_flux = 0.5 * dt2 * (PI_(k - 1, i, i3) * qp * (CC(k, i, i3) - CC(k - 1, i, i3)) -
+                                                      PI_(k - 1, i, i3) * qm * (CC(k - 1, i, i3) - CC(k, i, i3)));
+                                R = R + v_flux;
+                            }
+                        } else {
+                            double qp1 = std::fabs(0.5 * (QI(k - 1, i) + std::fabs(QI(k - 1, i))));
+                            double qp = std::fabs(0.5 * (QI(k, i) + std::fabs(QI(k, i))));
+                            double qm = std::fabs(0.5 * (QI(k, i) - std::fabs(QI(k, i))));
+                            double qm1 = std::fabs(0.5 * (QI(k - 1, i) - std::fabs(QI(k - 1, i))));
+                            v_adv = dt2 * (qp1 * CC(k - 1, i, i3) - qp * CC(k, i, i3) + qm * CC(k + 1, i, i3) -
+                                           qm1 * CC(k, i, i3));
+                            R = R + v_adv;
+                            if (p.v_flux_limiter > 0) {
+                                v_flux = 0.5 * dt2 *
+                                         (PI_(k - 1, i, i3) * qp1 * (CC(k, i, i3) - CC(k - 1, i, i3)) -
+                                          PI_(k, i, i3) * qp * (CC(k + 1, i, i3) - CC(k, i, i3)) +
+                                          PI_(k, i, i3) * qm * (CC(k, i, i3) - CC(k + 1, i, i3)) -
+                                          PI_(k - 1, i, i3) * qm1 * (CC(k - 1, i, i3) - CC(k, i, i3)));
+                                R = R + v_flux;
+                            }
+                        }
+                    }
+                }
+            }
+            if (!tridiagonal_solver(L, nvl, ntr, am.data(), bm.data(), cm.data(), rhs.data(), sol.data(), gm.data())) {
+                set_err(c, GOM_E_ZERO_PIVOT, 1285, i, 0, 0.0);
+                return GOM_E_ZERO_PIVOT;
+            }
+            for (int k = b; k <= t; ++k) {
+                int kk = t - k + 1;
+                for (int i3 = 1; i3 <= ntr; ++i3) {
+                    double s = sol[(size_t)(i3 - 1) * L + kk - 1];
+                    if (s >= 0.0 && s <= 50.0) CN(k, i, i3) = s;
+                    else if (s < 0.0) CN(k, i, i3) = 0.0;
+                    else if (s > 50.0) CN(k, i, i3) = 50.0;
+                }
+            }
+        }
+        // :1352-1372 copy back
+        for (int i = 1; i <= NC; ++i) {
+            int b = c->bottom_layer_at_element(i), t = top_el(i);
+            for (int k = b; k <= t; ++k)
+                for (int i3 = 1; i3 <= ntr; ++i3) CC(k, i, i3) = CN(k, i, i3);
+            for (int k = 0; k <= b - 1; ++k)
+                for (int i3 = 1; i3 <= ntr; ++i3) CC(k, i, i3) = 0.0;
+            for (int k = t + 1; k <= L + 1; ++k)
+                for (int i3 = 1; i3 <= ntr; ++i3) CC(k, i, i3) = 0.0;
+        }
+    }
+    // :1403-1467 node and face averages
+    for (int i = 1; i <= NN; ++i) {
+        for (int k = top_n(i); k >= c->bottom_layer_at_node(i); --k) {
+            if (top_n(i) == 0) break;
+            for (int i3 = 1; i3 <= ntr; ++i3) {
+                double s11 = 0.0, s22 = 0.0;
+                int count1 = 0;
+                for (int l = 1; l <= c->adj_cells_at_node(i); ++l) {
+                    int ii = c->adj_cellnum_at_node(l, i);
+                    if (k >= c->bottom_layer_at_element(ii) && k <= top_el(ii)) {
+                        s11 = s11 + c->area(ii) * dz_cn(k, ii);
+                        s22 = s22 + c->area(ii) * dz_cn(k, ii) * CN(k, ii, i3);
+                    } else {
+                        count1 = count1 + 1;
+                    }
+                }
+                if (s11 == 0.0) NDN(k, i, i3) = 0.0;
+                else NDN(k, i, i3) = s22 / s11;
+                if (count1 == c->adj_cells_at_node(i) && k != top_n(i)) NDN(k, i, i3) = NDN(k + 1, i, i3);
+            }
+        }
+    }
+    for (int j = 1; j <= NF; ++j) {
+        int n1 = c->nodenum_at_face(1, j), n2 = c->nodenum_at_face(2, j);
+        for (int k = c->bottom_layer_at_face(j); k <= top_f(j); ++k)
+            for (int i3 = 1; i3 <= ntr; ++i3) FCN(k, j, i3) = (NDN(k, n1, i3) + NDN(k, n2, i3)) * 0.5;
+    }
+    // :1471-1482 write back (slot 1 = salinity, slot 2 = temperature)
+    for (int i3 = 1; i3 <= ntr; ++i3) {
+        int tid = tran_id[i3 - 1];
+        int slot = tid;  // the reference copies con_*(:,:,1) to salt and (:,:,2) to temperature
+        if (slot > ntr) continue;
+        A2<double> dc = FD(c, tid == 1 ? GOM_F_SALT_CELL_NEW : GOM_F_TEMP_CELL_NEW);
+        A2<double> dn = FD(c, tid == 1 ? GOM_F_SALT_NODE : GOM_F_TEMP_NODE);
+        A2<double> df = FD(c, tid == 1 ? GOM_F_SALT_FACE : GOM_F_TEMP_FACE);
+        for (int i = 1; i <= NC; ++i)
+            for (int k = 1; k <= L; ++k) dc(k, i) = CN(k, i, slot);
+        for (int i = 1; i <= NN; ++i)
+            for (int k = 1; k <= L; ++k) dn(k, i) = NDN(k, i, slot);
+        for (int j = 1; j <= NF; ++j)
+            for (int k = 1; k <= L; ++k) df(k, j) = FCN(k, j, slot);
+    }
+    return GOM_OK;
+}
+
+// calculate_density_full.f90:13-246 (ana_density 0) and calculate_density_linear.f90:10 (1)
+namespace {
+double eos_surface(double rtemp, double rsalt) {
+    double t2 = rtemp * rtemp, t3 = t2 * rtemp, t4 = t2 * t2, t5 = t3 * t2;
+    double sq = std::sqrt(rsalt);
+    double sq3 = sq * sq * sq;
+    double c0 = (double)(1000.0f - 0.157406f);
+    return c0 + F(6.793952e-2f) * rtemp - F(9.095290e-3f) * t2 + F(1.001685e-4f) * t3 - F(1.120083e-6f) * t4 +
+           F(6.536332e-9f) * t5 +
+           rsalt * (F(0.824493f) - F(4.089900e-3f) * rtemp + F(7.643800e-5f) * t2 - F(8.246700e-7f) * t3 +
+                    F(5.387500e-9f) * t4) +
+           sq3 * (F(-5.72466e-3f) + F(1.022700e-4f) * rtemp - F(1.654600e-6f) * t2) + F(4.831400e-4f) * (rsalt * rsalt);
+}
+double eos_bulk(double rtemp, double rsalt, double pres) {
+    double t2 = rtemp * rtemp, t3 = t2 * rtemp, t4 = t2 * t2;
+    double sq = std::sqrt(rsalt);
+    double sq3 = sq * sq * sq;
+    double p2 = pres * pres;
+    return F(19652.21f) + F(148.4206f) * rtemp - F(2.327105f) * t2 + F(1.360477e-2f) * t3 - F(5.155288e-5f) * t4 +
+           pres * (F(3.239908f) + F(1.43713e-3f) * rtemp + F(1.16092e-4f) * t2 - F(5.77905e-7f) * t3) +
+           p2 * (F(8.50935e-5f) - F(6.12293e-6f) * rtemp + F(5.2787e-8f) * t2) +
+           rsalt * (F(54.6746f) - F(0.603459f) * rtemp + F(1.09987e-2f) * t2 - F(6.1670e-5f) * t3) +
+           sq3 * (F(7.944e-2f) + F(1.6483e-2f) * rtemp - F(5.3009e-4f) * t2) +
+           pres * rsalt * (F(2.2838e-3f) - F(1.0981e-5f) * rtemp - F(1.6078e-6f) * t2) +
+           F(1.91075e-4f) * pres * sq3 - F(9.9348e-7f) * p2 * rsalt + F(2.08160e-8f) * rtemp * p2 * rsalt +
+           F(9.1697e-10f) * t2 * p2 * rsalt;
+}
+}  // namespace
+
+int gom_step_density(gom_ctx *c) {
+    if (!c) return GOM_E_ARG;
+    const gom_params &p = c->p;
+    if (p.baroclinic_flag != 1) return GOM_OK;
+    const int L = c->L;
+    const double tmin = -5.0, tmax = 100.0, smin = -5.0, smax = 100.0;
+    A2<double> rho_node = FD(c, GOM_F_RHO_NODE), rho_face = FD(c, GOM_F_RHO_FACE), rho_cell = FD(c, GOM_F_RHO_CELL),
+               temp_node = FD(c, GOM_F_TEMP_NODE), salt_node = FD(c, GOM_F_SALT_NODE), temp_face = FD(c, GOM_F_TEMP_FACE),
+               salt_face = FD(c, GOM_F_SALT_FACE), dz_node = FD(c, GOM_F_DZ_NODE), dz_face = FD(c, GOM_F_DZ_FACE);
+    A1<int32_t> top_n = FI1(c, GOM_F_TOP_LAYER_NODE), top_f = FI1(c, GOM_F_TOP_LAYER_FACE),
+                top_el = FI1(c, GOM_F_TOP_LAYER_CELL);
+    const double c981 = F(9.81f), c1e5h = (double)(1.0e-5f * 0.5f), c1e5 = F(1.0e-5f);
+    auto column = [&](A2<double> rho, A2<double> tt, A2<double> ss, A2<double> dz, int e, int b, int t, int site) {
+        for (int k = b; k <= t; ++k) {
+            double rtemp = tt(k, e), rsalt = ss(k, e);
+            if (rtemp < tmin || rtemp > tmax || rsalt < smin || rsalt > smax) {
+                set_err(c, GOM_E_DENSITY, site, e, k, rtemp < tmin || rtemp > tmax ? rtemp : rsalt);
+                return false;
+            }
+            if (p.ana_density == 1) {
+                rho(k, e) = F(1000.0f) + F(0.7f) * rsalt;
+            } else {
+                rho(k, e) = eos_surface(rtemp, rsalt);
+                if (p.msl - c->zl(k) > F(100.0f)) {
+                    double pres = F(0.0f);
+                    for (int kk = k; kk <= t; ++kk) {
+                        double ptmp = c981 * rho(kk, e) * dz(kk, e);
+                        if (kk == k) pres = pres + c1e5h * ptmp;
+                        else pres = pres + c1e5 * ptmp;
+                    }
+                    double sbm = eos_bulk(rtemp, rsalt, pres);
+                    double ratio = 1.0 / (1.0 - pres / sbm);
+                    rho(k, e) = rho(k, e) * ratio;
+                }
+            }
+            if (rho(k, e) < F(980.0f)) {
+                set_err(c, GOM_E_DENSITY, site, e, k, rho(k, e));
+                return false;
+            }
+        }
+        for (int k = 1; k <= b - 1; ++k) rho(k, e) = rho(b, e);
+        for (int k = t + 1; k <= L; ++k) rho(k, e) = rho(t, e);
+        return true;
+    };
+    for (int i = 1; i <= c->NN; ++i)
+        if (top_n(i) != 0)
+            if (!column(rho_node, temp_node, salt_node, dz_node, i, c->bottom_layer_at_node(i), top_n(i), 43))
+                return GOM_E_DENSITY;
+    if (p.ana_density == 0)
+        for (int j = 1; j <= c->NF; ++j)
+            if (top_f(j) != 0)
+                if (!column(rho_face, temp_face, salt_face, dz_face, j, c->bottom_layer_at_face(j), top_f(j), 130))
+                    return GOM_E_DENSITY;
+    for (int i = 1; i <= c->NC; ++i) {
+        int t = top_el(i), b = c->bottom_layer_at_element(i);
+        if (t == 0) continue;
+        for (int k = b; k <= t; ++k) {
+            rho_cell(k, i) = F(0.0f);
+            int icount = 0;
+            for (int l = 1; l <= c->tri_or_quad(i); ++l) {
+                int nd = c->nodenum_at_cell(l, i);
+                if (top_n(nd) != 0) {
+                    icount = icount + 1;
+                    rho_cell(k, i) = rho_cell(k, i) + rho_node(k, nd);
+                }
+            }
+            if (icount == 0) {
+                set_err(c, GOM_E_DRY, 224, i, k, 0.0);
+                return GOM_E_DRY;
+            }
+            rho_cell(k, i) = rho_cell(k, i) / icount;
+        }
+        for (int k = 1; k <= b - 1; ++k) rho_cell(k, i) = rho_cell(b, i);
+        for (int k = t + 1; k <= L; ++k) rho_cell(k, i) = rho_cell(t, i);
+    }
+    return GOM_OK;
+}
+
+// update_variables.f90:16-31 (state part; the vertical means feed output only)
+int gom_step_swap(gom_ctx *c) {
+    if (!c) return GOM_E_ARG;
+    const int pairs[][2] = {{GOM_F_ETA_CELL, GOM_F_ETA_CELL_NEW},     {GOM_F_WN_CELL, GOM_F_WN_CELL_NEW},
+                            {GOM_F_DZ_CELL, GOM_F_DZ_CELL_NEW},       {GOM_F_DZHALF_CELL, GOM_F_DZHALF_CELL_NEW},
+                            {GOM_F_SALT_CELL, GOM_F_SALT_CELL_NEW},   {GOM_F_TEMP_CELL, GOM_F_TEMP_CELL_NEW},
+                            {GOM_F_UN_FACE, GOM_F_UN_FACE_NEW},       {GOM_F_VN_FACE, GOM_F_VN_FACE_NEW},
+                            {GOM_F_DZ_FACE, GOM_F_DZ_FACE_NEW},       {GOM_F_DZHALF_FACE, GOM_F_DZHALF_FACE_NEW},
+                            {GOM_F_DZ_NODE, GOM_F_DZ_NODE_NEW},       {GOM_F_DZHALF_NODE, GOM_F_DZHALF_NODE_NEW}};
+    for (auto &pr : pairs) c->fd[pr[0]] = c->fd[pr[1]];
+    return GOM_OK;
+}
+
+int gom_step_all(gom_ctx *c, int32_t *pcg_iters) {
+    if (!c) return GOM_E_ARG;
+    int e;
+    if ((e = gom_step_bottom_friction(c))) return e;
+    if ((e = gom_step_boundary_velocity(c))) return e;
+    if ((e = gom_step_advection(c))) return e;
+    if ((e = gom_step_momentum(c))) return e;
+    if ((e = gom_step_free_surface(c, pcg_iters))) return e;
+    if ((e = gom_step_velocities(c))) return e;
+    if ((e = gom_step_layers(c))) return e;
+    if ((e = gom_step_node_velocity(c))) return e;
+    if ((e = gom_step_transport(c))) return e;
+    if ((e = gom_step_density(c))) return e;
+    return gom_step_swap(c);
+}
+
+// spec: check_conservation.f90:28-57
+int gom_conservation(gom_ctx *c, double *volume, double *salt_mass) {
+    if (!c) return GOM_E_ARG;
+    A2<double> dz_cell = FD(c, GOM_F_DZ_CELL), salt = FD(c, GOM_F_SALT_CELL);
+    A1<int32_t> top_el = FI1(c, GOM_F_TOP_LAYER_CELL);
+    double v = 0.0, s = 0.0;
+    for (int i = 1; i <= c->NC; ++i) {
+        for (int k = c->bottom_layer_at_element(i); k <= top_el(i); ++k) {
+            double vv = c->area(i) * dz_cell(k, i);
+            v = v + vv;
+            s = s + vv * salt(k, i);
+        }
+    }
+    if (volume) *volume = v;
+    if (salt_mass) *salt_mass = s;
+    return GOM_OK;
+}
+
+}  // extern "C"
