@@ -53,10 +53,12 @@ PCG_BYTES_PER_CELL_ITERATION = 120
 FS_ASSEMBLY_BYTES_PER_CELL_LAYER = 64
 
 
-def make_deck(small: bool):
+def make_deck(size: str):
     from gom_release_gb300.deck import estuary
-    if small:
+    if size == "small":
         return estuary(nx=120, ny=50, dx=100.0, n_layers=20)
+    if size == "medium":
+        return estuary(nx=300, ny=125, dx=100.0, n_layers=20)
     return estuary()
 
 
@@ -240,7 +242,7 @@ def run_reference(args, world, rank):
     if rank != 0:
         return
     from gom_release_gb300.deck import active_cell_layers, initial_state
-    deck = make_deck(args.small)
+    deck = make_deck(args.size)
     st = initial_state(deck)
     ncl = active_cell_layers(deck, st)
     from gom_release_gb300.core import GomCore
@@ -275,8 +277,11 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--small", action="store_true", help="a 6k-cell estuary (profiling runs)")
+    ap.add_argument("--size", default="full", choices=["full", "medium", "small"],
+                    help="full: the benchmark workload; medium (38k cells) and small (6k cells) for profiling")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-phases", action="store_true", help="skip the per-phase timing pass")
+    ap.add_argument("--e2e-steps", type=int, default=0)
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":
@@ -289,7 +294,7 @@ def main():
     from gom_release_gb300.deck import HostForcing, active_cell_layers, initial_state
     from gom_release_gb300.driver import Run
 
-    deck = make_deck(args.small)
+    deck = make_deck(args.size)
     st = initial_state(deck)
     ncl = active_cell_layers(deck, st)
     lib = load_core()
@@ -309,7 +314,7 @@ def main():
     secs = reduce_max(secs, world)
     pcg_total = run.core.pcg_iterations_total()
     # ---- e2e: the public API with host buffers, forcing computed and result read every step
-    ke = max(10, args.steps // 4)
+    ke = args.e2e_steps or max(10, args.steps // 4)
     run.core.synchronize()
     t0 = time.perf_counter()
     e0 = torch_mod.cuda.Event(enable_timing=True)
@@ -333,11 +338,14 @@ def main():
     f.update(wind_stress_normal=run.forcing.wind_normal, wind_stress_tangnt=run.forcing.wind_tangnt,
              gamma_t=run.forcing.gamma_t)
     pcg_mean = (pcg_total / max(1, args.warmup + args.steps))
-    phases = time_phases(deck, snap, lib, f, torch_mod)
-    pb = phase_bytes(deck, ncl, pcg_mean)
-    dom = max(phases, key=phases.get)
     peak, peak_kind = measured_peak()
-    achieved = pb.get(dom, 0) / phases[dom] / 1e9
+    if args.no_phases:
+        phases, dom, achieved = {}, None, None
+    else:
+        phases = time_phases(deck, snap, lib, f, torch_mod)
+        pb = phase_bytes(deck, ncl, pcg_mean)
+        dom = max(phases, key=phases.get)
+        achieved = pb.get(dom, 0) / phases[dom] / 1e9
     if rank != 0:
         barrier(world)
         return
@@ -360,7 +368,7 @@ def main():
             "pcg_iters_mean": pcg_mean,
         },
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+                     "frac": (achieved / peak) if achieved else None, "peak_source": peak_kind, "traffic": None,
                      "phase_ms": {k: v * 1e3 for k, v in phases.items()}},
         "cpu_baseline": cpu,
         "e2e": {"value": ncl * ke * world / e2e_secs, "unit": UNIT, "h2d_bytes_per_step": h2d,

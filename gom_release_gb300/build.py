@@ -40,7 +40,7 @@ def build_core(verbose: bool = False, extra: list[str] | None = None) -> Path:
     OUT.mkdir(parents=True, exist_ok=True)
     nv = nvcc()
     extra = extra or []
-    headers = [CSRC / h for h in ("gom_device.cuh", "gom_launch.h")] + [PKG.parent / "include" / "gom_core.h"]
+    headers = [CSRC / h for h in ("gom_device.cuh", "gom_launch.h", "gom_pcg.cuh")] + [PKG.parent / "include" / "gom_core.h"]
     hdr_mtime = max(h.stat().st_mtime for h in headers)
 
     def compile_one(src):

@@ -1,0 +1,209 @@
+// gom_pcg.cuh -- the Jacobi-preconditioned conjugate gradient of pre_conj_grad.f90:9-230 as one
+// cooperative kernel, shared by the translation units that launch it.  Definitions have internal
+// linkage (anonymous namespace), so each including file gets its own copy.
+#pragma once
+
+#include "gom_device.cuh"
+
+namespace gom {
+namespace {
+
+// -------------------------------------------------------------------- grid-wide barrier
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Sense-counting barrier over all blocks of a cooperative launch.  Every wait is bounded: after
+// about 2 s the block records GOM_E_TIMEOUT and the caller leaves the kernel.
+__device__ bool grid_barrier(unsigned *bar, unsigned nblocks, gom_status *st) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned *vgen = bar + 1;
+        unsigned gen = *vgen;
+        __threadfence();
+        unsigned arrived = atomicAdd(bar, 1u);
+        int good = 1;
+        if (arrived == nblocks - 1) {
+            atomicExch(bar, 0u);
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            unsigned long long t0 = globaltimer_ns();
+            while (*vgen == gen) {
+                __nanosleep(64);
+                if (globaltimer_ns() - t0 > 2000000000ull) {
+                    record_error(st, GOM_E_TIMEOUT, 1, (int)blockIdx.x, 0, 0.0);
+                    good = 0;
+                    break;
+                }
+            }
+        }
+        __threadfence();
+        ok = good;
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+// block reduction of one double; result valid in every thread
+template <int THREADS>
+__device__ __forceinline__ double block_sum(double v, double *sh) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (w == 0) {
+        t = lane < THREADS / 32 ? sh[lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+        if (lane == 0) sh[32] = t;
+    }
+    __syncthreads();
+    double r = sh[32];
+    __syncthreads();
+    return r;
+}
+
+// sum of all block partials in a fixed order (identical in every block)
+__device__ __forceinline__ double sum_partials(const double *part, int n, double *sh) {
+    int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (w == 0) {
+        double t = 0.0;
+        for (int i = lane; i < n; i += 32) t += ((volatile const double *)part)[i];
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+        if (lane == 0) sh[33] = t;
+    }
+    __syncthreads();
+    double r = sh[33];
+    __syncthreads();
+    return r;
+}
+
+struct PcgArgs {
+    Geom g;
+    const double *sp, *b;
+    double *x, *minv, *r, *s, *q, *dA, *dB, *pdq, *pdelta;
+    unsigned *bar;
+    int *iters;
+    int maxit;
+    double tol;
+    gom_status *st;
+};
+
+// pre_conj_grad.f90:46-221 as one cooperative kernel: the matrix-vector product of row i uses
+// the row's own 5 coefficients in CSR order (diagonal first) and the neighbours' values; the
+// d-update of iteration n is fused into the product of iteration n+1 (d double-buffered), so one
+// iteration needs two grid barriers.
+constexpr int PCG_THREADS = 256;
+
+__global__ void __launch_bounds__(PCG_THREADS) k_pcg(PcgArgs a) {
+    __shared__ double sh[40];
+    const Geom &g = a.g;
+    const int n = g.NC;
+    const unsigned nblocks = gridDim.x;
+    const long stride = (long)gridDim.x * blockDim.x;
+    const long t0 = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    // initial residual, Jacobi preconditioner, d = M^-1 r
+    double loc = 0.0;
+    for (long i = t0; i < n; i += stride) {
+        const double *row = a.sp + i * 5;
+        int cell = (int)i + 1;
+        double sum = 0.0;
+        sum = sum + row[0] * a.x[i];
+        int tq = g.tri_or_quad[i];
+        for (int l = 1; l <= tq; ++l) {
+            int nb = g.cell_adj(l, cell);
+            if (nb != 0) sum = sum + row[l] * a.x[nb - 1];
+        }
+        double mi = 1.0 / row[0];
+        double ri = a.b[i] - sum;
+        double di = 0.0 + mi * ri;
+        a.minv[i] = mi;
+        a.r[i] = ri;
+        a.dA[i] = di;
+        loc += ri * di;
+    }
+    double bs = block_sum<PCG_THREADS>(loc, sh);
+    if (threadIdx.x == 0) a.pdelta[blockIdx.x] = bs;
+    if (!grid_barrier(a.bar, nblocks, a.st)) return;
+    double delta_new = sum_partials(a.pdelta, nblocks, sh);
+    const double delta_0 = delta_new;
+    int iters = 0;
+    if (delta_0 != 0.0) {
+        double beta = 0.0;
+        double *dcur = a.dA, *dnext = a.dB;
+        bool first = true;
+        for (int it = 1; it <= a.maxit; ++it) {
+            if (failed(a.st)) return;
+            // q = A d with d = s + beta*d_old fused in
+            loc = 0.0;
+            for (long i = t0; i < n; i += stride) {
+                const double *row = a.sp + i * 5;
+                int cell = (int)i + 1;
+                double di = first ? dcur[i] : a.s[i] + beta * dcur[i];
+                double sum = 0.0;
+                sum = sum + row[0] * di;
+                int tq = g.tri_or_quad[i];
+                for (int l = 1; l <= tq; ++l) {
+                    int nb = g.cell_adj(l, cell);
+                    if (nb != 0) {
+                        double dn = first ? dcur[nb - 1] : a.s[nb - 1] + beta * dcur[nb - 1];
+                        sum = sum + row[l] * dn;
+                    }
+                }
+                if (!first) dnext[i] = di;
+                a.q[i] = sum;
+                loc += di * sum;
+            }
+            bs = block_sum<PCG_THREADS>(loc, sh);
+            if (threadIdx.x == 0) a.pdq[blockIdx.x] = bs;
+            if (!grid_barrier(a.bar, nblocks, a.st)) return;
+            double dq = sum_partials(a.pdq, nblocks, sh);
+            double alpha = delta_new / dq;
+            double *dv = first ? dcur : dnext;
+            loc = 0.0;
+            for (long i = t0; i < n; i += stride) {
+                double di = dv[i];
+                a.x[i] = a.x[i] + alpha * di;
+                double ri = a.r[i] - alpha * a.q[i];
+                a.r[i] = ri;
+                double si = 0.0 + a.minv[i] * ri;
+                a.s[i] = si;
+                loc += ri * si;
+            }
+            bs = block_sum<PCG_THREADS>(loc, sh);
+            if (threadIdx.x == 0) a.pdelta[blockIdx.x] = bs;
+            if (!grid_barrier(a.bar, nblocks, a.st)) return;
+            double delta_old = delta_new;
+            delta_new = sum_partials(a.pdelta, nblocks, sh);
+            beta = delta_new / delta_old;
+            if (!first) {
+                double *t = dcur;
+                dcur = dnext;
+                dnext = t;
+            }
+            first = false;
+            iters = it;
+            if (sqrt(delta_new * delta_new / (delta_0 * delta_0)) < a.tol) break;
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *a.iters = iters;
+}
+
+// grid of the cooperative launch: enough blocks for one row per thread, at most two resident
+// blocks per SM (and never more than the occupancy allows)
+inline int pcg_blocks_for(long n_rows, int per_sm, int num_sms) {
+    if (per_sm < 1) per_sm = 1;
+    long need = (n_rows + PCG_THREADS - 1) / PCG_THREADS;
+    long maxb = (long)per_sm * num_sms;
+    long cap = (long)num_sms * (per_sm < 2 ? per_sm : 2);
+    if (cap > maxb) cap = maxb;
+    long b = need < cap ? need : cap;
+    return b < 1 ? 1 : (int)b;
+}
+
+}  // namespace
+}  // namespace gom
