@@ -311,6 +311,22 @@ int gom_get_status(struct gom_ctx *ctx, gom_status *status, int clear);
 /* Wait for all device work of the context. */
 int gom_synchronize(struct gom_ctx *ctx);
 
+/* Free-surface Jacobi-PCG solve that allocates nothing (no counterpart in the reference).
+ * For callers that cannot call cudaMalloc -- their arrays live in device memory owned by another
+ * runtime (OpenACC / CUDA Fortran data regions, a pooled service) -- so they cannot give the
+ * solver work vectors.  The work vectors live in a fixed file-scope device array of the library:
+ * n_cells must be <= 262144 (GOM_E_ARG otherwise).  Inputs and outputs are device pointers:
+ * tri_or_quad (n_cells), adj_cellnum_at_cell (4, n_cells), sparsem (0:4, n_cells: diagonal then
+ * the neighbour coefficients in local-face order, as solve_free_surface_equation.f90 builds them),
+ * rhs (n_cells), x (n_cells, initial guess in, solution out).  Work is ordered on `stream`
+ * (a cudaStream_t, NULL = legacy default stream).  With iterations != NULL the call waits and
+ * returns the solve's status and iteration count; with NULL it returns after the launch.  All
+ * calls share the array: calls that overlap on the GPU race.  The first call on a device does a
+ * one-time set-up and should come before any stream capture. */
+int gom_pcg_solve_noalloc(int32_t n_cells, const int32_t *tri_or_quad, const int32_t *adj_cellnum_at_cell,
+                          const double *sparsem, const double *rhs, double *x, int32_t max_iteration,
+                          double error_tolerance, void *stream, int32_t *iterations);
+
 /* The CUDA stream (cudaStream_t) all device work of the context is ordered on, so a caller can
  * record events or order its own work against the core.  NULL for a CPU implementation. */
 void *gom_stream(struct gom_ctx *ctx);
