@@ -389,6 +389,9 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
     if (e == cudaSuccess) e = dalloc(c, &W.sa2, L * NC * 2);
     if (e == cudaSuccess) e = dalloc(c, &W.obk, L * (size_t)d.n_ob * 2);
     if (e == cudaSuccess) e = dalloc(c, &W.qbk, L * (size_t)d.n_qb * 2);
+    if (e == cudaSuccess) e = dalloc(c, &W.uflf, (L + 1) * NF);
+    if (e == cudaSuccess) e = dalloc(c, &W.vflf, (L + 1) * NF);
+    if (e == cudaSuccess) e = dalloc(c, &W.node_weight, NN);
     if (e == cudaSuccess) e = dalloc(c, &W.cons, 2 + 2 * (size_t)((NC + 255) / 256));
     if (e == cudaSuccess) e = dalloc(c, &c->x.status, 1);
     if (e != cudaSuccess) return fail(e == cudaErrorMemoryAllocation ? GOM_E_NOMEM : GOM_E_CUDA);
@@ -434,6 +437,7 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
         return fail(GOM_E_NOMEM);
     std::memset(c->h_status, 0, sizeof(gom_status));
     if (pcg_configure(c->x, c->device) != cudaSuccess) return fail(GOM_E_CUDA);
+    if (launch_node_weights(c->x) != cudaSuccess) return fail(GOM_E_CUDA);
     {
         size_t nb = (size_t)c->x.w.pcg_blocks;
         if (dalloc(c, &W.partial_dq, nb) != cudaSuccess || dalloc(c, &W.partial_delta, nb) != cudaSuccess)

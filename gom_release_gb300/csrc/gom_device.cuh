@@ -104,9 +104,25 @@ __device__ inline void record_error(gom_status *st, int code, int site, int enti
 __device__ __forceinline__ bool failed(const gom_status *st) { return *(volatile const int *)&st->code != 0; }
 
 // -------------------------------------------------------------------- geometry helpers
-// mod_function_library.f90:49-60
+// mod_function_library.f90:49-60 (x/2 == x*0.5 exactly)
 __device__ __forceinline__ double calculate_area(double x1, double x2, double x3, double y1, double y2, double y3) {
-    return fabs((x1 - x3) * (y2 - y3) - (x2 - x3) * (y1 - y3)) / 2.0;
+    return fabs((x1 - x3) * (y2 - y3) - (x2 - x3) * (y1 - y3)) * 0.5;
+}
+
+// Exact decisions about a rounded quotient fl(num/den) (num >= 0, den > 0) against a constant c,
+// deciding from num and c*den when they are more than 1e-9 apart (far beyond every rounding
+// error involved) and dividing only otherwise.  Same outcome as the division, fewer FP64 ops.
+__device__ __forceinline__ bool quotient_gt(double num, double den, double c) {
+    double t = c * den;
+    if (num > t * (1.0 + 1e-9)) return true;
+    if (num < t * (1.0 - 1e-9)) return false;
+    return num / den > c;
+}
+__device__ __forceinline__ bool quotient_lt(double num, double den, double c) {
+    double t = c * den;
+    if (num < t * (1.0 - 1e-9)) return true;
+    if (num > t * (1.0 + 1e-9)) return false;
+    return num / den < c;
 }
 
 // set_geometry_1.f90:48-63

@@ -24,6 +24,8 @@ struct Work {
     double *psii = nullptr;                                     // (0:L, NC, 2)
     double *sa1 = nullptr, *sa2 = nullptr;                      // (L, NC, 2) limiter sums per layer
     double *obk = nullptr, *qbk = nullptr;                      // (L, NOB, 2), (L, NQB, 2)
+    // node velocities: face-level velocity / face length (0:L, NF), static node weights (NN)
+    double *uflf = nullptr, *vflf = nullptr, *node_weight = nullptr;
     // conservation
     double *cons = nullptr;                                     // [volume, salt]
 };
@@ -53,5 +55,7 @@ cudaError_t launch_conservation(const Launch &x);
 
 // cooperative PCG set-up (grid size from occupancy); called once per context
 cudaError_t pcg_configure(Launch &x, int device);
+// static per-node weights of calculate_velocity_at_node.f90:103; called once per context
+cudaError_t launch_node_weights(const Launch &x);
 
 }  // namespace gom

@@ -65,22 +65,31 @@ cudaError_t launch_boundary_velocity(const Launch &x) {
 
 // ============================================================================================
 // ELM
-// check_intersection.f90:14-50
+// check_intersection.f90:14-50.  tt1 = delta1/delta and tt2 = delta2/delta must both lie in
+// [0, 1]; the sign test is exact, the upper bound is decided from |delta_i| against |delta|
+// unless the two are within 1e-9 of each other, and tt1 is divided out only for a hit.
+__device__ __forceinline__ int unit_range(double num, double den) {
+    // 1 if fl(num/den) in [0,1], 0 if not (den != 0)
+    if (num == 0.0) return 1;
+    if ((num < 0.0) != (den < 0.0)) return 0;
+    double an = fabs(num), ad = fabs(den);
+    if (an < ad * (1.0 - 1e-9)) return 1;
+    if (an > ad * (1.0 + 1e-9)) return 0;
+    return num / den <= 1.0;
+}
+
 __device__ __forceinline__ int check_intersection(double x1, double x2, double x3, double x4, double y1, double y2,
                                                   double y3, double y4, double &xin, double &yin) {
     double delta = (x2 - x1) * (y3 - y4) - (y2 - y1) * (x3 - x4);
+    if (delta == 0.0) return 0;
     double delta1 = (x3 - x1) * (y3 - y4) - (y3 - y1) * (x3 - x4);
+    if (!unit_range(delta1, delta)) return 0;
     double delta2 = (x2 - x1) * (y3 - y1) - (y2 - y1) * (x3 - x1);
-    if (delta != 0.0) {
-        double tt1 = delta1 / delta;
-        double tt2 = delta2 / delta;
-        if (tt1 >= -0.0 && tt1 <= 1.0 && tt2 >= -0.0 && tt2 <= 1.0) {
-            xin = x1 + (x2 - x1) * tt1;
-            yin = y1 + (y2 - y1) * tt1;
-            return 1;
-        }
-    }
-    return 0;
+    if (!unit_range(delta2, delta)) return 0;
+    double tt1 = delta1 / delta;
+    xin = x1 + (x2 - x1) * tt1;
+    yin = y1 + (y2 - y1) * tt1;
+    return 1;
 }
 
 // bilinear_interpolation.f90:8-121: returns 0 or GOM_ELM_BILINEAR
@@ -171,10 +180,8 @@ __device__ int search_straight_line(const Geom &g, const State &s, const Params 
     double area1 = area_sum(g, nel, x0, y0);
     double area2 = area_sum(g, nel, xt, yt);
     double ar = g.area[nel - 1];
-    double ae = fabs(area1 - ar) / ar;
-    if (ae > small_06) return GOM_ELM_START_OUTSIDE;
-    ae = fabs(area2 - ar) / ar;
-    if (!(ae < small_06)) {
+    if (quotient_gt(fabs(area1 - ar), ar, small_06)) return GOM_ELM_START_OUTSIDE;
+    if (!quotient_lt(fabs(area2 - ar), ar, small_06)) {
         const double c1 = 1.0 - 1.0e-4;
         double xcg = c1 * x0 + 1.0e-4 * g.x_cell[nel - 1];
         double ycg = c1 * y0 + 1.0e-4 * g.y_cell[nel - 1];
@@ -231,8 +238,7 @@ __device__ int search_straight_line(const Geom &g, const State &s, const Params 
             nel = adjc;
             ar = g.area[nel - 1];
             area1 = area_sum(g, nel, xt, yt);
-            ae = fabs(area1 - ar) / ar;
-            if (ae < small_06) {
+            if (quotient_lt(fabs(area1 - ar), ar, small_06)) {
                 nnel = nel;
                 break;
             }
@@ -331,7 +337,7 @@ __device__ int elm_backtrace(const Geom &g, const State &s, const Params &p, int
             double aa3 = calculate_area(X3, X4, xt, Y3, Y4, yt);
             double aa4 = calculate_area(X4, X1, xt, Y4, Y1, yt);
             double aa = fabs(aa1) + fabs(aa2) + fabs(aa3) + fabs(aa4);
-            if (fabs(aa - ar) / ar > small_06) return GOM_ELM_QUAD_OUTSIDE;
+            if (quotient_gt(fabs(aa - ar), ar, small_06)) return GOM_ELM_QUAD_OUTSIDE;
             int b = bilinear_interpolation(X1, X2, X3, X4, Y1, Y2, Y3, Y4, xt, yt, sta);
             if (b) return b;
         }
@@ -352,35 +358,44 @@ __device__ int elm_backtrace(const Geom &g, const State &s, const Params &p, int
     return 0;
 }
 
-// solve_nonlinear_advection.f90:52-87: one thread per (node, layer)
+// solve_nonlinear_advection.f90:52-87: one thread per (node, layer).
+// INT(dev/0.1) and INT(2*w*dt/delta_z_min) are 0 whenever the operands are more than 1e-9 below
+// the thresholds; that case (the usual one) is decided from squared quantities without square
+// roots or divisions, and every other case is computed exactly as the reference does.
 __global__ void k_elm_substeps(Geom g, State s, Params p) {
     long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
     const int L = g.L;
     if (t >= (long)g.NN * L) return;
     int i = (int)(t / L) + 1, k = (int)(t % L) + 1;
     const double dt = p.dt;
+    const double c01 = F(1.e-1f);
+    const double kthr = c01 * c01 / (dt * dt) * (1.0 - 1e-9);
     int nadj = g.adj_cells_at_node[i - 1];
     double xi = g.x_node[i - 1], yi = g.y_node[i - 1];
     double ui = (s.u_node[ix0(k, i, L)] + s.u_node[ix0(k - 1, i, L)]) * 0.5;
     double vi = (s.v_node[ix0(k, i, L)] + s.v_node[ix0(k - 1, i, L)]) * 0.5;
     double wi = (s.w_node[ix0(k, i, L)] + s.w_node[ix0(k - 1, i, L)]) * 0.5;
-    int iw = (int)(2 * wi * dt / p.delta_z_min);
+    double aw = 2 * wi * dt;
+    int iw = fabs(aw) < p.delta_z_min * (1.0 - 1e-9) ? 0 : (int)(aw / p.delta_z_min);
     double summ = 0.0;
     for (int j = 1; j <= nadj; ++j) {
         int ie = g.node_cell(j, i), id = g.node_count(j, i);
         int tq = g.tri_or_quad[ie - 1];
-        double devm = 0.0;
+        int imax = 0;
         for (int l = 1; l <= 2; ++l) {
             int nd = g.cell_node(l == 1 ? start_end_node(tq, id, 1) : start_end_node(tq, id, tq - 1), ie);
             double dx = xi - g.x_node[nd - 1], dy = yi - g.y_node[nd - 1];
-            double rl = sqrt(dx * dx + dy * dy);
+            double rl2 = dx * dx + dy * dy;
             double u2 = (s.u_node[ix0(k, nd, L)] + s.u_node[ix0(k - 1, nd, L)]) * 0.5;
             double v2 = (s.v_node[ix0(k, nd, L)] + s.v_node[ix0(k - 1, nd, L)]) * 0.5;
             double du = ui - u2, dv = vi - v2;
-            double dev = sqrt(du * du + dv * dv) / rl * dt;
-            if (dev > devm) devm = dev;
+            double sq = du * du + dv * dv;
+            if (sq < rl2 * kthr) continue;   // dev/0.1 < 1: contributes INT 0
+            double dev = sqrt(sq) / sqrt(rl2) * dt;
+            int id_l = (int)(dev / c01);
+            if (id_l > imax) imax = id_l;
         }
-        int idelta = max((int)(devm / F(1.e-1f)), iw);
+        int idelta = max(imax, iw);
         summ = summ + (double)idelta / nadj;
     }
     s.num_sub_elm[ix(k, i, L)] = max(p.elm_min_iter, min(p.elm_max_iter, (int)summ));
@@ -559,6 +574,36 @@ __global__ void __launch_bounds__(128) k_momentum(Geom g, State s, Forcing f, Pa
     int ba2 = a2 != 0 ? g.bottom_cell[a2 - 1] : 0, ta2 = a2 != 0 ? s.top_cell[a2 - 1] : 0;
     int bn1 = g.bottom_node[node1 - 1], tn1 = s.top_node[node1 - 1];
     int bn2 = g.bottom_node[node2 - 1], tn2 = s.top_node[node2 - 1];
+    // Terms the reference re-evaluates in every layer although their operands do not depend on
+    // the layer; evaluated once per face with the same expression, hence the same value.
+    double bt_rtemp1 = 0.0, bt_rtemp2 = 0.0;    // (1-theta) barotropic gradient across the face
+    if (btype == 0) {
+        double rtemp0 = gravity * dt / dj * (1.0 - theta) * (eta2 - eta1);
+        bt_rtemp1 = rtemp0 * ct2;
+        bt_rtemp2 = rtemp0 * sn2;
+    } else if (btype > 0) {
+        int ie = g.ob_element_flag[a1 - 1];
+        bt_rtemp1 = gravity * dt / dj * (1.0 - theta) * (f.eta_at_ob_old[ie - 1] - eta1);
+    }
+    double along_rtemp0 = wet_nodes ? gravity * dt / fl * (1.0 - theta) * (eta_n2 - eta_n1) : 0.0;
+    double along = (btype == 0) ? (along_rtemp0 + bt_rtemp2) : along_rtemp0;
+    double air1 = rt0_air * ct2, air2 = rtemp3_air + rt0_air * sn2;
+    double bc_dj = -gravity * dt / (p.rho_o * dj), bc_fl = -gravity * dt / (p.rho_o * fl);
+    double fl2 = fl * fl;
+    double rl1 = 0.0, rl2 = 0.0, inv_tq1 = 0.0, inv_tq2 = 0.0;
+    int tq1 = 0, tq2 = 0;
+    if (a2 != 0) {
+        double ddx = g.x_cell[a1 - 1] - g.x_face[j - 1], ddy = g.y_cell[a1 - 1] - g.y_face[j - 1];
+        rl1 = sqrt(ddx * ddx + ddy * ddy);
+        ddx = g.x_cell[a2 - 1] - g.x_face[j - 1];
+        ddy = g.y_cell[a2 - 1] - g.y_face[j - 1];
+        rl2 = sqrt(ddx * ddx + ddy * ddy);
+        tq1 = g.tri_or_quad[a1 - 1];
+        tq2 = g.tri_or_quad[a2 - 1];
+        inv_tq1 = tq1 == 4 ? 0.25 : 0.0;   // x/4 == x*0.25 exactly; triangles divide
+        inv_tq2 = tq2 == 4 ? 0.25 : 0.0;
+    }
+    const double spin = f.scal[2];
     for (int k = 1; k <= nvl; ++k) {
         int kk = tj - k + 1;
         double dzk = s.dz_face[ix(kk, j, L)];
@@ -576,13 +621,16 @@ __global__ void __launch_bounds__(128) k_momentum(Geom g, State s, Forcing f, Pa
                 tmp[2 * l - 1] = -ut * sn + vt * ct;
             }
             for (int l = 1; l <= 2; ++l) {
-                int ie = g.face_cell(l, j);
-                int tq = g.tri_or_quad[ie - 1];
+                int ie = l == 1 ? a1 : a2;
+                int tq = l == 1 ? tq1 : tq2;
+                double itq = l == 1 ? inv_tq1 : inv_tq2;
                 double ut = 0.0, vt = 0.0;
                 for (int ll = 1; ll <= tq; ++ll) {
                     int nd = g.cell_node(ll, ie);
-                    ut = ut + (s.u_node[ix0(kk, nd, L)] + s.u_node[ix0(kk - 1, nd, L)]) * 0.5 / tq;
-                    vt = vt + (s.v_node[ix0(kk, nd, L)] + s.v_node[ix0(kk - 1, nd, L)]) * 0.5 / tq;
+                    double uu = (s.u_node[ix0(kk, nd, L)] + s.u_node[ix0(kk - 1, nd, L)]) * 0.5;
+                    double vv = (s.v_node[ix0(kk, nd, L)] + s.v_node[ix0(kk - 1, nd, L)]) * 0.5;
+                    ut = ut + (itq != 0.0 ? uu * itq : uu / tq);
+                    vt = vt + (itq != 0.0 ? vv * itq : vv / tq);
                 }
                 tmp[2 * l + 2] = ut * ct + vt * sn;
                 tmp[2 * l + 3] = -ut * sn + vt * ct;
@@ -596,39 +644,21 @@ __global__ void __launch_bounds__(128) k_momentum(Geom g, State s, Forcing f, Pa
             double khv = hdiff * g.area[a1 - 1];
             hdiff = hdiff + p.ah_0;
             s.kh[ix(k, j, L)] = khv + p.kh_0;
-            double d2udy = 4.0 * (tmp[2] + tmp[0] - 2 * unk) / (fl * fl);
-            double d2vdy = 4.0 * (tmp[3] + tmp[1] - 2 * vnk) / (fl * fl);
-            for (int l = 1; l <= 2; ++l) {
-                int ie = g.face_cell(l, j);
-                double ddx = g.x_cell[ie - 1] - g.x_face[j - 1], ddy = g.y_cell[ie - 1] - g.y_face[j - 1];
-                double rl = sqrt(ddx * ddx + ddy * ddy);
-                tmp[2 * l + 6] = (tmp[2 * l + 2] - unk) / rl;
-                tmp[2 * l + 7] = (tmp[2 * l + 3] - vnk) / rl;
-            }
+            double d2udy = 4.0 * (tmp[2] + tmp[0] - 2 * unk) / fl2;
+            double d2vdy = 4.0 * (tmp[3] + tmp[1] - 2 * vnk) / fl2;
+            tmp[8] = (tmp[4] - unk) / rl1;
+            tmp[9] = (tmp[5] - vnk) / rl1;
+            tmp[10] = (tmp[6] - unk) / rl2;
+            tmp[11] = (tmp[7] - vnk) / rl2;
             double d2udx = 2.0 * (tmp[8] + tmp[10]) / dj;
             double d2vdx = 2.0 * (tmp[9] + tmp[11]) / dj;
             G1 = G1 + dzk * dt * hdiff * (d2udx + d2udy);
             G2 = G2 + dzk * dt * hdiff * (d2vdx + d2vdy);
         }
         // :350-397 barotropic gradients at (1-theta)
-        double rtemp2 = 0.0;
-        if (btype == 0) {
-            double rtemp0 = gravity * dt / dj * (1.0 - theta) * (eta2 - eta1);
-            double rtemp1 = rtemp0 * ct2;
-            rtemp2 = rtemp0 * sn2;
-            G1 = G1 - dzk * rtemp1;
-        } else if (btype > 0) {
-            int ie = g.ob_element_flag[a1 - 1];
-            double rtemp1 = gravity * dt / dj * (1.0 - theta) * (f.eta_at_ob_old[ie - 1] - eta1);
-            G1 = G1 - dzk * rtemp1;
-        } else {
-            G1 = 0.0;
-        }
-        if (wet_nodes) {
-            double rtemp0 = gravity * dt / fl * (1.0 - theta) * (eta_n2 - eta_n1);
-            if (btype == 0) G2 = G2 - dzk * (rtemp0 + rtemp2);
-            else G2 = G2 - dzk * rtemp0;
-        }
+        if (btype >= 0) G1 = G1 - dzk * bt_rtemp1;
+        else G1 = 0.0;
+        if (wet_nodes) G2 = G2 - dzk * along;
         // :400-471 baroclinic pressure gradient
         if (p.baroclinic_flag == 1) {
             double sum1 = 0.0, sum2 = 0.0;
@@ -636,19 +666,18 @@ __global__ void __launch_bounds__(128) k_momentum(Geom g, State s, Forcing f, Pa
                 double dz2 = s.dz_face[ix(k2, j, L)];
                 if (a2 != 0 && k2 >= ba1 && k2 <= ta1 && k2 >= ba2 && k2 <= ta2) {
                     double dr = s.rho_cell[ix(k2, a2, L)] - s.rho_cell[ix(k2, a1, L)];
-                    sum1 = sum1 + (k2 == kk ? 0.5 * dr : 1.0 * dr) * dz2;
+                    sum1 = sum1 + (k2 == kk ? 0.5 * dr : dr) * dz2;
                 }
                 if (k2 >= bn1 && k2 <= tn1 && k2 >= bn2 && k2 <= tn2) {
                     double dr = s.rho_node[ix(k2, node2, L)] - s.rho_node[ix(k2, node1, L)];
-                    sum2 = sum2 + (k2 == kk ? 0.5 * dr : 1.0 * dr) * dz2;
+                    sum2 = sum2 + (k2 == kk ? 0.5 * dr : dr) * dz2;
                 }
             }
             double dzrow = s.dz_face[ix(k, j, L)];   // the reference uses the top-down row here
-            double rtemp1 = dzrow * (-gravity * dt / (p.rho_o * dj)) * sum1;
-            rtemp2 = dzrow * (-gravity * dt / (p.rho_o * fl)) * sum2;
+            double rtemp1 = dzrow * bc_dj * sum1;
+            double rtemp2 = dzrow * bc_fl * sum2;
             double rtemp3 = rtemp1 * ct2;
             double rtemp4 = rtemp1 * sn2;
-            const double spin = f.scal[2];
             G1 = G1 + rtemp3 * spin;
             G2 = G2 + (rtemp2 + rtemp4) * spin;
         }
@@ -659,8 +688,8 @@ __global__ void __launch_bounds__(128) k_momentum(Geom g, State s, Forcing f, Pa
         G1 = G1 + c069 * dzk * gravity * dt * 0.0;
         G2 = G2 + c069 * dzk * gravity * dt * 0.0;
         // :490-509 air pressure
-        G1 = G1 + dzk * (rt0_air * ct2);
-        G2 = G2 + dzk * (rtemp3_air + rt0_air * sn2);
+        G1 = G1 + dzk * air1;
+        G2 = G2 + dzk * air2;
         if (btype == -1) G1 = 0.0;
         if (ibnd > 0) G1 = G1 + dzk * s.qu_boundary[ibnd - 1];
         rhs[k - 1][0] = G1;

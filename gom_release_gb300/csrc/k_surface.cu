@@ -423,46 +423,54 @@ cudaError_t launch_layers(const Launch &x) {
 }
 
 // ============================================================================================
-// calculate_velocity_at_node.f90:31-60: face-level velocities, one thread per face column
-__global__ void k_face_level(Geom g, State s) {
+// calculate_velocity_at_node.f90:31-60: face-level velocities, one thread per face column.  The
+// node loop divides each face level by the face length; that quotient is formed once here.
+__global__ void k_face_level(Geom g, State s, Work w) {
     int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
     if (j > g.NF) return;
     const int L = g.L;
     int t = s.top_face[j - 1];
     if (t == 0) return;
     int b = g.bottom_face[j - 1];
-    double ct = g.cos_theta[j - 1], sn = g.sin_theta[j - 1];
+    double ct = g.cos_theta[j - 1], sn = g.sin_theta[j - 1], fl = g.face_length[j - 1];
     double uk = 0, vk = 0;
     {
         double un = s.un_face_new[ix(b, j, L)], vn = s.vn_face_new[ix(b, j, L)];
         uk = un * ct - vn * sn;
         vk = un * sn + vn * ct;
     }
-    s.u_face_level[ix0(b - 1, j, L)] = uk;
-    s.v_face_level[ix0(b - 1, j, L)] = vk;
+    long o = ix0(b - 1, j, L);
+    s.u_face_level[o] = uk;
+    s.v_face_level[o] = vk;
+    w.uflf[o] = uk / fl;
+    w.vflf[o] = vk / fl;
     for (int k = b; k <= t - 1; ++k) {
         double un = s.un_face_new[ix(k + 1, j, L)], vn = s.vn_face_new[ix(k + 1, j, L)];
         double u1 = un * ct - vn * sn;
         double v1 = un * sn + vn * ct;
         double fac = s.dz_face[ix(k, j, L)] * 0.5 / s.dzhalf_face[ix0(k, j, L)];
-        s.u_face_level[ix0(k, j, L)] = uk + fac * (u1 - uk);
-        s.v_face_level[ix0(k, j, L)] = vk + fac * (v1 - vk);
+        double ul = uk + fac * (u1 - uk), vl = vk + fac * (v1 - vk);
+        o = ix0(k, j, L);
+        s.u_face_level[o] = ul;
+        s.v_face_level[o] = vl;
+        w.uflf[o] = ul / fl;
+        w.vflf[o] = vl / fl;
         uk = u1;
         vk = v1;
     }
-    s.u_face_level[ix0(t, j, L)] = uk;
-    s.v_face_level[ix0(t, j, L)] = vk;
+    o = ix0(t, j, L);
+    s.u_face_level[o] = uk;
+    s.v_face_level[o] = vk;
+    w.uflf[o] = uk / fl;
+    w.vflf[o] = vk / fl;
 }
 
-// :67-138 node u, v (face-length weighted face levels) and w (area-weighted cell w):
-// one thread per (node, level)
-__global__ void k_node_uvw(Geom g, State s) {
-    long tt = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    const int L = g.L;
-    if (tt >= (long)g.NN * (L + 1)) return;
-    int i = (int)(tt / (L + 1)) + 1, k = (int)(tt % (L + 1));
-    double u = 0.0, v = 0.0, weight = 0.0;
-    int icount = 0;
+// :103 the weight sums factor_weight/face_length over the node's faces whatever their wetness:
+// a static per-node value, accumulated once in the reference's order
+__global__ void k_node_weight(Geom g, double *node_weight) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (i > g.NN) return;
+    double weight = 0.0;
     int na = g.adj_cells_at_node[i - 1];
     for (int j = 1; j <= na; ++j) {
         int isn = g.node_cell(j, i), nc = g.node_count(j, i);
@@ -470,18 +478,44 @@ __global__ void k_node_uvw(Geom g, State s) {
         for (int l = tq - 2; l <= tq - 1; ++l) {
             int ifn = g.cell_face(start_end_node(tq, nc, l), isn);
             double fw = g.face_cell(2, ifn) == 0 ? 2.0 : 1.0;
-            double fl = g.face_length[ifn - 1];
+            weight = weight + fw / g.face_length[ifn - 1];
+        }
+    }
+    node_weight[i - 1] = weight;
+}
+
+cudaError_t launch_node_weights(const Launch &x) {
+    k_node_weight<<<blocks_for(x.g.NN, 256), 256, 0, x.stream>>>(x.g, x.w.node_weight);
+    return cudaGetLastError();
+}
+
+// :67-138 node u, v (face-length weighted face levels) and w (area-weighted cell w):
+// one thread per (node, level)
+__global__ void k_node_uvw(Geom g, State s, Work wk) {
+    long tt = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int L = g.L;
+    if (tt >= (long)g.NN * (L + 1)) return;
+    int i = (int)(tt / (L + 1)) + 1, k = (int)(tt % (L + 1));
+    double u = 0.0, v = 0.0;
+    int icount = 0;
+    int na = g.adj_cells_at_node[i - 1];
+    for (int j = 1; j <= na; ++j) {
+        int isn = g.node_cell(j, i), nc = g.node_count(j, i);
+        int tq = g.tri_or_quad[isn - 1];
+        for (int l = tq - 2; l <= tq - 1; ++l) {
+            int ifn = g.cell_face(start_end_node(tq, nc, l), isn);
             int tf = s.top_face[ifn - 1];
             if (tf != 0 && k >= g.bottom_face[ifn - 1] - 1) {
-                int kvt = min(k, tf);
-                u = u + s.u_face_level[ix0(kvt, ifn, L)] / fl * fw;
-                v = v + s.v_face_level[ix0(kvt, ifn, L)] / fl * fw;
+                double fw = g.face_cell(2, ifn) == 0 ? 2.0 : 1.0;
+                long o = ix0(min(k, tf), ifn, L);
+                u = u + wk.uflf[o] * fw;
+                v = v + wk.vflf[o] * fw;
                 icount = icount + 1;
             }
-            weight = weight + fw / fl;
         }
     }
     if (icount != 0) {
+        double weight = wk.node_weight[i - 1];
         u = u / weight;
         v = v / weight;
     }
@@ -504,9 +538,9 @@ __global__ void k_node_uvw(Geom g, State s) {
 }
 
 cudaError_t launch_node_velocity(const Launch &x) {
-    k_face_level<<<blocks_for(x.g.NF, 128), 128, 0, x.stream>>>(x.g, x.s);
+    k_face_level<<<blocks_for(x.g.NF, 128), 128, 0, x.stream>>>(x.g, x.s, x.w);
     long n = (long)x.g.NN * (x.g.L + 1);
-    k_node_uvw<<<blocks_for(n, 256), 256, 0, x.stream>>>(x.g, x.s);
+    k_node_uvw<<<blocks_for(n, 256), 256, 0, x.stream>>>(x.g, x.s, x.w);
     return cudaGetLastError();
 }
 

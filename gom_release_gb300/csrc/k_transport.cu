@@ -17,6 +17,23 @@ __device__ __forceinline__ long ic(int k, int i, int t, int L, int NC) {
     return ((long)t * NC + (i - 1)) * (L + 2) + k;
 }
 
+// exact shortcuts (identical IEEE results, fewer FP64 instructions):
+//   q * sign with sign = +-1            -> sign flip
+//   |0.5*(q + |q|)|, |0.5*(q - |q|)|    -> positive / negative part selected with integer tests
+//   x / Nt with Nt a power of two       -> x * (1/Nt)
+__device__ __forceinline__ bool is_pos(double q) { return __double_as_longlong(q) > 0; }
+__device__ __forceinline__ bool is_neg(double q) {
+    long long b = __double_as_longlong(q);
+    return b < 0 && b != (long long)0x8000000000000000ull;
+}
+__device__ __forceinline__ double pos_part(double q) { return is_pos(q) ? q : 0.0; }
+__device__ __forceinline__ double neg_part(double q) { return is_neg(q) ? -q : 0.0; }
+__device__ __forceinline__ double flip(double q, int sgn) { return sgn > 0 ? q : -q; }
+__device__ __forceinline__ bool same_bits(double a, double b) { return __double_as_longlong(a) == __double_as_longlong(b); }
+
+struct TArgs;
+__device__ __forceinline__ double divnt(double x, const TArgs &a);
+
 struct TArgs {
     Geom g;
     State s;
@@ -28,9 +45,14 @@ struct TArgs {
     int tid[2];       // tran_id of each slot: 1 salinity, 2 temperature
     int Nt, sub;      // subcycles, current subcycle
     double dt2;
+    double inv_nt;    // 1/Nt, used only when Nt is a power of two (exact)
+    bool pow2;
+    bool changed_only;  // coefficient kernels: refresh only entries whose thickness changes
     const double *con;  // current concentrations
     double *con_new;    // next concentrations (full columns, zero outside the wet range)
 };
+
+__device__ __forceinline__ double divnt(double x, const TArgs &a) { return a.pow2 ? x * a.inv_nt : x / a.Nt; }
 
 // :88-173 load tracers into con (0:L+1) with the heat_option 2 surface term
 __global__ void k_tr_load(TArgs a) {
@@ -69,16 +91,16 @@ __global__ void k_tr_bc(TArgs a) {
         for (int l = 1; l <= tq; ++l) {
             int j2 = g.cell_face(l, i2);
             if (g.boundary_type_of_face[j2 - 1] <= 0) continue;
-            double sg = (double)g.cell_sign(l, i2);
+            int sg = g.cell_sign(l, i2);
             for (int k = b; k <= tl; ++k) {
                 double dzf = a.s.dz_face[ix(k, j2, L)];
-                double dz_old = dzf + (a.s.dz_face_new[ix(k, j2, L)] - dzf) * a.sub / a.Nt;
+                double dz_old = dzf + divnt((a.s.dz_face_new[ix(k, j2, L)] - dzf) * a.sub, a);
                 double q2 = g.face_length[j2 - 1] * dz_old *
-                            ((1.0 - theta) * a.s.un_face[ix(k, j2, L)] * sg + theta * a.s.un_face_new[ix(k, j2, L)] * sg);
+                            (flip((1.0 - theta) * a.s.un_face[ix(k, j2, L)], sg) + flip(theta * a.s.un_face_new[ix(k, j2, L)], sg));
                 for (int tr = 0; tr < a.ntr; ++tr) {
                     double bc = a.f.con_at_ob[((long)a.sub * 2 + (a.tid[tr] - 1)) * g.NOB + (i - 1)];
                     a.w.obk[((long)tr * g.NOB + i - 1) * L + k - 1] =
-                        q2 <= 0.0 ? bc : a.con[ic(k, i2, tr, L, g.NC)];
+                        !is_pos(q2) ? bc : a.con[ic(k, i2, tr, L, g.NC)];
                 }
             }
         }
@@ -103,10 +125,13 @@ __global__ void k_tr_face_coef(TArgs a) {
     if (t >= (long)g.NF * L) return;
     int j = (int)(t / L) + 1, k = (int)(t % L) + 1;
     int b = g.bottom_face[j - 1], tf = a.s.top_face[j - 1];
+    bool in = k >= b && k <= tf;
+    // later subcycles: entries whose thickness does not change keep the first subcycle's values
+    if (a.changed_only && (!in || same_bits(a.s.dz_face[t], a.s.dz_face_new[t]))) return;
     double Q = 0.0, D = 0.0, d = 0.0, phi = 0.0;
-    if (k >= b && k <= tf) {
+    if (in) {
         double dzf = a.s.dz_face[t];
-        double dz_old = dzf + (a.s.dz_face_new[t] - dzf) * a.sub / a.Nt;
+        double dz_old = dzf + divnt((a.s.dz_face_new[t] - dzf) * a.sub, a);
         double fl = g.face_length[j - 1];
         Q = fl * dz_old * ((1.0 - a.p.theta) * a.s.un_face[t] + a.p.theta * a.s.un_face_new[t]);
         D = fl * dz_old * a.s.kh[t] / g.delta_j[j - 1];
@@ -126,12 +151,14 @@ __global__ void k_tr_cell_coef(TArgs a) {
     if (t >= (long)g.NC * (L + 1)) return;
     int i = (int)(t / (L + 1)) + 1, k = (int)(t % (L + 1));
     int b = g.bottom_cell[i - 1], tl = a.s.top_cell[i - 1];
+    bool in = k >= b && k <= tl - 1;
+    if (a.changed_only && (!in || same_bits(a.s.dzhalf_cell[t], a.s.dzhalf_cell_new[t]))) return;
     double Q = 0.0, d = 0.0, phi = 0.0;
-    if (k >= b && k <= tl - 1) {
+    if (in) {
         double ar = g.area[i - 1];
         Q = ar * ((1.0 - a.p.theta) * a.s.wn_cell[t] + a.p.theta * a.s.wn_cell_new[t]);
         double dzh = a.s.dzhalf_cell[t];
-        double dz_old = dzh + (a.s.dzhalf_cell_new[t] - dzh) * a.sub / a.Nt;
+        double dz_old = dzh + divnt((a.s.dzhalf_cell_new[t] - dzh) * a.sub, a);
         double D = ar * a.s.kv[t] / dz_old;
         d = fmax(0.0, D - 0.5 * fabs(Q));
         phi = Q == 0.0 ? 1.0 : fmin(1.0, 2.0 * D / fabs(Q));
@@ -175,13 +202,12 @@ __global__ void k_tr_limiter_cells(TArgs a) {
     if (tl == 0) return;
     int nvl = tl - b + 1;
     int tq = g.tri_or_quad[i - 1];
-    int fj[4], nb[4];
-    double sg[4];
+    int fj[4], nb[4], sg[4];
     bool open[4];
     for (int l = 1; l <= tq; ++l) {
         fj[l - 1] = g.cell_face(l, i);
         nb[l - 1] = g.cell_adj(l, i);
-        sg[l - 1] = (double)g.cell_sign(l, i);
+        sg[l - 1] = g.cell_sign(l, i);
         open[l - 1] = face_open(g, fj[l - 1]);
     }
     double last1[2] = {0.0, 0.0}, last2[2] = {0.0, 0.0};
@@ -191,19 +217,16 @@ __global__ void k_tr_limiter_cells(TArgs a) {
             double ck = a.con[ic(k, i, tr, L, NC)];
             if (nvl != 1) {
                 if (k == b) {
-                    double q = a.w.qi[ix0(k, i, L)];
-                    double rt2 = fabs(0.5 * (q + fabs(q)));
+                    double rt2 = pos_part(a.w.qi[ix0(k, i, L)]);
                     s1a[tr] = rt2 * (ck - a.con[ic(k + 1, i, tr, L, NC)]);
                     s2a[tr] = rt2;
                 } else if (k == tl) {
-                    double q = a.w.qi[ix0(k - 1, i, L)];
-                    double rt1 = fabs(0.5 * (q + fabs(q)));
+                    double rt1 = pos_part(a.w.qi[ix0(k - 1, i, L)]);
                     s1a[tr] = rt1 * (ck - a.con[ic(k - 1, i, tr, L, NC)]);
                     s2a[tr] = rt1;
                 } else {
-                    double qm = a.w.qi[ix0(k - 1, i, L)], q = a.w.qi[ix0(k, i, L)];
-                    double rt1 = fabs(0.5 * (qm + fabs(qm)));
-                    double rt2 = fabs(0.5 * (q + fabs(q)));
+                    double rt1 = pos_part(a.w.qi[ix0(k - 1, i, L)]);
+                    double rt2 = pos_part(a.w.qi[ix0(k, i, L)]);
                     s1a[tr] = rt1 * (ck - a.con[ic(k - 1, i, tr, L, NC)]) + rt2 * (ck - a.con[ic(k + 1, i, tr, L, NC)]);
                     s2a[tr] = rt1 + rt2;
                 }
@@ -211,8 +234,8 @@ __global__ void k_tr_limiter_cells(TArgs a) {
         }
         for (int l = 0; l < tq; ++l) {
             if (!open[l]) continue;
-            double q2 = a.w.qj[ix(k, fj[l], L)] * sg[l];
-            if (q2 < 0.0) {
+            double q2 = flip(a.w.qj[ix(k, fj[l], L)], sg[l]);
+            if (is_neg(q2)) {
                 for (int tr = 0; tr < a.ntr; ++tr) {
                     double cik = nb[l] > 0 ? a.con[ic(k, nb[l], tr, L, NC)] : oqb_value(a, i, k, tr);
                     s1[tr] = s1[tr] + fabs(q2) * (a.con[ic(k, i, tr, L, NC)] - cik);
@@ -260,11 +283,11 @@ __global__ void k_tr_limiter_faces(TArgs a) {
         // a cell writes when it is wet, holds layer k and sees Q*sign >= 0; cell 2 comes later
         if (c2 != 0) {
             int t2 = a.s.top_cell[c2 - 1];
-            if (t2 != 0 && k >= g.bottom_cell[c2 - 1] && k <= t2 && Q * (double)(-1) >= 0.0) writer = c2;
+            if (t2 != 0 && k >= g.bottom_cell[c2 - 1] && k <= t2 && !is_pos(Q)) writer = c2;   // -Q >= 0
         }
         if (writer == 0) {
             int t1 = a.s.top_cell[c1 - 1];
-            if (t1 != 0 && k >= g.bottom_cell[c1 - 1] && k <= t1 && Q >= 0.0) writer = c1;
+            if (t1 != 0 && k >= g.bottom_cell[c1 - 1] && k <= t1 && !is_neg(Q)) writer = c1;   // Q >= 0
         }
     }
     for (int tr = 0; tr < a.ntr; ++tr) {
@@ -305,12 +328,12 @@ __global__ void __launch_bounds__(128) k_tr_solve(TArgs a) {
         am[kk - 1] = -dt2 * a.w.di[ix0(k, i, L)];
         cm[kk - 1] = -dt2 * a.w.di[ix0(k - 1, i, L)];
         double dzc = a.s.dz_cell[ix(k, i, L)];
-        double dz_new = dzc + (a.s.dz_cell_new[ix(k, i, L)] - dzc) * (sub + 1) / Nt;
+        double dz_new = dzc + divnt((a.s.dz_cell_new[ix(k, i, L)] - dzc) * (sub + 1), a);
         bm[kk - 1] = -am[kk - 1] + ar * dz_new - cm[kk - 1];
     }
     {
         double dzc = a.s.dz_cell[ix(tl, i, L)];
-        double dz_new = dzc + (a.s.dz_cell_new[ix(tl, i, L)] - dzc) * (sub + 1) / Nt;
+        double dz_new = dzc + divnt((a.s.dz_cell_new[ix(tl, i, L)] - dzc) * (sub + 1), a);
         if (tl == b) {
             bm[0] = ar * dz_new;
         } else {
@@ -318,18 +341,17 @@ __global__ void __launch_bounds__(128) k_tr_solve(TArgs a) {
             bm[0] = ar * dz_new - cm[0];
             am[nvl - 1] = -dt2 * a.w.di[ix0(b, i, L)];
             double dzb = a.s.dz_cell[ix(b, i, L)];
-            double dz_newb = dzb + (a.s.dz_cell_new[ix(b, i, L)] - dzb) * (sub + 1) / Nt;
+            double dz_newb = dzb + divnt((a.s.dz_cell_new[ix(b, i, L)] - dzb) * (sub + 1), a);
             bm[nvl - 1] = -am[nvl - 1] + ar * dz_newb;
         }
     }
     int tq = g.tri_or_quad[i - 1];
-    int fj[4], nb[4], fb[4], ft[4];
-    double sg[4];
+    int fj[4], nb[4], fb[4], ft[4], sg[4];
     bool open[4];
     for (int l = 1; l <= tq; ++l) {
         fj[l - 1] = g.cell_face(l, i);
         nb[l - 1] = g.cell_adj(l, i);
-        sg[l - 1] = (double)g.cell_sign(l, i);
+        sg[l - 1] = g.cell_sign(l, i);
         open[l - 1] = face_open(g, fj[l - 1]);
         fb[l - 1] = g.bottom_face[fj[l - 1] - 1];
         ft[l - 1] = a.s.top_face[fj[l - 1] - 1];
@@ -343,19 +365,20 @@ __global__ void __launch_bounds__(128) k_tr_solve(TArgs a) {
             if (!open[l]) continue;
             bool in_face = k >= fb[l] && k <= ft[l];
             long fo = ix(k, fj[l], L);
-            double q2 = in_face ? a.w.qj[fo] * sg[l] : 0.0 * sg[l];
+            double q2 = flip(in_face ? a.w.qj[fo] : 0.0, sg[l]);
             double dface = in_face ? a.w.dj[fo] : 0.0;
+            bool qpos = is_pos(q2), qneg = is_neg(q2);
             for (int tr = 0; tr < a.ntr; ++tr) {
                 double cik = nb[l] > 0 ? a.con[ic(k, nb[l], tr, L, NC)] : oqb_value(a, i, k, tr);
-                if (q2 > 0.0) sQi[tr] = sQi[tr] + fabs(q2) * ck[tr];
-                else if (q2 < 0.0) sQii[tr] = sQii[tr] + fabs(q2) * cik;
+                if (qpos) sQi[tr] = sQi[tr] + fabs(q2) * ck[tr];
+                else if (qneg) sQii[tr] = sQii[tr] + fabs(q2) * cik;
                 shd[tr] = shd[tr] + dface * (cik - ck[tr]);
                 double psi = (lim && in_face) ? a.w.psij[(long)tr * g.NF * L + fo] : 0.0;
                 shl[tr] = shl[tr] + psi * fabs(q2) * (ck[tr] - cik);
             }
         }
         double dzc = a.s.dz_cell[ix(k, i, L)];
-        double dz_old = dzc + (a.s.dz_cell_new[ix(k, i, L)] - dzc) * sub / Nt;
+        double dz_old = dzc + divnt((a.s.dz_cell_new[ix(k, i, L)] - dzc) * sub, a);
         for (int tr = 0; tr < a.ntr; ++tr) {
             double h_adv = dt2 * (sQii[tr] - sQi[tr]);
             double h_diff = dt2 * shd[tr];
@@ -374,7 +397,7 @@ __global__ void __launch_bounds__(128) k_tr_solve(TArgs a) {
                 double v = rhs[kk - 1][tr];
                 if (k == b) {
                     double q = a.w.qi[ix0(k, i, L)];
-                    double qp = fabs(0.5 * (q + fabs(q))), qm = fabs(0.5 * (q - fabs(q)));
+                    double qp = pos_part(q), qm = neg_part(q);
                     double cp1 = a.con[ic(k + 1, i, tr, L, NC)];
                     v = v + dt2 * (-qp * c0 + qm * cp1);
                     if (a.p.v_flux_limiter > 0) {
@@ -383,7 +406,7 @@ __global__ void __launch_bounds__(128) k_tr_solve(TArgs a) {
                     }
                 } else if (k == tl) {
                     double q = a.w.qi[ix0(k - 1, i, L)];
-                    double qp = fabs(0.5 * (q + fabs(q))), qm = fabs(0.5 * (q - fabs(q)));
+                    double qp = pos_part(q), qm = neg_part(q);
                     double cm1 = a.con[ic(k - 1, i, tr, L, NC)];
                     v = v + dt2 * (qp * cm1 - qm * c0);
                     if (a.p.v_flux_limiter > 0) {
@@ -392,8 +415,8 @@ __global__ void __launch_bounds__(128) k_tr_solve(TArgs a) {
                     }
                 } else {
                     double q1 = a.w.qi[ix0(k - 1, i, L)], q = a.w.qi[ix0(k, i, L)];
-                    double qp1 = fabs(0.5 * (q1 + fabs(q1))), qm1 = fabs(0.5 * (q1 - fabs(q1)));
-                    double qp = fabs(0.5 * (q + fabs(q))), qm = fabs(0.5 * (q - fabs(q)));
+                    double qp1 = pos_part(q1), qm1 = neg_part(q1);
+                    double qp = pos_part(q), qm = neg_part(q);
                     double cm1 = a.con[ic(k - 1, i, tr, L, NC)], cp1 = a.con[ic(k + 1, i, tr, L, NC)];
                     v = v + dt2 * (qp1 * cm1 - qp * c0 + qm * cp1 - qm1 * c0);
                     if (a.p.v_flux_limiter > 0) {
@@ -512,6 +535,9 @@ cudaError_t launch_transport(const Launch &x) {
     if (a.ntr == 0) return cudaSuccess;
     a.Nt = p.trans_sub_iter == 0 ? 1 : p.trans_sub_iter;
     a.dt2 = p.dt / a.Nt;
+    a.pow2 = (a.Nt & (a.Nt - 1)) == 0;
+    a.inv_nt = 1.0 / a.Nt;
+    a.changed_only = false;
     const Geom &g = x.g;
     const int L = g.L;
     a.con = x.w.con;
@@ -524,6 +550,7 @@ cudaError_t launch_transport(const Launch &x) {
         a.con = cur;
         a.con_new = nxt;
         if (g.NOB + g.NQB > 0) k_tr_bc<<<blocks_for(g.NOB + g.NQB, 128), 128, 0, x.stream>>>(a);
+        a.changed_only = sub > 0;
         k_tr_face_coef<<<blocks_for((long)g.NF * L, 256), 256, 0, x.stream>>>(a);
         k_tr_cell_coef<<<blocks_for((long)g.NC * (L + 1), 256), 256, 0, x.stream>>>(a);
         if (lim) {
