@@ -115,7 +115,7 @@ def kernel_launches_per_step(deck) -> int:
     p = deck.params
     n = 1                                   # bottom friction
     n += 1 if deck.n_qb else 0              # river boundary velocity
-    n += (2 if p.elm_backtrace_flag == 1 else 1) if p.advection_flag else 1
+    n += (3 if p.elm_backtrace_flag == 1 else 1) if p.advection_flag else 1
     n += 2                                  # momentum (dry-face clear + columns)
     n += 4                                  # assembly, PCG, node eta (wet, dry)
     n += 2                                  # face velocities, cell w

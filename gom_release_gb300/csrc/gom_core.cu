@@ -389,6 +389,7 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
     if (e == cudaSuccess) e = dalloc(c, &W.sa2, L * NC * 2);
     if (e == cudaSuccess) e = dalloc(c, &W.obk, L * (size_t)d.n_ob * 2);
     if (e == cudaSuccess) e = dalloc(c, &W.qbk, L * (size_t)d.n_qb * 2);
+    if (e == cudaSuccess) e = dalloc(c, &W.idev, L * NF);
     if (e == cudaSuccess) e = dalloc(c, &W.uflf, (L + 1) * NF);
     if (e == cudaSuccess) e = dalloc(c, &W.vflf, (L + 1) * NF);
     if (e == cudaSuccess) e = dalloc(c, &W.node_weight, NN);

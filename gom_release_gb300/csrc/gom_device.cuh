@@ -154,6 +154,16 @@ __device__ inline bool thomas(int n, const double *a, const double *b, const dou
     return true;
 }
 
+// -------------------------------------------------------------------- flat thread indices
+// Flat (entity, layer) thread indices stay in 32 bits: a 64-bit integer division is emulated
+// partly on the FP64 pipe, the scarcest unit of this GPU, while the 32-bit one is not.
+__device__ __forceinline__ unsigned flat_tid() { return blockIdx.x * blockDim.x + threadIdx.x; }
+__device__ __forceinline__ void split_index(unsigned t, unsigned n, int &e0, int &k0) {
+    unsigned q = t / n;
+    e0 = (int)q;
+    k0 = (int)(t - q * n);
+}
+
 // -------------------------------------------------------------------- launch helpers
 inline int blocks_for(long n, int threads) { return (int)((n + threads - 1) / threads); }
 

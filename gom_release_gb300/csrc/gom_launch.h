@@ -24,6 +24,8 @@ struct Work {
     double *psii = nullptr;                                     // (0:L, NC, 2)
     double *sa1 = nullptr, *sa2 = nullptr;                      // (L, NC, 2) limiter sums per layer
     double *obk = nullptr, *qbk = nullptr;                      // (L, NOB, 2), (L, NQB, 2)
+    // ELM: INT(dev/0.1) per (layer, face) edge
+    int *idev = nullptr;
     // node velocities: face-level velocity / face length (0:L, NF), static node weights (NN)
     double *uflf = nullptr, *vflf = nullptr, *node_weight = nullptr;
     // conservation

@@ -358,22 +358,53 @@ __device__ int elm_backtrace(const Geom &g, const State &s, const Params &p, int
     return 0;
 }
 
-// solve_nonlinear_advection.f90:52-87: one thread per (node, layer).
-// INT(dev/0.1) and INT(2*w*dt/delta_z_min) are 0 whenever the operands are more than 1e-9 below
-// the thresholds; that case (the usual one) is decided from squared quantities without square
-// roots or divisions, and every other case is computed exactly as the reference does.
-__global__ void k_elm_substeps(Geom g, State s, Params p) {
-    long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+// solve_nonlinear_advection.f90:52-87.  The reference evaluates, for every node, layer and
+// adjacent cell, INT(dev/0.1) of the two cell edges meeting at the node; dev depends only on the
+// edge (it is symmetric in its two nodes), so k_elm_edge_dev evaluates it once per edge (= face)
+// and layer, and k_elm_substeps combines the edges of each node.  INT(dev/0.1) and
+// INT(2*w*dt/delta_z_min) are 0 whenever the operands lie more than 1e-9 below the thresholds;
+// that usual case is decided from squared quantities without square roots or divisions, every
+// other case is computed exactly as the reference does.
+__global__ void k_elm_edge_dev(Geom g, State s, Params p, int *idev) {
+    unsigned t = flat_tid();
     const int L = g.L;
-    if (t >= (long)g.NN * L) return;
-    int i = (int)(t / L) + 1, k = (int)(t % L) + 1;
+    if (t >= (unsigned)g.NF * L) return;
+    int j, k;
+    split_index(t, L, j, k);
+    j += 1;
+    k += 1;
     const double dt = p.dt;
     const double c01 = F(1.e-1f);
     const double kthr = c01 * c01 / (dt * dt) * (1.0 - 1e-9);
+    int n1 = g.face_node(1, j), n2 = g.face_node(2, j);
+    double dx = g.x_node[n1 - 1] - g.x_node[n2 - 1], dy = g.y_node[n1 - 1] - g.y_node[n2 - 1];
+    double rl2 = dx * dx + dy * dy;
+    double u1 = (s.u_node[ix0(k, n1, L)] + s.u_node[ix0(k - 1, n1, L)]) * 0.5;
+    double v1 = (s.v_node[ix0(k, n1, L)] + s.v_node[ix0(k - 1, n1, L)]) * 0.5;
+    double u2 = (s.u_node[ix0(k, n2, L)] + s.u_node[ix0(k - 1, n2, L)]) * 0.5;
+    double v2 = (s.v_node[ix0(k, n2, L)] + s.v_node[ix0(k - 1, n2, L)]) * 0.5;
+    double du = u1 - u2, dv = v1 - v2;
+    double sq = du * du + dv * dv;
+    int id = 0;
+    if (!(sq < rl2 * kthr)) {
+        double dev = sqrt(sq) / sqrt(rl2) * dt;
+        id = (int)(dev / c01);
+    }
+    idev[t] = id;
+}
+
+__device__ __forceinline__ int wrap_edge(int l, int tq) { return l <= 0 ? l + tq : l; }
+
+__global__ void k_elm_substeps(Geom g, State s, Params p, const int *idev) {
+    unsigned t = flat_tid();
+    const int L = g.L;
+    if (t >= (unsigned)g.NN * L) return;
+    int i, k;
+    split_index(t, L, i, k);
+    i += 1;
+    k += 1;
+    const double dt = p.dt;
     int nadj = g.adj_cells_at_node[i - 1];
-    double xi = g.x_node[i - 1], yi = g.y_node[i - 1];
-    double ui = (s.u_node[ix0(k, i, L)] + s.u_node[ix0(k - 1, i, L)]) * 0.5;
-    double vi = (s.v_node[ix0(k, i, L)] + s.v_node[ix0(k - 1, i, L)]) * 0.5;
     double wi = (s.w_node[ix0(k, i, L)] + s.w_node[ix0(k - 1, i, L)]) * 0.5;
     double aw = 2 * wi * dt;
     int iw = fabs(aw) < p.delta_z_min * (1.0 - 1e-9) ? 0 : (int)(aw / p.delta_z_min);
@@ -381,59 +412,24 @@ __global__ void k_elm_substeps(Geom g, State s, Params p) {
     for (int j = 1; j <= nadj; ++j) {
         int ie = g.node_cell(j, i), id = g.node_count(j, i);
         int tq = g.tri_or_quad[ie - 1];
-        int imax = 0;
-        for (int l = 1; l <= 2; ++l) {
-            int nd = g.cell_node(l == 1 ? start_end_node(tq, id, 1) : start_end_node(tq, id, tq - 1), ie);
-            double dx = xi - g.x_node[nd - 1], dy = yi - g.y_node[nd - 1];
-            double rl2 = dx * dx + dy * dy;
-            double u2 = (s.u_node[ix0(k, nd, L)] + s.u_node[ix0(k - 1, nd, L)]) * 0.5;
-            double v2 = (s.v_node[ix0(k, nd, L)] + s.v_node[ix0(k - 1, nd, L)]) * 0.5;
-            double du = ui - u2, dv = vi - v2;
-            double sq = du * du + dv * dv;
-            if (sq < rl2 * kthr) continue;   // dev/0.1 < 1: contributes INT 0
-            double dev = sqrt(sq) / sqrt(rl2) * dt;
-            int id_l = (int)(dev / c01);
-            if (id_l > imax) imax = id_l;
-        }
+        // edges (id, id+1) and (id-1, id) of cell ie: local faces id-1 and id-2
+        int fa = g.cell_face(wrap_edge(id - 1, tq), ie);
+        int fb = g.cell_face(wrap_edge(id - 2, tq), ie);
+        int imax = max(idev[ix(k, fa, L)], idev[ix(k, fb, L)]);
         int idelta = max(imax, iw);
-        summ = summ + (double)idelta / nadj;
+        if (idelta != 0) summ = summ + (double)idelta / nadj;   // 0/nadj adds exactly 0
     }
     s.num_sub_elm[ix(k, i, L)] = max(p.elm_min_iter, min(p.elm_max_iter, (int)summ));
 }
 
-// solve_nonlinear_advection.f90:94-201: one thread per (face, layer)
-__global__ void k_elm_faces(Geom g, State s, Params p, gom_status *st) {
-    long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+// solve_nonlinear_advection.f90:94-201: one thread per face walks the face's wet layers (a warp's
+// FP64 work is spread over 32 faces instead of idling on dry layers)
+__device__ void elm_face_layer(const Geom &g, const State &s, const Params &p, gom_status *st, int j, int k, int ie0,
+                               int n1, int n2, double ct, double sn) {
     const int L = g.L;
-    if (t >= (long)g.NF * L) return;
-    int j = (int)(t / L) + 1, k = (int)(t % L) + 1;
     long o = ix(k, j, L);
-    int b = g.bottom_face[j - 1], tf = s.top_face[j - 1];
     double unf = s.un_face[o], vnf = s.vn_face[o];
-    s.elm_foot[o] = 0;
-    s.elm_near_edge[o] = 0;
-    if (k < b || k > tf) {
-        s.un_elm[o] = 0.0;
-        s.vn_elm[o] = 0.0;
-        return;
-    }
-    int n1 = g.face_node(1, j), n2 = g.face_node(2, j);
-    if (fabs(fmax(g.h_node[n1 - 1], g.h_node[n2 - 1])) < p.adv_onoff_depth) {
-        s.un_elm[o] = unf;
-        s.vn_elm[o] = vnf;
-        return;
-    }
-    int a1 = g.face_cell(1, j), a2 = g.face_cell(2, j);
-    int ie0;
-    if (s.top_cell[a1 - 1] != 0) ie0 = a1;
-    else if (a2 != 0 && s.top_cell[a2 - 1] != 0) ie0 = a2;
-    else {
-        s.un_elm[o] = unf;
-        s.vn_elm[o] = vnf;
-        return;
-    }
     int nnel = ie0, jlev = k;
-    double ct = g.cos_theta[j - 1], sn = g.sin_theta[j - 1];
     double x0 = g.x_face[j - 1], y0 = g.y_face[j - 1], z0;
     if (k == s.top_cell[nnel - 1]) z0 = p.msl + s.eta_cell[nnel - 1] - s.dz_cell[ix(k, nnel, L)] * 0.5;
     else z0 = g.z_level[k] - s.dz_cell[ix(k, nnel, L)] * 0.5;
@@ -462,10 +458,42 @@ __global__ void k_elm_faces(Geom g, State s, Params p, gom_status *st) {
     s.vn_elm[o] = -uu * sn + vv * ct;
 }
 
+__global__ void k_elm_faces(Geom g, State s, Params p, gom_status *st) {
+    int j = (int)flat_tid() + 1;
+    if (j > g.NF) return;
+    const int L = g.L;
+    int b = g.bottom_face[j - 1], tf = s.top_face[j - 1];
+    for (int k = 1; k <= L; ++k) {
+        long o = ix(k, j, L);
+        s.elm_foot[o] = 0;
+        s.elm_near_edge[o] = 0;
+        if (k < b || k > tf) {
+            s.un_elm[o] = 0.0;
+            s.vn_elm[o] = 0.0;
+        }
+    }
+    if (tf < b) return;
+    int n1 = g.face_node(1, j), n2 = g.face_node(2, j);
+    bool shallow = fabs(fmax(g.h_node[n1 - 1], g.h_node[n2 - 1])) < p.adv_onoff_depth;
+    int a1 = g.face_cell(1, j), a2 = g.face_cell(2, j);
+    int ie0 = 0;
+    if (s.top_cell[a1 - 1] != 0) ie0 = a1;
+    else if (a2 != 0 && s.top_cell[a2 - 1] != 0) ie0 = a2;
+    if (shallow || ie0 == 0) {
+        for (int k = b; k <= tf; ++k) {
+            long o = ix(k, j, L);
+            s.un_elm[o] = s.un_face[o];
+            s.vn_elm[o] = s.vn_face[o];
+        }
+        return;
+    }
+    double ct = g.cos_theta[j - 1], sn = g.sin_theta[j - 1];
+    for (int k = b; k <= tf; ++k) elm_face_layer(g, s, p, st, j, k, ie0, n1, n2, ct, sn);
+}
+
 __global__ void k_copy_elm(Geom g, State s) {
-    long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    long n = (long)g.NF * g.L;
-    if (t >= n) return;
+    unsigned t = flat_tid();
+    if (t >= (unsigned)g.NF * g.L) return;
     s.un_elm[t] = s.un_face[t];
     s.vn_elm[t] = s.vn_face[t];
     s.elm_foot[t] = 0;
@@ -479,10 +507,11 @@ cudaError_t launch_advection(const Launch &x) {
         return cudaGetLastError();
     }
     if (x.p.elm_backtrace_flag == 1) {
+        k_elm_edge_dev<<<blocks_for(nfl, 256), 256, 0, x.stream>>>(x.g, x.s, x.p, x.w.idev);
         long nnl = (long)x.g.NN * x.g.L;
-        k_elm_substeps<<<blocks_for(nnl, 256), 256, 0, x.stream>>>(x.g, x.s, x.p);
+        k_elm_substeps<<<blocks_for(nnl, 256), 256, 0, x.stream>>>(x.g, x.s, x.p, x.w.idev);
     }
-    k_elm_faces<<<blocks_for(nfl, 128), 128, 0, x.stream>>>(x.g, x.s, x.p, x.status);
+    k_elm_faces<<<blocks_for(x.g.NF, 64), 64, 0, x.stream>>>(x.g, x.s, x.p, x.status);
     return cudaGetLastError();
 }
 
@@ -720,10 +749,10 @@ __global__ void __launch_bounds__(128) k_momentum(Geom g, State s, Forcing f, Pa
 
 __global__ void k_zero_face_columns(Geom g, State s) {
     // faces that are dry keep zero results (the reference zeroes all four arrays first)
-    long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned t = flat_tid();
     const int L = g.L;
-    if (t >= (long)g.NF * L) return;
-    int j = (int)(t / L) + 1;
+    if (t >= (unsigned)g.NF * L) return;
+    int j = (int)(t / (unsigned)L) + 1;
     if (s.top_face[j - 1] != 0) return;
     s.ainvg1[t] = 0.0;
     s.ainvg2[t] = 0.0;

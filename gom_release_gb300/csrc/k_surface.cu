@@ -492,10 +492,12 @@ cudaError_t launch_node_weights(const Launch &x) {
 // :67-138 node u, v (face-length weighted face levels) and w (area-weighted cell w):
 // one thread per (node, level)
 __global__ void k_node_uvw(Geom g, State s, Work wk) {
-    long tt = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned tt = flat_tid();
     const int L = g.L;
-    if (tt >= (long)g.NN * (L + 1)) return;
-    int i = (int)(tt / (L + 1)) + 1, k = (int)(tt % (L + 1));
+    if (tt >= (unsigned)g.NN * (L + 1)) return;
+    int i, k;
+    split_index(tt, L + 1, i, k);
+    i += 1;
     double u = 0.0, v = 0.0;
     int icount = 0;
     int na = g.adj_cells_at_node[i - 1];

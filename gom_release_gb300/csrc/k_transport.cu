@@ -56,11 +56,13 @@ __device__ __forceinline__ double divnt(double x, const TArgs &a) { return a.pow
 
 // :88-173 load tracers into con (0:L+1) with the heat_option 2 surface term
 __global__ void k_tr_load(TArgs a) {
-    long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned t = flat_tid();
     const Geom &g = a.g;
     const int L = g.L;
-    if (t >= (long)g.NC * (L + 2)) return;
-    int i = (int)(t / (L + 2)) + 1, k = (int)(t % (L + 2));
+    if (t >= (unsigned)g.NC * (L + 2)) return;
+    int i, k;
+    split_index(t, L + 2, i, k);
+    i += 1;
     for (int tr = 0; tr < a.ntr; ++tr) {
         double v = 0.0;
         if (k >= 1 && k <= L) {
@@ -117,55 +119,82 @@ __global__ void k_tr_bc(TArgs a) {
     }
 }
 
-// :551-581 face coefficients, one thread per (face, layer)
-__global__ void k_tr_face_coef(TArgs a) {
-    long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    const Geom &g = a.g;
-    const int L = g.L;
-    if (t >= (long)g.NF * L) return;
-    int j = (int)(t / L) + 1, k = (int)(t % L) + 1;
-    int b = g.bottom_face[j - 1], tf = a.s.top_face[j - 1];
-    bool in = k >= b && k <= tf;
-    // later subcycles: entries whose thickness does not change keep the first subcycle's values
-    if (a.changed_only && (!in || same_bits(a.s.dz_face[t], a.s.dz_face_new[t]))) return;
-    double Q = 0.0, D = 0.0, d = 0.0, phi = 0.0;
-    if (in) {
-        double dzf = a.s.dz_face[t];
-        double dz_old = dzf + divnt((a.s.dz_face_new[t] - dzf) * a.sub, a);
-        double fl = g.face_length[j - 1];
-        Q = fl * dz_old * ((1.0 - a.p.theta) * a.s.un_face[t] + a.p.theta * a.s.un_face_new[t]);
-        D = fl * dz_old * a.s.kh[t] / g.delta_j[j - 1];
-        d = fmax(0.0, D - 0.5 * fabs(Q));
-        phi = Q == 0.0 ? 1.0 : fmin(1.0, 2.0 * D / fabs(Q));
-    }
+// :551-581 face coefficients.  One thread per face walks its wet layers, so the FP64 work of a
+// warp is spread over 32 wet faces (GB300 issues an FP64 warp instruction at the same cost however
+// few lanes are active).  Later subcycles refresh only layers whose thickness changes.
+__device__ __forceinline__ void face_coef_at(const TArgs &a, int j, int k, long t) {
+    double dzf = a.s.dz_face[t];
+    double dz_old = dzf + divnt((a.s.dz_face_new[t] - dzf) * a.sub, a);
+    double fl = a.g.face_length[j - 1];
+    double Q = fl * dz_old * ((1.0 - a.p.theta) * a.s.un_face[t] + a.p.theta * a.s.un_face_new[t]);
+    double D = fl * dz_old * a.s.kh[t] / a.g.delta_j[j - 1];
+    double d = fmax(0.0, D - 0.5 * fabs(Q));
+    double phi = Q == 0.0 ? 1.0 : fmin(1.0, 2.0 * D / fabs(Q));
     a.w.qj[t] = Q;
     a.w.dj[t] = d;
     a.w.phij[t] = phi;
 }
 
-// :585-610 vertical coefficients, one thread per (cell, interface 0..L)
-__global__ void k_tr_cell_coef(TArgs a) {
-    long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void k_tr_face_coef(TArgs a) {
+    int j = (int)flat_tid() + 1;
     const Geom &g = a.g;
+    if (j > g.NF) return;
     const int L = g.L;
-    if (t >= (long)g.NC * (L + 1)) return;
-    int i = (int)(t / (L + 1)) + 1, k = (int)(t % (L + 1));
-    int b = g.bottom_cell[i - 1], tl = a.s.top_cell[i - 1];
-    bool in = k >= b && k <= tl - 1;
-    if (a.changed_only && (!in || same_bits(a.s.dzhalf_cell[t], a.s.dzhalf_cell_new[t]))) return;
-    double Q = 0.0, d = 0.0, phi = 0.0;
-    if (in) {
-        double ar = g.area[i - 1];
-        Q = ar * ((1.0 - a.p.theta) * a.s.wn_cell[t] + a.p.theta * a.s.wn_cell_new[t]);
-        double dzh = a.s.dzhalf_cell[t];
-        double dz_old = dzh + divnt((a.s.dzhalf_cell_new[t] - dzh) * a.sub, a);
-        double D = ar * a.s.kv[t] / dz_old;
-        d = fmax(0.0, D - 0.5 * fabs(Q));
-        phi = Q == 0.0 ? 1.0 : fmin(1.0, 2.0 * D / fabs(Q));
+    int b = g.bottom_face[j - 1], tf = a.s.top_face[j - 1];
+    if (!a.changed_only) {
+        for (int k = 1; k <= L; ++k) {
+            long t = ix(k, j, L);
+            if (k >= b && k <= tf) {
+                face_coef_at(a, j, k, t);
+            } else {
+                a.w.qj[t] = 0.0;
+                a.w.dj[t] = 0.0;
+                a.w.phij[t] = 0.0;
+            }
+        }
+        return;
     }
+    for (int k = b; k <= tf; ++k) {
+        long t = ix(k, j, L);
+        if (!same_bits(a.s.dz_face[t], a.s.dz_face_new[t])) face_coef_at(a, j, k, t);
+    }
+}
+
+// :585-610 vertical coefficients, one thread per cell column (interfaces b..t-1)
+__device__ __forceinline__ void cell_coef_at(const TArgs &a, int i, long t) {
+    double ar = a.g.area[i - 1];
+    double Q = ar * ((1.0 - a.p.theta) * a.s.wn_cell[t] + a.p.theta * a.s.wn_cell_new[t]);
+    double dzh = a.s.dzhalf_cell[t];
+    double dz_old = dzh + divnt((a.s.dzhalf_cell_new[t] - dzh) * a.sub, a);
+    double D = ar * a.s.kv[t] / dz_old;
     a.w.qi[t] = Q;
-    a.w.di[t] = d;
-    a.w.phii[t] = phi;
+    a.w.di[t] = fmax(0.0, D - 0.5 * fabs(Q));
+    a.w.phii[t] = Q == 0.0 ? 1.0 : fmin(1.0, 2.0 * D / fabs(Q));
+}
+
+__global__ void k_tr_cell_coef(TArgs a) {
+    int i = (int)flat_tid() + 1;
+    const Geom &g = a.g;
+    if (i > g.NC) return;
+    const int L = g.L;
+    int b = g.bottom_cell[i - 1], tl = a.s.top_cell[i - 1];
+    if (!a.changed_only) {
+        for (int k = 0; k <= L; ++k) {
+            long t = ix0(k, i, L);
+            if (k >= b && k <= tl - 1) {
+                cell_coef_at(a, i, t);
+            } else {
+                a.w.qi[t] = 0.0;
+                a.w.di[t] = 0.0;
+                a.w.phii[t] = 0.0;
+            }
+        }
+        return;
+    }
+    for (int k = b; k <= tl - 1; ++k) {
+        long t = ix0(k, i, L);
+        if (!same_bits(a.s.dzhalf_cell[t], a.s.dzhalf_cell_new[t])) cell_coef_at(a, i, t);
+    }
 }
 
 __device__ __forceinline__ bool face_open(const Geom &g, int j) {
@@ -267,39 +296,39 @@ __global__ void k_tr_limiter_cells(TArgs a) {
     }
 }
 
-// :769-799 + :876-900 face ratio r_jk from its upwind cell (the last writer in cell order), PSI_jk
+// :769-799 + :876-900 face ratio r_jk from its upwind cell (the last writer in cell order), PSI_jk;
+// one thread per face walks its wet layers
 __global__ void k_tr_limiter_faces(TArgs a) {
-    long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    int j = (int)flat_tid() + 1;
     const Geom &g = a.g;
+    if (j > g.NF) return;
     const int L = g.L, NC = g.NC;
-    if (t >= (long)g.NF * L) return;
-    int j = (int)(t / L) + 1, k = (int)(t % L) + 1;
     int b = g.bottom_face[j - 1], tf = a.s.top_face[j - 1];
-    if (k < b || k > tf) return;
-    double Q = a.w.qj[t];
-    int writer = 0;
-    if (face_open(g, j)) {
-        int c1 = g.face_cell(1, j), c2 = g.face_cell(2, j);
-        // a cell writes when it is wet, holds layer k and sees Q*sign >= 0; cell 2 comes later
-        if (c2 != 0) {
-            int t2 = a.s.top_cell[c2 - 1];
-            if (t2 != 0 && k >= g.bottom_cell[c2 - 1] && k <= t2 && !is_pos(Q)) writer = c2;   // -Q >= 0
+    if (tf == 0) return;
+    bool open = face_open(g, j);
+    int c1 = g.face_cell(1, j), c2 = g.face_cell(2, j);
+    int t1 = a.s.top_cell[c1 - 1], b1 = g.bottom_cell[c1 - 1];
+    int t2 = c2 != 0 ? a.s.top_cell[c2 - 1] : 0, b2 = c2 != 0 ? g.bottom_cell[c2 - 1] : 0;
+    for (int k = b; k <= tf; ++k) {
+        long t = ix(k, j, L);
+        double Q = a.w.qj[t];
+        int writer = 0;
+        if (open) {
+            // a cell writes when it is wet, holds layer k and sees Q*sign >= 0; cell 2 comes later
+            if (c2 != 0 && t2 != 0 && k >= b2 && k <= t2 && !is_pos(Q)) writer = c2;   // -Q >= 0
+            else if (t1 != 0 && k >= b1 && k <= t1 && !is_neg(Q)) writer = c1;        // Q >= 0
         }
-        if (writer == 0) {
-            int t1 = a.s.top_cell[c1 - 1];
-            if (t1 != 0 && k >= g.bottom_cell[c1 - 1] && k <= t1 && !is_neg(Q)) writer = c1;   // Q >= 0
+        for (int tr = 0; tr < a.ntr; ++tr) {
+            double r = 1.0;
+            if (writer != 0) {
+                int i = writer;
+                int other = (writer == c1) ? c2 : c1;
+                double cik = other > 0 ? a.con[ic(k, other, tr, L, NC)] : oqb_value(a, i, k, tr);
+                double rtemp = a.w.sa2[((long)tr * NC + i - 1) * L + k - 1] * (cik - a.con[ic(k, i, tr, L, NC)]);
+                r = rtemp == 0.0 ? 1.0 : a.w.sa1[((long)tr * NC + i - 1) * L + k - 1] / rtemp;
+            }
+            a.w.psij[(long)tr * g.NF * L + t] = phi_limit(a.p.h_flux_limiter, a.w.phij[t], r);
         }
-    }
-    for (int tr = 0; tr < a.ntr; ++tr) {
-        double r = 1.0;
-        if (writer != 0) {
-            int i = writer;
-            int other = (writer == g.face_cell(1, j)) ? g.face_cell(2, j) : g.face_cell(1, j);
-            double cik = other > 0 ? a.con[ic(k, other, tr, L, NC)] : oqb_value(a, i, k, tr);
-            double rtemp = a.w.sa2[((long)tr * NC + i - 1) * L + k - 1] * (cik - a.con[ic(k, i, tr, L, NC)]);
-            r = rtemp == 0.0 ? 1.0 : a.w.sa1[((long)tr * NC + i - 1) * L + k - 1] / rtemp;
-        }
-        a.w.psij[(long)tr * g.NF * L + t] = phi_limit(a.p.h_flux_limiter, a.w.phij[t], r);
     }
 }
 
@@ -494,12 +523,15 @@ __global__ void k_tr_nodes(TArgs a) {
 }
 
 __global__ void k_tr_faces_cells(TArgs a) {
-    long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned t = flat_tid();
     const Geom &g = a.g;
     const int L = g.L, NC = g.NC;
-    long nfl = (long)g.NF * L, ncl = (long)g.NC * L;
+    unsigned nfl = (unsigned)g.NF * L, ncl = (unsigned)g.NC * L;
     if (t < nfl) {
-        int j = (int)(t / L) + 1, k = (int)(t % L) + 1;
+        int j, k;
+        split_index(t, L, j, k);
+        j += 1;
+        k += 1;
         int n1 = g.face_node(1, j), n2 = g.face_node(2, j);
         bool in = k >= g.bottom_face[j - 1] && k <= a.s.top_face[j - 1];
         for (int tr = 0; tr < a.ntr; ++tr) {
@@ -509,8 +541,11 @@ __global__ void k_tr_faces_cells(TArgs a) {
             dst[t] = in ? (src[ix(k, n1, L)] + src[ix(k, n2, L)]) * 0.5 : 0.0;
         }
     } else if (t < nfl + ncl) {
-        long u = t - nfl;
-        int i = (int)(u / L) + 1, k = (int)(u % L) + 1;
+        unsigned u = t - nfl;
+        int i, k;
+        split_index(u, L, i, k);
+        i += 1;
+        k += 1;
         for (int tr = 0; tr < a.ntr; ++tr) {
             if (a.tid[tr] > a.ntr) continue;
             double *dst = a.tid[tr] == 1 ? a.s.salt_cell_new : a.s.temp_cell_new;
@@ -551,11 +586,11 @@ cudaError_t launch_transport(const Launch &x) {
         a.con_new = nxt;
         if (g.NOB + g.NQB > 0) k_tr_bc<<<blocks_for(g.NOB + g.NQB, 128), 128, 0, x.stream>>>(a);
         a.changed_only = sub > 0;
-        k_tr_face_coef<<<blocks_for((long)g.NF * L, 256), 256, 0, x.stream>>>(a);
-        k_tr_cell_coef<<<blocks_for((long)g.NC * (L + 1), 256), 256, 0, x.stream>>>(a);
+        k_tr_face_coef<<<blocks_for(g.NF, 128), 128, 0, x.stream>>>(a);
+        k_tr_cell_coef<<<blocks_for(g.NC, 128), 128, 0, x.stream>>>(a);
         if (lim) {
             k_tr_limiter_cells<<<blocks_for(g.NC, 128), 128, 0, x.stream>>>(a);
-            k_tr_limiter_faces<<<blocks_for((long)g.NF * L, 256), 256, 0, x.stream>>>(a);
+            k_tr_limiter_faces<<<blocks_for(g.NF, 128), 128, 0, x.stream>>>(a);
         }
         k_tr_solve<<<blocks_for(g.NC, 128), 128, 0, x.stream>>>(a);
         double *t = cur;
