@@ -53,12 +53,13 @@ _PARAM_D = ["gravity", "rho_o", "msl", "dt", "theta", "adv_onoff_depth", "von_ka
             "denominator_min_for_matrix"]
 _PARAM_I = ["advection_flag", "elm_backtrace_flag", "elm_sub_iter", "elm_min_iter", "elm_max_iter",
             "bf_flag", "baroclinic_flag", "ana_density", "max_iteration_pcg", "transport_flag",
-            "trans_sub_iter", "h_flux_limiter", "v_flux_limiter", "is_salt", "is_temp", "heat_option"]
+            "trans_sub_iter", "h_flux_limiter", "v_flux_limiter", "is_salt", "is_temp", "heat_option",
+            "test_barrier_phantom_blocks"]
 
 
 class GomParams(C.Structure):
     _fields_ = [(n, C.c_double) for n in _PARAM_D] + [(n, C.c_int32) for n in _PARAM_I] + \
-               [("reserved", C.c_int32 * 4)]
+               [("reserved", C.c_int32 * 3)]
 
 
 _GEOM = [

@@ -7,6 +7,7 @@
 #include <cstdio>
 #include <algorithm>
 #include <cstring>
+#include <numeric>
 #include <string>
 #include <vector>
 
@@ -326,6 +327,19 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
     UP(delta_z, delta_z, L, true);
 #undef UP
     if (e != cudaSuccess) return fail(e == cudaErrorInvalidValue ? GOM_E_ARG : GOM_E_CUDA);
+    // column orders: entity ids (1-based) stably sorted by bottom layer
+    {
+        auto order = [&](const int32_t *bottom, size_t n, const int **dst) {
+            std::vector<int> ids(n);
+            std::iota(ids.begin(), ids.end(), 1);
+            std::stable_sort(ids.begin(), ids.end(), [&](int a, int b) { return bottom[a - 1] < bottom[b - 1]; });
+            return upload(c, dst, (const int *)ids.data(), n, true);
+        };
+        if (e == cudaSuccess) e = order(g->bottom_layer_at_element, NC, &G.cell_order);
+        if (e == cudaSuccess) e = order(g->bottom_layer_at_face, NF, &G.face_order);
+        if (e == cudaSuccess) e = order(g->bottom_layer_at_node, NN, &G.node_order);
+        if (e != cudaSuccess) return fail(GOM_E_CUDA);
+    }
     // state
     for (int f = 1; f < GOM_F_COUNT && e == cudaSuccess; ++f) {
         const FieldDesc &fd = c->fields[f];
@@ -429,6 +443,7 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
     P.is_salt = params->is_salt;
     P.is_temp = params->is_temp;
     P.heat_option = params->heat_option;
+    P.test_barrier_phantom_blocks = params->test_barrier_phantom_blocks;
     // pinned host staging
     c->stage_len = std::max<size_t>({NF, NN, NC, (size_t)d.n_ob * 2 * nt, (size_t)d.n_qb * 2 * nt}) * 10 + 64;
     if (cudaMallocHost((void **)&c->h_status, sizeof(gom_status)) != cudaSuccess ||

@@ -38,6 +38,9 @@ struct Geom {
     // boundaries / vertical grid
     const int *ob_cell_id, *qb_cell, *qb_face;
     const double *z_level, *delta_z;
+    // entity ids sorted by bottom layer: column kernels take their entity from these so that the
+    // 32 lanes of a warp walk columns of nearly equal height (results do not depend on the order)
+    const int *cell_order, *face_order, *node_order;
 
     // 1-based accessors of the (m, N) connectivity arrays
     __device__ __forceinline__ int cell_node(int l, int i) const { return nodenum_at_cell[(i - 1) * 4 + l - 1]; }
@@ -82,7 +85,7 @@ struct Params {
         kh_0, error_tolerance, delta_z_min, denominator_min_for_matrix;
     int advection_flag, elm_backtrace_flag, elm_sub_iter, elm_min_iter, elm_max_iter, bf_flag, baroclinic_flag,
         ana_density, max_iteration_pcg, transport_flag, trans_sub_iter, h_flux_limiter, v_flux_limiter, is_salt,
-        is_temp, heat_option;
+        is_temp, heat_option, test_barrier_phantom_blocks;
 };
 
 // -------------------------------------------------------------------- layer indexing

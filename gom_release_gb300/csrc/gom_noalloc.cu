@@ -118,6 +118,7 @@ extern "C" int gom_pcg_solve_noalloc(int32_t n_cells, const int32_t *tri_or_quad
     a.maxit = max_iteration;
     a.tol = error_tolerance;
     a.st = status_dev;
+    a.phantom = 0;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(blocks);
     cfg.blockDim = dim3(PCG_THREADS);

@@ -459,8 +459,9 @@ __device__ void elm_face_layer(const Geom &g, const State &s, const Params &p, g
 }
 
 __global__ void k_elm_faces(Geom g, State s, Params p, gom_status *st) {
-    int j = (int)flat_tid() + 1;
-    if (j > g.NF) return;
+    unsigned tid = flat_tid();
+    if (tid >= (unsigned)g.NF) return;
+    int j = g.face_order[tid];
     const int L = g.L;
     int b = g.bottom_face[j - 1], tf = s.top_face[j - 1];
     for (int k = 1; k <= L; ++k) {
@@ -551,8 +552,9 @@ __device__ double prev_rtemp0(const Geom &g, const State &s, const Forcing &f, c
 }
 
 __global__ void __launch_bounds__(128) k_momentum(Geom g, State s, Forcing f, Params p, gom_status *st) {
-    int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    if (j > g.NF) return;
+    unsigned tid = flat_tid();
+    if (tid >= (unsigned)g.NF) return;
+    int j = g.face_order[tid];
     const int L = g.L;
     int tj = s.top_face[j - 1];
     if (tj == 0) return;

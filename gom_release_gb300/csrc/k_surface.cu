@@ -159,6 +159,7 @@ cudaError_t launch_free_surface(const Launch &x) {
     a.maxit = x.p.max_iteration_pcg;
     a.tol = x.p.error_tolerance;
     a.st = x.status;
+    a.phantom = (unsigned)(x.p.test_barrier_phantom_blocks > 0 ? x.p.test_barrier_phantom_blocks : 0);
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(x.w.pcg_blocks);
     cfg.blockDim = dim3(x.w.pcg_threads);
@@ -179,8 +180,9 @@ cudaError_t launch_free_surface(const Launch &x) {
 // ============================================================================================
 // solve_velocities.f90:23-184: one thread per face column
 __global__ void k_face_velocity(Geom g, State s, Forcing f, Params p) {
-    int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    if (j > g.NF) return;
+    unsigned tid = flat_tid();
+    if (tid >= (unsigned)g.NF) return;
+    int j = g.face_order[tid];
     const int L = g.L;
     int tj = s.top_face[j - 1];
     if (tj == 0) {
@@ -242,8 +244,9 @@ __global__ void k_face_velocity(Geom g, State s, Forcing f, Params p) {
 
 // solve_velocities.f90:191-258: one thread per cell column
 __global__ void k_cell_w(Geom g, State s) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    if (i > g.NC) return;
+    unsigned tid = flat_tid();
+    if (tid >= (unsigned)g.NC) return;
+    int i = g.cell_order[tid];
     const int L = g.L;
     int t = s.top_cell[i - 1], b = g.bottom_cell[i - 1];
     if (t == 0) {
@@ -426,8 +429,9 @@ cudaError_t launch_layers(const Launch &x) {
 // calculate_velocity_at_node.f90:31-60: face-level velocities, one thread per face column.  The
 // node loop divides each face level by the face length; that quotient is formed once here.
 __global__ void k_face_level(Geom g, State s, Work w) {
-    int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    if (j > g.NF) return;
+    unsigned tid = flat_tid();
+    if (tid >= (unsigned)g.NF) return;
+    int j = g.face_order[tid];
     const int L = g.L;
     int t = s.top_face[j - 1];
     if (t == 0) return;

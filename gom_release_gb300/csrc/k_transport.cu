@@ -136,9 +136,10 @@ __device__ __forceinline__ void face_coef_at(const TArgs &a, int j, int k, long 
 }
 
 __global__ void k_tr_face_coef(TArgs a) {
-    int j = (int)flat_tid() + 1;
+    unsigned tid = flat_tid();
     const Geom &g = a.g;
-    if (j > g.NF) return;
+    if (tid >= (unsigned)g.NF) return;
+    int j = g.face_order[tid];
     const int L = g.L;
     int b = g.bottom_face[j - 1], tf = a.s.top_face[j - 1];
     if (!a.changed_only) {
@@ -173,9 +174,10 @@ __device__ __forceinline__ void cell_coef_at(const TArgs &a, int i, long t) {
 }
 
 __global__ void k_tr_cell_coef(TArgs a) {
-    int i = (int)flat_tid() + 1;
+    unsigned tid = flat_tid();
     const Geom &g = a.g;
-    if (i > g.NC) return;
+    if (tid >= (unsigned)g.NC) return;
+    int i = g.cell_order[tid];
     const int L = g.L;
     int b = g.bottom_cell[i - 1], tl = a.s.top_cell[i - 1];
     if (!a.changed_only) {
@@ -223,9 +225,10 @@ __device__ __forceinline__ double phi_limit(int code, double small_phi, double r
 // :624-871 per cell column: upwind-weighted differences of every layer (sum1_all, sum2_all) for
 // the face ratios r_jk, and the vertical ratios r_ik -> PSI_ik.
 __global__ void k_tr_limiter_cells(TArgs a) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    unsigned tid = flat_tid();
     const Geom &g = a.g;
-    if (i > g.NC) return;
+    if (tid >= (unsigned)g.NC) return;
+    int i = g.cell_order[tid];
     const int L = g.L, NC = g.NC;
     int tl = a.s.top_cell[i - 1], b = g.bottom_cell[i - 1];
     if (tl == 0) return;
@@ -299,9 +302,10 @@ __global__ void k_tr_limiter_cells(TArgs a) {
 // :769-799 + :876-900 face ratio r_jk from its upwind cell (the last writer in cell order), PSI_jk;
 // one thread per face walks its wet layers
 __global__ void k_tr_limiter_faces(TArgs a) {
-    int j = (int)flat_tid() + 1;
+    unsigned tid = flat_tid();
     const Geom &g = a.g;
-    if (j > g.NF) return;
+    if (tid >= (unsigned)g.NF) return;
+    int j = g.face_order[tid];
     const int L = g.L, NC = g.NC;
     int b = g.bottom_face[j - 1], tf = a.s.top_face[j - 1];
     if (tf == 0) return;
@@ -335,9 +339,10 @@ __global__ void k_tr_limiter_faces(TArgs a) {
 // :921-1346 per cell column: explicit horizontal fluxes + limiter, implicit vertical system,
 // Thomas solve, clamp to [0, 50]; writes the full next column (zero outside the wet range).
 __global__ void __launch_bounds__(128) k_tr_solve(TArgs a) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    unsigned tid = flat_tid();
     const Geom &g = a.g;
-    if (i > g.NC) return;
+    if (tid >= (unsigned)g.NC) return;
+    int i = g.cell_order[tid];
     const int L = g.L, NC = g.NC;
     int tl = a.s.top_cell[i - 1], b = g.bottom_cell[i - 1];
     const double dt2 = a.dt2;
@@ -488,9 +493,10 @@ __global__ void __launch_bounds__(128) k_tr_solve(TArgs a) {
 
 // :1403-1454 node averages (column, top-down) and :1457-1482 face averages + write-back
 __global__ void k_tr_nodes(TArgs a) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    unsigned tid = flat_tid();
     const Geom &g = a.g;
-    if (i > g.NN) return;
+    if (tid >= (unsigned)g.NN) return;
+    int i = g.node_order[tid];
     const int L = g.L, NC = g.NC;
     int tn = a.s.top_node[i - 1], bn = g.bottom_node[i - 1];
     int na = g.adj_cells_at_node[i - 1];
@@ -636,9 +642,10 @@ __device__ __forceinline__ double eos_bulk(double rtemp, double rsalt, double pr
 // one thread per node (kind 0) or face (kind 1) column
 template <int KIND>
 __global__ void k_density_col(Geom g, State s, Params p, gom_status *st) {
-    int e = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    unsigned tid = flat_tid();
     int n = KIND == 0 ? g.NN : g.NF;
-    if (e > n) return;
+    if (tid >= (unsigned)n) return;
+    int e = KIND == 0 ? g.node_order[tid] : g.face_order[tid];
     const int L = g.L;
     int t = KIND == 0 ? s.top_node[e - 1] : s.top_face[e - 1];
     if (t == 0) return;
@@ -683,8 +690,9 @@ __global__ void k_density_col(Geom g, State s, Params p, gom_status *st) {
 
 // :207-238 cell density = mean of its wet nodes
 __global__ void k_density_cells(Geom g, State s, gom_status *st) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    if (i > g.NC) return;
+    unsigned tid = flat_tid();
+    if (tid >= (unsigned)g.NC) return;
+    int i = g.cell_order[tid];
     const int L = g.L;
     int t = s.top_cell[i - 1];
     if (t == 0) return;

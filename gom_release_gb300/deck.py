@@ -65,6 +65,7 @@ class Params:
     is_salt: int = 1
     is_temp: int = 1
     heat_option: int = 2
+    test_barrier_phantom_blocks: int = 0
     # not part of the C ABI params (host-side start-up values)
     av_0: float = 1e-3
     kv_0: float = 1e-4
@@ -145,7 +146,7 @@ def _finish(name, raw, L, z_bottom, z_top, params, ob_pairs, q_pairs, q_portion,
     # the bracket being a default-REAL constant expression
     c = f32(np.float32(0.5) - np.float32(1.0e-4))
     params.denominator_min_for_matrix = min(params.dry_depth * c, dzmin * c)
-    ob_cell_id, ob_face_id = _boundaries(g, ob_pairs)
+    ob_cell_id, ob_face_id = _boundaries(g, ob_pairs) if ob_pairs else (np.zeros(0, np.int32), np.zeros(0, np.int32))
     qb_cell, qb_face = _boundaries(g, q_pairs) if q_pairs else (np.zeros(0, np.int32), np.zeros(0, np.int32))
     nf, nc, nn = g.n_faces, g.n_cells, g.n_nodes
     ob_element_flag = np.zeros(nc, np.int32)
@@ -180,7 +181,7 @@ def _finish(name, raw, L, z_bottom, z_top, params, ob_pairs, q_pairs, q_portion,
 
 # ----------------------------------------------------------------------------- configurations
 def tidal_basin(nx: int = 120, ny: int = 80, dx: float = 250.0, tri_rows: int = 4, n_layers: int = 10,
-                seed: int = 20240601, n_steps: int = 720, dt: float = 120.0) -> Deck:
+                seed: int = 20240601, n_steps: int = 720, dt: float = 120.0, closed: bool = False) -> Deck:
     """Barotropic tidal basin: h = 5 + 15(1 - y/Ly) + seeded Fourier noise (8 modes,
     2-15 km, 1 m), southern open boundary forced by 0.5 cos(2 pi t / 44712 s), closed
     elsewhere, uniform T = 20, S = 30, theta = 0.6, quadratic drag Cd = 0.0025."""
@@ -192,8 +193,8 @@ def tidal_basin(nx: int = 120, ny: int = 80, dx: float = 250.0, tri_rows: int = 
     raw = RawMesh(x=x, y=y, h=h, tri_or_quad=tq, cells=cells)
     params = Params(dt=dt, theta=0.6, error_tolerance=1e-10, baroclinic_flag=0,
                     trans_sub_iter=1, h_flux_limiter=0, v_flux_limiter=0)
-    # open boundary: south edge, node pairs (SW, SE) of the first row of squares
-    ob_pairs = [(i + 1, i + 2) for i in range(nx)]
+    # open boundary: south edge, node pairs (SW, SE) of the first row of squares (none if closed)
+    ob_pairs = [] if closed else [(i + 1, i + 2) for i in range(nx)]
     L = n_layers
     hmax = float(h.max())
     z_bottom = -math.ceil(hmax + 1.0)
@@ -234,6 +235,7 @@ def estuary(nx: int = 600, ny: int = 250, dx: float = 100.0, tri_rows: int = 4, 
     row = nx + 1
     ob_pairs = [((j + 1) * row + 1, j * row + 1) for j in range(ny)]
     # river: east edge faces SE -> NE of column nx-1, centred rows
+    n_river = max(1, min(n_river, ny - 2))
     j0 = ny // 2 - n_river // 2
     q_pairs = [(j * row + nx + 1, (j + 1) * row + nx + 1) for j in range(j0, j0 + n_river)]
     q_portion = [1.0 / n_river] * n_river
@@ -258,7 +260,7 @@ def estuary(nx: int = 600, ny: int = 250, dx: float = 100.0, tri_rows: int = 4, 
 
 
 # ----------------------------------------------------------------------------- initial state
-def initial_state(deck: Deck) -> dict:
+def initial_state(deck: Deck, eta0: np.ndarray | None = None) -> dict:
     """State after prepare_gom.f90 for a cold start: setup_cold_start.f90 (zero elevation and
     velocity), update_vertical_layers_0.f90 (layers and thicknesses), read_salt_init.f90 /
     read_temp_init.f90 (tracers), read_main_inp.f90 card C5_04 (Av, Kv) and C5_01
@@ -271,8 +273,19 @@ def initial_state(deck: Deck) -> dict:
     dzl = deck.delta_z
     msl = p.msl
     st: dict = {}
-    eta_cell_new = np.zeros(nc)
-    eta_node = np.zeros(nn)
+    eta_cell_new = np.zeros(nc) if eta0 is None else np.asarray(eta0, dtype=np.float64).copy()
+    if eta0 is None:
+        eta_node = np.zeros(nn)
+    else:
+        # node elevation = area-weighted mean of its cells (solve_free_surface_equation.f90:353-373)
+        num = np.zeros(nn)
+        den = np.zeros(nn)
+        for l in range(4):
+            m = l < a["tri_or_quad"]
+            nd = a["nodenum_at_cell"][m, l] - 1
+            np.add.at(num, nd, a["area"][m] * eta_cell_new[m])
+            np.add.at(den, nd, a["area"][m])
+        eta_node = num / den
 
     def column(h, eta, bottom, with_edges):
         """update_vertical_layers_0.f90:42-140 (cells, with_edges=False) and :146-263."""
@@ -330,7 +343,7 @@ def initial_state(deck: Deck) -> dict:
     if np.any((nsum2 == 0) & (top_c != 0)):
         raise ValueError("wet element with dry sides at start")
 
-    st["eta_cell"] = np.zeros(nc)
+    st["eta_cell"] = eta_cell_new.copy()
     st["eta_cell_new"] = eta_cell_new
     st["eta_node"] = eta_node
     st["wetdry_node"] = np.zeros(nn, np.int32)
@@ -429,6 +442,8 @@ class HostForcing:
     def eta_ob(self, elapsed, spin):
         """compute_boundary_eta.f90:72-90 (ob_eta_type 1, harmonic)."""
         d = self.deck
+        if d.n_ob == 0:
+            return np.zeros(0), np.zeros(0)
         tide = d.tide
         dt = d.params.dt
         old = 0.0

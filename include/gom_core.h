@@ -126,7 +126,10 @@ typedef struct gom_params {
     int32_t is_salt;           /* C7_2 is_tran(1) */
     int32_t is_temp;           /* C7_2 is_tran(2) */
     int32_t heat_option;       /* C7_3 (only 2 supported when is_temp) */
-    int32_t reserved[4];
+    int32_t test_barrier_phantom_blocks; /* tests only, normally 0: grid barriers of the PCG wait for
+                                            this many blocks that do not exist, so their bounded wait
+                                            runs out and the solve reports GOM_E_TIMEOUT */
+    int32_t reserved[3];
 } gom_params;
 
 /* ------------------------------------------------------------------ static geometry

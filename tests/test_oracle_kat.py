@@ -1,0 +1,221 @@
+"""Known-answer tests of the CPU restatement (the checker of the CUDA library), derived from the
+mathematics of the scheme rather than from reference outputs (the reference ships none)."""
+import numpy as np
+import pytest
+
+from fs_system import apply, assemble
+from gom_release_gb300.core import GomCore, GomError, TIME_LOOP, prepare
+from gom_release_gb300.deck import HostForcing, estuary, initial_state, tidal_basin
+from gom_release_gb300.driver import Run
+
+
+def _run(deck, so, state=None, steps=10):
+    r = Run(deck, GomCore(deck, lib_path=so), state if state is not None else initial_state(deck))
+    r.advance(steps)
+    return r
+
+
+def test_lake_at_rest_stays_at_rest(oracle_so):
+    deck = tidal_basin(nx=12, ny=8, closed=True)
+    r = _run(deck, oracle_so, steps=15)
+    c = r.core
+    for f in ("un_face", "vn_face", "wn_cell", "u_node", "v_node", "w_node", "eta_cell", "eta_node"):
+        assert np.all(c.get_field(f) == 0.0), f
+    assert np.all(r.pcg_iters == [0] * 15)   # zero residual: the initial guess is the solution
+    s = c.get_field("salt_cell").reshape(deck.n_cells, deck.n_layers)
+    top = c.get_field("top_layer_cell")
+    bot = deck.geo["bottom_layer_at_element"]
+    for i in range(deck.n_cells):   # implicit vertical diffusion of a uniform column: round-off only
+        assert np.abs(s[i, bot[i] - 1:top[i]] - 30.0).max() < 1e-12
+
+
+def test_uniform_tracers_stay_uniform_under_tide(oracle_so):
+    """The TVD update keeps a uniform tracer uniform when the free-surface system is solved
+    exactly; with the reference's PCG stop ratio of 1e-10 the deviation is ~1e-4, so the solver
+    runs to a ratio of 1e-24 here."""
+    deck = tidal_basin(nx=14, ny=10)
+    deck.params.error_tolerance = 1e-24
+    r = _run(deck, oracle_so, steps=30)
+    c = r.core
+    top = c.get_field("top_layer_cell")
+    bot = deck.geo["bottom_layer_at_element"]
+    s = c.get_field("salt_cell").reshape(deck.n_cells, deck.n_layers)
+    t = c.get_field("temp_cell").reshape(deck.n_cells, deck.n_layers)
+    for i in range(deck.n_cells):
+        sl = slice(bot[i] - 1, top[i])
+        assert np.abs(s[i, sl] - 30.0).max() < 1e-9
+        assert np.abs(t[i, sl] - 20.0).max() < 1e-9
+    assert np.abs(c.get_field("eta_cell")).max() > 1e-3   # the tide did move the water
+
+
+def test_volume_conserved_in_closed_basin(oracle_so):
+    """Sum of area*dz over wet layers is conserved up to the free-surface solver's residual: 2e-8
+    after 40 steps at the reference's stop ratio 1e-10, round-off at 1e-24."""
+    deck = tidal_basin(nx=14, ny=10, closed=True)
+    deck.params.error_tolerance = 1e-24
+    x = deck.geo["x_cell"]
+    eta0 = 0.2 * np.cos(np.pi * x / x.max())
+    st = initial_state(deck, eta0)
+    r = Run(deck, GomCore(deck, lib_path=oracle_so), st)
+    v0, _ = r.core.conservation()
+    r.advance(40)
+    v1, _ = r.core.conservation()
+    assert abs(np.abs(r.core.get_field("un_face")).max()) > 1e-3   # the water sloshes
+    assert abs(v1 - v0) / v0 < 1e-12
+
+
+def test_momentum_matrix_identity(oracle_so):
+    """A * AinvDeltaZ = dz for the vertical momentum matrix of each wet face (tridiagonal_solver)."""
+    deck = estuary(nx=16, ny=8, dx=100.0, n_layers=10, trans_sub_iter=2)
+    r = _run(deck, oracle_so, steps=3)
+    c = r.core
+    L = deck.n_layers
+    p = deck.params
+    c.set_forcing(r.forcing.full(r.it + 1))
+    for ph in TIME_LOOP[:TIME_LOOP.index("momentum") + 1]:
+        c.step(ph)
+    top = c.get_field("top_layer_face")
+    bot = deck.geo["bottom_layer_at_face"]
+    av = c.get_field("av").reshape(-1, L + 1)
+    dzh = c.get_field("dzhalf_face").reshape(-1, L + 1)
+    dz = c.get_field("dz_face").reshape(-1, L)
+    gb = c.get_field("gamma_b")
+    adz = c.get_field("ainvdz2").reshape(-1, L)
+    checked = 0
+    for j in range(0, deck.n_faces, 7):
+        t, b = top[j], bot[j]
+        if t == 0:
+            continue
+        n = t - b + 1
+        A = np.zeros((n, n))
+        for row in range(n):        # row 0 = top layer
+            k = t - row
+            A[row, row] = dz[j, k - 1]
+            if row > 0:             # coupling to the layer above (k+1)
+                cu = -p.dt * av[j, k] / dzh[j, k]
+                A[row, row - 1] = cu
+                A[row, row] -= cu
+            if k > b:               # coupling to the layer below (k-1)
+                lower = -p.dt * av[j, k - 1] / dzh[j, k - 1]
+                A[row, row + 1] = lower
+                A[row, row] -= lower
+            if k == b:
+                A[row, row] += gb[j] * p.dt
+        sol = adz[j, :n]
+        rhs = np.array([dz[j, t - row - 1] for row in range(n)])
+        assert np.allclose(A @ sol, rhs, rtol=1e-12, atol=1e-12), j
+        checked += 1
+    assert checked > 10
+
+
+def test_pcg_solution_meets_the_stop_criterion(oracle_so):
+    deck = estuary(nx=16, ny=8, dx=100.0, n_layers=10, trans_sub_iter=2)
+    r = _run(deck, oracle_so, steps=3)
+    c = r.core
+    f = r.forcing.full(r.it + 1)
+    c.set_forcing(f)
+    for ph in TIME_LOOP[:TIME_LOOP.index("free_surface")]:
+        c.step(ph)
+    snap = c.state()
+    x0 = snap["eta_cell_new"]
+    iters = c.step("free_surface")
+    x = c.get_field("eta_cell_new")
+    sp, b = assemble(deck, snap, f["eta_at_ob_new"])
+    minv = 1.0 / sp[:, 0]
+    r0 = b - apply(deck, sp, x0)
+    r1 = b - apply(deck, sp, x)
+    d0 = float(r0 @ (minv * r0))
+    d1 = float(r1 @ (minv * r1))
+    assert 0 < iters < deck.params.max_iteration_pcg
+    assert np.sqrt(d1 * d1 / (d0 * d0)) < 10 * deck.params.error_tolerance
+
+
+def test_uniform_flow_elm_feet(oracle_so):
+    """Uniform horizontal flow over squares: the foot of every face midpoint is x - U dt, the
+    interpolated velocity is U itself."""
+    deck = tidal_basin(nx=10, ny=8, tri_rows=0, closed=True)
+    st = initial_state(deck)
+    c = GomCore(deck, lib_path=oracle_so)
+    prepare(c, st)
+    U, V = 0.3, 0.1
+    g = deck.geo
+    L = deck.n_layers
+    ct, sn = g["cos_theta"], g["sin_theta"]
+    un = (U * ct + V * sn)[:, None].repeat(L, 1)
+    vn = (-U * sn + V * ct)[:, None].repeat(L, 1)
+    c.set_field("un_face", un)
+    c.set_field("vn_face", vn)
+    c.set_field("u_node", np.full((deck.n_nodes, L + 1), U))
+    c.set_field("v_node", np.full((deck.n_nodes, L + 1), V))
+    c.set_forcing(HostForcing(deck).full(1))
+    c.step("advection")
+    foot = c.get_field("elm_foot").reshape(-1, L)
+    uel = c.get_field("un_elm").reshape(-1, L)
+    top = c.get_field("top_layer_face")
+    bot = g["bottom_layer_at_face"]
+    dx = deck.meta["dx"]
+    nx, ny = deck.meta["nx"], deck.meta["ny"]
+    checked = 0
+    for j in range(deck.n_faces):
+        if g["adj_cellnum_at_face"][j, 1] == 0:
+            continue
+        xf = g["x_face"][j] - U * deck.params.dt
+        yf = g["y_face"][j] - V * deck.params.dt
+        ci, cj = int(xf // dx), int(yf // dx)
+        if not (0 <= ci < nx and 0 <= cj < ny):
+            continue
+        expect = cj * nx + ci + 1
+        for k in range(bot[j], top[j] + 1):
+            assert foot[j, k - 1] == expect, (j, k)
+            assert abs(uel[j, k - 1] - un[j, k - 1]) < 1e-12
+            checked += 1
+    assert checked > 100
+
+
+def test_unesco_density_check_value(oracle_so):
+    deck = estuary(nx=10, ny=6, dx=100.0, n_layers=6)
+    deck.init_salt_node[:] = 35.0
+    deck.init_temp_node[:] = 5.0
+    st = initial_state(deck)
+    c = GomCore(deck, lib_path=oracle_so)
+    prepare(c, st)
+    rho = c.get_field("rho_node").reshape(-1, deck.n_layers)
+    top = c.get_field("top_layer_node")
+    bot = deck.geo["bottom_layer_at_node"]
+    vals = np.concatenate([rho[i, bot[i] - 1:top[i]] for i in range(deck.n_nodes)])
+    # UNESCO (1981) check value at S = 35, T = 5 C, p = 0: 1027.67547 kg/m3
+    assert np.abs(vals - 1027.67547).max() < 2e-4
+
+
+def test_fault_codes(oracle_so):
+    deck = estuary(nx=12, ny=6, dx=100.0, n_layers=8, trans_sub_iter=2)
+    st = initial_state(deck)
+    c = GomCore(deck, lib_path=oracle_so)
+    prepare(c, st)
+    c.set_forcing(HostForcing(deck).full(1))
+    for ph in TIME_LOOP[:TIME_LOOP.index("free_surface")]:
+        c.step(ph)
+    bad = c.get_field("ainvdz1")
+    bad[:] = -1.0
+    c.set_field("ainvdz1", bad)
+    with pytest.raises(GomError) as e:
+        c.step("free_surface")
+    assert e.value.code == 3 and e.value.status.site == 100   # GOM_E_NOT_SPD
+    c.status(clear=True)
+    # zero pivot: a single-layer column with no thickness, no drag
+    c2 = GomCore(deck, lib_path=oracle_so)
+    prepare(c2, st)
+    c2.set_forcing(HostForcing(deck).full(1))
+    dz = c2.get_field("dz_face").reshape(deck.n_faces, deck.n_layers)
+    dz[:] = 0.0
+    c2.set_field("dz_face", dz)
+    with pytest.raises(GomError) as e:
+        c2.step("momentum")
+    assert e.value.code == 4                                 # GOM_E_ZERO_PIVOT
+
+
+def test_pcg_iteration_cap_returns(oracle_so):
+    deck = estuary(nx=12, ny=6, dx=100.0, n_layers=8, trans_sub_iter=2)
+    deck.params.max_iteration_pcg = 2
+    r = _run(deck, oracle_so, steps=2)
+    assert r.pcg_iters == [2, 2]
