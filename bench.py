@@ -53,13 +53,18 @@ PCG_BYTES_PER_CELL_ITERATION = 120
 FS_ASSEMBLY_BYTES_PER_CELL_LAYER = 64
 
 
-def make_deck(size: str):
+def make_deck(size: str, precision: str = "fp64"):
+    import dataclasses
     from gom_release_gb300.deck import estuary
     if size == "small":
-        return estuary(nx=120, ny=50, dx=100.0, n_layers=20)
-    if size == "medium":
-        return estuary(nx=300, ny=125, dx=100.0, n_layers=20)
-    return estuary()
+        d = estuary(nx=120, ny=50, dx=100.0, n_layers=20)
+    elif size == "medium":
+        d = estuary(nx=300, ny=125, dx=100.0, n_layers=20)
+    else:
+        d = estuary()
+    if precision == "mixed":
+        d = dataclasses.replace(d, params=dataclasses.replace(d.params, precision=1))
+    return d
 
 
 class ClockSampler:
@@ -128,6 +133,8 @@ def kernel_launches_per_step(deck) -> int:
         n += 1 + nt * per + 2
     if p.baroclinic_flag == 1:
         n += 3 if p.ana_density == 0 else 2
+    if p.turbulence_flag:
+        n += 2                              # closure: face columns, cell diffusivities
     return n
 
 
@@ -282,6 +289,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-phases", action="store_true", help="skip the per-phase timing pass")
     ap.add_argument("--e2e-steps", type=int, default=0)
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
+                    help="fp64: the drop-in path (bit-for-bit with the CPU restatement); mixed: FP32 layered state")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":
@@ -294,7 +303,7 @@ def main():
     from gom_release_gb300.deck import HostForcing, active_cell_layers, initial_state
     from gom_release_gb300.driver import Run
 
-    deck = make_deck(args.size)
+    deck = make_deck(args.size, args.precision)
     st = initial_state(deck)
     ncl = active_cell_layers(deck, st)
     lib = load_core()
@@ -356,12 +365,15 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": secs / args.steps * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+        "data": "synthetic",
         "config": {
+            "precision": args.precision,
             "workload": (f"estuary: {deck.n_cells} cells ({deck.meta['nx']}x{deck.meta['ny']} squares of "
                          f"{deck.meta['dx']:g} m + {deck.meta['tri_rows']}-row triangle strip), {deck.n_faces} faces, "
                          f"{deck.n_nodes} nodes, {deck.n_layers} layers, {ncl} active cell-layers, dt={deck.params.dt:g} s, "
-                         f"TVD limiter, {deck.params.trans_sub_iter} transport subcycles, baroclinic"),
+                         f"TVD limiter, {deck.params.trans_sub_iter} transport subcycles, baroclinic, "
+                         f"turbulence closure {deck.params.turbulence_flag}"),
             "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
             "l2": "state larger than L2 (each phase streams its arrays from HBM)",
             "simulated_hours_per_wall_s": deck.params.dt * args.steps / secs / 3600.0,

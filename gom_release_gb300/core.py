@@ -54,12 +54,13 @@ _PARAM_D = ["gravity", "rho_o", "msl", "dt", "theta", "adv_onoff_depth", "von_ka
 _PARAM_I = ["advection_flag", "elm_backtrace_flag", "elm_sub_iter", "elm_min_iter", "elm_max_iter",
             "bf_flag", "baroclinic_flag", "ana_density", "max_iteration_pcg", "transport_flag",
             "trans_sub_iter", "h_flux_limiter", "v_flux_limiter", "is_salt", "is_temp", "heat_option",
-            "test_barrier_phantom_blocks"]
+            "test_barrier_phantom_blocks", "precision", "turbulence_flag"]
+_PARAM_PP = ["pp_h1", "pp_h2", "pp_vdmax1", "pp_vdmax2", "pp_vdmin1", "pp_vdmin2", "pp_tdmin"]
 
 
 class GomParams(C.Structure):
     _fields_ = [(n, C.c_double) for n in _PARAM_D] + [(n, C.c_int32) for n in _PARAM_I] + \
-               [("reserved", C.c_int32 * 3)]
+               [("reserved", C.c_int32)] + [(n, C.c_double) for n in _PARAM_PP]
 
 
 _GEOM = [
@@ -105,8 +106,10 @@ class GomError(RuntimeError):
         super().__init__(s)
 
 
+ABI_VERSION = 2      # GOM_ABI_VERSION of include/gom_core.h
+
 _STEPS = ["bottom_friction", "boundary_velocity", "advection", "momentum", "velocities", "layers",
-          "node_velocity", "transport", "density", "swap"]
+          "node_velocity", "transport", "density", "turbulence", "swap"]
 
 
 def _bind(lib: C.CDLL) -> C.CDLL:
@@ -127,6 +130,8 @@ def _bind(lib: C.CDLL) -> C.CDLL:
         getattr(lib, f"gom_step_{s}").argtypes = [vp]
     lib.gom_step_free_surface.argtypes = [vp, C.POINTER(C.c_int32)]
     lib.gom_step_all.argtypes = [vp, C.POINTER(C.c_int32)]
+    lib.gom_step_launch.argtypes = [vp]
+    lib.gom_step_wait.argtypes = [vp, C.POINTER(C.c_int32)]
     lib.gom_conservation.argtypes = [vp, _D, _D]
     lib.gom_get_status.argtypes = [vp, C.POINTER(GomStatus), C.c_int]
     lib.gom_synchronize.argtypes = [vp]
@@ -143,8 +148,8 @@ def load_library(path: str | os.PathLike) -> C.CDLL:
         raise FileNotFoundError(f"{path} is not built")
     lib = _bind(C.CDLL(str(path), mode=C.RTLD_LOCAL))
     v = lib.gom_abi_version()
-    if v != 1:
-        raise RuntimeError(f"{path}: ABI version {v}, expected 1")
+    if v != ABI_VERSION:
+        raise RuntimeError(f"{path}: ABI version {v}, expected {ABI_VERSION}")
     return lib
 
 
@@ -180,7 +185,8 @@ class GomCore:
         d = deck
         p = d.params
         self.dims = GomDims(d.n_cells, d.n_faces, d.n_nodes, d.n_layers, d.max_nb, d.n_ob, d.n_qb, 0)
-        self.params = GomParams(*[getattr(p, n) for n in _PARAM_D], *[int(getattr(p, n)) for n in _PARAM_I])
+        self.params = GomParams(*[getattr(p, n) for n in _PARAM_D], *[int(getattr(p, n)) for n in _PARAM_I], 0,
+                                *[getattr(p, n) for n in _PARAM_PP])
         g = d.geo
         keep = {}
         for name, kind in _GEOM:
@@ -277,6 +283,14 @@ class GomCore:
         self._check(self.lib.gom_step_all(self.ctx, C.byref(it)), "step_all")
         return it.value
 
+    def step_launch(self):
+        self._check(self.lib.gom_step_launch(self.ctx), "step_launch")
+
+    def step_wait(self) -> int:
+        it = C.c_int32()
+        self._check(self.lib.gom_step_wait(self.ctx, C.byref(it)), "step_wait")
+        return it.value
+
     def synchronize(self):
         self._check(self.lib.gom_synchronize(self.ctx), "synchronize")
 
@@ -305,7 +319,7 @@ class GomCore:
 
 # ------------------------------------------------------------------ time loop (main.f90:53-304)
 TIME_LOOP = ["bottom_friction", "boundary_velocity", "advection", "momentum", "free_surface",
-             "velocities", "layers", "node_velocity", "transport", "density", "swap"]
+             "velocities", "layers", "node_velocity", "transport", "density", "turbulence", "swap"]
 
 
 def prepare(core: GomCore, state: dict):

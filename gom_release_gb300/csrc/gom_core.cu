@@ -22,6 +22,7 @@ struct FieldDesc {
     int lo;          // -1: 1-D entity array; else lower layer bound (0 or 1)
     int kind;        // 0 cells, 1 faces, 2 nodes, 3 river cells
     int is_int;
+    int dev_bytes;   // element size on the device: 4 (int32 or FP32 storage) or 8
 };
 
 }  // namespace
@@ -29,7 +30,9 @@ struct FieldDesc {
 struct gom_ctx {
     gom_dims d{};
     gom_params hp{};
-    Launch x;
+    Launch x;             // FP64 context; in a mixed context it holds the shared pieces
+    LaunchT<float> xf;    // mixed context: FP32 layered state, shared geometry/forcing/PCG work
+    bool mixed = false;
     int device = 0;
     std::vector<void *> allocs;
     std::string msg;
@@ -42,8 +45,11 @@ struct gom_ctx {
     gom_status *h_status = nullptr;
     int *h_iters = nullptr;
     double *h_cons = nullptr;
-    double *h_stage = nullptr;
-    size_t stage_len = 0;
+    double *h_stage = nullptr;      // two halves, used alternately by consecutive uploads
+    size_t stage_len = 0;           // doubles per half
+    int stage_half = 0;
+    cudaEvent_t stage_done[2] = {nullptr, nullptr};
+    bool step_pending = false;
     long long pcg_total = 0;
     cudaGraphExec_t graph = nullptr;
     bool graph_failed = false;
@@ -76,6 +82,32 @@ template <typename T> cudaError_t dalloc(gom_ctx *c, T **p, size_t n) {
     return e;
 }
 
+// transport and node-velocity work arrays in the layered-state type
+template <typename R> cudaError_t alloc_layered_work(gom_ctx *c, WorkT<R> &W) {
+    const size_t NC = c->d.n_cells, NF = c->d.n_faces, L = c->d.n_layers;
+    const size_t NOB = (size_t)c->d.n_ob, NQB = (size_t)c->d.n_qb;
+    cudaError_t e = cudaSuccess;
+    R **two[] = {&W.con, &W.con2};
+    for (R **p : two)
+        if (e == cudaSuccess) e = dalloc(c, p, (L + 2) * NC * 2);
+    R **face_l[] = {&W.qj, &W.dj, &W.phij};
+    for (R **p : face_l)
+        if (e == cudaSuccess) e = dalloc(c, p, L * NF);
+    R **cell_l0[] = {&W.qi, &W.di, &W.phii};
+    for (R **p : cell_l0)
+        if (e == cudaSuccess) e = dalloc(c, p, (L + 1) * NC);
+    if (e == cudaSuccess) e = dalloc(c, &W.psij, L * NF * 2);
+    if (e == cudaSuccess) e = dalloc(c, &W.psii, (L + 1) * NC * 2);
+    if (e == cudaSuccess) e = dalloc(c, &W.sa1, L * NC * 2);
+    if (e == cudaSuccess) e = dalloc(c, &W.sa2, L * NC * 2);
+    if (e == cudaSuccess) e = dalloc(c, &W.obk, L * NOB * 2);
+    if (e == cudaSuccess) e = dalloc(c, &W.qbk, L * NQB * 2);
+    if (e == cudaSuccess) e = dalloc(c, &W.uflf, (L + 1) * NF);
+    if (e == cudaSuccess) e = dalloc(c, &W.vflf, (L + 1) * NF);
+    if (e == cudaSuccess && c->hp.turbulence_flag != 0) e = dalloc(c, &W.kvf, (L + 1) * NF);
+    return e;
+}
+
 template <typename T> cudaError_t upload(gom_ctx *c, const T **dst, const T *src, size_t n, bool required) {
     T *p = nullptr;
     cudaError_t e = dalloc(c, &p, n);
@@ -92,14 +124,17 @@ int64_t field_count(const gom_dims &d, const FieldDesc &f) {
     return n * (int64_t)(d.n_layers - f.lo + 1);
 }
 
-void describe_fields(gom_ctx *c) {
-    State &s = c->x.s;
-    auto D = [&](int id, double **m, int lo, int kind) { c->fields[id] = FieldDesc{(void **)m, lo, kind, 0}; };
-    auto I = [&](int id, int **m, int lo, int kind) { c->fields[id] = FieldDesc{(void **)m, lo, kind, 1}; };
-    for (int f = 0; f < GOM_F_COUNT; ++f) c->fields[f] = FieldDesc{nullptr, -2, 0, 0};
-    D(GOM_F_ETA_CELL, &s.eta_cell, -1, 0);
-    D(GOM_F_ETA_CELL_NEW, &s.eta_cell_new, -1, 0);
-    D(GOM_F_ETA_NODE, &s.eta_node, -1, 2);
+// R: storage type of the layered state (double fields stay FP64 in every context)
+template <typename R> void describe_fields(gom_ctx *c, StateT<R> &s) {
+    auto E = [&](int id, double **m, int lo, int kind) { c->fields[id] = FieldDesc{(void **)m, lo, kind, 0, 8}; };
+    auto D = [&](int id, R **m, int lo, int kind) {
+        c->fields[id] = FieldDesc{(void **)m, lo, kind, 0, (int)sizeof(R)};
+    };
+    auto I = [&](int id, int **m, int lo, int kind) { c->fields[id] = FieldDesc{(void **)m, lo, kind, 1, 4}; };
+    for (int f = 0; f < GOM_F_COUNT; ++f) c->fields[f] = FieldDesc{nullptr, -2, 0, 0, 8};
+    E(GOM_F_ETA_CELL, &s.eta_cell, -1, 0);
+    E(GOM_F_ETA_CELL_NEW, &s.eta_cell_new, -1, 0);
+    E(GOM_F_ETA_NODE, &s.eta_node, -1, 2);
     I(GOM_F_WETDRY_NODE, &s.wetdry_node, -1, 2);
     D(GOM_F_UN_FACE, &s.un_face, 1, 1);
     D(GOM_F_VN_FACE, &s.vn_face, 1, 1);
@@ -144,13 +179,13 @@ void describe_fields(gom_ctx *c) {
     D(GOM_F_TEMP_NODE, &s.temp_node, 1, 2);
     D(GOM_F_SALT_FACE, &s.salt_face, 1, 1);
     D(GOM_F_TEMP_FACE, &s.temp_face, 1, 1);
-    D(GOM_F_RHO_CELL, &s.rho_cell, 1, 0);
-    D(GOM_F_RHO_NODE, &s.rho_node, 1, 2);
-    D(GOM_F_RHO_FACE, &s.rho_face, 1, 1);
+    E(GOM_F_RHO_CELL, &s.rho_cell, 1, 0);
+    E(GOM_F_RHO_NODE, &s.rho_node, 1, 2);
+    E(GOM_F_RHO_FACE, &s.rho_face, 1, 1);
     I(GOM_F_NUM_SUB_ELM, &s.num_sub_elm, 1, 2);
     D(GOM_F_CDB, &s.cdb, -1, 1);
     D(GOM_F_GAMMA_B, &s.gamma_b, -1, 1);
-    D(GOM_F_QU_BOUNDARY, &s.qu_boundary, -1, 3);
+    E(GOM_F_QU_BOUNDARY, &s.qu_boundary, -1, 3);
     I(GOM_F_ELM_FOOT, &s.elm_foot, 1, 1);
     I(GOM_F_ELM_NEAR_EDGE, &s.elm_near_edge, 1, 1);
 }
@@ -167,7 +202,7 @@ cudaError_t enqueue_swap(gom_ctx *c) {
     for (auto &pr : kSwapPairs) {
         const FieldDesc &a = c->fields[pr[0]];
         const FieldDesc &b = c->fields[pr[1]];
-        size_t bytes = (size_t)field_count(c->d, a) * 8;
+        size_t bytes = (size_t)field_count(c->d, a) * a.dev_bytes;
         cudaError_t e = cudaMemcpyAsync(*a.dev, *b.dev, bytes, cudaMemcpyDeviceToDevice, c->x.stream);
         if (e != cudaSuccess) return e;
     }
@@ -175,8 +210,7 @@ cudaError_t enqueue_swap(gom_ctx *c) {
 }
 
 // the phases of main.f90:94-272 in order
-cudaError_t enqueue_step(gom_ctx *c) {
-    const Launch &x = c->x;
+template <typename R> cudaError_t enqueue_step_t(gom_ctx *c, const LaunchT<R> &x) {
     cudaError_t e;
     if ((e = launch_bottom_friction(x))) return e;
     if ((e = launch_boundary_velocity(x))) return e;
@@ -188,8 +222,14 @@ cudaError_t enqueue_step(gom_ctx *c) {
     if ((e = launch_node_velocity(x))) return e;
     if ((e = launch_transport(x))) return e;
     if ((e = launch_density(x))) return e;
+    if ((e = launch_turbulence(x))) return e;
     return enqueue_swap(c);
 }
+
+cudaError_t enqueue_step(gom_ctx *c) { return c->mixed ? enqueue_step_t(c, c->xf) : enqueue_step_t(c, c->x); }
+
+// a phase launcher on the context's state type
+#define GOM_PHASE(fn) [](gom_ctx *c) { return c->mixed ? fn(c->xf) : fn(c->x); }
 
 // copy status and PCG iterations to pinned memory, wait, translate to a return code
 int finish(gom_ctx *c, int32_t *pcg_iters, bool had_pcg) {
@@ -203,9 +243,9 @@ int finish(gom_ctx *c, int32_t *pcg_iters, bool had_pcg) {
     return c->h_status->code;
 }
 
-int run_phase(gom_ctx *c, cudaError_t (*fn)(const Launch &)) {
+template <typename Fn> int run_phase(gom_ctx *c, Fn fn) {
     if (!c) return GOM_E_ARG;
-    CK(fn(c->x));
+    CK(fn(c));
     return finish(c, nullptr, false);
 }
 
@@ -238,11 +278,11 @@ const char *gom_last_message(const gom_ctx *ctx) { return ctx ? ctx->msg.c_str()
 int gom_field_info(const gom_dims *dims, int field, int64_t *count, int32_t *elem_bytes) {
     if (!dims || field <= 0 || field >= GOM_F_COUNT) return GOM_E_ARG;
     gom_ctx tmp;
-    describe_fields(&tmp);
+    describe_fields(&tmp, tmp.x.s);
     const FieldDesc &f = tmp.fields[field];
     if (f.lo == -2) return GOM_E_ARG;
     if (count) *count = field_count(*dims, f);
-    if (elem_bytes) *elem_bytes = f.is_int ? 4 : 8;
+    if (elem_bytes) *elem_bytes = f.is_int ? 4 : 8;   // host-side element: int32 or FP64
     return GOM_OK;
 }
 
@@ -254,13 +294,17 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
         d.max_nb <= 0 || d.max_nb > GOM_MAXNB || d.n_ob < 0 || d.n_qb < 0)
         return GOM_E_ARG;
     if (params->transport_flag && params->is_salt == 0 && params->is_temp == 1) return GOM_E_ARG;
+    if (params->precision != GOM_PRECISION_FP64 && params->precision != GOM_PRECISION_MIXED) return GOM_E_ARG;
+    if (params->turbulence_flag < 0 || params->turbulence_flag > 2) return GOM_E_ARG;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return GOM_E_CUDA;
     gom_ctx *c = new gom_ctx();
     c->d = d;
     c->hp = *params;
     cudaGetDevice(&c->device);
-    describe_fields(c);
+    c->mixed = params->precision == GOM_PRECISION_MIXED;
+    if (c->mixed) describe_fields(c, c->xf.s);
+    else describe_fields(c, c->x.s);
     auto fail = [&](int code) {
         gom_destroy(c);
         return code;
@@ -346,6 +390,7 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
         if (fd.lo == -2) continue;
         size_t n = (size_t)field_count(d, fd);
         if (fd.is_int) e = dalloc(c, (int **)fd.dev, n);
+        else if (fd.dev_bytes == 4) e = dalloc(c, (float **)fd.dev, n);
         else e = dalloc(c, (double **)fd.dev, n);
     }
     // forcing
@@ -389,23 +434,8 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
     if (e == cudaSuccess) e = dalloc(c, &W.d1, NC);
     if (e == cudaSuccess) e = dalloc(c, &W.barrier, 2);
     if (e == cudaSuccess) e = dalloc(c, &W.pcg_iters, 1);
-    if (e == cudaSuccess) e = dalloc(c, &W.con, (L + 2) * NC * 2);
-    if (e == cudaSuccess) e = dalloc(c, &W.con2, (L + 2) * NC * 2);
-    if (e == cudaSuccess) e = dalloc(c, &W.qj, L * NF);
-    if (e == cudaSuccess) e = dalloc(c, &W.dj, L * NF);
-    if (e == cudaSuccess) e = dalloc(c, &W.phij, L * NF);
-    if (e == cudaSuccess) e = dalloc(c, &W.qi, (L + 1) * NC);
-    if (e == cudaSuccess) e = dalloc(c, &W.di, (L + 1) * NC);
-    if (e == cudaSuccess) e = dalloc(c, &W.phii, (L + 1) * NC);
-    if (e == cudaSuccess) e = dalloc(c, &W.psij, L * NF * 2);
-    if (e == cudaSuccess) e = dalloc(c, &W.psii, (L + 1) * NC * 2);
-    if (e == cudaSuccess) e = dalloc(c, &W.sa1, L * NC * 2);
-    if (e == cudaSuccess) e = dalloc(c, &W.sa2, L * NC * 2);
-    if (e == cudaSuccess) e = dalloc(c, &W.obk, L * (size_t)d.n_ob * 2);
-    if (e == cudaSuccess) e = dalloc(c, &W.qbk, L * (size_t)d.n_qb * 2);
+    if (e == cudaSuccess) e = c->mixed ? alloc_layered_work(c, c->xf.w) : alloc_layered_work(c, W);
     if (e == cudaSuccess) e = dalloc(c, &W.idev, L * NF);
-    if (e == cudaSuccess) e = dalloc(c, &W.uflf, (L + 1) * NF);
-    if (e == cudaSuccess) e = dalloc(c, &W.vflf, (L + 1) * NF);
     if (e == cudaSuccess) e = dalloc(c, &W.node_weight, NN);
     if (e == cudaSuccess) e = dalloc(c, &W.cons, 2 + 2 * (size_t)((NC + 255) / 256));
     if (e == cudaSuccess) e = dalloc(c, &c->x.status, 1);
@@ -444,13 +474,23 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
     P.is_temp = params->is_temp;
     P.heat_option = params->heat_option;
     P.test_barrier_phantom_blocks = params->test_barrier_phantom_blocks;
+    P.turbulence_flag = params->turbulence_flag;
+    P.pp_h1 = params->pp_h1;
+    P.pp_h2 = params->pp_h2;
+    P.pp_vdmax1 = params->pp_vdmax1;
+    P.pp_vdmax2 = params->pp_vdmax2;
+    P.pp_vdmin1 = params->pp_vdmin1;
+    P.pp_vdmin2 = params->pp_vdmin2;
+    P.pp_tdmin = params->pp_tdmin;
     // pinned host staging
     c->stage_len = std::max<size_t>({NF, NN, NC, (size_t)d.n_ob * 2 * nt, (size_t)d.n_qb * 2 * nt}) * 10 + 64;
     if (cudaMallocHost((void **)&c->h_status, sizeof(gom_status)) != cudaSuccess ||
         cudaMallocHost((void **)&c->h_iters, sizeof(int)) != cudaSuccess ||
         cudaMallocHost((void **)&c->h_cons, 2 * sizeof(double)) != cudaSuccess ||
-        cudaMallocHost((void **)&c->h_stage, c->stage_len * sizeof(double)) != cudaSuccess)
+        cudaMallocHost((void **)&c->h_stage, 2 * c->stage_len * sizeof(double)) != cudaSuccess)
         return fail(GOM_E_NOMEM);
+    for (int h = 0; h < 2; ++h)
+        if (cudaEventCreateWithFlags(&c->stage_done[h], cudaEventDisableTiming) != cudaSuccess) return fail(GOM_E_CUDA);
     std::memset(c->h_status, 0, sizeof(gom_status));
     if (pcg_configure(c->x, c->device) != cudaSuccess) return fail(GOM_E_CUDA);
     if (launch_node_weights(c->x) != cudaSuccess) return fail(GOM_E_CUDA);
@@ -458,6 +498,36 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
         size_t nb = (size_t)c->x.w.pcg_blocks;
         if (dalloc(c, &W.partial_dq, nb) != cudaSuccess || dalloc(c, &W.partial_delta, nb) != cudaSuccess)
             return fail(GOM_E_NOMEM);
+    }
+    if (c->mixed) {
+        // the FP32 context shares geometry, forcing, parameters, status, stream and the FP64
+        // work arrays (free-surface system, PCG vectors, ELM counts, node weights, sums)
+        LaunchT<float> &X = c->xf;
+        X.g = c->x.g;
+        X.f = c->x.f;
+        X.p = c->x.p;
+        X.status = c->x.status;
+        X.stream = c->x.stream;
+        X.num_sms = c->x.num_sms;
+        X.w.sparsem = W.sparsem;
+        X.w.rhs = W.rhs;
+        X.w.minv = W.minv;
+        X.w.r = W.r;
+        X.w.s = W.s;
+        X.w.q = W.q;
+        X.w.d0 = W.d0;
+        X.w.d1 = W.d1;
+        X.w.partial_dq = W.partial_dq;
+        X.w.partial_delta = W.partial_delta;
+        X.w.barrier = W.barrier;
+        X.w.pcg_iters = W.pcg_iters;
+        X.w.pcg_blocks = W.pcg_blocks;
+        X.w.pcg_threads = W.pcg_threads;
+        X.w.idev = W.idev;
+        X.w.node_weight = W.node_weight;
+        X.w.cons = W.cons;
+        // FP32 copy of the free-surface system for the FP32 inner PCG iterations
+        if (dalloc(c, &X.w.sp32, 5 * NC) != cudaSuccess) return fail(GOM_E_NOMEM);
     }
     if (cudaDeviceSynchronize() != cudaSuccess) return fail(GOM_E_CUDA);
     *out = c;
@@ -473,6 +543,8 @@ void gom_destroy(gom_ctx *c) {
     if (c->h_iters) cudaFreeHost(c->h_iters);
     if (c->h_cons) cudaFreeHost(c->h_cons);
     if (c->h_stage) cudaFreeHost(c->h_stage);
+    for (int h = 0; h < 2; ++h)
+        if (c->stage_done[h]) cudaEventDestroy(c->stage_done[h]);
     if (c->x.stream) cudaStreamDestroy(c->x.stream);
     delete c;
 }
@@ -481,6 +553,15 @@ int gom_set_field(gom_ctx *c, int field, const void *host, int64_t count) {
     if (!c || !host || field <= 0 || field >= GOM_F_COUNT) return GOM_E_ARG;
     const FieldDesc &f = c->fields[field];
     if (f.lo == -2 || count != field_count(c->d, f)) return GOM_E_ARG;
+    if (!f.is_int && f.dev_bytes == 4) {
+        // FP32 storage: round the FP64 host array to nearest
+        std::vector<float> tmp((size_t)count);
+        const double *h = (const double *)host;
+        for (int64_t k = 0; k < count; ++k) tmp[k] = (float)h[k];
+        CK(cudaMemcpyAsync(*f.dev, tmp.data(), (size_t)count * 4, cudaMemcpyHostToDevice, c->x.stream));
+        CK(cudaStreamSynchronize(c->x.stream));
+        return GOM_OK;
+    }
     CK(cudaMemcpyAsync(*f.dev, host, (size_t)count * (f.is_int ? 4 : 8), cudaMemcpyHostToDevice, c->x.stream));
     CK(cudaStreamSynchronize(c->x.stream));
     return GOM_OK;
@@ -490,6 +571,14 @@ int gom_get_field(gom_ctx *c, int field, void *host, int64_t count) {
     if (!c || !host || field <= 0 || field >= GOM_F_COUNT) return GOM_E_ARG;
     const FieldDesc &f = c->fields[field];
     if (f.lo == -2 || count != field_count(c->d, f)) return GOM_E_ARG;
+    if (!f.is_int && f.dev_bytes == 4) {
+        std::vector<float> tmp((size_t)count);
+        CK(cudaMemcpyAsync(tmp.data(), *f.dev, (size_t)count * 4, cudaMemcpyDeviceToHost, c->x.stream));
+        CK(cudaStreamSynchronize(c->x.stream));
+        double *h = (double *)host;
+        for (int64_t k = 0; k < count; ++k) h[k] = (double)tmp[k];
+        return GOM_OK;
+    }
     CK(cudaMemcpyAsync(host, *f.dev, (size_t)count * (f.is_int ? 4 : 8), cudaMemcpyDeviceToHost, c->x.stream));
     CK(cudaStreamSynchronize(c->x.stream));
     return GOM_OK;
@@ -515,19 +604,26 @@ int gom_set_forcing(gom_ctx *c, const gom_forcing *fo) {
                  {fo->con_at_ob, c->f_con_ob, (size_t)d.n_ob * 2 * nt},
                  {fo->con_at_qb, c->f_con_qb, (size_t)d.n_qb * 2 * nt},
                  {fo->phi_sw, c->f_phi_sw, (size_t)d.n_cells}};
-    // wait for the previous upload through the staging buffer before overwriting it
-    CK(cudaStreamSynchronize(c->x.stream));
+    // alternate between the two staging halves; wait only until the upload that last used this
+    // half has left it (so one step can be in flight while the next step's forcing is staged)
+    int h = c->stage_half;
+    c->stage_half ^= 1;
+    double *stage = c->h_stage + (size_t)h * c->stage_len;
+    CK(cudaEventSynchronize(c->stage_done[h]));
     size_t off = 0;
     for (auto &it : items) {
         if (!it.src || it.n == 0) continue;
         if (off + it.n > c->stage_len) {
+            // larger than the staging half: copied straight from the caller's buffer (synchronous)
             CK(cudaMemcpyAsync(it.dst, it.src, it.n * 8, cudaMemcpyHostToDevice, c->x.stream));
+            CK(cudaStreamSynchronize(c->x.stream));
             continue;
         }
-        std::memcpy(c->h_stage + off, it.src, it.n * 8);
-        CK(cudaMemcpyAsync(it.dst, c->h_stage + off, it.n * 8, cudaMemcpyHostToDevice, c->x.stream));
+        std::memcpy(stage + off, it.src, it.n * 8);
+        CK(cudaMemcpyAsync(it.dst, stage + off, it.n * 8, cudaMemcpyHostToDevice, c->x.stream));
         off += it.n;
     }
+    CK(cudaEventRecord(c->stage_done[h], c->x.stream));
     return GOM_OK;
 }
 
@@ -554,19 +650,20 @@ int64_t gom_pcg_iterations_total(gom_ctx *c) { return c ? c->pcg_total : 0; }
 
 void *gom_stream(gom_ctx *c) { return c ? (void *)c->x.stream : nullptr; }
 
-int gom_step_bottom_friction(gom_ctx *c) { return run_phase(c, launch_bottom_friction); }
-int gom_step_boundary_velocity(gom_ctx *c) { return run_phase(c, launch_boundary_velocity); }
-int gom_step_advection(gom_ctx *c) { return run_phase(c, launch_advection); }
-int gom_step_momentum(gom_ctx *c) { return run_phase(c, launch_momentum); }
-int gom_step_velocities(gom_ctx *c) { return run_phase(c, launch_velocities); }
-int gom_step_layers(gom_ctx *c) { return run_phase(c, launch_layers); }
-int gom_step_node_velocity(gom_ctx *c) { return run_phase(c, launch_node_velocity); }
-int gom_step_transport(gom_ctx *c) { return run_phase(c, launch_transport); }
-int gom_step_density(gom_ctx *c) { return run_phase(c, launch_density); }
+int gom_step_bottom_friction(gom_ctx *c) { return run_phase(c, GOM_PHASE(launch_bottom_friction)); }
+int gom_step_boundary_velocity(gom_ctx *c) { return run_phase(c, GOM_PHASE(launch_boundary_velocity)); }
+int gom_step_advection(gom_ctx *c) { return run_phase(c, GOM_PHASE(launch_advection)); }
+int gom_step_momentum(gom_ctx *c) { return run_phase(c, GOM_PHASE(launch_momentum)); }
+int gom_step_velocities(gom_ctx *c) { return run_phase(c, GOM_PHASE(launch_velocities)); }
+int gom_step_layers(gom_ctx *c) { return run_phase(c, GOM_PHASE(launch_layers)); }
+int gom_step_node_velocity(gom_ctx *c) { return run_phase(c, GOM_PHASE(launch_node_velocity)); }
+int gom_step_transport(gom_ctx *c) { return run_phase(c, GOM_PHASE(launch_transport)); }
+int gom_step_density(gom_ctx *c) { return run_phase(c, GOM_PHASE(launch_density)); }
+int gom_step_turbulence(gom_ctx *c) { return run_phase(c, GOM_PHASE(launch_turbulence)); }
 
 int gom_step_free_surface(gom_ctx *c, int32_t *pcg_iters) {
     if (!c) return GOM_E_ARG;
-    CK(launch_free_surface(c->x));
+    CK(c->mixed ? launch_free_surface(c->xf) : launch_free_surface(c->x));
     return finish(c, pcg_iters, true);
 }
 
@@ -576,7 +673,7 @@ int gom_step_swap(gom_ctx *c) {
     return finish(c, nullptr, false);
 }
 
-int gom_step_all(gom_ctx *c, int32_t *pcg_iters) {
+int gom_step_launch(gom_ctx *c) {
     if (!c) return GOM_E_ARG;
     // The timestep is captured once into a CUDA graph and replayed: every kernel argument is a
     // device pointer or a constant of the context, and per-step forcing lives in device memory.
@@ -599,12 +696,32 @@ int gom_step_all(gom_ctx *c, int32_t *pcg_iters) {
     }
     if (c->graph) CK(cudaGraphLaunch(c->graph, c->x.stream));
     else CK(enqueue_step(c));
-    return finish(c, pcg_iters, true);
+    CK(cudaMemcpyAsync(c->h_status, c->x.status, sizeof(gom_status), cudaMemcpyDeviceToHost, c->x.stream));
+    CK(cudaMemcpyAsync(c->h_iters, c->x.w.pcg_iters, sizeof(int), cudaMemcpyDeviceToHost, c->x.stream));
+    c->step_pending = true;
+    return GOM_OK;
+}
+
+int gom_step_wait(gom_ctx *c, int32_t *pcg_iters) {
+    if (!c) return GOM_E_ARG;
+    CK(cudaStreamSynchronize(c->x.stream));
+    if (c->step_pending) {
+        c->step_pending = false;
+        c->pcg_total += *c->h_iters;
+        if (pcg_iters) *pcg_iters = *c->h_iters;
+    }
+    return c->h_status->code;
+}
+
+int gom_step_all(gom_ctx *c, int32_t *pcg_iters) {
+    int rc = gom_step_launch(c);
+    if (rc != GOM_OK) return rc;
+    return gom_step_wait(c, pcg_iters);
 }
 
 int gom_conservation(gom_ctx *c, double *volume, double *salt_mass) {
     if (!c) return GOM_E_ARG;
-    CK(launch_conservation(c->x));
+    CK(c->mixed ? launch_conservation(c->xf) : launch_conservation(c->x));
     CK(cudaMemcpyAsync(c->h_cons, c->x.w.cons, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->x.stream));
     CK(cudaStreamSynchronize(c->x.stream));
     if (volume) *volume = c->h_cons[0];

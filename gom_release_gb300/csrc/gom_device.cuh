@@ -55,22 +55,27 @@ struct Geom {
 };
 
 // -------------------------------------------------------------------- state (device)
-struct State {
+// R is the storage type of the layered state: double for the FP64 path (bit-for-bit with the
+// reference restatement), float for the mixed-precision path.  Elevations (the free-surface
+// solution), densities and the river boundary velocity stay double in both.
+template <typename R> struct StateT {
     double *eta_cell, *eta_cell_new, *eta_node;
     int *wetdry_node;
-    double *un_face, *vn_face, *un_face_new, *vn_face_new, *un_elm, *vn_elm;
-    double *wn_cell, *wn_cell_new, *u_node, *v_node, *w_node, *u_face_level, *v_face_level;
-    double *dz_cell, *dz_cell_new, *dzhalf_cell, *dzhalf_cell_new;
-    double *dz_face, *dz_face_new, *dzhalf_face, *dzhalf_face_new;
-    double *dz_node, *dz_node_new, *dzhalf_node, *dzhalf_node_new;
+    R *un_face, *vn_face, *un_face_new, *vn_face_new, *un_elm, *vn_elm;
+    R *wn_cell, *wn_cell_new, *u_node, *v_node, *w_node, *u_face_level, *v_face_level;
+    R *dz_cell, *dz_cell_new, *dzhalf_cell, *dzhalf_cell_new;
+    R *dz_face, *dz_face_new, *dzhalf_face, *dzhalf_face_new;
+    R *dz_node, *dz_node_new, *dzhalf_node, *dzhalf_node_new;
     int *top_cell, *top_face, *top_node;
-    double *ainvg1, *ainvg2, *ainvdz1, *ainvdz2, *kh, *av, *kv;
-    double *salt_cell, *salt_cell_new, *temp_cell, *temp_cell_new, *salt_node, *temp_node, *salt_face, *temp_face;
-    double *rho_cell, *rho_node, *rho_face;
+    R *ainvg1, *ainvg2, *ainvdz1, *ainvdz2, *kh, *av, *kv;
+    R *salt_cell, *salt_cell_new, *temp_cell, *temp_cell_new, *salt_node, *temp_node, *salt_face, *temp_face;
+    double *rho_cell, *rho_node, *rho_face;   // FP64 in both: baroclinic terms difference them
     int *num_sub_elm;
-    double *cdb, *gamma_b, *qu_boundary;
+    R *cdb, *gamma_b;
+    double *qu_boundary;
     int *elm_foot, *elm_near_edge;
 };
+using State = StateT<double>;
 
 // per-step forcing (device copies)
 struct Forcing {
@@ -85,7 +90,8 @@ struct Params {
         kh_0, error_tolerance, delta_z_min, denominator_min_for_matrix;
     int advection_flag, elm_backtrace_flag, elm_sub_iter, elm_min_iter, elm_max_iter, bf_flag, baroclinic_flag,
         ana_density, max_iteration_pcg, transport_flag, trans_sub_iter, h_flux_limiter, v_flux_limiter, is_salt,
-        is_temp, heat_option, test_barrier_phantom_blocks;
+        is_temp, heat_option, test_barrier_phantom_blocks, turbulence_flag;
+    double pp_h1, pp_h2, pp_vdmax1, pp_vdmax2, pp_vdmin1, pp_vdmin2, pp_tdmin;
 };
 
 // -------------------------------------------------------------------- layer indexing
@@ -134,19 +140,18 @@ __device__ __forceinline__ int start_end_node(int k, int i, int j) {
     return v > k ? v - k : v;
 }
 
-// tridiagonal_solver.f90:15-61, one right-hand side held in registers/local memory.
+// tridiagonal_solver.f90:15-61, NRHS right-hand sides held in registers/local memory.
 // Returns false on a zero pivot.
-template <int NRHS>
-__device__ inline bool thomas(int n, const double *a, const double *b, const double *c, double (*rhs)[NRHS],
-                              double *gam) {
-    if (b[0] == 0.0) return false;
-    double den = b[0];
+template <int NRHS, typename R>
+__device__ inline bool thomas(int n, const R *a, const R *b, const R *c, R (*rhs)[NRHS], R *gam) {
+    if (b[0] == R(0)) return false;
+    R den = b[0];
 #pragma unroll
     for (int r = 0; r < NRHS; ++r) rhs[0][r] = rhs[0][r] / den;
     for (int j = 1; j < n; ++j) {
         gam[j] = c[j - 1] / den;
         den = b[j] - a[j] * gam[j];
-        if (den == 0.0) return false;
+        if (den == R(0)) return false;
 #pragma unroll
         for (int r = 0; r < NRHS; ++r) rhs[j][r] = (rhs[j][r] - a[j] * rhs[j - 1][r]) / den;
     }

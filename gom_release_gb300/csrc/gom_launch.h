@@ -6,9 +6,9 @@
 
 namespace gom {
 
-// device work buffers owned by a context
-struct Work {
-    // free surface / PCG
+// device work buffers owned by a context (R: storage type of the layered state)
+template <typename R> struct WorkT {
+    // free surface / PCG (the system, its right-hand side and the solution are always FP64)
     double *sparsem = nullptr;   // (0:4, NC)
     double *rhs = nullptr;       // (NC)
     double *minv = nullptr, *r = nullptr, *s = nullptr, *q = nullptr, *d0 = nullptr, *d1 = nullptr;
@@ -16,48 +16,60 @@ struct Work {
     unsigned *barrier = nullptr;                               // [count, generation]
     int *pcg_iters = nullptr;                                  // device: iterations of the last solve
     int pcg_blocks = 0, pcg_threads = 256;
+    float *sp32 = nullptr;       // mixed precision: FP32 copy of the system (0:4, NC)
     // transport
-    double *con = nullptr, *con2 = nullptr;   // (0:L+1, NC, 2)
-    double *qj = nullptr, *dj = nullptr, *phij = nullptr;       // (L, NF)
-    double *qi = nullptr, *di = nullptr, *phii = nullptr;       // (0:L, NC)
-    double *psij = nullptr;                                     // (L, NF, 2)
-    double *psii = nullptr;                                     // (0:L, NC, 2)
-    double *sa1 = nullptr, *sa2 = nullptr;                      // (L, NC, 2) limiter sums per layer
-    double *obk = nullptr, *qbk = nullptr;                      // (L, NOB, 2), (L, NQB, 2)
+    R *con = nullptr, *con2 = nullptr;        // (0:L+1, NC, 2)
+    R *qj = nullptr, *dj = nullptr, *phij = nullptr;            // (L, NF)
+    R *qi = nullptr, *di = nullptr, *phii = nullptr;            // (0:L, NC)
+    R *psij = nullptr;                                          // (L, NF, 2)
+    R *psii = nullptr;                                          // (0:L, NC, 2)
+    R *sa1 = nullptr, *sa2 = nullptr;                           // (L, NC, 2) limiter sums per layer
+    R *obk = nullptr, *qbk = nullptr;                           // (L, NOB, 2), (L, NQB, 2)
     // ELM: INT(dev/0.1) per (layer, face) edge
     int *idev = nullptr;
     // node velocities: face-level velocity / face length (0:L, NF), static node weights (NN)
-    double *uflf = nullptr, *vflf = nullptr, *node_weight = nullptr;
+    R *uflf = nullptr, *vflf = nullptr;
+    double *node_weight = nullptr;
+    // turbulence closure: face diffusivity per interface (0:L, NF)
+    R *kvf = nullptr;
     // conservation
     double *cons = nullptr;                                     // [volume, salt]
 };
+using Work = WorkT<double>;
 
-struct Launch {
+template <typename R> struct LaunchT {
     Geom g;
-    State s;
+    StateT<R> s;
     Forcing f;
     Params p;
-    Work w;
+    WorkT<R> w;
     gom_status *status = nullptr;   // device
     cudaStream_t stream = nullptr;
     int num_sms = 0;
 };
+using Launch = LaunchT<double>;
 
-cudaError_t launch_bottom_friction(const Launch &x);
-cudaError_t launch_boundary_velocity(const Launch &x);
-cudaError_t launch_advection(const Launch &x);
-cudaError_t launch_momentum(const Launch &x);
-cudaError_t launch_free_surface(const Launch &x);
-cudaError_t launch_velocities(const Launch &x);
-cudaError_t launch_layers(const Launch &x);
-cudaError_t launch_node_velocity(const Launch &x);
-cudaError_t launch_transport(const Launch &x);
-cudaError_t launch_density(const Launch &x);
-cudaError_t launch_conservation(const Launch &x);
+template <typename R> cudaError_t launch_bottom_friction(const LaunchT<R> &x);
+template <typename R> cudaError_t launch_boundary_velocity(const LaunchT<R> &x);
+template <typename R> cudaError_t launch_advection(const LaunchT<R> &x);
+template <typename R> cudaError_t launch_momentum(const LaunchT<R> &x);
+template <typename R> cudaError_t launch_free_surface(const LaunchT<R> &x);
+template <typename R> cudaError_t launch_velocities(const LaunchT<R> &x);
+template <typename R> cudaError_t launch_layers(const LaunchT<R> &x);
+template <typename R> cudaError_t launch_node_velocity(const LaunchT<R> &x);
+template <typename R> cudaError_t launch_transport(const LaunchT<R> &x);
+template <typename R> cudaError_t launch_density(const LaunchT<R> &x);
+template <typename R> cudaError_t launch_turbulence(const LaunchT<R> &x);
+template <typename R> cudaError_t launch_conservation(const LaunchT<R> &x);
 
 // cooperative PCG set-up (grid size from occupancy); called once per context
-cudaError_t pcg_configure(Launch &x, int device);
+template <typename R> cudaError_t pcg_configure(LaunchT<R> &x, int device);
 // static per-node weights of calculate_velocity_at_node.f90:103; called once per context
-cudaError_t launch_node_weights(const Launch &x);
+template <typename R> cudaError_t launch_node_weights(const LaunchT<R> &x);
+
+// explicit instantiations live in the kernel files
+#define GOM_INSTANTIATE_LAUNCH(fn)                              \
+    template cudaError_t fn<double>(const LaunchT<double> &x); \
+    template cudaError_t fn<float>(const LaunchT<float> &x);
 
 }  // namespace gom

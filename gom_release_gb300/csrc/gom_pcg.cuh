@@ -194,6 +194,162 @@ __global__ void __launch_bounds__(PCG_THREADS) k_pcg(PcgArgs a) {
     if (blockIdx.x == 0 && threadIdx.x == 0) *a.iters = iters;
 }
 
+// -------------------------------------------------------------------- mixed precision
+// FP32 inner PCG iterations inside FP64 iterative refinement.  Each refinement step forms the
+// true residual r = b - A x of the FP64 system in FP64 and its Jacobi norm delta = r^T M^-1 r;
+// the stop test is the reference's, sqrt(delta^2 / delta_0^2) < tol, on that FP64 residual
+// (delta_0 of the initial guess).  The correction equation A e = r is then solved by PCG in FP32
+// (FP32 copy of the system, FP32 vectors) from e = 0 until its own ratio falls below what the
+// outer test still needs, bounded below by what FP32 vectors can reach; every inner step adds its
+// FP32 increment alpha*d to the FP64 solution x.  iters counts inner iterations; maxit bounds them.
+struct PcgMixedArgs {
+    Geom g;
+    const double *sp, *b;
+    double *x;
+    float *sp32;                          // (5, NC) FP32 copy of the system
+    float *minv, *r, *s, *q, *dA, *dB;
+    double *pdq, *pdelta;
+    unsigned *bar;
+    int *iters;
+    int maxit;
+    double tol;
+    gom_status *st;
+    unsigned phantom;
+};
+
+// block reduction of one float (accumulated in FP32 within the block)
+template <int THREADS>
+__device__ __forceinline__ float block_sumf(float v, double *sh) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float *shf = reinterpret_cast<float *>(sh);
+    if (lane == 0) shf[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        float t = lane < THREADS / 32 ? shf[lane] : 0.0f;
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+        if (lane == 0) shf[68] = t;
+    }
+    __syncthreads();
+    float r = shf[68];
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(PCG_THREADS) k_pcg_mixed(PcgMixedArgs a) {
+    __shared__ double sh[40];
+    const Geom &g = a.g;
+    const int n = g.NC;
+    const unsigned nblocks = gridDim.x + a.phantom;
+    const long stride = (long)gridDim.x * blockDim.x;
+    const long t0 = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const float FP32_FLOOR = 1e-10f;   // inner ratio below which FP32 recurrences stop paying
+    for (long i = t0; i < n; i += stride) {
+        const double *row = a.sp + i * 5;
+        float *row32 = a.sp32 + i * 5;
+        for (int l = 0; l < 5; ++l) row32[l] = (float)row[l];
+        a.minv[i] = (float)(1.0 / row[0]);
+    }
+    double delta_0 = 0.0;
+    int iters = 0;
+    for (int outer = 0;; ++outer) {
+        // true residual r = b - A x and its Jacobi norm in FP64; the FP32 residual, d = M^-1 r and
+        // the inner r^T d in the same pass (the previous inner step's barrier ordered the x update)
+        double loc = 0.0;
+        float floc = 0.0f;
+        for (long i = t0; i < n; i += stride) {
+            const double *row = a.sp + i * 5;
+            int cell = (int)i + 1;
+            double sum = row[0] * a.x[i];
+            int tq = g.tri_or_quad[i];
+            for (int l = 1; l <= tq; ++l) {
+                int nb = g.cell_adj(l, cell);
+                if (nb != 0) sum = fma(row[l], a.x[nb - 1], sum);
+            }
+            double ri = a.b[i] - sum;
+            loc = fma(ri, ri / row[0], loc);
+            float rf = (float)ri;
+            float df = a.minv[i] * rf;
+            a.r[i] = rf;
+            a.dA[i] = df;
+            floc = fmaf(rf, df, floc);
+        }
+        double bs = block_sum<PCG_THREADS>(loc, sh);
+        float fbs = block_sumf<PCG_THREADS>(floc, sh);
+        if (threadIdx.x == 0) {
+            a.pdelta[blockIdx.x] = bs;
+            a.pdq[blockIdx.x] = (double)fbs;
+        }
+        if (!grid_barrier(a.bar, nblocks, a.st)) return;
+        double delta_true = sum_partials(a.pdelta, gridDim.x, sh);
+        float delta_new = (float)sum_partials(a.pdq, gridDim.x, sh);
+        if (outer == 0) {
+            delta_0 = delta_true;
+            if (delta_0 == 0.0) break;
+        } else if (sqrt(delta_true * delta_true / (delta_0 * delta_0)) < a.tol) {
+            break;
+        }
+        if (iters >= a.maxit || !(delta_new > 0.0f)) break;
+        const float inner_tol = fmaxf((float)(0.25 * a.tol * delta_0 / delta_true), FP32_FLOOR);
+        const float din0 = delta_new;
+        float beta = 0.0f;
+        float *dcur = a.dA, *dnext = a.dB;
+        bool first = true;
+        while (iters < a.maxit) {
+            if (failed(a.st)) return;
+            floc = 0.0f;
+            for (long i = t0; i < n; i += stride) {
+                const float *row = a.sp32 + i * 5;
+                int cell = (int)i + 1;
+                float di = first ? dcur[i] : fmaf(beta, dcur[i], a.s[i]);
+                float sum = row[0] * di;
+                int tq = g.tri_or_quad[i];
+                for (int l = 1; l <= tq; ++l) {
+                    int nb = g.cell_adj(l, cell);
+                    if (nb != 0) {
+                        float dn = first ? dcur[nb - 1] : fmaf(beta, dcur[nb - 1], a.s[nb - 1]);
+                        sum = fmaf(row[l], dn, sum);
+                    }
+                }
+                if (!first) dnext[i] = di;
+                a.q[i] = sum;
+                floc = fmaf(di, sum, floc);
+            }
+            fbs = block_sumf<PCG_THREADS>(floc, sh);
+            if (threadIdx.x == 0) a.pdq[blockIdx.x] = (double)fbs;
+            if (!grid_barrier(a.bar, nblocks, a.st)) return;
+            float dq = (float)sum_partials(a.pdq, gridDim.x, sh);
+            float alpha = delta_new / dq;
+            float *dv = first ? dcur : dnext;
+            floc = 0.0f;
+            for (long i = t0; i < n; i += stride) {
+                float di = dv[i];
+                a.x[i] = a.x[i] + (double)(alpha * di);
+                float ri = fmaf(-alpha, a.q[i], a.r[i]);
+                a.r[i] = ri;
+                float si = a.minv[i] * ri;
+                a.s[i] = si;
+                floc = fmaf(ri, si, floc);
+            }
+            fbs = block_sumf<PCG_THREADS>(floc, sh);
+            if (threadIdx.x == 0) a.pdelta[blockIdx.x] = (double)fbs;
+            if (!grid_barrier(a.bar, nblocks, a.st)) return;
+            float delta_old = delta_new;
+            delta_new = (float)sum_partials(a.pdelta, gridDim.x, sh);
+            beta = delta_new / delta_old;
+            if (!first) {
+                float *t = dcur;
+                dcur = dnext;
+                dnext = t;
+            }
+            first = false;
+            ++iters;
+            if (delta_new < inner_tol * din0 || !(delta_new > 0.0f)) break;
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *a.iters = iters;
+}
+
 // grid of the cooperative launch: enough blocks for one row per thread, at most two resident
 // blocks per SM (and never more than the occupancy allows)
 inline int pcg_blocks_for(long n_rows, int per_sm, int num_sms) {

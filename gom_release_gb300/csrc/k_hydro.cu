@@ -13,7 +13,7 @@ namespace gom {
 
 // ============================================================================================
 // calculate_bottom_friction.f90:21-63; bf_flag 3 is the constant-Cd extension. One thread per face.
-__global__ void k_bottom_friction(Geom g, State s, Params p) {
+template <typename R> __global__ void k_bottom_friction(Geom g, StateT<R> s, Params p) {
     int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
     if (j > g.NF) return;
     const int L = g.L;
@@ -34,17 +34,17 @@ __global__ void k_bottom_friction(Geom g, State s, Params p) {
         double u = s.un_face[ix(k, j, L)], v = s.vn_face[ix(k, j, L)];
         gb = cdb * sqrt(u * u + v * v);
     }
-    s.cdb[j - 1] = cdb;
-    s.gamma_b[j - 1] = gb;
+    s.cdb[j - 1] = (R)cdb;
+    s.gamma_b[j - 1] = (R)gb;
 }
 
-cudaError_t launch_bottom_friction(const Launch &x) {
+template <typename R> cudaError_t launch_bottom_friction(const LaunchT<R> &x) {
     k_bottom_friction<<<blocks_for(x.g.NF, 256), 256, 0, x.stream>>>(x.g, x.s, x.p);
     return cudaGetLastError();
 }
 
 // compute_boundary_velocity.f90:71-92. One thread per river cell.
-__global__ void k_boundary_velocity(Geom g, State s, Forcing f, Params p, gom_status *st) {
+template <typename R> __global__ void k_boundary_velocity(Geom g, StateT<R> s, Forcing f, Params p, gom_status *st) {
     int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     if (i > g.NQB) return;
     int j = g.qb_face[i - 1];
@@ -57,7 +57,7 @@ __global__ void k_boundary_velocity(Geom g, State s, Forcing f, Params p, gom_st
     s.qu_boundary[i - 1] = -f.q_add[i - 1] / (g.face_length[j - 1] * depth);
 }
 
-cudaError_t launch_boundary_velocity(const Launch &x) {
+template <typename R> cudaError_t launch_boundary_velocity(const LaunchT<R> &x) {
     if (x.g.NQB == 0) return cudaSuccess;
     k_boundary_velocity<<<blocks_for(x.g.NQB, 128), 128, 0, x.stream>>>(x.g, x.s, x.f, x.p, x.status);
     return cudaGetLastError();
@@ -155,7 +155,7 @@ __device__ int bilinear_interpolation(double x1, double x2, double x3, double x4
     return 0;
 }
 
-__device__ __forceinline__ int top_el(const State &s, int e) { return e == 0 ? 0 : s.top_cell[e - 1]; }
+template <typename R> __device__ __forceinline__ int top_el(const StateT<R> &s, int e) { return e == 0 ? 0 : s.top_cell[e - 1]; }
 
 __device__ __forceinline__ double area_sum(const Geom &g, int nel, double x, double y) {
     int tq = g.tri_or_quad[nel - 1];
@@ -168,7 +168,8 @@ __device__ __forceinline__ double area_sum(const Geom &g, int nel, double x, dou
 }
 
 // search_straight_line.f90:15-399 (mode 1). Returns 0 or a GOM_ELM_* site.
-__device__ int search_straight_line(const Geom &g, const State &s, const Params &p, int &nnel, int &jlev, double time,
+template <typename R>
+__device__ int search_straight_line(const Geom &g, const StateT<R> &s, const Params &p, int &nnel, int &jlev, double time,
                                     double x0, double y0, double z0, double &xt, double &yt, double &zt, int &nfl) {
     const double small_06 = F(1.e-6f);
     const double MSL = p.msl;
@@ -289,7 +290,8 @@ __device__ double edge_distance(const Geom &g, int nel, double x, double y) {
 }
 
 // ELM_backtrace_v1.f90:40-200 (mode 1)
-__device__ int elm_backtrace(const Geom &g, const State &s, const Params &p, int bt_step, double bt_dt, double &uu,
+template <typename R>
+__device__ int elm_backtrace(const Geom &g, const StateT<R> &s, const Params &p, int bt_step, double bt_dt, double &uu,
                              double &vv, double &ww, double x0, double y0, double z0, int &nnel, int &jlev,
                              int &near_edge) {
     const double small_06 = F(1.e-6f);
@@ -365,7 +367,7 @@ __device__ int elm_backtrace(const Geom &g, const State &s, const Params &p, int
 // INT(2*w*dt/delta_z_min) are 0 whenever the operands lie more than 1e-9 below the thresholds;
 // that usual case is decided from squared quantities without square roots or divisions, every
 // other case is computed exactly as the reference does.
-__global__ void k_elm_edge_dev(Geom g, State s, Params p, int *idev) {
+template <typename R> __global__ void k_elm_edge_dev(Geom g, StateT<R> s, Params p, int *idev) {
     unsigned t = flat_tid();
     const int L = g.L;
     if (t >= (unsigned)g.NF * L) return;
@@ -395,7 +397,7 @@ __global__ void k_elm_edge_dev(Geom g, State s, Params p, int *idev) {
 
 __device__ __forceinline__ int wrap_edge(int l, int tq) { return l <= 0 ? l + tq : l; }
 
-__global__ void k_elm_substeps(Geom g, State s, Params p, const int *idev) {
+template <typename R> __global__ void k_elm_substeps(Geom g, StateT<R> s, Params p, const int *idev) {
     unsigned t = flat_tid();
     const int L = g.L;
     if (t >= (unsigned)g.NN * L) return;
@@ -424,7 +426,8 @@ __global__ void k_elm_substeps(Geom g, State s, Params p, const int *idev) {
 
 // solve_nonlinear_advection.f90:94-201: one thread per face walks the face's wet layers (a warp's
 // FP64 work is spread over 32 faces instead of idling on dry layers)
-__device__ void elm_face_layer(const Geom &g, const State &s, const Params &p, gom_status *st, int j, int k, int ie0,
+template <typename R>
+__device__ void elm_face_layer(const Geom &g, const StateT<R> &s, const Params &p, gom_status *st, int j, int k, int ie0,
                                int n1, int n2, double ct, double sn) {
     const int L = g.L;
     long o = ix(k, j, L);
@@ -440,8 +443,8 @@ __device__ void elm_face_layer(const Geom &g, const State &s, const Params &p, g
     double ww = (wdown + wup) * 0.5;
     double vmag = sqrt(uu * uu + vv * vv + ww * ww);
     if (vmag <= F(1.e-4f)) {
-        s.un_elm[o] = unf;
-        s.vn_elm[o] = vnf;
+        s.un_elm[o] = s.un_face[o];
+        s.vn_elm[o] = s.vn_face[o];
         return;
     }
     int bt_step = (int)((double)(s.num_sub_elm[ix(k, n1, L)] + s.num_sub_elm[ix(k, n2, L)]) * 0.5);
@@ -454,11 +457,11 @@ __device__ void elm_face_layer(const Geom &g, const State &s, const Params &p, g
     }
     s.elm_foot[o] = nnel;
     s.elm_near_edge[o] = near;
-    s.un_elm[o] = uu * ct + vv * sn;
-    s.vn_elm[o] = -uu * sn + vv * ct;
+    s.un_elm[o] = (R)(uu * ct + vv * sn);
+    s.vn_elm[o] = (R)(-uu * sn + vv * ct);
 }
 
-__global__ void k_elm_faces(Geom g, State s, Params p, gom_status *st) {
+template <typename R> __global__ void k_elm_faces(Geom g, StateT<R> s, Params p, gom_status *st) {
     unsigned tid = flat_tid();
     if (tid >= (unsigned)g.NF) return;
     int j = g.face_order[tid];
@@ -469,8 +472,8 @@ __global__ void k_elm_faces(Geom g, State s, Params p, gom_status *st) {
         s.elm_foot[o] = 0;
         s.elm_near_edge[o] = 0;
         if (k < b || k > tf) {
-            s.un_elm[o] = 0.0;
-            s.vn_elm[o] = 0.0;
+            s.un_elm[o] = R(0);
+            s.vn_elm[o] = R(0);
         }
     }
     if (tf < b) return;
@@ -492,7 +495,7 @@ __global__ void k_elm_faces(Geom g, State s, Params p, gom_status *st) {
     for (int k = b; k <= tf; ++k) elm_face_layer(g, s, p, st, j, k, ie0, n1, n2, ct, sn);
 }
 
-__global__ void k_copy_elm(Geom g, State s) {
+template <typename R> __global__ void k_copy_elm(Geom g, StateT<R> s) {
     unsigned t = flat_tid();
     if (t >= (unsigned)g.NF * g.L) return;
     s.un_elm[t] = s.un_face[t];
@@ -501,7 +504,7 @@ __global__ void k_copy_elm(Geom g, State s) {
     s.elm_near_edge[t] = 0;
 }
 
-cudaError_t launch_advection(const Launch &x) {
+template <typename R> cudaError_t launch_advection(const LaunchT<R> &x) {
     long nfl = (long)x.g.NF * x.g.L;
     if (x.p.advection_flag == 0) {
         k_copy_elm<<<blocks_for(nfl, 256), 256, 0, x.stream>>>(x.g, x.s);
@@ -522,7 +525,9 @@ cudaError_t launch_advection(const Launch &x) {
 // rtemp0 of the reference carries over between faces: on a boundary face whose nodes are not both
 // wet, the air-pressure term at :503-505 reuses the last rtemp0 assigned for an earlier wet face
 // (serial order).  prev_rtemp0() restates that by walking back to the nearest such face.
-__device__ double face_final_rtemp0(const Geom &g, const State &s, const Forcing &f, const Params &p, int j, bool &known) {
+template <typename R>
+__device__ double face_final_rtemp0(const Geom &g, const StateT<R> &s, const Forcing &f, const Params &p, int j,
+                                    bool &known) {
     known = true;
     int a2 = g.face_cell(2, j);
     if (a2 != 0) {
@@ -541,7 +546,8 @@ __device__ double face_final_rtemp0(const Geom &g, const State &s, const Forcing
     return 0.0;
 }
 
-__device__ double prev_rtemp0(const Geom &g, const State &s, const Forcing &f, const Params &p, int j) {
+template <typename R>
+__device__ double prev_rtemp0(const Geom &g, const StateT<R> &s, const Forcing &f, const Params &p, int j) {
     for (int jj = j - 1; jj >= 1; --jj) {
         if (s.top_face[jj - 1] == 0) continue;
         bool known;
@@ -551,7 +557,11 @@ __device__ double prev_rtemp0(const Geom &g, const State &s, const Forcing &f, c
     return 0.0;
 }
 
-__global__ void __launch_bounds__(128) k_momentum(Geom g, State s, Forcing f, Params p, gom_status *st) {
+// Per-face terms (elevation gradients, air pressure, geometry) are formed in FP64 once per face
+// and rounded to R; the layer loop, the Smagorinsky diffusion, the baroclinic integral and the
+// tridiagonal solve run in R.  With R = double every expression is the reference's.
+template <typename R>
+__global__ void __launch_bounds__(128) k_momentum(Geom g, StateT<R> s, Forcing f, Params p, gom_status *st) {
     unsigned tid = flat_tid();
     if (tid >= (unsigned)g.NF) return;
     int j = g.face_order[tid];
@@ -559,6 +569,7 @@ __global__ void __launch_bounds__(128) k_momentum(Geom g, State s, Forcing f, Pa
     int tj = s.top_face[j - 1];
     if (tj == 0) return;
     const double dt = p.dt, gravity = p.gravity, theta = p.theta;
+    const R dtR = (R)dt;
     int bj = g.bottom_face[j - 1];
     int nvl = tj - bj + 1;
     int node1 = g.face_node(1, j), node2 = g.face_node(2, j);
@@ -566,23 +577,24 @@ __global__ void __launch_bounds__(128) k_momentum(Geom g, State s, Forcing f, Pa
     int btype = g.boundary_type_of_face[j - 1];
     const double dj = g.delta_j[j - 1], fl = g.face_length[j - 1];
     const double ct = g.cos_theta[j - 1], sn = g.sin_theta[j - 1], ct2 = g.cos_theta2[j - 1], sn2 = g.sin_theta2[j - 1];
-    const double cor = g.coriolis_factor[j - 1];
-    double a[GOM_MAXL], bd[GOM_MAXL], cu[GOM_MAXL], gam[GOM_MAXL];
-    double rhs[GOM_MAXL][3];
+    const R ctR = (R)ct, snR = (R)sn, ct2R = (R)ct2, sn2R = (R)sn2;
+    const R cordt = (R)(g.coriolis_factor[j - 1] * dt);
+    R a[GOM_MAXL], bd[GOM_MAXL], cu[GOM_MAXL], gam[GOM_MAXL];
+    R rhs[GOM_MAXL][3];
     // :120-169
     for (int k = bj + 1; k <= tj - 1; ++k) {
         int kk = tj - k + 1;
-        a[kk - 1] = -dt * s.av[ix0(k, j, L)] / s.dzhalf_face[ix0(k, j, L)];
-        cu[kk - 1] = -dt * s.av[ix0(k - 1, j, L)] / s.dzhalf_face[ix0(k - 1, j, L)];
+        a[kk - 1] = -dtR * s.av[ix0(k, j, L)] / s.dzhalf_face[ix0(k, j, L)];
+        cu[kk - 1] = -dtR * s.av[ix0(k - 1, j, L)] / s.dzhalf_face[ix0(k - 1, j, L)];
         bd[kk - 1] = -a[kk - 1] + s.dz_face[ix(k, j, L)] - cu[kk - 1];
     }
     if (tj == bj) {
-        bd[0] = s.dz_face[ix(tj, j, L)] + s.gamma_b[j - 1] * dt;
+        bd[0] = s.dz_face[ix(tj, j, L)] + s.gamma_b[j - 1] * dtR;
     } else {
-        cu[0] = -dt * s.av[ix0(tj - 1, j, L)] / s.dzhalf_face[ix0(tj - 1, j, L)];
-        bd[0] = f.gamma_t[j - 1] * dt + s.dz_face[ix(tj, j, L)] - cu[0];
-        a[nvl - 1] = -dt * s.av[ix0(bj, j, L)] / s.dzhalf_face[ix0(bj, j, L)];
-        bd[nvl - 1] = -a[nvl - 1] + s.dz_face[ix(bj, j, L)] + s.gamma_b[j - 1] * dt;
+        cu[0] = -dtR * s.av[ix0(tj - 1, j, L)] / s.dzhalf_face[ix0(tj - 1, j, L)];
+        bd[0] = (R)f.gamma_t[j - 1] * dtR + s.dz_face[ix(tj, j, L)] - cu[0];
+        a[nvl - 1] = -dtR * s.av[ix0(bj, j, L)] / s.dzhalf_face[ix0(bj, j, L)];
+        bd[nvl - 1] = -a[nvl - 1] + s.dz_face[ix(bj, j, L)] + s.gamma_b[j - 1] * dtR;
     }
     bool wet_nodes = s.wetdry_node[node1 - 1] == 0 && s.wetdry_node[node2 - 1] == 0;
     double eta_n1 = s.eta_node[node1 - 1], eta_n2 = s.eta_node[node2 - 1];
@@ -597,7 +609,7 @@ __global__ void __launch_bounds__(128) k_momentum(Geom g, State s, Forcing f, Pa
         rt0_air = prev_rtemp0(g, s, f, p, j);
     }
     double rtemp3_air = -dt / p.rho_o * ((f.air_p[node2 - 1] - f.air_p[node1 - 1]) / fl);
-    const double c069 = F(0.69f);
+    const R c069 = (R)F(0.69f);
     int ibnd = g.isflowside3[j - 1];
     double eta1 = s.eta_cell[a1 - 1];
     double eta2 = a2 != 0 ? s.eta_cell[a2 - 1] : 0.0;
@@ -617,112 +629,119 @@ __global__ void __launch_bounds__(128) k_momentum(Geom g, State s, Forcing f, Pa
         bt_rtemp1 = gravity * dt / dj * (1.0 - theta) * (f.eta_at_ob_old[ie - 1] - eta1);
     }
     double along_rtemp0 = wet_nodes ? gravity * dt / fl * (1.0 - theta) * (eta_n2 - eta_n1) : 0.0;
-    double along = (btype == 0) ? (along_rtemp0 + bt_rtemp2) : along_rtemp0;
-    double air1 = rt0_air * ct2, air2 = rtemp3_air + rt0_air * sn2;
-    double bc_dj = -gravity * dt / (p.rho_o * dj), bc_fl = -gravity * dt / (p.rho_o * fl);
-    double fl2 = fl * fl;
-    double rl1 = 0.0, rl2 = 0.0, inv_tq1 = 0.0, inv_tq2 = 0.0;
+    const R bt1 = (R)bt_rtemp1;
+    const R along = (R)((btype == 0) ? (along_rtemp0 + bt_rtemp2) : along_rtemp0);
+    const R air1 = (R)(rt0_air * ct2), air2 = (R)(rtemp3_air + rt0_air * sn2);
+    const R bc_dj = (R)(-gravity * dt / (p.rho_o * dj)), bc_fl = (R)(-gravity * dt / (p.rho_o * fl));
+    const R djR = (R)dj, flR = (R)fl, fl2 = (R)(fl * fl);
+    const R gdt0 = (R)(gravity * dt);
+    const R wsn = (R)(dt * f.wind_stress_normal[j - 1]), wst = (R)(dt * f.wind_stress_tangnt[j - 1]);
+    const R qub = ibnd > 0 ? (R)s.qu_boundary[ibnd - 1] : R(0);
+    const R smag = (R)p.smagorinsky, ah0 = (R)p.ah_0, kh0 = (R)p.kh_0, area1 = (R)g.area[a1 - 1];
+    R rl1 = R(0), rl2 = R(0), inv_tq1 = R(0), inv_tq2 = R(0);
     int tq1 = 0, tq2 = 0;
     if (a2 != 0) {
         double ddx = g.x_cell[a1 - 1] - g.x_face[j - 1], ddy = g.y_cell[a1 - 1] - g.y_face[j - 1];
-        rl1 = sqrt(ddx * ddx + ddy * ddy);
+        rl1 = (R)sqrt(ddx * ddx + ddy * ddy);
         ddx = g.x_cell[a2 - 1] - g.x_face[j - 1];
         ddy = g.y_cell[a2 - 1] - g.y_face[j - 1];
-        rl2 = sqrt(ddx * ddx + ddy * ddy);
+        rl2 = (R)sqrt(ddx * ddx + ddy * ddy);
         tq1 = g.tri_or_quad[a1 - 1];
         tq2 = g.tri_or_quad[a2 - 1];
-        inv_tq1 = tq1 == 4 ? 0.25 : 0.0;   // x/4 == x*0.25 exactly; triangles divide
-        inv_tq2 = tq2 == 4 ? 0.25 : 0.0;
+        inv_tq1 = tq1 == 4 ? R(0.25) : R(0);   // x/4 == x*0.25 exactly; triangles divide
+        inv_tq2 = tq2 == 4 ? R(0.25) : R(0);
     }
-    const double spin = f.scal[2];
+    const R spin = (R)f.scal[2];
+    const R half = R(0.5);
     for (int k = 1; k <= nvl; ++k) {
         int kk = tj - k + 1;
-        double dzk = s.dz_face[ix(kk, j, L)];
-        double unk = s.un_face[ix(kk, j, L)], vnk = s.vn_face[ix(kk, j, L)];
-        double G1 = dzk * (s.un_elm[ix(kk, j, L)] + cor * dt * vnk);
-        double G2 = dzk * (s.vn_elm[ix(kk, j, L)] - cor * dt * unk);
+        R dzk = s.dz_face[ix(kk, j, L)];
+        R unk = s.un_face[ix(kk, j, L)], vnk = s.vn_face[ix(kk, j, L)];
+        R G1 = dzk * (s.un_elm[ix(kk, j, L)] + cordt * vnk);
+        R G2 = dzk * (s.vn_elm[ix(kk, j, L)] - cordt * unk);
         if (a2 != 0) {
             // :269-344 Smagorinsky horizontal diffusion
-            double tmp[12];
+            R tmp[12];
             for (int l = 1; l <= 2; ++l) {
                 int nd = g.face_node(l, j);
-                double ut = (s.u_node[ix0(kk, nd, L)] + s.u_node[ix0(kk - 1, nd, L)]) * 0.5;
-                double vt = (s.v_node[ix0(kk, nd, L)] + s.v_node[ix0(kk - 1, nd, L)]) * 0.5;
-                tmp[2 * l - 2] = ut * ct + vt * sn;
-                tmp[2 * l - 1] = -ut * sn + vt * ct;
+                R ut = (s.u_node[ix0(kk, nd, L)] + s.u_node[ix0(kk - 1, nd, L)]) * half;
+                R vt = (s.v_node[ix0(kk, nd, L)] + s.v_node[ix0(kk - 1, nd, L)]) * half;
+                tmp[2 * l - 2] = ut * ctR + vt * snR;
+                tmp[2 * l - 1] = -ut * snR + vt * ctR;
             }
             for (int l = 1; l <= 2; ++l) {
                 int ie = l == 1 ? a1 : a2;
                 int tq = l == 1 ? tq1 : tq2;
-                double itq = l == 1 ? inv_tq1 : inv_tq2;
-                double ut = 0.0, vt = 0.0;
+                R itq = l == 1 ? inv_tq1 : inv_tq2;
+                R ut = R(0), vt = R(0);
                 for (int ll = 1; ll <= tq; ++ll) {
                     int nd = g.cell_node(ll, ie);
-                    double uu = (s.u_node[ix0(kk, nd, L)] + s.u_node[ix0(kk - 1, nd, L)]) * 0.5;
-                    double vv = (s.v_node[ix0(kk, nd, L)] + s.v_node[ix0(kk - 1, nd, L)]) * 0.5;
-                    ut = ut + (itq != 0.0 ? uu * itq : uu / tq);
-                    vt = vt + (itq != 0.0 ? vv * itq : vv / tq);
+                    R uu = (s.u_node[ix0(kk, nd, L)] + s.u_node[ix0(kk - 1, nd, L)]) * half;
+                    R vv = (s.v_node[ix0(kk, nd, L)] + s.v_node[ix0(kk - 1, nd, L)]) * half;
+                    ut = ut + (itq != R(0) ? uu * itq : uu / (R)tq);
+                    vt = vt + (itq != R(0) ? vv * itq : vv / (R)tq);
                 }
-                tmp[2 * l + 2] = ut * ct + vt * sn;
-                tmp[2 * l + 3] = -ut * sn + vt * ct;
+                tmp[2 * l + 2] = ut * ctR + vt * snR;
+                tmp[2 * l + 3] = -ut * snR + vt * ctR;
             }
-            double dudx = (tmp[6] - tmp[4]) / dj;
-            double dvdx = (tmp[7] - tmp[5]) / dj;
-            double dudy = (tmp[2] - tmp[0]) / fl;
-            double dvdy = (tmp[3] - tmp[1]) / fl;
-            double sdd = dvdx + dudy;
-            double hdiff = p.smagorinsky * sqrt(dudx * dudx + dvdy * dvdy + 0.5 * (sdd * sdd));
-            double khv = hdiff * g.area[a1 - 1];
-            hdiff = hdiff + p.ah_0;
-            s.kh[ix(k, j, L)] = khv + p.kh_0;
-            double d2udy = 4.0 * (tmp[2] + tmp[0] - 2 * unk) / fl2;
-            double d2vdy = 4.0 * (tmp[3] + tmp[1] - 2 * vnk) / fl2;
+            R dudx = (tmp[6] - tmp[4]) / djR;
+            R dvdx = (tmp[7] - tmp[5]) / djR;
+            R dudy = (tmp[2] - tmp[0]) / flR;
+            R dvdy = (tmp[3] - tmp[1]) / flR;
+            R sdd = dvdx + dudy;
+            R hdiff = smag * sqrt(dudx * dudx + dvdy * dvdy + half * (sdd * sdd));
+            R khv = hdiff * area1;
+            hdiff = hdiff + ah0;
+            s.kh[ix(k, j, L)] = khv + kh0;
+            R d2udy = R(4) * (tmp[2] + tmp[0] - R(2) * unk) / fl2;
+            R d2vdy = R(4) * (tmp[3] + tmp[1] - R(2) * vnk) / fl2;
             tmp[8] = (tmp[4] - unk) / rl1;
             tmp[9] = (tmp[5] - vnk) / rl1;
             tmp[10] = (tmp[6] - unk) / rl2;
             tmp[11] = (tmp[7] - vnk) / rl2;
-            double d2udx = 2.0 * (tmp[8] + tmp[10]) / dj;
-            double d2vdx = 2.0 * (tmp[9] + tmp[11]) / dj;
-            G1 = G1 + dzk * dt * hdiff * (d2udx + d2udy);
-            G2 = G2 + dzk * dt * hdiff * (d2vdx + d2vdy);
+            R d2udx = R(2) * (tmp[8] + tmp[10]) / djR;
+            R d2vdx = R(2) * (tmp[9] + tmp[11]) / djR;
+            G1 = G1 + dzk * dtR * hdiff * (d2udx + d2udy);
+            G2 = G2 + dzk * dtR * hdiff * (d2vdx + d2vdy);
         }
         // :350-397 barotropic gradients at (1-theta)
-        if (btype >= 0) G1 = G1 - dzk * bt_rtemp1;
-        else G1 = 0.0;
+        if (btype >= 0) G1 = G1 - dzk * bt1;
+        else G1 = R(0);
         if (wet_nodes) G2 = G2 - dzk * along;
-        // :400-471 baroclinic pressure gradient
+        // :400-471 baroclinic pressure gradient (density differences formed in FP64)
         if (p.baroclinic_flag == 1) {
-            double sum1 = 0.0, sum2 = 0.0;
+            R sum1 = R(0), sum2 = R(0);
             for (int k2 = kk; k2 <= tj; ++k2) {
-                double dz2 = s.dz_face[ix(k2, j, L)];
+                R dz2 = s.dz_face[ix(k2, j, L)];
                 if (a2 != 0 && k2 >= ba1 && k2 <= ta1 && k2 >= ba2 && k2 <= ta2) {
-                    double dr = s.rho_cell[ix(k2, a2, L)] - s.rho_cell[ix(k2, a1, L)];
-                    sum1 = sum1 + (k2 == kk ? 0.5 * dr : dr) * dz2;
+                    R dr = (R)(s.rho_cell[ix(k2, a2, L)] - s.rho_cell[ix(k2, a1, L)]);
+                    sum1 = sum1 + (k2 == kk ? half * dr : dr) * dz2;
                 }
                 if (k2 >= bn1 && k2 <= tn1 && k2 >= bn2 && k2 <= tn2) {
-                    double dr = s.rho_node[ix(k2, node2, L)] - s.rho_node[ix(k2, node1, L)];
-                    sum2 = sum2 + (k2 == kk ? 0.5 * dr : dr) * dz2;
+                    R dr = (R)(s.rho_node[ix(k2, node2, L)] - s.rho_node[ix(k2, node1, L)]);
+                    sum2 = sum2 + (k2 == kk ? half * dr : dr) * dz2;
                 }
             }
-            double dzrow = s.dz_face[ix(k, j, L)];   // the reference uses the top-down row here
-            double rtemp1 = dzrow * bc_dj * sum1;
-            double rtemp2 = dzrow * bc_fl * sum2;
-            double rtemp3 = rtemp1 * ct2;
-            double rtemp4 = rtemp1 * sn2;
+            R dzrow = s.dz_face[ix(k, j, L)];   // the reference uses the top-down row here
+            R rtemp1 = dzrow * bc_dj * sum1;
+            R rtemp2 = dzrow * bc_fl * sum2;
+            R rtemp3 = rtemp1 * ct2R;
+            R rtemp4 = rtemp1 * sn2R;
             G1 = G1 + rtemp3 * spin;
             G2 = G2 + (rtemp2 + rtemp4) * spin;
         }
         if (k == 1) {
-            G1 = G1 + dt * f.wind_stress_normal[j - 1];
-            G2 = G2 + dt * f.wind_stress_tangnt[j - 1];
+            G1 = G1 + wsn;
+            G2 = G2 + wst;
         }
-        G1 = G1 + c069 * dzk * gravity * dt * 0.0;
-        G2 = G2 + c069 * dzk * gravity * dt * 0.0;
+        // :485-486 tide-generating potential, zero in this build (kept for the signed-zero result)
+        G1 = G1 + c069 * dzk * gdt0 * R(0);
+        G2 = G2 + c069 * dzk * gdt0 * R(0);
         // :490-509 air pressure
         G1 = G1 + dzk * air1;
         G2 = G2 + dzk * air2;
-        if (btype == -1) G1 = 0.0;
-        if (ibnd > 0) G1 = G1 + dzk * s.qu_boundary[ibnd - 1];
+        if (btype == -1) G1 = R(0);
+        if (ibnd > 0) G1 = G1 + dzk * qub;
         rhs[k - 1][0] = G1;
         rhs[k - 1][1] = G2;
         rhs[k - 1][2] = dzk;
@@ -736,37 +755,42 @@ __global__ void __launch_bounds__(128) k_momentum(Geom g, State s, Forcing f, Pa
     for (int k = 1; k <= L; ++k) {
         long o = ix(k, j, L);
         if (k <= nvl) {
-            s.ainvg1[o] = zero_g1 ? 0.0 : rhs[k - 1][0];
+            s.ainvg1[o] = zero_g1 ? R(0) : rhs[k - 1][0];
             s.ainvg2[o] = rhs[k - 1][1];
-            s.ainvdz1[o] = zero_dz1 ? 0.0 : rhs[k - 1][2];
+            s.ainvdz1[o] = zero_dz1 ? R(0) : rhs[k - 1][2];
             s.ainvdz2[o] = rhs[k - 1][2];
         } else {
-            s.ainvg1[o] = 0.0;
-            s.ainvg2[o] = 0.0;
-            s.ainvdz1[o] = 0.0;
-            s.ainvdz2[o] = 0.0;
+            s.ainvg1[o] = R(0);
+            s.ainvg2[o] = R(0);
+            s.ainvdz1[o] = R(0);
+            s.ainvdz2[o] = R(0);
         }
     }
 }
 
-__global__ void k_zero_face_columns(Geom g, State s) {
+template <typename R> __global__ void k_zero_face_columns(Geom g, StateT<R> s) {
     // faces that are dry keep zero results (the reference zeroes all four arrays first)
     unsigned t = flat_tid();
     const int L = g.L;
     if (t >= (unsigned)g.NF * L) return;
     int j = (int)(t / (unsigned)L) + 1;
     if (s.top_face[j - 1] != 0) return;
-    s.ainvg1[t] = 0.0;
-    s.ainvg2[t] = 0.0;
-    s.ainvdz1[t] = 0.0;
-    s.ainvdz2[t] = 0.0;
+    s.ainvg1[t] = R(0);
+    s.ainvg2[t] = R(0);
+    s.ainvdz1[t] = R(0);
+    s.ainvdz2[t] = R(0);
 }
 
-cudaError_t launch_momentum(const Launch &x) {
+template <typename R> cudaError_t launch_momentum(const LaunchT<R> &x) {
     long nfl = (long)x.g.NF * x.g.L;
     k_zero_face_columns<<<blocks_for(nfl, 256), 256, 0, x.stream>>>(x.g, x.s);
     k_momentum<<<blocks_for(x.g.NF, 128), 128, 0, x.stream>>>(x.g, x.s, x.f, x.p, x.status);
     return cudaGetLastError();
 }
+
+GOM_INSTANTIATE_LAUNCH(launch_bottom_friction)
+GOM_INSTANTIATE_LAUNCH(launch_boundary_velocity)
+GOM_INSTANTIATE_LAUNCH(launch_advection)
+GOM_INSTANTIATE_LAUNCH(launch_momentum)
 
 }  // namespace gom

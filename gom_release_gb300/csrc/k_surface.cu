@@ -11,7 +11,9 @@ namespace gom {
 
 // ============================================================================================
 // solve_free_surface_equation.f90:65-214: one thread per cell builds its 5-point row and RHS.
-__global__ void k_fs_assemble(Geom g, State s, Forcing f, Params p, double *sparsem, double *rhs, gom_status *st) {
+// The system and its right-hand side are formed in FP64 whatever the storage type R.
+template <typename R>
+__global__ void k_fs_assemble(Geom g, StateT<R> s, Forcing f, Params p, double *sparsem, double *rhs, gom_status *st) {
     int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     if (i > g.NC) return;
     const int L = g.L;
@@ -32,7 +34,7 @@ __global__ void k_fs_assemble(Geom g, State s, Forcing f, Params p, double *spar
         for (int k = 1; k <= nvl; ++k) {
             int kk = tj + 1 - k;
             double dz = s.dz_face[ix(kk, j, L)];
-            sdz = sdz + dz * s.ainvdz1[ix(k, j, L)];
+            sdz = sdz + dz * (double)s.ainvdz1[ix(k, j, L)];
         }
         double base = gdt2th2 * g.face_length[j - 1] / g.delta_j[j - 1] * sdz;
         double coef = base * g.cos_theta2[j - 1];
@@ -55,8 +57,8 @@ __global__ void k_fs_assemble(Geom g, State s, Forcing f, Params p, double *spar
         for (int k = 1; k <= nvl; ++k) {
             int kk = tj + 1 - k;
             double dz = s.dz_face[ix(kk, j, L)];
-            c1 = c1 + dz * s.un_face[ix(kk, j, L)];
-            c2 = c2 + dz * s.ainvg1[ix(k, j, L)];
+            c1 = c1 + dz * (double)s.un_face[ix(kk, j, L)];
+            c2 = c2 + dz * (double)s.ainvg1[ix(k, j, L)];
         }
         double sgn = (double)g.cell_sign(l, i);
         double fl = g.face_length[j - 1];
@@ -70,7 +72,8 @@ __global__ void k_fs_assemble(Geom g, State s, Forcing f, Params p, double *spar
             if (g.boundary_type_of_face[j - 1] > 0 && tj != 0) {
                 int nvl = tj - g.bottom_face[j - 1] + 1;
                 double sdz = 0.0;
-                for (int k = 1; k <= nvl; ++k) sdz = sdz + s.dz_face[ix(tj + 1 - k, j, L)] * s.ainvdz1[ix(k, j, L)];
+                for (int k = 1; k <= nvl; ++k)
+                    sdz = sdz + (double)s.dz_face[ix(tj + 1 - k, j, L)] * (double)s.ainvdz1[ix(k, j, L)];
                 double base = gdt2th2 * g.face_length[j - 1] / g.delta_j[j - 1] * sdz;
                 r = r + base * f.eta_at_ob_new[obf - 1];
             }
@@ -86,7 +89,7 @@ __global__ void k_fs_assemble(Geom g, State s, Forcing f, Params p, double *spar
 }
 
 // :353-375 node elevation from wet cells; wetdry_node
-__global__ void k_node_eta(Geom g, State s) {
+template <typename R> __global__ void k_node_eta(Geom g, StateT<R> s) {
     int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     if (i > g.NN) return;
     int wd = 0;
@@ -106,7 +109,7 @@ __global__ void k_node_eta(Geom g, State s) {
 }
 
 // :378-394 dry nodes take the mean of their wet neighbours
-__global__ void k_node_eta_dry(Geom g, State s) {
+template <typename R> __global__ void k_node_eta_dry(Geom g, StateT<R> s) {
     int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     if (i > g.NN) return;
     if (s.wetdry_node[i - 1] != 1) return;
@@ -123,10 +126,14 @@ __global__ void k_node_eta_dry(Geom g, State s) {
     if (icount != 0) s.eta_node[i - 1] = sum0 / icount;
 }
 
-cudaError_t pcg_configure(Launch &x, int device) {
-    int per_sm = 0;
+template <typename R> cudaError_t pcg_configure(LaunchT<R> &x, int device) {
+    int per_sm = 0, per_sm_mixed = 0;
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg, PCG_THREADS, 0);
     if (e != cudaSuccess) return e;
+    // every block of the cooperative grid must be resident for either solver
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_mixed, k_pcg_mixed, PCG_THREADS, 0);
+    if (e != cudaSuccess) return e;
+    if (per_sm_mixed < per_sm) per_sm = per_sm_mixed;
     if (per_sm < 1) per_sm = 1;
     int coop = 0;
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device);
@@ -136,11 +143,50 @@ cudaError_t pcg_configure(Launch &x, int device) {
     return cudaSuccess;
 }
 
-cudaError_t launch_free_surface(const Launch &x) {
+template <typename R> cudaError_t launch_free_surface(const LaunchT<R> &x) {
     const Geom &g = x.g;
     k_fs_assemble<<<blocks_for(g.NC, 128), 128, 0, x.stream>>>(x.g, x.s, x.f, x.p, x.w.sparsem, x.w.rhs, x.status);
     cudaError_t e = cudaMemsetAsync(x.w.barrier, 0, 2 * sizeof(unsigned), x.stream);
     if (e != cudaSuccess) return e;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(x.w.pcg_blocks);
+    cfg.blockDim = dim3(x.w.pcg_threads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = x.stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const unsigned phantom = (unsigned)(x.p.test_barrier_phantom_blocks > 0 ? x.p.test_barrier_phantom_blocks : 0);
+    if (x.w.sp32) {
+        // mixed precision: the FP64 work vectors hold the FP32 inner vectors
+        PcgMixedArgs m;
+        m.g = g;
+        m.sp = x.w.sparsem;
+        m.b = x.w.rhs;
+        m.x = x.s.eta_cell_new;
+        m.sp32 = x.w.sp32;
+        m.minv = reinterpret_cast<float *>(x.w.minv);
+        m.r = reinterpret_cast<float *>(x.w.r);
+        m.s = reinterpret_cast<float *>(x.w.s);
+        m.q = reinterpret_cast<float *>(x.w.q);
+        m.dA = reinterpret_cast<float *>(x.w.d0);
+        m.dB = reinterpret_cast<float *>(x.w.d1);
+        m.pdq = x.w.partial_dq;
+        m.pdelta = x.w.partial_delta;
+        m.bar = x.w.barrier;
+        m.iters = x.w.pcg_iters;
+        m.maxit = x.p.max_iteration_pcg;
+        m.tol = x.p.error_tolerance;
+        m.st = x.status;
+        m.phantom = phantom;
+        e = cudaLaunchKernelEx(&cfg, k_pcg_mixed, m);
+        if (e != cudaSuccess) return e;
+        k_node_eta<<<blocks_for(g.NN, 256), 256, 0, x.stream>>>(x.g, x.s);
+        k_node_eta_dry<<<blocks_for(g.NN, 256), 256, 0, x.stream>>>(x.g, x.s);
+        return cudaGetLastError();
+    }
     PcgArgs a;
     a.g = g;
     a.sp = x.w.sparsem;
@@ -159,17 +205,7 @@ cudaError_t launch_free_surface(const Launch &x) {
     a.maxit = x.p.max_iteration_pcg;
     a.tol = x.p.error_tolerance;
     a.st = x.status;
-    a.phantom = (unsigned)(x.p.test_barrier_phantom_blocks > 0 ? x.p.test_barrier_phantom_blocks : 0);
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(x.w.pcg_blocks);
-    cfg.blockDim = dim3(x.w.pcg_threads);
-    cfg.dynamicSmemBytes = 0;
-    cfg.stream = x.stream;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeCooperative;
-    attr[0].val.cooperative = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
+    a.phantom = phantom;
     e = cudaLaunchKernelEx(&cfg, k_pcg, a);
     if (e != cudaSuccess) return e;
     k_node_eta<<<blocks_for(g.NN, 256), 256, 0, x.stream>>>(x.g, x.s);
@@ -178,8 +214,9 @@ cudaError_t launch_free_surface(const Launch &x) {
 }
 
 // ============================================================================================
-// solve_velocities.f90:23-184: one thread per face column
-__global__ void k_face_velocity(Geom g, State s, Forcing f, Params p) {
+// solve_velocities.f90:23-184: one thread per face column.  The elevation gradients are formed
+// in FP64 per face; the per-layer products run in R.
+template <typename R> __global__ void k_face_velocity(Geom g, StateT<R> s, Forcing f, Params p) {
     unsigned tid = flat_tid();
     if (tid >= (unsigned)g.NF) return;
     int j = g.face_order[tid];
@@ -187,8 +224,8 @@ __global__ void k_face_velocity(Geom g, State s, Forcing f, Params p) {
     int tj = s.top_face[j - 1];
     if (tj == 0) {
         for (int k = 1; k <= L; ++k) {
-            s.un_face_new[ix(k, j, L)] = 0.0;
-            s.vn_face_new[ix(k, j, L)] = 0.0;
+            s.un_face_new[ix(k, j, L)] = R(0);
+            s.vn_face_new[ix(k, j, L)] = R(0);
         }
         return;
     }
@@ -204,38 +241,41 @@ __global__ void k_face_velocity(Geom g, State s, Forcing f, Params p) {
     if (btype == 0) dEta = s.eta_cell_new[a2 - 1] - s.eta_cell_new[a1 - 1];
     else if (btype > 0) dEta = f.eta_at_ob_new[g.ob_element_flag[a1 - 1] - 1] - s.eta_cell_new[a1 - 1];
     double dEtaN = s.eta_node[n2 - 1] - s.eta_node[n1 - 1];
+    // theta*g*dt/dj*dEta and theta*g*dt/fl*dEtaN: the layer-independent left factors
+    const R cj = (R)(theta * gravity * dt / dj * dEta), cn = (R)(theta * gravity * dt / fl * dEtaN);
+    const R ct2 = (R)g.cos_theta2[j - 1], sn2 = (R)g.sin_theta2[j - 1];
     for (int k = 1; k <= tj - bj + 1; ++k) {
         int kk = tj + 1 - k;
         long o = ix(kk, j, L), ok = ix(k, j, L);
-        double rtemp2 = 0.0;
+        R rtemp2 = R(0);
         if (btype == -1) {
-            s.un_face_new[o] = 0.0;
+            s.un_face_new[o] = R(0);
         } else if (btype == 0) {
-            double rtemp0 = theta * gravity * dt / dj * dEta * s.ainvdz1[ok];
-            double rtemp1 = rtemp0 * g.cos_theta2[j - 1];
-            rtemp2 = rtemp0 * g.sin_theta2[j - 1];
+            R rtemp0 = cj * s.ainvdz1[ok];
+            R rtemp1 = rtemp0 * ct2;
+            rtemp2 = rtemp0 * sn2;
             s.un_face_new[o] = s.ainvg1[ok] - rtemp1;
         } else {
-            double rtemp0 = theta * gravity * dt / dj * dEta * s.ainvdz1[ok];
+            R rtemp0 = cj * s.ainvdz1[ok];
             s.un_face_new[o] = s.ainvg1[ok] - rtemp0;
         }
         if (wet) {
-            double rtemp1 = theta * gravity * dt / fl * dEtaN * s.ainvdz2[ok];
+            R rtemp1 = cn * s.ainvdz2[ok];
             if (btype == 0) s.vn_face_new[o] = s.ainvg2[ok] - (rtemp1 + rtemp2);
             else s.vn_face_new[o] = s.ainvg2[ok] - rtemp1;
         }
-        if (init_dry) s.vn_face_new[o] = fmax(-5.0, fmin(s.vn_face_new[o], 5.0));
+        if (init_dry) s.vn_face_new[o] = fmax(R(-5), fmin(s.vn_face_new[o], R(5)));
     }
     int ibnd = g.isflowside3[j - 1];
     if (ibnd > 0) {
-        double qu = s.qu_boundary[ibnd - 1];
+        R qu = (R)s.qu_boundary[ibnd - 1];
         for (int k = bj; k <= tj; ++k) s.un_face_new[ix(k, j, L)] = qu;
     }
     for (int k = 1; k <= bj - 1; ++k) {
-        s.un_face_new[ix(k, j, L)] = 0.0;
-        s.vn_face_new[ix(k, j, L)] = 0.0;
+        s.un_face_new[ix(k, j, L)] = R(0);
+        s.vn_face_new[ix(k, j, L)] = R(0);
     }
-    double ut = s.un_face_new[ix(tj, j, L)], vt = s.vn_face_new[ix(tj, j, L)];
+    R ut = s.un_face_new[ix(tj, j, L)], vt = s.vn_face_new[ix(tj, j, L)];
     for (int k = tj + 1; k <= L; ++k) {
         s.un_face_new[ix(k, j, L)] = ut;
         s.vn_face_new[ix(k, j, L)] = vt;
@@ -243,31 +283,31 @@ __global__ void k_face_velocity(Geom g, State s, Forcing f, Params p) {
 }
 
 // solve_velocities.f90:191-258: one thread per cell column
-__global__ void k_cell_w(Geom g, State s) {
+template <typename R> __global__ void k_cell_w(Geom g, StateT<R> s) {
     unsigned tid = flat_tid();
     if (tid >= (unsigned)g.NC) return;
     int i = g.cell_order[tid];
     const int L = g.L;
     int t = s.top_cell[i - 1], b = g.bottom_cell[i - 1];
     if (t == 0) {
-        for (int k = 0; k <= L; ++k) s.wn_cell_new[ix0(k, i, L)] = 0.0;
+        for (int k = 0; k <= L; ++k) s.wn_cell_new[ix0(k, i, L)] = R(0);
         return;
     }
     int tq = g.tri_or_quad[i - 1];
     int fj[4], fb[4], ft[4];
-    double fsl[4];
+    R fsl[4];
     for (int l = 1; l <= tq; ++l) {
         int jt = g.cell_face(l, i);
         fj[l - 1] = jt;
         fb[l - 1] = g.bottom_face[jt - 1];
         ft[l - 1] = s.top_face[jt - 1];
-        fsl[l - 1] = (double)g.cell_sign(l, i) * g.face_length[jt - 1];
+        fsl[l - 1] = (R)((double)g.cell_sign(l, i) * g.face_length[jt - 1]);
     }
-    double ar = g.area[i - 1];
-    double w = 0.0;
-    s.wn_cell_new[ix0(b - 1, i, L)] = 0.0;
+    const R ar = (R)g.area[i - 1];
+    R w = R(0);
+    s.wn_cell_new[ix0(b - 1, i, L)] = R(0);
     for (int k = b; k <= t; ++k) {
-        double sum1 = 0.0;
+        R sum1 = R(0);
         for (int l = 0; l < tq; ++l) {
             if (k >= fb[l] && k <= ft[l])
                 sum1 = sum1 + fsl[l] * s.dz_face[ix(k, fj[l], L)] * s.un_face_new[ix(k, fj[l], L)];
@@ -275,11 +315,11 @@ __global__ void k_cell_w(Geom g, State s) {
         w = w - sum1 / ar;
         s.wn_cell_new[ix0(k, i, L)] = w;
     }
-    for (int k = 0; k <= b - 2; ++k) s.wn_cell_new[ix0(k, i, L)] = 0.0;
+    for (int k = 0; k <= b - 2; ++k) s.wn_cell_new[ix0(k, i, L)] = R(0);
     for (int k = t + 1; k <= L; ++k) s.wn_cell_new[ix0(k, i, L)] = w;
 }
 
-cudaError_t launch_velocities(const Launch &x) {
+template <typename R> cudaError_t launch_velocities(const LaunchT<R> &x) {
     k_face_velocity<<<blocks_for(x.g.NF, 128), 128, 0, x.stream>>>(x.g, x.s, x.f, x.p);
     k_cell_w<<<blocks_for(x.g.NC, 128), 128, 0, x.stream>>>(x.g, x.s);
     return cudaGetLastError();
@@ -288,9 +328,9 @@ cudaError_t launch_velocities(const Launch &x) {
 // ============================================================================================
 // update_vertical_layers_1.f90: new top layers and thicknesses for an entity column.
 // kind 0 = cell (:42-133), 1 = face (:139-198), 2 = node (:204-254)
-template <int KIND>
-__device__ __forceinline__ int new_column(const Geom &g, const Params &p, double h, double eta, int b, double *dz,
-                                          double *dzh, long base_dz, long base_dzh, bool &bad) {
+template <int KIND, typename R>
+__device__ __forceinline__ int new_column(const Geom &g, const Params &p, double h, double eta, int b, R *dz, R *dzh,
+                                          long base_dz, long base_dzh, bool &bad) {
     const int L = g.L;
     const double MSL = p.msl;
     int tnew = 0;
@@ -301,7 +341,7 @@ __device__ __forceinline__ int new_column(const Geom &g, const Params &p, double
     for (int k = L - 1; k >= 0; --k) {
         if (tmp > g.z_level[k] && tmp <= g.z_level[k + 1]) {
             tnew = k + 1;
-            dz[base_dz + tnew - 1] = tmp - g.z_level[k];
+            dz[base_dz + tnew - 1] = (R)(tmp - g.z_level[k]);
             break;
         }
     }
@@ -310,13 +350,13 @@ __device__ __forceinline__ int new_column(const Geom &g, const Params &p, double
         return tnew;
     }
     if (tnew == b) {
-        dz[base_dz + tnew - 1] = total;
-        if (KIND == 1) dzh[base_dzh + tnew - 1] = total;
-        dzh[base_dzh + tnew] = total;
+        dz[base_dz + tnew - 1] = (R)total;
+        if (KIND == 1) dzh[base_dzh + tnew - 1] = (R)total;
+        dzh[base_dzh + tnew] = (R)total;
     } else {
-        dz[base_dz + b - 1] = g.z_level[b] - (MSL - h);
-        for (int k = b + 1; k <= tnew - 1; ++k) dz[base_dz + k - 1] = g.delta_z[k - 1];
-        for (int k = b; k <= tnew - 1; ++k) dzh[base_dzh + k] = (dz[base_dz + k] + dz[base_dz + k - 1]) * 0.5;
+        dz[base_dz + b - 1] = (R)(g.z_level[b] - (MSL - h));
+        for (int k = b + 1; k <= tnew - 1; ++k) dz[base_dz + k - 1] = (R)g.delta_z[k - 1];
+        for (int k = b; k <= tnew - 1; ++k) dzh[base_dzh + k] = (dz[base_dz + k] + dz[base_dz + k - 1]) * R(0.5);
         if (KIND != 2) {
             dzh[base_dzh + tnew] = dz[base_dz + tnew - 1];
             dzh[base_dzh + b - 1] = dz[base_dz + b - 1];
@@ -325,7 +365,7 @@ __device__ __forceinline__ int new_column(const Geom &g, const Params &p, double
     return tnew;
 }
 
-__global__ void k_layers_cells(Geom g, State s, Params p, gom_status *st) {
+template <typename R> __global__ void k_layers_cells(Geom g, StateT<R> s, Params p, gom_status *st) {
     int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     if (i > g.NC) return;
     const int L = g.L;
@@ -338,11 +378,11 @@ __global__ void k_layers_cells(Geom g, State s, Params p, gom_status *st) {
         return;
     }
     if (s.top_cell[i - 1] == 0 && tnew != 0)
-        for (int k = 0; k <= L; ++k) s.wn_cell_new[ix0(k, i, L)] = 0.0;
+        for (int k = 0; k <= L; ++k) s.wn_cell_new[ix0(k, i, L)] = R(0);
     s.top_cell[i - 1] = tnew;
 }
 
-__global__ void k_layers_faces(Geom g, State s, Params p, gom_status *st) {
+template <typename R> __global__ void k_layers_faces(Geom g, StateT<R> s, Params p, gom_status *st) {
     int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
     if (j > g.NF) return;
     const int L = g.L;
@@ -366,7 +406,7 @@ __global__ void k_layers_faces(Geom g, State s, Params p, gom_status *st) {
     }
 }
 
-__global__ void k_layers_nodes(Geom g, State s, Params p, gom_status *st) {
+template <typename R> __global__ void k_layers_nodes(Geom g, StateT<R> s, Params p, gom_status *st) {
     int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     if (i > g.NN) return;
     const int L = g.L;
@@ -389,7 +429,7 @@ __global__ void k_layers_nodes(Geom g, State s, Params p, gom_status *st) {
 }
 
 // :260-296 an element is dry when all its nodes are dry; consistency checks
-__global__ void k_layers_check(Geom g, State s, Params p, gom_status *st) {
+template <typename R> __global__ void k_layers_check(Geom g, StateT<R> s, Params p, gom_status *st) {
     int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     if (i > g.NC) return;
     const int L = g.L;
@@ -417,7 +457,7 @@ __global__ void k_layers_check(Geom g, State s, Params p, gom_status *st) {
     }
 }
 
-cudaError_t launch_layers(const Launch &x) {
+template <typename R> cudaError_t launch_layers(const LaunchT<R> &x) {
     k_layers_cells<<<blocks_for(x.g.NC, 256), 256, 0, x.stream>>>(x.g, x.s, x.p, x.status);
     k_layers_faces<<<blocks_for(x.g.NF, 256), 256, 0, x.stream>>>(x.g, x.s, x.p, x.status);
     k_layers_nodes<<<blocks_for(x.g.NN, 256), 256, 0, x.stream>>>(x.g, x.s, x.p, x.status);
@@ -428,7 +468,7 @@ cudaError_t launch_layers(const Launch &x) {
 // ============================================================================================
 // calculate_velocity_at_node.f90:31-60: face-level velocities, one thread per face column.  The
 // node loop divides each face level by the face length; that quotient is formed once here.
-__global__ void k_face_level(Geom g, State s, Work w) {
+template <typename R> __global__ void k_face_level(Geom g, StateT<R> s, WorkT<R> w) {
     unsigned tid = flat_tid();
     if (tid >= (unsigned)g.NF) return;
     int j = g.face_order[tid];
@@ -436,10 +476,10 @@ __global__ void k_face_level(Geom g, State s, Work w) {
     int t = s.top_face[j - 1];
     if (t == 0) return;
     int b = g.bottom_face[j - 1];
-    double ct = g.cos_theta[j - 1], sn = g.sin_theta[j - 1], fl = g.face_length[j - 1];
-    double uk = 0, vk = 0;
+    const R ct = (R)g.cos_theta[j - 1], sn = (R)g.sin_theta[j - 1], fl = (R)g.face_length[j - 1];
+    R uk, vk;
     {
-        double un = s.un_face_new[ix(b, j, L)], vn = s.vn_face_new[ix(b, j, L)];
+        R un = s.un_face_new[ix(b, j, L)], vn = s.vn_face_new[ix(b, j, L)];
         uk = un * ct - vn * sn;
         vk = un * sn + vn * ct;
     }
@@ -449,11 +489,11 @@ __global__ void k_face_level(Geom g, State s, Work w) {
     w.uflf[o] = uk / fl;
     w.vflf[o] = vk / fl;
     for (int k = b; k <= t - 1; ++k) {
-        double un = s.un_face_new[ix(k + 1, j, L)], vn = s.vn_face_new[ix(k + 1, j, L)];
-        double u1 = un * ct - vn * sn;
-        double v1 = un * sn + vn * ct;
-        double fac = s.dz_face[ix(k, j, L)] * 0.5 / s.dzhalf_face[ix0(k, j, L)];
-        double ul = uk + fac * (u1 - uk), vl = vk + fac * (v1 - vk);
+        R un = s.un_face_new[ix(k + 1, j, L)], vn = s.vn_face_new[ix(k + 1, j, L)];
+        R u1 = un * ct - vn * sn;
+        R v1 = un * sn + vn * ct;
+        R fac = s.dz_face[ix(k, j, L)] * R(0.5) / s.dzhalf_face[ix0(k, j, L)];
+        R ul = uk + fac * (u1 - uk), vl = vk + fac * (v1 - vk);
         o = ix0(k, j, L);
         s.u_face_level[o] = ul;
         s.v_face_level[o] = vl;
@@ -488,21 +528,21 @@ __global__ void k_node_weight(Geom g, double *node_weight) {
     node_weight[i - 1] = weight;
 }
 
-cudaError_t launch_node_weights(const Launch &x) {
+template <typename R> cudaError_t launch_node_weights(const LaunchT<R> &x) {
     k_node_weight<<<blocks_for(x.g.NN, 256), 256, 0, x.stream>>>(x.g, x.w.node_weight);
     return cudaGetLastError();
 }
 
 // :67-138 node u, v (face-length weighted face levels) and w (area-weighted cell w):
 // one thread per (node, level)
-__global__ void k_node_uvw(Geom g, State s, Work wk) {
+template <typename R> __global__ void k_node_uvw(Geom g, StateT<R> s, WorkT<R> wk) {
     unsigned tt = flat_tid();
     const int L = g.L;
     if (tt >= (unsigned)g.NN * (L + 1)) return;
     int i, k;
     split_index(tt, L + 1, i, k);
     i += 1;
-    double u = 0.0, v = 0.0;
+    R u = R(0), v = R(0);
     int icount = 0;
     int na = g.adj_cells_at_node[i - 1];
     for (int j = 1; j <= na; ++j) {
@@ -512,7 +552,7 @@ __global__ void k_node_uvw(Geom g, State s, Work wk) {
             int ifn = g.cell_face(start_end_node(tq, nc, l), isn);
             int tf = s.top_face[ifn - 1];
             if (tf != 0 && k >= g.bottom_face[ifn - 1] - 1) {
-                double fw = g.face_cell(2, ifn) == 0 ? 2.0 : 1.0;
+                R fw = g.face_cell(2, ifn) == 0 ? R(2) : R(1);
                 long o = ix0(min(k, tf), ifn, L);
                 u = u + wk.uflf[o] * fw;
                 v = v + wk.vflf[o] * fw;
@@ -521,33 +561,41 @@ __global__ void k_node_uvw(Geom g, State s, Work wk) {
         }
     }
     if (icount != 0) {
-        double weight = wk.node_weight[i - 1];
+        R weight = (R)wk.node_weight[i - 1];
         u = u / weight;
         v = v / weight;
     }
-    double w = 0.0, tw = 0.0;
+    R w = R(0), tw = R(0);
     for (int j = 1; j <= na; ++j) {
         int ite = g.node_cell(j, i);
         int te = s.top_cell[ite - 1];
         if (te != 0 && k >= g.bottom_cell[ite - 1] - 1) {
             int kvt = min(k, te);
-            double ar = g.area[ite - 1];
+            R ar = (R)g.area[ite - 1];
             tw = tw + ar;
             w = w + s.wn_cell[ix0(kvt, ite, L)] * ar;
         }
     }
-    if (tw != 0.0) w = w / tw;
+    if (tw != R(0)) w = w / tw;
     long o = ix0(k, i, L);
     s.u_node[o] = u;
     s.v_node[o] = v;
     s.w_node[o] = w;
 }
 
-cudaError_t launch_node_velocity(const Launch &x) {
+template <typename R> cudaError_t launch_node_velocity(const LaunchT<R> &x) {
     k_face_level<<<blocks_for(x.g.NF, 128), 128, 0, x.stream>>>(x.g, x.s, x.w);
     long n = (long)x.g.NN * (x.g.L + 1);
     k_node_uvw<<<blocks_for(n, 256), 256, 0, x.stream>>>(x.g, x.s, x.w);
     return cudaGetLastError();
 }
+
+template cudaError_t pcg_configure<double>(LaunchT<double> &x, int device);
+template cudaError_t pcg_configure<float>(LaunchT<float> &x, int device);
+GOM_INSTANTIATE_LAUNCH(launch_free_surface)
+GOM_INSTANTIATE_LAUNCH(launch_velocities)
+GOM_INSTANTIATE_LAUNCH(launch_layers)
+GOM_INSTANTIATE_LAUNCH(launch_node_velocity)
+GOM_INSTANTIATE_LAUNCH(launch_node_weights)
 
 }  // namespace gom

@@ -28,34 +28,43 @@ __device__ __forceinline__ bool is_neg(double q) {
 }
 __device__ __forceinline__ double pos_part(double q) { return is_pos(q) ? q : 0.0; }
 __device__ __forceinline__ double neg_part(double q) { return is_neg(q) ? -q : 0.0; }
-__device__ __forceinline__ double flip(double q, int sgn) { return sgn > 0 ? q : -q; }
 __device__ __forceinline__ bool same_bits(double a, double b) { return __double_as_longlong(a) == __double_as_longlong(b); }
+__device__ __forceinline__ bool is_pos(float q) { return __float_as_int(q) > 0; }
+__device__ __forceinline__ bool is_neg(float q) {
+    int b = __float_as_int(q);
+    return b < 0 && b != (int)0x80000000u;
+}
+__device__ __forceinline__ float pos_part(float q) { return is_pos(q) ? q : 0.0f; }
+__device__ __forceinline__ float neg_part(float q) { return is_neg(q) ? -q : 0.0f; }
+__device__ __forceinline__ bool same_bits(float a, float b) { return __float_as_int(a) == __float_as_int(b); }
+template <typename R> __device__ __forceinline__ R flip(R q, int sgn) { return sgn > 0 ? q : -q; }
 
-struct TArgs;
-__device__ __forceinline__ double divnt(double x, const TArgs &a);
-
-struct TArgs {
+// R: storage and arithmetic type of the tracers and coefficients
+template <typename R> struct TArgs {
     Geom g;
-    State s;
+    StateT<R> s;
     Forcing f;
     Params p;
-    Work w;
+    WorkT<R> w;
     gom_status *st;
     int ntr;          // active tracers
     int tid[2];       // tran_id of each slot: 1 salinity, 2 temperature
     int Nt, sub;      // subcycles, current subcycle
-    double dt2;
-    double inv_nt;    // 1/Nt, used only when Nt is a power of two (exact)
+    R dt2;
+    R inv_nt;         // 1/Nt, used only when Nt is a power of two (exact)
+    R theta, om_theta;  // theta and 1 - theta
     bool pow2;
     bool changed_only;  // coefficient kernels: refresh only entries whose thickness changes
-    const double *con;  // current concentrations
-    double *con_new;    // next concentrations (full columns, zero outside the wet range)
+    const R *con;       // current concentrations
+    R *con_new;         // next concentrations (full columns, zero outside the wet range)
 };
 
-__device__ __forceinline__ double divnt(double x, const TArgs &a) { return a.pow2 ? x * a.inv_nt : x / a.Nt; }
+template <typename R> __device__ __forceinline__ R divnt(R x, const TArgs<R> &a) {
+    return a.pow2 ? x * a.inv_nt : x / (R)a.Nt;
+}
 
 // :88-173 load tracers into con (0:L+1) with the heat_option 2 surface term
-__global__ void k_tr_load(TArgs a) {
+template <typename R> __global__ void k_tr_load(TArgs<R> a) {
     unsigned t = flat_tid();
     const Geom &g = a.g;
     const int L = g.L;
@@ -64,43 +73,42 @@ __global__ void k_tr_load(TArgs a) {
     split_index(t, L + 2, i, k);
     i += 1;
     for (int tr = 0; tr < a.ntr; ++tr) {
-        double v = 0.0;
+        R v = R(0);
         if (k >= 1 && k <= L) {
             v = a.tid[tr] == 1 ? a.s.salt_cell[ix(k, i, L)] : a.s.temp_cell[ix(k, i, L)];
             if (a.tid[tr] == 2 && a.p.heat_option == 2) {
                 int tl = a.s.top_cell[i - 1];
                 if (tl > 0)
-                    v = v + a.p.dt * a.f.phi_sw[i - 1] / (a.p.rho_o * 4186.0 * a.s.dz_cell[ix(tl, i, L)]);
+                    v = v + (R)(a.p.dt * a.f.phi_sw[i - 1]) / ((R)(a.p.rho_o * 4186.0) * a.s.dz_cell[ix(tl, i, L)]);
             }
         }
-        ((double *)a.con)[ic(k, i, tr, L, g.NC)] = v;
+        ((R *)a.con)[ic(k, i, tr, L, g.NC)] = v;
     }
 }
 
 // :232-397 boundary concentrations of the open-boundary and river cells for this subcycle
-__global__ void k_tr_bc(TArgs a) {
+template <typename R> __global__ void k_tr_bc(TArgs<R> a) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     const Geom &g = a.g;
     const int L = g.L;
-    const double theta = a.p.theta;
     if (t < g.NOB) {
         int i = t + 1;
         int i2 = g.ob_cell_id[i - 1];
         int tl = a.s.top_cell[i2 - 1], b = g.bottom_cell[i2 - 1];
         for (int k = 1; k <= L; ++k)
-            for (int tr = 0; tr < a.ntr; ++tr) a.w.obk[((long)tr * g.NOB + i - 1) * L + k - 1] = 0.0;
+            for (int tr = 0; tr < a.ntr; ++tr) a.w.obk[((long)tr * g.NOB + i - 1) * L + k - 1] = R(0);
         int tq = g.tri_or_quad[i2 - 1];
         for (int l = 1; l <= tq; ++l) {
             int j2 = g.cell_face(l, i2);
             if (g.boundary_type_of_face[j2 - 1] <= 0) continue;
             int sg = g.cell_sign(l, i2);
             for (int k = b; k <= tl; ++k) {
-                double dzf = a.s.dz_face[ix(k, j2, L)];
-                double dz_old = dzf + divnt((a.s.dz_face_new[ix(k, j2, L)] - dzf) * a.sub, a);
-                double q2 = g.face_length[j2 - 1] * dz_old *
-                            (flip((1.0 - theta) * a.s.un_face[ix(k, j2, L)], sg) + flip(theta * a.s.un_face_new[ix(k, j2, L)], sg));
+                R dzf = a.s.dz_face[ix(k, j2, L)];
+                R dz_old = dzf + divnt((a.s.dz_face_new[ix(k, j2, L)] - dzf) * (R)a.sub, a);
+                R q2 = (R)g.face_length[j2 - 1] * dz_old *
+                       (flip(a.om_theta * a.s.un_face[ix(k, j2, L)], sg) + flip(a.theta * a.s.un_face_new[ix(k, j2, L)], sg));
                 for (int tr = 0; tr < a.ntr; ++tr) {
-                    double bc = a.f.con_at_ob[((long)a.sub * 2 + (a.tid[tr] - 1)) * g.NOB + (i - 1)];
+                    R bc = (R)a.f.con_at_ob[((long)a.sub * 2 + (a.tid[tr] - 1)) * g.NOB + (i - 1)];
                     a.w.obk[((long)tr * g.NOB + i - 1) * L + k - 1] =
                         !is_pos(q2) ? bc : a.con[ic(k, i2, tr, L, g.NC)];
                 }
@@ -112,8 +120,8 @@ __global__ void k_tr_bc(TArgs a) {
         int tl = a.s.top_cell[i2 - 1], b = g.bottom_cell[i2 - 1];
         for (int k = 1; k <= L; ++k)
             for (int tr = 0; tr < a.ntr; ++tr) {
-                double v = 0.0;
-                if (k >= b && k <= tl) v = a.f.con_at_qb[((long)a.sub * 2 + (a.tid[tr] - 1)) * g.NQB + (i - 1)];
+                R v = R(0);
+                if (k >= b && k <= tl) v = (R)a.f.con_at_qb[((long)a.sub * 2 + (a.tid[tr] - 1)) * g.NQB + (i - 1)];
                 a.w.qbk[((long)tr * g.NQB + i - 1) * L + k - 1] = v;
             }
     }
@@ -122,20 +130,20 @@ __global__ void k_tr_bc(TArgs a) {
 // :551-581 face coefficients.  One thread per face walks its wet layers, so the FP64 work of a
 // warp is spread over 32 wet faces (GB300 issues an FP64 warp instruction at the same cost however
 // few lanes are active).  Later subcycles refresh only layers whose thickness changes.
-__device__ __forceinline__ void face_coef_at(const TArgs &a, int j, int k, long t) {
-    double dzf = a.s.dz_face[t];
-    double dz_old = dzf + divnt((a.s.dz_face_new[t] - dzf) * a.sub, a);
-    double fl = a.g.face_length[j - 1];
-    double Q = fl * dz_old * ((1.0 - a.p.theta) * a.s.un_face[t] + a.p.theta * a.s.un_face_new[t]);
-    double D = fl * dz_old * a.s.kh[t] / a.g.delta_j[j - 1];
-    double d = fmax(0.0, D - 0.5 * fabs(Q));
-    double phi = Q == 0.0 ? 1.0 : fmin(1.0, 2.0 * D / fabs(Q));
+template <typename R> __device__ __forceinline__ void face_coef_at(const TArgs<R> &a, int j, int k, long t) {
+    R dzf = a.s.dz_face[t];
+    R dz_old = dzf + divnt((a.s.dz_face_new[t] - dzf) * (R)a.sub, a);
+    R fl = (R)a.g.face_length[j - 1];
+    R Q = fl * dz_old * (a.om_theta * a.s.un_face[t] + a.theta * a.s.un_face_new[t]);
+    R D = fl * dz_old * a.s.kh[t] / (R)a.g.delta_j[j - 1];
+    R d = fmax(R(0), D - R(0.5) * fabs(Q));
+    R phi = Q == R(0) ? R(1) : fmin(R(1), R(2) * D / fabs(Q));
     a.w.qj[t] = Q;
     a.w.dj[t] = d;
     a.w.phij[t] = phi;
 }
 
-__global__ void k_tr_face_coef(TArgs a) {
+template <typename R> __global__ void k_tr_face_coef(TArgs<R> a) {
     unsigned tid = flat_tid();
     const Geom &g = a.g;
     if (tid >= (unsigned)g.NF) return;
@@ -148,9 +156,9 @@ __global__ void k_tr_face_coef(TArgs a) {
             if (k >= b && k <= tf) {
                 face_coef_at(a, j, k, t);
             } else {
-                a.w.qj[t] = 0.0;
-                a.w.dj[t] = 0.0;
-                a.w.phij[t] = 0.0;
+                a.w.qj[t] = R(0);
+                a.w.dj[t] = R(0);
+                a.w.phij[t] = R(0);
             }
         }
         return;
@@ -162,18 +170,18 @@ __global__ void k_tr_face_coef(TArgs a) {
 }
 
 // :585-610 vertical coefficients, one thread per cell column (interfaces b..t-1)
-__device__ __forceinline__ void cell_coef_at(const TArgs &a, int i, long t) {
-    double ar = a.g.area[i - 1];
-    double Q = ar * ((1.0 - a.p.theta) * a.s.wn_cell[t] + a.p.theta * a.s.wn_cell_new[t]);
-    double dzh = a.s.dzhalf_cell[t];
-    double dz_old = dzh + divnt((a.s.dzhalf_cell_new[t] - dzh) * a.sub, a);
-    double D = ar * a.s.kv[t] / dz_old;
+template <typename R> __device__ __forceinline__ void cell_coef_at(const TArgs<R> &a, int i, long t) {
+    R ar = (R)a.g.area[i - 1];
+    R Q = ar * (a.om_theta * a.s.wn_cell[t] + a.theta * a.s.wn_cell_new[t]);
+    R dzh = a.s.dzhalf_cell[t];
+    R dz_old = dzh + divnt((a.s.dzhalf_cell_new[t] - dzh) * (R)a.sub, a);
+    R D = ar * a.s.kv[t] / dz_old;
     a.w.qi[t] = Q;
-    a.w.di[t] = fmax(0.0, D - 0.5 * fabs(Q));
-    a.w.phii[t] = Q == 0.0 ? 1.0 : fmin(1.0, 2.0 * D / fabs(Q));
+    a.w.di[t] = fmax(R(0), D - R(0.5) * fabs(Q));
+    a.w.phii[t] = Q == R(0) ? R(1) : fmin(R(1), R(2) * D / fabs(Q));
 }
 
-__global__ void k_tr_cell_coef(TArgs a) {
+template <typename R> __global__ void k_tr_cell_coef(TArgs<R> a) {
     unsigned tid = flat_tid();
     const Geom &g = a.g;
     if (tid >= (unsigned)g.NC) return;
@@ -186,9 +194,9 @@ __global__ void k_tr_cell_coef(TArgs a) {
             if (k >= b && k <= tl - 1) {
                 cell_coef_at(a, i, t);
             } else {
-                a.w.qi[t] = 0.0;
-                a.w.di[t] = 0.0;
-                a.w.phii[t] = 0.0;
+                a.w.qi[t] = R(0);
+                a.w.di[t] = R(0);
+                a.w.phii[t] = R(0);
             }
         }
         return;
@@ -204,27 +212,27 @@ __device__ __forceinline__ bool face_open(const Geom &g, int j) {
 }
 
 // boundary concentration seen through a boundary face of cell i at layer k
-__device__ __forceinline__ double oqb_value(const TArgs &a, int i, int k, int tr) {
+template <typename R> __device__ __forceinline__ R oqb_value(const TArgs<R> &a, int i, int k, int tr) {
     const Geom &g = a.g;
     int ith_qb = g.qb_element_flag[i - 1];
     if (ith_qb > 0) return a.w.qbk[((long)tr * g.NQB + ith_qb - 1) * g.L + k - 1];
     int ith_ob = g.ob_element_flag[i - 1];
     if (ith_ob > 0) return a.w.obk[((long)tr * g.NOB + ith_ob - 1) * g.L + k - 1];
-    return 0.0;
+    return R(0);
 }
 
-__device__ __forceinline__ double phi_limit(int code, double small_phi, double r) {
+template <typename R> __device__ __forceinline__ R phi_limit(int code, R small_phi, R r) {
     switch (code) {
-    case 1: return fmax(small_phi, fmin(1.0, r)) - small_phi;
-    case 2: return fmax(small_phi, (r + fabs(r)) / (1.0 + fabs(r))) - small_phi;
-    case 3: return fmax(fmax(small_phi, fmin(1.0, 2.0 * r)), fmin(2.0, r)) - small_phi;
-    default: return 0.0;
+    case 1: return fmax(small_phi, fmin(R(1), r)) - small_phi;
+    case 2: return fmax(small_phi, (r + fabs(r)) / (R(1) + fabs(r))) - small_phi;
+    case 3: return fmax(fmax(small_phi, fmin(R(1), R(2) * r)), fmin(R(2), r)) - small_phi;
+    default: return R(0);
     }
 }
 
 // :624-871 per cell column: upwind-weighted differences of every layer (sum1_all, sum2_all) for
 // the face ratios r_jk, and the vertical ratios r_ik -> PSI_ik.
-__global__ void k_tr_limiter_cells(TArgs a) {
+template <typename R> __global__ void k_tr_limiter_cells(TArgs<R> a) {
     unsigned tid = flat_tid();
     const Geom &g = a.g;
     if (tid >= (unsigned)g.NC) return;
@@ -242,23 +250,23 @@ __global__ void k_tr_limiter_cells(TArgs a) {
         sg[l - 1] = g.cell_sign(l, i);
         open[l - 1] = face_open(g, fj[l - 1]);
     }
-    double last1[2] = {0.0, 0.0}, last2[2] = {0.0, 0.0};
+    R last1[2] = {R(0.0), R(0.0)}, last2[2] = {R(0.0), R(0.0)};
     for (int k = b; k <= tl; ++k) {
-        double s1a[2] = {0.0, 0.0}, s2a[2] = {0.0, 0.0}, s1[2] = {0.0, 0.0}, s2[2] = {0.0, 0.0};
+        R s1a[2] = {R(0.0), R(0.0)}, s2a[2] = {R(0.0), R(0.0)}, s1[2] = {R(0.0), R(0.0)}, s2[2] = {R(0.0), R(0.0)};
         for (int tr = 0; tr < a.ntr; ++tr) {
-            double ck = a.con[ic(k, i, tr, L, NC)];
+            R ck = a.con[ic(k, i, tr, L, NC)];
             if (nvl != 1) {
                 if (k == b) {
-                    double rt2 = pos_part(a.w.qi[ix0(k, i, L)]);
+                    R rt2 = pos_part(a.w.qi[ix0(k, i, L)]);
                     s1a[tr] = rt2 * (ck - a.con[ic(k + 1, i, tr, L, NC)]);
                     s2a[tr] = rt2;
                 } else if (k == tl) {
-                    double rt1 = pos_part(a.w.qi[ix0(k - 1, i, L)]);
+                    R rt1 = pos_part(a.w.qi[ix0(k - 1, i, L)]);
                     s1a[tr] = rt1 * (ck - a.con[ic(k - 1, i, tr, L, NC)]);
                     s2a[tr] = rt1;
                 } else {
-                    double rt1 = pos_part(a.w.qi[ix0(k - 1, i, L)]);
-                    double rt2 = pos_part(a.w.qi[ix0(k, i, L)]);
+                    R rt1 = pos_part(a.w.qi[ix0(k - 1, i, L)]);
+                    R rt2 = pos_part(a.w.qi[ix0(k, i, L)]);
                     s1a[tr] = rt1 * (ck - a.con[ic(k - 1, i, tr, L, NC)]) + rt2 * (ck - a.con[ic(k + 1, i, tr, L, NC)]);
                     s2a[tr] = rt1 + rt2;
                 }
@@ -266,10 +274,10 @@ __global__ void k_tr_limiter_cells(TArgs a) {
         }
         for (int l = 0; l < tq; ++l) {
             if (!open[l]) continue;
-            double q2 = flip(a.w.qj[ix(k, fj[l], L)], sg[l]);
+            R q2 = flip(a.w.qj[ix(k, fj[l], L)], sg[l]);
             if (is_neg(q2)) {
                 for (int tr = 0; tr < a.ntr; ++tr) {
-                    double cik = nb[l] > 0 ? a.con[ic(k, nb[l], tr, L, NC)] : oqb_value(a, i, k, tr);
+                    R cik = nb[l] > 0 ? a.con[ic(k, nb[l], tr, L, NC)] : oqb_value(a, i, k, tr);
                     s1[tr] = s1[tr] + fabs(q2) * (a.con[ic(k, i, tr, L, NC)] - cik);
                     s2[tr] = s2[tr] + fabs(q2);
                 }
@@ -286,14 +294,14 @@ __global__ void k_tr_limiter_cells(TArgs a) {
     }
     // :806-840 (Q_ik_theta at the top interface is never assigned: 0 -> first branch)
     for (int tr = 0; tr < a.ntr; ++tr) {
-        double *psi = a.w.psii + (long)tr * NC * (L + 1);
+        R *psi = a.w.psii + (long)tr * NC * (L + 1);
         for (int k = b; k <= tl - 1; ++k) {
-            double qm = (k - 1 >= b) ? a.w.qi[ix0(k - 1, i, L)] : 0.0;
-            double ck = a.con[ic(k, i, tr, L, NC)];
-            double rt1 = last1[tr] + fabs(qm) * (ck - a.con[ic(k - 1, i, tr, L, NC)]);
-            double rt2 = last2[tr] + fabs(qm);
-            double rtemp = (a.con[ic(k + 1, i, tr, L, NC)] - ck) * rt2;
-            double r = rtemp == 0.0 ? 1.0 : rt1 / rtemp;
+            R qm = (k - 1 >= b) ? a.w.qi[ix0(k - 1, i, L)] : R(0.0);
+            R ck = a.con[ic(k, i, tr, L, NC)];
+            R rt1 = last1[tr] + fabs(qm) * (ck - a.con[ic(k - 1, i, tr, L, NC)]);
+            R rt2 = last2[tr] + fabs(qm);
+            R rtemp = (a.con[ic(k + 1, i, tr, L, NC)] - ck) * rt2;
+            R r = rtemp == R(0.0) ? R(1.0) : rt1 / rtemp;
             psi[ix0(k, i, L)] = phi_limit(a.p.h_flux_limiter, a.w.phii[ix0(k, i, L)], r);
         }
     }
@@ -301,7 +309,7 @@ __global__ void k_tr_limiter_cells(TArgs a) {
 
 // :769-799 + :876-900 face ratio r_jk from its upwind cell (the last writer in cell order), PSI_jk;
 // one thread per face walks its wet layers
-__global__ void k_tr_limiter_faces(TArgs a) {
+template <typename R> __global__ void k_tr_limiter_faces(TArgs<R> a) {
     unsigned tid = flat_tid();
     const Geom &g = a.g;
     if (tid >= (unsigned)g.NF) return;
@@ -315,7 +323,7 @@ __global__ void k_tr_limiter_faces(TArgs a) {
     int t2 = c2 != 0 ? a.s.top_cell[c2 - 1] : 0, b2 = c2 != 0 ? g.bottom_cell[c2 - 1] : 0;
     for (int k = b; k <= tf; ++k) {
         long t = ix(k, j, L);
-        double Q = a.w.qj[t];
+        R Q = a.w.qj[t];
         int writer = 0;
         if (open) {
             // a cell writes when it is wet, holds layer k and sees Q*sign >= 0; cell 2 comes later
@@ -323,13 +331,13 @@ __global__ void k_tr_limiter_faces(TArgs a) {
             else if (t1 != 0 && k >= b1 && k <= t1 && !is_neg(Q)) writer = c1;        // Q >= 0
         }
         for (int tr = 0; tr < a.ntr; ++tr) {
-            double r = 1.0;
+            R r = R(1.0);
             if (writer != 0) {
                 int i = writer;
                 int other = (writer == c1) ? c2 : c1;
-                double cik = other > 0 ? a.con[ic(k, other, tr, L, NC)] : oqb_value(a, i, k, tr);
-                double rtemp = a.w.sa2[((long)tr * NC + i - 1) * L + k - 1] * (cik - a.con[ic(k, i, tr, L, NC)]);
-                r = rtemp == 0.0 ? 1.0 : a.w.sa1[((long)tr * NC + i - 1) * L + k - 1] / rtemp;
+                R cik = other > 0 ? a.con[ic(k, other, tr, L, NC)] : oqb_value(a, i, k, tr);
+                R rtemp = a.w.sa2[((long)tr * NC + i - 1) * L + k - 1] * (cik - a.con[ic(k, i, tr, L, NC)]);
+                r = rtemp == R(0.0) ? R(1.0) : a.w.sa1[((long)tr * NC + i - 1) * L + k - 1] / rtemp;
             }
             a.w.psij[(long)tr * g.NF * L + t] = phi_limit(a.p.h_flux_limiter, a.w.phij[t], r);
         }
@@ -338,44 +346,44 @@ __global__ void k_tr_limiter_faces(TArgs a) {
 
 // :921-1346 per cell column: explicit horizontal fluxes + limiter, implicit vertical system,
 // Thomas solve, clamp to [0, 50]; writes the full next column (zero outside the wet range).
-__global__ void __launch_bounds__(128) k_tr_solve(TArgs a) {
+template <typename R> __global__ void __launch_bounds__(128) k_tr_solve(TArgs<R> a) {
     unsigned tid = flat_tid();
     const Geom &g = a.g;
     if (tid >= (unsigned)g.NC) return;
     int i = g.cell_order[tid];
     const int L = g.L, NC = g.NC;
     int tl = a.s.top_cell[i - 1], b = g.bottom_cell[i - 1];
-    const double dt2 = a.dt2;
+    const R dt2 = a.dt2;
     const int Nt = a.Nt, sub = a.sub;
     const bool lim = a.p.h_flux_limiter > 0 || a.p.v_flux_limiter > 0;
     if (tl == 0) {
         for (int k = 0; k <= L + 1; ++k)
-            for (int tr = 0; tr < a.ntr; ++tr) a.con_new[ic(k, i, tr, L, NC)] = 0.0;
+            for (int tr = 0; tr < a.ntr; ++tr) a.con_new[ic(k, i, tr, L, NC)] = R(0.0);
         return;
     }
     int nvl = tl - b + 1;
-    double ar = g.area[i - 1];
-    double am[GOM_MAXL], bm[GOM_MAXL], cm[GOM_MAXL], gm[GOM_MAXL];
-    double rhs[GOM_MAXL][2];
+    const R ar = (R)g.area[i - 1];
+    R am[GOM_MAXL], bm[GOM_MAXL], cm[GOM_MAXL], gm[GOM_MAXL];
+    R rhs[GOM_MAXL][2];
     for (int k = b + 1; k <= tl - 1; ++k) {
         int kk = tl + 1 - k;
         am[kk - 1] = -dt2 * a.w.di[ix0(k, i, L)];
         cm[kk - 1] = -dt2 * a.w.di[ix0(k - 1, i, L)];
-        double dzc = a.s.dz_cell[ix(k, i, L)];
-        double dz_new = dzc + divnt((a.s.dz_cell_new[ix(k, i, L)] - dzc) * (sub + 1), a);
+        R dzc = a.s.dz_cell[ix(k, i, L)];
+        R dz_new = dzc + divnt((a.s.dz_cell_new[ix(k, i, L)] - dzc) * (sub + 1), a);
         bm[kk - 1] = -am[kk - 1] + ar * dz_new - cm[kk - 1];
     }
     {
-        double dzc = a.s.dz_cell[ix(tl, i, L)];
-        double dz_new = dzc + divnt((a.s.dz_cell_new[ix(tl, i, L)] - dzc) * (sub + 1), a);
+        R dzc = a.s.dz_cell[ix(tl, i, L)];
+        R dz_new = dzc + divnt((a.s.dz_cell_new[ix(tl, i, L)] - dzc) * (sub + 1), a);
         if (tl == b) {
             bm[0] = ar * dz_new;
         } else {
             cm[0] = -dt2 * a.w.di[ix0(tl - 1, i, L)];
             bm[0] = ar * dz_new - cm[0];
             am[nvl - 1] = -dt2 * a.w.di[ix0(b, i, L)];
-            double dzb = a.s.dz_cell[ix(b, i, L)];
-            double dz_newb = dzb + divnt((a.s.dz_cell_new[ix(b, i, L)] - dzb) * (sub + 1), a);
+            R dzb = a.s.dz_cell[ix(b, i, L)];
+            R dz_newb = dzb + divnt((a.s.dz_cell_new[ix(b, i, L)] - dzb) * (sub + 1), a);
             bm[nvl - 1] = -am[nvl - 1] + ar * dz_newb;
         }
     }
@@ -392,32 +400,32 @@ __global__ void __launch_bounds__(128) k_tr_solve(TArgs a) {
     }
     for (int k = b; k <= tl; ++k) {
         int kk = tl + 1 - k;
-        double sQi[2] = {0, 0}, sQii[2] = {0, 0}, shd[2] = {0, 0}, shl[2] = {0, 0};
-        double ck[2];
+        R sQi[2] = {0, 0}, sQii[2] = {0, 0}, shd[2] = {0, 0}, shl[2] = {0, 0};
+        R ck[2];
         for (int tr = 0; tr < a.ntr; ++tr) ck[tr] = a.con[ic(k, i, tr, L, NC)];
         for (int l = 0; l < tq; ++l) {
             if (!open[l]) continue;
             bool in_face = k >= fb[l] && k <= ft[l];
             long fo = ix(k, fj[l], L);
-            double q2 = flip(in_face ? a.w.qj[fo] : 0.0, sg[l]);
-            double dface = in_face ? a.w.dj[fo] : 0.0;
+            R q2 = flip(in_face ? a.w.qj[fo] : R(0.0), sg[l]);
+            R dface = in_face ? a.w.dj[fo] : R(0.0);
             bool qpos = is_pos(q2), qneg = is_neg(q2);
             for (int tr = 0; tr < a.ntr; ++tr) {
-                double cik = nb[l] > 0 ? a.con[ic(k, nb[l], tr, L, NC)] : oqb_value(a, i, k, tr);
+                R cik = nb[l] > 0 ? a.con[ic(k, nb[l], tr, L, NC)] : oqb_value(a, i, k, tr);
                 if (qpos) sQi[tr] = sQi[tr] + fabs(q2) * ck[tr];
                 else if (qneg) sQii[tr] = sQii[tr] + fabs(q2) * cik;
                 shd[tr] = shd[tr] + dface * (cik - ck[tr]);
-                double psi = (lim && in_face) ? a.w.psij[(long)tr * g.NF * L + fo] : 0.0;
+                R psi = (lim && in_face) ? a.w.psij[(long)tr * g.NF * L + fo] : R(0.0);
                 shl[tr] = shl[tr] + psi * fabs(q2) * (ck[tr] - cik);
             }
         }
-        double dzc = a.s.dz_cell[ix(k, i, L)];
-        double dz_old = dzc + divnt((a.s.dz_cell_new[ix(k, i, L)] - dzc) * sub, a);
+        R dzc = a.s.dz_cell[ix(k, i, L)];
+        R dz_old = dzc + divnt((a.s.dz_cell_new[ix(k, i, L)] - dzc) * sub, a);
         for (int tr = 0; tr < a.ntr; ++tr) {
-            double h_adv = dt2 * (sQii[tr] - sQi[tr]);
-            double h_diff = dt2 * shd[tr];
-            double h_flux = 0.5 * dt2 * shl[tr];
-            double v = ar * dz_old * ck[tr] + h_adv + h_diff;
+            R h_adv = dt2 * (sQii[tr] - sQi[tr]);
+            R h_diff = dt2 * shd[tr];
+            R h_flux = R(0.5) * dt2 * shl[tr];
+            R v = ar * dz_old * ck[tr] + h_adv + h_diff;
             if (a.p.h_flux_limiter > 0) v = v + h_flux;
             rhs[kk - 1][tr] = v;
         }
@@ -426,36 +434,36 @@ __global__ void __launch_bounds__(128) k_tr_solve(TArgs a) {
         for (int k = b; k <= tl; ++k) {
             int kk = tl + 1 - k;
             for (int tr = 0; tr < a.ntr; ++tr) {
-                const double *psi = a.w.psii + (long)tr * NC * (L + 1);
-                double c0 = a.con[ic(k, i, tr, L, NC)];
-                double v = rhs[kk - 1][tr];
+                const R *psi = a.w.psii + (long)tr * NC * (L + 1);
+                R c0 = a.con[ic(k, i, tr, L, NC)];
+                R v = rhs[kk - 1][tr];
                 if (k == b) {
-                    double q = a.w.qi[ix0(k, i, L)];
-                    double qp = pos_part(q), qm = neg_part(q);
-                    double cp1 = a.con[ic(k + 1, i, tr, L, NC)];
+                    R q = a.w.qi[ix0(k, i, L)];
+                    R qp = pos_part(q), qm = neg_part(q);
+                    R cp1 = a.con[ic(k + 1, i, tr, L, NC)];
                     v = v + dt2 * (-qp * c0 + qm * cp1);
                     if (a.p.v_flux_limiter > 0) {
-                        double ps = lim ? psi[ix0(k, i, L)] : 0.0;
-                        v = v + 0.5 * dt2 * (-ps * qp * (cp1 - c0) + ps * qm * (c0 - cp1));
+                        R ps = lim ? psi[ix0(k, i, L)] : R(0.0);
+                        v = v + R(0.5) * dt2 * (-ps * qp * (cp1 - c0) + ps * qm * (c0 - cp1));
                     }
                 } else if (k == tl) {
-                    double q = a.w.qi[ix0(k - 1, i, L)];
-                    double qp = pos_part(q), qm = neg_part(q);
-                    double cm1 = a.con[ic(k - 1, i, tr, L, NC)];
+                    R q = a.w.qi[ix0(k - 1, i, L)];
+                    R qp = pos_part(q), qm = neg_part(q);
+                    R cm1 = a.con[ic(k - 1, i, tr, L, NC)];
                     v = v + dt2 * (qp * cm1 - qm * c0);
                     if (a.p.v_flux_limiter > 0) {
-                        double ps = lim ? psi[ix0(k - 1, i, L)] : 0.0;
-                        v = v + 0.5 * dt2 * (ps * qp * (c0 - cm1) - ps * qm * (cm1 - c0));
+                        R ps = lim ? psi[ix0(k - 1, i, L)] : R(0.0);
+                        v = v + R(0.5) * dt2 * (ps * qp * (c0 - cm1) - ps * qm * (cm1 - c0));
                     }
                 } else {
-                    double q1 = a.w.qi[ix0(k - 1, i, L)], q = a.w.qi[ix0(k, i, L)];
-                    double qp1 = pos_part(q1), qm1 = neg_part(q1);
-                    double qp = pos_part(q), qm = neg_part(q);
-                    double cm1 = a.con[ic(k - 1, i, tr, L, NC)], cp1 = a.con[ic(k + 1, i, tr, L, NC)];
+                    R q1 = a.w.qi[ix0(k - 1, i, L)], q = a.w.qi[ix0(k, i, L)];
+                    R qp1 = pos_part(q1), qm1 = neg_part(q1);
+                    R qp = pos_part(q), qm = neg_part(q);
+                    R cm1 = a.con[ic(k - 1, i, tr, L, NC)], cp1 = a.con[ic(k + 1, i, tr, L, NC)];
                     v = v + dt2 * (qp1 * cm1 - qp * c0 + qm * cp1 - qm1 * c0);
                     if (a.p.v_flux_limiter > 0) {
-                        double p1 = lim ? psi[ix0(k - 1, i, L)] : 0.0, p0 = lim ? psi[ix0(k, i, L)] : 0.0;
-                        v = v + 0.5 * dt2 *
+                        R p1 = lim ? psi[ix0(k - 1, i, L)] : R(0.0), p0 = lim ? psi[ix0(k, i, L)] : R(0.0);
+                        v = v + R(0.5) * dt2 *
                                     (p1 * qp1 * (c0 - cm1) - p0 * qp * (cp1 - c0) + p0 * qm * (c0 - cp1) -
                                      p1 * qm1 * (cm1 - c0));
                     }
@@ -467,7 +475,7 @@ __global__ void __launch_bounds__(128) k_tr_solve(TArgs a) {
     bool okp;
     if (a.ntr == 2) okp = thomas<2>(nvl, am, bm, cm, rhs, gm);
     else {
-        double r1[GOM_MAXL][1];
+        R r1[GOM_MAXL][1];
         for (int k = 0; k < nvl; ++k) r1[k][0] = rhs[k][0];
         okp = thomas<1>(nvl, am, bm, cm, r1, gm);
         for (int k = 0; k < nvl; ++k) rhs[k][0] = r1[k][0];
@@ -478,12 +486,12 @@ __global__ void __launch_bounds__(128) k_tr_solve(TArgs a) {
     }
     for (int tr = 0; tr < a.ntr; ++tr) {
         for (int k = 0; k <= L + 1; ++k) {
-            double v = 0.0;
+            R v = R(0.0);
             if (k >= b && k <= tl) {
-                double sv = rhs[tl - k][tr];
-                if (sv >= 0.0 && sv <= 50.0) v = sv;
-                else if (sv < 0.0) v = 0.0;
-                else if (sv > 50.0) v = 50.0;
+                R sv = rhs[tl - k][tr];
+                if (sv >= R(0.0) && sv <= R(50.0)) v = sv;
+                else if (sv < R(0.0)) v = R(0.0);
+                else if (sv > R(50.0)) v = R(50.0);
                 else v = a.con[ic(k, i, tr, L, NC)];   // NaN: the reference keeps the previous value
             }
             a.con_new[ic(k, i, tr, L, NC)] = v;
@@ -492,7 +500,7 @@ __global__ void __launch_bounds__(128) k_tr_solve(TArgs a) {
 }
 
 // :1403-1454 node averages (column, top-down) and :1457-1482 face averages + write-back
-__global__ void k_tr_nodes(TArgs a) {
+template <typename R> __global__ void k_tr_nodes(TArgs<R> a) {
     unsigned tid = flat_tid();
     const Geom &g = a.g;
     if (tid >= (unsigned)g.NN) return;
@@ -501,25 +509,25 @@ __global__ void k_tr_nodes(TArgs a) {
     int tn = a.s.top_node[i - 1], bn = g.bottom_node[i - 1];
     int na = g.adj_cells_at_node[i - 1];
     for (int tr = 0; tr < a.ntr; ++tr) {
-        double *dst = a.tid[tr] == 1 ? a.s.salt_node : a.s.temp_node;
+        R *dst = a.tid[tr] == 1 ? a.s.salt_node : a.s.temp_node;
         bool write = a.tid[tr] <= a.ntr;   // slot 1 -> salt, slot 2 -> temperature
-        double above = 0.0;
+        R above = R(0.0);
         for (int k = L; k >= 1; --k) {
-            double v = 0.0;
+            R v = R(0.0);
             if (tn != 0 && k <= tn && k >= bn) {
-                double s11 = 0.0, s22 = 0.0;
+                R s11 = R(0.0), s22 = R(0.0);
                 int count1 = 0;
                 for (int l = 1; l <= na; ++l) {
                     int ii = g.node_cell(l, i);
                     if (k >= g.bottom_cell[ii - 1] && k <= a.s.top_cell[ii - 1]) {
-                        double w = g.area[ii - 1] * a.s.dz_cell_new[ix(k, ii, L)];
+                        R w = (R)g.area[ii - 1] * a.s.dz_cell_new[ix(k, ii, L)];
                         s11 = s11 + w;
                         s22 = s22 + w * a.con[ic(k, ii, tr, L, NC)];
                     } else {
                         count1 = count1 + 1;
                     }
                 }
-                v = s11 == 0.0 ? 0.0 : s22 / s11;
+                v = s11 == R(0.0) ? R(0.0) : s22 / s11;
                 if (count1 == na && k != tn) v = above;
             }
             if (write) dst[ix(k, i, L)] = v;
@@ -528,7 +536,7 @@ __global__ void k_tr_nodes(TArgs a) {
     }
 }
 
-__global__ void k_tr_faces_cells(TArgs a) {
+template <typename R> __global__ void k_tr_faces_cells(TArgs<R> a) {
     unsigned t = flat_tid();
     const Geom &g = a.g;
     const int L = g.L, NC = g.NC;
@@ -542,9 +550,9 @@ __global__ void k_tr_faces_cells(TArgs a) {
         bool in = k >= g.bottom_face[j - 1] && k <= a.s.top_face[j - 1];
         for (int tr = 0; tr < a.ntr; ++tr) {
             if (a.tid[tr] > a.ntr) continue;
-            const double *src = a.tid[tr] == 1 ? a.s.salt_node : a.s.temp_node;
-            double *dst = a.tid[tr] == 1 ? a.s.salt_face : a.s.temp_face;
-            dst[t] = in ? (src[ix(k, n1, L)] + src[ix(k, n2, L)]) * 0.5 : 0.0;
+            const R *src = a.tid[tr] == 1 ? a.s.salt_node : a.s.temp_node;
+            R *dst = a.tid[tr] == 1 ? a.s.salt_face : a.s.temp_face;
+            dst[t] = in ? (src[ix(k, n1, L)] + src[ix(k, n2, L)]) * R(0.5) : R(0.0);
         }
     } else if (t < nfl + ncl) {
         unsigned u = t - nfl;
@@ -554,16 +562,16 @@ __global__ void k_tr_faces_cells(TArgs a) {
         k += 1;
         for (int tr = 0; tr < a.ntr; ++tr) {
             if (a.tid[tr] > a.ntr) continue;
-            double *dst = a.tid[tr] == 1 ? a.s.salt_cell_new : a.s.temp_cell_new;
+            R *dst = a.tid[tr] == 1 ? a.s.salt_cell_new : a.s.temp_cell_new;
             dst[u] = a.con[ic(k, i, tr, L, NC)];
         }
     }
 }
 
-cudaError_t launch_transport(const Launch &x) {
+template <typename R> cudaError_t launch_transport(const LaunchT<R> &x) {
     const Params &p = x.p;
     if (!p.transport_flag) return cudaSuccess;
-    TArgs a;
+    TArgs<R> a;
     a.g = x.g;
     a.s = x.s;
     a.f = x.f;
@@ -575,9 +583,11 @@ cudaError_t launch_transport(const Launch &x) {
     if (p.is_temp) a.tid[a.ntr++] = 2;
     if (a.ntr == 0) return cudaSuccess;
     a.Nt = p.trans_sub_iter == 0 ? 1 : p.trans_sub_iter;
-    a.dt2 = p.dt / a.Nt;
+    a.dt2 = (R)(p.dt / a.Nt);
     a.pow2 = (a.Nt & (a.Nt - 1)) == 0;
-    a.inv_nt = 1.0 / a.Nt;
+    a.inv_nt = (R)(1.0 / a.Nt);
+    a.theta = (R)p.theta;
+    a.om_theta = (R)(1.0 - p.theta);
     a.changed_only = false;
     const Geom &g = x.g;
     const int L = g.L;
@@ -585,7 +595,7 @@ cudaError_t launch_transport(const Launch &x) {
     a.con_new = x.w.con2;
     k_tr_load<<<blocks_for((long)g.NC * (L + 2), 256), 256, 0, x.stream>>>(a);
     bool lim = p.h_flux_limiter > 0 || p.v_flux_limiter > 0;
-    double *cur = x.w.con, *nxt = x.w.con2;
+    R *cur = x.w.con, *nxt = x.w.con2;
     for (int sub = 0; sub < a.Nt; ++sub) {
         a.sub = sub;
         a.con = cur;
@@ -599,7 +609,7 @@ cudaError_t launch_transport(const Launch &x) {
             k_tr_limiter_faces<<<blocks_for(g.NF, 128), 128, 0, x.stream>>>(a);
         }
         k_tr_solve<<<blocks_for(g.NC, 128), 128, 0, x.stream>>>(a);
-        double *t = cur;
+        R *t = cur;
         cur = nxt;
         nxt = t;
     }
@@ -640,8 +650,8 @@ __device__ __forceinline__ double eos_bulk(double rtemp, double rsalt, double pr
 }
 
 // one thread per node (kind 0) or face (kind 1) column
-template <int KIND>
-__global__ void k_density_col(Geom g, State s, Params p, gom_status *st) {
+template <int KIND, typename R>
+__global__ void k_density_col(Geom g, StateT<R> s, Params p, gom_status *st) {
     unsigned tid = flat_tid();
     int n = KIND == 0 ? g.NN : g.NF;
     if (tid >= (unsigned)n) return;
@@ -651,9 +661,9 @@ __global__ void k_density_col(Geom g, State s, Params p, gom_status *st) {
     if (t == 0) return;
     int b = KIND == 0 ? g.bottom_node[e - 1] : g.bottom_face[e - 1];
     double *rho = KIND == 0 ? s.rho_node : s.rho_face;
-    const double *tt = KIND == 0 ? s.temp_node : s.temp_face;
-    const double *ss = KIND == 0 ? s.salt_node : s.salt_face;
-    const double *dz = KIND == 0 ? s.dz_node : s.dz_face;
+    const R *tt = KIND == 0 ? s.temp_node : s.temp_face;
+    const R *ss = KIND == 0 ? s.salt_node : s.salt_face;
+    const R *dz = KIND == 0 ? s.dz_node : s.dz_face;
     const double c981 = F(9.81f), c1e5h = (double)(1.0e-5f * 0.5f), c1e5 = F(1.0e-5f);
     for (int k = b; k <= t; ++k) {
         double rtemp = tt[ix(k, e, L)], rsalt = ss[ix(k, e, L)];
@@ -670,7 +680,7 @@ __global__ void k_density_col(Geom g, State s, Params p, gom_status *st) {
             if (p.msl - g.z_level[k] > F(100.0f)) {
                 double pres = 0.0;
                 for (int kk = k; kk <= t; ++kk) {
-                    double ptmp = c981 * rho[ix(kk, e, L)] * dz[ix(kk, e, L)];
+                    double ptmp = c981 * rho[ix(kk, e, L)] * (double)dz[ix(kk, e, L)];
                     pres = pres + (kk == k ? c1e5h : c1e5) * ptmp;
                 }
                 double sbm = eos_bulk(rtemp, rsalt, pres);
@@ -689,7 +699,7 @@ __global__ void k_density_col(Geom g, State s, Params p, gom_status *st) {
 }
 
 // :207-238 cell density = mean of its wet nodes
-__global__ void k_density_cells(Geom g, State s, gom_status *st) {
+template <typename R> __global__ void k_density_cells(Geom g, StateT<R> s, gom_status *st) {
     unsigned tid = flat_tid();
     if (tid >= (unsigned)g.NC) return;
     int i = g.cell_order[tid];
@@ -719,27 +729,140 @@ __global__ void k_density_cells(Geom g, State s, gom_status *st) {
     for (int k = t + 1; k <= L; ++k) s.rho_cell[ix(k, i, L)] = rt;
 }
 
-cudaError_t launch_density(const Launch &x) {
+template <typename R> cudaError_t launch_density(const LaunchT<R> &x) {
     if (x.p.baroclinic_flag != 1) return cudaSuccess;
-    k_density_col<0><<<blocks_for(x.g.NN, 128), 128, 0, x.stream>>>(x.g, x.s, x.p, x.status);
-    if (x.p.ana_density == 0) k_density_col<1><<<blocks_for(x.g.NF, 128), 128, 0, x.stream>>>(x.g, x.s, x.p, x.status);
+    k_density_col<0, R><<<blocks_for(x.g.NN, 128), 128, 0, x.stream>>>(x.g, x.s, x.p, x.status);
+    if (x.p.ana_density == 0) k_density_col<1, R><<<blocks_for(x.g.NF, 128), 128, 0, x.stream>>>(x.g, x.s, x.p, x.status);
     k_density_cells<<<blocks_for(x.g.NC, 128), 128, 0, x.stream>>>(x.g, x.s, x.status);
     return cudaGetLastError();
 }
 
 // ============================================================================================
-// volume and salt mass in FP64: per-block sums, then one block adds the block sums in order
-__global__ void k_conservation_partial(Geom g, State s, double *part) {
+// turbulence_closure_v1.f90:72-138, schemes 1 (step function of Ri) and 2 (Pacanowski-Philander).
+// The routine names another model's arrays; here srho -> rho_face, velocity_normal/tangnt ->
+// un/vn_face_new, dzhalf -> dzhalf_face_new, h_at_face_center -> h_face, ref_water_density ->
+// rho_o.  Interface k of a face (top of layer k) gets Av(k) and a face diffusivity; a cell's Kv(k)
+// is the mean of its wet faces' diffusivities at the level clamped to each face's wet range
+// (the nodal averaging of :446-470 applied to cells), 1e-2 where no face is wet.
+// One thread per face column; Ri differences densities in FP64, the rest runs in R.
+template <typename R> __global__ void k_turbulence_faces(Geom g, StateT<R> s, Params p, R *kvf) {
+    unsigned tid = flat_tid();
+    if (tid >= (unsigned)g.NF) return;
+    int i = g.face_order[tid];
+    const int L = g.L;
+    int t = s.top_face[i - 1];
+    if (t == 0) return;
+    int b = g.bottom_face[i - 1];
+    R vmax = R(0), vmin = R(0);
+    if (p.turbulence_flag == 2) {
+        double h = g.h_face[i - 1];
+        if (h <= p.pp_h1) {
+            vmax = (R)p.pp_vdmax1;
+            vmin = (R)p.pp_vdmin1;
+        } else if (h < p.pp_h2) {
+            vmax = (R)(p.pp_vdmax1 + (p.pp_vdmax2 - p.pp_vdmax1) * (h - p.pp_h1) / (p.pp_h2 - p.pp_h1));
+            vmin = (R)(p.pp_vdmin1 + (p.pp_vdmin2 - p.pp_vdmin1) * (h - p.pp_h1) / (p.pp_h2 - p.pp_h1));
+        } else {
+            vmax = (R)p.pp_vdmax2;
+            vmin = (R)p.pp_vdmin2;
+        }
+    }
+    const R gR = (R)p.gravity, rho_o = (R)p.rho_o;
+    const R gsound = (R)(p.gravity / (double)(1.5e3f * 1.5e3f));
+    const R tdmin = (R)p.pp_tdmin;
+    for (int k = b; k <= t; ++k) {
+        R ri = R(0);
+        if (k != t) {
+            R dzh = s.dzhalf_face_new[ix0(k, i, L)];
+            R drhodz = (R)(s.rho_face[ix(k + 1, i, L)] - s.rho_face[ix(k, i, L)]) / dzh;
+            R bvf = -gR * (drhodz / rho_o + gsound);
+            R dundz = (s.un_face_new[ix(k + 1, i, L)] - s.un_face_new[ix(k, i, L)]) / dzh;
+            R dutdz = (s.vn_face_new[ix(k + 1, i, L)] - s.vn_face_new[ix(k, i, L)]) / dzh;
+            R shear2 = dundz * dundz + dutdz * dutdz;
+            shear2 = fmax(shear2, (R)1.0e-10);
+            ri = fmax(bvf / shear2, R(0));
+        }
+        R a, d;
+        if (p.turbulence_flag == 1) {
+            if (ri < R(0.25)) {
+                a = (R)1.0e-3;
+                d = (R)1.0e-3;
+            } else {
+                a = (R)1.0e-5;
+                d = (R)1.0e-5;
+            }
+        } else {
+            R x = R(1) + R(5) * ri;
+            a = vmax / (x * x) + vmin;
+            d = a / (R(1) + R(5) * ri) + tdmin;
+        }
+        s.av[ix0(k, i, L)] = a;
+        kvf[ix0(k, i, L)] = d;
+    }
+}
+
+template <typename R> __global__ void k_turbulence_cells(Geom g, StateT<R> s, const R *kvf) {
+    unsigned tid = flat_tid();
+    if (tid >= (unsigned)g.NC) return;
+    int i = g.cell_order[tid];
+    const int L = g.L;
+    int t = s.top_cell[i - 1];
+    if (t == 0) return;
+    int tq = g.tri_or_quad[i - 1];
+    int fj[4], fb[4], ft[4];
+    for (int l = 1; l <= tq; ++l) {
+        fj[l - 1] = g.cell_face(l, i);
+        fb[l - 1] = g.bottom_face[fj[l - 1] - 1];
+        ft[l - 1] = s.top_face[fj[l - 1] - 1];
+    }
+    for (int k = g.bottom_cell[i - 1]; k <= t; ++k) {
+        R sum = R(0);
+        int icount = 0;
+        for (int l = 0; l < tq; ++l) {
+            if (ft[l] != 0) {
+                icount = icount + 1;
+                int klev = min(max(k, fb[l]), ft[l]);
+                sum = sum + kvf[ix0(klev, fj[l], L)];
+            }
+        }
+        s.kv[ix0(k, i, L)] = icount == 0 ? (R)F(1.0e-2f) : sum / (R)icount;
+    }
+}
+
+template <typename R> cudaError_t launch_turbulence(const LaunchT<R> &x) {
+    if (x.p.turbulence_flag != 1 && x.p.turbulence_flag != 2) return cudaSuccess;
+    k_turbulence_faces<<<blocks_for(x.g.NF, 128), 128, 0, x.stream>>>(x.g, x.s, x.p, x.w.kvf);
+    k_turbulence_cells<<<blocks_for(x.g.NC, 128), 128, 0, x.stream>>>(x.g, x.s, (const R *)x.w.kvf);
+    return cudaGetLastError();
+}
+
+// ============================================================================================
+// volume and salt mass in FP64: per-block sums, then one block adds the block sums in order.
+// A mixed-precision context stores thicknesses in FP32; its sums use the FP64 thickness of each
+// wet layer recomputed from the FP64 elevation as update_vertical_layers_1.f90:42-133 forms it,
+// so the volume is conserved to the free-surface solve's accuracy, not to FP32 rounding.
+template <typename R>
+__device__ __forceinline__ double layer_dz64(const Geom &g, const StateT<R> &s, const Params &p, int i, int k, int b,
+                                              int t) {
+    if (sizeof(R) == sizeof(double)) return (double)s.dz_cell[ix(k, i, g.L)];
+    double h = g.h_cell[i - 1], eta = s.eta_cell[i - 1];
+    if (t == b) return h + eta;
+    if (k == t) return (p.msl + eta) - g.z_level[t - 1];
+    if (k == b) return g.z_level[b] - (p.msl - h);
+    return g.delta_z[k - 1];
+}
+
+template <typename R> __global__ void k_conservation_partial(Geom g, StateT<R> s, Params p, double *part) {
     __shared__ double sv[256], ss[256];
     int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int L = g.L;
     double v = 0.0, m = 0.0;
     if (i <= g.NC) {
-        int t = s.top_cell[i - 1];
-        for (int k = g.bottom_cell[i - 1]; k <= t; ++k) {
-            double vv = g.area[i - 1] * s.dz_cell[ix(k, i, L)];
+        int t = s.top_cell[i - 1], b = g.bottom_cell[i - 1];
+        for (int k = b; k <= t; ++k) {
+            double vv = g.area[i - 1] * layer_dz64(g, s, p, i, k, b, t);
             v = v + vv;
-            m = m + vv * s.salt_cell[ix(k, i, L)];
+            m = m + vv * (double)s.salt_cell[ix(k, i, L)];
         }
     }
     sv[threadIdx.x] = v;
@@ -769,11 +892,16 @@ __global__ void k_conservation_final(double *part, int nblocks) {
     part[1] = m;
 }
 
-cudaError_t launch_conservation(const Launch &x) {
+template <typename R> cudaError_t launch_conservation(const LaunchT<R> &x) {
     int nb = blocks_for(x.g.NC, 256);
-    k_conservation_partial<<<nb, 256, 0, x.stream>>>(x.g, x.s, x.w.cons);
+    k_conservation_partial<<<nb, 256, 0, x.stream>>>(x.g, x.s, x.p, x.w.cons);
     k_conservation_final<<<1, 32, 0, x.stream>>>(x.w.cons, nb);
     return cudaGetLastError();
 }
+
+GOM_INSTANTIATE_LAUNCH(launch_transport)
+GOM_INSTANTIATE_LAUNCH(launch_density)
+GOM_INSTANTIATE_LAUNCH(launch_turbulence)
+GOM_INSTANTIATE_LAUNCH(launch_conservation)
 
 }  // namespace gom

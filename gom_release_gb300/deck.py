@@ -66,6 +66,17 @@ class Params:
     is_temp: int = 1
     heat_option: int = 2
     test_barrier_phantom_blocks: int = 0
+    precision: int = 0              # 0 FP64, 1 mixed (FP32 layered state)
+    # turbulence_closure_v1.f90: 0 off (reference time loop), 1 step-Ri, 2 Pacanowski-Philander;
+    # the coefficients are the closure's usual values (the reference reads none of them)
+    turbulence_flag: int = 0
+    pp_h1: float = 20.0
+    pp_h2: float = 50.0
+    pp_vdmax1: float = 1.0e-2
+    pp_vdmax2: float = 1.0e-2
+    pp_vdmin1: float = 1.0e-5
+    pp_vdmin2: float = 1.0e-5
+    pp_tdmin: float = 1.0e-5
     # not part of the C ABI params (host-side start-up values)
     av_0: float = 1e-3
     kv_0: float = 1e-4
@@ -211,11 +222,11 @@ def tidal_basin(nx: int = 120, ny: int = 80, dx: float = 250.0, tri_rows: int = 
 
 def estuary(nx: int = 600, ny: int = 250, dx: float = 100.0, tri_rows: int = 4, n_layers: int = 20,
             seed: int = 20240602, n_steps: int = 2880, dt: float = 60.0, n_river: int = 10,
-            trans_sub_iter: int = 4) -> Deck:
+            trans_sub_iter: int = 4, turbulence_flag: int = 2) -> Deck:
     """Baroclinic estuary: ocean open boundary on the west edge (M2 0.6 m, S = 35, T = 18),
     river of 500 m3/s at S = 0, T = 24 over ``n_river`` faces of the east edge (channel head),
-    initial salinity linear along the channel, TVD limiter on, uniform wind stress 0.1 Pa at a
-    seeded direction.  The seeded sinusoidal coastline is a shoal along y = yc(x) carved into
+    initial salinity linear along the channel, TVD limiter on, turbulence closure on
+    (Pacanowski-Philander), uniform wind stress 0.1 Pa at a seeded direction.  The seeded sinusoidal coastline is a shoal along y = yc(x) carved into
     the bathymetry (the mesh boundary itself is straight)."""
     rng = np.random.default_rng(seed)
     x, y, cells, tq = square_strip_mesh(nx, ny, dx, tri_rows)
@@ -230,7 +241,7 @@ def estuary(nx: int = 600, ny: int = 250, dx: float = 100.0, tri_rows: int = 4, 
     raw = RawMesh(x=x, y=y, h=h, tri_or_quad=tq, cells=cells)
     params = Params(dt=dt, theta=0.6, error_tolerance=1e-10, baroclinic_flag=1, ana_density=0,
                     trans_sub_iter=trans_sub_iter, h_flux_limiter=1, v_flux_limiter=1,
-                    smagorinsky=0.021, kh_0=0.1, av_0=1e-3, kv_0=1e-5)
+                    smagorinsky=0.021, kh_0=0.1, av_0=1e-3, kv_0=1e-5, turbulence_flag=turbulence_flag)
     # west edge: faces NW -> SW of squares in column 0, i.e. node (0, j+1) -> (0, j)
     row = nx + 1
     ob_pairs = [((j + 1) * row + 1, j * row + 1) for j in range(ny)]

@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define GOM_ABI_VERSION 1
+#define GOM_ABI_VERSION 2
 
 typedef struct gom_ctx gom_ctx;
 
@@ -129,8 +129,25 @@ typedef struct gom_params {
     int32_t test_barrier_phantom_blocks; /* tests only, normally 0: grid barriers of the PCG wait for
                                             this many blocks that do not exist, so their bounded wait
                                             runs out and the solve reports GOM_E_TIMEOUT */
-    int32_t reserved[3];
+    int32_t precision;         /* GOM_PRECISION_FP64 (default) or GOM_PRECISION_MIXED */
+    int32_t turbulence_flag;   /* i_turbulence_flag of turbulence_closure_v1.f90: 0 off (Av, Kv keep
+                                  their values, as in the reference time loop), 1 step function of
+                                  the Richardson number, 2 Pacanowski-Philander */
+    int32_t reserved;
+    /* Pacanowski-Philander coefficients (h1_pp, h2_pp, vdmax_pp1, vdmax_pp2, vdmin_pp1, vdmin_pp2,
+       tdmin_pp of mod_global_variables.f90:909-910) */
+    double pp_h1, pp_h2, pp_vdmax1, pp_vdmax2, pp_vdmin1, pp_vdmin2, pp_tdmin;
 } gom_params;
+
+/* Arithmetic of a context (no reference counterpart: the reference is FP64 throughout).
+ *   GOM_PRECISION_FP64   every state array and every operation in FP64, the reference's order;
+ *   GOM_PRECISION_MIXED  layered state (velocities, thicknesses, tracers, momentum coefficients)
+ *                        stored and computed in FP32; elevations, the free-surface system and its
+ *                        solve, densities, ELM foot coordinates and conservation sums in FP64.
+ * The host interface is the same for both: gom_set_field / gom_get_field take and return FP64
+ * arrays and convert on the way. */
+#define GOM_PRECISION_FP64 0
+#define GOM_PRECISION_MIXED 1
 
 /* ------------------------------------------------------------------ static geometry
  * Produced once on the host by read_node_inp/read_cell_inp, set_geometry_1, set_geometry_2,
@@ -298,11 +315,20 @@ int gom_step_layers(struct gom_ctx *ctx);            /* update_vertical_layers_1
 int gom_step_node_velocity(struct gom_ctx *ctx);     /* calculate_velocity_at_node.f90:10    */
 int gom_step_transport(struct gom_ctx *ctx);         /* solve_transport_equation_v19.f90:7   */
 int gom_step_density(struct gom_ctx *ctx);           /* calculate_density_full.f90:13 / _linear.f90:10 */
+int gom_step_turbulence(struct gom_ctx *ctx);        /* turbulence_closure_v1.f90:9 (schemes 1, 2) */
 int gom_step_swap(struct gom_ctx *ctx);              /* update_variables.f90:4 (state part)  */
 
-/* The whole per-timestep core after forcing, main.f90:94-272 order.  The CUDA library
- * replays it as a captured CUDA graph.  pcg_iters may be NULL. */
+/* The whole per-timestep core after forcing, main.f90:94-272 order, with the turbulence closure
+ * (when turbulence_flag != 0) after the density update.  The CUDA library replays it as a
+ * captured CUDA graph.  pcg_iters may be NULL. */
 int gom_step_all(struct gom_ctx *ctx, int32_t *pcg_iters);
+
+/* gom_step_all split in two, so that many contexts (one per run of an ensemble, each with its own
+ * stream) can have a step in flight at once: gom_step_launch enqueues the step and returns;
+ * gom_step_wait waits for it and returns its status.  gom_set_forcing may stage the next step's
+ * forcing while one step is in flight. */
+int gom_step_launch(struct gom_ctx *ctx);
+int gom_step_wait(struct gom_ctx *ctx, int32_t *pcg_iters);
 
 /* Volume and salt mass of the wet cells: sum(area*dz_cell), sum(area*dz_cell*salt_cell),
  * accumulated in FP64 (spec: check_conservation.f90:28-57). */

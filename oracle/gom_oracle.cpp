@@ -62,6 +62,8 @@ struct gom_ctx {
     Err err;
     std::string msg;
     long long pcg_total = 0;
+    int pending_rc = 0;
+    int32_t pending_iters = 0;
 
     // ---------------- geometry storage
     std::vector<double> g_x_node, g_y_node, g_h_node, g_x_cell, g_y_cell, g_h_cell, g_area;
@@ -2111,6 +2113,89 @@ int gom_step_density(gom_ctx *c) {
     return GOM_OK;
 }
 
+// turbulence_closure_v1.f90:72-138 (i_turbulence_flag 1 and 2).  The reference routine is never
+// called by its time loop and names arrays of another model; they map here to this model's:
+// srho -> rho_face, velocity_normal/tangnt -> un/vn_face (the step's new velocities),
+// dzhalf -> dzhalf_face (new), h_at_face_center -> h_face, ref_water_density -> rho_o.  The face
+// viscosity of interface k (top of layer k) is Av(k, face); the transport diffusivity of a cell
+// interface is the mean over the cell's wet faces of the face diffusivity at the level clamped to
+// the face's wet range, as :446-470 forms it for nodes, with 1e-2 where no face is wet.
+int gom_step_turbulence(gom_ctx *c) {
+    if (!c) return GOM_E_ARG;
+    const gom_params &p = c->p;
+    if (p.turbulence_flag != 1 && p.turbulence_flag != 2) return GOM_OK;
+    const int L = c->L;
+    A2<double> rho_face = FD(c, GOM_F_RHO_FACE), un = FD(c, GOM_F_UN_FACE_NEW), vn = FD(c, GOM_F_VN_FACE_NEW),
+               dzh = FD(c, GOM_F_DZHALF_FACE_NEW), av = FD(c, GOM_F_AV), kv = FD(c, GOM_F_KV);
+    A1<int32_t> top_f = FI1(c, GOM_F_TOP_LAYER_FACE), top_el = FI1(c, GOM_F_TOP_LAYER_CELL);
+    std::vector<double> kvf_store((size_t)(L + 1) * c->NF, 0.0);
+    A2<double> kvf{kvf_store.data(), 0, L + 1};
+    const double g = p.gravity;
+    for (int i = 1; i <= c->NF; ++i) {
+        int b = c->bottom_layer_at_face(i), t = top_f(i);
+        double vmax = 0.0, vmin = 0.0;
+        if (p.turbulence_flag == 2) {
+            double h = c->h_face(i);
+            if (h <= p.pp_h1) {
+                vmax = p.pp_vdmax1;
+                vmin = p.pp_vdmin1;
+            } else if (h < p.pp_h2) {
+                vmax = p.pp_vdmax1 + (p.pp_vdmax2 - p.pp_vdmax1) * (h - p.pp_h1) / (p.pp_h2 - p.pp_h1);
+                vmin = p.pp_vdmin1 + (p.pp_vdmin2 - p.pp_vdmin1) * (h - p.pp_h1) / (p.pp_h2 - p.pp_h1);
+            } else {
+                vmax = p.pp_vdmax2;
+                vmin = p.pp_vdmin2;
+            }
+        }
+        for (int k = b; k <= t; ++k) {
+            double ri;
+            if (k == t) {
+                ri = F(0.0f);
+            } else {
+                double drhodz = (rho_face(k + 1, i) - rho_face(k, i)) / dzh(k, i);
+                double bvf = -g * (drhodz / p.rho_o + g / (double)(1.5e3f * 1.5e3f));
+                double dundz = (un(k + 1, i) - un(k, i)) / dzh(k, i);
+                double dutdz = (vn(k + 1, i) - vn(k, i)) / dzh(k, i);
+                double shear2 = dundz * dundz + dutdz * dutdz;
+                shear2 = std::max(shear2, 1.0e-10);
+                ri = std::max(bvf / shear2, 0.0);
+            }
+            if (p.turbulence_flag == 1) {
+                const double vdiffc = 1.0e-3, tdiffc = F(1.0f) * vdiffc;
+                if (ri < F(0.25f)) {
+                    av(k, i) = vdiffc;
+                    kvf(k, i) = tdiffc;
+                } else {
+                    av(k, i) = 1.0e-5;
+                    kvf(k, i) = 1.0e-5;
+                }
+            } else {
+                double x = 1.0 + 5.0 * ri;
+                av(k, i) = vmax / (x * x) + vmin;
+                kvf(k, i) = av(k, i) / (F(1.0f) + F(5.0f) * ri) + p.pp_tdmin;
+            }
+        }
+    }
+    for (int i = 1; i <= c->NC; ++i) {
+        int t = top_el(i);
+        if (t == 0) continue;
+        for (int k = c->bottom_layer_at_element(i); k <= t; ++k) {
+            double sum = 0.0;
+            int icount = 0;
+            for (int l = 1; l <= c->tri_or_quad(i); ++l) {
+                int isd = c->facenum_at_cell(l, i);
+                if (top_f(isd) != 0) {
+                    icount = icount + 1;
+                    int klev = std::min(std::max(k, c->bottom_layer_at_face(isd)), top_f(isd));
+                    sum = sum + kvf(klev, isd);
+                }
+            }
+            kv(k, i) = icount == 0 ? F(1.0e-2f) : sum / icount;
+        }
+    }
+    return GOM_OK;
+}
+
 // update_variables.f90:16-31 (state part; the vertical means feed output only)
 int gom_step_swap(gom_ctx *c) {
     if (!c) return GOM_E_ARG;
@@ -2137,7 +2222,20 @@ int gom_step_all(gom_ctx *c, int32_t *pcg_iters) {
     if ((e = gom_step_node_velocity(c))) return e;
     if ((e = gom_step_transport(c))) return e;
     if ((e = gom_step_density(c))) return e;
+    if ((e = gom_step_turbulence(c))) return e;
     return gom_step_swap(c);
+}
+
+int gom_step_launch(gom_ctx *c) {
+    if (!c) return GOM_E_ARG;
+    c->pending_rc = gom_step_all(c, &c->pending_iters);
+    return GOM_OK;
+}
+
+int gom_step_wait(gom_ctx *c, int32_t *pcg_iters) {
+    if (!c) return GOM_E_ARG;
+    if (pcg_iters) *pcg_iters = c->pending_iters;
+    return c->pending_rc;
 }
 
 // spec: check_conservation.f90:28-57

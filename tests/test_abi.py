@@ -6,7 +6,7 @@ from pathlib import Path
 
 import pytest
 
-from gom_release_gb300.core import FIELDS, GomCore, GomDims, GomError, load_library
+from gom_release_gb300.core import ABI_VERSION, FIELDS, GomCore, GomDims, GomError, load_library
 
 ROOT = Path(__file__).resolve().parent.parent
 HEADER = ROOT / "include" / "gom_core.h"
@@ -43,7 +43,7 @@ def test_oracle_exports_the_time_loop_abi(oracle_so):
 def test_abi_version_and_field_sizes(core_so, oracle_so):
     for so in (core_so, oracle_so):
         lib = load_library(so)
-        assert lib.gom_abi_version() == 1
+        assert lib.gom_abi_version() == ABI_VERSION
         d = GomDims(10, 23, 14, 5, 12, 3, 1, 0)
         n = C.c_int64()
         eb = C.c_int32()

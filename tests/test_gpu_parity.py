@@ -124,3 +124,27 @@ def test_fused_graph_equals_per_phase(oracle_so, gpu_lib):
             b.step(ph)
     for name in FIELDS:
         assert _exact_mismatch(a.get_field(name), b.get_field(name)) == 0, name
+
+
+def test_async_launch_overlaps_next_forcing(gpu_lib):
+    """gom_step_launch returns before the step ends; the next step's forcing is staged while it
+    runs, and the state equals the synchronous gom_step_all sequence."""
+    deck = estuary(nx=20, ny=10, dx=100.0, n_layers=8, trans_sub_iter=2)
+    st = initial_state(deck)
+    a = GomCore(deck, lib=gpu_lib)
+    b = GomCore(deck, lib=gpu_lib)
+    prepare(a, st)
+    prepare(b, st)
+    fa, fb = HostForcing(deck), HostForcing(deck)   # each sends the constant arrays once
+    b.set_forcing(fb.step(1))
+    b.step_launch()
+    for it in range(1, 7):
+        a.set_forcing(fa.step(it))
+        a.step_all()
+        if it < 6:
+            b.set_forcing(fb.step(it + 1))   # staged while step `it` may still run
+        b.step_wait()
+        if it < 6:
+            b.step_launch()
+    for name in FIELDS:
+        assert _exact_mismatch(a.get_field(name), b.get_field(name)) == 0, name

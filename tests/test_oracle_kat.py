@@ -219,3 +219,76 @@ def test_pcg_iteration_cap_returns(oracle_so):
     deck.params.max_iteration_pcg = 2
     r = _run(deck, oracle_so, steps=2)
     assert r.pcg_iters == [2, 2]
+
+
+# ----------------------------------------------------------------- turbulence closure (A13)
+def _closure_core(so, flag, rho_profile, shear):
+    """A small estuary column set-up with prescribed face densities and velocity shear."""
+    deck = estuary(nx=8, ny=6, dx=100.0, n_layers=8, trans_sub_iter=1, turbulence_flag=flag)
+    core = GomCore(deck, lib_path=so)
+    prepare(core, initial_state(deck))
+    L = deck.n_layers
+    nf = deck.n_faces
+    k = np.arange(1, L + 1, dtype=float)
+    core.set_field("rho_face", np.tile(rho_profile(k), nf))
+    core.set_field("un_face_new", np.tile(shear * k, nf))
+    core.set_field("vn_face_new", np.zeros(nf * L))
+    core.set_field("dzhalf_face_new", core.get_field("dzhalf_face"))
+    core.step("turbulence")
+    return deck, core
+
+
+def _wet_interfaces(deck, core):
+    top = core.get_field("top_layer_face")
+    bot = deck.geo["bottom_layer_at_face"]
+    L = deck.n_layers
+    av = core.get_field("av").reshape(deck.n_faces, L + 1)
+    for j in range(deck.n_faces):
+        if top[j]:
+            yield j, range(bot[j], top[j] + 1), av[j]
+
+
+def test_pp_closure_neutral_limit(oracle_so):
+    """Uniform density: N^2 = -g^2/c^2 < 0, so Ri = 0 and Av = vmax + vmin at every wet interface
+    (depth below h1: vmax = vdmax1); the cell diffusivity is the face value Av + tdmin."""
+    deck, core = _closure_core(oracle_so, 2, lambda k: np.full_like(k, 1020.0), 0.0)
+    p = deck.params
+    want_av = p.pp_vdmax1 / 1.0 + p.pp_vdmin1
+    n = 0
+    for j, ks, av in _wet_interfaces(deck, core):
+        if deck.geo["h_face"][j] <= p.pp_h1:
+            for k in ks:
+                assert av[k] == want_av
+                n += 1
+    assert n > 0
+    kv = core.get_field("kv").reshape(deck.n_cells, deck.n_layers + 1)
+    top = core.get_field("top_layer_cell")
+    bot = deck.geo["bottom_layer_at_element"]
+    for i in range(deck.n_cells):
+        if top[i] and deck.geo["h_cell"][i] < p.pp_h1:
+            np.testing.assert_allclose(kv[i, bot[i]:top[i] + 1], want_av + p.pp_tdmin, rtol=1e-15)
+
+
+def test_pp_closure_strong_stratification_limit(oracle_so):
+    """Density decreasing upwards with no shear: Ri = N^2 / 1e-10 is huge, Av -> vmin and the face
+    diffusivity -> tdmin below the surface interface (where Ri = 0 by definition)."""
+    deck, core = _closure_core(oracle_so, 2, lambda k: 1025.0 - 0.5 * k, 0.0)
+    p = deck.params
+    for j, ks, av in _wet_interfaces(deck, core):
+        ks = list(ks)
+        for k in ks[:-1]:
+            assert abs(av[k] - p.pp_vdmin1) < 1e-12 * max(1.0, p.pp_vdmax1) or deck.geo["h_face"][j] > p.pp_h1
+        assert av[ks[-1]] >= p.pp_vdmin1   # surface interface: Ri = 0
+
+
+def test_step_closure_switches_at_critical_richardson(oracle_so):
+    """Scheme 1: Av = Kv = 1e-3 where Ri < 0.25 and 1e-5 otherwise; strong shear with weak
+    stratification is sub-critical, no shear with stable stratification is super-critical."""
+    deck, core = _closure_core(oracle_so, 1, lambda k: 1025.0 - 0.01 * k, 0.5)
+    for _, ks, av in _wet_interfaces(deck, core):
+        assert all(av[k] == 1e-3 for k in ks)
+    deck, core = _closure_core(oracle_so, 1, lambda k: 1025.0 - 0.5 * k, 0.0)
+    for _, ks, av in _wet_interfaces(deck, core):
+        ks = list(ks)
+        assert all(av[k] == 1e-5 for k in ks[:-1])
+        assert av[ks[-1]] == 1e-3
