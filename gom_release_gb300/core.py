@@ -31,7 +31,29 @@ FIELDS = [
     "salt_cell", "salt_cell_new", "temp_cell", "temp_cell_new", "salt_node", "temp_node",
     "salt_face", "temp_face", "rho_cell", "rho_node", "rho_face", "num_sub_elm",
     "cdb", "gamma_b", "qu_boundary", "elm_foot", "elm_near_edge",
+    "wind_stress_normal", "wind_stress_tangnt", "gamma_t", "air_p", "eta_at_ob_old", "eta_at_ob_new",
 ]
+
+_CELL_FIELDS = {"eta_cell", "eta_cell_new", "wn_cell", "wn_cell_new", "dz_cell", "dz_cell_new", "dzhalf_cell",
+                "dzhalf_cell_new", "top_layer_cell", "kv", "salt_cell", "salt_cell_new", "temp_cell",
+                "temp_cell_new", "rho_cell"}
+_NODE_FIELDS = {"eta_node", "wetdry_node", "u_node", "v_node", "w_node", "dz_node", "dz_node_new", "dzhalf_node",
+                "dzhalf_node_new", "top_layer_node", "salt_node", "temp_node", "rho_node", "num_sub_elm"}
+
+
+def field_kind(name: str) -> str:
+    """Entity a field is indexed by: 'cell', 'face', 'node', 'qb' (river cells) or 'ob'."""
+    if name == "qu_boundary":
+        return "qb"
+    if name in ("eta_at_ob_old", "eta_at_ob_new"):
+        return "ob"
+    if name == "air_p":
+        return "node"
+    if name in _CELL_FIELDS:
+        return "cell"
+    if name in _NODE_FIELDS:
+        return "node"
+    return "face"
 FIELD_ID = {name: i + 1 for i, name in enumerate(FIELDS)}
 
 ERR_NAMES = {0: "GOM_OK", 1: "GOM_E_ARG", 2: "GOM_E_CUDA", 3: "GOM_E_NOT_SPD", 4: "GOM_E_ZERO_PIVOT",
@@ -45,7 +67,7 @@ _I = C.POINTER(C.c_int32)
 class GomDims(C.Structure):
     _fields_ = [("n_cells", C.c_int32), ("n_faces", C.c_int32), ("n_nodes", C.c_int32),
                 ("n_layers", C.c_int32), ("max_nb", C.c_int32), ("n_ob", C.c_int32),
-                ("n_qb", C.c_int32), ("reserved", C.c_int32)]
+                ("n_qb", C.c_int32), ("n_runs", C.c_int32)]
 
 
 _PARAM_D = ["gravity", "rho_o", "msl", "dt", "theta", "adv_onoff_depth", "von_karman", "cd_const",
@@ -75,6 +97,7 @@ _GEOM = [
     ("adj_cellnum_at_face", _I), ("nodenum_at_face", _I), ("bottom_layer_at_face", _I),
     ("boundary_type_of_face", _I), ("isflowside3", _I), ("coriolis_factor", _D), ("manning", _D),
     ("bf_height", _D), ("ob_cell_id", _I), ("qb_cell", _I), ("qb_face", _I), ("z_level", _D), ("delta_z", _D),
+    ("run_cell_start", _I), ("run_face_start", _I), ("run_node_start", _I), ("run_ob_start", _I),
 ]
 
 
@@ -87,6 +110,11 @@ class GomForcing(C.Structure):
                 ("reserved", C.c_double), ("eta_at_ob_old", _D), ("eta_at_ob_new", _D), ("q_add", _D),
                 ("wind_stress_normal", _D), ("wind_stress_tangnt", _D), ("gamma_t", _D), ("air_p", _D),
                 ("con_at_ob", _D), ("con_at_qb", _D), ("phi_sw", _D)]
+
+
+class GomStorm(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("x0", "y0", "heading", "speed", "rmax", "dp", "b", "coriolis",
+                                           "tide_amplitude", "tide_period", "tide_phase", "spinup")]
 
 
 class GomStatus(C.Structure):
@@ -133,6 +161,10 @@ def _bind(lib: C.CDLL) -> C.CDLL:
     lib.gom_step_launch.argtypes = [vp]
     lib.gom_step_wait.argtypes = [vp, C.POINTER(C.c_int32)]
     lib.gom_conservation.argtypes = [vp, _D, _D]
+    lib.gom_set_storms.argtypes = [vp, C.c_int32, C.POINTER(GomStorm), C.c_double]
+    lib.gom_cold_start.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_double]
+    lib.gom_device_bytes.argtypes = [vp]
+    lib.gom_device_bytes.restype = C.c_int64
     lib.gom_get_status.argtypes = [vp, C.POINTER(GomStatus), C.c_int]
     lib.gom_synchronize.argtypes = [vp]
     lib.gom_pcg_iterations_total.argtypes = [vp]
@@ -184,7 +216,9 @@ class GomCore:
         self.deck = deck
         d = deck
         p = d.params
-        self.dims = GomDims(d.n_cells, d.n_faces, d.n_nodes, d.n_layers, d.max_nb, d.n_ob, d.n_qb, 0)
+        runs = getattr(d, "runs", None)
+        self.dims = GomDims(d.n_cells, d.n_faces, d.n_nodes, d.n_layers, d.max_nb, d.n_ob, d.n_qb,
+                            len(runs["run_cell_start"]) - 1 if runs else 0)
         self.params = GomParams(*[getattr(p, n) for n in _PARAM_D], *[int(getattr(p, n)) for n in _PARAM_I], 0,
                                 *[getattr(p, n) for n in _PARAM_PP])
         g = d.geo
@@ -198,6 +232,11 @@ class GomCore:
                 arr = d.z_level
             elif name == "delta_z":
                 arr = d.delta_z
+            elif name.startswith("run_"):
+                if not runs:
+                    keep[name] = None
+                    continue
+                arr = runs[name]
             else:
                 arr = g[name]
             keep[name] = _dbl(arr) if kind is _D else _int(arr)
@@ -293,6 +332,19 @@ class GomCore:
 
     def synchronize(self):
         self._check(self.lib.gom_synchronize(self.ctx), "synchronize")
+
+    def cold_start(self, salt: float, temp: float, av_0: float, kv_0: float):
+        """Initial state built on the device (then ``step("density")`` as prepare does)."""
+        self._check(self.lib.gom_cold_start(self.ctx, salt, temp, av_0, kv_0), "cold_start")
+
+    def device_bytes(self) -> int:
+        return int(self.lib.gom_device_bytes(self.ctx))
+
+    def set_storms(self, storms, elapsed_time: float = 0.0):
+        """Device-side storm forcing, one storm per run (objects with gom_storm's fields)."""
+        arr = (GomStorm * len(storms))(*[GomStorm(*[float(getattr(s, n)) for n, _ in GomStorm._fields_])
+                                         for s in storms])
+        self._check(self.lib.gom_set_storms(self.ctx, len(storms), arr, float(elapsed_time)), "set_storms")
 
     def conservation(self) -> tuple[float, float]:
         v = C.c_double()

@@ -35,6 +35,7 @@ struct gom_ctx {
     bool mixed = false;
     int device = 0;
     std::vector<void *> allocs;
+    size_t bytes = 0;     // device memory held by the context
     std::string msg;
     FieldDesc fields[GOM_F_COUNT];
     // forcing arrays on the device (the Forcing view points into these)
@@ -53,6 +54,9 @@ struct gom_ctx {
     long long pcg_total = 0;
     cudaGraphExec_t graph = nullptr;
     bool graph_failed = false;
+    // device-side storm forcing (gom_set_storms)
+    double *d_storms = nullptr, *storm_wu = nullptr, *storm_wv = nullptr;
+    int n_storms = 0;
 };
 
 namespace {
@@ -77,6 +81,7 @@ template <typename T> cudaError_t dalloc(gom_ctx *c, T **p, size_t n) {
     cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
     if (e == cudaSuccess) {
         c->allocs.push_back(*p);
+        c->bytes += n * sizeof(T);
         e = cudaMemset(*p, 0, n * sizeof(T));
     }
     return e;
@@ -119,7 +124,7 @@ template <typename T> cudaError_t upload(gom_ctx *c, const T **dst, const T *src
 }
 
 int64_t field_count(const gom_dims &d, const FieldDesc &f) {
-    int64_t n = f.kind == 0 ? d.n_cells : f.kind == 1 ? d.n_faces : f.kind == 2 ? d.n_nodes : d.n_qb;
+    int64_t n = f.kind == 0 ? d.n_cells : f.kind == 1 ? d.n_faces : f.kind == 2 ? d.n_nodes : f.kind == 3 ? d.n_qb : d.n_ob;
     if (f.lo < 0) return n;
     return n * (int64_t)(d.n_layers - f.lo + 1);
 }
@@ -188,7 +193,16 @@ template <typename R> void describe_fields(gom_ctx *c, StateT<R> &s) {
     E(GOM_F_QU_BOUNDARY, &s.qu_boundary, -1, 3);
     I(GOM_F_ELM_FOOT, &s.elm_foot, 1, 1);
     I(GOM_F_ELM_NEAR_EDGE, &s.elm_near_edge, 1, 1);
+    // forcing arrays (allocated with the forcing, not with the state)
+    E(GOM_F_WIND_STRESS_NORMAL, &c->f_wsn, -1, 1);
+    E(GOM_F_WIND_STRESS_TANGNT, &c->f_wst, -1, 1);
+    E(GOM_F_GAMMA_T, &c->f_gamma_t, -1, 1);
+    E(GOM_F_AIR_P, &c->f_air_p, -1, 2);
+    E(GOM_F_ETA_AT_OB_OLD, &c->f_eta_old, -1, 4);
+    E(GOM_F_ETA_AT_OB_NEW, &c->f_eta_new, -1, 4);
 }
+
+bool is_forcing_field(int f) { return f >= GOM_F_WIND_STRESS_NORMAL && f <= GOM_F_ETA_AT_OB_NEW; }
 
 // state arrays that update_variables.f90:16-31 copies from *_new to the old name
 const int kSwapPairs[][2] = {{GOM_F_ETA_CELL, GOM_F_ETA_CELL_NEW},   {GOM_F_WN_CELL, GOM_F_WN_CELL_NEW},
@@ -212,6 +226,9 @@ cudaError_t enqueue_swap(gom_ctx *c) {
 // the phases of main.f90:94-272 in order
 template <typename R> cudaError_t enqueue_step_t(gom_ctx *c, const LaunchT<R> &x) {
     cudaError_t e;
+    if (c->n_storms > 0 &&
+        (e = launch_storm_forcing(x.g, x.f, x.p, x.stream, c->d_storms, c->storm_wu, c->storm_wv)))
+        return e;
     if ((e = launch_bottom_friction(x))) return e;
     if ((e = launch_boundary_velocity(x))) return e;
     if ((e = launch_advection(x))) return e;
@@ -370,6 +387,23 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
     UP(z_level, z_level, L + 1, true);
     UP(delta_z, delta_z, L, true);
 #undef UP
+    G.NR = d.n_runs > 1 ? d.n_runs : 1;
+    if (d.n_runs > 1 && e == cudaSuccess) {
+        // packed runs: each range starts at 0, never decreases and ends at the entity count
+        const int32_t *starts[4] = {g->run_cell_start, g->run_face_start, g->run_node_start, g->run_ob_start};
+        const int32_t totals[4] = {d.n_cells, d.n_faces, d.n_nodes, d.n_ob};
+        for (int t = 0; t < 4; ++t) {
+            const int32_t *v = starts[t];
+            if (!v || v[0] != 0 || v[d.n_runs] != totals[t]) return fail(GOM_E_ARG);
+            for (int r = 0; r < d.n_runs; ++r)
+                if (v[r + 1] < v[r] || (t == 0 && v[r + 1] == v[r])) return fail(GOM_E_ARG);
+        }
+        const size_t NR1 = (size_t)d.n_runs + 1;
+        e = upload(c, &G.run_cell_start, (const int *)g->run_cell_start, NR1, true);
+        if (e == cudaSuccess) e = upload(c, &G.run_face_start, (const int *)g->run_face_start, NR1, true);
+        if (e == cudaSuccess) e = upload(c, &G.run_node_start, (const int *)g->run_node_start, NR1, true);
+        if (e == cudaSuccess) e = upload(c, &G.run_ob_start, (const int *)g->run_ob_start, NR1, true);
+    }
     if (e != cudaSuccess) return fail(e == cudaErrorInvalidValue ? GOM_E_ARG : GOM_E_CUDA);
     // column orders: entity ids (1-based) stably sorted by bottom layer
     {
@@ -387,7 +421,7 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
     // state
     for (int f = 1; f < GOM_F_COUNT && e == cudaSuccess; ++f) {
         const FieldDesc &fd = c->fields[f];
-        if (fd.lo == -2) continue;
+        if (fd.lo == -2 || is_forcing_field(f)) continue;
         size_t n = (size_t)field_count(d, fd);
         if (fd.is_int) e = dalloc(c, (int **)fd.dev, n);
         else if (fd.dev_bytes == 4) e = dalloc(c, (float **)fd.dev, n);
@@ -434,6 +468,8 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
     if (e == cudaSuccess) e = dalloc(c, &W.d1, NC);
     if (e == cudaSuccess) e = dalloc(c, &W.barrier, 2);
     if (e == cudaSuccess) e = dalloc(c, &W.pcg_iters, 1);
+    if (e == cudaSuccess) e = dalloc(c, &W.run_block_start, (size_t)G.NR + 1);
+    if (e == cudaSuccess) e = dalloc(c, &W.run_iters, (size_t)G.NR);
     if (e == cudaSuccess) e = c->mixed ? alloc_layered_work(c, c->xf.w) : alloc_layered_work(c, W);
     if (e == cudaSuccess) e = dalloc(c, &W.idev, L * NF);
     if (e == cudaSuccess) e = dalloc(c, &W.node_weight, NN);
@@ -492,7 +528,14 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
     for (int h = 0; h < 2; ++h)
         if (cudaEventCreateWithFlags(&c->stage_done[h], cudaEventDisableTiming) != cudaSuccess) return fail(GOM_E_CUDA);
     std::memset(c->h_status, 0, sizeof(gom_status));
-    if (pcg_configure(c->x, c->device) != cudaSuccess) return fail(GOM_E_CUDA);
+    {
+        cudaError_t pe = pcg_configure(c->x, c->device);
+        if (pe == cudaErrorInvalidValue) {
+            c->msg = "packed runs: more runs than the free-surface solver grid holds";
+            return fail(GOM_E_ARG);
+        }
+        if (pe != cudaSuccess) return fail(GOM_E_CUDA);
+    }
     if (launch_node_weights(c->x) != cudaSuccess) return fail(GOM_E_CUDA);
     {
         size_t nb = (size_t)c->x.w.pcg_blocks;
@@ -523,6 +566,8 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
         X.w.pcg_iters = W.pcg_iters;
         X.w.pcg_blocks = W.pcg_blocks;
         X.w.pcg_threads = W.pcg_threads;
+        X.w.run_block_start = W.run_block_start;
+        X.w.run_iters = W.run_iters;
         X.w.idev = W.idev;
         X.w.node_weight = W.node_weight;
         X.w.cons = W.cons;
@@ -648,6 +693,8 @@ int gom_synchronize(gom_ctx *c) {
 
 int64_t gom_pcg_iterations_total(gom_ctx *c) { return c ? c->pcg_total : 0; }
 
+int64_t gom_device_bytes(const gom_ctx *c) { return c ? (int64_t)c->bytes : 0; }
+
 void *gom_stream(gom_ctx *c) { return c ? (void *)c->x.stream : nullptr; }
 
 int gom_step_bottom_friction(gom_ctx *c) { return run_phase(c, GOM_PHASE(launch_bottom_friction)); }
@@ -717,6 +764,45 @@ int gom_step_all(gom_ctx *c, int32_t *pcg_iters) {
     int rc = gom_step_launch(c);
     if (rc != GOM_OK) return rc;
     return gom_step_wait(c, pcg_iters);
+}
+
+int gom_cold_start(gom_ctx *c, double salt, double temp, double av_0, double kv_0) {
+    if (!c) return GOM_E_ARG;
+    // every state field starts at zero (setup_cold_start.f90)
+    for (int f = 1; f < GOM_F_COUNT; ++f) {
+        const FieldDesc &fd = c->fields[f];
+        if (fd.lo == -2 || is_forcing_field(f)) continue;
+        CK(cudaMemsetAsync(*fd.dev, 0, (size_t)field_count(c->d, fd) * fd.dev_bytes, c->x.stream));
+    }
+    CK(cudaMemsetAsync(c->x.status, 0, sizeof(gom_status), c->x.stream));
+    CK(c->mixed ? launch_cold_start(c->xf, salt, temp, av_0, kv_0) : launch_cold_start(c->x, salt, temp, av_0, kv_0));
+    return finish(c, nullptr, false);
+}
+
+int gom_set_storms(gom_ctx *c, int32_t n_storms, const gom_storm *storms, double elapsed_time) {
+    if (!c || !storms || n_storms != c->x.g.NR) return GOM_E_ARG;
+    static_assert(sizeof(gom_storm) == 12 * sizeof(double), "gom_storm is 12 doubles");
+    for (int r = 0; r < n_storms; ++r) {
+        const gom_storm &s = storms[r];
+        if (!(s.rmax > 0.0) || !(s.dp >= 0.0) || !(s.b > 0.0) || !(s.tide_period > 0.0) || s.coriolis == 0.0)
+            return GOM_E_ARG;
+    }
+    CK(cudaStreamSynchronize(c->x.stream));
+    if (!c->d_storms) {
+        CK(dalloc(c, &c->d_storms, (size_t)12 * n_storms));
+        CK(dalloc(c, &c->storm_wu, (size_t)c->d.n_nodes));
+        CK(dalloc(c, &c->storm_wv, (size_t)c->d.n_nodes));
+    }
+    CK(cudaMemcpy(c->d_storms, storms, sizeof(gom_storm) * n_storms, cudaMemcpyHostToDevice));
+    const double scal0[1] = {elapsed_time};
+    CK(cudaMemcpy(c->f_scal, scal0, sizeof(double), cudaMemcpyHostToDevice));
+    c->n_storms = n_storms;
+    // the captured step gains the forcing kernels: capture again on the next launch
+    if (c->graph) {
+        cudaGraphExecDestroy(c->graph);
+        c->graph = nullptr;
+    }
+    return GOM_OK;
 }
 
 int gom_conservation(gom_ctx *c, double *volume, double *salt_mass) {

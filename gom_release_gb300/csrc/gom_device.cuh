@@ -41,6 +41,9 @@ struct Geom {
     // entity ids sorted by bottom layer: column kernels take their entity from these so that the
     // 32 lanes of a warp walk columns of nearly equal height (results do not depend on the order)
     const int *cell_order, *face_order, *node_order;
+    // packed runs (NR > 1): 0-based first cell / face / node / open-boundary cell of each run
+    int NR;
+    const int *run_cell_start, *run_face_start, *run_node_start, *run_ob_start;
 
     // 1-based accessors of the (m, N) connectivity arrays
     __device__ __forceinline__ int cell_node(int l, int i) const { return nodenum_at_cell[(i - 1) * 4 + l - 1]; }

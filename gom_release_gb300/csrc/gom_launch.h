@@ -16,6 +16,8 @@ template <typename R> struct WorkT {
     unsigned *barrier = nullptr;                               // [count, generation]
     int *pcg_iters = nullptr;                                  // device: iterations of the last solve
     int pcg_blocks = 0, pcg_threads = 256;
+    int *run_block_start = nullptr;   // packed runs: first PCG block of each run (NR + 1), device
+    int *run_iters = nullptr;         // packed runs: PCG iterations of each run's last solve, device
     float *sp32 = nullptr;       // mixed precision: FP32 copy of the system (0:4, NC)
     // transport
     R *con = nullptr, *con2 = nullptr;        // (0:L+1, NC, 2)
@@ -66,6 +68,15 @@ template <typename R> cudaError_t launch_conservation(const LaunchT<R> &x);
 template <typename R> cudaError_t pcg_configure(LaunchT<R> &x, int device);
 // static per-node weights of calculate_velocity_at_node.f90:103; called once per context
 template <typename R> cudaError_t launch_node_weights(const LaunchT<R> &x);
+
+// cold start on the device (all state fields must have been cleared first)
+template <typename R>
+cudaError_t launch_cold_start(const LaunchT<R> &x, double salt, double temp, double av0, double kv0);
+
+// per-step storm-surge forcing on the device (k_forcing.cu): advances the elapsed time by dt and
+// writes the forcing arrays of f from the runs' storms (12 doubles each, gom_storm order)
+cudaError_t launch_storm_forcing(const Geom &g, const Forcing &f, const Params &p, cudaStream_t stream,
+                                 const double *storms, double *wu, double *wv);
 
 // explicit instantiations live in the kernel files
 #define GOM_INSTANTIATE_LAUNCH(fn)                              \

@@ -350,6 +350,349 @@ __global__ void __launch_bounds__(PCG_THREADS) k_pcg_mixed(PcgMixedArgs a) {
     if (blockIdx.x == 0 && threadIdx.x == 0) *a.iters = iters;
 }
 
+// -------------------------------------------------------------------- packed runs
+// A packed context holds several independent runs; its free-surface matrix is block diagonal.
+// Each run keeps its own PCG: the grid's blocks are split among the runs (run_block_start), a
+// block works only on its run's rows, and after every grid barrier each block recomputes every
+// run's scalars from the per-block partial sums in a fixed order, so all blocks agree on every
+// run's alpha, beta and stop test, and on when all runs have stopped.  A converged run freezes
+// while the others continue; the kernel ends when every run has stopped.
+constexpr int PCG_MAX_RUNS = 256;
+
+struct RunRows {
+    int run, c0, c1;     // run index, rows [c0, c1)
+    long start, stride;  // first row of this thread, row stride within the run
+};
+
+__device__ __forceinline__ RunRows run_rows(const Geom &g, const int *run_block_start) {
+    int lo = 0, hi = g.NR;   // find r with run_block_start[r] <= blockIdx.x < run_block_start[r+1]
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (run_block_start[mid] <= (int)blockIdx.x) lo = mid;
+        else hi = mid;
+    }
+    RunRows rr;
+    rr.run = lo;
+    rr.c0 = g.run_cell_start[lo];
+    rr.c1 = g.run_cell_start[lo + 1];
+    int nb = run_block_start[lo + 1] - run_block_start[lo];
+    rr.start = rr.c0 + (long)(blockIdx.x - run_block_start[lo]) * blockDim.x + threadIdx.x;
+    rr.stride = (long)nb * blockDim.x;
+    return rr;
+}
+
+// sum of run r's block partials in block order
+__device__ __forceinline__ double run_sum(const double *part, const int *run_block_start, int r) {
+    double t = 0.0;
+    for (int b = run_block_start[r]; b < run_block_start[r + 1]; ++b) t += ((volatile const double *)part)[b];
+    return t;
+}
+
+struct PcgSegArgs {
+    Geom g;
+    const double *sp, *b;
+    double *x, *minv, *r, *s, *q, *dA, *dB, *pdq, *pdelta;
+    const int *run_block_start;
+    int *run_iters;
+    unsigned *bar;
+    int *iters;
+    int maxit;
+    double tol;
+    gom_status *st;
+    unsigned phantom;
+};
+
+__global__ void __launch_bounds__(PCG_THREADS) k_pcg_seg(PcgSegArgs a) {
+    __shared__ double sh[40];
+    __shared__ double s_d0[PCG_MAX_RUNS], s_dn[PCG_MAX_RUNS], s_alpha[PCG_MAX_RUNS], s_beta[PCG_MAX_RUNS];
+    __shared__ int s_done[PCG_MAX_RUNS], s_it[PCG_MAX_RUNS];
+    const Geom &g = a.g;
+    const int NR = g.NR;
+    const unsigned nblocks = gridDim.x + a.phantom;
+    const RunRows me = run_rows(g, a.run_block_start);
+    double loc = 0.0;
+    for (long i = me.start; i < me.c1; i += me.stride) {
+        const double *row = a.sp + i * 5;
+        int cell = (int)i + 1;
+        double sum = row[0] * a.x[i];
+        int tq = g.tri_or_quad[i];
+        for (int l = 1; l <= tq; ++l) {
+            int nb = g.cell_adj(l, cell);
+            if (nb != 0) sum = fma(row[l], a.x[nb - 1], sum);
+        }
+        double mi = 1.0 / row[0];
+        double ri = a.b[i] - sum;
+        double di = mi * ri;
+        a.minv[i] = mi;
+        a.r[i] = ri;
+        a.dA[i] = di;
+        loc = fma(ri, di, loc);
+    }
+    double bs = block_sum<PCG_THREADS>(loc, sh);
+    if (threadIdx.x == 0) a.pdelta[blockIdx.x] = bs;
+    if (!grid_barrier(a.bar, nblocks, a.st)) return;
+    for (int r = threadIdx.x; r < NR; r += blockDim.x) {
+        double d0 = run_sum(a.pdelta, a.run_block_start, r);
+        s_d0[r] = d0;
+        s_dn[r] = d0;
+        s_done[r] = d0 == 0.0;
+        s_it[r] = 0;
+    }
+    __syncthreads();
+    double *dcur = a.dA, *dnext = a.dB;
+    bool first = true;
+    for (int it = 1; it <= a.maxit; ++it) {
+        if (failed(a.st)) return;
+        int active = 0;
+        for (int r = 0; r < NR; ++r) active |= !s_done[r];
+        if (!active) break;
+        const bool mine = !s_done[me.run];
+        loc = 0.0;
+        if (mine) {
+            const double beta = s_beta[me.run];
+            for (long i = me.start; i < me.c1; i += me.stride) {
+                const double *row = a.sp + i * 5;
+                int cell = (int)i + 1;
+                double di = first ? dcur[i] : fma(beta, dcur[i], a.s[i]);
+                double sum = row[0] * di;
+                int tq = g.tri_or_quad[i];
+                for (int l = 1; l <= tq; ++l) {
+                    int nb = g.cell_adj(l, cell);
+                    if (nb != 0) {
+                        double dn = first ? dcur[nb - 1] : fma(beta, dcur[nb - 1], a.s[nb - 1]);
+                        sum = fma(row[l], dn, sum);
+                    }
+                }
+                if (!first) dnext[i] = di;
+                a.q[i] = sum;
+                loc = fma(di, sum, loc);
+            }
+        }
+        bs = block_sum<PCG_THREADS>(loc, sh);
+        if (threadIdx.x == 0) a.pdq[blockIdx.x] = bs;
+        if (!grid_barrier(a.bar, nblocks, a.st)) return;
+        for (int r = threadIdx.x; r < NR; r += blockDim.x)
+            if (!s_done[r]) s_alpha[r] = s_dn[r] / run_sum(a.pdq, a.run_block_start, r);
+        __syncthreads();
+        loc = 0.0;
+        if (mine) {
+            const double alpha = s_alpha[me.run];
+            double *dv = first ? dcur : dnext;
+            for (long i = me.start; i < me.c1; i += me.stride) {
+                double di = dv[i];
+                a.x[i] = fma(alpha, di, a.x[i]);
+                double ri = fma(-alpha, a.q[i], a.r[i]);
+                a.r[i] = ri;
+                double si = a.minv[i] * ri;
+                a.s[i] = si;
+                loc = fma(ri, si, loc);
+            }
+        }
+        bs = block_sum<PCG_THREADS>(loc, sh);
+        if (threadIdx.x == 0) a.pdelta[blockIdx.x] = bs;
+        if (!grid_barrier(a.bar, nblocks, a.st)) return;
+        for (int r = threadIdx.x; r < NR; r += blockDim.x) {
+            if (s_done[r]) continue;
+            double dold = s_dn[r];
+            double dn = run_sum(a.pdelta, a.run_block_start, r);
+            s_dn[r] = dn;
+            s_beta[r] = dn / dold;
+            s_it[r] = it;
+            if (sqrt(dn * dn / (s_d0[r] * s_d0[r])) < a.tol) s_done[r] = 1;
+        }
+        __syncthreads();
+        if (!first) {
+            double *t = dcur;
+            dcur = dnext;
+            dnext = t;
+        }
+        first = false;
+    }
+    if (blockIdx.x == 0) {
+        for (int r = threadIdx.x; r < NR; r += blockDim.x) a.run_iters[r] = s_it[r];
+        if (threadIdx.x == 0) {
+            int mx = 0;
+            for (int r = 0; r < NR; ++r) mx = max(mx, s_it[r]);
+            *a.iters = mx;
+        }
+    }
+}
+
+// mixed precision, packed runs: each run runs the refinement / inner-iteration scheme of
+// k_pcg_mixed as a state machine (true-residual pass, then inner iterations until its inner
+// stop, then a residual pass again ...); all runs advance in lockstep through the same two
+// barriers per step, each doing the work its own state asks for.
+struct PcgMixedSegArgs {
+    Geom g;
+    const double *sp, *b;
+    double *x;
+    float *sp32, *minv, *r, *s, *q, *dA, *dB;
+    double *pdq, *pdelta;
+    const int *run_block_start;
+    int *run_iters;
+    unsigned *bar;
+    int *iters;
+    int maxit;
+    double tol;
+    gom_status *st;
+    unsigned phantom;
+};
+
+enum { RUN_RESID = 0, RUN_INNER = 1, RUN_DONE = 2 };
+
+__global__ void __launch_bounds__(PCG_THREADS) k_pcg_mixed_seg(PcgMixedSegArgs a) {
+    __shared__ double sh[40];
+    __shared__ double s_d0[PCG_MAX_RUNS];
+    __shared__ float s_dn[PCG_MAX_RUNS], s_din0[PCG_MAX_RUNS], s_itol[PCG_MAX_RUNS], s_alpha[PCG_MAX_RUNS],
+        s_beta[PCG_MAX_RUNS];
+    __shared__ int s_mode[PCG_MAX_RUNS], s_first[PCG_MAX_RUNS], s_dpar[PCG_MAX_RUNS], s_outer[PCG_MAX_RUNS],
+        s_it[PCG_MAX_RUNS], s_passb[PCG_MAX_RUNS];
+    const Geom &g = a.g;
+    const int NR = g.NR;
+    const unsigned nblocks = gridDim.x + a.phantom;
+    const RunRows me = run_rows(g, a.run_block_start);
+    const float FP32_FLOOR = 1e-10f;
+    for (long i = me.start; i < me.c1; i += me.stride) {
+        const double *row = a.sp + i * 5;
+        float *row32 = a.sp32 + i * 5;
+        for (int l = 0; l < 5; ++l) row32[l] = (float)row[l];
+        a.minv[i] = (float)(1.0 / row[0]);
+    }
+    for (int r = threadIdx.x; r < NR; r += blockDim.x) {
+        s_mode[r] = RUN_RESID;
+        s_outer[r] = 0;
+        s_it[r] = 0;
+        s_first[r] = 1;
+        s_dpar[r] = 0;
+    }
+    __syncthreads();
+    for (int step = 0;; ++step) {
+        if (failed(a.st)) return;
+        int active = 0;
+        for (int r = 0; r < NR; ++r) active |= s_mode[r] != RUN_DONE;
+        if (!active) break;
+        const int mode = s_mode[me.run];
+        const bool first = s_first[me.run] != 0;
+        float *dcur = s_dpar[me.run] ? a.dB : a.dA, *dnext = s_dpar[me.run] ? a.dA : a.dB;
+        // pass A: true residual (RESID) or inner matrix-vector product (INNER)
+        double loc = 0.0;
+        float floc = 0.0f;
+        if (mode == RUN_RESID) {
+            for (long i = me.start; i < me.c1; i += me.stride) {
+                const double *row = a.sp + i * 5;
+                int cell = (int)i + 1;
+                double sum = row[0] * a.x[i];
+                int tq = g.tri_or_quad[i];
+                for (int l = 1; l <= tq; ++l) {
+                    int nb = g.cell_adj(l, cell);
+                    if (nb != 0) sum = fma(row[l], a.x[nb - 1], sum);
+                }
+                double ri = a.b[i] - sum;
+                loc = fma(ri, ri / row[0], loc);
+                float rf = (float)ri;
+                float df = a.minv[i] * rf;
+                a.r[i] = rf;
+                a.dA[i] = df;
+                floc = fmaf(rf, df, floc);
+            }
+        } else if (mode == RUN_INNER) {
+            const float beta = s_beta[me.run];
+            for (long i = me.start; i < me.c1; i += me.stride) {
+                const float *row = a.sp32 + i * 5;
+                int cell = (int)i + 1;
+                float di = first ? dcur[i] : fmaf(beta, dcur[i], a.s[i]);
+                float sum = row[0] * di;
+                int tq = g.tri_or_quad[i];
+                for (int l = 1; l <= tq; ++l) {
+                    int nb = g.cell_adj(l, cell);
+                    if (nb != 0) {
+                        float dn = first ? dcur[nb - 1] : fmaf(beta, dcur[nb - 1], a.s[nb - 1]);
+                        sum = fmaf(row[l], dn, sum);
+                    }
+                }
+                if (!first) dnext[i] = di;
+                a.q[i] = sum;
+                floc = fmaf(di, sum, floc);
+            }
+        }
+        double bs = block_sum<PCG_THREADS>(loc, sh);
+        float fbs = block_sumf<PCG_THREADS>(floc, sh);
+        if (threadIdx.x == 0) {
+            a.pdelta[blockIdx.x] = bs;
+            a.pdq[blockIdx.x] = (double)fbs;
+        }
+        if (!grid_barrier(a.bar, nblocks, a.st)) return;
+        for (int r = threadIdx.x; r < NR; r += blockDim.x) {
+            s_passb[r] = 0;
+            if (s_mode[r] == RUN_RESID) {
+                double dt = run_sum(a.pdelta, a.run_block_start, r);
+                float di = (float)run_sum(a.pdq, a.run_block_start, r);
+                bool stop;
+                if (s_outer[r] == 0) {
+                    s_d0[r] = dt;
+                    stop = dt == 0.0;
+                } else {
+                    stop = sqrt(dt * dt / (s_d0[r] * s_d0[r])) < a.tol;
+                }
+                if (stop || s_it[r] >= a.maxit || !(di > 0.0f)) {
+                    s_mode[r] = RUN_DONE;
+                } else {
+                    s_mode[r] = RUN_INNER;
+                    s_outer[r] += 1;
+                    s_din0[r] = di;
+                    s_dn[r] = di;
+                    s_itol[r] = fmaxf((float)(0.25 * a.tol * s_d0[r] / dt), FP32_FLOOR);
+                    s_first[r] = 1;
+                    s_dpar[r] = 0;
+                }
+                if (s_outer[r] == 0) s_outer[r] = 1;
+            } else if (s_mode[r] == RUN_INNER) {
+                s_alpha[r] = s_dn[r] / (float)run_sum(a.pdq, a.run_block_start, r);
+                s_passb[r] = 1;
+            }
+        }
+        __syncthreads();
+        // pass B: inner updates of the runs that did a matrix-vector product in pass A
+        floc = 0.0f;
+        if (s_passb[me.run]) {
+            const float alpha = s_alpha[me.run];
+            float *dv = first ? dcur : dnext;
+            for (long i = me.start; i < me.c1; i += me.stride) {
+                float di = dv[i];
+                a.x[i] = a.x[i] + (double)(alpha * di);
+                float ri = fmaf(-alpha, a.q[i], a.r[i]);
+                a.r[i] = ri;
+                float si = a.minv[i] * ri;
+                a.s[i] = si;
+                floc = fmaf(ri, si, floc);
+            }
+        }
+        fbs = block_sumf<PCG_THREADS>(floc, sh);
+        if (threadIdx.x == 0) a.pdelta[blockIdx.x] = (double)fbs;
+        if (!grid_barrier(a.bar, nblocks, a.st)) return;
+        for (int r = threadIdx.x; r < NR; r += blockDim.x) {
+            if (!s_passb[r]) continue;
+            float dold = s_dn[r];
+            float dn = (float)run_sum(a.pdelta, a.run_block_start, r);
+            s_dn[r] = dn;
+            s_beta[r] = dn / dold;
+            if (!s_first[r]) s_dpar[r] ^= 1;
+            s_first[r] = 0;
+            s_it[r] += 1;
+            if (dn < s_itol[r] * s_din0[r] || !(dn > 0.0f) || s_it[r] >= a.maxit) s_mode[r] = RUN_RESID;
+        }
+        __syncthreads();
+    }
+    if (blockIdx.x == 0) {
+        for (int r = threadIdx.x; r < NR; r += blockDim.x) a.run_iters[r] = s_it[r];
+        if (threadIdx.x == 0) {
+            int mx = 0;
+            for (int r = 0; r < NR; ++r) mx = max(mx, s_it[r]);
+            *a.iters = mx;
+        }
+    }
+}
+
 // grid of the cooperative launch: enough blocks for one row per thread, at most two resident
 // blocks per SM (and never more than the occupancy allows)
 inline int pcg_blocks_for(long n_rows, int per_sm, int num_sms) {

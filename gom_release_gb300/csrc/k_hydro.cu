@@ -276,17 +276,17 @@ __device__ int search_straight_line(const Geom &g, const StateT<R> &s, const Par
     return 0;
 }
 
-__device__ double edge_distance(const Geom &g, int nel, double x, double y) {
-    double dmin = 1e300;
+// diagnostic for foot parity: (x, y) lies within 1e-12 m of an edge line of element nel, tested
+// as cross^2 < (1e-12)^2 * |edge|^2 (cross = edge x (point - edge start)): no root, no division
+__device__ bool near_edge_line(const Geom &g, int nel, double x, double y) {
     int tq = g.tri_or_quad[nel - 1];
     for (int l = 1; l <= tq; ++l) {
         int a = g.cell_node(l, nel), b = g.cell_node(start_end_node(tq, l, 1), nel);
         double ex = g.x_node[b - 1] - g.x_node[a - 1], ey = g.y_node[b - 1] - g.y_node[a - 1];
-        double len = sqrt(ex * ex + ey * ey);
-        double cr = fabs(ex * (y - g.y_node[a - 1]) - ey * (x - g.x_node[a - 1])) / len;
-        dmin = fmin(dmin, cr);
+        double cr = ex * (y - g.y_node[a - 1]) - ey * (x - g.x_node[a - 1]);
+        if (cr * cr < 1e-24 * (ex * ex + ey * ey)) return true;
     }
-    return dmin;
+    return false;
 }
 
 // ELM_backtrace_v1.f90:40-200 (mode 1)
@@ -351,7 +351,7 @@ __device__ int elm_backtrace(const Geom &g, const StateT<R> &s, const Params &p,
             vv = vv + vyn[j] * sta[j];
             ww = ww + vzn[j] * sta[j];
         }
-        if (edge_distance(g, nnel, xt, yt) < 1e-12) near_edge = 1;
+        if (near_edge_line(g, nnel, xt, yt)) near_edge = 1;
         if (nfl == 1) break;
         x0 = xt;
         y0 = yt;
@@ -548,7 +548,17 @@ __device__ double face_final_rtemp0(const Geom &g, const StateT<R> &s, const For
 
 template <typename R>
 __device__ double prev_rtemp0(const Geom &g, const StateT<R> &s, const Forcing &f, const Params &p, int j) {
-    for (int jj = j - 1; jj >= 1; --jj) {
+    int first = 1;   // first face of j's run: the walk never leaves the run (each starts at 0)
+    if (g.NR > 1) {
+        int lo = 0, hi = g.NR;
+        while (hi - lo > 1) {
+            int mid = (lo + hi) >> 1;
+            if (g.run_face_start[mid] <= j - 1) lo = mid;
+            else hi = mid;
+        }
+        first = g.run_face_start[lo] + 1;
+    }
+    for (int jj = j - 1; jj >= first; --jj) {
         if (s.top_face[jj - 1] == 0) continue;
         bool known;
         double v = face_final_rtemp0(g, s, f, p, jj, known);

@@ -7,6 +7,9 @@
 #include "gom_launch.h"
 #include "gom_pcg.cuh"
 
+#include <algorithm>
+#include <vector>
+
 namespace gom {
 
 // ============================================================================================
@@ -127,20 +130,59 @@ template <typename R> __global__ void k_node_eta_dry(Geom g, StateT<R> s) {
 }
 
 template <typename R> cudaError_t pcg_configure(LaunchT<R> &x, int device) {
-    int per_sm = 0, per_sm_mixed = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg, PCG_THREADS, 0);
-    if (e != cudaSuccess) return e;
-    // every block of the cooperative grid must be resident for either solver
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_mixed, k_pcg_mixed, PCG_THREADS, 0);
-    if (e != cudaSuccess) return e;
-    if (per_sm_mixed < per_sm) per_sm = per_sm_mixed;
+    // every block of the cooperative grid must be resident, whichever solver the context uses
+    int per_sm = 1 << 30;
+    const void *kernels[] = {(const void *)k_pcg, (const void *)k_pcg_mixed, (const void *)k_pcg_seg,
+                             (const void *)k_pcg_mixed_seg};
+    for (const void *k : kernels) {
+        int n = 0;
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, PCG_THREADS, 0);
+        if (e != cudaSuccess) return e;
+        per_sm = std::min(per_sm, n);
+    }
     if (per_sm < 1) per_sm = 1;
     int coop = 0;
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device);
     if (!coop) return cudaErrorNotSupported;
-    x.w.pcg_blocks = pcg_blocks_for(x.g.NC, per_sm, x.num_sms);
     x.w.pcg_threads = PCG_THREADS;
-    return cudaSuccess;
+    if (x.g.NR <= 1) {
+        x.w.pcg_blocks = pcg_blocks_for(x.g.NC, per_sm, x.num_sms);
+        return cudaSuccess;
+    }
+    // packed runs: one block at least per run, the rest of the grid split in proportion to the
+    // rows (largest remainders), never more blocks than rows / threads
+    const int NR = x.g.NR;
+    std::vector<int> cs(NR + 1);
+    cudaError_t e = cudaMemcpy(cs.data(), x.g.run_cell_start, (NR + 1) * sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return e;
+    const long cap = (long)x.num_sms * std::min(per_sm, 2);
+    if (NR > PCG_MAX_RUNS || NR > cap) return cudaErrorInvalidValue;
+    std::vector<long> want(NR), got(NR, 1);
+    long spare = cap - NR;
+    const double total = (double)cs[NR];
+    std::vector<std::pair<double, int>> rem;
+    for (int r = 0; r < NR; ++r) {
+        long rows = cs[r + 1] - cs[r];
+        want[r] = std::max(1L, (rows + PCG_THREADS - 1) / PCG_THREADS);
+        double share = spare * (rows / total);
+        long extra = std::min((long)share, want[r] - 1);
+        got[r] += extra;
+        rem.push_back({share - (double)(long)share, r});
+    }
+    long used = 0;
+    for (long v : got) used += v;
+    std::sort(rem.begin(), rem.end(), [](auto &p, auto &q) { return p.first > q.first || (p.first == q.first && p.second < q.second); });
+    for (auto &pr : rem) {
+        if (used >= cap) break;
+        if (got[pr.second] < want[pr.second]) {
+            got[pr.second] += 1;
+            used += 1;
+        }
+    }
+    std::vector<int> rbs(NR + 1, 0);
+    for (int r = 0; r < NR; ++r) rbs[r + 1] = rbs[r] + (int)got[r];
+    x.w.pcg_blocks = rbs[NR];
+    return cudaMemcpy(x.w.run_block_start, rbs.data(), (NR + 1) * sizeof(int), cudaMemcpyHostToDevice);
 }
 
 template <typename R> cudaError_t launch_free_surface(const LaunchT<R> &x) {
@@ -159,6 +201,60 @@ template <typename R> cudaError_t launch_free_surface(const LaunchT<R> &x) {
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     const unsigned phantom = (unsigned)(x.p.test_barrier_phantom_blocks > 0 ? x.p.test_barrier_phantom_blocks : 0);
+    if (g.NR > 1 && x.w.sp32) {
+        PcgMixedSegArgs m;
+        m.g = g;
+        m.sp = x.w.sparsem;
+        m.b = x.w.rhs;
+        m.x = x.s.eta_cell_new;
+        m.sp32 = x.w.sp32;
+        m.minv = reinterpret_cast<float *>(x.w.minv);
+        m.r = reinterpret_cast<float *>(x.w.r);
+        m.s = reinterpret_cast<float *>(x.w.s);
+        m.q = reinterpret_cast<float *>(x.w.q);
+        m.dA = reinterpret_cast<float *>(x.w.d0);
+        m.dB = reinterpret_cast<float *>(x.w.d1);
+        m.pdq = x.w.partial_dq;
+        m.pdelta = x.w.partial_delta;
+        m.run_block_start = x.w.run_block_start;
+        m.run_iters = x.w.run_iters;
+        m.bar = x.w.barrier;
+        m.iters = x.w.pcg_iters;
+        m.maxit = x.p.max_iteration_pcg;
+        m.tol = x.p.error_tolerance;
+        m.st = x.status;
+        m.phantom = phantom;
+        e = cudaLaunchKernelEx(&cfg, k_pcg_mixed_seg, m);
+    } else if (g.NR > 1) {
+        PcgSegArgs m;
+        m.g = g;
+        m.sp = x.w.sparsem;
+        m.b = x.w.rhs;
+        m.x = x.s.eta_cell_new;
+        m.minv = x.w.minv;
+        m.r = x.w.r;
+        m.s = x.w.s;
+        m.q = x.w.q;
+        m.dA = x.w.d0;
+        m.dB = x.w.d1;
+        m.pdq = x.w.partial_dq;
+        m.pdelta = x.w.partial_delta;
+        m.run_block_start = x.w.run_block_start;
+        m.run_iters = x.w.run_iters;
+        m.bar = x.w.barrier;
+        m.iters = x.w.pcg_iters;
+        m.maxit = x.p.max_iteration_pcg;
+        m.tol = x.p.error_tolerance;
+        m.st = x.status;
+        m.phantom = phantom;
+        e = cudaLaunchKernelEx(&cfg, k_pcg_seg, m);
+    }
+    if (g.NR > 1) {
+        if (e != cudaSuccess) return e;
+        k_node_eta<<<blocks_for(g.NN, 256), 256, 0, x.stream>>>(x.g, x.s);
+        k_node_eta_dry<<<blocks_for(g.NN, 256), 256, 0, x.stream>>>(x.g, x.s);
+        return cudaGetLastError();
+    }
     if (x.w.sp32) {
         // mixed precision: the FP64 work vectors hold the FP32 inner vectors
         PcgMixedArgs m;
@@ -464,6 +560,112 @@ template <typename R> cudaError_t launch_layers(const LaunchT<R> &x) {
     k_layers_check<<<blocks_for(x.g.NC, 256), 256, 0, x.stream>>>(x.g, x.s, x.p, x.status);
     return cudaGetLastError();
 }
+
+// ============================================================================================
+// Cold start on the device (setup_cold_start.f90: eta = 0, no motion; update_vertical_layers_0.f90:
+// the first layers and thicknesses; uniform tracers), for contexts whose initial 3-D state is
+// too large to build on the host.  update_vertical_layers_0.f90 gives the edge half-thicknesses
+// to faces and nodes (:146-263), not to cells.
+template <int KIND, typename R>
+__global__ void k_cold_layers(Geom g, Params p, int n, const double *h, const int *bottom, int *top, R *dz, R *dzh,
+                              gom_status *st) {
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    const int L = g.L;
+    const double msl = p.msl, eta = 0.0;
+    const double he = h[e], total = he + eta;
+    R *z = dz + (long)e * L;
+    R *zh = dzh + (long)e * (L + 1);
+    int t = 0;
+    if (total > p.dry_depth) {
+        const double tmp = msl + eta;
+        for (int k = L - 1; k >= 0; --k) {
+            if (tmp > g.z_level[k] && tmp <= g.z_level[k + 1]) {
+                t = k + 1;
+                z[t - 1] = (R)(tmp - g.z_level[k]);
+                break;
+            }
+        }
+        const int b = bottom[e];
+        if (t < b) {
+            record_error(st, GOM_E_LAYER, 66, e + 1, t, eta);
+            return;
+        }
+        if (t == b) {
+            z[t - 1] = (R)total;
+            if (KIND == 1) zh[t - 1] = (R)total;
+            zh[t] = (R)total;
+        } else {
+            z[b - 1] = (R)(g.z_level[b] - (msl - he));
+            for (int k = b + 1; k <= t - 1; ++k) z[k - 1] = (R)g.delta_z[k - 1];
+            for (int k = b; k <= t - 1; ++k) zh[k] = (z[k] + z[k - 1]) * R(0.5);
+            if (KIND != 0) {
+                zh[t] = z[t - 1];
+                zh[b - 1] = z[b - 1];
+            }
+        }
+    }
+    top[e] = t;
+}
+
+// :270-286 an element all of whose nodes are dry is dry; tracers, Av, Kv and ELM substeps
+template <typename R>
+__global__ void k_cold_cells(Geom g, StateT<R> s, Params p, R salt, R temp, R av0, R kv0, gom_status *st) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int L = g.L;
+    if (i <= g.NC) {
+        int n1 = 0, n2 = 0, tq = g.tri_or_quad[i - 1];
+        for (int l = 1; l <= tq; ++l) {
+            n1 += s.top_node[g.cell_node(l, i) - 1];
+            n2 += s.top_face[g.cell_face(l, i) - 1];
+        }
+        if (n1 == 0) s.top_cell[i - 1] = 0;
+        if (n2 == 0 && s.top_cell[i - 1] != 0) record_error(st, GOM_E_DRY, 273, i, 0, 0.0);
+        for (int k = 1; k <= L; ++k) {
+            long o = ix(k, i, L);
+            s.salt_cell[o] = salt;
+            s.salt_cell_new[o] = salt;
+            s.temp_cell[o] = temp;
+            s.temp_cell_new[o] = temp;
+            s.kv[ix0(k, i, L)] = kv0;
+        }
+    }
+    if (i <= g.NF) {
+        for (int k = 1; k <= L; ++k) {
+            long o = ix(k, i, L);
+            s.salt_face[o] = salt;
+            s.temp_face[o] = temp;
+            s.av[ix0(k, i, L)] = av0;
+        }
+    }
+    if (i <= g.NN) {
+        int nsub = p.elm_backtrace_flag == 0 ? p.elm_sub_iter : p.elm_backtrace_flag == 1 ? 1 : 0;
+        for (int k = 1; k <= L; ++k) {
+            long o = ix(k, i, L);
+            s.salt_node[o] = salt;
+            s.temp_node[o] = temp;
+            s.num_sub_elm[o] = nsub;
+        }
+    }
+}
+
+template <typename R>
+cudaError_t launch_cold_start(const LaunchT<R> &x, double salt, double temp, double av0, double kv0) {
+    const Geom &g = x.g;
+    k_cold_layers<0, R><<<blocks_for(g.NC, 256), 256, 0, x.stream>>>(g, x.p, g.NC, g.h_cell, g.bottom_cell,
+                                                                       x.s.top_cell, x.s.dz_cell, x.s.dzhalf_cell, x.status);
+    k_cold_layers<1, R><<<blocks_for(g.NF, 256), 256, 0, x.stream>>>(g, x.p, g.NF, g.h_face, g.bottom_face,
+                                                                       x.s.top_face, x.s.dz_face, x.s.dzhalf_face, x.status);
+    k_cold_layers<2, R><<<blocks_for(g.NN, 256), 256, 0, x.stream>>>(g, x.p, g.NN, g.h_node, g.bottom_node,
+                                                                       x.s.top_node, x.s.dz_node, x.s.dzhalf_node, x.status);
+    int n = std::max(g.NC, std::max(g.NF, g.NN));
+    k_cold_cells<R><<<blocks_for(n, 256), 256, 0, x.stream>>>(g, x.s, x.p, (R)salt, (R)temp, (R)av0, (R)kv0,
+                                                                 x.status);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_cold_start<double>(const LaunchT<double> &, double, double, double, double);
+template cudaError_t launch_cold_start<float>(const LaunchT<float> &, double, double, double, double);
 
 // ============================================================================================
 // calculate_velocity_at_node.f90:31-60: face-level velocities, one thread per face column.  The

@@ -20,7 +20,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from .mesh import (RawMesh, build_geometry, bottom_layers, find_element_and_face,
+from .mesh import (RawMesh, build_geometry, bottom_layers, find_elements_and_faces,
                    fourier_noise, square_strip_mesh)
 
 PI = 3.141592653589793          # mod_global_variables.f90: pi
@@ -117,6 +117,7 @@ class Deck:
     init_salt_node: np.ndarray | None = None        # (N_n, L)
     init_temp_node: np.ndarray | None = None
     meta: dict = field(default_factory=dict)
+    runs: dict | None = None        # packed runs: run_{cell,face,node,ob}_start (n_runs + 1)
 
     @property
     def n_ob(self) -> int:
@@ -136,14 +137,10 @@ def uniform_z_levels(z_bottom: float, z_top: float, n_layers: int) -> tuple[np.n
 
 
 def _boundaries(geo, pairs):
-    cells, faces = [], []
-    for n1, n2 in pairs:
-        e, f = find_element_and_face(geo, int(n1), int(n2))
-        if e == 0 or f == 0:
-            raise ValueError("boundary node pair not found in CCW order")
-        cells.append(e)
-        faces.append(f)
-    return np.array(cells, dtype=np.int32), np.array(faces, dtype=np.int32)
+    cells, faces = find_elements_and_faces(geo, pairs)
+    if np.any(cells == 0) or np.any(faces == 0):
+        raise ValueError("boundary node pair not found in CCW order")
+    return cells.astype(np.int32), faces.astype(np.int32)
 
 
 def _finish(name, raw, L, z_bottom, z_top, params, ob_pairs, q_pairs, q_portion, **kw) -> Deck:
@@ -299,41 +296,45 @@ def initial_state(deck: Deck, eta0: np.ndarray | None = None) -> dict:
         eta_node = num / den
 
     def column(h, eta, bottom, with_edges):
-        """update_vertical_layers_0.f90:42-140 (cells, with_edges=False) and :146-263."""
+        """update_vertical_layers_0.f90:42-140 (cells, with_edges=False) and :146-263, for all
+        entities at once with the same per-element arithmetic."""
         n = len(h)
-        top = np.zeros(n, np.int32)
+        h = np.asarray(h, dtype=np.float64)
+        eta = np.asarray(eta, dtype=np.float64)
+        b = np.asarray(bottom, dtype=np.int64)
+        total = h + eta
+        tmp = msl + eta
+        wet = total > p.dry_depth
+        t = np.searchsorted(z, tmp, side="left")        # count of z_level below tmp
+        t = np.where(wet & (t >= 1) & (t <= L), t, 0)
+        if np.any(wet & (t < b)):
+            raise ValueError("impossible elevation at start (update_vertical_layers_0.f90:66-81)")
         dz = np.zeros((n, L))
         dzh = np.zeros((n, L + 1))
-        for e in range(n):
-            total = h[e] + eta[e]
-            if total <= p.dry_depth:
-                continue
-            tmp = msl + eta[e]
-            t = 0
-            for k in range(L - 1, -1, -1):
-                if tmp > z[k] and tmp <= z[k + 1]:
-                    t = k + 1
-                    dz[e, t - 1] = tmp - z[k]
-                    break
-            b = bottom[e]
-            if t < b:
-                raise ValueError("impossible elevation at start (update_vertical_layers_0.f90:66-81)")
-            if t == b:
-                dz[e, t - 1] = total
-                if with_edges == "face":
-                    dzh[e, t - 1] = total
-                dzh[e, t] = total
-            else:
-                dz[e, b - 1] = z[b] - (msl - h[e])
-                for k in range(b + 1, t):
-                    dz[e, k - 1] = dzl[k - 1]
-                for k in range(b, t):
-                    dzh[e, k] = (dz[e, k] + dz[e, k - 1]) * 0.5
-                if with_edges in ("face", "node"):
-                    dzh[e, t] = dz[e, t - 1]
-                    dzh[e, b - 1] = dz[e, b - 1]
-            top[e] = t
-        return top, dz, dzh
+        single = np.nonzero(wet & (t == b))[0]
+        multi = np.nonzero(wet & (t > b))[0]
+        tm, bm = t[multi], b[multi]
+        dz[multi, tm - 1] = tmp[multi] - z[tm - 1]
+        dz[multi, bm - 1] = z[bm] - (msl - h[multi])
+        K = np.arange(1, L + 1)[None, :]
+        mid = np.zeros((n, L), bool)
+        mid[multi] = (K > bm[:, None]) & (K < tm[:, None])
+        dz[mid] = np.broadcast_to(dzl[None, :], (n, L))[mid]
+        half = np.zeros((n, L + 1))
+        half[:, 1:L] = (dz[:, 1:] + dz[:, :-1]) * 0.5
+        KK = np.arange(L + 1)[None, :]
+        inner = np.zeros((n, L + 1), bool)
+        inner[multi] = (KK >= bm[:, None]) & (KK <= tm[:, None] - 1)
+        dzh[inner] = half[inner]
+        if with_edges in ("face", "node"):
+            dzh[multi, tm] = dz[multi, tm - 1]
+            dzh[multi, bm - 1] = dz[multi, bm - 1]
+        ts = t[single]
+        dz[single, ts - 1] = total[single]
+        if with_edges == "face":
+            dzh[single, ts - 1] = total[single]
+        dzh[single, ts] = total[single]
+        return t.astype(np.int32), dz, dzh
 
     top_c, dz_c, dzh_c = column(a["h_cell"], eta_cell_new, a["bottom_layer_at_element"], "cell")
     eta_face = eta_cell_new[a["adj_cellnum_at_face"][:, 0] - 1].copy()

@@ -409,6 +409,41 @@ def find_element_and_face(geo: Geometry, n1: int, n2: int) -> tuple[int, int]:
     return element_id, face_id
 
 
+def find_elements_and_faces(geo: Geometry, pairs) -> tuple[np.ndarray, np.ndarray]:
+    """find_element_and_face.f90:9-67 for many node pairs at once: for each (n1, n2), the lowest
+    cell id whose CCW node list holds n1 then n2 consecutively, and the lowest face stored as
+    (n1, n2); 1-based ids, 0 if absent."""
+    a = geo.arrays
+    cells = a["nodenum_at_cell"]
+    pairs = np.asarray(pairs, dtype=np.int64).reshape(-1, 2)
+    base = np.int64(geo.n_nodes + 1)
+    keys, ids = [], []
+    cell_ids = np.arange(1, cells.shape[0] + 1, dtype=np.int64)
+    for j1 in range(4):
+        nod1 = cells[:, j1].astype(np.int64)
+        nod2 = cells[:, (j1 + 1) % 4].astype(np.int64)
+        nod2 = np.where(nod2 != 0, nod2, cells[:, 0])
+        m = nod1 != 0
+        keys.append(nod1[m] * base + nod2[m])
+        ids.append(cell_ids[m])
+
+    def lookup(k_all, id_all, q):
+        order = np.lexsort((id_all, k_all))
+        ks, vs = k_all[order], id_all[order]
+        first = np.ones(len(ks), bool)
+        first[1:] = ks[1:] != ks[:-1]
+        ks, vs = ks[first], vs[first]
+        pos = np.searchsorted(ks, q)
+        pos = np.minimum(pos, len(ks) - 1)
+        return np.where(ks[pos] == q, vs[pos], 0).astype(np.int32)
+
+    q = pairs[:, 0] * base + pairs[:, 1]
+    elem = lookup(np.concatenate(keys), np.concatenate(ids), q)
+    fn = a["nodenum_at_face"].astype(np.int64)
+    face = lookup(fn[:, 0] * base + fn[:, 1], np.arange(1, fn.shape[0] + 1, dtype=np.int64), q)
+    return elem, face
+
+
 def bottom_layers(h: np.ndarray, msl: float, z_level: np.ndarray) -> np.ndarray:
     """set_geometry_2.f90:101-189: first k with z_level(k) <= MSL-h < z_level(k+1), plus 1."""
     L = len(z_level) - 1

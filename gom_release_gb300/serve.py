@@ -1,0 +1,180 @@
+"""Serving storm-surge runs on one GPU: continuous batching of independent contexts.
+
+A request is one storm-surge run (mesh, storm, horizon).  The server keeps every admitted run's
+state resident in HBM in its own context (own CUDA stream and captured step graph).  Each tick it
+launches one step of every in-flight run (gom_step_launch: the graphs of all runs are queued
+before any is waited for, so their kernels overlap on the device), then waits for them
+(gom_step_wait) and retires the runs that reached their horizon.  Requests that arrive while
+others run are admitted at the next tick when the memory budget has room: the device bytes of a
+new context are estimated from the bytes per cell-layer of the contexts created so far, and the
+estimate is checked against the context's real size once created.
+
+``serve_fifo`` is the comparison the configuration asks for: the same requests served one at a
+time, in arrival order, each run to its horizon before the next starts.
+"""
+from __future__ import annotations
+
+import dataclasses
+import time
+
+import numpy as np
+
+from .core import GomCore
+from .deck import Deck
+
+
+@dataclasses.dataclass
+class Request:
+    rid: int
+    deck: Deck                # mesh + parameters (precision set by the server)
+    storm: object             # gom_storm fields
+    steps: int                # horizon in timesteps
+    arrival: float            # seconds after the start of the stream
+    cell_layers: int = 0      # active cell-layers at the start (work per step)
+    started: float = -1.0
+    finished: float = -1.0
+    done_steps: int = 0
+
+
+def _context(lib, deck: Deck, precision: int, storm) -> GomCore:
+    d = dataclasses.replace(deck, params=dataclasses.replace(deck.params, precision=precision))
+    c = GomCore(d, lib=lib)
+    p = d.params
+    c.cold_start(p.ref_salt, p.ref_temp, p.av_0, p.kv_0)
+    c.step("density")
+    nt = max(1, p.trans_sub_iter)
+    cob = np.zeros((d.n_ob, 2, nt))
+    cob[:, 0, :] = p.ref_salt
+    cob[:, 1, :] = p.ref_temp
+    c.set_forcing({"elapsed_time": 0.0, "spinup_tide": 1.0, "spinup_baroclinic": 1.0, "con_at_ob": cob})
+    c.set_storms([storm], elapsed_time=0.0)
+    return c
+
+
+def active_cell_layers(core: GomCore, deck: Deck) -> int:
+    top = core.get_field("top_layer_cell")
+    bot = deck.geo["bottom_layer_at_element"]
+    wet = top > 0
+    return int(np.sum(top[wet] - bot[wet] + 1))
+
+
+class Server:
+    """Continuous batching of storm-surge runs under a device-memory budget."""
+
+    def __init__(self, lib, budget_bytes: float, precision: int = 1):
+        self.lib = lib
+        self.budget = float(budget_bytes)
+        self.precision = precision
+        self.active: list[tuple[Request, GomCore]] = []
+        self.waiting: list[Request] = []
+        self.used = 0.0
+        self.bytes_per_cell_layer = None   # learned from created contexts
+        self.peak_bytes = 0.0
+        self.peak_active = 0
+
+    def _estimate(self, req: Request) -> float:
+        cl = req.deck.n_cells * (req.deck.n_layers + 2)
+        return cl * (self.bytes_per_cell_layer or 0.0)
+
+    def admit(self, now: float):
+        while self.waiting:
+            req = self.waiting[0]
+            if self.active and self.used + self._estimate(req) > self.budget:
+                return
+            self.waiting.pop(0)
+            core = _context(self.lib, req.deck, self.precision, req.storm)
+            nbytes = core.device_bytes()
+            self.bytes_per_cell_layer = max(self.bytes_per_cell_layer or 0.0,
+                                            nbytes / (req.deck.n_cells * (req.deck.n_layers + 2)))
+            req.cell_layers = active_cell_layers(core, req.deck)
+            req.started = now
+            self.used += nbytes
+            self.peak_bytes = max(self.peak_bytes, self.used)
+            self.active.append((req, core))
+            self.peak_active = max(self.peak_active, len(self.active))
+
+    def tick(self, clock) -> list[Request]:
+        for _, core in self.active:
+            core.step_launch()
+        for _, core in self.active:
+            core.step_wait()
+        now = clock()
+        done, keep = [], []
+        for req, core in self.active:
+            req.done_steps += 1
+            if req.done_steps >= req.steps:
+                req.finished = now
+                self.used -= core.device_bytes()
+                core.close()
+                done.append(req)
+            else:
+                keep.append((req, core))
+        self.active = keep
+        return done
+
+
+def serve(lib, requests: list[Request], budget_bytes: float, precision: int = 1) -> dict:
+    """Replay a request stream in wall time; returns per-request latency and totals."""
+    srv = Server(lib, budget_bytes, precision)
+    pending = sorted(requests, key=lambda r: r.arrival)
+    t0 = time.perf_counter()
+    clock = lambda: time.perf_counter() - t0  # noqa: E731
+    finished: list[Request] = []
+    i = 0
+    work = 0
+    while len(finished) < len(requests):
+        now = clock()
+        while i < len(pending) and pending[i].arrival <= now:
+            srv.waiting.append(pending[i])
+            i += 1
+        srv.admit(now)
+        if not srv.active:
+            if i < len(pending):
+                time.sleep(max(0.0, min(0.01, pending[i].arrival - now)))
+            continue
+        work += sum(r.cell_layers for r, _ in srv.active)
+        finished += srv.tick(clock)
+    wall = clock()
+    return _summary(requests, wall, work, srv.peak_bytes, srv.peak_active)
+
+
+def serve_fifo(lib, requests: list[Request], precision: int = 0) -> dict:
+    """The same requests served one at a time in arrival order."""
+    pending = sorted(requests, key=lambda r: r.arrival)
+    t0 = time.perf_counter()
+    clock = lambda: time.perf_counter() - t0  # noqa: E731
+    work = 0
+    peak = 0.0
+    for req in pending:
+        now = clock()
+        if now < req.arrival:
+            time.sleep(req.arrival - now)
+        core = _context(lib, req.deck, precision, req.storm)
+        peak = max(peak, core.device_bytes())
+        req.cell_layers = active_cell_layers(core, req.deck)
+        req.started = clock()
+        for _ in range(req.steps):
+            core.step_launch()
+            core.step_wait()
+        req.finished = clock()
+        req.done_steps = req.steps
+        work += req.cell_layers * req.steps
+        core.close()
+    return _summary(requests, clock(), work, peak, 1)
+
+
+def _summary(requests, wall, work, peak_bytes, peak_active) -> dict:
+    lat = np.array([r.finished - r.arrival for r in requests])
+    return {"requests": len(requests), "wall_s": wall, "cell_layer_steps": int(work),
+            "throughput": work / wall if wall > 0 else 0.0,
+            "latency_p50_s": float(np.percentile(lat, 50)), "latency_p99_s": float(np.percentile(lat, 99)),
+            "latency_mean_s": float(lat.mean()), "peak_device_bytes": float(peak_bytes),
+            "peak_in_flight": int(peak_active)}
+
+
+def poisson_arrivals(n: int, rate: float, seed: int) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    return np.cumsum(rng.exponential(1.0 / rate, size=n))
+
+
+__all__ = ["Request", "Server", "serve", "serve_fifo", "poisson_arrivals", "active_cell_layers"]

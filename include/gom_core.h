@@ -89,7 +89,12 @@ typedef struct gom_dims {
     int32_t max_nb;     /* max_no_neighbor_node    */
     int32_t n_ob;       /* num_ob_cell             */
     int32_t n_qb;       /* num_Qb_cell             */
-    int32_t reserved;
+    int32_t n_runs;     /* independent runs packed into this context (0 or 1: one run; no
+                           reference counterpart).  A packed context holds several runs' meshes
+                           as one disconnected mesh: each run's cells, faces, nodes and open-
+                           boundary cells are contiguous, connectivity is global, and every
+                           phase advances all runs in one launch; the free-surface solve keeps a
+                           separate PCG (own scalars, own stop test) per run. */
 } gom_dims;
 
 /* ------------------------------------------------------------------ scalar configuration
@@ -190,6 +195,9 @@ typedef struct gom_geom {
     /* vertical grid */
     const double  *z_level;                              /* (0:L)               */
     const double  *delta_z;                              /* (L)                 */
+    /* packed runs (n_runs > 1, else NULL): 0-based first cell / face / node / open-boundary cell
+       of each run, n_runs + 1 entries each, the last being the total */
+    const int32_t *run_cell_start, *run_face_start, *run_node_start, *run_ob_start;
 } gom_geom;
 
 /* ------------------------------------------------------------------ per-step forcing
@@ -273,6 +281,14 @@ typedef enum gom_field {
     GOM_F_QU_BOUNDARY,         /* (n_qb)       */
     GOM_F_ELM_FOOT,            /* (L, N_f) int: element holding the final ELM foot, 0 = no walk */
     GOM_F_ELM_NEAR_EDGE,       /* (L, N_f) int: 1 if a foot landed within 1e-12 m of an edge    */
+    /* per-step forcing arrays (gom_set_forcing uploads them; with storms set the device writes
+       them every step) */
+    GOM_F_WIND_STRESS_NORMAL,  /* (N_f)        */
+    GOM_F_WIND_STRESS_TANGNT,  /* (N_f)        */
+    GOM_F_GAMMA_T,             /* (N_f)        */
+    GOM_F_AIR_P,               /* (N_n)  Pa    */
+    GOM_F_ETA_AT_OB_OLD,       /* (n_ob)       */
+    GOM_F_ETA_AT_OB_NEW,       /* (n_ob)       */
     GOM_F_COUNT
 } gom_field;
 
@@ -329,6 +345,45 @@ int gom_step_all(struct gom_ctx *ctx, int32_t *pcg_iters);
  * forcing while one step is in flight. */
 int gom_step_launch(struct gom_ctx *ctx);
 int gom_step_wait(struct gom_ctx *ctx, int32_t *pcg_iters);
+
+/* Device-side storm-surge forcing (no single reference counterpart: it moves onto the GPU what
+ * the Fortran driver computes on the host each step in setup_spinup.f90, compute_boundary_eta.f90,
+ * holland_storm_surge.f90 and calculate_wind_stress.f90).  One storm per run of the context
+ * (n_runs of gom_dims, 1 for a single run).  Once set, every step of the context first advances
+ * the elapsed time by dt on the device, then evaluates for each run at that time: a Holland
+ * vortex moving on a straight track (the gradient wind of holland_storm_surge.f90:131-188 with a
+ * Holland exponent b, 0.95 gradient-to-surface factor, 18 degree inflow, translation asymmetry),
+ * air pressure p_far - dp (1 - exp(-(rmax/r)^b)) at the nodes, face wind stress by the drag law
+ * of calculate_wind_stress.f90:105-137, and the open-boundary elevation = tide + inverse
+ * barometer, all ramped by tanh(2 t / spinup) as setup_spinup.f90 ramps the tide.  gom_set_forcing
+ * is then needed only for what the storms leave alone (boundary tracer concentrations). */
+typedef struct gom_storm {
+    double x0, y0;             /* eye position at elapsed time 0 (m, mesh coordinates) */
+    double heading;            /* direction of travel (radians from +x)                */
+    double speed;              /* translation speed (m/s)                              */
+    double rmax;               /* radius of maximum winds (m)                          */
+    double dp;                 /* central pressure deficit (Pa, > 0)                   */
+    double b;                  /* Holland exponent                                     */
+    double coriolis;           /* Coriolis parameter at the eye (1/s)                  */
+    double tide_amplitude;     /* open-boundary tide (m)                               */
+    double tide_period;        /* (s)                                                  */
+    double tide_phase;         /* (rad)                                                */
+    double spinup;             /* ramp period (s); 0 = none                            */
+} gom_storm;
+int gom_set_storms(struct gom_ctx *ctx, int32_t n_storms, const gom_storm *storms, double elapsed_time);
+
+/* Cold start computed on the device (no reference counterpart as one routine: it is what
+ * setup_cold_start.f90 + update_vertical_layers_0.f90 + uniform read_salt_init.f90 /
+ * read_temp_init.f90 leave before the time loop): zero elevation and motion, first layers and
+ * thicknesses from the bathymetry, uniform salinity and temperature at cells, faces and nodes,
+ * Av = av_0 and Kv = kv_0 at levels 1..L, ELM substeps as card C5_01 sets them.  Densities are
+ * left at zero: call gom_step_density next, as prepare_gom does.  For contexts too large to
+ * upload a host-built initial state field by field. */
+int gom_cold_start(struct gom_ctx *ctx, double salt, double temp, double av_0, double kv_0);
+
+/* Device memory the context holds (bytes), for admission by memory budget when many contexts
+ * share a GPU. */
+int64_t gom_device_bytes(const struct gom_ctx *ctx);
 
 /* Volume and salt mass of the wet cells: sum(area*dz_cell), sum(area*dz_cell*salt_cell),
  * accumulated in FP64 (spec: check_conservation.f90:28-57). */

@@ -74,6 +74,8 @@ struct gom_ctx {
         g_nodenum_at_cell, g_facenum_at_cell, g_adj_cellnum_at_cell, g_sign_in_outflow, g_bottom_cell,
         g_ob_element_flag, g_qb_element_flag, g_adj_cellnum_at_face, g_nodenum_at_face, g_bottom_face,
         g_boundary_type_of_face, g_isflowside3, g_ob_cell_id, g_qb_cell, g_qb_face;
+    std::vector<int32_t> run_cell_start;   // packed runs: first cell of each run (0-based), n_runs + 1
+    std::vector<int32_t> run_face_start;   // packed runs: first face of each run (0-based), n_runs + 1
 
     // ---------------- state storage, indexed by gom_field
     std::vector<double> fd[GOM_F_COUNT];
@@ -136,6 +138,9 @@ FieldShape field_shape(int f) {
     case GOM_F_TOP_LAYER_NODE: return {-1, 2, 1, 0};
     case GOM_F_CDB: case GOM_F_GAMMA_B: return {-1, 1, 0, 0};
     case GOM_F_QU_BOUNDARY: return {-1, 3, 0, 0};
+    case GOM_F_WIND_STRESS_NORMAL: case GOM_F_WIND_STRESS_TANGNT: case GOM_F_GAMMA_T: return {-1, 1, 0, 0};
+    case GOM_F_AIR_P: return {-1, 2, 0, 0};
+    case GOM_F_ETA_AT_OB_OLD: case GOM_F_ETA_AT_OB_NEW: return {-1, 4, 0, 0};
     default: return {-2, 0, 0, 0};
     }
 }
@@ -143,7 +148,7 @@ FieldShape field_shape(int f) {
 int64_t field_count(const gom_dims &d, int f, int32_t *eb) {
     FieldShape s = field_shape(f);
     if (s.lo == -2) return -1;
-    int64_t n = s.kind == 0 ? d.n_cells : s.kind == 1 ? d.n_faces : s.kind == 2 ? d.n_nodes : d.n_qb;
+    int64_t n = s.kind == 0 ? d.n_cells : s.kind == 1 ? d.n_faces : s.kind == 2 ? d.n_nodes : s.kind == 3 ? d.n_qb : d.n_ob;
     if (eb) *eb = s.is_int ? 4 : 8;
     if (s.lo == -1) return n;
     return n * (int64_t)(d.n_layers - s.lo + 1);
@@ -300,19 +305,18 @@ int bilinear_interpolation(double x1, double x2, double x3, double x4, double y1
     return 0;
 }
 
-// distance from (x, y) to the nearest edge line of element nel (diagnostic for foot parity)
-double edge_distance(gom_ctx *c, int nel, double x, double y) {
-    double dmin = 1e300;
+// diagnostic for foot parity: (x, y) lies within 1e-12 m of an edge line of element nel, tested
+// as cross^2 < (1e-12)^2 * |edge|^2 (cross = edge x (point - edge start))
+bool near_edge_line(gom_ctx *c, int nel, double x, double y) {
     int tq = c->tri_or_quad(nel);
     for (int l = 1; l <= tq; ++l) {
         int a = c->nodenum_at_cell(l, nel);
         int b = c->nodenum_at_cell(start_end_node(tq, l, 1), nel);
         double ex = c->x_node(b) - c->x_node(a), ey = c->y_node(b) - c->y_node(a);
-        double len = std::sqrt(ex * ex + ey * ey);
-        double cr = std::fabs(ex * (y - c->y_node(a)) - ey * (x - c->x_node(a))) / len;
-        dmin = std::min(dmin, cr);
+        double cr = ex * (y - c->y_node(a)) - ey * (x - c->x_node(a));
+        if (cr * cr < 1e-24 * (ex * ex + ey * ey)) return true;
     }
-    return dmin;
+    return false;
 }
 
 // ============================================================================================
@@ -516,7 +520,7 @@ int elm_backtrace(gom_ctx *c, int bt_step, double bt_dt, double &uuint, double &
             vvint = vvint + vyn[j - 1] * staint[j - 1];
             wwint = wwint + vzn[j - 1] * staint[j - 1];
         }
-        if (edge_distance(c, nnel, xt, yt) < 1e-12) near_edge = 1;
+        if (near_edge_line(c, nnel, xt, yt)) near_edge = 1;
         if (nfl == 1) break;
         x0 = xt;
         y0 = yt;
@@ -624,6 +628,21 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
     copy_in(c->g_qb_face, g->qb_face, (size_t)d.n_qb);
     copy_in(c->g_z_level, g->z_level, L + 1);
     copy_in(c->g_delta_z, g->delta_z, L);
+    if (d.n_runs > 1) {
+        if (!g->run_cell_start) {
+            delete c;
+            return GOM_E_ARG;
+        }
+        copy_in(c->run_cell_start, g->run_cell_start, (size_t)d.n_runs + 1);
+        if (!g->run_face_start) {
+            delete c;
+            return GOM_E_ARG;
+        }
+        copy_in(c->run_face_start, g->run_face_start, (size_t)d.n_runs + 1);
+    } else {
+        c->run_cell_start = {0, d.n_cells};
+        c->run_face_start = {0, d.n_faces};
+    }
 
     c->x_node.p = c->g_x_node.data();
     c->y_node.p = c->g_y_node.data();
@@ -693,11 +712,28 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
 
 void gom_destroy(gom_ctx *ctx) { delete ctx; }
 
+// forcing arrays exposed as fields
+std::vector<double> *forcing_field(gom_ctx *c, int field) {
+    switch (field) {
+    case GOM_F_WIND_STRESS_NORMAL: return &c->wind_stress_normal;
+    case GOM_F_WIND_STRESS_TANGNT: return &c->wind_stress_tangnt;
+    case GOM_F_GAMMA_T: return &c->gamma_t;
+    case GOM_F_AIR_P: return &c->air_p;
+    case GOM_F_ETA_AT_OB_OLD: return &c->eta_at_ob_old;
+    case GOM_F_ETA_AT_OB_NEW: return &c->eta_at_ob_new;
+    default: return nullptr;
+    }
+}
+
 int gom_set_field(gom_ctx *c, int field, const void *host, int64_t count) {
     if (!c || !host) return GOM_E_ARG;
     int32_t eb = 0;
     int64_t n = field_count(c->d, field, &eb);
     if (n < 0 || n != count) return GOM_E_ARG;
+    if (std::vector<double> *v = forcing_field(c, field)) {
+        std::memcpy(v->data(), host, (size_t)n * 8);
+        return GOM_OK;
+    }
     if (eb == 4) std::memcpy(c->fi[field].data(), host, (size_t)n * 4);
     else std::memcpy(c->fd[field].data(), host, (size_t)n * 8);
     return GOM_OK;
@@ -708,6 +744,10 @@ int gom_get_field(gom_ctx *c, int field, void *host, int64_t count) {
     int32_t eb = 0;
     int64_t n = field_count(c->d, field, &eb);
     if (n < 0 || n != count) return GOM_E_ARG;
+    if (std::vector<double> *v = forcing_field(c, field)) {
+        std::memcpy(host, v->data(), (size_t)n * 8);
+        return GOM_OK;
+    }
     if (eb == 4) std::memcpy(host, c->fi[field].data(), (size_t)n * 4);
     else std::memcpy(host, c->fd[field].data(), (size_t)n * 8);
     return GOM_OK;
@@ -736,6 +776,10 @@ int gom_set_forcing(gom_ctx *c, const gom_forcing *f) {
     return GOM_OK;
 }
 
+// the CPU restatement takes all forcing from the host, and its initial state from the host
+int gom_set_storms(gom_ctx *c, int32_t, const gom_storm *, double) { return c ? GOM_E_ARG : GOM_E_ARG; }
+int gom_cold_start(gom_ctx *c, double, double, double, double) { return c ? GOM_E_ARG : GOM_E_ARG; }
+
 int gom_get_status(gom_ctx *c, gom_status *s, int clear) {
     if (!c || !s) return GOM_E_ARG;
     s->code = c->err.code;
@@ -750,6 +794,8 @@ int gom_get_status(gom_ctx *c, gom_status *s, int clear) {
 int gom_synchronize(gom_ctx *c) { return c ? GOM_OK : GOM_E_ARG; }
 
 int64_t gom_pcg_iterations_total(gom_ctx *c) { return c ? c->pcg_total : 0; }
+
+int64_t gom_device_bytes(const gom_ctx *) { return 0; }
 
 void *gom_stream(gom_ctx *c) {
     (void)c;
@@ -960,7 +1006,13 @@ int gom_step_momentum(gom_ctx *c) {
     double temp[12] = {0};
     double rtemp0 = 0.0, rtemp1 = 0.0, rtemp2 = 0.0, rtemp3 = 0.0, rtemp4 = 0.0;
     const double c069 = F(0.69f);
+    size_t next_run = 1;
     for (int j = 1; j <= c->NF; ++j) {
+        // each packed run starts with rtemp0 = 0, as one call of the reference does
+        while (next_run < c->run_face_start.size() && j - 1 == c->run_face_start[next_run - 1]) {
+            rtemp0 = 0.0;
+            ++next_run;
+        }
         if (top_f(j) == 0) continue;
         int node1 = c->nodenum_at_face(1, j), node2 = c->nodenum_at_face(2, j);
         int tj = top_f(j), bj = c->bottom_layer_at_face(j);
@@ -1214,46 +1266,53 @@ int gom_step_free_surface(gom_ctx *c, int32_t *pcg_iters) {
         }
     }
     ia[NC] = (int)ja.size();
-    // pre_conj_grad.f90:46-221
+    // pre_conj_grad.f90:46-221, once per packed run on that run's rows (the system is block
+    // diagonal across runs); a context with one run is the reference's single solve
     std::vector<double> Minv(NC), r(NC), d(NC), q(NC), s(NC);
-    for (int i = 0; i < NC; ++i) {
-        double sum1 = 0.0;
-        for (int k = ia[i]; k < ia[i + 1]; ++k) {
-            if (ja[k] == i + 1) Minv[i] = 1.0 / a1[k];
-            sum1 = sum1 + a1[k] * x[ja[k] - 1];
-        }
-        r[i] = rhs_1[i] - sum1;
-    }
-    for (int i = 0; i < NC; ++i) d[i] = Minv[i] * r[i];
-    double delta_new = 0.0;
-    for (int i = 0; i < NC; ++i) delta_new = delta_new + r[i] * d[i];
-    double delta_0 = delta_new;
     int cgit2 = 0;
-    // A zero initial residual would make the reference divide 0 by 0 (alpha = delta/dq);
-    // the restatement returns the initial guess instead.
-    if (delta_0 != 0.0) {
-        for (int cgit = 1; cgit <= p.max_iteration_pcg; ++cgit) {
-            for (int i = 0; i < NC; ++i) {
-                double sum1 = 0.0;
-                for (int k = ia[i]; k < ia[i + 1]; ++k) sum1 = sum1 + a1[k] * d[ja[k] - 1];
-                q[i] = sum1;
+    const int nruns = (int)c->run_cell_start.size() - 1;
+    for (int run = 0; run < nruns; ++run) {
+        const int i0 = c->run_cell_start[run], i1 = c->run_cell_start[run + 1];
+        for (int i = i0; i < i1; ++i) {
+            double sum1 = 0.0;
+            for (int k = ia[i]; k < ia[i + 1]; ++k) {
+                if (ja[k] == i + 1) Minv[i] = 1.0 / a1[k];
+                sum1 = sum1 + a1[k] * x[ja[k] - 1];
             }
-            double dq = 0.0;
-            for (int i = 0; i < NC; ++i) dq = dq + d[i] * q[i];
-            double alpha = delta_new / dq;
-            for (int i = 0; i < NC; ++i) {
-                x[i] = x[i] + alpha * d[i];
-                r[i] = r[i] - alpha * q[i];
-            }
-            for (int i = 0; i < NC; ++i) s[i] = Minv[i] * r[i];
-            double delta_old = delta_new;
-            delta_new = 0.0;
-            for (int i = 0; i < NC; ++i) delta_new = delta_new + r[i] * s[i];
-            double beta = delta_new / delta_old;
-            for (int i = 0; i < NC; ++i) d[i] = s[i] + beta * d[i];
-            cgit2 = cgit;
-            if (std::sqrt(delta_new * delta_new / (delta_0 * delta_0)) < p.error_tolerance) break;
+            r[i] = rhs_1[i] - sum1;
         }
+        for (int i = i0; i < i1; ++i) d[i] = Minv[i] * r[i];
+        double delta_new = 0.0;
+        for (int i = i0; i < i1; ++i) delta_new = delta_new + r[i] * d[i];
+        double delta_0 = delta_new;
+        int run_it = 0;
+        // A zero initial residual would make the reference divide 0 by 0 (alpha = delta/dq);
+        // the restatement returns the initial guess instead.
+        if (delta_0 != 0.0) {
+            for (int cgit = 1; cgit <= p.max_iteration_pcg; ++cgit) {
+                for (int i = i0; i < i1; ++i) {
+                    double sum1 = 0.0;
+                    for (int k = ia[i]; k < ia[i + 1]; ++k) sum1 = sum1 + a1[k] * d[ja[k] - 1];
+                    q[i] = sum1;
+                }
+                double dq = 0.0;
+                for (int i = i0; i < i1; ++i) dq = dq + d[i] * q[i];
+                double alpha = delta_new / dq;
+                for (int i = i0; i < i1; ++i) {
+                    x[i] = x[i] + alpha * d[i];
+                    r[i] = r[i] - alpha * q[i];
+                }
+                for (int i = i0; i < i1; ++i) s[i] = Minv[i] * r[i];
+                double delta_old = delta_new;
+                delta_new = 0.0;
+                for (int i = i0; i < i1; ++i) delta_new = delta_new + r[i] * s[i];
+                double beta = delta_new / delta_old;
+                for (int i = i0; i < i1; ++i) d[i] = s[i] + beta * d[i];
+                run_it = cgit;
+                if (std::sqrt(delta_new * delta_new / (delta_0 * delta_0)) < p.error_tolerance) break;
+            }
+        }
+        cgit2 = std::max(cgit2, run_it);
     }
     if (pcg_iters) *pcg_iters = cgit2;
     c->pcg_total += cgit2;
