@@ -24,6 +24,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -278,6 +279,194 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def time_core_steps(core, k: int) -> float:
+    """k steps of a context with device-side forcing, CUDA events on its stream."""
+    import torch
+    stream = torch.cuda.ExternalStream(core.stream_handle())
+    core.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(k):
+        core.step_launch()
+    e1.record(stream)
+    e1.synchronize()
+    core.step_wait()
+    return e0.elapsed_time(e1) / 1e3
+
+
+def bench_ensemble(args):
+    """Storm-surge ensemble: every run packed into one mixed-precision context (one launch per
+    phase for all runs, per-run PCG, device-side forcing) against the plain FP64 path serving
+    the same runs one at a time on the same GPU."""
+    from gom_release_gb300.core import load_core
+    from gom_release_gb300.ensemble import ensemble_decks, pack
+    from gom_release_gb300.serve import active_cell_layers, storm_context
+    lib = load_core()
+    t0 = time.perf_counter()
+    decks = ensemble_decks(n_runs=args.runs, seed=7, min_cells=max(200, int(5000 * args.scale)),
+                           max_cells=max(400, int(400000 * args.scale)))
+    gen_s = time.perf_counter() - t0
+    storms = [d.meta["storm"] for d in decks]
+    pk = pack(decks)
+    k = args.steps
+    w = max(3, args.warmup)
+    res = {}
+    with ClockSampler(0) as clocks:
+        for label, prec in (("mixed_packed", 1), ("fp64_packed", 0)):
+            if label == "fp64_packed" and args.skip_fp64_packed:
+                continue
+            core = storm_context(lib, pk, prec, storms)
+            ncl = active_cell_layers(core, pk)
+            nbytes = core.device_bytes()
+            time_core_steps(core, w)
+            core.autotune(reps=2)
+            time_core_steps(core, 1)
+            secs = time_core_steps(core, k)
+            res[label] = {"value": ncl * k / secs, "ms_per_step": secs / k * 1e3, "device_gb": nbytes / 1e9,
+                          "active_cell_layers": ncl, "pcg_iters_total": core.pcg_iterations_total()}
+            core.close()
+        kb = max(2, k // 5)
+        for label, prec in (("fp64_one_at_a_time", 0), ("mixed_one_at_a_time", 1)):
+            work = 0
+            tsum = 0.0
+            for d, s in zip(decks, storms):
+                core = storm_context(lib, d, prec, [s])
+                ncl = active_cell_layers(core, d)
+                time_core_steps(core, 1)
+                tsum += time_core_steps(core, kb)
+                work += ncl * kb
+                core.close()
+            res[label] = {"value": work / tsum, "steps_per_run": kb, "seconds": tsum}
+    cells = [d.n_cells for d in decks]
+    layers = [d.meta["n_layers_run"] for d in decks]
+    line = {
+        "metric": METRIC, "value": res["mixed_packed"]["value"], "unit": UNIT, "n_gpus": 1, "steps": k, "warmup": w,
+        "ms_per_step": res["mixed_packed"]["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": (f"storm-surge ensemble: {len(decks)} runs, {sum(cells)} cells "
+                                f"(log-uniform {min(cells)}-{max(cells)}), deepest water {min(layers)}-{max(layers)} "
+                                f"of {pk.n_layers} shared 1 m levels, Holland vortex + M2 tide forcing on the "
+                                f"device, dt={pk.params.dt:g} s"),
+                   "generation_s": gen_s, "l2": "state larger than L2"},
+        "ensemble": res,
+        "speedup_vs_fp64_one_at_a_time": res["mixed_packed"]["value"] / res["fp64_one_at_a_time"]["value"],
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def bench_serving(args):
+    """Poisson stream of storm-surge requests (rate 2/s, horizons U(6, 48) h scaled by
+    --horizon-scale), meshes drawn from an ensemble-like pool: continuous batching of mixed-
+    precision contexts under a 150 GB device-memory budget against the plain FP64 path serving the
+    same requests one at a time."""
+    import dataclasses as dc
+    from gom_release_gb300.core import load_core
+    from gom_release_gb300.ensemble import ensemble_decks
+    from gom_release_gb300.serve import Request, poisson_arrivals, serve, serve_fifo
+    lib = load_core()
+    t0 = time.perf_counter()
+    pool = ensemble_decks(n_runs=args.pool, seed=5, min_cells=max(200, int(5000 * args.scale)),
+                          max_cells=max(400, int(400000 * args.scale)))
+    gen_s = time.perf_counter() - t0
+    arrivals = poisson_arrivals(args.requests, 2.0, seed=3)
+
+    def make_requests():
+        out = []
+        r2 = np.random.default_rng(17)
+        for i, t in enumerate(arrivals):
+            d = pool[int(r2.integers(len(pool)))]
+            st = dc.replace(d.meta["storm"], dp=float(r2.uniform(20e2, 80e2)), rmax=float(r2.uniform(20e3, 60e3)),
+                            b=float(r2.uniform(1.0, 1.8)), speed=float(r2.uniform(3.0, 8.0)))
+            hours = float(r2.uniform(6.0, 48.0)) * args.horizon_scale
+            steps = max(1, int(round(hours * 3600.0 / d.params.dt)))
+            out.append(Request(rid=i, deck=d, storm=st, steps=steps, arrival=float(t)))
+        return out
+
+    with ClockSampler(0) as clocks:
+        mixed = serve(lib, make_requests(), budget_bytes=150e9, precision=1)
+        fifo = serve_fifo(lib, make_requests(), precision=0)
+    line = {
+        "metric": METRIC, "value": mixed["throughput"], "unit": UNIT, "n_gpus": 1, "steps": None, "warmup": 0,
+        "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic",
+        "config": {"workload": (f"serving: {args.requests} Poisson requests (rate 2/s), horizons U(6,48) h x "
+                                f"{args.horizon_scale:g}, meshes from a pool of {len(pool)} storm-surge runs "
+                                f"({min(d.n_cells for d in pool)}-{max(d.n_cells for d in pool)} cells), "
+                                "HBM budget 150 GB"), "generation_s": gen_s},
+        "serving_mixed": mixed, "serving_fp64_one_at_a_time": fifo,
+        "latency_p50_s": mixed["latency_p50_s"], "latency_p99_s": mixed["latency_p99_s"],
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def bench_precision(args):
+    """The tidal-basin generator scaled up (default 2M cells x 40 layers), run in plain FP64 and
+    in mixed precision from the same cold start for the same steps: per-field max and RMS error
+    of the mixed run against the FP64 run (which tracks the CPU restatement to 1e-8), volume and
+    salt-mass difference, and both throughputs."""
+    import dataclasses as dc
+    from gom_release_gb300.core import GomCore, load_core
+    from gom_release_gb300.deck import HostForcing, tidal_basin
+    from gom_release_gb300.serve import active_cell_layers
+    lib = load_core()
+    ny = int(round(math.sqrt(args.cells / 1.5)))
+    nx = int(round(args.cells / ny))
+    t0 = time.perf_counter()
+    deck = tidal_basin(nx=nx, ny=ny, dx=250.0, n_layers=args.layers, dt=60.0)
+    gen_s = time.perf_counter() - t0
+    out = {}
+    fields = ("eta_cell", "un_face", "vn_face", "wn_cell", "u_node", "w_node", "salt_cell", "temp_cell", "dz_cell")
+    snaps = {}
+    for label, prec in (("fp64", 0), ("mixed", 1)):
+        d = dc.replace(deck, params=dc.replace(deck.params, precision=prec))
+        core = GomCore(d, lib=lib)
+        p = d.params
+        core.cold_start(p.ref_salt, p.ref_temp, p.av_0, p.kv_0)
+        core.step("density")
+        ncl = active_cell_layers(core, d)
+        hf = HostForcing(d)
+        v0, s0 = core.conservation()
+        secs = 0.0
+        import torch
+        stream = torch.cuda.ExternalStream(core.stream_handle())
+        for it in range(1, args.steps + 1):
+            core.set_forcing(hf.step(it))
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            core.step_launch()
+            e1.record(stream)
+            core.step_wait()
+            if it > 3:
+                secs += e0.elapsed_time(e1) / 1e3
+        v1, s1 = core.conservation()
+        snaps[label] = {f: core.get_field(f) for f in fields}
+        out[label] = {"value": ncl * (args.steps - 3) / secs, "ms_per_step": secs / (args.steps - 3) * 1e3,
+                      "device_gb": core.device_bytes() / 1e9, "active_cell_layers": ncl, "volume": v1,
+                      "salt_mass": s1, "volume_change_rel": (v1 - v0) / v0, "pcg_iters_total": core.pcg_iterations_total()}
+        core.close()
+    err = {}
+    for f in fields:
+        a, b = snaps["mixed"][f], snaps["fp64"][f]
+        scale = max(float(np.abs(b).max()), 1e-30)
+        err[f] = {"max_abs": float(np.abs(a - b).max()), "rms_abs": float(np.sqrt(np.mean((a - b) ** 2))),
+                  "max_rel_to_field_max": float(np.abs(a - b).max()) / scale}
+    line = {
+        "metric": METRIC, "value": out["mixed"]["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps - 3,
+        "warmup": 3, "ms_per_step": out["mixed"]["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": (f"precision: tidal basin {deck.n_cells} cells x {deck.n_layers} layers, "
+                                f"dt=60 s, {args.steps} steps from a cold start, FP64 vs mixed"), "generation_s": gen_s},
+        "precision": out, "mixed_vs_fp64_error": err,
+        "volume_diff_rel": abs(out["mixed"]["volume"] - out["fp64"]["volume"]) / out["fp64"]["volume"],
+        "salt_mass_diff_rel": abs(out["mixed"]["salt_mass"] - out["fp64"]["salt_mass"]) / out["fp64"]["salt_mass"],
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -287,14 +476,38 @@ def main():
     ap.add_argument("--size", default="full", choices=["full", "medium", "small"],
                     help="full: the benchmark workload; medium (38k cells) and small (6k cells) for profiling")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
     ap.add_argument("--no-phases", action="store_true", help="skip the per-phase timing pass")
     ap.add_argument("--e2e-steps", type=int, default=0)
+    ap.add_argument("--workload", default="estuary", choices=["estuary", "ensemble", "serving", "precision"],
+                    help="estuary: the single-run benchmark; ensemble: packed storm-surge ensemble; "
+                         "serving: Poisson request stream with continuous batching")
+    ap.add_argument("--requests", type=int, default=48, help="serving: number of requests")
+    ap.add_argument("--cells", type=int, default=2_000_000, help="precision: cell count")
+    ap.add_argument("--layers", type=int, default=40, help="precision: z-layers")
+    ap.add_argument("--pool", type=int, default=16, help="serving: distinct meshes")
+    ap.add_argument("--horizon-scale", type=float, default=1.0, help="serving: scale of the 6-48 h horizons")
+    ap.add_argument("--runs", type=int, default=96, help="ensemble: number of runs")
+    ap.add_argument("--scale", type=float, default=1.0, help="ensemble: cell-count scale (1 = 5k-400k)")
+    ap.add_argument("--skip-fp64-packed", action="store_true")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
                     help="fp64: the drop-in path (bit-for-bit with the CPU restatement); mixed: FP32 layered state")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)
+        return
+    if args.workload == "ensemble":
+        if rank == 0:
+            bench_ensemble(args)
+        return
+    if args.workload == "serving":
+        if rank == 0:
+            bench_serving(args)
+        return
+    if args.workload == "precision":
+        if rank == 0:
+            bench_precision(args)
         return
     if args.warmup < 3:
         args.warmup = 3
@@ -310,6 +523,7 @@ def main():
     run = Run(deck, GomCore(deck, lib=lib), st)
     torch_mod, stream = stream_events(run.core)
     run.advance(args.warmup)
+    tune = run.core.autotune(reps=3) if not args.no_autotune else None
     # ---- value: K steps, state resident in HBM, host forcing precomputed
     hf = HostForcing(deck)
     hf.julian_day = run.forcing.julian_day
@@ -377,6 +591,7 @@ def main():
             "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
             "l2": "state larger than L2 (each phase streams its arrays from HBM)",
             "simulated_hours_per_wall_s": deck.params.dt * args.steps / secs / 3600.0,
+            "autotune": tune,
             "pcg_iters_mean": pcg_mean,
         },
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",

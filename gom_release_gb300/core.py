@@ -163,6 +163,7 @@ def _bind(lib: C.CDLL) -> C.CDLL:
     lib.gom_conservation.argtypes = [vp, _D, _D]
     lib.gom_set_storms.argtypes = [vp, C.c_int32, C.POINTER(GomStorm), C.c_double]
     lib.gom_cold_start.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_double]
+    lib.gom_autotune.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32)]
     lib.gom_device_bytes.argtypes = [vp]
     lib.gom_device_bytes.restype = C.c_int64
     lib.gom_get_status.argtypes = [vp, C.POINTER(GomStatus), C.c_int]
@@ -336,6 +337,12 @@ class GomCore:
     def cold_start(self, salt: float, temp: float, av_0: float, kv_0: float):
         """Initial state built on the device (then ``step("density")`` as prepare does)."""
         self._check(self.lib.gom_cold_start(self.ctx, salt, temp, av_0, kv_0), "cold_start")
+
+    def autotune(self, reps: int = 3) -> list[int]:
+        """Pick the fastest compiled variant of each tunable launch on the current state."""
+        out = (C.c_int32 * 4)()
+        self._check(self.lib.gom_autotune(self.ctx, reps, out), "autotune")
+        return list(out)
 
     def device_bytes(self) -> int:
         return int(self.lib.gom_device_bytes(self.ctx))

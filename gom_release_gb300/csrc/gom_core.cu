@@ -5,6 +5,7 @@
 // CUDA stream, pinned staging for the per-step forcing, and a CUDA graph of the whole timestep
 // (captured on first use of gom_step_all).  Host arrays are read only during a call.
 #include <cstdio>
+#include <mutex>
 #include <algorithm>
 #include <cstring>
 #include <numeric>
@@ -52,7 +53,11 @@ struct gom_ctx {
     cudaEvent_t stage_done[2] = {nullptr, nullptr};
     bool step_pending = false;
     long long pcg_total = 0;
-    cudaGraphExec_t graph = nullptr;
+    // the timestep as three captured graphs: before the free surface, the free surface (whose
+    // cooperative PCG runs on the process-wide solver stream, one solve at a time on the GPU),
+    // after it
+    cudaGraphExec_t graph = nullptr, graph_fs = nullptr, graph_post = nullptr;
+    cudaEvent_t ev_to_solver = nullptr, ev_from_solver = nullptr;
     bool graph_failed = false;
     // device-side storm forcing (gom_set_storms)
     double *d_storms = nullptr, *storm_wu = nullptr, *storm_wv = nullptr;
@@ -110,6 +115,13 @@ template <typename R> cudaError_t alloc_layered_work(gom_ctx *c, WorkT<R> &W) {
     if (e == cudaSuccess) e = dalloc(c, &W.uflf, (L + 1) * NF);
     if (e == cudaSuccess) e = dalloc(c, &W.vflf, (L + 1) * NF);
     if (e == cudaSuccess && c->hp.turbulence_flag != 0) e = dalloc(c, &W.kvf, (L + 1) * NF);
+    if (sizeof(R) == sizeof(float) && c->hp.transport_flag) {
+        R **rows[] = {&W.tr_a, &W.tr_b, &W.tr_c};
+        for (R **p : rows)
+            if (e == cudaSuccess) e = dalloc(c, p, L * NC);
+        if (e == cudaSuccess) e = dalloc(c, &W.tr_rhs, L * NC * 2);
+        if (e == cudaSuccess) e = dalloc(c, &W.tr_last, 4 * NC);
+    }
     return e;
 }
 
@@ -223,17 +235,24 @@ cudaError_t enqueue_swap(gom_ctx *c) {
     return cudaSuccess;
 }
 
-// the phases of main.f90:94-272 in order
-template <typename R> cudaError_t enqueue_step_t(gom_ctx *c, const LaunchT<R> &x) {
+// the phases of main.f90:94-272 in order; part 0 = up to the momentum equation, 1 = the free
+// surface, 2 = the rest, -1 = all
+template <typename R> cudaError_t enqueue_step_t(gom_ctx *c, const LaunchT<R> &x, int part) {
     cudaError_t e;
-    if (c->n_storms > 0 &&
-        (e = launch_storm_forcing(x.g, x.f, x.p, x.stream, c->d_storms, c->storm_wu, c->storm_wv)))
-        return e;
-    if ((e = launch_bottom_friction(x))) return e;
-    if ((e = launch_boundary_velocity(x))) return e;
-    if ((e = launch_advection(x))) return e;
-    if ((e = launch_momentum(x))) return e;
-    if ((e = launch_free_surface(x))) return e;
+    if (part <= 0) {
+        if (c->n_storms > 0 &&
+            (e = launch_storm_forcing(x.g, x.f, x.p, x.stream, c->d_storms, c->storm_wu, c->storm_wv)))
+            return e;
+        if ((e = launch_bottom_friction(x))) return e;
+        if ((e = launch_boundary_velocity(x))) return e;
+        if ((e = launch_advection(x))) return e;
+        if ((e = launch_momentum(x))) return e;
+        if (part == 0) return cudaSuccess;
+    }
+    if (part <= 1) {
+        if ((e = launch_free_surface(x))) return e;
+        if (part == 1) return cudaSuccess;
+    }
     if ((e = launch_velocities(x))) return e;
     if ((e = launch_layers(x))) return e;
     if ((e = launch_node_velocity(x))) return e;
@@ -243,7 +262,47 @@ template <typename R> cudaError_t enqueue_step_t(gom_ctx *c, const LaunchT<R> &x
     return enqueue_swap(c);
 }
 
-cudaError_t enqueue_step(gom_ctx *c) { return c->mixed ? enqueue_step_t(c, c->xf) : enqueue_step_t(c, c->x); }
+cudaError_t enqueue_step(gom_ctx *c, int part = -1) {
+    return c->mixed ? enqueue_step_t(c, c->xf, part) : enqueue_step_t(c, c->x, part);
+}
+
+// One stream per device shared by every context of the process for the free-surface phase: its
+// cooperative PCG kernel spins on grid barriers, and two such grids resident at once on one GPU
+// (contexts stepped concurrently on their own streams) could each wait for blocks the other
+// holds.  Queuing the free-surface graphs of all contexts on one stream runs one solve at a time.
+std::mutex g_solver_mutex;
+cudaStream_t g_solver_stream[64] = {};
+
+cudaError_t solver_stream(int device, cudaStream_t *out) {
+    if (device < 0 || device >= 64) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_solver_mutex);
+    if (!g_solver_stream[device]) {
+        cudaError_t e = cudaStreamCreateWithFlags(&g_solver_stream[device], cudaStreamNonBlocking);
+        if (e != cudaSuccess) return e;
+    }
+    *out = g_solver_stream[device];
+    return cudaSuccess;
+}
+
+cudaError_t capture(gom_ctx *c, int part, cudaGraphExec_t *out) {
+    cudaGraph_t gr = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(c->x.stream, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        cudaError_t e2 = enqueue_step(c, part);
+        e = cudaStreamEndCapture(c->x.stream, &gr);
+        if (e2 != cudaSuccess) e = e2;
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(out, gr, 0);
+    if (gr) cudaGraphDestroy(gr);
+    return e;
+}
+
+void drop_graphs(gom_ctx *c) {
+    for (cudaGraphExec_t *g : {&c->graph, &c->graph_fs, &c->graph_post}) {
+        if (*g) cudaGraphExecDestroy(*g);
+        *g = nullptr;
+    }
+}
 
 // a phase launcher on the context's state type
 #define GOM_PHASE(fn) [](gom_ctx *c) { return c->mixed ? fn(c->xf) : fn(c->x); }
@@ -527,6 +586,9 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
         return fail(GOM_E_NOMEM);
     for (int h = 0; h < 2; ++h)
         if (cudaEventCreateWithFlags(&c->stage_done[h], cudaEventDisableTiming) != cudaSuccess) return fail(GOM_E_CUDA);
+    if (cudaEventCreateWithFlags(&c->ev_to_solver, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_from_solver, cudaEventDisableTiming) != cudaSuccess)
+        return fail(GOM_E_CUDA);
     std::memset(c->h_status, 0, sizeof(gom_status));
     {
         cudaError_t pe = pcg_configure(c->x, c->device);
@@ -582,7 +644,9 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
 void gom_destroy(gom_ctx *c) {
     if (!c) return;
     if (c->x.stream) cudaStreamSynchronize(c->x.stream);
-    if (c->graph) cudaGraphExecDestroy(c->graph);
+    drop_graphs(c);
+    if (c->ev_to_solver) cudaEventDestroy(c->ev_to_solver);
+    if (c->ev_from_solver) cudaEventDestroy(c->ev_from_solver);
     for (void *p : c->allocs) cudaFree(p);
     if (c->h_status) cudaFreeHost(c->h_status);
     if (c->h_iters) cudaFreeHost(c->h_iters);
@@ -722,27 +786,32 @@ int gom_step_swap(gom_ctx *c) {
 
 int gom_step_launch(gom_ctx *c) {
     if (!c) return GOM_E_ARG;
-    // The timestep is captured once into a CUDA graph and replayed: every kernel argument is a
+    // The timestep is captured once into CUDA graphs and replayed: every kernel argument is a
     // device pointer or a constant of the context, and per-step forcing lives in device memory.
     if (!c->graph && !c->graph_failed) {
-        cudaGraph_t gr = nullptr;
-        cudaError_t e = cudaStreamBeginCapture(c->x.stream, cudaStreamCaptureModeThreadLocal);
-        if (e == cudaSuccess) {
-            cudaError_t e2 = enqueue_step(c);
-            e = cudaStreamEndCapture(c->x.stream, &gr);
-            if (e2 != cudaSuccess) e = e2;
-        }
-        if (e == cudaSuccess) e = cudaGraphInstantiate(&c->graph, gr, 0);
-        if (gr) cudaGraphDestroy(gr);
+        cudaError_t e = capture(c, 0, &c->graph);
+        if (e == cudaSuccess) e = capture(c, 1, &c->graph_fs);
+        if (e == cudaSuccess) e = capture(c, 2, &c->graph_post);
         if (e != cudaSuccess) {
             cudaGetLastError();
+            drop_graphs(c);
             c->graph_failed = true;
-            c->graph = nullptr;
             c->msg = std::string("graph capture unavailable: ") + cudaGetErrorString(e);
         }
     }
-    if (c->graph) CK(cudaGraphLaunch(c->graph, c->x.stream));
-    else CK(enqueue_step(c));
+    cudaStream_t solver = nullptr;
+    CK(solver_stream(c->device, &solver));
+    if (c->graph) {
+        CK(cudaGraphLaunch(c->graph, c->x.stream));
+        CK(cudaEventRecord(c->ev_to_solver, c->x.stream));
+        CK(cudaStreamWaitEvent(solver, c->ev_to_solver, 0));
+        CK(cudaGraphLaunch(c->graph_fs, solver));
+        CK(cudaEventRecord(c->ev_from_solver, solver));
+        CK(cudaStreamWaitEvent(c->x.stream, c->ev_from_solver, 0));
+        CK(cudaGraphLaunch(c->graph_post, c->x.stream));
+    } else {
+        CK(enqueue_step(c));
+    }
     CK(cudaMemcpyAsync(c->h_status, c->x.status, sizeof(gom_status), cudaMemcpyDeviceToHost, c->x.stream));
     CK(cudaMemcpyAsync(c->h_iters, c->x.w.pcg_iters, sizeof(int), cudaMemcpyDeviceToHost, c->x.stream));
     c->step_pending = true;
@@ -779,6 +848,53 @@ int gom_cold_start(gom_ctx *c, double salt, double temp, double av_0, double kv_
     return finish(c, nullptr, false);
 }
 
+int gom_autotune(gom_ctx *c, int32_t reps, int32_t *choice) {
+    if (!c || reps < 1) return GOM_E_ARG;
+    struct Site {
+        int site;
+        cudaError_t (*run)(gom_ctx *);
+    };
+    const Site sites[] = {{TUNE_ELM, GOM_PHASE(launch_advection)},
+                          {TUNE_MOMENTUM, GOM_PHASE(launch_momentum)},
+                          {TUNE_TR_SOLVE, GOM_PHASE(launch_transport)},
+                          {TUNE_TR_LIMITER, GOM_PHASE(launch_transport)}};
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    int rc = GOM_OK;
+    for (const Site &st : sites) {
+        int best = 0;
+        float best_ms = 1e30f;
+        for (int v = 0; v < TUNE_VARIANTS[st.site] && rc == GOM_OK; ++v) {
+            c->x.tune[st.site] = v;
+            c->xf.tune[st.site] = v;
+            cudaError_t e = st.run(c);                        // warm-up (and first-touch)
+            if (e == cudaSuccess) e = cudaEventRecord(e0, c->x.stream);
+            for (int r = 0; r < reps && e == cudaSuccess; ++r) e = st.run(c);
+            if (e == cudaSuccess) e = cudaEventRecord(e1, c->x.stream);
+            if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+            float ms = 0.0f;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+            if (e != cudaSuccess) {
+                rc = set_cuda_error(c, e, "autotune");
+                break;
+            }
+            if (ms < best_ms) {
+                best_ms = ms;
+                best = v;
+            }
+        }
+        c->x.tune[st.site] = best;
+        c->xf.tune[st.site] = best;
+        if (choice) choice[st.site] = best;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc != GOM_OK) return rc;
+    drop_graphs(c);   // captured again with the chosen variants
+    return finish(c, nullptr, false);
+}
+
 int gom_set_storms(gom_ctx *c, int32_t n_storms, const gom_storm *storms, double elapsed_time) {
     if (!c || !storms || n_storms != c->x.g.NR) return GOM_E_ARG;
     static_assert(sizeof(gom_storm) == 12 * sizeof(double), "gom_storm is 12 doubles");
@@ -798,10 +914,7 @@ int gom_set_storms(gom_ctx *c, int32_t n_storms, const gom_storm *storms, double
     CK(cudaMemcpy(c->f_scal, scal0, sizeof(double), cudaMemcpyHostToDevice));
     c->n_storms = n_storms;
     // the captured step gains the forcing kernels: capture again on the next launch
-    if (c->graph) {
-        cudaGraphExecDestroy(c->graph);
-        c->graph = nullptr;
-    }
+    drop_graphs(c);
     return GOM_OK;
 }
 

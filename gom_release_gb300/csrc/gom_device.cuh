@@ -120,6 +120,10 @@ __device__ __forceinline__ bool failed(const gom_status *st) { return *(volatile
 __device__ __forceinline__ double calculate_area(double x1, double x2, double x3, double y1, double y2, double y3) {
     return fabs((x1 - x3) * (y2 - y3) - (x2 - x3) * (y1 - y3)) * 0.5;
 }
+template <typename T>
+__device__ __forceinline__ T calculate_area_t(T x1, T x2, T x3, T y1, T y2, T y3) {
+    return fabs((x1 - x3) * (y2 - y3) - (x2 - x3) * (y1 - y3)) * T(0.5);
+}
 
 // Exact decisions about a rounded quotient fl(num/den) (num >= 0, den > 0) against a constant c,
 // deciding from num and c*den when they are more than 1e-9 apart (far beyond every rounding

@@ -34,12 +34,21 @@ template <typename R> struct WorkT {
     double *node_weight = nullptr;
     // turbulence closure: face diffusivity per interface (0:L, NF)
     R *kvf = nullptr;
+    // mixed-precision transport: rows of the vertical systems (L, NC) and right-hand sides
+    // (L, NC, 2); top-layer horizontal sums of the limiter (2, NC, 2)
+    R *tr_a = nullptr, *tr_b = nullptr, *tr_c = nullptr, *tr_rhs = nullptr, *tr_last = nullptr;
     // conservation
     double *cons = nullptr;                                     // [volume, salt]
 };
 using Work = WorkT<double>;
 
+// Tunable launches: each picks one of a few compiled variants (block size, minimum resident
+// blocks per SM); gom_autotune times the variants on the context's state and keeps the fastest.
+enum TuneSite { TUNE_ELM = 0, TUNE_MOMENTUM, TUNE_TR_SOLVE, TUNE_TR_LIMITER, TUNE_COUNT };
+constexpr int TUNE_VARIANTS[TUNE_COUNT] = {5, 3, 3, 3};
+
 template <typename R> struct LaunchT {
+    int tune[TUNE_COUNT] = {0, 0, 0, 0};
     Geom g;
     StateT<R> s;
     Forcing f;

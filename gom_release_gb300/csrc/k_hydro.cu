@@ -93,47 +93,48 @@ __device__ __forceinline__ int check_intersection(double x1, double x2, double x
 }
 
 // bilinear_interpolation.f90:8-121: returns 0 or GOM_ELM_BILINEAR
-__device__ int bilinear_interpolation(double x1, double x2, double x3, double x4, double y1, double y2, double y3,
-                                      double y4, double x, double y, double shapef[4]) {
-    const double small3 = F(1.e-5f), small_06 = F(1.e-6f), b11 = F(1.1f);
-    double xi = 0.0, eta = 0.0;
-    double x0 = (x1 + x2 + x3 + x4) / 4.0;
-    double y0 = (y1 + y2 + y3 + y4) / 4.0;
-    double axi0 = x2 - x1 + x3 - x4, axi1 = y2 - y1 + y3 - y4;
-    double aet0 = x3 + x4 - x1 - x2, aet1 = y3 + y4 - y1 - y2;
-    double bxy0 = x1 - x2 + x3 - x4, bxy1 = y1 - y2 + y3 - y4;
-    double dxi = 2.0 * ((x3 - x4) * (y1 - y2) - (y3 - y4) * (x1 - x2));
-    double deta = 2.0 * ((x4 - x1) * (y3 - y2) - (y4 - y1) * (x3 - x2));
+// (T = T: the reference arithmetic; T = float: the mixed path, on element-local coordinates)
+template <typename T>
+__device__ int bilinear_interpolation(T x1, T x2, T x3, T x4, T y1, T y2, T y3, T y4, T x, T y, T shapef[4]) {
+    const T small3 = (T)F(1.e-5f), small_06 = (T)F(1.e-6f), b11 = (T)F(1.1f);
+    T xi = T(0.0), eta = T(0.0);
+    T x0 = (x1 + x2 + x3 + x4) / T(4.0);
+    T y0 = (y1 + y2 + y3 + y4) / T(4.0);
+    T axi0 = x2 - x1 + x3 - x4, axi1 = y2 - y1 + y3 - y4;
+    T aet0 = x3 + x4 - x1 - x2, aet1 = y3 + y4 - y1 - y2;
+    T bxy0 = x1 - x2 + x3 - x4, bxy1 = y1 - y2 + y3 - y4;
+    T dxi = T(2.0) * ((x3 - x4) * (y1 - y2) - (y3 - y4) * (x1 - x2));
+    T deta = T(2.0) * ((x4 - x1) * (y3 - y2) - (y4 - y1) * (x3 - x2));
     if ((fabs(bxy0) < small3 && fabs(bxy1) < small3) || (fabs(dxi) < small3 && fabs(deta) < small3)) {
-        double dd = axi0 * aet1 - axi1 * aet0;
-        if (dd == 0.0) return GOM_ELM_BILINEAR;
-        xi = 4.0 * (aet1 * (x - x0) - aet0 * (y - y0)) / dd;
-        eta = 4.0 * (axi0 * (y - y0) - axi1 * (x - x0)) / dd;
+        T dd = axi0 * aet1 - axi1 * aet0;
+        if (dd == T(0.0)) return GOM_ELM_BILINEAR;
+        xi = T(4.0) * (aet1 * (x - x0) - aet0 * (y - y0)) / dd;
+        eta = T(4.0) * (axi0 * (y - y0) - axi1 * (x - x0)) / dd;
     } else if (fabs(dxi) < small3 && fabs(deta) >= small3) {
-        eta = 4.0 * (bxy1 * (x - x0) - bxy0 * (y - y0)) / deta;
-        double t1 = axi0 + eta * bxy0, t2 = axi1 + eta * bxy1;
-        double dd = t1 * t1 + t2 * t2;
-        if (dd == 0.0) return GOM_ELM_BILINEAR;
-        xi = ((4.0 * (x - x0) - eta * aet0) * (axi0 + eta * bxy0) + (4.0 * (y - y0) - eta * aet1) * (axi1 + eta * bxy1)) / dd;
+        eta = T(4.0) * (bxy1 * (x - x0) - bxy0 * (y - y0)) / deta;
+        T t1 = axi0 + eta * bxy0, t2 = axi1 + eta * bxy1;
+        T dd = t1 * t1 + t2 * t2;
+        if (dd == T(0.0)) return GOM_ELM_BILINEAR;
+        xi = ((T(4.0) * (x - x0) - eta * aet0) * (axi0 + eta * bxy0) + (T(4.0) * (y - y0) - eta * aet1) * (axi1 + eta * bxy1)) / dd;
     } else if (fabs(dxi) >= small3 && fabs(deta) < small3) {
-        xi = 4.0 * (bxy1 * (x - x0) - bxy0 * (y - y0)) / dxi;
-        double t1 = aet0 + xi * bxy0, t2 = aet1 + xi * bxy1;
-        double dd = t1 * t1 + t2 * t2;
-        if (dd == 0.0) return GOM_ELM_BILINEAR;
-        eta = ((4.0 * (x - x0) - xi * axi0) * (aet0 + xi * bxy0) + (4.0 * (y - y0) - xi * axi1) * (aet1 + xi * bxy1)) / dd;
+        xi = T(4.0) * (bxy1 * (x - x0) - bxy0 * (y - y0)) / dxi;
+        T t1 = aet0 + xi * bxy0, t2 = aet1 + xi * bxy1;
+        T dd = t1 * t1 + t2 * t2;
+        if (dd == T(0.0)) return GOM_ELM_BILINEAR;
+        eta = ((T(4.0) * (x - x0) - xi * axi0) * (aet0 + xi * bxy0) + (T(4.0) * (y - y0) - xi * axi1) * (aet1 + xi * bxy1)) / dd;
     } else {
-        double beta = aet1 * axi0 - aet0 * axi1 - 4 * (bxy1 * (x - x0) - bxy0 * (y - y0));
-        double gamma = 4.0 * (aet0 * (y - y0) - aet1 * (x - x0));
-        double delta = beta * beta - 4 * gamma * dxi;
-        if (delta == 0.0) {
+        T beta = aet1 * axi0 - aet0 * axi1 - 4 * (bxy1 * (x - x0) - bxy0 * (y - y0));
+        T gamma = T(4.0) * (aet0 * (y - y0) - aet1 * (x - x0));
+        T delta = beta * beta - 4 * gamma * dxi;
+        if (delta == T(0.0)) {
             xi = -beta / 2 / dxi;
-            eta = (4.0 * (bxy1 * (x - x0) - bxy0 * (y - y0)) - xi * dxi) / deta;
+            eta = (T(4.0) * (bxy1 * (x - x0) - bxy0 * (y - y0)) - xi * dxi) / deta;
         } else if (delta > 0) {
-            double sq = sqrt(delta);
-            double rx[2] = {(-beta + sq) / 2 / dxi, (-beta - sq) / 2 / dxi};
+            T sq = sqrt(delta);
+            T rx[2] = {(-beta + sq) / 2 / dxi, (-beta - sq) / 2 / dxi};
             int icount = 0;
             for (int i = 0; i < 2; ++i) {
-                double re = (4 * (bxy1 * (x - x0) - bxy0 * (y - y0)) - rx[i] * dxi) / deta;
+                T re = (4 * (bxy1 * (x - x0) - bxy0 * (y - y0)) - rx[i] * dxi) / deta;
                 if (fabs(rx[i]) <= b11 && fabs(re) <= b11) {
                     xi = rx[i];
                     eta = re;
@@ -146,8 +147,8 @@ __device__ int bilinear_interpolation(double x1, double x2, double x3, double x4
         }
     }
     if (fabs(xi) > b11 || fabs(eta) > b11) return GOM_ELM_BILINEAR;
-    xi = fmin(1.0, fmax(xi, -1.0));
-    eta = fmin(1.0, fmax(eta, -1.0));
+    xi = fmin(T(1.0), fmax(xi, -T(1.0)));
+    eta = fmin(T(1.0), fmax(eta, -T(1.0)));
     shapef[0] = (1 - xi) * (1 - eta) / 4;
     shapef[1] = (1 + xi) * (1 - eta) / 4;
     shapef[2] = (1 + xi) * (1 + eta) / 4;
@@ -167,10 +168,109 @@ __device__ __forceinline__ double area_sum(const Geom &g, int nel, double x, dou
     return a;
 }
 
-// search_straight_line.f90:15-399 (mode 1). Returns 0 or a GOM_ELM_* site.
-template <typename R>
+// ---------------------------------------------------------------- point-in-element tests
+// The reference's test (search_straight_line.f90, ELM_backtrace_v1.f90:151-164): the sum of the
+// areas of the triangles (point, edge) against the element area, relative tolerance small_06.
+// For a convex counter-clockwise element with edge cross products c_l = e_l x (p - a_l) the
+// excess sum - area equals the sum of |c_l| over the negative c_l (exactly, in exact arithmetic).
+// The mixed path evaluates the c_l in FP32 on element-local coordinates with a bound on their
+// error and decides from the bound when the margin allows; otherwise it evaluates the reference's
+// FP64 expression.  Either way the decision is the FP64 reference's.
+__device__ __forceinline__ bool in_elem64(const Geom &g, int nel, double x, double y) {
+    double ar = g.area[nel - 1];
+    return quotient_lt(fabs(area_sum(g, nel, x, y) - ar), ar, F(1.e-6f));
+}
+__device__ __forceinline__ bool out_elem64(const Geom &g, int nel, double x, double y) {
+    double ar = g.area[nel - 1];
+    return quotient_gt(fabs(area_sum(g, nel, x, y) - ar), ar, F(1.e-6f));
+}
+
+// element nodes as FP32 offsets from the element centre
+struct LocalElem {
+    int tq;
+    double xc, yc;
+    float x[4], y[4];
+    float ar;
+};
+
+__device__ __forceinline__ void load_local(const Geom &g, int nel, LocalElem &e) {
+    e.tq = g.tri_or_quad[nel - 1];
+    e.xc = g.x_cell[nel - 1];
+    e.yc = g.y_cell[nel - 1];
+    e.ar = (float)g.area[nel - 1];
+    for (int l = 0; l < 4; ++l) {
+        e.x[l] = 0.0f;
+        e.y[l] = 0.0f;
+        if (l < e.tq) {
+            int n = g.cell_node(l + 1, nel);
+            e.x[l] = (float)(g.x_node[n - 1] - e.xc);
+            e.y[l] = (float)(g.y_node[n - 1] - e.yc);
+        }
+    }
+}
+
+// 1: inside by the reference's test, 0: outside, -1: not decidable in FP32.  near: an edge line
+// passes within the FP32 error bound of the point.
+__device__ __forceinline__ int classify_f32(const LocalElem &e, float px, float py, bool &near) {
+    const float u = 5.97e-8f;   // 2^-24
+    float lo = 0.0f, hi = 0.0f;
+    near = false;
+    float twice_area = 0.0f;   // counter-clockwise elements only (as cell.inp requires)
+    for (int l = 0; l < e.tq; ++l) {
+        int m = l + 1 == e.tq ? 0 : l + 1;
+        twice_area += e.x[l] * e.y[m] - e.x[m] * e.y[l];
+    }
+    if (!(twice_area > 0.0f)) {
+        near = true;
+        return -1;
+    }
+    for (int l = 0; l < e.tq; ++l) {
+        int m = l + 1 == e.tq ? 0 : l + 1;
+        float ex = e.x[m] - e.x[l], ey = e.y[m] - e.y[l];
+        float dx = px - e.x[l], dy = py - e.y[l];
+        float c = ex * dy - ey * dx;
+        // inputs rounded from FP64 differences, two subtractions, two products, one subtraction
+        float mag = (fabsf(e.x[m]) + fabsf(e.x[l]) + fabsf(e.y[m]) + fabsf(e.y[l])) *
+                    (fabsf(px) + fabsf(py) + fabsf(e.x[l]) + fabsf(e.y[l]));
+        float bnd = 16.0f * u * mag + 1e-30f;
+        if (c <= -bnd) {
+            lo += -c - bnd;
+            hi += -c + bnd;
+        } else if (c < bnd) {
+            hi += fmaxf(-c, 0.0f) + bnd;
+        }
+        if (fabsf(c) < 2.0f * bnd) near = true;
+    }
+    const float thr = (float)F(1.e-6f) * e.ar;
+    if (hi < thr * (1.0f - 1e-4f)) return 1;
+    if (lo > thr * (1.0f + 1e-4f)) return 0;
+    return -1;
+}
+
+__device__ __forceinline__ bool in_elem_mixed(const Geom &g, int nel, double x, double y) {
+    LocalElem e;
+    load_local(g, nel, e);
+    bool near;
+    int r = classify_f32(e, (float)(x - e.xc), (float)(y - e.yc), near);
+    return r >= 0 ? r == 1 : in_elem64(g, nel, x, y);
+}
+__device__ __forceinline__ bool out_elem_mixed(const Geom &g, int nel, double x, double y) {
+    LocalElem e;
+    load_local(g, nel, e);
+    bool near;
+    int r = classify_f32(e, (float)(x - e.xc), (float)(y - e.yc), near);
+    return r >= 0 ? r == 0 : out_elem64(g, nel, x, y);
+}
+
+// search_straight_line.f90:15-399 (mode 1). Returns 0 or a GOM_ELM_* site.  start_on_edge: the
+// start point is the midpoint of an edge of the start element (the first substep of a face), for
+// which the reference's start test (:37-46) always passes -- its area excess is zero up to FP64
+// rounding, far below the tolerance -- so it is not evaluated.  MIXED selects the FP32-filtered
+// point-in-element tests (same decisions).
+template <typename R, bool MIXED>
 __device__ int search_straight_line(const Geom &g, const StateT<R> &s, const Params &p, int &nnel, int &jlev, double time,
-                                    double x0, double y0, double z0, double &xt, double &yt, double &zt, int &nfl) {
+                                    double x0, double y0, double z0, double &xt, double &yt, double &zt, int &nfl,
+                                    bool start_on_edge) {
     const double small_06 = F(1.e-6f);
     const double MSL = p.msl;
     const int L = g.L;
@@ -178,11 +278,9 @@ __device__ int search_straight_line(const Geom &g, const StateT<R> &s, const Par
     nfl = 0;
     double trm = time;
     int nel = nnel;
-    double area1 = area_sum(g, nel, x0, y0);
-    double area2 = area_sum(g, nel, xt, yt);
-    double ar = g.area[nel - 1];
-    if (quotient_gt(fabs(area1 - ar), ar, small_06)) return GOM_ELM_START_OUTSIDE;
-    if (!quotient_lt(fabs(area2 - ar), ar, small_06)) {
+    if (!start_on_edge && (MIXED ? out_elem_mixed(g, nel, x0, y0) : out_elem64(g, nel, x0, y0)))
+        return GOM_ELM_START_OUTSIDE;
+    if (!(MIXED ? in_elem_mixed(g, nel, xt, yt) : in_elem64(g, nel, xt, yt))) {
         const double c1 = 1.0 - 1.0e-4;
         double xcg = c1 * x0 + 1.0e-4 * g.x_cell[nel - 1];
         double ycg = c1 * y0 + 1.0e-4 * g.y_cell[nel - 1];
@@ -237,9 +335,7 @@ __device__ int search_straight_line(const Geom &g, const StateT<R> &s, const Par
                 break;
             }
             nel = adjc;
-            ar = g.area[nel - 1];
-            area1 = area_sum(g, nel, xt, yt);
-            if (quotient_lt(fabs(area1 - ar), ar, small_06)) {
+            if (MIXED ? in_elem_mixed(g, nel, xt, yt) : in_elem64(g, nel, xt, yt)) {
                 nnel = nel;
                 break;
             }
@@ -289,8 +385,11 @@ __device__ bool near_edge_line(const Geom &g, int nel, double x, double y) {
     return false;
 }
 
-// ELM_backtrace_v1.f90:40-200 (mode 1)
-template <typename R>
+// ELM_backtrace_v1.f90:40-200 (mode 1).  The first substep starts at the face midpoint, on an
+// edge of the start element.  MIXED: the same walk (FP64 foot coordinates, the reference's
+// point-in-element decisions), interpolation weights and velocities in FP32 on element-local
+// coordinates.
+template <typename R, bool MIXED>
 __device__ int elm_backtrace(const Geom &g, const StateT<R> &s, const Params &p, int bt_step, double bt_dt, double &uu,
                              double &vv, double &ww, double x0, double y0, double z0, int &nnel, int &jlev,
                              int &near_edge) {
@@ -301,57 +400,99 @@ __device__ int elm_backtrace(const Geom &g, const StateT<R> &s, const Params &p,
         double yt = y0 - bt_dt * vv;
         double zt = z0 - bt_dt * ww;
         int nfl = 0;
-        int e = search_straight_line(g, s, p, nnel, jlev, bt_dt, x0, y0, z0, xt, yt, zt, nfl);
+        int e = search_straight_line<R, MIXED>(g, s, p, nnel, jlev, bt_dt, x0, y0, z0, xt, yt, zt, nfl, idt == 1);
         if (e) return e;
         int tq = g.tri_or_quad[nnel - 1];
         double zup = (jlev == s.top_cell[nnel - 1]) ? p.msl + s.eta_cell[nnel - 1] : g.z_level[jlev];
         if (zt > zup) return GOM_ELM_Z_ABOVE;
-        double zrat = (zup - zt) / s.dz_cell[ix(jlev, nnel, L)];
-        double vxn[4], vyn[4], vzn[4], sta[4];
-        for (int l = 1; l <= tq; ++l) {
-            int nd = g.cell_node(l, nnel);
-            long i1 = ix0(jlev - 1, nd, L), i2 = ix0(jlev, nd, L);
-            vxn[l - 1] = s.u_node[i2] * (1 - zrat) + s.u_node[i1] * zrat;
-            vyn[l - 1] = s.v_node[i2] * (1 - zrat) + s.v_node[i1] * zrat;
-            vzn[l - 1] = s.w_node[i2] * (1 - zrat) + s.w_node[i1] * zrat;
-        }
-        int n1 = g.cell_node(1, nnel), n2 = g.cell_node(2, nnel), n3 = g.cell_node(3, nnel);
-        double X1 = g.x_node[n1 - 1], X2 = g.x_node[n2 - 1], X3 = g.x_node[n3 - 1];
-        double Y1 = g.y_node[n1 - 1], Y2 = g.y_node[n2 - 1], Y3 = g.y_node[n3 - 1];
-        double ar = g.area[nnel - 1];
-        if (tq == 3) {
-            sta[0] = calculate_area(xt, X2, X3, yt, Y2, Y3) / ar;
-            sta[1] = calculate_area(X1, xt, X3, Y1, yt, Y3) / ar;
-            sta[2] = calculate_area(X1, X2, xt, Y1, Y2, yt) / ar;
-            sta[0] = fmax(0.0, fmin(1.0, sta[0]));
-            sta[1] = fmax(0.0, fmin(1.0, sta[1]));
-            if (sta[0] + sta[1] > 1) {
-                sta[2] = 0;
-                sta[1] = 1.0 - sta[0];
+        if constexpr (MIXED) {
+            const float zrat = (float)(zup - zt) / (float)s.dz_cell[ix(jlev, nnel, L)];
+            LocalElem el;
+            load_local(g, nnel, el);
+            const float px = (float)(xt - el.xc), py = (float)(yt - el.yc);
+            float sta[4];
+            if (tq == 3) {
+                const float ar = el.ar;
+                sta[0] = calculate_area_t(px, el.x[1], el.x[2], py, el.y[1], el.y[2]) / ar;
+                sta[1] = calculate_area_t(el.x[0], px, el.x[2], el.y[0], py, el.y[2]) / ar;
+                sta[2] = calculate_area_t(el.x[0], el.x[1], px, el.y[0], el.y[1], py) / ar;
+                sta[0] = fmaxf(0.0f, fminf(1.0f, sta[0]));
+                sta[1] = fmaxf(0.0f, fminf(1.0f, sta[1]));
+                if (sta[0] + sta[1] > 1.0f) {
+                    sta[2] = 0.0f;
+                    sta[1] = 1.0f - sta[0];
+                } else {
+                    sta[2] = 1.0f - sta[0] - sta[1];
+                }
             } else {
-                sta[2] = 1.0 - sta[0] - sta[1];
+                if (out_elem_mixed(g, nnel, xt, yt)) return GOM_ELM_QUAD_OUTSIDE;
+                int b = bilinear_interpolation<float>(el.x[0], el.x[1], el.x[2], el.x[3], el.y[0], el.y[1], el.y[2],
+                                                      el.y[3], px, py, sta);
+                if (b) return b;
             }
+            float fu = 0.0f, fv = 0.0f, fw = 0.0f;
+            for (int l = 1; l <= tq; ++l) {
+                int nd = g.cell_node(l, nnel);
+                long i1 = ix0(jlev - 1, nd, L), i2 = ix0(jlev, nd, L);
+                float w = sta[l - 1];
+                fu = fu + ((float)s.u_node[i2] * (1.0f - zrat) + (float)s.u_node[i1] * zrat) * w;
+                fv = fv + ((float)s.v_node[i2] * (1.0f - zrat) + (float)s.v_node[i1] * zrat) * w;
+                fw = fw + ((float)s.w_node[i2] * (1.0f - zrat) + (float)s.w_node[i1] * zrat) * w;
+            }
+            uu = fu;
+            vv = fv;
+            ww = fw;
+            bool near;
+            (void)classify_f32(el, px, py, near);
+            if (near && near_edge_line(g, nnel, xt, yt)) near_edge = 1;
         } else {
-            int n4 = g.cell_node(4, nnel);
-            double X4 = g.x_node[n4 - 1], Y4 = g.y_node[n4 - 1];
-            double aa1 = calculate_area(X1, X2, xt, Y1, Y2, yt);
-            double aa2 = calculate_area(X2, X3, xt, Y2, Y3, yt);
-            double aa3 = calculate_area(X3, X4, xt, Y3, Y4, yt);
-            double aa4 = calculate_area(X4, X1, xt, Y4, Y1, yt);
-            double aa = fabs(aa1) + fabs(aa2) + fabs(aa3) + fabs(aa4);
-            if (quotient_gt(fabs(aa - ar), ar, small_06)) return GOM_ELM_QUAD_OUTSIDE;
-            int b = bilinear_interpolation(X1, X2, X3, X4, Y1, Y2, Y3, Y4, xt, yt, sta);
-            if (b) return b;
+            double zrat = (zup - zt) / s.dz_cell[ix(jlev, nnel, L)];
+            double vxn[4], vyn[4], vzn[4], sta[4];
+            for (int l = 1; l <= tq; ++l) {
+                int nd = g.cell_node(l, nnel);
+                long i1 = ix0(jlev - 1, nd, L), i2 = ix0(jlev, nd, L);
+                vxn[l - 1] = s.u_node[i2] * (1 - zrat) + s.u_node[i1] * zrat;
+                vyn[l - 1] = s.v_node[i2] * (1 - zrat) + s.v_node[i1] * zrat;
+                vzn[l - 1] = s.w_node[i2] * (1 - zrat) + s.w_node[i1] * zrat;
+            }
+            int n1 = g.cell_node(1, nnel), n2 = g.cell_node(2, nnel), n3 = g.cell_node(3, nnel);
+            double X1 = g.x_node[n1 - 1], X2 = g.x_node[n2 - 1], X3 = g.x_node[n3 - 1];
+            double Y1 = g.y_node[n1 - 1], Y2 = g.y_node[n2 - 1], Y3 = g.y_node[n3 - 1];
+            double ar = g.area[nnel - 1];
+            if (tq == 3) {
+                sta[0] = calculate_area(xt, X2, X3, yt, Y2, Y3) / ar;
+                sta[1] = calculate_area(X1, xt, X3, Y1, yt, Y3) / ar;
+                sta[2] = calculate_area(X1, X2, xt, Y1, Y2, yt) / ar;
+                sta[0] = fmax(0.0, fmin(1.0, sta[0]));
+                sta[1] = fmax(0.0, fmin(1.0, sta[1]));
+                if (sta[0] + sta[1] > 1) {
+                    sta[2] = 0;
+                    sta[1] = 1.0 - sta[0];
+                } else {
+                    sta[2] = 1.0 - sta[0] - sta[1];
+                }
+            } else {
+                int n4 = g.cell_node(4, nnel);
+                double X4 = g.x_node[n4 - 1], Y4 = g.y_node[n4 - 1];
+                double aa1 = calculate_area(X1, X2, xt, Y1, Y2, yt);
+                double aa2 = calculate_area(X2, X3, xt, Y2, Y3, yt);
+                double aa3 = calculate_area(X3, X4, xt, Y3, Y4, yt);
+                double aa4 = calculate_area(X4, X1, xt, Y4, Y1, yt);
+                double aa = fabs(aa1) + fabs(aa2) + fabs(aa3) + fabs(aa4);
+                if (quotient_gt(fabs(aa - ar), ar, small_06)) return GOM_ELM_QUAD_OUTSIDE;
+                int b = bilinear_interpolation<double>(X1, X2, X3, X4, Y1, Y2, Y3, Y4, xt, yt, sta);
+                if (b) return b;
+            }
+            uu = 0.0;
+            vv = 0.0;
+            ww = 0.0;
+            for (int j = 0; j < tq; ++j) {
+                uu = uu + vxn[j] * sta[j];
+                vv = vv + vyn[j] * sta[j];
+                ww = ww + vzn[j] * sta[j];
+            }
+            if (near_edge_line(g, nnel, xt, yt)) near_edge = 1;
         }
-        uu = 0.0;
-        vv = 0.0;
-        ww = 0.0;
-        for (int j = 0; j < tq; ++j) {
-            uu = uu + vxn[j] * sta[j];
-            vv = vv + vyn[j] * sta[j];
-            ww = ww + vzn[j] * sta[j];
-        }
-        if (near_edge_line(g, nnel, xt, yt)) near_edge = 1;
         if (nfl == 1) break;
         x0 = xt;
         y0 = yt;
@@ -450,7 +591,8 @@ __device__ void elm_face_layer(const Geom &g, const StateT<R> &s, const Params &
     int bt_step = (int)((double)(s.num_sub_elm[ix(k, n1, L)] + s.num_sub_elm[ix(k, n2, L)]) * 0.5);
     double bt_dt = p.dt / bt_step;
     int near = 0;
-    int e = elm_backtrace(g, s, p, bt_step, bt_dt, uu, vv, ww, x0, y0, z0, nnel, jlev, near);
+    int e = elm_backtrace<R, sizeof(R) == sizeof(float)>(g, s, p, bt_step, bt_dt, uu, vv, ww, x0, y0, z0, nnel, jlev,
+                                                          near);
     if (e) {
         record_error(st, GOM_E_ELM, e, j, k, 0.0);
         return;
@@ -461,7 +603,8 @@ __device__ void elm_face_layer(const Geom &g, const StateT<R> &s, const Params &
     s.vn_elm[o] = (R)(-uu * sn + vv * ct);
 }
 
-template <typename R> __global__ void k_elm_faces(Geom g, StateT<R> s, Params p, gom_status *st) {
+template <typename R, int BS, int MINB>
+__global__ void __launch_bounds__(BS, MINB) k_elm_faces(Geom g, StateT<R> s, Params p, gom_status *st) {
     unsigned tid = flat_tid();
     if (tid >= (unsigned)g.NF) return;
     int j = g.face_order[tid];
@@ -515,7 +658,14 @@ template <typename R> cudaError_t launch_advection(const LaunchT<R> &x) {
         long nnl = (long)x.g.NN * x.g.L;
         k_elm_substeps<<<blocks_for(nnl, 256), 256, 0, x.stream>>>(x.g, x.s, x.p, x.w.idev);
     }
-    k_elm_faces<<<blocks_for(x.g.NF, 64), 64, 0, x.stream>>>(x.g, x.s, x.p, x.status);
+    // variants: threads per block and minimum resident blocks per SM (register budget)
+    switch (x.tune[TUNE_ELM]) {
+    case 1: k_elm_faces<R, 32, 1><<<blocks_for(x.g.NF, 32), 32, 0, x.stream>>>(x.g, x.s, x.p, x.status); break;
+    case 2: k_elm_faces<R, 128, 1><<<blocks_for(x.g.NF, 128), 128, 0, x.stream>>>(x.g, x.s, x.p, x.status); break;
+    case 3: k_elm_faces<R, 64, 12><<<blocks_for(x.g.NF, 64), 64, 0, x.stream>>>(x.g, x.s, x.p, x.status); break;
+    case 4: k_elm_faces<R, 64, 16><<<blocks_for(x.g.NF, 64), 64, 0, x.stream>>>(x.g, x.s, x.p, x.status); break;
+    default: k_elm_faces<R, 64, 1><<<blocks_for(x.g.NF, 64), 64, 0, x.stream>>>(x.g, x.s, x.p, x.status); break;
+    }
     return cudaGetLastError();
 }
 
@@ -571,7 +721,7 @@ __device__ double prev_rtemp0(const Geom &g, const StateT<R> &s, const Forcing &
 // and rounded to R; the layer loop, the Smagorinsky diffusion, the baroclinic integral and the
 // tridiagonal solve run in R.  With R = double every expression is the reference's.
 template <typename R>
-__global__ void __launch_bounds__(128) k_momentum(Geom g, StateT<R> s, Forcing f, Params p, gom_status *st) {
+__global__ void __launch_bounds__(256) k_momentum(Geom g, StateT<R> s, Forcing f, Params p, gom_status *st) {
     unsigned tid = flat_tid();
     if (tid >= (unsigned)g.NF) return;
     int j = g.face_order[tid];
@@ -794,7 +944,8 @@ template <typename R> __global__ void k_zero_face_columns(Geom g, StateT<R> s) {
 template <typename R> cudaError_t launch_momentum(const LaunchT<R> &x) {
     long nfl = (long)x.g.NF * x.g.L;
     k_zero_face_columns<<<blocks_for(nfl, 256), 256, 0, x.stream>>>(x.g, x.s);
-    k_momentum<<<blocks_for(x.g.NF, 128), 128, 0, x.stream>>>(x.g, x.s, x.f, x.p, x.status);
+    const int bs = x.tune[TUNE_MOMENTUM] == 1 ? 64 : x.tune[TUNE_MOMENTUM] == 2 ? 256 : 128;
+    k_momentum<<<blocks_for(x.g.NF, bs), bs, 0, x.stream>>>(x.g, x.s, x.f, x.p, x.status);
     return cudaGetLastError();
 }
 

@@ -424,6 +424,15 @@ template <typename R> cudaError_t launch_velocities(const LaunchT<R> &x) {
 // ============================================================================================
 // update_vertical_layers_1.f90: new top layers and thicknesses for an entity column.
 // kind 0 = cell (:42-133), 1 = face (:139-198), 2 = node (:204-254)
+// FP64 thickness of layer k of a column with bottom layer b and top layer t > b
+__device__ __forceinline__ double column_dz(const Geom &g, double msl, double h, double eta, int b, int t, int k) {
+    if (k == t) return (msl + eta) - g.z_level[t - 1];
+    if (k == b) return g.z_level[b] - (msl - h);
+    return g.delta_z[k - 1];
+}
+
+// Thicknesses are formed in FP64 and rounded once to the storage type (with R = double this is
+// the reference's arithmetic, half-thicknesses included).
 template <int KIND, typename R>
 __device__ __forceinline__ int new_column(const Geom &g, const Params &p, double h, double eta, int b, R *dz, R *dzh,
                                           long base_dz, long base_dzh, bool &bad) {
@@ -450,12 +459,13 @@ __device__ __forceinline__ int new_column(const Geom &g, const Params &p, double
         if (KIND == 1) dzh[base_dzh + tnew - 1] = (R)total;
         dzh[base_dzh + tnew] = (R)total;
     } else {
-        dz[base_dz + b - 1] = (R)(g.z_level[b] - (MSL - h));
-        for (int k = b + 1; k <= tnew - 1; ++k) dz[base_dz + k - 1] = (R)g.delta_z[k - 1];
-        for (int k = b; k <= tnew - 1; ++k) dzh[base_dzh + k] = (dz[base_dz + k] + dz[base_dz + k - 1]) * R(0.5);
+        for (int k = b; k <= tnew - 1; ++k) dz[base_dz + k - 1] = (R)column_dz(g, MSL, h, eta, b, tnew, k);
+        for (int k = b; k <= tnew - 1; ++k)
+            dzh[base_dzh + k] =
+                (R)((column_dz(g, MSL, h, eta, b, tnew, k + 1) + column_dz(g, MSL, h, eta, b, tnew, k)) * 0.5);
         if (KIND != 2) {
-            dzh[base_dzh + tnew] = dz[base_dz + tnew - 1];
-            dzh[base_dzh + b - 1] = dz[base_dz + b - 1];
+            dzh[base_dzh + tnew] = (R)column_dz(g, MSL, h, eta, b, tnew, tnew);
+            dzh[base_dzh + b - 1] = (R)column_dz(g, MSL, h, eta, b, tnew, b);
         }
     }
     return tnew;
@@ -596,12 +606,12 @@ __global__ void k_cold_layers(Geom g, Params p, int n, const double *h, const in
             if (KIND == 1) zh[t - 1] = (R)total;
             zh[t] = (R)total;
         } else {
-            z[b - 1] = (R)(g.z_level[b] - (msl - he));
-            for (int k = b + 1; k <= t - 1; ++k) z[k - 1] = (R)g.delta_z[k - 1];
-            for (int k = b; k <= t - 1; ++k) zh[k] = (z[k] + z[k - 1]) * R(0.5);
+            for (int k = b; k <= t - 1; ++k) z[k - 1] = (R)column_dz(g, msl, he, eta, b, t, k);
+            for (int k = b; k <= t - 1; ++k)
+                zh[k] = (R)((column_dz(g, msl, he, eta, b, t, k + 1) + column_dz(g, msl, he, eta, b, t, k)) * 0.5);
             if (KIND != 0) {
-                zh[t] = z[t - 1];
-                zh[b - 1] = z[b - 1];
+                zh[t] = (R)column_dz(g, msl, he, eta, b, t, t);
+                zh[b - 1] = (R)column_dz(g, msl, he, eta, b, t, b);
             }
         }
     }

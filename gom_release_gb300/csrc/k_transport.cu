@@ -38,6 +38,7 @@ __device__ __forceinline__ float pos_part(float q) { return is_pos(q) ? q : 0.0f
 __device__ __forceinline__ float neg_part(float q) { return is_neg(q) ? -q : 0.0f; }
 __device__ __forceinline__ bool same_bits(float a, float b) { return __float_as_int(a) == __float_as_int(b); }
 template <typename R> __device__ __forceinline__ R flip(R q, int sgn) { return sgn > 0 ? q : -q; }
+constexpr unsigned FULL_MASK = 0xffffffffu;
 
 // R: storage and arithmetic type of the tracers and coefficients
 template <typename R> struct TArgs {
@@ -232,11 +233,8 @@ template <typename R> __device__ __forceinline__ R phi_limit(int code, R small_p
 
 // :624-871 per cell column: upwind-weighted differences of every layer (sum1_all, sum2_all) for
 // the face ratios r_jk, and the vertical ratios r_ik -> PSI_ik.
-template <typename R> __global__ void k_tr_limiter_cells(TArgs<R> a) {
-    unsigned tid = flat_tid();
+template <typename R> __device__ void limiter_column(const TArgs<R> &a, int i) {
     const Geom &g = a.g;
-    if (tid >= (unsigned)g.NC) return;
-    int i = g.cell_order[tid];
     const int L = g.L, NC = g.NC;
     int tl = a.s.top_cell[i - 1], b = g.bottom_cell[i - 1];
     if (tl == 0) return;
@@ -307,50 +305,173 @@ template <typename R> __global__ void k_tr_limiter_cells(TArgs<R> a) {
     }
 }
 
+template <typename R> __global__ void k_tr_limiter_cells(TArgs<R> a) {
+    unsigned tid = flat_tid();
+    if (tid >= (unsigned)a.g.NC) return;
+    limiter_column(a, a.g.cell_order[tid]);
+}
+
+// FP32 path, :624-805 with one thread per (cell, layer): the upwind-weighted differences of the
+// layer, and the top layer's horizontal sums kept for the vertical ratios
+__global__ void __launch_bounds__(256) k_tr_sums_cl(TArgs<float> a) {
+    const Geom &g = a.g;
+    unsigned t = flat_tid();
+    const int L = g.L, NC = g.NC;
+    if (t >= (unsigned)NC * L) return;
+    int i, k;
+    split_index(t, L, i, k);
+    i += 1;
+    k += 1;
+    const int tl = a.s.top_cell[i - 1], b = g.bottom_cell[i - 1];
+    if (tl == 0 || k < b || k > tl) return;
+    const int nvl = tl - b + 1;
+    const int tq = g.tri_or_quad[i - 1];
+    float ck[2] = {0.0f, 0.0f}, s1a[2] = {0.0f, 0.0f}, s2a[2] = {0.0f, 0.0f}, s1[2] = {0.0f, 0.0f},
+          s2[2] = {0.0f, 0.0f};
+    for (int tr = 0; tr < a.ntr; ++tr) {
+        ck[tr] = a.con[ic(k, i, tr, L, NC)];
+        if (nvl != 1) {
+            if (k > b) {
+                float rt1 = pos_part(a.w.qi[ix0(k - 1, i, L)]);
+                s1a[tr] = rt1 * (ck[tr] - a.con[ic(k - 1, i, tr, L, NC)]);
+                s2a[tr] = rt1;
+            }
+            if (k < tl) {
+                float rt2 = pos_part(a.w.qi[ix0(k, i, L)]);
+                s1a[tr] = s1a[tr] + rt2 * (ck[tr] - a.con[ic(k + 1, i, tr, L, NC)]);
+                s2a[tr] = s2a[tr] + rt2;
+            }
+        }
+    }
+    for (int l = 1; l <= tq; ++l) {
+        const int fj = g.cell_face(l, i);
+        if (!face_open(g, fj)) continue;
+        const float q2 = flip(a.w.qj[ix(k, fj, L)], g.cell_sign(l, i));
+        if (is_neg(q2)) {
+            const int nb = g.cell_adj(l, i);
+            for (int tr = 0; tr < a.ntr; ++tr) {
+                float cik = nb > 0 ? a.con[ic(k, nb, tr, L, NC)] : oqb_value(a, i, k, tr);
+                s1[tr] = s1[tr] + fabsf(q2) * (ck[tr] - cik);
+                s2[tr] = s2[tr] + fabsf(q2);
+            }
+        }
+    }
+    for (int tr = 0; tr < a.ntr; ++tr) {
+        a.w.sa1[((long)tr * NC + i - 1) * L + k - 1] = s1a[tr] + s1[tr];
+        a.w.sa2[((long)tr * NC + i - 1) * L + k - 1] = s2a[tr] + s2[tr];
+        if (k == tl) {
+            a.w.tr_last[((long)tr * NC + i - 1) * 2] = s1[tr];
+            a.w.tr_last[((long)tr * NC + i - 1) * 2 + 1] = s2[tr];
+        }
+    }
+}
+
+// FP32 path, :806-871 with one thread per (cell, interface)
+__global__ void __launch_bounds__(256) k_tr_vpsi_cl(TArgs<float> a) {
+    const Geom &g = a.g;
+    unsigned t = flat_tid();
+    const int L = g.L, NC = g.NC;
+    if (t >= (unsigned)NC * L) return;
+    int i, k;
+    split_index(t, L, i, k);
+    i += 1;
+    k += 1;
+    const int tl = a.s.top_cell[i - 1], b = g.bottom_cell[i - 1];
+    if (tl == 0 || k < b || k > tl - 1) return;
+    for (int tr = 0; tr < a.ntr; ++tr) {
+        const float last1 = a.w.tr_last[((long)tr * NC + i - 1) * 2], last2 = a.w.tr_last[((long)tr * NC + i - 1) * 2 + 1];
+        float *psi = a.w.psii + (long)tr * NC * (L + 1);
+        float ck = a.con[ic(k, i, tr, L, NC)];
+        float qm = k > b ? a.w.qi[ix0(k - 1, i, L)] : 0.0f;
+        float rt1 = last1 + fabsf(qm) * (ck - a.con[ic(k - 1, i, tr, L, NC)]);
+        float rt2 = last2 + fabsf(qm);
+        float rtemp = (a.con[ic(k + 1, i, tr, L, NC)] - ck) * rt2;
+        float r = rtemp == 0.0f ? 1.0f : rt1 / rtemp;
+        psi[ix0(k, i, L)] = phi_limit(a.p.h_flux_limiter, a.w.phii[ix0(k, i, L)], r);
+    }
+}
+
 // :769-799 + :876-900 face ratio r_jk from its upwind cell (the last writer in cell order), PSI_jk;
 // one thread per face walks its wet layers
+template <typename R> __device__ __forceinline__ void limiter_face_layer(const TArgs<R> &a, int j, int k, bool open,
+                                                                     int c1, int c2, int t1, int b1, int t2, int b2) {
+    const Geom &g = a.g;
+    const int L = g.L, NC = g.NC;
+    long t = ix(k, j, L);
+    R Q = a.w.qj[t];
+    int writer = 0;
+    if (open) {
+        // a cell writes when it is wet, holds layer k and sees Q*sign >= 0; cell 2 comes later
+        if (c2 != 0 && t2 != 0 && k >= b2 && k <= t2 && !is_pos(Q)) writer = c2;   // -Q >= 0
+        else if (t1 != 0 && k >= b1 && k <= t1 && !is_neg(Q)) writer = c1;        // Q >= 0
+    }
+    for (int tr = 0; tr < a.ntr; ++tr) {
+        R r = R(1.0);
+        if (writer != 0) {
+            int i = writer;
+            int other = (writer == c1) ? c2 : c1;
+            R cik = other > 0 ? a.con[ic(k, other, tr, L, NC)] : oqb_value(a, i, k, tr);
+            R rtemp = a.w.sa2[((long)tr * NC + i - 1) * L + k - 1] * (cik - a.con[ic(k, i, tr, L, NC)]);
+            r = rtemp == R(0.0) ? R(1.0) : a.w.sa1[((long)tr * NC + i - 1) * L + k - 1] / rtemp;
+        }
+        a.w.psij[(long)tr * g.NF * L + t] = phi_limit(a.p.h_flux_limiter, a.w.phij[t], r);
+    }
+}
+
 template <typename R> __global__ void k_tr_limiter_faces(TArgs<R> a) {
     unsigned tid = flat_tid();
     const Geom &g = a.g;
     if (tid >= (unsigned)g.NF) return;
     int j = g.face_order[tid];
-    const int L = g.L, NC = g.NC;
     int b = g.bottom_face[j - 1], tf = a.s.top_face[j - 1];
     if (tf == 0) return;
     bool open = face_open(g, j);
     int c1 = g.face_cell(1, j), c2 = g.face_cell(2, j);
     int t1 = a.s.top_cell[c1 - 1], b1 = g.bottom_cell[c1 - 1];
     int t2 = c2 != 0 ? a.s.top_cell[c2 - 1] : 0, b2 = c2 != 0 ? g.bottom_cell[c2 - 1] : 0;
-    for (int k = b; k <= tf; ++k) {
-        long t = ix(k, j, L);
-        R Q = a.w.qj[t];
-        int writer = 0;
-        if (open) {
-            // a cell writes when it is wet, holds layer k and sees Q*sign >= 0; cell 2 comes later
-            if (c2 != 0 && t2 != 0 && k >= b2 && k <= t2 && !is_pos(Q)) writer = c2;   // -Q >= 0
-            else if (t1 != 0 && k >= b1 && k <= t1 && !is_neg(Q)) writer = c1;        // Q >= 0
-        }
-        for (int tr = 0; tr < a.ntr; ++tr) {
-            R r = R(1.0);
-            if (writer != 0) {
-                int i = writer;
-                int other = (writer == c1) ? c2 : c1;
-                R cik = other > 0 ? a.con[ic(k, other, tr, L, NC)] : oqb_value(a, i, k, tr);
-                R rtemp = a.w.sa2[((long)tr * NC + i - 1) * L + k - 1] * (cik - a.con[ic(k, i, tr, L, NC)]);
-                r = rtemp == R(0.0) ? R(1.0) : a.w.sa1[((long)tr * NC + i - 1) * L + k - 1] / rtemp;
-            }
-            a.w.psij[(long)tr * g.NF * L + t] = phi_limit(a.p.h_flux_limiter, a.w.phij[t], r);
-        }
+    for (int k = b; k <= tf; ++k) limiter_face_layer(a, j, k, open, c1, c2, t1, b1, t2, b2);
+}
+
+// FP32 path: one thread per (face, layer), layers of a face on consecutive lanes
+template <typename R> __global__ void k_tr_limiter_faces_flat(TArgs<R> a) {
+    unsigned t = flat_tid();
+    const Geom &g = a.g;
+    if (t >= (unsigned)g.NF * g.L) return;
+    int j, k;
+    split_index(t, g.L, j, k);
+    j += 1;
+    k += 1;
+    int b = g.bottom_face[j - 1], tf = a.s.top_face[j - 1];
+    if (k < b || k > tf) return;
+    int c1 = g.face_cell(1, j), c2 = g.face_cell(2, j);
+    int t1 = a.s.top_cell[c1 - 1], b1 = g.bottom_cell[c1 - 1];
+    int t2 = c2 != 0 ? a.s.top_cell[c2 - 1] : 0, b2 = c2 != 0 ? g.bottom_cell[c2 - 1] : 0;
+    limiter_face_layer(a, j, k, face_open(g, j), c1, c2, t1, b1, t2, b2);
+}
+
+// FP32 path: face coefficients, one thread per (face, layer)
+template <typename R> __global__ void k_tr_face_coef_flat(TArgs<R> a) {
+    unsigned t = flat_tid();
+    const Geom &g = a.g;
+    if (t >= (unsigned)g.NF * g.L) return;
+    int j, k;
+    split_index(t, g.L, j, k);
+    j += 1;
+    k += 1;
+    int b = g.bottom_face[j - 1], tf = a.s.top_face[j - 1];
+    if (k >= b && k <= tf) {
+        if (!a.changed_only || !same_bits(a.s.dz_face[t], a.s.dz_face_new[t])) face_coef_at(a, j, k, (long)t);
+    } else if (!a.changed_only) {
+        a.w.qj[t] = R(0);
+        a.w.dj[t] = R(0);
+        a.w.phij[t] = R(0);
     }
 }
 
 // :921-1346 per cell column: explicit horizontal fluxes + limiter, implicit vertical system,
 // Thomas solve, clamp to [0, 50]; writes the full next column (zero outside the wet range).
-template <typename R> __global__ void __launch_bounds__(128) k_tr_solve(TArgs<R> a) {
-    unsigned tid = flat_tid();
+template <typename R> __device__ void tr_solve_column(const TArgs<R> &a, int i) {
     const Geom &g = a.g;
-    if (tid >= (unsigned)g.NC) return;
-    int i = g.cell_order[tid];
     const int L = g.L, NC = g.NC;
     int tl = a.s.top_cell[i - 1], b = g.bottom_cell[i - 1];
     const R dt2 = a.dt2;
@@ -499,6 +620,152 @@ template <typename R> __global__ void __launch_bounds__(128) k_tr_solve(TArgs<R>
     }
 }
 
+template <typename R> __global__ void __launch_bounds__(256) k_tr_solve(TArgs<R> a) {
+    unsigned tid = flat_tid();
+    if (tid >= (unsigned)a.g.NC) return;
+    tr_solve_column(a, a.g.cell_order[tid]);
+}
+
+// ---------------------------------------------------------------------------- FP32 cell-layers
+// The mixed-precision path forms the transport fluxes with one thread per (cell, layer): layers of
+// a cell sit on consecutive lanes, so the layer-contiguous arrays are read in coalesced runs and
+// the GPU holds enough threads to hide the latency of the neighbour gathers.  Each row of the
+// implicit vertical system is written to work arrays, and one thread per column then runs the
+// tridiagonal solve.  FP32 arithmetic is cheap on GB300, so the lanes of dry layers are simply
+// idle.
+__device__ __forceinline__ float clamp_tracer(float sv, float prev) {
+    if (sv >= 0.0f && sv <= 50.0f) return sv;
+    if (sv < 0.0f) return 0.0f;
+    if (sv > 50.0f) return 50.0f;
+    return prev;   // NaN: the reference keeps the previous value
+}
+
+// :921-1250 for one wet cell-layer: right-hand sides and the row of the implicit system
+// (a couples the layer below, c the layer above)
+__global__ void __launch_bounds__(256) k_tr_rows_cl(TArgs<float> a) {
+    const Geom &g = a.g;
+    unsigned t = flat_tid();
+    const int L = g.L, NC = g.NC;
+    if (t >= (unsigned)NC * L) return;
+    int i, k;
+    split_index(t, L, i, k);
+    i += 1;
+    k += 1;
+    const int tl = a.s.top_cell[i - 1], b = g.bottom_cell[i - 1];
+    if (tl == 0 || k < b || k > tl) return;
+    const float dt2 = a.dt2;
+    const int sub = a.sub;
+    const bool lim = a.p.h_flux_limiter > 0 || a.p.v_flux_limiter > 0;
+    const float ar = (float)g.area[i - 1];
+    const int tq = g.tri_or_quad[i - 1];
+    float c0[2] = {0.0f, 0.0f};
+    for (int tr = 0; tr < a.ntr; ++tr) c0[tr] = a.con[ic(k, i, tr, L, NC)];
+    float sQi[2] = {0, 0}, sQii[2] = {0, 0}, shd[2] = {0, 0}, shl[2] = {0, 0};
+    for (int l = 1; l <= tq; ++l) {
+        const int fj = g.cell_face(l, i);
+        if (!face_open(g, fj)) continue;
+        const int nb = g.cell_adj(l, i), sg = g.cell_sign(l, i);
+        const bool in_face = k >= g.bottom_face[fj - 1] && k <= a.s.top_face[fj - 1];
+        const long fo = ix(k, fj, L);
+        const float q2 = flip(in_face ? a.w.qj[fo] : 0.0f, sg);
+        const float dface = in_face ? a.w.dj[fo] : 0.0f;
+        const bool qpos = is_pos(q2), qneg = is_neg(q2);
+        for (int tr = 0; tr < a.ntr; ++tr) {
+            float cik = nb > 0 ? a.con[ic(k, nb, tr, L, NC)] : oqb_value(a, i, k, tr);
+            if (qpos) sQi[tr] = sQi[tr] + fabsf(q2) * c0[tr];
+            else if (qneg) sQii[tr] = sQii[tr] + fabsf(q2) * cik;
+            shd[tr] = shd[tr] + dface * (cik - c0[tr]);
+            float psi = (lim && in_face) ? a.w.psij[(long)tr * g.NF * L + fo] : 0.0f;
+            shl[tr] = shl[tr] + psi * fabsf(q2) * (c0[tr] - cik);
+        }
+    }
+    const float dzc = a.s.dz_cell[ix(k, i, L)], dzn = a.s.dz_cell_new[ix(k, i, L)];
+    const float dz_old = dzc + divnt((dzn - dzc) * (float)sub, a);
+    const float dz_new = dzc + divnt((dzn - dzc) * (float)(sub + 1), a);
+    const int nvl = tl - b + 1;
+    const float qlo = k > b ? a.w.qi[ix0(k - 1, i, L)] : 0.0f;   // interface below layer k
+    const float qhi = k < tl ? a.w.qi[ix0(k, i, L)] : 0.0f;      // interface above
+    for (int tr = 0; tr < a.ntr; ++tr) {
+        float v = ar * dz_old * c0[tr] + dt2 * (sQii[tr] - sQi[tr]) + dt2 * shd[tr];
+        if (a.p.h_flux_limiter > 0) v = v + 0.5f * dt2 * shl[tr];
+        if (nvl != 1) {
+            const float *psi = a.w.psii + (long)tr * NC * (L + 1);
+            const float c = c0[tr];
+            if (k > b) {
+                float qp1 = pos_part(qlo), qm1 = neg_part(qlo);
+                float cm1 = a.con[ic(k - 1, i, tr, L, NC)];
+                v = v + dt2 * (qp1 * cm1 - qm1 * c);
+                if (a.p.v_flux_limiter > 0) {
+                    float p1 = lim ? psi[ix0(k - 1, i, L)] : 0.0f;
+                    v = v + 0.5f * dt2 * (p1 * qp1 * (c - cm1) - p1 * qm1 * (cm1 - c));
+                }
+            }
+            if (k < tl) {
+                float qp = pos_part(qhi), qm = neg_part(qhi);
+                float cp1 = a.con[ic(k + 1, i, tr, L, NC)];
+                v = v + dt2 * (qm * cp1 - qp * c);
+                if (a.p.v_flux_limiter > 0) {
+                    float p0 = lim ? psi[ix0(k, i, L)] : 0.0f;
+                    v = v + 0.5f * dt2 * (-p0 * qp * (cp1 - c) + p0 * qm * (c - cp1));
+                }
+            }
+        }
+        a.w.tr_rhs[((long)tr * NC + i - 1) * L + k - 1] = v;
+    }
+    const float am = k > b ? -dt2 * a.w.di[ix0(k - 1, i, L)] : 0.0f;
+    const float cm = k < tl ? -dt2 * a.w.di[ix0(k, i, L)] : 0.0f;
+    const long o = (long)(i - 1) * L + k - 1;
+    a.w.tr_a[o] = am;
+    a.w.tr_b[o] = ar * dz_new - am - cm;
+    a.w.tr_c[o] = cm;
+}
+
+// one thread per column: tridiagonal solve of the rows (top layer first, as
+// tridiagonal_solver.f90 is called), clamp to [0, 50], full next column
+__global__ void __launch_bounds__(256) k_tr_thomas_col(TArgs<float> a) {
+    const Geom &g = a.g;
+    unsigned tid = flat_tid();
+    if (tid >= (unsigned)g.NC) return;
+    const int i = g.cell_order[tid];
+    const int L = g.L, NC = g.NC;
+    const int tl = a.s.top_cell[i - 1], b = g.bottom_cell[i - 1];
+    if (tl == 0) {
+        for (int k = 0; k <= L + 1; ++k)
+            for (int tr = 0; tr < a.ntr; ++tr) a.con_new[ic(k, i, tr, L, NC)] = 0.0f;
+        return;
+    }
+    const int nvl = tl - b + 1;
+    const long base = (long)(i - 1) * L;
+    float gam[GOM_MAXL], x[GOM_MAXL][2];
+    // row r = 1..nvl is layer k = tl + 1 - r: its lower neighbour (row r - 1) is the layer above
+    float den = a.w.tr_b[base + tl - 1];
+    bool ok = den != 0.0f;
+    for (int tr = 0; tr < a.ntr; ++tr) x[0][tr] = a.w.tr_rhs[((long)tr * NC + i - 1) * L + tl - 1] / den;
+    for (int r = 2; r <= nvl && ok; ++r) {
+        const int k = tl + 1 - r;
+        const float lower = a.w.tr_c[base + k - 1];       // coupling to the layer above
+        const float upper_prev = a.w.tr_a[base + k];       // previous row's coupling to this layer
+        gam[r - 1] = upper_prev / den;
+        den = a.w.tr_b[base + k - 1] - lower * gam[r - 1];
+        ok = den != 0.0f;
+        for (int tr = 0; tr < a.ntr; ++tr)
+            x[r - 1][tr] = (a.w.tr_rhs[((long)tr * NC + i - 1) * L + k - 1] - lower * x[r - 2][tr]) / den;
+    }
+    if (!ok) {
+        record_error(a.st, GOM_E_ZERO_PIVOT, 1285, i, 0, 0.0);
+        return;
+    }
+    for (int r = nvl - 1; r >= 1; --r)
+        for (int tr = 0; tr < a.ntr; ++tr) x[r - 1][tr] = x[r - 1][tr] - gam[r] * x[r][tr];
+    for (int tr = 0; tr < a.ntr; ++tr) {
+        for (int k = 0; k <= L + 1; ++k) {
+            float v = 0.0f;
+            if (k >= b && k <= tl) v = clamp_tracer(x[tl - k][tr], a.con[ic(k, i, tr, L, NC)]);
+            a.con_new[ic(k, i, tr, L, NC)] = v;
+        }
+    }
+}
+
 // :1403-1454 node averages (column, top-down) and :1457-1482 face averages + write-back
 template <typename R> __global__ void k_tr_nodes(TArgs<R> a) {
     unsigned tid = flat_tid();
@@ -595,6 +862,8 @@ template <typename R> cudaError_t launch_transport(const LaunchT<R> &x) {
     a.con_new = x.w.con2;
     k_tr_load<<<blocks_for((long)g.NC * (L + 2), 256), 256, 0, x.stream>>>(a);
     bool lim = p.h_flux_limiter > 0 || p.v_flux_limiter > 0;
+    const int bs_solve = x.tune[TUNE_TR_SOLVE] == 1 ? 64 : x.tune[TUNE_TR_SOLVE] == 2 ? 256 : 128;
+    const int bs_lim = x.tune[TUNE_TR_LIMITER] == 1 ? 64 : x.tune[TUNE_TR_LIMITER] == 2 ? 256 : 128;
     R *cur = x.w.con, *nxt = x.w.con2;
     for (int sub = 0; sub < a.Nt; ++sub) {
         a.sub = sub;
@@ -602,13 +871,29 @@ template <typename R> cudaError_t launch_transport(const LaunchT<R> &x) {
         a.con_new = nxt;
         if (g.NOB + g.NQB > 0) k_tr_bc<<<blocks_for(g.NOB + g.NQB, 128), 128, 0, x.stream>>>(a);
         a.changed_only = sub > 0;
-        k_tr_face_coef<<<blocks_for(g.NF, 128), 128, 0, x.stream>>>(a);
+        if constexpr (sizeof(R) == sizeof(float))
+            k_tr_face_coef_flat<<<blocks_for((long)g.NF * L, 256), 256, 0, x.stream>>>(a);
+        else
+            k_tr_face_coef<<<blocks_for(g.NF, 128), 128, 0, x.stream>>>(a);
         k_tr_cell_coef<<<blocks_for(g.NC, 128), 128, 0, x.stream>>>(a);
         if (lim) {
-            k_tr_limiter_cells<<<blocks_for(g.NC, 128), 128, 0, x.stream>>>(a);
-            k_tr_limiter_faces<<<blocks_for(g.NF, 128), 128, 0, x.stream>>>(a);
+            if constexpr (sizeof(R) == sizeof(float)) {
+                k_tr_sums_cl<<<blocks_for((long)g.NC * L, bs_lim), bs_lim, 0, x.stream>>>(a);
+                k_tr_vpsi_cl<<<blocks_for((long)g.NC * L, bs_lim), bs_lim, 0, x.stream>>>(a);
+            } else {
+                k_tr_limiter_cells<<<blocks_for(g.NC, bs_lim), bs_lim, 0, x.stream>>>(a);
+            }
+            if constexpr (sizeof(R) == sizeof(float))
+                k_tr_limiter_faces_flat<<<blocks_for((long)g.NF * L, 256), 256, 0, x.stream>>>(a);
+            else
+                k_tr_limiter_faces<<<blocks_for(g.NF, 128), 128, 0, x.stream>>>(a);
         }
-        k_tr_solve<<<blocks_for(g.NC, 128), 128, 0, x.stream>>>(a);
+        if constexpr (sizeof(R) == sizeof(float)) {
+            k_tr_rows_cl<<<blocks_for((long)g.NC * L, bs_solve), bs_solve, 0, x.stream>>>(a);
+            k_tr_thomas_col<<<blocks_for(g.NC, 128), 128, 0, x.stream>>>(a);
+        } else {
+            k_tr_solve<<<blocks_for(g.NC, bs_solve), bs_solve, 0, x.stream>>>(a);
+        }
         R *t = cur;
         cur = nxt;
         nxt = t;

@@ -32,9 +32,9 @@ M2_PERIOD_H = 12.42
 
 
 def ensemble_z_grid(max_layers: int = 30):
-    """Shared vertical grid of an ensemble: 1 m levels from -(max_layers + 0.5) m to +2.5 m (no
-    level at MSL, read_main_inp.f90 card C2_1)."""
-    return -float(max_layers) - 0.5, 2.5, max_layers + 3
+    """Shared vertical grid of an ensemble: 1 m levels from -(max_layers + 0.5) m to +6.5 m, room
+    for surge + tide above MSL (no level at MSL, read_main_inp.f90 card C2_1)."""
+    return -float(max_layers) - 0.5, 6.5, max_layers + 7
 
 
 @dataclasses.dataclass

@@ -19,7 +19,7 @@ import time
 
 import numpy as np
 
-from .core import GomCore
+from .core import GomCore, GomError
 from .deck import Deck
 
 
@@ -34,9 +34,12 @@ class Request:
     started: float = -1.0
     finished: float = -1.0
     done_steps: int = 0
+    error: str = ""
 
 
-def _context(lib, deck: Deck, precision: int, storm) -> GomCore:
+def storm_context(lib, deck: Deck, precision: int, storms: list) -> GomCore:
+    """A context for a storm-surge deck (one run or a packed ensemble, one storm per run) with
+    its initial state and forcing set up on the device."""
     d = dataclasses.replace(deck, params=dataclasses.replace(deck.params, precision=precision))
     c = GomCore(d, lib=lib)
     p = d.params
@@ -47,7 +50,7 @@ def _context(lib, deck: Deck, precision: int, storm) -> GomCore:
     cob[:, 0, :] = p.ref_salt
     cob[:, 1, :] = p.ref_temp
     c.set_forcing({"elapsed_time": 0.0, "spinup_tide": 1.0, "spinup_baroclinic": 1.0, "con_at_ob": cob})
-    c.set_storms([storm], elapsed_time=0.0)
+    c.set_storms(storms, elapsed_time=0.0)
     return c
 
 
@@ -61,8 +64,9 @@ def active_cell_layers(core: GomCore, deck: Deck) -> int:
 class Server:
     """Continuous batching of storm-surge runs under a device-memory budget."""
 
-    def __init__(self, lib, budget_bytes: float, precision: int = 1):
+    def __init__(self, lib, budget_bytes: float, precision: int = 1, on_finish=None):
         self.lib = lib
+        self.on_finish = on_finish         # called with (request, context) before a run is retired
         self.budget = float(budget_bytes)
         self.precision = precision
         self.active: list[tuple[Request, GomCore]] = []
@@ -82,7 +86,7 @@ class Server:
             if self.active and self.used + self._estimate(req) > self.budget:
                 return
             self.waiting.pop(0)
-            core = _context(self.lib, req.deck, self.precision, req.storm)
+            core = storm_context(self.lib, req.deck, self.precision, [req.storm])
             nbytes = core.device_bytes()
             self.bytes_per_cell_layer = max(self.bytes_per_cell_layer or 0.0,
                                             nbytes / (req.deck.n_cells * (req.deck.n_layers + 2)))
@@ -96,14 +100,21 @@ class Server:
     def tick(self, clock) -> list[Request]:
         for _, core in self.active:
             core.step_launch()
-        for _, core in self.active:
-            core.step_wait()
+        failed = set()
+        for req, core in self.active:
+            try:
+                core.step_wait()
+            except GomError as e:      # a run that stops (as the reference would) leaves the mix
+                req.error = str(e)
+                failed.add(req.rid)
         now = clock()
         done, keep = [], []
         for req, core in self.active:
             req.done_steps += 1
-            if req.done_steps >= req.steps:
+            if req.done_steps >= req.steps or req.rid in failed:
                 req.finished = now
+                if self.on_finish:
+                    self.on_finish(req, core)
                 self.used -= core.device_bytes()
                 core.close()
                 done.append(req)
@@ -149,13 +160,16 @@ def serve_fifo(lib, requests: list[Request], precision: int = 0) -> dict:
         now = clock()
         if now < req.arrival:
             time.sleep(req.arrival - now)
-        core = _context(lib, req.deck, precision, req.storm)
+        core = storm_context(lib, req.deck, precision, [req.storm])
         peak = max(peak, core.device_bytes())
         req.cell_layers = active_cell_layers(core, req.deck)
         req.started = clock()
-        for _ in range(req.steps):
-            core.step_launch()
-            core.step_wait()
+        try:
+            for _ in range(req.steps):
+                core.step_launch()
+                core.step_wait()
+        except GomError as e:
+            req.error = str(e)
         req.finished = clock()
         req.done_steps = req.steps
         work += req.cell_layers * req.steps
@@ -165,7 +179,9 @@ def serve_fifo(lib, requests: list[Request], precision: int = 0) -> dict:
 
 def _summary(requests, wall, work, peak_bytes, peak_active) -> dict:
     lat = np.array([r.finished - r.arrival for r in requests])
-    return {"requests": len(requests), "wall_s": wall, "cell_layer_steps": int(work),
+    return {"requests": len(requests), "failed": sum(1 for r in requests if r.error),
+            "errors": sorted({r.error for r in requests if r.error}), "wall_s": wall,
+            "cell_layer_steps": int(work),
             "throughput": work / wall if wall > 0 else 0.0,
             "latency_p50_s": float(np.percentile(lat, 50)), "latency_p99_s": float(np.percentile(lat, 99)),
             "latency_mean_s": float(lat.mean()), "peak_device_bytes": float(peak_bytes),
@@ -177,4 +193,4 @@ def poisson_arrivals(n: int, rate: float, seed: int) -> np.ndarray:
     return np.cumsum(rng.exponential(1.0 / rate, size=n))
 
 
-__all__ = ["Request", "Server", "serve", "serve_fifo", "poisson_arrivals", "active_cell_layers"]
+__all__ = ["Request", "Server", "serve", "serve_fifo", "poisson_arrivals", "active_cell_layers", "storm_context"]

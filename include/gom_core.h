@@ -381,6 +381,16 @@ int gom_set_storms(struct gom_ctx *ctx, int32_t n_storms, const gom_storm *storm
  * upload a host-built initial state field by field. */
 int gom_cold_start(struct gom_ctx *ctx, double salt, double temp, double av_0, double kv_0);
 
+/* Autotuner (no reference counterpart): times the compiled variants of the tunable launches
+ * (ELM walk: threads per block and register budget; momentum columns, transport column solve
+ * and limiter: threads per block) on the context's current state, `reps` runs each, keeps the
+ * fastest and re-captures the step graph.  The phases it runs only overwrite arrays that the
+ * next step recomputes before reading them (ELM velocities, momentum coefficients, transport
+ * outputs), so the run's results do not change.  Call between steps.  choice (may be NULL)
+ * receives the variant picked per site. */
+#define GOM_TUNE_SITES 4
+int gom_autotune(struct gom_ctx *ctx, int32_t reps, int32_t *choice);
+
 /* Device memory the context holds (bytes), for admission by memory budget when many contexts
  * share a GPU. */
 int64_t gom_device_bytes(const struct gom_ctx *ctx);

@@ -779,6 +779,13 @@ int gom_set_forcing(gom_ctx *c, const gom_forcing *f) {
 // the CPU restatement takes all forcing from the host, and its initial state from the host
 int gom_set_storms(gom_ctx *c, int32_t, const gom_storm *, double) { return c ? GOM_E_ARG : GOM_E_ARG; }
 int gom_cold_start(gom_ctx *c, double, double, double, double) { return c ? GOM_E_ARG : GOM_E_ARG; }
+// nothing to tune on the CPU
+int gom_autotune(gom_ctx *c, int32_t, int32_t *choice) {
+    if (!c) return GOM_E_ARG;
+    if (choice)
+        for (int k = 0; k < GOM_TUNE_SITES; ++k) choice[k] = 0;
+    return GOM_OK;
+}
 
 int gom_get_status(gom_ctx *c, gom_status *s, int clear) {
     if (!c || !s) return GOM_E_ARG;

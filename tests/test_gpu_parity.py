@@ -148,3 +148,29 @@ def test_async_launch_overlaps_next_forcing(gpu_lib):
             b.step_launch()
     for name in FIELDS:
         assert _exact_mismatch(a.get_field(name), b.get_field(name)) == 0, name
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_autotune_changes_speed_not_results(gpu_lib, precision):
+    """gom_autotune runs the tunable phases on the current state and only switches launch shapes:
+    what those phases overwrite is recomputed by the next step before it is read, so every later
+    step is unchanged bit for bit."""
+    import dataclasses
+    deck = estuary(nx=24, ny=12, dx=100.0, n_layers=10, trans_sub_iter=2)
+    deck = dataclasses.replace(deck, params=dataclasses.replace(deck.params, precision=precision))
+    st = initial_state(deck)
+    a = GomCore(deck, lib=gpu_lib)
+    b = GomCore(deck, lib=gpu_lib)
+    prepare(a, st)
+    prepare(b, st)
+    fa, fb = HostForcing(deck), HostForcing(deck)
+    for it in range(1, 9):
+        a.set_forcing(fa.step(it))
+        b.set_forcing(fb.step(it))
+        a.step_all()
+        b.step_all()
+        if it == 3:
+            choice = b.autotune(reps=2)
+            assert len(choice) == 4 and all(c >= 0 for c in choice)
+    for n in FIELDS:
+        assert _exact_mismatch(a.get_field(n), b.get_field(n)) == 0, n
