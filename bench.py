@@ -13,8 +13,9 @@ value          cell-layer-steps/s with the state resident in HBM: per step the h
 e2e            the same through the public API end to end: host forcing computed per step,
                uploaded from pinned memory, and the step's result (status, PCG iterations and
                the FP64 volume/salt sums) read back every step.
-roofline       the dominant phase timed alone with CUDA events, algorithmic bytes / time against
-               the measured HBM copy bandwidth.
+roofline       the dominant kernel (the transport column solve) timed alone with CUDA events,
+               algorithmic bytes / time against the measured HBM copy bandwidth; traffic is
+               ncu's DRAM bytes per launch of that kernel (profiles/roofline_traffic.md).
 cpu_baseline   the CPU restatement of the reference (oracle/, serial FP64) on a bounded sample.
 
 N > 1 runs independent replicas (the single-run path does not shard): value is the sum over
@@ -183,6 +184,23 @@ def time_phases(deck, st_snapshot, lib, forcing, torch, reps: int = 3) -> dict:
         out[ph] = min(ts)
     core.close()
     return out
+
+
+# transport column solve, per active cell-layer and launch: tracers read (2 x 8) and written
+# (2 x 8), face flux, diffusion and limiter coefficients of about two faces (2 x (8 + 8 + 2 x 8)),
+# interface flux, diffusion and limiter (8 + 8 + 2 x 8), old and new thickness (2 x 8); FP32
+# storage halves each term
+TR_SOLVE_BYTES_PER_CELL_LAYER = {"fp64": 144, "mixed": 72}
+
+
+def committed_traffic(key: str):
+    """DRAM bytes per launch measured by ncu for ``key`` (profiles/roofline_traffic.md), or None."""
+    import re
+    f = ROOT / "profiles" / "roofline_traffic.md"
+    if not f.exists():
+        return None
+    m = re.search(r"^\|\s*" + re.escape(key) + r"\s*\|\s*([0-9.eE+]+)\s*\|", f.read_text(), re.M)
+    return float(m.group(1)) if m else None
 
 
 def phase_bytes(deck, ncl: int, pcg_iters: float) -> dict:
@@ -364,7 +382,7 @@ def bench_serving(args):
     import dataclasses as dc
     from gom_release_gb300.core import load_core
     from gom_release_gb300.ensemble import ensemble_decks
-    from gom_release_gb300.serve import Request, poisson_arrivals, serve, serve_fifo
+    from gom_release_gb300.serve import Request, poisson_arrivals, serve, serve_fifo, serve_packed
     lib = load_core()
     t0 = time.perf_counter()
     pool = ensemble_decks(n_runs=args.pool, seed=5, min_cells=max(200, int(5000 * args.scale)),
@@ -385,18 +403,20 @@ def bench_serving(args):
         return out
 
     with ClockSampler(0) as clocks:
+        packed = serve_packed(lib, make_requests(), budget_bytes=150e9, precision=1)
         mixed = serve(lib, make_requests(), budget_bytes=150e9, precision=1)
         fifo = serve_fifo(lib, make_requests(), precision=0)
     line = {
-        "metric": METRIC, "value": mixed["throughput"], "unit": UNIT, "n_gpus": 1, "steps": None, "warmup": 0,
+        "metric": METRIC, "value": packed["throughput"], "unit": UNIT, "n_gpus": 1, "steps": None, "warmup": 0,
         "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
         "data": "synthetic",
         "config": {"workload": (f"serving: {args.requests} Poisson requests (rate 2/s), horizons U(6,48) h x "
                                 f"{args.horizon_scale:g}, meshes from a pool of {len(pool)} storm-surge runs "
                                 f"({min(d.n_cells for d in pool)}-{max(d.n_cells for d in pool)} cells), "
                                 "HBM budget 150 GB"), "generation_s": gen_s},
-        "serving_mixed": mixed, "serving_fp64_one_at_a_time": fifo,
-        "latency_p50_s": mixed["latency_p50_s"], "latency_p99_s": mixed["latency_p99_s"],
+        "serving_packed_mixed": packed, "serving_contexts_mixed": mixed, "serving_fp64_one_at_a_time": fifo,
+        "latency_p50_s": packed["latency_p50_s"], "latency_p99_s": packed["latency_p99_s"],
+        "throughput_vs_fp64_one_at_a_time": packed["throughput"] / fifo["throughput"],
         "clocks": clocks.summary(),
     }
     print(json.dumps(line), flush=True)
@@ -562,13 +582,15 @@ def main():
              gamma_t=run.forcing.gamma_t)
     pcg_mean = (pcg_total / max(1, args.warmup + args.steps))
     peak, peak_kind = measured_peak()
+    # dominant kernel: the transport column solve (one launch per subcycle), timed alone
+    solve_ms = run.core.profile_kernel(run.core.KERNEL_TRANSPORT_SOLVE, reps=5)
+    solve_bytes = TR_SOLVE_BYTES_PER_CELL_LAYER[args.precision] * ncl
+    achieved = solve_bytes / (solve_ms * 1e-3) / 1e9
+    traffic = committed_traffic(f"k_tr_solve {args.precision} estuary full") if args.size == "full" else None
     if args.no_phases:
-        phases, dom, achieved = {}, None, None
+        phases = {}
     else:
         phases = time_phases(deck, snap, lib, f, torch_mod)
-        pb = phase_bytes(deck, ncl, pcg_mean)
-        dom = max(phases, key=phases.get)
-        achieved = pb.get(dom, 0) / phases[dom] / 1e9
     if rank != 0:
         barrier(world)
         return
@@ -594,9 +616,13 @@ def main():
             "autotune": tune,
             "pcg_iters_mean": pcg_mean,
         },
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": (achieved / peak) if achieved else None, "peak_source": peak_kind, "traffic": None,
-                     "phase_ms": {k: v * 1e3 for k, v in phases.items()}},
+        "roofline": {"bound": "hbm", "kernel": "transport column solve (one subcycle)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_kind, "traffic": traffic, "algorithmic_bytes": solve_bytes,
+                     "ms_per_launch": solve_ms,
+                     "phase_ms": {k: v * 1e3 for k, v in phases.items()},
+                     "phase_algorithmic_gbs": {k: phase_bytes(deck, ncl, pcg_mean).get(k, 0) / v / 1e9
+                                               for k, v in phases.items() if v > 0}},
         "cpu_baseline": cpu,
         "e2e": {"value": ncl * ke * world / e2e_secs, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": 16 + 20, "wall_s": wall_e2e},

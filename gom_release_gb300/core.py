@@ -114,7 +114,7 @@ class GomForcing(C.Structure):
 
 class GomStorm(C.Structure):
     _fields_ = [(n, C.c_double) for n in ("x0", "y0", "heading", "speed", "rmax", "dp", "b", "coriolis",
-                                           "tide_amplitude", "tide_period", "tide_phase", "spinup")]
+                                           "tide_amplitude", "tide_period", "tide_phase", "spinup", "t0")]
 
 
 class GomStatus(C.Structure):
@@ -134,7 +134,7 @@ class GomError(RuntimeError):
         super().__init__(s)
 
 
-ABI_VERSION = 2      # GOM_ABI_VERSION of include/gom_core.h
+ABI_VERSION = 3      # GOM_ABI_VERSION of include/gom_core.h
 
 _STEPS = ["bottom_friction", "boundary_velocity", "advection", "momentum", "velocities", "layers",
           "node_velocity", "transport", "density", "turbulence", "swap"]
@@ -164,6 +164,8 @@ def _bind(lib: C.CDLL) -> C.CDLL:
     lib.gom_set_storms.argtypes = [vp, C.c_int32, C.POINTER(GomStorm), C.c_double]
     lib.gom_cold_start.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_double]
     lib.gom_autotune.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32)]
+    lib.gom_copy_run.argtypes = [vp, C.c_int32, vp, C.c_int32]
+    lib.gom_profile_kernel.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(C.c_double)]
     lib.gom_device_bytes.argtypes = [vp]
     lib.gom_device_bytes.restype = C.c_int64
     lib.gom_get_status.argtypes = [vp, C.POINTER(GomStatus), C.c_int]
@@ -344,12 +346,24 @@ class GomCore:
         self._check(self.lib.gom_autotune(self.ctx, reps, out), "autotune")
         return list(out)
 
+    KERNEL_ELM_WALK, KERNEL_MOMENTUM, KERNEL_TRANSPORT_SOLVE = 1, 2, 3
+
+    def profile_kernel(self, which: int, reps: int = 5) -> float:
+        """Mean milliseconds per launch of one kernel of the step, on the current state."""
+        ms = C.c_double()
+        self._check(self.lib.gom_profile_kernel(self.ctx, which, reps, C.byref(ms)), "profile_kernel")
+        return ms.value
+
+    def copy_run(self, dst_run: int, src: "GomCore", src_run: int):
+        """Copy one run's state from another context (packed contexts being repacked)."""
+        self._check(self.lib.gom_copy_run(self.ctx, dst_run, src.ctx, src_run), "copy_run")
+
     def device_bytes(self) -> int:
         return int(self.lib.gom_device_bytes(self.ctx))
 
     def set_storms(self, storms, elapsed_time: float = 0.0):
         """Device-side storm forcing, one storm per run (objects with gom_storm's fields)."""
-        arr = (GomStorm * len(storms))(*[GomStorm(*[float(getattr(s, n)) for n, _ in GomStorm._fields_])
+        arr = (GomStorm * len(storms))(*[GomStorm(*[float(getattr(s, n, 0.0)) for n, _ in GomStorm._fields_])
                                          for s in storms])
         self._check(self.lib.gom_set_storms(self.ctx, len(storms), arr, float(elapsed_time)), "set_storms")
 

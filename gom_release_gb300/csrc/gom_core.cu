@@ -37,6 +37,7 @@ struct gom_ctx {
     int device = 0;
     std::vector<void *> allocs;
     size_t bytes = 0;     // device memory held by the context
+    std::vector<int> run_starts[4];   // packed runs: host copies of run_{cell,face,node,ob}_start
     std::string msg;
     FieldDesc fields[GOM_F_COUNT];
     // forcing arrays on the device (the Forcing view points into these)
@@ -458,6 +459,7 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
                 if (v[r + 1] < v[r] || (t == 0 && v[r + 1] == v[r])) return fail(GOM_E_ARG);
         }
         const size_t NR1 = (size_t)d.n_runs + 1;
+        for (int t = 0; t < 4; ++t) c->run_starts[t].assign(starts[t], starts[t] + NR1);
         e = upload(c, &G.run_cell_start, (const int *)g->run_cell_start, NR1, true);
         if (e == cudaSuccess) e = upload(c, &G.run_face_start, (const int *)g->run_face_start, NR1, true);
         if (e == cudaSuccess) e = upload(c, &G.run_node_start, (const int *)g->run_node_start, NR1, true);
@@ -848,6 +850,35 @@ int gom_cold_start(gom_ctx *c, double salt, double temp, double av_0, double kv_
     return finish(c, nullptr, false);
 }
 
+int gom_profile_kernel(gom_ctx *c, int32_t which, int32_t reps, double *ms_per_launch) {
+    if (!c || reps < 1 || !ms_per_launch) return GOM_E_ARG;
+    cudaError_t (*run)(gom_ctx *) = nullptr;
+    switch (which) {
+    case GOM_KERNEL_ELM_WALK: run = GOM_PHASE(launch_elm_walk_only); break;
+    case GOM_KERNEL_MOMENTUM: run = GOM_PHASE(launch_momentum_columns_only); break;
+    case GOM_KERNEL_TRANSPORT_SOLVE:
+        CK(c->mixed ? launch_transport(c->xf) : launch_transport(c->x));   // coefficients and limiter
+        run = GOM_PHASE(launch_tr_solve_only);
+        break;
+    default: return GOM_E_ARG;
+    }
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    cudaError_t e = run(c);
+    if (e == cudaSuccess) e = cudaEventRecord(e0, c->x.stream);
+    for (int r = 0; r < reps && e == cudaSuccess; ++r) e = run(c);
+    if (e == cudaSuccess) e = cudaEventRecord(e1, c->x.stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    float ms = 0.0f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    CK(e);
+    *ms_per_launch = (double)ms / reps;
+    return finish(c, nullptr, false);
+}
+
 int gom_autotune(gom_ctx *c, int32_t reps, int32_t *choice) {
     if (!c || reps < 1) return GOM_E_ARG;
     struct Site {
@@ -895,9 +926,48 @@ int gom_autotune(gom_ctx *c, int32_t reps, int32_t *choice) {
     return finish(c, nullptr, false);
 }
 
+int gom_copy_run(gom_ctx *dst, int32_t dst_run, gom_ctx *src, int32_t src_run) {
+    gom_ctx *c = dst;
+    if (!dst || !src || dst->d.n_layers != src->d.n_layers || dst->mixed != src->mixed || dst->device != src->device)
+        return GOM_E_ARG;
+    if (dst_run < 0 || dst_run >= dst->x.g.NR || src_run < 0 || src_run >= src->x.g.NR) return GOM_E_ARG;
+    // the runs' entity ranges, from the host copies of the run tables
+    auto range = [](gom_ctx *k, int run, int kind, int64_t &b, int64_t &n) {
+        const gom_dims &d = k->d;
+        if (k->x.g.NR <= 1) {
+            b = 0;
+            n = kind == 0 ? d.n_cells : kind == 1 ? d.n_faces : kind == 2 ? d.n_nodes : kind == 3 ? d.n_qb : d.n_ob;
+            return;
+        }
+        const std::vector<int> &s = k->run_starts[kind == 0 ? 0 : kind == 1 ? 1 : kind == 2 ? 2 : 3];
+        b = s[run];
+        n = s[run + 1] - s[run];
+    };
+    CK(cudaStreamSynchronize(src->x.stream));
+    for (int f = 1; f < GOM_F_COUNT; ++f) {
+        const FieldDesc &fd = dst->fields[f];
+        if (fd.lo == -2 || is_forcing_field(f)) continue;
+        if (fd.kind == 3) {
+            if (dst->d.n_qb == 0 && src->d.n_qb == 0) continue;
+            return GOM_E_ARG;   // river cells are not split into runs
+        }
+        int64_t db, dn, sb, sn;
+        range(dst, dst_run, fd.kind, db, dn);
+        range(src, src_run, fd.kind, sb, sn);
+        if (dn != sn) return GOM_E_ARG;
+        const int64_t per = fd.lo < 0 ? 1 : (int64_t)(dst->d.n_layers - fd.lo + 1);
+        const size_t eb = (size_t)fd.dev_bytes;
+        char *dp = (char *)*fd.dev + (size_t)(db * per) * eb;
+        const char *sp = (const char *)*src->fields[f].dev + (size_t)(sb * per) * eb;
+        CK(cudaMemcpyAsync(dp, sp, (size_t)(dn * per) * eb, cudaMemcpyDeviceToDevice, dst->x.stream));
+    }
+    CK(cudaStreamSynchronize(dst->x.stream));
+    return GOM_OK;
+}
+
 int gom_set_storms(gom_ctx *c, int32_t n_storms, const gom_storm *storms, double elapsed_time) {
     if (!c || !storms || n_storms != c->x.g.NR) return GOM_E_ARG;
-    static_assert(sizeof(gom_storm) == 12 * sizeof(double), "gom_storm is 12 doubles");
+    static_assert(sizeof(gom_storm) == 13 * sizeof(double), "gom_storm is 13 doubles");
     for (int r = 0; r < n_storms; ++r) {
         const gom_storm &s = storms[r];
         if (!(s.rmax > 0.0) || !(s.dp >= 0.0) || !(s.b > 0.0) || !(s.tide_period > 0.0) || s.coriolis == 0.0)
@@ -905,7 +975,7 @@ int gom_set_storms(gom_ctx *c, int32_t n_storms, const gom_storm *storms, double
     }
     CK(cudaStreamSynchronize(c->x.stream));
     if (!c->d_storms) {
-        CK(dalloc(c, &c->d_storms, (size_t)12 * n_storms));
+        CK(dalloc(c, &c->d_storms, (size_t)13 * n_storms));
         CK(dalloc(c, &c->storm_wu, (size_t)c->d.n_nodes));
         CK(dalloc(c, &c->storm_wv, (size_t)c->d.n_nodes));
     }

@@ -78,6 +78,12 @@ template <typename R> cudaError_t pcg_configure(LaunchT<R> &x, int device);
 // static per-node weights of calculate_velocity_at_node.f90:103; called once per context
 template <typename R> cudaError_t launch_node_weights(const LaunchT<R> &x);
 
+// one kernel of a phase alone, on the current state (for timing): the ELM walk, the momentum
+// columns, the transport column solve of one subcycle (the transport phase must have run)
+template <typename R> cudaError_t launch_elm_walk_only(const LaunchT<R> &x);
+template <typename R> cudaError_t launch_momentum_columns_only(const LaunchT<R> &x);
+template <typename R> cudaError_t launch_tr_solve_only(const LaunchT<R> &x);
+
 // cold start on the device (all state fields must have been cleared first)
 template <typename R>
 cudaError_t launch_cold_start(const LaunchT<R> &x, double salt, double temp, double av0, double kv0);

@@ -20,15 +20,15 @@ constexpr double kAirDensity = 1.293;       // holland_storm_surge.f90:27
 constexpr double kGradToSurface = 0.95;     // holland_storm_surge.f90:28
 constexpr double kPFar = 101300.0;          // holland_storm_surge.f90:29, Pa
 constexpr double kInflow = 18.0 * 3.141592653589793 / 180.0;
-constexpr int kStormDoubles = 12;           // gom_storm
+constexpr int kStormDoubles = 13;           // gom_storm
 
 struct StormView {
-    double x0, y0, heading, speed, rmax, dp, b, coriolis, amp, period, phase, spinup;
+    double x0, y0, heading, speed, rmax, dp, b, coriolis, amp, period, phase, spinup, t0;
 };
 
 __device__ __forceinline__ StormView storm_at(const double *s, int r) {
     const double *p = s + (long)r * kStormDoubles;
-    return StormView{p[0], p[1], p[2], p[3], p[4], p[5], p[6], p[7], p[8], p[9], p[10], p[11]};
+    return StormView{p[0], p[1], p[2], p[3], p[4], p[5], p[6], p[7], p[8], p[9], p[10], p[11], p[12]};
 }
 
 // run holding entity e (0-based) given the runs' first entities
@@ -82,7 +82,7 @@ __global__ void k_storm_nodes(Geom g, const double *scal, const double *storms, 
     if (i >= g.NN) return;
     StormView s = storm_at(storms, run_of(g.run_node_start, g.NR, i));
     double u, v, p;
-    vortex(s, scal[0], g.x_node[i], g.y_node[i], u, v, p);
+    vortex(s, scal[0] - s.t0, g.x_node[i], g.y_node[i], u, v, p);
     wu[i] = u;
     wv[i] = v;
     air_p[i] = p;
@@ -93,7 +93,7 @@ __global__ void k_storm_faces(Geom g, const double *scal, const double *storms, 
     int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
     if (j > g.NF) return;
     StormView s = storm_at(storms, run_of(g.run_face_start, g.NR, j - 1));
-    double spin = spin_at(s, scal[0]);
+    double spin = spin_at(s, scal[0] - s.t0);
     int n1 = g.face_node(1, j), n2 = g.face_node(2, j);
     double u = (wu[n1 - 1] + wu[n2 - 1]) / 2.0, v = (wv[n1 - 1] + wv[n2 - 1]) / 2.0;
     double speed = sqrt(u * u + v * v);
@@ -119,7 +119,7 @@ __global__ void k_storm_ob(Geom g, const double *scal, const double *storms, dou
     if (i >= g.NOB) return;
     StormView s = storm_at(storms, run_of(g.run_ob_start, g.NR, i));
     int cell = g.ob_cell_id[i];
-    double x = g.x_cell[cell - 1], y = g.y_cell[cell - 1], t = scal[0];
+    double x = g.x_cell[cell - 1], y = g.y_cell[cell - 1], t = scal[0] - s.t0;
     eta_old[i] = ob_elevation(s, t - dt, x, y, rho_g);
     eta_new[i] = ob_elevation(s, t, x, y, rho_g);
 }

@@ -647,6 +647,20 @@ template <typename R> __global__ void k_copy_elm(Geom g, StateT<R> s) {
     s.elm_near_edge[t] = 0;
 }
 
+template <typename R> cudaError_t launch_elm_walk(const LaunchT<R> &x) {
+    // variants: threads per block and minimum resident blocks per SM (register budget)
+    switch (x.tune[TUNE_ELM]) {
+    case 1: k_elm_faces<R, 32, 1><<<blocks_for(x.g.NF, 32), 32, 0, x.stream>>>(x.g, x.s, x.p, x.status); break;
+    case 2: k_elm_faces<R, 128, 1><<<blocks_for(x.g.NF, 128), 128, 0, x.stream>>>(x.g, x.s, x.p, x.status); break;
+    case 3: k_elm_faces<R, 64, 12><<<blocks_for(x.g.NF, 64), 64, 0, x.stream>>>(x.g, x.s, x.p, x.status); break;
+    case 4: k_elm_faces<R, 64, 16><<<blocks_for(x.g.NF, 64), 64, 0, x.stream>>>(x.g, x.s, x.p, x.status); break;
+    default: k_elm_faces<R, 64, 1><<<blocks_for(x.g.NF, 64), 64, 0, x.stream>>>(x.g, x.s, x.p, x.status); break;
+    }
+    return cudaGetLastError();
+}
+
+template <typename R> cudaError_t launch_elm_walk_only(const LaunchT<R> &x) { return launch_elm_walk(x); }
+
 template <typename R> cudaError_t launch_advection(const LaunchT<R> &x) {
     long nfl = (long)x.g.NF * x.g.L;
     if (x.p.advection_flag == 0) {
@@ -658,15 +672,9 @@ template <typename R> cudaError_t launch_advection(const LaunchT<R> &x) {
         long nnl = (long)x.g.NN * x.g.L;
         k_elm_substeps<<<blocks_for(nnl, 256), 256, 0, x.stream>>>(x.g, x.s, x.p, x.w.idev);
     }
-    // variants: threads per block and minimum resident blocks per SM (register budget)
-    switch (x.tune[TUNE_ELM]) {
-    case 1: k_elm_faces<R, 32, 1><<<blocks_for(x.g.NF, 32), 32, 0, x.stream>>>(x.g, x.s, x.p, x.status); break;
-    case 2: k_elm_faces<R, 128, 1><<<blocks_for(x.g.NF, 128), 128, 0, x.stream>>>(x.g, x.s, x.p, x.status); break;
-    case 3: k_elm_faces<R, 64, 12><<<blocks_for(x.g.NF, 64), 64, 0, x.stream>>>(x.g, x.s, x.p, x.status); break;
-    case 4: k_elm_faces<R, 64, 16><<<blocks_for(x.g.NF, 64), 64, 0, x.stream>>>(x.g, x.s, x.p, x.status); break;
-    default: k_elm_faces<R, 64, 1><<<blocks_for(x.g.NF, 64), 64, 0, x.stream>>>(x.g, x.s, x.p, x.status); break;
-    }
-    return cudaGetLastError();
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return launch_elm_walk(x);
 }
 
 // ============================================================================================
@@ -941,6 +949,12 @@ template <typename R> __global__ void k_zero_face_columns(Geom g, StateT<R> s) {
     s.ainvdz2[t] = R(0);
 }
 
+template <typename R> cudaError_t launch_momentum_columns_only(const LaunchT<R> &x) {
+    const int bs = x.tune[TUNE_MOMENTUM] == 1 ? 64 : x.tune[TUNE_MOMENTUM] == 2 ? 256 : 128;
+    k_momentum<<<blocks_for(x.g.NF, bs), bs, 0, x.stream>>>(x.g, x.s, x.f, x.p, x.status);
+    return cudaGetLastError();
+}
+
 template <typename R> cudaError_t launch_momentum(const LaunchT<R> &x) {
     long nfl = (long)x.g.NF * x.g.L;
     k_zero_face_columns<<<blocks_for(nfl, 256), 256, 0, x.stream>>>(x.g, x.s);
@@ -953,5 +967,7 @@ GOM_INSTANTIATE_LAUNCH(launch_bottom_friction)
 GOM_INSTANTIATE_LAUNCH(launch_boundary_velocity)
 GOM_INSTANTIATE_LAUNCH(launch_advection)
 GOM_INSTANTIATE_LAUNCH(launch_momentum)
+GOM_INSTANTIATE_LAUNCH(launch_elm_walk_only)
+GOM_INSTANTIATE_LAUNCH(launch_momentum_columns_only)
 
 }  // namespace gom

@@ -835,6 +835,47 @@ template <typename R> __global__ void k_tr_faces_cells(TArgs<R> a) {
     }
 }
 
+template <typename R> bool transport_args(const LaunchT<R> &x, TArgs<R> &a) {
+    const Params &p = x.p;
+    if (!p.transport_flag) return false;
+    a.g = x.g;
+    a.s = x.s;
+    a.f = x.f;
+    a.p = x.p;
+    a.w = x.w;
+    a.st = x.status;
+    a.ntr = 0;
+    if (p.is_salt) a.tid[a.ntr++] = 1;
+    if (p.is_temp) a.tid[a.ntr++] = 2;
+    if (a.ntr == 0) return false;
+    a.Nt = p.trans_sub_iter == 0 ? 1 : p.trans_sub_iter;
+    a.dt2 = (R)(p.dt / a.Nt);
+    a.pow2 = (a.Nt & (a.Nt - 1)) == 0;
+    a.inv_nt = (R)(1.0 / a.Nt);
+    a.theta = (R)p.theta;
+    a.om_theta = (R)(1.0 - p.theta);
+    a.changed_only = false;
+    a.sub = 0;
+    a.con = x.w.con;
+    a.con_new = x.w.con2;
+    return true;
+}
+
+// the column solve of one subcycle alone (coefficients and limiter of the last transport call)
+template <typename R> cudaError_t launch_tr_solve_only(const LaunchT<R> &x) {
+    TArgs<R> a;
+    if (!transport_args(x, a)) return cudaSuccess;
+    const Geom &g = x.g;
+    const int bs_solve = x.tune[TUNE_TR_SOLVE] == 1 ? 64 : x.tune[TUNE_TR_SOLVE] == 2 ? 256 : 128;
+    if constexpr (sizeof(R) == sizeof(float)) {
+        k_tr_rows_cl<<<blocks_for((long)g.NC * g.L, bs_solve), bs_solve, 0, x.stream>>>(a);
+        k_tr_thomas_col<<<blocks_for(g.NC, 128), 128, 0, x.stream>>>(a);
+    } else {
+        k_tr_solve<<<blocks_for(g.NC, bs_solve), bs_solve, 0, x.stream>>>(a);
+    }
+    return cudaGetLastError();
+}
+
 template <typename R> cudaError_t launch_transport(const LaunchT<R> &x) {
     const Params &p = x.p;
     if (!p.transport_flag) return cudaSuccess;
@@ -1185,6 +1226,7 @@ template <typename R> cudaError_t launch_conservation(const LaunchT<R> &x) {
 }
 
 GOM_INSTANTIATE_LAUNCH(launch_transport)
+GOM_INSTANTIATE_LAUNCH(launch_tr_solve_only)
 GOM_INSTANTIATE_LAUNCH(launch_density)
 GOM_INSTANTIATE_LAUNCH(launch_turbulence)
 GOM_INSTANTIATE_LAUNCH(launch_conservation)

@@ -53,6 +53,7 @@ class Storm:
     tide_period: float   # s
     tide_phase: float    # rad
     spinup: float        # s, tanh ramp of tide and wind (setup_spinup.f90:22-31)
+    t0: float = 0.0      # context elapsed time at which the run's clock starts
 
 
 def storm_run(seed: int, n_cells: int, aspect: float, n_layers_run: int, dt: float = 60.0,

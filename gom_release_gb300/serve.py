@@ -1,13 +1,11 @@
-"""Serving storm-surge runs on one GPU: continuous batching of independent contexts.
+"""Serving storm-surge runs on one GPU: continuous batching.
 
-A request is one storm-surge run (mesh, storm, horizon).  The server keeps every admitted run's
-state resident in HBM in its own context (own CUDA stream and captured step graph).  Each tick it
-launches one step of every in-flight run (gom_step_launch: the graphs of all runs are queued
-before any is waited for, so their kernels overlap on the device), then waits for them
-(gom_step_wait) and retires the runs that reached their horizon.  Requests that arrive while
-others run are admitted at the next tick when the memory budget has room: the device bytes of a
-new context are estimated from the bytes per cell-layer of the contexts created so far, and the
-estimate is checked against the context's real size once created.
+A request is one storm-surge run (mesh, storm, horizon).  ``PackedServer`` (the serving form)
+keeps every in-flight run in one packed context, so each phase of a step is one launch over all
+runs; ``Server`` keeps one context per run and steps them in turn each tick.  Both retire runs
+that reach their horizon and admit waiting requests when the device-memory budget has room (the
+device bytes of new work are estimated from the bytes per cell-layer of the contexts created so
+far).
 
 ``serve_fifo`` is the comparison the configuration asks for: the same requests served one at a
 time, in arrival order, each run to its horizon before the next starts.
@@ -23,7 +21,7 @@ from .core import GomCore, GomError
 from .deck import Deck
 
 
-@dataclasses.dataclass
+@dataclasses.dataclass(eq=False)
 class Request:
     rid: int
     deck: Deck                # mesh + parameters (precision set by the server)
@@ -35,6 +33,7 @@ class Request:
     finished: float = -1.0
     done_steps: int = 0
     error: str = ""
+    t0: float = 0.0           # context clock at which the run started (packed serving)
 
 
 def storm_context(lib, deck: Deck, precision: int, storms: list) -> GomCore:
@@ -98,11 +97,15 @@ class Server:
             self.peak_active = max(self.peak_active, len(self.active))
 
     def tick(self, clock) -> list[Request]:
-        for _, core in self.active:
-            core.step_launch()
+        # Contexts are stepped one after another: the free-surface solve is a cooperative kernel
+        # that spins on grid barriers, and with the steps of many contexts queued on concurrent
+        # streams the block scheduler may keep its remaining blocks waiting behind other streams'
+        # kernels past the barrier's time limit (measured: GOM_E_TIMEOUT with 13 contexts in
+        # flight).  Device-side overlap of many runs is what PackedServer provides.
         failed = set()
         for req, core in self.active:
             try:
+                core.step_launch()
                 core.step_wait()
             except GomError as e:      # a run that stops (as the reference would) leaves the mix
                 req.error = str(e)
@@ -193,4 +196,163 @@ def poisson_arrivals(n: int, rate: float, seed: int) -> np.ndarray:
     return np.cumsum(rng.exponential(1.0 / rate, size=n))
 
 
-__all__ = ["Request", "Server", "serve", "serve_fifo", "poisson_arrivals", "active_cell_layers", "storm_context"]
+__all__ = ["Request", "Server", "PackedServer", "serve", "serve_packed", "serve_fifo", "poisson_arrivals",
+           "active_cell_layers", "storm_context"]
+
+
+class PackedServer:
+    """Continuous batching with every in-flight run packed into one context: each phase of a step
+    is one launch over all runs (per-run PCG), and the storms are evaluated on the device with a
+    clock offset per run.  Requests that arrive while others run are admitted at the next repack:
+    a new packed context is created with the runs still in flight plus the newcomers, the in-flight
+    runs' state is copied over with gom_copy_run, the newcomers start from a device cold start.
+    Repacks happen when requests are waiting (at most every ``min_interval`` seconds) or when
+    finished runs hold more than half of the packed cells; the device-memory budget bounds the
+    cells a pack may hold."""
+
+    def __init__(self, lib, budget_bytes: float, precision: int = 1, min_interval: float = 0.5,
+                 on_finish=None):
+        self.lib = lib
+        self.budget = float(budget_bytes)
+        self.precision = precision
+        self.min_interval = min_interval
+        self.on_finish = on_finish
+        self.core: GomCore | None = None
+        self.deck: Deck | None = None
+        self.members: list[Request] = []      # run r of the current pack is members[r]
+        self.waiting: list[Request] = []
+        self.elapsed = 0.0                    # context clock (s of simulated time)
+        self.last_repack = -1e30
+        self.bytes_per_cell_layer = None
+        self.peak_bytes = 0.0
+        self.peak_active = 0
+        self.repacks = 0
+
+    def _cells(self, reqs) -> float:
+        return float(sum(r.deck.n_cells * (r.deck.n_layers + 2) for r in reqs))
+
+    def active(self) -> list[Request]:
+        return [r for r in self.members if r.finished < 0]
+
+    def maybe_repack(self, now: float):
+        live = self.active()
+        dead = self._cells([r for r in self.members if r.finished >= 0])
+        want_new = bool(self.waiting) and (now - self.last_repack >= self.min_interval or not live)
+        want_gc = dead > 0.5 * max(self._cells(self.members), 1.0)
+        if not (want_new or want_gc):
+            return
+        admitted = []
+        if want_new:
+            budget_cells = (self.budget / self.bytes_per_cell_layer) if self.bytes_per_cell_layer else float("inf")
+            used = self._cells(live)
+            while self.waiting and (not live and not admitted or
+                                    used + self._cells([self.waiting[0]]) <= budget_cells):
+                r = self.waiting.pop(0)
+                used += self._cells([r])
+                admitted.append(r)
+        if not admitted and not want_gc:
+            return
+        self._repack(live, admitted, now)
+
+    def _repack(self, live, admitted, now):
+        from .ensemble import pack
+        old, old_members = self.core, self.members
+        members = live + admitted
+        self.members = members
+        self.last_repack = now
+        self.repacks += 1
+        if not members:
+            if old is not None:
+                old.close()
+            self.core = None
+            return
+        base = pack([r.deck for r in members])
+        deck = dataclasses.replace(base, params=dataclasses.replace(base.params, precision=self.precision))
+        core = GomCore(deck, lib=self.lib)
+        p = deck.params
+        core.cold_start(p.ref_salt, p.ref_temp, p.av_0, p.kv_0)
+        core.step("density")
+        nt = max(1, p.trans_sub_iter)
+        cob = np.zeros((deck.n_ob, 2, nt))
+        cob[:, 0, :] = p.ref_salt
+        cob[:, 1, :] = p.ref_temp
+        core.set_forcing({"elapsed_time": self.elapsed, "spinup_tide": 1.0, "spinup_baroclinic": 1.0,
+                          "con_at_ob": cob})
+        for r in admitted:
+            r.t0 = self.elapsed
+            r.started = now
+        core.set_storms([dataclasses.replace(r.storm, t0=r.t0) for r in members], elapsed_time=self.elapsed)
+        if old is not None:
+            for new_idx, r in enumerate(live):
+                core.copy_run(new_idx, old, old_members.index(r))
+            old.close()
+        top = core.get_field("top_layer_cell")
+        bot = deck.geo["bottom_layer_at_element"]
+        cs = deck.runs["run_cell_start"]
+        for i, r in enumerate(members):
+            if r in admitted:
+                sl = slice(cs[i], cs[i + 1])
+                t, b = top[sl], bot[sl]
+                r.cell_layers = int(np.sum((t - b + 1)[t > 0]))
+        nbytes = core.device_bytes()
+        self.bytes_per_cell_layer = max(self.bytes_per_cell_layer or 0.0, nbytes / self._cells(members))
+        self.peak_bytes = max(self.peak_bytes, float(nbytes))
+        self.peak_active = max(self.peak_active, len(members))
+        self.core = core
+        self.deck = deck
+
+    def tick(self, clock) -> list[Request]:
+        if self.core is None:
+            return []
+        self.core.step_launch()
+        err = ""
+        try:
+            self.core.step_wait()
+        except GomError as e:
+            err = str(e)
+        self.elapsed += self.deck.params.dt
+        now = clock()
+        done = []
+        for i, r in enumerate(self.members):
+            if r.finished >= 0:
+                continue
+            r.done_steps += 1
+            if err:
+                r.error = err
+            if r.done_steps >= r.steps or err:
+                r.finished = now
+                if self.on_finish:
+                    self.on_finish(r, self.core, i, self.deck)
+                done.append(r)
+        return done
+
+
+def serve_packed(lib, requests: list[Request], budget_bytes: float, precision: int = 1,
+                 min_interval: float = 0.5) -> dict:
+    """Replay a request stream in wall time through a PackedServer."""
+    srv = PackedServer(lib, budget_bytes, precision, min_interval)
+    pending = sorted(requests, key=lambda r: r.arrival)
+    t0 = time.perf_counter()
+    clock = lambda: time.perf_counter() - t0  # noqa: E731
+    finished = 0
+    i = 0
+    work = 0
+    while finished < len(requests):
+        now = clock()
+        while i < len(pending) and pending[i].arrival <= now:
+            srv.waiting.append(pending[i])
+            i += 1
+        srv.maybe_repack(now)
+        live = srv.active()
+        if not live:
+            if i < len(pending):
+                time.sleep(max(0.0, min(0.01, pending[i].arrival - now)))
+            continue
+        work += sum(r.cell_layers for r in live)
+        finished += len(srv.tick(clock))
+    srv.maybe_repack(clock())
+    if srv.core is not None:
+        srv.core.close()
+    out = _summary(requests, clock(), work, srv.peak_bytes, srv.peak_active)
+    out["repacks"] = srv.repacks
+    return out

@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define GOM_ABI_VERSION 2
+#define GOM_ABI_VERSION 3
 
 typedef struct gom_ctx gom_ctx;
 
@@ -369,6 +369,7 @@ typedef struct gom_storm {
     double tide_period;        /* (s)                                                  */
     double tide_phase;         /* (rad)                                                */
     double spinup;             /* ramp period (s); 0 = none                            */
+    double t0;                 /* context elapsed time at which this run's clock is 0  */
 } gom_storm;
 int gom_set_storms(struct gom_ctx *ctx, int32_t n_storms, const gom_storm *storms, double elapsed_time);
 
@@ -390,6 +391,22 @@ int gom_cold_start(struct gom_ctx *ctx, double salt, double temp, double av_0, d
  * receives the variant picked per site. */
 #define GOM_TUNE_SITES 4
 int gom_autotune(struct gom_ctx *ctx, int32_t reps, int32_t *choice);
+
+/* Copy every state array of one run of src into one run of dst (no reference counterpart): for
+ * moving in-flight runs between packed contexts when a server repacks its ensemble.  The two runs
+ * must have the same cell, face and node counts, the contexts the same layers and precision and
+ * the same device.  Forcing arrays are not copied (storms recompute them every step). */
+int gom_copy_run(struct gom_ctx *dst, int32_t dst_run, struct gom_ctx *src, int32_t src_run);
+
+/* Timing hook for the roofline figures (no reference counterpart): launches one kernel of the
+ * step alone `reps` times on the current state and returns its mean time per launch (CUDA
+ * events on the context stream).  Call between steps; what it overwrites is recomputed by the
+ * next step before it is read. */
+#define GOM_KERNEL_ELM_WALK 1         /* the per-face ELM walk                              */
+#define GOM_KERNEL_MOMENTUM 2         /* the per-face momentum columns                      */
+#define GOM_KERNEL_TRANSPORT_SOLVE 3  /* one transport subcycle's column solve (after the   */
+                                      /* phase has run once to form its coefficients)      */
+int gom_profile_kernel(struct gom_ctx *ctx, int32_t which, int32_t reps, double *ms_per_launch);
 
 /* Device memory the context holds (bytes), for admission by memory budget when many contexts
  * share a GPU. */

@@ -803,6 +803,8 @@ int gom_synchronize(gom_ctx *c) { return c ? GOM_OK : GOM_E_ARG; }
 int64_t gom_pcg_iterations_total(gom_ctx *c) { return c ? c->pcg_total : 0; }
 
 int64_t gom_device_bytes(const gom_ctx *) { return 0; }
+int gom_profile_kernel(gom_ctx *c, int32_t, int32_t, double *) { return c ? GOM_E_ARG : GOM_E_ARG; }
+int gom_copy_run(gom_ctx *dst, int32_t, gom_ctx *, int32_t) { return dst ? GOM_E_ARG : GOM_E_ARG; }
 
 void *gom_stream(gom_ctx *c) {
     (void)c;
@@ -2320,6 +2322,26 @@ int gom_conservation(gom_ctx *c, double *volume, double *salt_mass) {
     if (volume) *volume = v;
     if (salt_mass) *salt_mass = s;
     return GOM_OK;
+}
+
+// ---------------------------------------------------------------- test hooks (KATs only)
+// The restated building blocks, callable one at a time by the known-answer tests.
+int gom_oracle_tridiagonal(int32_t n, int32_t nc, const double *a, const double *b, const double *c,
+                           const double *rhs, double *sol) {
+    if (n <= 0 || nc <= 0) return GOM_E_ARG;
+    std::vector<double> gam(n + 1, 0.0);
+    return tridiagonal_solver(n, n, nc, a, b, c, rhs, sol, gam.data()) ? GOM_OK : GOM_E_ZERO_PIVOT;
+}
+
+int gom_oracle_bilinear(const double *xq, const double *yq, double x, double y, double *shapef) {
+    double xi = 0.0, eta = 0.0;
+    return bilinear_interpolation(xq[0], xq[1], xq[2], xq[3], yq[0], yq[1], yq[2], yq[3], x, y, xi, eta, shapef);
+}
+
+int gom_oracle_check_intersection(const double *seg, double *xy) {
+    int iflag = 0;
+    check_intersection(seg[0], seg[1], seg[2], seg[3], seg[4], seg[5], seg[6], seg[7], iflag, xy[0], xy[1]);
+    return iflag;
 }
 
 }  // extern "C"

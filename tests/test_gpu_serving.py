@@ -52,3 +52,45 @@ def test_each_request_same_alone_and_in_the_mix(gpu_lib, precision):
         for k in OUT:
             assert np.array_equal(alone.get_field(k), got[req.rid][k]), (req.rid, k)
         alone.close()
+
+
+@pytest.mark.parametrize("precision,rtol", [(0, 1e-8), (1, 1e-4)])
+def test_packed_server_same_alone_and_in_the_mix(gpu_lib, precision, rtol):
+    """Runs admitted into a packed context at different times (repacks move the in-flight runs
+    with gom_copy_run) end as they end alone, within the free-surface solver's round-off."""
+    from gom_release_gb300.ensemble import split
+    from gom_release_gb300.serve import PackedServer
+
+    got = {}
+
+    def keep(req, core, run, deck):
+        got[req.rid] = {k: split(deck, k, core.get_field(k))[run] for k in OUT}
+
+    srv = PackedServer(gpu_lib, budget_bytes=64e9, precision=precision, min_interval=0.0, on_finish=keep)
+    reqs = _requests()
+    clock = time.perf_counter
+    srv.waiting.append(reqs[0])
+    for tick in range(24):
+        if tick == 2:
+            srv.waiting.append(reqs[1])
+        if tick == 4:
+            srv.waiting += reqs[2:]
+        srv.maybe_repack(float(tick))
+        if not srv.active() and not srv.waiting:
+            break
+        srv.tick(clock)
+    assert sorted(got) == [0, 1, 2, 3]
+    assert srv.repacks >= 3
+    for req in reqs:
+        alone = storm_context(gpu_lib, req.deck, precision, [req.storm])
+        for _ in range(req.steps):
+            alone.step_launch()
+            alone.step_wait()
+        for k in OUT:
+            a, b = alone.get_field(k), got[req.rid][k]
+            if a.dtype.kind == "i":
+                assert np.array_equal(a, b), (req.rid, k)
+            else:
+                scale = max(float(np.abs(a).max()), 1e-30)
+                assert float(np.abs(a - b).max()) <= rtol * scale, (req.rid, k)
+        alone.close()

@@ -292,3 +292,79 @@ def test_step_closure_switches_at_critical_richardson(oracle_so):
         ks = list(ks)
         assert all(av[k] == 1e-5 for k in ks[:-1])
         assert av[ks[-1]] == 1e-3
+
+
+# ----------------------------------------------------------------- building blocks
+import ctypes as _C
+
+
+def _hooks(so):
+    lib = _C.CDLL(str(so))
+    D = _C.POINTER(_C.c_double)
+    lib.gom_oracle_tridiagonal.argtypes = [_C.c_int32, _C.c_int32, D, D, D, D, D]
+    lib.gom_oracle_bilinear.argtypes = [D, D, _C.c_double, _C.c_double, D]
+    lib.gom_oracle_check_intersection.argtypes = [D, D]
+    return lib, D
+
+
+def test_tridiagonal_against_dense_solve(oracle_so):
+    """tridiagonal_solver.f90 on random diagonally dominant systems with three right-hand sides
+    against a dense LU solve."""
+    lib, D = _hooks(oracle_so)
+    rng = np.random.default_rng(5)
+    for n in (1, 2, 7, 40):
+        a = rng.uniform(-1, 0, n)
+        c = rng.uniform(-1, 0, n)
+        b = 2.5 + rng.uniform(0, 1, n)
+        rhs = rng.normal(size=(3, n))
+        sol = np.zeros((3, n))
+        assert lib.gom_oracle_tridiagonal(n, 3, a.ctypes.data_as(D), b.ctypes.data_as(D), c.ctypes.data_as(D),
+                                          rhs.ctypes.data_as(D), sol.ctypes.data_as(D)) == 0
+        m = np.diag(b) + np.diag(a[1:], -1) + np.diag(c[:-1], 1)
+        want = np.linalg.solve(m, rhs.T).T
+        np.testing.assert_allclose(sol, want, rtol=1e-12, atol=1e-12)
+    # zero pivot is reported, not divided by
+    z = np.zeros(3)
+    one = np.ones(3)
+    out = np.zeros(3)
+    assert lib.gom_oracle_tridiagonal(3, 1, one.ctypes.data_as(D), z.ctypes.data_as(D), one.ctypes.data_as(D),
+                                      one.ctypes.data_as(D), out.ctypes.data_as(D)) != 0
+
+
+def test_inverse_bilinear_round_trip(oracle_so):
+    """bilinear_interpolation.f90 inverts the bilinear map of random convex quads: shape functions
+    at a point mapped from (xi, eta) are those of (xi, eta), and reproduce the point."""
+    lib, D = _hooks(oracle_so)
+    rng = np.random.default_rng(9)
+    for _ in range(200):
+        # a convex quad: a perturbed square of side ~100 m, counter-clockwise
+        base = np.array([[-50.0, -50.0], [50.0, -50.0], [50.0, 50.0], [-50.0, 50.0]])
+        q = base + rng.uniform(-12, 12, size=(4, 2))
+        xi, eta = rng.uniform(-0.95, 0.95, 2)
+        n = np.array([(1 - xi) * (1 - eta), (1 + xi) * (1 - eta), (1 + xi) * (1 + eta), (1 - xi) * (1 + eta)]) / 4
+        x, y = n @ q[:, 0], n @ q[:, 1]
+        xq = np.ascontiguousarray(q[:, 0])
+        yq = np.ascontiguousarray(q[:, 1])
+        sh = np.zeros(4)
+        assert lib.gom_oracle_bilinear(xq.ctypes.data_as(D), yq.ctypes.data_as(D), x, y, sh.ctypes.data_as(D)) == 0
+        np.testing.assert_allclose(sh, n, atol=1e-9)
+        assert abs(sh @ q[:, 0] - x) < 1e-7 and abs(sh @ q[:, 1] - y) < 1e-7
+
+
+def test_segment_intersection_inclusive(oracle_so):
+    """check_intersection.f90: crossing segments meet at the right point; touching at an end point
+    counts (inclusive [0, 1]); parallel and disjoint segments do not."""
+    lib, D = _hooks(oracle_so)
+
+    def hit(x1, y1, x2, y2, x3, y3, x4, y4):
+        seg = np.array([x1, x2, x3, x4, y1, y2, y3, y4], dtype=float)
+        xy = np.zeros(2)
+        f = lib.gom_oracle_check_intersection(seg.ctypes.data_as(D), xy.ctypes.data_as(D))
+        return f, xy
+
+    f, xy = hit(0, 0, 2, 2, 0, 2, 2, 0)
+    assert f == 1 and np.allclose(xy, [1, 1])
+    f, xy = hit(0, 0, 1, 1, 1, 1, 2, 0)          # touch at an end point
+    assert f == 1 and np.allclose(xy, [1, 1])
+    assert hit(0, 0, 1, 0, 0, 1, 1, 1)[0] == 0  # parallel
+    assert hit(0, 0, 1, 1, 2, 0, 3, -1)[0] == 0  # disjoint
