@@ -313,6 +313,25 @@ def time_core_steps(core, k: int) -> float:
     return e0.elapsed_time(e1) / 1e3
 
 
+def phase_times_in_place(core) -> dict:
+    """One step run phase by phase (the context's own forcing kernels excluded), each phase timed
+    with CUDA events on the context stream."""
+    import torch
+    from gom_release_gb300.core import TIME_LOOP
+    stream = torch.cuda.ExternalStream(core.stream_handle())
+    out = {}
+    for ph in TIME_LOOP:
+        core.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        core.step(ph)
+        e1.record(stream)
+        e1.synchronize()
+        out[ph] = e0.elapsed_time(e1)
+    return out
+
+
 def bench_ensemble(args):
     """Storm-surge ensemble: every run packed into one mixed-precision context (one launch per
     phase for all runs, per-run PCG, device-side forcing) against the plain FP64 path serving
@@ -338,11 +357,12 @@ def bench_ensemble(args):
             ncl = active_cell_layers(core, pk)
             nbytes = core.device_bytes()
             time_core_steps(core, w)
-            core.autotune(reps=2)
+            tune = core.autotune(reps=2)
             time_core_steps(core, 1)
             secs = time_core_steps(core, k)
             res[label] = {"value": ncl * k / secs, "ms_per_step": secs / k * 1e3, "device_gb": nbytes / 1e9,
-                          "active_cell_layers": ncl, "pcg_iters_total": core.pcg_iterations_total()}
+                          "active_cell_layers": ncl, "pcg_iters_total": core.pcg_iterations_total(),
+                          "autotune": tune, "phase_ms": phase_times_in_place(core)}
             core.close()
         kb = max(2, k // 5)
         for label, prec in (("fp64_one_at_a_time", 0), ("mixed_one_at_a_time", 1)):

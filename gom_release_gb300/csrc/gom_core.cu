@@ -122,6 +122,10 @@ template <typename R> cudaError_t alloc_layered_work(gom_ctx *c, WorkT<R> &W) {
             if (e == cudaSuccess) e = dalloc(c, p, L * NC);
         if (e == cudaSuccess) e = dalloc(c, &W.tr_rhs, L * NC * 2);
         if (e == cudaSuccess) e = dalloc(c, &W.tr_last, 4 * NC);
+        if (e == cudaSuccess) e = dalloc(c, &W.cl_list, L * NC);
+        if (e == cudaSuccess) e = dalloc(c, &W.cl_off, NC);
+        if (e == cudaSuccess) e = dalloc(c, &W.cl_bsum, NC / 1024 + 2);
+        if (e == cudaSuccess) e = dalloc(c, &W.cl_count, 1);
     }
     return e;
 }
@@ -607,6 +611,10 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
             return fail(GOM_E_NOMEM);
     }
     if (c->mixed) {
+        float *el = nullptr;
+        if (dalloc(c, &el, 8 * NC) != cudaSuccess) return fail(GOM_E_NOMEM);
+        c->x.g.elem_local = el;
+        if (launch_elem_local(c->x.g, el, c->x.stream) != cudaSuccess) return fail(GOM_E_CUDA);
         // the FP32 context shares geometry, forcing, parameters, status, stream and the FP64
         // work arrays (free-surface system, PCG vectors, ELM counts, node weights, sums)
         LaunchT<float> &X = c->xf;

@@ -41,6 +41,8 @@ struct Geom {
     // entity ids sorted by bottom layer: column kernels take their entity from these so that the
     // 32 lanes of a warp walk columns of nearly equal height (results do not depend on the order)
     const int *cell_order, *face_order, *node_order;
+    // element node offsets from the element centre in FP32, (8, NC): x1..x4, y1..y4 (mixed path)
+    const float *elem_local;
     // packed runs (NR > 1): 0-based first cell / face / node / open-boundary cell of each run
     int NR;
     const int *run_cell_start, *run_face_start, *run_node_start, *run_ob_start;

@@ -37,6 +37,8 @@ template <typename R> struct WorkT {
     // mixed-precision transport: rows of the vertical systems (L, NC) and right-hand sides
     // (L, NC, 2); top-layer horizontal sums of the limiter (2, NC, 2)
     R *tr_a = nullptr, *tr_b = nullptr, *tr_c = nullptr, *tr_rhs = nullptr, *tr_last = nullptr;
+    // mixed-precision transport: compact list of the wet (cell, layer) pairs and its scan arrays
+    int *cl_list = nullptr, *cl_off = nullptr, *cl_bsum = nullptr, *cl_count = nullptr;
     // conservation
     double *cons = nullptr;                                     // [volume, salt]
 };
@@ -83,6 +85,9 @@ template <typename R> cudaError_t launch_node_weights(const LaunchT<R> &x);
 template <typename R> cudaError_t launch_elm_walk_only(const LaunchT<R> &x);
 template <typename R> cudaError_t launch_momentum_columns_only(const LaunchT<R> &x);
 template <typename R> cudaError_t launch_tr_solve_only(const LaunchT<R> &x);
+
+// FP32 element node offsets (8 per element) for the mixed-precision ELM, once per context
+cudaError_t launch_elem_local(const Geom &g, float *out, cudaStream_t stream);
 
 // cold start on the device (all state fields must have been cleared first)
 template <typename R>

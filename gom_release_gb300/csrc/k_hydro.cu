@@ -7,6 +7,8 @@
 //   search_straight_line.f90:15-399, check_intersection.f90:14-50,
 //   bilinear_interpolation.f90:8-121, solve_momentum_equation.f90:15-656,
 //   tridiagonal_solver.f90:15-90.
+#include <type_traits>
+
 #include "gom_launch.h"
 
 namespace gom {
@@ -193,20 +195,44 @@ struct LocalElem {
     float ar;
 };
 
+// FP32 node offsets of every element, formed once per context
+__global__ void k_elem_local(Geom g, float *out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (i > g.NC) return;
+    int tq = g.tri_or_quad[i - 1];
+    double xc = g.x_cell[i - 1], yc = g.y_cell[i - 1];
+    float *o = out + (long)(i - 1) * 8;
+    for (int l = 0; l < 4; ++l) {
+        o[l] = 0.0f;
+        o[4 + l] = 0.0f;
+        if (l < tq) {
+            int n = g.cell_node(l + 1, i);
+            o[l] = (float)(g.x_node[n - 1] - xc);
+            o[4 + l] = (float)(g.y_node[n - 1] - yc);
+        }
+    }
+}
+
+cudaError_t launch_elem_local(const Geom &g, float *out, cudaStream_t stream) {
+    k_elem_local<<<blocks_for(g.NC, 256), 256, 0, stream>>>(g, out);
+    return cudaGetLastError();
+}
+
 __device__ __forceinline__ void load_local(const Geom &g, int nel, LocalElem &e) {
     e.tq = g.tri_or_quad[nel - 1];
     e.xc = g.x_cell[nel - 1];
     e.yc = g.y_cell[nel - 1];
     e.ar = (float)g.area[nel - 1];
-    for (int l = 0; l < 4; ++l) {
-        e.x[l] = 0.0f;
-        e.y[l] = 0.0f;
-        if (l < e.tq) {
-            int n = g.cell_node(l + 1, nel);
-            e.x[l] = (float)(g.x_node[n - 1] - e.xc);
-            e.y[l] = (float)(g.y_node[n - 1] - e.yc);
-        }
-    }
+    const float4 *v = reinterpret_cast<const float4 *>(g.elem_local + (long)(nel - 1) * 8);
+    const float4 xs = v[0], ys = v[1];
+    e.x[0] = xs.x;
+    e.x[1] = xs.y;
+    e.x[2] = xs.z;
+    e.x[3] = xs.w;
+    e.y[0] = ys.x;
+    e.y[1] = ys.y;
+    e.y[2] = ys.z;
+    e.y[3] = ys.w;
 }
 
 // 1: inside by the reference's test, 0: outside, -1: not decidable in FP32.  near: an edge line
@@ -362,11 +388,13 @@ __device__ int search_straight_line(const Geom &g, const StateT<R> &s, const Par
     if (top_el(s, nnel) == 0 || MSL - g.h_cell[nnel - 1] > MSL + s.eta_cell[nnel - 1]) return GOM_ELM_END_DRY;
     zt = fmin(fmax(zt, MSL - g.h_cell[nnel - 1]), MSL + s.eta_cell[nnel - 1]);
     if (zt <= g.z_level[0] || zt > g.z_level[L]) return GOM_ELM_Z_RANGE;
-    for (int k = 0; k <= L - 1; ++k) {
-        if (zt > g.z_level[k] && zt <= g.z_level[k + 1]) {
-            jlev = k + 1;
-            break;
-        }
+    // :376-396 the level k with z_level(k) < zt <= z_level(k+1), unique for increasing levels:
+    // searched from the start layer outwards instead of from the bottom (same k)
+    {
+        int k = min(max(jlev - 1, 0), L - 1);
+        while (k < L - 1 && zt > g.z_level[k + 1]) ++k;
+        while (k > 0 && zt <= g.z_level[k]) --k;
+        jlev = k + 1;
     }
     jlev = min(max(jlev, g.bottom_cell[nnel - 1]), top_el(s, nnel));
     return 0;
@@ -410,6 +438,8 @@ __device__ int elm_backtrace(const Geom &g, const StateT<R> &s, const Params &p,
             LocalElem el;
             load_local(g, nnel, el);
             const float px = (float)(xt - el.xc), py = (float)(yt - el.yc);
+            bool near;
+            const int cls = classify_f32(el, px, py, near);
             float sta[4];
             if (tq == 3) {
                 const float ar = el.ar;
@@ -425,7 +455,7 @@ __device__ int elm_backtrace(const Geom &g, const StateT<R> &s, const Params &p,
                     sta[2] = 1.0f - sta[0] - sta[1];
                 }
             } else {
-                if (out_elem_mixed(g, nnel, xt, yt)) return GOM_ELM_QUAD_OUTSIDE;
+                if (cls >= 0 ? cls == 0 : out_elem64(g, nnel, xt, yt)) return GOM_ELM_QUAD_OUTSIDE;
                 int b = bilinear_interpolation<float>(el.x[0], el.x[1], el.x[2], el.x[3], el.y[0], el.y[1], el.y[2],
                                                       el.y[3], px, py, sta);
                 if (b) return b;
@@ -442,8 +472,6 @@ __device__ int elm_backtrace(const Geom &g, const StateT<R> &s, const Params &p,
             uu = fu;
             vv = fv;
             ww = fw;
-            bool near;
-            (void)classify_f32(el, px, py, near);
             if (near && near_edge_line(g, nnel, xt, yt)) near_edge = 1;
         } else {
             double zrat = (zup - zt) / s.dz_cell[ix(jlev, nnel, L)];
@@ -516,10 +544,25 @@ template <typename R> __global__ void k_elm_edge_dev(Geom g, StateT<R> s, Params
     split_index(t, L, j, k);
     j += 1;
     k += 1;
+    int n1 = g.face_node(1, j), n2 = g.face_node(2, j);
+    if constexpr (sizeof(R) == sizeof(float)) {
+        // mixed path: the same count in FP32 (the node velocities are FP32 already)
+        const float dt = (float)p.dt, c01 = 0.1f;
+        const float dx = (float)(g.x_node[n1 - 1] - g.x_node[n2 - 1]), dy = (float)(g.y_node[n1 - 1] - g.y_node[n2 - 1]);
+        const float rl2 = dx * dx + dy * dy;
+        float du = (s.u_node[ix0(k, n1, L)] + s.u_node[ix0(k - 1, n1, L)]) * 0.5f -
+                   (s.u_node[ix0(k, n2, L)] + s.u_node[ix0(k - 1, n2, L)]) * 0.5f;
+        float dv = (s.v_node[ix0(k, n1, L)] + s.v_node[ix0(k - 1, n1, L)]) * 0.5f -
+                   (s.v_node[ix0(k, n2, L)] + s.v_node[ix0(k - 1, n2, L)]) * 0.5f;
+        float sq = du * du + dv * dv;
+        int id = 0;
+        if (!(sq < rl2 * (c01 * c01 / (dt * dt)) * (1.0f - 1e-5f))) id = (int)(sqrtf(sq) / sqrtf(rl2) * dt / c01);
+        idev[t] = id;
+        return;
+    }
     const double dt = p.dt;
     const double c01 = F(1.e-1f);
     const double kthr = c01 * c01 / (dt * dt) * (1.0 - 1e-9);
-    int n1 = g.face_node(1, j), n2 = g.face_node(2, j);
     double dx = g.x_node[n1 - 1] - g.x_node[n2 - 1], dy = g.y_node[n1 - 1] - g.y_node[n2 - 1];
     double rl2 = dx * dx + dy * dy;
     double u1 = (s.u_node[ix0(k, n1, L)] + s.u_node[ix0(k - 1, n1, L)]) * 0.5;
@@ -546,12 +589,21 @@ template <typename R> __global__ void k_elm_substeps(Geom g, StateT<R> s, Params
     split_index(t, L, i, k);
     i += 1;
     k += 1;
-    const double dt = p.dt;
     int nadj = g.adj_cells_at_node[i - 1];
-    double wi = (s.w_node[ix0(k, i, L)] + s.w_node[ix0(k - 1, i, L)]) * 0.5;
-    double aw = 2 * wi * dt;
-    int iw = fabs(aw) < p.delta_z_min * (1.0 - 1e-9) ? 0 : (int)(aw / p.delta_z_min);
-    double summ = 0.0;
+    int iw;
+    if constexpr (sizeof(R) == sizeof(float)) {
+        // mixed path: the same count in FP32
+        float aw = 2.0f * ((s.w_node[ix0(k, i, L)] + s.w_node[ix0(k - 1, i, L)]) * 0.5f) * (float)p.dt;
+        float dzm = (float)p.delta_z_min;
+        iw = fabsf(aw) < dzm * (1.0f - 1e-5f) ? 0 : (int)(aw / dzm);
+    } else {
+        const double dt = p.dt;
+        double wi = (s.w_node[ix0(k, i, L)] + s.w_node[ix0(k - 1, i, L)]) * 0.5;
+        double aw = 2 * wi * dt;
+        iw = fabs(aw) < p.delta_z_min * (1.0 - 1e-9) ? 0 : (int)(aw / p.delta_z_min);
+    }
+    using Sum = typename std::conditional<sizeof(R) == sizeof(float), float, double>::type;
+    Sum summ = Sum(0);
     for (int j = 1; j <= nadj; ++j) {
         int ie = g.node_cell(j, i), id = g.node_count(j, i);
         int tq = g.tri_or_quad[ie - 1];
@@ -560,7 +612,7 @@ template <typename R> __global__ void k_elm_substeps(Geom g, StateT<R> s, Params
         int fb = g.cell_face(wrap_edge(id - 2, tq), ie);
         int imax = max(idev[ix(k, fa, L)], idev[ix(k, fb, L)]);
         int idelta = max(imax, iw);
-        if (idelta != 0) summ = summ + (double)idelta / nadj;   // 0/nadj adds exactly 0
+        if (idelta != 0) summ = summ + (Sum)idelta / (Sum)nadj;   // 0/nadj adds exactly 0
     }
     s.num_sub_elm[ix(k, i, L)] = max(p.elm_min_iter, min(p.elm_max_iter, (int)summ));
 }
@@ -766,17 +818,6 @@ __global__ void __launch_bounds__(256) k_momentum(Geom g, StateT<R> s, Forcing f
     }
     bool wet_nodes = s.wetdry_node[node1 - 1] == 0 && s.wetdry_node[node2 - 1] == 0;
     double eta_n1 = s.eta_node[node1 - 1], eta_n2 = s.eta_node[node2 - 1];
-    // rtemp0 reaching the air-pressure term of a boundary face
-    double rt0_air;
-    if (a2 != 0) {
-        bool known;
-        rt0_air = face_final_rtemp0(g, s, f, p, j, known);
-    } else if (wet_nodes) {
-        rt0_air = gravity * dt / fl * (1.0 - theta) * (eta_n2 - eta_n1);
-    } else {
-        rt0_air = prev_rtemp0(g, s, f, p, j);
-    }
-    double rtemp3_air = -dt / p.rho_o * ((f.air_p[node2 - 1] - f.air_p[node1 - 1]) / fl);
     const R c069 = (R)F(0.69f);
     int ibnd = g.isflowside3[j - 1];
     double eta1 = s.eta_cell[a1 - 1];
@@ -785,22 +826,74 @@ __global__ void __launch_bounds__(256) k_momentum(Geom g, StateT<R> s, Forcing f
     int ba2 = a2 != 0 ? g.bottom_cell[a2 - 1] : 0, ta2 = a2 != 0 ? s.top_cell[a2 - 1] : 0;
     int bn1 = g.bottom_node[node1 - 1], tn1 = s.top_node[node1 - 1];
     int bn2 = g.bottom_node[node2 - 1], tn2 = s.top_node[node2 - 1];
-    // Terms the reference re-evaluates in every layer although their operands do not depend on
-    // the layer; evaluated once per face with the same expression, hence the same value.
-    double bt_rtemp1 = 0.0, bt_rtemp2 = 0.0;    // (1-theta) barotropic gradient across the face
-    if (btype == 0) {
-        double rtemp0 = gravity * dt / dj * (1.0 - theta) * (eta2 - eta1);
-        bt_rtemp1 = rtemp0 * ct2;
-        bt_rtemp2 = rtemp0 * sn2;
-    } else if (btype > 0) {
-        int ie = g.ob_element_flag[a1 - 1];
-        bt_rtemp1 = gravity * dt / dj * (1.0 - theta) * (f.eta_at_ob_old[ie - 1] - eta1);
+    R bt1, along, air1, air2, bc_dj, bc_fl;
+    if constexpr (sizeof(R) == sizeof(float)) {
+        // Mixed path: the same terms from FP64 differences of elevations and pressures, the
+        // divisions and products in FP32 (no FP64 division per face)
+        const float gdt = (float)(gravity * dt), om = (float)(1.0 - theta), dtr = (float)(dt / p.rho_o);
+        const float inv_dj = 1.0f / (float)dj, inv_fl = 1.0f / (float)fl;
+        float bt_rtemp1 = 0.0f, bt_rtemp2 = 0.0f;
+        if (btype == 0) {
+            float rtemp0 = gdt * inv_dj * om * (float)(eta2 - eta1);
+            bt_rtemp1 = rtemp0 * ct2R;
+            bt_rtemp2 = rtemp0 * sn2R;
+        } else if (btype > 0) {
+            int ie = g.ob_element_flag[a1 - 1];
+            bt_rtemp1 = gdt * inv_dj * om * (float)(f.eta_at_ob_old[ie - 1] - eta1);
+        }
+        const float along0 = wet_nodes ? gdt * inv_fl * om * (float)(eta_n2 - eta_n1) : 0.0f;
+        const double pref = f.air_p[node1 - 1];
+        float rt0_air;
+        if (a2 != 0) {
+            // mean air pressure of each adjacent cell, relative to a node value
+            float m1 = 0.0f, m2 = 0.0f;
+            int tqa = g.tri_or_quad[a1 - 1], tqb = g.tri_or_quad[a2 - 1];
+            for (int ll = 1; ll <= tqa; ++ll) m1 += (float)(f.air_p[g.cell_node(ll, a1) - 1] - pref);
+            for (int ll = 1; ll <= tqb; ++ll) m2 += (float)(f.air_p[g.cell_node(ll, a2) - 1] - pref);
+            rt0_air = -dtr * (m2 / (float)tqb - m1 / (float)tqa) * inv_dj;
+        } else if (wet_nodes) {
+            rt0_air = along0;
+        } else {
+            rt0_air = (float)prev_rtemp0(g, s, f, p, j);
+        }
+        const float rtemp3_air = -dtr * (float)(f.air_p[node2 - 1] - pref) * inv_fl;
+        bt1 = bt_rtemp1;
+        along = (btype == 0) ? (along0 + bt_rtemp2) : along0;
+        air1 = rt0_air * ct2R;
+        air2 = rtemp3_air + rt0_air * sn2R;
+        bc_dj = -(gdt / (float)p.rho_o) * inv_dj;
+        bc_fl = -(gdt / (float)p.rho_o) * inv_fl;
+    } else {
+        // rtemp0 reaching the air-pressure term of a boundary face
+        double rt0_air;
+        if (a2 != 0) {
+            bool known;
+            rt0_air = face_final_rtemp0(g, s, f, p, j, known);
+        } else if (wet_nodes) {
+            rt0_air = gravity * dt / fl * (1.0 - theta) * (eta_n2 - eta_n1);
+        } else {
+            rt0_air = prev_rtemp0(g, s, f, p, j);
+        }
+        double rtemp3_air = -dt / p.rho_o * ((f.air_p[node2 - 1] - f.air_p[node1 - 1]) / fl);
+        // Terms the reference re-evaluates in every layer although their operands do not depend
+        // on the layer; evaluated once per face with the same expression, hence the same value.
+        double bt_rtemp1 = 0.0, bt_rtemp2 = 0.0;    // (1-theta) barotropic gradient across the face
+        if (btype == 0) {
+            double rtemp0 = gravity * dt / dj * (1.0 - theta) * (eta2 - eta1);
+            bt_rtemp1 = rtemp0 * ct2;
+            bt_rtemp2 = rtemp0 * sn2;
+        } else if (btype > 0) {
+            int ie = g.ob_element_flag[a1 - 1];
+            bt_rtemp1 = gravity * dt / dj * (1.0 - theta) * (f.eta_at_ob_old[ie - 1] - eta1);
+        }
+        double along_rtemp0 = wet_nodes ? gravity * dt / fl * (1.0 - theta) * (eta_n2 - eta_n1) : 0.0;
+        bt1 = (R)bt_rtemp1;
+        along = (R)((btype == 0) ? (along_rtemp0 + bt_rtemp2) : along_rtemp0);
+        air1 = (R)(rt0_air * ct2);
+        air2 = (R)(rtemp3_air + rt0_air * sn2);
+        bc_dj = (R)(-gravity * dt / (p.rho_o * dj));
+        bc_fl = (R)(-gravity * dt / (p.rho_o * fl));
     }
-    double along_rtemp0 = wet_nodes ? gravity * dt / fl * (1.0 - theta) * (eta_n2 - eta_n1) : 0.0;
-    const R bt1 = (R)bt_rtemp1;
-    const R along = (R)((btype == 0) ? (along_rtemp0 + bt_rtemp2) : along_rtemp0);
-    const R air1 = (R)(rt0_air * ct2), air2 = (R)(rtemp3_air + rt0_air * sn2);
-    const R bc_dj = (R)(-gravity * dt / (p.rho_o * dj)), bc_fl = (R)(-gravity * dt / (p.rho_o * fl));
     const R djR = (R)dj, flR = (R)fl, fl2 = (R)(fl * fl);
     const R gdt0 = (R)(gravity * dt);
     const R wsn = (R)(dt * f.wind_stress_normal[j - 1]), wst = (R)(dt * f.wind_stress_tangnt[j - 1]);
@@ -810,10 +903,14 @@ __global__ void __launch_bounds__(256) k_momentum(Geom g, StateT<R> s, Forcing f
     int tq1 = 0, tq2 = 0;
     if (a2 != 0) {
         double ddx = g.x_cell[a1 - 1] - g.x_face[j - 1], ddy = g.y_cell[a1 - 1] - g.y_face[j - 1];
-        rl1 = (R)sqrt(ddx * ddx + ddy * ddy);
-        ddx = g.x_cell[a2 - 1] - g.x_face[j - 1];
-        ddy = g.y_cell[a2 - 1] - g.y_face[j - 1];
-        rl2 = (R)sqrt(ddx * ddx + ddy * ddy);
+        double ddx2 = g.x_cell[a2 - 1] - g.x_face[j - 1], ddy2 = g.y_cell[a2 - 1] - g.y_face[j - 1];
+        if constexpr (sizeof(R) == sizeof(float)) {
+            rl1 = sqrtf((float)ddx * (float)ddx + (float)ddy * (float)ddy);
+            rl2 = sqrtf((float)ddx2 * (float)ddx2 + (float)ddy2 * (float)ddy2);
+        } else {
+            rl1 = (R)sqrt(ddx * ddx + ddy * ddy);
+            rl2 = (R)sqrt(ddx2 * ddx2 + ddy2 * ddy2);
+        }
         tq1 = g.tri_or_quad[a1 - 1];
         tq2 = g.tri_or_quad[a2 - 1];
         inv_tq1 = tq1 == 4 ? R(0.25) : R(0);   // x/4 == x*0.25 exactly; triangles divide

@@ -721,6 +721,43 @@ template <typename R> __global__ void k_face_level(Geom g, StateT<R> s, WorkT<R>
     w.vflf[o] = vk / fl;
 }
 
+// FP32 path: one thread per (face, level)
+__global__ void k_face_level_flat(Geom g, StateT<float> s, WorkT<float> w) {
+    unsigned tt = flat_tid();
+    const int L = g.L;
+    if (tt >= (unsigned)g.NF * (L + 1)) return;
+    int j, k;
+    split_index(tt, L + 1, j, k);   // k = level 0..L
+    j += 1;
+    const int t = s.top_face[j - 1], b = g.bottom_face[j - 1];
+    if (t == 0 || k < b - 1 || k > t) return;
+    const float ct = (float)g.cos_theta[j - 1], sn = (float)g.sin_theta[j - 1], fl = (float)g.face_length[j - 1];
+    // the face velocity of layer m rotated to x/y
+    auto rot = [&](int m, float &u, float &v) {
+        float un = s.un_face_new[ix(m, j, L)], vn = s.vn_face_new[ix(m, j, L)];
+        u = un * ct - vn * sn;
+        v = un * sn + vn * ct;
+    };
+    float ul, vl;
+    if (k == b - 1) {
+        rot(b, ul, vl);
+    } else if (k == t) {
+        rot(t, ul, vl);
+    } else {
+        float uk, vk, u1, v1;
+        rot(k, uk, vk);
+        rot(k + 1, u1, v1);
+        float fac = s.dz_face[ix(k, j, L)] * 0.5f / s.dzhalf_face[ix0(k, j, L)];
+        ul = uk + fac * (u1 - uk);
+        vl = vk + fac * (v1 - vk);
+    }
+    const long o = ix0(k, j, L);
+    s.u_face_level[o] = ul;
+    s.v_face_level[o] = vl;
+    w.uflf[o] = ul / fl;
+    w.vflf[o] = vl / fl;
+}
+
 // :103 the weight sums factor_weight/face_length over the node's faces whatever their wetness:
 // a static per-node value, accumulated once in the reference's order
 __global__ void k_node_weight(Geom g, double *node_weight) {
@@ -796,7 +833,10 @@ template <typename R> __global__ void k_node_uvw(Geom g, StateT<R> s, WorkT<R> w
 }
 
 template <typename R> cudaError_t launch_node_velocity(const LaunchT<R> &x) {
-    k_face_level<<<blocks_for(x.g.NF, 128), 128, 0, x.stream>>>(x.g, x.s, x.w);
+    if constexpr (sizeof(R) == sizeof(float))
+        k_face_level_flat<<<blocks_for((long)x.g.NF * (x.g.L + 1), 256), 256, 0, x.stream>>>(x.g, x.s, x.w);
+    else
+        k_face_level<<<blocks_for(x.g.NF, 128), 128, 0, x.stream>>>(x.g, x.s, x.w);
     long n = (long)x.g.NN * (x.g.L + 1);
     k_node_uvw<<<blocks_for(n, 256), 256, 0, x.stream>>>(x.g, x.s, x.w);
     return cudaGetLastError();

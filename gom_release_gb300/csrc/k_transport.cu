@@ -38,7 +38,6 @@ __device__ __forceinline__ float pos_part(float q) { return is_pos(q) ? q : 0.0f
 __device__ __forceinline__ float neg_part(float q) { return is_neg(q) ? -q : 0.0f; }
 __device__ __forceinline__ bool same_bits(float a, float b) { return __float_as_int(a) == __float_as_int(b); }
 template <typename R> __device__ __forceinline__ R flip(R q, int sgn) { return sgn > 0 ? q : -q; }
-constexpr unsigned FULL_MASK = 0xffffffffu;
 
 // R: storage and arithmetic type of the tracers and coefficients
 template <typename R> struct TArgs {
@@ -62,6 +61,19 @@ template <typename R> struct TArgs {
 
 template <typename R> __device__ __forceinline__ R divnt(R x, const TArgs<R> &a) {
     return a.pow2 ? x * a.inv_nt : x / (R)a.Nt;
+}
+
+// Margin of the exact quotient filters below: far larger than one rounding of R, far smaller
+// than any value the limiter distinguishes.
+template <typename R> __device__ __forceinline__ R filter_margin();
+template <> __device__ __forceinline__ double filter_margin<double>() { return 1e-9; }
+template <> __device__ __forceinline__ float filter_margin<float>() { return 1e-5f; }
+
+// fmin(1, 2 D / |Q|) for Q != 0, the quotient formed only when it can be below 1
+template <typename R> __device__ __forceinline__ R diffusive_share(R D, R Q) {
+    const R aq = fabs(Q);
+    if (R(2) * D > aq * (R(1) + filter_margin<R>())) return R(1);
+    return fmin(R(1), R(2) * D / aq);
 }
 
 // :88-173 load tracers into con (0:L+1) with the heat_option 2 surface term
@@ -138,7 +150,7 @@ template <typename R> __device__ __forceinline__ void face_coef_at(const TArgs<R
     R Q = fl * dz_old * (a.om_theta * a.s.un_face[t] + a.theta * a.s.un_face_new[t]);
     R D = fl * dz_old * a.s.kh[t] / (R)a.g.delta_j[j - 1];
     R d = fmax(R(0), D - R(0.5) * fabs(Q));
-    R phi = Q == R(0) ? R(1) : fmin(R(1), R(2) * D / fabs(Q));
+    R phi = Q == R(0) ? R(1) : diffusive_share(D, Q);
     a.w.qj[t] = Q;
     a.w.dj[t] = d;
     a.w.phij[t] = phi;
@@ -179,7 +191,7 @@ template <typename R> __device__ __forceinline__ void cell_coef_at(const TArgs<R
     R D = ar * a.s.kv[t] / dz_old;
     a.w.qi[t] = Q;
     a.w.di[t] = fmax(R(0), D - R(0.5) * fabs(Q));
-    a.w.phii[t] = Q == R(0) ? R(1) : fmin(R(1), R(2) * D / fabs(Q));
+    a.w.phii[t] = Q == R(0) ? R(1) : diffusive_share(D, Q);
 }
 
 template <typename R> __global__ void k_tr_cell_coef(TArgs<R> a) {
@@ -229,6 +241,25 @@ template <typename R> __device__ __forceinline__ R phi_limit(int code, R small_p
     case 3: return fmax(fmax(small_phi, fmin(R(1), R(2) * r)), fmin(R(2), r)) - small_phi;
     default: return R(0);
     }
+}
+
+// phi_limit(code, small_phi, r) with r = num / den (r = 1 when den = 0, as the reference sets
+// it): where the ratio lies clearly below 0, below small_phi, or above the limiter's flat top
+// (1 for codes 1 and 2... 2 for code 3), the result is known without the division and equals
+// the reference's bit for bit; the quotient is formed only in between.
+template <typename R> __device__ __forceinline__ R limited_ratio(int code, R small_phi, R num, R den) {
+    if (den == R(0)) return phi_limit(code, small_phi, R(1));
+    if (code >= 1 && code <= 3 && num != R(0)) {
+        const R m = filter_margin<R>();
+        if ((num < R(0)) != (den < R(0))) return R(0);   // r < 0: every code gives small_phi - small_phi
+        const R an = fabs(num), ad = fabs(den);
+        if (code == 1 && an > ad * (R(1) + m)) return fmax(small_phi, R(1)) - small_phi;
+        if (code == 3 && an > R(2) * ad * (R(1) + m)) return fmax(fmax(small_phi, R(1)), R(2)) - small_phi;
+        if ((code == 1 || code == 3) && small_phi > R(0) && an < small_phi * ad * (R(1) - m) &&
+            (code == 1 || an < R(0.5) * small_phi * ad * (R(1) - m)))
+            return R(0);
+    }
+    return phi_limit(code, small_phi, num / den);
 }
 
 // :624-871 per cell column: upwind-weighted differences of every layer (sum1_all, sum2_all) for
@@ -299,8 +330,7 @@ template <typename R> __device__ void limiter_column(const TArgs<R> &a, int i) {
             R rt1 = last1[tr] + fabs(qm) * (ck - a.con[ic(k - 1, i, tr, L, NC)]);
             R rt2 = last2[tr] + fabs(qm);
             R rtemp = (a.con[ic(k + 1, i, tr, L, NC)] - ck) * rt2;
-            R r = rtemp == R(0.0) ? R(1.0) : rt1 / rtemp;
-            psi[ix0(k, i, L)] = phi_limit(a.p.h_flux_limiter, a.w.phii[ix0(k, i, L)], r);
+            psi[ix0(k, i, L)] = limited_ratio(a.p.h_flux_limiter, a.w.phii[ix0(k, i, L)], rt1, rtemp);
         }
     }
 }
@@ -311,19 +341,105 @@ template <typename R> __global__ void k_tr_limiter_cells(TArgs<R> a) {
     limiter_column(a, a.g.cell_order[tid]);
 }
 
+// ---------------------------------------------------------------------------- wet cell-layer list
+// The mixed path walks the wet (cell, layer) pairs of the step from a compact list rebuilt after
+// the layer update: every lane of every warp then works on a wet layer.  Entry = (cell << 6) |
+// (layer - 1), cells in natural order, layers ascending.  Count per cell, scan per block of 1024
+// cells, scan of the block sums in one block, scatter.
+constexpr int CL_BLOCK = 1024;
+
+__global__ void __launch_bounds__(CL_BLOCK) k_cl_scan_blocks(Geom g, const int *top, int *off, int *bsum) {
+    __shared__ int warp_tot[CL_BLOCK / 32];
+    const int i = blockIdx.x * CL_BLOCK + threadIdx.x;   // 0-based cell
+    int n = 0;
+    if (i < g.NC) {
+        int t = top[i];
+        n = t > 0 ? t - g.bottom_cell[i] + 1 : 0;
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int v = n;
+    for (int o = 1; o < 32; o <<= 1) {
+        int u = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += u;
+    }
+    if (lane == 31) warp_tot[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        int x = lane < CL_BLOCK / 32 ? warp_tot[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            int u = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += u;
+        }
+        if (lane < CL_BLOCK / 32) warp_tot[lane] = x;   // inclusive warp totals
+    }
+    __syncthreads();
+    const int before = (w > 0 ? warp_tot[w - 1] : 0) + v - n;   // exclusive within the block
+    if (i < g.NC) off[i] = before;
+    if (threadIdx.x == CL_BLOCK - 1) bsum[blockIdx.x] = warp_tot[CL_BLOCK / 32 - 1];
+}
+
+__global__ void __launch_bounds__(CL_BLOCK) k_cl_scan_sums(int nblocks, int *bsum, int *count) {
+    __shared__ int carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < nblocks; base += CL_BLOCK) {
+        const int i = base + threadIdx.x;
+        int n = i < nblocks ? bsum[i] : 0;
+        // block-wide exclusive scan of this chunk
+        __shared__ int warp_tot[CL_BLOCK / 32];
+        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+        int v = n;
+        for (int o = 1; o < 32; o <<= 1) {
+            int u = __shfl_up_sync(0xffffffffu, v, o);
+            if (lane >= o) v += u;
+        }
+        if (lane == 31) warp_tot[w] = v;
+        __syncthreads();
+        if (w == 0) {
+            int x = lane < CL_BLOCK / 32 ? warp_tot[lane] : 0;
+            for (int o = 1; o < 32; o <<= 1) {
+                int u = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += u;
+            }
+            if (lane < CL_BLOCK / 32) warp_tot[lane] = x;
+        }
+        __syncthreads();
+        const int excl = carry + (w > 0 ? warp_tot[w - 1] : 0) + v - n;
+        if (i < nblocks) bsum[i] = excl;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += warp_tot[CL_BLOCK / 32 - 1];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *count = carry;
+}
+
+__global__ void k_cl_scatter(Geom g, const int *top, const int *off, const int *bsum, int *list) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.NC) return;
+    const int t = top[i];
+    if (t <= 0) return;
+    const int b = g.bottom_cell[i];
+    int o = bsum[i / CL_BLOCK] + off[i];
+    for (int k = b; k <= t; ++k) list[o++] = ((i + 1) << 6) | (k - 1);
+}
+
+cudaError_t build_cell_layer_list(const Geom &g, const int *top, int *off, int *bsum, int *list, int *count,
+                                  cudaStream_t stream) {
+    const int nb = blocks_for(g.NC, CL_BLOCK);
+    k_cl_scan_blocks<<<nb, CL_BLOCK, 0, stream>>>(g, top, off, bsum);
+    k_cl_scan_sums<<<1, CL_BLOCK, 0, stream>>>(nb, bsum, count);
+    k_cl_scatter<<<blocks_for(g.NC, 256), 256, 0, stream>>>(g, top, off, bsum, list);
+    return cudaGetLastError();
+}
+
 // FP32 path, :624-805 with one thread per (cell, layer): the upwind-weighted differences of the
 // layer, and the top layer's horizontal sums kept for the vertical ratios
-__global__ void __launch_bounds__(256) k_tr_sums_cl(TArgs<float> a) {
+__device__ __forceinline__ void tr_sums_at(const TArgs<float> &a, int i, int k) {
     const Geom &g = a.g;
-    unsigned t = flat_tid();
     const int L = g.L, NC = g.NC;
-    if (t >= (unsigned)NC * L) return;
-    int i, k;
-    split_index(t, L, i, k);
-    i += 1;
-    k += 1;
     const int tl = a.s.top_cell[i - 1], b = g.bottom_cell[i - 1];
-    if (tl == 0 || k < b || k > tl) return;
+    (void)L;
+    (void)NC;
     const int nvl = tl - b + 1;
     const int tq = g.tri_or_quad[i - 1];
     float ck[2] = {0.0f, 0.0f}, s1a[2] = {0.0f, 0.0f}, s2a[2] = {0.0f, 0.0f}, s1[2] = {0.0f, 0.0f},
@@ -366,7 +482,46 @@ __global__ void __launch_bounds__(256) k_tr_sums_cl(TArgs<float> a) {
     }
 }
 
+__global__ void __launch_bounds__(256) k_tr_sums_cl(TArgs<float> a) {
+    const Geom &g = a.g;
+    unsigned t = flat_tid();
+    const int L = g.L, NC = g.NC;
+    if (t >= (unsigned)NC * L) return;
+    int i, k;
+    split_index(t, L, i, k);
+    i += 1;
+    k += 1;
+    const int tl = a.s.top_cell[i - 1], b = g.bottom_cell[i - 1];
+    if (tl == 0 || k < b || k > tl) return;
+    tr_sums_at(a, i, k);
+}
+
+__global__ void __launch_bounds__(256) k_tr_sums_list(TArgs<float> a) {
+    const int n = *a.w.cl_count;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const int code = a.w.cl_list[t];
+        const int i = code >> 6, k = (code & 63) + 1;
+        tr_sums_at(a, i, k);
+    }
+}
+
 // FP32 path, :806-871 with one thread per (cell, interface)
+__device__ __forceinline__ void tr_vpsi_at(const TArgs<float> &a, int i, int k) {
+    const Geom &g = a.g;
+    const int L = g.L, NC = g.NC;
+    const int b = g.bottom_cell[i - 1];
+    for (int tr = 0; tr < a.ntr; ++tr) {
+        const float last1 = a.w.tr_last[((long)tr * NC + i - 1) * 2], last2 = a.w.tr_last[((long)tr * NC + i - 1) * 2 + 1];
+        float *psi = a.w.psii + (long)tr * NC * (L + 1);
+        float ck = a.con[ic(k, i, tr, L, NC)];
+        float qm = k > b ? a.w.qi[ix0(k - 1, i, L)] : 0.0f;
+        float rt1 = last1 + fabsf(qm) * (ck - a.con[ic(k - 1, i, tr, L, NC)]);
+        float rt2 = last2 + fabsf(qm);
+        float rtemp = (a.con[ic(k + 1, i, tr, L, NC)] - ck) * rt2;
+        psi[ix0(k, i, L)] = limited_ratio(a.p.h_flux_limiter, a.w.phii[ix0(k, i, L)], rt1, rtemp);
+    }
+}
+
 __global__ void __launch_bounds__(256) k_tr_vpsi_cl(TArgs<float> a) {
     const Geom &g = a.g;
     unsigned t = flat_tid();
@@ -378,16 +533,29 @@ __global__ void __launch_bounds__(256) k_tr_vpsi_cl(TArgs<float> a) {
     k += 1;
     const int tl = a.s.top_cell[i - 1], b = g.bottom_cell[i - 1];
     if (tl == 0 || k < b || k > tl - 1) return;
-    for (int tr = 0; tr < a.ntr; ++tr) {
-        const float last1 = a.w.tr_last[((long)tr * NC + i - 1) * 2], last2 = a.w.tr_last[((long)tr * NC + i - 1) * 2 + 1];
-        float *psi = a.w.psii + (long)tr * NC * (L + 1);
-        float ck = a.con[ic(k, i, tr, L, NC)];
-        float qm = k > b ? a.w.qi[ix0(k - 1, i, L)] : 0.0f;
-        float rt1 = last1 + fabsf(qm) * (ck - a.con[ic(k - 1, i, tr, L, NC)]);
-        float rt2 = last2 + fabsf(qm);
-        float rtemp = (a.con[ic(k + 1, i, tr, L, NC)] - ck) * rt2;
-        float r = rtemp == 0.0f ? 1.0f : rt1 / rtemp;
-        psi[ix0(k, i, L)] = phi_limit(a.p.h_flux_limiter, a.w.phii[ix0(k, i, L)], r);
+    tr_vpsi_at(a, i, k);
+}
+
+__global__ void __launch_bounds__(256) k_tr_vpsi_list(TArgs<float> a) {
+    const int n = *a.w.cl_count;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const int code = a.w.cl_list[t];
+        const int i = code >> 6, k = (code & 63) + 1;
+        if (k >= a.s.top_cell[i - 1]) continue;   // interfaces b .. top - 1
+        tr_vpsi_at(a, i, k);
+    }
+}
+
+// FP32 path: vertical coefficients of the wet interfaces from the wet cell-layer list (the FP32
+// kernels never read the entries outside a column's wet interfaces, so they are not cleared)
+__global__ void __launch_bounds__(256) k_tr_cell_coef_list(TArgs<float> a) {
+    const int n = *a.w.cl_count;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const int code = a.w.cl_list[t];
+        const int i = code >> 6, k = (code & 63) + 1;
+        if (k >= a.s.top_cell[i - 1]) continue;   // interfaces b .. top - 1
+        const long o = ix0(k, i, a.g.L);
+        if (!a.changed_only || !same_bits(a.s.dzhalf_cell[o], a.s.dzhalf_cell_new[o])) cell_coef_at(a, i, o);
     }
 }
 
@@ -406,15 +574,17 @@ template <typename R> __device__ __forceinline__ void limiter_face_layer(const T
         else if (t1 != 0 && k >= b1 && k <= t1 && !is_neg(Q)) writer = c1;        // Q >= 0
     }
     for (int tr = 0; tr < a.ntr; ++tr) {
-        R r = R(1.0);
+        R v;
         if (writer != 0) {
             int i = writer;
             int other = (writer == c1) ? c2 : c1;
             R cik = other > 0 ? a.con[ic(k, other, tr, L, NC)] : oqb_value(a, i, k, tr);
             R rtemp = a.w.sa2[((long)tr * NC + i - 1) * L + k - 1] * (cik - a.con[ic(k, i, tr, L, NC)]);
-            r = rtemp == R(0.0) ? R(1.0) : a.w.sa1[((long)tr * NC + i - 1) * L + k - 1] / rtemp;
+            v = limited_ratio(a.p.h_flux_limiter, a.w.phij[t], a.w.sa1[((long)tr * NC + i - 1) * L + k - 1], rtemp);
+        } else {
+            v = phi_limit(a.p.h_flux_limiter, a.w.phij[t], R(1.0));
         }
-        a.w.psij[(long)tr * g.NF * L + t] = phi_limit(a.p.h_flux_limiter, a.w.phij[t], r);
+        a.w.psij[(long)tr * g.NF * L + t] = v;
     }
 }
 
@@ -642,17 +812,12 @@ __device__ __forceinline__ float clamp_tracer(float sv, float prev) {
 
 // :921-1250 for one wet cell-layer: right-hand sides and the row of the implicit system
 // (a couples the layer below, c the layer above)
-__global__ void __launch_bounds__(256) k_tr_rows_cl(TArgs<float> a) {
+__device__ __forceinline__ void tr_rows_at(const TArgs<float> &a, int i, int k) {
     const Geom &g = a.g;
-    unsigned t = flat_tid();
     const int L = g.L, NC = g.NC;
-    if (t >= (unsigned)NC * L) return;
-    int i, k;
-    split_index(t, L, i, k);
-    i += 1;
-    k += 1;
     const int tl = a.s.top_cell[i - 1], b = g.bottom_cell[i - 1];
-    if (tl == 0 || k < b || k > tl) return;
+    (void)L;
+    (void)NC;
     const float dt2 = a.dt2;
     const int sub = a.sub;
     const bool lim = a.p.h_flux_limiter > 0 || a.p.v_flux_limiter > 0;
@@ -718,6 +883,29 @@ __global__ void __launch_bounds__(256) k_tr_rows_cl(TArgs<float> a) {
     a.w.tr_a[o] = am;
     a.w.tr_b[o] = ar * dz_new - am - cm;
     a.w.tr_c[o] = cm;
+}
+
+__global__ void __launch_bounds__(256) k_tr_rows_cl(TArgs<float> a) {
+    const Geom &g = a.g;
+    unsigned t = flat_tid();
+    const int L = g.L, NC = g.NC;
+    if (t >= (unsigned)NC * L) return;
+    int i, k;
+    split_index(t, L, i, k);
+    i += 1;
+    k += 1;
+    const int tl = a.s.top_cell[i - 1], b = g.bottom_cell[i - 1];
+    if (tl == 0 || k < b || k > tl) return;
+    tr_rows_at(a, i, k);
+}
+
+__global__ void __launch_bounds__(256) k_tr_rows_list(TArgs<float> a) {
+    const int n = *a.w.cl_count;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const int code = a.w.cl_list[t];
+        const int i = code >> 6, k = (code & 63) + 1;
+        tr_rows_at(a, i, k);
+    }
 }
 
 // one thread per column: tridiagonal solve of the rows (top layer first, as
@@ -902,6 +1090,12 @@ template <typename R> cudaError_t launch_transport(const LaunchT<R> &x) {
     a.con = x.w.con;
     a.con_new = x.w.con2;
     k_tr_load<<<blocks_for((long)g.NC * (L + 2), 256), 256, 0, x.stream>>>(a);
+    if constexpr (sizeof(R) == sizeof(float)) {
+        cudaError_t e = build_cell_layer_list(g, x.s.top_cell, x.w.cl_off, x.w.cl_bsum, x.w.cl_list, x.w.cl_count,
+                                              x.stream);
+        if (e != cudaSuccess) return e;
+    }
+    const int list_grid = x.num_sms * 8;   // grid-stride over the wet cell-layers
     bool lim = p.h_flux_limiter > 0 || p.v_flux_limiter > 0;
     const int bs_solve = x.tune[TUNE_TR_SOLVE] == 1 ? 64 : x.tune[TUNE_TR_SOLVE] == 2 ? 256 : 128;
     const int bs_lim = x.tune[TUNE_TR_LIMITER] == 1 ? 64 : x.tune[TUNE_TR_LIMITER] == 2 ? 256 : 128;
@@ -916,11 +1110,14 @@ template <typename R> cudaError_t launch_transport(const LaunchT<R> &x) {
             k_tr_face_coef_flat<<<blocks_for((long)g.NF * L, 256), 256, 0, x.stream>>>(a);
         else
             k_tr_face_coef<<<blocks_for(g.NF, 128), 128, 0, x.stream>>>(a);
-        k_tr_cell_coef<<<blocks_for(g.NC, 128), 128, 0, x.stream>>>(a);
+        if constexpr (sizeof(R) == sizeof(float))
+            k_tr_cell_coef_list<<<list_grid, 256, 0, x.stream>>>(a);
+        else
+            k_tr_cell_coef<<<blocks_for(g.NC, 128), 128, 0, x.stream>>>(a);
         if (lim) {
             if constexpr (sizeof(R) == sizeof(float)) {
-                k_tr_sums_cl<<<blocks_for((long)g.NC * L, bs_lim), bs_lim, 0, x.stream>>>(a);
-                k_tr_vpsi_cl<<<blocks_for((long)g.NC * L, bs_lim), bs_lim, 0, x.stream>>>(a);
+                k_tr_sums_list<<<list_grid, bs_lim, 0, x.stream>>>(a);
+                k_tr_vpsi_list<<<list_grid, bs_lim, 0, x.stream>>>(a);
             } else {
                 k_tr_limiter_cells<<<blocks_for(g.NC, bs_lim), bs_lim, 0, x.stream>>>(a);
             }
@@ -930,7 +1127,7 @@ template <typename R> cudaError_t launch_transport(const LaunchT<R> &x) {
                 k_tr_limiter_faces<<<blocks_for(g.NF, 128), 128, 0, x.stream>>>(a);
         }
         if constexpr (sizeof(R) == sizeof(float)) {
-            k_tr_rows_cl<<<blocks_for((long)g.NC * L, bs_solve), bs_solve, 0, x.stream>>>(a);
+            k_tr_rows_list<<<list_grid, bs_solve, 0, x.stream>>>(a);
             k_tr_thomas_col<<<blocks_for(g.NC, 128), 128, 0, x.stream>>>(a);
         } else {
             k_tr_solve<<<blocks_for(g.NC, bs_solve), bs_solve, 0, x.stream>>>(a);
