@@ -164,6 +164,8 @@ def _bind(lib: C.CDLL) -> C.CDLL:
     lib.gom_set_storms.argtypes = [vp, C.c_int32, C.POINTER(GomStorm), C.c_double]
     lib.gom_cold_start.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_double]
     lib.gom_autotune.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32)]
+    lib.gom_tuning_variants.argtypes = [C.POINTER(C.c_int32)]
+    lib.gom_set_tuning.argtypes = [vp, C.POINTER(C.c_int32)]
     lib.gom_copy_run.argtypes = [vp, C.c_int32, vp, C.c_int32]
     lib.gom_profile_kernel.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(C.c_double)]
     lib.gom_device_bytes.argtypes = [vp]
@@ -345,6 +347,17 @@ class GomCore:
         out = (C.c_int32 * 4)()
         self._check(self.lib.gom_autotune(self.ctx, reps, out), "autotune")
         return list(out)
+
+    def tuning_variants(self) -> list[int]:
+        """Number of compiled variants of each tunable launch."""
+        out = (C.c_int32 * 4)()
+        self._check(self.lib.gom_tuning_variants(out), "tuning_variants")
+        return list(out)
+
+    def set_tuning(self, choice) -> None:
+        """Select the variant of each tunable launch (-1 keeps the current one)."""
+        arr = (C.c_int32 * 4)(*choice)
+        self._check(self.lib.gom_set_tuning(self.ctx, arr), "set_tuning")
 
     KERNEL_ELM_WALK, KERNEL_MOMENTUM, KERNEL_TRANSPORT_SOLVE = 1, 2, 3
 

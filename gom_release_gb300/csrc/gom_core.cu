@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "gom_launch.h"
+#include "gom_scan.cuh"
 
 using namespace gom;
 
@@ -125,7 +126,7 @@ template <typename R> cudaError_t alloc_layered_work(gom_ctx *c, WorkT<R> &W) {
         if (e == cudaSuccess) e = dalloc(c, &W.cl_list, L * NC);
         if (e == cudaSuccess) e = dalloc(c, &W.cl_off, NC);
         if (e == cudaSuccess) e = dalloc(c, &W.cl_bsum, NC / 1024 + 2);
-        if (e == cudaSuccess) e = dalloc(c, &W.cl_count, 1);
+        if (e == cudaSuccess) e = dalloc(c, &W.cl_count, 2);
     }
     return e;
 }
@@ -372,7 +373,8 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
     *out = nullptr;
     const gom_dims &d = *dims;
     if (d.n_cells <= 0 || d.n_faces <= 0 || d.n_nodes <= 0 || d.n_layers <= 0 || d.n_layers > GOM_MAXL ||
-        d.max_nb <= 0 || d.max_nb > GOM_MAXNB || d.n_ob < 0 || d.n_qb < 0)
+        d.max_nb <= 0 || d.max_nb > GOM_MAXNB || d.n_ob < 0 || d.n_qb < 0 || d.n_cells >= LIST_MAX_ENTITIES ||
+        d.n_faces >= LIST_MAX_ENTITIES)
         return GOM_E_ARG;
     if (params->transport_flag && params->is_salt == 0 && params->is_temp == 1) return GOM_E_ARG;
     if (params->precision != GOM_PRECISION_FP64 && params->precision != GOM_PRECISION_MIXED) return GOM_E_ARG;
@@ -537,6 +539,12 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
     if (e == cudaSuccess) e = dalloc(c, &W.run_iters, (size_t)G.NR);
     if (e == cudaSuccess) e = c->mixed ? alloc_layered_work(c, c->xf.w) : alloc_layered_work(c, W);
     if (e == cudaSuccess) e = dalloc(c, &W.idev, L * NF);
+    if (params->advection_flag != 0) {
+        if (e == cudaSuccess) e = dalloc(c, &W.fl_list, L * NF);
+        if (e == cudaSuccess) e = dalloc(c, &W.fl_off, NF);
+        if (e == cudaSuccess) e = dalloc(c, &W.fl_bsum, NF / LIST_BLOCK + 2);
+        if (e == cudaSuccess) e = dalloc(c, &W.fl_count, 2);
+    }
     if (e == cudaSuccess) e = dalloc(c, &W.node_weight, NN);
     if (e == cudaSuccess) e = dalloc(c, &W.cons, 2 + 2 * (size_t)((NC + 255) / 256));
     if (e == cudaSuccess) e = dalloc(c, &c->x.status, 1);
@@ -641,6 +649,10 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
         X.w.run_block_start = W.run_block_start;
         X.w.run_iters = W.run_iters;
         X.w.idev = W.idev;
+        X.w.fl_list = W.fl_list;
+        X.w.fl_off = W.fl_off;
+        X.w.fl_bsum = W.fl_bsum;
+        X.w.fl_count = W.fl_count;
         X.w.node_weight = W.node_weight;
         X.w.cons = W.cons;
         // FP32 copy of the free-surface system for the FP32 inner PCG iterations
@@ -932,6 +944,25 @@ int gom_autotune(gom_ctx *c, int32_t reps, int32_t *choice) {
     if (rc != GOM_OK) return rc;
     drop_graphs(c);   // captured again with the chosen variants
     return finish(c, nullptr, false);
+}
+
+int gom_tuning_variants(int32_t counts[GOM_TUNE_SITES]) {
+    if (!counts) return GOM_E_ARG;
+    for (int k = 0; k < GOM_TUNE_SITES; ++k) counts[k] = TUNE_VARIANTS[k];
+    return GOM_OK;
+}
+
+int gom_set_tuning(gom_ctx *c, const int32_t choice[GOM_TUNE_SITES]) {
+    if (!c || !choice) return GOM_E_ARG;
+    for (int k = 0; k < GOM_TUNE_SITES; ++k)
+        if (choice[k] < -1 || choice[k] >= TUNE_VARIANTS[k]) return GOM_E_ARG;
+    for (int k = 0; k < GOM_TUNE_SITES; ++k)
+        if (choice[k] >= 0) {
+            c->x.tune[k] = choice[k];
+            c->xf.tune[k] = choice[k];
+        }
+    drop_graphs(c);
+    return GOM_OK;
 }
 
 int gom_copy_run(gom_ctx *dst, int32_t dst_run, gom_ctx *src, int32_t src_run) {

@@ -29,6 +29,9 @@ template <typename R> struct WorkT {
     R *obk = nullptr, *qbk = nullptr;                           // (L, NOB, 2), (L, NQB, 2)
     // ELM: INT(dev/0.1) per (layer, face) edge
     int *idev = nullptr;
+    // ELM: compact list of the face-layers the walk visits (gom_scan.cuh); fl_count = [length,
+    // work-queue counter]; null when the mesh has too many faces for the list encoding
+    int *fl_list = nullptr, *fl_off = nullptr, *fl_bsum = nullptr, *fl_count = nullptr;
     // node velocities: face-level velocity / face length (0:L, NF), static node weights (NN)
     R *uflf = nullptr, *vflf = nullptr;
     double *node_weight = nullptr;
@@ -47,7 +50,7 @@ using Work = WorkT<double>;
 // Tunable launches: each picks one of a few compiled variants (block size, minimum resident
 // blocks per SM); gom_autotune times the variants on the context's state and keeps the fastest.
 enum TuneSite { TUNE_ELM = 0, TUNE_MOMENTUM, TUNE_TR_SOLVE, TUNE_TR_LIMITER, TUNE_COUNT };
-constexpr int TUNE_VARIANTS[TUNE_COUNT] = {5, 3, 3, 3};
+constexpr int TUNE_VARIANTS[TUNE_COUNT] = {7, 3, 3, 3};
 
 template <typename R> struct LaunchT {
     int tune[TUNE_COUNT] = {0, 0, 0, 0};

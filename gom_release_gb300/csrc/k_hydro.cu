@@ -10,6 +10,7 @@
 #include <type_traits>
 
 #include "gom_launch.h"
+#include "gom_scan.cuh"
 
 namespace gom {
 
@@ -690,6 +691,73 @@ __global__ void __launch_bounds__(BS, MINB) k_elm_faces(Geom g, StateT<R> s, Par
     for (int k = b; k <= tf; ++k) elm_face_layer(g, s, p, st, j, k, ie0, n1, n2, ct, sn);
 }
 
+// The same walk with one thread per wet face-layer of a walked face, taken from a compact list
+// (gom_scan.cuh): the layers of one face sit on neighbouring lanes, walk nearly the same path and
+// read the same element and node data, and no lane idles on a dry layer.  Warps take 4x32 entries
+// at a time from a work queue, so a warp that drew long walks does not hold up the others.
+struct FaceWalkRange {
+    const int *bottom_face, *top_face, *top_cell, *face_cell, *face_node;
+    const double *h_node;
+    double adv_onoff_depth;
+    __device__ int2 operator()(int i) const {
+        const int b = bottom_face[i], tf = top_face[i];
+        const int n1 = face_node[2 * i], n2 = face_node[2 * i + 1];
+        const bool shallow = fabs(fmax(h_node[n1 - 1], h_node[n2 - 1])) < adv_onoff_depth;
+        const int a1 = face_cell[2 * i], a2 = face_cell[2 * i + 1];
+        const bool start = top_cell[a1 - 1] != 0 || (a2 != 0 && top_cell[a2 - 1] != 0);
+        return (tf >= b && !shallow && start) ? make_int2(b, tf) : make_int2(1, 0);
+    }
+};
+
+// every face-layer's result before the walk: no foot, the face's own velocity inside the wet
+// range (what a walk that is skipped leaves), 0 outside it
+template <typename R> __global__ void k_elm_init(Geom g, StateT<R> s) {
+    unsigned t = flat_tid();
+    if (t >= (unsigned)g.NF * g.L) return;
+    int j, k;
+    split_index(t, g.L, j, k);
+    s.elm_foot[t] = 0;
+    s.elm_near_edge[t] = 0;
+    const bool wet = k + 1 >= g.bottom_face[j] && k + 1 <= s.top_face[j];
+    s.un_elm[t] = wet ? s.un_face[t] : R(0);
+    s.vn_elm[t] = wet ? s.vn_face[t] : R(0);
+}
+
+template <typename R, int BS>
+__global__ void __launch_bounds__(BS) k_elm_list(Geom g, StateT<R> s, Params p, const int *list, int *count,
+                                                 gom_status *st) {
+    const int n = count[0];
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(&count[1], 128);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n) break;
+        for (int r = 0; r < 4; ++r) {
+            const int e = base + 32 * r + lane;
+            if (e >= n) break;
+            const int code = list[e];
+            const int j = list_entity(code), k = list_layer(code);
+            const int n1 = g.face_node(1, j), n2 = g.face_node(2, j);
+            const int a1 = g.face_cell(1, j);
+            const int ie0 = s.top_cell[a1 - 1] != 0 ? a1 : g.face_cell(2, j);
+            elm_face_layer(g, s, p, st, j, k, ie0, n1, n2, g.cos_theta[j - 1], g.sin_theta[j - 1]);
+        }
+    }
+}
+
+template <typename R, int BS> cudaError_t launch_elm_list(const LaunchT<R> &x) {
+    const Geom &g = x.g;
+    k_elm_init<<<blocks_for((long)g.NF * g.L, 256), 256, 0, x.stream>>>(g, x.s);
+    FaceWalkRange r{g.bottom_face, x.s.top_face, x.s.top_cell, g.adj_cellnum_at_face, g.nodenum_at_face, g.h_node,
+                    x.p.adv_onoff_depth};
+    cudaError_t e = build_layer_list(g.NF, r, x.w.fl_off, x.w.fl_bsum, x.w.fl_list, x.w.fl_count, x.stream);
+    if (e != cudaSuccess) return e;
+    k_elm_list<R, BS><<<x.num_sms * (2048 / BS), BS, 0, x.stream>>>(g, x.s, x.p, x.w.fl_list, x.w.fl_count,
+                                                                      x.status);
+    return cudaGetLastError();
+}
+
 template <typename R> __global__ void k_copy_elm(Geom g, StateT<R> s) {
     unsigned t = flat_tid();
     if (t >= (unsigned)g.NF * g.L) return;
@@ -701,7 +769,10 @@ template <typename R> __global__ void k_copy_elm(Geom g, StateT<R> s) {
 
 template <typename R> cudaError_t launch_elm_walk(const LaunchT<R> &x) {
     // variants: threads per block and minimum resident blocks per SM (register budget)
-    switch (x.tune[TUNE_ELM]) {
+    const int v = x.w.fl_list ? x.tune[TUNE_ELM] : 0;
+    switch (v) {
+    case 5: return launch_elm_list<R, 64>(x);
+    case 6: return launch_elm_list<R, 128>(x);
     case 1: k_elm_faces<R, 32, 1><<<blocks_for(x.g.NF, 32), 32, 0, x.stream>>>(x.g, x.s, x.p, x.status); break;
     case 2: k_elm_faces<R, 128, 1><<<blocks_for(x.g.NF, 128), 128, 0, x.stream>>>(x.g, x.s, x.p, x.status); break;
     case 3: k_elm_faces<R, 64, 12><<<blocks_for(x.g.NF, 64), 64, 0, x.stream>>>(x.g, x.s, x.p, x.status); break;

@@ -9,6 +9,7 @@
 // (face layers outside a face's wet range, Q_ik_theta at the bottom and top interfaces); those
 // reads are defined here as 0, i.e. no flux, exactly like the CPU restatement.
 #include "gom_launch.h"
+#include "gom_scan.cuh"
 
 namespace gom {
 
@@ -342,94 +343,19 @@ template <typename R> __global__ void k_tr_limiter_cells(TArgs<R> a) {
 }
 
 // ---------------------------------------------------------------------------- wet cell-layer list
-// The mixed path walks the wet (cell, layer) pairs of the step from a compact list rebuilt after
-// the layer update: every lane of every warp then works on a wet layer.  Entry = (cell << 6) |
-// (layer - 1), cells in natural order, layers ascending.  Count per cell, scan per block of 1024
-// cells, scan of the block sums in one block, scatter.
-constexpr int CL_BLOCK = 1024;
-
-__global__ void __launch_bounds__(CL_BLOCK) k_cl_scan_blocks(Geom g, const int *top, int *off, int *bsum) {
-    __shared__ int warp_tot[CL_BLOCK / 32];
-    const int i = blockIdx.x * CL_BLOCK + threadIdx.x;   // 0-based cell
-    int n = 0;
-    if (i < g.NC) {
-        int t = top[i];
-        n = t > 0 ? t - g.bottom_cell[i] + 1 : 0;
+// The mixed path walks the wet (cell, layer) pairs of the step from a compact list (gom_scan.cuh)
+// rebuilt after the layer update: every lane of every warp then works on a wet layer.
+struct CellWetRange {
+    const int *top, *bottom;
+    __device__ int2 operator()(int i) const {
+        const int t = top[i];
+        return make_int2(bottom[i], t > 0 ? t : 0);
     }
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int v = n;
-    for (int o = 1; o < 32; o <<= 1) {
-        int u = __shfl_up_sync(0xffffffffu, v, o);
-        if (lane >= o) v += u;
-    }
-    if (lane == 31) warp_tot[w] = v;
-    __syncthreads();
-    if (w == 0) {
-        int x = lane < CL_BLOCK / 32 ? warp_tot[lane] : 0;
-        for (int o = 1; o < 32; o <<= 1) {
-            int u = __shfl_up_sync(0xffffffffu, x, o);
-            if (lane >= o) x += u;
-        }
-        if (lane < CL_BLOCK / 32) warp_tot[lane] = x;   // inclusive warp totals
-    }
-    __syncthreads();
-    const int before = (w > 0 ? warp_tot[w - 1] : 0) + v - n;   // exclusive within the block
-    if (i < g.NC) off[i] = before;
-    if (threadIdx.x == CL_BLOCK - 1) bsum[blockIdx.x] = warp_tot[CL_BLOCK / 32 - 1];
-}
-
-__global__ void __launch_bounds__(CL_BLOCK) k_cl_scan_sums(int nblocks, int *bsum, int *count) {
-    __shared__ int carry;
-    if (threadIdx.x == 0) carry = 0;
-    __syncthreads();
-    for (int base = 0; base < nblocks; base += CL_BLOCK) {
-        const int i = base + threadIdx.x;
-        int n = i < nblocks ? bsum[i] : 0;
-        // block-wide exclusive scan of this chunk
-        __shared__ int warp_tot[CL_BLOCK / 32];
-        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-        int v = n;
-        for (int o = 1; o < 32; o <<= 1) {
-            int u = __shfl_up_sync(0xffffffffu, v, o);
-            if (lane >= o) v += u;
-        }
-        if (lane == 31) warp_tot[w] = v;
-        __syncthreads();
-        if (w == 0) {
-            int x = lane < CL_BLOCK / 32 ? warp_tot[lane] : 0;
-            for (int o = 1; o < 32; o <<= 1) {
-                int u = __shfl_up_sync(0xffffffffu, x, o);
-                if (lane >= o) x += u;
-            }
-            if (lane < CL_BLOCK / 32) warp_tot[lane] = x;
-        }
-        __syncthreads();
-        const int excl = carry + (w > 0 ? warp_tot[w - 1] : 0) + v - n;
-        if (i < nblocks) bsum[i] = excl;
-        __syncthreads();
-        if (threadIdx.x == 0) carry += warp_tot[CL_BLOCK / 32 - 1];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) *count = carry;
-}
-
-__global__ void k_cl_scatter(Geom g, const int *top, const int *off, const int *bsum, int *list) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= g.NC) return;
-    const int t = top[i];
-    if (t <= 0) return;
-    const int b = g.bottom_cell[i];
-    int o = bsum[i / CL_BLOCK] + off[i];
-    for (int k = b; k <= t; ++k) list[o++] = ((i + 1) << 6) | (k - 1);
-}
+};
 
 cudaError_t build_cell_layer_list(const Geom &g, const int *top, int *off, int *bsum, int *list, int *count,
                                   cudaStream_t stream) {
-    const int nb = blocks_for(g.NC, CL_BLOCK);
-    k_cl_scan_blocks<<<nb, CL_BLOCK, 0, stream>>>(g, top, off, bsum);
-    k_cl_scan_sums<<<1, CL_BLOCK, 0, stream>>>(nb, bsum, count);
-    k_cl_scatter<<<blocks_for(g.NC, 256), 256, 0, stream>>>(g, top, off, bsum, list);
-    return cudaGetLastError();
+    return build_layer_list(g.NC, CellWetRange{top, g.bottom_cell}, off, bsum, list, count, stream);
 }
 
 // FP32 path, :624-805 with one thread per (cell, layer): the upwind-weighted differences of the
@@ -500,7 +426,7 @@ __global__ void __launch_bounds__(256) k_tr_sums_list(TArgs<float> a) {
     const int n = *a.w.cl_count;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         const int code = a.w.cl_list[t];
-        const int i = code >> 6, k = (code & 63) + 1;
+        const int i = list_entity(code), k = list_layer(code);
         tr_sums_at(a, i, k);
     }
 }
@@ -540,7 +466,7 @@ __global__ void __launch_bounds__(256) k_tr_vpsi_list(TArgs<float> a) {
     const int n = *a.w.cl_count;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         const int code = a.w.cl_list[t];
-        const int i = code >> 6, k = (code & 63) + 1;
+        const int i = list_entity(code), k = list_layer(code);
         if (k >= a.s.top_cell[i - 1]) continue;   // interfaces b .. top - 1
         tr_vpsi_at(a, i, k);
     }
@@ -552,7 +478,7 @@ __global__ void __launch_bounds__(256) k_tr_cell_coef_list(TArgs<float> a) {
     const int n = *a.w.cl_count;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         const int code = a.w.cl_list[t];
-        const int i = code >> 6, k = (code & 63) + 1;
+        const int i = list_entity(code), k = list_layer(code);
         if (k >= a.s.top_cell[i - 1]) continue;   // interfaces b .. top - 1
         const long o = ix0(k, i, a.g.L);
         if (!a.changed_only || !same_bits(a.s.dzhalf_cell[o], a.s.dzhalf_cell_new[o])) cell_coef_at(a, i, o);
@@ -903,7 +829,7 @@ __global__ void __launch_bounds__(256) k_tr_rows_list(TArgs<float> a) {
     const int n = *a.w.cl_count;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         const int code = a.w.cl_list[t];
-        const int i = code >> 6, k = (code & 63) + 1;
+        const int i = list_entity(code), k = list_layer(code);
         tr_rows_at(a, i, k);
     }
 }

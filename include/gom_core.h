@@ -308,7 +308,8 @@ int gom_field_info(const gom_dims *dims, int field, int64_t *count, int32_t *ele
 
 /* Create a context: validates dims/params, copies geometry to the device.
  * Replaces the allocation part of allocate_variables.f90 for the hot-path arrays.
- * The caller then uploads the initial state with gom_set_field (cold or hot start). */
+ * The caller then uploads the initial state with gom_set_field (cold or hot start).
+ * Limits: n_layers <= 64, n_cells and n_faces below 2^26 (GOM_E_ARG otherwise). */
 int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *geom,
                struct gom_ctx **out);
 void gom_destroy(struct gom_ctx *ctx);
@@ -383,14 +384,23 @@ int gom_set_storms(struct gom_ctx *ctx, int32_t n_storms, const gom_storm *storm
 int gom_cold_start(struct gom_ctx *ctx, double salt, double temp, double av_0, double kv_0);
 
 /* Autotuner (no reference counterpart): times the compiled variants of the tunable launches
- * (ELM walk: threads per block and register budget; momentum columns, transport column solve
- * and limiter: threads per block) on the context's current state, `reps` runs each, keeps the
+ * (ELM walk: one thread per face or per listed wet face-layer, threads per block, register
+ * budget; momentum columns, transport column solve and limiter: threads per block) on the
+ * context's current state, `reps` runs each, keeps the
  * fastest and re-captures the step graph.  The phases it runs only overwrite arrays that the
  * next step recomputes before reading them (ELM velocities, momentum coefficients, transport
  * outputs), so the run's results do not change.  Call between steps.  choice (may be NULL)
  * receives the variant picked per site. */
 #define GOM_TUNE_SITES 4
 int gom_autotune(struct gom_ctx *ctx, int32_t reps, int32_t *choice);
+
+/* Number of compiled variants per tunable site (no reference counterpart). */
+int gom_tuning_variants(int32_t counts[GOM_TUNE_SITES]);
+
+/* Select the variant of each tunable site, e.g. an earlier gom_autotune result reused for a mesh
+ * of the same shape (no reference counterpart); -1 keeps a site's current variant, GOM_E_ARG for
+ * a variant out of range.  Every variant computes the same results bit for bit. */
+int gom_set_tuning(struct gom_ctx *ctx, const int32_t choice[GOM_TUNE_SITES]);
 
 /* Copy every state array of one run of src into one run of dst (no reference counterpart): for
  * moving in-flight runs between packed contexts when a server repacks its ensemble.  The two runs

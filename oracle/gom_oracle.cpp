@@ -22,19 +22,47 @@
 // Parity is unpinned: the reference has no tests or golden vectors and cannot be compiled in
 // this environment (no Fortran compiler), so this file is checked against known-answer tests
 // derived from the mathematics (tests/test_oracle_kat.py) and the CUDA library against it.
+//
+// Built a second time with -fopenmp -DGOM_ORACLE_OMP (oracle/Makefile, libgomoracle_omp.so) as
+// the multithreaded CPU timing baseline: the entity loops the reference runs as OpenMP parallel
+// do (every hot subroutine) become parallel for loops, the dot products become reductions, and
+// the reference's serial parts (the CSR pack of solve_free_surface_equation.f90:235-258, the
+// boundary-cell loops) stay serial.  That build is for timing only: the order-dependent values
+// above (stale rtemp0, last-writer r_jk) and the PCG sums then depend on the thread split, as
+// they do in the reference's own OpenMP build.  Without GOM_ORACLE_OMP the pragmas vanish and
+// the loops run serially in index order.
 
 #include "../include/gom_core.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <string>
 #include <vector>
+#ifdef GOM_ORACLE_OMP
+#include <omp.h>
+#endif
+
+#define GOM_PRAGMA(x) _Pragma(#x)
+#ifdef GOM_ORACLE_OMP
+#define OMP_FOR GOM_PRAGMA(omp parallel for schedule(dynamic, 256))
+#define OMP_FOR_SUM(v) GOM_PRAGMA(omp parallel for reduction(+ : v) schedule(static))
+#define OMP_FOR_FIRSTPRIVATE(v) GOM_PRAGMA(omp parallel for firstprivate(v) schedule(static))
+#define OMP_CRITICAL GOM_PRAGMA(omp critical(gom_err))
+#else
+#define OMP_FOR
+#define OMP_FOR_SUM(v)
+#define OMP_FOR_FIRSTPRIVATE(v)
+#define OMP_CRITICAL
+#endif
 
 namespace {
 
 inline double F(float x) { return (double)x; }
+
+constexpr int GOM_ORACLE_MAXL = 64;   // largest n_layers gom_create accepts
 
 // 1-D array with 1-based index
 template <typename T> struct A1 {
@@ -155,6 +183,7 @@ int64_t field_count(const gom_dims &d, int f, int32_t *eb) {
 }
 
 void set_err(gom_ctx *c, int code, int site, int entity, int layer, double value) {
+    OMP_CRITICAL
     if (c->err.code == 0) {
         c->err.code = code;
         c->err.site = site;
@@ -569,8 +598,8 @@ int gom_field_info(const gom_dims *dims, int field, int64_t *count, int32_t *ele
 int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g, gom_ctx **out) {
     if (!dims || !params || !g || !out) return GOM_E_ARG;
     const gom_dims &d = *dims;
-    if (d.n_cells <= 0 || d.n_faces <= 0 || d.n_nodes <= 0 || d.n_layers <= 0 || d.max_nb <= 0 || d.n_ob < 0 ||
-        d.n_qb < 0)
+    if (d.n_cells <= 0 || d.n_faces <= 0 || d.n_nodes <= 0 || d.n_layers <= 0 || d.n_layers > GOM_ORACLE_MAXL ||
+        d.max_nb <= 0 || d.n_ob < 0 || d.n_qb < 0)
         return GOM_E_ARG;
     if (params->transport_flag && params->is_salt == 0 && params->is_temp == 1) return GOM_E_ARG;
     gom_ctx *c = new gom_ctx();
@@ -787,6 +816,19 @@ int gom_autotune(gom_ctx *c, int32_t, int32_t *choice) {
     return GOM_OK;
 }
 
+int gom_tuning_variants(int32_t counts[GOM_TUNE_SITES]) {
+    if (!counts) return GOM_E_ARG;
+    for (int k = 0; k < GOM_TUNE_SITES; ++k) counts[k] = 1;
+    return GOM_OK;
+}
+
+int gom_set_tuning(gom_ctx *c, const int32_t choice[GOM_TUNE_SITES]) {
+    if (!c || !choice) return GOM_E_ARG;
+    for (int k = 0; k < GOM_TUNE_SITES; ++k)
+        if (choice[k] < -1 || choice[k] > 0) return GOM_E_ARG;
+    return GOM_OK;
+}
+
 int gom_get_status(gom_ctx *c, gom_status *s, int clear) {
     if (!c || !s) return GOM_E_ARG;
     s->code = c->err.code;
@@ -902,6 +944,7 @@ int gom_step_advection(gom_ctx *c) {
     // :52-87 adaptive substep count
     if (p.elm_backtrace_flag == 1) {
         double dt = p.dt;
+        OMP_FOR
         for (int i = 1; i <= c->NN; ++i) {
             for (int k = 1; k <= L; ++k) {
                 double summ = 0.0;
@@ -933,8 +976,11 @@ int gom_step_advection(gom_ctx *c) {
             }
         }
     }
-    // :94-201 face loop
+    // :94-201 face loop; after an error the remaining faces are skipped (the serial run stops)
+    std::atomic<int> rc{GOM_OK};
+    OMP_FOR
     for (int j = 1; j <= c->NF; ++j) {
+        if (rc.load(std::memory_order_relaxed) != GOM_OK) continue;
         int n1 = c->nodenum_at_face(1, j), n2 = c->nodenum_at_face(2, j);
         double adv_turn_off_depth = std::max(c->h_node(n1), c->h_node(n2));
         int b = c->bottom_layer_at_face(j), t = top_f(j);
@@ -977,7 +1023,8 @@ int gom_step_advection(gom_ctx *c) {
                 int e = elm_backtrace(c, bt_step, bt_dt, uuint, vvint, wwint, x0, y0, z0, nnel, jlev, ne);
                 if (e) {
                     set_err(c, GOM_E_ELM, e, j, k, 0.0);
-                    return GOM_E_ELM;
+                    rc = GOM_E_ELM;
+                    break;
                 }
                 foot(k, j) = nnel;
                 near(k, j) = ne;
@@ -986,7 +1033,7 @@ int gom_step_advection(gom_ctx *c) {
             }
         }
     }
-    return GOM_OK;
+    return rc.load();
 }
 
 // solve_momentum_equation.f90:15-656
@@ -1010,19 +1057,22 @@ int gom_step_momentum(gom_ctx *c) {
     std::fill(c->fd[GOM_F_AINVDZ1].begin(), c->fd[GOM_F_AINVDZ1].end(), 0.0);
     std::fill(c->fd[GOM_F_AINVDZ2].begin(), c->fd[GOM_F_AINVDZ2].end(), 0.0);
     const int nmax = L + 1;
-    std::vector<double> G1(nmax, 0.0), G2(nmax, 0.0), a(nmax, 0.0), bd(nmax, 0.0), cu(nmax, 0.0), gam(nmax, 0.0);
-    std::vector<double> rhs(nmax * 3, 0.0), sol(nmax * 3, 0.0);
-    double temp[12] = {0};
-    double rtemp0 = 0.0, rtemp1 = 0.0, rtemp2 = 0.0, rtemp3 = 0.0, rtemp4 = 0.0;
+    // each packed run starts with rtemp0 = 0, as one call of the reference does
+    std::vector<char> run_first_face(c->NF + 2, 0);
+    for (size_t r = 0; r + 1 < c->run_face_start.size(); ++r) run_first_face[c->run_face_start[r] + 1] = 1;
+    double rtemp0 = 0.0;
     const double c069 = F(0.69f);
-    size_t next_run = 1;
+    std::atomic<int> rc{GOM_OK};
+    OMP_FOR_FIRSTPRIVATE(rtemp0)
     for (int j = 1; j <= c->NF; ++j) {
-        // each packed run starts with rtemp0 = 0, as one call of the reference does
-        while (next_run < c->run_face_start.size() && j - 1 == c->run_face_start[next_run - 1]) {
-            rtemp0 = 0.0;
-            ++next_run;
-        }
+        if (run_first_face[j]) rtemp0 = 0.0;
+        if (rc.load(std::memory_order_relaxed) != GOM_OK) continue;
         if (top_f(j) == 0) continue;
+        double G1[GOM_ORACLE_MAXL + 1] = {0}, G2[GOM_ORACLE_MAXL + 1] = {0}, a[GOM_ORACLE_MAXL + 1] = {0},
+               bd[GOM_ORACLE_MAXL + 1] = {0}, cu[GOM_ORACLE_MAXL + 1] = {0}, gam[GOM_ORACLE_MAXL + 1] = {0};
+        double rhs[(GOM_ORACLE_MAXL + 1) * 3] = {0}, sol[(GOM_ORACLE_MAXL + 1) * 3] = {0};
+        double temp[12] = {0};
+        double rtemp1 = 0.0, rtemp2 = 0.0, rtemp3 = 0.0, rtemp4 = 0.0;
         int node1 = c->nodenum_at_face(1, j), node2 = c->nodenum_at_face(2, j);
         int tj = top_f(j), bj = c->bottom_layer_at_face(j);
         int nvl = tj - bj + 1;
@@ -1173,9 +1223,10 @@ int gom_step_momentum(gom_ctx *c) {
             rhs[1 * nmax + k - 1] = G2[k - 1];
             rhs[2 * nmax + k - 1] = dz_face(kk, j);
         }
-        if (!tridiagonal_solver(nmax, nvl, 3, a.data(), bd.data(), cu.data(), rhs.data(), sol.data(), gam.data())) {
+        if (!tridiagonal_solver(nmax, nvl, 3, a, bd, cu, rhs, sol, gam)) {
             set_err(c, GOM_E_ZERO_PIVOT, 587, j, 0, 0.0);
-            return GOM_E_ZERO_PIVOT;
+            rc = GOM_E_ZERO_PIVOT;
+            continue;
         }
         for (int k = 1; k <= nvl; ++k) {
             AinvG1(k, j) = sol[0 * nmax + k - 1];
@@ -1190,7 +1241,7 @@ int gom_step_momentum(gom_ctx *c) {
         if (btype == -1)
             for (int k = 1; k <= nvl; ++k) AinvDZ1(k, j) = 0.0;
     }
-    return GOM_OK;
+    return rc.load();
 }
 
 // solve_free_surface_equation.f90:17-396 with pre_conj_grad.f90:9-230 (serial, CSR order)
@@ -1206,7 +1257,10 @@ int gom_step_free_surface(gom_ctx *c, int32_t *pcg_iters) {
                 wetdry = FI1(c, GOM_F_WETDRY_NODE);
     std::vector<double> sparsem(5 * (size_t)NC, 0.0), rhs_1(NC, 0.0);
     auto SP = [&](int l, int i) -> double & { return sparsem[(size_t)(i - 1) * 5 + l]; };
+    std::atomic<int> rc{GOM_OK};
+    OMP_FOR
     for (int i = 1; i <= NC; ++i) {
+        if (rc.load(std::memory_order_relaxed) != GOM_OK) continue;
         SP(0, i) = c->area(i);
         int tq = c->tri_or_quad(i);
         for (int l = 1; l <= tq; ++l) {
@@ -1220,12 +1274,14 @@ int gom_step_free_surface(gom_ctx *c, int32_t *pcg_iters) {
                 s = s * c->cos_theta2(j);
                 if (s < 0.0) {
                     set_err(c, GOM_E_NOT_SPD, 100, i, 0, s);
-                    return GOM_E_NOT_SPD;
+                    rc = GOM_E_NOT_SPD;
+                    break;
                 }
                 SP(0, i) = SP(0, i) + s;
                 if (ii != 0) SP(l, i) = -s;
             }
         }
+        if (rc.load(std::memory_order_relaxed) != GOM_OK) continue;
         rhs_1[i - 1] = c->area(i) * eta_cell(i);
         for (int l = 1; l <= tq; ++l) {
             int j = c->facenum_at_cell(l, i);
@@ -1255,7 +1311,8 @@ int gom_step_free_surface(gom_ctx *c, int32_t *pcg_iters) {
             }
         }
     }
-    // CSR (:233-258): diagonal first, then neighbours in local order
+    if (rc.load() != GOM_OK) return rc.load();
+    // CSR (:233-258): diagonal first, then neighbours in local order (serial, as in the reference)
     std::vector<int> ia(NC + 1), ja;
     std::vector<double> a1;
     ja.reserve(5 * (size_t)NC);
@@ -1282,6 +1339,7 @@ int gom_step_free_surface(gom_ctx *c, int32_t *pcg_iters) {
     const int nruns = (int)c->run_cell_start.size() - 1;
     for (int run = 0; run < nruns; ++run) {
         const int i0 = c->run_cell_start[run], i1 = c->run_cell_start[run + 1];
+        OMP_FOR
         for (int i = i0; i < i1; ++i) {
             double sum1 = 0.0;
             for (int k = ia[i]; k < ia[i + 1]; ++k) {
@@ -1290,8 +1348,10 @@ int gom_step_free_surface(gom_ctx *c, int32_t *pcg_iters) {
             }
             r[i] = rhs_1[i] - sum1;
         }
+        OMP_FOR
         for (int i = i0; i < i1; ++i) d[i] = Minv[i] * r[i];
         double delta_new = 0.0;
+        OMP_FOR_SUM(delta_new)
         for (int i = i0; i < i1; ++i) delta_new = delta_new + r[i] * d[i];
         double delta_0 = delta_new;
         int run_it = 0;
@@ -1299,23 +1359,29 @@ int gom_step_free_surface(gom_ctx *c, int32_t *pcg_iters) {
         // the restatement returns the initial guess instead.
         if (delta_0 != 0.0) {
             for (int cgit = 1; cgit <= p.max_iteration_pcg; ++cgit) {
+                OMP_FOR
                 for (int i = i0; i < i1; ++i) {
                     double sum1 = 0.0;
                     for (int k = ia[i]; k < ia[i + 1]; ++k) sum1 = sum1 + a1[k] * d[ja[k] - 1];
                     q[i] = sum1;
                 }
                 double dq = 0.0;
+                OMP_FOR_SUM(dq)
                 for (int i = i0; i < i1; ++i) dq = dq + d[i] * q[i];
                 double alpha = delta_new / dq;
+                OMP_FOR
                 for (int i = i0; i < i1; ++i) {
                     x[i] = x[i] + alpha * d[i];
                     r[i] = r[i] - alpha * q[i];
                 }
+                OMP_FOR
                 for (int i = i0; i < i1; ++i) s[i] = Minv[i] * r[i];
                 double delta_old = delta_new;
                 delta_new = 0.0;
+                OMP_FOR_SUM(delta_new)
                 for (int i = i0; i < i1; ++i) delta_new = delta_new + r[i] * s[i];
                 double beta = delta_new / delta_old;
+                OMP_FOR
                 for (int i = i0; i < i1; ++i) d[i] = s[i] + beta * d[i];
                 run_it = cgit;
                 if (std::sqrt(delta_new * delta_new / (delta_0 * delta_0)) < p.error_tolerance) break;
@@ -1327,6 +1393,7 @@ int gom_step_free_surface(gom_ctx *c, int32_t *pcg_iters) {
     c->pcg_total += cgit2;
     for (int i = 1; i <= NC; ++i) eta_new(i) = x[i - 1];
     // :353-396 node elevation and wet/dry nodes
+    OMP_FOR
     for (int i = 1; i <= c->NN; ++i) {
         wetdry(i) = 0;
         double sum1 = 0.0, sum0 = 0.0;
@@ -1340,6 +1407,7 @@ int gom_step_free_surface(gom_ctx *c, int32_t *pcg_iters) {
         }
         if (wetdry(i) == 0) eta_node(i) = sum1 / sum0;
     }
+    OMP_FOR
     for (int i = 1; i <= c->NN; ++i) {
         if (wetdry(i) == 1) {
             double sum0 = 0.0;
@@ -1369,6 +1437,7 @@ int gom_step_velocities(gom_ctx *c) {
     A1<double> eta_new = FD1(c, GOM_F_ETA_CELL_NEW), eta_node = FD1(c, GOM_F_ETA_NODE), Qu = FD1(c, GOM_F_QU_BOUNDARY);
     A1<int32_t> top_f = FI1(c, GOM_F_TOP_LAYER_FACE), top_el = FI1(c, GOM_F_TOP_LAYER_CELL),
                 wetdry = FI1(c, GOM_F_WETDRY_NODE);
+    OMP_FOR
     for (int j = 1; j <= c->NF; ++j) {
         int n1 = c->nodenum_at_face(1, j), n2 = c->nodenum_at_face(2, j);
         int tj = top_f(j), bj = c->bottom_layer_at_face(j);
@@ -1418,6 +1487,7 @@ int gom_step_velocities(gom_ctx *c) {
             vn_new(k, j) = vn_new(tj, j);
         }
     }
+    OMP_FOR
     for (int i = 1; i <= c->NC; ++i) {
         int t = top_el(i), b = c->bottom_layer_at_element(i);
         if (t == 0) {
@@ -1584,10 +1654,11 @@ int gom_step_node_velocity(gom_ctx *c) {
                u_node = FD(c, GOM_F_U_NODE), v_node = FD(c, GOM_F_V_NODE), w_node = FD(c, GOM_F_W_NODE),
                wn_cell = FD(c, GOM_F_WN_CELL);
     A1<int32_t> top_f = FI1(c, GOM_F_TOP_LAYER_FACE), top_el = FI1(c, GOM_F_TOP_LAYER_CELL);
-    std::vector<double> uf(L + 2, 0.0), vf(L + 2, 0.0);
+    OMP_FOR
     for (int j = 1; j <= c->NF; ++j) {
         int t = top_f(j), b = c->bottom_layer_at_face(j);
         if (t == 0) continue;
+        double uf[GOM_ORACLE_MAXL + 2] = {0}, vf[GOM_ORACLE_MAXL + 2] = {0};
         for (int k = b; k <= t; ++k) {
             uf[k] = un_new(k, j) * c->cos_theta(j) - vn_new(k, j) * c->sin_theta(j);
             vf[k] = un_new(k, j) * c->sin_theta(j) + vn_new(k, j) * c->cos_theta(j);
@@ -1601,6 +1672,7 @@ int gom_step_node_velocity(gom_ctx *c) {
             vfl(k, j) = vf[k] + dz_face(k, j) * 0.5 / dzhalf_face(k, j) * (vf[k + 1] - vf[k]);
         }
     }
+    OMP_FOR
     for (int i = 1; i <= c->NN; ++i) {
         for (int k = 0; k <= L; ++k) {
             u_node(k, i) = 0.0;
@@ -1629,6 +1701,7 @@ int gom_step_node_velocity(gom_ctx *c) {
             }
         }
     }
+    OMP_FOR
     for (int i = 1; i <= c->NN; ++i) {
         for (int k = 0; k <= L; ++k) {
             w_node(k, i) = 0.0;
@@ -1679,6 +1752,7 @@ int gom_step_transport(gom_ctx *c) {
     const double cp = 4186.0;
     // :88-173 load tracers
     for (int i3 = 1; i3 <= ntr; ++i3) {
+        OMP_FOR
         for (int i = 1; i <= NC; ++i) {
             for (int k = 1; k <= L; ++k) CC(k, i, i3) = tran_id[i3 - 1] == 1 ? salt_cell(k, i) : temp_cell(k, i);
             CC(0, i, i3) = 0.0;
@@ -1717,9 +1791,6 @@ int gom_step_transport(gom_ctx *c) {
     std::vector<double> con_at_obk((size_t)L * c->NOB * ntr), con_at_qbk((size_t)L * c->NQB * ntr);
     auto OBK = [&](int k, int i, int t) -> double & { return con_at_obk[((size_t)(t - 1) * c->NOB + i - 1) * L + k - 1]; };
     auto QBK = [&](int k, int i, int t) -> double & { return con_at_qbk[((size_t)(t - 1) * c->NQB + i - 1) * L + k - 1]; };
-    std::vector<double> oQb((size_t)L * ntr, 0.0);
-    auto OQB = [&](int k, int t) -> double & { return oQb[(size_t)(t - 1) * L + k - 1]; };
-    std::vector<double> am(L + 1), bm(L + 1), cm(L + 1), gm(L + 1), rhs((size_t)L * ntr), sol((size_t)L * ntr);
     // con_at_ob(i, i3) for subcycle s: host array (n_ob, 2, Nt), slot 1 = salt, 2 = temperature
     auto con_ob = [&](int i, int i3, int s) {
         return c->con_at_ob[((size_t)s * 2 + (tran_id[i3 - 1] - 1)) * c->NOB + (i - 1)];
@@ -1758,6 +1829,7 @@ int gom_step_transport(gom_ctx *c) {
                 for (int i3 = 1; i3 <= ntr; ++i3) QBK(k, i, i3) = con_qb(i, i3, subcycle);
         }
         // :551-581 face coefficients
+        OMP_FOR
         for (int j = 1; j <= NF; ++j) {
             int b = c->bottom_layer_at_face(j), t = top_f(j);
             for (int k = b; k <= t; ++k) {
@@ -1770,6 +1842,7 @@ int gom_step_transport(gom_ctx *c) {
             }
         }
         // :585-610 vertical coefficients
+        OMP_FOR
         for (int i = 1; i <= NC; ++i) {
             int b = c->bottom_layer_at_element(i), t = top_el(i);
             for (int k = b; k <= t - 1; ++k) {
@@ -1781,26 +1854,31 @@ int gom_step_transport(gom_ctx *c) {
                 else pI(k, i) = std::min(1.0, 2.0 * DI(k, i) / std::fabs(QI(k, i)));
             }
         }
-        auto load_oqb = [&](int i, int b, int t) {
+        // boundary concentrations of an open-boundary or river cell's layers, into a per-cell
+        // buffer oqb (L, 2); only faces without a neighbour cell read it
+        auto load_oqb = [&](double *oqb, int i, int b, int t) {
             int ith_ob = c->ob_element_flag(i), ith_Qb = c->Qb_element_flag(i);
             if (ith_ob > 0)
                 for (int k = b; k <= t; ++k)
-                    for (int i3 = 1; i3 <= ntr; ++i3) OQB(k, i3) = OBK(k, ith_ob, i3);
+                    for (int i3 = 1; i3 <= ntr; ++i3) oqb[(size_t)(i3 - 1) * L + k - 1] = OBK(k, ith_ob, i3);
             if (ith_Qb > 0)
                 for (int k = b; k <= t; ++k)
-                    for (int i3 = 1; i3 <= ntr; ++i3) OQB(k, i3) = QBK(k, ith_Qb, i3);
+                    for (int i3 = 1; i3 <= ntr; ++i3) oqb[(size_t)(i3 - 1) * L + k - 1] = QBK(k, ith_Qb, i3);
         };
         auto face_open = [&](int j) {
             return c->boundary_type_of_face(j) != -1 || c->isflowside3(j) > 0;
         };
         // :615-904 limiter
         if (p.h_flux_limiter > 0 || p.v_flux_limiter > 0) {
-            double sum1[2], sum2[2], s1a[2], s2a[2], cik[2], Q2[4];
+            OMP_FOR
             for (int i = 1; i <= NC; ++i) {
                 int t = top_el(i), b = c->bottom_layer_at_element(i);
                 if (t == 0) continue;
                 int nvl = t - b + 1;
-                load_oqb(i, b, t);
+                double sum1[2], sum2[2], s1a[2], s2a[2], cik[2], Q2[4];
+                double oqb[2 * GOM_ORACLE_MAXL] = {0};
+                auto OQB = [&](int k, int t3) { return oqb[(size_t)(t3 - 1) * L + k - 1]; };
+                load_oqb(oqb, i, b, t);
                 int tq = c->tri_or_quad(i);
                 for (int k = b; k <= t; ++k) {
                     for (int i3 = 0; i3 < 2; ++i3) sum1[i3] = sum2[i3] = s1a[i3] = s2a[i3] = 0.0;
@@ -1892,11 +1970,13 @@ int gom_step_transport(gom_ctx *c) {
                 default: return 0.0;
                 }
             };
+            OMP_FOR
             for (int i = 1; i <= NC; ++i) {
                 int b = c->bottom_layer_at_element(i), t = top_el(i);
                 for (int k = b; k <= t - 1; ++k)
                     for (int i3 = 1; i3 <= ntr; ++i3) PI_(k, i, i3) = limiter(pI(k, i), RI(k, i, i3));
             }
+            OMP_FOR
             for (int j = 1; j <= NF; ++j) {
                 int b = c->bottom_layer_at_face(j), t = top_f(j);
                 for (int k = b; k <= t; ++k)
@@ -1904,10 +1984,17 @@ int gom_step_transport(gom_ctx *c) {
             }
         }
         // :921-1346 implicit vertical solve per cell
+        std::atomic<int> rc{GOM_OK};
+        OMP_FOR
         for (int i = 1; i <= NC; ++i) {
+            if (rc.load(std::memory_order_relaxed) != GOM_OK) continue;
             int b = c->bottom_layer_at_element(i), t = top_el(i);
             if (t == 0) continue;
             int nvl = t - b + 1;
+            double am[GOM_ORACLE_MAXL + 1] = {0}, bm[GOM_ORACLE_MAXL + 1] = {0}, cm[GOM_ORACLE_MAXL + 1] = {0},
+                   gm[GOM_ORACLE_MAXL + 1] = {0}, rhs[2 * GOM_ORACLE_MAXL] = {0}, sol[2 * GOM_ORACLE_MAXL] = {0};
+            double oqb[2 * GOM_ORACLE_MAXL] = {0};
+            auto OQB = [&](int k, int t3) { return oqb[(size_t)(t3 - 1) * L + k - 1]; };
             double ar = c->area(i);
             for (int k = b + 1; k <= t - 1; ++k) {
                 int kk = t + 1 - k;
@@ -1927,7 +2014,7 @@ int gom_step_transport(gom_ctx *c) {
                 dz_new = dz_cell(b, i) + (dz_cn(b, i) - dz_cell(b, i)) * (subcycle + 1) / Nt;
                 bm[nvl - 1] = -am[nvl - 1] + ar * dz_new;
             }
-            load_oqb(i, b, t);
+            load_oqb(oqb, i, b, t);
             int tq = c->tri_or_quad(i);
             for (int k = b; k <= t; ++k) {
                 int kk = t + 1 - k;
@@ -2004,9 +2091,10 @@ int gom_step_transport(gom_ctx *c) {
                     }
                 }
             }
-            if (!tridiagonal_solver(L, nvl, ntr, am.data(), bm.data(), cm.data(), rhs.data(), sol.data(), gm.data())) {
+            if (!tridiagonal_solver(L, nvl, ntr, am, bm, cm, rhs, sol, gm)) {
                 set_err(c, GOM_E_ZERO_PIVOT, 1285, i, 0, 0.0);
-                return GOM_E_ZERO_PIVOT;
+                rc = GOM_E_ZERO_PIVOT;
+                continue;
             }
             for (int k = b; k <= t; ++k) {
                 int kk = t - k + 1;
@@ -2018,7 +2106,9 @@ int gom_step_transport(gom_ctx *c) {
                 }
             }
         }
+        if (rc.load() != GOM_OK) return rc.load();
         // :1352-1372 copy back
+        OMP_FOR
         for (int i = 1; i <= NC; ++i) {
             int b = c->bottom_layer_at_element(i), t = top_el(i);
             for (int k = b; k <= t; ++k)
@@ -2030,6 +2120,7 @@ int gom_step_transport(gom_ctx *c) {
         }
     }
     // :1403-1467 node and face averages
+    OMP_FOR
     for (int i = 1; i <= NN; ++i) {
         for (int k = top_n(i); k >= c->bottom_layer_at_node(i); --k) {
             if (top_n(i) == 0) break;
@@ -2051,6 +2142,7 @@ int gom_step_transport(gom_ctx *c) {
             }
         }
     }
+    OMP_FOR
     for (int j = 1; j <= NF; ++j) {
         int n1 = c->nodenum_at_face(1, j), n2 = c->nodenum_at_face(2, j);
         for (int k = c->bottom_layer_at_face(j); k <= top_f(j); ++k)
@@ -2064,10 +2156,13 @@ int gom_step_transport(gom_ctx *c) {
         A2<double> dc = FD(c, tid == 1 ? GOM_F_SALT_CELL_NEW : GOM_F_TEMP_CELL_NEW);
         A2<double> dn = FD(c, tid == 1 ? GOM_F_SALT_NODE : GOM_F_TEMP_NODE);
         A2<double> df = FD(c, tid == 1 ? GOM_F_SALT_FACE : GOM_F_TEMP_FACE);
+        OMP_FOR
         for (int i = 1; i <= NC; ++i)
             for (int k = 1; k <= L; ++k) dc(k, i) = CN(k, i, slot);
+        OMP_FOR
         for (int i = 1; i <= NN; ++i)
             for (int k = 1; k <= L; ++k) dn(k, i) = NDN(k, i, slot);
+        OMP_FOR
         for (int j = 1; j <= NF; ++j)
             for (int k = 1; k <= L; ++k) df(k, j) = FCN(k, j, slot);
     }
@@ -2326,6 +2421,18 @@ int gom_conservation(gom_ctx *c, double *volume, double *salt_mass) {
 
 // ---------------------------------------------------------------- test hooks (KATs only)
 // The restated building blocks, callable one at a time by the known-answer tests.
+// threads of the OpenMP timing build (n > 0 sets them); returns the count a parallel loop uses
+// (always 1 in the serial build)
+int gom_oracle_threads(int32_t n) {
+#ifdef GOM_ORACLE_OMP
+    if (n > 0) omp_set_num_threads(n);
+    return omp_get_max_threads();
+#else
+    (void)n;
+    return 1;
+#endif
+}
+
 int gom_oracle_tridiagonal(int32_t n, int32_t nc, const double *a, const double *b, const double *c,
                            const double *rhs, double *sol) {
     if (n <= 0 || nc <= 0) return GOM_E_ARG;

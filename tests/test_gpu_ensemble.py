@@ -140,3 +140,40 @@ def test_device_cold_start_equals_host_initial_state(gpu_lib, precision):
     from gom_release_gb300.core import FIELDS
     for name in FIELDS:
         assert np.array_equal(a.get_field(name), b.get_field(name)), name
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_every_launch_variant_gives_the_same_results(gpu_lib, precision):
+    """Each compiled variant of each tunable launch (gom_set_tuning) changes the launch shape only:
+    twelve storm-forced steps of a packed ensemble end bit for bit where variant 0 ends, ELM foot
+    elements included."""
+    from gom_release_gb300.core import FIELDS
+    members = runs()
+    pk = pack(members)
+    pk = dataclasses.replace(pk, params=dataclasses.replace(pk.params, precision=precision))
+    st = initial_state(pk)
+    storms = [d.meta["storm"] for d in members]
+
+    def run(choice):
+        c = GomCore(pk, lib=gpu_lib)
+        prepare(c, st)
+        c.set_tuning(choice)
+        c.set_forcing(PackedForcing(pk).step(1))
+        c.set_storms(storms, elapsed_time=0.0)
+        for _ in range(12):
+            c.step_all()
+        out = {n: c.get_field(n) for n in FIELDS}
+        c.close()
+        return out
+
+    base = run([0, 0, 0, 0])
+    assert np.count_nonzero(base["elm_foot"]) > 0
+    counts = GomCore(pk, lib=gpu_lib).tuning_variants()
+    for site, n in enumerate(counts):
+        for v in range(1, n):
+            choice = [0, 0, 0, 0]
+            choice[site] = v
+            got = run(choice)
+            for name in FIELDS:
+                a, b = got[name], base[name]
+                assert a.tobytes() == b.tobytes(), (site, v, name)
