@@ -546,6 +546,7 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
         if (e == cudaSuccess) e = dalloc(c, &W.fl_count, 2);
     }
     if (e == cudaSuccess) e = dalloc(c, &W.node_weight, NN);
+    if (e == cudaSuccess) e = dalloc(c, &W.fs_sums, 3 * NF);
     if (e == cudaSuccess) e = dalloc(c, &W.cons, 2 + 2 * (size_t)((NC + 255) / 256));
     if (e == cudaSuccess) e = dalloc(c, &c->x.status, 1);
     if (e != cudaSuccess) return fail(e == cudaErrorMemoryAllocation ? GOM_E_NOMEM : GOM_E_CUDA);
@@ -555,6 +556,7 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
     P.rho_o = params->rho_o;
     P.msl = params->msl;
     P.dt = params->dt;
+    for (int n = 1; n <= GOM_BT_TABLE; ++n) P.bt_dt[n - 1] = params->dt / n;
     P.theta = params->theta;
     P.adv_onoff_depth = params->adv_onoff_depth;
     P.von_karman = params->von_karman;
@@ -623,6 +625,7 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
         if (dalloc(c, &el, 8 * NC) != cudaSuccess) return fail(GOM_E_NOMEM);
         c->x.g.elem_local = el;
         if (launch_elem_local(c->x.g, el, c->x.stream) != cudaSuccess) return fail(GOM_E_CUDA);
+        if (prepare_momentum_tile(L) != cudaSuccess) return fail(GOM_E_CUDA);
         // the FP32 context shares geometry, forcing, parameters, status, stream and the FP64
         // work arrays (free-surface system, PCG vectors, ELM counts, node weights, sums)
         LaunchT<float> &X = c->xf;
@@ -654,6 +657,7 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
         X.w.fl_bsum = W.fl_bsum;
         X.w.fl_count = W.fl_count;
         X.w.node_weight = W.node_weight;
+        X.w.fs_sums = W.fs_sums;
         X.w.cons = W.cons;
         // FP32 copy of the free-surface system for the FP32 inner PCG iterations
         if (dalloc(c, &X.w.sp32, 5 * NC) != cudaSuccess) return fail(GOM_E_NOMEM);

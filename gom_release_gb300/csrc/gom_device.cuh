@@ -14,6 +14,7 @@
 #include "../../include/gom_core.h"
 
 #define GOM_MAXL 64          // largest n_layers a context accepts
+#define GOM_BT_TABLE 32      // ELM substep counts with a precomputed dt / n
 #define GOM_MAXNB 16         // largest max_no_neighbor_node a context accepts
 
 namespace gom {
@@ -97,6 +98,7 @@ struct Params {
         ana_density, max_iteration_pcg, transport_flag, trans_sub_iter, h_flux_limiter, v_flux_limiter, is_salt,
         is_temp, heat_option, test_barrier_phantom_blocks, turbulence_flag;
     double pp_h1, pp_h2, pp_vdmax1, pp_vdmax2, pp_vdmin1, pp_vdmin2, pp_tdmin;
+    double bt_dt[GOM_BT_TABLE];   // dt / n for ELM substep counts n = 1..GOM_BT_TABLE
 };
 
 // -------------------------------------------------------------------- layer indexing
@@ -104,6 +106,15 @@ struct Params {
 __device__ __forceinline__ long ix(int k, int e, int L) { return (long)(e - 1) * L + (k - 1); }
 // (0:L, N) arrays
 __device__ __forceinline__ long ix0(int k, int e, int L) { return (long)(e - 1) * (L + 1) + k; }
+
+// Column kernels take their entity from a bottom-layer-sorted order in the FP64 path (the 32
+// columns of a warp have nearly equal heights, which keeps the FP64 pipe busy); the FP32 path
+// takes entities in natural order, where neighbouring lanes work on neighbouring columns of the
+// (layer, entity) arrays and share their memory sectors.
+template <typename R> __device__ __forceinline__ int column_entity(const int *order, unsigned tid) {
+    if constexpr (sizeof(R) == sizeof(float)) return (int)tid + 1;
+    else return order[tid];
+}
 
 // -------------------------------------------------------------------- error status
 __device__ inline void record_error(gom_status *st, int code, int site, int entity, int layer, double value) {

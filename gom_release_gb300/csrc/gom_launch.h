@@ -44,13 +44,14 @@ template <typename R> struct WorkT {
     int *cl_list = nullptr, *cl_off = nullptr, *cl_bsum = nullptr, *cl_count = nullptr;
     // conservation
     double *cons = nullptr;                                     // [volume, salt]
+    double *fs_sums = nullptr;                                  // free-surface column sums (3, NF)
 };
 using Work = WorkT<double>;
 
 // Tunable launches: each picks one of a few compiled variants (block size, minimum resident
 // blocks per SM); gom_autotune times the variants on the context's state and keeps the fastest.
 enum TuneSite { TUNE_ELM = 0, TUNE_MOMENTUM, TUNE_TR_SOLVE, TUNE_TR_LIMITER, TUNE_COUNT };
-constexpr int TUNE_VARIANTS[TUNE_COUNT] = {7, 3, 3, 3};
+constexpr int TUNE_VARIANTS[TUNE_COUNT] = {7, 4, 3, 3};
 
 template <typename R> struct LaunchT {
     int tune[TUNE_COUNT] = {0, 0, 0, 0};
@@ -64,6 +65,9 @@ template <typename R> struct LaunchT {
     int num_sms = 0;
 };
 using Launch = LaunchT<double>;
+
+// raises the dynamic shared-memory limit of the tiled FP32 momentum kernel for L layers
+cudaError_t prepare_momentum_tile(int L);
 
 template <typename R> cudaError_t launch_bottom_friction(const LaunchT<R> &x);
 template <typename R> cudaError_t launch_boundary_velocity(const LaunchT<R> &x);

@@ -251,6 +251,18 @@ __device__ __forceinline__ int classify_f32(const LocalElem &e, float px, float 
         near = true;
         return -1;
     }
+    if (e.tq == 4) {
+        // the excess identity needs a convex quad (then its two-triangle area is the polygon's)
+        for (int l = 0; l < 4; ++l) {
+            const int m = (l + 1) & 3, n = (l + 2) & 3;
+            const float turn = (e.x[m] - e.x[l]) * (e.y[n] - e.y[m]) - (e.y[m] - e.y[l]) * (e.x[n] - e.x[m]);
+            const float mag = (fabsf(e.x[l]) + fabsf(e.x[m]) + fabsf(e.x[n])) * (fabsf(e.y[l]) + fabsf(e.y[m]) + fabsf(e.y[n]));
+            if (!(turn > 16.0f * u * mag)) {
+                near = true;
+                return -1;
+            }
+        }
+    }
     for (int l = 0; l < e.tq; ++l) {
         int m = l + 1 == e.tq ? 0 : l + 1;
         float ex = e.x[m] - e.x[l], ey = e.y[m] - e.y[l];
@@ -274,40 +286,224 @@ __device__ __forceinline__ int classify_f32(const LocalElem &e, float px, float 
     return -1;
 }
 
-__device__ __forceinline__ bool in_elem_mixed(const Geom &g, int nel, double x, double y) {
-    LocalElem e;
-    load_local(g, nel, e);
+// The last FP32 classification of the search (mixed path): when the search ends because the foot
+// tested inside element nnel, the caller reuses that element's local data and test instead of
+// repeating them.
+struct LastTest {
+    bool valid = false;
+    LocalElem el;
+    float px, py;
+    int cls;
     bool near;
-    int r = classify_f32(e, (float)(x - e.xc), (float)(y - e.yc), near);
-    return r >= 0 ? r == 1 : in_elem64(g, nel, x, y);
-}
-__device__ __forceinline__ bool out_elem_mixed(const Geom &g, int nel, double x, double y) {
-    LocalElem e;
-    load_local(g, nel, e);
-    bool near;
-    int r = classify_f32(e, (float)(x - e.xc), (float)(y - e.yc), near);
-    return r >= 0 ? r == 0 : out_elem64(g, nel, x, y);
+};
+
+__device__ __forceinline__ bool in_elem_mixed_rec(const Geom &g, int nel, double x, double y, LastTest &t) {
+    load_local(g, nel, t.el);
+    t.px = (float)(x - t.el.xc);
+    t.py = (float)(y - t.el.yc);
+    t.cls = classify_f32(t.el, t.px, t.py, t.near);
+    return t.cls >= 0 ? t.cls == 1 : in_elem64(g, nel, x, y);
 }
 
-// search_straight_line.f90:15-399 (mode 1). Returns 0 or a GOM_ELM_* site.  start_on_edge: the
-// start point is the midpoint of an edge of the start element (the first substep of a face), for
-// which the reference's start test (:37-46) always passes -- its area excess is zero up to FP64
-// rounding, far below the tolerance -- so it is not evaluated.  MIXED selects the FP32-filtered
-// point-in-element tests (same decisions).
+// Mixed path: check_intersection.f90 on element-local FP32 coordinates, deciding only where an
+// error bound on the FP32 determinants settles the reference's FP64 outcome (tt1 and tt2 in [0, 1],
+// the sign and magnitude tests of unit_range): 1 crossed (crossing point set), 0 not crossed,
+// -1 not decidable in FP32.  Bound: with Mx, My the sums of the |coordinates|, every coordinate
+// difference is within 2u Mx (2u My) of its exact value (rounding of the FP64 offsets to FP32 and
+// of the difference), so each determinant of two products is within about 12.3 u Mx My; 16 u Mx
+// My is used.
+__device__ __forceinline__ int cross_f32(float x1, float x2, float x3, float x4, float y1, float y2, float y3,
+                                         float y4, float &xin, float &yin) {
+    const float u = 5.97e-8f;   // 2^-24
+    const float ax = x2 - x1, ay = y2 - y1, bx = x3 - x4, by = y3 - y4, cx = x3 - x1, cy = y3 - y1;
+    const float mx = fabsf(x1) + fabsf(x2) + fabsf(x3) + fabsf(x4), my = fabsf(y1) + fabsf(y2) + fabsf(y3) + fabsf(y4);
+    const float ed = 16.0f * u * mx * my + 1e-30f, e1 = ed, e2 = ed;
+    const float delta = ax * by - ay * bx;
+    if (fabsf(delta) <= ed) return -1;
+    const float d1 = cx * by - cy * bx;
+    const float d2 = ax * cy - ay * cx;
+    // tt = d / delta in [0, 1]: d on delta's side of 0 and |d| <= |delta|; a parameter settled
+    // outside decides "not crossed" whatever the other one is
+    int r = 1;
+    const float dd[2] = {d1, d2}, ee[2] = {e1, e2};
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        const float d = dd[q], e = ee[q];
+        const float m = fabsf(d) - fabsf(delta);
+        if (fabsf(d) > e && (d < 0.0f) != (delta < 0.0f)) return 0;   // tt < 0
+        if (m > e + ed) return 0;                                      // tt > 1
+        if (fabsf(d) <= e || fabsf(m) <= e + ed) r = -1;               // tt near 0 or 1
+    }
+    if (r < 0) return -1;
+    const float t1 = d1 / delta;
+    xin = x1 + ax * t1;
+    yin = y1 + ay * t1;
+    return 1;
+}
+
+// Mixed path: the element-to-element walk of search_straight_line.f90:47-283 with the segment,
+// the crossing points and the remaining-path bookkeeping in FP32 on coordinates relative to the
+// centre of the element being crossed (re-based in FP64 at every element); every edge and
+// in-element decision is the reference's (FP32 under an error bound, FP64 where that does not
+// settle it), the foot itself stays FP64.  Entered when the foot is not in the start
+// element; on return the foot is in nnel (last holds that test) or nfl = 1 (stopped at a dry or
+// land edge, foot moved to the crossing point).
+// edge l of element nel crossed by the segment (xcg, ycg) -> (xt, yt): the FP32 decision, or the
+// reference's FP64 check_intersection where that is not settled; crossing point in nel's frame
+__device__ __forceinline__ bool crosses(const Geom &g, int nel, const LocalElem &e, int l, float sx, float sy, float tx,
+                                        float ty, double xcg, double ycg, double xt, double yt, float &xin,
+                                        float &yin) {
+    const int a = l % e.tq, b = (l + 1) % e.tq;   // local nodes start_end_node(tq, l, 1..2) - 1
+    const int r = cross_f32(sx, tx, e.x[a], e.x[b], sy, ty, e.y[a], e.y[b], xin, yin);
+    if (r >= 0) return r == 1;
+    const int jd1 = g.cell_node(start_end_node(e.tq, l, 1), nel), jd2 = g.cell_node(start_end_node(e.tq, l, 2), nel);
+    double xi = 0.0, yi = 0.0;
+    if (!check_intersection(xcg, xt, g.x_node[jd1 - 1], g.x_node[jd2 - 1], ycg, yt, g.y_node[jd1 - 1],
+                            g.y_node[jd2 - 1], xi, yi))
+        return false;
+    xin = (float)(xi - e.xc);
+    yin = (float)(yi - e.yc);
+    return true;
+}
+
+template <typename R>
+__device__ int walk_f32(const Geom &g, const StateT<R> &s, int &nnel, double time, double x0, double y0, double z0,
+                        double &xt, double &yt, double &zt, int &nfl, LastTest &last) {
+    const double c1d = 1.0 - 1.0e-4;
+    const float c1 = (float)c1d;
+    int nel = nnel;
+    LocalElem e;
+    load_local(g, nel, e);
+    // the reference's nudged start xcg = c1 x0 + 1e-4 x_cell is c1 (x0 - x_cell) from the centre
+    float sx = c1 * (float)(x0 - e.xc), sy = c1 * (float)(y0 - e.yc);
+    float tx = (float)(xt - e.xc), ty = (float)(yt - e.yc);
+    float pathl = sqrtf((tx - sx) * (tx - sx) + (ty - sy) * (ty - sy));
+    if (pathl == 0.0f) return GOM_ELM_ZERO_PATH;
+    // the reference's FP64 segment start, for the edges FP32 cannot decide
+    const double xcg = c1d * x0 + 1.0e-4 * g.x_cell[nel - 1], ycg = c1d * y0 + 1.0e-4 * g.y_cell[nel - 1];
+    int nel_j = 0;
+    float xin = 0.0f, yin = 0.0f;
+    for (int l = 1; l <= e.tq; ++l) {
+        if (crosses(g, nel, e, l, sx, sy, tx, ty, xcg, ycg, xt, yt, xin, yin)) {
+            nel_j = l;
+            break;
+        }
+    }
+    if (nel_j == 0) return GOM_ELM_NO_FIRST_EDGE;
+    // A walk that stops on an edge takes its foot from that crossing point, formed in FP64: FP32
+    // offsets lose the small components of a path running nearly along the edge.  The height
+    // there is the reference's zin, the product of the remaining-path ratios of all crossings,
+    // which telescopes to |T - crossing| / |T - start|.
+    const double pathl0 = sqrt((xt - xcg) * (xt - xcg) + (yt - ycg) * (yt - ycg));
+    auto stop_at_edge = [&](int el, int l, const LocalElem &le, float fxin, float fyin, double &xi, double &yi) {
+        const int q = le.tq;
+        const int jd1 = g.cell_node(start_end_node(q, l, 1), el), jd2 = g.cell_node(start_end_node(q, l, 2), el);
+        if (!check_intersection(xcg, xt, g.x_node[jd1 - 1], g.x_node[jd2 - 1], ycg, yt, g.y_node[jd1 - 1],
+                                g.y_node[jd2 - 1], xi, yi)) {
+            xi = le.xc + (double)fxin;   // not reached: the FP32 crossing decision is the FP64 one
+            yi = le.yc + (double)fyin;
+        }
+        const double dist = sqrt((xi - xt) * (xi - xt) + (yi - yt) * (yi - yt));
+        zt = zt - dist / pathl0 * (zt - z0);
+    };
+    float trm = (float)time;
+    int iteration = 0;
+    for (;;) {
+        iteration = iteration + 1;
+        if (iteration > 1000) {
+            double xi, yi;
+            stop_at_edge(nel, nel_j, e, xin, yin, xi, yi);
+            nfl = 1;
+            xt = xi;
+            yt = yi;
+            nnel = nel;
+            last.valid = false;
+            return 0;
+        }
+        const int tqn = e.tq;
+        const int md1 = g.cell_node(start_end_node(tqn, nel_j, 1), nel);
+        const int md2 = g.cell_node(start_end_node(tqn, nel_j, 2), nel);
+        const float dist = sqrtf((xin - tx) * (xin - tx) + (yin - ty) * (yin - ty));
+        const float ratio = dist / pathl;
+        if (ratio > 1.0f + 1.0e-4f) return GOM_ELM_OVERSHOOT;
+        trm = trm * dist / pathl;
+        pathl = dist;
+        if (pathl == 0.0f || trm == 0.0f) return GOM_ELM_ZERO_REMAIN;
+        const int adjc = g.cell_adj(nel_j, nel);
+        if (adjc == 0 || top_el(s, adjc) == 0) {
+            const int isd = g.cell_face(nel_j, nel);
+            if (g.face_node(1, isd) + g.face_node(2, isd) != md1 + md2) return GOM_ELM_FACE_MISMATCH;
+            double xi, yi;
+            stop_at_edge(nel, nel_j, e, xin, yin, xi, yi);
+            nfl = 1;
+            xt = c1d * xi + 1.0e-4 * g.x_cell[nel - 1];
+            yt = c1d * yi + 1.0e-4 * g.y_cell[nel - 1];
+            nnel = nel;
+            last.valid = false;
+            return 0;
+        }
+        nel = adjc;
+        LocalElem e2;
+        load_local(g, nel, e2);
+        const float dx = (float)(e.xc - e2.xc), dy = (float)(e.yc - e2.yc);
+        sx += dx;
+        sy += dy;
+        xin += dx;
+        yin += dy;
+        e = e2;
+        tx = (float)(xt - e.xc);
+        ty = (float)(yt - e.yc);
+        last.el = e;
+        last.px = tx;
+        last.py = ty;
+        last.cls = classify_f32(e, tx, ty, last.near);
+        if (last.cls >= 0 ? last.cls == 1 : in_elem64(g, nel, xt, yt)) {
+            nnel = nel;
+            last.valid = true;
+            return 0;
+        }
+        bool found = false;
+        for (int l = 1; l <= e.tq; ++l) {
+            const int jd1 = g.cell_node(start_end_node(e.tq, l, 1), nel);
+            const int jd2 = g.cell_node(start_end_node(e.tq, l, 2), nel);
+            if ((jd1 == md1 && jd2 == md2) || (jd2 == md1 && jd1 == md2)) continue;
+            if (crosses(g, nel, e, l, sx, sy, tx, ty, xcg, ycg, xt, yt, xin, yin)) {
+                nel_j = l;
+                found = true;
+                break;
+            }
+        }
+        if (!found) return GOM_ELM_NO_NEXT_EDGE;
+    }
+}
+
 template <typename R, bool MIXED>
 __device__ int search_straight_line(const Geom &g, const StateT<R> &s, const Params &p, int &nnel, int &jlev, double time,
                                     double x0, double y0, double z0, double &xt, double &yt, double &zt, int &nfl,
-                                    bool start_on_edge) {
+                                    bool first_substep, LastTest &last) {
     const double small_06 = F(1.e-6f);
     const double MSL = p.msl;
     const int L = g.L;
-    if (top_el(s, nnel) == 0 || MSL - g.h_cell[nnel - 1] > MSL + s.eta_cell[nnel - 1]) return GOM_ELM_START_DRY;
+    // The reference's start tests (:26-46) are known to pass and not evaluated, except the dry
+    // test of the first substep.  The start-in-element test of the first substep: the start is the
+    // midpoint of an edge of the start element, area excess zero up to FP64 rounding, far below
+    // the tolerance.  Both tests of a later substep: it starts at the previous foot, and the
+    // previous search ended only after that foot tested inside nnel (the complementary test on the
+    // same operands) and nnel passed the same dry test (:370).
+    if (first_substep && (top_el(s, nnel) == 0 || MSL - g.h_cell[nnel - 1] > MSL + s.eta_cell[nnel - 1]))
+        return GOM_ELM_START_DRY;
     nfl = 0;
+    last.valid = false;
     double trm = time;
     int nel = nnel;
-    if (!start_on_edge && (MIXED ? out_elem_mixed(g, nel, x0, y0) : out_elem64(g, nel, x0, y0)))
-        return GOM_ELM_START_OUTSIDE;
-    if (!(MIXED ? in_elem_mixed(g, nel, xt, yt) : in_elem64(g, nel, xt, yt))) {
+    if constexpr (MIXED) {
+        if (!in_elem_mixed_rec(g, nel, xt, yt, last)) {
+            int e = walk_f32(g, s, nnel, time, x0, y0, z0, xt, yt, zt, nfl, last);
+            if (e) return e;
+        } else {
+            last.valid = true;
+        }
+    } else if (!in_elem64(g, nel, xt, yt)) {
         const double c1 = 1.0 - 1.0e-4;
         double xcg = c1 * x0 + 1.0e-4 * g.x_cell[nel - 1];
         double ycg = c1 * y0 + 1.0e-4 * g.y_cell[nel - 1];
@@ -362,7 +558,7 @@ __device__ int search_straight_line(const Geom &g, const StateT<R> &s, const Par
                 break;
             }
             nel = adjc;
-            if (MIXED ? in_elem_mixed(g, nel, xt, yt) : in_elem64(g, nel, xt, yt)) {
+            if (in_elem64(g, nel, xt, yt)) {
                 nnel = nel;
                 break;
             }
@@ -415,32 +611,38 @@ __device__ bool near_edge_line(const Geom &g, int nel, double x, double y) {
 }
 
 // ELM_backtrace_v1.f90:40-200 (mode 1).  The first substep starts at the face midpoint, on an
-// edge of the start element.  MIXED: the same walk (FP64 foot coordinates, the reference's
-// point-in-element decisions), interpolation weights and velocities in FP32 on element-local
-// coordinates.
+// edge of the start element.  MIXED: FP64 foot coordinates and the reference's point-in-element
+// decisions (FP32 with an error bound, FP64 where that does not decide); the crossing walk,
+// interpolation weights and velocities in FP32 on element-local coordinates.
 template <typename R, bool MIXED>
 __device__ int elm_backtrace(const Geom &g, const StateT<R> &s, const Params &p, int bt_step, double bt_dt, double &uu,
                              double &vv, double &ww, double x0, double y0, double z0, int &nnel, int &jlev,
                              int &near_edge) {
     const double small_06 = F(1.e-6f);
     const int L = g.L;
+    LastTest last;
     for (int idt = 1; idt <= bt_step; ++idt) {
         double xt = x0 - bt_dt * uu;
         double yt = y0 - bt_dt * vv;
         double zt = z0 - bt_dt * ww;
         int nfl = 0;
-        int e = search_straight_line<R, MIXED>(g, s, p, nnel, jlev, bt_dt, x0, y0, z0, xt, yt, zt, nfl, idt == 1);
+        int e = search_straight_line<R, MIXED>(g, s, p, nnel, jlev, bt_dt, x0, y0, z0, xt, yt, zt, nfl, idt == 1, last);
         if (e) return e;
         int tq = g.tri_or_quad[nnel - 1];
         double zup = (jlev == s.top_cell[nnel - 1]) ? p.msl + s.eta_cell[nnel - 1] : g.z_level[jlev];
         if (zt > zup) return GOM_ELM_Z_ABOVE;
         if constexpr (MIXED) {
             const float zrat = (float)(zup - zt) / (float)s.dz_cell[ix(jlev, nnel, L)];
-            LocalElem el;
-            load_local(g, nnel, el);
-            const float px = (float)(xt - el.xc), py = (float)(yt - el.yc);
-            bool near;
-            const int cls = classify_f32(el, px, py, near);
+            if (!last.valid) {
+                load_local(g, nnel, last.el);
+                last.px = (float)(xt - last.el.xc);
+                last.py = (float)(yt - last.el.yc);
+                last.cls = classify_f32(last.el, last.px, last.py, last.near);
+            }
+            const LocalElem &el = last.el;
+            const float px = last.px, py = last.py;
+            const bool near = last.near;
+            const int cls = last.cls;
             float sta[4];
             if (tq == 3) {
                 const float ar = el.ar;
@@ -624,43 +826,60 @@ template <typename R>
 __device__ void elm_face_layer(const Geom &g, const StateT<R> &s, const Params &p, gom_status *st, int j, int k, int ie0,
                                int n1, int n2, double ct, double sn) {
     const int L = g.L;
+    constexpr bool MIXED = sizeof(R) == sizeof(float);
     long o = ix(k, j, L);
-    double unf = s.un_face[o], vnf = s.vn_face[o];
     int nnel = ie0, jlev = k;
     double x0 = g.x_face[j - 1], y0 = g.y_face[j - 1], z0;
     if (k == s.top_cell[nnel - 1]) z0 = p.msl + s.eta_cell[nnel - 1] - s.dz_cell[ix(k, nnel, L)] * 0.5;
     else z0 = g.z_level[k] - s.dz_cell[ix(k, nnel, L)] * 0.5;
+    // the velocity at the face-layer midpoint and the walk threshold of :166 (vmag = sqrt(q) <=
+    // thr), decided on q against thr^2 away from the threshold; in FP64 in both paths, so a
+    // face-layer at the threshold is walked or not as in the FP64 path
+    double unf = s.un_face[o], vnf = s.vn_face[o];
     double uu = unf * ct - vnf * sn;
     double vv = unf * sn + vnf * ct;
     double wdown = (s.w_node[ix0(k - 1, n1, L)] + s.w_node[ix0(k - 1, n2, L)]) * 0.5;
     double wup = (s.w_node[ix0(k, n1, L)] + s.w_node[ix0(k, n2, L)]) * 0.5;
     double ww = (wdown + wup) * 0.5;
-    double vmag = sqrt(uu * uu + vv * vv + ww * ww);
-    if (vmag <= F(1.e-4f)) {
+    bool slow;
+    {
+        const double thr = F(1.e-4f), q = uu * uu + vv * vv + ww * ww, t2 = thr * thr;
+        if (q < t2 * (1.0 - 1e-9)) slow = true;
+        else if (q > t2 * (1.0 + 1e-9)) slow = false;
+        else slow = sqrt(q) <= thr;
+    }
+    if (slow) {
         s.un_elm[o] = s.un_face[o];
         s.vn_elm[o] = s.vn_face[o];
         return;
     }
-    int bt_step = (int)((double)(s.num_sub_elm[ix(k, n1, L)] + s.num_sub_elm[ix(k, n2, L)]) * 0.5);
-    double bt_dt = p.dt / bt_step;
+    // INT((n1 + n2) * 0.5) of two integers is their truncated integer half; dt / bt_step from the
+    // table of dt / n (the same correctly rounded quotients) when n is in its range
+    int bt_step = (s.num_sub_elm[ix(k, n1, L)] + s.num_sub_elm[ix(k, n2, L)]) / 2;
+    double bt_dt = (bt_step >= 1 && bt_step <= GOM_BT_TABLE) ? p.bt_dt[bt_step - 1] : p.dt / bt_step;
     int near = 0;
-    int e = elm_backtrace<R, sizeof(R) == sizeof(float)>(g, s, p, bt_step, bt_dt, uu, vv, ww, x0, y0, z0, nnel, jlev,
-                                                          near);
+    int e = elm_backtrace<R, MIXED>(g, s, p, bt_step, bt_dt, uu, vv, ww, x0, y0, z0, nnel, jlev, near);
     if (e) {
         record_error(st, GOM_E_ELM, e, j, k, 0.0);
         return;
     }
     s.elm_foot[o] = nnel;
     s.elm_near_edge[o] = near;
-    s.un_elm[o] = (R)(uu * ct + vv * sn);
-    s.vn_elm[o] = (R)(-uu * sn + vv * ct);
+    if constexpr (MIXED) {
+        const float ctf = (float)ct, snf = (float)sn, uf = (float)uu, vf = (float)vv;
+        s.un_elm[o] = uf * ctf + vf * snf;
+        s.vn_elm[o] = -uf * snf + vf * ctf;
+    } else {
+        s.un_elm[o] = (R)(uu * ct + vv * sn);
+        s.vn_elm[o] = (R)(-uu * sn + vv * ct);
+    }
 }
 
 template <typename R, int BS, int MINB>
 __global__ void __launch_bounds__(BS, MINB) k_elm_faces(Geom g, StateT<R> s, Params p, gom_status *st) {
     unsigned tid = flat_tid();
     if (tid >= (unsigned)g.NF) return;
-    int j = g.face_order[tid];
+    int j = column_entity<R>(g.face_order, tid);
     const int L = g.L;
     int b = g.bottom_face[j - 1], tf = s.top_face[j - 1];
     for (int k = 1; k <= L; ++k) {
@@ -851,53 +1070,62 @@ __device__ double prev_rtemp0(const Geom &g, const StateT<R> &s, const Forcing &
 // Per-face terms (elevation gradients, air pressure, geometry) are formed in FP64 once per face
 // and rounded to R; the layer loop, the Smagorinsky diffusion, the baroclinic integral and the
 // tridiagonal solve run in R.  With R = double every expression is the reference's.
+// Per-face quantities of a momentum column, formed once per face.
+template <typename R> struct MomFace {
+    int j, tj, bj, nvl, node1, node2, a1, a2, btype, ibnd, tq1, tq2, ba1, ta1, ba2, ta2, bn1, tn1, bn2, tn2;
+    int cn1[4], cn2[4];   // nodes of the two adjacent cells
+    bool wet_nodes;
+    R dtR, cordt, ctR, snR, ct2R, sn2R, bt1, along, air1, air2, bc_dj, bc_fl, djR, flR, fl2, gdt0, wsn, wst, qub,
+        smag, ah0, kh0, area1, rl1, rl2, inv_tq1, inv_tq2, spin, c069, gbdt, gtdt;
+};
+
+// false for a dry face (no column)
 template <typename R>
-__global__ void __launch_bounds__(256) k_momentum(Geom g, StateT<R> s, Forcing f, Params p, gom_status *st) {
-    unsigned tid = flat_tid();
-    if (tid >= (unsigned)g.NF) return;
-    int j = g.face_order[tid];
-    const int L = g.L;
-    int tj = s.top_face[j - 1];
-    if (tj == 0) return;
+__device__ bool momentum_setup(const Geom &g, const StateT<R> &s, const Forcing &f, const Params &p, int j,
+                               MomFace<R> &m) {
+    const int tj = s.top_face[j - 1];
+    m.j = j;
+    m.tj = tj;
+    if (tj == 0) return false;
     const double dt = p.dt, gravity = p.gravity, theta = p.theta;
     const R dtR = (R)dt;
-    int bj = g.bottom_face[j - 1];
-    int nvl = tj - bj + 1;
-    int node1 = g.face_node(1, j), node2 = g.face_node(2, j);
-    int a1 = g.face_cell(1, j), a2 = g.face_cell(2, j);
-    int btype = g.boundary_type_of_face[j - 1];
+    m.dtR = dtR;
+    const int bj = g.bottom_face[j - 1];
+    m.bj = bj;
+    m.nvl = tj - bj + 1;
+    const int node1 = g.face_node(1, j), node2 = g.face_node(2, j);
+    const int a1 = g.face_cell(1, j), a2 = g.face_cell(2, j);
+    const int btype = g.boundary_type_of_face[j - 1];
+    m.node1 = node1;
+    m.node2 = node2;
+    m.a1 = a1;
+    m.a2 = a2;
+    m.btype = btype;
     const double dj = g.delta_j[j - 1], fl = g.face_length[j - 1];
     const double ct = g.cos_theta[j - 1], sn = g.sin_theta[j - 1], ct2 = g.cos_theta2[j - 1], sn2 = g.sin_theta2[j - 1];
-    const R ctR = (R)ct, snR = (R)sn, ct2R = (R)ct2, sn2R = (R)sn2;
-    const R cordt = (R)(g.coriolis_factor[j - 1] * dt);
-    R a[GOM_MAXL], bd[GOM_MAXL], cu[GOM_MAXL], gam[GOM_MAXL];
-    R rhs[GOM_MAXL][3];
-    // :120-169
-    for (int k = bj + 1; k <= tj - 1; ++k) {
-        int kk = tj - k + 1;
-        a[kk - 1] = -dtR * s.av[ix0(k, j, L)] / s.dzhalf_face[ix0(k, j, L)];
-        cu[kk - 1] = -dtR * s.av[ix0(k - 1, j, L)] / s.dzhalf_face[ix0(k - 1, j, L)];
-        bd[kk - 1] = -a[kk - 1] + s.dz_face[ix(k, j, L)] - cu[kk - 1];
-    }
-    if (tj == bj) {
-        bd[0] = s.dz_face[ix(tj, j, L)] + s.gamma_b[j - 1] * dtR;
-    } else {
-        cu[0] = -dtR * s.av[ix0(tj - 1, j, L)] / s.dzhalf_face[ix0(tj - 1, j, L)];
-        bd[0] = (R)f.gamma_t[j - 1] * dtR + s.dz_face[ix(tj, j, L)] - cu[0];
-        a[nvl - 1] = -dtR * s.av[ix0(bj, j, L)] / s.dzhalf_face[ix0(bj, j, L)];
-        bd[nvl - 1] = -a[nvl - 1] + s.dz_face[ix(bj, j, L)] + s.gamma_b[j - 1] * dtR;
-    }
-    bool wet_nodes = s.wetdry_node[node1 - 1] == 0 && s.wetdry_node[node2 - 1] == 0;
-    double eta_n1 = s.eta_node[node1 - 1], eta_n2 = s.eta_node[node2 - 1];
-    const R c069 = (R)F(0.69f);
-    int ibnd = g.isflowside3[j - 1];
-    double eta1 = s.eta_cell[a1 - 1];
-    double eta2 = a2 != 0 ? s.eta_cell[a2 - 1] : 0.0;
-    int ba1 = g.bottom_cell[a1 - 1], ta1 = s.top_cell[a1 - 1];
-    int ba2 = a2 != 0 ? g.bottom_cell[a2 - 1] : 0, ta2 = a2 != 0 ? s.top_cell[a2 - 1] : 0;
-    int bn1 = g.bottom_node[node1 - 1], tn1 = s.top_node[node1 - 1];
-    int bn2 = g.bottom_node[node2 - 1], tn2 = s.top_node[node2 - 1];
-    R bt1, along, air1, air2, bc_dj, bc_fl;
+    m.ctR = (R)ct;
+    m.snR = (R)sn;
+    m.ct2R = (R)ct2;
+    m.sn2R = (R)sn2;
+    const R ct2R = m.ct2R, sn2R = m.sn2R;
+    m.cordt = (R)(g.coriolis_factor[j - 1] * dt);
+    m.gbdt = s.gamma_b[j - 1] * dtR;
+    m.gtdt = (R)f.gamma_t[j - 1] * dtR;
+    const bool wet_nodes = s.wetdry_node[node1 - 1] == 0 && s.wetdry_node[node2 - 1] == 0;
+    m.wet_nodes = wet_nodes;
+    const double eta_n1 = s.eta_node[node1 - 1], eta_n2 = s.eta_node[node2 - 1];
+    m.c069 = (R)F(0.69f);
+    m.ibnd = g.isflowside3[j - 1];
+    const double eta1 = s.eta_cell[a1 - 1];
+    const double eta2 = a2 != 0 ? s.eta_cell[a2 - 1] : 0.0;
+    m.ba1 = g.bottom_cell[a1 - 1];
+    m.ta1 = s.top_cell[a1 - 1];
+    m.ba2 = a2 != 0 ? g.bottom_cell[a2 - 1] : 0;
+    m.ta2 = a2 != 0 ? s.top_cell[a2 - 1] : 0;
+    m.bn1 = g.bottom_node[node1 - 1];
+    m.tn1 = s.top_node[node1 - 1];
+    m.bn2 = g.bottom_node[node2 - 1];
+    m.tn2 = s.top_node[node2 - 1];
     if constexpr (sizeof(R) == sizeof(float)) {
         // Mixed path: the same terms from FP64 differences of elevations and pressures, the
         // divisions and products in FP32 (no FP64 division per face)
@@ -928,12 +1156,12 @@ __global__ void __launch_bounds__(256) k_momentum(Geom g, StateT<R> s, Forcing f
             rt0_air = (float)prev_rtemp0(g, s, f, p, j);
         }
         const float rtemp3_air = -dtr * (float)(f.air_p[node2 - 1] - pref) * inv_fl;
-        bt1 = bt_rtemp1;
-        along = (btype == 0) ? (along0 + bt_rtemp2) : along0;
-        air1 = rt0_air * ct2R;
-        air2 = rtemp3_air + rt0_air * sn2R;
-        bc_dj = -(gdt / (float)p.rho_o) * inv_dj;
-        bc_fl = -(gdt / (float)p.rho_o) * inv_fl;
+        m.bt1 = bt_rtemp1;
+        m.along = (btype == 0) ? (along0 + bt_rtemp2) : along0;
+        m.air1 = rt0_air * ct2R;
+        m.air2 = rtemp3_air + rt0_air * sn2R;
+        m.bc_dj = -(gdt / (float)p.rho_o) * inv_dj;
+        m.bc_fl = -(gdt / (float)p.rho_o) * inv_fl;
     } else {
         // rtemp0 reaching the air-pressure term of a boundary face
         double rt0_air;
@@ -958,136 +1186,196 @@ __global__ void __launch_bounds__(256) k_momentum(Geom g, StateT<R> s, Forcing f
             bt_rtemp1 = gravity * dt / dj * (1.0 - theta) * (f.eta_at_ob_old[ie - 1] - eta1);
         }
         double along_rtemp0 = wet_nodes ? gravity * dt / fl * (1.0 - theta) * (eta_n2 - eta_n1) : 0.0;
-        bt1 = (R)bt_rtemp1;
-        along = (R)((btype == 0) ? (along_rtemp0 + bt_rtemp2) : along_rtemp0);
-        air1 = (R)(rt0_air * ct2);
-        air2 = (R)(rtemp3_air + rt0_air * sn2);
-        bc_dj = (R)(-gravity * dt / (p.rho_o * dj));
-        bc_fl = (R)(-gravity * dt / (p.rho_o * fl));
+        m.bt1 = (R)bt_rtemp1;
+        m.along = (R)((btype == 0) ? (along_rtemp0 + bt_rtemp2) : along_rtemp0);
+        m.air1 = (R)(rt0_air * ct2);
+        m.air2 = (R)(rtemp3_air + rt0_air * sn2);
+        m.bc_dj = (R)(-gravity * dt / (p.rho_o * dj));
+        m.bc_fl = (R)(-gravity * dt / (p.rho_o * fl));
     }
-    const R djR = (R)dj, flR = (R)fl, fl2 = (R)(fl * fl);
-    const R gdt0 = (R)(gravity * dt);
-    const R wsn = (R)(dt * f.wind_stress_normal[j - 1]), wst = (R)(dt * f.wind_stress_tangnt[j - 1]);
-    const R qub = ibnd > 0 ? (R)s.qu_boundary[ibnd - 1] : R(0);
-    const R smag = (R)p.smagorinsky, ah0 = (R)p.ah_0, kh0 = (R)p.kh_0, area1 = (R)g.area[a1 - 1];
-    R rl1 = R(0), rl2 = R(0), inv_tq1 = R(0), inv_tq2 = R(0);
-    int tq1 = 0, tq2 = 0;
+    m.djR = (R)dj;
+    m.flR = (R)fl;
+    m.fl2 = (R)(fl * fl);
+    m.gdt0 = (R)(gravity * dt);
+    m.wsn = (R)(dt * f.wind_stress_normal[j - 1]);
+    m.wst = (R)(dt * f.wind_stress_tangnt[j - 1]);
+    m.qub = m.ibnd > 0 ? (R)s.qu_boundary[m.ibnd - 1] : R(0);
+    m.smag = (R)p.smagorinsky;
+    m.ah0 = (R)p.ah_0;
+    m.kh0 = (R)p.kh_0;
+    m.area1 = (R)g.area[a1 - 1];
+    m.rl1 = R(0);
+    m.rl2 = R(0);
+    m.inv_tq1 = R(0);
+    m.inv_tq2 = R(0);
+    m.tq1 = 0;
+    m.tq2 = 0;
     if (a2 != 0) {
         double ddx = g.x_cell[a1 - 1] - g.x_face[j - 1], ddy = g.y_cell[a1 - 1] - g.y_face[j - 1];
         double ddx2 = g.x_cell[a2 - 1] - g.x_face[j - 1], ddy2 = g.y_cell[a2 - 1] - g.y_face[j - 1];
         if constexpr (sizeof(R) == sizeof(float)) {
-            rl1 = sqrtf((float)ddx * (float)ddx + (float)ddy * (float)ddy);
-            rl2 = sqrtf((float)ddx2 * (float)ddx2 + (float)ddy2 * (float)ddy2);
+            m.rl1 = sqrtf((float)ddx * (float)ddx + (float)ddy * (float)ddy);
+            m.rl2 = sqrtf((float)ddx2 * (float)ddx2 + (float)ddy2 * (float)ddy2);
         } else {
-            rl1 = (R)sqrt(ddx * ddx + ddy * ddy);
-            rl2 = (R)sqrt(ddx2 * ddx2 + ddy2 * ddy2);
+            m.rl1 = (R)sqrt(ddx * ddx + ddy * ddy);
+            m.rl2 = (R)sqrt(ddx2 * ddx2 + ddy2 * ddy2);
         }
-        tq1 = g.tri_or_quad[a1 - 1];
-        tq2 = g.tri_or_quad[a2 - 1];
-        inv_tq1 = tq1 == 4 ? R(0.25) : R(0);   // x/4 == x*0.25 exactly; triangles divide
-        inv_tq2 = tq2 == 4 ? R(0.25) : R(0);
+        m.tq1 = g.tri_or_quad[a1 - 1];
+        m.tq2 = g.tri_or_quad[a2 - 1];
+        m.inv_tq1 = m.tq1 == 4 ? R(0.25) : R(0);   // x/4 == x*0.25 exactly; triangles divide
+        m.inv_tq2 = m.tq2 == 4 ? R(0.25) : R(0);
+#pragma unroll
+        for (int ll = 1; ll <= 4; ++ll) {
+            m.cn1[ll - 1] = ll <= m.tq1 ? g.cell_node(ll, a1) : 0;
+            m.cn2[ll - 1] = ll <= m.tq2 ? g.cell_node(ll, a2) : 0;
+        }
     }
-    const R spin = (R)f.scal[2];
+    m.spin = (R)f.scal[2];
+    return true;
+}
+
+// :120-169, row r (0 = top) of the column's tridiagonal matrix
+template <typename R>
+__device__ __forceinline__ void momentum_matrix_row(const StateT<R> &s, const MomFace<R> &m, int L, int r, R &a,
+                                                    R &bd, R &cu) {
+    const int j = m.j, tj = m.tj, bj = m.bj;
+    if (m.nvl == 1) {
+        bd = s.dz_face[ix(tj, j, L)] + m.gbdt;
+    } else if (r == 0) {
+        cu = -m.dtR * s.av[ix0(tj - 1, j, L)] / s.dzhalf_face[ix0(tj - 1, j, L)];
+        bd = m.gtdt + s.dz_face[ix(tj, j, L)] - cu;
+    } else if (r == m.nvl - 1) {
+        a = -m.dtR * s.av[ix0(bj, j, L)] / s.dzhalf_face[ix0(bj, j, L)];
+        bd = -a + s.dz_face[ix(bj, j, L)] + m.gbdt;
+    } else {
+        const int k = tj - r;
+        a = -m.dtR * s.av[ix0(k, j, L)] / s.dzhalf_face[ix0(k, j, L)];
+        cu = -m.dtR * s.av[ix0(k - 1, j, L)] / s.dzhalf_face[ix0(k - 1, j, L)];
+        bd = -a + s.dz_face[ix(k, j, L)] - cu;
+    }
+}
+
+// :254-551, right-hand sides of top-down row k (1-based; layer tj - k + 1); writes Kh of the row
+template <typename R>
+__device__ __forceinline__ void momentum_row(const Geom &g, const StateT<R> &s, const Params &p, const MomFace<R> &m,
+                                             int L, int k, R &G1o, R &G2o, R &dzo) {
+    const int j = m.j, tj = m.tj;
+    const int kk = tj - k + 1;
     const R half = R(0.5);
-    for (int k = 1; k <= nvl; ++k) {
-        int kk = tj - k + 1;
-        R dzk = s.dz_face[ix(kk, j, L)];
-        R unk = s.un_face[ix(kk, j, L)], vnk = s.vn_face[ix(kk, j, L)];
-        R G1 = dzk * (s.un_elm[ix(kk, j, L)] + cordt * vnk);
-        R G2 = dzk * (s.vn_elm[ix(kk, j, L)] - cordt * unk);
-        if (a2 != 0) {
-            // :269-344 Smagorinsky horizontal diffusion
-            R tmp[12];
-            for (int l = 1; l <= 2; ++l) {
-                int nd = g.face_node(l, j);
-                R ut = (s.u_node[ix0(kk, nd, L)] + s.u_node[ix0(kk - 1, nd, L)]) * half;
-                R vt = (s.v_node[ix0(kk, nd, L)] + s.v_node[ix0(kk - 1, nd, L)]) * half;
-                tmp[2 * l - 2] = ut * ctR + vt * snR;
-                tmp[2 * l - 1] = -ut * snR + vt * ctR;
-            }
-            for (int l = 1; l <= 2; ++l) {
-                int ie = l == 1 ? a1 : a2;
-                int tq = l == 1 ? tq1 : tq2;
-                R itq = l == 1 ? inv_tq1 : inv_tq2;
-                R ut = R(0), vt = R(0);
-                for (int ll = 1; ll <= tq; ++ll) {
-                    int nd = g.cell_node(ll, ie);
-                    R uu = (s.u_node[ix0(kk, nd, L)] + s.u_node[ix0(kk - 1, nd, L)]) * half;
-                    R vv = (s.v_node[ix0(kk, nd, L)] + s.v_node[ix0(kk - 1, nd, L)]) * half;
-                    ut = ut + (itq != R(0) ? uu * itq : uu / (R)tq);
-                    vt = vt + (itq != R(0) ? vv * itq : vv / (R)tq);
-                }
-                tmp[2 * l + 2] = ut * ctR + vt * snR;
-                tmp[2 * l + 3] = -ut * snR + vt * ctR;
-            }
-            R dudx = (tmp[6] - tmp[4]) / djR;
-            R dvdx = (tmp[7] - tmp[5]) / djR;
-            R dudy = (tmp[2] - tmp[0]) / flR;
-            R dvdy = (tmp[3] - tmp[1]) / flR;
-            R sdd = dvdx + dudy;
-            R hdiff = smag * sqrt(dudx * dudx + dvdy * dvdy + half * (sdd * sdd));
-            R khv = hdiff * area1;
-            hdiff = hdiff + ah0;
-            s.kh[ix(k, j, L)] = khv + kh0;
-            R d2udy = R(4) * (tmp[2] + tmp[0] - R(2) * unk) / fl2;
-            R d2vdy = R(4) * (tmp[3] + tmp[1] - R(2) * vnk) / fl2;
-            tmp[8] = (tmp[4] - unk) / rl1;
-            tmp[9] = (tmp[5] - vnk) / rl1;
-            tmp[10] = (tmp[6] - unk) / rl2;
-            tmp[11] = (tmp[7] - vnk) / rl2;
-            R d2udx = R(2) * (tmp[8] + tmp[10]) / djR;
-            R d2vdx = R(2) * (tmp[9] + tmp[11]) / djR;
-            G1 = G1 + dzk * dtR * hdiff * (d2udx + d2udy);
-            G2 = G2 + dzk * dtR * hdiff * (d2vdx + d2vdy);
+    const R ctR = m.ctR, snR = m.snR;
+    const R dtR = m.dtR, cordt = m.cordt;
+    R dzk = s.dz_face[ix(kk, j, L)];
+    R unk = s.un_face[ix(kk, j, L)], vnk = s.vn_face[ix(kk, j, L)];
+    R G1 = dzk * (s.un_elm[ix(kk, j, L)] + cordt * vnk);
+    R G2 = dzk * (s.vn_elm[ix(kk, j, L)] - cordt * unk);
+    if (m.a2 != 0) {
+        // :269-344 Smagorinsky horizontal diffusion
+        R tmp[12];
+        for (int l = 1; l <= 2; ++l) {
+            int nd = l == 1 ? m.node1 : m.node2;
+            R ut = (s.u_node[ix0(kk, nd, L)] + s.u_node[ix0(kk - 1, nd, L)]) * half;
+            R vt = (s.v_node[ix0(kk, nd, L)] + s.v_node[ix0(kk - 1, nd, L)]) * half;
+            tmp[2 * l - 2] = ut * ctR + vt * snR;
+            tmp[2 * l - 1] = -ut * snR + vt * ctR;
         }
-        // :350-397 barotropic gradients at (1-theta)
-        if (btype >= 0) G1 = G1 - dzk * bt1;
-        else G1 = R(0);
-        if (wet_nodes) G2 = G2 - dzk * along;
-        // :400-471 baroclinic pressure gradient (density differences formed in FP64)
-        if (p.baroclinic_flag == 1) {
-            R sum1 = R(0), sum2 = R(0);
-            for (int k2 = kk; k2 <= tj; ++k2) {
-                R dz2 = s.dz_face[ix(k2, j, L)];
-                if (a2 != 0 && k2 >= ba1 && k2 <= ta1 && k2 >= ba2 && k2 <= ta2) {
-                    R dr = (R)(s.rho_cell[ix(k2, a2, L)] - s.rho_cell[ix(k2, a1, L)]);
-                    sum1 = sum1 + (k2 == kk ? half * dr : dr) * dz2;
-                }
-                if (k2 >= bn1 && k2 <= tn1 && k2 >= bn2 && k2 <= tn2) {
-                    R dr = (R)(s.rho_node[ix(k2, node2, L)] - s.rho_node[ix(k2, node1, L)]);
-                    sum2 = sum2 + (k2 == kk ? half * dr : dr) * dz2;
-                }
+        for (int l = 1; l <= 2; ++l) {
+            int tq = l == 1 ? m.tq1 : m.tq2;
+            R itq = l == 1 ? m.inv_tq1 : m.inv_tq2;
+            R ut = R(0), vt = R(0);
+#pragma unroll
+            for (int ll = 1; ll <= 4; ++ll) {
+                if (ll > tq) break;
+                int nd = l == 1 ? m.cn1[ll - 1] : m.cn2[ll - 1];
+                R uu = (s.u_node[ix0(kk, nd, L)] + s.u_node[ix0(kk - 1, nd, L)]) * half;
+                R vv = (s.v_node[ix0(kk, nd, L)] + s.v_node[ix0(kk - 1, nd, L)]) * half;
+                ut = ut + (itq != R(0) ? uu * itq : uu / (R)tq);
+                vt = vt + (itq != R(0) ? vv * itq : vv / (R)tq);
             }
-            R dzrow = s.dz_face[ix(k, j, L)];   // the reference uses the top-down row here
-            R rtemp1 = dzrow * bc_dj * sum1;
-            R rtemp2 = dzrow * bc_fl * sum2;
-            R rtemp3 = rtemp1 * ct2R;
-            R rtemp4 = rtemp1 * sn2R;
-            G1 = G1 + rtemp3 * spin;
-            G2 = G2 + (rtemp2 + rtemp4) * spin;
+            tmp[2 * l + 2] = ut * ctR + vt * snR;
+            tmp[2 * l + 3] = -ut * snR + vt * ctR;
         }
-        if (k == 1) {
-            G1 = G1 + wsn;
-            G2 = G2 + wst;
-        }
-        // :485-486 tide-generating potential, zero in this build (kept for the signed-zero result)
-        G1 = G1 + c069 * dzk * gdt0 * R(0);
-        G2 = G2 + c069 * dzk * gdt0 * R(0);
-        // :490-509 air pressure
-        G1 = G1 + dzk * air1;
-        G2 = G2 + dzk * air2;
-        if (btype == -1) G1 = R(0);
-        if (ibnd > 0) G1 = G1 + dzk * qub;
-        rhs[k - 1][0] = G1;
-        rhs[k - 1][1] = G2;
-        rhs[k - 1][2] = dzk;
+        R dudx = (tmp[6] - tmp[4]) / m.djR;
+        R dvdx = (tmp[7] - tmp[5]) / m.djR;
+        R dudy = (tmp[2] - tmp[0]) / m.flR;
+        R dvdy = (tmp[3] - tmp[1]) / m.flR;
+        R sdd = dvdx + dudy;
+        R hdiff = m.smag * sqrt(dudx * dudx + dvdy * dvdy + half * (sdd * sdd));
+        R khv = hdiff * m.area1;
+        hdiff = hdiff + m.ah0;
+        s.kh[ix(k, j, L)] = khv + m.kh0;
+        R d2udy = R(4) * (tmp[2] + tmp[0] - R(2) * unk) / m.fl2;
+        R d2vdy = R(4) * (tmp[3] + tmp[1] - R(2) * vnk) / m.fl2;
+        tmp[8] = (tmp[4] - unk) / m.rl1;
+        tmp[9] = (tmp[5] - vnk) / m.rl1;
+        tmp[10] = (tmp[6] - unk) / m.rl2;
+        tmp[11] = (tmp[7] - vnk) / m.rl2;
+        R d2udx = R(2) * (tmp[8] + tmp[10]) / m.djR;
+        R d2vdx = R(2) * (tmp[9] + tmp[11]) / m.djR;
+        G1 = G1 + dzk * dtR * hdiff * (d2udx + d2udy);
+        G2 = G2 + dzk * dtR * hdiff * (d2vdx + d2vdy);
     }
+    // :350-397 barotropic gradients at (1-theta)
+    if (m.btype >= 0) G1 = G1 - dzk * m.bt1;
+    else G1 = R(0);
+    if (m.wet_nodes) G2 = G2 - dzk * m.along;
+    // :400-471 baroclinic pressure gradient (density differences formed in FP64)
+    if (p.baroclinic_flag == 1) {
+        R sum1 = R(0), sum2 = R(0);
+        for (int k2 = kk; k2 <= tj; ++k2) {
+            R dz2 = s.dz_face[ix(k2, j, L)];
+            if (m.a2 != 0 && k2 >= m.ba1 && k2 <= m.ta1 && k2 >= m.ba2 && k2 <= m.ta2) {
+                R dr = (R)(s.rho_cell[ix(k2, m.a2, L)] - s.rho_cell[ix(k2, m.a1, L)]);
+                sum1 = sum1 + (k2 == kk ? half * dr : dr) * dz2;
+            }
+            if (k2 >= m.bn1 && k2 <= m.tn1 && k2 >= m.bn2 && k2 <= m.tn2) {
+                R dr = (R)(s.rho_node[ix(k2, m.node2, L)] - s.rho_node[ix(k2, m.node1, L)]);
+                sum2 = sum2 + (k2 == kk ? half * dr : dr) * dz2;
+            }
+        }
+        R dzrow = s.dz_face[ix(k, j, L)];   // the reference uses the top-down row here
+        R rtemp1 = dzrow * m.bc_dj * sum1;
+        R rtemp2 = dzrow * m.bc_fl * sum2;
+        R rtemp3 = rtemp1 * m.ct2R;
+        R rtemp4 = rtemp1 * m.sn2R;
+        G1 = G1 + rtemp3 * m.spin;
+        G2 = G2 + (rtemp2 + rtemp4) * m.spin;
+    }
+    if (k == 1) {
+        G1 = G1 + m.wsn;
+        G2 = G2 + m.wst;
+    }
+    // :485-486 tide-generating potential, zero in this build (kept for the signed-zero result)
+    G1 = G1 + m.c069 * dzk * m.gdt0 * R(0);
+    G2 = G2 + m.c069 * dzk * m.gdt0 * R(0);
+    // :490-509 air pressure
+    G1 = G1 + dzk * m.air1;
+    G2 = G2 + dzk * m.air2;
+    if (m.btype == -1) G1 = R(0);
+    if (m.ibnd > 0) G1 = G1 + dzk * m.qub;
+    G1o = G1;
+    G2o = G2;
+    dzo = dzk;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_momentum(Geom g, StateT<R> s, Forcing f, Params p, gom_status *st) {
+    unsigned tid = flat_tid();
+    if (tid >= (unsigned)g.NF) return;
+    const int j = column_entity<R>(g.face_order, tid);
+    const int L = g.L;
+    MomFace<R> m;
+    if (!momentum_setup(g, s, f, p, j, m)) return;
+    const int nvl = m.nvl;
+    R a[GOM_MAXL], bd[GOM_MAXL], cu[GOM_MAXL], gam[GOM_MAXL];
+    R rhs[GOM_MAXL][3];
+    for (int r = 0; r < nvl; ++r) momentum_matrix_row(s, m, L, r, a[r], bd[r], cu[r]);
+    for (int k = 1; k <= nvl; ++k) momentum_row(g, s, p, m, L, k, rhs[k - 1][0], rhs[k - 1][1], rhs[k - 1][2]);
     if (!thomas<3>(nvl, a, bd, cu, rhs, gam)) {
         record_error(st, GOM_E_ZERO_PIVOT, 587, j, 0, 0.0);
         return;
     }
-    bool zero_g1 = (btype == -1 && ibnd == 0);
-    bool zero_dz1 = (btype == -1);
+    const bool zero_g1 = (m.btype == -1 && m.ibnd == 0);
+    const bool zero_dz1 = (m.btype == -1);
     for (int k = 1; k <= L; ++k) {
         long o = ix(k, j, L);
         if (k <= nvl) {
@@ -1104,6 +1392,102 @@ __global__ void __launch_bounds__(256) k_momentum(Geom g, StateT<R> s, Forcing f
     }
 }
 
+// FP32 path, the same columns by tiles: a block takes MT_TILE consecutive faces; the per-face
+// setup is formed once per face into shared memory, every (face, row) slot forms its matrix row
+// and right-hand sides in its own thread (neighbouring lanes read neighbouring layers of the same
+// columns and nodes), one thread per face runs the Thomas sweeps in shared memory, and the block
+// writes its (L, face) tile of the four outputs coalesced.  Same values as k_momentum<float>.
+constexpr int MT_TILE = 32;
+constexpr int MT_ARRAYS = 7;   // a, bd, cu, gam and the three right-hand sides, MT_TILE x L each
+
+inline size_t momentum_tile_smem(int L) { return (size_t)MT_ARRAYS * MT_TILE * L * sizeof(float); }
+
+__global__ void __launch_bounds__(256) k_momentum_tile(Geom g, StateT<float> s, Forcing f, Params p, gom_status *st) {
+    extern __shared__ float msm[];
+    __shared__ MomFace<float> mf[MT_TILE];
+    __shared__ int ok_s[MT_TILE];
+    const int L = g.L;
+    const int j0 = blockIdx.x * MT_TILE;
+    const int nf = min(MT_TILE, g.NF - j0);
+    for (int c = threadIdx.x; c < nf; c += blockDim.x) {
+        MomFace<float> m;
+        ok_s[c] = momentum_setup(g, s, f, p, j0 + c + 1, m) ? 1 : 0;
+        mf[c] = m;
+    }
+    __syncthreads();
+    const int TL = MT_TILE * L;
+    float *A = msm, *B = A + TL, *C = B + TL, *GM = C + TL, *R0 = GM + TL, *R1 = R0 + TL, *R2 = R1 + TL;
+    for (int t = threadIdx.x; t < nf * L; t += blockDim.x) {
+        const int c = t / L, r = t - c * L;
+        if (!ok_s[c] || r >= mf[c].nvl) continue;
+        const int q = c * L + r;
+        momentum_matrix_row(s, mf[c], L, r, A[q], B[q], C[q]);
+        momentum_row(g, s, p, mf[c], L, r + 1, R0[q], R1[q], R2[q]);
+    }
+    __syncthreads();
+    for (int c = threadIdx.x; c < nf; c += blockDim.x) {
+        if (!ok_s[c]) continue;
+        const int n = mf[c].nvl, q = c * L;
+        // thomas<3> on the shared rows
+        bool good = B[q] != 0.0f;
+        if (good) {
+            float den = B[q];
+            R0[q] = R0[q] / den;
+            R1[q] = R1[q] / den;
+            R2[q] = R2[q] / den;
+            for (int jr = 1; jr < n; ++jr) {
+                const float gm = C[q + jr - 1] / den;
+                GM[q + jr] = gm;
+                den = B[q + jr] - A[q + jr] * gm;
+                if (den == 0.0f) {
+                    good = false;
+                    break;
+                }
+                const float aj = A[q + jr];
+                R0[q + jr] = (R0[q + jr] - aj * R0[q + jr - 1]) / den;
+                R1[q + jr] = (R1[q + jr] - aj * R1[q + jr - 1]) / den;
+                R2[q + jr] = (R2[q + jr] - aj * R2[q + jr - 1]) / den;
+            }
+        }
+        if (good) {
+            for (int jr = n - 2; jr >= 0; --jr) {
+                const float gm = GM[q + jr + 1];
+                R0[q + jr] = R0[q + jr] - gm * R0[q + jr + 1];
+                R1[q + jr] = R1[q + jr] - gm * R1[q + jr + 1];
+                R2[q + jr] = R2[q + jr] - gm * R2[q + jr + 1];
+            }
+        } else {
+            record_error(st, GOM_E_ZERO_PIVOT, 587, mf[c].j, 0, 0.0);
+            ok_s[c] = 0;
+        }
+    }
+    __syncthreads();
+    const long base = (long)j0 * L;
+    for (int t = threadIdx.x; t < nf * L; t += blockDim.x) {
+        const int c = t / L, r = t - c * L;
+        if (!ok_s[c]) continue;   // dry faces: k_zero_face_columns; a failed solve writes nothing
+        const long o = base + t;
+        const MomFace<float> &m = mf[c];
+        if (r < m.nvl) {
+            const int q = c * L + r;
+            s.ainvg1[o] = (m.btype == -1 && m.ibnd == 0) ? 0.0f : R0[q];
+            s.ainvg2[o] = R1[q];
+            s.ainvdz1[o] = m.btype == -1 ? 0.0f : R2[q];
+            s.ainvdz2[o] = R2[q];
+        } else {
+            s.ainvg1[o] = 0.0f;
+            s.ainvg2[o] = 0.0f;
+            s.ainvdz1[o] = 0.0f;
+            s.ainvdz2[o] = 0.0f;
+        }
+    }
+}
+
+cudaError_t prepare_momentum_tile(int L) {
+    return cudaFuncSetAttribute(k_momentum_tile, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)momentum_tile_smem(L));
+}
+
 template <typename R> __global__ void k_zero_face_columns(Geom g, StateT<R> s) {
     // faces that are dry keep zero results (the reference zeroes all four arrays first)
     unsigned t = flat_tid();
@@ -1117,8 +1501,18 @@ template <typename R> __global__ void k_zero_face_columns(Geom g, StateT<R> s) {
     s.ainvdz2[t] = R(0);
 }
 
+// variants: one thread per column with 128 / 64 / 256 threads per block, or (FP32 contexts) the
+// tiled kernel; FP64 contexts run variant 3 as variant 0
 template <typename R> cudaError_t launch_momentum_columns_only(const LaunchT<R> &x) {
-    const int bs = x.tune[TUNE_MOMENTUM] == 1 ? 64 : x.tune[TUNE_MOMENTUM] == 2 ? 256 : 128;
+    const int v = x.tune[TUNE_MOMENTUM];
+    if constexpr (sizeof(R) == sizeof(float)) {
+        if (v == 3) {
+            k_momentum_tile<<<blocks_for(x.g.NF, MT_TILE), 256, momentum_tile_smem(x.g.L), x.stream>>>(
+                x.g, x.s, x.f, x.p, x.status);
+            return cudaGetLastError();
+        }
+    }
+    const int bs = v == 1 ? 64 : v == 2 ? 256 : 128;
     k_momentum<<<blocks_for(x.g.NF, bs), bs, 0, x.stream>>>(x.g, x.s, x.f, x.p, x.status);
     return cudaGetLastError();
 }
@@ -1126,9 +1520,7 @@ template <typename R> cudaError_t launch_momentum_columns_only(const LaunchT<R> 
 template <typename R> cudaError_t launch_momentum(const LaunchT<R> &x) {
     long nfl = (long)x.g.NF * x.g.L;
     k_zero_face_columns<<<blocks_for(nfl, 256), 256, 0, x.stream>>>(x.g, x.s);
-    const int bs = x.tune[TUNE_MOMENTUM] == 1 ? 64 : x.tune[TUNE_MOMENTUM] == 2 ? 256 : 128;
-    k_momentum<<<blocks_for(x.g.NF, bs), bs, 0, x.stream>>>(x.g, x.s, x.f, x.p, x.status);
-    return cudaGetLastError();
+    return launch_momentum_columns_only(x);
 }
 
 GOM_INSTANTIATE_LAUNCH(launch_bottom_friction)

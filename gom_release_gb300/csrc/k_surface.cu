@@ -15,13 +15,40 @@ namespace gom {
 // ============================================================================================
 // solve_free_surface_equation.f90:65-214: one thread per cell builds its 5-point row and RHS.
 // The system and its right-hand side are formed in FP64 whatever the storage type R.
-template <typename R>
-__global__ void k_fs_assemble(Geom g, StateT<R> s, Forcing f, Params p, double *sparsem, double *rhs, gom_status *st) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    if (i > g.NC) return;
+// Per-face column sums of the assembly (:66-130, :134-151, :185-212), formed once per face
+// instead of once per adjacent cell (same expressions in the same order, hence the same values):
+// fs = [gravity dt^2 theta^2 fl/dj * sum dz AinvDZ1, sum dz un, sum dz AinvG1] per face.
+template <typename R> __global__ void k_fs_face_sums(Geom g, StateT<R> s, Params p, double *fs) {
+    unsigned tid = flat_tid();
+    if (tid >= (unsigned)g.NF) return;
+    const int j = column_entity<R>(g.face_order, tid);
     const int L = g.L;
+    const int tj = s.top_face[j - 1];
+    double *o = fs + (long)(j - 1) * 3;
+    if (tj == 0) return;   // not read
     const double dt = p.dt, gravity = p.gravity, theta = p.theta;
     const double gdt2th2 = gravity * (dt * dt) * (theta * theta);
+    const int nvl = tj - g.bottom_face[j - 1] + 1;
+    double sdz = 0.0, c1 = 0.0, c2 = 0.0;
+    for (int k = 1; k <= nvl; ++k) {
+        const int kk = tj + 1 - k;
+        const double dz = s.dz_face[ix(kk, j, L)];
+        sdz = sdz + dz * (double)s.ainvdz1[ix(k, j, L)];
+        c1 = c1 + dz * (double)s.un_face[ix(kk, j, L)];
+        c2 = c2 + dz * (double)s.ainvg1[ix(k, j, L)];
+    }
+    o[0] = gdt2th2 * g.face_length[j - 1] / g.delta_j[j - 1] * sdz;
+    o[1] = c1;
+    o[2] = c2;
+}
+
+// solve_free_surface_equation.f90:65-212: matrix row and right-hand side of each cell
+template <typename R>
+__global__ void k_fs_assemble(Geom g, StateT<R> s, Forcing f, Params p, const double *fs, double *sparsem, double *rhs,
+                              gom_status *st) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (i > g.NC) return;
+    const double dt = p.dt, theta = p.theta;
     int tq = g.tri_or_quad[i - 1];
     double ar = g.area[i - 1];
     double diag = ar;
@@ -30,39 +57,20 @@ __global__ void k_fs_assemble(Geom g, StateT<R> s, Forcing f, Params p, double *
     int obf = g.ob_element_flag[i - 1];
     for (int l = 1; l <= tq; ++l) {
         int j = g.cell_face(l, i);
-        int tj = s.top_face[j - 1];
-        if (tj == 0) continue;
-        int nvl = tj - g.bottom_face[j - 1] + 1;
-        double sdz = 0.0, c1 = 0.0, c2 = 0.0;
-        for (int k = 1; k <= nvl; ++k) {
-            int kk = tj + 1 - k;
-            double dz = s.dz_face[ix(kk, j, L)];
-            sdz = sdz + dz * (double)s.ainvdz1[ix(k, j, L)];
-        }
-        double base = gdt2th2 * g.face_length[j - 1] / g.delta_j[j - 1] * sdz;
-        double coef = base * g.cos_theta2[j - 1];
+        if (s.top_face[j - 1] == 0) continue;
+        double coef = fs[(long)(j - 1) * 3] * g.cos_theta2[j - 1];
         if (coef < 0.0) {
             record_error(st, GOM_E_NOT_SPD, 100, i, 0, coef);
             return;
         }
         diag = diag + coef;
         if (g.cell_adj(l, i) != 0) off[l - 1] = -coef;
-        (void)c1;
-        (void)c2;
     }
     // RHS (:134-151), computed in a second pass like the reference
     for (int l = 1; l <= tq; ++l) {
         int j = g.cell_face(l, i);
-        int tj = s.top_face[j - 1];
-        if (tj == 0) continue;
-        int nvl = tj - g.bottom_face[j - 1] + 1;
-        double c1 = 0.0, c2 = 0.0;
-        for (int k = 1; k <= nvl; ++k) {
-            int kk = tj + 1 - k;
-            double dz = s.dz_face[ix(kk, j, L)];
-            c1 = c1 + dz * (double)s.un_face[ix(kk, j, L)];
-            c2 = c2 + dz * (double)s.ainvg1[ix(k, j, L)];
-        }
+        if (s.top_face[j - 1] == 0) continue;
+        const double c1 = fs[(long)(j - 1) * 3 + 1], c2 = fs[(long)(j - 1) * 3 + 2];
         double sgn = (double)g.cell_sign(l, i);
         double fl = g.face_length[j - 1];
         r = r - (1.0 - theta) * dt * sgn * fl * c1 - theta * dt * sgn * fl * c2;
@@ -71,15 +79,8 @@ __global__ void k_fs_assemble(Geom g, StateT<R> s, Forcing f, Params p, double *
     if (obf > 0) {
         for (int l = 1; l <= tq; ++l) {
             int j = g.cell_face(l, i);
-            int tj = s.top_face[j - 1];
-            if (g.boundary_type_of_face[j - 1] > 0 && tj != 0) {
-                int nvl = tj - g.bottom_face[j - 1] + 1;
-                double sdz = 0.0;
-                for (int k = 1; k <= nvl; ++k)
-                    sdz = sdz + (double)s.dz_face[ix(tj + 1 - k, j, L)] * (double)s.ainvdz1[ix(k, j, L)];
-                double base = gdt2th2 * g.face_length[j - 1] / g.delta_j[j - 1] * sdz;
-                r = r + base * f.eta_at_ob_new[obf - 1];
-            }
+            if (g.boundary_type_of_face[j - 1] > 0 && s.top_face[j - 1] != 0)
+                r = r + fs[(long)(j - 1) * 3] * f.eta_at_ob_new[obf - 1];
         }
     }
     double *row = sparsem + (long)(i - 1) * 5;
@@ -187,7 +188,9 @@ template <typename R> cudaError_t pcg_configure(LaunchT<R> &x, int device) {
 
 template <typename R> cudaError_t launch_free_surface(const LaunchT<R> &x) {
     const Geom &g = x.g;
-    k_fs_assemble<<<blocks_for(g.NC, 128), 128, 0, x.stream>>>(x.g, x.s, x.f, x.p, x.w.sparsem, x.w.rhs, x.status);
+    k_fs_face_sums<<<blocks_for(g.NF, 128), 128, 0, x.stream>>>(x.g, x.s, x.p, x.w.fs_sums);
+    k_fs_assemble<<<blocks_for(g.NC, 128), 128, 0, x.stream>>>(x.g, x.s, x.f, x.p, x.w.fs_sums, x.w.sparsem, x.w.rhs,
+                                                               x.status);
     cudaError_t e = cudaMemsetAsync(x.w.barrier, 0, 2 * sizeof(unsigned), x.stream);
     if (e != cudaSuccess) return e;
     cudaLaunchConfig_t cfg = {};
@@ -315,7 +318,7 @@ template <typename R> cudaError_t launch_free_surface(const LaunchT<R> &x) {
 template <typename R> __global__ void k_face_velocity(Geom g, StateT<R> s, Forcing f, Params p) {
     unsigned tid = flat_tid();
     if (tid >= (unsigned)g.NF) return;
-    int j = g.face_order[tid];
+    int j = column_entity<R>(g.face_order, tid);
     const int L = g.L;
     int tj = s.top_face[j - 1];
     if (tj == 0) {
@@ -378,11 +381,94 @@ template <typename R> __global__ void k_face_velocity(Geom g, StateT<R> s, Forci
     }
 }
 
+// FP32 path, the same per face: a block takes VT_TILE consecutive faces, forms each face's
+// FP64 elevation factors once into shared memory, then sweeps the block's (layer, face) tile --
+// contiguous in the (L, NF) arrays -- one thread per slot, so loads and stores are coalesced.
+// Values and operation order are those of k_face_velocity<float>.  A face with a dry node keeps
+// vn_face_new of its wet layers as it is (clamped at initially dry nodes), as the column kernel
+// does; the layers above the top copy the top layer's values.
+constexpr int VT_TILE = 64;
+
+__global__ void __launch_bounds__(256) k_face_velocity_tile(Geom g, StateT<float> s, Forcing f, Params p) {
+    __shared__ float cj_s[VT_TILE], cn_s[VT_TILE], ct2_s[VT_TILE], sn2_s[VT_TILE], qu_s[VT_TILE];
+    __shared__ int tj_s[VT_TILE], bj_s[VT_TILE], bt_s[VT_TILE], fl_s[VT_TILE];
+    const int j0 = blockIdx.x * VT_TILE;   // 0-based first face of the tile
+    const int nf = min(VT_TILE, g.NF - j0);
+    const int L = g.L;
+    for (int t = threadIdx.x; t < nf; t += blockDim.x) {
+        const int j = j0 + t + 1;
+        const int tj = s.top_face[j - 1];
+        tj_s[t] = tj;
+        bj_s[t] = g.bottom_face[j - 1];
+        if (tj == 0) continue;
+        const int n1 = g.face_node(1, j), n2 = g.face_node(2, j);
+        const int btype = g.boundary_type_of_face[j - 1];
+        const int a1 = g.face_cell(1, j), a2 = g.face_cell(2, j);
+        const bool wet = s.wetdry_node[n1 - 1] == 0 && s.wetdry_node[n2 - 1] == 0;
+        const bool init_dry = g.initial_wetdry_node[n1 - 1] == 1 || g.initial_wetdry_node[n2 - 1] == 1;
+        double dEta = 0.0;
+        if (btype == 0) dEta = s.eta_cell_new[a2 - 1] - s.eta_cell_new[a1 - 1];
+        else if (btype > 0) dEta = f.eta_at_ob_new[g.ob_element_flag[a1 - 1] - 1] - s.eta_cell_new[a1 - 1];
+        const double dEtaN = s.eta_node[n2 - 1] - s.eta_node[n1 - 1];
+        cj_s[t] = (float)(p.theta * p.gravity * p.dt / g.delta_j[j - 1] * dEta);
+        cn_s[t] = (float)(p.theta * p.gravity * p.dt / g.face_length[j - 1] * dEtaN);
+        ct2_s[t] = (float)g.cos_theta2[j - 1];
+        sn2_s[t] = (float)g.sin_theta2[j - 1];
+        bt_s[t] = btype;
+        const int ibnd = g.isflowside3[j - 1];
+        qu_s[t] = ibnd > 0 ? (float)s.qu_boundary[ibnd - 1] : 0.0f;
+        fl_s[t] = (wet ? 1 : 0) | (init_dry ? 2 : 0) | (ibnd > 0 ? 4 : 0);
+    }
+    __syncthreads();
+    const long base = (long)j0 * L;
+    for (int t = threadIdx.x; t < nf * L; t += blockDim.x) {
+        const int fi = t / L, kk = t - fi * L + 1;
+        const long o = base + t;
+        const int tj = tj_s[fi], bj = bj_s[fi];
+        if (tj == 0 || kk < bj) {
+            s.un_face_new[o] = 0.0f;
+            s.vn_face_new[o] = 0.0f;
+            continue;
+        }
+        const int kq = kk > tj ? tj : kk;       // layers above the top take the top layer's values
+        const long oq = base + (long)fi * L + (kq - 1);
+        const long orow = base + (long)fi * L + (tj - kq);   // top-down row tj + 1 - kq
+        const int btype = bt_s[fi], fl = fl_s[fi];
+        const float cj = cj_s[fi];
+        float un, rtemp2 = 0.0f;
+        if (btype == -1) {
+            un = 0.0f;
+        } else if (btype == 0) {
+            const float rtemp0 = cj * s.ainvdz1[orow];
+            const float rtemp1 = rtemp0 * ct2_s[fi];
+            rtemp2 = rtemp0 * sn2_s[fi];
+            un = s.ainvg1[orow] - rtemp1;
+        } else {
+            const float rtemp0 = cj * s.ainvdz1[orow];
+            un = s.ainvg1[orow] - rtemp0;
+        }
+        if (fl & 4) un = qu_s[fi];
+        s.un_face_new[o] = un;
+        float vn;
+        bool write_v = true;
+        if (fl & 1) {
+            const float rtemp1 = cn_s[fi] * s.ainvdz2[orow];
+            if (btype == 0) vn = s.ainvg2[orow] - (rtemp1 + rtemp2);
+            else vn = s.ainvg2[orow] - rtemp1;
+        } else {
+            vn = s.vn_face_new[oq];   // kept from before
+            write_v = kk != kq || (fl & 2);
+        }
+        if (fl & 2) vn = fmaxf(-5.0f, fminf(vn, 5.0f));
+        if (write_v) s.vn_face_new[o] = vn;
+    }
+}
+
 // solve_velocities.f90:191-258: one thread per cell column
 template <typename R> __global__ void k_cell_w(Geom g, StateT<R> s) {
     unsigned tid = flat_tid();
     if (tid >= (unsigned)g.NC) return;
-    int i = g.cell_order[tid];
+    int i = column_entity<R>(g.cell_order, tid);
     const int L = g.L;
     int t = s.top_cell[i - 1], b = g.bottom_cell[i - 1];
     if (t == 0) {
@@ -415,9 +501,76 @@ template <typename R> __global__ void k_cell_w(Geom g, StateT<R> s) {
     for (int k = t + 1; k <= L; ++k) s.wn_cell_new[ix0(k, i, L)] = w;
 }
 
+// FP32 path, the same per cell: a block takes VT_TILE consecutive cells; each (cell, layer) slot
+// forms its face-flux sum divided by the area in one thread, each cell integrates its column
+// upwards in shared memory in the column kernel's order, and the block writes its (0:L, cell)
+// tile with coalesced stores.
+__global__ void __launch_bounds__(256) k_cell_w_tile(Geom g, StateT<float> s) {
+    __shared__ float inc[VT_TILE][GOM_MAXL + 1];
+    __shared__ float fsl_s[VT_TILE][4];
+    __shared__ int fj_s[VT_TILE][4], fb_s[VT_TILE][4], ft_s[VT_TILE][4];
+    __shared__ int t_s[VT_TILE], b_s[VT_TILE], tq_s[VT_TILE];
+    __shared__ float ar_s[VT_TILE];
+    const int i0 = blockIdx.x * VT_TILE;
+    const int nc = min(VT_TILE, g.NC - i0);
+    const int L = g.L;
+    for (int c = threadIdx.x; c < nc; c += blockDim.x) {
+        const int i = i0 + c + 1;
+        const int t = s.top_cell[i - 1];
+        t_s[c] = t;
+        b_s[c] = g.bottom_cell[i - 1];
+        const int tq = g.tri_or_quad[i - 1];
+        tq_s[c] = tq;
+        ar_s[c] = (float)g.area[i - 1];
+        for (int l = 1; l <= tq; ++l) {
+            const int jt = g.cell_face(l, i);
+            fj_s[c][l - 1] = jt;
+            fb_s[c][l - 1] = g.bottom_face[jt - 1];
+            ft_s[c][l - 1] = s.top_face[jt - 1];
+            fsl_s[c][l - 1] = (float)((double)g.cell_sign(l, i) * g.face_length[jt - 1]);
+        }
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < nc * L; t += blockDim.x) {
+        const int c = t / L, k = t - c * L + 1;
+        if (t_s[c] == 0 || k < b_s[c] || k > t_s[c]) continue;
+        float sum1 = 0.0f;
+        for (int l = 0; l < tq_s[c]; ++l) {
+            if (k >= fb_s[c][l] && k <= ft_s[c][l]) {
+                const long of = (long)(fj_s[c][l] - 1) * L + (k - 1);
+                sum1 = sum1 + fsl_s[c][l] * s.dz_face[of] * s.un_face_new[of];
+            }
+        }
+        inc[c][k] = sum1 / ar_s[c];
+    }
+    __syncthreads();
+    for (int c = threadIdx.x; c < nc; c += blockDim.x) {
+        if (t_s[c] == 0) continue;
+        float w = 0.0f;
+        for (int k = b_s[c]; k <= t_s[c]; ++k) {
+            w = w - inc[c][k];
+            inc[c][k] = w;
+        }
+    }
+    __syncthreads();
+    const long base = (long)i0 * (L + 1);
+    for (int t = threadIdx.x; t < nc * (L + 1); t += blockDim.x) {
+        const int c = t / (L + 1), k = t - c * (L + 1);
+        const int tt = t_s[c], bb = b_s[c];
+        float v = 0.0f;
+        if (tt != 0 && k >= bb) v = inc[c][k > tt ? tt : k];
+        s.wn_cell_new[base + t] = v;
+    }
+}
+
 template <typename R> cudaError_t launch_velocities(const LaunchT<R> &x) {
-    k_face_velocity<<<blocks_for(x.g.NF, 128), 128, 0, x.stream>>>(x.g, x.s, x.f, x.p);
-    k_cell_w<<<blocks_for(x.g.NC, 128), 128, 0, x.stream>>>(x.g, x.s);
+    if constexpr (sizeof(R) == sizeof(float)) {
+        k_face_velocity_tile<<<blocks_for(x.g.NF, VT_TILE), 256, 0, x.stream>>>(x.g, x.s, x.f, x.p);
+        k_cell_w_tile<<<blocks_for(x.g.NC, VT_TILE), 256, 0, x.stream>>>(x.g, x.s);
+    } else {
+        k_face_velocity<<<blocks_for(x.g.NF, 128), 128, 0, x.stream>>>(x.g, x.s, x.f, x.p);
+        k_cell_w<<<blocks_for(x.g.NC, 128), 128, 0, x.stream>>>(x.g, x.s);
+    }
     return cudaGetLastError();
 }
 

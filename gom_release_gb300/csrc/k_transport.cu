@@ -840,7 +840,7 @@ __global__ void __launch_bounds__(256) k_tr_thomas_col(TArgs<float> a) {
     const Geom &g = a.g;
     unsigned tid = flat_tid();
     if (tid >= (unsigned)g.NC) return;
-    const int i = g.cell_order[tid];
+    const int i = column_entity<float>(g.cell_order, tid);
     const int L = g.L, NC = g.NC;
     const int tl = a.s.top_cell[i - 1], b = g.bottom_cell[i - 1];
     if (tl == 0) {
@@ -885,7 +885,7 @@ template <typename R> __global__ void k_tr_nodes(TArgs<R> a) {
     unsigned tid = flat_tid();
     const Geom &g = a.g;
     if (tid >= (unsigned)g.NN) return;
-    int i = g.node_order[tid];
+    int i = column_entity<R>(g.node_order, tid);
     const int L = g.L, NC = g.NC;
     int tn = a.s.top_node[i - 1], bn = g.bottom_node[i - 1];
     int na = g.adj_cells_at_node[i - 1];
@@ -914,6 +914,79 @@ template <typename R> __global__ void k_tr_nodes(TArgs<R> a) {
             if (write) dst[ix(k, i, L)] = v;
             above = v;
         }
+    }
+}
+
+// FP32 path, the same per node: a block takes NT_TILE consecutive nodes, gathers each node's
+// adjacent cells once into shared memory, forms every (node, layer) average in its own thread
+// (neighbouring lanes read neighbouring layers of the same cells), resolves the fill from above
+// per node in the column kernel's order, and writes the block's (L, node) tile coalesced.
+constexpr int NT_TILE = 32;
+
+__global__ void __launch_bounds__(256) k_tr_nodes_tile(TArgs<float> a) {
+    __shared__ float col[NT_TILE][GOM_MAXL + 2];
+    __shared__ unsigned char fill[NT_TILE][GOM_MAXL + 2];
+    __shared__ int cell_s[NT_TILE][GOM_MAXNB], cb_s[NT_TILE][GOM_MAXNB], ct_s[NT_TILE][GOM_MAXNB];
+    __shared__ float car_s[NT_TILE][GOM_MAXNB];
+    __shared__ int tn_s[NT_TILE], bn_s[NT_TILE], na_s[NT_TILE];
+    const Geom &g = a.g;
+    const int L = g.L, NC = g.NC;
+    const int i0 = blockIdx.x * NT_TILE;
+    const int nn = min(NT_TILE, g.NN - i0);
+    for (int c = threadIdx.x; c < nn; c += blockDim.x) {
+        const int i = i0 + c + 1;
+        tn_s[c] = a.s.top_node[i - 1];
+        bn_s[c] = g.bottom_node[i - 1];
+        const int na = g.adj_cells_at_node[i - 1];
+        na_s[c] = na;
+        for (int l = 1; l <= na; ++l) {
+            const int ii = g.node_cell(l, i);
+            cell_s[c][l - 1] = ii;
+            cb_s[c][l - 1] = g.bottom_cell[ii - 1];
+            ct_s[c][l - 1] = a.s.top_cell[ii - 1];
+            car_s[c][l - 1] = (float)g.area[ii - 1];
+        }
+    }
+    __syncthreads();
+    const long base = (long)i0 * L;
+    for (int tr = 0; tr < a.ntr; ++tr) {
+        if (a.tid[tr] > a.ntr) continue;   // slot 1 -> salinity, slot 2 -> temperature
+        float *dst = a.tid[tr] == 1 ? a.s.salt_node : a.s.temp_node;
+        for (int t = threadIdx.x; t < nn * L; t += blockDim.x) {
+            const int c = t / L, k = t - c * L + 1;
+            const int tn = tn_s[c];
+            float v = 0.0f;
+            bool f = false;
+            if (tn != 0 && k <= tn && k >= bn_s[c]) {
+                float s11 = 0.0f, s22 = 0.0f;
+                int count1 = 0;
+                const int na = na_s[c];
+                for (int l = 0; l < na; ++l) {
+                    const int ii = cell_s[c][l];
+                    if (k >= cb_s[c][l] && k <= ct_s[c][l]) {
+                        const float w = car_s[c][l] * a.s.dz_cell_new[ix(k, ii, L)];
+                        s11 = s11 + w;
+                        s22 = s22 + w * a.con[ic(k, ii, tr, L, NC)];
+                    } else {
+                        count1 = count1 + 1;
+                    }
+                }
+                v = s11 == 0.0f ? 0.0f : s22 / s11;
+                f = count1 == na && k != tn;
+            }
+            col[c][k] = v;
+            fill[c][k] = f;
+        }
+        __syncthreads();
+        for (int c = threadIdx.x; c < nn; c += blockDim.x)
+            for (int k = tn_s[c] - 1; k >= 1; --k)
+                if (fill[c][k]) col[c][k] = col[c][k + 1];
+        __syncthreads();
+        for (int t = threadIdx.x; t < nn * L; t += blockDim.x) {
+            const int c = t / L, k = t - c * L + 1;
+            dst[base + t] = col[c][k];
+        }
+        __syncthreads();
     }
 }
 
@@ -1063,7 +1136,10 @@ template <typename R> cudaError_t launch_transport(const LaunchT<R> &x) {
         nxt = t;
     }
     a.con = cur;
-    k_tr_nodes<<<blocks_for(g.NN, 128), 128, 0, x.stream>>>(a);
+    if constexpr (sizeof(R) == sizeof(float))
+        k_tr_nodes_tile<<<blocks_for(g.NN, NT_TILE), 256, 0, x.stream>>>(a);
+    else
+        k_tr_nodes<<<blocks_for(g.NN, 128), 128, 0, x.stream>>>(a);
     long n = (long)g.NF * L + (long)g.NC * L;
     k_tr_faces_cells<<<blocks_for(n, 256), 256, 0, x.stream>>>(a);
     return cudaGetLastError();
@@ -1104,7 +1180,7 @@ __global__ void k_density_col(Geom g, StateT<R> s, Params p, gom_status *st) {
     unsigned tid = flat_tid();
     int n = KIND == 0 ? g.NN : g.NF;
     if (tid >= (unsigned)n) return;
-    int e = KIND == 0 ? g.node_order[tid] : g.face_order[tid];
+    int e = column_entity<R>(KIND == 0 ? g.node_order : g.face_order, tid);
     const int L = g.L;
     int t = KIND == 0 ? s.top_node[e - 1] : s.top_face[e - 1];
     if (t == 0) return;
@@ -1151,7 +1227,7 @@ __global__ void k_density_col(Geom g, StateT<R> s, Params p, gom_status *st) {
 template <typename R> __global__ void k_density_cells(Geom g, StateT<R> s, gom_status *st) {
     unsigned tid = flat_tid();
     if (tid >= (unsigned)g.NC) return;
-    int i = g.cell_order[tid];
+    int i = column_entity<R>(g.cell_order, tid);
     const int L = g.L;
     int t = s.top_cell[i - 1];
     if (t == 0) return;
@@ -1197,7 +1273,7 @@ template <typename R> cudaError_t launch_density(const LaunchT<R> &x) {
 template <typename R> __global__ void k_turbulence_faces(Geom g, StateT<R> s, Params p, R *kvf) {
     unsigned tid = flat_tid();
     if (tid >= (unsigned)g.NF) return;
-    int i = g.face_order[tid];
+    int i = column_entity<R>(g.face_order, tid);
     const int L = g.L;
     int t = s.top_face[i - 1];
     if (t == 0) return;
@@ -1253,7 +1329,7 @@ template <typename R> __global__ void k_turbulence_faces(Geom g, StateT<R> s, Pa
 template <typename R> __global__ void k_turbulence_cells(Geom g, StateT<R> s, const R *kvf) {
     unsigned tid = flat_tid();
     if (tid >= (unsigned)g.NC) return;
-    int i = g.cell_order[tid];
+    int i = column_entity<R>(g.cell_order, tid);
     const int L = g.L;
     int t = s.top_cell[i - 1];
     if (t == 0) return;
