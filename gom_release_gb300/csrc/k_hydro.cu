@@ -406,7 +406,16 @@ __device__ int walk_f32(const Geom &g, const StateT<R> &s, int &nnel, double tim
         const double dist = sqrt((xi - xt) * (xi - xt) + (yi - yt) * (yi - yt));
         zt = zt - dist / pathl0 * (zt - z0);
     };
-    float trm = (float)time;
+    // FP64 distance from the crossing on edge l of element el to the foot (the reference's dist)
+    auto dist64 = [&](int el, int l) {
+        const int q = g.tri_or_quad[el - 1];
+        const int jd1 = g.cell_node(start_end_node(q, l, 1), el), jd2 = g.cell_node(start_end_node(q, l, 2), el);
+        double xi = 0.0, yi = 0.0;
+        check_intersection(xcg, xt, g.x_node[jd1 - 1], g.x_node[jd2 - 1], ycg, yt, g.y_node[jd1 - 1],
+                           g.y_node[jd2 - 1], xi, yi);
+        return sqrt((xi - xt) * (xi - xt) + (yi - yt) * (yi - yt));
+    };
+    int prev_el = 0, prev_l = 0;   // the previous crossing (none: the remaining path is pathl0)
     int iteration = 0;
     for (;;) {
         iteration = iteration + 1;
@@ -423,12 +432,18 @@ __device__ int walk_f32(const Geom &g, const StateT<R> &s, int &nnel, double tim
         const int tqn = e.tq;
         const int md1 = g.cell_node(start_end_node(tqn, nel_j, 1), nel);
         const int md2 = g.cell_node(start_end_node(tqn, nel_j, 2), nel);
+        // the reference's checks of the remaining path (:199-222): the FP32 lengths lose accuracy
+        // on paths nearly along an edge, so a check they fail is repeated with FP64 crossings
         const float dist = sqrtf((xin - tx) * (xin - tx) + (yin - ty) * (yin - ty));
-        const float ratio = dist / pathl;
-        if (ratio > 1.0f + 1.0e-4f) return GOM_ELM_OVERSHOOT;
-        trm = trm * dist / pathl;
+        if (dist > pathl * (1.0f + 0.5e-4f) || dist == 0.0f) {
+            const double d = dist64(nel, nel_j);
+            const double dprev = prev_el ? dist64(prev_el, prev_l) : pathl0;
+            if (d / dprev > 1.0 + 1.0e-4) return GOM_ELM_OVERSHOOT;
+            if (d == 0.0 || time * d / pathl0 == 0.0) return GOM_ELM_ZERO_REMAIN;
+        }
         pathl = dist;
-        if (pathl == 0.0f || trm == 0.0f) return GOM_ELM_ZERO_REMAIN;
+        prev_el = nel;
+        prev_l = nel_j;
         const int adjc = g.cell_adj(nel_j, nel);
         if (adjc == 0 || top_el(s, adjc) == 0) {
             const int isd = g.cell_face(nel_j, nel);
@@ -1366,23 +1381,51 @@ __global__ void __launch_bounds__(256) k_momentum(Geom g, StateT<R> s, Forcing f
     MomFace<R> m;
     if (!momentum_setup(g, s, f, p, j, m)) return;
     const int nvl = m.nvl;
-    R a[GOM_MAXL], bd[GOM_MAXL], cu[GOM_MAXL], gam[GOM_MAXL];
-    R rhs[GOM_MAXL][3];
-    for (int r = 0; r < nvl; ++r) momentum_matrix_row(s, m, L, r, a[r], bd[r], cu[r]);
-    for (int k = 1; k <= nvl; ++k) momentum_row(g, s, p, m, L, k, rhs[k - 1][0], rhs[k - 1][1], rhs[k - 1][2]);
-    if (!thomas<3>(nvl, a, bd, cu, rhs, gam)) {
-        record_error(st, GOM_E_ZERO_PIVOT, 587, j, 0, 0.0);
-        return;
+    // thomas<3> with each row's matrix entries and right-hand sides formed as its forward
+    // elimination step reaches it (the same operations in the same order; only the elimination
+    // factors and partial solutions are kept)
+    R gam[GOM_MAXL], sol[GOM_MAXL][3];
+    R den = R(0), cu_prev = R(0);
+    for (int r = 0; r < nvl; ++r) {
+        R a_r = R(0), bd_r = R(0), cu_r = R(0), g1, g2, dzr;
+        momentum_matrix_row(s, m, L, r, a_r, bd_r, cu_r);
+        momentum_row(g, s, p, m, L, r + 1, g1, g2, dzr);
+        if (r == 0) {
+            if (bd_r == R(0)) {
+                record_error(st, GOM_E_ZERO_PIVOT, 587, j, 0, 0.0);
+                return;
+            }
+            den = bd_r;
+            sol[0][0] = g1 / den;
+            sol[0][1] = g2 / den;
+            sol[0][2] = dzr / den;
+        } else {
+            gam[r] = cu_prev / den;
+            den = bd_r - a_r * gam[r];
+            if (den == R(0)) {
+                record_error(st, GOM_E_ZERO_PIVOT, 587, j, 0, 0.0);
+                return;
+            }
+            sol[r][0] = (g1 - a_r * sol[r - 1][0]) / den;
+            sol[r][1] = (g2 - a_r * sol[r - 1][1]) / den;
+            sol[r][2] = (dzr - a_r * sol[r - 1][2]) / den;
+        }
+        cu_prev = cu_r;
+    }
+    for (int r = nvl - 2; r >= 0; --r) {
+        sol[r][0] = sol[r][0] - gam[r + 1] * sol[r + 1][0];
+        sol[r][1] = sol[r][1] - gam[r + 1] * sol[r + 1][1];
+        sol[r][2] = sol[r][2] - gam[r + 1] * sol[r + 1][2];
     }
     const bool zero_g1 = (m.btype == -1 && m.ibnd == 0);
     const bool zero_dz1 = (m.btype == -1);
     for (int k = 1; k <= L; ++k) {
         long o = ix(k, j, L);
         if (k <= nvl) {
-            s.ainvg1[o] = zero_g1 ? R(0) : rhs[k - 1][0];
-            s.ainvg2[o] = rhs[k - 1][1];
-            s.ainvdz1[o] = zero_dz1 ? R(0) : rhs[k - 1][2];
-            s.ainvdz2[o] = rhs[k - 1][2];
+            s.ainvg1[o] = zero_g1 ? R(0) : sol[k - 1][0];
+            s.ainvg2[o] = sol[k - 1][1];
+            s.ainvdz1[o] = zero_dz1 ? R(0) : sol[k - 1][2];
+            s.ainvdz2[o] = sol[k - 1][2];
         } else {
             s.ainvg1[o] = R(0);
             s.ainvg2[o] = R(0);
