@@ -170,6 +170,12 @@ def _bind(lib: C.CDLL) -> C.CDLL:
     lib.gom_profile_kernel.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(C.c_double)]
     lib.gom_device_bytes.argtypes = [vp]
     lib.gom_device_bytes.restype = C.c_int64
+    lib.gom_snapshot_begin.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_void_p)]
+    lib.gom_snapshot_ready.argtypes = [vp]
+    lib.gom_snapshot_wait.argtypes = [vp]
+    lib.gom_host_alloc.argtypes = [C.c_int64, C.POINTER(C.c_void_p)]
+    lib.gom_host_free.argtypes = [C.c_void_p]
+    lib.gom_host_free.restype = None
     lib.gom_get_status.argtypes = [vp, C.POINTER(GomStatus), C.c_int]
     lib.gom_synchronize.argtypes = [vp]
     lib.gom_pcg_iterations_total.argtypes = [vp]
@@ -373,6 +379,23 @@ class GomCore:
 
     def device_bytes(self) -> int:
         return int(self.lib.gom_device_bytes(self.ctx))
+
+    # ------------------------------------------------------------------ asynchronous snapshots
+    def snapshot_begin(self, names, buffers) -> None:
+        """Enqueue a copy of the named fields into the given arrays (pinned for overlap) after the
+        work enqueued so far; read them only after snapshot_wait / snapshot_ready."""
+        ids = (C.c_int32 * len(names))(*[FIELD_ID[n] for n in names])
+        ptrs = (C.c_void_p * len(names))(*[b.ctypes.data for b in buffers])
+        self._check(self.lib.gom_snapshot_begin(self.ctx, len(names), ids, ptrs), "snapshot_begin")
+
+    def snapshot_ready(self) -> bool:
+        rc = self.lib.gom_snapshot_ready(self.ctx)
+        if rc < 0:
+            self._check(rc, "snapshot_ready")
+        return rc == 1
+
+    def snapshot_wait(self) -> None:
+        self._check(self.lib.gom_snapshot_wait(self.ctx), "snapshot_wait")
 
     def set_storms(self, storms, elapsed_time: float = 0.0):
         """Device-side storm forcing, one storm per run (objects with gom_storm's fields)."""

@@ -64,6 +64,12 @@ struct gom_ctx {
     // device-side storm forcing (gom_set_storms)
     double *d_storms = nullptr, *storm_wu = nullptr, *storm_wv = nullptr;
     int n_storms = 0;
+    // asynchronous output snapshots (gom_snapshot_begin): device staging area, copy stream
+    char *snap_dev = nullptr;
+    size_t snap_cap = 0;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_snap_staged = nullptr, ev_snap_done = nullptr;
+    bool snap_pending = false;
 };
 
 namespace {
@@ -625,7 +631,26 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
         if (dalloc(c, &el, 8 * NC) != cudaSuccess) return fail(GOM_E_NOMEM);
         c->x.g.elem_local = el;
         if (launch_elem_local(c->x.g, el, c->x.stream) != cudaSuccess) return fail(GOM_E_CUDA);
-        if (prepare_momentum_tile(L) != cudaSuccess) return fail(GOM_E_CUDA);
+        struct {
+            const double *src;
+            const float **dst;
+            long n;
+        } f32[] = {{c->x.g.area, &c->x.g.area_f, NC},
+                   {c->x.g.face_length, &c->x.g.face_length_f, NF},
+                   {c->x.g.delta_j, &c->x.g.delta_j_f, NF},
+                   {c->x.g.cos_theta, &c->x.g.cos_theta_f, NF},
+                   {c->x.g.sin_theta, &c->x.g.sin_theta_f, NF},
+                   {W.node_weight, &c->x.g.node_weight_f, NN}};
+        for (auto &cv : f32) {
+            float *d = nullptr;
+            if (dalloc(c, &d, (size_t)cv.n) != cudaSuccess) return fail(GOM_E_NOMEM);
+            if (launch_to_float(cv.src, d, cv.n, c->x.stream) != cudaSuccess) return fail(GOM_E_CUDA);
+            *cv.dst = d;
+        }
+        float *el2 = nullptr;
+        if (dalloc(c, &el2, NF) != cudaSuccess) return fail(GOM_E_NOMEM);
+        if (launch_edge_len2(c->x.g, el2, c->x.stream) != cudaSuccess) return fail(GOM_E_CUDA);
+        c->x.g.edge_len2_f = el2;
         // the FP32 context shares geometry, forcing, parameters, status, stream and the FP64
         // work arrays (free-surface system, PCG vectors, ELM counts, node weights, sums)
         LaunchT<float> &X = c->xf;
@@ -680,8 +705,95 @@ void gom_destroy(gom_ctx *c) {
     if (c->h_stage) cudaFreeHost(c->h_stage);
     for (int h = 0; h < 2; ++h)
         if (c->stage_done[h]) cudaEventDestroy(c->stage_done[h]);
+    if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
+    if (c->snap_dev) cudaFree(c->snap_dev);
+    if (c->ev_snap_staged) cudaEventDestroy(c->ev_snap_staged);
+    if (c->ev_snap_done) cudaEventDestroy(c->ev_snap_done);
+    if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     if (c->x.stream) cudaStreamDestroy(c->x.stream);
     delete c;
+}
+
+int gom_snapshot_begin(gom_ctx *c, int32_t n_fields, const int32_t *fields, void *const *host) {
+    if (!c || n_fields < 0 || (n_fields > 0 && (!fields || !host)) || c->snap_pending) return GOM_E_ARG;
+    size_t total = 0;
+    for (int q = 0; q < n_fields; ++q) {
+        if (fields[q] <= 0 || fields[q] >= GOM_F_COUNT || !host[q]) return GOM_E_ARG;
+        const FieldDesc &f = c->fields[fields[q]];
+        if (f.lo == -2) return GOM_E_ARG;
+        total += (size_t)field_count(c->d, f) * (f.is_int ? 4 : 8);
+    }
+    if (!c->copy_stream) {
+        CK(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&c->ev_snap_staged, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&c->ev_snap_done, cudaEventDisableTiming));
+    }
+    if (total > c->snap_cap) {
+        // no snapshot is in flight, so the old area is free once the context stream has passed it
+        CK(cudaStreamSynchronize(c->x.stream));
+        if (c->snap_dev) {
+            cudaFree(c->snap_dev);
+            c->bytes -= c->snap_cap;
+        }
+        c->snap_dev = nullptr;
+        c->snap_cap = 0;
+        if (cudaMalloc(&c->snap_dev, total) != cudaSuccess) return GOM_E_NOMEM;
+        c->snap_cap = total;
+        c->bytes += total;
+    }
+    // stage on the context stream, after the work enqueued so far (FP32 fields widened to FP64)
+    size_t off = 0;
+    for (int q = 0; q < n_fields; ++q) {
+        const FieldDesc &f = c->fields[fields[q]];
+        const long n = (long)field_count(c->d, f);
+        const size_t nb = (size_t)n * (f.is_int ? 4 : 8);
+        if (!f.is_int && f.dev_bytes == 4)
+            CK(launch_to_double((const float *)*f.dev, (double *)(c->snap_dev + off), n, c->x.stream));
+        else
+            CK(cudaMemcpyAsync(c->snap_dev + off, *f.dev, nb, cudaMemcpyDeviceToDevice, c->x.stream));
+        off += nb;
+    }
+    CK(cudaEventRecord(c->ev_snap_staged, c->x.stream));
+    // transfer on the copy stream while later steps run on the context stream
+    CK(cudaStreamWaitEvent(c->copy_stream, c->ev_snap_staged, 0));
+    off = 0;
+    for (int q = 0; q < n_fields; ++q) {
+        const FieldDesc &f = c->fields[fields[q]];
+        const size_t nb = (size_t)field_count(c->d, f) * (f.is_int ? 4 : 8);
+        CK(cudaMemcpyAsync(host[q], c->snap_dev + off, nb, cudaMemcpyDeviceToHost, c->copy_stream));
+        off += nb;
+    }
+    CK(cudaEventRecord(c->ev_snap_done, c->copy_stream));
+    c->snap_pending = true;
+    return GOM_OK;
+}
+
+int gom_snapshot_ready(gom_ctx *c) {
+    if (!c) return GOM_E_ARG;
+    if (!c->snap_pending) return 1;
+    cudaError_t e = cudaEventQuery(c->ev_snap_done);
+    if (e == cudaErrorNotReady) return 0;
+    CK(e);
+    return 1;
+}
+
+int gom_snapshot_wait(gom_ctx *c) {
+    if (!c) return GOM_E_ARG;
+    if (!c->snap_pending) return GOM_OK;
+    c->snap_pending = false;
+    CK(cudaEventSynchronize(c->ev_snap_done));
+    return GOM_OK;
+}
+
+int gom_host_alloc(int64_t bytes, void **out) {
+    if (!out || bytes <= 0) return GOM_E_ARG;
+    *out = nullptr;
+    if (cudaHostAlloc(out, (size_t)bytes, cudaHostAllocDefault) != cudaSuccess) return GOM_E_NOMEM;
+    return GOM_OK;
+}
+
+void gom_host_free(void *p) {
+    if (p) cudaFreeHost(p);
 }
 
 int gom_set_field(gom_ctx *c, int field, const void *host, int64_t count) {

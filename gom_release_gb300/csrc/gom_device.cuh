@@ -44,6 +44,10 @@ struct Geom {
     const int *cell_order, *face_order, *node_order;
     // element node offsets from the element centre in FP32, (8, NC): x1..x4, y1..y4 (mixed path)
     const float *elem_local;
+    // FP32 copies of per-entity geometry and of the static node weights for the mixed path (null
+    // in FP64 contexts): a conversion from FP64 runs on the FP64 pipe, so FP32 kernels read these
+    const float *area_f, *face_length_f, *delta_j_f, *cos_theta_f, *sin_theta_f, *node_weight_f;
+    const float *edge_len2_f;   // squared node-to-node length of each face
     // packed runs (NR > 1): 0-based first cell / face / node / open-boundary cell of each run
     int NR;
     const int *run_cell_start, *run_face_start, *run_node_start, *run_ob_start;
@@ -114,6 +118,13 @@ __device__ __forceinline__ long ix0(int k, int e, int L) { return (long)(e - 1) 
 template <typename R> __device__ __forceinline__ int column_entity(const int *order, unsigned tid) {
     if constexpr (sizeof(R) == sizeof(float)) return (int)tid + 1;
     else return order[tid];
+}
+
+// an entity's geometry value in the layered-state type: the FP64 array for R = double, its FP32
+// copy for R = float
+template <typename R> __device__ __forceinline__ R geo(const double *d, const float *f, int i) {
+    if constexpr (sizeof(R) == sizeof(float)) return f[i];
+    else return d[i];
 }
 
 // -------------------------------------------------------------------- error status

@@ -51,7 +51,7 @@ using Work = WorkT<double>;
 // Tunable launches: each picks one of a few compiled variants (block size, minimum resident
 // blocks per SM); gom_autotune times the variants on the context's state and keeps the fastest.
 enum TuneSite { TUNE_ELM = 0, TUNE_MOMENTUM, TUNE_TR_SOLVE, TUNE_TR_LIMITER, TUNE_COUNT };
-constexpr int TUNE_VARIANTS[TUNE_COUNT] = {7, 4, 3, 3};
+constexpr int TUNE_VARIANTS[TUNE_COUNT] = {7, 3, 3, 3};
 
 template <typename R> struct LaunchT {
     int tune[TUNE_COUNT] = {0, 0, 0, 0};
@@ -65,9 +65,6 @@ template <typename R> struct LaunchT {
     int num_sms = 0;
 };
 using Launch = LaunchT<double>;
-
-// raises the dynamic shared-memory limit of the tiled FP32 momentum kernel for L layers
-cudaError_t prepare_momentum_tile(int L);
 
 template <typename R> cudaError_t launch_bottom_friction(const LaunchT<R> &x);
 template <typename R> cudaError_t launch_boundary_velocity(const LaunchT<R> &x);
@@ -95,6 +92,11 @@ template <typename R> cudaError_t launch_tr_solve_only(const LaunchT<R> &x);
 
 // FP32 element node offsets (8 per element) for the mixed-precision ELM, once per context
 cudaError_t launch_elem_local(const Geom &g, float *out, cudaStream_t stream);
+cudaError_t launch_edge_len2(const Geom &g, float *out, cudaStream_t stream);
+// FP64 copy of an FP32 array (n elements)
+cudaError_t launch_to_double(const float *in, double *out, long n, cudaStream_t stream);
+// FP32 copy of an FP64 array (n elements)
+cudaError_t launch_to_float(const double *in, float *out, long n, cudaStream_t stream);
 
 // cold start on the device (all state fields must have been cleared first)
 template <typename R>

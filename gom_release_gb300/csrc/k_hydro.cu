@@ -214,6 +214,42 @@ __global__ void k_elem_local(Geom g, float *out) {
     }
 }
 
+// squared node-to-node length of each face in FP32, from the FP64 coordinate differences
+__global__ void k_edge_len2(Geom g, float *out) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (j > g.NF) return;
+    const int n1 = g.face_node(1, j), n2 = g.face_node(2, j);
+    const float dx = (float)(g.x_node[n1 - 1] - g.x_node[n2 - 1]), dy = (float)(g.y_node[n1 - 1] - g.y_node[n2 - 1]);
+    out[j - 1] = dx * dx + dy * dy;
+}
+
+cudaError_t launch_edge_len2(const Geom &g, float *out, cudaStream_t stream) {
+    k_edge_len2<<<blocks_for(g.NF, 256), 256, 0, stream>>>(g, out);
+    return cudaGetLastError();
+}
+
+__global__ void k_to_float(const double *in, float *out, long n) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (float)in[i];
+}
+
+__global__ void k_to_double(const float *in, double *out, long n) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (double)in[i];
+}
+
+cudaError_t launch_to_double(const float *in, double *out, long n, cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    k_to_double<<<blocks_for(n, 256), 256, 0, stream>>>(in, out, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_to_float(const double *in, float *out, long n, cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    k_to_float<<<blocks_for(n, 256), 256, 0, stream>>>(in, out, n);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_elem_local(const Geom &g, float *out, cudaStream_t stream) {
     k_elem_local<<<blocks_for(g.NC, 256), 256, 0, stream>>>(g, out);
     return cudaGetLastError();
@@ -223,7 +259,7 @@ __device__ __forceinline__ void load_local(const Geom &g, int nel, LocalElem &e)
     e.tq = g.tri_or_quad[nel - 1];
     e.xc = g.x_cell[nel - 1];
     e.yc = g.y_cell[nel - 1];
-    e.ar = (float)g.area[nel - 1];
+    e.ar = g.area_f[nel - 1];
     const float4 *v = reinterpret_cast<const float4 *>(g.elem_local + (long)(nel - 1) * 8);
     const float4 xs = v[0], ys = v[1];
     e.x[0] = xs.x;
@@ -766,8 +802,7 @@ template <typename R> __global__ void k_elm_edge_dev(Geom g, StateT<R> s, Params
     if constexpr (sizeof(R) == sizeof(float)) {
         // mixed path: the same count in FP32 (the node velocities are FP32 already)
         const float dt = (float)p.dt, c01 = 0.1f;
-        const float dx = (float)(g.x_node[n1 - 1] - g.x_node[n2 - 1]), dy = (float)(g.y_node[n1 - 1] - g.y_node[n2 - 1]);
-        const float rl2 = dx * dx + dy * dy;
+        const float rl2 = g.edge_len2_f[j - 1];
         float du = (s.u_node[ix0(k, n1, L)] + s.u_node[ix0(k - 1, n1, L)]) * 0.5f -
                    (s.u_node[ix0(k, n2, L)] + s.u_node[ix0(k - 1, n2, L)]) * 0.5f;
         float dv = (s.v_node[ix0(k, n1, L)] + s.v_node[ix0(k - 1, n1, L)]) * 0.5f -
@@ -848,20 +883,50 @@ __device__ void elm_face_layer(const Geom &g, const StateT<R> &s, const Params &
     if (k == s.top_cell[nnel - 1]) z0 = p.msl + s.eta_cell[nnel - 1] - s.dz_cell[ix(k, nnel, L)] * 0.5;
     else z0 = g.z_level[k] - s.dz_cell[ix(k, nnel, L)] * 0.5;
     // the velocity at the face-layer midpoint and the walk threshold of :166 (vmag = sqrt(q) <=
-    // thr), decided on q against thr^2 away from the threshold; in FP64 in both paths, so a
-    // face-layer at the threshold is walked or not as in the FP64 path
-    double unf = s.un_face[o], vnf = s.vn_face[o];
-    double uu = unf * ct - vnf * sn;
-    double vv = unf * sn + vnf * ct;
-    double wdown = (s.w_node[ix0(k - 1, n1, L)] + s.w_node[ix0(k - 1, n2, L)]) * 0.5;
-    double wup = (s.w_node[ix0(k, n1, L)] + s.w_node[ix0(k, n2, L)]) * 0.5;
-    double ww = (wdown + wup) * 0.5;
+    // thr), decided on q against thr^2 away from the threshold; in both paths the decision is
+    // that of the FP64 arithmetic, so a face-layer at the threshold is walked or not as in the FP64
+    // path.  The mixed path first tries the rotation-free FP32 norm un^2 + vn^2 + w^2 (within
+    // 1e-6 of the FP64 q) and needs the FP64 q only within 1e-5 of the threshold.
+    const double thr = F(1.e-4f), t2 = thr * thr;
+    int decided = -1;   // 1 slow, 0 walk
+    if constexpr (MIXED) {
+        const float unf = s.un_face[o], vnf = s.vn_face[o];
+        const float wd = (s.w_node[ix0(k - 1, n1, L)] + s.w_node[ix0(k - 1, n2, L)]) * 0.5f;
+        const float wu = (s.w_node[ix0(k, n1, L)] + s.w_node[ix0(k, n2, L)]) * 0.5f;
+        const float wf = (wd + wu) * 0.5f;
+        const float qf = unf * unf + vnf * vnf + wf * wf, t2f = (float)t2;
+        if (qf < t2f * (1.0f - 1e-5f)) decided = 1;
+        else if (qf > t2f * (1.0f + 1e-5f)) decided = 0;
+    }
+    double uu, vv, ww;
     bool slow;
-    {
-        const double thr = F(1.e-4f), q = uu * uu + vv * vv + ww * ww, t2 = thr * thr;
-        if (q < t2 * (1.0 - 1e-9)) slow = true;
-        else if (q > t2 * (1.0 + 1e-9)) slow = false;
-        else slow = sqrt(q) <= thr;
+    if (decided == 1) {
+        slow = true;
+        uu = vv = ww = 0.0;
+    } else {
+        double unf = s.un_face[o], vnf = s.vn_face[o];
+        if constexpr (MIXED) {
+            // the walk starts from FP32 velocities (rotated with the FP32 direction cosines)
+            const float ctf = g.cos_theta_f[j - 1], snf = g.sin_theta_f[j - 1];
+            const float u32 = s.un_face[o], v32 = s.vn_face[o];
+            uu = u32 * ctf - v32 * snf;
+            vv = u32 * snf + v32 * ctf;
+        } else {
+            uu = unf * ct - vnf * sn;
+            vv = unf * sn + vnf * ct;
+        }
+        double wdown = (s.w_node[ix0(k - 1, n1, L)] + s.w_node[ix0(k - 1, n2, L)]) * 0.5;
+        double wup = (s.w_node[ix0(k, n1, L)] + s.w_node[ix0(k, n2, L)]) * 0.5;
+        ww = (wdown + wup) * 0.5;
+        if (decided == 0) {
+            slow = false;
+        } else {
+            const double u64 = unf * ct - vnf * sn, v64 = unf * sn + vnf * ct;
+            const double q = u64 * u64 + v64 * v64 + ww * ww;
+            if (q < t2 * (1.0 - 1e-9)) slow = true;
+            else if (q > t2 * (1.0 + 1e-9)) slow = false;
+            else slow = sqrt(q) <= thr;
+        }
     }
     if (slow) {
         s.un_elm[o] = s.un_face[o];
@@ -881,7 +946,7 @@ __device__ void elm_face_layer(const Geom &g, const StateT<R> &s, const Params &
     s.elm_foot[o] = nnel;
     s.elm_near_edge[o] = near;
     if constexpr (MIXED) {
-        const float ctf = (float)ct, snf = (float)sn, uf = (float)uu, vf = (float)vv;
+        const float ctf = g.cos_theta_f[j - 1], snf = g.sin_theta_f[j - 1], uf = (float)uu, vf = (float)vv;
         s.un_elm[o] = uf * ctf + vf * snf;
         s.vn_elm[o] = -uf * snf + vf * ctf;
     } else {
@@ -1435,102 +1500,6 @@ __global__ void __launch_bounds__(256) k_momentum(Geom g, StateT<R> s, Forcing f
     }
 }
 
-// FP32 path, the same columns by tiles: a block takes MT_TILE consecutive faces; the per-face
-// setup is formed once per face into shared memory, every (face, row) slot forms its matrix row
-// and right-hand sides in its own thread (neighbouring lanes read neighbouring layers of the same
-// columns and nodes), one thread per face runs the Thomas sweeps in shared memory, and the block
-// writes its (L, face) tile of the four outputs coalesced.  Same values as k_momentum<float>.
-constexpr int MT_TILE = 32;
-constexpr int MT_ARRAYS = 7;   // a, bd, cu, gam and the three right-hand sides, MT_TILE x L each
-
-inline size_t momentum_tile_smem(int L) { return (size_t)MT_ARRAYS * MT_TILE * L * sizeof(float); }
-
-__global__ void __launch_bounds__(256) k_momentum_tile(Geom g, StateT<float> s, Forcing f, Params p, gom_status *st) {
-    extern __shared__ float msm[];
-    __shared__ MomFace<float> mf[MT_TILE];
-    __shared__ int ok_s[MT_TILE];
-    const int L = g.L;
-    const int j0 = blockIdx.x * MT_TILE;
-    const int nf = min(MT_TILE, g.NF - j0);
-    for (int c = threadIdx.x; c < nf; c += blockDim.x) {
-        MomFace<float> m;
-        ok_s[c] = momentum_setup(g, s, f, p, j0 + c + 1, m) ? 1 : 0;
-        mf[c] = m;
-    }
-    __syncthreads();
-    const int TL = MT_TILE * L;
-    float *A = msm, *B = A + TL, *C = B + TL, *GM = C + TL, *R0 = GM + TL, *R1 = R0 + TL, *R2 = R1 + TL;
-    for (int t = threadIdx.x; t < nf * L; t += blockDim.x) {
-        const int c = t / L, r = t - c * L;
-        if (!ok_s[c] || r >= mf[c].nvl) continue;
-        const int q = c * L + r;
-        momentum_matrix_row(s, mf[c], L, r, A[q], B[q], C[q]);
-        momentum_row(g, s, p, mf[c], L, r + 1, R0[q], R1[q], R2[q]);
-    }
-    __syncthreads();
-    for (int c = threadIdx.x; c < nf; c += blockDim.x) {
-        if (!ok_s[c]) continue;
-        const int n = mf[c].nvl, q = c * L;
-        // thomas<3> on the shared rows
-        bool good = B[q] != 0.0f;
-        if (good) {
-            float den = B[q];
-            R0[q] = R0[q] / den;
-            R1[q] = R1[q] / den;
-            R2[q] = R2[q] / den;
-            for (int jr = 1; jr < n; ++jr) {
-                const float gm = C[q + jr - 1] / den;
-                GM[q + jr] = gm;
-                den = B[q + jr] - A[q + jr] * gm;
-                if (den == 0.0f) {
-                    good = false;
-                    break;
-                }
-                const float aj = A[q + jr];
-                R0[q + jr] = (R0[q + jr] - aj * R0[q + jr - 1]) / den;
-                R1[q + jr] = (R1[q + jr] - aj * R1[q + jr - 1]) / den;
-                R2[q + jr] = (R2[q + jr] - aj * R2[q + jr - 1]) / den;
-            }
-        }
-        if (good) {
-            for (int jr = n - 2; jr >= 0; --jr) {
-                const float gm = GM[q + jr + 1];
-                R0[q + jr] = R0[q + jr] - gm * R0[q + jr + 1];
-                R1[q + jr] = R1[q + jr] - gm * R1[q + jr + 1];
-                R2[q + jr] = R2[q + jr] - gm * R2[q + jr + 1];
-            }
-        } else {
-            record_error(st, GOM_E_ZERO_PIVOT, 587, mf[c].j, 0, 0.0);
-            ok_s[c] = 0;
-        }
-    }
-    __syncthreads();
-    const long base = (long)j0 * L;
-    for (int t = threadIdx.x; t < nf * L; t += blockDim.x) {
-        const int c = t / L, r = t - c * L;
-        if (!ok_s[c]) continue;   // dry faces: k_zero_face_columns; a failed solve writes nothing
-        const long o = base + t;
-        const MomFace<float> &m = mf[c];
-        if (r < m.nvl) {
-            const int q = c * L + r;
-            s.ainvg1[o] = (m.btype == -1 && m.ibnd == 0) ? 0.0f : R0[q];
-            s.ainvg2[o] = R1[q];
-            s.ainvdz1[o] = m.btype == -1 ? 0.0f : R2[q];
-            s.ainvdz2[o] = R2[q];
-        } else {
-            s.ainvg1[o] = 0.0f;
-            s.ainvg2[o] = 0.0f;
-            s.ainvdz1[o] = 0.0f;
-            s.ainvdz2[o] = 0.0f;
-        }
-    }
-}
-
-cudaError_t prepare_momentum_tile(int L) {
-    return cudaFuncSetAttribute(k_momentum_tile, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)momentum_tile_smem(L));
-}
-
 template <typename R> __global__ void k_zero_face_columns(Geom g, StateT<R> s) {
     // faces that are dry keep zero results (the reference zeroes all four arrays first)
     unsigned t = flat_tid();
@@ -1544,17 +1513,9 @@ template <typename R> __global__ void k_zero_face_columns(Geom g, StateT<R> s) {
     s.ainvdz2[t] = R(0);
 }
 
-// variants: one thread per column with 128 / 64 / 256 threads per block, or (FP32 contexts) the
-// tiled kernel; FP64 contexts run variant 3 as variant 0
+// variants: one thread per column with 128 / 64 / 256 threads per block
 template <typename R> cudaError_t launch_momentum_columns_only(const LaunchT<R> &x) {
     const int v = x.tune[TUNE_MOMENTUM];
-    if constexpr (sizeof(R) == sizeof(float)) {
-        if (v == 3) {
-            k_momentum_tile<<<blocks_for(x.g.NF, MT_TILE), 256, momentum_tile_smem(x.g.L), x.stream>>>(
-                x.g, x.s, x.f, x.p, x.status);
-            return cudaGetLastError();
-        }
-    }
     const int bs = v == 1 ? 64 : v == 2 ? 256 : 128;
     k_momentum<<<blocks_for(x.g.NF, bs), bs, 0, x.stream>>>(x.g, x.s, x.f, x.p, x.status);
     return cudaGetLastError();

@@ -521,7 +521,7 @@ __global__ void __launch_bounds__(256) k_cell_w_tile(Geom g, StateT<float> s) {
         b_s[c] = g.bottom_cell[i - 1];
         const int tq = g.tri_or_quad[i - 1];
         tq_s[c] = tq;
-        ar_s[c] = (float)g.area[i - 1];
+        ar_s[c] = g.area_f[i - 1];
         for (int l = 1; l <= tq; ++l) {
             const int jt = g.cell_face(l, i);
             fj_s[c][l - 1] = jt;
@@ -884,7 +884,7 @@ __global__ void k_face_level_flat(Geom g, StateT<float> s, WorkT<float> w) {
     j += 1;
     const int t = s.top_face[j - 1], b = g.bottom_face[j - 1];
     if (t == 0 || k < b - 1 || k > t) return;
-    const float ct = (float)g.cos_theta[j - 1], sn = (float)g.sin_theta[j - 1], fl = (float)g.face_length[j - 1];
+    const float ct = g.cos_theta_f[j - 1], sn = g.sin_theta_f[j - 1], fl = g.face_length_f[j - 1];
     // the face velocity of layer m rotated to x/y
     auto rot = [&](int m, float &u, float &v) {
         float un = s.un_face_new[ix(m, j, L)], vn = s.vn_face_new[ix(m, j, L)];
@@ -963,7 +963,7 @@ template <typename R> __global__ void k_node_uvw(Geom g, StateT<R> s, WorkT<R> w
         }
     }
     if (icount != 0) {
-        R weight = (R)wk.node_weight[i - 1];
+        R weight = geo<R>(wk.node_weight, g.node_weight_f, i - 1);
         u = u / weight;
         v = v / weight;
     }
@@ -973,7 +973,7 @@ template <typename R> __global__ void k_node_uvw(Geom g, StateT<R> s, WorkT<R> w
         int te = s.top_cell[ite - 1];
         if (te != 0 && k >= g.bottom_cell[ite - 1] - 1) {
             int kvt = min(k, te);
-            R ar = (R)g.area[ite - 1];
+            R ar = geo<R>(g.area, g.area_f, ite - 1);
             tw = tw + ar;
             w = w + s.wn_cell[ix0(kvt, ite, L)] * ar;
         }
@@ -985,13 +985,96 @@ template <typename R> __global__ void k_node_uvw(Geom g, StateT<R> s, WorkT<R> w
     s.w_node[o] = w;
 }
 
+// FP32 path, the same per node by tiles: a block takes NV_TILE consecutive nodes and lists each
+// node's faces (with weight and level range) and cells once in shared memory, in the order the
+// per-(node, level) kernel visits them; every (node, level) slot then sums from the lists.  Same
+// values as k_node_uvw<float>.
+constexpr int NV_TILE = 32;
+
+__global__ void __launch_bounds__(256) k_node_uvw_tile(Geom g, StateT<float> s, WorkT<float> wk) {
+    __shared__ int fid[NV_TILE][2 * GOM_MAXNB], flo[NV_TILE][2 * GOM_MAXNB], fhi[NV_TILE][2 * GOM_MAXNB];
+    __shared__ float fwt[NV_TILE][2 * GOM_MAXNB];
+    __shared__ int cid[NV_TILE][GOM_MAXNB], clo[NV_TILE][GOM_MAXNB], chi[NV_TILE][GOM_MAXNB];
+    __shared__ float car[NV_TILE][GOM_MAXNB];
+    __shared__ int nf_s[NV_TILE], nc_s[NV_TILE];
+    __shared__ float wgt_s[NV_TILE];
+    const int L = g.L;
+    const int i0 = blockIdx.x * NV_TILE;
+    const int nn = min(NV_TILE, g.NN - i0);
+    for (int c = threadIdx.x; c < nn; c += blockDim.x) {
+        const int i = i0 + c + 1;
+        const int na = g.adj_cells_at_node[i - 1];
+        int nf = 0, nc = 0;
+        for (int j = 1; j <= na; ++j) {
+            const int isn = g.node_cell(j, i), ncnt = g.node_count(j, i);
+            const int tq = g.tri_or_quad[isn - 1];
+            for (int l = tq - 2; l <= tq - 1; ++l) {
+                const int ifn = g.cell_face(start_end_node(tq, ncnt, l), isn);
+                const int tf = s.top_face[ifn - 1];
+                if (tf == 0) continue;   // contributes nothing at any level
+                fid[c][nf] = ifn;
+                flo[c][nf] = g.bottom_face[ifn - 1] - 1;
+                fhi[c][nf] = tf;
+                fwt[c][nf] = g.face_cell(2, ifn) == 0 ? 2.0f : 1.0f;
+                ++nf;
+            }
+            const int te = s.top_cell[isn - 1];
+            if (te != 0) {
+                cid[c][nc] = isn;
+                clo[c][nc] = g.bottom_cell[isn - 1] - 1;
+                chi[c][nc] = te;
+                car[c][nc] = g.area_f[isn - 1];
+                ++nc;
+            }
+        }
+        nf_s[c] = nf;
+        nc_s[c] = nc;
+        wgt_s[c] = g.node_weight_f[i - 1];
+    }
+    __syncthreads();
+    const long base = (long)i0 * (L + 1);
+    for (int t = threadIdx.x; t < nn * (L + 1); t += blockDim.x) {
+        const int c = t / (L + 1), k = t - c * (L + 1);
+        float u = 0.0f, v = 0.0f;
+        int icount = 0;
+        for (int q = 0; q < nf_s[c]; ++q) {
+            if (k >= flo[c][q]) {
+                const long o = ix0(min(k, fhi[c][q]), fid[c][q], L);
+                u = u + wk.uflf[o] * fwt[c][q];
+                v = v + wk.vflf[o] * fwt[c][q];
+                icount = icount + 1;
+            }
+        }
+        if (icount != 0) {
+            u = u / wgt_s[c];
+            v = v / wgt_s[c];
+        }
+        float w = 0.0f, tw = 0.0f;
+        for (int q = 0; q < nc_s[c]; ++q) {
+            if (k >= clo[c][q]) {
+                const float ar = car[c][q];
+                tw = tw + ar;
+                w = w + s.wn_cell[ix0(min(k, chi[c][q]), cid[c][q], L)] * ar;
+            }
+        }
+        if (tw != 0.0f) w = w / tw;
+        s.u_node[base + t] = u;
+        s.v_node[base + t] = v;
+        s.w_node[base + t] = w;
+    }
+}
+
 template <typename R> cudaError_t launch_node_velocity(const LaunchT<R> &x) {
     if constexpr (sizeof(R) == sizeof(float))
         k_face_level_flat<<<blocks_for((long)x.g.NF * (x.g.L + 1), 256), 256, 0, x.stream>>>(x.g, x.s, x.w);
     else
         k_face_level<<<blocks_for(x.g.NF, 128), 128, 0, x.stream>>>(x.g, x.s, x.w);
-    long n = (long)x.g.NN * (x.g.L + 1);
-    k_node_uvw<<<blocks_for(n, 256), 256, 0, x.stream>>>(x.g, x.s, x.w);
+    if constexpr (sizeof(R) == sizeof(float)) {
+        k_node_uvw_tile<<<blocks_for(x.g.NN, NV_TILE), 256, 0, x.stream>>>(x.g, x.s, x.w);
+    } else {
+        long n = (long)x.g.NN * (x.g.L + 1);
+        k_node_uvw<<<blocks_for(n, 256), 256, 0, x.stream>>>(x.g, x.s, x.w);
+    }
     return cudaGetLastError();
 }
 

@@ -147,9 +147,9 @@ template <typename R> __global__ void k_tr_bc(TArgs<R> a) {
 template <typename R> __device__ __forceinline__ void face_coef_at(const TArgs<R> &a, int j, int k, long t) {
     R dzf = a.s.dz_face[t];
     R dz_old = dzf + divnt((a.s.dz_face_new[t] - dzf) * (R)a.sub, a);
-    R fl = (R)a.g.face_length[j - 1];
+    R fl = geo<R>(a.g.face_length, a.g.face_length_f, j - 1);
     R Q = fl * dz_old * (a.om_theta * a.s.un_face[t] + a.theta * a.s.un_face_new[t]);
-    R D = fl * dz_old * a.s.kh[t] / (R)a.g.delta_j[j - 1];
+    R D = fl * dz_old * a.s.kh[t] / geo<R>(a.g.delta_j, a.g.delta_j_f, j - 1);
     R d = fmax(R(0), D - R(0.5) * fabs(Q));
     R phi = Q == R(0) ? R(1) : diffusive_share(D, Q);
     a.w.qj[t] = Q;
@@ -185,7 +185,7 @@ template <typename R> __global__ void k_tr_face_coef(TArgs<R> a) {
 
 // :585-610 vertical coefficients, one thread per cell column (interfaces b..t-1)
 template <typename R> __device__ __forceinline__ void cell_coef_at(const TArgs<R> &a, int i, long t) {
-    R ar = (R)a.g.area[i - 1];
+    R ar = geo<R>(a.g.area, a.g.area_f, i - 1);
     R Q = ar * (a.om_theta * a.s.wn_cell[t] + a.theta * a.s.wn_cell_new[t]);
     R dzh = a.s.dzhalf_cell[t];
     R dz_old = dzh + divnt((a.s.dzhalf_cell_new[t] - dzh) * (R)a.sub, a);
@@ -579,7 +579,7 @@ template <typename R> __device__ void tr_solve_column(const TArgs<R> &a, int i) 
         return;
     }
     int nvl = tl - b + 1;
-    const R ar = (R)g.area[i - 1];
+    const R ar = geo<R>(g.area, g.area_f, i - 1);
     R am[GOM_MAXL], bm[GOM_MAXL], cm[GOM_MAXL], gm[GOM_MAXL];
     R rhs[GOM_MAXL][2];
     for (int k = b + 1; k <= tl - 1; ++k) {
@@ -747,7 +747,7 @@ __device__ __forceinline__ void tr_rows_at(const TArgs<float> &a, int i, int k) 
     const float dt2 = a.dt2;
     const int sub = a.sub;
     const bool lim = a.p.h_flux_limiter > 0 || a.p.v_flux_limiter > 0;
-    const float ar = (float)g.area[i - 1];
+    const float ar = g.area_f[i - 1];
     const int tq = g.tri_or_quad[i - 1];
     float c0[2] = {0.0f, 0.0f};
     for (int tr = 0; tr < a.ntr; ++tr) c0[tr] = a.con[ic(k, i, tr, L, NC)];
@@ -944,7 +944,7 @@ __global__ void __launch_bounds__(256) k_tr_nodes_tile(TArgs<float> a) {
             cell_s[c][l - 1] = ii;
             cb_s[c][l - 1] = g.bottom_cell[ii - 1];
             ct_s[c][l - 1] = a.s.top_cell[ii - 1];
-            car_s[c][l - 1] = (float)g.area[ii - 1];
+            car_s[c][l - 1] = g.area_f[ii - 1];
         }
     }
     __syncthreads();

@@ -57,9 +57,11 @@ class Storm:
 
 
 def storm_run(seed: int, n_cells: int, aspect: float, n_layers_run: int, dt: float = 60.0,
-              dx: float = 250.0, max_layers: int = 30, tri_rows: int = 2) -> Deck:
+              dx: float = 250.0, max_layers: int = 30, tri_rows: int = 2, h_coast: float = 2.0,
+              h_min: float = 1.0) -> Deck:
     """One storm-surge run of about ``n_cells`` cells, domain aspect ``aspect`` (x / y), deepest
-    water using ``n_layers_run`` of the shared 1 m levels."""
+    water using ``n_layers_run`` of the shared 1 m levels; the shelf rises to ``h_coast`` at the
+    closed northern coast, depths at least ``h_min``."""
     rng = np.random.default_rng(seed)
     ny = max(6, int(round(math.sqrt(n_cells / aspect))))
     nx = max(6, int(round(n_cells / ny)) - tri_rows)
@@ -68,10 +70,10 @@ def storm_run(seed: int, n_cells: int, aspect: float, n_layers_run: int, dt: flo
     lx = nx * dx
     hmax = min(float(n_layers_run) - 1.5, max_layers - 1.5)
     shelf = (1.0 - y / ly) ** 1.3
-    h = 2.0 + (hmax - 2.0) * shelf
+    h = h_coast + (hmax - h_coast) * shelf
     lam = max(4.0 * dx, 0.25 * min(lx, ly))
     h = h + fourier_noise(x, y, rng, lam_min=lam, lam_max=4.0 * lam, amplitude=0.3)
-    h = np.clip(h, 1.0, hmax)
+    h = np.clip(h, h_min, hmax)
     raw = RawMesh(x=x, y=y, h=h, tri_or_quad=tq, cells=cells)
     params = Params(dt=dt, theta=0.6, error_tolerance=1e-10, baroclinic_flag=0, trans_sub_iter=1,
                     h_flux_limiter=0, v_flux_limiter=0, cd_const=0.0025, bf_flag=3)
@@ -102,7 +104,8 @@ def storm_run(seed: int, n_cells: int, aspect: float, n_layers_run: int, dt: flo
 
 
 def ensemble_decks(n_runs: int = 96, seed: int = 7, min_cells: int = 5000, max_cells: int = 400000,
-                   dt: float = 60.0, max_layers: int = 30, dx: float = 250.0):
+                   dt: float = 60.0, max_layers: int = 30, dx: float = 250.0, h_coast: float = 2.0,
+                   h_min: float = 1.0):
     """Runs with cell counts log-uniform in [min_cells, max_cells], aspect 1-4, 10-30 layers."""
     rng = np.random.default_rng(seed)
     out = []
@@ -110,7 +113,8 @@ def ensemble_decks(n_runs: int = 96, seed: int = 7, min_cells: int = 5000, max_c
         n = int(math.exp(rng.uniform(math.log(min_cells), math.log(max_cells))))
         aspect = float(rng.uniform(1.0, 4.0))
         layers = int(rng.integers(10, max_layers + 1))
-        out.append(storm_run(int(rng.integers(1 << 30)), n, aspect, layers, dt=dt, dx=dx, max_layers=max_layers))
+        out.append(storm_run(int(rng.integers(1 << 30)), n, aspect, layers, dt=dt, dx=dx, max_layers=max_layers,
+                             h_coast=h_coast, h_min=h_min))
     return out
 
 

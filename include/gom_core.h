@@ -422,6 +422,23 @@ int gom_profile_kernel(struct gom_ctx *ctx, int32_t which, int32_t reps, double 
  * share a GPU. */
 int64_t gom_device_bytes(const struct gom_ctx *ctx);
 
+/* Asynchronous output snapshots for the output writers (write_dump3D.f90:4, write_restart.f90:7,
+ * write_tser_out_files.f90 read the state between steps; the overlap has no reference
+ * counterpart).  gom_snapshot_begin enqueues, after the work already enqueued on the context
+ * (a step launched by gom_step_launch included), a copy of the listed fields into a device
+ * staging area and their transfer into host[q] (FP64 for real fields whatever the context's
+ * precision, int32 for integer fields; sizes as gom_get_field) on a separate copy stream, and
+ * returns: the following steps run while the transfer proceeds.  The host buffers should be
+ * pinned (gom_host_alloc) for the transfer to overlap, and must not be read before
+ * gom_snapshot_wait (blocks until the data has landed) or gom_snapshot_ready (1 landed, 0 still
+ * in flight) says so.  One snapshot may be in flight per context (GOM_E_ARG otherwise). */
+int gom_snapshot_begin(struct gom_ctx *ctx, int32_t n_fields, const int32_t *fields, void *const *host);
+int gom_snapshot_ready(struct gom_ctx *ctx);
+int gom_snapshot_wait(struct gom_ctx *ctx);
+/* Pinned (page-locked) host memory for snapshot buffers. */
+int gom_host_alloc(int64_t bytes, void **out);
+void gom_host_free(void *p);
+
 /* Volume and salt mass of the wet cells: sum(area*dz_cell), sum(area*dz_cell*salt_cell),
  * accumulated in FP64 (spec: check_conservation.f90:28-57). */
 int gom_conservation(struct gom_ctx *ctx, double *volume, double *salt_mass);

@@ -38,6 +38,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -87,6 +88,7 @@ struct gom_ctx {
     gom_dims d{};
     gom_params p{};
     int L = 0, NC = 0, NF = 0, NN = 0, NB = 0, NOB = 0, NQB = 0;
+    bool snap_pending = false;
     Err err;
     std::string msg;
     long long pcg_total = 0;
@@ -815,6 +817,32 @@ int gom_autotune(gom_ctx *c, int32_t, int32_t *choice) {
         for (int k = 0; k < GOM_TUNE_SITES; ++k) choice[k] = 0;
     return GOM_OK;
 }
+
+// snapshots are taken synchronously on the CPU
+int gom_snapshot_begin(gom_ctx *c, int32_t n_fields, const int32_t *fields, void *const *host) {
+    if (!c || n_fields < 0 || (n_fields > 0 && (!fields || !host)) || c->snap_pending) return GOM_E_ARG;
+    for (int q = 0; q < n_fields; ++q) {
+        int32_t eb = 0;
+        const int64_t n = (fields[q] > 0 && fields[q] < GOM_F_COUNT) ? field_count(c->d, fields[q], &eb) : -1;
+        if (n < 0 || !host[q]) return GOM_E_ARG;
+        int rc = gom_get_field(c, fields[q], host[q], n);
+        if (rc != GOM_OK) return rc;
+    }
+    c->snap_pending = true;
+    return GOM_OK;
+}
+int gom_snapshot_ready(gom_ctx *c) { return c ? 1 : GOM_E_ARG; }
+int gom_snapshot_wait(gom_ctx *c) {
+    if (!c) return GOM_E_ARG;
+    c->snap_pending = false;
+    return GOM_OK;
+}
+int gom_host_alloc(int64_t bytes, void **out) {
+    if (!out || bytes <= 0) return GOM_E_ARG;
+    *out = std::malloc((size_t)bytes);
+    return *out ? GOM_OK : GOM_E_NOMEM;
+}
+void gom_host_free(void *p) { std::free(p); }
 
 int gom_tuning_variants(int32_t counts[GOM_TUNE_SITES]) {
     if (!counts) return GOM_E_ARG;
