@@ -394,6 +394,22 @@ def bench_ensemble(args):
     pk = pack(decks)
     k = args.steps
     w = max(3, args.warmup, int(round(args.warm_hours * 3600.0 / pk.params.dt)))
+    if args.profile_step:
+        # for kernel profiles: warm up, autotune, then one step phase by phase inside an NVTX
+        # range named prof_step (ncu --nvtx --nvtx-include "prof_step/")
+        import torch
+        from gom_release_gb300.core import TIME_LOOP
+        core = storm_context(lib, pk, 1, storms)
+        time_core_steps(core, w)
+        tune = core.autotune(reps=2)
+        core.synchronize()
+        torch.cuda.nvtx.range_push("prof_step")
+        for ph in TIME_LOOP:
+            core.step(ph)
+        core.synchronize()
+        torch.cuda.nvtx.range_pop()
+        print(json.dumps({"profile_step": "done", "cells": pk.n_cells, "warm_steps": w, "autotune": tune}))
+        return
     res = {}
     with ClockSampler(0) as clocks:
         for label, prec in (("mixed_packed", 1), ("fp64_packed", 0)):
@@ -585,6 +601,9 @@ def main():
     ap.add_argument("--warm-hours", type=float, default=0.0,
                     help="ensemble: simulated hours stepped before timing (the storms ramp up over 6 h)")
     ap.add_argument("--skip-mixed-alone", action="store_true", help="ensemble: skip the mixed one-at-a-time arm")
+    ap.add_argument("--profile-step", action="store_true",
+                    help="ensemble: warm up, autotune and run one packed step phase by phase in an NVTX range "
+                         "prof_step (for ncu), then exit")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
                     help="fp64: the drop-in path (bit-for-bit with the CPU restatement); mixed: FP32 layered state")
     args = ap.parse_args()

@@ -500,6 +500,18 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
         else if (fd.dev_bytes == 4) e = dalloc(c, (float **)fd.dev, n);
         else e = dalloc(c, (double **)fd.dev, n);
     }
+    // derived per-cell arrays of the ELM walk (static bottom height; surface height and dry test
+    // refreshed at the start of every advection phase)
+    {
+        double **ztop = c->mixed ? &c->xf.s.ztop_cell : &c->x.s.ztop_cell;
+        int **dry = c->mixed ? &c->xf.s.dry_cell : &c->x.s.dry_cell;
+        double *zbot = nullptr;
+        if (e == cudaSuccess) e = dalloc(c, ztop, NC);
+        if (e == cudaSuccess) e = dalloc(c, dry, NC);
+        if (e == cudaSuccess) e = dalloc(c, &zbot, NC);
+        if (e == cudaSuccess) e = launch_cell_zbot(G, params->msl, zbot, c->x.stream);
+        G.zbot_cell = zbot;
+    }
     // forcing
     int nt = params->trans_sub_iter > 0 ? params->trans_sub_iter : 1;
     if (e == cudaSuccess) e = dalloc(c, &c->f_eta_old, (size_t)d.n_ob);

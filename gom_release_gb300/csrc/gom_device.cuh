@@ -48,6 +48,7 @@ struct Geom {
     // in FP64 contexts): a conversion from FP64 runs on the FP64 pipe, so FP32 kernels read these
     const float *area_f, *face_length_f, *delta_j_f, *cos_theta_f, *sin_theta_f, *node_weight_f;
     const float *edge_len2_f;   // squared node-to-node length of each face
+    const double *zbot_cell;    // MSL - h of each cell
     // packed runs (NR > 1): 0-based first cell / face / node / open-boundary cell of each run
     int NR;
     const int *run_cell_start, *run_face_start, *run_node_start, *run_ob_start;
@@ -84,6 +85,9 @@ template <typename R> struct StateT {
     R *cdb, *gamma_b;
     double *qu_boundary;
     int *elm_foot, *elm_near_edge;
+    // derived at the start of each ELM step (not fields): MSL + eta and the ELM dry test per cell
+    double *ztop_cell;
+    int *dry_cell;
 };
 using State = StateT<double>;
 

@@ -244,6 +244,17 @@ cudaError_t launch_to_double(const float *in, double *out, long n, cudaStream_t 
     return cudaGetLastError();
 }
 
+// MSL - h of every cell (the bottom of its water column), static
+__global__ void k_cell_zbot(Geom g, double msl, double *out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < g.NC) out[i] = msl - g.h_cell[i];
+}
+
+cudaError_t launch_cell_zbot(const Geom &g, double msl, double *out, cudaStream_t stream) {
+    k_cell_zbot<<<blocks_for(g.NC, 256), 256, 0, stream>>>(g, msl, out);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_to_float(const double *in, float *out, long n, cudaStream_t stream) {
     if (n <= 0) return cudaSuccess;
     k_to_float<<<blocks_for(n, 256), 256, 0, stream>>>(in, out, n);
@@ -541,7 +552,7 @@ __device__ int search_straight_line(const Geom &g, const StateT<R> &s, const Par
     // the tolerance.  Both tests of a later substep: it starts at the previous foot, and the
     // previous search ended only after that foot tested inside nnel (the complementary test on the
     // same operands) and nnel passed the same dry test (:370).
-    if (first_substep && (top_el(s, nnel) == 0 || MSL - g.h_cell[nnel - 1] > MSL + s.eta_cell[nnel - 1]))
+    if (first_substep && s.dry_cell[nnel - 1])
         return GOM_ELM_START_DRY;
     nfl = 0;
     last.valid = false;
@@ -633,8 +644,8 @@ __device__ int search_straight_line(const Geom &g, const StateT<R> &s, const Par
     } else {
         nnel = nel;
     }
-    if (top_el(s, nnel) == 0 || MSL - g.h_cell[nnel - 1] > MSL + s.eta_cell[nnel - 1]) return GOM_ELM_END_DRY;
-    zt = fmin(fmax(zt, MSL - g.h_cell[nnel - 1]), MSL + s.eta_cell[nnel - 1]);
+    if (s.dry_cell[nnel - 1]) return GOM_ELM_END_DRY;
+    zt = fmin(fmax(zt, g.zbot_cell[nnel - 1]), s.ztop_cell[nnel - 1]);
     if (zt <= g.z_level[0] || zt > g.z_level[L]) return GOM_ELM_Z_RANGE;
     // :376-396 the level k with z_level(k) < zt <= z_level(k+1), unique for increasing levels:
     // searched from the start layer outwards instead of from the bottom (same k)
@@ -680,7 +691,7 @@ __device__ int elm_backtrace(const Geom &g, const StateT<R> &s, const Params &p,
         int e = search_straight_line<R, MIXED>(g, s, p, nnel, jlev, bt_dt, x0, y0, z0, xt, yt, zt, nfl, idt == 1, last);
         if (e) return e;
         int tq = g.tri_or_quad[nnel - 1];
-        double zup = (jlev == s.top_cell[nnel - 1]) ? p.msl + s.eta_cell[nnel - 1] : g.z_level[jlev];
+        double zup = (jlev == s.top_cell[nnel - 1]) ? s.ztop_cell[nnel - 1] : g.z_level[jlev];
         if (zt > zup) return GOM_ELM_Z_ABOVE;
         if constexpr (MIXED) {
             const float zrat = (float)(zup - zt) / (float)s.dz_cell[ix(jlev, nnel, L)];
@@ -880,7 +891,7 @@ __device__ void elm_face_layer(const Geom &g, const StateT<R> &s, const Params &
     long o = ix(k, j, L);
     int nnel = ie0, jlev = k;
     double x0 = g.x_face[j - 1], y0 = g.y_face[j - 1], z0;
-    if (k == s.top_cell[nnel - 1]) z0 = p.msl + s.eta_cell[nnel - 1] - s.dz_cell[ix(k, nnel, L)] * 0.5;
+    if (k == s.top_cell[nnel - 1]) z0 = s.ztop_cell[nnel - 1] - s.dz_cell[ix(k, nnel, L)] * 0.5;
     else z0 = g.z_level[k] - s.dz_cell[ix(k, nnel, L)] * 0.5;
     // the velocity at the face-layer midpoint and the walk threshold of :166 (vmag = sqrt(q) <=
     // thr), decided on q against thr^2 away from the threshold; in both paths the decision is
@@ -1081,10 +1092,28 @@ template <typename R> cudaError_t launch_elm_walk(const LaunchT<R> &x) {
     return cudaGetLastError();
 }
 
-template <typename R> cudaError_t launch_elm_walk_only(const LaunchT<R> &x) { return launch_elm_walk(x); }
+template <typename R> __global__ void k_cell_z(Geom g, StateT<R> s, Params p);
+
+template <typename R> cudaError_t launch_elm_walk_only(const LaunchT<R> &x) {
+    k_cell_z<<<blocks_for(x.g.NC, 256), 256, 0, x.stream>>>(x.g, x.s, x.p);
+    return launch_elm_walk(x);
+}
+
+// The cell's surface height MSL + eta and its dry test of search_straight_line.f90:37-46 and
+// :363-372 (no layer, or MSL - h above MSL + eta), once per cell per step instead of at every
+// substep of every face-layer; the same FP64 expressions, hence the same values.
+template <typename R> __global__ void k_cell_z(Geom g, StateT<R> s, Params p) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.NC) return;
+    const double ztop = p.msl + s.eta_cell[i];
+    s.ztop_cell[i] = ztop;
+    s.dry_cell[i] = (s.top_cell[i] == 0 || g.zbot_cell[i] > ztop) ? 1 : 0;
+}
 
 template <typename R> cudaError_t launch_advection(const LaunchT<R> &x) {
     long nfl = (long)x.g.NF * x.g.L;
+    if (x.p.advection_flag != 0)
+        k_cell_z<<<blocks_for(x.g.NC, 256), 256, 0, x.stream>>>(x.g, x.s, x.p);
     if (x.p.advection_flag == 0) {
         k_copy_elm<<<blocks_for(nfl, 256), 256, 0, x.stream>>>(x.g, x.s);
         return cudaGetLastError();

@@ -58,10 +58,12 @@ class Storm:
 
 def storm_run(seed: int, n_cells: int, aspect: float, n_layers_run: int, dt: float = 60.0,
               dx: float = 250.0, max_layers: int = 30, tri_rows: int = 2, h_coast: float = 2.0,
-              h_min: float = 1.0) -> Deck:
+              h_min: float = 1.0, av_0: float = 0.05, open_sides: bool = False) -> Deck:
     """One storm-surge run of about ``n_cells`` cells, domain aspect ``aspect`` (x / y), deepest
     water using ``n_layers_run`` of the shared 1 m levels; the shelf rises to ``h_coast`` at the
-    closed northern coast, depths at least ``h_min``."""
+    closed northern coast, depths at least ``h_min``.  The vertical eddy viscosity ``av_0`` is a
+    storm-surge value (m^2/s): with the 1e-3 of a calm estuary the 1 m surface layer under
+    hurricane winds decouples from the column and its velocity grows without bound."""
     rng = np.random.default_rng(seed)
     ny = max(6, int(round(math.sqrt(n_cells / aspect))))
     nx = max(6, int(round(n_cells / ny)) - tri_rows)
@@ -76,9 +78,14 @@ def storm_run(seed: int, n_cells: int, aspect: float, n_layers_run: int, dt: flo
     h = np.clip(h, h_min, hmax)
     raw = RawMesh(x=x, y=y, h=h, tri_or_quad=tq, cells=cells)
     params = Params(dt=dt, theta=0.6, error_tolerance=1e-10, baroclinic_flag=0, trans_sub_iter=1,
-                    h_flux_limiter=0, v_flux_limiter=0, cd_const=0.0025, bf_flag=3)
+                    h_flux_limiter=0, v_flux_limiter=0, cd_const=0.0025, bf_flag=3, av_0=av_0)
     z_bottom, z_top, L = ensemble_z_grid(max_layers)
     ob_pairs = [(i + 1, i + 2) for i in range(nx)]         # southern edge
+    if open_sides:
+        # western and eastern edges of the square rows above the southern corner cells
+        for jrow in range(1, ny):
+            ob_pairs.append(((jrow + 1) * (nx + 1) + 1, jrow * (nx + 1) + 1))
+            ob_pairs.append((jrow * (nx + 1) + nx + 1, (jrow + 1) * (nx + 1) + nx + 1))
     amp = float(rng.uniform(0.3, 0.8))
     deck = _finish("storm_run", raw, L, z_bottom, z_top, params, ob_pairs, [], [],
                    tide=dict(amplitude=[amp], period_h=[M2_PERIOD_H], phase=[0.0], nodal=[1.0],
@@ -105,7 +112,7 @@ def storm_run(seed: int, n_cells: int, aspect: float, n_layers_run: int, dt: flo
 
 def ensemble_decks(n_runs: int = 96, seed: int = 7, min_cells: int = 5000, max_cells: int = 400000,
                    dt: float = 60.0, max_layers: int = 30, dx: float = 250.0, h_coast: float = 2.0,
-                   h_min: float = 1.0):
+                   h_min: float = 1.0, open_sides: bool = False):
     """Runs with cell counts log-uniform in [min_cells, max_cells], aspect 1-4, 10-30 layers."""
     rng = np.random.default_rng(seed)
     out = []
@@ -114,7 +121,7 @@ def ensemble_decks(n_runs: int = 96, seed: int = 7, min_cells: int = 5000, max_c
         aspect = float(rng.uniform(1.0, 4.0))
         layers = int(rng.integers(10, max_layers + 1))
         out.append(storm_run(int(rng.integers(1 << 30)), n, aspect, layers, dt=dt, dx=dx, max_layers=max_layers,
-                             h_coast=h_coast, h_min=h_min))
+                             h_coast=h_coast, h_min=h_min, open_sides=open_sides))
     return out
 
 
