@@ -57,7 +57,7 @@ PCG_BYTES_PER_CELL_ITERATION = 120
 FS_ASSEMBLY_BYTES_PER_CELL_LAYER = 64
 
 
-def make_deck(size: str, precision: str = "fp64"):
+def make_deck(size: str, precision: str = "fp64", transport_solver: int = 1):
     import dataclasses
     from gom_release_gb300.deck import estuary
     if size == "small":
@@ -68,6 +68,9 @@ def make_deck(size: str, precision: str = "fp64"):
         d = estuary()
     if precision == "mixed":
         d = dataclasses.replace(d, params=dataclasses.replace(d.params, precision=1))
+    if transport_solver == 2:
+        # the ELM transport has no subcycles
+        d = dataclasses.replace(d, params=dataclasses.replace(d.params, transport_solver=2, trans_sub_iter=1))
     return d
 
 
@@ -294,7 +297,7 @@ def run_reference(args, world, rank):
     if rank != 0:
         return
     from gom_release_gb300.deck import active_cell_layers, initial_state
-    deck = make_deck(args.size)
+    deck = make_deck(args.size, "fp64", args.transport_solver)
     st = initial_state(deck)
     ncl = active_cell_layers(deck, st)
     k, dt, threads = time_oracle(deck, st, max(1, args.steps), 20.0)
@@ -604,6 +607,8 @@ def main():
     ap.add_argument("--profile-step", action="store_true",
                     help="ensemble: warm up, autotune and run one packed step phase by phase in an NVTX range "
                          "prof_step (for ncu), then exit")
+    ap.add_argument("--transport-solver", type=int, default=1, choices=[1, 2],
+                    help="estuary: 1 TVD transport (the configuration), 2 ELM transport (transport_solver 2)")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
                     help="fp64: the drop-in path (bit-for-bit with the CPU restatement); mixed: FP32 layered state")
     args = ap.parse_args()
@@ -630,7 +635,7 @@ def main():
     from gom_release_gb300.deck import HostForcing, active_cell_layers, initial_state
     from gom_release_gb300.driver import Run
 
-    deck = make_deck(args.size, args.precision)
+    deck = make_deck(args.size, args.precision, args.transport_solver)
     st = initial_state(deck)
     ncl = active_cell_layers(deck, st)
     lib = load_core()
@@ -703,7 +708,9 @@ def main():
             "workload": (f"estuary: {deck.n_cells} cells ({deck.meta['nx']}x{deck.meta['ny']} squares of "
                          f"{deck.meta['dx']:g} m + {deck.meta['tri_rows']}-row triangle strip), {deck.n_faces} faces, "
                          f"{deck.n_nodes} nodes, {deck.n_layers} layers, {ncl} active cell-layers, dt={deck.params.dt:g} s, "
-                         f"TVD limiter, {deck.params.trans_sub_iter} transport subcycles, baroclinic, "
+                         + (f"TVD limiter, {deck.params.trans_sub_iter} transport subcycles, "
+                            if deck.params.transport_solver != 2 else "ELM transport (transport_solver 2), ") +
+                         f"baroclinic, "
                          f"turbulence closure {deck.params.turbulence_flag}"),
             "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
             "l2": "state larger than L2 (each phase streams its arrays from HBM)",

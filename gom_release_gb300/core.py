@@ -76,13 +76,13 @@ _PARAM_D = ["gravity", "rho_o", "msl", "dt", "theta", "adv_onoff_depth", "von_ka
 _PARAM_I = ["advection_flag", "elm_backtrace_flag", "elm_sub_iter", "elm_min_iter", "elm_max_iter",
             "bf_flag", "baroclinic_flag", "ana_density", "max_iteration_pcg", "transport_flag",
             "trans_sub_iter", "h_flux_limiter", "v_flux_limiter", "is_salt", "is_temp", "heat_option",
-            "test_barrier_phantom_blocks", "precision", "turbulence_flag"]
+            "test_barrier_phantom_blocks", "precision", "turbulence_flag", "transport_solver"]
 _PARAM_PP = ["pp_h1", "pp_h2", "pp_vdmax1", "pp_vdmax2", "pp_vdmin1", "pp_vdmin2", "pp_tdmin"]
 
 
 class GomParams(C.Structure):
     _fields_ = [(n, C.c_double) for n in _PARAM_D] + [(n, C.c_int32) for n in _PARAM_I] + \
-               [("reserved", C.c_int32)] + [(n, C.c_double) for n in _PARAM_PP]
+               [(n, C.c_double) for n in _PARAM_PP]
 
 
 _GEOM = [
@@ -230,7 +230,8 @@ class GomCore:
         runs = getattr(d, "runs", None)
         self.dims = GomDims(d.n_cells, d.n_faces, d.n_nodes, d.n_layers, d.max_nb, d.n_ob, d.n_qb,
                             len(runs["run_cell_start"]) - 1 if runs else 0)
-        self.params = GomParams(*[getattr(p, n) for n in _PARAM_D], *[int(getattr(p, n)) for n in _PARAM_I], 0,
+        self.params = GomParams(*[getattr(p, n) for n in _PARAM_D], *[int(getattr(p, n, 1 if n == "transport_solver" else 0))
+                                                                      for n in _PARAM_I],
                                 *[getattr(p, n) for n in _PARAM_PP])
         g = d.geo
         keep = {}

@@ -383,6 +383,7 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
         d.n_faces >= LIST_MAX_ENTITIES)
         return GOM_E_ARG;
     if (params->transport_flag && params->is_salt == 0 && params->is_temp == 1) return GOM_E_ARG;
+    if (params->transport_solver < 0 || params->transport_solver > 2) return GOM_E_ARG;
     if (params->precision != GOM_PRECISION_FP64 && params->precision != GOM_PRECISION_MIXED) return GOM_E_ARG;
     if (params->turbulence_flag < 0 || params->turbulence_flag > 2) return GOM_E_ARG;
     int ndev = 0;
@@ -596,6 +597,7 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
     P.ana_density = params->ana_density;
     P.max_iteration_pcg = params->max_iteration_pcg;
     P.transport_flag = params->transport_flag;
+    P.transport_solver = params->transport_solver;
     P.trans_sub_iter = params->trans_sub_iter;
     P.h_flux_limiter = params->h_flux_limiter;
     P.v_flux_limiter = params->v_flux_limiter;

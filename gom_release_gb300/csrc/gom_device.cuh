@@ -104,7 +104,7 @@ struct Params {
         kh_0, error_tolerance, delta_z_min, denominator_min_for_matrix;
     int advection_flag, elm_backtrace_flag, elm_sub_iter, elm_min_iter, elm_max_iter, bf_flag, baroclinic_flag,
         ana_density, max_iteration_pcg, transport_flag, trans_sub_iter, h_flux_limiter, v_flux_limiter, is_salt,
-        is_temp, heat_option, test_barrier_phantom_blocks, turbulence_flag;
+        is_temp, heat_option, test_barrier_phantom_blocks, turbulence_flag, transport_solver;
     double pp_h1, pp_h2, pp_vdmax1, pp_vdmax2, pp_vdmin1, pp_vdmin2, pp_tdmin;
     double bt_dt[GOM_BT_TABLE];   // dt / n for ELM substep counts n = 1..GOM_BT_TABLE
 };

@@ -72,6 +72,7 @@ template <typename R> cudaError_t launch_advection(const LaunchT<R> &x);
 template <typename R> cudaError_t launch_momentum(const LaunchT<R> &x);
 template <typename R> cudaError_t launch_free_surface(const LaunchT<R> &x);
 template <typename R> cudaError_t launch_velocities(const LaunchT<R> &x);
+template <typename R> cudaError_t launch_transport_elm(const LaunchT<R> &x);
 template <typename R> cudaError_t launch_layers(const LaunchT<R> &x);
 template <typename R> cudaError_t launch_node_velocity(const LaunchT<R> &x);
 template <typename R> cudaError_t launch_transport(const LaunchT<R> &x);

@@ -676,10 +676,17 @@ __device__ bool near_edge_line(const Geom &g, int nel, double x, double y) {
 // edge of the start element.  MIXED: FP64 foot coordinates and the reference's point-in-element
 // decisions (FP32 with an error bound, FP64 where that does not decide); the crossing walk,
 // interpolation weights and velocities in FP32 on element-local coordinates.
+// the last substep's foot, the surface or level height above it and the interpolation weights
+// (the ELM transport interpolates the tracers with them, ELM_backtrace_v1.f90:216-473)
+struct ElmFinal {
+    double xt, yt, zt, zup;
+    double staint[4];
+};
+
 template <typename R, bool MIXED>
 __device__ int elm_backtrace(const Geom &g, const StateT<R> &s, const Params &p, int bt_step, double bt_dt, double &uu,
                              double &vv, double &ww, double x0, double y0, double z0, int &nnel, int &jlev,
-                             int &near_edge) {
+                             int &near_edge, ElmFinal *fin = nullptr) {
     const double small_06 = F(1.e-6f);
     const int L = g.L;
     LastTest last;
@@ -738,6 +745,10 @@ __device__ int elm_backtrace(const Geom &g, const StateT<R> &s, const Params &p,
             vv = fv;
             ww = fw;
             if (near && near_edge_line(g, nnel, xt, yt)) near_edge = 1;
+            if (fin) {
+                *fin = ElmFinal{xt, yt, zt, zup, {0.0, 0.0, 0.0, 0.0}};
+                for (int l = 0; l < tq; ++l) fin->staint[l] = sta[l];
+            }
         } else {
             double zrat = (zup - zt) / s.dz_cell[ix(jlev, nnel, L)];
             double vxn[4], vyn[4], vzn[4], sta[4];
@@ -785,6 +796,10 @@ __device__ int elm_backtrace(const Geom &g, const StateT<R> &s, const Params &p,
                 ww = ww + vzn[j] * sta[j];
             }
             if (near_edge_line(g, nnel, xt, yt)) near_edge = 1;
+            if (fin) {
+                *fin = ElmFinal{xt, yt, zt, zup, {0.0, 0.0, 0.0, 0.0}};
+                for (int l = 0; l < tq; ++l) fin->staint[l] = sta[l];
+            }
         }
         if (nfl == 1) break;
         x0 = xt;
@@ -1126,6 +1141,373 @@ template <typename R> cudaError_t launch_advection(const LaunchT<R> &x) {
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     return launch_elm_walk(x);
+}
+
+// ============================================================================================
+// solve_transport_equation_ELM_v8.f90:7-346 (transport_solver = 2).  The reference's quirks are
+// kept: the horizontal sums use the face's second cell as the neighbour and go to the other
+// tracer (salinity differences to temperature, :137-151), the top row's upper coefficient is
+// -dt + Kv/dzhalf (:188), no clamp, dry cells and dry nodes keep their previous values, face
+// values average the two nodes in every layer.  The heat source term of :120 is left out (phi_sz
+// comes from the heat-balance module, not part of the core).  Work: con holds the backtracked values and
+// con2 the explicit right-hand sides, tracer slot 0 temperature and 1 salinity.
+
+// ELM_backtrace_v1.f90:216-473: temperature and salinity at the foot (FP64 geometry, tracers in R)
+template <typename R>
+__device__ int elm_tracer_at_foot(const Geom &g, const StateT<R> &s, const Forcing &f, const ElmFinal &fin, int nnel,
+                                  int jlev, double &ttint, double &ssint) {
+    const double small_06 = F(1.e-6f);
+    const int L = g.L;
+    const double xt = fin.xt, yt = fin.yt, zt = fin.zt, zup = fin.zup;
+    const int ibnd1 = g.ob_element_flag[nnel - 1], ibnd2 = g.qb_element_flag[nnel - 1];
+    ttint = 0.0;
+    ssint = 0.0;
+    if (ibnd1 > 0) {   // the boundary concentration, the same in every layer
+        ssint = f.con_at_ob[ibnd1 - 1];
+        ttint = f.con_at_ob[g.NOB + ibnd1 - 1];
+        return 0;
+    }
+    if (ibnd2 > 0) {
+        ssint = f.con_at_qb[ibnd2 - 1];
+        ttint = f.con_at_qb[g.NQB + ibnd2 - 1];
+        return 0;
+    }
+    const double zanchor = zup - (double)s.dz_cell[ix(jlev, nnel, L)] * 0.5;
+    int k1, k2;
+    double zrat2;
+    if (jlev == s.top_cell[nnel - 1] && zt > zanchor) {
+        k1 = jlev;
+        k2 = jlev;
+        zrat2 = 0.5;
+    } else if (zt > zanchor) {
+        k1 = jlev;
+        k2 = jlev + 1;
+        zrat2 = (zt - zanchor) / (double)s.dzhalf_cell[ix0(jlev, nnel, L)];
+    } else {
+        k1 = max(jlev - 1, g.bottom_cell[nnel - 1]);
+        k2 = jlev;
+        zrat2 = 1.0 - (zanchor - zt) / (double)s.dzhalf_cell[ix0(k1, nnel, L)];
+    }
+    zrat2 = fmax(0.0, fmin(1.0, zrat2));
+    auto lev = [&](const R *a, int e) {
+        return (double)a[ix(k1, e, L)] * (1 - zrat2) + (double)a[ix(k2, e, L)] * zrat2;
+    };
+    const int tq = g.tri_or_quad[nnel - 1];
+    int icount = 0;
+    double ta = 0.0, sa = 0.0, t_xi[4] = {0, 0, 0, 0}, s_xi[4] = {0, 0, 0, 0};
+    for (int l = 1; l <= tq; ++l) {
+        const int nd = g.cell_node(l, nnel);
+        if (s.top_node[nd - 1] != 0) {
+            icount = icount + 1;
+            t_xi[l - 1] = lev(s.temp_node, nd);
+            s_xi[l - 1] = lev(s.salt_node, nd);
+            ta = ta + t_xi[l - 1];
+            sa = sa + s_xi[l - 1];
+        }
+    }
+    if (icount == 0) return GOM_ELM_ALL_DRY;
+    ta = ta / icount;
+    sa = sa / icount;
+    if (icount != tq) {
+        ttint = ta;
+        ssint = sa;
+    } else {
+        ttint = 0.0;
+        ssint = 0.0;
+        for (int l = 1; l <= tq; ++l) {
+            ttint = ttint + t_xi[l - 1] * fin.staint[l - 1];
+            ssint = ssint + s_xi[l - 1] * fin.staint[l - 1];
+        }
+    }
+    const double ar = g.area[nnel - 1];
+    int index_1 = 0;
+    if (tq == 3) {
+        for (int l = 1; l <= 4; ++l) {
+            double aa1, aa2, aa3;
+            int n1 = 0, f1 = 0, f2, f3;
+            if (l <= 3) {
+                n1 = g.cell_node(l, nnel);
+                f2 = g.cell_face(start_end_node(tq, l, 2), nnel);
+                f3 = g.cell_face(start_end_node(tq, l, 1), nnel);
+                aa1 = calculate_area(xt, g.x_face[f2 - 1], g.x_face[f3 - 1], yt, g.y_face[f2 - 1], g.y_face[f3 - 1]);
+                aa2 = calculate_area(g.x_node[n1 - 1], xt, g.x_face[f3 - 1], g.y_node[n1 - 1], yt, g.y_face[f3 - 1]);
+                aa3 = calculate_area(g.x_node[n1 - 1], g.x_face[f2 - 1], xt, g.y_node[n1 - 1], g.y_face[f2 - 1], yt);
+            } else {
+                f1 = g.cell_face(1, nnel);
+                f2 = g.cell_face(2, nnel);
+                f3 = g.cell_face(3, nnel);
+                aa1 = calculate_area(xt, g.x_face[f2 - 1], g.x_face[f3 - 1], yt, g.y_face[f2 - 1], g.y_face[f3 - 1]);
+                aa2 = calculate_area(g.x_face[f1 - 1], xt, g.x_face[f3 - 1], g.y_face[f1 - 1], yt, g.y_face[f3 - 1]);
+                aa3 = calculate_area(g.x_face[f1 - 1], g.x_face[f2 - 1], xt, g.y_face[f1 - 1], g.y_face[f2 - 1], yt);
+            }
+            const double aa = fabs(aa1) + fabs(aa2) + fabs(aa3);
+            const double subrat = fabs(aa - ar / 4) * 4 / ar;
+            if (subrat < 100 * small_06) {
+                index_1 = 1;
+                double sig[3];
+                sig[0] = aa1 * 4 / ar;
+                sig[1] = aa2 * 4 / ar;
+                sig[0] = fmax(0.0, fmin(1.0, sig[0]));
+                sig[1] = fmax(0.0, fmin(1.0, sig[1]));
+                if (sig[0] + sig[1] > 1) {
+                    sig[2] = 0;
+                    sig[1] = 1 - sig[0];
+                } else {
+                    sig[2] = 1 - sig[0] - sig[1];
+                }
+                const bool wet = l <= 3 ? (s.top_node[n1 - 1] != 0 && s.top_face[f2 - 1] != 0 && s.top_face[f3 - 1] != 0)
+                                        : (s.top_face[f1 - 1] != 0 && s.top_face[f2 - 1] != 0 && s.top_face[f3 - 1] != 0);
+                if (wet) {
+                    const double t0 = l <= 3 ? lev(s.temp_node, n1) : lev(s.temp_face, f1);
+                    const double s0 = l <= 3 ? lev(s.salt_node, n1) : lev(s.salt_face, f1);
+                    ttint = t0 * sig[0] + lev(s.temp_face, f2) * sig[1] + lev(s.temp_face, f3) * sig[2];
+                    ssint = s0 * sig[0] + lev(s.salt_face, f2) * sig[1] + lev(s.salt_face, f3) * sig[2];
+                    break;
+                }
+            }
+        }
+    } else {
+        const double xc = g.x_cell[nnel - 1], yc = g.y_cell[nnel - 1];
+        for (int l = 1; l <= 4; ++l) {
+            const int n1 = g.cell_node(l, nnel);
+            const int f2 = g.cell_face(start_end_node(tq, l, 3), nnel), f4 = g.cell_face(start_end_node(tq, l, 2), nnel);
+            const double xn = g.x_node[n1 - 1], yn = g.y_node[n1 - 1];
+            const double x2 = g.x_face[f2 - 1], y2 = g.y_face[f2 - 1], x4 = g.x_face[f4 - 1], y4 = g.y_face[f4 - 1];
+            const double aa1 = calculate_area(xn, x2, xt, yn, y2, yt);
+            const double aa2 = calculate_area(x2, xc, xt, y2, yc, yt);
+            const double aa3 = calculate_area(xc, x4, xt, yc, y4, yt);
+            const double aa4 = calculate_area(x4, xn, xt, y4, yn, yt);
+            const double bb1 = calculate_area(xn, x2, x4, yn, y2, y4);
+            const double bb2 = calculate_area(x2, xc, x4, y2, yc, y4);
+            if (bb1 <= 0 || bb2 <= 0) return GOM_ELM_NEG_SUBELEMENT;
+            const double bb = bb1 + bb2;
+            const double aa = fabs(aa1) + fabs(aa2) + fabs(aa3) + fabs(aa4);
+            const double subrat = fabs(aa - bb) / bb;
+            if (subrat < 4.0 * small_06) {
+                index_1 = 1;
+                double st4[4];
+                const int b = bilinear_interpolation<double>(xn, x2, xc, x4, yn, y2, yc, y4, xt, yt, st4);
+                if (b) return b;
+                if (s.top_node[n1 - 1] != 0 && s.top_face[f2 - 1] != 0 && s.top_face[f4 - 1] != 0) {
+                    const double tx[4] = {lev(s.temp_node, n1), lev(s.temp_face, f2), ta, lev(s.temp_face, f4)};
+                    const double sx[4] = {lev(s.salt_node, n1), lev(s.salt_face, f2), sa, lev(s.salt_face, f4)};
+                    ttint = 0.0;
+                    ssint = 0.0;
+                    for (int j = 0; j < 4; ++j) {
+                        ttint = ttint + tx[j] * st4[j];
+                        ssint = ssint + sx[j] * st4[j];
+                    }
+                }
+            }
+        }
+    }
+    if (index_1 == 0) return GOM_ELM_NO_SUBELEMENT;
+    return 0;
+}
+
+// :59-125, one thread per (cell, layer)
+template <typename R> __global__ void k_elmtr_backtrack(Geom g, StateT<R> s, Forcing f, Params p, R *con, gom_status *st) {
+    constexpr bool MIXED = sizeof(R) == sizeof(float);
+    unsigned t = flat_tid();
+    const int L = g.L, NC = g.NC;
+    if (t >= (unsigned)NC * L) return;
+    int i, k;
+    split_index(t, L, i, k);
+    i += 1;
+    k += 1;
+    const long oT = (long)(i - 1) * L + (k - 1), oS = (long)NC * L + oT;
+    const int top = s.top_cell[i - 1];
+    if (top == 0) {
+        con[oT] = R(0);
+        con[oS] = R(0);
+        return;
+    }
+    if (k < g.bottom_cell[i - 1] || k > top) return;
+    int nnel = i, jlev = k;
+    const double x0 = g.x_cell[i - 1], y0 = g.y_cell[i - 1];
+    double z0;
+    if (k == top) z0 = s.ztop_cell[i - 1] - (double)s.dz_cell[ix(k, i, L)] * 0.5;
+    else z0 = g.z_level[k] - (double)s.dz_cell[ix(k, i, L)] * 0.5;
+    double u_temp = 0.0, v_temp = 0.0;
+    int bt_step = 0;
+    const int tq = g.tri_or_quad[i - 1];
+    for (int l = 1; l <= tq; ++l) {
+        const int nd = g.cell_node(l, i);
+        u_temp = u_temp + ((double)s.u_node[ix0(k, nd, L)] + (double)s.u_node[ix0(k - 1, nd, L)]) * 0.5;
+        v_temp = v_temp + ((double)s.v_node[ix0(k, nd, L)] + (double)s.v_node[ix0(k - 1, nd, L)]) * 0.5;
+        bt_step = bt_step + s.num_sub_elm[ix(k, nd, L)];
+    }
+    u_temp = u_temp / tq;
+    v_temp = v_temp / tq;
+    bt_step = bt_step / tq;
+    double uu = u_temp, vv = v_temp;
+    double ww = ((double)s.wn_cell[ix0(k, i, L)] + (double)s.wn_cell[ix0(k - 1, i, L)]) * 0.5;
+    double tc, sc;
+    if (sqrt(uu * uu + vv * vv + ww * ww) <= F(1.e-4f)) {
+        tc = s.temp_cell[ix(k, i, L)];
+        sc = s.salt_cell[ix(k, i, L)];
+    } else {
+        const double bt_dt = (bt_step >= 1 && bt_step <= GOM_BT_TABLE) ? p.bt_dt[bt_step - 1] : p.dt / bt_step;
+        int near = 0;
+        ElmFinal fin;
+        int e = elm_backtrace<R, MIXED>(g, s, p, bt_step, bt_dt, uu, vv, ww, x0, y0, z0, nnel, jlev, near, &fin);
+        if (!e) e = elm_tracer_at_foot(g, s, f, fin, nnel, jlev, tc, sc);
+        if (e) {
+            record_error(st, GOM_E_ELM, e, i, k, 0.0);
+            return;
+        }
+    }
+    con[oT] = (R)tc;
+    con[oS] = (R)sc;
+}
+
+// :133-154, one thread per (cell, layer)
+template <typename R> __global__ void k_elmtr_hdiff(Geom g, StateT<R> s, Params p, const R *con, R *rhs) {
+    unsigned t = flat_tid();
+    const int L = g.L, NC = g.NC;
+    if (t >= (unsigned)NC * L) return;
+    int i, k;
+    split_index(t, L, i, k);
+    i += 1;
+    k += 1;
+    const int top = s.top_cell[i - 1];
+    if (top == 0 || k < g.bottom_cell[i - 1] || k > top) return;
+    R sum1 = R(0), sum2 = R(0);
+    for (int l = 1; l <= g.tri_or_quad[i - 1]; ++l) {
+        const int j = g.cell_face(l, i);
+        const int ie = g.face_cell(2, j);
+        if (ie != 0) {
+            const R rtemp1 = geo<R>(g.face_length, g.face_length_f, j - 1) * s.dz_face[ix(k, j, L)] *
+                             s.kh[ix(k, j, L)] / geo<R>(g.delta_j, g.delta_j_f, j - 1);
+            sum1 = sum1 + rtemp1 * (s.salt_cell[ix(k, ie, L)] - s.salt_cell[ix(k, i, L)]);
+            sum2 = sum2 + rtemp1 * (s.temp_cell[ix(k, ie, L)] - s.temp_cell[ix(k, i, L)]);
+        }
+    }
+    const R dtR = (R)p.dt, den = geo<R>(g.area, g.area_f, i - 1) * s.dz_cell[ix(k, i, L)];
+    sum1 = sum1 * dtR / den;
+    sum2 = sum2 * dtR / den;
+    const long oT = (long)(i - 1) * L + (k - 1), oS = (long)NC * L + oT;
+    rhs[oT] = con[oT] + sum1;
+    rhs[oS] = con[oS] + sum2;
+}
+
+// :163-236, one thread per cell column: implicit vertical diffusion, extension below and above
+template <typename R> __global__ void k_elmtr_vsolve(Geom g, StateT<R> s, Params p, const R *rhs, gom_status *st) {
+    unsigned tid = flat_tid();
+    if (tid >= (unsigned)g.NC) return;
+    const int i = column_entity<R>(g.cell_order, tid);
+    const int L = g.L, NC = g.NC;
+    const int t = s.top_cell[i - 1], b = g.bottom_cell[i - 1];
+    if (t == 0) return;   // dry cells keep their previous values
+    const int nvl = t - b + 1;
+    const R dtR = (R)p.dt;
+    R am[GOM_MAXL], bm[GOM_MAXL], cm[GOM_MAXL], gm[GOM_MAXL], rr[GOM_MAXL][2];
+    for (int k = b + 1; k <= t - 1; ++k) {
+        const int kk = t - k + 1;
+        am[kk - 1] = -dtR * s.kv[ix0(k, i, L)] / s.dzhalf_cell[ix0(k, i, L)];
+        cm[kk - 1] = -dtR * s.kv[ix0(k - 1, i, L)] / s.dzhalf_cell[ix0(k - 1, i, L)];
+        bm[kk - 1] = -am[kk - 1] + s.dz_cell[ix(k, i, L)] - cm[kk - 1];
+    }
+    if (t == b) {
+        bm[0] = s.dz_cell[ix(t, i, L)];
+    } else {
+        cm[0] = -dtR + s.kv[ix0(t - 1, i, L)] / s.dzhalf_cell[ix0(t - 1, i, L)];
+        bm[0] = s.dz_cell[ix(t, i, L)] - cm[0];
+        am[nvl - 1] = -dtR * s.kv[ix0(b, i, L)] / s.dzhalf_cell[ix0(b, i, L)];
+        bm[nvl - 1] = -am[nvl - 1] + s.dz_cell[ix(b, i, L)];
+    }
+    for (int k = 1; k <= nvl; ++k) {
+        const int kk = t - k + 1;
+        const long oT = (long)(i - 1) * L + (kk - 1);
+        rr[k - 1][0] = s.dz_cell[ix(kk, i, L)] * rhs[oT];
+        rr[k - 1][1] = s.dz_cell[ix(kk, i, L)] * rhs[(long)NC * L + oT];
+    }
+    if (!thomas<2>(nvl, am, bm, cm, rr, gm)) {
+        record_error(st, GOM_E_ZERO_PIVOT, 210, i, 0, 0.0);
+        return;
+    }
+    for (int k = 1; k <= L; ++k) {
+        const int kq = k < b ? b : (k > t ? t : k);
+        const int row = t + 1 - kq;
+        s.temp_cell_new[ix(k, i, L)] = rr[row - 1][0];
+        s.salt_cell_new[ix(k, i, L)] = rr[row - 1][1];
+    }
+}
+
+// :262-330, one thread per node column: averages with the fill from above, extension of wet nodes
+template <typename R> __global__ void k_elmtr_nodes(Geom g, StateT<R> s) {
+    unsigned tid = flat_tid();
+    if (tid >= (unsigned)g.NN) return;
+    const int i = column_entity<R>(g.node_order, tid);
+    const int L = g.L;
+    const int tn = s.top_node[i - 1], bn = g.bottom_node[i - 1];
+    if (tn == 0) return;   // dry nodes keep their previous values
+    const int na = g.adj_cells_at_node[i - 1];
+    for (int k = tn; k >= bn; --k) {
+        R sum0 = R(0), sum1 = R(0), sum2 = R(0);
+        int icount = 0;
+        for (int l = 1; l <= na; ++l) {
+            const int ie = g.node_cell(l, i);
+            if (k >= g.bottom_cell[ie - 1] && k <= s.top_cell[ie - 1]) {
+                const R ar = geo<R>(g.area, g.area_f, ie - 1), dzn = s.dz_cell_new[ix(k, ie, L)];
+                sum0 = sum0 + ar * dzn;
+                sum1 = sum1 + ar * dzn * s.temp_cell_new[ix(k, ie, L)];
+                sum2 = sum2 + ar * dzn * s.salt_cell_new[ix(k, ie, L)];
+            } else {
+                icount = icount + 1;
+            }
+        }
+        R tv, sv;
+        if (sum0 == R(0)) {
+            tv = R(0);
+            sv = R(0);
+        } else {
+            tv = sum1 / sum0;
+            sv = sum2 / sum0;
+        }
+        if (icount == na && k != tn) {
+            tv = s.temp_node[ix(k + 1, i, L)];
+            sv = s.salt_node[ix(k + 1, i, L)];
+        }
+        s.temp_node[ix(k, i, L)] = tv;
+        s.salt_node[ix(k, i, L)] = sv;
+    }
+    for (int k = 1; k <= bn - 1; ++k) {
+        s.temp_node[ix(k, i, L)] = s.temp_node[ix(bn, i, L)];
+        s.salt_node[ix(k, i, L)] = s.salt_node[ix(bn, i, L)];
+    }
+    for (int k = tn + 1; k <= L; ++k) {
+        s.temp_node[ix(k, i, L)] = s.temp_node[ix(tn, i, L)];
+        s.salt_node[ix(k, i, L)] = s.salt_node[ix(tn, i, L)];
+    }
+}
+
+// :332-339, one thread per (face, layer)
+template <typename R> __global__ void k_elmtr_faces(Geom g, StateT<R> s) {
+    unsigned t = flat_tid();
+    const int L = g.L;
+    if (t >= (unsigned)g.NF * L) return;
+    int j, k;
+    split_index(t, L, j, k);
+    j += 1;
+    k += 1;
+    const int n1 = g.face_node(1, j), n2 = g.face_node(2, j);
+    s.salt_face[t] = (s.salt_node[ix(k, n1, L)] + s.salt_node[ix(k, n2, L)]) * R(0.5);
+    s.temp_face[t] = (s.temp_node[ix(k, n1, L)] + s.temp_node[ix(k, n2, L)]) * R(0.5);
+}
+
+template <typename R> __global__ void k_cell_z(Geom g, StateT<R> s, Params p);
+
+template <typename R> cudaError_t launch_transport_elm(const LaunchT<R> &x) {
+    const Geom &g = x.g;
+    const long ncl = (long)g.NC * g.L;
+    k_cell_z<<<blocks_for(g.NC, 256), 256, 0, x.stream>>>(g, x.s, x.p);
+    k_elmtr_backtrack<<<blocks_for(ncl, 64), 64, 0, x.stream>>>(g, x.s, x.f, x.p, x.w.con, x.status);
+    k_elmtr_hdiff<<<blocks_for(ncl, 256), 256, 0, x.stream>>>(g, x.s, x.p, x.w.con, x.w.con2);
+    k_elmtr_vsolve<<<blocks_for(g.NC, 128), 128, 0, x.stream>>>(g, x.s, x.p, x.w.con2, x.status);
+    k_elmtr_nodes<<<blocks_for(g.NN, 128), 128, 0, x.stream>>>(g, x.s);
+    k_elmtr_faces<<<blocks_for((long)g.NF * g.L, 256), 256, 0, x.stream>>>(g, x.s);
+    return cudaGetLastError();
 }
 
 // ============================================================================================
@@ -1562,5 +1944,6 @@ GOM_INSTANTIATE_LAUNCH(launch_advection)
 GOM_INSTANTIATE_LAUNCH(launch_momentum)
 GOM_INSTANTIATE_LAUNCH(launch_elm_walk_only)
 GOM_INSTANTIATE_LAUNCH(launch_momentum_columns_only)
+GOM_INSTANTIATE_LAUNCH(launch_transport_elm)
 
 }  // namespace gom

@@ -1066,6 +1066,7 @@ template <typename R> cudaError_t launch_tr_solve_only(const LaunchT<R> &x) {
 template <typename R> cudaError_t launch_transport(const LaunchT<R> &x) {
     const Params &p = x.p;
     if (!p.transport_flag) return cudaSuccess;
+    if (p.transport_solver == 2) return launch_transport_elm(x);
     TArgs<R> a;
     a.g = x.g;
     a.s = x.s;

@@ -70,6 +70,7 @@ class Params:
     # turbulence_closure_v1.f90: 0 off (reference time loop), 1 step-Ri, 2 Pacanowski-Philander;
     # the coefficients are the closure's usual values (the reference reads none of them)
     turbulence_flag: int = 0
+    transport_solver: int = 1     # 1 TVD (solve_transport_equation_v19), 2 ELM (..._ELM_v8)
     pp_h1: float = 20.0
     pp_h2: float = 50.0
     pp_vdmax1: float = 1.0e-2

@@ -69,7 +69,10 @@ enum {
     GOM_ELM_Z_RANGE = 10,         /* search_straight_line.f90:379-385 */
     GOM_ELM_Z_ABOVE = 11,         /* ELM_backtrace_v1.f90:107-113     */
     GOM_ELM_QUAD_OUTSIDE = 12,    /* ELM_backtrace_v1.f90:164-170     */
-    GOM_ELM_BILINEAR = 13         /* bilinear_interpolation.f90:41-113 */
+    GOM_ELM_BILINEAR = 13,        /* bilinear_interpolation.f90:41-113 */
+    GOM_ELM_ALL_DRY = 14,         /* ELM_backtrace_v1.f90:275-277 (ELM transport) */
+    GOM_ELM_NEG_SUBELEMENT = 15,  /* ELM_backtrace_v1.f90:420-423 (ELM transport) */
+    GOM_ELM_NO_SUBELEMENT = 16    /* ELM_backtrace_v1.f90:463-467 (ELM transport) */
 };
 
 typedef struct gom_status {
@@ -124,7 +127,7 @@ typedef struct gom_params {
     int32_t baroclinic_flag;   /* C5_03 */
     int32_t ana_density;       /* C5_03: 0 full UNESCO EOS, 1 linear */
     int32_t max_iteration_pcg; /* C6 */
-    int32_t transport_flag;    /* C7 (transport_solver must be 1, TVD) */
+    int32_t transport_flag;    /* C7 */
     int32_t trans_sub_iter;    /* C7_1 */
     int32_t h_flux_limiter;    /* C7_1 */
     int32_t v_flux_limiter;    /* C7_1 */
@@ -138,7 +141,8 @@ typedef struct gom_params {
     int32_t turbulence_flag;   /* i_turbulence_flag of turbulence_closure_v1.f90: 0 off (Av, Kv keep
                                   their values, as in the reference time loop), 1 step function of
                                   the Richardson number, 2 Pacanowski-Philander */
-    int32_t reserved;
+    int32_t transport_solver;  /* C7 transport_solver: 0 or 1 TVD (solve_transport_equation_v19),
+                                  2 ELM (solve_transport_equation_ELM_v8) */
     /* Pacanowski-Philander coefficients (h1_pp, h2_pp, vdmax_pp1, vdmax_pp2, vdmin_pp1, vdmin_pp2,
        tdmin_pp of mod_global_variables.f90:909-910) */
     double pp_h1, pp_h2, pp_vdmax1, pp_vdmax2, pp_vdmin1, pp_vdmin2, pp_tdmin;

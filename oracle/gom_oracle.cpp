@@ -480,8 +480,15 @@ int search_straight_line(gom_ctx *c, int &nnel, int &jlev, double time, double x
 }
 
 // ELM_backtrace_v1.f90:15-200 (i_which_backtrack = 1).  Returns 0 or a GOM_ELM_* site.
+// the last substep's foot, surface or level height above it and interpolation weights, which the
+// transport mode of ELM_backtrace_v1.f90:216-473 interpolates the tracers with
+struct ElmFinal {
+    double xt = 0.0, yt = 0.0, zt = 0.0, zup = 0.0;
+    double staint[4] = {0.0, 0.0, 0.0, 0.0};
+};
+
 int elm_backtrace(gom_ctx *c, int bt_step, double bt_dt, double &uuint, double &vvint, double &wwint,
-                  double &x0, double &y0, double &z0, int &nnel, int &jlev, int &near_edge) {
+                  double &x0, double &y0, double &z0, int &nnel, int &jlev, int &near_edge, ElmFinal *fin = nullptr) {
     const double small_06 = F(1.e-6f);
     A2<double> u_node = FD(c, GOM_F_U_NODE), v_node = FD(c, GOM_F_V_NODE), w_node = FD(c, GOM_F_W_NODE);
     A2<double> dz_cell = FD(c, GOM_F_DZ_CELL);
@@ -552,11 +559,186 @@ int elm_backtrace(gom_ctx *c, int bt_step, double bt_dt, double &uuint, double &
             wwint = wwint + vzn[j - 1] * staint[j - 1];
         }
         if (near_edge_line(c, nnel, xt, yt)) near_edge = 1;
+        if (fin) {
+            fin->xt = xt;
+            fin->yt = yt;
+            fin->zt = zt;
+            fin->zup = zup;
+            for (int l = 0; l < 4; ++l) fin->staint[l] = staint[l];
+        }
         if (nfl == 1) break;
         x0 = xt;
         y0 = yt;
         z0 = zt;
     }
+    return 0;
+}
+
+// ELM_backtrace_v1.f90:216-473 (i_which_backtrack = 2): temperature and salinity at the foot.
+// Open-boundary and river cells take the boundary concentrations; otherwise a vertical anchor
+// at the layer middle picks two levels of node and face values, and the foot is located in the
+// element's sub-elements (triangles: three corner triangles and the central one of the face
+// midpoints; quads: four quads of a node, two face midpoints and the cell centre) for an
+// interpolation of node and face values; with a dry node the mean of the wet nodes stands.
+// Returns 0 or a GOM_ELM_* site.
+int elm_tracer_at_foot(gom_ctx *c, const ElmFinal &fin, int nnel, int jlev, double &ttint, double &ssint) {
+    const double small_06 = F(1.e-6f);
+    A2<double> dz_cell = FD(c, GOM_F_DZ_CELL), dzh_c = FD(c, GOM_F_DZHALF_CELL);
+    A2<double> salt_node = FD(c, GOM_F_SALT_NODE), temp_node = FD(c, GOM_F_TEMP_NODE),
+               salt_face = FD(c, GOM_F_SALT_FACE), temp_face = FD(c, GOM_F_TEMP_FACE);
+    A1<int32_t> top = FI1(c, GOM_F_TOP_LAYER_CELL), top_n = FI1(c, GOM_F_TOP_LAYER_NODE),
+                top_f = FI1(c, GOM_F_TOP_LAYER_FACE);
+    const double xt = fin.xt, yt = fin.yt, zt = fin.zt, zup = fin.zup;
+    const int ibnd1 = c->ob_element_flag(nnel), ibnd2 = c->Qb_element_flag(nnel);
+    ttint = 0.0;
+    ssint = 0.0;
+    if (ibnd1 > 0) {
+        // salt_at_obck(jlev, ibnd1): the boundary concentration, the same in every layer
+        ssint = c->con_at_ob[(size_t)0 * c->NOB + (ibnd1 - 1)];
+        ttint = c->con_at_ob[(size_t)1 * c->NOB + (ibnd1 - 1)];
+        return 0;
+    }
+    if (ibnd2 > 0) {
+        ssint = c->con_at_qb[(size_t)0 * c->NQB + (ibnd2 - 1)];
+        ttint = c->con_at_qb[(size_t)1 * c->NQB + (ibnd2 - 1)];
+        return 0;
+    }
+    const double zanchor = zup - dz_cell(jlev, nnel) * 0.5;
+    int k1, k2;
+    double zrat2;
+    if (jlev == top(nnel) && zt > zanchor) {
+        k1 = jlev;
+        k2 = jlev;
+        zrat2 = 0.5;
+    } else if (zt > zanchor) {
+        k1 = jlev;
+        k2 = jlev + 1;
+        zrat2 = (zt - zanchor) / dzh_c(jlev, nnel);
+    } else {
+        k1 = std::max(jlev - 1, (int)c->bottom_layer_at_element(nnel));
+        k2 = jlev;
+        zrat2 = 1.0 - (zanchor - zt) / dzh_c(k1, nnel);
+    }
+    zrat2 = std::max(0.0, std::min(1.0, zrat2));
+    const int tq = c->tri_or_quad(nnel);
+    int icount = 0;
+    double ta = 0.0, sa = 0.0, t_xi[4] = {0, 0, 0, 0}, s_xi[4] = {0, 0, 0, 0};
+    for (int l = 1; l <= tq; ++l) {
+        int nd = c->nodenum_at_cell(l, nnel);
+        if (top_n(nd) != 0) {
+            icount = icount + 1;
+            t_xi[l - 1] = temp_node(k1, nd) * (1 - zrat2) + temp_node(k2, nd) * zrat2;
+            s_xi[l - 1] = salt_node(k1, nd) * (1 - zrat2) + salt_node(k2, nd) * zrat2;
+            ta = ta + t_xi[l - 1];
+            sa = sa + s_xi[l - 1];
+        }
+    }
+    if (icount == 0) return GOM_ELM_ALL_DRY;
+    if (icount != tq) {
+        ta = ta / icount;
+        sa = sa / icount;
+        ttint = ta;
+        ssint = sa;
+    } else {
+        ta = ta / icount;
+        sa = sa / icount;
+        ttint = 0.0;
+        ssint = 0.0;
+        for (int l = 1; l <= tq; ++l) {
+            ttint = ttint + t_xi[l - 1] * fin.staint[l - 1];
+            ssint = ssint + s_xi[l - 1] * fin.staint[l - 1];
+        }
+    }
+    auto lev = [&](const A2<double> &a, int e) { return a(k1, e) * (1 - zrat2) + a(k2, e) * zrat2; };
+    const double ar = c->area(nnel);
+    int index_1 = 0;
+    if (tq == 3) {
+        for (int l = 1; l <= 4; ++l) {
+            double aa1, aa2, aa3;
+            int n1 = 0, f1 = 0, f2, f3;
+            if (l <= 3) {
+                n1 = c->nodenum_at_cell(l, nnel);
+                f2 = c->facenum_at_cell(start_end_node(tq, l, 2), nnel);
+                f3 = c->facenum_at_cell(start_end_node(tq, l, 1), nnel);
+                aa1 = calculate_area(xt, c->x_face(f2), c->x_face(f3), yt, c->y_face(f2), c->y_face(f3));
+                aa2 = calculate_area(c->x_node(n1), xt, c->x_face(f3), c->y_node(n1), yt, c->y_face(f3));
+                aa3 = calculate_area(c->x_node(n1), c->x_face(f2), xt, c->y_node(n1), c->y_face(f2), yt);
+            } else {
+                f1 = c->facenum_at_cell(1, nnel);
+                f2 = c->facenum_at_cell(2, nnel);
+                f3 = c->facenum_at_cell(3, nnel);
+                aa1 = calculate_area(xt, c->x_face(f2), c->x_face(f3), yt, c->y_face(f2), c->y_face(f3));
+                aa2 = calculate_area(c->x_face(f1), xt, c->x_face(f3), c->y_face(f1), yt, c->y_face(f3));
+                aa3 = calculate_area(c->x_face(f1), c->x_face(f2), xt, c->y_face(f1), c->y_face(f2), yt);
+            }
+            double aa = std::fabs(aa1) + std::fabs(aa2) + std::fabs(aa3);
+            double subrat = std::fabs(aa - ar / 4) * 4 / ar;
+            if (subrat < 100 * small_06) {
+                index_1 = 1;
+                double sig[3];
+                sig[0] = aa1 * 4 / ar;
+                sig[1] = aa2 * 4 / ar;
+                sig[0] = std::max(0.0, std::min(1.0, sig[0]));
+                sig[1] = std::max(0.0, std::min(1.0, sig[1]));
+                if (sig[0] + sig[1] > 1) {
+                    sig[2] = 0;
+                    sig[1] = 1 - sig[0];
+                } else {
+                    sig[2] = 1 - sig[0] - sig[1];
+                }
+                bool wet = l <= 3 ? (top_n(n1) != 0 && top_f(f2) != 0 && top_f(f3) != 0)
+                                  : (top_f(f1) != 0 && top_f(f2) != 0 && top_f(f3) != 0);
+                if (wet) {
+                    double tx[3], sx[3];
+                    tx[0] = l <= 3 ? lev(temp_node, n1) : lev(temp_face, f1);
+                    sx[0] = l <= 3 ? lev(salt_node, n1) : lev(salt_face, f1);
+                    tx[1] = lev(temp_face, f2);
+                    tx[2] = lev(temp_face, f3);
+                    sx[1] = lev(salt_face, f2);
+                    sx[2] = lev(salt_face, f3);
+                    ttint = tx[0] * sig[0] + tx[1] * sig[1] + tx[2] * sig[2];
+                    ssint = sx[0] * sig[0] + sx[1] * sig[1] + sx[2] * sig[2];
+                    break;
+                }
+            }
+        }
+    } else {
+        for (int l = 1; l <= 4; ++l) {
+            int n1 = c->nodenum_at_cell(l, nnel);
+            int f2 = c->facenum_at_cell(start_end_node(tq, l, 3), nnel);
+            int f4 = c->facenum_at_cell(start_end_node(tq, l, 2), nnel);
+            const double xc = c->x_cell(nnel), yc = c->y_cell(nnel);
+            double aa1 = calculate_area(c->x_node(n1), c->x_face(f2), xt, c->y_node(n1), c->y_face(f2), yt);
+            double aa2 = calculate_area(c->x_face(f2), xc, xt, c->y_face(f2), yc, yt);
+            double aa3 = calculate_area(xc, c->x_face(f4), xt, yc, c->y_face(f4), yt);
+            double aa4 = calculate_area(c->x_face(f4), c->x_node(n1), xt, c->y_face(f4), c->y_node(n1), yt);
+            double bb1 = calculate_area(c->x_node(n1), c->x_face(f2), c->x_face(f4), c->y_node(n1), c->y_face(f2),
+                                        c->y_face(f4));
+            double bb2 = calculate_area(c->x_face(f2), xc, c->x_face(f4), c->y_face(f2), yc, c->y_face(f4));
+            if (bb1 <= 0 || bb2 <= 0) return GOM_ELM_NEG_SUBELEMENT;
+            double bb = bb1 + bb2;
+            double aa = std::fabs(aa1) + std::fabs(aa2) + std::fabs(aa3) + std::fabs(aa4);
+            double subrat = std::fabs(aa - bb) / bb;
+            if (subrat < 4.0 * small_06) {
+                index_1 = 1;
+                double csi, etta, st4[4];
+                int b = bilinear_interpolation(c->x_node(n1), c->x_face(f2), xc, c->x_face(f4), c->y_node(n1),
+                                               c->y_face(f2), yc, c->y_face(f4), xt, yt, csi, etta, st4);
+                if (b) return b;
+                if (top_n(n1) != 0 && top_f(f2) != 0 && top_f(f4) != 0) {
+                    double tx[4] = {lev(temp_node, n1), lev(temp_face, f2), ta, lev(temp_face, f4)};
+                    double sx[4] = {lev(salt_node, n1), lev(salt_face, f2), sa, lev(salt_face, f4)};
+                    ttint = 0.0;
+                    ssint = 0.0;
+                    for (int j = 0; j < 4; ++j) {
+                        ttint = ttint + tx[j] * st4[j];
+                        ssint = ssint + sx[j] * st4[j];
+                    }
+                }
+            }
+        }
+    }
+    if (index_1 == 0) return GOM_ELM_NO_SUBELEMENT;
     return 0;
 }
 
@@ -604,6 +786,7 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
         d.max_nb <= 0 || d.n_ob < 0 || d.n_qb < 0)
         return GOM_E_ARG;
     if (params->transport_flag && params->is_salt == 0 && params->is_temp == 1) return GOM_E_ARG;
+    if (params->transport_solver < 0 || params->transport_solver > 2) return GOM_E_ARG;
     gom_ctx *c = new gom_ctx();
     c->d = d;
     c->p = *params;
@@ -1749,10 +1932,203 @@ int gom_step_node_velocity(gom_ctx *c) {
 }
 
 // solve_transport_equation_v19.f90:7-1482 (transport_solver = 1, tracers S and T)
+// solve_transport_equation_ELM_v8.f90:7-346 (transport_solver = 2): temperature and salinity
+// backtracked from every wet cell-layer centre (ELM_backtrace_v1 in transport mode), explicit
+// horizontal diffusion, implicit vertical diffusion, node and face averages.  Reproduced as the
+// reference has them: the horizontal sums use the face's second cell as the neighbour and the
+// salinity sums go to temperature and the temperature sums to salinity (:137-151); the top row's
+// upper coefficient is -dt + Kv/dzhalf (:188); no clamp; dry cells and dry nodes keep their
+// previous values; face values are the mean of the two node values in every layer.  The heat
+// source term of :120 is left out (phi_sz comes from the heat-balance module, not part of the
+// core).
+static int transport_elm(gom_ctx *c) {
+    const gom_params &p = c->p;
+    const int L = c->L, NC = c->NC, NF = c->NF, NN = c->NN;
+    const double dt = p.dt;
+    A2<double> salt_cell = FD(c, GOM_F_SALT_CELL), temp_cell = FD(c, GOM_F_TEMP_CELL), dz_cell = FD(c, GOM_F_DZ_CELL),
+               dzh_c = FD(c, GOM_F_DZHALF_CELL), dz_face = FD(c, GOM_F_DZ_FACE), dz_cn = FD(c, GOM_F_DZ_CELL_NEW),
+               wn_cell = FD(c, GOM_F_WN_CELL), u_node = FD(c, GOM_F_U_NODE), v_node = FD(c, GOM_F_V_NODE),
+               Kh = FD(c, GOM_F_KH), Kv = FD(c, GOM_F_KV);
+    A2<double> salt_new = FD(c, GOM_F_SALT_CELL_NEW), temp_new = FD(c, GOM_F_TEMP_CELL_NEW),
+               salt_node = FD(c, GOM_F_SALT_NODE), temp_node = FD(c, GOM_F_TEMP_NODE),
+               salt_face = FD(c, GOM_F_SALT_FACE), temp_face = FD(c, GOM_F_TEMP_FACE);
+    A2<int32_t> nsub = FI(c, GOM_F_NUM_SUB_ELM);
+    A1<double> eta_cell = FD1(c, GOM_F_ETA_CELL);
+    A1<int32_t> top = FI1(c, GOM_F_TOP_LAYER_CELL), top_n = FI1(c, GOM_F_TOP_LAYER_NODE);
+    std::vector<double> tc_bt((size_t)L * NC, 0.0), sc_bt((size_t)L * NC, 0.0), trhs((size_t)L * NC, 0.0),
+        srhs((size_t)L * NC, 0.0);
+    auto AT = [&](std::vector<double> &v, int k, int i) -> double & { return v[(size_t)(i - 1) * L + k - 1]; };
+    // :59-125 backtracking
+    std::atomic<int> rc{GOM_OK};
+    OMP_FOR
+    for (int i = 1; i <= NC; ++i) {
+        if (rc.load(std::memory_order_relaxed) != GOM_OK) continue;
+        if (top(i) == 0) continue;   // tc_bt = sc_bt = 0
+        for (int k = c->bottom_layer_at_element(i); k <= top(i); ++k) {
+            int nnel = i, jlev = k;
+            double x0 = c->x_cell(i), y0 = c->y_cell(i), z0;
+            if (k == top(nnel)) z0 = p.msl + eta_cell(nnel) - dz_cell(k, nnel) * 0.5;
+            else z0 = c->zl(k) - dz_cell(k, nnel) * 0.5;
+            double u_temp = 0.0, v_temp = 0.0;
+            int bt_step = 0;
+            const int tq = c->tri_or_quad(i);
+            for (int l = 1; l <= tq; ++l) {
+                int nd = c->nodenum_at_cell(l, i);
+                u_temp = u_temp + (u_node(k, nd) + u_node(k - 1, nd)) * 0.5;
+                v_temp = v_temp + (v_node(k, nd) + v_node(k - 1, nd)) * 0.5;
+                bt_step = bt_step + nsub(k, nd);
+            }
+            u_temp = u_temp / tq;
+            v_temp = v_temp / tq;
+            bt_step = bt_step / tq;
+            double uuint = u_temp, vvint = v_temp, wwint = (wn_cell(k, i) + wn_cell(k - 1, i)) * 0.5;
+            double vmag = std::sqrt(uuint * uuint + vvint * vvint + wwint * wwint);
+            if (vmag <= F(1.e-4f)) {
+                AT(tc_bt, k, i) = temp_cell(k, i);
+                AT(sc_bt, k, i) = salt_cell(k, i);
+            } else {
+                double bt_dt = dt / bt_step;
+                int near = 0;
+                ElmFinal fin;
+                int e = elm_backtrace(c, bt_step, bt_dt, uuint, vvint, wwint, x0, y0, z0, nnel, jlev, near, &fin);
+                double ttint = 0.0, ssint = 0.0;
+                if (!e) e = elm_tracer_at_foot(c, fin, nnel, jlev, ttint, ssint);
+                if (e) {
+                    set_err(c, GOM_E_ELM, e, i, k, 0.0);
+                    rc = GOM_E_ELM;
+                    break;
+                }
+                AT(tc_bt, k, i) = ttint;
+                AT(sc_bt, k, i) = ssint;
+            }
+        }
+    }
+    if (rc.load() != GOM_OK) return rc.load();
+    // :133-154 explicit horizontal diffusion
+    OMP_FOR
+    for (int i = 1; i <= NC; ++i) {
+        for (int k = c->bottom_layer_at_element(i); k <= top(i); ++k) {
+            double sum1 = 0.0, sum2 = 0.0;
+            for (int l = 1; l <= c->tri_or_quad(i); ++l) {
+                int j = c->facenum_at_cell(l, i);
+                int ie = c->adj_cellnum_at_face(2, j);
+                if (ie != 0) {
+                    double rtemp1 = c->face_length(j) * dz_face(k, j) * Kh(k, j) / c->delta_j(j);
+                    sum1 = sum1 + rtemp1 * (salt_cell(k, ie) - salt_cell(k, i));
+                    sum2 = sum2 + rtemp1 * (temp_cell(k, ie) - temp_cell(k, i));
+                }
+            }
+            sum1 = sum1 * dt / (c->area(i) * dz_cell(k, i));
+            sum2 = sum2 * dt / (c->area(i) * dz_cell(k, i));
+            AT(trhs, k, i) = AT(tc_bt, k, i) + sum1;
+            AT(srhs, k, i) = AT(sc_bt, k, i) + sum2;
+        }
+    }
+    // :163-236 implicit vertical diffusion, extension below the bottom and above the top
+    OMP_FOR
+    for (int i = 1; i <= NC; ++i) {
+        if (rc.load(std::memory_order_relaxed) != GOM_OK) continue;
+        const int t = top(i), b = c->bottom_layer_at_element(i);
+        if (t == 0) continue;
+        const int nvl = t - b + 1;
+        double am[GOM_ORACLE_MAXL + 1] = {0}, bm[GOM_ORACLE_MAXL + 1] = {0}, cm[GOM_ORACLE_MAXL + 1] = {0},
+               gm[GOM_ORACLE_MAXL + 1] = {0}, rr[(GOM_ORACLE_MAXL + 1) * 2] = {0}, sol[(GOM_ORACLE_MAXL + 1) * 2] = {0};
+        const int nmax = L + 1;
+        for (int k = b + 1; k <= t - 1; ++k) {
+            int kk = t - k + 1;
+            am[kk - 1] = -dt * Kv(k, i) / dzh_c(k, i);
+            cm[kk - 1] = -dt * Kv(k - 1, i) / dzh_c(k - 1, i);
+            bm[kk - 1] = -am[kk - 1] + dz_cell(k, i) - cm[kk - 1];
+        }
+        if (t == b) {
+            bm[0] = dz_cell(t, i);
+        } else {
+            cm[0] = -dt + Kv(t - 1, i) / dzh_c(t - 1, i);
+            bm[0] = dz_cell(t, i) - cm[0];
+            am[nvl - 1] = -dt * Kv(b, i) / dzh_c(b, i);
+            bm[nvl - 1] = -am[nvl - 1] + dz_cell(b, i);
+        }
+        for (int k = 1; k <= nvl; ++k) {
+            int kk = t - k + 1;
+            rr[0 * nmax + k - 1] = dz_cell(kk, i) * AT(trhs, kk, i);
+            rr[1 * nmax + k - 1] = dz_cell(kk, i) * AT(srhs, kk, i);
+        }
+        if (!tridiagonal_solver(nmax, nvl, 2, am, bm, cm, rr, sol, gm)) {
+            set_err(c, GOM_E_ZERO_PIVOT, 210, i, 0, 0.0);
+            rc = GOM_E_ZERO_PIVOT;
+            continue;
+        }
+        for (int k = 1; k <= nvl; ++k) {
+            int klev = t + 1 - k;
+            temp_new(klev, i) = sol[0 * nmax + k - 1];
+            salt_new(klev, i) = sol[1 * nmax + k - 1];
+        }
+        for (int k = 1; k <= b - 1; ++k) {
+            temp_new(k, i) = temp_new(b, i);
+            salt_new(k, i) = salt_new(b, i);
+        }
+        for (int k = t + 1; k <= L; ++k) {
+            temp_new(k, i) = temp_new(t, i);
+            salt_new(k, i) = salt_new(t, i);
+        }
+    }
+    if (rc.load() != GOM_OK) return rc.load();
+    // :262-330 node averages with the fill from above, then the extension of wet nodes
+    OMP_FOR
+    for (int i = 1; i <= NN; ++i) {
+        for (int k = top_n(i); k >= c->bottom_layer_at_node(i); --k) {
+            double sum0 = 0.0, sum1 = 0.0, sum2 = 0.0;
+            int icount = 0;
+            for (int l = 1; l <= c->adj_cells_at_node(i); ++l) {
+                int ie = c->adj_cellnum_at_node(l, i);
+                if (k >= c->bottom_layer_at_element(ie) && k <= top(ie)) {
+                    sum0 = sum0 + c->area(ie) * dz_cn(k, ie);
+                    sum1 = sum1 + c->area(ie) * dz_cn(k, ie) * temp_new(k, ie);
+                    sum2 = sum2 + c->area(ie) * dz_cn(k, ie) * salt_new(k, ie);
+                } else {
+                    icount = icount + 1;
+                }
+            }
+            if (sum0 == 0.0) {
+                temp_node(k, i) = 0.0;
+                salt_node(k, i) = 0.0;
+            } else {
+                temp_node(k, i) = sum1 / sum0;
+                salt_node(k, i) = sum2 / sum0;
+            }
+            if (icount == c->adj_cells_at_node(i) && k != top_n(i)) {
+                temp_node(k, i) = temp_node(k + 1, i);
+                salt_node(k, i) = salt_node(k + 1, i);
+            }
+        }
+        if (top_n(i) == 0) continue;
+        const int kb = c->bottom_layer_at_node(i), kt = top_n(i);
+        for (int k = 1; k <= kb - 1; ++k) {
+            temp_node(k, i) = temp_node(kb, i);
+            salt_node(k, i) = salt_node(kb, i);
+        }
+        for (int k = kt + 1; k <= L; ++k) {
+            temp_node(k, i) = temp_node(kt, i);
+            salt_node(k, i) = salt_node(kt, i);
+        }
+    }
+    // :332-339 face values
+    OMP_FOR
+    for (int j = 1; j <= NF; ++j) {
+        int n1 = c->nodenum_at_face(1, j), n2 = c->nodenum_at_face(2, j);
+        for (int k = 1; k <= L; ++k) {
+            salt_face(k, j) = (salt_node(k, n1) + salt_node(k, n2)) * F(0.5f);
+            temp_face(k, j) = (temp_node(k, n1) + temp_node(k, n2)) * F(0.5f);
+        }
+    }
+    return GOM_OK;
+}
+
 int gom_step_transport(gom_ctx *c) {
     if (!c) return GOM_E_ARG;
     const gom_params &p = c->p;
     if (!p.transport_flag) return GOM_OK;
+    if (p.transport_solver == 2) return transport_elm(c);
     const int L = c->L, NC = c->NC, NF = c->NF, NN = c->NN;
     const double dt = p.dt, theta = p.theta, rho_o = p.rho_o;
     const int ntr = (p.is_salt ? 1 : 0) + (p.is_temp ? 1 : 0);

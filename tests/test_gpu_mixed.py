@@ -146,3 +146,22 @@ def test_mixed_volume_conserved_in_closed_basin(gpu_lib):
     v1, _ = g.conservation()
     assert abs(v1 - v0) <= 1e-12 * v0, f"volume drift {abs(v1 - v0) / v0:.3e}"
     assert np.abs(g.get_field("eta_cell")).max() > 1e-3
+
+
+def test_elm_transport_mixed_tracks_fp64(gpu_lib):
+    """The ELM transport in a mixed-precision context tracks the FP64 one (15 steps)."""
+    deck = estuary(nx=30, ny=14, dx=100.0, n_layers=12, trans_sub_iter=1)
+    deck = dataclasses.replace(deck, params=dataclasses.replace(deck.params, transport_solver=2))
+    st = initial_state(deck)
+    a = GomCore(deck, lib=gpu_lib)
+    b = GomCore(mixed(deck), lib=gpu_lib)
+    prepare(a, st)
+    prepare(b, st)
+    fa, fb = HostForcing(deck), HostForcing(deck)
+    for it in range(1, 16):
+        a.set_forcing(fa.step(it))
+        b.set_forcing(fb.step(it))
+        a.step_all()
+        b.step_all()
+    for name in ("salt_cell", "temp_cell", "salt_node"):
+        assert rel_err(b.get_field(name), a.get_field(name)) < 2e-5, name

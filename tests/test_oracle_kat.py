@@ -368,3 +368,54 @@ def test_segment_intersection_inclusive(oracle_so):
     assert f == 1 and np.allclose(xy, [1, 1])
     assert hit(0, 0, 1, 0, 0, 1, 1, 1)[0] == 0  # parallel
     assert hit(0, 0, 1, 1, 2, 0, 3, -1)[0] == 0  # disjoint
+
+
+def test_elm_transport_keeps_uniform_tracers(oracle_so):
+    """transport_solver = 2 (solve_transport_equation_ELM_v8): with uniform tracers every
+    backtracked value, every diffusive difference and every vertical solve returns the uniform
+    value (the reference's top-row coefficient -dt + Kv/dzhalf keeps the row sums), so the
+    tracers stay uniform under the tide while the walk does move feet."""
+    import dataclasses
+    deck = tidal_basin(nx=14, ny=10)
+    deck = dataclasses.replace(deck, params=dataclasses.replace(deck.params, transport_solver=2))
+    r = _run(deck, oracle_so, steps=20)
+    c = r.core
+    top = c.get_field("top_layer_cell")
+    bot = deck.geo["bottom_layer_at_element"]
+    s = c.get_field("salt_cell").reshape(deck.n_cells, deck.n_layers)
+    t = c.get_field("temp_cell").reshape(deck.n_cells, deck.n_layers)
+    for i in range(deck.n_cells):
+        sl = slice(bot[i] - 1, top[i])
+        assert np.abs(s[i, sl] - 30.0).max() < 1e-9
+        assert np.abs(t[i, sl] - 20.0).max() < 1e-9
+    assert np.abs(c.get_field("salt_node") - 30.0).max() < 1e-9
+    assert np.count_nonzero(c.get_field("elm_foot")) > 0
+
+
+def test_elm_transport_swaps_the_horizontal_sums(oracle_so):
+    """The explicit horizontal step of solve_transport_equation_ELM_v8.f90:137-151 adds the
+    salinity differences to temperature and the temperature differences to salinity: with a
+    salinity gradient and uniform temperature at rest, temperature changes and salinity does
+    not (no advection, no vertical gradient)."""
+    import dataclasses
+    deck = tidal_basin(nx=10, ny=8, closed=True)
+    deck = dataclasses.replace(deck, params=dataclasses.replace(deck.params, transport_solver=2, kh_0=10.0))
+    st = initial_state(deck)
+    L = deck.n_layers
+    x = np.repeat(deck.geo["x_cell"], L)
+    st["salt_cell"] = 20.0 + 10.0 * x / x.max()
+    core = GomCore(deck, lib_path=oracle_so)
+    prepare(core, st)
+    core.set_forcing(HostForcing(deck).step(1))
+    for ph in TIME_LOOP:
+        core.step(ph)
+    t_new = core.get_field("temp_cell_new")
+    s_new = core.get_field("salt_cell_new")
+    top = core.get_field("top_layer_cell")
+    bot = deck.geo["bottom_layer_at_element"]
+    wet = np.zeros_like(t_new, dtype=bool).reshape(deck.n_cells, L)
+    for i in range(deck.n_cells):
+        wet[i, bot[i] - 1:top[i]] = True
+    wet = wet.ravel()
+    assert np.abs(t_new[wet] - 20.0).max() > 1e-6
+    assert np.abs(s_new[wet] - st["salt_cell"][wet]).max() < 1e-9
