@@ -510,6 +510,7 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
         if (e == cudaSuccess) e = dalloc(c, ztop, NC);
         if (e == cudaSuccess) e = dalloc(c, dry, NC);
         if (e == cudaSuccess) e = dalloc(c, &zbot, NC);
+        if (e == cudaSuccess && c->mixed) e = dalloc(c, &c->xf.s.ztop_cell_f, NC);
         if (e == cudaSuccess) e = launch_cell_zbot(G, params->msl, zbot, c->x.stream);
         G.zbot_cell = zbot;
     }
@@ -654,7 +655,8 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
                    {c->x.g.delta_j, &c->x.g.delta_j_f, NF},
                    {c->x.g.cos_theta, &c->x.g.cos_theta_f, NF},
                    {c->x.g.sin_theta, &c->x.g.sin_theta_f, NF},
-                   {W.node_weight, &c->x.g.node_weight_f, NN}};
+                   {W.node_weight, &c->x.g.node_weight_f, NN},
+                   {c->x.g.z_level, &c->x.g.z_level_f, (long)c->x.g.L + 1}};
         for (auto &cv : f32) {
             float *d = nullptr;
             if (dalloc(c, &d, (size_t)cv.n) != cudaSuccess) return fail(GOM_E_NOMEM);

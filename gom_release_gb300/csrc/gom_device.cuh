@@ -48,6 +48,7 @@ struct Geom {
     // in FP64 contexts): a conversion from FP64 runs on the FP64 pipe, so FP32 kernels read these
     const float *area_f, *face_length_f, *delta_j_f, *cos_theta_f, *sin_theta_f, *node_weight_f;
     const float *edge_len2_f;   // squared node-to-node length of each face
+    const float *z_level_f;     // the L + 1 level heights
     const double *zbot_cell;    // MSL - h of each cell
     // packed runs (NR > 1): 0-based first cell / face / node / open-boundary cell of each run
     int NR;
@@ -87,6 +88,7 @@ template <typename R> struct StateT {
     int *elm_foot, *elm_near_edge;
     // derived at the start of each ELM step (not fields): MSL + eta and the ELM dry test per cell
     double *ztop_cell;
+    float *ztop_cell_f;   // FP32 copy of ztop_cell (mixed contexts only)
     int *dry_cell;
 };
 using State = StateT<double>;

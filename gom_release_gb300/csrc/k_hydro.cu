@@ -646,10 +646,20 @@ __device__ int search_straight_line(const Geom &g, const StateT<R> &s, const Par
     }
     if (s.dry_cell[nnel - 1]) return GOM_ELM_END_DRY;
     zt = fmin(fmax(zt, g.zbot_cell[nnel - 1]), s.ztop_cell[nnel - 1]);
-    if (zt <= g.z_level[0] || zt > g.z_level[L]) return GOM_ELM_Z_RANGE;
-    // :376-396 the level k with z_level(k) < zt <= z_level(k+1), unique for increasing levels:
-    // searched from the start layer outwards instead of from the bottom (same k)
-    {
+    if constexpr (MIXED) {
+        // the mixed path locates the layer of the (FP64) foot height in FP32: near a level the
+        // two neighbouring layers give the same interpolated velocity
+        // (the lower bound in FP64: a height just above the grid bottom may round onto it)
+        const float ztf = (float)zt;
+        if (zt <= g.z_level[0] || ztf > g.z_level_f[L]) return GOM_ELM_Z_RANGE;
+        int k = min(max(jlev - 1, 0), L - 1);
+        while (k < L - 1 && ztf > g.z_level_f[k + 1]) ++k;
+        while (k > 0 && ztf <= g.z_level_f[k]) --k;
+        jlev = k + 1;
+    } else {
+        if (zt <= g.z_level[0] || zt > g.z_level[L]) return GOM_ELM_Z_RANGE;
+        // :376-396 the level k with z_level(k) < zt <= z_level(k+1), unique for increasing
+        // levels: searched from the start layer outwards instead of from the bottom (same k)
         int k = min(max(jlev - 1, 0), L - 1);
         while (k < L - 1 && zt > g.z_level[k + 1]) ++k;
         while (k > 0 && zt <= g.z_level[k]) --k;
@@ -698,10 +708,13 @@ __device__ int elm_backtrace(const Geom &g, const StateT<R> &s, const Params &p,
         int e = search_straight_line<R, MIXED>(g, s, p, nnel, jlev, bt_dt, x0, y0, z0, xt, yt, zt, nfl, idt == 1, last);
         if (e) return e;
         int tq = g.tri_or_quad[nnel - 1];
-        double zup = (jlev == s.top_cell[nnel - 1]) ? s.ztop_cell[nnel - 1] : g.z_level[jlev];
-        if (zt > zup) return GOM_ELM_Z_ABOVE;
+        const bool top_layer = jlev == s.top_cell[nnel - 1];
         if constexpr (MIXED) {
-            const float zrat = (float)(zup - zt) / (float)s.dz_cell[ix(jlev, nnel, L)];
+            const float ztf = (float)zt;
+            const float zupf = top_layer ? s.ztop_cell_f[nnel - 1] : g.z_level_f[jlev];
+            if (ztf > zupf) return GOM_ELM_Z_ABOVE;
+            const float zrat = (zupf - ztf) / (float)s.dz_cell[ix(jlev, nnel, L)];
+            const double zup = fin ? (top_layer ? s.ztop_cell[nnel - 1] : g.z_level[jlev]) : 0.0;
             if (!last.valid) {
                 load_local(g, nnel, last.el);
                 last.px = (float)(xt - last.el.xc);
@@ -750,6 +763,8 @@ __device__ int elm_backtrace(const Geom &g, const StateT<R> &s, const Params &p,
                 for (int l = 0; l < tq; ++l) fin->staint[l] = sta[l];
             }
         } else {
+            const double zup = top_layer ? s.ztop_cell[nnel - 1] : g.z_level[jlev];
+            if (zt > zup) return GOM_ELM_Z_ABOVE;
             double zrat = (zup - zt) / s.dz_cell[ix(jlev, nnel, L)];
             double vxn[4], vyn[4], vzn[4], sta[4];
             for (int l = 1; l <= tq; ++l) {
@@ -937,13 +952,16 @@ __device__ void elm_face_layer(const Geom &g, const StateT<R> &s, const Params &
             const float u32 = s.un_face[o], v32 = s.vn_face[o];
             uu = u32 * ctf - v32 * snf;
             vv = u32 * snf + v32 * ctf;
+            const float wd = (s.w_node[ix0(k - 1, n1, L)] + s.w_node[ix0(k - 1, n2, L)]) * 0.5f;
+            const float wu = (s.w_node[ix0(k, n1, L)] + s.w_node[ix0(k, n2, L)]) * 0.5f;
+            ww = (wd + wu) * 0.5f;
         } else {
             uu = unf * ct - vnf * sn;
             vv = unf * sn + vnf * ct;
+            double wdown = (s.w_node[ix0(k - 1, n1, L)] + s.w_node[ix0(k - 1, n2, L)]) * 0.5;
+            double wup = (s.w_node[ix0(k, n1, L)] + s.w_node[ix0(k, n2, L)]) * 0.5;
+            ww = (wdown + wup) * 0.5;
         }
-        double wdown = (s.w_node[ix0(k - 1, n1, L)] + s.w_node[ix0(k - 1, n2, L)]) * 0.5;
-        double wup = (s.w_node[ix0(k, n1, L)] + s.w_node[ix0(k, n2, L)]) * 0.5;
-        ww = (wdown + wup) * 0.5;
         if (decided == 0) {
             slow = false;
         } else {
@@ -1122,6 +1140,7 @@ template <typename R> __global__ void k_cell_z(Geom g, StateT<R> s, Params p) {
     if (i >= g.NC) return;
     const double ztop = p.msl + s.eta_cell[i];
     s.ztop_cell[i] = ztop;
+    if constexpr (sizeof(R) == 4) s.ztop_cell_f[i] = (float)ztop;
     s.dry_cell[i] = (s.top_cell[i] == 0 || g.zbot_cell[i] > ztop) ? 1 : 0;
 }
 
