@@ -513,6 +513,12 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
         if (e == cudaSuccess && c->mixed) e = dalloc(c, &c->xf.s.ztop_cell_f, NC);
         if (e == cudaSuccess) e = launch_cell_zbot(G, params->msl, zbot, c->x.stream);
         G.zbot_cell = zbot;
+        if (c->mixed) {
+            float *zbf = nullptr;
+            if (e == cudaSuccess) e = dalloc(c, &zbf, NC);
+            if (e == cudaSuccess) e = launch_cell_zbot_f(G, zbot, zbf, c->x.stream);
+            G.zbot_cell_f = zbf;
+        }
     }
     // forcing
     int nt = params->trans_sub_iter > 0 ? params->trans_sub_iter : 1;

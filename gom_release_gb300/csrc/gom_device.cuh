@@ -50,6 +50,7 @@ struct Geom {
     const float *edge_len2_f;   // squared node-to-node length of each face
     const float *z_level_f;     // the L + 1 level heights
     const double *zbot_cell;    // MSL - h of each cell
+    const float *zbot_cell_f;   // its FP32 copy (mixed contexts), kept above z_level[0] where it is
     // packed runs (NR > 1): 0-based first cell / face / node / open-boundary cell of each run
     int NR;
     const int *run_cell_start, *run_face_start, *run_node_start, *run_ob_start;

@@ -95,6 +95,7 @@ template <typename R> cudaError_t launch_tr_solve_only(const LaunchT<R> &x);
 cudaError_t launch_elem_local(const Geom &g, float *out, cudaStream_t stream);
 cudaError_t launch_edge_len2(const Geom &g, float *out, cudaStream_t stream);
 cudaError_t launch_cell_zbot(const Geom &g, double msl, double *out, cudaStream_t stream);
+cudaError_t launch_cell_zbot_f(const Geom &g, const double *zbot, float *out, cudaStream_t stream);
 // FP64 copy of an FP32 array (n elements)
 cudaError_t launch_to_double(const float *in, double *out, long n, cudaStream_t stream);
 // FP32 copy of an FP64 array (n elements)

@@ -255,6 +255,22 @@ cudaError_t launch_cell_zbot(const Geom &g, double msl, double *out, cudaStream_
     return cudaGetLastError();
 }
 
+// FP32 copy of the cell bottom heights for the mixed walk: a bottom above the lowest level stays
+// above its FP32 copy (the walk's range test then fails only where the FP64 one does)
+__global__ void k_cell_zbot_f(Geom g, const double *zbot, float *out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.NC) return;
+    const float z0f = (float)g.z_level[0];
+    float zf = (float)zbot[i];
+    if (zbot[i] > g.z_level[0] && !(zf > z0f)) zf = nextafterf(z0f, INFINITY);
+    out[i] = zf;
+}
+
+cudaError_t launch_cell_zbot_f(const Geom &g, const double *zbot, float *out, cudaStream_t stream) {
+    k_cell_zbot_f<<<blocks_for(g.NC, 256), 256, 0, stream>>>(g, zbot, out);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_to_float(const double *in, float *out, long n, cudaStream_t stream) {
     if (n <= 0) return cudaSuccess;
     k_to_float<<<blocks_for(n, 256), 256, 0, stream>>>(in, out, n);
@@ -283,16 +299,27 @@ __device__ __forceinline__ void load_local(const Geom &g, int nel, LocalElem &e)
     e.y[3] = ys.w;
 }
 
+// v[i] of a 4-entry register array for a run-time i in 0..3 (selects: a dynamic index would put
+// the array in local memory)
+__device__ __forceinline__ float sel4(const float (&v)[4], int i) {
+    return i == 0 ? v[0] : i == 1 ? v[1] : i == 2 ? v[2] : v[3];
+}
+
 // 1: inside by the reference's test, 0: outside, -1: not decidable in FP32.  near: an edge line
-// passes within the FP32 error bound of the point.
-__device__ __forceinline__ int classify_f32(const LocalElem &e, float px, float py, bool &near) {
+// passes within the FP32 error bound of the point.  (px, py) is within u (|px| + |py| + pext) of
+// the point's exact offset from the element centre (pext = 0: rounded from the FP64 offset).
+__device__ __forceinline__ int classify_f32(const LocalElem &e, float px, float py, bool &near, float pext = 0.0f) {
     const float u = 5.97e-8f;   // 2^-24
     float lo = 0.0f, hi = 0.0f;
     near = false;
     float twice_area = 0.0f;   // counter-clockwise elements only (as cell.inp requires)
-    for (int l = 0; l < e.tq; ++l) {
-        int m = l + 1 == e.tq ? 0 : l + 1;
-        twice_area += e.x[l] * e.y[m] - e.x[m] * e.y[l];
+    // (loops unrolled over the 4 slots so that every index is a constant)
+#pragma unroll
+    for (int l = 0; l < 4; ++l) {
+        if (l >= e.tq) break;
+        const bool wrap = l + 1 == e.tq;
+        const float xm = wrap ? e.x[0] : e.x[(l + 1) & 3], ym = wrap ? e.y[0] : e.y[(l + 1) & 3];
+        twice_area += e.x[l] * ym - xm * e.y[l];
     }
     if (!(twice_area > 0.0f)) {
         near = true;
@@ -300,6 +327,7 @@ __device__ __forceinline__ int classify_f32(const LocalElem &e, float px, float 
     }
     if (e.tq == 4) {
         // the excess identity needs a convex quad (then its two-triangle area is the polygon's)
+#pragma unroll
         for (int l = 0; l < 4; ++l) {
             const int m = (l + 1) & 3, n = (l + 2) & 3;
             const float turn = (e.x[m] - e.x[l]) * (e.y[n] - e.y[m]) - (e.y[m] - e.y[l]) * (e.x[n] - e.x[m]);
@@ -310,14 +338,17 @@ __device__ __forceinline__ int classify_f32(const LocalElem &e, float px, float 
             }
         }
     }
-    for (int l = 0; l < e.tq; ++l) {
-        int m = l + 1 == e.tq ? 0 : l + 1;
-        float ex = e.x[m] - e.x[l], ey = e.y[m] - e.y[l];
+#pragma unroll
+    for (int l = 0; l < 4; ++l) {
+        if (l >= e.tq) break;
+        const bool wrap = l + 1 == e.tq;
+        const float xm = wrap ? e.x[0] : e.x[(l + 1) & 3], ym = wrap ? e.y[0] : e.y[(l + 1) & 3];
+        float ex = xm - e.x[l], ey = ym - e.y[l];
         float dx = px - e.x[l], dy = py - e.y[l];
         float c = ex * dy - ey * dx;
         // inputs rounded from FP64 differences, two subtractions, two products, one subtraction
-        float mag = (fabsf(e.x[m]) + fabsf(e.x[l]) + fabsf(e.y[m]) + fabsf(e.y[l])) *
-                    (fabsf(px) + fabsf(py) + fabsf(e.x[l]) + fabsf(e.y[l]));
+        float mag = (fabsf(xm) + fabsf(e.x[l]) + fabsf(ym) + fabsf(e.y[l])) *
+                    (fabsf(px) + fabsf(py) + pext + fabsf(e.x[l]) + fabsf(e.y[l]));
         float bnd = 16.0f * u * mag + 1e-30f;
         if (c <= -bnd) {
             lo += -c - bnd;
@@ -343,14 +374,6 @@ struct LastTest {
     int cls;
     bool near;
 };
-
-__device__ __forceinline__ bool in_elem_mixed_rec(const Geom &g, int nel, double x, double y, LastTest &t) {
-    load_local(g, nel, t.el);
-    t.px = (float)(x - t.el.xc);
-    t.py = (float)(y - t.el.yc);
-    t.cls = classify_f32(t.el, t.px, t.py, t.near);
-    return t.cls >= 0 ? t.cls == 1 : in_elem64(g, nel, x, y);
-}
 
 // Mixed path: check_intersection.f90 on element-local FP32 coordinates, deciding only where an
 // error bound on the FP32 determinants settles the reference's FP64 outcome (tt1 and tt2 in [0, 1],
@@ -401,7 +424,7 @@ __device__ __forceinline__ bool crosses(const Geom &g, int nel, const LocalElem 
                                         float ty, double xcg, double ycg, double xt, double yt, float &xin,
                                         float &yin) {
     const int a = l % e.tq, b = (l + 1) % e.tq;   // local nodes start_end_node(tq, l, 1..2) - 1
-    const int r = cross_f32(sx, tx, e.x[a], e.x[b], sy, ty, e.y[a], e.y[b], xin, yin);
+    const int r = cross_f32(sx, tx, sel4(e.x, a), sel4(e.x, b), sy, ty, sel4(e.y, a), sel4(e.y, b), xin, yin);
     if (r >= 0) return r == 1;
     const int jd1 = g.cell_node(start_end_node(e.tq, l, 1), nel), jd2 = g.cell_node(start_end_node(e.tq, l, 2), nel);
     double xi = 0.0, yi = 0.0;
@@ -539,12 +562,11 @@ __device__ int walk_f32(const Geom &g, const StateT<R> &s, int &nnel, double tim
     }
 }
 
-template <typename R, bool MIXED>
+template <typename R>
 __device__ int search_straight_line(const Geom &g, const StateT<R> &s, const Params &p, int &nnel, int &jlev, double time,
                                     double x0, double y0, double z0, double &xt, double &yt, double &zt, int &nfl,
-                                    bool first_substep, LastTest &last) {
+                                    bool first_substep) {
     const double small_06 = F(1.e-6f);
-    const double MSL = p.msl;
     const int L = g.L;
     // The reference's start tests (:26-46) are known to pass and not evaluated, except the dry
     // test of the first substep.  The start-in-element test of the first substep: the start is the
@@ -555,17 +577,9 @@ __device__ int search_straight_line(const Geom &g, const StateT<R> &s, const Par
     if (first_substep && s.dry_cell[nnel - 1])
         return GOM_ELM_START_DRY;
     nfl = 0;
-    last.valid = false;
     double trm = time;
     int nel = nnel;
-    if constexpr (MIXED) {
-        if (!in_elem_mixed_rec(g, nel, xt, yt, last)) {
-            int e = walk_f32(g, s, nnel, time, x0, y0, z0, xt, yt, zt, nfl, last);
-            if (e) return e;
-        } else {
-            last.valid = true;
-        }
-    } else if (!in_elem64(g, nel, xt, yt)) {
+    if (!in_elem64(g, nel, xt, yt)) {
         const double c1 = 1.0 - 1.0e-4;
         double xcg = c1 * x0 + 1.0e-4 * g.x_cell[nel - 1];
         double ycg = c1 * y0 + 1.0e-4 * g.y_cell[nel - 1];
@@ -646,20 +660,10 @@ __device__ int search_straight_line(const Geom &g, const StateT<R> &s, const Par
     }
     if (s.dry_cell[nnel - 1]) return GOM_ELM_END_DRY;
     zt = fmin(fmax(zt, g.zbot_cell[nnel - 1]), s.ztop_cell[nnel - 1]);
-    if constexpr (MIXED) {
-        // the mixed path locates the layer of the (FP64) foot height in FP32: near a level the
-        // two neighbouring layers give the same interpolated velocity
-        // (the lower bound in FP64: a height just above the grid bottom may round onto it)
-        const float ztf = (float)zt;
-        if (zt <= g.z_level[0] || ztf > g.z_level_f[L]) return GOM_ELM_Z_RANGE;
-        int k = min(max(jlev - 1, 0), L - 1);
-        while (k < L - 1 && ztf > g.z_level_f[k + 1]) ++k;
-        while (k > 0 && ztf <= g.z_level_f[k]) --k;
-        jlev = k + 1;
-    } else {
-        if (zt <= g.z_level[0] || zt > g.z_level[L]) return GOM_ELM_Z_RANGE;
-        // :376-396 the level k with z_level(k) < zt <= z_level(k+1), unique for increasing
-        // levels: searched from the start layer outwards instead of from the bottom (same k)
+    if (zt <= g.z_level[0] || zt > g.z_level[L]) return GOM_ELM_Z_RANGE;
+    // :376-396 the level k with z_level(k) < zt <= z_level(k+1), unique for increasing levels:
+    // searched from the start layer outwards instead of from the bottom (same k)
+    {
         int k = min(max(jlev - 1, 0), L - 1);
         while (k < L - 1 && zt > g.z_level[k + 1]) ++k;
         while (k > 0 && zt <= g.z_level[k]) --k;
@@ -682,10 +686,6 @@ __device__ bool near_edge_line(const Geom &g, int nel, double x, double y) {
     return false;
 }
 
-// ELM_backtrace_v1.f90:40-200 (mode 1).  The first substep starts at the face midpoint, on an
-// edge of the start element.  MIXED: FP64 foot coordinates and the reference's point-in-element
-// decisions (FP32 with an error bound, FP64 where that does not decide); the crossing walk,
-// interpolation weights and velocities in FP32 on element-local coordinates.
 // the last substep's foot, the surface or level height above it and the interpolation weights
 // (the ELM transport interpolates the tracers with them, ELM_backtrace_v1.f90:216-473)
 struct ElmFinal {
@@ -693,76 +693,161 @@ struct ElmFinal {
     double staint[4];
 };
 
+// Mixed path of ELM_backtrace_v1.f90:40-200.  The foot is an FP32 offset (dx, dy) from an FP64
+// origin (ox, oy), the start point: the foot's FP64 position is ox + dx, formed only where an FP64
+// decision or the final position needs it, so a substep whose foot stays in its element runs on
+// the FP32 pipe alone.  The element-local offset px = bx + dx with bx = ox - x_centre rounded to
+// FP32 once per element is within u (|px| + |bx|) + 2^-53 |ox + dx| of the exact offset of that
+// FP64 position; classify_f32 decides the reference's point-in-element test under that bound
+// (pext = |bx| + |by| + 2^-28 (|ox| + |oy|)) and in_elem64 at the FP64 position decides the rest,
+// so every decision is the FP64 test of one well-defined point.  A foot that leaves its element
+// is walked by walk_f32 from the FP64 positions.  The height and the layer search are FP32 (the
+// level heights and the column's bottom and surface heights rounded to FP32; near a level the
+// neighbouring layers give the same interpolated velocity), velocities and weights FP32.
+template <typename R>
+__device__ int elm_backtrace_mixed(const Geom &g, const StateT<R> &s, int bt_step, double bt_dt, double &uu,
+                                   double &vv, double &ww, double x0, double y0, double z0, int &nnel, int &jlev,
+                                   int &near_edge, ElmFinal *fin) {
+    const int L = g.L;
+    const float btf = (float)bt_dt;
+    const double ox = x0, oy = y0;
+    const float omag = ldexpf(fabsf((float)ox) + fabsf((float)oy), -28);
+    float uf = (float)uu, vf = (float)vv, wf = (float)ww;
+    float dx0 = 0.0f, dy0 = 0.0f, zs = (float)z0;   // start of the substep
+    int bel = 0;                                    // element of (bx, by)
+    float bx = 0.0f, by = 0.0f;
+    LastTest last;
+    for (int idt = 1; idt <= bt_step; ++idt) {
+        const float dxt = dx0 - btf * uf, dyt = dy0 - btf * vf;
+        float zt = zs - btf * wf;
+        // start tests of search_straight_line.f90:26-46: only the dry test of the first substep
+        // is evaluated (the others are known to pass, as in the FP64 path)
+        if (idt == 1 && s.dry_cell[nnel - 1]) return GOM_ELM_START_DRY;
+        int nfl = 0;
+        double xt64 = 0.0, yt64 = 0.0;   // the foot moved onto an edge crossing (nfl = 1)
+        {
+            LocalElem &el = last.el;
+            load_local(g, nnel, el);
+            if (bel != nnel) {
+                bx = (float)(ox - el.xc);
+                by = (float)(oy - el.yc);
+                bel = nnel;
+            }
+            last.px = bx + dxt;
+            last.py = by + dyt;
+            last.cls = classify_f32(el, last.px, last.py, last.near, fabsf(bx) + fabsf(by) + omag);
+            last.valid = true;
+            if (!(last.cls >= 0 ? last.cls == 1 : in_elem64(g, nnel, ox + (double)dxt, oy + (double)dyt))) {
+                double xt = ox + (double)dxt, yt = oy + (double)dyt, ztd = zt;
+                last.valid = false;
+                int e = walk_f32(g, s, nnel, bt_dt, ox + (double)dx0, oy + (double)dy0, (double)zs, xt, yt, ztd, nfl,
+                                 last);
+                if (e) return e;
+                zt = (float)ztd;
+                xt64 = xt;
+                yt64 = yt;
+            }
+        }
+        if (s.dry_cell[nnel - 1]) return GOM_ELM_END_DRY;
+        zt = fminf(fmaxf(zt, g.zbot_cell_f[nnel - 1]), s.ztop_cell_f[nnel - 1]);
+        if (zt <= g.z_level_f[0] || zt > g.z_level_f[L]) return GOM_ELM_Z_RANGE;
+        {
+            int k = min(max(jlev - 1, 0), L - 1);
+            while (k < L - 1 && zt > g.z_level_f[k + 1]) ++k;
+            while (k > 0 && zt <= g.z_level_f[k]) --k;
+            jlev = k + 1;
+        }
+        jlev = min(max(jlev, g.bottom_cell[nnel - 1]), top_el(s, nnel));
+        const bool top_layer = jlev == s.top_cell[nnel - 1];
+        const float zup = top_layer ? s.ztop_cell_f[nnel - 1] : g.z_level_f[jlev];
+        if (zt > zup) return GOM_ELM_Z_ABOVE;
+        const float zrat = (zup - zt) / (float)s.dz_cell[ix(jlev, nnel, L)];
+        if (!last.valid) {   // the walk stopped on an edge: the foot is the FP64 crossing point
+            load_local(g, nnel, last.el);
+            last.px = (float)(xt64 - last.el.xc);
+            last.py = (float)(yt64 - last.el.yc);
+            last.cls = classify_f32(last.el, last.px, last.py, last.near);
+        }
+        // the foot's FP64 position, formed where needed
+        auto foot_x = [&]() { return nfl ? xt64 : ox + (double)dxt; };
+        auto foot_y = [&]() { return nfl ? yt64 : oy + (double)dyt; };
+        const LocalElem &el = last.el;
+        const float px = last.px, py = last.py;
+        const int tq = el.tq;
+        float sta[4];
+        if (tq == 3) {
+            const float ar = el.ar;
+            sta[0] = calculate_area_t(px, el.x[1], el.x[2], py, el.y[1], el.y[2]) / ar;
+            sta[1] = calculate_area_t(el.x[0], px, el.x[2], el.y[0], py, el.y[2]) / ar;
+            sta[2] = calculate_area_t(el.x[0], el.x[1], px, el.y[0], el.y[1], py) / ar;
+            sta[0] = fmaxf(0.0f, fminf(1.0f, sta[0]));
+            sta[1] = fmaxf(0.0f, fminf(1.0f, sta[1]));
+            if (sta[0] + sta[1] > 1.0f) {
+                sta[2] = 0.0f;
+                sta[1] = 1.0f - sta[0];
+            } else {
+                sta[2] = 1.0f - sta[0] - sta[1];
+            }
+        } else {
+            if (last.cls >= 0 ? last.cls == 0 : out_elem64(g, nnel, foot_x(), foot_y())) return GOM_ELM_QUAD_OUTSIDE;
+            int b = bilinear_interpolation<float>(el.x[0], el.x[1], el.x[2], el.x[3], el.y[0], el.y[1], el.y[2],
+                                                  el.y[3], px, py, sta);
+            if (b) return b;
+        }
+        float fu = 0.0f, fv = 0.0f, fw = 0.0f;
+#pragma unroll
+        for (int l = 1; l <= 4; ++l) {
+            if (l > tq) break;
+            int nd = g.cell_node(l, nnel);
+            long i1 = ix0(jlev - 1, nd, L), i2 = ix0(jlev, nd, L);
+            float w = sta[l - 1];
+            fu = fu + ((float)s.u_node[i2] * (1.0f - zrat) + (float)s.u_node[i1] * zrat) * w;
+            fv = fv + ((float)s.v_node[i2] * (1.0f - zrat) + (float)s.v_node[i1] * zrat) * w;
+            fw = fw + ((float)s.w_node[i2] * (1.0f - zrat) + (float)s.w_node[i1] * zrat) * w;
+        }
+        uf = fu;
+        vf = fv;
+        wf = fw;
+        if (last.near && near_edge_line(g, nnel, foot_x(), foot_y())) near_edge = 1;
+        if (fin) {
+            const double zup64 = top_layer ? s.ztop_cell[nnel - 1] : g.z_level[jlev];
+            *fin = ElmFinal{foot_x(), foot_y(), (double)zt, zup64, {0.0, 0.0, 0.0, 0.0}};
+#pragma unroll
+            for (int l = 0; l < 4; ++l)
+                if (l < tq) fin->staint[l] = sta[l];
+        }
+        if (nfl == 1) break;
+        dx0 = dxt;
+        dy0 = dyt;
+        zs = zt;
+    }
+    uu = uf;
+    vv = vf;
+    ww = wf;
+    return 0;
+}
+
+// ELM_backtrace_v1.f90:40-200 (mode 1).  The first substep starts at the face midpoint, on an
+// edge of the start element (the ELM transport starts at the cell centre).  MIXED: see
+// elm_backtrace_mixed.
 template <typename R, bool MIXED>
 __device__ int elm_backtrace(const Geom &g, const StateT<R> &s, const Params &p, int bt_step, double bt_dt, double &uu,
                              double &vv, double &ww, double x0, double y0, double z0, int &nnel, int &jlev,
                              int &near_edge, ElmFinal *fin = nullptr) {
-    const double small_06 = F(1.e-6f);
-    const int L = g.L;
-    LastTest last;
-    for (int idt = 1; idt <= bt_step; ++idt) {
-        double xt = x0 - bt_dt * uu;
-        double yt = y0 - bt_dt * vv;
-        double zt = z0 - bt_dt * ww;
-        int nfl = 0;
-        int e = search_straight_line<R, MIXED>(g, s, p, nnel, jlev, bt_dt, x0, y0, z0, xt, yt, zt, nfl, idt == 1, last);
-        if (e) return e;
-        int tq = g.tri_or_quad[nnel - 1];
-        const bool top_layer = jlev == s.top_cell[nnel - 1];
-        if constexpr (MIXED) {
-            const float ztf = (float)zt;
-            const float zupf = top_layer ? s.ztop_cell_f[nnel - 1] : g.z_level_f[jlev];
-            if (ztf > zupf) return GOM_ELM_Z_ABOVE;
-            const float zrat = (zupf - ztf) / (float)s.dz_cell[ix(jlev, nnel, L)];
-            const double zup = fin ? (top_layer ? s.ztop_cell[nnel - 1] : g.z_level[jlev]) : 0.0;
-            if (!last.valid) {
-                load_local(g, nnel, last.el);
-                last.px = (float)(xt - last.el.xc);
-                last.py = (float)(yt - last.el.yc);
-                last.cls = classify_f32(last.el, last.px, last.py, last.near);
-            }
-            const LocalElem &el = last.el;
-            const float px = last.px, py = last.py;
-            const bool near = last.near;
-            const int cls = last.cls;
-            float sta[4];
-            if (tq == 3) {
-                const float ar = el.ar;
-                sta[0] = calculate_area_t(px, el.x[1], el.x[2], py, el.y[1], el.y[2]) / ar;
-                sta[1] = calculate_area_t(el.x[0], px, el.x[2], el.y[0], py, el.y[2]) / ar;
-                sta[2] = calculate_area_t(el.x[0], el.x[1], px, el.y[0], el.y[1], py) / ar;
-                sta[0] = fmaxf(0.0f, fminf(1.0f, sta[0]));
-                sta[1] = fmaxf(0.0f, fminf(1.0f, sta[1]));
-                if (sta[0] + sta[1] > 1.0f) {
-                    sta[2] = 0.0f;
-                    sta[1] = 1.0f - sta[0];
-                } else {
-                    sta[2] = 1.0f - sta[0] - sta[1];
-                }
-            } else {
-                if (cls >= 0 ? cls == 0 : out_elem64(g, nnel, xt, yt)) return GOM_ELM_QUAD_OUTSIDE;
-                int b = bilinear_interpolation<float>(el.x[0], el.x[1], el.x[2], el.x[3], el.y[0], el.y[1], el.y[2],
-                                                      el.y[3], px, py, sta);
-                if (b) return b;
-            }
-            float fu = 0.0f, fv = 0.0f, fw = 0.0f;
-            for (int l = 1; l <= tq; ++l) {
-                int nd = g.cell_node(l, nnel);
-                long i1 = ix0(jlev - 1, nd, L), i2 = ix0(jlev, nd, L);
-                float w = sta[l - 1];
-                fu = fu + ((float)s.u_node[i2] * (1.0f - zrat) + (float)s.u_node[i1] * zrat) * w;
-                fv = fv + ((float)s.v_node[i2] * (1.0f - zrat) + (float)s.v_node[i1] * zrat) * w;
-                fw = fw + ((float)s.w_node[i2] * (1.0f - zrat) + (float)s.w_node[i1] * zrat) * w;
-            }
-            uu = fu;
-            vv = fv;
-            ww = fw;
-            if (near && near_edge_line(g, nnel, xt, yt)) near_edge = 1;
-            if (fin) {
-                *fin = ElmFinal{xt, yt, zt, zup, {0.0, 0.0, 0.0, 0.0}};
-                for (int l = 0; l < tq; ++l) fin->staint[l] = sta[l];
-            }
-        } else {
+    if constexpr (MIXED) {
+        return elm_backtrace_mixed(g, s, bt_step, bt_dt, uu, vv, ww, x0, y0, z0, nnel, jlev, near_edge, fin);
+    } else {
+        const double small_06 = F(1.e-6f);
+        const int L = g.L;
+        for (int idt = 1; idt <= bt_step; ++idt) {
+            double xt = x0 - bt_dt * uu;
+            double yt = y0 - bt_dt * vv;
+            double zt = z0 - bt_dt * ww;
+            int nfl = 0;
+            int e = search_straight_line<R>(g, s, p, nnel, jlev, bt_dt, x0, y0, z0, xt, yt, zt, nfl, idt == 1);
+            if (e) return e;
+            int tq = g.tri_or_quad[nnel - 1];
+            const bool top_layer = jlev == s.top_cell[nnel - 1];
             const double zup = top_layer ? s.ztop_cell[nnel - 1] : g.z_level[jlev];
             if (zt > zup) return GOM_ELM_Z_ABOVE;
             double zrat = (zup - zt) / s.dz_cell[ix(jlev, nnel, L)];
@@ -815,13 +900,13 @@ __device__ int elm_backtrace(const Geom &g, const StateT<R> &s, const Params &p,
                 *fin = ElmFinal{xt, yt, zt, zup, {0.0, 0.0, 0.0, 0.0}};
                 for (int l = 0; l < tq; ++l) fin->staint[l] = sta[l];
             }
+            if (nfl == 1) break;
+            x0 = xt;
+            y0 = yt;
+            z0 = zt;
         }
-        if (nfl == 1) break;
-        x0 = xt;
-        y0 = yt;
-        z0 = zt;
+        return 0;
     }
-    return 0;
 }
 
 // solve_nonlinear_advection.f90:52-87.  The reference evaluates, for every node, layer and
