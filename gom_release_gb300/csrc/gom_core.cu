@@ -559,7 +559,8 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
     if (e == cudaSuccess) e = dalloc(c, &W.q, NC);
     if (e == cudaSuccess) e = dalloc(c, &W.d0, NC);
     if (e == cudaSuccess) e = dalloc(c, &W.d1, NC);
-    if (e == cudaSuccess) e = dalloc(c, &W.barrier, 2);
+    // grid barrier (count, generation) or one pair per packed run
+    if (e == cudaSuccess) e = dalloc(c, &W.barrier, 2 * (size_t)PCG_MAX_RUNS);
     if (e == cudaSuccess) e = dalloc(c, &W.pcg_iters, 1);
     if (e == cudaSuccess) e = dalloc(c, &W.run_block_start, (size_t)G.NR + 1);
     if (e == cudaSuccess) e = dalloc(c, &W.run_iters, (size_t)G.NR);
@@ -643,7 +644,8 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
     }
     if (launch_node_weights(c->x) != cudaSuccess) return fail(GOM_E_CUDA);
     {
-        size_t nb = (size_t)c->x.w.pcg_blocks;
+        // two halves: the mixed solvers alternate them with every barrier
+        size_t nb = 2 * (size_t)c->x.w.pcg_blocks;
         if (dalloc(c, &W.partial_dq, nb) != cudaSuccess || dalloc(c, &W.partial_delta, nb) != cudaSuccess)
             return fail(GOM_E_NOMEM);
     }

@@ -53,6 +53,9 @@ using Work = WorkT<double>;
 enum TuneSite { TUNE_ELM = 0, TUNE_MOMENTUM, TUNE_TR_SOLVE, TUNE_TR_LIMITER, TUNE_COUNT };
 constexpr int TUNE_VARIANTS[TUNE_COUNT] = {7, 3, 3, 3};
 
+// packed runs a free-surface solve holds (one barrier pair and one state per run)
+constexpr int PCG_MAX_RUNS = 256;
+
 template <typename R> struct LaunchT {
     int tune[TUNE_COUNT] = {0, 0, 0, 0};
     Geom g;

@@ -252,6 +252,12 @@ __global__ void __launch_bounds__(PCG_THREADS) k_pcg_mixed(PcgMixedArgs a) {
     }
     double delta_0 = 0.0;
     int iters = 0;
+    // The partial sums alternate between two halves of pdq / pdelta with every grid barrier: a
+    // block that has read the sums behind one barrier may write the next ones while a slower
+    // block still reads, and the half it writes is the other one (the barrier after that write
+    // orders the next reuse).
+    int par = 0;
+    const unsigned P = gridDim.x;
     for (int outer = 0;; ++outer) {
         // true residual r = b - A x and its Jacobi norm in FP64; the FP32 residual, d = M^-1 r and
         // the inner r^T d in the same pass (the previous inner step's barrier ordered the x update)
@@ -277,12 +283,13 @@ __global__ void __launch_bounds__(PCG_THREADS) k_pcg_mixed(PcgMixedArgs a) {
         double bs = block_sum<PCG_THREADS>(loc, sh);
         float fbs = block_sumf<PCG_THREADS>(floc, sh);
         if (threadIdx.x == 0) {
-            a.pdelta[blockIdx.x] = bs;
-            a.pdq[blockIdx.x] = (double)fbs;
+            a.pdelta[par * P + blockIdx.x] = bs;
+            a.pdq[par * P + blockIdx.x] = (double)fbs;
         }
         if (!grid_barrier(a.bar, nblocks, a.st)) return;
-        double delta_true = sum_partials(a.pdelta, gridDim.x, sh);
-        float delta_new = (float)sum_partials(a.pdq, gridDim.x, sh);
+        double delta_true = sum_partials(a.pdelta + par * P, gridDim.x, sh);
+        float delta_new = (float)sum_partials(a.pdq + par * P, gridDim.x, sh);
+        par ^= 1;
         if (outer == 0) {
             delta_0 = delta_true;
             if (delta_0 == 0.0) break;
@@ -316,9 +323,10 @@ __global__ void __launch_bounds__(PCG_THREADS) k_pcg_mixed(PcgMixedArgs a) {
                 floc = fmaf(di, sum, floc);
             }
             fbs = block_sumf<PCG_THREADS>(floc, sh);
-            if (threadIdx.x == 0) a.pdq[blockIdx.x] = (double)fbs;
+            if (threadIdx.x == 0) a.pdq[par * P + blockIdx.x] = (double)fbs;
             if (!grid_barrier(a.bar, nblocks, a.st)) return;
-            float dq = (float)sum_partials(a.pdq, gridDim.x, sh);
+            float dq = (float)sum_partials(a.pdq + par * P, gridDim.x, sh);
+            par ^= 1;
             float alpha = delta_new / dq;
             float *dv = first ? dcur : dnext;
             floc = 0.0f;
@@ -332,10 +340,11 @@ __global__ void __launch_bounds__(PCG_THREADS) k_pcg_mixed(PcgMixedArgs a) {
                 floc = fmaf(ri, si, floc);
             }
             fbs = block_sumf<PCG_THREADS>(floc, sh);
-            if (threadIdx.x == 0) a.pdelta[blockIdx.x] = (double)fbs;
+            if (threadIdx.x == 0) a.pdelta[par * P + blockIdx.x] = (double)fbs;
             if (!grid_barrier(a.bar, nblocks, a.st)) return;
             float delta_old = delta_new;
-            delta_new = (float)sum_partials(a.pdelta, gridDim.x, sh);
+            delta_new = (float)sum_partials(a.pdelta + par * P, gridDim.x, sh);
+            par ^= 1;
             beta = delta_new / delta_old;
             if (!first) {
                 float *t = dcur;
@@ -357,7 +366,6 @@ __global__ void __launch_bounds__(PCG_THREADS) k_pcg_mixed(PcgMixedArgs a) {
 // run's scalars from the per-block partial sums in a fixed order, so all blocks agree on every
 // run's alpha, beta and stop test, and on when all runs have stopped.  A converged run freezes
 // while the others continue; the kernel ends when every run has stopped.
-constexpr int PCG_MAX_RUNS = 256;
 
 struct RunRows {
     int run, c0, c1;     // run index, rows [c0, c1)
@@ -520,8 +528,12 @@ __global__ void __launch_bounds__(PCG_THREADS) k_pcg_seg(PcgSegArgs a) {
 
 // mixed precision, packed runs: each run runs the refinement / inner-iteration scheme of
 // k_pcg_mixed as a state machine (true-residual pass, then inner iterations until its inner
-// stop, then a residual pass again ...); all runs advance in lockstep through the same two
-// barriers per step, each doing the work its own state asks for.
+// stop, then a residual pass again ...).  The runs are independent, so each run's blocks meet
+// only at the run's own barrier (bar + 2 r): a run's step costs a barrier over its few blocks
+// instead of the whole grid, a run that has converged leaves, and the others do not wait for
+// it.  All blocks of a run recompute its scalars from its block partials in block order, so they
+// agree on every decision.  Partial sums alternate between two halves of pdq / pdelta with every
+// barrier (as in k_pcg_mixed).
 struct PcgMixedSegArgs {
     Geom g;
     const double *sp, *b;
@@ -531,7 +543,7 @@ struct PcgMixedSegArgs {
     const int *run_block_start;
     int *run_iters;
     unsigned *bar;
-    int *iters;
+    int *iters;   // zero at launch; the largest per-run inner count on return
     int maxit;
     double tol;
     gom_status *st;
@@ -542,15 +554,13 @@ enum { RUN_RESID = 0, RUN_INNER = 1, RUN_DONE = 2 };
 
 __global__ void __launch_bounds__(PCG_THREADS) k_pcg_mixed_seg(PcgMixedSegArgs a) {
     __shared__ double sh[40];
-    __shared__ double s_d0[PCG_MAX_RUNS];
-    __shared__ float s_dn[PCG_MAX_RUNS], s_din0[PCG_MAX_RUNS], s_itol[PCG_MAX_RUNS], s_alpha[PCG_MAX_RUNS],
-        s_beta[PCG_MAX_RUNS];
-    __shared__ int s_mode[PCG_MAX_RUNS], s_first[PCG_MAX_RUNS], s_dpar[PCG_MAX_RUNS], s_outer[PCG_MAX_RUNS],
-        s_it[PCG_MAX_RUNS], s_passb[PCG_MAX_RUNS];
     const Geom &g = a.g;
-    const int NR = g.NR;
-    const unsigned nblocks = gridDim.x + a.phantom;
     const RunRows me = run_rows(g, a.run_block_start);
+    const int run = me.run;
+    const int b0 = a.run_block_start[run];
+    const unsigned nbar = (unsigned)(a.run_block_start[run + 1] - b0) + a.phantom;
+    unsigned *bar = a.bar + 2 * run;
+    const unsigned P = gridDim.x;
     const float FP32_FLOOR = 1e-10f;
     for (long i = me.start; i < me.c1; i += me.stride) {
         const double *row = a.sp + i * 5;
@@ -558,22 +568,15 @@ __global__ void __launch_bounds__(PCG_THREADS) k_pcg_mixed_seg(PcgMixedSegArgs a
         for (int l = 0; l < 5; ++l) row32[l] = (float)row[l];
         a.minv[i] = (float)(1.0 / row[0]);
     }
-    for (int r = threadIdx.x; r < NR; r += blockDim.x) {
-        s_mode[r] = RUN_RESID;
-        s_outer[r] = 0;
-        s_it[r] = 0;
-        s_first[r] = 1;
-        s_dpar[r] = 0;
-    }
-    __syncthreads();
-    for (int step = 0;; ++step) {
+    // the run's state (identical in all of its blocks)
+    int mode = RUN_RESID, outer = 0, its = 0, dpar = 0, par = 0;
+    bool first = true;
+    double d0 = 0.0;
+    float dn = 0.0f, din0 = 0.0f, itol = 0.0f, beta = 0.0f;
+    for (;;) {
         if (failed(a.st)) return;
-        int active = 0;
-        for (int r = 0; r < NR; ++r) active |= s_mode[r] != RUN_DONE;
-        if (!active) break;
-        const int mode = s_mode[me.run];
-        const bool first = s_first[me.run] != 0;
-        float *dcur = s_dpar[me.run] ? a.dB : a.dA, *dnext = s_dpar[me.run] ? a.dA : a.dB;
+        if (mode == RUN_DONE) break;
+        float *dcur = dpar ? a.dB : a.dA, *dnext = dpar ? a.dA : a.dB;
         // pass A: true residual (RESID) or inner matrix-vector product (INNER)
         double loc = 0.0;
         float floc = 0.0f;
@@ -595,8 +598,7 @@ __global__ void __launch_bounds__(PCG_THREADS) k_pcg_mixed_seg(PcgMixedSegArgs a
                 a.dA[i] = df;
                 floc = fmaf(rf, df, floc);
             }
-        } else if (mode == RUN_INNER) {
-            const float beta = s_beta[me.run];
+        } else {
             for (long i = me.start; i < me.c1; i += me.stride) {
                 const float *row = a.sp32 + i * 5;
                 int cell = (int)i + 1;
@@ -606,8 +608,8 @@ __global__ void __launch_bounds__(PCG_THREADS) k_pcg_mixed_seg(PcgMixedSegArgs a
                 for (int l = 1; l <= tq; ++l) {
                     int nb = g.cell_adj(l, cell);
                     if (nb != 0) {
-                        float dn = first ? dcur[nb - 1] : fmaf(beta, dcur[nb - 1], a.s[nb - 1]);
-                        sum = fmaf(row[l], dn, sum);
+                        float dnb = first ? dcur[nb - 1] : fmaf(beta, dcur[nb - 1], a.s[nb - 1]);
+                        sum = fmaf(row[l], dnb, sum);
                     }
                 }
                 if (!first) dnext[i] = di;
@@ -618,44 +620,40 @@ __global__ void __launch_bounds__(PCG_THREADS) k_pcg_mixed_seg(PcgMixedSegArgs a
         double bs = block_sum<PCG_THREADS>(loc, sh);
         float fbs = block_sumf<PCG_THREADS>(floc, sh);
         if (threadIdx.x == 0) {
-            a.pdelta[blockIdx.x] = bs;
-            a.pdq[blockIdx.x] = (double)fbs;
+            a.pdelta[par * P + blockIdx.x] = bs;
+            a.pdq[par * P + blockIdx.x] = (double)fbs;
         }
-        if (!grid_barrier(a.bar, nblocks, a.st)) return;
-        for (int r = threadIdx.x; r < NR; r += blockDim.x) {
-            s_passb[r] = 0;
-            if (s_mode[r] == RUN_RESID) {
-                double dt = run_sum(a.pdelta, a.run_block_start, r);
-                float di = (float)run_sum(a.pdq, a.run_block_start, r);
-                bool stop;
-                if (s_outer[r] == 0) {
-                    s_d0[r] = dt;
-                    stop = dt == 0.0;
-                } else {
-                    stop = sqrt(dt * dt / (s_d0[r] * s_d0[r])) < a.tol;
-                }
-                if (stop || s_it[r] >= a.maxit || !(di > 0.0f)) {
-                    s_mode[r] = RUN_DONE;
-                } else {
-                    s_mode[r] = RUN_INNER;
-                    s_outer[r] += 1;
-                    s_din0[r] = di;
-                    s_dn[r] = di;
-                    s_itol[r] = fmaxf((float)(0.25 * a.tol * s_d0[r] / dt), FP32_FLOOR);
-                    s_first[r] = 1;
-                    s_dpar[r] = 0;
-                }
-                if (s_outer[r] == 0) s_outer[r] = 1;
-            } else if (s_mode[r] == RUN_INNER) {
-                s_alpha[r] = s_dn[r] / (float)run_sum(a.pdq, a.run_block_start, r);
-                s_passb[r] = 1;
+        if (!grid_barrier(bar, nbar, a.st)) return;
+        if (mode == RUN_RESID) {
+            const double dt = run_sum(a.pdelta + par * P, a.run_block_start, run);
+            const float di = (float)run_sum(a.pdq + par * P, a.run_block_start, run);
+            par ^= 1;
+            bool stop;
+            if (outer == 0) {
+                d0 = dt;
+                stop = dt == 0.0;
+            } else {
+                stop = sqrt(dt * dt / (d0 * d0)) < a.tol;
             }
+            if (stop || its >= a.maxit || !(di > 0.0f)) {
+                mode = RUN_DONE;
+            } else {
+                mode = RUN_INNER;
+                outer += 1;
+                din0 = di;
+                dn = di;
+                itol = fmaxf((float)(0.25 * a.tol * d0 / dt), FP32_FLOOR);
+                first = true;
+                dpar = 0;
+            }
+            if (outer == 0) outer = 1;
+            continue;
         }
-        __syncthreads();
-        // pass B: inner updates of the runs that did a matrix-vector product in pass A
+        // pass B: the inner update
+        const float alpha = dn / (float)run_sum(a.pdq + par * P, a.run_block_start, run);
+        par ^= 1;
         floc = 0.0f;
-        if (s_passb[me.run]) {
-            const float alpha = s_alpha[me.run];
+        {
             float *dv = first ? dcur : dnext;
             for (long i = me.start; i < me.c1; i += me.stride) {
                 float di = dv[i];
@@ -668,28 +666,20 @@ __global__ void __launch_bounds__(PCG_THREADS) k_pcg_mixed_seg(PcgMixedSegArgs a
             }
         }
         fbs = block_sumf<PCG_THREADS>(floc, sh);
-        if (threadIdx.x == 0) a.pdelta[blockIdx.x] = (double)fbs;
-        if (!grid_barrier(a.bar, nblocks, a.st)) return;
-        for (int r = threadIdx.x; r < NR; r += blockDim.x) {
-            if (!s_passb[r]) continue;
-            float dold = s_dn[r];
-            float dn = (float)run_sum(a.pdelta, a.run_block_start, r);
-            s_dn[r] = dn;
-            s_beta[r] = dn / dold;
-            if (!s_first[r]) s_dpar[r] ^= 1;
-            s_first[r] = 0;
-            s_it[r] += 1;
-            if (dn < s_itol[r] * s_din0[r] || !(dn > 0.0f) || s_it[r] >= a.maxit) s_mode[r] = RUN_RESID;
-        }
-        __syncthreads();
+        if (threadIdx.x == 0) a.pdelta[par * P + blockIdx.x] = (double)fbs;
+        if (!grid_barrier(bar, nbar, a.st)) return;
+        const float dold = dn;
+        dn = (float)run_sum(a.pdelta + par * P, a.run_block_start, run);
+        par ^= 1;
+        beta = dn / dold;
+        if (!first) dpar ^= 1;
+        first = false;
+        its += 1;
+        if (dn < itol * din0 || !(dn > 0.0f) || its >= a.maxit) mode = RUN_RESID;
     }
-    if (blockIdx.x == 0) {
-        for (int r = threadIdx.x; r < NR; r += blockDim.x) a.run_iters[r] = s_it[r];
-        if (threadIdx.x == 0) {
-            int mx = 0;
-            for (int r = 0; r < NR; ++r) mx = max(mx, s_it[r]);
-            *a.iters = mx;
-        }
+    if ((int)blockIdx.x == b0 && threadIdx.x == 0) {
+        a.run_iters[run] = its;
+        atomicMax(a.iters, its);
     }
 }
 

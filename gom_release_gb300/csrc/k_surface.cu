@@ -191,7 +191,7 @@ template <typename R> cudaError_t launch_free_surface(const LaunchT<R> &x) {
     k_fs_face_sums<<<blocks_for(g.NF, 128), 128, 0, x.stream>>>(x.g, x.s, x.p, x.w.fs_sums);
     k_fs_assemble<<<blocks_for(g.NC, 128), 128, 0, x.stream>>>(x.g, x.s, x.f, x.p, x.w.fs_sums, x.w.sparsem, x.w.rhs,
                                                                x.status);
-    cudaError_t e = cudaMemsetAsync(x.w.barrier, 0, 2 * sizeof(unsigned), x.stream);
+    cudaError_t e = cudaMemsetAsync(x.w.barrier, 0, 2 * sizeof(unsigned) * (size_t)std::max(1, g.NR), x.stream);
     if (e != cudaSuccess) return e;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(x.w.pcg_blocks);
@@ -227,7 +227,8 @@ template <typename R> cudaError_t launch_free_surface(const LaunchT<R> &x) {
         m.tol = x.p.error_tolerance;
         m.st = x.status;
         m.phantom = phantom;
-        e = cudaLaunchKernelEx(&cfg, k_pcg_mixed_seg, m);
+        e = cudaMemsetAsync(x.w.pcg_iters, 0, sizeof(int), x.stream);
+        if (e == cudaSuccess) e = cudaLaunchKernelEx(&cfg, k_pcg_mixed_seg, m);
     } else if (g.NR > 1) {
         PcgSegArgs m;
         m.g = g;
