@@ -51,7 +51,7 @@ using Work = WorkT<double>;
 // Tunable launches: each picks one of a few compiled variants (block size, minimum resident
 // blocks per SM); gom_autotune times the variants on the context's state and keeps the fastest.
 enum TuneSite { TUNE_ELM = 0, TUNE_MOMENTUM, TUNE_TR_SOLVE, TUNE_TR_LIMITER, TUNE_COUNT };
-constexpr int TUNE_VARIANTS[TUNE_COUNT] = {7, 3, 3, 3};
+constexpr int TUNE_VARIANTS[TUNE_COUNT] = {7, 4, 3, 3};
 
 // packed runs a free-surface solve holds (one barrier pair and one state per run)
 constexpr int PCG_MAX_RUNS = 256;

@@ -1952,7 +1952,10 @@ __device__ __forceinline__ void momentum_row(const Geom &g, const StateT<R> &s, 
     dzo = dzk;
 }
 
-template <typename R>
+// SH: the elimination factors and partial solutions in dynamic shared memory, entry (q, r) of
+// thread t at (q L + r) blockDim + t (q = 0 factor, 1..3 solutions), instead of per-thread
+// local arrays that the resident columns push out of L1 (same operations, same results)
+template <typename R, bool SH = false>
 __global__ void __launch_bounds__(256) k_momentum(Geom g, StateT<R> s, Forcing f, Params p, gom_status *st) {
     unsigned tid = flat_tid();
     if (tid >= (unsigned)g.NF) return;
@@ -1964,7 +1967,18 @@ __global__ void __launch_bounds__(256) k_momentum(Geom g, StateT<R> s, Forcing f
     // thomas<3> with each row's matrix entries and right-hand sides formed as its forward
     // elimination step reaches it (the same operations in the same order; only the elimination
     // factors and partial solutions are kept)
-    R gam[GOM_MAXL], sol[GOM_MAXL][3];
+    extern __shared__ __align__(16) unsigned char mom_smem[];
+    R *const shm = reinterpret_cast<R *>(mom_smem) + threadIdx.x;
+    const int bs = blockDim.x;
+    R gam_l[SH ? 1 : GOM_MAXL], sol_l[SH ? 1 : GOM_MAXL][3];
+    auto gam = [&](int r) -> R & {
+        if constexpr (SH) return shm[r * bs];
+        else return gam_l[r];
+    };
+    auto sol = [&](int r, int c) -> R & {
+        if constexpr (SH) return shm[((c + 1) * L + r) * bs];
+        else return sol_l[r][c];
+    };
     R den = R(0), cu_prev = R(0);
     for (int r = 0; r < nvl; ++r) {
         R a_r = R(0), bd_r = R(0), cu_r = R(0), g1, g2, dzr;
@@ -1976,36 +1990,38 @@ __global__ void __launch_bounds__(256) k_momentum(Geom g, StateT<R> s, Forcing f
                 return;
             }
             den = bd_r;
-            sol[0][0] = g1 / den;
-            sol[0][1] = g2 / den;
-            sol[0][2] = dzr / den;
+            sol(0, 0) = g1 / den;
+            sol(0, 1) = g2 / den;
+            sol(0, 2) = dzr / den;
         } else {
-            gam[r] = cu_prev / den;
-            den = bd_r - a_r * gam[r];
+            const R gr = cu_prev / den;
+            gam(r) = gr;
+            den = bd_r - a_r * gr;
             if (den == R(0)) {
                 record_error(st, GOM_E_ZERO_PIVOT, 587, j, 0, 0.0);
                 return;
             }
-            sol[r][0] = (g1 - a_r * sol[r - 1][0]) / den;
-            sol[r][1] = (g2 - a_r * sol[r - 1][1]) / den;
-            sol[r][2] = (dzr - a_r * sol[r - 1][2]) / den;
+            sol(r, 0) = (g1 - a_r * sol(r - 1, 0)) / den;
+            sol(r, 1) = (g2 - a_r * sol(r - 1, 1)) / den;
+            sol(r, 2) = (dzr - a_r * sol(r - 1, 2)) / den;
         }
         cu_prev = cu_r;
     }
     for (int r = nvl - 2; r >= 0; --r) {
-        sol[r][0] = sol[r][0] - gam[r + 1] * sol[r + 1][0];
-        sol[r][1] = sol[r][1] - gam[r + 1] * sol[r + 1][1];
-        sol[r][2] = sol[r][2] - gam[r + 1] * sol[r + 1][2];
+        const R gn = gam(r + 1);
+        sol(r, 0) = sol(r, 0) - gn * sol(r + 1, 0);
+        sol(r, 1) = sol(r, 1) - gn * sol(r + 1, 1);
+        sol(r, 2) = sol(r, 2) - gn * sol(r + 1, 2);
     }
     const bool zero_g1 = (m.btype == -1 && m.ibnd == 0);
     const bool zero_dz1 = (m.btype == -1);
     for (int k = 1; k <= L; ++k) {
         long o = ix(k, j, L);
         if (k <= nvl) {
-            s.ainvg1[o] = zero_g1 ? R(0) : sol[k - 1][0];
-            s.ainvg2[o] = sol[k - 1][1];
-            s.ainvdz1[o] = zero_dz1 ? R(0) : sol[k - 1][2];
-            s.ainvdz2[o] = sol[k - 1][2];
+            s.ainvg1[o] = zero_g1 ? R(0) : sol(k - 1, 0);
+            s.ainvg2[o] = sol(k - 1, 1);
+            s.ainvdz1[o] = zero_dz1 ? R(0) : sol(k - 1, 2);
+            s.ainvdz2[o] = sol(k - 1, 2);
         } else {
             s.ainvg1[o] = R(0);
             s.ainvg2[o] = R(0);
@@ -2028,11 +2044,22 @@ template <typename R> __global__ void k_zero_face_columns(Geom g, StateT<R> s) {
     s.ainvdz2[t] = R(0);
 }
 
-// variants: one thread per column with 128 / 64 / 256 threads per block
+// variants: one thread per column with 128 / 64 / 256 threads per block (local arrays), or 3:
+// the shared-memory form with the largest of 64 / 32 threads whose 4 L entries per thread fit
+// in 48 KB (the local form where none does)
 template <typename R> cudaError_t launch_momentum_columns_only(const LaunchT<R> &x) {
     const int v = x.tune[TUNE_MOMENTUM];
+    if (v == 3) {
+        const size_t per_thread = 4 * (size_t)x.g.L * sizeof(R);
+        for (int bs : {64, 32}) {
+            const size_t smem = per_thread * bs;
+            if (smem > 48 * 1024) continue;
+            k_momentum<R, true><<<blocks_for(x.g.NF, bs), bs, smem, x.stream>>>(x.g, x.s, x.f, x.p, x.status);
+            return cudaGetLastError();
+        }
+    }
     const int bs = v == 1 ? 64 : v == 2 ? 256 : 128;
-    k_momentum<<<blocks_for(x.g.NF, bs), bs, 0, x.stream>>>(x.g, x.s, x.f, x.p, x.status);
+    k_momentum<R, false><<<blocks_for(x.g.NF, bs), bs, 0, x.stream>>>(x.g, x.s, x.f, x.p, x.status);
     return cudaGetLastError();
 }
 
