@@ -161,6 +161,8 @@ def _bind(lib: C.CDLL) -> C.CDLL:
     lib.gom_step_launch.argtypes = [vp]
     lib.gom_step_wait.argtypes = [vp, C.POINTER(C.c_int32)]
     lib.gom_conservation.argtypes = [vp, _D, _D]
+    lib.gom_set_stations.argtypes = [vp, C.c_int32, C.c_int32, _I, _I]
+    lib.gom_station_series.argtypes = [vp, _D]
     lib.gom_set_storms.argtypes = [vp, C.c_int32, C.POINTER(GomStorm), C.c_double]
     lib.gom_cold_start.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_double]
     lib.gom_autotune.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32)]
@@ -409,6 +411,24 @@ class GomCore:
         s = C.c_double()
         self._check(self.lib.gom_conservation(self.ctx, C.byref(v), C.byref(s)), "conservation")
         return v.value, s.value
+
+    # ------------------------------------------------------------------ station time series
+    def set_stations(self, hloc: int, station_cell=None, station_node=None) -> None:
+        """Register the time-series stations (1-based ids): hloc 1 at cells, 2 at nodes."""
+        ids = station_cell if hloc == 1 else station_node
+        arr = np.ascontiguousarray(np.asarray(ids if ids is not None else [], dtype=np.int32))
+        cells = arr.ctypes.data_as(_I) if hloc == 1 else None
+        nodes = arr.ctypes.data_as(_I) if hloc == 2 else None
+        self._check(self.lib.gom_set_stations(self.ctx, hloc, len(arr), cells, nodes), "set_stations")
+        self._n_stations = len(arr)
+
+    def station_series(self) -> np.ndarray:
+        """(n_stations, 7 + 4 L) records: eta, H, ubar, u(1:L), vbar, v(1:L), sbar, salt(1:L),
+        tbar, temp(1:L), air pressure (write_tser_out_files.f90 values)."""
+        n = getattr(self, "_n_stations", 0)
+        out = np.zeros((n, 7 + 4 * self.dims.n_layers), dtype=np.float64)
+        self._check(self.lib.gom_station_series(self.ctx, out.ctypes.data_as(_D)), "station_series")
+        return out
 
     def status(self, clear: bool = False) -> GomStatus:
         st = GomStatus()

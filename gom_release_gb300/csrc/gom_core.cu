@@ -70,6 +70,10 @@ struct gom_ctx {
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t ev_snap_staged = nullptr, ev_snap_done = nullptr;
     bool snap_pending = false;
+    // station time series (gom_set_stations): station ids and the records, on the device
+    int *st_ids = nullptr;
+    double *st_out = nullptr;
+    int st_n = 0, st_hloc = 0;
 };
 
 namespace {
@@ -734,6 +738,8 @@ void gom_destroy(gom_ctx *c) {
     if (c->ev_snap_staged) cudaEventDestroy(c->ev_snap_staged);
     if (c->ev_snap_done) cudaEventDestroy(c->ev_snap_done);
     if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+    if (c->st_ids) cudaFree(c->st_ids);
+    if (c->st_out) cudaFree(c->st_out);
     if (c->x.stream) cudaStreamDestroy(c->x.stream);
     delete c;
 }
@@ -1164,6 +1170,44 @@ int gom_set_storms(gom_ctx *c, int32_t n_storms, const gom_storm *storms, double
     c->n_storms = n_storms;
     // the captured step gains the forcing kernels: capture again on the next launch
     drop_graphs(c);
+    return GOM_OK;
+}
+
+int gom_set_stations(gom_ctx *c, int32_t hloc, int32_t n_stations, const int32_t *station_cell,
+                     const int32_t *station_node) {
+    if (!c || (hloc != 1 && hloc != 2) || n_stations < 0) return GOM_E_ARG;
+    const int32_t *ids = hloc == 1 ? station_cell : station_node;
+    const int limit = hloc == 1 ? c->d.n_cells : c->d.n_nodes;
+    if (n_stations > 0 && !ids) return GOM_E_ARG;
+    for (int q = 0; q < n_stations; ++q)
+        if (ids[q] < 1 || ids[q] > limit) return GOM_E_ARG;
+    CK(cudaStreamSynchronize(c->x.stream));
+    if (c->st_ids) cudaFree(c->st_ids);
+    if (c->st_out) cudaFree(c->st_out);
+    if (c->st_n > 0) c->bytes -= (size_t)c->st_n * (4 + 8 * (7 + 4 * (size_t)c->d.n_layers));
+    c->st_ids = nullptr;
+    c->st_out = nullptr;
+    c->st_n = 0;
+    c->st_hloc = hloc;
+    if (n_stations == 0) return GOM_OK;
+    const size_t rec = 7 + 4 * (size_t)c->d.n_layers;
+    if (cudaMalloc(&c->st_ids, sizeof(int) * n_stations) != cudaSuccess ||
+        cudaMalloc(&c->st_out, sizeof(double) * rec * n_stations) != cudaSuccess)
+        return GOM_E_NOMEM;
+    CK(cudaMemcpy(c->st_ids, ids, sizeof(int) * n_stations, cudaMemcpyHostToDevice));
+    c->st_n = n_stations;
+    c->bytes += (size_t)n_stations * (4 + 8 * rec);
+    return GOM_OK;
+}
+
+int gom_station_series(gom_ctx *c, double *out) {
+    if (!c || (c->st_n > 0 && !out)) return GOM_E_ARG;
+    if (c->st_n == 0) return GOM_OK;
+    const size_t rec = 7 + 4 * (size_t)c->d.n_layers;
+    CK(c->mixed ? launch_station_series(c->xf, c->st_hloc, c->st_n, c->st_ids, c->st_out)
+                : launch_station_series(c->x, c->st_hloc, c->st_n, c->st_ids, c->st_out));
+    CK(cudaMemcpyAsync(out, c->st_out, sizeof(double) * rec * c->st_n, cudaMemcpyDeviceToHost, c->x.stream));
+    CK(cudaStreamSynchronize(c->x.stream));
     return GOM_OK;
 }
 

@@ -82,6 +82,9 @@ template <typename R> cudaError_t launch_transport(const LaunchT<R> &x);
 template <typename R> cudaError_t launch_density(const LaunchT<R> &x);
 template <typename R> cudaError_t launch_turbulence(const LaunchT<R> &x);
 template <typename R> cudaError_t launch_conservation(const LaunchT<R> &x);
+// station records of write_tser_out_files.f90 (7 + 4 L doubles per station) into out
+template <typename R>
+cudaError_t launch_station_series(const LaunchT<R> &x, int hloc, int n, const int *ids, double *out);
 
 // cooperative PCG set-up (grid size from occupancy); called once per context
 template <typename R> cudaError_t pcg_configure(LaunchT<R> &x, int device);

@@ -1425,6 +1425,108 @@ template <typename R> cudaError_t launch_conservation(const LaunchT<R> &x) {
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------- station series
+// write_tser_out_files.f90:9-330: one thread per station forms the station's record
+// [eta, H, ubar, u(1:L), vbar, v(1:L), sbar, salt(1:L), tbar, temp(1:L), air pressure] in the
+// reference's order of operations (the means are serial sums over the layers, as there), so the
+// FP64 path writes the same bits as the reference formulas.
+template <typename R>
+__global__ void k_station_series(Geom g, StateT<R> s, Forcing f, int hloc, int n, const int *ids, double *out) {
+    const int is = blockIdx.x * blockDim.x + threadIdx.x;
+    if (is >= n) return;
+    const int L = g.L;
+    double *o = out + (long)is * (7 + 4 * L);
+    double *ou = o + 2, *ov = o + 3 + L, *os = o + 4 + 2 * L, *ot = o + 5 + 3 * L;
+    const int e = ids[is];
+    if (hloc == 1) {
+        const int ie = e;
+        const double eta = s.eta_cell[ie - 1];
+        o[0] = eta;
+        o[1] = g.h_cell[ie - 1] + eta;
+        const int t = s.top_cell[ie - 1], b = g.bottom_cell[ie - 1];
+        for (int k = 0; k <= L; ++k) ou[k] = ov[k] = 0.0;
+        double sb = 0.0, tb = 0.0;
+        if (t != 0) {
+            // :100-117 (u), :145-162 (v): cell velocity from the node columns, then the depth mean
+            const int tq = g.tri_or_quad[ie - 1];
+            const int nvl = t - b + 1;
+            double ub = 0.0, vb = 0.0;
+            for (int k = b; k <= t; ++k) {
+                double uc = 0.0, vc = 0.0;
+                for (int l = 1; l <= tq; ++l) {
+                    const int nd = g.cell_node(l, ie);
+                    uc = uc + (double)s.u_node[ix0(k - 1, nd, L)] + (double)s.u_node[ix0(k, nd, L)];
+                    vc = vc + (double)s.v_node[ix0(k - 1, nd, L)] + (double)s.v_node[ix0(k, nd, L)];
+                }
+                uc = uc / (double)(tq * 2);
+                vc = vc / (double)(tq * 2);
+                ou[k] = uc;
+                ov[k] = vc;
+            }
+            for (int k = b; k <= t; ++k) ub = ub + ou[k];
+            for (int k = b; k <= t; ++k) vb = vb + ov[k];
+            ou[0] = ub / (double)nvl;
+            ov[0] = vb / (double)nvl;
+            // :189-195, :239-245
+            for (int k = b; k <= t; ++k) sb = sb + (double)s.salt_cell[ix(k, ie, L)];
+            for (int k = b; k <= t; ++k) tb = tb + (double)s.temp_cell[ix(k, ie, L)];
+            sb = sb / (double)nvl;
+            tb = tb / (double)nvl;
+        }
+        os[0] = sb;
+        ot[0] = tb;
+        for (int k = 1; k <= L; ++k) {
+            os[k] = (double)s.salt_cell[ix(k, ie, L)];
+            ot[k] = (double)s.temp_cell[ix(k, ie, L)];
+        }
+        // :312 reads the node array air_p1 at the cell id
+        o[6 + 4 * L] = (ie <= g.NN && f.air_p) ? f.air_p[ie - 1] : 0.0;
+    } else {
+        const int nd = e;
+        const double eta = s.eta_node[nd - 1];
+        o[0] = eta;
+        o[1] = g.h_node[nd - 1] + eta;
+        // update_variables.f90:36-72: depth means of the node columns
+        const int t = s.top_node[nd - 1], b = g.bottom_node[nd - 1];
+        const int nvl = t - b + 1;
+        double ub = 0.0, vb = 0.0, sb = 0.0, tb = 0.0;
+        if (nvl != 0) {
+            for (int k = b - 1; k <= t; ++k) {
+                ub = ub + (double)s.u_node[ix0(k, nd, L)];
+                vb = vb + (double)s.v_node[ix0(k, nd, L)];
+            }
+            ub = ub / (double)(nvl + 1);
+            vb = vb / (double)(nvl + 1);
+            for (int k = b; k <= t; ++k) {
+                sb = sb + (double)s.salt_node[ix(k, nd, L)];
+                tb = tb + (double)s.temp_node[ix(k, nd, L)];
+            }
+            sb = sb / (double)nvl;
+            tb = tb / (double)nvl;
+        }
+        ou[0] = ub;
+        ov[0] = vb;
+        os[0] = sb;
+        ot[0] = tb;
+        for (int k = 1; k <= L; ++k) {
+            ou[k] = (double)s.u_node[ix0(k, nd, L)];
+            ov[k] = (double)s.v_node[ix0(k, nd, L)];
+            os[k] = (double)s.salt_node[ix(k, nd, L)];
+            ot[k] = (double)s.temp_node[ix(k, nd, L)];
+        }
+        o[6 + 4 * L] = f.air_p ? f.air_p[nd - 1] : 0.0;
+    }
+}
+
+template <typename R>
+cudaError_t launch_station_series(const LaunchT<R> &x, int hloc, int n, const int *ids, double *out) {
+    if (n <= 0) return cudaSuccess;
+    k_station_series<<<blocks_for(n, 64), 64, 0, x.stream>>>(x.g, x.s, x.f, hloc, n, ids, out);
+    return cudaGetLastError();
+}
+template cudaError_t launch_station_series<double>(const LaunchT<double> &, int, int, const int *, double *);
+template cudaError_t launch_station_series<float>(const LaunchT<float> &, int, int, const int *, double *);
+
 GOM_INSTANTIATE_LAUNCH(launch_transport)
 GOM_INSTANTIATE_LAUNCH(launch_tr_solve_only)
 GOM_INSTANTIATE_LAUNCH(launch_density)

@@ -10,7 +10,12 @@ such a snapshot:
   ``<id_restart_out><it as I7.7>.out``;
 * ``write_dump3d``: one time slice of the node dump of write_dump3D.f90:4-42, text
   (``IS3D_dump_binary = 0``, one ``F15.5`` time line, then per node ``1 + 6 L + 3`` values in
-  ``E15.5E4``) or unformatted (``IS3D_dump_binary = 1``).
+  ``E15.5E4``) or unformatted (``IS3D_dump_binary = 1``);
+* ``tser_header`` / ``tser_row``: the station time-series files of open_tser_outfiles_tec.f90,
+  open_tser_outfiles_vtk.f90, open_tser_outfiles_sub.f90:28-58 (headers) and
+  write_tser_out_files.f90:30-330 (one row per output step), from the station records of
+  ``GomCore.station_series`` (``gom_station_series``: the values are gathered on the GPU, so an
+  output step moves a few kB instead of whole fields).
 
 Arrays keep the library's layout (layer fastest per entity, ``gom_get_field`` sizes).
 """
@@ -191,3 +196,57 @@ def write_dump3d(fh, time_value: float, st: dict, n_layers: int, binary: bool = 
     fh.write(f"{time_value:15.5f}\n")
     for r in rows:
         fh.write("".join(_fortran_e(float(x)) for x in r) + "\n")
+
+
+# ---------------------------------------------------------------------------- station time series
+# file stems of mod_file_definition.f90:129-142 (.dat Tecplot, .txt Paraview) and titles of
+# open_tser_outfiles_tec.f90:24-38, by tser_list order
+TSER_KINDS = ("eta", "H", "u", "v", "salt", "temp", "airp")
+TSER_FILES = {"eta": "eta_tser_from_msl", "H": "H_tser", "u": "u_tser", "v": "v_tser", "salt": "salt_tser",
+              "temp": "temp_tser", "airp": "airp_tser"}
+_TSER_TITLES = {"eta": "Water elevation time series from msl", "H": "Total water depth (H) time series",
+                "u": "Velocity 2d u time series", "v": "Velocity 2d v time series", "salt": "Salinity time series",
+                "temp": "Temperature time series", "airp": "Air pressure time series"}
+# tser_time -> unit label and tser_time_conv (open_tser_out_files.f90:21-29)
+TSER_TIME = {1: ("sec", 86400.0), 2: ("min", 1440.0), 3: ("hr", 24.0), 4: ("day", 1.0)}
+
+
+def tser_time_value(julian_day: float, tser_time: int) -> float:
+    """The first column of every row: julian_day * tser_time_conv."""
+    return julian_day * TSER_TIME[tser_time][1]
+
+
+def tser_header(kind: str, hloc: int, tser_time: int, names, n_layers: int, fmt: str = "tec") -> str:
+    """Header lines of one time-series file (fmt "tec" for the .dat file, "vtk" for .txt).
+
+    eta and H name one column per station; the layered kinds name the depth mean and each layer
+    as ``<station>_(kk)``, kk = 00..L.  (The reference opens no air-pressure file: its rows go to
+    the unit's default file, so only eta..temp have headers there.)"""
+    out = []
+    if fmt == "tec":
+        out.append('Title = "' + _TSER_TITLES[kind] + (' at cell"' if hloc == 1 else ' at node"') + "\n")
+        first = 'Variables = "Elapsed Time [' + TSER_TIME[tser_time][0] + ']"'
+    else:
+        first = '"Elapsed Time [' + TSER_TIME[tser_time][0] + ']"'
+    if kind in ("eta", "H"):
+        cols = "".join(', "' + str(n).strip() + '"' for n in names)
+    else:
+        cols = "".join(', "' + str(n).strip() + "_(" + f"{k:02d}" + ')"' for n in names for k in range(n_layers + 1))
+    out.append(first + cols + "\n")
+    return "".join(out)
+
+
+def tser_values(kind: str, records: np.ndarray, n_layers: int) -> np.ndarray:
+    """The values one row of ``kind`` writes, per station, from (n_stations, 7 + 4 L) records."""
+    L = n_layers
+    r = np.asarray(records, dtype=np.float64).reshape(-1, 7 + 4 * L)
+    start = {"eta": 0, "H": 1, "u": 2, "v": 3 + L, "salt": 4 + 2 * L, "temp": 5 + 3 * L, "airp": 6 + 4 * L}[kind]
+    width = L + 1 if kind in ("u", "v", "salt", "temp") else 1
+    return r[:, start:start + width]
+
+
+def tser_row(kind: str, time_value: float, records: np.ndarray, n_layers: int) -> str:
+    """One line of write_tser_out_files.f90: E15.5E4 time, then ',' and E15.5E4 per value
+    (format1 for eta, H, air pressure; format2, mean then layers 1..L per station, otherwise)."""
+    vals = tser_values(kind, records, n_layers).ravel()
+    return _fortran_e(float(time_value)) + "".join("," + _fortran_e(float(x)) for x in vals) + "\n"

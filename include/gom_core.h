@@ -447,6 +447,23 @@ void gom_host_free(void *p);
  * accumulated in FP64 (spec: check_conservation.f90:28-57). */
 int gom_conservation(struct gom_ctx *ctx, double *volume, double *salt_mass);
 
+/* Station time series (replaces the state reads of write_tser_out_files.f90:9-330; station ids as
+ * read at read_main_inp.f90:1143-1154).  gom_set_stations keeps the station ids on the device:
+ * hloc 1 = stations at cells (station_cell used), 2 = at nodes (station_node used), 1-based ids.
+ * gom_station_series then gathers, after the work already enqueued, the values the reference
+ * writes for every station and waits for them: out is (7 + 4 L, n_stations) FP64, one record per
+ * station [eta, H, ubar, u(1:L), vbar, v(1:L), sbar, salt(1:L), tbar, temp(1:L), air pressure],
+ * formed as write_tser_out_files.f90 forms them (hloc 1: cell velocities from the node columns,
+ * depth means over the wet layers; hloc 2: node columns and the depth means of
+ * update_variables.f90:36-72).  Air pressure: hloc 1 reads the per-node air_p at the station's
+ * CELL id, as the reference indexes air_p1 (0 where that id exceeds n_nodes); hloc 2 reads air_p at
+ * the node (the reference writes airp_at_node there, the wind-series pressure of
+ * IDW_windp_ser.f90:97 that the host driver holds).  Call it after gom_step_swap / gom_step_all,
+ * where the reference calls write_output_files (main.f90:276). */
+int gom_set_stations(struct gom_ctx *ctx, int32_t hloc, int32_t n_stations, const int32_t *station_cell,
+                     const int32_t *station_node);
+int gom_station_series(struct gom_ctx *ctx, double *out);
+
 /* First recorded failure; clear != 0 resets it. */
 int gom_get_status(struct gom_ctx *ctx, gom_status *status, int clear);
 

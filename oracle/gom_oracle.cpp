@@ -106,6 +106,9 @@ struct gom_ctx {
         g_boundary_type_of_face, g_isflowside3, g_ob_cell_id, g_qb_cell, g_qb_face;
     std::vector<int32_t> run_cell_start;   // packed runs: first cell of each run (0-based), n_runs + 1
     std::vector<int32_t> run_face_start;   // packed runs: first face of each run (0-based), n_runs + 1
+    // time-series stations (gom_set_stations): tser_hloc and the station cells or nodes
+    int tser_hloc = 0;
+    std::vector<int32_t> tser_station;
 
     // ---------------- state storage, indexed by gom_field
     std::vector<double> fd[GOM_F_COUNT];
@@ -2806,6 +2809,118 @@ int gom_step_wait(gom_ctx *c, int32_t *pcg_iters) {
 }
 
 // spec: check_conservation.f90:28-57
+// read_main_inp.f90:1143-1154 (station ids), kept for write_tser_out_files
+int gom_set_stations(gom_ctx *c, int32_t hloc, int32_t n_stations, const int32_t *station_cell,
+                     const int32_t *station_node) {
+    if (!c || (hloc != 1 && hloc != 2) || n_stations < 0) return GOM_E_ARG;
+    const int32_t *ids = hloc == 1 ? station_cell : station_node;
+    if (n_stations > 0 && !ids) return GOM_E_ARG;
+    for (int q = 0; q < n_stations; ++q)
+        if (ids[q] < 1 || ids[q] > (hloc == 1 ? c->NC : c->NN)) return GOM_E_ARG;
+    c->tser_hloc = hloc;
+    c->tser_station.assign(ids, ids + n_stations);
+    return GOM_OK;
+}
+
+// write_tser_out_files.f90:9-330 with the node means of update_variables.f90:36-72; one record of
+// 7 + 4 L values per station: eta, H, ubar, u(1:L), vbar, v(1:L), sbar, salt(1:L), tbar,
+// temp(1:L), air pressure
+int gom_station_series(gom_ctx *c, double *out) {
+    const int n = c ? (int)c->tser_station.size() : 0;
+    if (!c || (n > 0 && !out)) return GOM_E_ARG;
+    const int L = c->L, rec = 7 + 4 * L;
+    A1<double> eta_cell = FD1(c, GOM_F_ETA_CELL), eta_node = FD1(c, GOM_F_ETA_NODE);
+    A2<double> u_node = FD(c, GOM_F_U_NODE), v_node = FD(c, GOM_F_V_NODE);
+    A2<double> salt_cell = FD(c, GOM_F_SALT_CELL), temp_cell = FD(c, GOM_F_TEMP_CELL);
+    A2<double> salt_node = FD(c, GOM_F_SALT_NODE), temp_node = FD(c, GOM_F_TEMP_NODE);
+    A1<int32_t> top_el = FI1(c, GOM_F_TOP_LAYER_CELL), top_nd = FI1(c, GOM_F_TOP_LAYER_NODE);
+    for (int is = 1; is <= n; ++is) {
+        double *o = out + (long)(is - 1) * rec;
+        // record slots: eta, H, then for X in u, v, salt, temp the mean at X(0) and X(1:L)
+        auto U = [&](int k) -> double & { return o[2 + k]; };
+        auto V = [&](int k) -> double & { return o[3 + L + k]; };
+        auto S = [&](int k) -> double & { return o[4 + 2 * L + k]; };
+        auto T = [&](int k) -> double & { return o[5 + 3 * L + k]; };
+        if (c->tser_hloc == 1) {
+            const int ie = c->tser_station[is - 1];
+            o[0] = eta_cell(ie);
+            o[1] = c->h_cell(ie) + eta_cell(ie);
+            double u_cell[GOM_ORACLE_MAXL + 1] = {0.0}, v_cell[GOM_ORACLE_MAXL + 1] = {0.0};
+            double ubar = 0.0, vbar = 0.0, sbar = 0.0, tbar = 0.0;
+            if (top_el(ie) != 0) {
+                const int nvl = top_el(ie) - c->bottom_layer_at_element(ie) + 1;
+                for (int k = c->bottom_layer_at_element(ie); k <= top_el(ie); ++k) {
+                    for (int l = 1; l <= c->tri_or_quad(ie); ++l) {
+                        const int nd = c->nodenum_at_cell(l, ie);
+                        u_cell[k] = u_cell[k] + u_node(k - 1, nd) + u_node(k, nd);
+                    }
+                    u_cell[k] = u_cell[k] / (c->tri_or_quad(ie) * 2);
+                }
+                for (int k = c->bottom_layer_at_element(ie); k <= top_el(ie); ++k) ubar = ubar + u_cell[k];
+                ubar = ubar / nvl;
+                for (int k = c->bottom_layer_at_element(ie); k <= top_el(ie); ++k) {
+                    for (int l = 1; l <= c->tri_or_quad(ie); ++l) {
+                        const int nd = c->nodenum_at_cell(l, ie);
+                        v_cell[k] = v_cell[k] + v_node(k - 1, nd) + v_node(k, nd);
+                    }
+                    v_cell[k] = v_cell[k] / (c->tri_or_quad(ie) * 2);
+                }
+                for (int k = c->bottom_layer_at_element(ie); k <= top_el(ie); ++k) vbar = vbar + v_cell[k];
+                vbar = vbar / nvl;
+                for (int k = c->bottom_layer_at_element(ie); k <= top_el(ie); ++k) sbar = sbar + salt_cell(k, ie);
+                sbar = sbar / nvl;
+                for (int k = c->bottom_layer_at_element(ie); k <= top_el(ie); ++k) tbar = tbar + temp_cell(k, ie);
+                tbar = tbar / nvl;
+            }
+            U(0) = ubar;
+            V(0) = vbar;
+            S(0) = sbar;
+            T(0) = tbar;
+            for (int k = 1; k <= L; ++k) {
+                U(k) = u_cell[k];
+                V(k) = v_cell[k];
+                S(k) = salt_cell(k, ie);
+                T(k) = temp_cell(k, ie);
+            }
+            // :312: air_p1 has n_nodes entries and is read at the cell id
+            o[6 + 4 * L] = ie <= c->NN ? c->air_p[ie - 1] : 0.0;
+        } else {
+            const int i = c->tser_station[is - 1];
+            o[0] = eta_node(i);
+            o[1] = c->h_node(i) + eta_node(i);
+            const int nvl = top_nd(i) - c->bottom_layer_at_node(i) + 1;
+            double ubar = 0.0, vbar = 0.0, sbar = 0.0, tbar = 0.0;
+            if (nvl != 0) {
+                double su = 0.0, sv = 0.0, ss = 0.0, st = 0.0;
+                for (int k = c->bottom_layer_at_node(i) - 1; k <= top_nd(i); ++k) {
+                    su = su + u_node(k, i);
+                    sv = sv + v_node(k, i);
+                }
+                ubar = su / (nvl + 1);
+                vbar = sv / (nvl + 1);
+                for (int k = c->bottom_layer_at_node(i); k <= top_nd(i); ++k) {
+                    ss = ss + salt_node(k, i);
+                    st = st + temp_node(k, i);
+                }
+                sbar = ss / nvl;
+                tbar = st / nvl;
+            }
+            U(0) = ubar;
+            V(0) = vbar;
+            S(0) = sbar;
+            T(0) = tbar;
+            for (int k = 1; k <= L; ++k) {
+                U(k) = u_node(k, i);
+                V(k) = v_node(k, i);
+                S(k) = salt_node(k, i);
+                T(k) = temp_node(k, i);
+            }
+            o[6 + 4 * L] = c->air_p[i - 1];
+        }
+    }
+    return GOM_OK;
+}
+
 int gom_conservation(gom_ctx *c, double *volume, double *salt_mass) {
     if (!c) return GOM_E_ARG;
     A2<double> dz_cell = FD(c, GOM_F_DZ_CELL), salt = FD(c, GOM_F_SALT_CELL);
