@@ -588,6 +588,8 @@ def main():
                     help="full: the benchmark workload; medium (38k cells) and small (6k cells) for profiling")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
+    ap.add_argument("--tuning", default=None,
+                    help="launch variants per tunable site, e.g. 1,3,3,1 (set instead of autotuning)")
     ap.add_argument("--no-phases", action="store_true", help="skip the per-phase timing pass")
     ap.add_argument("--e2e-steps", type=int, default=0)
     ap.add_argument("--workload", default="estuary", choices=["estuary", "ensemble", "serving", "precision"],
@@ -642,7 +644,11 @@ def main():
     run = Run(deck, GomCore(deck, lib=lib), st)
     torch_mod, stream = stream_events(run.core)
     run.advance(args.warmup)
-    tune = run.core.autotune(reps=3) if not args.no_autotune else None
+    if args.tuning:
+        tune = [int(v) for v in args.tuning.split(",")]
+        run.core.set_tuning(tune)
+    else:
+        tune = run.core.autotune(reps=3) if not args.no_autotune else None
     # ---- value: K steps, state resident in HBM, host forcing precomputed
     hf = HostForcing(deck)
     hf.julian_day = run.forcing.julian_day
@@ -686,7 +692,10 @@ def main():
     solve_ms = run.core.profile_kernel(run.core.KERNEL_TRANSPORT_SOLVE, reps=5)
     solve_bytes = TR_SOLVE_BYTES_PER_CELL_LAYER[args.precision] * ncl
     achieved = solve_bytes / (solve_ms * 1e-3) / 1e9
-    traffic = committed_traffic(f"k_tr_solve {args.precision} estuary full") if args.size == "full" else None
+    # FP64 solve variant 3 runs the solve as two kernels (rows per wet cell-layer, column Thomas)
+    list_solve = args.precision == "fp64" and tune is not None and tune[2] == 3
+    solve_kernel = "k_tr_rows64_list + k_tr_thomas_col" if list_solve else "k_tr_solve"
+    traffic = committed_traffic(f"{solve_kernel} {args.precision} estuary full") if args.size == "full" else None
     if args.no_phases:
         phases = {}
     else:
@@ -718,7 +727,7 @@ def main():
             "autotune": tune,
             "pcg_iters_mean": pcg_mean,
         },
-        "roofline": {"bound": "hbm", "kernel": "transport column solve (one subcycle)",
+        "roofline": {"bound": "hbm", "kernel": f"transport solve, one subcycle ({solve_kernel})",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind, "traffic": traffic, "algorithmic_bytes": solve_bytes,
                      "ms_per_launch": solve_ms,

@@ -127,11 +127,16 @@ template <typename R> cudaError_t alloc_layered_work(gom_ctx *c, WorkT<R> &W) {
     if (e == cudaSuccess) e = dalloc(c, &W.uflf, (L + 1) * NF);
     if (e == cudaSuccess) e = dalloc(c, &W.vflf, (L + 1) * NF);
     if (e == cudaSuccess && c->hp.turbulence_flag != 0) e = dalloc(c, &W.kvf, (L + 1) * NF);
-    if (sizeof(R) == sizeof(float) && c->hp.transport_flag) {
+    // rows of the vertical systems: the FP32 transport, and the FP64 list-form solve variant
+    if (c->hp.transport_flag) {
         R **rows[] = {&W.tr_a, &W.tr_b, &W.tr_c};
         for (R **p : rows)
             if (e == cudaSuccess) e = dalloc(c, p, L * NC);
         if (e == cudaSuccess) e = dalloc(c, &W.tr_rhs, L * NC * 2);
+    }
+    // the wet cell-layer list and the top-layer limiter sums: always in the FP32 path, in the FP64
+    // path for its list-form limiter variant
+    if (c->hp.transport_flag) {
         if (e == cudaSuccess) e = dalloc(c, &W.tr_last, 4 * NC);
         if (e == cudaSuccess) e = dalloc(c, &W.cl_list, L * NC);
         if (e == cudaSuccess) e = dalloc(c, &W.cl_off, NC);

@@ -51,7 +51,11 @@ using Work = WorkT<double>;
 // Tunable launches: each picks one of a few compiled variants (block size, minimum resident
 // blocks per SM); gom_autotune times the variants on the context's state and keeps the fastest.
 enum TuneSite { TUNE_ELM = 0, TUNE_MOMENTUM, TUNE_TR_SOLVE, TUNE_TR_LIMITER, TUNE_COUNT };
-constexpr int TUNE_VARIANTS[TUNE_COUNT] = {7, 4, 3, 3};
+// TUNE_TR_SOLVE: FP64 column solve with 128 / 64 / 256 threads, or (3) rows per listed wet
+// cell-layer then one thread per column (the FP32 path's form); TUNE_TR_LIMITER: column kernels
+// with 128 / 64 / 256 threads, or (3) the per-(entity, layer) list kernels (the only form of the
+// FP32 path).  Variant 3 changes nothing in an FP32 context.
+constexpr int TUNE_VARIANTS[TUNE_COUNT] = {7, 4, 4, 4};
 
 // packed runs a free-surface solve holds (one barrier pair and one state per run)
 constexpr int PCG_MAX_RUNS = 256;

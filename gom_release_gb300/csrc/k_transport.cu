@@ -358,43 +358,47 @@ cudaError_t build_cell_layer_list(const Geom &g, const int *top, int *off, int *
     return build_layer_list(g.NC, CellWetRange{top, g.bottom_cell}, off, bsum, list, count, stream);
 }
 
-// FP32 path, :624-805 with one thread per (cell, layer): the upwind-weighted differences of the
-// layer, and the top layer's horizontal sums kept for the vertical ratios
-__device__ __forceinline__ void tr_sums_at(const TArgs<float> &a, int i, int k) {
+// :624-805 with one thread per (cell, layer): the upwind-weighted differences of the layer, and the
+// top layer's horizontal sums kept for the vertical ratios.  Same expressions and order as
+// limiter_column, so the FP64 list form gives the column form's results bit for bit.
+template <typename R> __device__ __forceinline__ void tr_sums_at(const TArgs<R> &a, int i, int k) {
     const Geom &g = a.g;
     const int L = g.L, NC = g.NC;
     const int tl = a.s.top_cell[i - 1], b = g.bottom_cell[i - 1];
-    (void)L;
-    (void)NC;
     const int nvl = tl - b + 1;
     const int tq = g.tri_or_quad[i - 1];
-    float ck[2] = {0.0f, 0.0f}, s1a[2] = {0.0f, 0.0f}, s2a[2] = {0.0f, 0.0f}, s1[2] = {0.0f, 0.0f},
-          s2[2] = {0.0f, 0.0f};
+    R ck[2] = {R(0), R(0)}, s1a[2] = {R(0), R(0)}, s2a[2] = {R(0), R(0)}, s1[2] = {R(0), R(0)},
+      s2[2] = {R(0), R(0)};
     for (int tr = 0; tr < a.ntr; ++tr) {
         ck[tr] = a.con[ic(k, i, tr, L, NC)];
         if (nvl != 1) {
-            if (k > b) {
-                float rt1 = pos_part(a.w.qi[ix0(k - 1, i, L)]);
+            if (k == b) {
+                R rt2 = pos_part(a.w.qi[ix0(k, i, L)]);
+                s1a[tr] = rt2 * (ck[tr] - a.con[ic(k + 1, i, tr, L, NC)]);
+                s2a[tr] = rt2;
+            } else if (k == tl) {
+                R rt1 = pos_part(a.w.qi[ix0(k - 1, i, L)]);
                 s1a[tr] = rt1 * (ck[tr] - a.con[ic(k - 1, i, tr, L, NC)]);
                 s2a[tr] = rt1;
-            }
-            if (k < tl) {
-                float rt2 = pos_part(a.w.qi[ix0(k, i, L)]);
-                s1a[tr] = s1a[tr] + rt2 * (ck[tr] - a.con[ic(k + 1, i, tr, L, NC)]);
-                s2a[tr] = s2a[tr] + rt2;
+            } else {
+                R rt1 = pos_part(a.w.qi[ix0(k - 1, i, L)]);
+                R rt2 = pos_part(a.w.qi[ix0(k, i, L)]);
+                s1a[tr] = rt1 * (ck[tr] - a.con[ic(k - 1, i, tr, L, NC)]) +
+                          rt2 * (ck[tr] - a.con[ic(k + 1, i, tr, L, NC)]);
+                s2a[tr] = rt1 + rt2;
             }
         }
     }
     for (int l = 1; l <= tq; ++l) {
         const int fj = g.cell_face(l, i);
         if (!face_open(g, fj)) continue;
-        const float q2 = flip(a.w.qj[ix(k, fj, L)], g.cell_sign(l, i));
+        const R q2 = flip(a.w.qj[ix(k, fj, L)], g.cell_sign(l, i));
         if (is_neg(q2)) {
             const int nb = g.cell_adj(l, i);
             for (int tr = 0; tr < a.ntr; ++tr) {
-                float cik = nb > 0 ? a.con[ic(k, nb, tr, L, NC)] : oqb_value(a, i, k, tr);
-                s1[tr] = s1[tr] + fabsf(q2) * (ck[tr] - cik);
-                s2[tr] = s2[tr] + fabsf(q2);
+                R cik = nb > 0 ? a.con[ic(k, nb, tr, L, NC)] : oqb_value(a, i, k, tr);
+                s1[tr] = s1[tr] + fabs(q2) * (ck[tr] - cik);
+                s2[tr] = s2[tr] + fabs(q2);
             }
         }
     }
@@ -422,7 +426,7 @@ __global__ void __launch_bounds__(256) k_tr_sums_cl(TArgs<float> a) {
     tr_sums_at(a, i, k);
 }
 
-__global__ void __launch_bounds__(256) k_tr_sums_list(TArgs<float> a) {
+template <typename R> __global__ void __launch_bounds__(256) k_tr_sums_list(TArgs<R> a) {
     const int n = *a.w.cl_count;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         const int code = a.w.cl_list[t];
@@ -431,19 +435,19 @@ __global__ void __launch_bounds__(256) k_tr_sums_list(TArgs<float> a) {
     }
 }
 
-// FP32 path, :806-871 with one thread per (cell, interface)
-__device__ __forceinline__ void tr_vpsi_at(const TArgs<float> &a, int i, int k) {
+// :806-871 with one thread per (cell, interface), the expressions of limiter_column
+template <typename R> __device__ __forceinline__ void tr_vpsi_at(const TArgs<R> &a, int i, int k) {
     const Geom &g = a.g;
     const int L = g.L, NC = g.NC;
     const int b = g.bottom_cell[i - 1];
     for (int tr = 0; tr < a.ntr; ++tr) {
-        const float last1 = a.w.tr_last[((long)tr * NC + i - 1) * 2], last2 = a.w.tr_last[((long)tr * NC + i - 1) * 2 + 1];
-        float *psi = a.w.psii + (long)tr * NC * (L + 1);
-        float ck = a.con[ic(k, i, tr, L, NC)];
-        float qm = k > b ? a.w.qi[ix0(k - 1, i, L)] : 0.0f;
-        float rt1 = last1 + fabsf(qm) * (ck - a.con[ic(k - 1, i, tr, L, NC)]);
-        float rt2 = last2 + fabsf(qm);
-        float rtemp = (a.con[ic(k + 1, i, tr, L, NC)] - ck) * rt2;
+        const R last1 = a.w.tr_last[((long)tr * NC + i - 1) * 2], last2 = a.w.tr_last[((long)tr * NC + i - 1) * 2 + 1];
+        R *psi = a.w.psii + (long)tr * NC * (L + 1);
+        R ck = a.con[ic(k, i, tr, L, NC)];
+        R qm = k > b ? a.w.qi[ix0(k - 1, i, L)] : R(0.0);
+        R rt1 = last1 + fabs(qm) * (ck - a.con[ic(k - 1, i, tr, L, NC)]);
+        R rt2 = last2 + fabs(qm);
+        R rtemp = (a.con[ic(k + 1, i, tr, L, NC)] - ck) * rt2;
         psi[ix0(k, i, L)] = limited_ratio(a.p.h_flux_limiter, a.w.phii[ix0(k, i, L)], rt1, rtemp);
     }
 }
@@ -462,7 +466,7 @@ __global__ void __launch_bounds__(256) k_tr_vpsi_cl(TArgs<float> a) {
     tr_vpsi_at(a, i, k);
 }
 
-__global__ void __launch_bounds__(256) k_tr_vpsi_list(TArgs<float> a) {
+template <typename R> __global__ void __launch_bounds__(256) k_tr_vpsi_list(TArgs<R> a) {
     const int n = *a.w.cl_count;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         const int code = a.w.cl_list[t];
@@ -729,10 +733,10 @@ template <typename R> __global__ void __launch_bounds__(256) k_tr_solve(TArgs<R>
 // implicit vertical system is written to work arrays, and one thread per column then runs the
 // tridiagonal solve.  FP32 arithmetic is cheap on GB300, so the lanes of dry layers are simply
 // idle.
-__device__ __forceinline__ float clamp_tracer(float sv, float prev) {
-    if (sv >= 0.0f && sv <= 50.0f) return sv;
-    if (sv < 0.0f) return 0.0f;
-    if (sv > 50.0f) return 50.0f;
+template <typename R> __device__ __forceinline__ R clamp_tracer(R sv, R prev) {
+    if (sv >= R(0) && sv <= R(50)) return sv;
+    if (sv < R(0)) return R(0);
+    if (sv > R(50)) return R(50);
     return prev;   // NaN: the reference keeps the previous value
 }
 
@@ -811,6 +815,115 @@ __device__ __forceinline__ void tr_rows_at(const TArgs<float> &a, int i, int k) 
     a.w.tr_c[o] = cm;
 }
 
+// FP64 list form of tr_solve_column: the row of one wet (cell, layer) of the implicit vertical
+// system and its right-hand sides, formed with the column kernel's expressions in its order (so
+// the list-form solve gives the column form's results bit for bit), written for k_tr_thomas_col:
+// tr_a couples the layer below, tr_c the layer above.
+__device__ __forceinline__ void tr_rows64_at(const TArgs<double> &a, int i, int k) {
+    const Geom &g = a.g;
+    const int L = g.L, NC = g.NC;
+    const int tl = a.s.top_cell[i - 1], b = g.bottom_cell[i - 1];
+    const double dt2 = a.dt2;
+    const int sub = a.sub;
+    const bool lim = a.p.h_flux_limiter > 0 || a.p.v_flux_limiter > 0;
+    const double ar = g.area[i - 1];
+    const int nvl = tl - b + 1;
+    const double dzc = a.s.dz_cell[ix(k, i, L)];
+    const double dz_new = dzc + divnt((a.s.dz_cell_new[ix(k, i, L)] - dzc) * (sub + 1), a);
+    double am = 0.0, bm, cm = 0.0;   // am: the layer above, cm: the layer below
+    if (tl == b) {
+        bm = ar * dz_new;
+    } else if (k == tl) {
+        cm = -dt2 * a.w.di[ix0(tl - 1, i, L)];
+        bm = ar * dz_new - cm;
+    } else if (k == b) {
+        am = -dt2 * a.w.di[ix0(b, i, L)];
+        bm = -am + ar * dz_new;
+    } else {
+        am = -dt2 * a.w.di[ix0(k, i, L)];
+        cm = -dt2 * a.w.di[ix0(k - 1, i, L)];
+        bm = -am + ar * dz_new - cm;
+    }
+    const int tq = g.tri_or_quad[i - 1];
+    double sQi[2] = {0, 0}, sQii[2] = {0, 0}, shd[2] = {0, 0}, shl[2] = {0, 0};
+    double ck[2] = {0, 0};
+    for (int tr = 0; tr < a.ntr; ++tr) ck[tr] = a.con[ic(k, i, tr, L, NC)];
+    for (int l = 1; l <= tq; ++l) {
+        const int fj = g.cell_face(l, i);
+        if (!face_open(g, fj)) continue;
+        const int nb = g.cell_adj(l, i);
+        const bool in_face = k >= g.bottom_face[fj - 1] && k <= a.s.top_face[fj - 1];
+        const long fo = ix(k, fj, L);
+        const double q2 = flip(in_face ? a.w.qj[fo] : 0.0, g.cell_sign(l, i));
+        const double dface = in_face ? a.w.dj[fo] : 0.0;
+        const bool qpos = is_pos(q2), qneg = is_neg(q2);
+        for (int tr = 0; tr < a.ntr; ++tr) {
+            double cik = nb > 0 ? a.con[ic(k, nb, tr, L, NC)] : oqb_value(a, i, k, tr);
+            if (qpos) sQi[tr] = sQi[tr] + fabs(q2) * ck[tr];
+            else if (qneg) sQii[tr] = sQii[tr] + fabs(q2) * cik;
+            shd[tr] = shd[tr] + dface * (cik - ck[tr]);
+            double psi = (lim && in_face) ? a.w.psij[(long)tr * g.NF * L + fo] : 0.0;
+            shl[tr] = shl[tr] + psi * fabs(q2) * (ck[tr] - cik);
+        }
+    }
+    const double dz_old = dzc + divnt((a.s.dz_cell_new[ix(k, i, L)] - dzc) * sub, a);
+    for (int tr = 0; tr < a.ntr; ++tr) {
+        double h_adv = dt2 * (sQii[tr] - sQi[tr]);
+        double h_diff = dt2 * shd[tr];
+        double h_flux = 0.5 * dt2 * shl[tr];
+        double v = ar * dz_old * ck[tr] + h_adv + h_diff;
+        if (a.p.h_flux_limiter > 0) v = v + h_flux;
+        if (nvl != 1) {
+            const double *psi = a.w.psii + (long)tr * NC * (L + 1);
+            const double c0 = ck[tr];
+            if (k == b) {
+                double q = a.w.qi[ix0(k, i, L)];
+                double qp = pos_part(q), qm = neg_part(q);
+                double cp1 = a.con[ic(k + 1, i, tr, L, NC)];
+                v = v + dt2 * (-qp * c0 + qm * cp1);
+                if (a.p.v_flux_limiter > 0) {
+                    double ps = lim ? psi[ix0(k, i, L)] : 0.0;
+                    v = v + 0.5 * dt2 * (-ps * qp * (cp1 - c0) + ps * qm * (c0 - cp1));
+                }
+            } else if (k == tl) {
+                double q = a.w.qi[ix0(k - 1, i, L)];
+                double qp = pos_part(q), qm = neg_part(q);
+                double cm1 = a.con[ic(k - 1, i, tr, L, NC)];
+                v = v + dt2 * (qp * cm1 - qm * c0);
+                if (a.p.v_flux_limiter > 0) {
+                    double ps = lim ? psi[ix0(k - 1, i, L)] : 0.0;
+                    v = v + 0.5 * dt2 * (ps * qp * (c0 - cm1) - ps * qm * (cm1 - c0));
+                }
+            } else {
+                double q1 = a.w.qi[ix0(k - 1, i, L)], q = a.w.qi[ix0(k, i, L)];
+                double qp1 = pos_part(q1), qm1 = neg_part(q1);
+                double qp = pos_part(q), qm = neg_part(q);
+                double cm1 = a.con[ic(k - 1, i, tr, L, NC)], cp1 = a.con[ic(k + 1, i, tr, L, NC)];
+                v = v + dt2 * (qp1 * cm1 - qp * c0 + qm * cp1 - qm1 * c0);
+                if (a.p.v_flux_limiter > 0) {
+                    double p1 = lim ? psi[ix0(k - 1, i, L)] : 0.0, p0 = lim ? psi[ix0(k, i, L)] : 0.0;
+                    v = v + 0.5 * dt2 *
+                                (p1 * qp1 * (c0 - cm1) - p0 * qp * (cp1 - c0) + p0 * qm * (c0 - cp1) -
+                                 p1 * qm1 * (cm1 - c0));
+                }
+            }
+        }
+        a.w.tr_rhs[((long)tr * NC + i - 1) * L + k - 1] = v;
+    }
+    const long o = (long)(i - 1) * L + k - 1;
+    a.w.tr_a[o] = cm;
+    a.w.tr_b[o] = bm;
+    a.w.tr_c[o] = am;
+}
+
+__global__ void __launch_bounds__(128) k_tr_rows64_list(TArgs<double> a) {
+    const int n = *a.w.cl_count;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const int code = a.w.cl_list[t];
+        tr_rows64_at(a, list_entity(code), list_layer(code));
+    }
+}
+
 __global__ void __launch_bounds__(256) k_tr_rows_cl(TArgs<float> a) {
     const Geom &g = a.g;
     unsigned t = flat_tid();
@@ -836,32 +949,33 @@ __global__ void __launch_bounds__(256) k_tr_rows_list(TArgs<float> a) {
 
 // one thread per column: tridiagonal solve of the rows (top layer first, as
 // tridiagonal_solver.f90 is called), clamp to [0, 50], full next column
-__global__ void __launch_bounds__(256) k_tr_thomas_col(TArgs<float> a) {
+template <typename R> __global__ void __launch_bounds__(256) k_tr_thomas_col(TArgs<R> a) {
     const Geom &g = a.g;
     unsigned tid = flat_tid();
     if (tid >= (unsigned)g.NC) return;
-    const int i = column_entity<float>(g.cell_order, tid);
+    const int i = column_entity<R>(g.cell_order, tid);
     const int L = g.L, NC = g.NC;
     const int tl = a.s.top_cell[i - 1], b = g.bottom_cell[i - 1];
     if (tl == 0) {
         for (int k = 0; k <= L + 1; ++k)
-            for (int tr = 0; tr < a.ntr; ++tr) a.con_new[ic(k, i, tr, L, NC)] = 0.0f;
+            for (int tr = 0; tr < a.ntr; ++tr) a.con_new[ic(k, i, tr, L, NC)] = R(0);
         return;
     }
     const int nvl = tl - b + 1;
     const long base = (long)(i - 1) * L;
-    float gam[GOM_MAXL], x[GOM_MAXL][2];
-    // row r = 1..nvl is layer k = tl + 1 - r: its lower neighbour (row r - 1) is the layer above
-    float den = a.w.tr_b[base + tl - 1];
-    bool ok = den != 0.0f;
+    R gam[GOM_MAXL], x[GOM_MAXL][2];
+    // row r = 1..nvl is layer k = tl + 1 - r: its lower neighbour (row r - 1) is the layer above;
+    // the operations of thomas<> (tridiagonal_solver.f90) in the same order
+    R den = a.w.tr_b[base + tl - 1];
+    bool ok = den != R(0);
     for (int tr = 0; tr < a.ntr; ++tr) x[0][tr] = a.w.tr_rhs[((long)tr * NC + i - 1) * L + tl - 1] / den;
     for (int r = 2; r <= nvl && ok; ++r) {
         const int k = tl + 1 - r;
-        const float lower = a.w.tr_c[base + k - 1];       // coupling to the layer above
-        const float upper_prev = a.w.tr_a[base + k];       // previous row's coupling to this layer
+        const R lower = a.w.tr_c[base + k - 1];       // coupling to the layer above
+        const R upper_prev = a.w.tr_a[base + k];       // previous row's coupling to this layer
         gam[r - 1] = upper_prev / den;
         den = a.w.tr_b[base + k - 1] - lower * gam[r - 1];
-        ok = den != 0.0f;
+        ok = den != R(0);
         for (int tr = 0; tr < a.ntr; ++tr)
             x[r - 1][tr] = (a.w.tr_rhs[((long)tr * NC + i - 1) * L + k - 1] - lower * x[r - 2][tr]) / den;
     }
@@ -873,7 +987,7 @@ __global__ void __launch_bounds__(256) k_tr_thomas_col(TArgs<float> a) {
         for (int tr = 0; tr < a.ntr; ++tr) x[r - 1][tr] = x[r - 1][tr] - gam[r] * x[r][tr];
     for (int tr = 0; tr < a.ntr; ++tr) {
         for (int k = 0; k <= L + 1; ++k) {
-            float v = 0.0f;
+            R v = R(0);
             if (k >= b && k <= tl) v = clamp_tracer(x[tl - k][tr], a.con[ic(k, i, tr, L, NC)]);
             a.con_new[ic(k, i, tr, L, NC)] = v;
         }
@@ -1057,6 +1171,10 @@ template <typename R> cudaError_t launch_tr_solve_only(const LaunchT<R> &x) {
     if constexpr (sizeof(R) == sizeof(float)) {
         k_tr_rows_cl<<<blocks_for((long)g.NC * g.L, bs_solve), bs_solve, 0, x.stream>>>(a);
         k_tr_thomas_col<<<blocks_for(g.NC, 128), 128, 0, x.stream>>>(a);
+    } else if (x.tune[TUNE_TR_SOLVE] == 3 && x.w.tr_a) {
+        // rows from the wet cell-layer list the last transport call built
+        k_tr_rows64_list<<<x.num_sms * 8, 128, 0, x.stream>>>(a);
+        k_tr_thomas_col<<<blocks_for(g.NC, 128), 128, 0, x.stream>>>(a);
     } else {
         k_tr_solve<<<blocks_for(g.NC, bs_solve), bs_solve, 0, x.stream>>>(a);
     }
@@ -1090,7 +1208,12 @@ template <typename R> cudaError_t launch_transport(const LaunchT<R> &x) {
     a.con = x.w.con;
     a.con_new = x.w.con2;
     k_tr_load<<<blocks_for((long)g.NC * (L + 2), 256), 256, 0, x.stream>>>(a);
-    if constexpr (sizeof(R) == sizeof(float)) {
+    // FP64 limiter variant 3: face coefficients and limiters per (entity, layer) from the wet
+    // cell-layer list, as the FP32 path always runs them (same expressions, same results)
+    const bool flat_lim = sizeof(R) == sizeof(float) || (x.tune[TUNE_TR_LIMITER] == 3 && x.w.cl_list);
+    // FP64 solve variant 3: rows per listed wet cell-layer, then one thread per column
+    const bool list_solve = sizeof(R) == sizeof(double) && x.tune[TUNE_TR_SOLVE] == 3 && x.w.cl_list && x.w.tr_a;
+    if (flat_lim || list_solve) {
         cudaError_t e = build_cell_layer_list(g, x.s.top_cell, x.w.cl_off, x.w.cl_bsum, x.w.cl_list, x.w.cl_count,
                                               x.stream);
         if (e != cudaSuccess) return e;
@@ -1106,7 +1229,7 @@ template <typename R> cudaError_t launch_transport(const LaunchT<R> &x) {
         a.con_new = nxt;
         if (g.NOB + g.NQB > 0) k_tr_bc<<<blocks_for(g.NOB + g.NQB, 128), 128, 0, x.stream>>>(a);
         a.changed_only = sub > 0;
-        if constexpr (sizeof(R) == sizeof(float))
+        if (flat_lim)
             k_tr_face_coef_flat<<<blocks_for((long)g.NF * L, 256), 256, 0, x.stream>>>(a);
         else
             k_tr_face_coef<<<blocks_for(g.NF, 128), 128, 0, x.stream>>>(a);
@@ -1115,19 +1238,20 @@ template <typename R> cudaError_t launch_transport(const LaunchT<R> &x) {
         else
             k_tr_cell_coef<<<blocks_for(g.NC, 128), 128, 0, x.stream>>>(a);
         if (lim) {
-            if constexpr (sizeof(R) == sizeof(float)) {
+            if (flat_lim) {
                 k_tr_sums_list<<<list_grid, bs_lim, 0, x.stream>>>(a);
                 k_tr_vpsi_list<<<list_grid, bs_lim, 0, x.stream>>>(a);
+                k_tr_limiter_faces_flat<<<blocks_for((long)g.NF * L, 256), 256, 0, x.stream>>>(a);
             } else {
                 k_tr_limiter_cells<<<blocks_for(g.NC, bs_lim), bs_lim, 0, x.stream>>>(a);
-            }
-            if constexpr (sizeof(R) == sizeof(float))
-                k_tr_limiter_faces_flat<<<blocks_for((long)g.NF * L, 256), 256, 0, x.stream>>>(a);
-            else
                 k_tr_limiter_faces<<<blocks_for(g.NF, 128), 128, 0, x.stream>>>(a);
+            }
         }
         if constexpr (sizeof(R) == sizeof(float)) {
             k_tr_rows_list<<<list_grid, bs_solve, 0, x.stream>>>(a);
+            k_tr_thomas_col<<<blocks_for(g.NC, 128), 128, 0, x.stream>>>(a);
+        } else if (list_solve) {
+            k_tr_rows64_list<<<list_grid, 128, 0, x.stream>>>(a);
             k_tr_thomas_col<<<blocks_for(g.NC, 128), 128, 0, x.stream>>>(a);
         } else {
             k_tr_solve<<<blocks_for(g.NC, bs_solve), bs_solve, 0, x.stream>>>(a);
