@@ -64,6 +64,13 @@ template <typename R> __device__ __forceinline__ R divnt(R x, const TArgs<R> &a)
     return a.pow2 ? x * a.inv_nt : x / (R)a.Nt;
 }
 
+// :1294-1300 assigns con_cell_new only for a solution in [0, 50] or outside it, so a NaN solution
+// leaves the previous subcycle's value, which the copy-back of :1352-1357 also put into con
+// (the current concentrations), and on the first subcycle the 0 of :80
+template <typename R> __device__ __forceinline__ R nan_keep(const TArgs<R> &a, int k, int i, int tr) {
+    return a.sub == 0 ? R(0) : a.con[ic(k, i, tr, a.g.L, a.g.NC)];
+}
+
 // Margin of the exact quotient filters below: far larger than one rounding of R, far smaller
 // than any value the limiter distinguishes.
 template <typename R> __device__ __forceinline__ R filter_margin();
@@ -713,7 +720,7 @@ template <typename R> __device__ void tr_solve_column(const TArgs<R> &a, int i) 
                 if (sv >= R(0.0) && sv <= R(50.0)) v = sv;
                 else if (sv < R(0.0)) v = R(0.0);
                 else if (sv > R(50.0)) v = R(50.0);
-                else v = a.con[ic(k, i, tr, L, NC)];   // NaN: the reference keeps the previous value
+                else v = nan_keep(a, k, i, tr);
             }
             a.con_new[ic(k, i, tr, L, NC)] = v;
         }
@@ -988,7 +995,7 @@ template <typename R> __global__ void __launch_bounds__(256) k_tr_thomas_col(TAr
     for (int tr = 0; tr < a.ntr; ++tr) {
         for (int k = 0; k <= L + 1; ++k) {
             R v = R(0);
-            if (k >= b && k <= tl) v = clamp_tracer(x[tl - k][tr], a.con[ic(k, i, tr, L, NC)]);
+            if (k >= b && k <= tl) v = clamp_tracer(x[tl - k][tr], nan_keep(a, k, i, tr));
             a.con_new[ic(k, i, tr, L, NC)] = v;
         }
     }

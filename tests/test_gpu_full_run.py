@@ -1,0 +1,84 @@
+"""The CPU-runnable tidal-basin configuration at full size through its whole run on the GPU beside
+the CPU restatement: 120 x 80 squares of 250 m plus a 4-row triangle strip, 10 layers, harmonic
+open boundary 0.5 cos(2 pi t / 44712 s), uniform T = 20 and S = 30, dt = 120 s, 720 steps.
+
+Wet/dry masks and layer indices must be equal after the run; the element in which each ELM foot
+lands must be equal except for feet the oracle flags within 1e-12 m of an element edge; elevation,
+velocities, tracers and densities within the stated tolerances of the oracle; volume and salt
+mass equal to FP64 round-off.  The GPU's PCG sums its dot products in a different order, which is
+the only source of difference (every other phase is bit-for-bit, test_gpu_parity.py).
+
+The run passes through the event where a cell's top layer rises into a layer that was dry: the
+heat_option 2 term of the transport (solve_transport_equation_v19.f90:157-159) then divides by that
+layer's old thickness, 0, the column's solution is NaN, and the reference's clamp leaves the value
+of the previous subcycle (0 on the first).  NaN positions must agree too."""
+import numpy as np
+import pytest
+
+from gom_release_gb300.core import GomCore, prepare
+from gom_release_gb300.deck import HostForcing, initial_state, tidal_basin
+
+pytestmark = pytest.mark.gpu
+
+ETA_ABS = 1e-11       # metres, after 720 steps (measured: 3e-15)
+FIELD_RTOL = 1e-9     # velocities, tracers, densities, thicknesses: relative to the field's maximum
+                      # (measured: 5e-12 for w, 1e-13 or less for the rest)
+VOLUME_RTOL = 1e-12   # volume and salt mass against the oracle (measured: 1e-15)
+
+
+def basin_full_run(oracle_so, gpu_lib, steps=None):
+    deck = tidal_basin()
+    n = steps or deck.n_steps
+    st = initial_state(deck)
+    ref = GomCore(deck, lib_path=oracle_so)
+    gpu = GomCore(deck, lib=gpu_lib)
+    prepare(ref, st)
+    prepare(gpu, st)
+    fr = HostForcing(deck)
+    walked = mism = near = 0
+    for it in range(1, n + 1):
+        f = fr.step(it)
+        ref.set_forcing(f)
+        gpu.set_forcing(f)
+        ref.step_all()
+        gpu.step_all()
+        fa, fb = gpu.get_field("elm_foot"), ref.get_field("elm_foot")
+        nb = ref.get_field("elm_near_edge")
+        walked += int(np.count_nonzero(fb))
+        bad = fa != fb
+        mism += int(np.count_nonzero(bad & (nb == 0)))
+        near += int(np.count_nonzero(nb))
+    out = {"steps": n, "cells": deck.n_cells, "feet_walked": walked, "feet_mismatch_not_near_edge": mism,
+           "feet_near_edge": near}
+    for name in ("top_layer_cell", "top_layer_face", "top_layer_node", "wetdry_node"):
+        out["mismatch_" + name] = int(np.count_nonzero(gpu.get_field(name) != ref.get_field(name)))
+    a, b = gpu.get_field("eta_cell"), ref.get_field("eta_cell")
+    out["eta_cell_max_abs"] = float(np.abs(a - b).max())
+    out["eta_range"] = float(np.abs(b).max())
+    for name in ("un_face", "vn_face", "wn_cell", "u_node", "v_node", "salt_cell", "temp_cell", "rho_cell",
+                 "dz_cell"):
+        a, b = gpu.get_field(name), ref.get_field(name)
+        na, nb_ = np.isnan(a), np.isnan(b)
+        out["nan_mismatch_" + name] = int(np.count_nonzero(na != nb_))
+        out["nan_count_" + name] = int(np.count_nonzero(nb_))
+        ok = ~(na | nb_)
+        scale = max(float(np.abs(b[ok]).max()), 1e-30) if ok.any() else 1.0
+        out[name + "_rel"] = float(np.abs(a[ok] - b[ok]).max()) / scale if ok.any() else 0.0
+    (va, sa), (vb, sb) = gpu.conservation(), ref.conservation()
+    out["volume_rel"] = abs(va - vb) / abs(vb)
+    out["salt_rel"] = abs(sa - sb) / abs(sb)
+    return out
+
+
+def test_tidal_basin_full_run_matches_oracle(oracle_so, gpu_lib):
+    r = basin_full_run(oracle_so, gpu_lib)
+    assert r["feet_walked"] > 0
+    for k, v in r.items():
+        if k.startswith("mismatch_") or k.startswith("nan_mismatch_"):
+            assert v == 0, (k, v)
+    assert r["feet_mismatch_not_near_edge"] == 0, r
+    assert r["eta_cell_max_abs"] < ETA_ABS, r
+    for k, v in r.items():
+        if k.endswith("_rel") and k not in ("volume_rel", "salt_rel"):
+            assert v < FIELD_RTOL, (k, v)
+    assert r["volume_rel"] < VOLUME_RTOL and r["salt_rel"] < VOLUME_RTOL, r
