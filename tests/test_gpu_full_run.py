@@ -26,9 +26,8 @@ FIELD_RTOL = 1e-9     # velocities, tracers, densities, thicknesses: relative to
 VOLUME_RTOL = 1e-12   # volume and salt mass against the oracle (measured: 1e-15)
 
 
-def basin_full_run(oracle_so, gpu_lib, steps=None):
-    deck = tidal_basin()
-    n = steps or deck.n_steps
+def full_run(oracle_so, gpu_lib, deck, steps):
+    n = steps
     st = initial_state(deck)
     ref = GomCore(deck, lib_path=oracle_so)
     gpu = GomCore(deck, lib=gpu_lib)
@@ -70,15 +69,23 @@ def basin_full_run(oracle_so, gpu_lib, steps=None):
     return out
 
 
-def test_tidal_basin_full_run_matches_oracle(oracle_so, gpu_lib):
-    r = basin_full_run(oracle_so, gpu_lib)
+def basin_full_run(oracle_so, gpu_lib):
+    deck = tidal_basin()
+    return full_run(oracle_so, gpu_lib, deck, deck.n_steps)
+
+
+def _check(r, eta_abs, field_rtol):
     assert r["feet_walked"] > 0
     for k, v in r.items():
         if k.startswith("mismatch_") or k.startswith("nan_mismatch_"):
             assert v == 0, (k, v)
     assert r["feet_mismatch_not_near_edge"] == 0, r
-    assert r["eta_cell_max_abs"] < ETA_ABS, r
+    assert r["eta_cell_max_abs"] < eta_abs, r
     for k, v in r.items():
         if k.endswith("_rel") and k not in ("volume_rel", "salt_rel"):
-            assert v < FIELD_RTOL, (k, v)
+            assert v < field_rtol, (k, v)
     assert r["volume_rel"] < VOLUME_RTOL and r["salt_rel"] < VOLUME_RTOL, r
+
+
+def test_tidal_basin_full_run_matches_oracle(oracle_so, gpu_lib):
+    _check(basin_full_run(oracle_so, gpu_lib), ETA_ABS, FIELD_RTOL)
