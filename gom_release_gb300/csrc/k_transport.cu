@@ -255,9 +255,17 @@ template <typename R> __device__ __forceinline__ R phi_limit(int code, R small_p
 // it): where the ratio lies clearly below 0, below small_phi, or above the limiter's flat top
 // (1 for codes 1 and 2... 2 for code 3), the result is known without the division and equals
 // the reference's bit for bit; the quotient is formed only in between.
+// NaN tests on the bit patterns (integer pipe): a NaN concentration (the heat_option 2 term over
+// a layer of zero old thickness) reaches the limiter sums, and the sign and size filters below
+// are exact only for numbers; with a NaN operand the ratio is formed, as the reference forms it
+__device__ __forceinline__ bool nan_bits(double x) {
+    return (__double_as_longlong(x) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
+}
+__device__ __forceinline__ bool nan_bits(float x) { return (__float_as_int(x) & 0x7fffffff) > 0x7f800000; }
+
 template <typename R> __device__ __forceinline__ R limited_ratio(int code, R small_phi, R num, R den) {
     if (den == R(0)) return phi_limit(code, small_phi, R(1));
-    if (code >= 1 && code <= 3 && num != R(0)) {
+    if (code >= 1 && code <= 3 && num != R(0) && !nan_bits(num) && !nan_bits(den)) {
         const R m = filter_margin<R>();
         if ((num < R(0)) != (den < R(0))) return R(0);   // r < 0: every code gives small_phi - small_phi
         const R an = fabs(num), ad = fabs(den);

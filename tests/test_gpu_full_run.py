@@ -12,11 +12,13 @@ The run passes through the event where a cell's top layer rises into a layer tha
 heat_option 2 term of the transport (solve_transport_equation_v19.f90:157-159) then divides by that
 layer's old thickness, 0, the column's solution is NaN, and the reference's clamp leaves the value
 of the previous subcycle (0 on the first).  NaN positions must agree too."""
+import dataclasses
+
 import numpy as np
 import pytest
 
 from gom_release_gb300.core import GomCore, prepare
-from gom_release_gb300.deck import HostForcing, initial_state, tidal_basin
+from gom_release_gb300.deck import HostForcing, estuary, initial_state, tidal_basin
 
 pytestmark = pytest.mark.gpu
 
@@ -74,6 +76,19 @@ def basin_full_run(oracle_so, gpu_lib):
     return full_run(oracle_so, gpu_lib, deck, deck.n_steps)
 
 
+def estuary_tidal_cycle(oracle_so, gpu_lib):
+    """The baroclinic estuary generator (river inflow, TVD limiter, wind, density-driven flow) on a
+    80 x 40 mesh of 100 m squares with 20 layers, 720 steps of 60 s (one M2 cycle), turbulence
+    closure off: with the Pacanowski-Philander closure on, the reference's own trajectory is
+    chaotic at round-off level (two CPU runs one ulp apart in salinity differ by 8 % in velocity
+    after 200 steps), so that case is compared phase by phase instead (test_gpu_parity.py).  The
+    run passes wetting fronts where the heat_option 2 term is NaN and the NaN reaches the TVD
+    limiter's ratios (step 666)."""
+    deck = estuary(nx=80, ny=40, dx=100.0, n_layers=20)
+    deck = dataclasses.replace(deck, params=dataclasses.replace(deck.params, turbulence_flag=0))
+    return full_run(oracle_so, gpu_lib, deck, 720)
+
+
 def _check(r, eta_abs, field_rtol):
     assert r["feet_walked"] > 0
     for k, v in r.items():
@@ -89,3 +104,7 @@ def _check(r, eta_abs, field_rtol):
 
 def test_tidal_basin_full_run_matches_oracle(oracle_so, gpu_lib):
     _check(basin_full_run(oracle_so, gpu_lib), ETA_ABS, FIELD_RTOL)
+
+
+def test_estuary_tidal_cycle_matches_oracle(oracle_so, gpu_lib):
+    _check(estuary_tidal_cycle(oracle_so, gpu_lib), ETA_ABS, FIELD_RTOL)
