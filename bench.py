@@ -15,8 +15,10 @@ e2e            the same through the public API end to end: host forcing computed
                the FP64 volume/salt sums) read back every step.
 roofline       the dominant kernel (the transport column solve) timed alone with CUDA events,
                algorithmic bytes / time against the measured HBM copy bandwidth; traffic is
-               ncu's DRAM bytes per launch of that kernel (profiles/roofline_traffic.md).
-cpu_baseline   the CPU restatement of the reference (oracle/, serial FP64) on a bounded sample.
+               the DRAM bytes per launch of that kernel from an ncu capture (a constant below,
+               with the capture it came from).
+cpu_baseline   the CPU restatement of the reference (oracle/), built with OpenMP over every
+               host thread, on a bounded sample of the same workload.
 
 N > 1 runs independent replicas (the single-run path does not shard): value is the sum over
 ranks of cell-layer-steps divided by the slowest rank's time.
@@ -198,14 +200,20 @@ def time_phases(deck, st_snapshot, lib, forcing, torch, reps: int = 3) -> dict:
 TR_SOLVE_BYTES_PER_CELL_LAYER = {"fp64": 144, "mixed": 72}
 
 
-def committed_traffic(key: str):
-    """DRAM bytes per launch measured by ncu for ``key`` (profiles/roofline_traffic.md), or None."""
-    import re
-    f = ROOT / "profiles" / "roofline_traffic.md"
-    if not f.exists():
-        return None
-    m = re.search(r"^\|\s*" + re.escape(key) + r"\s*\|\s*([0-9.eE+]+)\s*\|", f.read_text(), re.M)
-    return float(m.group(1)) if m else None
+# DRAM bytes per launch of the transport solve on the full estuary (1,363,169 active
+# cell-layers): dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture on the medium
+# estuary (349,122 active cell-layers), scaled by the active cell-layers (the solve reads and
+# writes a fixed set of arrays per wet cell-layer, so its traffic grows in proportion)
+SOLVE_TRAFFIC_FULL = {
+    "k_tr_solve fp64": 5.3638e8,
+    "k_tr_solve mixed": 3.5127e8,
+    "k_tr_rows64_list + k_tr_thomas_col fp64": 6.2223e8,
+}
+
+
+def solve_traffic(kernel: str, precision: str, size: str):
+    """ncu DRAM bytes per launch of the transport solve for the full estuary, or None."""
+    return SOLVE_TRAFFIC_FULL.get(f"{kernel} {precision}") if size == "full" else None
 
 
 def phase_bytes(deck, ncl: int, pcg_iters: float) -> dict:
@@ -695,7 +703,7 @@ def main():
     # FP64 solve variant 3 runs the solve as two kernels (rows per wet cell-layer, column Thomas)
     list_solve = args.precision == "fp64" and tune is not None and tune[2] == 3
     solve_kernel = "k_tr_rows64_list + k_tr_thomas_col" if list_solve else "k_tr_solve"
-    traffic = committed_traffic(f"{solve_kernel} {args.precision} estuary full") if args.size == "full" else None
+    traffic = solve_traffic(solve_kernel, args.precision, args.size)
     if args.no_phases:
         phases = {}
     else:

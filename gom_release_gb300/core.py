@@ -109,7 +109,7 @@ class GomForcing(C.Structure):
     _fields_ = [("elapsed_time", C.c_double), ("spinup_tide", C.c_double), ("spinup_baroclinic", C.c_double),
                 ("reserved", C.c_double), ("eta_at_ob_old", _D), ("eta_at_ob_new", _D), ("q_add", _D),
                 ("wind_stress_normal", _D), ("wind_stress_tangnt", _D), ("gamma_t", _D), ("air_p", _D),
-                ("con_at_ob", _D), ("con_at_qb", _D), ("phi_sw", _D)]
+                ("con_at_ob", _D), ("con_at_qb", _D), ("phi_sw", _D), ("phi_sz", _D)]
 
 
 class GomStorm(C.Structure):
@@ -119,7 +119,7 @@ class GomStorm(C.Structure):
 
 class GomStatus(C.Structure):
     _fields_ = [("code", C.c_int32), ("site", C.c_int32), ("entity", C.c_int32), ("layer", C.c_int32),
-                ("value", C.c_double)]
+                ("value", C.c_double), ("entity_kind", C.c_int32), ("run", C.c_int32)]
 
 
 class GomError(RuntimeError):
@@ -134,7 +134,7 @@ class GomError(RuntimeError):
         super().__init__(s)
 
 
-ABI_VERSION = 3      # GOM_ABI_VERSION of include/gom_core.h
+ABI_VERSION = 4      # GOM_ABI_VERSION of include/gom_core.h
 
 _STEPS = ["bottom_friction", "boundary_velocity", "advection", "momentum", "velocities", "layers",
           "node_velocity", "transport", "density", "turbulence", "swap"]
@@ -319,7 +319,7 @@ class GomCore:
         s = GomForcing(f.get("elapsed_time", 0.0), f.get("spinup_tide", 1.0), f.get("spinup_baroclinic", 1.0), 0.0,
                        arr("eta_at_ob_old"), arr("eta_at_ob_new"), arr("q_add"), arr("wind_stress_normal"),
                        arr("wind_stress_tangnt"), arr("gamma_t"), arr("air_p"), arr("con_at_ob"),
-                       arr("con_at_qb"), arr("phi_sw"))
+                       arr("con_at_qb"), arr("phi_sw"), arr("phi_sz"))
         self._forcing_keep = keep
         self._check(self.lib.gom_set_forcing(self.ctx, C.byref(s)), "set_forcing")
 

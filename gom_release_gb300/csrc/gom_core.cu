@@ -4,6 +4,7 @@
 // resident in HBM in the reference's (k, entity) layout, the work buffers of the phases, one
 // CUDA stream, pinned staging for the per-step forcing, and a CUDA graph of the whole timestep
 // (captured on first use of gom_step_all).  Host arrays are read only during a call.
+#include <cmath>
 #include <cstdio>
 #include <mutex>
 #include <algorithm>
@@ -44,7 +45,8 @@ struct gom_ctx {
     // forcing arrays on the device (the Forcing view points into these)
     double *f_scal = nullptr;
     double *f_eta_old = nullptr, *f_eta_new = nullptr, *f_q_add = nullptr, *f_wsn = nullptr, *f_wst = nullptr,
-           *f_gamma_t = nullptr, *f_air_p = nullptr, *f_con_ob = nullptr, *f_con_qb = nullptr, *f_phi_sw = nullptr;
+           *f_gamma_t = nullptr, *f_air_p = nullptr, *f_con_ob = nullptr, *f_con_qb = nullptr, *f_phi_sw = nullptr,
+           *f_phi_sz = nullptr;
     // pinned host mirrors
     gom_status *h_status = nullptr;
     int *h_iters = nullptr;
@@ -340,6 +342,18 @@ int finish(gom_ctx *c, int32_t *pcg_iters, bool had_pcg) {
     return c->h_status->code;
 }
 
+// the packed run holding the entity a status names (0 in a single-run context, -1 if not known)
+int status_run(const gom_ctx *c, const gom_status &st) {
+    const int kind = st.entity_kind;
+    if (st.code == 0 || kind < GOM_ENTITY_CELL || kind > GOM_ENTITY_NODE || st.entity < 1) return -1;
+    if (c->d.n_runs <= 1) return 0;
+    const std::vector<int> &v = c->run_starts[kind == GOM_ENTITY_CELL ? 0 : kind == GOM_ENTITY_FACE ? 1 : 2];
+    // run r holds the 0-based entities [v[r], v[r+1])
+    auto it = std::upper_bound(v.begin(), v.end(), st.entity - 1);
+    int r = (int)(it - v.begin()) - 1;
+    return (r >= 0 && r < c->d.n_runs) ? r : -1;
+}
+
 template <typename Fn> int run_phase(gom_ctx *c, Fn fn) {
     if (!c) return GOM_E_ARG;
     CK(fn(c));
@@ -395,6 +409,8 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
     if (params->transport_solver < 0 || params->transport_solver > 2) return GOM_E_ARG;
     if (params->precision != GOM_PRECISION_FP64 && params->precision != GOM_PRECISION_MIXED) return GOM_E_ARG;
     if (params->turbulence_flag < 0 || params->turbulence_flag > 2) return GOM_E_ARG;
+    if (params->transport_flag && params->is_temp && params->heat_option != 1 && params->heat_option != 2)
+        return GOM_E_ARG;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return GOM_E_CUDA;
     gom_ctx *c = new gom_ctx();
@@ -469,6 +485,28 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
     UP(z_level, z_level, L + 1, true);
     UP(delta_z, delta_z, L, true);
 #undef UP
+    // calculate_bottom_friction.f90:25-60 on the host where the result is static (the C library's
+    // pow and log, which the reference calls)
+    if (e == cudaSuccess && (params->bf_flag == 1 || params->bf_flag == 2)) {
+        std::vector<double> cdb(NF, 0.0), arg(NF, -1.0);
+        for (size_t j = 0; j < NF; ++j) {
+            const double hf = g->h_face[j];
+            if (!(hf > params->dry_depth)) continue;
+            if (params->bf_flag == 1) {
+                const double expo = 1.0 / 6.0;
+                const double chezy = std::pow(std::max(1.0, hf), expo) / g->manning[j];
+                cdb[j] = params->gravity / (chezy * chezy);
+            } else {
+                const int b = g->bottom_layer_at_face[j];
+                if (b < 1 || b > (int)L) continue;
+                arg[j] = g->z_level[b] - (params->msl - hf);
+                const double lg = std::log(std::max(0.5, arg[j]) / g->bf_height[j]);
+                cdb[j] = params->von_karman * params->von_karman / (lg * lg);
+            }
+        }
+        e = upload(c, &G.cdb_static, (const double *)cdb.data(), NF, true);
+        if (e == cudaSuccess) e = upload(c, &G.cdb_arg, (const double *)arg.data(), NF, true);
+    }
     G.NR = d.n_runs > 1 ? d.n_runs : 1;
     if (d.n_runs > 1 && e == cudaSuccess) {
         // packed runs: each range starts at 0, never decreases and ends at the entity count
@@ -541,6 +579,7 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
     if (e == cudaSuccess) e = dalloc(c, &c->f_con_ob, (size_t)d.n_ob * 2 * nt);
     if (e == cudaSuccess) e = dalloc(c, &c->f_con_qb, (size_t)d.n_qb * 2 * nt);
     if (e == cudaSuccess) e = dalloc(c, &c->f_phi_sw, NC);
+    if (e == cudaSuccess) e = dalloc(c, &c->f_phi_sz, L * NC);
     if (e == cudaSuccess) e = dalloc(c, &c->f_scal, 4);
     if (e == cudaSuccess) {
         const double one[4] = {0.0, 1.0, 1.0, 0.0};
@@ -558,6 +597,7 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
     F.con_at_ob = c->f_con_ob;
     F.con_at_qb = c->f_con_qb;
     F.phi_sw = c->f_phi_sw;
+    F.phi_sz = c->f_phi_sz;
     // work
     Work &W = c->x.w;
     if (e == cudaSuccess) e = dalloc(c, &W.sparsem, 5 * NC);
@@ -568,6 +608,11 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
     if (e == cudaSuccess) e = dalloc(c, &W.q, NC);
     if (e == cudaSuccess) e = dalloc(c, &W.d0, NC);
     if (e == cudaSuccess) e = dalloc(c, &W.d1, NC);
+    if (!c->mixed && d.n_runs <= 1) {
+        if (e == cudaSuccess) e = dalloc(c, &W.cg_s1, NC);
+        if (e == cudaSuccess) e = dalloc(c, &W.cg_w1, NC);
+        if (e == cudaSuccess) e = dalloc(c, &W.cg_xs, NC);
+    }
     // grid barrier (count, generation) or one pair per packed run
     if (e == cudaSuccess) e = dalloc(c, &W.barrier, 2 * (size_t)PCG_MAX_RUNS);
     if (e == cudaSuccess) e = dalloc(c, &W.pcg_iters, 1);
@@ -654,7 +699,7 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
     if (launch_node_weights(c->x) != cudaSuccess) return fail(GOM_E_CUDA);
     {
         // two halves: the mixed solvers alternate them with every barrier
-        size_t nb = 2 * (size_t)c->x.w.pcg_blocks;
+        size_t nb = 2 * (size_t)std::max(c->x.w.pcg_blocks, c->x.num_sms);
         if (dalloc(c, &W.partial_dq, nb) != cudaSuccess || dalloc(c, &W.partial_delta, nb) != cudaSuccess)
             return fail(GOM_E_NOMEM);
     }
@@ -885,7 +930,8 @@ int gom_set_forcing(gom_ctx *c, const gom_forcing *fo) {
                  {fo->air_p, c->f_air_p, (size_t)d.n_nodes},
                  {fo->con_at_ob, c->f_con_ob, (size_t)d.n_ob * 2 * nt},
                  {fo->con_at_qb, c->f_con_qb, (size_t)d.n_qb * 2 * nt},
-                 {fo->phi_sw, c->f_phi_sw, (size_t)d.n_cells}};
+                 {fo->phi_sw, c->f_phi_sw, (size_t)d.n_cells},
+                 {fo->phi_sz, c->f_phi_sz, (size_t)d.n_cells * d.n_layers}};
     // alternate between the two staging halves; wait only until the upload that last used this
     // half has left it (so one step can be in flight while the next step's forcing is staged)
     int h = c->stage_half;
@@ -914,6 +960,7 @@ int gom_get_status(gom_ctx *c, gom_status *s, int clear) {
     CK(cudaMemcpyAsync(c->h_status, c->x.status, sizeof(gom_status), cudaMemcpyDeviceToHost, c->x.stream));
     CK(cudaStreamSynchronize(c->x.stream));
     *s = *c->h_status;
+    s->run = status_run(c, *s);
     if (clear) {
         CK(cudaMemsetAsync(c->x.status, 0, sizeof(gom_status), c->x.stream));
         CK(cudaStreamSynchronize(c->x.stream));

@@ -36,6 +36,11 @@ struct Geom {
     const double *x_face, *y_face, *h_face, *face_length, *delta_j, *cos_theta, *sin_theta, *cos_theta2,
         *sin_theta2, *coriolis_factor, *manning, *bf_height;
     const int *adj_cellnum_at_face, *nodenum_at_face, *bottom_face, *boundary_type_of_face, *isflowside3;
+    // bottom drag coefficients formed on the host with the C library's pow / log (the functions
+    // the reference calls): bf_flag 1 Manning Cdb per face; bf_flag 2 the log-law Cdb of the
+    // static bottom half-thickness (z_level(b) - (MSL - h) of a column with more than one layer)
+    // and that half-thickness; null otherwise
+    const double *cdb_static, *cdb_arg;
     // boundaries / vertical grid
     const int *ob_cell_id, *qb_cell, *qb_face;
     const double *z_level, *delta_z;
@@ -99,6 +104,7 @@ struct Forcing {
     const double *scal;   // [elapsed_time, spinup_tide, spinup_baroclinic] in device memory
     const double *eta_at_ob_old, *eta_at_ob_new, *q_add, *wind_stress_normal, *wind_stress_tangnt, *gamma_t, *air_p,
         *con_at_ob, *con_at_qb, *phi_sw;
+    const double *phi_sz;   // (L, NC) heat source per layer (heat_option 1, ELM transport)
 };
 
 // scalar parameters
@@ -135,12 +141,16 @@ template <typename R> __device__ __forceinline__ R geo(const double *d, const fl
 }
 
 // -------------------------------------------------------------------- error status
-__device__ inline void record_error(gom_status *st, int code, int site, int entity, int layer, double value) {
+// The first failure wins; kind is the GOM_ENTITY_* that entity indexes (the host maps it to a
+// packed run).
+__device__ inline void record_error(gom_status *st, int code, int site, int entity, int layer, double value,
+                                    int kind) {
     if (atomicCAS(&st->code, 0, code) == 0) {
         st->site = site;
         st->entity = entity;
         st->layer = layer;
         st->value = value;
+        st->entity_kind = kind;
     }
 }
 

@@ -12,7 +12,9 @@ template <typename R> struct WorkT {
     double *sparsem = nullptr;   // (0:4, NC)
     double *rhs = nullptr;       // (NC)
     double *minv = nullptr, *r = nullptr, *s = nullptr, *q = nullptr, *d0 = nullptr, *d1 = nullptr;
-    double *partial_dq = nullptr, *partial_delta = nullptr;   // (max_blocks)
+    // single-run FP64 solver: second buffers of s and w, scaled solution x'
+    double *cg_s1 = nullptr, *cg_w1 = nullptr, *cg_xs = nullptr;
+    double *partial_dq = nullptr, *partial_delta = nullptr;   // (2 x max_blocks)
     unsigned *barrier = nullptr;                               // [count, generation]
     int *pcg_iters = nullptr;                                  // device: iterations of the last solve
     int pcg_blocks = 0, pcg_threads = 256;

@@ -12,14 +12,19 @@
 // exists on every GPU that loads the library for the life of the process.
 //
 // Limits and rules:
-//   * at most GOM_NOALLOC_MAX_CELLS rows (262144): 6 work vectors of that length plus the
-//     reduction partials, about 12 MB per GPU;
+//   * at most GOM_NOALLOC_MAX_CELLS rows (262144): 9 work vectors of that length plus the
+//     reduction partials, about 19 MB per GPU;
 //   * every call shares the one array, and a call leaves its contents behind: the barrier
-//     counters, iteration count and status are cleared at the start of each call, the vectors are
+//     counter, iteration count and status are cleared at the start of each call, the vectors are
 //     fully rewritten before they are read; calls that overlap on the GPU (two streams, two
 //     threads) race on the array and must be serialised by the caller;
-//   * the first call on a device looks up the array's device address (cudaGetSymbolAddress) and
-//     the solver's occupancy; make that first call before any stream capture.
+//   * the solver is a cooperative kernel that spins on grid barriers: it must not run at the same
+//     time as another spinning solve of this library (a context's free-surface phase), or the two
+//     grids can each wait for blocks the other holds until the barrier's time limit reports
+//     GOM_E_TIMEOUT -- order such work on one stream (gom_stream of the context) or serialise it;
+//   * the first call on a device reads the solver's occupancy and the SM count once; make that
+//     first call before any stream capture.  The array's device address is looked up with
+//     cudaGetSymbolAddress on every call, in the caller's current context, so it never goes stale.
 #include <mutex>
 
 #include "gom_launch.h"
@@ -33,43 +38,42 @@ namespace {
 
 using namespace gom;
 
-// doubles: minv | r | s | q | d0 | d1 (6 x MAX_CELLS) | partial_dq | partial_delta (MAX_BLOCKS each)
-// | control block (barrier counters, iteration count, status)
+// doubles: dr | xs | p | r0 | r1 | s0 | s1 | w0 | w1 (9 x MAX_CELLS) | gamma and delta partials
+// (2 halves x MAX_BLOCKS each) | control block (barrier counter, iteration count, status)
 constexpr size_t kVec = GOM_NOALLOC_MAX_CELLS;
+constexpr size_t kNumVec = 9;
+constexpr size_t kPartials = 2 * GOM_NOALLOC_MAX_BLOCKS;
 constexpr size_t kControlDoubles = 16;
-constexpr size_t kScratchDoubles = 6 * kVec + 2 * GOM_NOALLOC_MAX_BLOCKS + kControlDoubles;
+constexpr size_t kScratchDoubles = kNumVec * kVec + 2 * kPartials + kControlDoubles;
 
 static __device__ __align__(256) double g_noalloc_scratch[kScratchDoubles];
 
-struct ScratchInfo {
-    double *base = nullptr;   // device address of g_noalloc_scratch on this device
-    int per_sm = 0;
+struct LaunchInfo {
     int num_sms = 0;
     bool ready = false;
 };
 
 std::mutex g_setup_mutex;
-ScratchInfo g_devices[GOM_NOALLOC_MAX_DEVICES];
+LaunchInfo g_devices[GOM_NOALLOC_MAX_DEVICES];
 
-// Once per device, with that device current: the array's device address and launch geometry.
-int setup_device(int dev, ScratchInfo **out) {
+// Once per device, with that device current: the SM count, and checks that one block of either
+// solver form fits on an SM and that the device runs cooperative launches.
+int setup_device(int dev, int *num_sms) {
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    ScratchInfo &s = g_devices[dev];
+    LaunchInfo &s = g_devices[dev];
     if (!s.ready) {
-        double *ptr = nullptr;
-        if (cudaGetSymbolAddress((void **)&ptr, g_noalloc_scratch) != cudaSuccess) return GOM_E_CUDA;
         int per_sm = 0, sms = 0, coop = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg, PCG_THREADS, 0) != cudaSuccess)
-            return GOM_E_CUDA;
+        for (const void *k : {(const void *)k_pcg_cg1<PCG_CG_ROWS>, (const void *)k_pcg_cg1<0>})
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, PCG_CG_THREADS, 0) != cudaSuccess ||
+                per_sm < 1)
+                return GOM_E_CUDA;
         if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return GOM_E_CUDA;
         if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop)
             return GOM_E_CUDA;
-        s.base = ptr;
-        s.per_sm = per_sm;
         s.num_sms = sms;
         s.ready = true;
     }
-    *out = &s;
+    *num_sms = s.num_sms;
     return GOM_OK;
 }
 
@@ -77,22 +81,24 @@ int setup_device(int dev, ScratchInfo **out) {
 
 extern "C" int gom_pcg_solve_noalloc(int32_t n_cells, const int32_t *tri_or_quad, const int32_t *adj_cellnum_at_cell,
                                      const double *sparsem, const double *rhs, double *x, int32_t max_iteration,
-                                     double error_tolerance, void *stream, int32_t *iterations) {
+                                     double error_tolerance, void *stream, int32_t *iterations,
+                                     int32_t *device_result) {
     if (n_cells <= 0 || n_cells > GOM_NOALLOC_MAX_CELLS) return GOM_E_ARG;   // beyond the fixed scratch
     if (!tri_or_quad || !adj_cellnum_at_cell || !sparsem || !rhs || !x || max_iteration < 0) return GOM_E_ARG;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= GOM_NOALLOC_MAX_DEVICES) return GOM_E_CUDA;
-    ScratchInfo *info = nullptr;
-    int rc = setup_device(dev, &info);
+    int num_sms = 0;
+    int rc = setup_device(dev, &num_sms);
     if (rc != GOM_OK) return rc;
-    const int blocks = pcg_blocks_for(n_cells, info->per_sm, info->num_sms);
-    if (blocks > GOM_NOALLOC_MAX_BLOCKS) return GOM_E_ARG;
+    if (num_sms > GOM_NOALLOC_MAX_BLOCKS) return GOM_E_ARG;   // the grid has at most one block per SM
+    // the device address of the array in the current context (host code cannot use its name)
+    double *base = nullptr;
+    if (cudaGetSymbolAddress((void **)&base, g_noalloc_scratch) != cudaSuccess || !base) return GOM_E_CUDA;
     cudaStream_t st = (cudaStream_t)stream;
-    double *base = info->base;
-    double *control = base + 6 * kVec + 2 * GOM_NOALLOC_MAX_BLOCKS;
-    unsigned *bar = reinterpret_cast<unsigned *>(control);                  // [count, generation]
+    double *control = base + kNumVec * kVec + 2 * kPartials;
+    unsigned *bar = reinterpret_cast<unsigned *>(control);                  // barrier counter
     int *iters_dev = reinterpret_cast<int *>(control + 1);
-    gom_status *status_dev = reinterpret_cast<gom_status *>(control + 2);    // 24 bytes
+    gom_status *status_dev = reinterpret_cast<gom_status *>(control + 2);    // 32 bytes
     // the barrier, iteration count and status must start at zero; the vectors are written
     // before they are read
     if (cudaMemsetAsync(control, 0, kControlDoubles * sizeof(double), st) != cudaSuccess) return GOM_E_CUDA;
@@ -105,30 +111,35 @@ extern "C" int gom_pcg_solve_noalloc(int32_t n_cells, const int32_t *tri_or_quad
     a.sp = sparsem;
     a.b = rhs;
     a.x = x;
-    a.minv = base + 0 * kVec;
-    a.r = base + 1 * kVec;
-    a.s = base + 2 * kVec;
-    a.q = base + 3 * kVec;
-    a.dA = base + 4 * kVec;
-    a.dB = base + 5 * kVec;
-    a.pdq = base + 6 * kVec;
-    a.pdelta = base + 6 * kVec + GOM_NOALLOC_MAX_BLOCKS;
+    a.dr = base + 0 * kVec;
+    a.xs = base + 1 * kVec;
+    a.p = base + 2 * kVec;
+    a.r[0] = base + 3 * kVec;
+    a.r[1] = base + 4 * kVec;
+    a.s[0] = base + 5 * kVec;
+    a.s[1] = base + 6 * kVec;
+    a.w[0] = base + 7 * kVec;
+    a.w[1] = base + 8 * kVec;
+    a.pg = base + kNumVec * kVec;
+    a.pd = base + kNumVec * kVec + kPartials;
     a.bar = bar;
     a.iters = iters_dev;
     a.maxit = max_iteration;
     a.tol = error_tolerance;
     a.st = status_dev;
     a.phantom = 0;
+    a.check_diag = 1;   // the caller built the system: a non-positive diagonal is GOM_E_NOT_SPD
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(blocks);
-    cfg.blockDim = dim3(PCG_THREADS);
     cfg.stream = st;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeCooperative;
-    attr[0].val.cooperative = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    if (cudaLaunchKernelEx(&cfg, k_pcg, a) != cudaSuccess) return GOM_E_CUDA;
+    if (launch_pcg_cg1(cfg, a, num_sms) != cudaSuccess) return GOM_E_CUDA;
+    // status code and iteration count into the caller's device memory, ordered on `stream`
+    if (device_result) {
+        if (cudaMemcpyAsync(device_result, &status_dev->code, sizeof(int32_t), cudaMemcpyDeviceToDevice, st) !=
+                cudaSuccess ||
+            cudaMemcpyAsync(device_result + 1, iters_dev, sizeof(int32_t), cudaMemcpyDeviceToDevice, st) !=
+                cudaSuccess)
+            return GOM_E_CUDA;
+    }
     if (!iterations) return GOM_OK;   // asynchronous: the caller orders its own reads on `stream`
     struct {
         int iters;

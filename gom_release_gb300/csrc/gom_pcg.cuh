@@ -35,7 +35,7 @@ __device__ bool grid_barrier(unsigned *bar, unsigned nblocks, gom_status *st) {
             while (*vgen == gen) {
                 __nanosleep(64);
                 if (globaltimer_ns() - t0 > 1000000000ull) {
-                    record_error(st, GOM_E_TIMEOUT, 1, (int)blockIdx.x, 0, 0.0);
+                    record_error(st, GOM_E_TIMEOUT, 1, (int)blockIdx.x, 0, 0.0, GOM_ENTITY_OTHER);
                     good = 0;
                     break;
                 }
@@ -82,117 +82,385 @@ __device__ __forceinline__ double sum_partials(const double *part, int n, double
     return r;
 }
 
+// block reduction of two doubles at once (one pair of __syncthreads); results valid in every thread
+template <int THREADS>
+__device__ __forceinline__ void block_sum2(double &a, double &b, double *sh) {
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b += __shfl_down_sync(0xffffffffu, b, o);
+    }
+    int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) {
+        sh[w] = a;
+        sh[32 + w] = b;
+    }
+    __syncthreads();
+    if (w == 0) {
+        double ta = lane < THREADS / 32 ? sh[lane] : 0.0;
+        double tb = lane < THREADS / 32 ? sh[32 + lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) {
+            ta += __shfl_down_sync(0xffffffffu, ta, o);
+            tb += __shfl_down_sync(0xffffffffu, tb, o);
+        }
+        if (lane == 0) {
+            sh[64] = ta;
+            sh[65] = tb;
+        }
+    }
+    __syncthreads();
+    a = sh[64];
+    b = sh[65];
+    __syncthreads();
+}
+
+// -------------------------------------------------------------------- single-run FP64 solver
+// Grid barrier on a counter that only grows within a launch (cleared before it): barrier number k
+// waits until the counter reaches k x (blocks + phantom).  Arrival is a release reduction (the
+// block's earlier writes become visible before the count), the wait an acquire load; each wait
+// gives up after about 1 s with GOM_E_TIMEOUT.
+struct GridSync {
+    unsigned *bar;
+    unsigned nblocks;   // blocks of the grid + phantom blocks (tests)
+    unsigned k;
+    gom_status *st;
+    __device__ bool sync() {
+        __shared__ int ok;
+        __syncthreads();
+        ++k;
+        if (threadIdx.x == 0) {
+            asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(bar), "r"(1u) : "memory");
+            const unsigned target = k * nblocks;
+            int good = 1;
+            const unsigned long long t0 = globaltimer_ns();
+            unsigned spins = 0, v;
+            for (;;) {
+                asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(bar) : "memory");
+                if (v >= target) break;
+                if ((++spins & 255u) == 0 && globaltimer_ns() - t0 > 1000000000ull) {
+                    record_error(st, GOM_E_TIMEOUT, 1, (int)blockIdx.x, 0, 0.0, GOM_ENTITY_OTHER);
+                    good = 0;
+                    break;
+                }
+            }
+            __threadfence();
+            ok = good;
+        }
+        __syncthreads();
+        return ok != 0;
+    }
+};
+
+// pre_conj_grad.f90:9-230 -- the Jacobi-preconditioned CG of the reference, restated for GB300:
+//  * the Jacobi preconditioner is folded into the matrix: CG on A' = D^-1/2 A D^-1/2 with
+//    x' = D^1/2 x and r' = D^-1/2 r produces the iterates of Jacobi-PCG on A (M = D), with the
+//    reference's stop quantity r^T M^-1 r = r'^T r' -- and no M^-1 products per iteration
+//    (GB300 issues about 1 TFLOP/s of FP64, so FP64 operations per row set the cost);
+//  * the single-reduction form of Chronopoulos and Gear (J. Comput. Appl. Math. 25, 1989): both
+//    inner products of an iteration, gamma = r'^T r' and delta = w^T r' (w = A' r'), are reduced
+//    together, so an iteration needs ONE grid barrier.  Recurrences (s = A' p):
+//        p = r' + beta p,  s = w + beta s,  x' = x' + alpha p,  r' = r' - alpha s,  w = A' r',
+//        beta = gamma_new / gamma,  alpha = gamma_new / (delta_new - beta gamma_new / alpha).
+//    The product w = A' r' of a row needs the neighbours' new r', which the neighbours form in the
+//    same pass; each row recomputes them from the neighbours' previous r', s and w (the very
+//    operations the neighbour performs, so the values are identical), and r', s, w alternate
+//    between two buffers so that the previous values stay readable until the next barrier;
+//  * the stop test is the reference's, sqrt(gamma^2 / gamma_0^2) < tol after every iteration; one
+//    thread of each block forms the scalars from the block partials summed in a fixed order (so
+//    every block takes the same decisions); a zero initial residual leaves x untouched (the
+//    reference would divide 0 by 0).
+// The sums run in parallel, so the solution differs from a serial run in the last bits.
 struct PcgArgs {
-    Geom g;
-    const double *sp, *b;
-    double *x, *minv, *r, *s, *q, *dA, *dB, *pdq, *pdelta;
+    Geom g;                     // NC, tri_or_quad, adj_cellnum_at_cell
+    const double *sp, *b;       // (0:4, NC) rows, diagonal first; right-hand side
+    double *x;                  // initial guess in, solution out
+    double *dr;                 // D^-1/2 (work)
+    double *xs, *p;             // x' and p (work of the form without register rows)
+    double *r[2], *s[2], *w[2]; // r', A' p, A' r' (two buffers each)
+    double *pg, *pd;            // block partials of gamma and delta, two halves of gridDim.x each
     unsigned *bar;
     int *iters;
     int maxit;
     double tol;
     gom_status *st;
-    unsigned phantom;   // blocks the barriers wait for in addition to the grid (tests only)
+    unsigned phantom;           // blocks the barriers wait for in addition to the grid (tests only)
+    int check_diag;             // 1: a non-positive diagonal is GOM_E_NOT_SPD (systems the caller built)
 };
 
-// pre_conj_grad.f90:46-221 as one cooperative kernel: the matrix-vector product of row i uses
-// the row's own 5 coefficients in CSR order (diagonal first) and the neighbours' values; the
-// d-update of iteration n is fused into the product of iteration n+1 (d double-buffered), so one
-// iteration needs two grid barriers.  The solver's dot products are reduced in parallel (so its
-// result already differs from a serial run in the last bits); inside it every multiply-add is a
-// fused FMA, which halves its FP64 instruction count.
-constexpr int PCG_THREADS = 256;
+constexpr int PCG_CG_THREADS = 256;
+constexpr int PCG_CG_ROWS = 4;   // rows per thread of the register form
 
-__global__ void __launch_bounds__(PCG_THREADS) k_pcg(PcgArgs a) {
-    __shared__ double sh[40];
+// warp 0 sums the block partials (fixed order, reads from L2); with first, gamma_0 and alpha_0,
+// else one thread forms the iteration's scalars and the stop decision
+__device__ __forceinline__ void cg_scalars(const double *pg, const double *pd, int n, bool first, double &gamma,
+                                           double &alpha, double &beta, double gamma_0, double tol, int &stop,
+                                           double *sh) {
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (w == 0) {
+        double ta = 0.0, tb = 0.0;
+        for (int i = lane; i < n; i += 32) {
+            ta += __ldcg(pg + i);
+            tb += __ldcg(pd + i);
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            ta += __shfl_down_sync(0xffffffffu, ta, o);
+            tb += __shfl_down_sync(0xffffffffu, tb, o);
+        }
+        if (lane == 0) {
+            const double gn = ta, dn = tb;
+            sh[66] = gn;
+            if (first) {
+                sh[67] = 0.0;
+                sh[68] = gn / dn;
+                sh[69] = 0.0;
+            } else {
+                sh[69] = sqrt(gn * gn / (gamma_0 * gamma_0)) < tol ? 1.0 : 0.0;
+                const double bt = gn / gamma;
+                sh[67] = bt;
+                sh[68] = gn / (dn - bt * gn / alpha);
+            }
+        }
+    }
+    __syncthreads();
+    gamma = sh[66];
+    beta = sh[67];
+    alpha = sh[68];
+    stop = sh[69] != 0.0;
+    __syncthreads();
+}
+
+// ROWS > 0: each thread keeps its ROWS rows (scaled coefficients, neighbour ids, x', p, r', s, w)
+// in registers for the whole solve (grid x PCG_CG_THREADS x ROWS >= NC); ROWS == 0: rows
+// grid-strided, vectors in memory (any NC).  Both forms evaluate the same expressions in the same
+// order, so they give the same solution bit for bit.
+template <int ROWS> __global__ void __launch_bounds__(PCG_CG_THREADS, 1) k_pcg_cg1(PcgArgs a) {
+    constexpr int T = PCG_CG_THREADS;
+    constexpr int RR = ROWS > 0 ? ROWS : 1;
+    __shared__ double sh[72];
     const Geom &g = a.g;
     const int n = g.NC;
-    const unsigned nblocks = gridDim.x + a.phantom;
-    const long stride = (long)gridDim.x * blockDim.x;
-    const long t0 = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    // initial residual, Jacobi preconditioner, d = M^-1 r
-    double loc = 0.0;
-    for (long i = t0; i < n; i += stride) {
-        const double *row = a.sp + i * 5;
-        int cell = (int)i + 1;
-        double sum = row[0] * a.x[i];
-        int tq = g.tri_or_quad[i];
-        for (int l = 1; l <= tq; ++l) {
-            int nb = g.cell_adj(l, cell);
-            if (nb != 0) sum = fma(row[l], a.x[nb - 1], sum);
-        }
-        double mi = 1.0 / row[0];
-        double ri = a.b[i] - sum;
-        double di = mi * ri;
-        a.minv[i] = mi;
-        a.r[i] = ri;
-        a.dA[i] = di;
-        loc = fma(ri, di, loc);
+    const int P = gridDim.x;
+    const int stride = gridDim.x * T;
+    const int t0 = blockIdx.x * T + threadIdx.x;
+    GridSync B{a.bar, gridDim.x + a.phantom, 0u, a.st};
+    // D^-1/2
+    for (int i = t0; i < n; i += stride) {
+        const double d = a.sp[(long)i * 5];
+        if (a.check_diag && !(d > 0.0)) record_error(a.st, GOM_E_NOT_SPD, 100, i + 1, 0, d, GOM_ENTITY_CELL);
+        a.dr[i] = 1.0 / sqrt(d);
     }
-    double bs = block_sum<PCG_THREADS>(loc, sh);
-    if (threadIdx.x == 0) a.pdelta[blockIdx.x] = bs;
-    if (!grid_barrier(a.bar, nblocks, a.st)) return;
-    double delta_new = sum_partials(a.pdelta, gridDim.x, sh);
-    const double delta_0 = delta_new;
+    if (!B.sync() || failed(a.st)) return;
+    // scaled rows a'_il = dr_i a_il dr_m; r' = dr (b - A x); x' = x / dr
+    double spr[RR][4], xr[RR], pr[RR], rr[RR], sr[RR], wr[RR];
+    int nbr[RR][4];
+    if constexpr (ROWS > 0) {
+#pragma unroll
+        for (int q = 0; q < ROWS; ++q) {
+            const int i = t0 + q * stride;
+            const int ii = i < n ? i : 0;
+            const double *row = a.sp + (long)ii * 5;
+            const double di = a.dr[ii];
+            const int tq = g.tri_or_quad[ii];
+            double sum = row[0] * a.x[ii];
+#pragma unroll
+            for (int l = 0; l < 4; ++l) {
+                nbr[q][l] = l < tq ? g.adj_cellnum_at_cell[(long)ii * 4 + l] : 0;
+                spr[q][l] = 0.0;
+                if (nbr[q][l] != 0) {
+                    const int m = nbr[q][l] - 1;
+                    sum = fma(row[l + 1], a.x[m], sum);
+                    spr[q][l] = di * row[l + 1] * __ldcg(a.dr + m);
+                }
+            }
+            rr[q] = (a.b[ii] - sum) * di;
+            xr[q] = a.x[ii] / di;
+            pr[q] = 0.0;
+            sr[q] = 0.0;
+            if (i < n) {
+                a.r[0][i] = rr[q];
+                a.s[0][i] = 0.0;
+            }
+        }
+    } else {
+        for (int i = t0; i < n; i += stride) {
+            const double *row = a.sp + (long)i * 5;
+            const double di = a.dr[i];
+            const int tq = g.tri_or_quad[i];
+            double sum = row[0] * a.x[i];
+            for (int l = 0; l < tq; ++l) {
+                const int nb = g.adj_cellnum_at_cell[(long)i * 4 + l];
+                if (nb != 0) sum = fma(row[l + 1], a.x[nb - 1], sum);
+            }
+            a.r[0][i] = (a.b[i] - sum) * di;
+            a.xs[i] = a.x[i] / di;
+            a.p[i] = 0.0;
+            a.s[0][i] = 0.0;
+        }
+    }
+    if (!B.sync()) return;
+    // w = A' r', gamma_0, delta_0
+    double gl = 0.0, dl = 0.0;
+    if constexpr (ROWS > 0) {
+#pragma unroll
+        for (int q = 0; q < ROWS; ++q) {
+            const int i = t0 + q * stride;
+            double wsum = rr[q];
+#pragma unroll
+            for (int l = 0; l < 4; ++l)
+                if (nbr[q][l] != 0) wsum = fma(spr[q][l], __ldcg(a.r[0] + nbr[q][l] - 1), wsum);
+            wr[q] = wsum;
+            if (i < n) {
+                a.w[0][i] = wsum;
+                gl = fma(rr[q], rr[q], gl);
+                dl = fma(wsum, rr[q], dl);
+            }
+        }
+    } else {
+        for (int i = t0; i < n; i += stride) {
+            const double *row = a.sp + (long)i * 5;
+            const double di = a.dr[i];
+            const double ri = a.r[0][i];
+            const int tq = g.tri_or_quad[i];
+            double wsum = ri;
+            for (int l = 0; l < tq; ++l) {
+                const int nb = g.adj_cellnum_at_cell[(long)i * 4 + l];
+                if (nb != 0) wsum = fma(di * row[l + 1] * __ldcg(a.dr + nb - 1), __ldcg(a.r[0] + nb - 1), wsum);
+            }
+            a.w[0][i] = wsum;
+            gl = fma(ri, ri, gl);
+            dl = fma(wsum, ri, dl);
+        }
+    }
+    block_sum2<T>(gl, dl, sh);
+    if (threadIdx.x == 0) {
+        a.pg[blockIdx.x] = gl;
+        a.pd[blockIdx.x] = dl;
+    }
+    if (!B.sync()) return;
+    double gamma = 0.0, alpha = 0.0, beta = 0.0;
+    int stop = 0;
+    cg_scalars(a.pg, a.pd, P, true, gamma, alpha, beta, 0.0, 0.0, stop, sh);
+    const double gamma_0 = gamma;
     int iters = 0;
-    if (delta_0 != 0.0) {
-        double beta = 0.0;
-        double *dcur = a.dA, *dnext = a.dB;
-        bool first = true;
+    if (gamma_0 != 0.0) {
+        int cur = 0, par = 1;
         for (int it = 1; it <= a.maxit; ++it) {
             if (failed(a.st)) return;
-            // q = A d with d = s + beta*d_old fused in
-            loc = 0.0;
-            for (long i = t0; i < n; i += stride) {
-                const double *row = a.sp + i * 5;
-                int cell = (int)i + 1;
-                double di = first ? dcur[i] : fma(beta, dcur[i], a.s[i]);
-                double sum = row[0] * di;
-                int tq = g.tri_or_quad[i];
-                for (int l = 1; l <= tq; ++l) {
-                    int nb = g.cell_adj(l, cell);
-                    if (nb != 0) {
-                        double dn = first ? dcur[nb - 1] : fma(beta, dcur[nb - 1], a.s[nb - 1]);
-                        sum = fma(row[l], dn, sum);
+            const double *rc = a.r[cur], *sc = a.s[cur], *wc = a.w[cur];
+            double *rn = a.r[cur ^ 1], *sn = a.s[cur ^ 1], *wn = a.w[cur ^ 1];
+            gl = 0.0;
+            dl = 0.0;
+            if constexpr (ROWS > 0) {
+                double nr[ROWS][4], ns[ROWS][4], nw[ROWS][4];
+#pragma unroll
+                for (int q = 0; q < ROWS; ++q)
+#pragma unroll
+                    for (int l = 0; l < 4; ++l) {
+                        const int m = nbr[q][l] != 0 ? nbr[q][l] - 1 : 0;
+                        nr[q][l] = __ldcg(rc + m);
+                        ns[q][l] = __ldcg(sc + m);
+                        nw[q][l] = __ldcg(wc + m);
+                    }
+#pragma unroll
+                for (int q = 0; q < ROWS; ++q) {
+                    const int i = t0 + q * stride;
+                    const double pi = fma(beta, pr[q], rr[q]);
+                    const double si = fma(beta, sr[q], wr[q]);
+                    pr[q] = pi;
+                    xr[q] = fma(alpha, pi, xr[q]);
+                    const double rni = fma(-alpha, si, rr[q]);
+                    double wsum = rni;
+#pragma unroll
+                    for (int l = 0; l < 4; ++l)
+                        if (nbr[q][l] != 0)
+                            wsum = fma(spr[q][l], fma(-alpha, fma(beta, ns[q][l], nw[q][l]), nr[q][l]), wsum);
+                    rr[q] = rni;
+                    sr[q] = si;
+                    wr[q] = wsum;
+                    if (i < n) {
+                        rn[i] = rni;
+                        sn[i] = si;
+                        wn[i] = wsum;
+                        gl = fma(rni, rni, gl);
+                        dl = fma(wsum, rni, dl);
                     }
                 }
-                if (!first) dnext[i] = di;
-                a.q[i] = sum;
-                loc = fma(di, sum, loc);
+            } else {
+                for (int i = t0; i < n; i += stride) {
+                    const double *row = a.sp + (long)i * 5;
+                    const double di = a.dr[i];
+                    const double pi = fma(beta, a.p[i], rc[i]);
+                    const double si = fma(beta, sc[i], wc[i]);
+                    a.p[i] = pi;
+                    a.xs[i] = fma(alpha, pi, a.xs[i]);
+                    const double rni = fma(-alpha, si, rc[i]);
+                    double wsum = rni;
+                    const int tq = g.tri_or_quad[i];
+                    for (int l = 0; l < tq; ++l) {
+                        const int nb = g.adj_cellnum_at_cell[(long)i * 4 + l];
+                        if (nb != 0) {
+                            const int m = nb - 1;
+                            const double al = di * row[l + 1] * __ldcg(a.dr + m);
+                            wsum = fma(al, fma(-alpha, fma(beta, __ldcg(sc + m), __ldcg(wc + m)), __ldcg(rc + m)), wsum);
+                        }
+                    }
+                    rn[i] = rni;
+                    sn[i] = si;
+                    wn[i] = wsum;
+                    gl = fma(rni, rni, gl);
+                    dl = fma(wsum, rni, dl);
+                }
             }
-            bs = block_sum<PCG_THREADS>(loc, sh);
-            if (threadIdx.x == 0) a.pdq[blockIdx.x] = bs;
-            if (!grid_barrier(a.bar, nblocks, a.st)) return;
-            double dq = sum_partials(a.pdq, gridDim.x, sh);
-            double alpha = delta_new / dq;
-            double *dv = first ? dcur : dnext;
-            loc = 0.0;
-            for (long i = t0; i < n; i += stride) {
-                double di = dv[i];
-                a.x[i] = fma(alpha, di, a.x[i]);
-                double ri = fma(-alpha, a.q[i], a.r[i]);
-                a.r[i] = ri;
-                double si = a.minv[i] * ri;
-                a.s[i] = si;
-                loc = fma(ri, si, loc);
+            block_sum2<T>(gl, dl, sh);
+            if (threadIdx.x == 0) {
+                a.pg[par * P + blockIdx.x] = gl;
+                a.pd[par * P + blockIdx.x] = dl;
             }
-            bs = block_sum<PCG_THREADS>(loc, sh);
-            if (threadIdx.x == 0) a.pdelta[blockIdx.x] = bs;
-            if (!grid_barrier(a.bar, nblocks, a.st)) return;
-            double delta_old = delta_new;
-            delta_new = sum_partials(a.pdelta, gridDim.x, sh);
-            beta = delta_new / delta_old;
-            if (!first) {
-                double *t = dcur;
-                dcur = dnext;
-                dnext = t;
-            }
-            first = false;
+            if (!B.sync()) return;
+            cg_scalars(a.pg + par * P, a.pd + par * P, P, false, gamma, alpha, beta, gamma_0, a.tol, stop, sh);
+            par ^= 1;
+            cur ^= 1;
             iters = it;
-            if (sqrt(delta_new * delta_new / (delta_0 * delta_0)) < a.tol) break;
+            if (stop) break;
+        }
+    }
+    // x = D^-1/2 x' (a solve without iterations leaves x as it came)
+    if (iters > 0) {
+        if constexpr (ROWS > 0) {
+#pragma unroll
+            for (int q = 0; q < ROWS; ++q) {
+                const int i = t0 + q * stride;
+                if (i < n) a.x[i] = xr[q] * a.dr[i];
+            }
+        } else {
+            for (int i = t0; i < n; i += stride) a.x[i] = a.xs[i] * a.dr[i];
         }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) *a.iters = iters;
 }
+
+// Launch of the single-run solver (cooperative, on cfg's stream): the register form when the rows
+// fit num_sms x PCG_CG_THREADS x PCG_CG_ROWS, else the strided form on one block per SM.
+inline cudaError_t launch_pcg_cg1(cudaLaunchConfig_t cfg, const PcgArgs &a, int num_sms) {
+    const long n = a.g.NC;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cfg.blockDim = dim3(PCG_CG_THREADS);
+    cfg.dynamicSmemBytes = 0;
+    const long per_block = (long)PCG_CG_THREADS * PCG_CG_ROWS;
+    if (n <= per_block * num_sms) {
+        long b = (n + per_block - 1) / per_block;
+        cfg.gridDim = dim3((unsigned)(b < 1 ? 1 : b));
+        return cudaLaunchKernelEx(&cfg, k_pcg_cg1<PCG_CG_ROWS>, a);
+    }
+    cfg.gridDim = dim3((unsigned)num_sms);
+    return cudaLaunchKernelEx(&cfg, k_pcg_cg1<0>, a);
+}
+
+// threads per block of the mixed-precision and packed-run solvers below
+constexpr int PCG_THREADS = 256;
 
 // -------------------------------------------------------------------- mixed precision
 // FP32 inner PCG iterations inside FP64 iterative refinement.  Each refinement step forms the
@@ -449,8 +717,9 @@ __global__ void __launch_bounds__(PCG_THREADS) k_pcg_seg(PcgSegArgs a) {
     __syncthreads();
     double *dcur = a.dA, *dnext = a.dB;
     bool first = true;
+    // no early exit on a failure recorded elsewhere: a failure belongs to one run, and the other
+    // runs' solves must complete (a barrier that times out ends the solve by itself)
     for (int it = 1; it <= a.maxit; ++it) {
-        if (failed(a.st)) return;
         int active = 0;
         for (int r = 0; r < NR; ++r) active |= !s_done[r];
         if (!active) break;
@@ -573,8 +842,9 @@ __global__ void __launch_bounds__(PCG_THREADS) k_pcg_mixed_seg(PcgMixedSegArgs a
     bool first = true;
     double d0 = 0.0;
     float dn = 0.0f, din0 = 0.0f, itol = 0.0f, beta = 0.0f;
+    // no early exit on a failure recorded elsewhere: it belongs to one run, and the others' solves
+    // must complete (a barrier of this run that times out ends this run's solve by itself)
     for (;;) {
-        if (failed(a.st)) return;
         if (mode == RUN_DONE) break;
         float *dcur = dpar ? a.dB : a.dA, *dnext = dpar ? a.dA : a.dB;
         // pass A: true residual (RESID) or inner matrix-vector product (INNER)

@@ -16,6 +16,10 @@ namespace gom {
 
 // ============================================================================================
 // calculate_bottom_friction.f90:21-63; bf_flag 3 is the constant-Cd extension. One thread per face.
+// Manning's Cdb depends on the static depth alone and comes formed on the host (the C library's
+// pow, as the reference calls it); the log law's comes formed on the host for the static bottom
+// half-thickness of a column with more than one layer, and is formed here only for a column of
+// one layer, whose half-thickness is its depth (CUDA's log, within 1 ulp of the C library's).
 template <typename R> __global__ void k_bottom_friction(Geom g, StateT<R> s, Params p) {
     int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
     if (j > g.NF) return;
@@ -25,12 +29,15 @@ template <typename R> __global__ void k_bottom_friction(Geom g, StateT<R> s, Par
     if (p.bf_flag >= 1 && p.bf_flag <= 3 && hf > p.dry_depth) {
         int k = g.bottom_face[j - 1];
         if (p.bf_flag == 1) {
-            double hr = fmax(1.0, hf);
-            double chezy = pow(hr, 1.0 / 6.0) / g.manning[j - 1];
-            cdb = p.gravity / (chezy * chezy);
+            cdb = g.cdb_static[j - 1];
         } else if (p.bf_flag == 2) {
-            double lg = log(fmax(0.5, s.dzhalf_face[ix0(k - 1, j, L)]) / g.bf_height[j - 1]);
-            cdb = p.von_karman * p.von_karman / (lg * lg);
+            const double dzh = s.dzhalf_face[ix0(k - 1, j, L)];
+            if (dzh == g.cdb_arg[j - 1]) {
+                cdb = g.cdb_static[j - 1];
+            } else {
+                double lg = log(fmax(0.5, dzh) / g.bf_height[j - 1]);
+                cdb = p.von_karman * p.von_karman / (lg * lg);
+            }
         } else {
             cdb = p.cd_const;
         }
@@ -54,7 +61,7 @@ template <typename R> __global__ void k_boundary_velocity(Geom g, StateT<R> s, F
     int n1 = g.face_node(1, j), n2 = g.face_node(2, j);
     double depth = g.h_face[j - 1] + (s.eta_node[n1 - 1] + s.eta_node[n2 - 1]) * 0.5;
     if (depth < p.dry_depth) {
-        record_error(st, GOM_E_DRY, 80, i, 0, depth);
+        record_error(st, GOM_E_DRY, 80, i, 0, depth, GOM_ENTITY_OTHER);
         return;
     }
     s.qu_boundary[i - 1] = -f.q_add[i - 1] / (g.face_length[j - 1] * depth);
@@ -1069,7 +1076,7 @@ __device__ void elm_face_layer(const Geom &g, const StateT<R> &s, const Params &
     int near = 0;
     int e = elm_backtrace<R, MIXED>(g, s, p, bt_step, bt_dt, uu, vv, ww, x0, y0, z0, nnel, jlev, near);
     if (e) {
-        record_error(st, GOM_E_ELM, e, j, k, 0.0);
+        record_error(st, GOM_E_ELM, e, j, k, 0.0, GOM_ENTITY_FACE);
         return;
     }
     s.elm_foot[o] = nnel;
@@ -1457,10 +1464,12 @@ template <typename R> __global__ void k_elmtr_backtrack(Geom g, StateT<R> s, For
         int e = elm_backtrace<R, MIXED>(g, s, p, bt_step, bt_dt, uu, vv, ww, x0, y0, z0, nnel, jlev, near, &fin);
         if (!e) e = elm_tracer_at_foot(g, s, f, fin, nnel, jlev, tc, sc);
         if (e) {
-            record_error(st, GOM_E_ELM, e, i, k, 0.0);
+            record_error(st, GOM_E_ELM, e, i, k, 0.0, GOM_ENTITY_CELL);
             return;
         }
     }
+    // :120 the per-layer heat source (zero unless the host's heat-balance model sets phi_sz)
+    tc = tc + p.dt * f.phi_sz[ix(k, i, L)] / (p.rho_o * 4186.0 * (double)s.dz_cell[ix(k, i, L)]);
     con[oT] = (R)tc;
     con[oS] = (R)sc;
 }
@@ -1527,7 +1536,7 @@ template <typename R> __global__ void k_elmtr_vsolve(Geom g, StateT<R> s, Params
         rr[k - 1][1] = s.dz_cell[ix(kk, i, L)] * rhs[(long)NC * L + oT];
     }
     if (!thomas<2>(nvl, am, bm, cm, rr, gm)) {
-        record_error(st, GOM_E_ZERO_PIVOT, 210, i, 0, 0.0);
+        record_error(st, GOM_E_ZERO_PIVOT, 210, i, 0, 0.0, GOM_ENTITY_CELL);
         return;
     }
     for (int k = 1; k <= L; ++k) {
@@ -1986,7 +1995,7 @@ __global__ void __launch_bounds__(256) k_momentum(Geom g, StateT<R> s, Forcing f
         momentum_row(g, s, p, m, L, r + 1, g1, g2, dzr);
         if (r == 0) {
             if (bd_r == R(0)) {
-                record_error(st, GOM_E_ZERO_PIVOT, 587, j, 0, 0.0);
+                record_error(st, GOM_E_ZERO_PIVOT, 587, j, 0, 0.0, GOM_ENTITY_FACE);
                 return;
             }
             den = bd_r;
@@ -1998,7 +2007,7 @@ __global__ void __launch_bounds__(256) k_momentum(Geom g, StateT<R> s, Forcing f
             gam(r) = gr;
             den = bd_r - a_r * gr;
             if (den == R(0)) {
-                record_error(st, GOM_E_ZERO_PIVOT, 587, j, 0, 0.0);
+                record_error(st, GOM_E_ZERO_PIVOT, 587, j, 0, 0.0, GOM_ENTITY_FACE);
                 return;
             }
             sol(r, 0) = (g1 - a_r * sol(r - 1, 0)) / den;

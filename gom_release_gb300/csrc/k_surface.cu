@@ -60,7 +60,7 @@ __global__ void k_fs_assemble(Geom g, StateT<R> s, Forcing f, Params p, const do
         if (s.top_face[j - 1] == 0) continue;
         double coef = fs[(long)(j - 1) * 3] * g.cos_theta2[j - 1];
         if (coef < 0.0) {
-            record_error(st, GOM_E_NOT_SPD, 100, i, 0, coef);
+            record_error(st, GOM_E_NOT_SPD, 100, i, 0, coef, GOM_ENTITY_CELL);
             return;
         }
         diag = diag + coef;
@@ -133,8 +133,7 @@ template <typename R> __global__ void k_node_eta_dry(Geom g, StateT<R> s) {
 template <typename R> cudaError_t pcg_configure(LaunchT<R> &x, int device) {
     // every block of the cooperative grid must be resident, whichever solver the context uses
     int per_sm = 1 << 30;
-    const void *kernels[] = {(const void *)k_pcg, (const void *)k_pcg_mixed, (const void *)k_pcg_seg,
-                             (const void *)k_pcg_mixed_seg};
+    const void *kernels[] = {(const void *)k_pcg_mixed, (const void *)k_pcg_seg, (const void *)k_pcg_mixed_seg};
     for (const void *k : kernels) {
         int n = 0;
         cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, PCG_THREADS, 0);
@@ -148,6 +147,13 @@ template <typename R> cudaError_t pcg_configure(LaunchT<R> &x, int device) {
     x.w.pcg_threads = PCG_THREADS;
     if (x.g.NR <= 1) {
         x.w.pcg_blocks = pcg_blocks_for(x.g.NC, per_sm, x.num_sms);
+        // the single-run FP64 solver: one block of PCG_CG_THREADS per SM
+        for (const void *k : {(const void *)k_pcg_cg1<PCG_CG_ROWS>, (const void *)k_pcg_cg1<0>}) {
+            int cg_per_sm = 0;
+            cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cg_per_sm, k, PCG_CG_THREADS, 0);
+            if (e != cudaSuccess) return e;
+            if (cg_per_sm < 1) return cudaErrorNotSupported;
+        }
         return cudaSuccess;
     }
     // packed runs: one block at least per run, the rest of the grid split in proportion to the
@@ -292,21 +298,25 @@ template <typename R> cudaError_t launch_free_surface(const LaunchT<R> &x) {
     a.sp = x.w.sparsem;
     a.b = x.w.rhs;
     a.x = x.s.eta_cell_new;
-    a.minv = x.w.minv;
-    a.r = x.w.r;
-    a.s = x.w.s;
-    a.q = x.w.q;
-    a.dA = x.w.d0;
-    a.dB = x.w.d1;
-    a.pdq = x.w.partial_dq;
-    a.pdelta = x.w.partial_delta;
+    a.dr = x.w.minv;
+    a.xs = x.w.cg_xs;
+    a.p = x.w.d0;
+    a.r[0] = x.w.r;
+    a.r[1] = x.w.d1;
+    a.s[0] = x.w.s;
+    a.s[1] = x.w.cg_s1;
+    a.w[0] = x.w.q;
+    a.w[1] = x.w.cg_w1;
+    a.pg = x.w.partial_dq;
+    a.pd = x.w.partial_delta;
     a.bar = x.w.barrier;
     a.iters = x.w.pcg_iters;
     a.maxit = x.p.max_iteration_pcg;
     a.tol = x.p.error_tolerance;
     a.st = x.status;
     a.phantom = phantom;
-    e = cudaLaunchKernelEx(&cfg, k_pcg, a);
+    a.check_diag = 0;   // k_fs_assemble has checked every row
+    e = launch_pcg_cg1(cfg, a, x.num_sms);
     if (e != cudaSuccess) return e;
     k_node_eta<<<blocks_for(g.NN, 256), 256, 0, x.stream>>>(x.g, x.s);
     k_node_eta_dry<<<blocks_for(g.NN, 256), 256, 0, x.stream>>>(x.g, x.s);
@@ -634,7 +644,7 @@ template <typename R> __global__ void k_layers_cells(Geom g, StateT<R> s, Params
     int tnew = new_column<0>(g, p, g.h_cell[i - 1], s.eta_cell_new[i - 1], b, s.dz_cell_new, s.dzhalf_cell_new,
                              (long)(i - 1) * L, (long)(i - 1) * (L + 1), bad);
     if (bad) {
-        record_error(st, GOM_E_LAYER, 66, i, tnew, s.eta_cell_new[i - 1]);
+        record_error(st, GOM_E_LAYER, 66, i, tnew, s.eta_cell_new[i - 1], GOM_ENTITY_CELL);
         return;
     }
     if (s.top_cell[i - 1] == 0 && tnew != 0)
@@ -653,14 +663,14 @@ template <typename R> __global__ void k_layers_faces(Geom g, StateT<R> s, Params
     int tnew = new_column<1>(g, p, g.h_face[j - 1], eta_max, b, s.dz_face_new, s.dzhalf_face_new, (long)(j - 1) * L,
                              (long)(j - 1) * (L + 1), bad);
     if (bad) {
-        record_error(st, GOM_E_LAYER, 166, j, tnew, eta_max);
+        record_error(st, GOM_E_LAYER, 166, j, tnew, eta_max, GOM_ENTITY_FACE);
         return;
     }
     s.top_face[j - 1] = tnew;
     for (int k = b; k <= tnew - 1; ++k) {
         double v = s.dzhalf_face_new[ix0(k, j, L)];
         if (v < p.denominator_min_for_matrix) {
-            record_error(st, GOM_E_LAYER, 301, j, k, v);
+            record_error(st, GOM_E_LAYER, 301, j, k, v, GOM_ENTITY_FACE);
             return;
         }
     }
@@ -675,14 +685,14 @@ template <typename R> __global__ void k_layers_nodes(Geom g, StateT<R> s, Params
     int tnew = new_column<2>(g, p, g.h_node[i - 1], s.eta_node[i - 1], b, s.dz_node_new, s.dzhalf_node_new,
                              (long)(i - 1) * L, (long)(i - 1) * (L + 1), bad);
     if (bad) {
-        record_error(st, GOM_E_LAYER, 224, i, tnew, s.eta_node[i - 1]);
+        record_error(st, GOM_E_LAYER, 224, i, tnew, s.eta_node[i - 1], GOM_ENTITY_NODE);
         return;
     }
     s.top_node[i - 1] = tnew;
     for (int k = b; k <= tnew - 1; ++k) {
         double v = s.dzhalf_node_new[ix0(k, i, L)];
         if (v < p.denominator_min_for_matrix) {
-            record_error(st, GOM_E_LAYER, 318, i, k, v);
+            record_error(st, GOM_E_LAYER, 318, i, k, v, GOM_ENTITY_NODE);
             return;
         }
     }
@@ -705,13 +715,13 @@ template <typename R> __global__ void k_layers_check(Geom g, StateT<R> s, Params
         s.top_cell[i - 1] = 0;
     }
     if (nsum2 == 0 && t != 0) {
-        record_error(st, GOM_E_DRY, 273, i, 0, 0.0);
+        record_error(st, GOM_E_DRY, 273, i, 0, 0.0, GOM_ENTITY_CELL);
         return;
     }
     for (int k = g.bottom_cell[i - 1]; k <= t - 1; ++k) {
         double v = s.dzhalf_cell_new[ix0(k, i, L)];
         if (v < p.denominator_min_for_matrix) {
-            record_error(st, GOM_E_LAYER, 284, i, k, v);
+            record_error(st, GOM_E_LAYER, 284, i, k, v, GOM_ENTITY_CELL);
             return;
         }
     }
@@ -752,7 +762,7 @@ __global__ void k_cold_layers(Geom g, Params p, int n, const double *h, const in
         }
         const int b = bottom[e];
         if (t < b) {
-            record_error(st, GOM_E_LAYER, 66, e + 1, t, eta);
+            record_error(st, GOM_E_LAYER, 66, e + 1, t, eta, GOM_ENTITY_CELL);
             return;
         }
         if (t == b) {
@@ -784,7 +794,7 @@ __global__ void k_cold_cells(Geom g, StateT<R> s, Params p, R salt, R temp, R av
             n2 += s.top_face[g.cell_face(l, i) - 1];
         }
         if (n1 == 0) s.top_cell[i - 1] = 0;
-        if (n2 == 0 && s.top_cell[i - 1] != 0) record_error(st, GOM_E_DRY, 273, i, 0, 0.0);
+        if (n2 == 0 && s.top_cell[i - 1] != 0) record_error(st, GOM_E_DRY, 273, i, 0, 0.0, GOM_ENTITY_CELL);
         for (int k = 1; k <= L; ++k) {
             long o = ix(k, i, L);
             s.salt_cell[o] = salt;

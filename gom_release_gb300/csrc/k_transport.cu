@@ -84,7 +84,8 @@ template <typename R> __device__ __forceinline__ R diffusive_share(R D, R Q) {
     return fmin(R(1), R(2) * D / aq);
 }
 
-// :88-173 load tracers into con (0:L+1) with the heat_option 2 surface term
+// :88-173 load tracers into con (0:L+1) with the heat_option 1 per-layer source or the heat_option 2
+// surface term
 template <typename R> __global__ void k_tr_load(TArgs<R> a) {
     unsigned t = flat_tid();
     const Geom &g = a.g;
@@ -101,6 +102,10 @@ template <typename R> __global__ void k_tr_load(TArgs<R> a) {
                 int tl = a.s.top_cell[i - 1];
                 if (tl > 0)
                     v = v + (R)(a.p.dt * a.f.phi_sw[i - 1]) / ((R)(a.p.rho_o * 4186.0) * a.s.dz_cell[ix(tl, i, L)]);
+            } else if (a.tid[tr] == 2 && a.p.heat_option == 1) {
+                // :109-131 the per-layer source over the wet layers
+                if (k >= a.g.bottom_cell[i - 1] && k <= a.s.top_cell[i - 1])
+                    v = v + (R)(a.p.dt * a.f.phi_sz[ix(k, i, L)]) / ((R)(a.p.rho_o * 4186.0) * a.s.dz_cell[ix(k, i, L)]);
             }
         }
         ((R *)a.con)[ic(k, i, tr, L, g.NC)] = v;
@@ -717,7 +722,7 @@ template <typename R> __device__ void tr_solve_column(const TArgs<R> &a, int i) 
         for (int k = 0; k < nvl; ++k) rhs[k][0] = r1[k][0];
     }
     if (!okp) {
-        record_error(a.st, GOM_E_ZERO_PIVOT, 1285, i, 0, 0.0);
+        record_error(a.st, GOM_E_ZERO_PIVOT, 1285, i, 0, 0.0, GOM_ENTITY_CELL);
         return;
     }
     for (int tr = 0; tr < a.ntr; ++tr) {
@@ -995,7 +1000,7 @@ template <typename R> __global__ void __launch_bounds__(256) k_tr_thomas_col(TAr
             x[r - 1][tr] = (a.w.tr_rhs[((long)tr * NC + i - 1) * L + k - 1] - lower * x[r - 2][tr]) / den;
     }
     if (!ok) {
-        record_error(a.st, GOM_E_ZERO_PIVOT, 1285, i, 0, 0.0);
+        record_error(a.st, GOM_E_ZERO_PIVOT, 1285, i, 0, 0.0, GOM_ENTITY_CELL);
         return;
     }
     for (int r = nvl - 1; r >= 1; --r)
@@ -1333,7 +1338,7 @@ __global__ void k_density_col(Geom g, StateT<R> s, Params p, gom_status *st) {
     for (int k = b; k <= t; ++k) {
         double rtemp = tt[ix(k, e, L)], rsalt = ss[ix(k, e, L)];
         if (rtemp < -5.0 || rtemp > 100.0 || rsalt < -5.0 || rsalt > 100.0) {
-            record_error(st, GOM_E_DENSITY, KIND == 0 ? 43 : 130, e, k, (rtemp < -5.0 || rtemp > 100.0) ? rtemp : rsalt);
+            record_error(st, GOM_E_DENSITY, KIND == 0 ? 43 : 130, e, k, (rtemp < -5.0 || rtemp > 100.0) ? rtemp : rsalt, KIND == 0 ? GOM_ENTITY_NODE : GOM_ENTITY_FACE);
             return;
         }
         double r;
@@ -1354,7 +1359,7 @@ __global__ void k_density_col(Geom g, StateT<R> s, Params p, gom_status *st) {
         }
         rho[ix(k, e, L)] = r;
         if (r < F(980.0f)) {
-            record_error(st, GOM_E_DENSITY, KIND == 0 ? 103 : 188, e, k, r);
+            record_error(st, GOM_E_DENSITY, KIND == 0 ? 103 : 188, e, k, r, KIND == 0 ? GOM_ENTITY_NODE : GOM_ENTITY_FACE);
             return;
         }
     }
@@ -1384,7 +1389,7 @@ template <typename R> __global__ void k_density_cells(Geom g, StateT<R> s, gom_s
             }
         }
         if (icount == 0) {
-            record_error(st, GOM_E_DRY, 224, i, k, 0.0);
+            record_error(st, GOM_E_DRY, 224, i, k, 0.0, GOM_ENTITY_CELL);
             return;
         }
         s.rho_cell[ix(k, i, L)] = r / icount;

@@ -206,9 +206,18 @@ class PackedServer:
     clock offset per run.  Requests that arrive while others run are admitted at the next repack:
     a new packed context is created with the runs still in flight plus the newcomers, the in-flight
     runs' state is copied over with gom_copy_run, the newcomers start from a device cold start.
-    Repacks happen when requests are waiting (at most every ``min_interval`` seconds) or when
-    finished runs hold more than half of the packed cells; the device-memory budget bounds the
-    cells a pack may hold."""
+    Repacks happen when requests are waiting (at most every ``min_interval`` seconds), when
+    finished runs hold more than half of the packed cells, or when a run has failed.
+
+    Memory: a repack holds the old and the new context at once, so a request is admitted only
+    while the old context's bytes plus the new pack's estimated bytes fit the budget; the bytes per
+    cell-layer are measured on a one-run context before the first admission and refined from
+    every pack created.  ``peak_bytes`` counts that transient.
+
+    Failures: the device reports the first failing entity of a step and the library maps it to its
+    run (gom_status.run).  Only that run is retired with the error; the step completed for the
+    others (their phases never read another run's values), which continue in the next pack.  A
+    failure that names no run (a solver barrier that timed out) fails every run of the pack."""
 
     def __init__(self, lib, budget_bytes: float, precision: int = 1, min_interval: float = 0.5,
                  on_finish=None):
@@ -227,6 +236,10 @@ class PackedServer:
         self.peak_bytes = 0.0
         self.peak_active = 0
         self.repacks = 0
+        self.repack_s: list[float] = []       # wall seconds of every repack
+        self.failed_runs = 0
+        self.rejected: list[Request] = []     # requests larger than the whole budget
+        self._gc_now = False                  # a run failed: drop it at the next repack
 
     def _cells(self, reqs) -> float:
         return float(sum(r.deck.n_cells * (r.deck.n_layers + 2) for r in reqs))
@@ -234,28 +247,51 @@ class PackedServer:
     def active(self) -> list[Request]:
         return [r for r in self.members if r.finished < 0]
 
+    def _measure_bytes_per_cell_layer(self, req: Request) -> float:
+        """Device bytes per cell-layer of a one-run context of ``req`` (created and closed)."""
+        c = storm_context(self.lib, req.deck, self.precision, [req.storm])
+        try:
+            return c.device_bytes() / self._cells([req])
+        finally:
+            c.close()
+
     def maybe_repack(self, now: float):
         live = self.active()
         dead = self._cells([r for r in self.members if r.finished >= 0])
         want_new = bool(self.waiting) and (now - self.last_repack >= self.min_interval or not live)
-        want_gc = dead > 0.5 * max(self._cells(self.members), 1.0)
+        want_gc = self._gc_now or dead > 0.5 * max(self._cells(self.members), 1.0)
         if not (want_new or want_gc):
             return
+        old_bytes = float(self.core.device_bytes()) if self.core is not None else 0.0
         admitted = []
         if want_new:
-            budget_cells = (self.budget / self.bytes_per_cell_layer) if self.bytes_per_cell_layer else float("inf")
+            if self.bytes_per_cell_layer is None:
+                self.bytes_per_cell_layer = self._measure_bytes_per_cell_layer(self.waiting[0])
+            bpcl = self.bytes_per_cell_layer
             used = self._cells(live)
-            while self.waiting and (not live and not admitted or
-                                    used + self._cells([self.waiting[0]]) <= budget_cells):
+            # the old context stays alive while the new one is filled
+            while self.waiting and old_bytes + bpcl * (used + self._cells([self.waiting[0]])) <= self.budget:
                 r = self.waiting.pop(0)
                 used += self._cells([r])
                 admitted.append(r)
+            if not admitted and not live and self.waiting:
+                # nothing in flight and the first request alone exceeds the budget: it cannot run
+                r = self.waiting.pop(0)
+                r.error = "request exceeds the device-memory budget"
+                r.started = r.finished = now
+                r.done_steps = 0
+                self.rejected.append(r)
         if not admitted and not want_gc:
             return
-        self._repack(live, admitted, now)
+        if (not admitted and live and self.bytes_per_cell_layer
+                and old_bytes + self.bytes_per_cell_layer * self._cells(live) > self.budget):
+            return   # the shrunk pack does not fit beside the old one yet; wait for runs to finish
+        self._gc_now = False
+        self._repack(live, admitted, now, old_bytes)
 
-    def _repack(self, live, admitted, now):
+    def _repack(self, live, admitted, now, old_bytes=0.0):
         from .ensemble import pack
+        t_start = time.perf_counter()
         old, old_members = self.core, self.members
         members = live + admitted
         self.members = members
@@ -265,6 +301,7 @@ class PackedServer:
             if old is not None:
                 old.close()
             self.core = None
+            self.repack_s.append(time.perf_counter() - t_start)
             return
         base = pack([r.deck for r in members])
         deck = dataclasses.replace(base, params=dataclasses.replace(base.params, precision=self.precision))
@@ -282,6 +319,8 @@ class PackedServer:
             r.t0 = self.elapsed
             r.started = now
         core.set_storms([dataclasses.replace(r.storm, t0=r.t0) for r in members], elapsed_time=self.elapsed)
+        nbytes = core.device_bytes()
+        self.peak_bytes = max(self.peak_bytes, float(nbytes) + old_bytes)   # both contexts are alive here
         if old is not None:
             for new_idx, r in enumerate(live):
                 core.copy_run(new_idx, old, old_members.index(r))
@@ -294,22 +333,31 @@ class PackedServer:
                 sl = slice(cs[i], cs[i + 1])
                 t, b = top[sl], bot[sl]
                 r.cell_layers = int(np.sum((t - b + 1)[t > 0]))
-        nbytes = core.device_bytes()
         self.bytes_per_cell_layer = max(self.bytes_per_cell_layer or 0.0, nbytes / self._cells(members))
-        self.peak_bytes = max(self.peak_bytes, float(nbytes))
         self.peak_active = max(self.peak_active, len(members))
         self.core = core
         self.deck = deck
+        self.repack_s.append(time.perf_counter() - t_start)
+
+    def _step(self) -> GomError | None:
+        """One step of every run in the pack; the step's error, if any."""
+        self.core.step_launch()
+        try:
+            self.core.step_wait()
+        except GomError as e:
+            return e
+        return None
 
     def tick(self, clock) -> list[Request]:
         if self.core is None:
             return []
-        self.core.step_launch()
-        err = ""
-        try:
-            self.core.step_wait()
-        except GomError as e:
-            err = str(e)
+        err = self._step()
+        culprit = None
+        if err is not None:
+            st = err.status
+            if st is not None and st.code and 0 <= st.run < len(self.members):
+                culprit = st.run
+            self.core.status(clear=True)
         self.elapsed += self.deck.params.dt
         now = clock()
         done = []
@@ -317,13 +365,17 @@ class PackedServer:
             if r.finished >= 0:
                 continue
             r.done_steps += 1
-            if err:
-                r.error = err
-            if r.done_steps >= r.steps or err:
+            failed = err is not None and (culprit is None or culprit == i)
+            if failed:
+                r.error = str(err)
+                self.failed_runs += 1
+            if r.done_steps >= r.steps or failed:
                 r.finished = now
                 if self.on_finish:
                     self.on_finish(r, self.core, i, self.deck)
                 done.append(r)
+        if culprit is not None:
+            self._gc_now = True
         return done
 
 
@@ -343,6 +395,8 @@ def serve_packed(lib, requests: list[Request], budget_bytes: float, precision: i
             srv.waiting.append(pending[i])
             i += 1
         srv.maybe_repack(now)
+        finished += len(srv.rejected)
+        srv.rejected.clear()
         live = srv.active()
         if not live:
             if i < len(pending):
@@ -355,4 +409,9 @@ def serve_packed(lib, requests: list[Request], budget_bytes: float, precision: i
         srv.core.close()
     out = _summary(requests, clock(), work, srv.peak_bytes, srv.peak_active)
     out["repacks"] = srv.repacks
+    rs = np.array(srv.repack_s) if srv.repack_s else np.zeros(1)
+    out["repack_s_mean"] = float(rs.mean())
+    out["repack_s_max"] = float(rs.max())
+    out["repack_s_total"] = float(rs.sum())
+    out["failed_runs"] = srv.failed_runs
     return out

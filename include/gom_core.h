@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define GOM_ABI_VERSION 3
+#define GOM_ABI_VERSION 4
 
 typedef struct gom_ctx gom_ctx;
 
@@ -75,12 +75,24 @@ enum {
     GOM_ELM_NO_SUBELEMENT = 16    /* ELM_backtrace_v1.f90:463-467 (ELM transport) */
 };
 
+/* Kind of entity gom_status.entity indexes. */
+enum {
+    GOM_ENTITY_OTHER = 0,         /* a boundary index, a solver block, or none */
+    GOM_ENTITY_CELL = 1,
+    GOM_ENTITY_FACE = 2,
+    GOM_ENTITY_NODE = 3
+};
+
 typedef struct gom_status {
-    int32_t code;      /* gom_err of the first failure, 0 if none            */
-    int32_t site;      /* sub-site (GOM_ELM_*) or reference line of the stop */
-    int32_t entity;    /* 1-based face / cell / node index                   */
-    int32_t layer;     /* layer index, 0 if not applicable                    */
-    double value;      /* offending value where the reference prints one     */
+    int32_t code;        /* gom_err of the first failure, 0 if none            */
+    int32_t site;        /* sub-site (GOM_ELM_*) or reference line of the stop */
+    int32_t entity;      /* 1-based face / cell / node index                   */
+    int32_t layer;       /* layer index, 0 if not applicable                    */
+    double value;        /* offending value where the reference prints one     */
+    int32_t entity_kind; /* GOM_ENTITY_* of entity (no reference counterpart)  */
+    int32_t run;         /* packed context: 0-based run holding the entity, found from the
+                            run_*_start tables (0 in a single-run context); -1 when the entity is
+                            not a cell, face or node (no reference counterpart) */
 } gom_status;
 
 /* ------------------------------------------------------------------ sizes */
@@ -133,7 +145,9 @@ typedef struct gom_params {
     int32_t v_flux_limiter;    /* C7_1 */
     int32_t is_salt;           /* C7_2 is_tran(1) */
     int32_t is_temp;           /* C7_2 is_tran(2) */
-    int32_t heat_option;       /* C7_3 (only 2 supported when is_temp) */
+    int32_t heat_option;       /* C7_3: 1 per-layer source phi_sz, 2 surface term phi_sw (both
+                                  arrays come with gom_set_forcing; their heat-balance models stay
+                                  with the host) */
     int32_t test_barrier_phantom_blocks; /* tests only, normally 0: grid barriers of the PCG wait for
                                             this many blocks that do not exist, so their bounded wait
                                             runs out and the solve reports GOM_E_TIMEOUT */
@@ -223,6 +237,8 @@ typedef struct gom_forcing {
     const double *con_at_ob;           /* (n_ob, 2, Nt): con_at_ob(i,i3) per subcycle */
     const double *con_at_qb;           /* (n_qb, 2, Nt): con_at_Qb(i,i3) per subcycle */
     const double *phi_sw;              /* (N_c) surface heat term of heat_option 2   */
+    const double *phi_sz;              /* (L, N_c) heat source per layer of heat_option 1 and of the
+                                          ELM transport (phi_sz of heat_term_by_term.f90), W/m2 */
 } gom_forcing;
 
 /* ------------------------------------------------------------------ state fields
@@ -477,14 +493,19 @@ int gom_synchronize(struct gom_ctx *ctx);
  * n_cells must be <= 262144 (GOM_E_ARG otherwise).  Inputs and outputs are device pointers:
  * tri_or_quad (n_cells), adj_cellnum_at_cell (4, n_cells), sparsem (0:4, n_cells: diagonal then
  * the neighbour coefficients in local-face order, as solve_free_surface_equation.f90 builds them),
- * rhs (n_cells), x (n_cells, initial guess in, solution out).  Work is ordered on `stream`
- * (a cudaStream_t, NULL = legacy default stream).  With iterations != NULL the call waits and
- * returns the solve's status and iteration count; with NULL it returns after the launch.  All
- * calls share the array: calls that overlap on the GPU race.  The first call on a device does a
- * one-time set-up and should come before any stream capture. */
+ * rhs (n_cells), x (n_cells, initial guess in, solution out).  A row whose diagonal is not
+ * positive stops the solve with GOM_E_NOT_SPD.  Work is ordered on `stream` (a cudaStream_t,
+ * NULL = legacy default stream).  With iterations != NULL the call waits and returns the solve's
+ * status and iteration count; with NULL it returns after the launch.  device_result (may be NULL)
+ * is device memory for 2 int32 that receive, ordered on `stream`, the solve's status code and
+ * iteration count: the way an asynchronous caller learns of a failure (GOM_E_TIMEOUT, GOM_E_NOT_SPD)
+ * once it has synchronised `stream`.  All calls share the array: calls that overlap on the GPU race.
+ * The solve is a cooperative kernel that spins on grid barriers, so it must not overlap on the GPU
+ * with a context's free-surface phase either (order both on one stream, e.g. gom_stream(ctx)).  The
+ * first call on a device does a one-time set-up and should come before any stream capture. */
 int gom_pcg_solve_noalloc(int32_t n_cells, const int32_t *tri_or_quad, const int32_t *adj_cellnum_at_cell,
                           const double *sparsem, const double *rhs, double *x, int32_t max_iteration,
-                          double error_tolerance, void *stream, int32_t *iterations);
+                          double error_tolerance, void *stream, int32_t *iterations, int32_t *device_result);
 
 /* The CUDA stream (cudaStream_t) all device work of the context is ordered on, so a caller can
  * record events or order its own work against the core.  NULL for a CPU implementation. */

@@ -80,6 +80,7 @@ template <typename T> struct A2 {
 struct Err {
     int code = 0, site = 0, entity = 0, layer = 0;
     double value = 0;
+    int kind = 0;   // GOM_ENTITY_* of entity
 };
 
 }  // namespace
@@ -106,6 +107,7 @@ struct gom_ctx {
         g_boundary_type_of_face, g_isflowside3, g_ob_cell_id, g_qb_cell, g_qb_face;
     std::vector<int32_t> run_cell_start;   // packed runs: first cell of each run (0-based), n_runs + 1
     std::vector<int32_t> run_face_start;   // packed runs: first face of each run (0-based), n_runs + 1
+    std::vector<int32_t> run_node_start;   // packed runs: first node of each run (0-based), n_runs + 1
     // time-series stations (gom_set_stations): tser_hloc and the station cells or nodes
     int tser_hloc = 0;
     std::vector<int32_t> tser_station;
@@ -117,7 +119,7 @@ struct gom_ctx {
     // ---------------- forcing
     double elapsed_time = 0, spinup_tide = 1, spinup_baroclinic = 1;
     std::vector<double> eta_at_ob_old, eta_at_ob_new, q_add, wind_stress_normal, wind_stress_tangnt, gamma_t,
-        air_p, con_at_ob, con_at_qb, phi_sw;
+        air_p, con_at_ob, con_at_qb, phi_sw, phi_sz;
 
     // ---------------- accessors (geometry)
     A1<double> x_node, y_node, h_node, x_cell, y_cell, h_cell, area, x_face, y_face, h_face, face_length, delta_j,
@@ -187,7 +189,7 @@ int64_t field_count(const gom_dims &d, int f, int32_t *eb) {
     return n * (int64_t)(d.n_layers - s.lo + 1);
 }
 
-void set_err(gom_ctx *c, int code, int site, int entity, int layer, double value) {
+void set_err(gom_ctx *c, int code, int site, int entity, int layer, double value, int kind) {
     OMP_CRITICAL
     if (c->err.code == 0) {
         c->err.code = code;
@@ -195,6 +197,7 @@ void set_err(gom_ctx *c, int code, int site, int entity, int layer, double value
         c->err.entity = entity;
         c->err.layer = layer;
         c->err.value = value;
+        c->err.kind = kind;
     }
 }
 
@@ -856,9 +859,12 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
             return GOM_E_ARG;
         }
         copy_in(c->run_face_start, g->run_face_start, (size_t)d.n_runs + 1);
+        if (g->run_node_start) copy_in(c->run_node_start, g->run_node_start, (size_t)d.n_runs + 1);
+        else c->run_node_start = {0, d.n_nodes};
     } else {
         c->run_cell_start = {0, d.n_cells};
         c->run_face_start = {0, d.n_faces};
+        c->run_node_start = {0, d.n_nodes};
     }
 
     c->x_node.p = c->g_x_node.data();
@@ -923,6 +929,7 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
     c->con_at_ob.assign((size_t)d.n_ob * 2 * nt, 0.0);
     c->con_at_qb.assign((size_t)d.n_qb * 2 * nt, 0.0);
     c->phi_sw.assign(NC, 0.0);
+    c->phi_sz.assign((size_t)L * NC, 0.0);
     *out = c;
     return GOM_OK;
 }
@@ -989,6 +996,7 @@ int gom_set_forcing(gom_ctx *c, const gom_forcing *f) {
     up(c->con_at_ob, f->con_at_ob);
     up(c->con_at_qb, f->con_at_qb);
     up(c->phi_sw, f->phi_sw);
+    up(c->phi_sz, f->phi_sz);
     (void)nt;
     return GOM_OK;
 }
@@ -1050,6 +1058,19 @@ int gom_get_status(gom_ctx *c, gom_status *s, int clear) {
     s->entity = c->err.entity;
     s->layer = c->err.layer;
     s->value = c->err.value;
+    s->entity_kind = c->err.kind;
+    s->run = -1;
+    if (s->code != 0 && s->entity >= 1 && s->entity_kind >= GOM_ENTITY_CELL && s->entity_kind <= GOM_ENTITY_NODE) {
+        if (c->d.n_runs <= 1) {
+            s->run = 0;
+        } else {
+            const std::vector<int32_t> &v = s->entity_kind == GOM_ENTITY_CELL   ? c->run_cell_start
+                                            : s->entity_kind == GOM_ENTITY_FACE ? c->run_face_start
+                                                                                : c->run_node_start;
+            for (int r = 0; r + 1 < (int)v.size(); ++r)
+                if (s->entity - 1 >= v[r] && s->entity - 1 < v[r + 1]) s->run = r;
+        }
+    }
     if (clear) c->err = Err();
     return GOM_OK;
 }
@@ -1122,7 +1143,7 @@ int gom_step_boundary_velocity(gom_ctx *c) {
         int n1 = c->nodenum_at_face(1, j), n2 = c->nodenum_at_face(2, j);
         double temp_depth = c->h_face(j) + (eta_node(n1) + eta_node(n2)) * 0.5;
         if (temp_depth < c->p.dry_depth) {
-            set_err(c, GOM_E_DRY, 80, i, 0, temp_depth);
+            set_err(c, GOM_E_DRY, 80, i, 0, temp_depth, GOM_ENTITY_OTHER);
             return GOM_E_DRY;
         }
         Qu(i) = -c->q_add[i - 1] / (channel_width * temp_depth);
@@ -1236,7 +1257,7 @@ int gom_step_advection(gom_ctx *c) {
                 int ne = 0;
                 int e = elm_backtrace(c, bt_step, bt_dt, uuint, vvint, wwint, x0, y0, z0, nnel, jlev, ne);
                 if (e) {
-                    set_err(c, GOM_E_ELM, e, j, k, 0.0);
+                    set_err(c, GOM_E_ELM, e, j, k, 0.0, GOM_ENTITY_FACE);
                     rc = GOM_E_ELM;
                     break;
                 }
@@ -1438,7 +1459,7 @@ int gom_step_momentum(gom_ctx *c) {
             rhs[2 * nmax + k - 1] = dz_face(kk, j);
         }
         if (!tridiagonal_solver(nmax, nvl, 3, a, bd, cu, rhs, sol, gam)) {
-            set_err(c, GOM_E_ZERO_PIVOT, 587, j, 0, 0.0);
+            set_err(c, GOM_E_ZERO_PIVOT, 587, j, 0, 0.0, GOM_ENTITY_FACE);
             rc = GOM_E_ZERO_PIVOT;
             continue;
         }
@@ -1487,7 +1508,7 @@ int gom_step_free_surface(gom_ctx *c, int32_t *pcg_iters) {
                 s = gravity * (dt * dt) * (theta * theta) * c->face_length(j) / c->delta_j(j) * s;
                 s = s * c->cos_theta2(j);
                 if (s < 0.0) {
-                    set_err(c, GOM_E_NOT_SPD, 100, i, 0, s);
+                    set_err(c, GOM_E_NOT_SPD, 100, i, 0, s, GOM_ENTITY_CELL);
                     rc = GOM_E_NOT_SPD;
                     break;
                 }
@@ -1749,7 +1770,7 @@ int gom_step_layers(gom_ctx *c) {
                     break;
                 }
             if (tnew < b) {
-                set_err(c, GOM_E_LAYER, 66, i, tnew, eta_new(i));
+                set_err(c, GOM_E_LAYER, 66, i, tnew, eta_new(i), GOM_ENTITY_CELL);
                 return GOM_E_LAYER;
             }
             if (tnew == b) {
@@ -1782,7 +1803,7 @@ int gom_step_layers(gom_ctx *c) {
                     break;
                 }
             if (tnew < b) {
-                set_err(c, GOM_E_LAYER, 166, j, tnew, eta_max);
+                set_err(c, GOM_E_LAYER, 166, j, tnew, eta_max, GOM_ENTITY_FACE);
                 return GOM_E_LAYER;
             }
             if (tnew == b) {
@@ -1812,7 +1833,7 @@ int gom_step_layers(gom_ctx *c) {
                     break;
                 }
             if (tnew < b) {
-                set_err(c, GOM_E_LAYER, 224, i, tnew, eta_node(i));
+                set_err(c, GOM_E_LAYER, 224, i, tnew, eta_node(i), GOM_ENTITY_NODE);
                 return GOM_E_LAYER;
             }
             if (tnew == b) {
@@ -1834,26 +1855,26 @@ int gom_step_layers(gom_ctx *c) {
         }
         if (nsum1 == 0) top_el(i) = 0;
         if (nsum2 == 0 && top_el(i) != 0) {
-            set_err(c, GOM_E_DRY, 273, i, 0, 0.0);
+            set_err(c, GOM_E_DRY, 273, i, 0, 0.0, GOM_ENTITY_CELL);
             return GOM_E_DRY;
         }
     }
     for (int i = 1; i <= c->NC; ++i)
         for (int k = c->bottom_layer_at_element(i); k <= top_el(i) - 1; ++k)
             if (dzh_cn(k, i) < p.denominator_min_for_matrix) {
-                set_err(c, GOM_E_LAYER, 284, i, k, dzh_cn(k, i));
+                set_err(c, GOM_E_LAYER, 284, i, k, dzh_cn(k, i), GOM_ENTITY_CELL);
                 return GOM_E_LAYER;
             }
     for (int j = 1; j <= c->NF; ++j)
         for (int k = c->bottom_layer_at_face(j); k <= top_f(j) - 1; ++k)
             if (dzh_fn(k, j) < p.denominator_min_for_matrix) {
-                set_err(c, GOM_E_LAYER, 301, j, k, dzh_fn(k, j));
+                set_err(c, GOM_E_LAYER, 301, j, k, dzh_fn(k, j), GOM_ENTITY_FACE);
                 return GOM_E_LAYER;
             }
     for (int i = 1; i <= c->NN; ++i)
         for (int k = c->bottom_layer_at_node(i); k <= top_n(i) - 1; ++k)
             if (dzh_nn(k, i) < p.denominator_min_for_matrix) {
-                set_err(c, GOM_E_LAYER, 318, i, k, dzh_nn(k, i));
+                set_err(c, GOM_E_LAYER, 318, i, k, dzh_nn(k, i), GOM_ENTITY_NODE);
                 return GOM_E_LAYER;
             }
     return GOM_OK;
@@ -1942,8 +1963,7 @@ int gom_step_node_velocity(gom_ctx *c) {
 // salinity sums go to temperature and the temperature sums to salinity (:137-151); the top row's
 // upper coefficient is -dt + Kv/dzhalf (:188); no clamp; dry cells and dry nodes keep their
 // previous values; face values are the mean of the two node values in every layer.  The heat
-// source term of :120 is left out (phi_sz comes from the heat-balance module, not part of the
-// core).
+// source of :120 adds dt phi_sz / (rho_o cp dz) to every wet cell-layer (phi_sz from the host).
 static int transport_elm(gom_ctx *c) {
     const gom_params &p = c->p;
     const int L = c->L, NC = c->NC, NF = c->NF, NN = c->NN;
@@ -1997,13 +2017,15 @@ static int transport_elm(gom_ctx *c) {
                 double ttint = 0.0, ssint = 0.0;
                 if (!e) e = elm_tracer_at_foot(c, fin, nnel, jlev, ttint, ssint);
                 if (e) {
-                    set_err(c, GOM_E_ELM, e, i, k, 0.0);
+                    set_err(c, GOM_E_ELM, e, i, k, 0.0, GOM_ENTITY_CELL);
                     rc = GOM_E_ELM;
                     break;
                 }
                 AT(tc_bt, k, i) = ttint;
                 AT(sc_bt, k, i) = ssint;
             }
+            // :120 the per-layer heat source
+            AT(tc_bt, k, i) = AT(tc_bt, k, i) + dt * c->phi_sz[(size_t)(i - 1) * L + k - 1] / (p.rho_o * 4186.0 * dz_cell(k, i));
         }
     }
     if (rc.load() != GOM_OK) return rc.load();
@@ -2057,7 +2079,7 @@ static int transport_elm(gom_ctx *c) {
             rr[1 * nmax + k - 1] = dz_cell(kk, i) * AT(srhs, kk, i);
         }
         if (!tridiagonal_solver(nmax, nvl, 2, am, bm, cm, rr, sol, gm)) {
-            set_err(c, GOM_E_ZERO_PIVOT, 210, i, 0, 0.0);
+            set_err(c, GOM_E_ZERO_PIVOT, 210, i, 0, 0.0, GOM_ENTITY_CELL);
             rc = GOM_E_ZERO_PIVOT;
             continue;
         }
@@ -2171,6 +2193,10 @@ int gom_step_transport(gom_ctx *c) {
                 if (t > 0)
                     for (int k = 1; k <= L; ++k)
                         CC(k, i, i3) = CC(k, i, i3) + dt * c->phi_sw[i - 1] / (rho_o * cp * dz_cell(t, i));
+            } else if (tran_id[i3 - 1] == 2 && p.heat_option == 1) {
+                // :100-131 the per-layer source phi_sz over the wet layers
+                for (int k = c->bottom_layer_at_element(i); k <= top_el(i); ++k)
+                    CC(k, i, i3) = CC(k, i, i3) + dt * c->phi_sz[(size_t)(i - 1) * L + k - 1] / (rho_o * cp * dz_cell(k, i));
             }
         }
     }
@@ -2499,7 +2525,7 @@ int gom_step_transport(gom_ctx *c) {
                 }
             }
             if (!tridiagonal_solver(L, nvl, ntr, am, bm, cm, rhs, sol, gm)) {
-                set_err(c, GOM_E_ZERO_PIVOT, 1285, i, 0, 0.0);
+                set_err(c, GOM_E_ZERO_PIVOT, 1285, i, 0, 0.0, GOM_ENTITY_CELL);
                 rc = GOM_E_ZERO_PIVOT;
                 continue;
             }
@@ -2617,11 +2643,12 @@ int gom_step_density(gom_ctx *c) {
     A1<int32_t> top_n = FI1(c, GOM_F_TOP_LAYER_NODE), top_f = FI1(c, GOM_F_TOP_LAYER_FACE),
                 top_el = FI1(c, GOM_F_TOP_LAYER_CELL);
     const double c981 = F(9.81f), c1e5h = (double)(1.0e-5f * 0.5f), c1e5 = F(1.0e-5f);
-    auto column = [&](A2<double> rho, A2<double> tt, A2<double> ss, A2<double> dz, int e, int b, int t, int site) {
+    auto column = [&](A2<double> rho, A2<double> tt, A2<double> ss, A2<double> dz, int e, int b, int t, int site,
+                      int kind) {
         for (int k = b; k <= t; ++k) {
             double rtemp = tt(k, e), rsalt = ss(k, e);
             if (rtemp < tmin || rtemp > tmax || rsalt < smin || rsalt > smax) {
-                set_err(c, GOM_E_DENSITY, site, e, k, rtemp < tmin || rtemp > tmax ? rtemp : rsalt);
+                set_err(c, GOM_E_DENSITY, site, e, k, rtemp < tmin || rtemp > tmax ? rtemp : rsalt, kind);
                 return false;
             }
             if (p.ana_density == 1) {
@@ -2641,7 +2668,7 @@ int gom_step_density(gom_ctx *c) {
                 }
             }
             if (rho(k, e) < F(980.0f)) {
-                set_err(c, GOM_E_DENSITY, site, e, k, rho(k, e));
+                set_err(c, GOM_E_DENSITY, site, e, k, rho(k, e), kind);
                 return false;
             }
         }
@@ -2651,12 +2678,12 @@ int gom_step_density(gom_ctx *c) {
     };
     for (int i = 1; i <= c->NN; ++i)
         if (top_n(i) != 0)
-            if (!column(rho_node, temp_node, salt_node, dz_node, i, c->bottom_layer_at_node(i), top_n(i), 43))
+            if (!column(rho_node, temp_node, salt_node, dz_node, i, c->bottom_layer_at_node(i), top_n(i), 43, GOM_ENTITY_NODE))
                 return GOM_E_DENSITY;
     if (p.ana_density == 0)
         for (int j = 1; j <= c->NF; ++j)
             if (top_f(j) != 0)
-                if (!column(rho_face, temp_face, salt_face, dz_face, j, c->bottom_layer_at_face(j), top_f(j), 130))
+                if (!column(rho_face, temp_face, salt_face, dz_face, j, c->bottom_layer_at_face(j), top_f(j), 130, GOM_ENTITY_FACE))
                     return GOM_E_DENSITY;
     for (int i = 1; i <= c->NC; ++i) {
         int t = top_el(i), b = c->bottom_layer_at_element(i);
@@ -2672,7 +2699,7 @@ int gom_step_density(gom_ctx *c) {
                 }
             }
             if (icount == 0) {
-                set_err(c, GOM_E_DRY, 224, i, k, 0.0);
+                set_err(c, GOM_E_DRY, 224, i, k, 0.0, GOM_ENTITY_CELL);
                 return GOM_E_DRY;
             }
             rho_cell(k, i) = rho_cell(k, i) / icount;

@@ -419,3 +419,59 @@ def test_elm_transport_swaps_the_horizontal_sums(oracle_so):
     wet = wet.ravel()
     assert np.abs(t_new[wet] - 20.0).max() > 1e-6
     assert np.abs(s_new[wet] - st["salt_cell"][wet]).max() < 1e-9
+
+
+def test_heat_option1_source_heats_each_layer(oracle_so):
+    """heat_option 1 (solve_transport_equation_v19.f90:100-131) in a basin at rest with no
+    vertical diffusion: each wet layer warms by dt phi_sz / (rho_o cp dz) per step."""
+    import dataclasses
+    deck = tidal_basin(nx=8, ny=6, closed=True)
+    deck = dataclasses.replace(deck, params=dataclasses.replace(deck.params, heat_option=1, kv_0=0.0))
+    st = initial_state(deck)
+    c = GomCore(deck, lib_path=oracle_so)
+    prepare(c, st)
+    fr = HostForcing(deck)
+    L, nc = deck.n_layers, deck.n_cells
+    q = np.full((nc, L), 250.0)
+    steps = 4
+    for it in range(1, steps + 1):
+        f = fr.step(it)
+        f["phi_sz"] = q
+        c.set_forcing(f)
+        c.step_all()
+    t = c.get_field("temp_cell").reshape(nc, L)
+    dz = c.get_field("dz_cell").reshape(nc, L)
+    top = c.get_field("top_layer_cell")
+    bot = deck.geo["bottom_layer_at_element"]
+    p = deck.params
+    for i in range(nc):
+        for k in range(bot[i], top[i] + 1):
+            expect = 20.0 + steps * p.dt * 250.0 / (p.rho_o * 4186.0 * dz[i, k - 1])
+            assert abs(t[i, k - 1] - expect) < 1e-11, (i, k, t[i, k - 1], expect)
+
+
+def test_packed_status_names_the_failing_run(oracle_so):
+    """A packed context reports the first failing entity; gom_get_status maps it to the run that
+    holds it, so a server can retire that run alone.  The failure is made on the host: one run's
+    elevation is set above the highest level."""
+    from gom_release_gb300.ensemble import PackedForcing, pack, storm_run
+    runs = [storm_run(41, 300, 1.5, 10, max_layers=12), storm_run(42, 400, 2.0, 12, max_layers=12),
+            storm_run(43, 250, 1.0, 10, max_layers=12)]
+    pk = pack(runs)
+    c = GomCore(pk, lib_path=oracle_so)
+    prepare(c, initial_state(pk))
+    fp = PackedForcing(pk)
+    for it in range(1, 3):
+        c.set_forcing(fp.step(it))
+        c.step_all()
+    eta = c.get_field("eta_cell")
+    cs = pk.runs["run_cell_start"]
+    eta[cs[1]:cs[2]] = pk.z_level[-1] + 5.0
+    c.set_field("eta_cell", eta)
+    c.set_field("eta_cell_new", eta)
+    c.set_forcing(fp.step(3))
+    with pytest.raises(GomError) as info:
+        c.step_all()
+    st = info.value.status
+    assert st.code != 0 and st.entity_kind in (1, 2, 3)
+    assert st.run == 1, (st.code, st.site, st.entity, st.entity_kind, st.run)
