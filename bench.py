@@ -211,6 +211,15 @@ SOLVE_TRAFFIC_FULL = {
 }
 
 
+# FP64 instructions (DADD + DMUL + DFMA, ncu smsp__sass_thread_inst_executed_op_d{add,mul,fma}_pred_on.sum)
+# per active cell-layer and launch of the FP64 transport solve, from one ncu capture of the medium
+# estuary (349,122 active cell-layers; the count per cell-layer does not depend on the mesh size)
+SOLVE_FP64_INSTR_PER_CELL_LAYER = {
+    "k_tr_rows64_list + k_tr_thomas_col": 155.6 + 31.9,
+    "k_tr_solve": 186.5,
+}
+
+
 def solve_traffic(kernel: str, precision: str, size: str):
     """ncu DRAM bytes per launch of the transport solve for the full estuary, or None."""
     return SOLVE_TRAFFIC_FULL.get(f"{kernel} {precision}") if size == "full" else None
@@ -704,6 +713,19 @@ def main():
     list_solve = args.precision == "fp64" and tune is not None and tune[2] == 3
     solve_kernel = "k_tr_rows64_list + k_tr_thomas_col" if list_solve else "k_tr_solve"
     traffic = solve_traffic(solve_kernel, args.precision, args.size)
+    # FP64 roofline of the same launch: FP64 instructions per second against the measured issue
+    # peak (the library's FMA-chain kernel; an FMA is one instruction and two flops)
+    roof_fp64 = None
+    if args.precision == "fp64":
+        from gom_release_gb300.core import measure_fp64_peak
+        peak_gflops = measure_fp64_peak(lib)
+        instr = SOLVE_FP64_INSTR_PER_CELL_LAYER[solve_kernel] * ncl
+        ach = instr / (solve_ms * 1e-3) / 1e9
+        roof_fp64 = {"bound": "fp64", "kernel": solve_kernel, "achieved": ach, "peak": peak_gflops / 2.0,
+                     "unit": "G FP64 instructions/s", "frac": ach / (peak_gflops / 2.0),
+                     "instructions_per_cell_layer": SOLVE_FP64_INSTR_PER_CELL_LAYER[solve_kernel],
+                     "peak_fma_gflops": peak_gflops,
+                     "peak_source": "measured: gom_measure_fp64_peak (independent FMA chains, CUDA events)"}
     if args.no_phases:
         phases = {}
     else:
@@ -742,6 +764,7 @@ def main():
                      "phase_ms": {k: v * 1e3 for k, v in phases.items()},
                      "phase_algorithmic_gbs": {k: phase_bytes(deck, ncl, pcg_mean).get(k, 0) / v / 1e9
                                                for k, v in phases.items() if v > 0}},
+        "roofline_fp64": roof_fp64,
         "cpu_baseline": cpu,
         "e2e": {"value": ncl * ke * world / e2e_secs, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": 16 + 20, "wall_s": wall_e2e},

@@ -184,7 +184,17 @@ def _bind(lib: C.CDLL) -> C.CDLL:
     lib.gom_pcg_iterations_total.restype = C.c_int64
     lib.gom_stream.argtypes = [vp]
     lib.gom_stream.restype = vp
+    lib.gom_measure_fp64_peak.argtypes = [_D]
     return lib
+
+
+def measure_fp64_peak(lib: C.CDLL) -> float:
+    """FP64 FMA throughput of the current GPU (GFLOP/s), measured by the library."""
+    v = C.c_double()
+    rc = lib.gom_measure_fp64_peak(C.byref(v))
+    if rc != 0:
+        raise GomError(rc, "gom_measure_fp64_peak")
+    return v.value
 
 
 def load_library(path: str | os.PathLike) -> C.CDLL:

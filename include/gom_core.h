@@ -507,6 +507,12 @@ int gom_pcg_solve_noalloc(int32_t n_cells, const int32_t *tri_or_quad, const int
                           const double *sparsem, const double *rhs, double *x, int32_t max_iteration,
                           double error_tolerance, void *stream, int32_t *iterations, int32_t *device_result);
 
+/* FP64 arithmetic peak of the current GPU in GFLOP/s (no reference counterpart: the roofline of
+ * the plain FP64 path, whose kernels are bound by FP64 issue).  Times one kernel of independent
+ * FMA chains with CUDA events; allocates 8 bytes of device memory for the duration of the call.
+ * GOM_E_ARG from a CPU implementation. */
+int gom_measure_fp64_peak(double *gflops);
+
 /* The CUDA stream (cudaStream_t) all device work of the context is ordered on, so a caller can
  * record events or order its own work against the core.  NULL for a CPU implementation. */
 void *gom_stream(struct gom_ctx *ctx);

@@ -1077,6 +1077,12 @@ int gom_get_status(gom_ctx *c, gom_status *s, int clear) {
 
 int gom_synchronize(gom_ctx *c) { return c ? GOM_OK : GOM_E_ARG; }
 
+// a GPU measurement: nothing to measure on the CPU
+int gom_measure_fp64_peak(double *gflops) {
+    if (gflops) *gflops = 0.0;
+    return GOM_E_ARG;
+}
+
 int64_t gom_pcg_iterations_total(gom_ctx *c) { return c ? c->pcg_total : 0; }
 
 int64_t gom_device_bytes(const gom_ctx *) { return 0; }
