@@ -145,10 +145,20 @@ def _boundaries(geo, pairs):
 
 
 def _finish(name, raw, L, z_bottom, z_top, params, ob_pairs, q_pairs, q_portion, **kw) -> Deck:
-    g = build_geometry(raw, max_nb=12, voronoi=1)
+    z_level, _, _ = uniform_z_levels(z_bottom, z_top, L)
+    return _finish_levels(name, raw, z_level, params, ob_pairs, q_pairs, q_portion, **kw)
+
+
+def _finish_levels(name, raw, z_level, params, ob_pairs, q_pairs, q_portion, voronoi: int = 1, max_nb: int = 12,
+                   coriolis_on: bool = True, **kw) -> Deck:
+    """Geometry, vertical grid and boundaries of a deck whose level heights z_level(0:L) are given
+    (read_main_inp.f90 cards C2/C2_1, set_geometry_1.f90, set_geometry_2.f90)."""
+    g = build_geometry(raw, max_nb=max_nb, voronoi=voronoi)
     a = g.arrays
-    z_level, delta_z, dzmin = uniform_z_levels(z_bottom, z_top, L)
-    if np.any(np.abs(z_level - params.msl) < 1e-5):
+    L = len(z_level) - 1
+    delta_z = np.array([z_level[k] - z_level[k - 1] for k in range(1, L + 1)])
+    dzmin = float(delta_z.min())
+    if np.any(np.abs(z_level[1:] - params.msl) < 1e-5):
         raise ValueError("a z_level coincides with MSL (read_main_inp.f90 card C2_1)")
     params.delta_z_min = dzmin
     # read_main_inp.f90 card C5_03: min(dry_depth*(0.5-1.0e-4), delta_z_min*(0.5-1.e-4)),
@@ -179,7 +189,7 @@ def _finish(name, raw, L, z_bottom, z_top, params, ob_pairs, q_pairs, q_portion,
     )
     # calculate_coriolis_factor.f90:17-23 (option 1): omega is a default-REAL literal
     omega = f32(7.292e-5)
-    a["coriolis_factor"] = np.full(nf, 2 * omega * math.sin(params.coriolis_lat * DEG2RAD))
+    a["coriolis_factor"] = np.full(nf, 2 * omega * math.sin(params.coriolis_lat * DEG2RAD) if coriolis_on else 0.0)
     a["manning"] = np.full(nf, params.manning)
     a["bf_height"] = np.full(nf, params.bf_height)
     return Deck(name=name, geo=a, n_nodes=nn, n_cells=nc, n_faces=nf, n_layers=L, max_nb=g.max_nb,
