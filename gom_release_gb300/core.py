@@ -32,6 +32,7 @@ FIELDS = [
     "salt_face", "temp_face", "rho_cell", "rho_node", "rho_face", "num_sub_elm",
     "cdb", "gamma_b", "qu_boundary", "elm_foot", "elm_near_edge",
     "wind_stress_normal", "wind_stress_tangnt", "gamma_t", "air_p", "eta_at_ob_old", "eta_at_ob_new",
+    "q_add",
 ]
 
 _CELL_FIELDS = {"eta_cell", "eta_cell_new", "wn_cell", "wn_cell_new", "dz_cell", "dz_cell_new", "dzhalf_cell",
@@ -117,6 +118,21 @@ class GomStorm(C.Structure):
                                            "tide_amplitude", "tide_period", "tide_phase", "spinup", "t0")]
 
 
+class GomSeries(C.Structure):
+    _fields_ = [("n_series", C.c_int32), ("reserved", C.c_int32), ("start", _I), ("time", _D), ("value", _D)]
+
+
+class GomBoundarySeries(C.Structure):
+    _fields_ = [("julian_day", C.c_double), ("tide_spinup_period", C.c_double),
+                ("baroclinic_spinup_period", C.c_double), ("step", C.c_int32), ("reference_diff_days", C.c_int32),
+                ("tide_spinup", C.c_int32), ("baroclinic_spinup", C.c_int32), ("q_interp_method", C.c_int32),
+                ("n_harmonic", C.c_int32)] + \
+        [(n, _I) for n in ("ob_eta_type", "ob_harmonic_id", "ob_eta_id", "ob_salt_id", "ob_temp_id", "qb_q_id",
+                           "qb_salt_id", "qb_temp_id")] + [("qb_portion", _D), ("harmonic_start", _I)] + \
+        [(n, _D) for n in ("amplitude", "period_h", "nodal", "eq_arg", "phase", "phase_shift")] + \
+        [(n, GomSeries) for n in ("eta", "q", "salt", "temp")]
+
+
 class GomStatus(C.Structure):
     _fields_ = [("code", C.c_int32), ("site", C.c_int32), ("entity", C.c_int32), ("layer", C.c_int32),
                 ("value", C.c_double), ("entity_kind", C.c_int32), ("run", C.c_int32)]
@@ -164,6 +180,7 @@ def _bind(lib: C.CDLL) -> C.CDLL:
     lib.gom_set_stations.argtypes = [vp, C.c_int32, C.c_int32, _I, _I]
     lib.gom_station_series.argtypes = [vp, _D]
     lib.gom_set_storms.argtypes = [vp, C.c_int32, C.POINTER(GomStorm), C.c_double]
+    lib.gom_set_boundary_series.argtypes = [vp, C.POINTER(GomBoundarySeries)]
     lib.gom_cold_start.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_double]
     lib.gom_autotune.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32)]
     lib.gom_tuning_variants.argtypes = [C.POINTER(C.c_int32)]
@@ -415,6 +432,38 @@ class GomCore:
         arr = (GomStorm * len(storms))(*[GomStorm(*[float(getattr(s, n, 0.0)) for n, _ in GomStorm._fields_])
                                          for s in storms])
         self._check(self.lib.gom_set_storms(self.ctx, len(storms), arr, float(elapsed_time)), "set_storms")
+
+    def set_boundary_series(self, bs) -> None:
+        """Hold a ``series.BoundarySeries`` on the device: every later ``step_all`` /
+        ``step_launch`` advances the clock and forms the boundary forcing from it first."""
+        keep = []
+
+        def ints(a):
+            a = np.ascontiguousarray(np.asarray(a, dtype=np.int32))
+            keep.append(a)
+            return a.ctypes.data_as(_I)
+
+        def dbls(a):
+            a = np.ascontiguousarray(np.asarray(a, dtype=np.float64))
+            keep.append(a)
+            return a.ctypes.data_as(_D)
+
+        sets = {}
+        for kind in ("eta", "q", "salt", "temp"):
+            start, t, v = bs.flat(kind)
+            sets[kind] = GomSeries(len(start) - 1, 0, ints(start), dbls(t), dbls(v))
+        hs, amp, per, nod, eq, ph, shift = bs.flat_harmonics()
+        arg = GomBoundarySeries(
+            julian_day=float(bs.julian_day), tide_spinup_period=float(bs.tide_spinup_period),
+            baroclinic_spinup_period=float(bs.baroclinic_spinup_period), step=int(bs.step),
+            reference_diff_days=int(bs.reference_diff_days), tide_spinup=int(bs.tide_spinup),
+            baroclinic_spinup=int(bs.baroclinic_spinup), q_interp_method=int(bs.q_interp_method),
+            n_harmonic=len(hs) - 1, ob_eta_type=ints(bs.ob_eta_type), ob_harmonic_id=ints(bs.ob_harmonic_id),
+            ob_eta_id=ints(bs.ob_eta_id), ob_salt_id=ints(bs.ob_salt_id), ob_temp_id=ints(bs.ob_temp_id),
+            qb_q_id=ints(bs.qb_q_id), qb_salt_id=ints(bs.qb_salt_id), qb_temp_id=ints(bs.qb_temp_id),
+            qb_portion=dbls(bs.qb_portion), harmonic_start=ints(hs), amplitude=dbls(amp), period_h=dbls(per),
+            nodal=dbls(nod), eq_arg=dbls(eq), phase=dbls(ph), phase_shift=dbls(shift), **sets)
+        self._check(self.lib.gom_set_boundary_series(self.ctx, C.byref(arg)), "set_boundary_series")
 
     def conservation(self) -> tuple[float, float]:
         v = C.c_double()

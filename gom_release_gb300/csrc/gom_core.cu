@@ -66,6 +66,11 @@ struct gom_ctx {
     // device-side storm forcing (gom_set_storms)
     double *d_storms = nullptr, *storm_wu = nullptr, *storm_wv = nullptr;
     int n_storms = 0;
+    // device-side boundary series (gom_set_boundary_series): their own device allocations
+    SeriesDev series{};
+    bool has_series = false;
+    std::vector<void *> series_allocs;
+    size_t series_bytes = 0;
     // asynchronous output snapshots (gom_snapshot_begin): device staging area, copy stream
     char *snap_dev = nullptr;
     size_t snap_cap = 0;
@@ -235,9 +240,10 @@ template <typename R> void describe_fields(gom_ctx *c, StateT<R> &s) {
     E(GOM_F_AIR_P, &c->f_air_p, -1, 2);
     E(GOM_F_ETA_AT_OB_OLD, &c->f_eta_old, -1, 4);
     E(GOM_F_ETA_AT_OB_NEW, &c->f_eta_new, -1, 4);
+    E(GOM_F_Q_ADD, &c->f_q_add, -1, 3);
 }
 
-bool is_forcing_field(int f) { return f >= GOM_F_WIND_STRESS_NORMAL && f <= GOM_F_ETA_AT_OB_NEW; }
+bool is_forcing_field(int f) { return f >= GOM_F_WIND_STRESS_NORMAL && f <= GOM_F_Q_ADD; }
 
 // state arrays that update_variables.f90:16-31 copies from *_new to the old name
 const int kSwapPairs[][2] = {{GOM_F_ETA_CELL, GOM_F_ETA_CELL_NEW},   {GOM_F_WN_CELL, GOM_F_WN_CELL_NEW},
@@ -263,6 +269,7 @@ cudaError_t enqueue_swap(gom_ctx *c) {
 template <typename R> cudaError_t enqueue_step_t(gom_ctx *c, const LaunchT<R> &x, int part) {
     cudaError_t e;
     if (part <= 0) {
+        if (c->has_series && (e = launch_series_forcing(x.g, x.f, x.p, c->series, x.s.eta_cell, x.status, x.stream))) return e;
         if (c->n_storms > 0 &&
             (e = launch_storm_forcing(x.g, x.f, x.p, x.stream, c->d_storms, c->storm_wu, c->storm_wv)))
             return e;
@@ -580,9 +587,10 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
     if (e == cudaSuccess) e = dalloc(c, &c->f_con_qb, (size_t)d.n_qb * 2 * nt);
     if (e == cudaSuccess) e = dalloc(c, &c->f_phi_sw, NC);
     if (e == cudaSuccess) e = dalloc(c, &c->f_phi_sz, L * NC);
-    if (e == cudaSuccess) e = dalloc(c, &c->f_scal, 4);
+    // [elapsed_time, spinup_tide, spinup_baroclinic, -, julian_day, it, -, -]
+    if (e == cudaSuccess) e = dalloc(c, &c->f_scal, 8);
     if (e == cudaSuccess) {
-        const double one[4] = {0.0, 1.0, 1.0, 0.0};
+        const double one[8] = {0.0, 1.0, 1.0, 0.0, 0.0, 0.0, 0.0, 0.0};
         e = cudaMemcpy(c->f_scal, one, sizeof(one), cudaMemcpyHostToDevice);
     }
     Forcing &F = c->x.f;
@@ -777,6 +785,7 @@ void gom_destroy(gom_ctx *c) {
     if (c->ev_to_solver) cudaEventDestroy(c->ev_to_solver);
     if (c->ev_from_solver) cudaEventDestroy(c->ev_from_solver);
     for (void *p : c->allocs) cudaFree(p);
+    for (void *p : c->series_allocs) cudaFree(p);
     if (c->h_status) cudaFreeHost(c->h_status);
     if (c->h_iters) cudaFreeHost(c->h_iters);
     if (c->h_cons) cudaFreeHost(c->h_cons);
@@ -1203,7 +1212,7 @@ int gom_copy_run(gom_ctx *dst, int32_t dst_run, gom_ctx *src, int32_t src_run) {
 }
 
 int gom_set_storms(gom_ctx *c, int32_t n_storms, const gom_storm *storms, double elapsed_time) {
-    if (!c || !storms || n_storms != c->x.g.NR) return GOM_E_ARG;
+    if (!c || !storms || n_storms != c->x.g.NR || c->has_series) return GOM_E_ARG;
     static_assert(sizeof(gom_storm) == 13 * sizeof(double), "gom_storm is 13 doubles");
     for (int r = 0; r < n_storms; ++r) {
         const gom_storm &s = storms[r];
@@ -1222,6 +1231,126 @@ int gom_set_storms(gom_ctx *c, int32_t n_storms, const gom_storm *storms, double
     c->n_storms = n_storms;
     // the captured step gains the forcing kernels: capture again on the next launch
     drop_graphs(c);
+    return GOM_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+template <typename T> cudaError_t series_upload(gom_ctx *c, const T **dst, const T *src, size_t n) {
+    T *p = nullptr;
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc((void **)&p, n * sizeof(T));
+    if (e != cudaSuccess) return e;
+    c->series_allocs.push_back(p);
+    c->series_bytes += n * sizeof(T);
+    e = src ? cudaMemcpy(p, src, n * sizeof(T), cudaMemcpyHostToDevice) : cudaMemset(p, 0, n * sizeof(T));
+    *dst = p;
+    return e;
+}
+
+void series_free(gom_ctx *c) {
+    for (void *p : c->series_allocs) cudaFree(p);
+    c->series_allocs.clear();
+    c->bytes -= c->series_bytes;
+    c->series_bytes = 0;
+    c->has_series = false;
+}
+
+// a series set is usable: offsets start at 0 and grow, times never decrease within a series
+bool series_ok(const gom_series &s) {
+    if (s.n_series < 0) return false;
+    if (s.n_series == 0) return true;
+    if (!s.start || !s.time || !s.value || s.start[0] != 0) return false;
+    for (int k = 0; k < s.n_series; ++k) {
+        if (s.start[k + 1] < s.start[k]) return false;
+        for (int q = s.start[k] + 1; q < s.start[k + 1]; ++q)
+            if (!(s.time[q] >= s.time[q - 1])) return false;
+    }
+    return true;
+}
+
+bool ids_ok(const int32_t *ids, int n, int n_series) {
+    if (n > 0 && !ids) return false;
+    for (int i = 0; i < n; ++i)
+        if (ids[i] < 0 || ids[i] > n_series) return false;
+    return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gom_set_boundary_series(gom_ctx *c, const gom_boundary_series *bs) {
+    if (!c || !bs || c->n_storms > 0 || c->d.n_runs > 1) return GOM_E_ARG;
+    const int nob = c->d.n_ob, nqb = c->d.n_qb;
+    const gom_series *sets[4] = {&bs->eta, &bs->q, &bs->salt, &bs->temp};
+    for (const gom_series *sr : sets)
+        if (!series_ok(*sr)) return GOM_E_ARG;
+    if (bs->n_harmonic < 0 || (bs->n_harmonic > 0 && (!bs->harmonic_start || !bs->amplitude || !bs->period_h ||
+                                                       !bs->nodal || !bs->eq_arg || !bs->phase || !bs->phase_shift)))
+        return GOM_E_ARG;
+    if (bs->n_harmonic > 0 && bs->harmonic_start[0] != 0) return GOM_E_ARG;
+    for (int k = 0; k < bs->n_harmonic; ++k)
+        if (bs->harmonic_start[k + 1] < bs->harmonic_start[k]) return GOM_E_ARG;
+    if (nob > 0 && !bs->ob_eta_type) return GOM_E_ARG;
+    for (int i = 0; i < nob; ++i)
+        if (bs->ob_eta_type[i] < -1 || bs->ob_eta_type[i] > 3) return GOM_E_ARG;   // read_main_inp.f90:460-464
+    if (!ids_ok(bs->ob_harmonic_id, nob, bs->n_harmonic) || !ids_ok(bs->ob_eta_id, nob, bs->eta.n_series) ||
+        !ids_ok(bs->ob_salt_id, nob, bs->salt.n_series) || !ids_ok(bs->ob_temp_id, nob, bs->temp.n_series) ||
+        !ids_ok(bs->qb_q_id, nqb, bs->q.n_series) || !ids_ok(bs->qb_salt_id, nqb, bs->salt.n_series) ||
+        !ids_ok(bs->qb_temp_id, nqb, bs->temp.n_series) || (nqb > 0 && !bs->qb_portion))
+        return GOM_E_ARG;
+    if (bs->q_interp_method != 1 && bs->q_interp_method != 2) return GOM_E_ARG;
+    CK(cudaStreamSynchronize(c->x.stream));
+    series_free(c);
+    SeriesDev &S = c->series;
+    S = SeriesDev{};
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < 4 && e == cudaSuccess; ++k) {
+        const gom_series &sr = *sets[k];
+        S.n[k] = sr.n_series;
+        const size_t len = sr.n_series > 0 ? (size_t)sr.start[sr.n_series] : 0;
+        e = series_upload(c, &S.start[k], sr.n_series > 0 ? sr.start : nullptr, (size_t)sr.n_series + 1);
+        if (e == cudaSuccess) e = series_upload(c, &S.time[k], sr.n_series > 0 ? sr.time : nullptr, len);
+        if (e == cudaSuccess) e = series_upload(c, &S.value[k], sr.n_series > 0 ? sr.value : nullptr, len);
+    }
+    if (e == cudaSuccess) e = series_upload(c, &S.ob_type, bs->ob_eta_type, (size_t)nob);
+    if (e == cudaSuccess) e = series_upload(c, &S.ob_h, bs->ob_harmonic_id, (size_t)nob);
+    if (e == cudaSuccess) e = series_upload(c, &S.ob_eta, bs->ob_eta_id, (size_t)nob);
+    if (e == cudaSuccess) e = series_upload(c, &S.ob_salt, bs->ob_salt_id, (size_t)nob);
+    if (e == cudaSuccess) e = series_upload(c, &S.ob_temp, bs->ob_temp_id, (size_t)nob);
+    if (e == cudaSuccess) e = series_upload(c, &S.qb_q, bs->qb_q_id, (size_t)nqb);
+    if (e == cudaSuccess) e = series_upload(c, &S.qb_salt, bs->qb_salt_id, (size_t)nqb);
+    if (e == cudaSuccess) e = series_upload(c, &S.qb_temp, bs->qb_temp_id, (size_t)nqb);
+    if (e == cudaSuccess) e = series_upload(c, &S.qb_portion, bs->qb_portion, (size_t)nqb);
+    const int nh = bs->n_harmonic;
+    const size_t nc = nh > 0 ? (size_t)bs->harmonic_start[nh] : 0;
+    S.n_harm = nh;
+    if (e == cudaSuccess) e = series_upload(c, &S.h_start, nh > 0 ? bs->harmonic_start : nullptr, (size_t)nh + 1);
+    if (e == cudaSuccess) e = series_upload(c, &S.amp, nh > 0 ? bs->amplitude : nullptr, nc);
+    if (e == cudaSuccess) e = series_upload(c, &S.per_h, nh > 0 ? bs->period_h : nullptr, nc);
+    if (e == cudaSuccess) e = series_upload(c, &S.nodal, nh > 0 ? bs->nodal : nullptr, nc);
+    if (e == cudaSuccess) e = series_upload(c, &S.eq, nh > 0 ? bs->eq_arg : nullptr, nc);
+    if (e == cudaSuccess) e = series_upload(c, &S.ph, nh > 0 ? bs->phase : nullptr, nc);
+    if (e == cudaSuccess) e = series_upload(c, &S.shift, nh > 0 ? bs->phase_shift : nullptr, (size_t)nh);
+    if (e != cudaSuccess) {
+        series_free(c);
+        return set_cuda_error(c, e, "gom_set_boundary_series");
+    }
+    c->bytes += c->series_bytes;
+    // reference_diff_days * 86400.0: an integer times a default-REAL constant, in single precision
+    S.rdd_s = (double)((float)bs->reference_diff_days * 86400.0f);
+    S.tide_per_s = bs->tide_spinup == 1 ? bs->tide_spinup_period * 86400.0 : 0.0;
+    S.bc_per_s = (bs->baroclinic_spinup == 1 && c->hp.baroclinic_flag == 1) ? bs->baroclinic_spinup_period * 86400.0
+                                                                                : 0.0;
+    S.q_method = bs->q_interp_method;
+    // the device clock: elapsed time and spin-up of the last step, its julian day and step number
+    const double scal[8] = {bs->step * c->hp.dt, 1.0, 1.0, 0.0, bs->julian_day, (double)bs->step, 0.0, 0.0};
+    CK(cudaMemcpy(c->f_scal, scal, sizeof(scal), cudaMemcpyHostToDevice));
+    c->has_series = true;
+    drop_graphs(c);   // the captured step gains the series kernels
     return GOM_OK;
 }
 

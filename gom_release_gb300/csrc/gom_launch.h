@@ -122,6 +122,29 @@ cudaError_t launch_cold_start(const LaunchT<R> &x, double salt, double temp, dou
 cudaError_t launch_storm_forcing(const Geom &g, const Forcing &f, const Params &p, cudaStream_t stream,
                                  const double *storms, double *wu, double *wv);
 
+// device copies of a gom_boundary_series (k_forcing.cu evaluates them at the start of every step)
+struct SeriesDev {
+    int n[4];                              // series per kind: 0 eta, 1 Q, 2 salinity, 3 temperature
+    const int *start[4];                   // (n + 1) offsets per kind
+    const double *time[4], *value[4];
+    const int *ob_type, *ob_h, *ob_eta, *ob_salt, *ob_temp;   // (NOB)
+    const int *qb_q, *qb_salt, *qb_temp;                      // (NQB)
+    const double *qb_portion;                                 // (NQB)
+    int n_harm;
+    const int *h_start;                    // (n_harm + 1)
+    const double *amp, *per_h, *nodal, *eq, *ph, *shift;
+    double rdd_s;                          // reference_diff_days x 86400.0 (single precision, widened)
+    double tide_per_s, bc_per_s;           // spin-up periods in seconds, 0 = no ramp
+    int q_method;
+};
+
+// per-step boundary forcing from the series (k_forcing.cu): advances the device clock in f.scal
+// ([0] elapsed_time, [1] spin-up tide, [2] spin-up baroclinic, [4] julian_day, [5] it), then
+// writes eta_at_ob_old/new (type -1 from eta_cell; an isolated cell records GOM_E_ARG in
+// status), q_add and the boundary concentrations of every subcycle
+cudaError_t launch_series_forcing(const Geom &g, const Forcing &f, const Params &p, const SeriesDev &s,
+                                  const double *eta_cell, gom_status *status, cudaStream_t stream);
+
 // explicit instantiations live in the kernel files
 #define GOM_INSTANTIATE_LAUNCH(fn)                              \
     template cudaError_t fn<double>(const LaunchT<double> &x); \

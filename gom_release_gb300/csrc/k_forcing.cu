@@ -124,6 +124,174 @@ __global__ void k_storm_ob(Geom g, const double *scal, const double *storms, dou
     eta_new[i] = ob_elevation(s, t, x, y, rho_g);
 }
 
+// ---------------------------------------------------------------------------- boundary series
+// The value of series id (1-based) of one kind at model time u2: the first interval of the
+// reference's search (compute_boundary_eta.f90:100-111, calculate_Q.f90:30-41,
+// solve_transport_equation_v19.f90:245-257) with u1 <= u2 <= u3 on times minus reference_diff_days,
+// found by bisection (series times never decrease, checked when they are set), and
+// v2 = (u2 - u1)(v3 - v1)/(u3 - u1) + v1.  False when no interval holds u2.
+__device__ bool series_at(const SeriesDev &S, int kind, int id, double u2, double &v) {
+    if (id < 1 || id > S.n[kind]) return false;
+    const int s0 = S.start[kind][id - 1], n = S.start[kind][id] - s0;
+    const double *t = S.time[kind] + s0, *val = S.value[kind] + s0;
+    if (n < 2) return false;
+    int lo = 0, hi = n;   // first index with t - rdd >= u2
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (t[mid] - S.rdd_s >= u2) hi = mid;
+        else lo = mid + 1;
+    }
+    int k;
+    if (lo == 0) {
+        if (!(t[0] - S.rdd_s == u2)) return false;
+        k = 1;
+    } else if (lo >= n) {
+        return false;
+    } else {
+        k = lo;
+    }
+    const double u1 = t[k - 1] - S.rdd_s, u3 = t[k] - S.rdd_s;
+    v = (u2 - u1) * (val[k] - val[k - 1]) / (u3 - u1) + val[k - 1];
+    return true;
+}
+
+// setup_spinup.f90:12-31 and main.f90:54-56 (elapsed_time = it dt, julian_day += dt / 86400)
+__global__ void k_series_clock(double *scal, double dt, double tide_per, double bc_per) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const double it = scal[5] + 1.0;
+    const double elapsed = it * dt;
+    scal[5] = it;
+    scal[0] = elapsed;
+    scal[4] = scal[4] + dt / 86400.0;
+    scal[1] = (tide_per > 0.0 && elapsed < tide_per) ? tanh(2.0 * elapsed / tide_per) : 1.0;
+    scal[2] = (bc_per > 0.0 && elapsed < bc_per) ? tanh(2.0 * elapsed / bc_per) : 1.0;
+}
+
+// compute_boundary_eta.f90:45-124 (types 1 and 2) and the open-boundary concentrations of every
+// subcycle (solve_transport_equation_v19.f90:229-282); one thread per open-boundary cell
+__global__ void k_series_ob(Geom g, Forcing f, Params p, SeriesDev S, const double *eta_cell, gom_status *st,
+                            int ntr_salt, int ntr_temp, int nt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.NOB) return;
+    const double elapsed = f.scal[0], spin = f.scal[1], spin_bc = f.scal[2], jd_s = f.scal[4] * 86400.0;
+    const double dt = p.dt;
+    double *eta_old = const_cast<double *>(f.eta_at_ob_old), *eta_new = const_cast<double *>(f.eta_at_ob_new);
+    const int type = S.ob_type[i];
+    if (type == -1) {
+        // compute_boundary_eta.f90:45-70: the mean elevation of the interior cells around the
+        // open-boundary cell's nodes (each counted once per node it shares), old level only;
+        // the elevations are those the step starts from (nothing before this phase changes them)
+        const int cell = g.ob_cell_id[i];
+        double sum0 = 0.0;
+        int icount = 0;
+        for (int l = 1; l <= g.tri_or_quad[cell - 1]; ++l) {
+            const int nd = g.cell_node(l, cell);
+            for (int i2 = 1; i2 <= g.adj_cells_at_node[nd - 1]; ++i2) {
+                const int ie = g.node_cell(i2, nd);
+                if (g.ob_element_flag[ie - 1] == 0) {
+                    icount = icount + 1;
+                    sum0 = sum0 + eta_cell[ie - 1];
+                }
+            }
+        }
+        if (icount == 0) record_error(st, GOM_E_ARG, 0, i + 1, 0, 0.0, GOM_ENTITY_OTHER);   // an isolated cell
+        else eta_old[i] = sum0 / icount;
+    } else if (type == 1) {
+        const double deg2rad = 3.141592653589793 / 180.0;
+        const int h = S.ob_h[i];
+        double o = 0.0, nw = 0.0;
+        if (h >= 1 && h <= S.n_harm) {
+            for (int j = S.h_start[h - 1]; j < S.h_start[h]; ++j) {
+                const double w = 2.0 * 3.141592653589793 / (S.per_h[j] * 3600.0);
+                const double a = spin * S.amp[j] * S.nodal[j];
+                o = o + a * cos(w * (elapsed - dt) + S.eq[j] * deg2rad - S.ph[j] * deg2rad - S.shift[h - 1] * deg2rad);
+                nw = nw + a * cos(w * elapsed + S.eq[j] * deg2rad - S.ph[j] * deg2rad - S.shift[h - 1] * deg2rad);
+            }
+        }
+        eta_old[i] = o;
+        eta_new[i] = nw;
+    } else if (type == 2) {
+        double v;
+        if (series_at(S, 0, S.ob_eta[i], jd_s - dt, v)) eta_old[i] = spin * v;
+        if (series_at(S, 0, S.ob_eta[i], jd_s, v)) eta_new[i] = spin * v;
+    }
+    double *con = const_cast<double *>(f.con_at_ob);
+    const double dt2 = dt / nt;
+    for (int sub = 0; sub < nt; ++sub) {
+        const double u2 = (jd_s - dt) + (sub + 1) * dt2;
+        double v;
+        if (ntr_salt) {
+            double *c = con + ((long)sub * 2 + 0) * g.NOB + i;
+            if (S.ob_salt[i] <= 0) *c = 0.0;
+            else if (series_at(S, 2, S.ob_salt[i], u2, v)) *c = spin_bc * v;
+        }
+        if (ntr_temp) {
+            double *c = con + ((long)sub * 2 + 1) * g.NOB + i;
+            if (S.ob_temp[i] <= 0) *c = 0.0;
+            else if (series_at(S, 3, S.ob_temp[i], u2, v)) *c = spin_bc * v;
+        }
+    }
+}
+
+// calculate_Q.f90:47-75, second-order Lagrange through three samples (raw series times)
+__device__ double q_lagrange(const SeriesDev &S, int id, double u2) {
+    const int s0 = S.start[1][id - 1], n = S.start[1][id] - s0;
+    const double *t = S.time[1] + s0, *val = S.value[1] + s0;
+    int min_index = 0;
+    double best = 0.0;
+    for (int k = 0; k < n; ++k) {
+        const double d = t[k] - u2;
+        if (d >= 0.0 && (min_index == 0 || d < best)) {
+            best = d;
+            min_index = k + 1;
+        }
+    }
+    if (min_index == 0) min_index = n;
+    if (min_index == 1) min_index = min_index + 1;
+    min_index = min_index - 1;
+    const int shift = (min_index + 2) - n;
+    if (shift > 0) min_index = min_index - shift;
+    if (min_index < 1) min_index = 1;
+    double total = 0.0;
+    for (int ii = 0; ii <= 2; ++ii) {
+        double prod = val[min_index - 1 + ii];
+        for (int jj = 0; jj <= 2; ++jj)
+            if (jj != ii) prod = prod * (u2 - t[min_index - 1 + jj]) / (t[min_index - 1 + ii] - t[min_index - 1 + jj]);
+        total = total + prod;
+    }
+    return total;
+}
+
+// calculate_Q.f90:21-75 and the river concentrations (solve_transport_equation_v19.f90:326-382)
+__global__ void k_series_qb(Geom g, Forcing f, Params p, SeriesDev S, int ntr_salt, int ntr_temp, int nt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.NQB) return;
+    const double spin_bc = f.scal[2], jd_s = f.scal[4] * 86400.0, dt = p.dt;
+    double *q = const_cast<double *>(f.q_add);
+    const int qid = S.qb_q[i];
+    if (qid >= 1 && qid <= S.n[1]) {
+        double v;
+        if (S.q_method == 2) q[i] = q_lagrange(S, qid, jd_s) * S.qb_portion[i];
+        else if (series_at(S, 1, qid, jd_s, v)) q[i] = v * S.qb_portion[i];
+    }
+    double *con = const_cast<double *>(f.con_at_qb);
+    const double dt2 = dt / nt;
+    for (int sub = 0; sub < nt; ++sub) {
+        const double u2 = (jd_s - dt) + (sub + 1) * dt2;
+        double v;
+        if (ntr_salt) {
+            double *c = con + ((long)sub * 2 + 0) * g.NQB + i;
+            if (S.qb_salt[i] <= 0) *c = 0.0;
+            else if (series_at(S, 2, S.qb_salt[i], u2, v)) *c = spin_bc * v;
+        }
+        if (ntr_temp) {
+            double *c = con + ((long)sub * 2 + 1) * g.NQB + i;
+            if (S.qb_temp[i] <= 0) *c = 0.0;
+            else if (series_at(S, 3, S.qb_temp[i], u2, v)) *c = spin_bc * v;
+        }
+    }
+}
+
 }  // namespace
 
 cudaError_t launch_storm_forcing(const Geom &g, const Forcing &f, const Params &p, cudaStream_t stream,
@@ -138,6 +306,16 @@ cudaError_t launch_storm_forcing(const Geom &g, const Forcing &f, const Params &
         k_storm_ob<<<blocks_for(g.NOB, 128), 128, 0, stream>>>(g, scal, storms, p.rho_o * p.gravity, p.dt,
                                                                 const_cast<double *>(f.eta_at_ob_old),
                                                                 const_cast<double *>(f.eta_at_ob_new));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_series_forcing(const Geom &g, const Forcing &f, const Params &p, const SeriesDev &s,
+                                  const double *eta_cell, gom_status *status, cudaStream_t stream) {
+    k_series_clock<<<1, 32, 0, stream>>>(const_cast<double *>(f.scal), p.dt, s.tide_per_s, s.bc_per_s);
+    const int nt = p.trans_sub_iter > 0 ? p.trans_sub_iter : 1;
+    const int salt = p.transport_flag && p.is_salt, temp = p.transport_flag && p.is_temp;
+    if (g.NOB > 0) k_series_ob<<<blocks_for(g.NOB, 128), 128, 0, stream>>>(g, f, p, s, eta_cell, status, salt, temp, nt);
+    if (g.NQB > 0) k_series_qb<<<blocks_for(g.NQB, 128), 128, 0, stream>>>(g, f, p, s, salt, temp, nt);
     return cudaGetLastError();
 }
 

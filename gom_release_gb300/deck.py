@@ -463,7 +463,8 @@ class HostForcing:
         return math.tanh(2.0 * elapsed / period)
 
     def eta_ob(self, elapsed, spin):
-        """compute_boundary_eta.f90:72-90 (ob_eta_type 1, harmonic)."""
+        """compute_boundary_eta.f90:72-90 (ob_eta_type 1, harmonic), in the reference's order of
+        operations: ((spin amp) nodal) cos(((w t + eq) - phase) - shift)."""
         d = self.deck
         if d.n_ob == 0:
             return np.zeros(0), np.zeros(0)
@@ -473,9 +474,10 @@ class HostForcing:
         new = 0.0
         for j in range(len(tide["amplitude"])):
             w = 2.0 * PI / (tide["period_h"][j] * 3600.0)
-            phase = tide["eq_arg"][j] * DEG2RAD - tide["phase"][j] * DEG2RAD - tide["shift"] * DEG2RAD
-            old = old + spin * tide["amplitude"][j] * tide["nodal"][j] * math.cos(w * (elapsed - dt) + phase)
-            new = new + spin * tide["amplitude"][j] * tide["nodal"][j] * math.cos(w * elapsed + phase)
+            eq, ph, sh = tide["eq_arg"][j] * DEG2RAD, tide["phase"][j] * DEG2RAD, tide["shift"] * DEG2RAD
+            a = spin * tide["amplitude"][j] * tide["nodal"][j]
+            old = old + a * math.cos(w * (elapsed - dt) + eq - ph - sh)
+            new = new + a * math.cos(w * elapsed + eq - ph - sh)
         return np.full(d.n_ob, old), np.full(d.n_ob, new)
 
     def step(self, it: int) -> dict:

@@ -222,6 +222,7 @@ module gom_core_abi
   integer(c_int), parameter :: GOM_F_AIR_P = 60
   integer(c_int), parameter :: GOM_F_ETA_AT_OB_OLD = 61
   integer(c_int), parameter :: GOM_F_ETA_AT_OB_NEW = 62
+  integer(c_int), parameter :: GOM_F_Q_ADD = 63
 
   interface
      integer(c_int) function gom_abi_version() bind(c, name="gom_abi_version")

@@ -456,7 +456,9 @@ def _lagrange2(times, values, u2):
     """calculate_Q.f90:47-75: second-order Lagrange interpolation through the three samples
     starting one before the first sample at or after u2 (series times as read, no offset)."""
     diff = np.where(times - u2 >= 0.0, times - u2, np.inf)
-    min_index = int(np.argmin(diff)) + 1 if np.isfinite(diff).any() else 1
+    # no sample at or after u2: minloc lands on the first padding entry past the series
+    # (difference = 9999999 there), which the steps below turn into the last three samples
+    min_index = int(np.argmin(diff)) + 1 if np.isfinite(diff).any() else len(times)
     if min_index == 1:
         min_index += 1
     min_index -= 1

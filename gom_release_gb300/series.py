@@ -1,0 +1,146 @@
+"""Boundary series held on the device (``gom_set_boundary_series``).
+
+GOM's Fortran driver turns its boundary tables into per-step forcing on the host every step:
+setup_spinup.f90 (tide and baroclinic spin-up), compute_boundary_eta.f90 (open-boundary elevation,
+ob_eta_type -1 / 1 harmonic / 2 time series), calculate_Q.f90 (river discharge, linear or
+second-order Lagrange) and the boundary-concentration interpolation of
+solve_transport_equation_v19.f90:229-397.  ``BoundarySeries`` is the set of tables those routines
+read -- the harmonic constituents of read_harmonic_ser.f90 and the series of read_eta_ser.f90,
+read_q_ser.f90, read_salt_ser.f90 and read_temp_ser.f90 with the per-boundary ids of cards C20_1
+and C22_1 -- in the flat layout the C ABI takes.  Once set on a context, every ``step_all`` /
+``step_launch`` evaluates them on the device before the first phase, so a run needs no host
+forcing per step.
+
+Two builders:
+
+* ``from_deck_data(deck)``  a reference deck read by ``gom_inputs.read_deck``;
+* ``from_synthetic(deck)``  a synthetic deck of ``deck.py``: one harmonic series from its tide,
+                            constant discharge and boundary-tracer series -- the same forcing
+                            ``deck.HostForcing`` computes on the host.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+
+@dataclass
+class BoundarySeries:
+    """The argument of ``gom_set_boundary_series`` as numpy arrays (ids are 1-based, 0 = none)."""
+
+    julian_day: float                     # julian_day before the next step
+    step: int                             # it of the last step taken
+    reference_diff_days: int
+    tide_spinup: int
+    tide_spinup_period: float             # days
+    baroclinic_spinup: int
+    baroclinic_spinup_period: float       # days
+    q_interp_method: int
+    ob_eta_type: np.ndarray               # (n_ob)
+    ob_harmonic_id: np.ndarray
+    ob_eta_id: np.ndarray
+    ob_salt_id: np.ndarray
+    ob_temp_id: np.ndarray
+    qb_q_id: np.ndarray                   # (n_qb)
+    qb_salt_id: np.ndarray
+    qb_temp_id: np.ndarray
+    qb_portion: np.ndarray
+    # harmonic series: per series a dict of constituent arrays amplitude, period_h, nodal,
+    # eq_arg, phase and the scalar phase_shift
+    harmonics: list = field(default_factory=list)
+    # kind -> list of (times, values) per series; kinds eta, q, salt, temp
+    series: dict = field(default_factory=dict)
+
+    def flat(self, kind: str):
+        """(start, time, value) of one kind: offsets (n + 1) and the concatenated samples."""
+        ser = self.series.get(kind, [])
+        start = np.zeros(len(ser) + 1, np.int32)
+        for k, (t, _) in enumerate(ser):
+            start[k + 1] = start[k] + len(t)
+        t = np.concatenate([np.asarray(t, np.float64) for t, _ in ser]) if ser else np.zeros(0)
+        v = np.concatenate([np.asarray(v, np.float64) for _, v in ser]) if ser else np.zeros(0)
+        return start, t, v
+
+    def flat_harmonics(self):
+        """(start, amplitude, period_h, nodal, eq_arg, phase, phase_shift) of the harmonic series."""
+        start = np.zeros(len(self.harmonics) + 1, np.int32)
+        cols = {k: [] for k in ("amplitude", "period_h", "nodal", "eq_arg", "phase")}
+        for h, s in enumerate(self.harmonics):
+            start[h + 1] = start[h] + len(s["amplitude"])
+            for k in cols:
+                cols[k].extend(float(x) for x in s[k])
+        shift = np.array([float(s["phase_shift"]) for s in self.harmonics], np.float64)
+        return (start, *[np.asarray(cols[k], np.float64) for k in ("amplitude", "period_h", "nodal", "eq_arg",
+                                                                   "phase")], shift)
+
+
+def from_deck_data(deck) -> BoundarySeries:
+    """The boundary tables of a reference deck (``deck.meta['reference']``, a ``DeckData``):
+    ids from cards C20_1 / C22_1, series as the readers store them (times and values already
+    adjusted and converted), start time from card C3 (julian.f90), reference_diff_days from
+    calculate_reference_diff_days.f90, spin-up from card C21."""
+    from .gom_inputs import julian_day0, reference_diff_days
+
+    data = deck.meta["reference"]
+    v = data.cards
+    ob = np.asarray(data.ob).reshape(-1, 7)
+    qb = np.asarray(data.qb).reshape(-1, 6)
+    if np.any(ob[:, 2] == 1):
+        raise ValueError("harmonic open boundaries need read_harmonic_ser tables, which the deck reader "
+                         "does not parse")
+    series = {k: list(zip(*data.series[k])) for k in ("eta", "q", "salt", "temp") if k in data.series}
+    return BoundarySeries(
+        julian_day=julian_day0(v), step=0, reference_diff_days=reference_diff_days(v),
+        tide_spinup=int(v.get("tide_spinup", 0)), tide_spinup_period=float(v.get("tide_spinup_period", 0.0)),
+        baroclinic_spinup=int(v.get("baroclinic_spinup", 0)),
+        baroclinic_spinup_period=float(v.get("baroclinic_spinup_period", 0.0)),
+        q_interp_method=int(v.get("q_interp_method", 1)),
+        ob_eta_type=ob[:, 2].astype(np.int32), ob_harmonic_id=ob[:, 3].astype(np.int32),
+        ob_eta_id=ob[:, 4].astype(np.int32), ob_salt_id=ob[:, 5].astype(np.int32),
+        ob_temp_id=ob[:, 6].astype(np.int32),
+        qb_q_id=qb[:, 2].astype(np.int32), qb_salt_id=qb[:, 4].astype(np.int32),
+        qb_temp_id=qb[:, 5].astype(np.int32), qb_portion=qb[:, 3].astype(np.float64),
+        series=series)
+
+
+def _constant(value: float):
+    """A two-sample series holding `value` at every time the run reaches: the interpolation
+    (u2 - u1)(v3 - v1)/(u3 - u1) + v1 then returns v1 exactly."""
+    return (np.array([-1.0e15, 1.0e15]), np.array([float(value), float(value)]))
+
+
+def from_synthetic(deck) -> BoundarySeries:
+    """The forcing of ``deck.HostForcing`` as device tables: every open boundary harmonic with
+    the deck's tide (series 1), the rivers on one constant discharge series of value q_total
+    split by q_portion, constant open-boundary and river salinity / temperature series (id 0
+    where the deck leaves them unset), tide spin-up over tide_spinup_days, julian day 0."""
+    n_ob, n_qb = deck.n_ob, deck.n_qb
+    tide = deck.tide
+    harm = [dict(amplitude=list(tide["amplitude"]), period_h=list(tide["period_h"]), nodal=list(tide["nodal"]),
+                 eq_arg=list(tide["eq_arg"]), phase=list(tide["phase"]), phase_shift=float(tide["shift"]))]
+    series = {"eta": [], "q": [], "salt": [], "temp": []}
+
+    def sid(kind, value):
+        if value is None:
+            return 0
+        series[kind].append(_constant(value))
+        return len(series[kind])
+
+    ob_salt, ob_temp = sid("salt", deck.ob_salt), sid("temp", deck.ob_temp)
+    q_id = sid("q", deck.q_total) if n_qb else 0
+    q_salt, q_temp = (sid("salt", deck.q_salt), sid("temp", deck.q_temp)) if n_qb else (0, 0)
+    spin_days = float(deck.tide_spinup_days)
+    ones_ob = np.ones(n_ob, np.int32)
+    ones_qb = np.ones(n_qb, np.int32)
+    return BoundarySeries(
+        julian_day=0.0, step=0, reference_diff_days=0, tide_spinup=1 if spin_days > 0.0 else 0,
+        tide_spinup_period=spin_days, baroclinic_spinup=0, baroclinic_spinup_period=0.0, q_interp_method=1,
+        ob_eta_type=ones_ob.copy(), ob_harmonic_id=ones_ob.copy(), ob_eta_id=np.zeros(n_ob, np.int32),
+        ob_salt_id=ones_ob * ob_salt, ob_temp_id=ones_ob * ob_temp,
+        qb_q_id=ones_qb * q_id, qb_salt_id=ones_qb * q_salt, qb_temp_id=ones_qb * q_temp,
+        qb_portion=np.asarray(deck.q_portion, np.float64).copy() if n_qb else np.zeros(0),
+        harmonics=harm, series=series)
+
+
+__all__ = ["BoundarySeries", "from_deck_data", "from_synthetic"]

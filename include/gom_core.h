@@ -309,6 +309,7 @@ typedef enum gom_field {
     GOM_F_AIR_P,               /* (N_n)  Pa    */
     GOM_F_ETA_AT_OB_OLD,       /* (n_ob)       */
     GOM_F_ETA_AT_OB_NEW,       /* (n_ob)       */
+    GOM_F_Q_ADD,               /* (n_qb)  m3/s */
     GOM_F_COUNT
 } gom_field;
 
@@ -393,6 +394,60 @@ typedef struct gom_storm {
     double t0;                 /* context elapsed time at which this run's clock is 0  */
 } gom_storm;
 int gom_set_storms(struct gom_ctx *ctx, int32_t n_storms, const gom_storm *storms, double elapsed_time);
+
+/* Boundary series evaluated on the device (no single reference counterpart: it moves onto the
+ * GPU what the Fortran driver computes on the host every step in setup_spinup.f90,
+ * compute_boundary_eta.f90 (ob_eta_type -1 interior mean, 1 harmonic, 2 time series), calculate_Q.f90 and the
+ * boundary-concentration interpolation of solve_transport_equation_v19.f90:229-397).  The tables
+ * are the ones read_harmonic_ser.f90, read_eta_ser.f90, read_q_ser.f90, read_salt_ser.f90 and
+ * read_temp_ser.f90 hold.  Once set, every gom_step_all / gom_step_launch first advances the
+ * device clock (it = it + 1, elapsed_time = it dt, julian_day = julian_day + dt / 86400), forms the
+ * spin-up factors, eta_at_ob_old / eta_at_ob_new, Q_add and the boundary salinity and temperature
+ * of every transport subcycle, with the reference's expressions (linear interpolation on series
+ * times minus reference_diff_days x 86400); a time outside a series keeps the value that entry
+ * had.  An open-boundary cell of type -1 with no interior cell around its nodes records GOM_E_ARG
+ * in the step status (the reference stops there).  Single-run contexts only.  The separate
+ * gom_step_* entry points do not run it.  gom_set_forcing is then needed only
+ * for what the series leave alone (wind stress, Gamma_T, air pressure, heat terms).  Not with
+ * gom_set_storms on the same context (GOM_E_ARG). */
+typedef struct gom_series {
+    int32_t n_series;          /* number of series                                          */
+    int32_t reserved;
+    const int32_t *start;      /* (n_series + 1) offsets of each series in time / value      */
+    const double *time;        /* seconds, as the readers store them: (t + adjust) x conv    */
+    const double *value;       /* (v + adjust) x conv                                        */
+} gom_series;
+
+typedef struct gom_boundary_series {
+    double julian_day;              /* julian_day before the next step (prepare_gom.f90:29)    */
+    double tide_spinup_period;      /* card C21, days                                           */
+    double baroclinic_spinup_period;/* card C21, days                                           */
+    int32_t step;                   /* it of the last step taken (the next one is step + 1)     */
+    int32_t reference_diff_days;    /* calculate_reference_diff_days.f90                        */
+    int32_t tide_spinup;            /* card C21 flag                                            */
+    int32_t baroclinic_spinup;      /* card C21 flag (used with baroclinic_flag 1)              */
+    int32_t q_interp_method;        /* 1 linear, 2 second-order Lagrange (calculate_Q.f90)      */
+    int32_t n_harmonic;             /* harmonic series (num_harmonic_ser)                       */
+    const int32_t *ob_eta_type;     /* (n_ob) -1 mean of the interior cells around (old level
+                                       only), 1 harmonic, 2 time series, 0 and 3 left as set     */
+    const int32_t *ob_harmonic_id;  /* (n_ob) 1-based series ids, 0 none                        */
+    const int32_t *ob_eta_id;
+    const int32_t *ob_salt_id;
+    const int32_t *ob_temp_id;
+    const int32_t *qb_q_id;         /* (n_qb) 1-based series ids, 0 none                        */
+    const int32_t *qb_salt_id;
+    const int32_t *qb_temp_id;
+    const double *qb_portion;       /* (n_qb) Q_portion                                         */
+    const int32_t *harmonic_start;  /* (n_harmonic + 1) offsets into the constituent arrays      */
+    const double *amplitude;        /* per constituent: tidal_amplitude (m)                     */
+    const double *period_h;         /* tidal_period (h)                                         */
+    const double *nodal;            /* tidal_nodal_factor                                       */
+    const double *eq_arg;           /* equilibrium_argument (degrees)                           */
+    const double *phase;            /* tidal_phase (degrees)                                    */
+    const double *phase_shift;      /* (n_harmonic) tidal_phase_shift (degrees)                 */
+    gom_series eta, q, salt, temp;
+} gom_boundary_series;
+int gom_set_boundary_series(struct gom_ctx *ctx, const gom_boundary_series *series);
 
 /* Cold start computed on the device (no reference counterpart as one routine: it is what
  * setup_cold_start.f90 + update_vertical_layers_0.f90 + uniform read_salt_init.f90 /

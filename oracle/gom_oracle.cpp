@@ -118,6 +118,14 @@ struct gom_ctx {
 
     // ---------------- forcing
     double elapsed_time = 0, spinup_tide = 1, spinup_baroclinic = 1;
+    // boundary series (gom_set_boundary_series), evaluated at the start of gom_step_all
+    bool has_series = false;
+    double jday = 0, rdd_s = 0, tide_per_s = 0, bc_per_s = 0;
+    int step_no = 0, q_method = 1, n_harm = 0;
+    std::vector<int32_t> sr_start[4];
+    std::vector<double> sr_time[4], sr_value[4];
+    std::vector<int32_t> ob_type, ob_h, ob_eta, ob_salt, ob_temp, qb_q, qb_salt, qb_temp, h_start;
+    std::vector<double> qb_portion, h_amp, h_per, h_nodal, h_eq, h_ph, h_shift;
     std::vector<double> eta_at_ob_old, eta_at_ob_new, q_add, wind_stress_normal, wind_stress_tangnt, gamma_t,
         air_p, con_at_ob, con_at_qb, phi_sw, phi_sz;
 
@@ -176,6 +184,7 @@ FieldShape field_shape(int f) {
     case GOM_F_WIND_STRESS_NORMAL: case GOM_F_WIND_STRESS_TANGNT: case GOM_F_GAMMA_T: return {-1, 1, 0, 0};
     case GOM_F_AIR_P: return {-1, 2, 0, 0};
     case GOM_F_ETA_AT_OB_OLD: case GOM_F_ETA_AT_OB_NEW: return {-1, 4, 0, 0};
+    case GOM_F_Q_ADD: return {-1, 3, 0, 0};
     default: return {-2, 0, 0, 0};
     }
 }
@@ -945,6 +954,7 @@ std::vector<double> *forcing_field(gom_ctx *c, int field) {
     case GOM_F_AIR_P: return &c->air_p;
     case GOM_F_ETA_AT_OB_OLD: return &c->eta_at_ob_old;
     case GOM_F_ETA_AT_OB_NEW: return &c->eta_at_ob_new;
+    case GOM_F_Q_ADD: return &c->q_add;
     default: return nullptr;
     }
 }
@@ -1003,6 +1013,237 @@ int gom_set_forcing(gom_ctx *c, const gom_forcing *f) {
 
 // the CPU restatement takes all forcing from the host, and its initial state from the host
 int gom_set_storms(gom_ctx *c, int32_t, const gom_storm *, double) { return c ? GOM_E_ARG : GOM_E_ARG; }
+
+// ---------------------------------------------------------------------------- boundary series
+// compute_boundary_eta.f90:22-125 (types 1 and 2), calculate_Q.f90:21-75, setup_spinup.f90:12-31 and
+// the boundary concentrations of solve_transport_equation_v19.f90:229-382, with a time outside a
+// series keeping that entry's previous value (the reference's value there is undefined)
+int gom_set_boundary_series(gom_ctx *c, const gom_boundary_series *bs) {
+    if (!c || !bs || c->d.n_runs > 1) return GOM_E_ARG;
+    const gom_series *sets[4] = {&bs->eta, &bs->q, &bs->salt, &bs->temp};
+    // the argument rules: series starts from 0 and never decrease, times never decrease within a
+    // series, ids within 0..n (0 = none), eta types -1..3, Q method 1 or 2
+    for (const gom_series *sr : sets) {
+        if (sr->n_series < 0) return GOM_E_ARG;
+        if (sr->n_series == 0) continue;
+        if (!sr->start || !sr->time || !sr->value || sr->start[0] != 0) return GOM_E_ARG;
+        for (int k = 0; k < sr->n_series; ++k) {
+            if (sr->start[k + 1] < sr->start[k]) return GOM_E_ARG;
+            for (int q = sr->start[k] + 1; q < sr->start[k + 1]; ++q)
+                if (!(sr->time[q] >= sr->time[q - 1])) return GOM_E_ARG;
+        }
+    }
+    const int nh = bs->n_harmonic;
+    if (nh < 0 || (nh > 0 && (!bs->harmonic_start || !bs->amplitude || !bs->period_h || !bs->nodal || !bs->eq_arg ||
+                              !bs->phase || !bs->phase_shift || bs->harmonic_start[0] != 0)))
+        return GOM_E_ARG;
+    for (int k = 0; k < nh; ++k)
+        if (bs->harmonic_start[k + 1] < bs->harmonic_start[k]) return GOM_E_ARG;
+    auto ids_ok = [](const int32_t *ids, int n, int limit) {
+        if (n > 0 && !ids) return false;
+        for (int i = 0; i < n; ++i)
+            if (ids[i] < 0 || ids[i] > limit) return false;
+        return true;
+    };
+    if (c->NOB > 0 && !bs->ob_eta_type) return GOM_E_ARG;
+    for (int i = 0; i < c->NOB; ++i)
+        if (bs->ob_eta_type[i] < -1 || bs->ob_eta_type[i] > 3) return GOM_E_ARG;   // read_main_inp.f90:460-464
+    if (!ids_ok(bs->ob_harmonic_id, c->NOB, nh) ||
+        !ids_ok(bs->ob_eta_id, c->NOB, bs->eta.n_series) || !ids_ok(bs->ob_salt_id, c->NOB, bs->salt.n_series) ||
+        !ids_ok(bs->ob_temp_id, c->NOB, bs->temp.n_series) || !ids_ok(bs->qb_q_id, c->NQB, bs->q.n_series) ||
+        !ids_ok(bs->qb_salt_id, c->NQB, bs->salt.n_series) || !ids_ok(bs->qb_temp_id, c->NQB, bs->temp.n_series) ||
+        (c->NQB > 0 && !bs->qb_portion))
+        return GOM_E_ARG;
+    if (bs->q_interp_method != 1 && bs->q_interp_method != 2) return GOM_E_ARG;
+    for (int k = 0; k < 4; ++k) {
+        const gom_series &sr = *sets[k];
+        c->sr_start[k].assign(1, 0);
+        c->sr_time[k].clear();
+        c->sr_value[k].clear();
+        if (sr.n_series > 0) {
+            c->sr_start[k].assign(sr.start, sr.start + sr.n_series + 1);
+            c->sr_time[k].assign(sr.time, sr.time + sr.start[sr.n_series]);
+            c->sr_value[k].assign(sr.value, sr.value + sr.start[sr.n_series]);
+        }
+    }
+    auto ids = [](std::vector<int32_t> &v, const int32_t *src, int n) {
+        v.assign((size_t)n, 0);
+        if (src) v.assign(src, src + n);
+    };
+    ids(c->ob_type, bs->ob_eta_type, c->NOB);
+    ids(c->ob_h, bs->ob_harmonic_id, c->NOB);
+    ids(c->ob_eta, bs->ob_eta_id, c->NOB);
+    ids(c->ob_salt, bs->ob_salt_id, c->NOB);
+    ids(c->ob_temp, bs->ob_temp_id, c->NOB);
+    ids(c->qb_q, bs->qb_q_id, c->NQB);
+    ids(c->qb_salt, bs->qb_salt_id, c->NQB);
+    ids(c->qb_temp, bs->qb_temp_id, c->NQB);
+    c->qb_portion.assign((size_t)c->NQB, 0.0);
+    if (bs->qb_portion) c->qb_portion.assign(bs->qb_portion, bs->qb_portion + c->NQB);
+    c->n_harm = bs->n_harmonic;
+    c->h_start.assign(1, 0);
+    c->h_amp.clear(), c->h_per.clear(), c->h_nodal.clear(), c->h_eq.clear(), c->h_ph.clear(), c->h_shift.clear();
+    if (bs->n_harmonic > 0) {
+        const int nh = bs->n_harmonic, nc = bs->harmonic_start[nh];
+        c->h_start.assign(bs->harmonic_start, bs->harmonic_start + nh + 1);
+        c->h_amp.assign(bs->amplitude, bs->amplitude + nc);
+        c->h_per.assign(bs->period_h, bs->period_h + nc);
+        c->h_nodal.assign(bs->nodal, bs->nodal + nc);
+        c->h_eq.assign(bs->eq_arg, bs->eq_arg + nc);
+        c->h_ph.assign(bs->phase, bs->phase + nc);
+        c->h_shift.assign(bs->phase_shift, bs->phase_shift + nh);
+    }
+    // reference_diff_days * 86400.0: an integer times a default-REAL constant, in single precision
+    c->rdd_s = (double)((float)bs->reference_diff_days * 86400.0f);
+    c->tide_per_s = bs->tide_spinup == 1 ? bs->tide_spinup_period * 86400.0 : 0.0;
+    c->bc_per_s = (bs->baroclinic_spinup == 1 && c->p.baroclinic_flag == 1) ? bs->baroclinic_spinup_period * 86400.0
+                                                                              : 0.0;
+    c->q_method = bs->q_interp_method;
+    c->jday = bs->julian_day;
+    c->step_no = bs->step;
+    c->has_series = true;
+    return GOM_OK;
+}
+
+namespace {
+
+// first interval t2 of the reference's search with u1 <= u2 <= u3 (times minus the offset)
+bool series_value(const gom_ctx *c, int kind, int id, double u2, double &v) {
+    if (id < 1 || id + 1 > (int)c->sr_start[kind].size()) return false;
+    const int s0 = c->sr_start[kind][id - 1], s1 = c->sr_start[kind][id];
+    for (int t2 = s0 + 1; t2 < s1; ++t2) {
+        const double u1 = c->sr_time[kind][t2 - 1] - c->rdd_s;
+        const double u3 = c->sr_time[kind][t2] - c->rdd_s;
+        if (u2 >= u1 && u2 <= u3) {
+            const double v1 = c->sr_value[kind][t2 - 1], v3 = c->sr_value[kind][t2];
+            v = (u2 - u1) * (v3 - v1) / (u3 - u1) + v1;
+            return true;
+        }
+    }
+    return false;
+}
+
+double q_lagrange(const gom_ctx *c, int id, double u2) {
+    const int s0 = c->sr_start[1][id - 1], n = c->sr_start[1][id] - s0;
+    const double *t = c->sr_time[1].data() + s0, *val = c->sr_value[1].data() + s0;
+    int min_index = 0;
+    double best = 0.0;
+    for (int k = 0; k < n; ++k) {
+        const double d = t[k] - u2;
+        if (d >= 0.0 && (min_index == 0 || d < best)) {
+            best = d;
+            min_index = k + 1;
+        }
+    }
+    if (min_index == 0) min_index = n;
+    if (min_index == 1) min_index = min_index + 1;
+    min_index = min_index - 1;
+    const int shift = (min_index + 2) - n;
+    if (shift > 0) min_index = min_index - shift;
+    if (min_index < 1) min_index = 1;
+    double total = 0.0;
+    for (int ii = 0; ii <= 2; ++ii) {
+        double prod = val[min_index - 1 + ii];
+        for (int jj = 0; jj <= 2; ++jj)
+            if (jj != ii) prod = prod * (u2 - t[min_index - 1 + jj]) / (t[min_index - 1 + ii] - t[min_index - 1 + jj]);
+        total = total + prod;
+    }
+    return total;
+}
+
+void series_forcing(gom_ctx *c) {
+    const double dt = c->p.dt;
+    c->step_no += 1;
+    const double elapsed = (double)c->step_no * dt;
+    c->elapsed_time = elapsed;
+    c->jday = c->jday + dt / 86400.0;
+    c->spinup_tide = (c->tide_per_s > 0.0 && elapsed < c->tide_per_s) ? std::tanh(2.0 * elapsed / c->tide_per_s) : 1.0;
+    c->spinup_baroclinic = (c->bc_per_s > 0.0 && elapsed < c->bc_per_s) ? std::tanh(2.0 * elapsed / c->bc_per_s) : 1.0;
+    const double spin = c->spinup_tide, spin_bc = c->spinup_baroclinic, jd_s = c->jday * 86400.0;
+    A1<double> eta_cell = FD1(c, GOM_F_ETA_CELL);
+    const double deg2rad = 3.141592653589793 / 180.0;
+    for (int i = 0; i < c->NOB; ++i) {
+        if (c->ob_type[i] == -1) {
+            // compute_boundary_eta.f90:45-70: the mean elevation of the interior cells around the
+            // open-boundary cell's nodes (each counted once per node it shares), old level only
+            const int cell = c->ob_cell_id(i + 1);
+            double sum0 = 0.0;
+            int icount = 0;
+            for (int l = 1; l <= c->tri_or_quad(cell); ++l) {
+                const int nd = c->nodenum_at_cell(l, cell);
+                for (int i2 = 1; i2 <= c->adj_cells_at_node(nd); ++i2) {
+                    const int ie = c->adj_cellnum_at_node(i2, nd);
+                    if (c->ob_element_flag(ie) == 0) {
+                        icount = icount + 1;
+                        sum0 = sum0 + eta_cell(ie);
+                    }
+                }
+            }
+            if (icount == 0) set_err(c, GOM_E_ARG, 0, i + 1, 0, 0.0, GOM_ENTITY_OTHER);
+            else c->eta_at_ob_old[i] = sum0 / icount;
+        } else if (c->ob_type[i] == 1) {
+            const int h = c->ob_h[i];
+            double o = 0.0, nw = 0.0;
+            if (h >= 1 && h <= c->n_harm) {
+                for (int j = c->h_start[h - 1]; j < c->h_start[h]; ++j) {
+                    const double w = 2.0 * 3.141592653589793 / (c->h_per[j] * 3600.0);
+                    const double a = spin * c->h_amp[j] * c->h_nodal[j];
+                    o = o + a * std::cos(w * (elapsed - dt) + c->h_eq[j] * deg2rad - c->h_ph[j] * deg2rad -
+                                         c->h_shift[h - 1] * deg2rad);
+                    nw = nw + a * std::cos(w * elapsed + c->h_eq[j] * deg2rad - c->h_ph[j] * deg2rad -
+                                           c->h_shift[h - 1] * deg2rad);
+                }
+            }
+            c->eta_at_ob_old[i] = o;
+            c->eta_at_ob_new[i] = nw;
+        } else if (c->ob_type[i] == 2) {
+            double v;
+            if (series_value(c, 0, c->ob_eta[i], jd_s - dt, v)) c->eta_at_ob_old[i] = spin * v;
+            if (series_value(c, 0, c->ob_eta[i], jd_s, v)) c->eta_at_ob_new[i] = spin * v;
+        }
+    }
+    for (int i = 0; i < c->NQB; ++i) {
+        const int q = c->qb_q[i];
+        double v;
+        if (q >= 1) {   // ids were checked against the series count when they were set
+            if (c->q_method == 2) c->q_add[i] = q_lagrange(c, q, jd_s) * c->qb_portion[i];
+            else if (series_value(c, 1, q, jd_s, v)) c->q_add[i] = v * c->qb_portion[i];
+        }
+    }
+    const int nt = std::max(1, c->p.trans_sub_iter);
+    const bool salt = c->p.transport_flag && c->p.is_salt, temp = c->p.transport_flag && c->p.is_temp;
+    const double dt2 = dt / nt;
+    for (int sub = 0; sub < nt; ++sub) {
+        const double u2 = (jd_s - dt) + (sub + 1) * dt2;
+        double v;
+        for (int i = 0; i < c->NOB; ++i) {
+            if (salt) {
+                double &x = c->con_at_ob[((size_t)sub * 2 + 0) * c->NOB + i];
+                if (c->ob_salt[i] <= 0) x = 0.0;
+                else if (series_value(c, 2, c->ob_salt[i], u2, v)) x = spin_bc * v;
+            }
+            if (temp) {
+                double &x = c->con_at_ob[((size_t)sub * 2 + 1) * c->NOB + i];
+                if (c->ob_temp[i] <= 0) x = 0.0;
+                else if (series_value(c, 3, c->ob_temp[i], u2, v)) x = spin_bc * v;
+            }
+        }
+        for (int i = 0; i < c->NQB; ++i) {
+            if (salt) {
+                double &x = c->con_at_qb[((size_t)sub * 2 + 0) * c->NQB + i];
+                if (c->qb_salt[i] <= 0) x = 0.0;
+                else if (series_value(c, 2, c->qb_salt[i], u2, v)) x = spin_bc * v;
+            }
+            if (temp) {
+                double &x = c->con_at_qb[((size_t)sub * 2 + 1) * c->NQB + i];
+                if (c->qb_temp[i] <= 0) x = 0.0;
+                else if (series_value(c, 3, c->qb_temp[i], u2, v)) x = spin_bc * v;
+            }
+        }
+    }
+}
+
+}  // namespace
 int gom_cold_start(gom_ctx *c, double, double, double, double) { return c ? GOM_E_ARG : GOM_E_ARG; }
 // nothing to tune on the CPU
 int gom_autotune(gom_ctx *c, int32_t, int32_t *choice) {
@@ -2815,6 +3056,7 @@ int gom_step_swap(gom_ctx *c) {
 int gom_step_all(gom_ctx *c, int32_t *pcg_iters) {
     if (!c) return GOM_E_ARG;
     int e;
+    if (c->has_series) series_forcing(c);
     if ((e = gom_step_bottom_friction(c))) return e;
     if ((e = gom_step_boundary_velocity(c))) return e;
     if ((e = gom_step_advection(c))) return e;

@@ -1,0 +1,143 @@
+"""Boundary series evaluated on the device (gom_set_boundary_series) against the CPU oracle's
+restatement and against host forcing: on the reference's Mobile Bay deck (elevation, discharge,
+salinity and temperature series, linear and Lagrange discharge) the device forcing equals the
+oracle's bit for bit every step; on a synthetic estuary with a harmonic tide and spin-up it agrees
+to the last bits of cos and tanh (CUDA's and the C library's differ by an ulp or two); the
+interior-mean boundary (type -1) bit for bit; the captured step graph runs the series."""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from gom_release_gb300.core import GomCore, GomError, prepare
+from gom_release_gb300.deck import HostForcing, estuary, initial_state
+from gom_release_gb300.gom_inputs import DeckData, SeriesForcing, deck_from_data
+from gom_release_gb300.series import from_deck_data, from_synthetic
+
+pytestmark = pytest.mark.gpu
+
+FIXTURE = Path(__file__).resolve().parent / "golden" / "mobile_bay.npz"
+FIELD_RTOL = 1e-9      # after a run, relative to the field's largest magnitude
+TIDE_ATOL = 1e-14      # metres: cos / tanh of CUDA against the C library, tide of 0.6 m
+
+
+def _close(a, b, rtol=FIELD_RTOL):
+    scale = max(float(np.abs(b).max()), 1e-30)
+    return float(np.abs(a - b).max()) / scale < rtol
+
+
+def _ctx(deck, st, **lib):
+    c = GomCore(deck, **lib)
+    prepare(c, st)
+    return c
+
+
+@pytest.mark.parametrize("q_method", [1, 2])
+def test_mobile_bay_device_series_equal_oracle(oracle_so, gpu_lib, q_method):
+    data = DeckData.from_npz(FIXTURE)
+    data.cards = dict(data.cards, q_interp_method=float(q_method))
+    deck = deck_from_data(data)
+    st = initial_state(deck)
+    ref = _ctx(deck, st, lib_path=oracle_so)
+    gpu = _ctx(deck, st, lib=gpu_lib)
+    static = SeriesForcing(deck).static()
+    bs = from_deck_data(deck)
+    for c in (ref, gpu):
+        c.set_forcing(static)
+        c.set_boundary_series(bs)
+    for it in range(1, 11):
+        ref.step_all()
+        gpu.step_all()
+        for name in ("eta_at_ob_old", "eta_at_ob_new", "q_add"):
+            a, b = gpu.get_field(name), ref.get_field(name)
+            assert np.array_equal(a, b), (it, name, float(np.abs(a - b).max()))
+    for name in ("eta_cell", "un_face", "salt_cell", "temp_cell"):
+        assert _close(gpu.get_field(name), ref.get_field(name)), name
+
+
+def test_mobile_bay_device_series_equal_host_series(gpu_lib):
+    """The same GPU path with the series on the device and with the host forcing every step."""
+    deck = deck_from_data(DeckData.from_npz(FIXTURE))
+    st = initial_state(deck)
+    host = _ctx(deck, st, lib=gpu_lib)
+    dev = _ctx(deck, st, lib=gpu_lib)
+    f = SeriesForcing(deck)
+    dev.set_forcing(f.static())
+    dev.set_boundary_series(from_deck_data(deck))
+    for it in range(1, 11):
+        host.set_forcing(f.full(it) if it == 1 else f.step(it))
+        host.step_all()
+        dev.step_all()
+    for name in ("eta_cell", "un_face", "salt_cell", "temp_cell", "eta_at_ob_new", "q_add"):
+        assert np.array_equal(host.get_field(name), dev.get_field(name)), name
+
+
+def test_estuary_harmonic_series(oracle_so, gpu_lib):
+    deck = estuary(nx=30, ny=12, dx=100.0, n_layers=8, trans_sub_iter=3)
+    deck.tide_spinup_days = 0.01
+    st = initial_state(deck)
+    ref = _ctx(deck, st, lib_path=oracle_so)
+    gpu = _ctx(deck, st, lib=gpu_lib)
+    hf = HostForcing(deck)
+    bs = from_synthetic(deck)
+    for c in (ref, gpu):
+        c.set_forcing(hf.static())
+        c.set_boundary_series(bs)
+    for it in range(1, 21):
+        ref.step_all()
+        gpu.step_all()
+        for name in ("eta_at_ob_old", "eta_at_ob_new"):
+            err = float(np.abs(gpu.get_field(name) - ref.get_field(name)).max())
+            assert err < TIDE_ATOL, (it, name, err)
+        assert np.array_equal(gpu.get_field("q_add"), ref.get_field("q_add"))
+    for name in ("eta_cell", "un_face", "salt_cell", "temp_cell"):
+        assert _close(gpu.get_field(name), ref.get_field(name), 1e-8), name
+
+
+def test_interior_mean_boundary_equals_oracle(oracle_so, gpu_lib):
+    deck = estuary(nx=16, ny=8, dx=100.0, n_layers=4, trans_sub_iter=2)
+    st = initial_state(deck)
+    st["eta_cell"] = np.random.default_rng(3).uniform(-0.2, 0.2, deck.n_cells)
+    ref = _ctx(deck, st, lib_path=oracle_so)
+    gpu = _ctx(deck, st, lib=gpu_lib)
+    bs = from_synthetic(deck)
+    bs.ob_eta_type = np.full(deck.n_ob, -1, np.int32)
+    f = HostForcing(deck).full(1)
+    for c in (ref, gpu):
+        c.set_forcing(f)
+        c.set_boundary_series(bs)
+        c.step_all()
+    assert np.array_equal(gpu.get_field("eta_at_ob_old"), ref.get_field("eta_at_ob_old"))
+    assert np.array_equal(gpu.get_field("eta_at_ob_new"), ref.get_field("eta_at_ob_new"))
+
+
+def test_graph_launch_runs_the_series(gpu_lib):
+    """step_launch / step_wait (the captured graph) and step_all advance the same clock."""
+    deck = estuary(nx=20, ny=8, dx=100.0, n_layers=6, trans_sub_iter=2)
+    deck.tide_spinup_days = 0.01
+    st = initial_state(deck)
+    a = _ctx(deck, st, lib=gpu_lib)
+    b = _ctx(deck, st, lib=gpu_lib)
+    hf = HostForcing(deck)
+    for c in (a, b):
+        c.set_forcing(hf.static())
+        c.set_boundary_series(from_synthetic(deck))
+    for _ in range(8):
+        a.step_all()
+        b.step_launch()
+        b.step_wait()
+    for name in ("eta_at_ob_new", "eta_cell", "salt_cell"):
+        assert np.array_equal(a.get_field(name), b.get_field(name)), name
+
+
+def test_argument_rules_and_storm_exclusion(gpu_lib):
+    deck = estuary(nx=8, ny=4, dx=100.0, n_layers=3, trans_sub_iter=1)
+    c = GomCore(deck, lib=gpu_lib)
+    bs = from_synthetic(deck)
+    bad = from_synthetic(deck)
+    bad.qb_q_id = np.full(deck.n_qb, 9, np.int32)
+    with pytest.raises(GomError):
+        c.set_boundary_series(bad)
+    c.set_boundary_series(bs)
+    with pytest.raises(GomError):
+        c.set_storms([object()])
