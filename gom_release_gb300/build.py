@@ -17,7 +17,7 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 OUT = PKG / "_build"
 SOURCES = ["gom_core.cu", "k_hydro.cu", "k_surface.cu", "k_transport.cu", "k_forcing.cu", "gom_noalloc.cu",
-           "gom_measure.cu"]
+           "gom_measure.cu", "k_geometry.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr"]

@@ -61,6 +61,10 @@ ERR_NAMES = {0: "GOM_OK", 1: "GOM_E_ARG", 2: "GOM_E_CUDA", 3: "GOM_E_NOT_SPD", 4
              5: "GOM_E_ELM", 6: "GOM_E_DRY", 7: "GOM_E_LAYER", 8: "GOM_E_DENSITY", 9: "GOM_E_PCG_MAXIT",
              10: "GOM_E_TIMEOUT", 11: "GOM_E_NOMEM"}
 
+# gom_status.site of a mesh gom_geometry_build rejects (GOM_GEO_* of include/gom_core.h)
+GOM_GEO = {"CONCAVE": 1, "AREA": 2, "MAX_NB": 3, "HANGING": 4, "SURROUNDING": 5, "FACE_COUNT": 6,
+           "FACE_LENGTH": 7, "BALL": 8, "VORONOI": 9, "CENTRES": 10, "BOUNDARY": 11, "VERTICAL": 12}
+
 _D = C.POINTER(C.c_double)
 _I = C.POINTER(C.c_int32)
 
@@ -133,6 +137,36 @@ class GomBoundarySeries(C.Structure):
         [(n, GomSeries) for n in ("eta", "q", "salt", "temp")]
 
 
+class GomMesh(C.Structure):
+    _fields_ = [(n, C.c_int32) for n in ("n_nodes", "n_cells", "max_nb", "voronoi", "n_layers", "n_ob", "n_qb",
+                                          "reserved")] + \
+        [("x_node", _D), ("y_node", _D), ("h_node", _D), ("tri_or_quad", _I), ("nodenum_at_cell", _I),
+         ("z_level", _D), ("msl", C.c_double), ("ob_nodes", _I), ("qb_nodes", _I)]
+
+
+# outputs of gom_geometry_build, in gom_mesh_geometry order: (name, ctype, per, width)
+# per: "node", "cell", "face", "ob", "qb"; width: values per entity ("nb" = max_nb, "nb1" = max_nb + 1)
+MESH_GEOMETRY_OUT = [
+    ("adj_cells_at_node", _I, "node", 1), ("adj_cellnum_at_node", _I, "node", "nb"),
+    ("node_count_each_element", _I, "node", "nb"), ("adj_nodes_at_node", _I, "node", 1),
+    ("adj_nodenum_at_node", _I, "node", "nb1"), ("bottom_layer_at_node", _I, "node", 1),
+    ("initial_wetdry_node", _I, "node", 1),
+    ("x_cell", _D, "cell", 1), ("y_cell", _D, "cell", 1), ("h_cell", _D, "cell", 1), ("area", _D, "cell", 1),
+    ("facenum_at_cell", _I, "cell", 4), ("adj_cellnum_at_cell", _I, "cell", 4), ("sign_in_outflow", _I, "cell", 4),
+    ("bottom_layer_at_element", _I, "cell", 1), ("ob_element_flag", _I, "cell", 1), ("qb_element_flag", _I, "cell", 1),
+    ("x_face", _D, "face", 1), ("y_face", _D, "face", 1), ("h_face", _D, "face", 1), ("face_length", _D, "face", 1),
+    ("delta_j", _D, "face", 1), ("cos_theta", _D, "face", 1), ("sin_theta", _D, "face", 1),
+    ("cos_theta2", _D, "face", 1), ("sin_theta2", _D, "face", 1), ("adj_cellnum_at_face", _I, "face", 2),
+    ("nodenum_at_face", _I, "face", 2), ("bottom_layer_at_face", _I, "face", 1),
+    ("boundary_type_of_face", _I, "face", 1), ("isflowside3", _I, "face", 1),
+    ("ob_cell_id", _I, "ob", 1), ("ob_face_id", _I, "ob", 1), ("qb_cell", _I, "qb", 1), ("qb_face", _I, "qb", 1),
+]
+
+
+class GomMeshGeometry(C.Structure):
+    _fields_ = [("face_capacity", C.c_int32), ("n_faces", C.c_int32)] + [(n, t) for n, t, _, _ in MESH_GEOMETRY_OUT]
+
+
 class GomStatus(C.Structure):
     _fields_ = [("code", C.c_int32), ("site", C.c_int32), ("entity", C.c_int32), ("layer", C.c_int32),
                 ("value", C.c_double), ("entity_kind", C.c_int32), ("run", C.c_int32)]
@@ -181,6 +215,7 @@ def _bind(lib: C.CDLL) -> C.CDLL:
     lib.gom_station_series.argtypes = [vp, _D]
     lib.gom_set_storms.argtypes = [vp, C.c_int32, C.POINTER(GomStorm), C.c_double]
     lib.gom_set_boundary_series.argtypes = [vp, C.POINTER(GomBoundarySeries)]
+    lib.gom_geometry_build.argtypes = [C.POINTER(GomMesh), C.POINTER(GomMeshGeometry), C.POINTER(GomStatus)]
     lib.gom_cold_start.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_double]
     lib.gom_autotune.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32)]
     lib.gom_tuning_variants.argtypes = [C.POINTER(C.c_int32)]
@@ -509,6 +544,43 @@ class GomCore:
 # ------------------------------------------------------------------ time loop (main.f90:53-304)
 TIME_LOOP = ["bottom_friction", "boundary_velocity", "advection", "momentum", "free_surface",
              "velocities", "layers", "node_velocity", "transport", "density", "turbulence", "swap"]
+
+
+def geometry_build(lib: C.CDLL, raw, max_nb: int, voronoi: int, z_level, msl: float, ob_pairs=(), q_pairs=()):
+    """gom_geometry_build of a library (the CUDA library, or the oracle in tests): the start-up
+    geometry of a mesh (``mesh.RawMesh``) with its vertical grid and boundary node pairs.
+    Returns a dict of arrays shaped as ``mesh.build_geometry`` and ``deck._finish_levels`` hold
+    them (n_faces rows for face arrays); raises GomError with the failing check's status."""
+    x, y, h = (np.ascontiguousarray(a, dtype=np.float64) for a in (raw.x, raw.y, raw.h))
+    tq = np.ascontiguousarray(raw.tri_or_quad, dtype=np.int32)
+    cells = np.ascontiguousarray(raw.cells, dtype=np.int32).reshape(-1, 4)
+    zl = np.ascontiguousarray(z_level, dtype=np.float64)
+    ob = np.ascontiguousarray(np.asarray(ob_pairs, dtype=np.int32).reshape(-1, 2))
+    qb = np.ascontiguousarray(np.asarray(q_pairs, dtype=np.int32).reshape(-1, 2))
+    nn, nc, L = len(x), len(tq), len(zl) - 1
+    m = GomMesh(nn, nc, int(max_nb), int(voronoi), L, len(ob), len(qb), 0,
+                x.ctypes.data_as(_D), y.ctypes.data_as(_D), h.ctypes.data_as(_D), tq.ctypes.data_as(_I),
+                cells.ctypes.data_as(_I), zl.ctypes.data_as(_D), float(msl), ob.ctypes.data_as(_I),
+                qb.ctypes.data_as(_I))
+    cap = int(tq.sum())
+    count = {"node": nn, "cell": nc, "face": cap, "ob": len(ob), "qb": len(qb)}
+    arrays = {}
+    out = GomMeshGeometry(face_capacity=cap)
+    for name, t, per, width in MESH_GEOMETRY_OUT:
+        w = {"nb": max_nb, "nb1": max_nb + 1}.get(width, width)
+        a = np.zeros((count[per], w) if w != 1 else count[per], dtype=np.int32 if t is _I else np.float64)
+        arrays[name] = a
+        setattr(out, name, a.ctypes.data_as(t))
+    st = GomStatus()
+    rc = lib.gom_geometry_build(C.byref(m), C.byref(out), C.byref(st))
+    if rc != 0:
+        raise GomError(rc, "gom_geometry_build", st if st.code else None)
+    nf = out.n_faces
+    for name, _, per, _ in MESH_GEOMETRY_OUT:
+        if per == "face":
+            arrays[name] = arrays[name][:nf].copy()
+    arrays["n_faces"] = nf
+    return arrays
 
 
 def prepare(core: GomCore, state: dict):

@@ -149,22 +149,31 @@ def _finish(name, raw, L, z_bottom, z_top, params, ob_pairs, q_pairs, q_portion,
     return _finish_levels(name, raw, z_level, params, ob_pairs, q_pairs, q_portion, **kw)
 
 
+def _device_geometry(lib, raw, z_level, msl, ob_pairs, q_pairs, voronoi, max_nb):
+    """set_geometry_1/2 through gom_geometry_build of `lib` (the CUDA library): the arrays of
+    build_geometry plus the boundary and bottom-layer arrays _finish_levels derives."""
+    from .core import geometry_build
+
+    r = geometry_build(lib, raw, max_nb, voronoi, z_level, msl, ob_pairs, q_pairs)
+    a = dict(x_node=raw.x, y_node=raw.y, h_node=raw.h, tri_or_quad=raw.tri_or_quad.astype(np.int32),
+             nodenum_at_cell=raw.cells.astype(np.int32))
+    ids = {k: r.pop(k) for k in ("ob_cell_id", "ob_face_id", "qb_cell", "qb_face")}
+    nf = r.pop("n_faces")
+    a.update(r)
+    return a, nf, ids
+
+
 def _finish_levels(name, raw, z_level, params, ob_pairs, q_pairs, q_portion, voronoi: int = 1, max_nb: int = 12,
-                   coriolis_on: bool = True, **kw) -> Deck:
+                   coriolis_on: bool = True, geometry_lib=None, **kw) -> Deck:
     """Geometry, vertical grid and boundaries of a deck whose level heights z_level(0:L) are given
-    (read_main_inp.f90 cards C2/C2_1, set_geometry_1.f90, set_geometry_2.f90)."""
+    (read_main_inp.f90 cards C2/C2_1, set_geometry_1.f90, set_geometry_2.f90).  With
+    ``geometry_lib`` (a loaded CUDA library) set_geometry_1/2 run on the GPU."""
+    if geometry_lib is not None:
+        return _finish_device(name, raw, z_level, params, ob_pairs, q_pairs, q_portion, voronoi, max_nb, coriolis_on,
+                              geometry_lib, **kw)
     g = build_geometry(raw, max_nb=max_nb, voronoi=voronoi)
     a = g.arrays
-    L = len(z_level) - 1
-    delta_z = np.array([z_level[k] - z_level[k - 1] for k in range(1, L + 1)])
-    dzmin = float(delta_z.min())
-    if np.any(np.abs(z_level[1:] - params.msl) < 1e-5):
-        raise ValueError("a z_level coincides with MSL (read_main_inp.f90 card C2_1)")
-    params.delta_z_min = dzmin
-    # read_main_inp.f90 card C5_03: min(dry_depth*(0.5-1.0e-4), delta_z_min*(0.5-1.e-4)),
-    # the bracket being a default-REAL constant expression
-    c = f32(np.float32(0.5) - np.float32(1.0e-4))
-    params.denominator_min_for_matrix = min(params.dry_depth * c, dzmin * c)
+    L, delta_z = _vertical(z_level, params)
     ob_cell_id, ob_face_id = _boundaries(g, ob_pairs) if ob_pairs else (np.zeros(0, np.int32), np.zeros(0, np.int32))
     qb_cell, qb_face = _boundaries(g, q_pairs) if q_pairs else (np.zeros(0, np.int32), np.zeros(0, np.int32))
     nf, nc, nn = g.n_faces, g.n_cells, g.n_nodes
@@ -187,20 +196,52 @@ def _finish_levels(name, raw, z_level, params, ob_pairs, q_pairs, q_portion, vor
         ob_element_flag=ob_element_flag, qb_element_flag=qb_element_flag,
         boundary_type_of_face=boundary_type_of_face, isflowside3=isflowside3,
     )
-    # calculate_coriolis_factor.f90:17-23 (option 1): omega is a default-REAL literal
-    omega = f32(7.292e-5)
-    a["coriolis_factor"] = np.full(nf, 2 * omega * math.sin(params.coriolis_lat * DEG2RAD) if coriolis_on else 0.0)
-    a["manning"] = np.full(nf, params.manning)
-    a["bf_height"] = np.full(nf, params.bf_height)
+    _face_constants(a, nf, params, coriolis_on)
     return Deck(name=name, geo=a, n_nodes=nn, n_cells=nc, n_faces=nf, n_layers=L, max_nb=g.max_nb,
                 params=params, z_level=z_level, delta_z=delta_z,
                 ob_cell_id=ob_cell_id, ob_face_id=ob_face_id, qb_cell=qb_cell, qb_face=qb_face,
                 q_portion=np.asarray(q_portion, dtype=np.float64), **kw)
 
 
+def _vertical(z_level, params):
+    """Cards C2 / C2_1 and C5_03 of read_main_inp.f90: layer thicknesses, the smallest, and
+    denominator_min_for_matrix."""
+    L = len(z_level) - 1
+    delta_z = np.array([z_level[k] - z_level[k - 1] for k in range(1, L + 1)])
+    dzmin = float(delta_z.min())
+    if np.any(np.abs(z_level[1:] - params.msl) < 1e-5):
+        raise ValueError("a z_level coincides with MSL (read_main_inp.f90 card C2_1)")
+    params.delta_z_min = dzmin
+    # card C5_03: min(dry_depth*(0.5-1.0e-4), delta_z_min*(0.5-1.e-4)), the bracket being a
+    # default-REAL constant expression
+    c = f32(np.float32(0.5) - np.float32(1.0e-4))
+    params.denominator_min_for_matrix = min(params.dry_depth * c, dzmin * c)
+    return L, delta_z
+
+
+def _face_constants(a, nf, params, coriolis_on):
+    # calculate_coriolis_factor.f90:17-23 (option 1): omega is a default-REAL literal
+    omega = f32(7.292e-5)
+    a["coriolis_factor"] = np.full(nf, 2 * omega * math.sin(params.coriolis_lat * DEG2RAD) if coriolis_on else 0.0)
+    a["manning"] = np.full(nf, params.manning)
+    a["bf_height"] = np.full(nf, params.bf_height)
+
+
+def _finish_device(name, raw, z_level, params, ob_pairs, q_pairs, q_portion, voronoi, max_nb, coriolis_on, lib,
+                   **kw) -> Deck:
+    L, delta_z = _vertical(z_level, params)
+    a, nf, ids = _device_geometry(lib, raw, z_level, params.msl, ob_pairs, q_pairs, voronoi, max_nb)
+    _face_constants(a, nf, params, coriolis_on)
+    return Deck(name=name, geo=a, n_nodes=len(raw.x), n_cells=len(raw.tri_or_quad), n_faces=nf, n_layers=L,
+                max_nb=max_nb, params=params, z_level=z_level, delta_z=delta_z,
+                ob_cell_id=ids["ob_cell_id"], ob_face_id=ids["ob_face_id"], qb_cell=ids["qb_cell"],
+                qb_face=ids["qb_face"], q_portion=np.asarray(q_portion, dtype=np.float64), **kw)
+
+
 # ----------------------------------------------------------------------------- configurations
 def tidal_basin(nx: int = 120, ny: int = 80, dx: float = 250.0, tri_rows: int = 4, n_layers: int = 10,
-                seed: int = 20240601, n_steps: int = 720, dt: float = 120.0, closed: bool = False) -> Deck:
+                seed: int = 20240601, n_steps: int = 720, dt: float = 120.0, closed: bool = False,
+                geometry_lib=None) -> Deck:
     """Barotropic tidal basin: h = 5 + 15(1 - y/Ly) + seeded Fourier noise (8 modes,
     2-15 km, 1 m), southern open boundary forced by 0.5 cos(2 pi t / 44712 s), closed
     elsewhere, uniform T = 20, S = 30, theta = 0.6, quadratic drag Cd = 0.0025."""
@@ -221,7 +262,7 @@ def tidal_basin(nx: int = 120, ny: int = 80, dx: float = 250.0, tri_rows: int = 
     deck = _finish("tidal_basin", raw, L, z_bottom, z_top, params, ob_pairs, [], [],
                    tide=dict(amplitude=[0.5], period_h=[12.42], phase=[0.0], nodal=[1.0], eq_arg=[0.0],
                              shift=0.0),
-                   ob_salt=30.0, ob_temp=20.0, n_steps=n_steps, seed=seed)
+                   ob_salt=30.0, ob_temp=20.0, n_steps=n_steps, seed=seed, geometry_lib=geometry_lib)
     deck.init_salt_node = np.full((deck.n_nodes, L), 30.0)
     deck.init_temp_node = np.full((deck.n_nodes, L), 20.0)
     deck.meta = dict(nx=nx, ny=ny, dx=dx, tri_rows=tri_rows)
@@ -230,7 +271,7 @@ def tidal_basin(nx: int = 120, ny: int = 80, dx: float = 250.0, tri_rows: int = 
 
 def estuary(nx: int = 600, ny: int = 250, dx: float = 100.0, tri_rows: int = 4, n_layers: int = 20,
             seed: int = 20240602, n_steps: int = 2880, dt: float = 60.0, n_river: int = 10,
-            trans_sub_iter: int = 4, turbulence_flag: int = 2) -> Deck:
+            trans_sub_iter: int = 4, turbulence_flag: int = 2, geometry_lib=None) -> Deck:
     """Baroclinic estuary: ocean open boundary on the west edge (M2 0.6 m, S = 35, T = 18),
     river of 500 m3/s at S = 0, T = 24 over ``n_river`` faces of the east edge (channel head),
     initial salinity linear along the channel, TVD limiter on, turbulence closure on
@@ -268,7 +309,7 @@ def estuary(nx: int = 600, ny: int = 250, dx: float = 100.0, tri_rows: int = 4, 
                              shift=0.0),
                    ob_salt=35.0, ob_temp=18.0, q_total=500.0, q_salt=0.0, q_temp=24.0,
                    wind_stress=(tau * math.cos(alpha), tau * math.sin(alpha)),
-                   n_steps=n_steps, seed=seed)
+                   n_steps=n_steps, seed=seed, geometry_lib=geometry_lib)
     L = n_layers
     s = 35.0 * (1.0 - x / lx)
     t = 18.0 + 6.0 * (x / lx)

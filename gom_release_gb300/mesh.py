@@ -182,15 +182,17 @@ def build_geometry(raw: RawMesh, max_nb: int = 12, voronoi: int = 1) -> Geometry
     adj_cellnum_at_node[nd_s - 1, pos] = ci_s
     node_count_each_element[nd_s - 1, pos] = li_s
 
-    # --- adj_nodenum_at_node (set_geometry_1.f90:112-130): for each node, the other nodes of
+    # --- adj_nodenum_at_node (set_geometry_1.f90:160-184): for each node, the other nodes of
     # its cells in discovery order (adjacent cell order, then local node order), no repeats.
+    # The reference tests nd == i inside its loop over the list, so a node that is the first
+    # local node of its first cell lists itself first; that is kept.
     rows_node, rows_seq, rows_nb = [], [], []
     for j in range(max_nb):
         cj = adj_cellnum_at_node[:, j]
         has = cj > 0
         for k in range(4):
             nbk = np.where(has, cells[np.maximum(cj, 1) - 1, k], 0)
-            okk = has & (k < tq[np.maximum(cj, 1) - 1]) & (nbk != np.arange(1, nn + 1))
+            okk = has & (k < tq[np.maximum(cj, 1) - 1]) & ((nbk != np.arange(1, nn + 1)) | (j == 0 and k == 0))
             idx = np.nonzero(okk)[0]
             rows_node.append(idx)
             rows_seq.append(np.full(len(idx), j * 4 + k))

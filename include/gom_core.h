@@ -449,6 +449,66 @@ typedef struct gom_boundary_series {
 } gom_boundary_series;
 int gom_set_boundary_series(struct gom_ctx *ctx, const gom_boundary_series *series);
 
+/* ------------------------------------------------------------------ mesh geometry on the device
+ * The start-up geometry of GOM built on the GPU: the areas of read_cell_inp.f90:54-87,
+ * set_geometry_1.f90 (node-cell and node-node adjacency, cell-cell adjacency, face numbering,
+ * face and cell centres, sign_in_outflow, delta_j, face angles), calculate_voronoi_center.f90
+ * (voronoi 1) and set_geometry_2.f90 (open-boundary cells and faces, boundary_type_of_face, bottom
+ * layers) plus the river cells and faces of read_main_inp.f90:810-829 and initial_wetdry_node of
+ * read_node_inp.f90:72-74.  Integer arrays and every double computed with + - x / and sqrt equal
+ * the reference's loops bit for bit; the four angle arrays come from CUDA's atan2 / cos / sin,
+ * which may differ from the C library's in the last bit or two. */
+typedef struct gom_mesh {
+    int32_t n_nodes, n_cells, max_nb, voronoi;
+    int32_t n_layers, n_ob, n_qb, reserved;
+    const double *x_node, *y_node, *h_node;   /* (N_n) node.inp                                  */
+    const int32_t *tri_or_quad;               /* (N_c) cell.inp                                  */
+    const int32_t *nodenum_at_cell;           /* (4, N_c) CCW nodes, 1-based, 0 in slot 4 of triangles */
+    const double *z_level;                    /* (0:L) card C2 / C2_1                            */
+    double msl;
+    const int32_t *ob_nodes;                  /* (2, n_ob) node pairs of card C20_1 (CCW)         */
+    const int32_t *qb_nodes;                  /* (2, n_qb) node pairs of card C22_1 (CCW)         */
+} gom_mesh;
+
+/* Outputs, in host memory the caller owns, laid out as gom_geom takes them.  Face arrays hold
+ * face_capacity entries (sum of tri_or_quad bounds the face count); n_faces receives maxface.
+ * A NULL array is not written. */
+typedef struct gom_mesh_geometry {
+    int32_t face_capacity;
+    int32_t n_faces;                          /* out                                             */
+    int32_t *adj_cells_at_node, *adj_cellnum_at_node, *node_count_each_element;
+    int32_t *adj_nodes_at_node, *adj_nodenum_at_node, *bottom_layer_at_node, *initial_wetdry_node;
+    double *x_cell, *y_cell, *h_cell, *area;
+    int32_t *facenum_at_cell, *adj_cellnum_at_cell, *sign_in_outflow, *bottom_layer_at_element;
+    int32_t *ob_element_flag, *qb_element_flag;
+    double *x_face, *y_face, *h_face, *face_length, *delta_j;
+    double *cos_theta, *sin_theta, *cos_theta2, *sin_theta2;
+    int32_t *adj_cellnum_at_face, *nodenum_at_face, *bottom_layer_at_face, *boundary_type_of_face, *isflowside3;
+    int32_t *ob_cell_id, *ob_face_id, *qb_cell, *qb_face;   /* (n_ob), (n_qb)                 */
+} gom_mesh_geometry;
+
+/* Sites recorded in gom_status.site when gom_geometry_build rejects a mesh (GOM_E_ARG), one per
+ * reference `stop`; entity is the smallest offending 1-based index of the first failing check. */
+enum {
+    GOM_GEO_CONCAVE = 1,          /* read_cell_inp.f90:76-79 (cell)                   */
+    GOM_GEO_AREA = 2,             /* read_cell_inp.f90:83-86 (cell)                   */
+    GOM_GEO_MAX_NB = 3,           /* set_geometry_1.f90:119-123 (node)                */
+    GOM_GEO_HANGING = 4,          /* set_geometry_1.f90:130-134 (node)                */
+    GOM_GEO_SURROUNDING = 5,      /* set_geometry_1.f90:178-182 (node)                */
+    GOM_GEO_FACE_COUNT = 6,       /* set_geometry_1.f90:254-257                       */
+    GOM_GEO_FACE_LENGTH = 7,      /* set_geometry_1.f90:321-324 (face)                */
+    GOM_GEO_BALL = 8,             /* set_geometry_1.f90:338-341 (cell)                */
+    GOM_GEO_VORONOI = 9,          /* calculate_voronoi_center.f90:58-64 (cell)        */
+    GOM_GEO_CENTRES = 10,         /* set_geometry_1.f90:466-469, calculate_voronoi_center.f90:121-124 (face) */
+    GOM_GEO_BOUNDARY = 11,        /* set_geometry_2.f90:37-41, read_main_inp.f90:810-822 (ob i, river n_ob + i) */
+    GOM_GEO_VERTICAL = 12         /* set_geometry_2.f90:101-189 (entity_kind: cell, face or node) */
+};
+
+/* Build the geometry of `mesh` on the current device (its own temporary device memory, freed
+ * before return) and copy it into `out`.  GOM_E_ARG for a bad argument or a mesh the reference
+ * stops on (failure, if not NULL, receives the site and entity). */
+int gom_geometry_build(const gom_mesh *mesh, gom_mesh_geometry *out, gom_status *failure);
+
 /* Cold start computed on the device (no reference counterpart as one routine: it is what
  * setup_cold_start.f90 + update_vertical_layers_0.f90 + uniform read_salt_init.f90 /
  * read_temp_init.f90 leave before the time loop): zero elevation and motion, first layers and
