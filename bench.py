@@ -19,6 +19,12 @@ roofline       the dominant kernel (the transport column solve) timed alone with
                with the capture it came from).
 cpu_baseline   the CPU restatement of the reference (oracle/), built with OpenMP over every
                host thread, on a bounded sample of the same workload.
+e2e_device_series
+               the e2e loop with the boundary forcing held on the device
+               (gom_set_boundary_series): no forcing upload per step.
+serving        a bounded storm-surge serving run (16 Poisson requests, quarter-scale meshes):
+               p50 / p99 latency and throughput of packed mixed precision against plain FP64
+               serving one request at a time on the same GPU (--no-serving skips it).
 
 N > 1 runs independent replicas (the single-run path does not shard): value is the sum over
 ranks of cell-layer-steps divided by the slowest rank's time.
@@ -363,6 +369,38 @@ def snapshot_overlap(run, k: int, ms_plain: float, every: int = 5) -> dict:
             "sync_get_field_ms": sync_read * 1e3}
 
 
+def e2e_device_series(run, deck, ncl: int, k: int, torch_mod, stream, world) -> dict:
+    """The e2e loop with the boundary forcing held on the device (gom_set_boundary_series of the
+    deck's tide, river and boundary tracers, the same values the host forcing computes): every
+    step is one gom_step_all plus the conservation read, with no forcing upload."""
+    from gom_release_gb300.series import from_synthetic
+    core = run.core
+    bs = from_synthetic(deck)
+    bs.step, bs.julian_day = run.it, run.forcing.julian_day
+    core.set_boundary_series(bs)
+    core.step_all()                     # captures the step graph with the series kernels
+    run.it += 1
+    run.forcing.step(run.it)
+    core.synchronize()
+    t0 = time.perf_counter()
+    e0 = torch_mod.cuda.Event(enable_timing=True)
+    e1 = torch_mod.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(k):
+        core.step_all()
+        core.conservation()
+    e1.record(stream)
+    e1.synchronize()
+    secs = reduce_max(e0.elapsed_time(e1) / 1e3, world)
+    wall = time.perf_counter() - t0
+    for _ in range(k):                  # the host clock follows the device's
+        run.it += 1
+        run.forcing.step(run.it)
+    return {"value": ncl * k * world / secs, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 16 + 20,
+            "wall_s": wall, "steps": k,
+            "forcing": "gom_set_boundary_series: harmonic tide, river discharge and boundary tracers on the device"}
+
+
 def time_core_steps(core, k: int) -> float:
     """k steps of a context with device-side forcing, CUDA events on its stream."""
     import torch
@@ -482,21 +520,21 @@ def bench_ensemble(args):
     print(json.dumps(line), flush=True)
 
 
-def bench_serving(args):
+def serving_record(lib, n_requests: int, scale: float, horizon_scale: float, pool_size: int, servers=None):
     """Poisson stream of storm-surge requests (rate 2/s, horizons U(6, 48) h scaled by
-    --horizon-scale), meshes drawn from an ensemble-like pool: continuous batching of mixed-
-    precision contexts under a 150 GB device-memory budget against the plain FP64 path serving the
-    same requests one at a time."""
+    horizon_scale), meshes drawn from an ensemble-like pool: continuous batching in one packed
+    mixed-precision context (and optionally one mixed context per run) under a 150 GB
+    device-memory budget, against the plain FP64 path serving the same requests one at a time on
+    the same GPU.  Returns per-server latency percentiles and throughput."""
     import dataclasses as dc
-    from gom_release_gb300.core import load_core
     from gom_release_gb300.ensemble import ensemble_decks
     from gom_release_gb300.serve import Request, poisson_arrivals, serve, serve_fifo, serve_packed
-    lib = load_core()
+    servers = servers or ("packed", "contexts", "fifo")
     t0 = time.perf_counter()
-    pool = ensemble_decks(n_runs=args.pool, seed=5, min_cells=max(200, int(5000 * args.scale)),
-                          max_cells=max(400, int(400000 * args.scale)))
+    pool = ensemble_decks(n_runs=pool_size, seed=5, min_cells=max(200, int(5000 * scale)),
+                          max_cells=max(400, int(400000 * scale)))
     gen_s = time.perf_counter() - t0
-    arrivals = poisson_arrivals(args.requests, 2.0, seed=3)
+    arrivals = poisson_arrivals(n_requests, 2.0, seed=3)
 
     def make_requests():
         out = []
@@ -505,29 +543,62 @@ def bench_serving(args):
             d = pool[int(r2.integers(len(pool)))]
             st = dc.replace(d.meta["storm"], dp=float(r2.uniform(20e2, 80e2)), rmax=float(r2.uniform(20e3, 60e3)),
                             b=float(r2.uniform(1.0, 1.8)), speed=float(r2.uniform(3.0, 8.0)))
-            hours = float(r2.uniform(6.0, 48.0)) * args.horizon_scale
+            hours = float(r2.uniform(6.0, 48.0)) * horizon_scale
             steps = max(1, int(round(hours * 3600.0 / d.params.dt)))
             out.append(Request(rid=i, deck=d, storm=st, steps=steps, arrival=float(t)))
         return out
 
+    res = {}
+    if "packed" in servers:
+        res["serving_packed_mixed"] = serve_packed(lib, make_requests(), budget_bytes=150e9, precision=1)
+    if "contexts" in servers:
+        res["serving_contexts_mixed"] = serve(lib, make_requests(), budget_bytes=150e9, precision=1)
+    if "fifo" in servers:
+        res["serving_fp64_one_at_a_time"] = serve_fifo(lib, make_requests(), precision=0)
+    workload = (f"serving: {n_requests} Poisson requests (rate 2/s), horizons U(6,48) h x {horizon_scale:g}, "
+                f"meshes from a pool of {len(pool)} storm-surge runs "
+                f"({min(d.n_cells for d in pool)}-{max(d.n_cells for d in pool)} cells), HBM budget 150 GB")
+    return res, workload, gen_s
+
+
+def bench_serving(args):
+    """The serving workload alone (serving_record at the command line's sizes)."""
+    from gom_release_gb300.core import load_core
+    lib = load_core()
     with ClockSampler(0) as clocks:
-        packed = serve_packed(lib, make_requests(), budget_bytes=150e9, precision=1)
-        mixed = serve(lib, make_requests(), budget_bytes=150e9, precision=1)
-        fifo = serve_fifo(lib, make_requests(), precision=0)
+        res, workload, gen_s = serving_record(lib, args.requests, args.scale, args.horizon_scale, args.pool)
+    packed, fifo = res["serving_packed_mixed"], res["serving_fp64_one_at_a_time"]
     line = {
         "metric": METRIC, "value": packed["throughput"], "unit": UNIT, "n_gpus": 1, "steps": None, "warmup": 0,
         "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
         "data": "synthetic",
-        "config": {"workload": (f"serving: {args.requests} Poisson requests (rate 2/s), horizons U(6,48) h x "
-                                f"{args.horizon_scale:g}, meshes from a pool of {len(pool)} storm-surge runs "
-                                f"({min(d.n_cells for d in pool)}-{max(d.n_cells for d in pool)} cells), "
-                                "HBM budget 150 GB"), "generation_s": gen_s},
-        "serving_packed_mixed": packed, "serving_contexts_mixed": mixed, "serving_fp64_one_at_a_time": fifo,
+        "config": {"workload": workload, "generation_s": gen_s},
+        **res,
         "latency_p50_s": packed["latency_p50_s"], "latency_p99_s": packed["latency_p99_s"],
         "throughput_vs_fp64_one_at_a_time": packed["throughput"] / fifo["throughput"],
         "clocks": clocks.summary(),
     }
     print(json.dumps(line), flush=True)
+
+
+def bounded_serving(lib) -> dict:
+    """The serving comparison at a bounded size for the default benchmark line: 16 requests,
+    quarter-scale meshes (1,250-100,000 cells), horizons 0.6-4.8 h; packed mixed precision against
+    plain FP64 one request at a time, p50 / p99 latency and throughput of each."""
+    t0 = time.perf_counter()
+    res, workload, _ = serving_record(lib, 16, 0.25, 0.1, 12, servers=("packed", "fifo"))
+    packed, fifo = res["serving_packed_mixed"], res["serving_fp64_one_at_a_time"]
+    keep = ("latency_p50_s", "latency_p99_s", "latency_mean_s", "throughput", "failed", "repacks",
+            "repack_s_mean", "peak_in_flight")
+
+    def short(r):
+        return {k: r[k] for k in keep if k in r}
+
+    return {"workload": workload, "packed_mixed": short(packed), "fp64_one_at_a_time": short(fifo),
+            "p50_ratio_fp64_over_packed": fifo["latency_p50_s"] / packed["latency_p50_s"],
+            "p99_ratio_fp64_over_packed": fifo["latency_p99_s"] / packed["latency_p99_s"],
+            "throughput_ratio": packed["throughput"] / fifo["throughput"],
+            "wall_s": time.perf_counter() - t0}
 
 
 def bench_precision(args):
@@ -604,6 +675,8 @@ def main():
     ap.add_argument("--size", default="full", choices=["full", "medium", "small"],
                     help="full: the benchmark workload; medium (38k cells) and small (6k cells) for profiling")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-serving", action="store_true",
+                    help="estuary: skip the bounded serving record (packed mixed vs FP64 latency) of the line")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
     ap.add_argument("--tuning", default=None,
                     help="launch variants per tunable site, e.g. 1,3,3,1 (set instead of autotuning)")
@@ -698,6 +771,7 @@ def main():
     e2e_secs = reduce_max(e0.elapsed_time(e1) / 1e3, world)
     wall_e2e = time.perf_counter() - t0
     snapshot = snapshot_overlap(run, ke, wall_e2e / ke)
+    e2e_series = e2e_device_series(run, deck, ncl, ke, torch_mod, stream, world)
     # ---- per-phase timing for the roofline
     snap = run.core.state()
     f = dict(run.forcing.step(run.it + 1))
@@ -734,6 +808,9 @@ def main():
         barrier(world)
         return
     value = ncl * args.steps * world / secs
+    serving = None
+    if not args.no_serving and args.size == "full":
+        serving = bounded_serving(lib)
     cpu = None
     if not args.no_cpu_baseline:
         cpu = cpu_baseline(deck, st, ncl)
@@ -771,6 +848,8 @@ def main():
         "gpu_launches": kernel_launches_per_step(deck) * args.steps,
         "clocks": clocks.summary(),
         "snapshot": snapshot,
+        "serving": serving,
+        "e2e_device_series": e2e_series,
     }
     print(json.dumps(line), flush=True)
     barrier(world)
