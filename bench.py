@@ -483,6 +483,8 @@ def bench_ensemble(args):
             res[label] = {"value": ncl * k / secs, "ms_per_step": secs / k * 1e3, "device_gb": nbytes / 1e9,
                           "active_cell_layers": ncl, "pcg_iters_total": core.pcg_iterations_total(),
                           "autotune": tune, "phase_ms": phase_times_in_place(core)}
+            if args.day and label == "mixed_packed":
+                res["mixed_packed_day"] = rest_of_day(core, ncl, w + 1 + k)
             core.close()
         # each run alone, timed over the same steps of the storm as the packed context (warm-up,
         # autotune, one step, then k timed steps)
@@ -559,6 +561,32 @@ def serving_record(lib, n_requests: int, scale: float, horizon_scale: float, poo
                 f"meshes from a pool of {len(pool)} storm-surge runs "
                 f"({min(d.n_cells for d in pool)}-{max(d.n_cells for d in pool)} cells), HBM budget 150 GB")
     return res, workload, gen_s
+
+
+def rest_of_day(core, ncl: int, done: int, day_steps: int = 1440) -> dict:
+    """Step a storm context through the rest of the 24 h day an hour (60 steps) at a time, timed
+    with CUDA events, checking the status after every hour: the storms' full strength and
+    landfall included."""
+    hours = []
+    left = day_steps - done
+    secs = 0.0
+    while left > 0:
+        n = min(60, left)
+        try:
+            t = time_core_steps(core, n)
+        except Exception as exc:   # a run failed: the library's error, with the status it read
+            hours.append({"steps": n, "ms_per_step": float("nan"), "status": -1, "error": str(exc)})
+            break
+        st = core.status()
+        hours.append({"steps": n, "ms_per_step": t / n * 1e3, "status": int(st.code)})
+        secs += t
+        left -= n
+        if st.code:
+            break
+    steps = sum(h["steps"] for h in hours if h["status"] == 0)
+    return {"steps": steps, "value": ncl * steps / secs if secs > 0 else 0.0, "failed": any(h["status"] for h in hours),
+            "last_step": done + steps, "ms_per_step_by_hour": [round(h["ms_per_step"], 2) for h in hours],
+            "pcg_iters_total": core.pcg_iterations_total()}
 
 
 def bench_serving(args):
@@ -696,6 +724,9 @@ def main():
     ap.add_argument("--warm-hours", type=float, default=0.0,
                     help="ensemble: simulated hours stepped before timing (the storms ramp up over 6 h)")
     ap.add_argument("--skip-mixed-alone", action="store_true", help="ensemble: skip the mixed one-at-a-time arm")
+    ap.add_argument("--day", action="store_true",
+                    help="ensemble: after its timed window, step the packed mixed context through the rest of the "
+                         "24 h day and report its throughput and status hour by hour")
     ap.add_argument("--profile-step", action="store_true",
                     help="ensemble: warm up, autotune and run one packed step phase by phase in an NVTX range "
                          "prof_step (for ncu), then exit")

@@ -58,12 +58,18 @@ class Storm:
 
 def storm_run(seed: int, n_cells: int, aspect: float, n_layers_run: int, dt: float = 60.0,
               dx: float = 250.0, max_layers: int = 30, tri_rows: int = 2, h_coast: float = 2.0,
-              h_min: float = 1.0, av_0: float = 0.05, open_sides: bool = False) -> Deck:
+              h_min: float = 1.0, av_0: float = 0.5, open_sides: bool = False) -> Deck:
     """One storm-surge run of about ``n_cells`` cells, domain aspect ``aspect`` (x / y), deepest
     water using ``n_layers_run`` of the shared 1 m levels; the shelf rises to ``h_coast`` at the
-    closed northern coast, depths at least ``h_min``.  The vertical eddy viscosity ``av_0`` is a
-    storm-surge value (m^2/s): with the 1e-3 of a calm estuary the 1 m surface layer under
-    hurricane winds decouples from the column and its velocity grows without bound."""
+    closed northern coast, depths at least ``h_min``.
+
+    The vertical eddy viscosity ``av_0`` (m^2/s) is a storm-surge value.  With a constant Av the
+    steady shear under a surface stress tau is du/dz = tau / (rho Av), so the column's top-to-
+    bottom velocity difference is tau h / (rho Av): a 68 m/s Holland wind gives a kinematic stress
+    Gamma_T W = 0.003 (rho_a / rho_o) W^2 = 0.017 m^2/s^2 (calculate_wind_stress.f90:105-137), i.e.
+    6 m/s over 18 m of water at Av = 0.05 and 0.6 m/s at Av = 0.5, on top of the bottom-drag
+    speed sqrt(tau / Cd) = 2.6 m/s where the wind drives flow through the clamped open boundary.
+    At 1e-3 (a calm estuary's value) the surface layer decouples from the column altogether."""
     rng = np.random.default_rng(seed)
     ny = max(6, int(round(math.sqrt(n_cells / aspect))))
     nx = max(6, int(round(n_cells / ny)) - tri_rows)

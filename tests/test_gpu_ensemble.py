@@ -177,3 +177,25 @@ def test_every_launch_variant_gives_the_same_results(gpu_lib, precision):
             for name in FIELDS:
                 a, b = got[name], base[name]
                 assert a.tobytes() == b.tobytes(), (site, v, name)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_strongest_storm_runs_a_full_day(gpu_lib, precision):
+    """The strongest vortex of the ensemble's range (80 hPa, Rmax 20 km, B 1.8: 68 m/s winds)
+    crossing a 30-layer shelf run, 1440 steps of 60 s with the storm forcing on the device, in
+    FP64 and in mixed precision: no failure, currents and surge within storm-surge bounds."""
+    from gom_release_gb300.serve import storm_context
+
+    d = storm_run(3, 4000, 4.0, 30)
+    s = dataclasses.replace(d.meta["storm"], dp=8000.0, b=1.8, rmax=20e3)
+    core = storm_context(gpu_lib, d, precision, [s])
+    umax = etamax = 0.0
+    for hour in range(24):
+        for _ in range(60):
+            core.step_launch()
+        core.step_wait()
+        umax = max(umax, float(np.abs(core.get_field("un_face")).max()))
+        etamax = max(etamax, float(np.abs(core.get_field("eta_cell")).max()))
+    assert core.status().code == 0
+    assert 0.5 < umax < 6.0, umax
+    assert 0.3 < etamax < 6.0, etamax

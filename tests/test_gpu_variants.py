@@ -161,3 +161,24 @@ def test_variant_run_matches_oracle(oracle_so, gpu_lib, name):
         bot = deck.geo["bottom_layer_at_element"]
         wet = np.nonzero(top > bot)[0]
         assert float(np.max(t[wet, top[wet] - 1] - t[wet, bot[wet] - 1])) > 1e-3
+
+
+def test_wind_setup_basin_matches_oracle(oracle_so, gpu_lib):
+    """The closed wind set-up basin of the oracle's known-answer test, 3000 steps on the GPU:
+    the same elevations as the oracle (the PCG sums in another order) and the analytic slope."""
+    from test_oracle_kat import wind_basin
+
+    d = wind_basin()
+    st = initial_state(d)
+    cores = [GomCore(d, lib_path=oracle_so), GomCore(d, lib=gpu_lib)]
+    for c in cores:
+        prepare(c, st)
+        f = HostForcing(d)
+        for it in range(1, 3001):
+            c.set_forcing(f.full(it) if it == 1 else f.step(it))
+            c.step_all()
+    a, b = (c.get_field("eta_cell") for c in cores)
+    assert float(np.abs(a - b).max()) < 1e-12
+    xc = d.geo["x_cell"]
+    slope = np.polyfit(xc, b, 1)[0]
+    assert abs(slope / (1e-4 / (d.params.gravity * 5.0)) - 1.0) < 2e-3

@@ -475,3 +475,48 @@ def test_packed_status_names_the_failing_run(oracle_so):
     st = info.value.status
     assert st.code != 0 and st.entity_kind in (1, 2, 3)
     assert st.run == 1, (st.code, st.site, st.entity, st.entity_kind, st.run)
+
+
+def wind_basin(coriolis_lat=0.0, theta=1.0):
+    """A closed 10 km x 1.5 km basin of 5 m depth, one layer, uniform wind stress 0.1 Pa along x
+    (ana_windp.f90: kinematic stress tau / 1000), no advection, no transport."""
+    from gom_release_gb300.deck import Params, _finish
+    from gom_release_gb300.mesh import RawMesh, square_strip_mesh
+
+    x, y, cells, tq = square_strip_mesh(20, 3, 500.0, 0)
+    raw = RawMesh(x=x, y=y, h=np.full(len(x), 5.0), tri_or_quad=tq, cells=cells)
+    p = Params(dt=120.0, theta=theta, error_tolerance=1e-12, baroclinic_flag=0, trans_sub_iter=1,
+               h_flux_limiter=0, v_flux_limiter=0, advection_flag=0, transport_flag=0, coriolis_lat=coriolis_lat)
+    d = _finish("wind_basin", raw, 1, -10.0, 2.0, p, [], [], [],
+                tide=dict(amplitude=[], period_h=[], phase=[], nodal=[], eq_arg=[], shift=0.0), wind_stress=(0.1, 0.0))
+    d.init_salt_node = np.full((d.n_nodes, 1), 30.0)
+    d.init_temp_node = np.full((d.n_nodes, 1), 20.0)
+    return d
+
+
+def test_wind_setup_of_a_closed_basin(oracle_so):
+    """Steady wind set-up: with one layer and no net flow the face momentum balance is
+    g (h + eta) d eta / dx = tau / rho_o (solve_momentum_equation.f90: wind stress in G1 of the
+    top layer, the free-surface gradient in the normal equation), so eta rises along the wind
+    with slope tau / (rho_o g (h + eta)); the normal velocities vanish."""
+    d = wind_basin()
+    c = GomCore(d, lib_path=oracle_so)
+    prepare(c, initial_state(d))
+    f = HostForcing(d)
+    for it in range(1, 3001):
+        c.set_forcing(f.full(it) if it == 1 else f.step(it))
+        c.step_all()
+    eta = c.get_field("eta_cell")
+    xc = d.geo["x_cell"]
+    tau_k = 0.1 / 1000.0
+    # the slope between neighbouring cells of the middle row against the local depth h + eta
+    row = np.argsort(xc[(d.geo["y_cell"] > 500) & (d.geo["y_cell"] < 1000)])
+    mid = np.nonzero((d.geo["y_cell"] > 500) & (d.geo["y_cell"] < 1000))[0][row]
+    slope = np.diff(eta[mid]) / np.diff(xc[mid])
+    depth = 5.0 + 0.5 * (eta[mid][1:] + eta[mid][:-1])
+    want = tau_k / (d.params.gravity * depth)
+    assert np.all(np.abs(slope / want - 1.0) < 2e-3), float(np.abs(slope / want - 1.0).max())
+    assert float(np.abs(c.get_field("un_face")).max()) < 1e-6
+    # the volume is kept (equal cell areas: the mean elevation stays 0 up to the PCG tolerance
+    # accumulated over the 3000 steps)
+    assert abs(float(eta.mean())) < 1e-8
