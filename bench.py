@@ -32,6 +32,7 @@ ranks of cell-layer-steps divided by the slowest rank's time.
 from __future__ import annotations
 
 import argparse
+import dataclasses
 import ctypes
 import json
 import math
@@ -484,7 +485,11 @@ def bench_ensemble(args):
                           "active_cell_layers": ncl, "pcg_iters_total": core.pcg_iterations_total(),
                           "autotune": tune, "phase_ms": phase_times_in_place(core)}
             if args.day and label == "mixed_packed":
-                res["mixed_packed_day"] = rest_of_day(core, ncl, w + 1 + k)
+                res["mixed_packed_day"] = day = rest_of_day(core, ncl, w + 1 + k)
+                if day["failure"] is not None and 0 <= day["failure"]["run"] < len(decks):
+                    r = day["failure"]["run"]
+                    day["failure"]["run_deck"] = {"cells": decks[r].n_cells, "layers": decks[r].meta["n_layers_run"],
+                                                  "storm": dataclasses.asdict(storms[r])}
             core.close()
         # each run alone, timed over the same steps of the storm as the packed context (warm-up,
         # autotune, one step, then k timed steps)
@@ -575,7 +580,9 @@ def rest_of_day(core, ncl: int, done: int, day_steps: int = 1440) -> dict:
         try:
             t = time_core_steps(core, n)
         except Exception as exc:   # a run failed: the library's error, with the status it read
-            hours.append({"steps": n, "ms_per_step": float("nan"), "status": -1, "error": str(exc)})
+            st = core.status()
+            hours.append({"steps": n, "ms_per_step": float("nan"), "status": -1, "error": str(exc),
+                          "failure": {k: getattr(st, k) for k, _ in st._fields_}})
             break
         st = core.status()
         hours.append({"steps": n, "ms_per_step": t / n * 1e3, "status": int(st.code)})
@@ -586,6 +593,7 @@ def rest_of_day(core, ncl: int, done: int, day_steps: int = 1440) -> dict:
     steps = sum(h["steps"] for h in hours if h["status"] == 0)
     return {"steps": steps, "value": ncl * steps / secs if secs > 0 else 0.0, "failed": any(h["status"] for h in hours),
             "last_step": done + steps, "ms_per_step_by_hour": [round(h["ms_per_step"], 2) for h in hours],
+            "failure": next((dict(h["failure"], error=h["error"]) for h in hours if "failure" in h), None),
             "pcg_iters_total": core.pcg_iterations_total()}
 
 

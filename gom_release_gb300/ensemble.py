@@ -32,9 +32,12 @@ M2_PERIOD_H = 12.42
 
 
 def ensemble_z_grid(max_layers: int = 30):
-    """Shared vertical grid of an ensemble: 1 m levels from -(max_layers + 0.5) m to +6.5 m, room
-    for surge + tide above MSL (no level at MSL, read_main_inp.f90 card C2_1)."""
-    return -float(max_layers) - 0.5, 6.5, max_layers + 7
+    """Shared vertical grid of an ensemble: 1 m levels from -(max_layers + 0.5) m to +10.5 m, room
+    for surge + tide above MSL (no level at MSL, read_main_inp.f90 card C2_1).  The slow, wide
+    vortices of the range (Rmax 40 km at 4-5 m/s) pile more than 6 m of surge against the
+    shallow northern coast; an elevation above the top level stops the run
+    (update_vertical_layers_1.f90)."""
+    return -float(max_layers) - 0.5, 10.5, max_layers + 11
 
 
 @dataclasses.dataclass
