@@ -20,7 +20,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from .mesh import (RawMesh, build_geometry, bottom_layers, find_elements_and_faces,
+from .mesh import (RawMesh, build_geometry, coastal_strip, bottom_layers, find_elements_and_faces,
                    fourier_noise, square_strip_mesh)
 
 PI = 3.141592653589793          # mod_global_variables.f90: pi
@@ -275,18 +275,38 @@ def estuary(nx: int = 600, ny: int = 250, dx: float = 100.0, tri_rows: int = 4, 
     """Baroclinic estuary: ocean open boundary on the west edge (M2 0.6 m, S = 35, T = 18),
     river of 500 m3/s at S = 0, T = 24 over ``n_river`` faces of the east edge (channel head),
     initial salinity linear along the channel, TVD limiter on, turbulence closure on
-    (Pacanowski-Philander), uniform wind stress 0.1 Pa at a seeded direction.  The seeded sinusoidal coastline is a shoal along y = yc(x) carved into
-    the bathymetry (the mesh boundary itself is straight)."""
+    (Pacanowski-Philander), uniform wind stress 0.1 Pa at a seeded direction.
+
+    The north coast is a seeded sinusoid: the ``tri_rows`` rows of triangles between the squares
+    and the coast follow it (strip height 0.7-1.3 times the equilateral one, so every triangle is
+    oblique and acute).  Along the coast an intertidal flat six cells wide rises from 0.9 m to
+    0.15 m below MSL, so a band of cells falls dry and floods again with the 0.6 m tide; seaward
+    of the flat the bed deepens to the estuary's along-channel profile."""
     rng = np.random.default_rng(seed)
     x, y, cells, tq = square_strip_mesh(nx, ny, dx, tri_rows)
     lx = nx * dx
-    ly = float(y.max())
-    lam = rng.uniform(0.2, 0.5) * lx
+    y0 = ny * dx
+    strip = tri_rows * dx * math.sqrt(3.0) / 2.0
+    # the coast's wavelength stays at least 40 cells, so the strip varies slowly over a cell
+    lam = max(rng.uniform(0.2, 0.5) * lx, 40.0 * dx)
     phase = rng.uniform(0, 2 * math.pi)
-    yc = ly * (0.8 + 0.08 * np.sin(2 * math.pi * x / lam + phase))
-    shoal = np.clip((yc - y) / (0.25 * ly), 0.0, 1.0)
-    h = 2.0 + (3.0 + 15.0 * (1.0 - x / lx)) * (0.25 + 0.75 * shoal)
-    h = h + fourier_noise(x, y, rng, lam_min=800.0, lam_max=6000.0, amplitude=0.5)
+
+    def coast(xx):
+        return y0 + strip * (1.0 + 0.3 * np.sin(2 * math.pi * xx / lam + phase))
+
+    if tri_rows > 0:
+        y = coastal_strip(x, y, y0, strip, coast)
+    yc = coast(x) if tri_rows > 0 else np.full_like(x, y0)
+    ly = float(y.max())
+    # depth: the along-channel profile of the estuary seaward of the flat, the flat from 0.9 m
+    # to 0.15 m at the coast (land above MSL makes the reference stop: a wet cell whose sides
+    # are all dry, update_vertical_layers_1.f90)
+    flat = 6.0 * dx
+    dist = np.maximum(yc - y, 0.0)
+    h_deep = 4.0 + 15.0 * (1.0 - x / lx)
+    w = np.clip((dist - flat) / (0.25 * ly), 0.0, 1.0) ** 0.7
+    h = np.where(dist < flat, 0.15 + 0.75 * dist / flat, 0.9 + (h_deep - 0.9) * w)
+    h = h + fourier_noise(x, y, rng, lam_min=800.0, lam_max=6000.0, amplitude=0.5) * w
     raw = RawMesh(x=x, y=y, h=h, tri_or_quad=tq, cells=cells)
     params = Params(dt=dt, theta=0.6, error_tolerance=1e-10, baroclinic_flag=1, ana_density=0,
                     trans_sub_iter=trans_sub_iter, h_flux_limiter=1, v_flux_limiter=1,
@@ -302,6 +322,9 @@ def estuary(nx: int = 600, ny: int = 250, dx: float = 100.0, tri_rows: int = 4, 
     hmax = float(h.max())
     z_bottom = -math.ceil(hmax + 1.0)
     z_top = 3.0
+    # no level within a quarter layer of MSL (read_main_inp.f90 card C2_1 rejects a level at MSL)
+    while np.any(np.abs(uniform_z_levels(z_bottom, z_top, n_layers)[0]) < 0.25 * (z_top - z_bottom) / n_layers):
+        z_top += 0.25
     alpha = rng.uniform(0.0, 2.0 * math.pi)
     tau = 0.1
     deck = _finish("estuary", raw, n_layers, z_bottom, z_top, params, ob_pairs, q_pairs, q_portion,

@@ -91,6 +91,19 @@ def square_strip_mesh(nx: int, ny: int, dx: float, tri_rows: int) -> tuple[np.nd
     return x, y, np.concatenate(cells).astype(np.int32), np.concatenate(tq)
 
 
+def coastal_strip(x: np.ndarray, y: np.ndarray, y0: float, strip: float, coast) -> np.ndarray:
+    """The strip nodes (y > y0) of ``square_strip_mesh`` moved so that the strip's north edge
+    follows ``coast(x)`` instead of the straight line y0 + strip: each node keeps its fraction of
+    the strip height.  With coast(x) - y0 between 0.7 and 1.3 strip heights and varying slowly
+    over one cell, every triangle stays acute, so its circumcentre stays inside it and the
+    centres of neighbouring cells stay on the perpendicular bisector of their shared side."""
+    out = y.copy()
+    m = y > y0 + 1e-9
+    frac = (y[m] - y0) / strip
+    out[m] = y0 + frac * (coast(x[m]) - y0)
+    return out
+
+
 def fourier_noise(x: np.ndarray, y: np.ndarray, rng: np.random.Generator, n_modes: int = 8,
                   lam_min: float = 2000.0, lam_max: float = 15000.0, amplitude: float = 1.0) -> np.ndarray:
     """Seeded smooth noise: ``n_modes`` plane waves with wavelengths in [lam_min, lam_max] whose
