@@ -207,14 +207,14 @@ def time_phases(deck, st_snapshot, lib, forcing, torch, reps: int = 3) -> dict:
 TR_SOLVE_BYTES_PER_CELL_LAYER = {"fp64": 144, "mixed": 72}
 
 
-# DRAM bytes per launch of the transport solve on the full estuary (1,363,169 active
-# cell-layers): dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture on the medium
-# estuary (349,122 active cell-layers), scaled by the active cell-layers (the solve reads and
-# writes a fixed set of arrays per wet cell-layer, so its traffic grows in proportion)
-SOLVE_TRAFFIC_FULL = {
-    "k_tr_solve fp64": 5.3638e8,
-    "k_tr_solve mixed": 3.5127e8,
-    "k_tr_rows64_list + k_tr_thomas_col fp64": 6.2223e8,
+# DRAM bytes per active cell-layer and launch of the transport solve: dram__bytes_read.sum +
+# dram__bytes_write.sum of one ncu capture of the solve on the medium estuary (--size medium) over
+# that case's active cell-layers.  The solve reads and writes a fixed set of arrays per wet
+# cell-layer, so a launch's traffic is this figure times the workload's active cell-layers.
+SOLVE_TRAFFIC_PER_CELL_LAYER = {
+    "k_tr_solve fp64": 393.5,
+    "k_tr_solve mixed": 257.7,
+    "k_tr_rows64_list + k_tr_thomas_col fp64": 460.7,
 }
 
 
@@ -227,9 +227,10 @@ SOLVE_FP64_INSTR_PER_CELL_LAYER = {
 }
 
 
-def solve_traffic(kernel: str, precision: str, size: str):
-    """ncu DRAM bytes per launch of the transport solve for the full estuary, or None."""
-    return SOLVE_TRAFFIC_FULL.get(f"{kernel} {precision}") if size == "full" else None
+def solve_traffic(kernel: str, precision: str, ncl: int):
+    """ncu DRAM bytes per launch of the transport solve on a workload of ncl active cell-layers."""
+    per = SOLVE_TRAFFIC_PER_CELL_LAYER.get(f"{kernel} {precision}")
+    return per * ncl if per is not None else None
 
 
 def phase_bytes(deck, ncl: int, pcg_iters: float) -> dict:
@@ -818,18 +819,26 @@ def main():
              gamma_t=run.forcing.gamma_t)
     pcg_mean = (pcg_total / max(1, args.warmup + args.steps))
     peak, peak_kind = measured_peak()
-    # dominant kernel: the transport column solve (one launch per subcycle), timed alone
-    solve_ms = run.core.profile_kernel(run.core.KERNEL_TRANSPORT_SOLVE, reps=5)
-    solve_bytes = TR_SOLVE_BYTES_PER_CELL_LAYER[args.precision] * ncl
+    # dominant kernel: the transport column solve (one launch per subcycle), timed alone; with the
+    # ELM transport (no TVD solve) the ELM walk of the advection instead
+    tvd = deck.params.transport_solver != 2
+    if tvd:
+        solve_ms = run.core.profile_kernel(run.core.KERNEL_TRANSPORT_SOLVE, reps=5)
+        solve_bytes = TR_SOLVE_BYTES_PER_CELL_LAYER[args.precision] * ncl
+        # FP64 solve variant 3 runs the solve as two kernels (rows per wet cell-layer, column Thomas)
+        list_solve = args.precision == "fp64" and tune is not None and tune[2] == 3
+        solve_kernel = "k_tr_rows64_list + k_tr_thomas_col" if list_solve else "k_tr_solve"
+        traffic = solve_traffic(solve_kernel, args.precision, ncl)
+        kernel_label = f"transport solve, one subcycle ({solve_kernel})"
+    else:
+        solve_ms = run.core.profile_kernel(run.core.KERNEL_ELM_WALK, reps=5)
+        solve_bytes = PHASE_BYTES_PER_CELL_LAYER["advection"] * ncl
+        solve_kernel, traffic, kernel_label = "ELM walk", None, "ELM walk of the advection (k_elm_faces / k_elm_list)"
     achieved = solve_bytes / (solve_ms * 1e-3) / 1e9
-    # FP64 solve variant 3 runs the solve as two kernels (rows per wet cell-layer, column Thomas)
-    list_solve = args.precision == "fp64" and tune is not None and tune[2] == 3
-    solve_kernel = "k_tr_rows64_list + k_tr_thomas_col" if list_solve else "k_tr_solve"
-    traffic = solve_traffic(solve_kernel, args.precision, args.size)
     # FP64 roofline of the same launch: FP64 instructions per second against the measured issue
     # peak (the library's FMA-chain kernel; an FMA is one instruction and two flops)
     roof_fp64 = None
-    if args.precision == "fp64":
+    if args.precision == "fp64" and tvd:
         from gom_release_gb300.core import measure_fp64_peak
         peak_gflops = measure_fp64_peak(lib)
         instr = SOLVE_FP64_INSTR_PER_CELL_LAYER[solve_kernel] * ncl
@@ -873,7 +882,7 @@ def main():
             "autotune": tune,
             "pcg_iters_mean": pcg_mean,
         },
-        "roofline": {"bound": "hbm", "kernel": f"transport solve, one subcycle ({solve_kernel})",
+        "roofline": {"bound": "hbm", "kernel": kernel_label,
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind, "traffic": traffic, "algorithmic_bytes": solve_bytes,
                      "ms_per_launch": solve_ms,

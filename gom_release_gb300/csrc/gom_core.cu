@@ -100,6 +100,11 @@ int set_cuda_error(gom_ctx *c, cudaError_t e, const char *where) {
         if (_e != cudaSuccess) return set_cuda_error(c, _e, #call);      \
     } while (0)
 
+// Host-side setup writes (zeroing, uploads) go through the legacy default stream, which does not
+// order with the context's non-blocking streams; each one is completed before the call returns,
+// so no kernel of the context can run before (or under) it.
+cudaError_t legacy_done() { return cudaStreamSynchronize(0); }
+
 template <typename T> cudaError_t dalloc(gom_ctx *c, T **p, size_t n) {
     if (n == 0) n = 1;
     cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
@@ -107,6 +112,7 @@ template <typename T> cudaError_t dalloc(gom_ctx *c, T **p, size_t n) {
         c->allocs.push_back(*p);
         c->bytes += n * sizeof(T);
         e = cudaMemset(*p, 0, n * sizeof(T));
+        if (e == cudaSuccess) e = legacy_done();
     }
     return e;
 }
@@ -159,6 +165,7 @@ template <typename T> cudaError_t upload(gom_ctx *c, const T **dst, const T *src
     if (e != cudaSuccess) return e;
     if (src) e = cudaMemcpy(p, src, n * sizeof(T), cudaMemcpyHostToDevice);
     else if (required) e = cudaErrorInvalidValue;
+    if (e == cudaSuccess) e = legacy_done();   // the DMA of a pageable copy may still be running
     *dst = p;
     return e;
 }
@@ -592,6 +599,7 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
     if (e == cudaSuccess) {
         const double one[8] = {0.0, 1.0, 1.0, 0.0, 0.0, 0.0, 0.0, 0.0};
         e = cudaMemcpy(c->f_scal, one, sizeof(one), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = legacy_done();
     }
     Forcing &F = c->x.f;
     F.scal = c->f_scal;
@@ -1084,6 +1092,8 @@ int gom_profile_kernel(gom_ctx *c, int32_t which, int32_t reps, double *ms_per_l
     case GOM_KERNEL_ELM_WALK: run = GOM_PHASE(launch_elm_walk_only); break;
     case GOM_KERNEL_MOMENTUM: run = GOM_PHASE(launch_momentum_columns_only); break;
     case GOM_KERNEL_TRANSPORT_SOLVE:
+        // the TVD solve exists only when the context runs the TVD transport
+        if (!c->hp.transport_flag || c->hp.transport_solver == 2) return GOM_E_ARG;
         CK(c->mixed ? launch_transport(c->xf) : launch_transport(c->x));   // coefficients and limiter
         run = GOM_PHASE(launch_tr_solve_only);
         break;
@@ -1226,8 +1236,10 @@ int gom_set_storms(gom_ctx *c, int32_t n_storms, const gom_storm *storms, double
         CK(dalloc(c, &c->storm_wv, (size_t)c->d.n_nodes));
     }
     CK(cudaMemcpy(c->d_storms, storms, sizeof(gom_storm) * n_storms, cudaMemcpyHostToDevice));
+    CK(legacy_done());
     const double scal0[1] = {elapsed_time};
     CK(cudaMemcpy(c->f_scal, scal0, sizeof(double), cudaMemcpyHostToDevice));
+    CK(legacy_done());
     c->n_storms = n_storms;
     // the captured step gains the forcing kernels: capture again on the next launch
     drop_graphs(c);
@@ -1246,6 +1258,7 @@ template <typename T> cudaError_t series_upload(gom_ctx *c, const T **dst, const
     c->series_allocs.push_back(p);
     c->series_bytes += n * sizeof(T);
     e = src ? cudaMemcpy(p, src, n * sizeof(T), cudaMemcpyHostToDevice) : cudaMemset(p, 0, n * sizeof(T));
+    if (e == cudaSuccess) e = legacy_done();
     *dst = p;
     return e;
 }
@@ -1349,6 +1362,7 @@ int gom_set_boundary_series(gom_ctx *c, const gom_boundary_series *bs) {
     // the device clock: elapsed time and spin-up of the last step, its julian day and step number
     const double scal[8] = {bs->step * c->hp.dt, 1.0, 1.0, 0.0, bs->julian_day, (double)bs->step, 0.0, 0.0};
     CK(cudaMemcpy(c->f_scal, scal, sizeof(scal), cudaMemcpyHostToDevice));
+    CK(legacy_done());
     c->has_series = true;
     drop_graphs(c);   // the captured step gains the series kernels
     return GOM_OK;
@@ -1376,6 +1390,7 @@ int gom_set_stations(gom_ctx *c, int32_t hloc, int32_t n_stations, const int32_t
         cudaMalloc(&c->st_out, sizeof(double) * rec * n_stations) != cudaSuccess)
         return GOM_E_NOMEM;
     CK(cudaMemcpy(c->st_ids, ids, sizeof(int) * n_stations, cudaMemcpyHostToDevice));
+    CK(legacy_done());
     c->st_n = n_stations;
     c->bytes += (size_t)n_stations * (4 + 8 * rec);
     return GOM_OK;

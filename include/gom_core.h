@@ -549,8 +549,9 @@ int gom_copy_run(struct gom_ctx *dst, int32_t dst_run, struct gom_ctx *src, int3
  * next step before it is read. */
 #define GOM_KERNEL_ELM_WALK 1         /* the per-face ELM walk                              */
 #define GOM_KERNEL_MOMENTUM 2         /* the per-face momentum columns                      */
-#define GOM_KERNEL_TRANSPORT_SOLVE 3  /* one transport subcycle's column solve (after the   */
-                                      /* phase has run once to form its coefficients)      */
+#define GOM_KERNEL_TRANSPORT_SOLVE 3  /* one TVD transport subcycle's column solve, its    */
+                                      /* coefficients formed first (GOM_E_ARG when the     */
+                                      /* context has no TVD transport)                     */
 int gom_profile_kernel(struct gom_ctx *ctx, int32_t which, int32_t reps, double *ms_per_launch);
 
 /* Device memory the context holds (bytes), for admission by memory budget when many contexts
