@@ -74,3 +74,31 @@ def test_barrier_wait_expires_and_device_stays_usable(gpu_lib):
     r = Run(deck2, GomCore(deck2, lib=gpu_lib), initial_state(deck2))
     r.advance(2)
     assert all(0 < i < deck2.params.max_iteration_pcg for i in r.pcg_iters)
+
+
+def test_contexts_created_one_after_another_give_identical_runs(gpu_lib):
+    """Context set-up zeroes and uploads its arrays through the legacy default stream while its
+    kernels run on a non-blocking stream: every set-up write must have finished before the first
+    kernel.  When they were not, a context created after another one (its memory recycled, its
+    set-up kernels racing the zeroing) followed another trajectory from the second step on; two
+    contexts of one 480k-cell basin, one after the other, must now agree bit for bit."""
+    import math
+
+    from gom_release_gb300.deck import HostForcing, tidal_basin
+
+    ny = int(round(math.sqrt(480_000 / 1.5)))
+    deck = tidal_basin(nx=int(round(480_000 / ny)), ny=ny, dx=250.0, n_layers=20, dt=60.0)
+    runs = []
+    for _ in range(2):
+        c = GomCore(deck, lib=gpu_lib)
+        p = deck.params
+        c.cold_start(p.ref_salt, p.ref_temp, p.av_0, p.kv_0)
+        c.step("density")
+        hf = HostForcing(deck)
+        for it in range(1, 6):
+            c.set_forcing(hf.step(it))
+            c.step_all()
+        runs.append({n: c.get_field(n) for n in ("eta_cell", "un_face", "salt_cell")})
+        c.close()
+    for n in runs[0]:
+        assert np.array_equal(runs[0][n], runs[1][n]), n
