@@ -56,8 +56,10 @@ enum TuneSite { TUNE_ELM = 0, TUNE_MOMENTUM, TUNE_TR_SOLVE, TUNE_TR_LIMITER, TUN
 // TUNE_TR_SOLVE: FP64 column solve with 128 / 64 / 256 threads, or (3) rows per listed wet
 // cell-layer then one thread per column (the FP32 path's form); TUNE_TR_LIMITER: column kernels
 // with 128 / 64 / 256 threads, or (3) the per-(entity, layer) list kernels (the only form of the
-// FP32 path).  Variant 3 changes nothing in an FP32 context.
-constexpr int TUNE_VARIANTS[TUNE_COUNT] = {7, 4, 4, 4};
+// FP32 path), or the two mixed: (4) cell sums per listed wet cell-layer with the face limiter per
+// face, (5) cell sums per column (64 threads) with the face limiter per face-layer, (6) variant 1
+// with the face coefficients per face-layer.  Variants 3-6 change nothing in an FP32 context.
+constexpr int TUNE_VARIANTS[TUNE_COUNT] = {7, 4, 4, 7};
 
 // packed runs a free-surface solve holds (one barrier pair and one state per run)
 constexpr int PCG_MAX_RUNS = 256;

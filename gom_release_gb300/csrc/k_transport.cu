@@ -292,8 +292,8 @@ template <typename R> __device__ void limiter_column(const TArgs<R> &a, int i) {
     if (tl == 0) return;
     int nvl = tl - b + 1;
     int tq = g.tri_or_quad[i - 1];
-    int fj[4], nb[4], sg[4];
-    bool open[4];
+    int fj[4] = {0, 0, 0, 0}, nb[4] = {0, 0, 0, 0}, sg[4] = {0, 0, 0, 0};
+    bool open[4] = {false, false, false, false};
     for (int l = 1; l <= tq; ++l) {
         fj[l - 1] = g.cell_face(l, i);
         nb[l - 1] = g.cell_adj(l, i);
@@ -303,37 +303,66 @@ template <typename R> __device__ void limiter_column(const TArgs<R> &a, int i) {
     R last1[2] = {R(0.0), R(0.0)}, last2[2] = {R(0.0), R(0.0)};
     for (int k = b; k <= tl; ++k) {
         R s1a[2] = {R(0.0), R(0.0)}, s2a[2] = {R(0.0), R(0.0)}, s1[2] = {R(0.0), R(0.0)}, s2[2] = {R(0.0), R(0.0)};
-        for (int tr = 0; tr < a.ntr; ++tr) {
-            R ck = a.con[ic(k, i, tr, L, NC)];
+        // every operand of the layer is loaded before any is used: the neighbours' concentrations
+        // whatever the sign of their flux (the selection below reads only those of inflow faces),
+        // so the loads of a layer overlap instead of waiting on the flux test
+        R ckv[2] = {R(0), R(0)}, cdn[2] = {R(0), R(0)}, cup[2] = {R(0), R(0)}, cnb[4][2], q2v[4];
+        const R qlo = k > b ? a.w.qi[ix0(k - 1, i, L)] : R(0), qhi = k < tl ? a.w.qi[ix0(k, i, L)] : R(0);
+#pragma unroll
+        for (int tr = 0; tr < 2; ++tr) {
+            if (tr >= a.ntr) break;
+            ckv[tr] = a.con[ic(k, i, tr, L, NC)];
+            if (k > b) cdn[tr] = a.con[ic(k - 1, i, tr, L, NC)];
+            if (k < tl) cup[tr] = a.con[ic(k + 1, i, tr, L, NC)];
+        }
+#pragma unroll
+        for (int l = 0; l < 4; ++l) {
+            q2v[l] = R(0);
+            cnb[l][0] = cnb[l][1] = R(0);
+            if (l < tq && open[l]) {
+                q2v[l] = flip(a.w.qj[ix(k, fj[l], L)], sg[l]);
+#pragma unroll
+                for (int tr = 0; tr < 2; ++tr)
+                    if (tr < a.ntr) cnb[l][tr] = nb[l] > 0 ? a.con[ic(k, nb[l], tr, L, NC)] : oqb_value(a, i, k, tr);
+            }
+        }
+#pragma unroll
+        for (int tr = 0; tr < 2; ++tr) {
+            if (tr >= a.ntr) break;
+            R ck = ckv[tr];
             if (nvl != 1) {
                 if (k == b) {
-                    R rt2 = pos_part(a.w.qi[ix0(k, i, L)]);
-                    s1a[tr] = rt2 * (ck - a.con[ic(k + 1, i, tr, L, NC)]);
+                    R rt2 = pos_part(qhi);
+                    s1a[tr] = rt2 * (ck - cup[tr]);
                     s2a[tr] = rt2;
                 } else if (k == tl) {
-                    R rt1 = pos_part(a.w.qi[ix0(k - 1, i, L)]);
-                    s1a[tr] = rt1 * (ck - a.con[ic(k - 1, i, tr, L, NC)]);
+                    R rt1 = pos_part(qlo);
+                    s1a[tr] = rt1 * (ck - cdn[tr]);
                     s2a[tr] = rt1;
                 } else {
-                    R rt1 = pos_part(a.w.qi[ix0(k - 1, i, L)]);
-                    R rt2 = pos_part(a.w.qi[ix0(k, i, L)]);
-                    s1a[tr] = rt1 * (ck - a.con[ic(k - 1, i, tr, L, NC)]) + rt2 * (ck - a.con[ic(k + 1, i, tr, L, NC)]);
+                    R rt1 = pos_part(qlo);
+                    R rt2 = pos_part(qhi);
+                    s1a[tr] = rt1 * (ck - cdn[tr]) + rt2 * (ck - cup[tr]);
                     s2a[tr] = rt1 + rt2;
                 }
             }
         }
-        for (int l = 0; l < tq; ++l) {
-            if (!open[l]) continue;
-            R q2 = flip(a.w.qj[ix(k, fj[l], L)], sg[l]);
+#pragma unroll
+        for (int l = 0; l < 4; ++l) {
+            if (l >= tq || !open[l]) continue;
+            R q2 = q2v[l];
             if (is_neg(q2)) {
-                for (int tr = 0; tr < a.ntr; ++tr) {
-                    R cik = nb[l] > 0 ? a.con[ic(k, nb[l], tr, L, NC)] : oqb_value(a, i, k, tr);
-                    s1[tr] = s1[tr] + fabs(q2) * (a.con[ic(k, i, tr, L, NC)] - cik);
+#pragma unroll
+                for (int tr = 0; tr < 2; ++tr) {
+                    if (tr >= a.ntr) break;
+                    s1[tr] = s1[tr] + fabs(q2) * (ckv[tr] - cnb[l][tr]);
                     s2[tr] = s2[tr] + fabs(q2);
                 }
             }
         }
-        for (int tr = 0; tr < a.ntr; ++tr) {
+#pragma unroll
+        for (int tr = 0; tr < 2; ++tr) {
+            if (tr >= a.ntr) break;
             s1a[tr] = s1a[tr] + s1[tr];
             s2a[tr] = s2a[tr] + s2[tr];
             a.w.sa1[((long)tr * NC + i - 1) * L + k - 1] = s1a[tr];
@@ -343,7 +372,9 @@ template <typename R> __device__ void limiter_column(const TArgs<R> &a, int i) {
         }
     }
     // :806-840 (Q_ik_theta at the top interface is never assigned: 0 -> first branch)
-    for (int tr = 0; tr < a.ntr; ++tr) {
+#pragma unroll
+    for (int tr = 0; tr < 2; ++tr) {
+        if (tr >= a.ntr) break;
         R *psi = a.w.psii + (long)tr * NC * (L + 1);
         for (int k = b; k <= tl - 1; ++k) {
             R qm = (k - 1 >= b) ? a.w.qi[ix0(k - 1, i, L)] : R(0.0);
@@ -523,16 +554,40 @@ template <typename R> __device__ __forceinline__ void limiter_face_layer(const T
         if (c2 != 0 && t2 != 0 && k >= b2 && k <= t2 && !is_pos(Q)) writer = c2;   // -Q >= 0
         else if (t1 != 0 && k >= b1 && k <= t1 && !is_neg(Q)) writer = c1;        // Q >= 0
     }
-    for (int tr = 0; tr < a.ntr; ++tr) {
+    const R phi = a.w.phij[t];
+    // the operands of both possible writers are loaded before the writer is known, so the loads
+    // overlap the flux test instead of following it
+    const bool in1 = t1 != 0 && k >= b1 && k <= t1, in2 = c2 != 0 && t2 != 0 && k >= b2 && k <= t2;
+    R con1[2] = {R(0), R(0)}, con2[2] = {R(0), R(0)}, s1w[2] = {R(0), R(0)}, s2w[2] = {R(0), R(0)},
+      s1o[2] = {R(0), R(0)}, s2o[2] = {R(0), R(0)}, cob[2] = {R(0), R(0)};
+#pragma unroll
+    for (int tr = 0; tr < 2; ++tr) {
+        if (tr >= a.ntr) break;
+        con1[tr] = a.con[ic(k, c1, tr, L, NC)];
+        if (c2 > 0) con2[tr] = a.con[ic(k, c2, tr, L, NC)];
+        else cob[tr] = oqb_value(a, c1, k, tr);
+        if (in1) {
+            s1w[tr] = a.w.sa1[((long)tr * NC + c1 - 1) * L + k - 1];
+            s2w[tr] = a.w.sa2[((long)tr * NC + c1 - 1) * L + k - 1];
+        }
+        if (in2) {
+            s1o[tr] = a.w.sa1[((long)tr * NC + c2 - 1) * L + k - 1];
+            s2o[tr] = a.w.sa2[((long)tr * NC + c2 - 1) * L + k - 1];
+        }
+    }
+#pragma unroll
+    for (int tr = 0; tr < 2; ++tr) {
+        if (tr >= a.ntr) break;
         R v;
         if (writer != 0) {
-            int i = writer;
-            int other = (writer == c1) ? c2 : c1;
-            R cik = other > 0 ? a.con[ic(k, other, tr, L, NC)] : oqb_value(a, i, k, tr);
-            R rtemp = a.w.sa2[((long)tr * NC + i - 1) * L + k - 1] * (cik - a.con[ic(k, i, tr, L, NC)]);
-            v = limited_ratio(a.p.h_flux_limiter, a.w.phij[t], a.w.sa1[((long)tr * NC + i - 1) * L + k - 1], rtemp);
+            // writer c1: the other side is c2 or the boundary value; writer c2: the other is c1
+            const bool w1 = writer == c1;
+            const R cik = w1 ? (c2 > 0 ? con2[tr] : cob[tr]) : con1[tr];
+            const R cw = w1 ? con1[tr] : con2[tr];
+            R rtemp = (w1 ? s2w[tr] : s2o[tr]) * (cik - cw);
+            v = limited_ratio(a.p.h_flux_limiter, phi, w1 ? s1w[tr] : s1o[tr], rtemp);
         } else {
-            v = phi_limit(a.p.h_flux_limiter, a.w.phij[t], R(1.0));
+            v = phi_limit(a.p.h_flux_limiter, phi, R(1.0));
         }
         a.w.psij[(long)tr * g.NF * L + t] = v;
     }
@@ -1231,9 +1286,15 @@ template <typename R> cudaError_t launch_transport(const LaunchT<R> &x) {
     // FP64 limiter variant 3: face coefficients and limiters per (entity, layer) from the wet
     // cell-layer list, as the FP32 path always runs them (same expressions, same results)
     const bool flat_lim = sizeof(R) == sizeof(float) || (x.tune[TUNE_TR_LIMITER] == 3 && x.w.cl_list);
+    // FP64 limiter variants 4 and 5 mix the forms: 4 the cell sums per listed wet cell-layer with
+    // the face limiter per face, 5 the cell sums per column with the face limiter per face-layer
+    const bool list_sums = !flat_lim && x.tune[TUNE_TR_LIMITER] == 4 && x.w.cl_list;
+    const bool flat_faces = !flat_lim && x.tune[TUNE_TR_LIMITER] == 5;
+    // variant 6: the column limiter of variant 1 with the face coefficients per face-layer
+    const bool flat_coef = flat_lim || x.tune[TUNE_TR_LIMITER] == 6;
     // FP64 solve variant 3: rows per listed wet cell-layer, then one thread per column
     const bool list_solve = sizeof(R) == sizeof(double) && x.tune[TUNE_TR_SOLVE] == 3 && x.w.cl_list && x.w.tr_a;
-    if (flat_lim || list_solve) {
+    if (flat_lim || list_solve || list_sums) {
         cudaError_t e = build_cell_layer_list(g, x.s.top_cell, x.w.cl_off, x.w.cl_bsum, x.w.cl_list, x.w.cl_count,
                                               x.stream);
         if (e != cudaSuccess) return e;
@@ -1241,7 +1302,8 @@ template <typename R> cudaError_t launch_transport(const LaunchT<R> &x) {
     const int list_grid = x.num_sms * 8;   // grid-stride over the wet cell-layers
     bool lim = p.h_flux_limiter > 0 || p.v_flux_limiter > 0;
     const int bs_solve = x.tune[TUNE_TR_SOLVE] == 1 ? 64 : x.tune[TUNE_TR_SOLVE] == 2 ? 256 : 128;
-    const int bs_lim = x.tune[TUNE_TR_LIMITER] == 1 ? 64 : x.tune[TUNE_TR_LIMITER] == 2 ? 256 : 128;
+    const int bs_lim = x.tune[TUNE_TR_LIMITER] == 1 || x.tune[TUNE_TR_LIMITER] >= 5 ? 64
+                       : x.tune[TUNE_TR_LIMITER] == 2 ? 256 : 128;
     R *cur = x.w.con, *nxt = x.w.con2;
     for (int sub = 0; sub < a.Nt; ++sub) {
         a.sub = sub;
@@ -1249,7 +1311,7 @@ template <typename R> cudaError_t launch_transport(const LaunchT<R> &x) {
         a.con_new = nxt;
         if (g.NOB + g.NQB > 0) k_tr_bc<<<blocks_for(g.NOB + g.NQB, 128), 128, 0, x.stream>>>(a);
         a.changed_only = sub > 0;
-        if (flat_lim)
+        if (flat_coef)
             k_tr_face_coef_flat<<<blocks_for((long)g.NF * L, 256), 256, 0, x.stream>>>(a);
         else
             k_tr_face_coef<<<blocks_for(g.NF, 128), 128, 0, x.stream>>>(a);
@@ -1263,8 +1325,16 @@ template <typename R> cudaError_t launch_transport(const LaunchT<R> &x) {
                 k_tr_vpsi_list<<<list_grid, bs_lim, 0, x.stream>>>(a);
                 k_tr_limiter_faces_flat<<<blocks_for((long)g.NF * L, 256), 256, 0, x.stream>>>(a);
             } else {
-                k_tr_limiter_cells<<<blocks_for(g.NC, bs_lim), bs_lim, 0, x.stream>>>(a);
-                k_tr_limiter_faces<<<blocks_for(g.NF, 128), 128, 0, x.stream>>>(a);
+                if (list_sums) {
+                    k_tr_sums_list<<<list_grid, bs_lim, 0, x.stream>>>(a);
+                    k_tr_vpsi_list<<<list_grid, bs_lim, 0, x.stream>>>(a);
+                } else {
+                    k_tr_limiter_cells<<<blocks_for(g.NC, bs_lim), bs_lim, 0, x.stream>>>(a);
+                }
+                if (flat_faces)
+                    k_tr_limiter_faces_flat<<<blocks_for((long)g.NF * L, 256), 256, 0, x.stream>>>(a);
+                else
+                    k_tr_limiter_faces<<<blocks_for(g.NF, 128), 128, 0, x.stream>>>(a);
             }
         }
         if constexpr (sizeof(R) == sizeof(float)) {

@@ -222,10 +222,13 @@ def test_elm_transport_matches_oracle(oracle_so, gpu_lib, warm_steps):
         assert float(np.abs(a - b).max()) / scale < FIELD_RTOL, name
 
 
-@pytest.mark.parametrize("choice", [[0, 0, 3, 0], [0, 0, 0, 3], [0, 0, 3, 3]], ids=["solve", "limiter", "both"])
+@pytest.mark.parametrize("choice", [[0, 0, 3, 0], [0, 0, 0, 3], [0, 0, 3, 3], [0, 0, 3, 4], [0, 0, 0, 5],
+                                    [0, 0, 3, 6]], ids=["solve", "limiter", "both", "list-sums", "flat-faces",
+                                                        "flat-coef"])
 def test_list_form_transport_matches_oracle(deck, oracle_so, gpu_lib, choice):
     """The FP64 transport's list-form variants (rows and limiter sums per wet cell-layer, limiter
-    per face-layer) give the oracle's results bit for bit on the oracle's state."""
+    per face-layer, and the two mixed limiter forms) give the oracle's results bit for bit on the
+    oracle's state."""
     st = initial_state(deck)
     ref = GomCore(deck, lib_path=oracle_so)
     gpu = GomCore(deck, lib=gpu_lib)
