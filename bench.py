@@ -214,7 +214,7 @@ TR_SOLVE_BYTES_PER_CELL_LAYER = {"fp64": 144, "mixed": 72}
 SOLVE_TRAFFIC_PER_CELL_LAYER = {
     "k_tr_solve fp64": 393.5,
     "k_tr_solve mixed": 257.7,
-    "k_tr_rows64_list + k_tr_thomas_col fp64": 460.7,
+    "k_tr_rows64_list + k_tr_thomas_col fp64": 436.4,
 }
 
 
