@@ -160,6 +160,106 @@ module gom_core_abi
      integer(c_int32_t) :: run
   end type
 
+  type, bind(c) :: gom_series
+     integer(c_int32_t) :: n_series
+     integer(c_int32_t) :: reserved
+     type(c_ptr) :: start
+     type(c_ptr) :: time
+     type(c_ptr) :: value
+  end type
+
+  type, bind(c) :: gom_boundary_series
+     real(c_double) :: julian_day
+     real(c_double) :: tide_spinup_period
+     real(c_double) :: baroclinic_spinup_period
+     integer(c_int32_t) :: step
+     integer(c_int32_t) :: reference_diff_days
+     integer(c_int32_t) :: tide_spinup
+     integer(c_int32_t) :: baroclinic_spinup
+     integer(c_int32_t) :: q_interp_method
+     integer(c_int32_t) :: n_harmonic
+     type(c_ptr) :: ob_eta_type
+     type(c_ptr) :: ob_harmonic_id
+     type(c_ptr) :: ob_eta_id
+     type(c_ptr) :: ob_salt_id
+     type(c_ptr) :: ob_temp_id
+     type(c_ptr) :: qb_q_id
+     type(c_ptr) :: qb_salt_id
+     type(c_ptr) :: qb_temp_id
+     type(c_ptr) :: qb_portion
+     type(c_ptr) :: harmonic_start
+     type(c_ptr) :: amplitude
+     type(c_ptr) :: period_h
+     type(c_ptr) :: nodal
+     type(c_ptr) :: eq_arg
+     type(c_ptr) :: phase
+     type(c_ptr) :: phase_shift
+     type(gom_series) :: eta
+     type(gom_series) :: q
+     type(gom_series) :: salt
+     type(gom_series) :: temp
+  end type
+
+  type, bind(c) :: gom_mesh
+     integer(c_int32_t) :: n_nodes
+     integer(c_int32_t) :: n_cells
+     integer(c_int32_t) :: max_nb
+     integer(c_int32_t) :: voronoi
+     integer(c_int32_t) :: n_layers
+     integer(c_int32_t) :: n_ob
+     integer(c_int32_t) :: n_qb
+     integer(c_int32_t) :: reserved
+     type(c_ptr) :: x_node
+     type(c_ptr) :: y_node
+     type(c_ptr) :: h_node
+     type(c_ptr) :: tri_or_quad
+     type(c_ptr) :: nodenum_at_cell
+     type(c_ptr) :: z_level
+     real(c_double) :: msl
+     type(c_ptr) :: ob_nodes
+     type(c_ptr) :: qb_nodes
+  end type
+
+  type, bind(c) :: gom_mesh_geometry
+     integer(c_int32_t) :: face_capacity
+     integer(c_int32_t) :: n_faces
+     type(c_ptr) :: adj_cells_at_node
+     type(c_ptr) :: adj_cellnum_at_node
+     type(c_ptr) :: node_count_each_element
+     type(c_ptr) :: adj_nodes_at_node
+     type(c_ptr) :: adj_nodenum_at_node
+     type(c_ptr) :: bottom_layer_at_node
+     type(c_ptr) :: initial_wetdry_node
+     type(c_ptr) :: x_cell
+     type(c_ptr) :: y_cell
+     type(c_ptr) :: h_cell
+     type(c_ptr) :: area
+     type(c_ptr) :: facenum_at_cell
+     type(c_ptr) :: adj_cellnum_at_cell
+     type(c_ptr) :: sign_in_outflow
+     type(c_ptr) :: bottom_layer_at_element
+     type(c_ptr) :: ob_element_flag
+     type(c_ptr) :: qb_element_flag
+     type(c_ptr) :: x_face
+     type(c_ptr) :: y_face
+     type(c_ptr) :: h_face
+     type(c_ptr) :: face_length
+     type(c_ptr) :: delta_j
+     type(c_ptr) :: cos_theta
+     type(c_ptr) :: sin_theta
+     type(c_ptr) :: cos_theta2
+     type(c_ptr) :: sin_theta2
+     type(c_ptr) :: adj_cellnum_at_face
+     type(c_ptr) :: nodenum_at_face
+     type(c_ptr) :: bottom_layer_at_face
+     type(c_ptr) :: boundary_type_of_face
+     type(c_ptr) :: isflowside3
+     type(c_ptr) :: ob_cell_id
+     type(c_ptr) :: ob_face_id
+     type(c_ptr) :: qb_cell
+     type(c_ptr) :: qb_face
+  end type
+
   integer(c_int), parameter :: GOM_F_ETA_CELL = 1
   integer(c_int), parameter :: GOM_F_ETA_CELL_NEW = 2
   integer(c_int), parameter :: GOM_F_ETA_NODE = 3
@@ -223,6 +323,18 @@ module gom_core_abi
   integer(c_int), parameter :: GOM_F_ETA_AT_OB_OLD = 61
   integer(c_int), parameter :: GOM_F_ETA_AT_OB_NEW = 62
   integer(c_int), parameter :: GOM_F_Q_ADD = 63
+  integer(c_int), parameter :: GOM_GEO_CONCAVE = 1
+  integer(c_int), parameter :: GOM_GEO_AREA = 2
+  integer(c_int), parameter :: GOM_GEO_MAX_NB = 3
+  integer(c_int), parameter :: GOM_GEO_HANGING = 4
+  integer(c_int), parameter :: GOM_GEO_SURROUNDING = 5
+  integer(c_int), parameter :: GOM_GEO_FACE_COUNT = 6
+  integer(c_int), parameter :: GOM_GEO_FACE_LENGTH = 7
+  integer(c_int), parameter :: GOM_GEO_BALL = 8
+  integer(c_int), parameter :: GOM_GEO_VORONOI = 9
+  integer(c_int), parameter :: GOM_GEO_CENTRES = 10
+  integer(c_int), parameter :: GOM_GEO_BOUNDARY = 11
+  integer(c_int), parameter :: GOM_GEO_VERTICAL = 12
 
   interface
      integer(c_int) function gom_abi_version() bind(c, name="gom_abi_version")
@@ -315,6 +427,17 @@ module gom_core_abi
        type(c_ptr), value :: ctx
        real(c_double), intent(out) :: volume, salt_mass
      end function
+     integer(c_int) function gom_set_boundary_series(ctx, series) bind(c, name="gom_set_boundary_series")
+       import
+       type(c_ptr), value :: ctx
+       type(gom_boundary_series), intent(in) :: series
+     end function
+     integer(c_int) function gom_geometry_build(mesh, out, failure) bind(c, name="gom_geometry_build")
+       import
+       type(gom_mesh), intent(in) :: mesh
+       type(gom_mesh_geometry), intent(inout) :: out
+       type(gom_status), intent(out) :: failure
+     end function
      integer(c_int) function gom_get_status(ctx, status, clear) bind(c, name="gom_get_status")
        import
        type(c_ptr), value :: ctx
@@ -332,7 +455,8 @@ module gom_core_shim
   use mod_file_definition, only : pw_run_log
   implicit none
   private
-  public :: gom_gpu_init, gom_gpu_step, gom_gpu_get, gom_gpu_set_forcing, gom_gpu_check, gom_ctx
+  public :: gom_gpu_init, gom_gpu_step, gom_gpu_get, gom_gpu_set_forcing, gom_gpu_check, gom_ctx, &
+       gom_gpu_set_boundary_series
 
   type(c_ptr), save :: gom_ctx = c_null_ptr
   type(gom_dims), save :: dims
@@ -602,6 +726,131 @@ contains
     if (is_temp == 1 .and. heat_option == 2) f%phi_sw = cptr_d(phi_sw)
     if (is_temp == 1 .and. heat_option == 1) f%phi_sz = cptr_d(phi_sz)
     call gom_gpu_check(gom_set_forcing(gom_ctx, f), 'gom_set_forcing')
+  end subroutine
+
+  ! The boundary tables of mod_global_variables held on the device (gom_set_boundary_series): the
+  ! harmonic constituents (read_harmonic_ser.f90), the elevation, discharge, salinity and
+  ! temperature series (read_eta_ser.f90, read_q_ser.f90, read_salt_ser.f90, read_temp_ser.f90) and
+  ! the ids of cards C20_1 / C22_1.  Call once after prepare_gom (step 0) or after a hot start (the
+  ! step it restarts from); every later gom_gpu_step then advances the clock and forms
+  ! setup_spinup, compute_boundary_eta, calculate_Q and the boundary concentrations of every
+  ! subcycle on the device, so gom_gpu_set_forcing is needed only for the wind and heat terms.
+  subroutine gom_gpu_set_boundary_series(step)
+    integer, intent(in) :: step
+    type(gom_boundary_series) :: bs
+    integer(c_int32_t), allocatable, target, save :: se(:), sq(:), ss(:), st(:), hs(:)
+    real(c_double), allocatable, target, save :: te(:), ve(:), tq(:), vq(:), ts(:), vs(:), tt(:), vt(:)
+    real(c_double), allocatable, target, save :: amp(:), per(:), nod(:), eq(:), ph(:), shift(:), portion(:)
+    integer(c_int32_t), allocatable, target, save :: obt(:), obh(:), obe(:), obs(:), obtm(:), qq(:), qs(:), qt(:)
+    integer :: h, j, m, nc
+    ! a kind without series (its reader's arrays unallocated) is passed as n_series = 0
+    bs%eta = gom_series(0, 0, c_null_ptr, c_null_ptr, c_null_ptr)
+    bs%q = bs%eta
+    bs%salt = bs%eta
+    bs%temp = bs%eta
+    if (num_eta_ser > 0) call pack_series(num_eta_ser, eta_ser_data_num, eta_ser_time, eta_ser_eta, se, te, ve, bs%eta)
+    if (num_Q_ser > 0) call pack_series(num_Q_ser, q_data_num, q_ser_time, q_ser_Q, sq, tq, vq, bs%q)
+    if (is_salt == 1 .and. num_salt_ser > 0) &
+         call pack_series(num_salt_ser, salt_ser_data_num, salt_ser_time, salt_ser_salt, ss, ts, vs, bs%salt)
+    if (is_temp == 1 .and. num_temp_ser > 0) &
+         call pack_series(num_temp_ser, temp_ser_data_num, temp_ser_time, temp_ser_temp, st, tt, vt, bs%temp)
+    ! harmonic series: constituents one series after another, offsets in hs
+    if (allocated(hs)) deallocate(hs, amp, per, nod, eq, ph, shift)
+    nc = 0
+    do h = 1, num_harmonic_ser
+       nc = nc + no_tidal_constituent(h)
+    end do
+    allocate(hs(num_harmonic_ser + 1), amp(max(nc, 1)), per(max(nc, 1)), nod(max(nc, 1)), eq(max(nc, 1)), &
+         ph(max(nc, 1)), shift(max(num_harmonic_ser, 1)))
+    hs(1) = 0
+    m = 0
+    do h = 1, num_harmonic_ser
+       do j = 1, no_tidal_constituent(h)
+          m = m + 1
+          amp(m) = tidal_amplitude(j, h)
+          per(m) = tidal_period(j, h)
+          nod(m) = tidal_nodal_factor(j, h)
+          eq(m) = equilibrium_argument(j, h)
+          ph(m) = tidal_phase(j, h)
+       end do
+       shift(h) = tidal_phase_shift(h)
+       hs(h + 1) = m
+    end do
+    if (allocated(obt)) deallocate(obt, obh, obe, obs, obtm, qq, qs, qt, portion)
+    allocate(obt(max(num_ob_cell, 1)), obh(max(num_ob_cell, 1)), obe(max(num_ob_cell, 1)), &
+         obs(max(num_ob_cell, 1)), obtm(max(num_ob_cell, 1)), qq(max(num_Qb_cell, 1)), qs(max(num_Qb_cell, 1)), &
+         qt(max(num_Qb_cell, 1)), portion(max(num_Qb_cell, 1)))
+    do j = 1, num_ob_cell
+       obt(j) = ob_eta_type(j)
+       obh(j) = harmonic_ser_id(j)
+       obe(j) = eta_ser_id(j)
+       obs(j) = salt_ser_id(j)
+       obtm(j) = temp_ser_id(j)
+    end do
+    do j = 1, num_Qb_cell
+       qq(j) = Q_ser_id(j)
+       qs(j) = Q_salt_ser_id(j)
+       qt(j) = Q_temp_ser_id(j)
+       portion(j) = Q_portion(j)
+    end do
+    bs%julian_day = julian_day
+    bs%tide_spinup_period = tide_spinup_period
+    bs%baroclinic_spinup_period = baroclinic_spinup_period
+    bs%step = step
+    bs%reference_diff_days = reference_diff_days
+    bs%tide_spinup = tide_spinup
+    bs%baroclinic_spinup = baroclinic_spinup
+    bs%q_interp_method = q_interp_method
+    bs%n_harmonic = num_harmonic_ser
+    bs%ob_eta_type = cptr_i(obt)
+    bs%ob_harmonic_id = cptr_i(obh)
+    bs%ob_eta_id = cptr_i(obe)
+    bs%ob_salt_id = cptr_i(obs)
+    bs%ob_temp_id = cptr_i(obtm)
+    bs%qb_q_id = cptr_i(qq)
+    bs%qb_salt_id = cptr_i(qs)
+    bs%qb_temp_id = cptr_i(qt)
+    bs%qb_portion = cptr_d(portion)
+    bs%harmonic_start = cptr_i(hs)
+    bs%amplitude = cptr_d(amp)
+    bs%period_h = cptr_d(per)
+    bs%nodal = cptr_d(nod)
+    bs%eq_arg = cptr_d(eq)
+    bs%phase = cptr_d(ph)
+    bs%phase_shift = cptr_d(shift)
+    call gom_gpu_check(gom_set_boundary_series(gom_ctx, bs), 'gom_set_boundary_series')
+  end subroutine
+
+  ! one kind of series, (max_len, n) columns with their lengths, as concatenated samples with offsets
+  subroutine pack_series(n, counts, times, values, start, t, v, ser)
+    integer, intent(in) :: n
+    integer, intent(in) :: counts(:)
+    real(dp), intent(in) :: times(:, :), values(:, :)
+    integer(c_int32_t), allocatable, target, intent(inout) :: start(:)
+    real(c_double), allocatable, target, intent(inout) :: t(:), v(:)
+    type(gom_series), intent(out) :: ser
+    integer :: k, q, m
+    if (allocated(start)) deallocate(start, t, v)
+    m = 0
+    do k = 1, n
+       m = m + counts(k)
+    end do
+    allocate(start(n + 1), t(max(m, 1)), v(max(m, 1)))
+    start(1) = 0
+    m = 0
+    do k = 1, n
+       do q = 1, counts(k)
+          m = m + 1
+          t(m) = times(q, k)
+          v(m) = values(q, k)
+       end do
+       start(k + 1) = m
+    end do
+    ser%n_series = n
+    ser%reserved = 0
+    ser%start = cptr_i(start)
+    ser%time = cptr_d(t)
+    ser%value = cptr_d(v)
   end subroutine
 
   ! linear interpolation of a series at model time u2 (series time minus reference_diff_days)

@@ -13,7 +13,9 @@ SHIM = ROOT / "gom_release_gb300" / "fortran" / "gom_core_shim.f90"
 HEADER = ROOT / "include" / "gom_core.h"
 
 STRUCTS = {"gom_dims": core.GomDims, "gom_params": core.GomParams, "gom_geom": core.GomGeom,
-           "gom_forcing": core.GomForcing, "gom_status": core.GomStatus}
+           "gom_forcing": core.GomForcing, "gom_status": core.GomStatus, "gom_series": core.GomSeries,
+           "gom_boundary_series": core.GomBoundarySeries, "gom_mesh": core.GomMesh,
+           "gom_mesh_geometry": core.GomMeshGeometry}
 
 
 def _fortran_types():
@@ -56,13 +58,16 @@ def _kind_of(ctype):
         return "real(c_double)"
     if ctype is core.C.c_int32:
         return "integer(c_int32_t)"
+    if ctype is core.GomSeries:
+        return "type(gom_series)"
     return "type(c_ptr)"
 
 
 def test_derived_types_match_header_and_ctypes():
     ft = _fortran_types()
     hs = _header_structs()
-    cmap = {"double": "real(c_double)", "int32_t": "integer(c_int32_t)", "ptr": "type(c_ptr)"}
+    cmap = {"double": "real(c_double)", "int32_t": "integer(c_int32_t)", "ptr": "type(c_ptr)",
+            "gom_series": "type(gom_series)"}
     for name, cls in STRUCTS.items():
         assert name in ft, f"{name} missing from the Fortran binding"
         f_fields = ft[name]
@@ -86,6 +91,13 @@ def test_interfaces_name_declared_entry_points_with_their_arity():
         assert cname in arity, f"{cname} is not declared in the header"
         n = 0 if not args.strip() else len(args.split(","))
         assert n == arity[cname], f"{cname}: {n} arguments, header has {arity[cname]}"
+
+
+def test_geometry_sites_match_header():
+    shim = SHIM.read_text()
+    sites = dict((n, int(v)) for n, v in re.findall(r"parameter :: GOM_GEO_(\w+) = (\d+)", shim))
+    hdr = dict((n, int(v)) for n, v in re.findall(r"GOM_GEO_(\w+) = (\d+)", HEADER.read_text()))
+    assert sites == hdr == core.GOM_GEO
 
 
 def test_field_ids_and_abi_version():
