@@ -25,6 +25,8 @@ e2e_device_series
 serving        a bounded storm-surge serving run (16 Poisson requests, quarter-scale meshes):
                p50 / p99 latency and throughput of packed mixed precision against plain FP64
                serving one request at a time on the same GPU (--no-serving skips it).
+ensemble       the 96-run storm-surge ensemble at full size, packed mixed precision against plain
+               FP64 one run at a time over the same 10 steps (--no-ensemble skips it).
 
 N > 1 runs independent replicas (the single-run path does not shard): value is the sum over
 ranks of cell-layer-steps divided by the slowest rank's time.
@@ -528,6 +530,44 @@ def bench_ensemble(args):
     print(json.dumps(line), flush=True)
 
 
+def bounded_ensemble(lib, steps: int = 10, warm: int = 5) -> dict:
+    """The ensemble comparison at full size for the default benchmark line: the 96 storm-surge
+    runs packed into one mixed-precision context against the plain FP64 path stepping every run
+    alone, each arm warmed up `warm` steps, autotuned, stepped once, then timed over `steps` steps
+    with CUDA events (the same steps of the storms for both arms)."""
+    from gom_release_gb300.ensemble import ensemble_decks, pack
+    from gom_release_gb300.serve import active_cell_layers, storm_context
+    t0 = time.perf_counter()
+    decks = ensemble_decks(n_runs=96, seed=7)
+    storms = [d.meta["storm"] for d in decks]
+    pk = pack(decks)
+    core = storm_context(lib, pk, 1, storms)
+    ncl = active_cell_layers(core, pk)
+    time_core_steps(core, warm)
+    tune = core.autotune(reps=2)
+    time_core_steps(core, 1)
+    secs = time_core_steps(core, steps)
+    packed = {"value": ncl * steps / secs, "ms_per_step": secs / steps * 1e3, "active_cell_layers": ncl,
+              "device_gb": core.device_bytes() / 1e9, "autotune": tune, "status": int(core.status().code)}
+    core.close()
+    work, tsum = 0, 0.0
+    for d, st in zip(decks, storms):
+        c = storm_context(lib, d, 0, [st])
+        n = active_cell_layers(c, d)
+        time_core_steps(c, warm)
+        c.autotune(reps=2)
+        time_core_steps(c, 1)
+        tsum += time_core_steps(c, steps)
+        work += n * steps
+        c.close()
+    fp64 = {"value": work / tsum, "seconds": tsum}
+    cells = [d.n_cells for d in decks]
+    return {"workload": (f"{len(decks)} storm-surge runs, {sum(cells)} cells (log-uniform {min(cells)}-{max(cells)}), "
+                         f"steps {warm + 2}-{warm + steps + 1} of the storms"),
+            "packed_mixed": packed, "fp64_one_at_a_time": fp64, "ratio": packed["value"] / fp64["value"],
+            "wall_s": time.perf_counter() - t0}
+
+
 def serving_record(lib, n_requests: int, scale: float, horizon_scale: float, pool_size: int, servers=None):
     """Poisson stream of storm-surge requests (rate 2/s, horizons U(6, 48) h scaled by
     horizon_scale), meshes drawn from an ensemble-like pool: continuous batching in one packed
@@ -714,6 +754,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serving", action="store_true",
                     help="estuary: skip the bounded serving record (packed mixed vs FP64 latency) of the line")
+    ap.add_argument("--no-ensemble", action="store_true",
+                    help="estuary: skip the ensemble record (96 runs packed mixed vs FP64 one at a time) of the line")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
     ap.add_argument("--tuning", default=None,
                     help="launch variants per tunable site, e.g. 1,3,3,1 (set instead of autotuning)")
@@ -856,9 +898,12 @@ def main():
         barrier(world)
         return
     value = ncl * args.steps * world / secs
-    serving = None
-    if not args.no_serving and args.size == "full":
+    # the single-GPU comparisons of the serving form (run once, at N = 1, on the full workload)
+    serving = ensemble = None
+    if not args.no_serving and args.size == "full" and world == 1:
         serving = bounded_serving(lib)
+    if not args.no_ensemble and args.size == "full" and world == 1:
+        ensemble = bounded_ensemble(lib)
     cpu = None
     if not args.no_cpu_baseline:
         cpu = cpu_baseline(deck, st, ncl)
@@ -897,6 +942,7 @@ def main():
         "clocks": clocks.summary(),
         "snapshot": snapshot,
         "serving": serving,
+        "ensemble": ensemble,
         "e2e_device_series": e2e_series,
     }
     print(json.dumps(line), flush=True)
