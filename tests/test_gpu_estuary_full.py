@@ -10,7 +10,7 @@ from gom_release_gb300.deck import HostForcing, estuary, initial_state
 pytestmark = pytest.mark.gpu
 
 ETA_TOL = 1e-10
-CHOICES = ([0, 3, 3, 1], [1, 3, 3, 1])   # launch variants chosen on this deck (ELM, momentum, solve, limiter)
+CHOICES = ([0, 3, 3, 1], [1, 3, 3, 1], [0, 1, 3, 0])   # launch variants chosen on this deck (ELM, momentum, solve, limiter)
 
 
 def _mismatch(a, b):
