@@ -134,7 +134,10 @@ class GomBoundarySeries(C.Structure):
         [(n, _I) for n in ("ob_eta_type", "ob_harmonic_id", "ob_eta_id", "ob_salt_id", "ob_temp_id", "qb_q_id",
                            "qb_salt_id", "qb_temp_id")] + [("qb_portion", _D), ("harmonic_start", _I)] + \
         [(n, _D) for n in ("amplitude", "period_h", "nodal", "eq_arg", "phase", "phase_shift")] + \
-        [(n, GomSeries) for n in ("eta", "q", "salt", "temp")]
+        [(n, GomSeries) for n in ("eta", "q", "salt", "temp")] + \
+        [(n, C.c_int32) for n in ("wind_flag", "wind_formular", "wind_spinup", "n_wind")] + \
+        [("wind_spinup_period", C.c_double), ("rho_a", C.c_double), ("wind_station_node", _I)] + \
+        [(n, GomSeries) for n in ("wind_u", "wind_v")]
 
 
 class GomMesh(C.Structure):
@@ -484,9 +487,10 @@ class GomCore:
             return a.ctypes.data_as(_D)
 
         sets = {}
-        for kind in ("eta", "q", "salt", "temp"):
+        for kind in ("eta", "q", "salt", "temp", "wind_u", "wind_v"):
             start, t, v = bs.flat(kind)
             sets[kind] = GomSeries(len(start) - 1, 0, ints(start), dbls(t), dbls(v))
+        wind = getattr(bs, "wind", None) or {}
         hs, amp, per, nod, eq, ph, shift = bs.flat_harmonics()
         arg = GomBoundarySeries(
             julian_day=float(bs.julian_day), tide_spinup_period=float(bs.tide_spinup_period),
@@ -497,7 +501,11 @@ class GomCore:
             ob_eta_id=ints(bs.ob_eta_id), ob_salt_id=ints(bs.ob_salt_id), ob_temp_id=ints(bs.ob_temp_id),
             qb_q_id=ints(bs.qb_q_id), qb_salt_id=ints(bs.qb_salt_id), qb_temp_id=ints(bs.qb_temp_id),
             qb_portion=dbls(bs.qb_portion), harmonic_start=ints(hs), amplitude=dbls(amp), period_h=dbls(per),
-            nodal=dbls(nod), eq_arg=dbls(eq), phase=dbls(ph), phase_shift=dbls(shift), **sets)
+            nodal=dbls(nod), eq_arg=dbls(eq), phase=dbls(ph), phase_shift=dbls(shift),
+            wind_flag=int(wind.get("flag", 0)), wind_formular=int(wind.get("formular", 1)),
+            wind_spinup=int(wind.get("spinup", 0)), n_wind=len(bs.series.get("wind_u", [])),
+            wind_spinup_period=float(wind.get("spinup_period", 0.0)), rho_a=float(wind.get("rho_a", 1.2)),
+            wind_station_node=ints(wind.get("station_node", [])), **sets)
         self._check(self.lib.gom_set_boundary_series(self.ctx, C.byref(arg)), "set_boundary_series")
 
     def conservation(self) -> tuple[float, float]:

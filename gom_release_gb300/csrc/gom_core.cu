@@ -1316,6 +1316,19 @@ int gom_set_boundary_series(gom_ctx *c, const gom_boundary_series *bs) {
         !ids_ok(bs->qb_temp_id, nqb, bs->temp.n_series) || (nqb > 0 && !bs->qb_portion))
         return GOM_E_ARG;
     if (bs->q_interp_method != 1 && bs->q_interp_method != 2) return GOM_E_ARG;
+    // station wind: one to three stations, each with u and v series, nodes inside the mesh
+    if (bs->wind_flag != 0 && bs->wind_flag != 1) return GOM_E_ARG;
+    if (bs->wind_flag == 1) {
+        if (bs->wind_formular < 1 || bs->wind_formular > 3 || bs->n_wind < 1 || bs->n_wind > 3 ||
+            bs->wind_u.n_series != bs->n_wind || bs->wind_v.n_series != bs->n_wind || !series_ok(bs->wind_u) ||
+            !series_ok(bs->wind_v) || !(bs->rho_a > 0.0))
+            return GOM_E_ARG;
+        if (bs->n_wind > 1) {
+            if (!bs->wind_station_node) return GOM_E_ARG;
+            for (int k = 0; k < bs->n_wind; ++k)
+                if (bs->wind_station_node[k] < 1 || bs->wind_station_node[k] > c->d.n_nodes) return GOM_E_ARG;
+        }
+    }
     CK(cudaStreamSynchronize(c->x.stream));
     series_free(c);
     SeriesDev &S = c->series;
@@ -1348,6 +1361,23 @@ int gom_set_boundary_series(gom_ctx *c, const gom_boundary_series *bs) {
     if (e == cudaSuccess) e = series_upload(c, &S.eq, nh > 0 ? bs->eq_arg : nullptr, nc);
     if (e == cudaSuccess) e = series_upload(c, &S.ph, nh > 0 ? bs->phase : nullptr, nc);
     if (e == cudaSuccess) e = series_upload(c, &S.shift, nh > 0 ? bs->phase_shift : nullptr, (size_t)nh);
+    const gom_series *wsets[2] = {&bs->wind_u, &bs->wind_v};
+    for (int k = 0; k < 2 && e == cudaSuccess; ++k) {
+        const gom_series &sr = *wsets[k];
+        const int ns = bs->wind_flag == 1 ? sr.n_series : 0;
+        S.n[4 + k] = ns;
+        const size_t len = ns > 0 ? (size_t)sr.start[ns] : 0;
+        e = series_upload(c, &S.start[4 + k], ns > 0 ? sr.start : nullptr, (size_t)ns + 1);
+        if (e == cudaSuccess) e = series_upload(c, &S.time[4 + k], ns > 0 ? sr.time : nullptr, len);
+        if (e == cudaSuccess) e = series_upload(c, &S.value[4 + k], ns > 0 ? sr.value : nullptr, len);
+    }
+    const int nw = bs->wind_flag == 1 ? bs->n_wind : 0;
+    if (e == cudaSuccess) e = series_upload(c, &S.wind_node, nw > 1 ? bs->wind_station_node : nullptr, (size_t)nw);
+    if (e == cudaSuccess) {
+        const double *ws = nullptr;
+        e = series_upload(c, &ws, (const double *)nullptr, 6);
+        S.wind_at_station = const_cast<double *>(ws);
+    }
     if (e != cudaSuccess) {
         series_free(c);
         return set_cuda_error(c, e, "gom_set_boundary_series");
@@ -1359,8 +1389,19 @@ int gom_set_boundary_series(gom_ctx *c, const gom_boundary_series *bs) {
     S.bc_per_s = (bs->baroclinic_spinup == 1 && c->hp.baroclinic_flag == 1) ? bs->baroclinic_spinup_period * 86400.0
                                                                                 : 0.0;
     S.q_method = bs->q_interp_method;
+    S.wind_flag = bs->wind_flag;
+    S.wind_formular = bs->wind_formular;
+    S.n_wind = nw;
+    S.wind_per_s = (bs->wind_flag == 1 && bs->wind_spinup == 1) ? bs->wind_spinup_period * 86400.0 : 0.0;
+    S.rho_ratio = bs->wind_flag == 1 ? bs->rho_a / c->hp.rho_o : 0.0;
+    // calculate_wind_stress.f90:20-33: the bounds are default-REAL expressions scaled in double
+    const float lo[3] = {0.75f + 0.067f * 4.0f, 0.61f + 0.063f * 6.0f, 0.80f + 0.065f * 1.0f};
+    const float hi[3] = {0.75f + 0.067f * 50.0f, 0.61f + 0.063f * 50.0f, 0.80f + 0.065f * 50.0f};
+    const int fi = bs->wind_formular >= 1 && bs->wind_formular <= 3 ? bs->wind_formular - 1 : 1;
+    S.cda_min = 0.001 * (double)lo[fi];
+    S.cda_max = 0.001 * (double)hi[fi];
     // the device clock: elapsed time and spin-up of the last step, its julian day and step number
-    const double scal[8] = {bs->step * c->hp.dt, 1.0, 1.0, 0.0, bs->julian_day, (double)bs->step, 0.0, 0.0};
+    const double scal[8] = {bs->step * c->hp.dt, 1.0, 1.0, 0.0, bs->julian_day, (double)bs->step, 1.0, 0.0};
     CK(cudaMemcpy(c->f_scal, scal, sizeof(scal), cudaMemcpyHostToDevice));
     CK(legacy_done());
     c->has_series = true;

@@ -126,9 +126,10 @@ cudaError_t launch_storm_forcing(const Geom &g, const Forcing &f, const Params &
 
 // device copies of a gom_boundary_series (k_forcing.cu evaluates them at the start of every step)
 struct SeriesDev {
-    int n[4];                              // series per kind: 0 eta, 1 Q, 2 salinity, 3 temperature
-    const int *start[4];                   // (n + 1) offsets per kind
-    const double *time[4], *value[4];
+    int n[6];                              // series per kind: 0 eta, 1 Q, 2 salinity, 3 temperature,
+                                           // 4 station wind u, 5 station wind v
+    const int *start[6];                   // (n + 1) offsets per kind
+    const double *time[6], *value[6];
     const int *ob_type, *ob_h, *ob_eta, *ob_salt, *ob_temp;   // (NOB)
     const int *qb_q, *qb_salt, *qb_temp;                      // (NQB)
     const double *qb_portion;                                 // (NQB)
@@ -138,10 +139,17 @@ struct SeriesDev {
     double rdd_s;                          // reference_diff_days x 86400.0 (single precision, widened)
     double tide_per_s, bc_per_s;           // spin-up periods in seconds, 0 = no ramp
     int q_method;
+    // station wind (get_windp_at_face.f90, IDW_windp_ser.f90, calculate_wind_stress.f90)
+    int wind_flag, wind_formular, n_wind;
+    double wind_per_s;                     // wind spin-up period in seconds, 0 = no ramp
+    double rho_ratio, cda_min, cda_max;    // rho_a / rho_o and the drag-coefficient bounds
+    const int *wind_node;                  // (n_wind) station nodes
+    double *wind_at_station;               // (2 n_wind) work: u, v of each station this step
 };
 
 // per-step boundary forcing from the series (k_forcing.cu): advances the device clock in f.scal
-// ([0] elapsed_time, [1] spin-up tide, [2] spin-up baroclinic, [4] julian_day, [5] it), then
+// ([0] elapsed_time, [1] spin-up tide, [2] spin-up baroclinic, [4] julian_day, [5] it, [6] spin-up
+// wind), forms the station wind stress when wind_flag is 1, then
 // writes eta_at_ob_old/new (type -1 from eta_cell; an isolated cell records GOM_E_ARG in
 // status), q_add and the boundary concentrations of every subcycle
 cudaError_t launch_series_forcing(const Geom &g, const Forcing &f, const Params &p, const SeriesDev &s,

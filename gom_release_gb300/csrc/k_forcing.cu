@@ -155,8 +155,8 @@ __device__ bool series_at(const SeriesDev &S, int kind, int id, double u2, doubl
     return true;
 }
 
-// setup_spinup.f90:12-31 and main.f90:54-56 (elapsed_time = it dt, julian_day += dt / 86400)
-__global__ void k_series_clock(double *scal, double dt, double tide_per, double bc_per) {
+// setup_spinup.f90:12-54 and main.f90:54-56 (elapsed_time = it dt, julian_day += dt / 86400)
+__global__ void k_series_clock(double *scal, double dt, double tide_per, double bc_per, double wind_per) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     const double it = scal[5] + 1.0;
     const double elapsed = it * dt;
@@ -165,6 +165,84 @@ __global__ void k_series_clock(double *scal, double dt, double tide_per, double 
     scal[4] = scal[4] + dt / 86400.0;
     scal[1] = (tide_per > 0.0 && elapsed < tide_per) ? tanh(2.0 * elapsed / tide_per) : 1.0;
     scal[2] = (bc_per > 0.0 && elapsed < bc_per) ? tanh(2.0 * elapsed / bc_per) : 1.0;
+    scal[6] = (wind_per > 0.0 && elapsed < wind_per) ? tanh(2.0 * elapsed / wind_per) : 1.0;
+}
+
+// get_windp_at_face.f90:18-38 / IDW_windp_ser.f90:27-52: each station's wind at u2 =
+// julian_day x 86400, v12 = (v13 - v11) / (u3 - u1) (u2 - u1) + v11 on the first interval that
+// holds u2, 0 when none does
+__global__ void k_series_wind_stations(Forcing f, SeriesDev S) {
+    const int k = threadIdx.x;
+    if (k >= S.n_wind) return;
+    const double u2 = f.scal[4] * 86400.0;
+    double vals[2] = {0.0, 0.0};
+    for (int c = 0; c < 2; ++c) {
+        const int kind = 4 + c;
+        const int s0 = S.start[kind][k], n = S.start[kind][k + 1] - s0;
+        const double *t = S.time[kind] + s0, *val = S.value[kind] + s0;
+        for (int q = 1; q < n; ++q) {
+            const double u1 = t[q - 1] - S.rdd_s, u3 = t[q] - S.rdd_s;
+            if (u2 >= u1 && u2 <= u3) {
+                vals[c] = (val[q] - val[q - 1]) / (u3 - u1) * (u2 - u1) + val[q - 1];
+                break;
+            }
+        }
+    }
+    S.wind_at_station[2 * k] = vals[0];
+    S.wind_at_station[2 * k + 1] = vals[1];
+}
+
+// IDW_windp_ser.f90:77-118 at one node (power 1): two stations weighted by the other's distance,
+// three by the product of the other two
+__device__ __forceinline__ void idw_node(const Geom &g, const SeriesDev &S, int node, double &u, double &v) {
+    const double x = g.x_node[node - 1], y = g.y_node[node - 1];
+    double dist[3];
+    for (int k = 0; k < S.n_wind; ++k) {
+        const int sn = S.wind_node[k];
+        const double dx = x - g.x_node[sn - 1], dy = y - g.y_node[sn - 1];
+        dist[k] = sqrt(dx * dx + dy * dy);
+    }
+    const double *w = S.wind_at_station;
+    if (S.n_wind == 2) {
+        const double r1 = dist[1], r2 = dist[0];
+        u = (r1 * w[0] + r2 * w[2]) / (r1 + r2);
+        v = (r1 * w[1] + r2 * w[3]) / (r1 + r2);
+    } else {
+        const double r1 = dist[1] * dist[2], r2 = dist[0] * dist[2], r3 = dist[0] * dist[1];
+        u = (r1 * w[0] + r2 * w[2] + r3 * w[4]) / (r1 + r2 + r3);
+        v = (r1 * w[1] + r2 * w[3] + r3 * w[5]) / (r1 + r2 + r3);
+    }
+}
+
+// get_windp_at_face.f90:40-48 and calculate_wind_stress.f90:41-65 (heat_model_flag 0): one thread
+// per face
+__global__ void k_series_wind_faces(Geom g, Forcing f, SeriesDev S) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= g.NF) return;
+    double u, v;
+    if (S.n_wind == 1) {
+        u = S.wind_at_station[0];
+        v = S.wind_at_station[1];
+    } else {
+        double u1, v1, u2, v2;
+        idw_node(g, S, g.nodenum_at_face[2 * j], u1, v1);
+        idw_node(g, S, g.nodenum_at_face[2 * j + 1], u2, v2);
+        u = (u1 + u2) * 0.5;
+        v = (v1 + v2) * 0.5;
+    }
+    const double speed = sqrt(u * u + v * v);
+    const double normal = u * g.cos_theta[j] + v * g.sin_theta[j];
+    const double tangent = -u * g.sin_theta[j] + v * g.cos_theta[j];
+    double cda;
+    if (S.wind_formular == 1) cda = 0.001 * (0.75 + 0.067 * speed);
+    else if (S.wind_formular == 2) cda = 0.001 * (0.61 + 0.063 * speed);
+    else cda = 0.001 * (0.80 + 0.065 * speed);
+    cda = fmin(fmax(cda, S.cda_min), S.cda_max);
+    const double gamma_t = cda * S.rho_ratio * speed;
+    const double spin = f.scal[6];
+    const_cast<double *>(f.gamma_t)[j] = gamma_t;
+    const_cast<double *>(f.wind_stress_normal)[j] = gamma_t * normal * spin;
+    const_cast<double *>(f.wind_stress_tangnt)[j] = gamma_t * tangent * spin;
 }
 
 // compute_boundary_eta.f90:45-124 (types 1 and 2) and the open-boundary concentrations of every
@@ -311,7 +389,11 @@ cudaError_t launch_storm_forcing(const Geom &g, const Forcing &f, const Params &
 
 cudaError_t launch_series_forcing(const Geom &g, const Forcing &f, const Params &p, const SeriesDev &s,
                                   const double *eta_cell, gom_status *status, cudaStream_t stream) {
-    k_series_clock<<<1, 32, 0, stream>>>(const_cast<double *>(f.scal), p.dt, s.tide_per_s, s.bc_per_s);
+    k_series_clock<<<1, 32, 0, stream>>>(const_cast<double *>(f.scal), p.dt, s.tide_per_s, s.bc_per_s, s.wind_per_s);
+    if (s.wind_flag == 1) {
+        k_series_wind_stations<<<1, 32, 0, stream>>>(f, s);
+        k_series_wind_faces<<<blocks_for(g.NF, 256), 256, 0, stream>>>(g, f, s);
+    }
     const int nt = p.trans_sub_iter > 0 ? p.trans_sub_iter : 1;
     const int salt = p.transport_flag && p.is_salt, temp = p.transport_flag && p.is_temp;
     if (g.NOB > 0) k_series_ob<<<blocks_for(g.NOB, 128), 128, 0, stream>>>(g, f, p, s, eta_cell, status, salt, temp, nt);

@@ -198,6 +198,15 @@ module gom_core_abi
      type(gom_series) :: q
      type(gom_series) :: salt
      type(gom_series) :: temp
+     integer(c_int32_t) :: wind_flag
+     integer(c_int32_t) :: wind_formular
+     integer(c_int32_t) :: wind_spinup
+     integer(c_int32_t) :: n_wind
+     real(c_double) :: wind_spinup_period
+     real(c_double) :: rho_a
+     type(c_ptr) :: wind_station_node
+     type(gom_series) :: wind_u
+     type(gom_series) :: wind_v
   end type
 
   type, bind(c) :: gom_mesh
@@ -734,7 +743,9 @@ contains
   ! the ids of cards C20_1 / C22_1.  Call once after prepare_gom (step 0) or after a hot start (the
   ! step it restarts from); every later gom_gpu_step then advances the clock and forms
   ! setup_spinup, compute_boundary_eta, calculate_Q and the boundary concentrations of every
-  ! subcycle on the device, so gom_gpu_set_forcing is needed only for the wind and heat terms.
+  ! subcycle on the device.  With station wind (wind_flag 1, heat_model_flag 0, card C30) the
+  ! device also forms get_windp_at_face and calculate_wind_stress every step, so
+  ! gom_gpu_set_forcing is then needed only for the heat terms.
   subroutine gom_gpu_set_boundary_series(step)
     integer, intent(in) :: step
     type(gom_boundary_series) :: bs
@@ -742,12 +753,16 @@ contains
     real(c_double), allocatable, target, save :: te(:), ve(:), tq(:), vq(:), ts(:), vs(:), tt(:), vt(:)
     real(c_double), allocatable, target, save :: amp(:), per(:), nod(:), eq(:), ph(:), shift(:), portion(:)
     integer(c_int32_t), allocatable, target, save :: obt(:), obh(:), obe(:), obs(:), obtm(:), qq(:), qs(:), qt(:)
+    integer(c_int32_t), allocatable, target, save :: swu(:), swv(:), wnode(:)
+    real(c_double), allocatable, target, save :: twu(:), vwu(:), twv(:), vwv(:)
     integer :: h, j, m, nc
     ! a kind without series (its reader's arrays unallocated) is passed as n_series = 0
     bs%eta = gom_series(0, 0, c_null_ptr, c_null_ptr, c_null_ptr)
     bs%q = bs%eta
     bs%salt = bs%eta
     bs%temp = bs%eta
+    bs%wind_u = bs%eta
+    bs%wind_v = bs%eta
     if (num_eta_ser > 0) call pack_series(num_eta_ser, eta_ser_data_num, eta_ser_time, eta_ser_eta, se, te, ve, bs%eta)
     if (num_Q_ser > 0) call pack_series(num_Q_ser, q_data_num, q_ser_time, q_ser_Q, sq, tq, vq, bs%q)
     if (is_salt == 1 .and. num_salt_ser > 0) &
@@ -818,6 +833,28 @@ contains
     bs%eq_arg = cptr_d(eq)
     bs%phase = cptr_d(ph)
     bs%phase_shift = cptr_d(shift)
+    ! station wind: both components share windp_ser_time
+    bs%wind_flag = 0
+    bs%wind_formular = wind_formular
+    bs%wind_spinup = wind_spinup
+    bs%n_wind = 0
+    bs%wind_spinup_period = wind_spinup_period
+    bs%rho_a = rho_a
+    bs%wind_station_node = c_null_ptr
+    if (wind_flag == 1 .and. heat_model_flag == 0 .and. num_windp_ser > 0) then
+       bs%wind_flag = 1
+       bs%n_wind = num_windp_ser
+       call pack_series(num_windp_ser, windp_ser_data_num, windp_ser_time, windp_u, swu, twu, vwu, bs%wind_u)
+       call pack_series(num_windp_ser, windp_ser_data_num, windp_ser_time, windp_v, swv, twv, vwv, bs%wind_v)
+       if (allocated(wnode)) deallocate(wnode)
+       allocate(wnode(num_windp_ser))
+       if (num_windp_ser > 1) then
+          do j = 1, num_windp_ser
+             wnode(j) = windp_station_node(j)
+          end do
+          bs%wind_station_node = cptr_i(wnode)
+       end if
+    end if
     call gom_gpu_check(gom_set_boundary_series(gom_ctx, bs), 'gom_set_boundary_series')
   end subroutine
 

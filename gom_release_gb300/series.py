@@ -11,12 +11,18 @@ and C22_1 -- in the flat layout the C ABI takes.  Once set on a context, every `
 ``step_launch`` evaluates them on the device before the first phase, so a run needs no host
 forcing per step.
 
-Two builders:
+Station wind (card C30, ``wind_flag`` 1 with ``windp_ser.inp``) rides along: with it set, the
+device also forms get_windp_at_face.f90 / IDW_windp_ser.f90 and calculate_wind_stress.f90 every
+step.
+
+Builders:
 
 * ``from_deck_data(deck)``  a reference deck read by ``gom_inputs.read_deck``;
 * ``from_synthetic(deck)``  a synthetic deck of ``deck.py``: one harmonic series from its tide,
                             constant discharge and boundary-tracer series -- the same forcing
-                            ``deck.HostForcing`` computes on the host.
+                            ``deck.HostForcing`` computes on the host;
+* ``with_station_wind(bs, deck, n_stations)``  adds seeded station-wind series (one to three
+                            stations on nodes spread over the mesh).
 """
 from __future__ import annotations
 
@@ -49,8 +55,11 @@ class BoundarySeries:
     # harmonic series: per series a dict of constituent arrays amplitude, period_h, nodal,
     # eq_arg, phase and the scalar phase_shift
     harmonics: list = field(default_factory=list)
-    # kind -> list of (times, values) per series; kinds eta, q, salt, temp
+    # kind -> list of (times, values) per series; kinds eta, q, salt, temp, and wind_u / wind_v
+    # (one series per wind station, the same times)
     series: dict = field(default_factory=dict)
+    # station wind (card C30): flag, formular, spinup, spinup_period (days), rho_a, station_node
+    wind: dict = field(default_factory=dict)
 
     def flat(self, kind: str):
         """(start, time, value) of one kind: offsets (n + 1) and the concatenated samples."""
@@ -143,4 +152,37 @@ def from_synthetic(deck) -> BoundarySeries:
         harmonics=harm, series=series)
 
 
-__all__ = ["BoundarySeries", "from_deck_data", "from_synthetic"]
+def with_station_wind(bs: BoundarySeries, deck, n_stations: int, *, hours: float = 6.0, formular: int = 1,
+                      spinup_days: float = 0.0, rho_a: float = 1.2, seed: int = 0) -> BoundarySeries:
+    """`bs` with `n_stations` (1..3) seeded wind stations: station k on the node nearest the k-th
+    of three points spread across the mesh, samples every 10 to 20 minutes from before the run's
+    start to `hours` after it (times in seconds since the reference day, as read_windp_ser.f90
+    stores them), winds of 5 to 25 m/s turning over the run; the last station's series starts
+    an hour late, so that get_windp_at_face.f90 gives it zero wind until then."""
+    from dataclasses import replace
+
+    if not 1 <= n_stations <= 3:
+        raise ValueError("IDW_windp_ser.f90 takes one to three stations")
+    rng = np.random.default_rng(seed)
+    x, y = deck.geo["x_node"], deck.geo["y_node"]
+    x0, x1, y0, y1 = float(x.min()), float(x.max()), float(y.min()), float(y.max())
+    targets = [(0.2, 0.3), (0.8, 0.5), (0.5, 0.9)]
+    nodes = [int(np.argmin((x - (x0 + fx * (x1 - x0))) ** 2 + (y - (y0 + fy * (y1 - y0))) ** 2)) + 1
+             for fx, fy in targets[:n_stations]]
+    t_start = bs.julian_day * 86400.0 + bs.reference_diff_days * 86400.0
+    u_ser, v_ser = [], []
+    for k in range(n_stations):
+        first = t_start - 900.0 + (3600.0 if k == n_stations - 1 and n_stations > 1 else 0.0)
+        steps = rng.uniform(600.0, 1200.0, size=int(hours * 3600.0 / 600.0) + 4)
+        t = first + np.concatenate([[0.0], np.cumsum(steps)])
+        speed = rng.uniform(5.0, 25.0, size=t.size)
+        angle = rng.uniform(0.0, 2.0 * np.pi) + np.linspace(0.0, 1.5, t.size)
+        u_ser.append((t, speed * np.cos(angle)))
+        v_ser.append((t.copy(), speed * np.sin(angle)))
+    series = dict(bs.series, wind_u=u_ser, wind_v=v_ser)
+    wind = dict(flag=1, formular=int(formular), spinup=1 if spinup_days > 0.0 else 0,
+                spinup_period=float(spinup_days), rho_a=float(rho_a), station_node=nodes)
+    return replace(bs, series=series, wind=wind)
+
+
+__all__ = ["BoundarySeries", "from_deck_data", "from_synthetic", "with_station_wind"]

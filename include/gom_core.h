@@ -446,6 +446,18 @@ typedef struct gom_boundary_series {
     const double *phase;            /* tidal_phase (degrees)                                    */
     const double *phase_shift;      /* (n_harmonic) tidal_phase_shift (degrees)                 */
     gom_series eta, q, salt, temp;
+    /* station wind (card C30, windp_ser.inp): get_windp_at_face.f90 (one station uniform, two or
+     * three by inverse distance to their nodes, IDW_windp_ser.f90) and calculate_wind_stress.f90
+     * (heat_model_flag 0) form wind_stress_normal / tangnt and Gamma_T every step; with wind_flag
+     * 0 the wind arrays are left as gom_set_forcing set them */
+    int32_t wind_flag;              /* 1: station wind series                                   */
+    int32_t wind_formular;          /* 1, 2 or 3 (the drag-coefficient formula)                 */
+    int32_t wind_spinup;            /* flag                                                     */
+    int32_t n_wind;                 /* num_windp_ser: 1..3 stations                             */
+    double wind_spinup_period;      /* days                                                     */
+    double rho_a;                   /* card C1 air density (kg/m3)                              */
+    const int32_t *wind_station_node; /* (n_wind) windp_station_node                            */
+    gom_series wind_u, wind_v;      /* per station: windp_u, windp_v on windp_ser_time          */
 } gom_boundary_series;
 int gom_set_boundary_series(struct gom_ctx *ctx, const gom_boundary_series *series);
 

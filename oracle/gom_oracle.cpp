@@ -122,8 +122,11 @@ struct gom_ctx {
     bool has_series = false;
     double jday = 0, rdd_s = 0, tide_per_s = 0, bc_per_s = 0;
     int step_no = 0, q_method = 1, n_harm = 0;
-    std::vector<int32_t> sr_start[4];
-    std::vector<double> sr_time[4], sr_value[4];
+    std::vector<int32_t> sr_start[6];   // eta, Q, salinity, temperature, station wind u, v
+    std::vector<double> sr_time[6], sr_value[6];
+    int wind_flag = 0, wind_formular = 1, n_wind = 0;
+    double wind_per_s = 0, rho_ratio = 0, cda_min = 0, cda_max = 0;
+    std::vector<int32_t> wind_node;
     std::vector<int32_t> ob_type, ob_h, ob_eta, ob_salt, ob_temp, qb_q, qb_salt, qb_temp, h_start;
     std::vector<double> qb_portion, h_amp, h_per, h_nodal, h_eq, h_ph, h_shift;
     std::vector<double> eta_at_ob_old, eta_at_ob_new, q_add, wind_stress_normal, wind_stress_tangnt, gamma_t,
@@ -1055,6 +1058,25 @@ int gom_set_boundary_series(gom_ctx *c, const gom_boundary_series *bs) {
         (c->NQB > 0 && !bs->qb_portion))
         return GOM_E_ARG;
     if (bs->q_interp_method != 1 && bs->q_interp_method != 2) return GOM_E_ARG;
+    if (bs->wind_flag != 0 && bs->wind_flag != 1) return GOM_E_ARG;
+    if (bs->wind_flag == 1) {
+        if (bs->wind_formular < 1 || bs->wind_formular > 3 || bs->n_wind < 1 || bs->n_wind > 3 ||
+            bs->wind_u.n_series != bs->n_wind || bs->wind_v.n_series != bs->n_wind || !(bs->rho_a > 0.0))
+            return GOM_E_ARG;
+        for (const gom_series *sr : {&bs->wind_u, &bs->wind_v}) {
+            if (!sr->start || !sr->time || !sr->value || sr->start[0] != 0) return GOM_E_ARG;
+            for (int k = 0; k < sr->n_series; ++k) {
+                if (sr->start[k + 1] < sr->start[k]) return GOM_E_ARG;
+                for (int q = sr->start[k] + 1; q < sr->start[k + 1]; ++q)
+                    if (!(sr->time[q] >= sr->time[q - 1])) return GOM_E_ARG;
+            }
+        }
+        if (bs->n_wind > 1) {
+            if (!bs->wind_station_node) return GOM_E_ARG;
+            for (int k = 0; k < bs->n_wind; ++k)
+                if (bs->wind_station_node[k] < 1 || bs->wind_station_node[k] > c->NN) return GOM_E_ARG;
+        }
+    }
     for (int k = 0; k < 4; ++k) {
         const gom_series &sr = *sets[k];
         c->sr_start[k].assign(1, 0);
@@ -1099,6 +1121,34 @@ int gom_set_boundary_series(gom_ctx *c, const gom_boundary_series *bs) {
     c->bc_per_s = (bs->baroclinic_spinup == 1 && c->p.baroclinic_flag == 1) ? bs->baroclinic_spinup_period * 86400.0
                                                                               : 0.0;
     c->q_method = bs->q_interp_method;
+    // station wind: the series as kinds 4 (u) and 5 (v), calculate_wind_stress.f90:20-33 bounds
+    // (default-REAL expressions scaled in double)
+    c->wind_flag = bs->wind_flag;
+    c->n_wind = bs->wind_flag == 1 ? bs->n_wind : 0;
+    c->wind_formular = bs->wind_formular;
+    const gom_series *wsets[2] = {&bs->wind_u, &bs->wind_v};
+    for (int k = 0; k < 2; ++k) {
+        const gom_series &sr = *wsets[k];
+        c->sr_start[4 + k].assign(1, 0);
+        c->sr_time[4 + k].clear();
+        c->sr_value[4 + k].clear();
+        if (c->n_wind > 0) {
+            c->sr_start[4 + k].assign(sr.start, sr.start + sr.n_series + 1);
+            c->sr_time[4 + k].assign(sr.time, sr.time + sr.start[sr.n_series]);
+            c->sr_value[4 + k].assign(sr.value, sr.value + sr.start[sr.n_series]);
+        }
+    }
+    c->wind_node.assign(c->n_wind, 0);
+    if (c->n_wind > 1) c->wind_node.assign(bs->wind_station_node, bs->wind_station_node + c->n_wind);
+    c->wind_per_s = (bs->wind_flag == 1 && bs->wind_spinup == 1) ? bs->wind_spinup_period * 86400.0 : 0.0;
+    c->rho_ratio = bs->wind_flag == 1 ? bs->rho_a / c->p.rho_o : 0.0;
+    {
+        const float lo[3] = {0.75f + 0.067f * 4.0f, 0.61f + 0.063f * 6.0f, 0.80f + 0.065f * 1.0f};
+        const float hi[3] = {0.75f + 0.067f * 50.0f, 0.61f + 0.063f * 50.0f, 0.80f + 0.065f * 50.0f};
+        const int fi = bs->wind_formular >= 1 && bs->wind_formular <= 3 ? bs->wind_formular - 1 : 1;
+        c->cda_min = 0.001 * (double)lo[fi];
+        c->cda_max = 0.001 * (double)hi[fi];
+    }
     c->jday = bs->julian_day;
     c->step_no = bs->step;
     c->has_series = true;
@@ -1151,6 +1201,76 @@ double q_lagrange(const gom_ctx *c, int id, double u2) {
     return total;
 }
 
+// setup_spinup.f90:44-54, get_windp_at_face.f90:18-48, IDW_windp_ser.f90:27-118 and
+// calculate_wind_stress.f90:41-65 (heat_model_flag 0)
+void station_wind(gom_ctx *c, double elapsed, double u2) {
+    const double spin_w = (c->wind_per_s > 0.0 && elapsed < c->wind_per_s) ? std::tanh(2.0 * elapsed / c->wind_per_s)
+                                                                               : 1.0;
+    double st[3][2] = {{0, 0}, {0, 0}, {0, 0}};
+    for (int k = 1; k <= c->n_wind; ++k) {
+        double v12 = 0.0, v22 = 0.0;
+        for (int comp = 0; comp < 2; ++comp) {
+            const std::vector<int32_t> &sta = c->sr_start[4 + comp];
+            const double *t = c->sr_time[4 + comp].data() + sta[k - 1];
+            const double *v = c->sr_value[4 + comp].data() + sta[k - 1];
+            const int n = sta[k] - sta[k - 1];
+            for (int q = 2; q <= n; ++q) {
+                const double u1 = t[q - 2] - c->rdd_s, u3 = t[q - 1] - c->rdd_s;
+                if (u2 >= u1 && u2 <= u3) {
+                    const double r = (v[q - 1] - v[q - 2]) / (u3 - u1) * (u2 - u1) + v[q - 2];
+                    if (comp == 0) v12 = r;
+                    else v22 = r;
+                    break;
+                }
+            }
+        }
+        st[k - 1][0] = v12;
+        st[k - 1][1] = v22;
+    }
+    auto idw = [&](int node, double &u, double &v) {
+        const double x = c->x_node(node), y = c->y_node(node);
+        double dist[3];
+        for (int k = 1; k <= c->n_wind; ++k) {
+            const double x1 = c->x_node(c->wind_node[k - 1]), y1 = c->y_node(c->wind_node[k - 1]);
+            dist[k - 1] = std::sqrt((x - x1) * (x - x1) + (y - y1) * (y - y1));
+        }
+        if (c->n_wind == 2) {
+            const double r1 = dist[1], r2 = dist[0];
+            u = (r1 * st[0][0] + r2 * st[1][0]) / (r1 + r2);
+            v = (r1 * st[0][1] + r2 * st[1][1]) / (r1 + r2);
+        } else {
+            const double r1 = dist[1] * dist[2], r2 = dist[0] * dist[2], r3 = dist[0] * dist[1];
+            u = (r1 * st[0][0] + r2 * st[1][0] + r3 * st[2][0]) / (r1 + r2 + r3);
+            v = (r1 * st[0][1] + r2 * st[1][1] + r3 * st[2][1]) / (r1 + r2 + r3);
+        }
+    };
+    for (int j = 1; j <= c->NF; ++j) {
+        double u, v;
+        if (c->n_wind == 1) {
+            u = st[0][0];
+            v = st[0][1];
+        } else {
+            double u1, v1, u2n, v2n;
+            idw(c->nodenum_at_face(1, j), u1, v1);
+            idw(c->nodenum_at_face(2, j), u2n, v2n);
+            u = (u1 + u2n) * 0.5;
+            v = (v1 + v2n) * 0.5;
+        }
+        const double speed = std::sqrt(u * u + v * v);
+        const double normal = u * c->cos_theta(j) + v * c->sin_theta(j);
+        const double tangent = -u * c->sin_theta(j) + v * c->cos_theta(j);
+        double cda;
+        if (c->wind_formular == 1) cda = 0.001 * (0.75 + 0.067 * speed);
+        else if (c->wind_formular == 2) cda = 0.001 * (0.61 + 0.063 * speed);
+        else cda = 0.001 * (0.80 + 0.065 * speed);
+        cda = std::min(std::max(cda, c->cda_min), c->cda_max);
+        const double gamma_t = cda * c->rho_ratio * speed;
+        c->gamma_t[j - 1] = gamma_t;
+        c->wind_stress_normal[j - 1] = gamma_t * normal * spin_w;
+        c->wind_stress_tangnt[j - 1] = gamma_t * tangent * spin_w;
+    }
+}
+
 void series_forcing(gom_ctx *c) {
     const double dt = c->p.dt;
     c->step_no += 1;
@@ -1161,6 +1281,7 @@ void series_forcing(gom_ctx *c) {
     c->spinup_baroclinic = (c->bc_per_s > 0.0 && elapsed < c->bc_per_s) ? std::tanh(2.0 * elapsed / c->bc_per_s) : 1.0;
     const double spin = c->spinup_tide, spin_bc = c->spinup_baroclinic, jd_s = c->jday * 86400.0;
     A1<double> eta_cell = FD1(c, GOM_F_ETA_CELL);
+    if (c->wind_flag == 1) station_wind(c, elapsed, jd_s);
     const double deg2rad = 3.141592653589793 / 180.0;
     for (int i = 0; i < c->NOB; ++i) {
         if (c->ob_type[i] == -1) {

@@ -5,6 +5,7 @@ interpolation of solve_transport_equation_v19.f90), bit for bit, on the referenc
 (elevation series, linear and Lagrange discharge, salinity / temperature series, 30 subcycles)
 and on a synthetic estuary (harmonic tide with spin-up, constant river and boundary tracers); the
 interior-mean open boundary (type -1) by hand; and the argument rules."""
+import math
 from dataclasses import replace
 from pathlib import Path
 
@@ -142,3 +143,102 @@ def test_argument_rules(oracle_so):
             c.set_boundary_series(bs)
         assert e.value.code == 1
     c.set_boundary_series(from_synthetic(deck))
+
+
+# ----------------------------------------------------------------------------- station wind
+def _station_wind_host(deck, bs, julian_day, elapsed):
+    """get_windp_at_face.f90:18-85, IDW_windp_ser.f90:27-118, setup_spinup.f90:44-54 and
+    calculate_wind_stress.f90:20-74 (heat_model_flag 0) restated in numpy, in the reference's order
+    of operations: (wind_stress_normal, wind_stress_tangnt, Gamma_T) of one step."""
+    w = bs.wind
+    a = deck.geo
+    u2 = julian_day * 86400.0
+    rdd = float(np.float32(bs.reference_diff_days) * np.float32(86400.0))
+    st = []
+    for (tu, vu), (tv, vv) in zip(bs.series["wind_u"], bs.series["wind_v"]):
+        val = [0.0, 0.0]
+        for comp, (t, v) in enumerate(((tu, vu), (tv, vv))):
+            for q in range(1, len(t)):
+                u1, u3 = t[q - 1] - rdd, t[q] - rdd
+                if u1 <= u2 <= u3:
+                    val[comp] = (v[q] - v[q - 1]) / (u3 - u1) * (u2 - u1) + v[q - 1]
+                    break
+        st.append(val)
+    n = len(st)
+    if n == 1:
+        u = np.full(deck.n_faces, st[0][0])
+        v = np.full(deck.n_faces, st[0][1])
+    else:
+        x, y = a["x_node"], a["y_node"]
+        dist = [np.sqrt((x - x[s - 1]) ** 2 + (y - y[s - 1]) ** 2) for s in w["station_node"]]
+        if n == 2:
+            r = [dist[1], dist[0]]
+        else:
+            r = [dist[1] * dist[2], dist[0] * dist[2], dist[0] * dist[1]]
+        den = r[0] + r[1] if n == 2 else r[0] + r[1] + r[2]
+        un = (r[0] * st[0][0] + r[1] * st[1][0]) if n == 2 else (r[0] * st[0][0] + r[1] * st[1][0] + r[2] * st[2][0])
+        vn = (r[0] * st[0][1] + r[1] * st[1][1]) if n == 2 else (r[0] * st[0][1] + r[1] * st[1][1] + r[2] * st[2][1])
+        un, vn = un / den, vn / den
+        n1, n2 = a["nodenum_at_face"][:, 0] - 1, a["nodenum_at_face"][:, 1] - 1
+        u = (un[n1] + un[n2]) * 0.5
+        v = (vn[n1] + vn[n2]) * 0.5
+    speed = np.sqrt(u * u + v * v)
+    normal = u * a["cos_theta"] + v * a["sin_theta"]
+    tangent = -u * a["sin_theta"] + v * a["cos_theta"]
+    base, slope, lo = {1: (0.75, 0.067, 4.0), 2: (0.61, 0.063, 6.0), 3: (0.80, 0.065, 1.0)}[w["formular"]]
+    f32 = np.float32
+    cmin = 0.001 * float(f32(base) + f32(slope) * f32(lo))
+    cmax = 0.001 * float(f32(base) + f32(slope) * f32(50.0))
+    cda = np.minimum(np.maximum(0.001 * (base + slope * speed), cmin), cmax)
+    per = w["spinup_period"] * 86400.0 if w["spinup"] == 1 else 0.0
+    spin = math.tanh(2.0 * elapsed / per) if per > 0.0 and elapsed < per else 1.0   # the C library's tanh
+    gamma = cda * (w["rho_a"] / deck.params.rho_o) * speed
+    return gamma * normal * spin, gamma * tangent * spin, gamma
+
+
+@pytest.mark.parametrize("n_stations,formular", [(1, 1), (2, 2), (3, 3), (3, 1)])
+def test_station_wind_equals_host_restatement(oracle_so, n_stations, formular):
+    """The wind stresses and Gamma_T the context forms from the station series equal the numpy
+    restatement every step (spin-up on, the last station silent for its first hour), and a context
+    fed that host forcing every step ends in the same state bit for bit."""
+    from gom_release_gb300.series import with_station_wind
+
+    deck = estuary(nx=14, ny=6, dx=100.0, n_layers=6, trans_sub_iter=2)
+    deck.tide_spinup_days = 0.01
+    bs = with_station_wind(from_synthetic(deck), deck, n_stations, formular=formular, spinup_days=0.02,
+                           seed=n_stations)
+    hf = HostForcing(deck)
+    a, b = _pair(deck, oracle_so, hf)
+    b.set_boundary_series(bs)
+    dt = deck.params.dt
+    steps = 6
+    for it in range(1, steps + 1):
+        f = hf.full(it) if it == 1 else hf.step(it)
+        tn, tt, gt = _station_wind_host(deck, bs, hf.julian_day, it * dt)
+        f.update(wind_stress_normal=tn, wind_stress_tangnt=tt, gamma_t=gt)
+        a.set_forcing(f)
+        a.step_all()
+        b.step_all()
+        for name, ref in (("wind_stress_normal", tn), ("wind_stress_tangnt", tt), ("gamma_t", gt)):
+            got = b.get_field(name)
+            assert np.array_equal(got, ref), (it, name, float(np.abs(got - ref).max()))
+    assert float(np.abs(b.get_field("wind_stress_normal")).max()) > 0.0
+    for name in STATE:
+        assert np.array_equal(a.get_field(name), b.get_field(name)), name
+
+
+def test_station_wind_argument_rules(oracle_so):
+    from gom_release_gb300.series import with_station_wind
+
+    deck = estuary(nx=8, ny=4, dx=100.0, n_layers=3, trans_sub_iter=1)
+    c = GomCore(deck, lib_path=oracle_so)
+    good = with_station_wind(from_synthetic(deck), deck, 2)
+    bad = [replace(good, wind=dict(good.wind, flag=2)), replace(good, wind=dict(good.wind, formular=4)),
+           replace(good, wind=dict(good.wind, station_node=[1, deck.n_nodes + 1])),
+           replace(good, wind=dict(good.wind, rho_a=0.0)),
+           replace(good, series=dict(good.series, wind_v=good.series["wind_v"][:1]))]
+    for bs in bad:
+        with pytest.raises(GomError) as e:
+            c.set_boundary_series(bs)
+        assert e.value.code == 1
+    c.set_boundary_series(good)

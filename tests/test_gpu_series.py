@@ -141,3 +141,36 @@ def test_argument_rules_and_storm_exclusion(gpu_lib):
     c.set_boundary_series(bs)
     with pytest.raises(GomError):
         c.set_storms([object()])
+
+
+@pytest.mark.parametrize("n_stations,spinup_days", [(1, 0.0), (2, 0.0), (3, 0.0), (3, 0.02)])
+def test_station_wind_equals_oracle(oracle_so, gpu_lib, n_stations, spinup_days):
+    """Station wind (get_windp_at_face.f90, IDW_windp_ser.f90, calculate_wind_stress.f90) formed on
+    the device equals the oracle's bit for bit without spin-up (sqrt and division are correctly
+    rounded on both); with the wind spin-up on, CUDA's tanh may differ from the C library's in
+    the last bit."""
+    from gom_release_gb300.series import with_station_wind
+
+    deck = estuary(nx=30, ny=12, dx=100.0, n_layers=8, trans_sub_iter=3)
+    deck.tide_spinup_days = 0.01
+    st = initial_state(deck)
+    ref = _ctx(deck, st, lib_path=oracle_so)
+    gpu = _ctx(deck, st, lib=gpu_lib)
+    bs = with_station_wind(from_synthetic(deck), deck, n_stations, formular=n_stations, spinup_days=spinup_days,
+                           seed=10 + n_stations)
+    static = HostForcing(deck).static()
+    for c in (ref, gpu):
+        c.set_forcing(static)
+        c.set_boundary_series(bs)
+    for it in range(1, 11):
+        ref.step_all()
+        gpu.step_all()
+        for name in ("wind_stress_normal", "wind_stress_tangnt", "gamma_t"):
+            a, b = gpu.get_field(name), ref.get_field(name)
+            if spinup_days == 0.0:
+                assert np.array_equal(a, b), (it, name, float(np.abs(a - b).max()))
+            else:
+                assert float(np.abs(a - b).max()) <= 4e-16 * float(np.abs(b).max()), (it, name)
+    assert float(np.abs(gpu.get_field("wind_stress_normal")).max()) > 0.0
+    for name in ("eta_cell", "un_face", "salt_cell", "temp_cell"):
+        assert _close(gpu.get_field(name), ref.get_field(name)), name
