@@ -137,7 +137,9 @@ class GomBoundarySeries(C.Structure):
         [(n, GomSeries) for n in ("eta", "q", "salt", "temp")] + \
         [(n, C.c_int32) for n in ("wind_flag", "wind_formular", "wind_spinup", "n_wind")] + \
         [("wind_spinup_period", C.c_double), ("rho_a", C.c_double), ("wind_station_node", _I)] + \
-        [(n, GomSeries) for n in ("wind_u", "wind_v")]
+        [(n, GomSeries) for n in ("wind_u", "wind_v")] + \
+        [("hurricane_flag", C.c_int32), ("hurricane_read_interval", C.c_int32), ("hurricane_start_jday", C.c_double),
+         ("hurricane_end_jday", C.c_double), ("hurricane_frames", _D)]
 
 
 class GomMesh(C.Structure):
@@ -218,6 +220,7 @@ def _bind(lib: C.CDLL) -> C.CDLL:
     lib.gom_station_series.argtypes = [vp, _D]
     lib.gom_set_storms.argtypes = [vp, C.c_int32, C.POINTER(GomStorm), C.c_double]
     lib.gom_set_boundary_series.argtypes = [vp, C.POINTER(GomBoundarySeries)]
+    lib.gom_push_hurricane_frame.argtypes = [vp, _D]
     lib.gom_geometry_build.argtypes = [C.POINTER(GomMesh), C.POINTER(GomMeshGeometry), C.POINTER(GomStatus)]
     lib.gom_cold_start.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_double]
     lib.gom_autotune.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32)]
@@ -491,6 +494,8 @@ class GomCore:
             start, t, v = bs.flat(kind)
             sets[kind] = GomSeries(len(start) - 1, 0, ints(start), dbls(t), dbls(v))
         wind = getattr(bs, "wind", None) or {}
+        hur = getattr(bs, "hurricane", None) or {}
+        frames = hur.get("frames")
         hs, amp, per, nod, eq, ph, shift = bs.flat_harmonics()
         arg = GomBoundarySeries(
             julian_day=float(bs.julian_day), tide_spinup_period=float(bs.tide_spinup_period),
@@ -505,8 +510,20 @@ class GomCore:
             wind_flag=int(wind.get("flag", 0)), wind_formular=int(wind.get("formular", 1)),
             wind_spinup=int(wind.get("spinup", 0)), n_wind=len(bs.series.get("wind_u", [])),
             wind_spinup_period=float(wind.get("spinup_period", 0.0)), rho_a=float(wind.get("rho_a", 1.2)),
-            wind_station_node=ints(wind.get("station_node", [])), **sets)
+            wind_station_node=ints(wind.get("station_node", [])),
+            hurricane_flag=int(hur.get("flag", 0)), hurricane_read_interval=int(hur.get("read_interval", 1)),
+            hurricane_start_jday=float(hur.get("start_jday", 0.0)), hurricane_end_jday=float(hur.get("end_jday", 0.0)),
+            hurricane_frames=dbls(np.asarray(frames, np.float64).reshape(3, 3, -1).ravel())
+            if frames is not None else None, **sets)
         self._check(self.lib.gom_set_boundary_series(self.ctx, C.byref(arg)), "set_boundary_series")
+
+    def push_hurricane_frame(self, frame) -> None:
+        """The next hurricane_ser.inp record, shape (3, n_nodes): wind_u, wind_v, air_p (Pa); the
+        device takes it at the next read step of the boundary series' hurricane frames."""
+        a = np.ascontiguousarray(np.asarray(frame, np.float64).reshape(3, -1))
+        if a.shape[1] != self.deck.n_nodes:
+            raise ValueError("a hurricane record has one (u, v, p) per node")
+        self._check(self.lib.gom_push_hurricane_frame(self.ctx, a.ctypes.data_as(_D)), "push_hurricane_frame")
 
     def conservation(self) -> tuple[float, float]:
         v = C.c_double()

@@ -1329,6 +1329,10 @@ int gom_set_boundary_series(gom_ctx *c, const gom_boundary_series *bs) {
                 if (bs->wind_station_node[k] < 1 || bs->wind_station_node[k] > c->d.n_nodes) return GOM_E_ARG;
         }
     }
+    // hurricane node frames: a read interval of at least one step, the three frames, air density
+    if (bs->hurricane_flag != 0 && bs->hurricane_flag != 1) return GOM_E_ARG;
+    if (bs->hurricane_flag == 1 && (bs->hurricane_read_interval < 1 || !bs->hurricane_frames || !(bs->rho_a > 0.0)))
+        return GOM_E_ARG;
     CK(cudaStreamSynchronize(c->x.stream));
     series_free(c);
     SeriesDev &S = c->series;
@@ -1378,6 +1382,22 @@ int gom_set_boundary_series(gom_ctx *c, const gom_boundary_series *bs) {
         e = series_upload(c, &ws, (const double *)nullptr, 6);
         S.wind_at_station = const_cast<double *>(ws);
     }
+    const bool hur = bs->hurricane_flag == 1;
+    const size_t nn = (size_t)c->d.n_nodes, nf = (size_t)c->d.n_faces;
+    if (e == cudaSuccess && hur) {
+        const double *fr = nullptr, *nx = nullptr, *fu = nullptr, *fv = nullptr;
+        const int *rd = nullptr;
+        e = series_upload(c, &fr, bs->hurricane_frames, 9 * nn);
+        if (e == cudaSuccess) e = series_upload(c, &nx, (const double *)nullptr, 3 * nn);
+        if (e == cudaSuccess) e = series_upload(c, &rd, (const int *)nullptr, 1);
+        if (e == cudaSuccess) e = series_upload(c, &fu, (const double *)nullptr, nf);
+        if (e == cudaSuccess) e = series_upload(c, &fv, (const double *)nullptr, nf);
+        S.hur_frames = const_cast<double *>(fr);
+        S.hur_next = const_cast<double *>(nx);
+        S.hur_ready = const_cast<int *>(rd);
+        S.face_u = const_cast<double *>(fu);
+        S.face_v = const_cast<double *>(fv);
+    }
     if (e != cudaSuccess) {
         series_free(c);
         return set_cuda_error(c, e, "gom_set_boundary_series");
@@ -1393,7 +1413,12 @@ int gom_set_boundary_series(gom_ctx *c, const gom_boundary_series *bs) {
     S.wind_formular = bs->wind_formular;
     S.n_wind = nw;
     S.wind_per_s = (bs->wind_flag == 1 && bs->wind_spinup == 1) ? bs->wind_spinup_period * 86400.0 : 0.0;
-    S.rho_ratio = bs->wind_flag == 1 ? bs->rho_a / c->hp.rho_o : 0.0;
+    S.rho_ratio = (bs->wind_flag == 1 || hur) ? bs->rho_a / c->hp.rho_o : 0.0;
+    S.hur_flag = hur ? 1 : 0;
+    S.hur_interval = hur ? bs->hurricane_read_interval : 1;
+    S.hur_start = bs->hurricane_start_jday;
+    S.hur_end = bs->hurricane_end_jday;
+    S.hur_cda_max = (double)0.003f;
     // calculate_wind_stress.f90:20-33: the bounds are default-REAL expressions scaled in double
     const float lo[3] = {0.75f + 0.067f * 4.0f, 0.61f + 0.063f * 6.0f, 0.80f + 0.065f * 1.0f};
     const float hi[3] = {0.75f + 0.067f * 50.0f, 0.61f + 0.063f * 50.0f, 0.80f + 0.065f * 50.0f};
@@ -1406,6 +1431,16 @@ int gom_set_boundary_series(gom_ctx *c, const gom_boundary_series *bs) {
     CK(legacy_done());
     c->has_series = true;
     drop_graphs(c);   // the captured step gains the series kernels
+    return GOM_OK;
+}
+
+int gom_push_hurricane_frame(gom_ctx *c, const double *frame) {
+    if (!c || !frame || !c->has_series || c->series.hur_flag != 1) return GOM_E_ARG;
+    const size_t bytes = 3 * (size_t)c->d.n_nodes * sizeof(double);
+    // on the context's stream: after every step already launched, before every later one
+    cudaError_t e = cudaMemcpyAsync(c->series.hur_next, frame, bytes, cudaMemcpyHostToDevice, c->x.stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->series.hur_ready, 1, sizeof(int), c->x.stream);
+    if (e != cudaSuccess) return set_cuda_error(c, e, "gom_push_hurricane_frame");
     return GOM_OK;
 }
 

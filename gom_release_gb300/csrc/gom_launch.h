@@ -145,11 +145,20 @@ struct SeriesDev {
     double rho_ratio, cda_min, cda_max;    // rho_a / rho_o and the drag-coefficient bounds
     const int *wind_node;                  // (n_wind) station nodes
     double *wind_at_station;               // (2 n_wind) work: u, v of each station this step
+    // hurricane node frames (read_hurricane_ser_1.f90, calculate_wind_stress.f90:105-137)
+    int hur_flag, hur_interval;
+    double hur_start, hur_end;             // julian-day window
+    double *hur_frames;                    // (NN, 3, 3): frames 0, 1, 2 of (u, v, air_p)
+    double *hur_next;                      // (NN, 3) the record pushed for the next read step
+    int *hur_ready;                        // nonzero once a record is pushed, cleared when taken
+    double *face_u, *face_v;               // (NF) wind_u_at_face / wind_v_at_face, kept between steps
+    double hur_cda_max;                    // MIN(0.003, Cda): the default-REAL 0.003 widened
 };
 
 // per-step boundary forcing from the series (k_forcing.cu): advances the device clock in f.scal
 // ([0] elapsed_time, [1] spin-up tide, [2] spin-up baroclinic, [4] julian_day, [5] it, [6] spin-up
-// wind), forms the station wind stress when wind_flag is 1, then
+// wind), forms the station wind stress when wind_flag is 1 (the hurricane drag law on the hurricane
+// or station face winds when hur_flag is 1, with air_p from the node frames), then
 // writes eta_at_ob_old/new (type -1 from eta_cell; an isolated cell records GOM_E_ARG in
 // status), q_add and the boundary concentrations of every subcycle
 cudaError_t launch_series_forcing(const Geom &g, const Forcing &f, const Params &p, const SeriesDev &s,

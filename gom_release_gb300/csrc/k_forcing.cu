@@ -230,6 +230,11 @@ __global__ void k_series_wind_faces(Geom g, Forcing f, SeriesDev S) {
         u = (u1 + u2) * 0.5;
         v = (v1 + v2) * 0.5;
     }
+    if (S.hur_flag == 1) {   // the hurricane drag law follows on these face winds
+        S.face_u[j] = u;
+        S.face_v[j] = v;
+        return;
+    }
     const double speed = sqrt(u * u + v * v);
     const double normal = u * g.cos_theta[j] + v * g.sin_theta[j];
     const double tangent = -u * g.sin_theta[j] + v * g.cos_theta[j];
@@ -238,6 +243,79 @@ __global__ void k_series_wind_faces(Geom g, Forcing f, SeriesDev S) {
     else if (S.wind_formular == 2) cda = 0.001 * (0.61 + 0.063 * speed);
     else cda = 0.001 * (0.80 + 0.065 * speed);
     cda = fmin(fmax(cda, S.cda_min), S.cda_max);
+    const double gamma_t = cda * S.rho_ratio * speed;
+    const double spin = f.scal[6];
+    const_cast<double *>(f.gamma_t)[j] = gamma_t;
+    const_cast<double *>(f.wind_stress_normal)[j] = gamma_t * normal * spin;
+    const_cast<double *>(f.wind_stress_tangnt)[j] = gamma_t * tangent * spin;
+}
+
+// main.f90:115-127: read_hurricane_ser_1 runs while julian_day (already advanced) lies in the window
+__device__ __forceinline__ bool hurricane_window(const Forcing &f, const SeriesDev &S) {
+    const double jd = f.scal[4];
+    return jd >= S.hur_start && jd <= S.hur_end;
+}
+
+__device__ __forceinline__ bool hurricane_read_step(const Forcing &f, const SeriesDev &S) {
+    return (long long)f.scal[5] % S.hur_interval == 0;
+}
+
+// read_hurricane_ser_1.f90:20-75 at one node: on a read step frames 0 and 1 take frame 2 and
+// frame 2 the pushed record; otherwise frame 1 steps by (frame 2 - frame 0) / real(interval)
+// (the integer widened through default REAL).  air_p (air_p1) follows frame 1.
+__global__ void k_hurricane_nodes(Geom g, Forcing f, SeriesDev S, gom_status *st) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.NN || !hurricane_window(f, S)) return;
+    const long nn = g.NN;
+    double *w0 = S.hur_frames, *w1 = S.hur_frames + 3 * nn, *w2 = S.hur_frames + 6 * nn;
+    if (hurricane_read_step(f, S)) {
+        const bool ready = *S.hur_ready != 0;
+        if (!ready && i == 0) record_error(st, GOM_E_ARG, 34, 0, 0, f.scal[5], GOM_ENTITY_OTHER);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const double v2 = w2[c * nn + i];
+            w0[c * nn + i] = v2;
+            w1[c * nn + i] = v2;
+            if (ready) w2[c * nn + i] = S.hur_next[c * nn + i];
+        }
+    } else {
+        const double den = (double)(float)S.hur_interval;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const double inc = (w2[c * nn + i] - w0[c * nn + i]) / den;
+            w1[c * nn + i] = w1[c * nn + i] + inc;
+        }
+    }
+    const_cast<double *>(f.air_p)[i] = w1[2 * nn + i];
+}
+
+// read_hurricane_ser_1.f90:52-59 / :78-84 (face winds from frame 1 inside the window) and
+// calculate_wind_stress.f90:105-137 on every face, every step
+__global__ void k_hurricane_faces(Geom g, Forcing f, SeriesDev S) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= g.NF) return;
+    const bool win = hurricane_window(f, S);
+    if (j == 0 && win && hurricane_read_step(f, S)) *S.hur_ready = 0;   // the record is taken
+    double u, v;
+    if (win) {
+        const double *w1 = S.hur_frames + 3 * (long)g.NN;
+        const int n1 = g.nodenum_at_face[2 * j] - 1, n2 = g.nodenum_at_face[2 * j + 1] - 1;
+        u = (w1[n1] + w1[n2]) * 0.5;
+        v = (w1[g.NN + n1] + w1[g.NN + n2]) * 0.5;
+        S.face_u[j] = u;
+        S.face_v[j] = v;
+    } else {
+        u = S.face_u[j];
+        v = S.face_v[j];
+    }
+    const double speed = sqrt(u * u + v * v);
+    const double normal = u * g.cos_theta[j] + v * g.sin_theta[j];
+    const double tangent = -u * g.sin_theta[j] + v * g.cos_theta[j];
+    double cda;
+    if (S.wind_formular == 1) cda = 0.001 * (0.75 + 0.067 * speed);
+    else if (S.wind_formular == 3) cda = 0.001 * (0.80 + 0.065 * speed);
+    else cda = 0.001 * (0.61 + 0.063 * speed);   // formula 2, and the reference's default
+    cda = fmin(S.hur_cda_max, cda);
     const double gamma_t = cda * S.rho_ratio * speed;
     const double spin = f.scal[6];
     const_cast<double *>(f.gamma_t)[j] = gamma_t;
@@ -393,6 +471,10 @@ cudaError_t launch_series_forcing(const Geom &g, const Forcing &f, const Params 
     if (s.wind_flag == 1) {
         k_series_wind_stations<<<1, 32, 0, stream>>>(f, s);
         k_series_wind_faces<<<blocks_for(g.NF, 256), 256, 0, stream>>>(g, f, s);
+    }
+    if (s.hur_flag == 1) {
+        k_hurricane_nodes<<<blocks_for(g.NN, 256), 256, 0, stream>>>(g, f, s, status);
+        k_hurricane_faces<<<blocks_for(g.NF, 256), 256, 0, stream>>>(g, f, s);
     }
     const int nt = p.trans_sub_iter > 0 ? p.trans_sub_iter : 1;
     const int salt = p.transport_flag && p.is_salt, temp = p.transport_flag && p.is_temp;

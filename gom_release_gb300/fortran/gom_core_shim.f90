@@ -207,6 +207,11 @@ module gom_core_abi
      type(c_ptr) :: wind_station_node
      type(gom_series) :: wind_u
      type(gom_series) :: wind_v
+     integer(c_int32_t) :: hurricane_flag
+     integer(c_int32_t) :: hurricane_read_interval
+     real(c_double) :: hurricane_start_jday
+     real(c_double) :: hurricane_end_jday
+     type(c_ptr) :: hurricane_frames
   end type
 
   type, bind(c) :: gom_mesh
@@ -440,6 +445,11 @@ module gom_core_abi
        import
        type(c_ptr), value :: ctx
        type(gom_boundary_series), intent(in) :: series
+     end function
+     integer(c_int) function gom_push_hurricane_frame(ctx, frame) bind(c, name="gom_push_hurricane_frame")
+       import
+       type(c_ptr), value :: ctx
+       real(c_double), intent(in) :: frame(*)
      end function
      integer(c_int) function gom_geometry_build(mesh, out, failure) bind(c, name="gom_geometry_build")
        import
@@ -754,6 +764,7 @@ contains
     real(c_double), allocatable, target, save :: amp(:), per(:), nod(:), eq(:), ph(:), shift(:), portion(:)
     integer(c_int32_t), allocatable, target, save :: obt(:), obh(:), obe(:), obs(:), obtm(:), qq(:), qs(:), qt(:)
     integer(c_int32_t), allocatable, target, save :: swu(:), swv(:), wnode(:)
+    real(c_double), allocatable, target, save :: hframes(:)
     real(c_double), allocatable, target, save :: twu(:), vwu(:), twv(:), vwv(:)
     integer :: h, j, m, nc
     ! a kind without series (its reader's arrays unallocated) is passed as n_series = 0
@@ -854,6 +865,30 @@ contains
           end do
           bs%wind_station_node = cptr_i(wnode)
        end if
+    end if
+    ! hurricane node frames (card C31, method 1): wind_u0 / v0 / air_p0, wind_u1 .., wind_u2 ..
+    bs%hurricane_flag = 0
+    bs%hurricane_read_interval = 1
+    bs%hurricane_start_jday = 0.0_dp
+    bs%hurricane_end_jday = 0.0_dp
+    bs%hurricane_frames = c_null_ptr
+    if (hurricane_flag == 1 .and. hurricane_interp_method == 1) then
+       if (allocated(hframes)) deallocate(hframes)
+       allocate(hframes(9 * maxnod))
+       hframes(1:maxnod) = wind_u0
+       hframes(maxnod + 1:2 * maxnod) = wind_v0
+       hframes(2 * maxnod + 1:3 * maxnod) = air_p0
+       hframes(3 * maxnod + 1:4 * maxnod) = wind_u1
+       hframes(4 * maxnod + 1:5 * maxnod) = wind_v1
+       hframes(5 * maxnod + 1:6 * maxnod) = air_p1
+       hframes(6 * maxnod + 1:7 * maxnod) = wind_u2
+       hframes(7 * maxnod + 1:8 * maxnod) = wind_v2
+       hframes(8 * maxnod + 1:9 * maxnod) = air_p2
+       bs%hurricane_flag = 1
+       bs%hurricane_read_interval = hurricane_read_interval
+       bs%hurricane_start_jday = hurricane_start_jday
+       bs%hurricane_end_jday = hurricane_end_jday
+       bs%hurricane_frames = cptr_d(hframes)
     end if
     call gom_gpu_check(gom_set_boundary_series(gom_ctx, bs), 'gom_set_boundary_series')
   end subroutine
@@ -995,4 +1030,30 @@ subroutine update_variables
   use gom_core_shim
   use gom_core_abi
   call gom_gpu_check(gom_step_swap(gom_ctx), 'update_variables')
+end subroutine
+
+subroutine read_hurricane_ser_1
+  ! With the boundary series on the device (gom_gpu_set_boundary_series) the ramp, the face winds,
+  ! air_p1 and the drag law run there; on a read step this replacement only reads the next record
+  ! of hurricane_ser.inp (read_hurricane_ser_1.f90:34-46) and hands it to the device, which takes it
+  ! in this step.
+  use iso_c_binding
+  use gom_core_shim
+  use gom_core_abi
+  use mod_global_variables
+  use mod_file_definition
+  real(c_double), allocatable :: rec(:)
+  integer :: i, j
+  if (mod(it, hurricane_read_interval) /= 0) return
+  allocate(rec(3 * maxnod))
+  do i = 1, maxnod
+     if (hurricane_data_type == 1) then
+        read(pw_hurricane_ser, *) j, rec(i), rec(maxnod + i), rec(2 * maxnod + i)
+     else
+        read(pw_hurricane_ser) j, rec(i), rec(maxnod + i), rec(2 * maxnod + i)
+     end if
+     rec(2 * maxnod + i) = rec(2 * maxnod + i) * 100.0_dp
+  end do
+  call gom_gpu_check(gom_push_hurricane_frame(gom_ctx, rec), 'read_hurricane_ser_1')
+  deallocate(rec)
 end subroutine

@@ -458,8 +458,31 @@ typedef struct gom_boundary_series {
     double rho_a;                   /* card C1 air density (kg/m3)                              */
     const int32_t *wind_station_node; /* (n_wind) windp_station_node                            */
     gom_series wind_u, wind_v;      /* per station: windp_u, windp_v on windp_ser_time          */
+    /* hurricane wind fields (card C31: hurricane_flag 1, hurricane_interp_method 1): node frames of
+     * hurricane_ser.inp taken every hurricane_read_interval steps while julian_day lies in
+     * [hurricane_start_jday, hurricane_end_jday] (main.f90:115-127); between two reads the node
+     * winds and air pressure step linearly, face winds are their node means
+     * (read_hurricane_ser_1.f90), and every step forms the hurricane drag law of
+     * calculate_wind_stress.f90:105-137 (Cda <= 0.003) into wind_stress_normal / tangnt and
+     * Gamma_T, and air_p from the node pressure.  Each frame after the first two comes from
+     * gom_push_hurricane_frame. */
+    int32_t hurricane_flag;         /* 1: hurricane node frames                                 */
+    int32_t hurricane_read_interval;/* int(hurricane_dt / dt) >= 1 (read_hurricane_ser_0.f90:27) */
+    double hurricane_start_jday;    /* find_hurricane_start_end_jday                            */
+    double hurricane_end_jday;
+    const double *hurricane_frames; /* (N_n, 3, 3): (wind_u, wind_v, air_p in Pa) of frames 0, 1
+                                       and 2 = wind_u0.., wind_u1.., wind_u2.. as the driver holds
+                                       them (after read_hurricane_ser_0 frame 1 is all zero)    */
 } gom_boundary_series;
 int gom_set_boundary_series(struct gom_ctx *ctx, const gom_boundary_series *series);
+
+/* The next hurricane_ser.inp record, (N_n, 3): wind_u, wind_v, air_p in Pa (the x 100 of
+ * read_hurricane_ser_1.f90:37-45 applied).  The device takes it at the next step whose
+ * it mod hurricane_read_interval is 0 inside the window; call once before each such step.  A read
+ * step with no record pushed records GOM_E_ARG in the step status and keeps the frame it has.
+ * Ordered on the context's stream: a record may be pushed while earlier steps still run.
+ * Replaces the record read of read_hurricane_ser_1.f90:34-46. */
+int gom_push_hurricane_frame(struct gom_ctx *ctx, const double *frame);
 
 /* ------------------------------------------------------------------ mesh geometry on the device
  * The start-up geometry of GOM built on the GPU: the areas of read_cell_inp.f90:54-87,

@@ -127,6 +127,12 @@ struct gom_ctx {
     int wind_flag = 0, wind_formular = 1, n_wind = 0;
     double wind_per_s = 0, rho_ratio = 0, cda_min = 0, cda_max = 0;
     std::vector<int32_t> wind_node;
+    // hurricane node frames (read_hurricane_ser_0/1.f90): wind_u0.. / wind_u1.. / wind_u2.. as
+    // (NN, 3, 3), the pushed record, wind_u_at_face / wind_v_at_face
+    int hur_flag = 0, hur_interval = 1;
+    bool hur_ready = false;
+    double hur_start = 0, hur_end = 0;
+    std::vector<double> hur_frames, hur_next, face_u, face_v;
     std::vector<int32_t> ob_type, ob_h, ob_eta, ob_salt, ob_temp, qb_q, qb_salt, qb_temp, h_start;
     std::vector<double> qb_portion, h_amp, h_per, h_nodal, h_eq, h_ph, h_shift;
     std::vector<double> eta_at_ob_old, eta_at_ob_new, q_add, wind_stress_normal, wind_stress_tangnt, gamma_t,
@@ -1058,6 +1064,9 @@ int gom_set_boundary_series(gom_ctx *c, const gom_boundary_series *bs) {
         (c->NQB > 0 && !bs->qb_portion))
         return GOM_E_ARG;
     if (bs->q_interp_method != 1 && bs->q_interp_method != 2) return GOM_E_ARG;
+    if (bs->hurricane_flag != 0 && bs->hurricane_flag != 1) return GOM_E_ARG;
+    if (bs->hurricane_flag == 1 && (bs->hurricane_read_interval < 1 || !bs->hurricane_frames || !(bs->rho_a > 0.0)))
+        return GOM_E_ARG;
     if (bs->wind_flag != 0 && bs->wind_flag != 1) return GOM_E_ARG;
     if (bs->wind_flag == 1) {
         if (bs->wind_formular < 1 || bs->wind_formular > 3 || bs->n_wind < 1 || bs->n_wind > 3 ||
@@ -1141,7 +1150,17 @@ int gom_set_boundary_series(gom_ctx *c, const gom_boundary_series *bs) {
     c->wind_node.assign(c->n_wind, 0);
     if (c->n_wind > 1) c->wind_node.assign(bs->wind_station_node, bs->wind_station_node + c->n_wind);
     c->wind_per_s = (bs->wind_flag == 1 && bs->wind_spinup == 1) ? bs->wind_spinup_period * 86400.0 : 0.0;
-    c->rho_ratio = bs->wind_flag == 1 ? bs->rho_a / c->p.rho_o : 0.0;
+    c->hur_flag = bs->hurricane_flag;
+    c->rho_ratio = (bs->wind_flag == 1 || c->hur_flag == 1) ? bs->rho_a / c->p.rho_o : 0.0;
+    c->hur_interval = c->hur_flag == 1 ? bs->hurricane_read_interval : 1;
+    c->hur_start = bs->hurricane_start_jday;
+    c->hur_end = bs->hurricane_end_jday;
+    c->hur_ready = false;
+    c->hur_frames.clear();
+    if (c->hur_flag == 1) c->hur_frames.assign(bs->hurricane_frames, bs->hurricane_frames + 9 * (size_t)c->NN);
+    c->hur_next.assign(c->hur_flag == 1 ? 3 * (size_t)c->NN : 0, 0.0);
+    c->face_u.assign(c->NF, 0.0);
+    c->face_v.assign(c->NF, 0.0);
     {
         const float lo[3] = {0.75f + 0.067f * 4.0f, 0.61f + 0.063f * 6.0f, 0.80f + 0.065f * 1.0f};
         const float hi[3] = {0.75f + 0.067f * 50.0f, 0.61f + 0.063f * 50.0f, 0.80f + 0.065f * 50.0f};
@@ -1256,6 +1275,9 @@ void station_wind(gom_ctx *c, double elapsed, double u2) {
             u = (u1 + u2n) * 0.5;
             v = (v1 + v2n) * 0.5;
         }
+        c->face_u[j - 1] = u;
+        c->face_v[j - 1] = v;
+        if (c->hur_flag == 1) continue;   // the hurricane branch below overwrites the stresses
         const double speed = std::sqrt(u * u + v * v);
         const double normal = u * c->cos_theta(j) + v * c->sin_theta(j);
         const double tangent = -u * c->sin_theta(j) + v * c->cos_theta(j);
@@ -1264,6 +1286,56 @@ void station_wind(gom_ctx *c, double elapsed, double u2) {
         else if (c->wind_formular == 2) cda = 0.001 * (0.61 + 0.063 * speed);
         else cda = 0.001 * (0.80 + 0.065 * speed);
         cda = std::min(std::max(cda, c->cda_min), c->cda_max);
+        const double gamma_t = cda * c->rho_ratio * speed;
+        c->gamma_t[j - 1] = gamma_t;
+        c->wind_stress_normal[j - 1] = gamma_t * normal * spin_w;
+        c->wind_stress_tangnt[j - 1] = gamma_t * tangent * spin_w;
+    }
+}
+
+// main.f90:115-127 with read_hurricane_ser_1.f90:20-86 (julian_day inside the window), then the
+// hurricane branch of calculate_wind_stress.f90:105-137 on every face
+void hurricane_wind(gom_ctx *c, double spin_w) {
+    const size_t nn = (size_t)c->NN;
+    double *w0 = c->hur_frames.data(), *w1 = w0 + 3 * nn, *w2 = w0 + 6 * nn;
+    const bool window = c->jday >= c->hur_start && c->jday <= c->hur_end;
+    if (window) {
+        const int read_count = c->step_no % c->hur_interval;
+        if (read_count == 0) {
+            for (size_t q = 0; q < 3 * nn; ++q) {
+                w0[q] = w2[q];
+                w1[q] = w2[q];
+            }
+            // the record of :34-46 (pushed by the driver)
+            if (!c->hur_ready) set_err(c, GOM_E_ARG, 34, 0, 0, (double)c->step_no, GOM_ENTITY_OTHER);
+            else std::copy(c->hur_next.begin(), c->hur_next.end(), w2);
+            c->hur_ready = false;
+        } else {
+            const double den = (double)(float)c->hur_interval;   // real(hurricane_read_interval)
+            for (size_t q = 0; q < 3 * nn; ++q) {
+                const double inc = (w2[q] - w0[q]) / den;
+                w1[q] = w1[q] + inc;
+            }
+        }
+        for (size_t i = 0; i < nn; ++i) c->air_p[i] = w1[2 * nn + i];
+        for (int j = 1; j <= c->NF; ++j) {
+            const int n1 = c->nodenum_at_face(1, j) - 1, n2 = c->nodenum_at_face(2, j) - 1;
+            c->face_u[j - 1] = (w1[n1] + w1[n2]) * 0.5;
+            c->face_v[j - 1] = (w1[nn + n1] + w1[nn + n2]) * 0.5;
+        }
+    }
+    const double cda_max = (double)0.003f;   // MIN(0.003, Cda): a default-REAL constant
+    for (int j = 1; j <= c->NF; ++j) {
+        const double u = c->face_u[j - 1], v = c->face_v[j - 1];
+        const double speed = std::sqrt(u * u + v * v);
+        const double normal = u * c->cos_theta(j) + v * c->sin_theta(j);
+        const double tangent = -u * c->sin_theta(j) + v * c->cos_theta(j);
+        double cda;
+        if (c->wind_formular == 1) cda = 0.001 * (0.75 + 0.067 * speed);
+        else if (c->wind_formular == 2) cda = 0.001 * (0.61 + 0.063 * speed);
+        else if (c->wind_formular == 3) cda = 0.001 * (0.80 + 0.065 * speed);
+        else cda = 0.001 * (0.61 + 0.063 * speed);
+        cda = std::min(cda_max, cda);
         const double gamma_t = cda * c->rho_ratio * speed;
         c->gamma_t[j - 1] = gamma_t;
         c->wind_stress_normal[j - 1] = gamma_t * normal * spin_w;
@@ -1282,6 +1354,9 @@ void series_forcing(gom_ctx *c) {
     const double spin = c->spinup_tide, spin_bc = c->spinup_baroclinic, jd_s = c->jday * 86400.0;
     A1<double> eta_cell = FD1(c, GOM_F_ETA_CELL);
     if (c->wind_flag == 1) station_wind(c, elapsed, jd_s);
+    if (c->hur_flag == 1)
+        hurricane_wind(c, (c->wind_per_s > 0.0 && elapsed < c->wind_per_s) ? std::tanh(2.0 * elapsed / c->wind_per_s)
+                                                                            : 1.0);
     const double deg2rad = 3.141592653589793 / 180.0;
     for (int i = 0; i < c->NOB; ++i) {
         if (c->ob_type[i] == -1) {
@@ -3206,6 +3281,13 @@ int gom_step_wait(gom_ctx *c, int32_t *pcg_iters) {
 
 // spec: check_conservation.f90:28-57
 // read_main_inp.f90:1143-1154 (station ids), kept for write_tser_out_files
+int gom_push_hurricane_frame(gom_ctx *c, const double *frame) {
+    if (!c || !frame || !c->has_series || c->hur_flag != 1) return GOM_E_ARG;
+    c->hur_next.assign(frame, frame + 3 * (size_t)c->NN);
+    c->hur_ready = true;
+    return GOM_OK;
+}
+
 int gom_set_stations(gom_ctx *c, int32_t hloc, int32_t n_stations, const int32_t *station_cell,
                      const int32_t *station_node) {
     if (!c || (hloc != 1 && hloc != 2) || n_stations < 0) return GOM_E_ARG;

@@ -242,3 +242,102 @@ def test_station_wind_argument_rules(oracle_so):
             c.set_boundary_series(bs)
         assert e.value.code == 1
     c.set_boundary_series(good)
+
+
+# ----------------------------------------------------------------------------- hurricane frames
+class _HurricaneHost:
+    """read_hurricane_ser_1.f90:20-86 under main.f90:115-127 and the hurricane branch of
+    calculate_wind_stress.f90:105-137, restated in numpy in the reference's order of operations."""
+
+    def __init__(self, deck, bs):
+        self.deck, self.h, self.w = deck, bs.hurricane, bs.wind
+        self.frames = np.array(self.h["frames"], np.float64)        # (frame, component, node)
+        self.face_u = np.zeros(deck.n_faces)
+        self.face_v = np.zeros(deck.n_faces)
+        self.next = None
+
+    def step(self, it, julian_day):
+        a = self.deck.geo
+        w0, w1, w2 = self.frames
+        if self.h["start_jday"] <= julian_day <= self.h["end_jday"]:
+            if it % self.h["read_interval"] == 0:
+                w0[:] = w2
+                w1[:] = w2
+                w2[:] = self.next
+                self.next = None
+            else:
+                den = float(np.float32(self.h["read_interval"]))
+                w1[:] = w1 + (w2 - w0) / den
+            n1, n2 = a["nodenum_at_face"][:, 0] - 1, a["nodenum_at_face"][:, 1] - 1
+            self.face_u = (w1[0][n1] + w1[0][n2]) * 0.5
+            self.face_v = (w1[1][n1] + w1[1][n2]) * 0.5
+        u, v = self.face_u, self.face_v
+        speed = np.sqrt(u * u + v * v)
+        normal = u * a["cos_theta"] + v * a["sin_theta"]
+        tangent = -u * a["sin_theta"] + v * a["cos_theta"]
+        base, slope = {1: (0.75, 0.067), 3: (0.80, 0.065)}.get(self.w["formular"], (0.61, 0.063))
+        cda = np.minimum(float(np.float32(0.003)), 0.001 * (base + slope * speed))
+        gamma = cda * (self.w["rho_a"] / self.deck.params.rho_o) * speed
+        return dict(wind_stress_normal=gamma * normal, wind_stress_tangnt=gamma * tangent, gamma_t=gamma,
+                    air_p=w1[2].copy())
+
+
+@pytest.mark.parametrize("formular", [1, 2, 5])
+def test_hurricane_frames_equal_host_restatement(oracle_so, formular):
+    """Node frames every third step inside a window that opens after step 2 and closes after
+    step 8 (the face winds then stay), frame 1 ramping from zero as read_hurricane_ser_0 leaves it:
+    the stresses, Gamma_T and air pressure equal the numpy restatement every step, and a context
+    fed that host forcing ends in the same state bit for bit."""
+    from gom_release_gb300.series import with_hurricane_frames
+
+    deck = estuary(nx=14, ny=6, dx=100.0, n_layers=6, trans_sub_iter=2)
+    dt = deck.params.dt
+    bs, records = with_hurricane_frames(from_synthetic(deck), deck, read_interval=3, n_records=6,
+                                        start_jday=2.5 * dt / 86400.0, end_jday=8.5 * dt / 86400.0,
+                                        formular=formular, seed=3)
+    host = _HurricaneHost(deck, bs)
+    hf = HostForcing(deck)
+    a, b = _pair(deck, oracle_so, hf)
+    b.set_boundary_series(bs)
+    pending = list(records)
+    for it in range(1, 12):
+        f = hf.full(it) if it == 1 else hf.step(it)
+        if it % 3 == 0 and 2.5 * dt / 86400.0 <= hf.julian_day <= 8.5 * dt / 86400.0:
+            rec = pending.pop(0)
+            b.push_hurricane_frame(rec)
+            host.next = rec
+        ref = host.step(it, hf.julian_day)
+        f.update(ref)
+        a.set_forcing(f)
+        a.step_all()
+        b.step_all()
+        for name, val in ref.items():
+            got = b.get_field(name)
+            assert np.array_equal(got, val), (it, name, float(np.abs(got - val).max()))
+    assert b.status().code == 0
+    assert float(np.abs(b.get_field("wind_stress_normal")).max()) > 0.0
+    for name in STATE:
+        assert np.array_equal(a.get_field(name), b.get_field(name)), name
+
+
+def test_hurricane_read_step_without_a_record(oracle_so):
+    from gom_release_gb300.series import with_hurricane_frames
+
+    deck = estuary(nx=8, ny=4, dx=100.0, n_layers=3, trans_sub_iter=1)
+    bs, _ = with_hurricane_frames(from_synthetic(deck), deck, read_interval=2, n_records=3, start_jday=0.0,
+                                  end_jday=1.0)
+    c = GomCore(deck, lib_path=oracle_so)
+    prepare(c, initial_state(deck))
+    c.set_forcing(HostForcing(deck).static())
+    c.set_boundary_series(bs)
+    c.step_all()
+    assert c.status().code == 0
+    try:
+        c.step_all()          # step 2 reads a record that was never pushed
+    except GomError:
+        pass
+    st = c.status()
+    assert st.code == 1 and st.site == 34 and st.value == 2.0, (st.code, st.site, st.value)
+    for bad in (dict(bs.hurricane, read_interval=0), dict(bs.hurricane, flag=2), dict(bs.hurricane, frames=None)):
+        with pytest.raises(GomError):
+            c.set_boundary_series(replace(bs, hurricane=bad))

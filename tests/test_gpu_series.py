@@ -174,3 +174,65 @@ def test_station_wind_equals_oracle(oracle_so, gpu_lib, n_stations, spinup_days)
     assert float(np.abs(gpu.get_field("wind_stress_normal")).max()) > 0.0
     for name in ("eta_cell", "un_face", "salt_cell", "temp_cell"):
         assert _close(gpu.get_field(name), ref.get_field(name)), name
+
+
+def _hurricane_case(deck, formular=1):
+    from gom_release_gb300.series import with_hurricane_frames
+
+    dt = deck.params.dt
+    start, end = 2.5 * dt / 86400.0, 14.5 * dt / 86400.0
+    bs, records = with_hurricane_frames(from_synthetic(deck), deck, read_interval=4, n_records=6, start_jday=start,
+                                        end_jday=end, formular=formular, seed=5)
+    read_steps = [it for it in range(1, 19) if it % 4 == 0 and start <= it * dt / 86400.0 <= end]
+    return bs, dict(zip(read_steps, records))
+
+
+@pytest.mark.parametrize("formular", [1, 3])
+def test_hurricane_frames_equal_oracle(oracle_so, gpu_lib, formular):
+    """Hurricane node frames (read_hurricane_ser_1.f90, calculate_wind_stress.f90:105-137) on the
+    device equal the oracle's bit for bit every step: ramps between reads, reads inside the
+    window, face winds kept after it closes."""
+    deck = estuary(nx=30, ny=12, dx=100.0, n_layers=8, trans_sub_iter=3)
+    st = initial_state(deck)
+    ref = _ctx(deck, st, lib_path=oracle_so)
+    gpu = _ctx(deck, st, lib=gpu_lib)
+    bs, pushes = _hurricane_case(deck, formular)
+    static = HostForcing(deck).static()
+    for c in (ref, gpu):
+        c.set_forcing(static)
+        c.set_boundary_series(bs)
+    for it in range(1, 19):
+        if it in pushes:
+            ref.push_hurricane_frame(pushes[it])
+            gpu.push_hurricane_frame(pushes[it])
+        ref.step_all()
+        gpu.step_all()
+        for name in ("wind_stress_normal", "wind_stress_tangnt", "gamma_t", "air_p"):
+            a, b = gpu.get_field(name), ref.get_field(name)
+            assert np.array_equal(a, b), (it, name, float(np.abs(a - b).max()))
+    assert gpu.status().code == 0
+    for name in ("eta_cell", "un_face", "salt_cell", "temp_cell"):
+        assert _close(gpu.get_field(name), ref.get_field(name)), name
+
+
+def test_hurricane_records_pushed_between_graph_launches(gpu_lib):
+    """Records pushed while earlier captured steps still run are taken at their read step: the
+    launched run ends where the synchronous one does, bit for bit."""
+    deck = estuary(nx=30, ny=12, dx=100.0, n_layers=8, trans_sub_iter=3)
+    st = initial_state(deck)
+    sync = _ctx(deck, st, lib=gpu_lib)
+    lau = _ctx(deck, st, lib=gpu_lib)
+    bs, pushes = _hurricane_case(deck)
+    static = HostForcing(deck).static()
+    for c in (sync, lau):
+        c.set_forcing(static)
+        c.set_boundary_series(bs)
+    for it in range(1, 19):
+        if it in pushes:
+            sync.push_hurricane_frame(pushes[it])
+            lau.push_hurricane_frame(pushes[it])
+        sync.step_all()
+        lau.step_launch()
+    lau.step_wait()
+    for name in ("eta_cell", "un_face", "wind_stress_normal", "air_p", "salt_cell"):
+        assert np.array_equal(lau.get_field(name), sync.get_field(name)), name
