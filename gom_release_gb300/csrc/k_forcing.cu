@@ -99,7 +99,7 @@ __global__ void k_storm_faces(Geom g, const double *scal, const double *storms, 
     double speed = sqrt(u * u + v * v);
     double ct = g.cos_theta[j - 1], sn = g.sin_theta[j - 1];
     double normal = u * ct + v * sn, tangent = -u * sn + v * ct;
-    double cda = fmin(0.001 * (0.75 + 0.067 * speed), 0.003);
+    double cda = fmin(0.001 * (0.75 + 0.067 * speed), (double)0.003f);   // MIN with a default-REAL 0.003
     double gt = cda * rho_ratio * speed;
     wsn[j - 1] = gt * normal * spin;
     wst[j - 1] = gt * tangent * spin;

@@ -245,7 +245,7 @@ def face_wind_stress(deck: Deck, un: np.ndarray, vn: np.ndarray, rho_o: float, s
     speed = np.sqrt(u * u + v * v)
     normal = u * g["cos_theta"] + v * g["sin_theta"]
     tangent = -u * g["sin_theta"] + v * g["cos_theta"]
-    cda = np.minimum(0.001 * (0.75 + 0.067 * speed), 0.003)
+    cda = np.minimum(0.001 * (0.75 + 0.067 * speed), float(np.float32(0.003)))   # a default-REAL 0.003
     gamma_t = cda * (AIR_DENSITY / rho_o) * speed
     return gamma_t * normal * spin, gamma_t * tangent * spin, gamma_t
 
