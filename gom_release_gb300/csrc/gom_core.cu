@@ -643,6 +643,12 @@ int gom_create(const gom_dims *dims, const gom_params *params, const gom_geom *g
         if (e == cudaSuccess) e = dalloc(c, &W.fl_count, 2);
     }
     if (e == cudaSuccess) e = dalloc(c, &W.node_weight, NN);
+    if (!c->mixed && L + 1 <= 64) {
+        if (e == cudaSuccess) e = dalloc(c, &W.nl_list, (size_t)(L + 1) * NN);
+        if (e == cudaSuccess) e = dalloc(c, &W.nl_off, NN);
+        if (e == cudaSuccess) e = dalloc(c, &W.nl_bsum, NN / LIST_BLOCK + 2);
+        if (e == cudaSuccess) e = dalloc(c, &W.nl_count, 2);
+    }
     if (e == cudaSuccess) e = dalloc(c, &W.fs_sums, 3 * NF);
     if (e == cudaSuccess) e = dalloc(c, &W.cons, 2 + 2 * (size_t)((NC + 255) / 256));
     if (e == cudaSuccess) e = dalloc(c, &c->x.status, 1);

@@ -37,6 +37,9 @@ template <typename R> struct WorkT {
     // node velocities: face-level velocity / face length (0:L, NF), static node weights (NN)
     R *uflf = nullptr, *vflf = nullptr;
     double *node_weight = nullptr;
+    // FP64 node velocities: static list of the (node, level + 1) pairs from the lowest level any
+    // face or cell of the node reaches (gom_scan.cuh); null when L + 1 exceeds the list encoding
+    int *nl_list = nullptr, *nl_off = nullptr, *nl_bsum = nullptr, *nl_count = nullptr;
     // turbulence closure: face diffusivity per interface (0:L, NF)
     R *kvf = nullptr;
     // mixed-precision transport: rows of the vertical systems (L, NC) and right-hand sides

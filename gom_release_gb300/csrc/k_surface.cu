@@ -6,6 +6,7 @@
 //   update_vertical_layers_1.f90:18-333, calculate_velocity_at_node.f90:10-140.
 #include "gom_launch.h"
 #include "gom_pcg.cuh"
+#include "gom_scan.cuh"
 
 #include <algorithm>
 #include <vector>
@@ -941,20 +942,38 @@ __global__ void k_node_weight(Geom g, double *node_weight) {
     node_weight[i - 1] = weight;
 }
 
+// the levels of node i (0-based) that a face or a cell of the node reaches, as list layers
+// (level + 1): from min(bottom - 1) over the faces and cells k_node_uvw visits, to L
+struct NodeLevelRange {
+    Geom g;
+    __device__ int2 operator()(int i0) const {
+        const int i = i0 + 1;
+        int lo = g.L + 1;
+        const int na = g.adj_cells_at_node[i - 1];
+        for (int j = 1; j <= na; ++j) {
+            const int isn = g.node_cell(j, i), nc = g.node_count(j, i);
+            const int tq = g.tri_or_quad[isn - 1];
+            for (int l = tq - 2; l <= tq - 1; ++l)
+                lo = min(lo, g.bottom_face[g.cell_face(start_end_node(tq, nc, l), isn) - 1] - 1);
+            lo = min(lo, g.bottom_cell[isn - 1] - 1);
+        }
+        return make_int2(max(lo, 0) + 1, g.L + 1);
+    }
+};
+
 template <typename R> cudaError_t launch_node_weights(const LaunchT<R> &x) {
     k_node_weight<<<blocks_for(x.g.NN, 256), 256, 0, x.stream>>>(x.g, x.w.node_weight);
+    if (x.w.nl_list)
+        return build_layer_list(x.g.NN, NodeLevelRange{x.g}, x.w.nl_off, x.w.nl_bsum, x.w.nl_list, x.w.nl_count,
+                                x.stream);
     return cudaGetLastError();
 }
 
-// :67-138 node u, v (face-length weighted face levels) and w (area-weighted cell w):
-// one thread per (node, level)
-template <typename R> __global__ void k_node_uvw(Geom g, StateT<R> s, WorkT<R> wk) {
-    unsigned tt = flat_tid();
+// :67-138 node u, v (face-length weighted face levels) and w (area-weighted cell w) at one
+// (node, level)
+template <typename R> __device__ __forceinline__ void node_uvw_at(const Geom &g, const StateT<R> &s,
+                                                                  const WorkT<R> &wk, int i, int k) {
     const int L = g.L;
-    if (tt >= (unsigned)g.NN * (L + 1)) return;
-    int i, k;
-    split_index(tt, L + 1, i, k);
-    i += 1;
     R u = R(0), v = R(0);
     int icount = 0;
     int na = g.adj_cells_at_node[i - 1];
@@ -994,6 +1013,27 @@ template <typename R> __global__ void k_node_uvw(Geom g, StateT<R> s, WorkT<R> w
     s.u_node[o] = u;
     s.v_node[o] = v;
     s.w_node[o] = w;
+}
+
+// one thread per (node, level)
+template <typename R> __global__ void k_node_uvw(Geom g, StateT<R> s, WorkT<R> wk) {
+    unsigned tt = flat_tid();
+    if (tt >= (unsigned)g.NN * (g.L + 1)) return;
+    int i, k;
+    split_index(tt, g.L + 1, i, k);
+    node_uvw_at(g, s, wk, i + 1, k);
+}
+
+// FP64: one thread per listed (node, level); the levels below every face and cell of a node are
+// 0 (no face or cell contributes there), written by a fill first.  GB300 issues an FP64 warp
+// instruction at the same cost however few lanes are active, and a node's low levels would leave
+// most lanes of its warps idle.
+template <typename R> __global__ void __launch_bounds__(256) k_node_uvw_list(Geom g, StateT<R> s, WorkT<R> wk) {
+    const int n = *wk.nl_count;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const int code = wk.nl_list[t];
+        node_uvw_at(g, s, wk, list_entity(code), list_layer(code) - 1);
+    }
 }
 
 // FP32 path, the same per node by tiles: a block takes NV_TILE consecutive nodes and lists each
@@ -1082,6 +1122,13 @@ template <typename R> cudaError_t launch_node_velocity(const LaunchT<R> &x) {
         k_face_level<<<blocks_for(x.g.NF, 128), 128, 0, x.stream>>>(x.g, x.s, x.w);
     if constexpr (sizeof(R) == sizeof(float)) {
         k_node_uvw_tile<<<blocks_for(x.g.NN, NV_TILE), 256, 0, x.stream>>>(x.g, x.s, x.w);
+    } else if (x.w.nl_list) {
+        const size_t bytes = (size_t)x.g.NN * (x.g.L + 1) * sizeof(R);
+        cudaError_t e = cudaMemsetAsync(x.s.u_node, 0, bytes, x.stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(x.s.v_node, 0, bytes, x.stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(x.s.w_node, 0, bytes, x.stream);
+        if (e != cudaSuccess) return e;
+        k_node_uvw_list<<<x.num_sms * 8, 256, 0, x.stream>>>(x.g, x.s, x.w);
     } else {
         long n = (long)x.g.NN * (x.g.L + 1);
         k_node_uvw<<<blocks_for(n, 256), 256, 0, x.stream>>>(x.g, x.s, x.w);

@@ -51,6 +51,7 @@ template <typename R> struct TArgs {
     int ntr;          // active tracers
     int tid[2];       // tran_id of each slot: 1 salinity, 2 temperature
     int Nt, sub;      // subcycles, current subcycle
+    R sub_r, sub1_r;  // sub and sub + 1 as R (the conversion done once, not per thread)
     R dt2;
     R inv_nt;         // 1/Nt, used only when Nt is a power of two (exact)
     R theta, om_theta;  // theta and 1 - theta
@@ -77,10 +78,39 @@ template <typename R> __device__ __forceinline__ R filter_margin();
 template <> __device__ __forceinline__ double filter_margin<double>() { return 1e-9; }
 template <> __device__ __forceinline__ float filter_margin<float>() { return 1e-5f; }
 
+// Comparisons on the bit patterns (integer pipe).  GB300's FP64 pipe issues a warp instruction in
+// about 80 cycles per SM sub-partition, comparisons included, so the limiter's sign and size
+// tests run as integer compares; each gives the FP64 comparison's result for every input the
+// caller can pass, NaN and signed zeros included:
+//   is_zero(x)            x == 0
+//   pos_finite_or_inf(x)  x > 0
+//   gt_nonneg(x, y)       x > y    for y >= +0 or NaN (never -0)
+//   lt_of_pos(x, y)       x < y    for x > 0, not NaN
+// Non-negative doubles (floats) are ordered as their bit patterns; an infinity's pattern is the
+// largest of them and a NaN's lies above it (sign clear) or below zero (sign set).
+__device__ __forceinline__ long long fbits(double x) { return __double_as_longlong(x); }
+__device__ __forceinline__ int fbits(float x) { return __float_as_int(x); }
+__device__ __forceinline__ long long inf_bits(double) { return 0x7ff0000000000000LL; }
+__device__ __forceinline__ int inf_bits(float) { return 0x7f800000; }
+__device__ __forceinline__ bool is_zero(double x) { return ((unsigned long long)fbits(x) << 1) == 0ull; }
+__device__ __forceinline__ bool is_zero(float x) { return ((unsigned)fbits(x) << 1) == 0u; }
+template <typename R> __device__ __forceinline__ bool pos_finite_or_inf(R x) {
+    const auto b = fbits(x);
+    return b > 0 && b <= inf_bits(x);
+}
+template <typename R> __device__ __forceinline__ bool gt_nonneg(R x, R y) {
+    const auto xb = fbits(x), yb = fbits(y);
+    return yb >= 0 && yb <= inf_bits(x) && xb > yb && xb <= inf_bits(x);
+}
+template <typename R> __device__ __forceinline__ bool lt_of_pos(R x, R y) {
+    const auto yb = fbits(y);
+    return yb <= inf_bits(x) && fbits(x) < yb;
+}
+
 // fmin(1, 2 D / |Q|) for Q != 0, the quotient formed only when it can be below 1
 template <typename R> __device__ __forceinline__ R diffusive_share(R D, R Q) {
     const R aq = fabs(Q);
-    if (R(2) * D > aq * (R(1) + filter_margin<R>())) return R(1);
+    if (gt_nonneg(R(2) * D, aq * (R(1) + filter_margin<R>()))) return R(1);   // aq > 0 or NaN
     return fmin(R(1), R(2) * D / aq);
 }
 
@@ -130,7 +160,7 @@ template <typename R> __global__ void k_tr_bc(TArgs<R> a) {
             int sg = g.cell_sign(l, i2);
             for (int k = b; k <= tl; ++k) {
                 R dzf = a.s.dz_face[ix(k, j2, L)];
-                R dz_old = dzf + divnt((a.s.dz_face_new[ix(k, j2, L)] - dzf) * (R)a.sub, a);
+                R dz_old = dzf + divnt((a.s.dz_face_new[ix(k, j2, L)] - dzf) * a.sub_r, a);
                 R q2 = (R)g.face_length[j2 - 1] * dz_old *
                        (flip(a.om_theta * a.s.un_face[ix(k, j2, L)], sg) + flip(a.theta * a.s.un_face_new[ix(k, j2, L)], sg));
                 for (int tr = 0; tr < a.ntr; ++tr) {
@@ -158,12 +188,12 @@ template <typename R> __global__ void k_tr_bc(TArgs<R> a) {
 // few lanes are active).  Later subcycles refresh only layers whose thickness changes.
 template <typename R> __device__ __forceinline__ void face_coef_at(const TArgs<R> &a, int j, int k, long t) {
     R dzf = a.s.dz_face[t];
-    R dz_old = dzf + divnt((a.s.dz_face_new[t] - dzf) * (R)a.sub, a);
+    R dz_old = dzf + divnt((a.s.dz_face_new[t] - dzf) * a.sub_r, a);
     R fl = geo<R>(a.g.face_length, a.g.face_length_f, j - 1);
     R Q = fl * dz_old * (a.om_theta * a.s.un_face[t] + a.theta * a.s.un_face_new[t]);
     R D = fl * dz_old * a.s.kh[t] / geo<R>(a.g.delta_j, a.g.delta_j_f, j - 1);
     R d = fmax(R(0), D - R(0.5) * fabs(Q));
-    R phi = Q == R(0) ? R(1) : diffusive_share(D, Q);
+    R phi = is_zero(Q) ? R(1) : diffusive_share(D, Q);
     a.w.qj[t] = Q;
     a.w.dj[t] = d;
     a.w.phij[t] = phi;
@@ -200,11 +230,11 @@ template <typename R> __device__ __forceinline__ void cell_coef_at(const TArgs<R
     R ar = geo<R>(a.g.area, a.g.area_f, i - 1);
     R Q = ar * (a.om_theta * a.s.wn_cell[t] + a.theta * a.s.wn_cell_new[t]);
     R dzh = a.s.dzhalf_cell[t];
-    R dz_old = dzh + divnt((a.s.dzhalf_cell_new[t] - dzh) * (R)a.sub, a);
+    R dz_old = dzh + divnt((a.s.dzhalf_cell_new[t] - dzh) * a.sub_r, a);
     R D = ar * a.s.kv[t] / dz_old;
     a.w.qi[t] = Q;
     a.w.di[t] = fmax(R(0), D - R(0.5) * fabs(Q));
-    a.w.phii[t] = Q == R(0) ? R(1) : diffusive_share(D, Q);
+    a.w.phii[t] = is_zero(Q) ? R(1) : diffusive_share(D, Q);
 }
 
 template <typename R> __global__ void k_tr_cell_coef(TArgs<R> a) {
@@ -269,15 +299,16 @@ __device__ __forceinline__ bool nan_bits(double x) {
 __device__ __forceinline__ bool nan_bits(float x) { return (__float_as_int(x) & 0x7fffffff) > 0x7f800000; }
 
 template <typename R> __device__ __forceinline__ R limited_ratio(int code, R small_phi, R num, R den) {
-    if (den == R(0)) return phi_limit(code, small_phi, R(1));
-    if (code >= 1 && code <= 3 && num != R(0) && !nan_bits(num) && !nan_bits(den)) {
+    if (is_zero(den)) return phi_limit(code, small_phi, R(1));
+    if (code >= 1 && code <= 3 && !is_zero(num) && !nan_bits(num) && !nan_bits(den)) {
         const R m = filter_margin<R>();
-        if ((num < R(0)) != (den < R(0))) return R(0);   // r < 0: every code gives small_phi - small_phi
-        const R an = fabs(num), ad = fabs(den);
-        if (code == 1 && an > ad * (R(1) + m)) return fmax(small_phi, R(1)) - small_phi;
-        if (code == 3 && an > R(2) * ad * (R(1) + m)) return fmax(fmax(small_phi, R(1)), R(2)) - small_phi;
-        if ((code == 1 || code == 3) && small_phi > R(0) && an < small_phi * ad * (R(1) - m) &&
-            (code == 1 || an < R(0.5) * small_phi * ad * (R(1) - m)))
+        // num, den: numbers, neither zero, so a sign bit is the sign of the value
+        if ((fbits(num) ^ fbits(den)) < 0) return R(0);   // r < 0: every code gives small_phi - small_phi
+        const R an = fabs(num), ad = fabs(den);           // > 0; the bounds below are > 0 or +0
+        if (code == 1 && gt_nonneg(an, ad * (R(1) + m))) return fmax(small_phi, R(1)) - small_phi;
+        if (code == 3 && gt_nonneg(an, R(2) * ad * (R(1) + m))) return fmax(fmax(small_phi, R(1)), R(2)) - small_phi;
+        if ((code == 1 || code == 3) && pos_finite_or_inf(small_phi) && lt_of_pos(an, small_phi * ad * (R(1) - m)) &&
+            (code == 1 || lt_of_pos(an, R(0.5) * small_phi * ad * (R(1) - m))))
             return R(0);
     }
     return phi_limit(code, small_phi, num / den);
@@ -294,11 +325,13 @@ template <typename R> __device__ void limiter_column(const TArgs<R> &a, int i) {
     int tq = g.tri_or_quad[i - 1];
     int fj[4] = {0, 0, 0, 0}, nb[4] = {0, 0, 0, 0}, sg[4] = {0, 0, 0, 0};
     bool open[4] = {false, false, false, false};
-    for (int l = 1; l <= tq; ++l) {
-        fj[l - 1] = g.cell_face(l, i);
-        nb[l - 1] = g.cell_adj(l, i);
-        sg[l - 1] = g.cell_sign(l, i);
-        open[l - 1] = face_open(g, fj[l - 1]);
+#pragma unroll
+    for (int l = 0; l < 4; ++l) {   // unrolled: the face arrays stay in registers
+        if (l >= tq) break;
+        fj[l] = g.cell_face(l + 1, i);
+        nb[l] = g.cell_adj(l + 1, i);
+        sg[l] = g.cell_sign(l + 1, i);
+        open[l] = face_open(g, fj[l]);
     }
     R last1[2] = {R(0.0), R(0.0)}, last2[2] = {R(0.0), R(0.0)};
     for (int k = b; k <= tl; ++k) {
@@ -899,12 +932,11 @@ __device__ __forceinline__ void tr_rows64_at(const TArgs<double> &a, int i, int 
     const int L = g.L, NC = g.NC;
     const int tl = a.s.top_cell[i - 1], b = g.bottom_cell[i - 1];
     const double dt2 = a.dt2;
-    const int sub = a.sub;
     const bool lim = a.p.h_flux_limiter > 0 || a.p.v_flux_limiter > 0;
     const double ar = g.area[i - 1];
     const int nvl = tl - b + 1;
     const double dzc = a.s.dz_cell[ix(k, i, L)];
-    const double dz_new = dzc + divnt((a.s.dz_cell_new[ix(k, i, L)] - dzc) * (sub + 1), a);
+    const double dz_new = dzc + divnt((a.s.dz_cell_new[ix(k, i, L)] - dzc) * a.sub1_r, a);
     double am = 0.0, bm, cm = 0.0;   // am: the layer above, cm: the layer below
     if (tl == b) {
         bm = ar * dz_new;
@@ -920,9 +952,15 @@ __device__ __forceinline__ void tr_rows64_at(const TArgs<double> &a, int i, int 
         bm = -am + ar * dz_new - cm;
     }
     const int tq = g.tri_or_quad[i - 1];
+    // GB300 issues an FP64 warp instruction at the same cost however few of its lanes are active,
+    // so the branches below select operands (integer work) and every lane then runs the same FP64
+    // instructions; each lane's operations and their order are those of the column form.  The
+    // tracer loops are unrolled so that the sums stay in registers.
     double sQi[2] = {0, 0}, sQii[2] = {0, 0}, shd[2] = {0, 0}, shl[2] = {0, 0};
     double ck[2] = {0, 0};
-    for (int tr = 0; tr < a.ntr; ++tr) ck[tr] = a.con[ic(k, i, tr, L, NC)];
+#pragma unroll
+    for (int tr = 0; tr < 2; ++tr)
+        if (tr < a.ntr) ck[tr] = a.con[ic(k, i, tr, L, NC)];
     for (int l = 1; l <= tq; ++l) {
         const int fj = g.cell_face(l, i);
         if (!face_open(g, fj)) continue;
@@ -932,55 +970,77 @@ __device__ __forceinline__ void tr_rows64_at(const TArgs<double> &a, int i, int 
         const double q2 = flip(in_face ? a.w.qj[fo] : 0.0, g.cell_sign(l, i));
         const double dface = in_face ? a.w.dj[fo] : 0.0;
         const bool qpos = is_pos(q2), qneg = is_neg(q2);
-        for (int tr = 0; tr < a.ntr; ++tr) {
-            double cik = nb > 0 ? a.con[ic(k, nb, tr, L, NC)] : oqb_value(a, i, k, tr);
-            if (qpos) sQi[tr] = sQi[tr] + fabs(q2) * ck[tr];
-            else if (qneg) sQii[tr] = sQii[tr] + fabs(q2) * cik;
+        const double aq = fabs(q2);
+#pragma unroll
+        for (int tr = 0; tr < 2; ++tr) {
+            if (tr >= a.ntr) break;
+            const double cik = nb > 0 ? a.con[ic(k, nb, tr, L, NC)] : oqb_value(a, i, k, tr);
+            // outflow adds |q2| ck to sQi, inflow |q2| cik to sQii: one product and one sum for
+            // every lane, the sum kept on the side the flux takes (neither for q2 = 0)
+            const double up = aq * (qpos ? ck[tr] : cik);
+            const double acc = (qpos ? sQi[tr] : sQii[tr]) + up;
+            if (qpos) sQi[tr] = acc;
+            else if (qneg) sQii[tr] = acc;
             shd[tr] = shd[tr] + dface * (cik - ck[tr]);
-            double psi = (lim && in_face) ? a.w.psij[(long)tr * g.NF * L + fo] : 0.0;
-            shl[tr] = shl[tr] + psi * fabs(q2) * (ck[tr] - cik);
+            const double psi = (lim && in_face) ? a.w.psij[(long)tr * g.NF * L + fo] : 0.0;
+            shl[tr] = shl[tr] + psi * aq * (ck[tr] - cik);
         }
     }
-    const double dz_old = dzc + divnt((a.s.dz_cell_new[ix(k, i, L)] - dzc) * sub, a);
-    for (int tr = 0; tr < a.ntr; ++tr) {
-        double h_adv = dt2 * (sQii[tr] - sQi[tr]);
-        double h_diff = dt2 * shd[tr];
-        double h_flux = 0.5 * dt2 * shl[tr];
+    const double dz_old = dzc + divnt((a.s.dz_cell_new[ix(k, i, L)] - dzc) * a.sub_r, a);
+    // the vertical terms: interior layers couple both interfaces; the bottom and the top layer
+    // one interface each, in two expressions of the same shape, x1 x2 + y1 y2 and, with the
+    // limiter, p1 d1 + p2 d2, whose operands the layer selects
+    const bool interior = nvl != 1 && k != b && k != tl;
+    const bool edge = nvl != 1 && (k == b || k == tl);
+    const bool bot = k == b;
+    double qlo = 0.0, qhi = 0.0;
+    if (nvl != 1) {
+        if (k > b) qlo = a.w.qi[ix0(k - 1, i, L)];
+        if (k < tl) qhi = a.w.qi[ix0(k, i, L)];
+    }
+    const double qe = bot ? qhi : qlo;   // the one interface of the bottom / top layer
+#pragma unroll
+    for (int tr = 0; tr < 2; ++tr) {
+        if (tr >= a.ntr) break;
+        const double h_adv = dt2 * (sQii[tr] - sQi[tr]);
+        const double h_diff = dt2 * shd[tr];
+        const double h_flux = 0.5 * dt2 * shl[tr];
         double v = ar * dz_old * ck[tr] + h_adv + h_diff;
         if (a.p.h_flux_limiter > 0) v = v + h_flux;
-        if (nvl != 1) {
-            const double *psi = a.w.psii + (long)tr * NC * (L + 1);
-            const double c0 = ck[tr];
-            if (k == b) {
-                double q = a.w.qi[ix0(k, i, L)];
-                double qp = pos_part(q), qm = neg_part(q);
-                double cp1 = a.con[ic(k + 1, i, tr, L, NC)];
-                v = v + dt2 * (-qp * c0 + qm * cp1);
-                if (a.p.v_flux_limiter > 0) {
-                    double ps = lim ? psi[ix0(k, i, L)] : 0.0;
-                    v = v + 0.5 * dt2 * (-ps * qp * (cp1 - c0) + ps * qm * (c0 - cp1));
-                }
-            } else if (k == tl) {
-                double q = a.w.qi[ix0(k - 1, i, L)];
-                double qp = pos_part(q), qm = neg_part(q);
-                double cm1 = a.con[ic(k - 1, i, tr, L, NC)];
-                v = v + dt2 * (qp * cm1 - qm * c0);
-                if (a.p.v_flux_limiter > 0) {
-                    double ps = lim ? psi[ix0(k - 1, i, L)] : 0.0;
-                    v = v + 0.5 * dt2 * (ps * qp * (c0 - cm1) - ps * qm * (cm1 - c0));
-                }
-            } else {
-                double q1 = a.w.qi[ix0(k - 1, i, L)], q = a.w.qi[ix0(k, i, L)];
-                double qp1 = pos_part(q1), qm1 = neg_part(q1);
-                double qp = pos_part(q), qm = neg_part(q);
-                double cm1 = a.con[ic(k - 1, i, tr, L, NC)], cp1 = a.con[ic(k + 1, i, tr, L, NC)];
-                v = v + dt2 * (qp1 * cm1 - qp * c0 + qm * cp1 - qm1 * c0);
-                if (a.p.v_flux_limiter > 0) {
-                    double p1 = lim ? psi[ix0(k - 1, i, L)] : 0.0, p0 = lim ? psi[ix0(k, i, L)] : 0.0;
-                    v = v + 0.5 * dt2 *
-                                (p1 * qp1 * (c0 - cm1) - p0 * qp * (cp1 - c0) + p0 * qm * (c0 - cp1) -
-                                 p1 * qm1 * (cm1 - c0));
-                }
+        const double *psi = a.w.psii + (long)tr * NC * (L + 1);
+        const double c0 = ck[tr];
+        const double cm1 = k > b ? a.con[ic(k - 1, i, tr, L, NC)] : 0.0;
+        const double cp1 = k < tl ? a.con[ic(k + 1, i, tr, L, NC)] : 0.0;
+        double plo = 0.0, phi = 0.0;   // the limiter of the interface below / above
+        if (a.p.v_flux_limiter > 0 && lim && nvl != 1) {
+            plo = k > b ? psi[ix0(k - 1, i, L)] : 0.0;
+            phi = k < tl ? psi[ix0(k, i, L)] : 0.0;
+        }
+        if (interior) {
+            const double qp1 = pos_part(qlo), qm1 = neg_part(qlo);
+            const double qp = pos_part(qhi), qm = neg_part(qhi);
+            v = v + dt2 * (qp1 * cm1 - qp * c0 + qm * cp1 - qm1 * c0);
+            if (a.p.v_flux_limiter > 0) {
+                const double p1 = lim ? plo : 0.0, p0 = lim ? phi : 0.0;
+                v = v + 0.5 * dt2 *
+                            (p1 * qp1 * (c0 - cm1) - p0 * qp * (cp1 - c0) + p0 * qm * (c0 - cp1) -
+                             p1 * qm1 * (cm1 - c0));
+            }
+        } else if (edge) {
+            // bottom: -qp c0 + qm c(k+1); top: qp c(k-1) - qm c0 = qp c(k-1) + (-qm) c0
+            const double qp = pos_part(qe), qm = neg_part(qe);
+            const double cn = bot ? cp1 : cm1;
+            const double x1 = bot ? -qp : qp, x2 = bot ? c0 : cn;
+            const double y1 = bot ? qm : -qm, y2 = bot ? cn : c0;
+            v = v + dt2 * (x1 * x2 + y1 * y2);
+            if (a.p.v_flux_limiter > 0) {
+                // bottom: -ps qp (c(k+1) - c0) + ps qm (c0 - c(k+1));
+                // top:     ps qp (c0 - c(k-1)) - ps qm (c(k-1) - c0)
+                const double ps = lim ? (bot ? phi : plo) : 0.0;
+                const double u1 = bot ? cn : c0, u2 = bot ? c0 : cn;
+                const double p1 = (bot ? -ps : ps) * qp;
+                const double p2 = (bot ? ps : -ps) * qm;
+                v = v + 0.5 * dt2 * (p1 * (u1 - u2) + p2 * (u2 - u1));
             }
         }
         a.w.tr_rhs[((long)tr * NC + i - 1) * L + k - 1] = v;
@@ -1232,6 +1292,8 @@ template <typename R> bool transport_args(const LaunchT<R> &x, TArgs<R> &a) {
     a.om_theta = (R)(1.0 - p.theta);
     a.changed_only = false;
     a.sub = 0;
+    a.sub_r = R(0);
+    a.sub1_r = R(1);
     a.con = x.w.con;
     a.con_new = x.w.con2;
     return true;
@@ -1307,6 +1369,8 @@ template <typename R> cudaError_t launch_transport(const LaunchT<R> &x) {
     R *cur = x.w.con, *nxt = x.w.con2;
     for (int sub = 0; sub < a.Nt; ++sub) {
         a.sub = sub;
+        a.sub_r = (R)sub;
+        a.sub1_r = (R)(sub + 1);
         a.con = cur;
         a.con_new = nxt;
         if (g.NOB + g.NQB > 0) k_tr_bc<<<blocks_for(g.NOB + g.NQB, 128), 128, 0, x.stream>>>(a);
