@@ -166,20 +166,54 @@ __device__ __forceinline__ T calculate_area_t(T x1, T x2, T x3, T y1, T y2, T y3
     return fabs((x1 - x3) * (y2 - y3) - (x2 - x3) * (y1 - y3)) * T(0.5);
 }
 
+// Comparisons on the bit patterns (integer pipe).  GB300's FP64 pipe issues a warp instruction in
+// about 80 cycles per SM sub-partition, comparisons included, so the sign and size tests of the
+// hot kernels run as integer compares; each gives the FP64 comparison's result for every input
+// the caller can pass, NaN and signed zeros included:
+//   is_zero(x)            x == 0
+//   pos_finite_or_inf(x)  x > 0
+//   gt_nonneg(x, y)       x > y    for y >= +0 or NaN (never -0)
+//   lt_of_nonneg(x, y)    x < y    for x with its sign bit clear (+0, positive, +inf, +NaN)
+// Non-negative doubles (floats) are ordered as their bit patterns; an infinity's pattern is the
+// largest of them and a NaN's lies above it (sign clear) or below zero (sign set).
+__device__ __forceinline__ long long fbits(double x) { return __double_as_longlong(x); }
+__device__ __forceinline__ int fbits(float x) { return __float_as_int(x); }
+__device__ __forceinline__ long long inf_bits(double) { return 0x7ff0000000000000LL; }
+__device__ __forceinline__ int inf_bits(float) { return 0x7f800000; }
+__device__ __forceinline__ bool is_zero(double x) { return ((unsigned long long)fbits(x) << 1) == 0ull; }
+__device__ __forceinline__ bool is_zero(float x) { return ((unsigned)fbits(x) << 1) == 0u; }
+template <typename R> __device__ __forceinline__ bool pos_finite_or_inf(R x) {
+    const auto b = fbits(x);
+    return b > 0 && b <= inf_bits(x);
+}
+template <typename R> __device__ __forceinline__ bool gt_nonneg(R x, R y) {
+    const auto xb = fbits(x), yb = fbits(y);
+    return yb >= 0 && yb <= inf_bits(x) && xb > yb && xb <= inf_bits(x);
+}
+__device__ __forceinline__ bool nan_bits(double x) {
+    return (__double_as_longlong(x) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
+}
+__device__ __forceinline__ bool nan_bits(float x) { return (__float_as_int(x) & 0x7fffffff) > 0x7f800000; }
+template <typename R> __device__ __forceinline__ bool lt_of_nonneg(R x, R y) {
+    const auto yb = fbits(y);
+    return yb <= inf_bits(x) && fbits(x) < yb;
+}
+
 // Exact decisions about a rounded quotient fl(num/den) (num >= 0, den > 0) against a constant c,
 // deciding from num and c*den when they are more than 1e-9 apart (far beyond every rounding
-// error involved) and dividing only otherwise.  Same outcome as the division, fewer FP64 ops.
+// error involved) and dividing only otherwise.  Same outcome as the division, fewer FP64 ops;
+// the comparisons on the bit patterns (num >= 0 and c den > 0).
 __device__ __forceinline__ bool quotient_gt(double num, double den, double c) {
     double t = c * den;
-    if (num > t * (1.0 + 1e-9)) return true;
-    if (num < t * (1.0 - 1e-9)) return false;
-    return num / den > c;
+    if (gt_nonneg(num, t * (1.0 + 1e-9))) return true;
+    if (lt_of_nonneg(num, t * (1.0 - 1e-9))) return false;
+    return gt_nonneg(num / den, c);
 }
 __device__ __forceinline__ bool quotient_lt(double num, double den, double c) {
     double t = c * den;
-    if (num < t * (1.0 - 1e-9)) return true;
-    if (num > t * (1.0 + 1e-9)) return false;
-    return num / den < c;
+    if (lt_of_nonneg(num, t * (1.0 - 1e-9))) return true;
+    if (gt_nonneg(num, t * (1.0 + 1e-9))) return false;
+    return lt_of_nonneg(num / den, c);
 }
 
 // set_geometry_1.f90:48-63

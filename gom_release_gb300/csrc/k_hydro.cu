@@ -79,19 +79,25 @@ template <typename R> cudaError_t launch_boundary_velocity(const LaunchT<R> &x) 
 // [0, 1]; the sign test is exact, the upper bound is decided from |delta_i| against |delta|
 // unless the two are within 1e-9 of each other, and tt1 is divided out only for a hit.
 __device__ __forceinline__ int unit_range(double num, double den) {
-    // 1 if fl(num/den) in [0,1], 0 if not (den != 0)
-    if (num == 0.0) return 1;
-    if ((num < 0.0) != (den < 0.0)) return 0;
+    // 1 if fl(num/den) in [0,1], 0 if not (den != 0); the tests on the bit patterns, with NaN
+    // operands on the FP64 comparisons
+    if (is_zero(num)) return 1;
+    if (nan_bits(num) || nan_bits(den)) {
+        if ((num < 0.0) != (den < 0.0)) return 0;
+        return num / den <= 1.0;
+    }
+    if ((fbits(num) ^ fbits(den)) < 0) return 0;   // numbers, neither zero: the sign bits differ
     double an = fabs(num), ad = fabs(den);
-    if (an < ad * (1.0 - 1e-9)) return 1;
-    if (an > ad * (1.0 + 1e-9)) return 0;
-    return num / den <= 1.0;
+    if (lt_of_nonneg(an, ad * (1.0 - 1e-9))) return 1;
+    if (gt_nonneg(an, ad * (1.0 + 1e-9))) return 0;
+    const double q = num / den;   // two numbers of one sign: +0 or more, or NaN (inf / inf)
+    return !nan_bits(q) && fbits(q) <= fbits(1.0);
 }
 
 __device__ __forceinline__ int check_intersection(double x1, double x2, double x3, double x4, double y1, double y2,
                                                   double y3, double y4, double &xin, double &yin) {
     double delta = (x2 - x1) * (y3 - y4) - (y2 - y1) * (x3 - x4);
-    if (delta == 0.0) return 0;
+    if (is_zero(delta)) return 0;
     double delta1 = (x3 - x1) * (y3 - y4) - (y3 - y1) * (x3 - x4);
     if (!unit_range(delta1, delta)) return 0;
     double delta2 = (x2 - x1) * (y3 - y1) - (y2 - y1) * (x3 - x1);
@@ -515,8 +521,8 @@ __device__ int walk_f32(const Geom &g, const StateT<R> &s, int &nnel, double tim
         if (dist > pathl * (1.0f + 0.5e-4f) || dist == 0.0f) {
             const double d = dist64(nel, nel_j);
             const double dprev = prev_el ? dist64(prev_el, prev_l) : pathl0;
-            if (d / dprev > 1.0 + 1.0e-4) return GOM_ELM_OVERSHOOT;
-            if (d == 0.0 || time * d / pathl0 == 0.0) return GOM_ELM_ZERO_REMAIN;
+            if (gt_nonneg(d / dprev, 1.0 + 1.0e-4)) return GOM_ELM_OVERSHOOT;   // d / dprev: +0 or more
+            if (is_zero(d) || is_zero(time * d / pathl0)) return GOM_ELM_ZERO_REMAIN;
         }
         pathl = dist;
         prev_el = nel;
@@ -622,11 +628,11 @@ __device__ int search_straight_line(const Geom &g, const StateT<R> &s, const Par
             int md1 = g.cell_node(start_end_node(tqn, nel_j, 1), nel);
             int md2 = g.cell_node(start_end_node(tqn, nel_j, 2), nel);
             double dist = sqrt((xin - xt) * (xin - xt) + (yin - yt) * (yin - yt));
-            if (dist / pathl > 1.0 + 1.0e-4) return GOM_ELM_OVERSHOOT;
+            if (gt_nonneg(dist / pathl, 1.0 + 1.0e-4)) return GOM_ELM_OVERSHOOT;   // dist / pathl: +0 or more
             zin = zt - dist / pathl * (zt - zin);
             trm = trm * dist / pathl;
             pathl = sqrt((xin - xt) * (xin - xt) + (yin - yt) * (yin - yt));
-            if (pathl == 0.0 || trm == 0.0) return GOM_ELM_ZERO_REMAIN;
+            if (is_zero(pathl) || is_zero(trm)) return GOM_ELM_ZERO_REMAIN;
             int adjc = g.cell_adj(nel_j, nel);
             if (adjc == 0 || top_el(s, adjc) == 0) {
                 int isd = g.cell_face(nel_j, nel);

@@ -78,35 +78,6 @@ template <typename R> __device__ __forceinline__ R filter_margin();
 template <> __device__ __forceinline__ double filter_margin<double>() { return 1e-9; }
 template <> __device__ __forceinline__ float filter_margin<float>() { return 1e-5f; }
 
-// Comparisons on the bit patterns (integer pipe).  GB300's FP64 pipe issues a warp instruction in
-// about 80 cycles per SM sub-partition, comparisons included, so the limiter's sign and size
-// tests run as integer compares; each gives the FP64 comparison's result for every input the
-// caller can pass, NaN and signed zeros included:
-//   is_zero(x)            x == 0
-//   pos_finite_or_inf(x)  x > 0
-//   gt_nonneg(x, y)       x > y    for y >= +0 or NaN (never -0)
-//   lt_of_pos(x, y)       x < y    for x > 0, not NaN
-// Non-negative doubles (floats) are ordered as their bit patterns; an infinity's pattern is the
-// largest of them and a NaN's lies above it (sign clear) or below zero (sign set).
-__device__ __forceinline__ long long fbits(double x) { return __double_as_longlong(x); }
-__device__ __forceinline__ int fbits(float x) { return __float_as_int(x); }
-__device__ __forceinline__ long long inf_bits(double) { return 0x7ff0000000000000LL; }
-__device__ __forceinline__ int inf_bits(float) { return 0x7f800000; }
-__device__ __forceinline__ bool is_zero(double x) { return ((unsigned long long)fbits(x) << 1) == 0ull; }
-__device__ __forceinline__ bool is_zero(float x) { return ((unsigned)fbits(x) << 1) == 0u; }
-template <typename R> __device__ __forceinline__ bool pos_finite_or_inf(R x) {
-    const auto b = fbits(x);
-    return b > 0 && b <= inf_bits(x);
-}
-template <typename R> __device__ __forceinline__ bool gt_nonneg(R x, R y) {
-    const auto xb = fbits(x), yb = fbits(y);
-    return yb >= 0 && yb <= inf_bits(x) && xb > yb && xb <= inf_bits(x);
-}
-template <typename R> __device__ __forceinline__ bool lt_of_pos(R x, R y) {
-    const auto yb = fbits(y);
-    return yb <= inf_bits(x) && fbits(x) < yb;
-}
-
 // fmin(1, 2 D / |Q|) for Q != 0, the quotient formed only when it can be below 1
 template <typename R> __device__ __forceinline__ R diffusive_share(R D, R Q) {
     const R aq = fabs(Q);
@@ -293,10 +264,6 @@ template <typename R> __device__ __forceinline__ R phi_limit(int code, R small_p
 // NaN tests on the bit patterns (integer pipe): a NaN concentration (the heat_option 2 term over
 // a layer of zero old thickness) reaches the limiter sums, and the sign and size filters below
 // are exact only for numbers; with a NaN operand the ratio is formed, as the reference forms it
-__device__ __forceinline__ bool nan_bits(double x) {
-    return (__double_as_longlong(x) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
-}
-__device__ __forceinline__ bool nan_bits(float x) { return (__float_as_int(x) & 0x7fffffff) > 0x7f800000; }
 
 template <typename R> __device__ __forceinline__ R limited_ratio(int code, R small_phi, R num, R den) {
     if (is_zero(den)) return phi_limit(code, small_phi, R(1));
@@ -307,8 +274,8 @@ template <typename R> __device__ __forceinline__ R limited_ratio(int code, R sma
         const R an = fabs(num), ad = fabs(den);           // > 0; the bounds below are > 0 or +0
         if (code == 1 && gt_nonneg(an, ad * (R(1) + m))) return fmax(small_phi, R(1)) - small_phi;
         if (code == 3 && gt_nonneg(an, R(2) * ad * (R(1) + m))) return fmax(fmax(small_phi, R(1)), R(2)) - small_phi;
-        if ((code == 1 || code == 3) && pos_finite_or_inf(small_phi) && lt_of_pos(an, small_phi * ad * (R(1) - m)) &&
-            (code == 1 || lt_of_pos(an, R(0.5) * small_phi * ad * (R(1) - m))))
+        if ((code == 1 || code == 3) && pos_finite_or_inf(small_phi) && lt_of_nonneg(an, small_phi * ad * (R(1) - m)) &&
+            (code == 1 || lt_of_nonneg(an, R(0.5) * small_phi * ad * (R(1) - m))))
             return R(0);
     }
     return phi_limit(code, small_phi, num / den);
@@ -1059,6 +1026,36 @@ __global__ void __launch_bounds__(128) k_tr_rows64_list(TArgs<double> a) {
     }
 }
 
+// the rows over the interior layers, then over the bottom and top layers: each warp then takes
+// one branch of the row's vertical terms (GB300 issues an FP64 warp instruction at the same cost
+// however few lanes take its branch)
+struct InteriorRange {
+    const int *top, *bottom;
+    __device__ int2 operator()(int i) const {
+        const int t = top[i];
+        return make_int2(bottom[i] + 1, t > 0 ? t - 1 : 0);
+    }
+};
+struct EdgeRange {   // entry layer 1: the bottom layer, 2: the top layer (when above the bottom)
+    const int *top, *bottom;
+    __device__ int2 operator()(int i) const {
+        const int t = top[i];
+        return make_int2(1, t <= 0 ? 0 : t > bottom[i] ? 2 : 1);
+    }
+};
+
+template <bool EDGE> __global__ void __launch_bounds__(128) k_tr_rows64_part(TArgs<double> a) {
+    const int *list = EDGE ? a.w.re_list : a.w.ri_list;
+    const int n = *(EDGE ? a.w.re_count : a.w.ri_count);
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const int code = list[t];
+        const int i = list_entity(code);
+        int k = list_layer(code);
+        if (EDGE) k = k == 1 ? a.g.bottom_cell[i - 1] : a.s.top_cell[i - 1];
+        tr_rows64_at(a, i, k);
+    }
+}
+
 __global__ void __launch_bounds__(256) k_tr_rows_cl(TArgs<float> a) {
     const Geom &g = a.g;
     unsigned t = flat_tid();
@@ -1309,8 +1306,13 @@ template <typename R> cudaError_t launch_tr_solve_only(const LaunchT<R> &x) {
         k_tr_rows_cl<<<blocks_for((long)g.NC * g.L, bs_solve), bs_solve, 0, x.stream>>>(a);
         k_tr_thomas_col<<<blocks_for(g.NC, 128), 128, 0, x.stream>>>(a);
     } else if (x.tune[TUNE_TR_SOLVE] == 3 && x.w.tr_a) {
-        // rows from the wet cell-layer list the last transport call built
-        k_tr_rows64_list<<<x.num_sms * 8, 128, 0, x.stream>>>(a);
+        // rows from the wet cell-layer lists the last transport call built
+        if (x.w.ri_list) {
+            k_tr_rows64_part<false><<<x.num_sms * 8, 128, 0, x.stream>>>(a);
+            k_tr_rows64_part<true><<<x.num_sms * 8, 128, 0, x.stream>>>(a);
+        } else {
+            k_tr_rows64_list<<<x.num_sms * 8, 128, 0, x.stream>>>(a);
+        }
         k_tr_thomas_col<<<blocks_for(g.NC, 128), 128, 0, x.stream>>>(a);
     } else {
         k_tr_solve<<<blocks_for(g.NC, bs_solve), bs_solve, 0, x.stream>>>(a);
@@ -1361,6 +1363,15 @@ template <typename R> cudaError_t launch_transport(const LaunchT<R> &x) {
                                               x.stream);
         if (e != cudaSuccess) return e;
     }
+    const bool part_solve = list_solve && x.w.ri_list;
+    if (part_solve) {
+        cudaError_t e = build_layer_list(g.NC, InteriorRange{x.s.top_cell, g.bottom_cell}, x.w.ri_off, x.w.ri_bsum,
+                                         x.w.ri_list, x.w.ri_count, x.stream);
+        if (e == cudaSuccess)
+            e = build_layer_list(g.NC, EdgeRange{x.s.top_cell, g.bottom_cell}, x.w.re_off, x.w.re_bsum, x.w.re_list,
+                                 x.w.re_count, x.stream);
+        if (e != cudaSuccess) return e;
+    }
     const int list_grid = x.num_sms * 8;   // grid-stride over the wet cell-layers
     bool lim = p.h_flux_limiter > 0 || p.v_flux_limiter > 0;
     const int bs_solve = x.tune[TUNE_TR_SOLVE] == 1 ? 64 : x.tune[TUNE_TR_SOLVE] == 2 ? 256 : 128;
@@ -1403,6 +1414,12 @@ template <typename R> cudaError_t launch_transport(const LaunchT<R> &x) {
         }
         if constexpr (sizeof(R) == sizeof(float)) {
             k_tr_rows_list<<<list_grid, bs_solve, 0, x.stream>>>(a);
+            k_tr_thomas_col<<<blocks_for(g.NC, 128), 128, 0, x.stream>>>(a);
+        } else if (part_solve) {
+            if constexpr (sizeof(R) == sizeof(double)) {
+                k_tr_rows64_part<false><<<list_grid, 128, 0, x.stream>>>(a);
+                k_tr_rows64_part<true><<<list_grid, 128, 0, x.stream>>>(a);
+            }
             k_tr_thomas_col<<<blocks_for(g.NC, 128), 128, 0, x.stream>>>(a);
         } else if (list_solve) {
             k_tr_rows64_list<<<list_grid, 128, 0, x.stream>>>(a);
