@@ -216,16 +216,24 @@ TR_SOLVE_BYTES_PER_CELL_LAYER = {"fp64": 144, "mixed": 72}
 SOLVE_TRAFFIC_PER_CELL_LAYER = {
     "k_tr_solve fp64": 393.5,
     "k_tr_solve mixed": 257.7,
-    "k_tr_rows64_list + k_tr_thomas_col fp64": 436.4,
+    "k_tr_rows64_sorted + k_tr_thomas_col fp64": 333.5 + 87.2,
 }
 
 
 # FP64 instructions (DADD + DMUL + DFMA, ncu smsp__sass_thread_inst_executed_op_d{add,mul,fma}_pred_on.sum)
 # per active cell-layer and launch of the FP64 transport solve, from one ncu capture of the medium
-# estuary (349,122 active cell-layers; the count per cell-layer does not depend on the mesh size)
+# estuary (359,706 active cell-layers; the count per cell-layer does not depend on the mesh size)
 SOLVE_FP64_INSTR_PER_CELL_LAYER = {
-    "k_tr_rows64_list + k_tr_thomas_col": 155.6 + 31.9,
+    "k_tr_rows64_sorted + k_tr_thomas_col": 157.3 + 32.0,
     "k_tr_solve": 186.5,
+}
+
+# FP64 warp instructions (ncu smsp__inst_executed_pipe_fp64.sum) per active cell-layer and launch,
+# same capture.  GB300's FP64 pipe takes a warp instruction at one cost however many of its lanes
+# are active, so its issue peak is the thread peak / 32 and this count, not the thread count, is
+# what the pipe spends its time on.
+SOLVE_FP64_WARP_INSTR_PER_CELL_LAYER = {
+    "k_tr_rows64_sorted + k_tr_thomas_col": 5.620 + 1.157,
 }
 
 
@@ -869,7 +877,7 @@ def main():
         solve_bytes = TR_SOLVE_BYTES_PER_CELL_LAYER[args.precision] * ncl
         # FP64 solve variant 3 runs the solve as two kernels (rows per wet cell-layer, column Thomas)
         list_solve = args.precision == "fp64" and tune is not None and tune[2] == 3
-        solve_kernel = "k_tr_rows64_list + k_tr_thomas_col" if list_solve else "k_tr_solve"
+        solve_kernel = "k_tr_rows64_sorted + k_tr_thomas_col" if list_solve else "k_tr_solve"
         traffic = solve_traffic(solve_kernel, args.precision, ncl)
         kernel_label = f"transport solve, one subcycle ({solve_kernel})"
     else:
@@ -890,6 +898,13 @@ def main():
                      "instructions_per_cell_layer": SOLVE_FP64_INSTR_PER_CELL_LAYER[solve_kernel],
                      "peak_fma_gflops": peak_gflops,
                      "peak_source": "measured: gom_measure_fp64_peak (independent FMA chains, CUDA events)"}
+        warp = SOLVE_FP64_WARP_INSTR_PER_CELL_LAYER.get(solve_kernel)
+        if warp is not None:
+            # the pipe's issue rate: warp instructions against the thread peak / 32
+            wach = warp * ncl / (solve_ms * 1e-3) / 1e9
+            roof_fp64["warp_issue"] = {"achieved": wach, "peak": peak_gflops / 2.0 / 32.0,
+                                       "unit": "G FP64 warp instructions/s", "frac": wach / (peak_gflops / 2.0 / 32.0),
+                                       "warp_instructions_per_cell_layer": warp}
     if args.no_phases:
         phases = {}
     else:

@@ -155,16 +155,6 @@ template <typename R> cudaError_t alloc_layered_work(gom_ctx *c, WorkT<R> &W) {
         if (e == cudaSuccess) e = dalloc(c, &W.cl_off, NC);
         if (e == cudaSuccess) e = dalloc(c, &W.cl_bsum, NC / 1024 + 2);
         if (e == cudaSuccess) e = dalloc(c, &W.cl_count, 2);
-        if (sizeof(R) == sizeof(double)) {
-            if (e == cudaSuccess) e = dalloc(c, &W.ri_list, L * NC);
-            if (e == cudaSuccess) e = dalloc(c, &W.ri_off, NC);
-            if (e == cudaSuccess) e = dalloc(c, &W.ri_bsum, NC / 1024 + 2);
-            if (e == cudaSuccess) e = dalloc(c, &W.ri_count, 2);
-            if (e == cudaSuccess) e = dalloc(c, &W.re_list, 2 * NC);
-            if (e == cudaSuccess) e = dalloc(c, &W.re_off, NC);
-            if (e == cudaSuccess) e = dalloc(c, &W.re_bsum, NC / 1024 + 2);
-            if (e == cudaSuccess) e = dalloc(c, &W.re_count, 2);
-        }
     }
     return e;
 }

@@ -47,10 +47,6 @@ template <typename R> struct WorkT {
     R *tr_a = nullptr, *tr_b = nullptr, *tr_c = nullptr, *tr_rhs = nullptr, *tr_last = nullptr;
     // mixed-precision transport: compact list of the wet (cell, layer) pairs and its scan arrays
     int *cl_list = nullptr, *cl_off = nullptr, *cl_bsum = nullptr, *cl_count = nullptr;
-    // FP64 list-form rows: the wet cell-layers split into interior layers (b < k < top) and the
-    // bottom / top layers (entry layer 1 = bottom, 2 = top), so that a warp takes one kind
-    int *ri_list = nullptr, *ri_off = nullptr, *ri_bsum = nullptr, *ri_count = nullptr;
-    int *re_list = nullptr, *re_off = nullptr, *re_bsum = nullptr, *re_count = nullptr;
     // conservation
     double *cons = nullptr;                                     // [volume, salt]
     double *fs_sums = nullptr;                                  // free-surface column sums (3, NF)

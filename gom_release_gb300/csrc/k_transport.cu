@@ -1018,41 +1018,51 @@ __device__ __forceinline__ void tr_rows64_at(const TArgs<double> &a, int i, int 
     a.w.tr_c[o] = am;
 }
 
-__global__ void __launch_bounds__(128) k_tr_rows64_list(TArgs<double> a) {
+// The rows per listed wet cell-layer, each block taking 256 consecutive entries (the layers of
+// about 28 columns) and reordering them in shared memory, interior layers first, then the bottom
+// and top layers: each warp then takes one branch of the row's vertical terms (GB300 issues an
+// FP64 warp instruction at the same cost however few lanes take its branch), and the two kinds of
+// warps of a block work on the same columns at the same time (the neighbours' data is read once).
+constexpr int ROWS_CHUNK = 256;
+
+__global__ void __launch_bounds__(ROWS_CHUNK) k_tr_rows64_sorted(TArgs<double> a) {
+    __shared__ int codes[ROWS_CHUNK];
+    __shared__ int count_in[ROWS_CHUNK / 32], count_edge[ROWS_CHUNK / 32];
     const int n = *a.w.cl_count;
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-        const int code = a.w.cl_list[t];
-        tr_rows64_at(a, list_entity(code), list_layer(code));
-    }
-}
-
-// the rows over the interior layers, then over the bottom and top layers: each warp then takes
-// one branch of the row's vertical terms (GB300 issues an FP64 warp instruction at the same cost
-// however few lanes take its branch)
-struct InteriorRange {
-    const int *top, *bottom;
-    __device__ int2 operator()(int i) const {
-        const int t = top[i];
-        return make_int2(bottom[i] + 1, t > 0 ? t - 1 : 0);
-    }
-};
-struct EdgeRange {   // entry layer 1: the bottom layer, 2: the top layer (when above the bottom)
-    const int *top, *bottom;
-    __device__ int2 operator()(int i) const {
-        const int t = top[i];
-        return make_int2(1, t <= 0 ? 0 : t > bottom[i] ? 2 : 1);
-    }
-};
-
-template <bool EDGE> __global__ void __launch_bounds__(128) k_tr_rows64_part(TArgs<double> a) {
-    const int *list = EDGE ? a.w.re_list : a.w.ri_list;
-    const int n = *(EDGE ? a.w.re_count : a.w.ri_count);
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-        const int code = list[t];
-        const int i = list_entity(code);
-        int k = list_layer(code);
-        if (EDGE) k = k == 1 ? a.g.bottom_cell[i - 1] : a.s.top_cell[i - 1];
-        tr_rows64_at(a, i, k);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int base = blockIdx.x * ROWS_CHUNK; base < n; base += gridDim.x * ROWS_CHUNK) {
+        const int t = base + threadIdx.x;
+        int code = 0, kind = 2;   // 0 interior layer, 1 bottom or top layer, 2 past the list
+        if (t < n) {
+            code = a.w.cl_list[t];
+            const int i = list_entity(code), k = list_layer(code);
+            kind = (k == a.g.bottom_cell[i - 1] || k == a.s.top_cell[i - 1]) ? 1 : 0;
+        }
+        const unsigned in_mask = __ballot_sync(0xffffffffu, kind == 0);
+        const unsigned edge_mask = __ballot_sync(0xffffffffu, kind == 1);
+        if (lane == 0) {
+            count_in[w] = __popc(in_mask);
+            count_edge[w] = __popc(edge_mask);
+        }
+        __syncthreads();
+        int in_before = 0, edge_before = 0, in_total = 0;
+#pragma unroll
+        for (int q = 0; q < ROWS_CHUNK / 32; ++q) {
+            if (q < w) {
+                in_before += count_in[q];
+                edge_before += count_edge[q];
+            }
+            in_total += count_in[q];
+        }
+        const unsigned below = (1u << lane) - 1u;
+        if (kind == 0) codes[in_before + __popc(in_mask & below)] = code;
+        else if (kind == 1) codes[in_total + edge_before + __popc(edge_mask & below)] = code;
+        __syncthreads();
+        if (threadIdx.x < n - base) {
+            const int c = codes[threadIdx.x];
+            tr_rows64_at(a, list_entity(c), list_layer(c));
+        }
+        __syncthreads();   // the next chunk reuses codes and the counts
     }
 }
 
@@ -1306,13 +1316,8 @@ template <typename R> cudaError_t launch_tr_solve_only(const LaunchT<R> &x) {
         k_tr_rows_cl<<<blocks_for((long)g.NC * g.L, bs_solve), bs_solve, 0, x.stream>>>(a);
         k_tr_thomas_col<<<blocks_for(g.NC, 128), 128, 0, x.stream>>>(a);
     } else if (x.tune[TUNE_TR_SOLVE] == 3 && x.w.tr_a) {
-        // rows from the wet cell-layer lists the last transport call built
-        if (x.w.ri_list) {
-            k_tr_rows64_part<false><<<x.num_sms * 8, 128, 0, x.stream>>>(a);
-            k_tr_rows64_part<true><<<x.num_sms * 8, 128, 0, x.stream>>>(a);
-        } else {
-            k_tr_rows64_list<<<x.num_sms * 8, 128, 0, x.stream>>>(a);
-        }
+        // rows from the wet cell-layer list the last transport call built
+        k_tr_rows64_sorted<<<x.num_sms * 3, ROWS_CHUNK, 0, x.stream>>>(a);
         k_tr_thomas_col<<<blocks_for(g.NC, 128), 128, 0, x.stream>>>(a);
     } else {
         k_tr_solve<<<blocks_for(g.NC, bs_solve), bs_solve, 0, x.stream>>>(a);
@@ -1363,15 +1368,7 @@ template <typename R> cudaError_t launch_transport(const LaunchT<R> &x) {
                                               x.stream);
         if (e != cudaSuccess) return e;
     }
-    const bool part_solve = list_solve && x.w.ri_list;
-    if (part_solve) {
-        cudaError_t e = build_layer_list(g.NC, InteriorRange{x.s.top_cell, g.bottom_cell}, x.w.ri_off, x.w.ri_bsum,
-                                         x.w.ri_list, x.w.ri_count, x.stream);
-        if (e == cudaSuccess)
-            e = build_layer_list(g.NC, EdgeRange{x.s.top_cell, g.bottom_cell}, x.w.re_off, x.w.re_bsum, x.w.re_list,
-                                 x.w.re_count, x.stream);
-        if (e != cudaSuccess) return e;
-    }
+
     const int list_grid = x.num_sms * 8;   // grid-stride over the wet cell-layers
     bool lim = p.h_flux_limiter > 0 || p.v_flux_limiter > 0;
     const int bs_solve = x.tune[TUNE_TR_SOLVE] == 1 ? 64 : x.tune[TUNE_TR_SOLVE] == 2 ? 256 : 128;
@@ -1415,14 +1412,9 @@ template <typename R> cudaError_t launch_transport(const LaunchT<R> &x) {
         if constexpr (sizeof(R) == sizeof(float)) {
             k_tr_rows_list<<<list_grid, bs_solve, 0, x.stream>>>(a);
             k_tr_thomas_col<<<blocks_for(g.NC, 128), 128, 0, x.stream>>>(a);
-        } else if (part_solve) {
-            if constexpr (sizeof(R) == sizeof(double)) {
-                k_tr_rows64_part<false><<<list_grid, 128, 0, x.stream>>>(a);
-                k_tr_rows64_part<true><<<list_grid, 128, 0, x.stream>>>(a);
-            }
-            k_tr_thomas_col<<<blocks_for(g.NC, 128), 128, 0, x.stream>>>(a);
         } else if (list_solve) {
-            k_tr_rows64_list<<<list_grid, 128, 0, x.stream>>>(a);
+            if constexpr (sizeof(R) == sizeof(double))
+                k_tr_rows64_sorted<<<x.num_sms * 3, ROWS_CHUNK, 0, x.stream>>>(a);
             k_tr_thomas_col<<<blocks_for(g.NC, 128), 128, 0, x.stream>>>(a);
         } else {
             k_tr_solve<<<blocks_for(g.NC, bs_solve), bs_solve, 0, x.stream>>>(a);
