@@ -900,11 +900,17 @@ def main():
                      "peak_source": "measured: gom_measure_fp64_peak (independent FMA chains, CUDA events)"}
         warp = SOLVE_FP64_WARP_INSTR_PER_CELL_LAYER.get(solve_kernel)
         if warp is not None:
-            # the pipe's issue rate: warp instructions against the thread peak / 32
+            # the pipe's issue rate: warp instructions against the measured warp-instruction rate
+            # (all lanes active, and one lane per warp active for the cost of a divergent warp)
+            from gom_release_gb300.core import measure_fp64_issue
+            wpeak = measure_fp64_issue(lib, 32) / 1e9
+            wone = measure_fp64_issue(lib, 1) / 1e9
             wach = warp * ncl / (solve_ms * 1e-3) / 1e9
-            roof_fp64["warp_issue"] = {"achieved": wach, "peak": peak_gflops / 2.0 / 32.0,
-                                       "unit": "G FP64 warp instructions/s", "frac": wach / (peak_gflops / 2.0 / 32.0),
-                                       "warp_instructions_per_cell_layer": warp}
+            roof_fp64["warp_issue"] = {"achieved": wach, "peak": wpeak, "peak_one_lane": wone,
+                                       "unit": "G FP64 warp instructions/s", "frac": wach / wpeak,
+                                       "warp_instructions_per_cell_layer": warp,
+                                       "peak_source": "measured: gom_measure_fp64_issue (FMA chains, 32 and 1 "
+                                                      "active lanes per warp, CUDA events)"}
     if args.no_phases:
         phases = {}
     else:

@@ -243,6 +243,7 @@ def _bind(lib: C.CDLL) -> C.CDLL:
     lib.gom_stream.argtypes = [vp]
     lib.gom_stream.restype = vp
     lib.gom_measure_fp64_peak.argtypes = [_D]
+    lib.gom_measure_fp64_issue.argtypes = [C.c_int32, _D]
     return lib
 
 
@@ -252,6 +253,16 @@ def measure_fp64_peak(lib: C.CDLL) -> float:
     rc = lib.gom_measure_fp64_peak(C.byref(v))
     if rc != 0:
         raise GomError(rc, "gom_measure_fp64_peak")
+    return v.value
+
+
+def measure_fp64_issue(lib: C.CDLL, active_lanes: int = 32) -> float:
+    """FP64 warp instructions per second with `active_lanes` lanes of every warp working,
+    measured by the library."""
+    v = C.c_double()
+    rc = lib.gom_measure_fp64_issue(int(active_lanes), C.byref(v))
+    if rc != 0:
+        raise GomError(rc, "gom_measure_fp64_issue")
     return v.value
 
 

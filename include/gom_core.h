@@ -664,6 +664,13 @@ int gom_pcg_solve_noalloc(int32_t n_cells, const int32_t *tri_or_quad, const int
  * GOM_E_ARG from a CPU implementation. */
 int gom_measure_fp64_peak(double *gflops);
 
+/* FP64 warp instructions per second of the current GPU with only the first active_lanes (1..32)
+ * lanes of every warp working (no reference counterpart): the same FMA chains as
+ * gom_measure_fp64_peak.  On GB300 the rate does not depend on active_lanes, so a warp
+ * instruction costs the FP64 pipe the same however many lanes take it.  GOM_E_ARG from a CPU
+ * implementation or for a lane count outside 1..32. */
+int gom_measure_fp64_issue(int32_t active_lanes, double *warp_instr_per_s);
+
 /* The CUDA stream (cudaStream_t) all device work of the context is ordered on, so a caller can
  * record events or order its own work against the core.  NULL for a CPU implementation. */
 void *gom_stream(struct gom_ctx *ctx);

@@ -1514,9 +1514,13 @@ int gom_get_status(gom_ctx *c, gom_status *s, int clear) {
 
 int gom_synchronize(gom_ctx *c) { return c ? GOM_OK : GOM_E_ARG; }
 
-// a GPU measurement: nothing to measure on the CPU
+// GPU measurements: nothing to measure on the CPU
 int gom_measure_fp64_peak(double *gflops) {
     if (gflops) *gflops = 0.0;
+    return GOM_E_ARG;
+}
+int gom_measure_fp64_issue(int32_t, double *warp_instr_per_s) {
+    if (warp_instr_per_s) *warp_instr_per_s = 0.0;
     return GOM_E_ARG;
 }
 
