@@ -244,6 +244,7 @@ def _bind(lib: C.CDLL) -> C.CDLL:
     lib.gom_stream.restype = vp
     lib.gom_measure_fp64_peak.argtypes = [_D]
     lib.gom_measure_fp64_issue.argtypes = [C.c_int32, _D]
+    lib.gom_selftest_compares.argtypes = [C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     return lib
 
 
@@ -264,6 +265,15 @@ def measure_fp64_issue(lib: C.CDLL, active_lanes: int = 32) -> float:
     if rc != 0:
         raise GomError(rc, "gom_measure_fp64_issue")
     return v.value
+
+
+def selftest_compares(lib: C.CDLL) -> tuple[int, int]:
+    """(comparisons checked, mismatches) of the library's bit-pattern comparison self-test."""
+    checked, bad = C.c_int64(), C.c_int64()
+    rc = lib.gom_selftest_compares(C.byref(checked), C.byref(bad))
+    if rc != 0:
+        raise GomError(rc, "gom_selftest_compares")
+    return checked.value, bad.value
 
 
 def load_library(path: str | os.PathLike) -> C.CDLL:

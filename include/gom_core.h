@@ -671,6 +671,13 @@ int gom_measure_fp64_peak(double *gflops);
  * implementation or for a lane count outside 1..32. */
 int gom_measure_fp64_issue(int32_t active_lanes, double *warp_instr_per_s);
 
+/* Self-test of the integer comparisons on bit patterns that the kernels use in place of FP
+ * comparisons (no reference counterpart): every helper against the FP comparison it stands for,
+ * on the device, over all pairs of a table of special and ordinary double and float values
+ * (signed zeros, subnormals, infinities, NaNs of both signs).  *checked: comparisons made;
+ * *mismatches: those that differed (0 expected).  GOM_E_ARG from a CPU implementation. */
+int gom_selftest_compares(int64_t *checked, int64_t *mismatches);
+
 /* The CUDA stream (cudaStream_t) all device work of the context is ordered on, so a caller can
  * record events or order its own work against the core.  NULL for a CPU implementation. */
 void *gom_stream(struct gom_ctx *ctx);

@@ -1523,6 +1523,11 @@ int gom_measure_fp64_issue(int32_t, double *warp_instr_per_s) {
     if (warp_instr_per_s) *warp_instr_per_s = 0.0;
     return GOM_E_ARG;
 }
+int gom_selftest_compares(int64_t *checked, int64_t *mismatches) {
+    if (checked) *checked = 0;
+    if (mismatches) *mismatches = 0;
+    return GOM_E_ARG;
+}
 
 int64_t gom_pcg_iterations_total(gom_ctx *c) { return c ? c->pcg_total : 0; }
 
