@@ -139,7 +139,8 @@ class GomBoundarySeries(C.Structure):
         [("wind_spinup_period", C.c_double), ("rho_a", C.c_double), ("wind_station_node", _I)] + \
         [(n, GomSeries) for n in ("wind_u", "wind_v")] + \
         [("hurricane_flag", C.c_int32), ("hurricane_read_interval", C.c_int32), ("hurricane_start_jday", C.c_double),
-         ("hurricane_end_jday", C.c_double), ("hurricane_frames", _D)]
+         ("hurricane_end_jday", C.c_double), ("hurricane_frames", _D), ("hurricane_interp_method", C.c_int32),
+         ("reserved_hurricane", C.c_int32), ("hurricane_track", C.c_double * 6)]
 
 
 class GomMesh(C.Structure):
@@ -221,6 +222,7 @@ def _bind(lib: C.CDLL) -> C.CDLL:
     lib.gom_set_storms.argtypes = [vp, C.c_int32, C.POINTER(GomStorm), C.c_double]
     lib.gom_set_boundary_series.argtypes = [vp, C.POINTER(GomBoundarySeries)]
     lib.gom_push_hurricane_frame.argtypes = [vp, _D]
+    lib.gom_push_hurricane_center.argtypes = [vp, C.c_double, C.c_double, C.c_double]
     lib.gom_geometry_build.argtypes = [C.POINTER(GomMesh), C.POINTER(GomMeshGeometry), C.POINTER(GomStatus)]
     lib.gom_cold_start.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_double]
     lib.gom_autotune.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32)]
@@ -535,7 +537,8 @@ class GomCore:
             hurricane_flag=int(hur.get("flag", 0)), hurricane_read_interval=int(hur.get("read_interval", 1)),
             hurricane_start_jday=float(hur.get("start_jday", 0.0)), hurricane_end_jday=float(hur.get("end_jday", 0.0)),
             hurricane_frames=dbls(np.asarray(frames, np.float64).reshape(3, 3, -1).ravel())
-            if frames is not None else None, **sets)
+            if frames is not None else None, hurricane_interp_method=int(hur.get("interp_method", 1)),
+            hurricane_track=(C.c_double * 6)(*[float(v) for v in hur.get("track", [0.0] * 6)]), **sets)
         self._check(self.lib.gom_set_boundary_series(self.ctx, C.byref(arg)), "set_boundary_series")
 
     def push_hurricane_frame(self, frame) -> None:
@@ -545,6 +548,12 @@ class GomCore:
         if a.shape[1] != self.deck.n_nodes:
             raise ValueError("a hurricane record has one (u, v, p) per node")
         self._check(self.lib.gom_push_hurricane_frame(self.ctx, a.ctypes.data_as(_D)), "push_hurricane_frame")
+
+    def push_hurricane_center(self, x: float, y: float, julian_day: float) -> None:
+        """Method 2: the next hurricane_center record (x, y, julian day), taken with the next
+        frame at the next read step."""
+        self._check(self.lib.gom_push_hurricane_center(self.ctx, float(x), float(y), float(julian_day)),
+                    "push_hurricane_center")
 
     def conservation(self) -> tuple[float, float]:
         v = C.c_double()

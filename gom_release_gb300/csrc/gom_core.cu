@@ -1337,8 +1337,13 @@ int gom_set_boundary_series(gom_ctx *c, const gom_boundary_series *bs) {
     }
     // hurricane node frames: a read interval of at least one step, the three frames, air density
     if (bs->hurricane_flag != 0 && bs->hurricane_flag != 1) return GOM_E_ARG;
-    if (bs->hurricane_flag == 1 && (bs->hurricane_read_interval < 1 || !bs->hurricane_frames || !(bs->rho_a > 0.0)))
+    if (bs->hurricane_flag == 1 && (bs->hurricane_read_interval < 1 || !bs->hurricane_frames || !(bs->rho_a > 0.0) ||
+                                    bs->hurricane_interp_method < 0 || bs->hurricane_interp_method > 2))
         return GOM_E_ARG;
+    // method 2 builds find_neighbour_nodes' lists by brute force over node pairs (as the
+    // reference does): bounded to meshes the reference itself can hold
+    const bool hur2 = bs->hurricane_flag == 1 && bs->hurricane_interp_method == 2;
+    if (hur2 && c->d.n_nodes > (1 << 19)) return GOM_E_ARG;
     CK(cudaStreamSynchronize(c->x.stream));
     series_free(c);
     SeriesDev &S = c->series;
@@ -1404,6 +1409,42 @@ int gom_set_boundary_series(gom_ctx *c, const gom_boundary_series *bs) {
         S.face_u = const_cast<double *>(fu);
         S.face_v = const_cast<double *>(fv);
     }
+    if (e == cudaSuccess && hur2) {
+        double track[12] = {0};
+        for (int k = 0; k < 6; ++k) track[k] = bs->hurricane_track[k];
+        const double *tk = nullptr, *wn = nullptr;
+        const int *tr = nullptr, *cnt = nullptr;
+        e = series_upload(c, &tk, (const double *)track, 12);
+        if (e == cudaSuccess) e = series_upload(c, &tr, (const int *)nullptr, 1);
+        if (e == cudaSuccess) e = series_upload(c, &wn, (const double *)nullptr, 3 * nn);
+        if (e == cudaSuccess) e = series_upload(c, &cnt, (const int *)nullptr, nn);
+        S.hur_track = const_cast<double *>(tk);
+        S.hur_track_ready = const_cast<int *>(tr);
+        S.hur_w1n = const_cast<double *>(wn);
+        // the lists: counts on the device, offsets on the host, then the ids
+        std::vector<int> h_count(nn);
+        std::vector<long long> h_start(nn + 1, 0);
+        if (e == cudaSuccess) e = hurricane_neighbour_counts(c->x.g, const_cast<int *>(cnt), c->x.stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->x.stream);
+        if (e == cudaSuccess) e = cudaMemcpy(h_count.data(), cnt, nn * sizeof(int), cudaMemcpyDeviceToHost);
+        bool empty = false;
+        for (size_t i = 0; i < nn && e == cudaSuccess; ++i) {
+            h_start[i + 1] = h_start[i] + h_count[i];
+            empty = empty || h_count[i] == 0;
+        }
+        if (e == cudaSuccess && empty) {
+            series_free(c);
+            return GOM_E_ARG;   // a node with no neighbour in range: IDW_5 would read outside its list
+        }
+        const long long *st = nullptr;
+        const int *nodes = nullptr;
+        if (e == cudaSuccess) e = series_upload(c, &st, (const long long *)h_start.data(), nn + 1);
+        if (e == cudaSuccess) e = series_upload(c, &nodes, (const int *)nullptr, (size_t)h_start[nn]);
+        if (e == cudaSuccess) e = hurricane_neighbour_fill(c->x.g, st, const_cast<int *>(nodes), c->x.stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->x.stream);
+        S.search_start = st;
+        S.search_nodes = nodes;
+    }
     if (e != cudaSuccess) {
         series_free(c);
         return set_cuda_error(c, e, "gom_set_boundary_series");
@@ -1425,6 +1466,7 @@ int gom_set_boundary_series(gom_ctx *c, const gom_boundary_series *bs) {
     S.hur_start = bs->hurricane_start_jday;
     S.hur_end = bs->hurricane_end_jday;
     S.hur_cda_max = (double)0.003f;
+    S.hur_method = hur2 ? 2 : 1;
     // calculate_wind_stress.f90:20-33: the bounds are default-REAL expressions scaled in double
     const float lo[3] = {0.75f + 0.067f * 4.0f, 0.61f + 0.063f * 6.0f, 0.80f + 0.065f * 1.0f};
     const float hi[3] = {0.75f + 0.067f * 50.0f, 0.61f + 0.063f * 50.0f, 0.80f + 0.065f * 50.0f};
@@ -1447,6 +1489,16 @@ int gom_push_hurricane_frame(gom_ctx *c, const double *frame) {
     cudaError_t e = cudaMemcpyAsync(c->series.hur_next, frame, bytes, cudaMemcpyHostToDevice, c->x.stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->series.hur_ready, 1, sizeof(int), c->x.stream);
     if (e != cudaSuccess) return set_cuda_error(c, e, "gom_push_hurricane_frame");
+    return GOM_OK;
+}
+
+int gom_push_hurricane_center(gom_ctx *c, double x, double y, double julian_day) {
+    if (!c || !c->has_series || c->series.hur_flag != 1 || c->series.hur_method != 2) return GOM_E_ARG;
+    const double rec[3] = {x, y, julian_day};
+    // pageable source: staged before the call returns; ordered after every step already launched
+    cudaError_t e = cudaMemcpyAsync(c->series.hur_track + 6, rec, sizeof(rec), cudaMemcpyHostToDevice, c->x.stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->series.hur_track_ready, 1, sizeof(int), c->x.stream);
+    if (e != cudaSuccess) return set_cuda_error(c, e, "gom_push_hurricane_center");
     return GOM_OK;
 }
 

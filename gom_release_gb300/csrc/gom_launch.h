@@ -156,6 +156,15 @@ struct SeriesDev {
     int *hur_ready;                        // nonzero once a record is pushed, cleared when taken
     double *face_u, *face_v;               // (NF) wind_u_at_face / wind_v_at_face, kept between steps
     double hur_cda_max;                    // MIN(0.003, Cda): the default-REAL 0.003 widened
+    // method 2 (read_hurricane_ser_2.f90, IDW_5.f90): the track [x1, y1, t1, x2, y2, t2], the
+    // pushed centre [6..8], this step's time ratio and centre shift [9..11]; find_neighbour_nodes'
+    // lists (CSR); the blended frame 1 of the step
+    int hur_method;
+    double *hur_track;
+    int *hur_track_ready;
+    const long long *search_start;         // (NN + 1)
+    const int *search_nodes;
+    double *hur_w1n;                       // (NN, 3)
 };
 
 // per-step boundary forcing from the series (k_forcing.cu): advances the device clock in f.scal
@@ -166,6 +175,10 @@ struct SeriesDev {
 // status), q_add and the boundary concentrations of every subcycle
 cudaError_t launch_series_forcing(const Geom &g, const Forcing &f, const Params &p, const SeriesDev &s,
                                   const double *eta_cell, gom_status *status, cudaStream_t stream);
+// find_neighbour_nodes.f90 on the device (hurricane method 2): per node the count of its
+// neighbours in range, then (start: NN + 1 offsets) their 1-based ids in node order
+cudaError_t hurricane_neighbour_counts(const Geom &g, int *count, cudaStream_t stream);
+cudaError_t hurricane_neighbour_fill(const Geom &g, const long long *start, int *nodes, cudaStream_t stream);
 
 // explicit instantiations live in the kernel files
 #define GOM_INSTANTIATE_LAUNCH(fn)                              \

@@ -260,14 +260,101 @@ __device__ __forceinline__ bool hurricane_read_step(const Forcing &f, const Seri
     return (long long)f.scal[5] % S.hur_interval == 0;
 }
 
+// read_hurricane_ser_2.f90:19-83: the storm centre of this step, by one thread before the nodes.
+// A read step moves the first centre to the second and takes the pushed one; otherwise the time
+// ratio and the centre shift of the step are kept for the nodes and the first centre and its
+// time advance (the reference's order).
+__global__ void k_hurricane_track(Forcing f, SeriesDev S, double dt, gom_status *st) {
+    if (threadIdx.x != 0 || blockIdx.x != 0 || !hurricane_window(f, S)) return;
+    double *t = S.hur_track;
+    if (hurricane_read_step(f, S)) {
+        t[0] = t[3];
+        t[1] = t[4];
+        if (*S.hur_track_ready == 0) {
+            record_error(st, GOM_E_ARG, 38, 0, 0, f.scal[5], GOM_ENTITY_OTHER);
+        } else {
+            t[3] = t[6];
+            t[4] = t[7];
+            t[5] = t[8];
+        }
+        *S.hur_track_ready = 0;
+        return;
+    }
+    const double tr = (f.scal[4] - t[2]) / (t[5] - t[2]);
+    const double dx = t[3] - t[0], dy = t[4] - t[1];
+    const double cx = t[0] + dx * tr, cy = t[1] + dy * tr;
+    t[9] = tr;
+    t[10] = dx;
+    t[11] = dy;
+    t[0] = cx;
+    t[1] = cy;
+    t[2] = t[2] + dt / 86400.0;
+}
+
+// IDW_5.f90:36-80 at (xn, yn) over node i's neighbour list (0-based i): the three nearest, the
+// first of equal distances (the list is in node order, as minloc scans it), with the reference's
+// taken-entry value 1.0e15 (default REAL) where the list is shorter than three
+__device__ void idw5(const Geom &g, const SeriesDev &S, int i, double xn, double yn, const double *v, long nn,
+                     double out[3]) {
+    const double far = (double)1.0e15f;
+    const long long s0 = S.search_start[i], cnt = S.search_start[i + 1] - s0;
+    double md[3] = {far, far, far};
+    int nsel[3] = {0, 0, 0};
+    for (long long k = 0; k < cnt; ++k) {
+        const int nd = S.search_nodes[s0 + k];
+        const double dx = xn - g.x_node[nd - 1], dy = yn - g.y_node[nd - 1];
+        const double d = sqrt(dx * dx + dy * dy);
+        // distances are +0 or more (or NaN): the bit-pattern order is their order
+        if (k < 3 || lt_of_nonneg(d, md[2])) {
+            if (k == 0 || lt_of_nonneg(d, md[0])) {
+                md[2] = md[1];
+                nsel[2] = nsel[1];
+                md[1] = md[0];
+                nsel[1] = nsel[0];
+                md[0] = d;
+                nsel[0] = nd;
+            } else if (k == 1 || lt_of_nonneg(d, md[1])) {
+                md[2] = md[1];
+                nsel[2] = nsel[1];
+                md[1] = d;
+                nsel[1] = nd;
+            } else {
+                md[2] = d;
+                nsel[2] = nd;
+            }
+        }
+    }
+    for (int q = (int)(cnt < 3 ? cnt : 3); q < 3; ++q) {   // minloc over taken entries only
+        md[q] = far;
+        nsel[q] = S.search_nodes[s0];
+    }
+    const double r1 = md[1] * md[2], r2 = md[0] * md[2], r3 = md[0] * md[1];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const double *w = v + c * nn;
+        out[c] = (r1 * w[nsel[0] - 1] + r2 * w[nsel[1] - 1] + r3 * w[nsel[2] - 1]) / (r1 + r2 + r3);
+    }
+}
+
 // read_hurricane_ser_1.f90:20-75 at one node: on a read step frames 0 and 1 take frame 2 and
 // frame 2 the pushed record; otherwise frame 1 steps by (frame 2 - frame 0) / real(interval)
-// (the integer widened through default REAL).  air_p (air_p1) follows frame 1.
+// (the integer widened through default REAL), or with method 2 (read_hurricane_ser_2.f90:84-125)
+// frames 1 and 2 are moved with the centre and blended into hur_w1n (k_hurricane_blend copies it
+// into frame 1 once every node has read the old one).  air_p (air_p1) follows frame 1.
 __global__ void k_hurricane_nodes(Geom g, Forcing f, SeriesDev S, gom_status *st) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= g.NN || !hurricane_window(f, S)) return;
     const long nn = g.NN;
     double *w0 = S.hur_frames, *w1 = S.hur_frames + 3 * nn, *w2 = S.hur_frames + 6 * nn;
+    if (S.hur_method == 2 && !hurricane_read_step(f, S)) {
+        const double tr = S.hur_track[9], dx = S.hur_track[10], dy = S.hur_track[11];
+        double o1[3], o2[3];
+        idw5(g, S, i, g.x_node[i] - dx * tr, g.y_node[i] - dy * tr, w1, nn, o1);
+        idw5(g, S, i, g.x_node[i] + dx * (1.0 - tr), g.y_node[i] + dy * (1.0 - tr), w2, nn, o2);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) S.hur_w1n[c * nn + i] = (1.0 - tr) * o1[c] + tr * o2[c];
+        return;
+    }
     if (hurricane_read_step(f, S)) {
         const bool ready = *S.hur_ready != 0;
         if (!ready && i == 0) record_error(st, GOM_E_ARG, 34, 0, 0, f.scal[5], GOM_ENTITY_OTHER);
@@ -286,6 +373,51 @@ __global__ void k_hurricane_nodes(Geom g, Forcing f, SeriesDev S, gom_status *st
             w1[c * nn + i] = w1[c * nn + i] + inc;
         }
     }
+    const_cast<double *>(f.air_p)[i] = w1[2 * nn + i];
+}
+
+// find_neighbour_nodes.f90:19-45 for node i (0-based): its nearest neighbour's distance (with
+// the default-REAL 1.0e15 standing in for itself), the search range (20 km when that neighbour is
+// nearer than 5 km, else four times its distance) and the nodes within it, in node order; pass 0
+// counts, pass 1 writes
+template <int PASS>
+__global__ void k_hur_neighbours(Geom g, int *count, const long long *start, int *nodes) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.NN) return;
+    const double far = (double)1.0e15f;
+    const double xi = g.x_node[i], yi = g.y_node[i];
+    double min_dist = far;
+    for (int ii = 0; ii < g.NN; ++ii) {
+        if (ii == i) continue;
+        const double dx = xi - g.x_node[ii], dy = yi - g.y_node[ii];
+        const double d = sqrt(dx * dx + dy * dy);
+        if (lt_of_nonneg(d, min_dist)) min_dist = d;
+    }
+    const double range = min_dist < 5000.0 ? (double)(20 * 1000.0f) : min_dist * 4;
+    long long o = PASS == 1 ? start[i] : 0;
+    int n = 0;
+    for (int ii = 0; ii < g.NN; ++ii) {
+        double d = far;
+        if (ii != i) {
+            const double dx = xi - g.x_node[ii], dy = yi - g.y_node[ii];
+            d = sqrt(dx * dx + dy * dy);
+        }
+        if (d <= range) {
+            if (PASS == 1) nodes[o++] = ii + 1;
+            ++n;
+        }
+    }
+    if (PASS == 0) count[i] = n;
+}
+
+// method 2, a step between reads: frame 1 takes the blend, air_p follows
+__global__ void k_hurricane_blend(Geom g, Forcing f, SeriesDev S) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.NN || !hurricane_window(f, S) || hurricane_read_step(f, S)) return;
+    const long nn = g.NN;
+    double *w1 = S.hur_frames + 3 * nn;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) w1[c * nn + i] = S.hur_w1n[c * nn + i];
     const_cast<double *>(f.air_p)[i] = w1[2 * nn + i];
 }
 
@@ -465,6 +597,16 @@ cudaError_t launch_storm_forcing(const Geom &g, const Forcing &f, const Params &
     return cudaGetLastError();
 }
 
+cudaError_t hurricane_neighbour_counts(const Geom &g, int *count, cudaStream_t stream) {
+    k_hur_neighbours<0><<<blocks_for(g.NN, 128), 128, 0, stream>>>(g, count, nullptr, nullptr);
+    return cudaGetLastError();
+}
+
+cudaError_t hurricane_neighbour_fill(const Geom &g, const long long *start, int *nodes, cudaStream_t stream) {
+    k_hur_neighbours<1><<<blocks_for(g.NN, 128), 128, 0, stream>>>(g, nullptr, start, nodes);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_series_forcing(const Geom &g, const Forcing &f, const Params &p, const SeriesDev &s,
                                   const double *eta_cell, gom_status *status, cudaStream_t stream) {
     k_series_clock<<<1, 32, 0, stream>>>(const_cast<double *>(f.scal), p.dt, s.tide_per_s, s.bc_per_s, s.wind_per_s);
@@ -473,7 +615,9 @@ cudaError_t launch_series_forcing(const Geom &g, const Forcing &f, const Params 
         k_series_wind_faces<<<blocks_for(g.NF, 256), 256, 0, stream>>>(g, f, s);
     }
     if (s.hur_flag == 1) {
+        if (s.hur_method == 2) k_hurricane_track<<<1, 32, 0, stream>>>(f, s, p.dt, status);
         k_hurricane_nodes<<<blocks_for(g.NN, 256), 256, 0, stream>>>(g, f, s, status);
+        if (s.hur_method == 2) k_hurricane_blend<<<blocks_for(g.NN, 256), 256, 0, stream>>>(g, f, s);
         k_hurricane_faces<<<blocks_for(g.NF, 256), 256, 0, stream>>>(g, f, s);
     }
     const int nt = p.trans_sub_iter > 0 ? p.trans_sub_iter : 1;

@@ -212,6 +212,9 @@ module gom_core_abi
      real(c_double) :: hurricane_start_jday
      real(c_double) :: hurricane_end_jday
      type(c_ptr) :: hurricane_frames
+     integer(c_int32_t) :: hurricane_interp_method
+     integer(c_int32_t) :: reserved_hurricane
+     real(c_double) :: hurricane_track(6)
   end type
 
   type, bind(c) :: gom_mesh
@@ -450,6 +453,11 @@ module gom_core_abi
        import
        type(c_ptr), value :: ctx
        real(c_double), intent(in) :: frame(*)
+     end function
+     integer(c_int) function gom_push_hurricane_center(ctx, x, y, julian_day) bind(c, name="gom_push_hurricane_center")
+       import
+       type(c_ptr), value :: ctx
+       real(c_double), value :: x, y, julian_day
      end function
      integer(c_int) function gom_geometry_build(mesh, out, failure) bind(c, name="gom_geometry_build")
        import
@@ -872,7 +880,10 @@ contains
     bs%hurricane_start_jday = 0.0_dp
     bs%hurricane_end_jday = 0.0_dp
     bs%hurricane_frames = c_null_ptr
-    if (hurricane_flag == 1 .and. hurricane_interp_method == 1) then
+    bs%hurricane_interp_method = 1
+    bs%reserved_hurricane = 0
+    bs%hurricane_track = 0.0_dp
+    if (hurricane_flag == 1 .and. (hurricane_interp_method == 1 .or. hurricane_interp_method == 2)) then
        if (allocated(hframes)) deallocate(hframes)
        allocate(hframes(9 * maxnod))
        hframes(1:maxnod) = wind_u0
@@ -889,6 +900,12 @@ contains
        bs%hurricane_start_jday = hurricane_start_jday
        bs%hurricane_end_jday = hurricane_end_jday
        bs%hurricane_frames = cptr_d(hframes)
+       bs%hurricane_interp_method = hurricane_interp_method
+       if (hurricane_interp_method == 2) then
+          ! read_hurricane_ser_0.f90:58-82: the two centres read so far
+          bs%hurricane_track = (/ hurric_x_1, hurric_y_1, hurricane_time_1, hurric_x_2, hurric_y_2, &
+               hurricane_time_2 /)
+       end if
     end if
     call gom_gpu_check(gom_set_boundary_series(gom_ctx, bs), 'gom_set_boundary_series')
   end subroutine
@@ -1055,5 +1072,36 @@ subroutine read_hurricane_ser_1
      rec(2 * maxnod + i) = rec(2 * maxnod + i) * 100.0_dp
   end do
   call gom_gpu_check(gom_push_hurricane_frame(gom_ctx, rec), 'read_hurricane_ser_1')
+  deallocate(rec)
+end subroutine
+
+subroutine read_hurricane_ser_2
+  ! Method 2: the device moves the frames with the storm centre (IDW_5 over the neighbour lists it
+  ! built); on a read step this replacement only reads the next centre record and the next frame
+  ! (read_hurricane_ser_2.f90:38-60) and hands both to the device, which takes them in this step.
+  use iso_c_binding
+  use gom_core_shim
+  use gom_core_abi
+  use mod_global_variables
+  use mod_file_definition
+  real(c_double), allocatable :: rec(:)
+  integer :: i, j
+  if (mod(it, hurricane_read_interval) /= 0) return
+  read(pw_hurricane_center, *) hurric_year_2, hurric_month_2, hurric_day_2, hurric_hour_2, hurric_minute_2, &
+       hurric_x_2, hurric_y_2, hurric_latitude_2, hurric_delta_pressure_2, hurric_mwr_2
+  call julian(hurric_year_2, hurric_month_2, hurric_day_2, hurric_hour_2, hurric_minute_2, 0, &
+       hurric_julian_day_2, hurric_julian_day_1900_2)
+  call gom_gpu_check(gom_push_hurricane_center(gom_ctx, hurric_x_2, hurric_y_2, hurric_julian_day_2), &
+       'read_hurricane_ser_2')
+  allocate(rec(3 * maxnod))
+  do i = 1, maxnod
+     if (hurricane_data_type == 1) then
+        read(pw_hurricane_ser, *) j, rec(i), rec(maxnod + i), rec(2 * maxnod + i)
+     else
+        read(pw_hurricane_ser) j, rec(i), rec(maxnod + i), rec(2 * maxnod + i)
+     end if
+     rec(2 * maxnod + i) = rec(2 * maxnod + i) * 100.0_dp
+  end do
+  call gom_gpu_check(gom_push_hurricane_frame(gom_ctx, rec), 'read_hurricane_ser_2')
   deallocate(rec)
 end subroutine

@@ -62,8 +62,9 @@ class BoundarySeries:
     series: dict = field(default_factory=dict)
     # station wind (card C30): flag, formular, spinup, spinup_period (days), rho_a, station_node
     wind: dict = field(default_factory=dict)
-    # hurricane node frames (card C31, method 1): flag, read_interval (steps), start_jday, end_jday,
-    # frames (3 frames, 3 components u / v / air_p in Pa, n_nodes) = frames 0, 1 and 2
+    # hurricane node frames (card C31): flag, read_interval (steps), start_jday, end_jday, frames
+    # (3 frames, 3 components u / v / air_p in Pa, n_nodes) = frames 0, 1 and 2, interp_method
+    # (1 or 2), and for method 2 the track [x1, y1, t1, x2, y2, t2] (julian days)
     hurricane: dict = field(default_factory=dict)
 
     def flat(self, kind: str):
@@ -190,6 +191,14 @@ def with_station_wind(bs: BoundarySeries, deck, n_stations: int, *, hours: float
     return replace(bs, series=series, wind=wind)
 
 
+def hurricane_center(deck, k: int) -> tuple[float, float]:
+    """Centre of record k of ``hurricane_record``: it crosses the mesh from west to east one tenth
+    of its width per record, along the middle."""
+    x, y = deck.geo["x_node"], deck.geo["y_node"]
+    x0, x1, y0, y1 = float(x.min()), float(x.max()), float(y.min()), float(y.max())
+    return x0 + 0.1 * k * (x1 - x0), y0 + 0.5 * (y1 - y0)
+
+
 def hurricane_record(deck, k: int, *, radius: float = 0.0, seed: int = 0) -> np.ndarray:
     """Record k of a seeded synthetic hurricane_ser.inp, shape (3, n_nodes): a vortex (peak wind
     about 35 m/s at `radius`, default a quarter of the mesh's width; central pressure 60 hPa below
@@ -200,7 +209,7 @@ def hurricane_record(deck, k: int, *, radius: float = 0.0, seed: int = 0) -> np.
     x0, x1, y0, y1 = float(x.min()), float(x.max()), float(y.min()), float(y.max())
     width = max(x1 - x0, y1 - y0)
     rmax = radius if radius > 0.0 else 0.25 * width
-    cx, cy = x0 + 0.1 * k * (x1 - x0), y0 + 0.5 * (y1 - y0)
+    cx, cy = hurricane_center(deck, k)
     bu, bv = rng.uniform(-3.0, 3.0, size=2)
     dx, dy = x - cx, y - cy
     r = np.sqrt(dx * dx + dy * dy) + 1.0
@@ -212,22 +221,34 @@ def hurricane_record(deck, k: int, *, radius: float = 0.0, seed: int = 0) -> np.
 
 
 def with_hurricane_frames(bs: BoundarySeries, deck, *, read_interval: int, n_records: int, start_jday: float,
-                          end_jday: float, formular: int = 1, rho_a: float = 1.2, seed: int = 0):
-    """`bs` with hurricane node frames (card C31, hurricane_interp_method 1) as read_hurricane_ser_0.f90
-    leaves them: frame 0 = record 0, frame 2 = record 1, frame 1 all zero; and the list of the
-    records 2 .. n_records - 1 to push with ``GomCore.push_hurricane_frame`` before each read step.
-    The drag formula and air density are the station wind's (``wind`` keeps its flag)."""
+                          end_jday: float, formular: int = 1, rho_a: float = 1.2, seed: int = 0,
+                          interp_method: int = 1, record_days: float = 0.0):
+    """`bs` with hurricane node frames (card C31) as read_hurricane_ser_0.f90 leaves them: frame 0 =
+    record 0, frame 2 = record 1, frame 1 all zero; and the list of the records 2 .. n_records - 1
+    to push with ``GomCore.push_hurricane_frame`` before each read step.  With interp_method 2
+    the track holds the centres of records 0 and 1 at julian days start_jday and start_jday +
+    record_days, and ``hurricane_centers`` gives the later ones.  The drag formula and air density
+    are the station wind's (``wind`` keeps its flag)."""
     from dataclasses import replace
 
     recs = [hurricane_record(deck, k, seed=seed + k) for k in range(n_records)]
     frames = np.stack([recs[0], np.zeros_like(recs[0]), recs[1]])
     hur = dict(flag=1, read_interval=int(read_interval), start_jday=float(start_jday), end_jday=float(end_jday),
-               frames=frames)
+               frames=frames, interp_method=int(interp_method))
+    if interp_method == 2:
+        (xa, ya), (xb, yb) = hurricane_center(deck, 0), hurricane_center(deck, 1)
+        hur["track"] = [xa, ya, float(start_jday), xb, yb, float(start_jday) + float(record_days)]
     wind = dict(bs.wind) if bs.wind else dict(flag=0, spinup=0, spinup_period=0.0)
     wind.setdefault("formular", int(formular))
     wind.setdefault("rho_a", float(rho_a))
     return replace(bs, hurricane=hur, wind=wind), recs[2:]
 
 
+def hurricane_centers(deck, n_records: int, start_jday: float, record_days: float) -> list:
+    """(x, y, julian day) of the centres of records 2 .. n_records - 1 (method 2), to push with
+    ``GomCore.push_hurricane_center`` alongside their frames."""
+    return [(*hurricane_center(deck, k), float(start_jday) + k * float(record_days)) for k in range(2, n_records)]
+
+
 __all__ = ["BoundarySeries", "from_deck_data", "from_synthetic", "with_station_wind", "hurricane_record",
-           "with_hurricane_frames"]
+           "hurricane_center", "hurricane_centers", "with_hurricane_frames"]

@@ -458,14 +458,17 @@ typedef struct gom_boundary_series {
     double rho_a;                   /* card C1 air density (kg/m3)                              */
     const int32_t *wind_station_node; /* (n_wind) windp_station_node                            */
     gom_series wind_u, wind_v;      /* per station: windp_u, windp_v on windp_ser_time          */
-    /* hurricane wind fields (card C31: hurricane_flag 1, hurricane_interp_method 1): node frames of
-     * hurricane_ser.inp taken every hurricane_read_interval steps while julian_day lies in
-     * [hurricane_start_jday, hurricane_end_jday] (main.f90:115-127); between two reads the node
-     * winds and air pressure step linearly, face winds are their node means
-     * (read_hurricane_ser_1.f90), and every step forms the hurricane drag law of
+    /* hurricane wind fields (card C31: hurricane_flag 1): node frames of hurricane_ser.inp taken
+     * every hurricane_read_interval steps while julian_day lies in [hurricane_start_jday,
+     * hurricane_end_jday] (main.f90:115-127).  Between two reads the node winds and air pressure
+     * step linearly (hurricane_interp_method 1, read_hurricane_ser_1.f90) or are the two frames
+     * moved with the storm centre and blended (method 2, read_hurricane_ser_2.f90 with IDW_5.f90
+     * over the neighbour lists of find_neighbour_nodes.f90, built on the device); face winds are
+     * their node means, and every step forms the hurricane drag law of
      * calculate_wind_stress.f90:105-137 (Cda <= 0.003) into wind_stress_normal / tangnt and
      * Gamma_T, and air_p from the node pressure.  Each frame after the first two comes from
-     * gom_push_hurricane_frame. */
+     * gom_push_hurricane_frame, each centre after the first two (method 2) from
+     * gom_push_hurricane_center. */
     int32_t hurricane_flag;         /* 1: hurricane node frames                                 */
     int32_t hurricane_read_interval;/* int(hurricane_dt / dt) >= 1 (read_hurricane_ser_0.f90:27) */
     double hurricane_start_jday;    /* find_hurricane_start_end_jday                            */
@@ -473,6 +476,10 @@ typedef struct gom_boundary_series {
     const double *hurricane_frames; /* (N_n, 3, 3): (wind_u, wind_v, air_p in Pa) of frames 0, 1
                                        and 2 = wind_u0.., wind_u1.., wind_u2.. as the driver holds
                                        them (after read_hurricane_ser_0 frame 1 is all zero)    */
+    int32_t hurricane_interp_method;/* 1 (or 0) linear in time, 2 moved with the storm centre     */
+    int32_t reserved_hurricane;
+    double hurricane_track[6];      /* method 2: hurric_x_1, hurric_y_1, hurricane_time_1,
+                                       hurric_x_2, hurric_y_2, hurricane_time_2 (julian days)   */
 } gom_boundary_series;
 int gom_set_boundary_series(struct gom_ctx *ctx, const gom_boundary_series *series);
 
@@ -483,6 +490,12 @@ int gom_set_boundary_series(struct gom_ctx *ctx, const gom_boundary_series *seri
  * Ordered on the context's stream: a record may be pushed while earlier steps still run.
  * Replaces the record read of read_hurricane_ser_1.f90:34-46. */
 int gom_push_hurricane_frame(struct gom_ctx *ctx, const double *frame);
+
+/* Method 2: the next hurricane_center record (its x, y and julian day, as julian.f90 converts
+ * it), taken with the next frame at the next read step (read_hurricane_ser_2.f90:38-45); call
+ * once before each read step.  A read step with no centre pushed records GOM_E_ARG in the step
+ * status.  GOM_E_ARG unless the context holds method-2 hurricane frames. */
+int gom_push_hurricane_center(struct gom_ctx *ctx, double x, double y, double julian_day);
 
 /* ------------------------------------------------------------------ mesh geometry on the device
  * The start-up geometry of GOM built on the GPU: the areas of read_cell_inp.f90:54-87,

@@ -129,10 +129,15 @@ struct gom_ctx {
     std::vector<int32_t> wind_node;
     // hurricane node frames (read_hurricane_ser_0/1.f90): wind_u0.. / wind_u1.. / wind_u2.. as
     // (NN, 3, 3), the pushed record, wind_u_at_face / wind_v_at_face
-    int hur_flag = 0, hur_interval = 1;
-    bool hur_ready = false;
+    int hur_flag = 0, hur_interval = 1, hur_method = 1;
+    bool hur_ready = false, track_ready = false;
     double hur_start = 0, hur_end = 0;
     std::vector<double> hur_frames, hur_next, face_u, face_v;
+    // method 2 (read_hurricane_ser_2.f90): hurric_x_1, hurric_y_1, hurricane_time_1, hurric_x_2,
+    // hurric_y_2, hurricane_time_2, the pushed centre, and find_neighbour_nodes' lists (CSR)
+    double track[6] = {0, 0, 0, 0, 0, 0}, track_next[3] = {0, 0, 0};
+    std::vector<int64_t> search_start;
+    std::vector<int32_t> search_nodes;
     std::vector<int32_t> ob_type, ob_h, ob_eta, ob_salt, ob_temp, qb_q, qb_salt, qb_temp, h_start;
     std::vector<double> qb_portion, h_amp, h_per, h_nodal, h_eq, h_ph, h_shift;
     std::vector<double> eta_at_ob_old, eta_at_ob_new, q_add, wind_stress_normal, wind_stress_tangnt, gamma_t,
@@ -1027,6 +1032,10 @@ int gom_set_storms(gom_ctx *c, int32_t, const gom_storm *, double) { return c ? 
 // compute_boundary_eta.f90:22-125 (types 1 and 2), calculate_Q.f90:21-75, setup_spinup.f90:12-31 and
 // the boundary concentrations of solve_transport_equation_v19.f90:229-382, with a time outside a
 // series keeping that entry's previous value (the reference's value there is undefined)
+namespace {
+bool find_neighbour_nodes(gom_ctx *c);   // hurricane method 2 (defined with the series forcing)
+}  // namespace
+
 int gom_set_boundary_series(gom_ctx *c, const gom_boundary_series *bs) {
     if (!c || !bs || c->d.n_runs > 1) return GOM_E_ARG;
     const gom_series *sets[4] = {&bs->eta, &bs->q, &bs->salt, &bs->temp};
@@ -1065,7 +1074,8 @@ int gom_set_boundary_series(gom_ctx *c, const gom_boundary_series *bs) {
         return GOM_E_ARG;
     if (bs->q_interp_method != 1 && bs->q_interp_method != 2) return GOM_E_ARG;
     if (bs->hurricane_flag != 0 && bs->hurricane_flag != 1) return GOM_E_ARG;
-    if (bs->hurricane_flag == 1 && (bs->hurricane_read_interval < 1 || !bs->hurricane_frames || !(bs->rho_a > 0.0)))
+    if (bs->hurricane_flag == 1 && (bs->hurricane_read_interval < 1 || !bs->hurricane_frames || !(bs->rho_a > 0.0) ||
+                                    bs->hurricane_interp_method < 0 || bs->hurricane_interp_method > 2))
         return GOM_E_ARG;
     if (bs->wind_flag != 0 && bs->wind_flag != 1) return GOM_E_ARG;
     if (bs->wind_flag == 1) {
@@ -1161,6 +1171,18 @@ int gom_set_boundary_series(gom_ctx *c, const gom_boundary_series *bs) {
     c->hur_next.assign(c->hur_flag == 1 ? 3 * (size_t)c->NN : 0, 0.0);
     c->face_u.assign(c->NF, 0.0);
     c->face_v.assign(c->NF, 0.0);
+    c->hur_method = (c->hur_flag == 1 && bs->hurricane_interp_method == 2) ? 2 : 1;
+    c->track_ready = false;
+    c->search_start.clear();
+    c->search_nodes.clear();
+    if (c->hur_flag == 1 && c->hur_method == 2) {
+        for (int k = 0; k < 6; ++k) c->track[k] = bs->hurricane_track[k];
+        if (!find_neighbour_nodes(c)) {
+            c->hur_flag = 0;
+            c->has_series = false;
+            return GOM_E_ARG;   // a node with no neighbour in range: IDW_5 would read outside its list
+        }
+    }
     {
         const float lo[3] = {0.75f + 0.067f * 4.0f, 0.61f + 0.063f * 6.0f, 0.80f + 0.065f * 1.0f};
         const float hi[3] = {0.75f + 0.067f * 50.0f, 0.61f + 0.063f * 50.0f, 0.80f + 0.065f * 50.0f};
@@ -1293,8 +1315,65 @@ void station_wind(gom_ctx *c, double elapsed, double u2) {
     }
 }
 
-// main.f90:115-127 with read_hurricane_ser_1.f90:20-86 (julian_day inside the window), then the
-// hurricane branch of calculate_wind_stress.f90:105-137 on every face
+// IDW_5.f90:36-80 at the point (xn, yn) over node i's neighbour list: the three nearest (minloc:
+// the first of equal distances; a taken entry becomes the default-REAL 1.0e15), weighted by the
+// products of the other two distances (power 1)
+void idw5(const gom_ctx *c, int i, double xn, double yn, const double *v, size_t nn, double out[3]) {
+    const double far = (double)1.0e15f;
+    const int64_t s0 = c->search_start[i - 1], cnt = c->search_start[i] - s0;
+    std::vector<double> dist(cnt);
+    for (int64_t k = 0; k < cnt; ++k) {
+        const int nd = c->search_nodes[s0 + k];
+        const double dx = xn - c->x_node(nd), dy = yn - c->y_node(nd);
+        dist[k] = std::sqrt(dx * dx + dy * dy);
+    }
+    int nsel[3];
+    double md[3];
+    for (int q = 0; q < 3; ++q) {
+        int64_t ii = 0;
+        for (int64_t k = 1; k < cnt; ++k)
+            if (dist[k] < dist[ii]) ii = k;
+        nsel[q] = c->search_nodes[s0 + ii];
+        md[q] = dist[ii];
+        dist[ii] = far;
+    }
+    const double r1 = md[1] * md[2], r2 = md[0] * md[2], r3 = md[0] * md[1];
+    for (int comp = 0; comp < 3; ++comp) {
+        const double *w = v + comp * nn;
+        out[comp] = (r1 * w[nsel[0] - 1] + r2 * w[nsel[1] - 1] + r3 * w[nsel[2] - 1]) / (r1 + r2 + r3);
+    }
+}
+
+// find_neighbour_nodes.f90:19-45: every node within 20 km of a node (when its nearest neighbour is
+// nearer than 5 km) or within four times that nearest distance, in node order; false when a node
+// has none (IDW_5 would then read outside its list)
+bool find_neighbour_nodes(gom_ctx *c) {
+    const double far = (double)1.0e15f;
+    const int nn = c->NN;
+    c->search_start.assign(nn + 1, 0);
+    std::vector<double> dist(nn);
+    for (int i = 1; i <= nn; ++i) {
+        double min_dist = far;
+        for (int ii = 1; ii <= nn; ++ii) {
+            if (ii == i) {
+                dist[ii - 1] = far;
+            } else {
+                const double dx = c->x_node(i) - c->x_node(ii), dy = c->y_node(i) - c->y_node(ii);
+                dist[ii - 1] = std::sqrt(dx * dx + dy * dy);
+            }
+            if (dist[ii - 1] < min_dist) min_dist = dist[ii - 1];
+        }
+        const double range = min_dist < 5000 ? (double)(20 * 1000.0f) : min_dist * 4;
+        for (int ii = 1; ii <= nn; ++ii)
+            if (dist[ii - 1] <= range) c->search_nodes.push_back(ii);
+        c->search_start[i] = (int64_t)c->search_nodes.size();
+        if (c->search_start[i] == c->search_start[i - 1]) return false;
+    }
+    return true;
+}
+
+// main.f90:115-127 with read_hurricane_ser_1.f90:20-86 or read_hurricane_ser_2.f90:19-146 (julian_day
+// inside the window), then the hurricane branch of calculate_wind_stress.f90:105-137 on every face
 void hurricane_wind(gom_ctx *c, double spin_w) {
     const size_t nn = (size_t)c->NN;
     double *w0 = c->hur_frames.data(), *w1 = w0 + 3 * nn, *w2 = w0 + 6 * nn;
@@ -1306,10 +1385,40 @@ void hurricane_wind(gom_ctx *c, double spin_w) {
                 w0[q] = w2[q];
                 w1[q] = w2[q];
             }
+            if (c->hur_method == 2) {
+                // read_hurricane_ser_2.f90:35-45: the centre moves on to the next record
+                c->track[0] = c->track[3];
+                c->track[1] = c->track[4];
+                if (!c->track_ready) {
+                    set_err(c, GOM_E_ARG, 38, 0, 0, (double)c->step_no, GOM_ENTITY_OTHER);
+                } else {
+                    c->track[3] = c->track_next[0];
+                    c->track[4] = c->track_next[1];
+                    c->track[5] = c->track_next[2];
+                }
+                c->track_ready = false;
+            }
             // the record of :34-46 (pushed by the driver)
             if (!c->hur_ready) set_err(c, GOM_E_ARG, 34, 0, 0, (double)c->step_no, GOM_ENTITY_OTHER);
             else std::copy(c->hur_next.begin(), c->hur_next.end(), w2);
             c->hur_ready = false;
+        } else if (c->hur_method == 2) {
+            // read_hurricane_ser_2.f90:73-134: both frames moved with the centre and blended
+            const double tr = (c->jday - c->track[2]) / (c->track[5] - c->track[2]);
+            const double dxc = c->track[3] - c->track[0], dyc = c->track[4] - c->track[1];
+            const double cx = c->track[0] + dxc * tr, cy = c->track[1] + dyc * tr;
+            c->track[0] = cx;
+            c->track[1] = cy;
+            c->track[2] = c->track[2] + c->p.dt / 86400.0;
+            std::vector<double> w1n(3 * nn), w2n(3 * nn);
+            for (size_t i = 1; i <= nn; ++i) {
+                double o[3];
+                idw5(c, (int)i, c->x_node((int)i) - dxc * tr, c->y_node((int)i) - dyc * tr, w1, nn, o);
+                for (int comp = 0; comp < 3; ++comp) w1n[comp * nn + i - 1] = o[comp];
+                idw5(c, (int)i, c->x_node((int)i) + dxc * (1.0 - tr), c->y_node((int)i) + dyc * (1.0 - tr), w2, nn, o);
+                for (int comp = 0; comp < 3; ++comp) w2n[comp * nn + i - 1] = o[comp];
+            }
+            for (size_t q = 0; q < 3 * nn; ++q) w1[q] = (1.0 - tr) * w1n[q] + tr * w2n[q];
         } else {
             const double den = (double)(float)c->hur_interval;   // real(hurricane_read_interval)
             for (size_t q = 0; q < 3 * nn; ++q) {
@@ -3294,6 +3403,15 @@ int gom_push_hurricane_frame(gom_ctx *c, const double *frame) {
     if (!c || !frame || !c->has_series || c->hur_flag != 1) return GOM_E_ARG;
     c->hur_next.assign(frame, frame + 3 * (size_t)c->NN);
     c->hur_ready = true;
+    return GOM_OK;
+}
+
+int gom_push_hurricane_center(gom_ctx *c, double x, double y, double julian_day) {
+    if (!c || !c->has_series || c->hur_flag != 1 || c->hur_method != 2) return GOM_E_ARG;
+    c->track_next[0] = x;
+    c->track_next[1] = y;
+    c->track_next[2] = julian_day;
+    c->track_ready = true;
     return GOM_OK;
 }
 

@@ -341,3 +341,114 @@ def test_hurricane_read_step_without_a_record(oracle_so):
     for bad in (dict(bs.hurricane, read_interval=0), dict(bs.hurricane, flag=2), dict(bs.hurricane, frames=None)):
         with pytest.raises(GomError):
             c.set_boundary_series(replace(bs, hurricane=bad))
+
+
+class _Hurricane2Host(_HurricaneHost):
+    """read_hurricane_ser_2.f90:19-146 with find_neighbour_nodes.f90 and IDW_5.f90 restated in
+    numpy: the frames moved with the storm centre between reads."""
+
+    FAR = float(np.float32(1.0e15))
+
+    def __init__(self, deck, bs):
+        super().__init__(deck, bs)
+        self.track = list(bs.hurricane["track"])
+        self.next_center = None
+        x, y = deck.geo["x_node"], deck.geo["y_node"]
+        self.lists = []
+        for i in range(len(x)):
+            d = np.sqrt((x[i] - x) * (x[i] - x) + (y[i] - y) * (y[i] - y))
+            d[i] = self.FAR
+            md = d.min()
+            rng = 20000.0 if md < 5000 else md * 4
+            self.lists.append(np.nonzero(d <= rng)[0])
+
+    def idw5(self, i, xn, yn, v):
+        x, y = self.deck.geo["x_node"], self.deck.geo["y_node"]
+        lst = self.lists[i]
+        d = np.sqrt((xn - x[lst]) * (xn - x[lst]) + (yn - y[lst]) * (yn - y[lst]))
+        sel, md = [], []
+        for _ in range(3):
+            ii = int(np.argmin(d))
+            sel.append(lst[ii])
+            md.append(d[ii])
+            d[ii] = self.FAR
+        r1, r2, r3 = md[1] * md[2], md[0] * md[2], md[0] * md[1]
+        return (r1 * v[:, sel[0]] + r2 * v[:, sel[1]] + r3 * v[:, sel[2]]) / (r1 + r2 + r3)
+
+    def step(self, it, julian_day):
+        h = self.h
+        w0, w1, w2 = self.frames
+        inside = h["start_jday"] <= julian_day <= h["end_jday"]
+        if inside and it % h["read_interval"] != 0:
+            t = self.track
+            tr = (julian_day - t[2]) / (t[5] - t[2])
+            dx, dy = t[3] - t[0], t[4] - t[1]
+            t[0], t[1] = t[0] + dx * tr, t[1] + dy * tr
+            t[2] = t[2] + self.deck.params.dt / 86400.0
+            x, y = self.deck.geo["x_node"], self.deck.geo["y_node"]
+            new = np.empty_like(w1)
+            for i in range(len(x)):
+                a = self.idw5(i, x[i] - dx * tr, y[i] - dy * tr, w1)
+                b = self.idw5(i, x[i] + dx * (1.0 - tr), y[i] + dy * (1.0 - tr), w2)
+                new[:, i] = (1.0 - tr) * a + tr * b
+            w1[:] = new
+            a = self.deck.geo
+            n1, n2 = a["nodenum_at_face"][:, 0] - 1, a["nodenum_at_face"][:, 1] - 1
+            self.face_u = (w1[0][n1] + w1[0][n2]) * 0.5
+            self.face_v = (w1[1][n1] + w1[1][n2]) * 0.5
+            return self.stress(w1)
+        if inside:
+            t = self.track
+            t[0], t[1] = t[3], t[4]
+            t[3], t[4], t[5] = self.next_center
+        return super().step(it, julian_day)
+
+    def stress(self, w1):
+        a = self.deck.geo
+        u, v = self.face_u, self.face_v
+        speed = np.sqrt(u * u + v * v)
+        normal = u * a["cos_theta"] + v * a["sin_theta"]
+        tangent = -u * a["sin_theta"] + v * a["cos_theta"]
+        base, slope = {1: (0.75, 0.067), 3: (0.80, 0.065)}.get(self.w["formular"], (0.61, 0.063))
+        cda = np.minimum(float(np.float32(0.003)), 0.001 * (base + slope * speed))
+        gamma = cda * (self.w["rho_a"] / self.deck.params.rho_o) * speed
+        return dict(wind_stress_normal=gamma * normal, wind_stress_tangnt=gamma * tangent, gamma_t=gamma,
+                    air_p=w1[2].copy())
+
+
+def test_hurricane_method2_equals_host_restatement(oracle_so):
+    """Method 2 (read_hurricane_ser_2.f90): frames moved with the storm centre through IDW_5 over
+    find_neighbour_nodes' lists and blended, centres pushed with the frames; stresses, Gamma_T and
+    air pressure equal the numpy restatement every step, and a context fed that host forcing ends in
+    the same state bit for bit."""
+    from gom_release_gb300.series import hurricane_centers, with_hurricane_frames
+
+    deck = estuary(nx=12, ny=5, dx=100.0, n_layers=5, trans_sub_iter=2)
+    dt = deck.params.dt
+    rec_days = 3 * dt / 86400.0
+    bs, records = with_hurricane_frames(from_synthetic(deck), deck, read_interval=3, n_records=5, start_jday=0.0,
+                                        end_jday=1.0, seed=7, interp_method=2, record_days=rec_days)
+    centers = hurricane_centers(deck, 5, 0.0, rec_days)
+    host = _Hurricane2Host(deck, bs)
+    hf = HostForcing(deck)
+    a, b = _pair(deck, oracle_so, hf)
+    b.set_boundary_series(bs)
+    pending, pending_c = list(records), list(centers)
+    for it in range(1, 10):
+        f = hf.full(it) if it == 1 else hf.step(it)
+        if it % 3 == 0:
+            rec, cen = pending.pop(0), pending_c.pop(0)
+            b.push_hurricane_frame(rec)
+            b.push_hurricane_center(*cen)
+            host.next, host.next_center = rec, cen
+        ref = host.step(it, hf.julian_day)
+        f.update(ref)
+        a.set_forcing(f)
+        a.step_all()
+        b.step_all()
+        for name, val in ref.items():
+            got = b.get_field(name)
+            assert np.array_equal(got, val), (it, name, float(np.abs(got - val).max()))
+    assert b.status().code == 0
+    for name in STATE:
+        assert np.array_equal(a.get_field(name), b.get_field(name)), name

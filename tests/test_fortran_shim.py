@@ -28,8 +28,9 @@ def _fortran_types():
             if not line:
                 continue
             kind, names = line.split("::")
-            for n in names.split(","):
-                fields.append((kind.strip(), n.strip()))
+            for n in re.findall(r"\w+(?:\(\d+\))?", names):
+                dim = re.match(r"(\w+)(?:\((\d+)\))?", n)
+                fields.append((kind.strip(), dim.group(1), int(dim.group(2) or 1)))
         out[m.group(1)] = fields
     return out
 
@@ -48,12 +49,15 @@ def _header_structs():
             for part in first.group(3).split(","):
                 part = part.strip()
                 ptr = part.startswith("*")
-                fields.append(("ptr" if ptr else base, part.lstrip("*").strip()))
+                dim = re.match(r"(\w+)(?:\[(\d+)\])?", part.lstrip("*").strip())
+                fields.append(("ptr" if ptr else base, dim.group(1), int(dim.group(2) or 1)))
         out[m.group(1)] = fields
     return out
 
 
 def _kind_of(ctype):
+    if hasattr(ctype, "_length_"):       # a fixed array: the element's kind
+        return _kind_of(ctype._type_)
     if ctype is core.C.c_double:
         return "real(c_double)"
     if ctype is core.C.c_int32:
@@ -71,8 +75,8 @@ def test_derived_types_match_header_and_ctypes():
     for name, cls in STRUCTS.items():
         assert name in ft, f"{name} missing from the Fortran binding"
         f_fields = ft[name]
-        c_fields = [(_kind_of(t), n) for n, t in cls._fields_]
-        h_fields = [(cmap[k], n) for k, n in hs[name]]
+        c_fields = [(_kind_of(t), n, getattr(t, "_length_", 1)) for n, t in cls._fields_]
+        h_fields = [(cmap[k], n, c) for k, n, c in hs[name]]
         assert f_fields == c_fields, f"{name}: Fortran and ctypes differ"
         assert f_fields == h_fields, f"{name}: Fortran and header differ"
 

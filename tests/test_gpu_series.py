@@ -236,3 +236,38 @@ def test_hurricane_records_pushed_between_graph_launches(gpu_lib):
     lau.step_wait()
     for name in ("eta_cell", "un_face", "wind_stress_normal", "air_p", "salt_cell"):
         assert np.array_equal(lau.get_field(name), sync.get_field(name)), name
+
+
+def test_hurricane_method2_equals_oracle(oracle_so, gpu_lib):
+    """Method 2 (read_hurricane_ser_2.f90 with IDW_5.f90 over find_neighbour_nodes' lists, built on
+    the device) equals the oracle bit for bit every step: the nearest three nodes, their weights
+    and the blend of the two moved frames."""
+    from gom_release_gb300.series import hurricane_centers, with_hurricane_frames
+
+    deck = estuary(nx=30, ny=12, dx=100.0, n_layers=8, trans_sub_iter=3)
+    dt = deck.params.dt
+    rec_days = 4 * dt / 86400.0
+    bs, records = with_hurricane_frames(from_synthetic(deck), deck, read_interval=4, n_records=6, start_jday=0.0,
+                                        end_jday=1.0, seed=9, interp_method=2, record_days=rec_days)
+    centers = hurricane_centers(deck, 6, 0.0, rec_days)
+    st = initial_state(deck)
+    ref = _ctx(deck, st, lib_path=oracle_so)
+    gpu = _ctx(deck, st, lib=gpu_lib)
+    static = HostForcing(deck).static()
+    for c in (ref, gpu):
+        c.set_forcing(static)
+        c.set_boundary_series(bs)
+    for it in range(1, 17):
+        if it % 4 == 0:
+            k = it // 4 - 1
+            for c in (ref, gpu):
+                c.push_hurricane_frame(records[k])
+                c.push_hurricane_center(*centers[k])
+        ref.step_all()
+        gpu.step_all()
+        for name in ("wind_stress_normal", "wind_stress_tangnt", "gamma_t", "air_p"):
+            a, b = gpu.get_field(name), ref.get_field(name)
+            assert np.array_equal(a, b), (it, name, float(np.abs(a - b).max()))
+    assert gpu.status().code == 0 and ref.status().code == 0
+    for name in ("eta_cell", "un_face", "salt_cell", "temp_cell"):
+        assert _close(gpu.get_field(name), ref.get_field(name)), name
