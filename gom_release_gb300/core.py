@@ -32,12 +32,12 @@ FIELDS = [
     "salt_face", "temp_face", "rho_cell", "rho_node", "rho_face", "num_sub_elm",
     "cdb", "gamma_b", "qu_boundary", "elm_foot", "elm_near_edge",
     "wind_stress_normal", "wind_stress_tangnt", "gamma_t", "air_p", "eta_at_ob_old", "eta_at_ob_new",
-    "q_add",
+    "q_add", "phi_sw", "phi_sz",
 ]
 
 _CELL_FIELDS = {"eta_cell", "eta_cell_new", "wn_cell", "wn_cell_new", "dz_cell", "dz_cell_new", "dzhalf_cell",
                 "dzhalf_cell_new", "top_layer_cell", "kv", "salt_cell", "salt_cell_new", "temp_cell",
-                "temp_cell_new", "rho_cell"}
+                "temp_cell_new", "rho_cell", "phi_sw", "phi_sz"}
 _NODE_FIELDS = {"eta_node", "wetdry_node", "u_node", "v_node", "w_node", "dz_node", "dz_node_new", "dzhalf_node",
                 "dzhalf_node_new", "top_layer_node", "salt_node", "temp_node", "rho_node", "num_sub_elm"}
 
@@ -140,7 +140,11 @@ class GomBoundarySeries(C.Structure):
         [(n, GomSeries) for n in ("wind_u", "wind_v")] + \
         [("hurricane_flag", C.c_int32), ("hurricane_read_interval", C.c_int32), ("hurricane_start_jday", C.c_double),
          ("hurricane_end_jday", C.c_double), ("hurricane_frames", _D), ("hurricane_interp_method", C.c_int32),
-         ("reserved_hurricane", C.c_int32), ("hurricane_track", C.c_double * 6)]
+         ("reserved_hurricane", C.c_int32), ("hurricane_track", C.c_double * 6)] + \
+        [(n, C.c_int32) for n in ("heat_flag", "sol_swr", "n_air", "reserved_heat")] + \
+        [(n, C.c_double) for n in ("fwz_a", "fwz_b", "fwz_c", "wind_height", "light_extinction", "sol_absorb",
+                                   "sed_water_exchange", "t_sed", "sed_temp_coeff")] + \
+        [("air_time", _D), ("air_values", _D)]
 
 
 class GomMesh(C.Structure):
@@ -519,6 +523,10 @@ class GomCore:
         wind = getattr(bs, "wind", None) or {}
         hur = getattr(bs, "hurricane", None) or {}
         frames = hur.get("frames")
+        heat = getattr(bs, "heat", None) or {}
+        air_t = np.asarray(heat.get("air_time", []), np.float64)
+        air_v = np.asarray(heat.get("air_values", np.zeros((5, 0))), np.float64).reshape(5, -1)
+        n_air = int(air_t.size)
         hs, amp, per, nod, eq, ph, shift = bs.flat_harmonics()
         arg = GomBoundarySeries(
             julian_day=float(bs.julian_day), tide_spinup_period=float(bs.tide_spinup_period),
@@ -538,7 +546,14 @@ class GomCore:
             hurricane_start_jday=float(hur.get("start_jday", 0.0)), hurricane_end_jday=float(hur.get("end_jday", 0.0)),
             hurricane_frames=dbls(np.asarray(frames, np.float64).reshape(3, 3, -1).ravel())
             if frames is not None else None, hurricane_interp_method=int(hur.get("interp_method", 1)),
-            hurricane_track=(C.c_double * 6)(*[float(v) for v in hur.get("track", [0.0] * 6)]), **sets)
+            hurricane_track=(C.c_double * 6)(*[float(v) for v in hur.get("track", [0.0] * 6)]),
+            heat_flag=int(heat.get("flag", 0)), sol_swr=int(heat.get("sol_swr", 2)), n_air=n_air,
+            fwz_a=float(heat.get("fwz_a", 9.2)), fwz_b=float(heat.get("fwz_b", 0.46)),
+            fwz_c=float(heat.get("fwz_c", 2.0)), wind_height=float(heat.get("wind_height", 2.0)),
+            light_extinction=float(heat.get("light_extinction", 0.45)), sol_absorb=float(heat.get("sol_absorb", 0.45)),
+            sed_water_exchange=float(heat.get("sed_water_exchange", 0.3)), t_sed=float(heat.get("t_sed", 11.5)),
+            sed_temp_coeff=float(heat.get("sed_temp_coeff", 0.0)),
+            air_time=dbls(air_t) if n_air else None, air_values=dbls(air_v) if n_air else None, **sets)
         self._check(self.lib.gom_set_boundary_series(self.ctx, C.byref(arg)), "set_boundary_series")
 
     def push_hurricane_frame(self, frame) -> None:

@@ -248,9 +248,11 @@ template <typename R> void describe_fields(gom_ctx *c, StateT<R> &s) {
     E(GOM_F_ETA_AT_OB_OLD, &c->f_eta_old, -1, 4);
     E(GOM_F_ETA_AT_OB_NEW, &c->f_eta_new, -1, 4);
     E(GOM_F_Q_ADD, &c->f_q_add, -1, 3);
+    E(GOM_F_PHI_SW, &c->f_phi_sw, -1, 0);
+    E(GOM_F_PHI_SZ, &c->f_phi_sz, 1, 0);
 }
 
-bool is_forcing_field(int f) { return f >= GOM_F_WIND_STRESS_NORMAL && f <= GOM_F_Q_ADD; }
+bool is_forcing_field(int f) { return f >= GOM_F_WIND_STRESS_NORMAL && f <= GOM_F_PHI_SZ; }
 
 // state arrays that update_variables.f90:16-31 copies from *_new to the old name
 const int kSwapPairs[][2] = {{GOM_F_ETA_CELL, GOM_F_ETA_CELL_NEW},   {GOM_F_WN_CELL, GOM_F_WN_CELL_NEW},
@@ -293,6 +295,8 @@ template <typename R> cudaError_t enqueue_step_t(gom_ctx *c, const LaunchT<R> &x
     if ((e = launch_velocities(x))) return e;
     if ((e = launch_layers(x))) return e;
     if ((e = launch_node_velocity(x))) return e;
+    if (c->has_series && c->series.heat_flag == 1 && (e = launch_heat_terms(x.g, x.f, x.s, c->series, x.stream)))
+        return e;
     if ((e = launch_transport(x))) return e;
     if ((e = launch_density(x))) return e;
     if ((e = launch_turbulence(x))) return e;
@@ -1344,6 +1348,16 @@ int gom_set_boundary_series(gom_ctx *c, const gom_boundary_series *bs) {
     // reference does): bounded to meshes the reference itself can hold
     const bool hur2 = bs->hurricane_flag == 1 && bs->hurricane_interp_method == 2;
     if (hur2 && c->d.n_nodes > (1 << 19)) return GOM_E_ARG;
+    // heat balance: heat_term_by_term runs for temperature transport with heat_option 1; the
+    // short-wave radiation from the air series (sol_swr 2); the series' times non-decreasing
+    if (bs->heat_flag != 0 && bs->heat_flag != 1) return GOM_E_ARG;
+    if (bs->heat_flag == 1) {
+        if (!c->hp.transport_flag || !c->hp.is_temp || c->hp.heat_option != 1 || bs->sol_swr != 2 || bs->n_air < 0 ||
+            (bs->n_air > 0 && (!bs->air_time || !bs->air_values)))
+            return GOM_E_ARG;
+        for (int t = 1; t < bs->n_air; ++t)
+            if (!(bs->air_time[t] >= bs->air_time[t - 1])) return GOM_E_ARG;
+    }
     CK(cudaStreamSynchronize(c->x.stream));
     series_free(c);
     SeriesDev &S = c->series;
@@ -1408,6 +1422,27 @@ int gom_set_boundary_series(gom_ctx *c, const gom_boundary_series *bs) {
         S.hur_ready = const_cast<int *>(rd);
         S.face_u = const_cast<double *>(fu);
         S.face_v = const_cast<double *>(fv);
+    }
+    if (e == cudaSuccess && bs->heat_flag == 1) {
+        const double *at = nullptr, *av = nullptr, *hs = nullptr;
+        const size_t na = (size_t)bs->n_air;
+        e = series_upload(c, &at, na > 0 ? bs->air_time : nullptr, na);
+        if (e == cudaSuccess) e = series_upload(c, &av, na > 0 ? bs->air_values : nullptr, 5 * na);
+        if (e == cudaSuccess) e = series_upload(c, &hs, (const double *)nullptr, 8);
+        S.air_time = at;
+        S.air_values = av;
+        S.heat_scal = const_cast<double *>(hs);
+        S.heat_flag = 1;
+        S.n_air = bs->n_air;
+        S.fwz_a = bs->fwz_a;
+        S.fwz_b = bs->fwz_b;
+        S.fwz_c = bs->fwz_c;
+        S.wind_height = bs->wind_height;
+        S.light_extinction = bs->light_extinction;
+        S.sol_absorb = bs->sol_absorb;
+        S.sed_water_exchange = bs->sed_water_exchange;
+        S.t_sed = bs->t_sed;
+        S.sed_temp_coeff = bs->sed_temp_coeff;
     }
     if (e == cudaSuccess && hur2) {
         double track[12] = {0};

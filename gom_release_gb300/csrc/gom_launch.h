@@ -165,6 +165,13 @@ struct SeriesDev {
     const long long *search_start;         // (NN + 1)
     const int *search_nodes;
     double *hur_w1n;                       // (NN, 3)
+    // heat balance (heat_term_by_term.f90, sol_swr 2): the air series, card C7_3 / C7_4 values and
+    // this step's scalar terms [Ta, phi_sn, phi_an, fWz, ea]
+    int heat_flag, n_air;
+    const double *air_time, *air_values;   // (n_air), (n_air, 5)
+    double fwz_a, fwz_b, fwz_c, wind_height, light_extinction, sol_absorb, sed_water_exchange, t_sed,
+        sed_temp_coeff;
+    double *heat_scal;
 };
 
 // per-step boundary forcing from the series (k_forcing.cu): advances the device clock in f.scal
@@ -175,6 +182,12 @@ struct SeriesDev {
 // status), q_add and the boundary concentrations of every subcycle
 cudaError_t launch_series_forcing(const Geom &g, const Forcing &f, const Params &p, const SeriesDev &s,
                                   const double *eta_cell, gom_status *status, cudaStream_t stream);
+// heat_term_by_term.f90 (sol_swr 2) before the transport: the air series at julian_day, then
+// phi_sz and phi_sw of every wet column from its top and bottom temperatures (R: the state type)
+template <typename R>
+cudaError_t launch_heat_terms(const Geom &g, const Forcing &f, const StateT<R> &s, const SeriesDev &S,
+                              cudaStream_t stream);
+
 // find_neighbour_nodes.f90 on the device (hurricane method 2): per node the count of its
 // neighbours in range, then (start: NN + 1 offsets) their 1-based ids in node order
 cudaError_t hurricane_neighbour_counts(const Geom &g, int *count, cudaStream_t stream);

@@ -597,6 +597,92 @@ cudaError_t launch_storm_forcing(const Geom &g, const Forcing &f, const Params &
     return cudaGetLastError();
 }
 
+// heat_term_by_term.f90:27-110 (sol_swr 2), one thread: the air series at u2 = julian_day x 86400
+// on the first interval that holds it ((u2 - u1)(v3 - v1)/(u3 - u1) + v1; none: zeros), then the
+// short-wave term, the atmospheric long-wave term, the wind function and the air vapour pressure.
+// Default-REAL constants are widened from single precision, as the reference's mixed expressions
+// widen them; integer powers are products (x^4 = (x^2)^2, x^6 = (x^2 x)^2).
+__global__ void k_heat_scalars(Forcing f, SeriesDev S) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const double u2 = f.scal[4] * 86400.0;
+    double v[5] = {0.0, 0.0, 0.0, 0.0, 0.0};   // Ta, Tdew, w_speed, sol_rad, cloudness
+    for (int t = 1; t < S.n_air; ++t) {
+        const double u1 = S.air_time[t - 1] - S.rdd_s, u3 = S.air_time[t] - S.rdd_s;
+        if (u2 >= u1 && u2 <= u3) {
+            for (int c = 0; c < 5; ++c) {
+                const double v1 = S.air_values[(long)c * S.n_air + t - 1], v3 = S.air_values[(long)c * S.n_air + t];
+                v[c] = (u2 - u1) * (v3 - v1) / (u3 - u1) + v1;
+            }
+            break;
+        }
+    }
+    const double Ta = v[0], Tdew = v[1], w_speed = v[2], sol_rad = v[3], cloud = v[4];
+    const double c2 = cloud * cloud;
+    const double phi_sn = (1.0 - (double)0.65f * c2) * sol_rad;
+    const double xa = Ta + 273.15;
+    double phi_ac;
+    if (Ta >= 5.0) {
+        const double x2 = xa * xa, x3 = x2 * xa;
+        phi_ac = (double)5.31e-13f * (x3 * x3);
+    } else {
+        const double x2 = xa * xa;
+        phi_ac = (double)5.67e-8f * (x2 * x2) * (1.0 - (double)0.261f * exp(-((double)7.77e-4f * (Ta * Ta))));
+    }
+    const double phi_an = phi_ac * (1.0 + (double)0.17f * c2) * 0.97;
+    const double z0 = w_speed <= (double)2.3f ? (double)0.001f : (double)0.005f;
+    const double alpha = log(S.wind_height / z0) / log(2.0 / z0);
+    const double bz = S.fwz_b / pow(alpha, S.fwz_c);
+    const double fwz = S.fwz_a + bz * pow(w_speed, S.fwz_c);
+    const double ea = exp(2.3026 * (7.5 * Tdew / (Tdew + 237.3) + (double)0.6609f));
+    S.heat_scal[0] = Ta;
+    S.heat_scal[1] = phi_sn;
+    S.heat_scal[2] = phi_an;
+    S.heat_scal[3] = fwz;
+    S.heat_scal[4] = ea;
+}
+
+// heat_term_by_term.f90:112-156 for one cell column: a dry column's phi_sz is 0 (phi_sw kept); a
+// wet one gets the net surface flux less the short-wave that passes the top layer, the short-wave
+// absorbed in each lower layer, and in every wet layer the sediment share and the bottom exchange
+// (layers above the top keep their values)
+template <typename R> __global__ void k_heat_cells(Geom g, Forcing f, StateT<R> s, SeriesDev S) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.NC) return;
+    const int L = g.L;
+    double *phi_sz = const_cast<double *>(f.phi_sz);
+    const int tl = s.top_cell[i], b = g.bottom_cell[i];
+    if (tl == 0) {
+        for (int k = 1; k <= L; ++k) phi_sz[(long)i * L + k - 1] = 0.0;
+        return;
+    }
+    const double Ta = S.heat_scal[0], phi_sn = S.heat_scal[1], phi_an = S.heat_scal[2], fwz = S.heat_scal[3],
+                 ea = S.heat_scal[4];
+    const double Tw = (double)s.temp_cell[ix(tl, i + 1, L)];
+    const double xw = Tw + (double)273.15f, x2 = xw * xw;
+    const double phi_br = (double)(0.97f * 5.67e-8f) * (x2 * x2);
+    const double es = Tw < 0.0 ? exp(2.3026 * (9.5 * Tw / (Tw + 265.5) + (double)0.6609f))
+                               : exp(2.3026 * (7.5 * Tw / (Tw + 237.3) + (double)0.6609f));
+    const double phi_e = fwz * (es - ea);
+    const double phi_c = 0.47 * fwz * (Tw - Ta);
+    const double phi_n = phi_sn + phi_an - phi_br - phi_e - phi_c;
+    const double Tb = (double)s.temp_cell[ix(b, i + 1, L)];
+    const double phi_sw = S.sed_water_exchange * (S.t_sed - Tb);
+    const_cast<double *>(f.phi_sw)[i] = phi_sw;
+    double sol_out = (1.0 - S.sol_absorb) * phi_sn * exp(-(S.light_extinction * (double)s.dz_cell[ix(tl, i + 1, L)]));
+    phi_sz[(long)i * L + tl - 1] = phi_n - sol_out;
+    for (int k = tl - 1; k >= b; --k) {
+        const double sol_in = sol_out;
+        sol_out = sol_in * exp(-(S.light_extinction * (double)s.dz_cell[ix(k, i + 1, L)]));
+        phi_sz[(long)i * L + k - 1] = sol_in - sol_out;
+    }
+    for (int k = b; k <= tl; ++k) {
+        double v = phi_sz[(long)i * L + k - 1];
+        v = v + sol_out * S.sed_temp_coeff;
+        v = v + phi_sw;
+        phi_sz[(long)i * L + k - 1] = v;
+    }
+}
+
 cudaError_t hurricane_neighbour_counts(const Geom &g, int *count, cudaStream_t stream) {
     k_hur_neighbours<0><<<blocks_for(g.NN, 128), 128, 0, stream>>>(g, count, nullptr, nullptr);
     return cudaGetLastError();
@@ -606,6 +692,18 @@ cudaError_t hurricane_neighbour_fill(const Geom &g, const long long *start, int 
     k_hur_neighbours<1><<<blocks_for(g.NN, 128), 128, 0, stream>>>(g, nullptr, start, nodes);
     return cudaGetLastError();
 }
+
+template <typename R>
+cudaError_t launch_heat_terms(const Geom &g, const Forcing &f, const StateT<R> &s, const SeriesDev &S,
+                              cudaStream_t stream) {
+    k_heat_scalars<<<1, 32, 0, stream>>>(f, S);
+    k_heat_cells<R><<<blocks_for(g.NC, 128), 128, 0, stream>>>(g, f, s, S);
+    return cudaGetLastError();
+}
+template cudaError_t launch_heat_terms<double>(const Geom &, const Forcing &, const StateT<double> &,
+                                               const SeriesDev &, cudaStream_t);
+template cudaError_t launch_heat_terms<float>(const Geom &, const Forcing &, const StateT<float> &,
+                                              const SeriesDev &, cudaStream_t);
 
 cudaError_t launch_series_forcing(const Geom &g, const Forcing &f, const Params &p, const SeriesDev &s,
                                   const double *eta_cell, gom_status *status, cudaStream_t stream) {

@@ -215,6 +215,21 @@ module gom_core_abi
      integer(c_int32_t) :: hurricane_interp_method
      integer(c_int32_t) :: reserved_hurricane
      real(c_double) :: hurricane_track(6)
+     integer(c_int32_t) :: heat_flag
+     integer(c_int32_t) :: sol_swr
+     integer(c_int32_t) :: n_air
+     integer(c_int32_t) :: reserved_heat
+     real(c_double) :: fwz_a
+     real(c_double) :: fwz_b
+     real(c_double) :: fwz_c
+     real(c_double) :: wind_height
+     real(c_double) :: light_extinction
+     real(c_double) :: sol_absorb
+     real(c_double) :: sed_water_exchange
+     real(c_double) :: t_sed
+     real(c_double) :: sed_temp_coeff
+     type(c_ptr) :: air_time
+     type(c_ptr) :: air_values
   end type
 
   type, bind(c) :: gom_mesh
@@ -340,6 +355,8 @@ module gom_core_abi
   integer(c_int), parameter :: GOM_F_ETA_AT_OB_OLD = 61
   integer(c_int), parameter :: GOM_F_ETA_AT_OB_NEW = 62
   integer(c_int), parameter :: GOM_F_Q_ADD = 63
+  integer(c_int), parameter :: GOM_F_PHI_SW = 64
+  integer(c_int), parameter :: GOM_F_PHI_SZ = 65
   integer(c_int), parameter :: GOM_GEO_CONCAVE = 1
   integer(c_int), parameter :: GOM_GEO_AREA = 2
   integer(c_int), parameter :: GOM_GEO_MAX_NB = 3
@@ -486,6 +503,9 @@ module gom_core_shim
        gom_gpu_set_boundary_series
 
   type(c_ptr), save :: gom_ctx = c_null_ptr
+  ! set when the device forms phi_sz / phi_sw itself (gom_gpu_set_boundary_series with the heat
+  ! balance): the host's heat_term_by_term result is then not uploaded
+  logical, save :: gom_device_heat = .false.
   type(gom_dims), save :: dims
   ! boundary concentrations per transport subcycle, (n, 2, Nt): slot 1 salinity, slot 2 temperature
   real(c_double), allocatable, target, save :: con_ob(:,:,:), con_qb(:,:,:)
@@ -751,7 +771,7 @@ contains
     f%phi_sw = c_null_ptr
     f%phi_sz = c_null_ptr
     if (is_temp == 1 .and. heat_option == 2) f%phi_sw = cptr_d(phi_sw)
-    if (is_temp == 1 .and. heat_option == 1) f%phi_sz = cptr_d(phi_sz)
+    if (is_temp == 1 .and. heat_option == 1 .and. .not. gom_device_heat) f%phi_sz = cptr_d(phi_sz)
     call gom_gpu_check(gom_set_forcing(gom_ctx, f), 'gom_set_forcing')
   end subroutine
 
@@ -772,7 +792,7 @@ contains
     real(c_double), allocatable, target, save :: amp(:), per(:), nod(:), eq(:), ph(:), shift(:), portion(:)
     integer(c_int32_t), allocatable, target, save :: obt(:), obh(:), obe(:), obs(:), obtm(:), qq(:), qs(:), qt(:)
     integer(c_int32_t), allocatable, target, save :: swu(:), swv(:), wnode(:)
-    real(c_double), allocatable, target, save :: hframes(:)
+    real(c_double), allocatable, target, save :: hframes(:), airt(:), airv(:)
     real(c_double), allocatable, target, save :: twu(:), vwu(:), twv(:), vwv(:)
     integer :: h, j, m, nc
     ! a kind without series (its reader's arrays unallocated) is passed as n_series = 0
@@ -906,6 +926,40 @@ contains
           bs%hurricane_track = (/ hurric_x_1, hurric_y_1, hurricane_time_1, hurric_x_2, hurric_y_2, &
                hurricane_time_2 /)
        end if
+    end if
+    ! heat balance (card C7_3 / C7_4, air_ser.inp): heat_term_by_term with sol_swr 2 on the device
+    bs%heat_flag = 0
+    bs%sol_swr = sol_swr
+    bs%n_air = 0
+    bs%reserved_heat = 0
+    bs%fwz_a = fWz_a
+    bs%fwz_b = fWz_b
+    bs%fwz_c = fWz_c
+    bs%wind_height = wind_height
+    bs%light_extinction = light_extinction
+    bs%sol_absorb = sol_absorb
+    bs%sed_water_exchange = sed_water_exchange
+    bs%t_sed = T_sed
+    bs%sed_temp_coeff = sed_temp_coeff
+    bs%air_time = c_null_ptr
+    bs%air_values = c_null_ptr
+    gom_device_heat = .false.
+    if (transport_flag == 1 .and. is_temp == 1 .and. heat_option == 1 .and. sol_swr == 2) then
+       if (allocated(airt)) deallocate(airt, airv)
+       allocate(airt(max(max_air_data_num, 1)), airv(5 * max(max_air_data_num, 1)))
+       do j = 1, max_air_data_num
+          airt(j) = air_ser_time(j)
+          airv(j) = T_air(j)
+          airv(max_air_data_num + j) = T_dew(j)
+          airv(2 * max_air_data_num + j) = air_wind_speed(j)
+          airv(3 * max_air_data_num + j) = solar_radiation(j)
+          airv(4 * max_air_data_num + j) = cloud(j)
+       end do
+       bs%heat_flag = 1
+       bs%n_air = max_air_data_num
+       bs%air_time = cptr_d(airt)
+       bs%air_values = cptr_d(airv)
+       gom_device_heat = .true.
     end if
     call gom_gpu_check(gom_set_boundary_series(gom_ctx, bs), 'gom_set_boundary_series')
   end subroutine

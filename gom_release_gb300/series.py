@@ -66,6 +66,10 @@ class BoundarySeries:
     # (3 frames, 3 components u / v / air_p in Pa, n_nodes) = frames 0, 1 and 2, interp_method
     # (1 or 2), and for method 2 the track [x1, y1, t1, x2, y2, t2] (julian days)
     hurricane: dict = field(default_factory=dict)
+    # heat balance (heat_option 1, sol_swr 2): flag, card C7_3 / C7_4 values (fwz_a, fwz_b, fwz_c,
+    # wind_height, light_extinction, sol_absorb, sed_water_exchange, t_sed, sed_temp_coeff),
+    # air_time (n_air) and air_values (5, n_air): T_air, T_dew, wind speed, solar radiation, cloud
+    heat: dict = field(default_factory=dict)
 
     def flat(self, kind: str):
         """(start, time, value) of one kind: offsets (n + 1) and the concatenated samples."""
@@ -244,11 +248,36 @@ def with_hurricane_frames(bs: BoundarySeries, deck, *, read_interval: int, n_rec
     return replace(bs, hurricane=hur, wind=wind), recs[2:]
 
 
+def with_heat_balance(bs: BoundarySeries, *, hours: float = 48.0, seed: int = 0, sed_temp_coeff: float = 0.3,
+                      **cards) -> BoundarySeries:
+    """`bs` with a seeded hourly air series (air temperature 15-30 C, dew point 5-10 C below it,
+    wind 0-8 m/s, a diurnal short-wave cycle up to 900 W/m2 under seeded cloud cover) from an hour
+    before the run's start, and the heat-balance cards of the Mobile Bay deck (C7_3: 9.2, 0.46, 2.0,
+    2 m; C7_4: 0.45, 0.45, 0.3, 11.5 C) with the given sediment share; ``cards`` overrides them."""
+    from dataclasses import replace
+
+    rng = np.random.default_rng(seed)
+    n = int(hours) + 3
+    t0 = (bs.julian_day + bs.reference_diff_days) * 86400.0 - 3600.0
+    t = t0 + 3600.0 * np.arange(n)
+    hour_of_day = (t / 3600.0) % 24.0
+    ta = 22.5 + 7.5 * np.sin(2.0 * np.pi * (hour_of_day - 9.0) / 24.0) + rng.normal(0.0, 0.5, n)
+    td = ta - rng.uniform(5.0, 10.0, n)
+    ws = rng.uniform(0.0, 8.0, n)
+    cloud = rng.uniform(0.0, 1.0, n)
+    sol = np.maximum(0.0, 900.0 * np.sin(np.pi * (hour_of_day - 6.0) / 12.0))
+    heat = dict(flag=1, sol_swr=2, fwz_a=9.2, fwz_b=0.46, fwz_c=2.0, wind_height=2.0, light_extinction=0.45,
+                sol_absorb=0.45, sed_water_exchange=0.3, t_sed=11.5, sed_temp_coeff=float(sed_temp_coeff),
+                air_time=t, air_values=np.stack([ta, td, ws, sol, cloud]))
+    heat.update(cards)
+    return replace(bs, heat=heat)
+
+
 def hurricane_centers(deck, n_records: int, start_jday: float, record_days: float) -> list:
     """(x, y, julian day) of the centres of records 2 .. n_records - 1 (method 2), to push with
     ``GomCore.push_hurricane_center`` alongside their frames."""
     return [(*hurricane_center(deck, k), float(start_jday) + k * float(record_days)) for k in range(2, n_records)]
 
 
-__all__ = ["BoundarySeries", "from_deck_data", "from_synthetic", "with_station_wind", "hurricane_record",
-           "hurricane_center", "hurricane_centers", "with_hurricane_frames"]
+__all__ = ["BoundarySeries", "from_deck_data", "from_synthetic", "with_station_wind", "with_heat_balance",
+           "hurricane_record", "hurricane_center", "hurricane_centers", "with_hurricane_frames"]

@@ -310,6 +310,8 @@ typedef enum gom_field {
     GOM_F_ETA_AT_OB_OLD,       /* (n_ob)       */
     GOM_F_ETA_AT_OB_NEW,       /* (n_ob)       */
     GOM_F_Q_ADD,               /* (n_qb)  m3/s */
+    GOM_F_PHI_SW,              /* (N_c)   W/m2 */
+    GOM_F_PHI_SZ,              /* (L, N_c) W/m2 */
     GOM_F_COUNT
 } gom_field;
 
@@ -480,6 +482,20 @@ typedef struct gom_boundary_series {
     int32_t reserved_hurricane;
     double hurricane_track[6];      /* method 2: hurric_x_1, hurric_y_1, hurricane_time_1,
                                        hurric_x_2, hurric_y_2, hurricane_time_2 (julian days)   */
+    /* heat balance (heat_option 1 with temperature transport, heat_term_by_term.f90 with sol_swr
+     * 2): every step, before the transport, the air series of air_ser.inp interpolated at
+     * julian_day, the short-wave, long-wave, back-radiation, evaporation and conduction terms, and
+     * phi_sz (per wet layer) and phi_sw from the top and bottom temperatures and the layer
+     * thicknesses; with heat_flag 0 phi_sz / phi_sw are left as gom_set_forcing set them */
+    int32_t heat_flag;              /* 1: form phi_sz and phi_sw on the device                  */
+    int32_t sol_swr;                /* 2: short-wave radiation from the air series              */
+    int32_t n_air;                  /* samples of air_ser.inp                                   */
+    int32_t reserved_heat;
+    double fwz_a, fwz_b, fwz_c, wind_height;                               /* card C7_3 */
+    double light_extinction, sol_absorb, sed_water_exchange, t_sed, sed_temp_coeff;   /* C7_4 */
+    const double *air_time;         /* (n_air) air_ser_time (s, as read_air_ser.f90 stores it)  */
+    const double *air_values;       /* (n_air, 5): T_air, T_dew, air_wind_speed,
+                                       solar_radiation, cloud                                   */
 } gom_boundary_series;
 int gom_set_boundary_series(struct gom_ctx *ctx, const gom_boundary_series *series);
 

@@ -138,6 +138,11 @@ struct gom_ctx {
     double track[6] = {0, 0, 0, 0, 0, 0}, track_next[3] = {0, 0, 0};
     std::vector<int64_t> search_start;
     std::vector<int32_t> search_nodes;
+    // heat balance (heat_term_by_term.f90, sol_swr 2): air series and card values
+    int heat_flag = 0;
+    std::vector<double> air_time, air_values;
+    double fwz_a = 0, fwz_b = 0, fwz_c = 0, wind_height = 0, light_extinction = 0, sol_absorb = 0,
+           sed_water_exchange = 0, t_sed = 0, sed_temp_coeff = 0;
     std::vector<int32_t> ob_type, ob_h, ob_eta, ob_salt, ob_temp, qb_q, qb_salt, qb_temp, h_start;
     std::vector<double> qb_portion, h_amp, h_per, h_nodal, h_eq, h_ph, h_shift;
     std::vector<double> eta_at_ob_old, eta_at_ob_new, q_add, wind_stress_normal, wind_stress_tangnt, gamma_t,
@@ -199,6 +204,8 @@ FieldShape field_shape(int f) {
     case GOM_F_AIR_P: return {-1, 2, 0, 0};
     case GOM_F_ETA_AT_OB_OLD: case GOM_F_ETA_AT_OB_NEW: return {-1, 4, 0, 0};
     case GOM_F_Q_ADD: return {-1, 3, 0, 0};
+    case GOM_F_PHI_SW: return {-1, 0, 0, 0};
+    case GOM_F_PHI_SZ: return {1, 0, 0, 0};
     default: return {-2, 0, 0, 0};
     }
 }
@@ -969,6 +976,8 @@ std::vector<double> *forcing_field(gom_ctx *c, int field) {
     case GOM_F_ETA_AT_OB_OLD: return &c->eta_at_ob_old;
     case GOM_F_ETA_AT_OB_NEW: return &c->eta_at_ob_new;
     case GOM_F_Q_ADD: return &c->q_add;
+    case GOM_F_PHI_SW: return &c->phi_sw;
+    case GOM_F_PHI_SZ: return &c->phi_sz;
     default: return nullptr;
     }
 }
@@ -1077,6 +1086,14 @@ int gom_set_boundary_series(gom_ctx *c, const gom_boundary_series *bs) {
     if (bs->hurricane_flag == 1 && (bs->hurricane_read_interval < 1 || !bs->hurricane_frames || !(bs->rho_a > 0.0) ||
                                     bs->hurricane_interp_method < 0 || bs->hurricane_interp_method > 2))
         return GOM_E_ARG;
+    if (bs->heat_flag != 0 && bs->heat_flag != 1) return GOM_E_ARG;
+    if (bs->heat_flag == 1) {
+        if (!c->p.transport_flag || !c->p.is_temp || c->p.heat_option != 1 || bs->sol_swr != 2 || bs->n_air < 0 ||
+            (bs->n_air > 0 && (!bs->air_time || !bs->air_values)))
+            return GOM_E_ARG;
+        for (int t = 1; t < bs->n_air; ++t)
+            if (!(bs->air_time[t] >= bs->air_time[t - 1])) return GOM_E_ARG;
+    }
     if (bs->wind_flag != 0 && bs->wind_flag != 1) return GOM_E_ARG;
     if (bs->wind_flag == 1) {
         if (bs->wind_formular < 1 || bs->wind_formular > 3 || bs->n_wind < 1 || bs->n_wind > 3 ||
@@ -1171,6 +1188,22 @@ int gom_set_boundary_series(gom_ctx *c, const gom_boundary_series *bs) {
     c->hur_next.assign(c->hur_flag == 1 ? 3 * (size_t)c->NN : 0, 0.0);
     c->face_u.assign(c->NF, 0.0);
     c->face_v.assign(c->NF, 0.0);
+    c->heat_flag = bs->heat_flag;
+    c->air_time.clear();
+    c->air_values.clear();
+    if (bs->heat_flag == 1 && bs->n_air > 0) {
+        c->air_time.assign(bs->air_time, bs->air_time + bs->n_air);
+        c->air_values.assign(bs->air_values, bs->air_values + 5 * (size_t)bs->n_air);
+    }
+    c->fwz_a = bs->fwz_a;
+    c->fwz_b = bs->fwz_b;
+    c->fwz_c = bs->fwz_c;
+    c->wind_height = bs->wind_height;
+    c->light_extinction = bs->light_extinction;
+    c->sol_absorb = bs->sol_absorb;
+    c->sed_water_exchange = bs->sed_water_exchange;
+    c->t_sed = bs->t_sed;
+    c->sed_temp_coeff = bs->sed_temp_coeff;
     c->hur_method = (c->hur_flag == 1 && bs->hurricane_interp_method == 2) ? 2 : 1;
     c->track_ready = false;
     c->search_start.clear();
@@ -3367,6 +3400,76 @@ int gom_step_swap(gom_ctx *c) {
     return GOM_OK;
 }
 
+// heat_term_by_term.f90:27-156 with sol_swr 2, before the transport: the air series at
+// julian_day (no interval: zeros), the scalar terms, then per wet column phi_sw and phi_sz from its
+// top and bottom temperatures (the top layer after the layer update, the old thicknesses).  Default-
+// REAL constants widened from single precision; integer powers as products (x^4 = (x^2)^2,
+// x^6 = (x^2 x)^2); exp, log and pow of the C library (the GPU's differ in the last bits)
+static void heat_terms(gom_ctx *c) {
+    const int L = c->L, NC = c->NC, n = (int)c->air_time.size();
+    const double u2 = c->jday * 86400.0;
+    double v[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int t = 1; t < n; ++t) {
+        const double u1 = c->air_time[t - 1] - c->rdd_s, u3 = c->air_time[t] - c->rdd_s;
+        if (u2 >= u1 && u2 <= u3) {
+            for (int k = 0; k < 5; ++k) {
+                const double v1 = c->air_values[(size_t)k * n + t - 1], v3 = c->air_values[(size_t)k * n + t];
+                v[k] = (u2 - u1) * (v3 - v1) / (u3 - u1) + v1;
+            }
+            break;
+        }
+    }
+    const double Ta = v[0], Tdew = v[1], w_speed = v[2], sol_rad = v[3], cloud = v[4];
+    const double c2 = cloud * cloud;
+    const double phi_sn = (1.0 - (double)0.65f * c2) * sol_rad;
+    const double xa = Ta + 273.15;
+    double phi_ac;
+    if (Ta >= 5.0) {
+        const double x2 = xa * xa, x3 = x2 * xa;
+        phi_ac = (double)5.31e-13f * (x3 * x3);
+    } else {
+        const double x2 = xa * xa;
+        phi_ac = (double)5.67e-8f * (x2 * x2) * (1.0 - (double)0.261f * std::exp(-((double)7.77e-4f * (Ta * Ta))));
+    }
+    const double phi_an = phi_ac * (1.0 + (double)0.17f * c2) * 0.97;
+    const double z0 = w_speed <= (double)2.3f ? (double)0.001f : (double)0.005f;
+    const double alpha = std::log(c->wind_height / z0) / std::log(2.0 / z0);
+    const double bz = c->fwz_b / std::pow(alpha, c->fwz_c);
+    const double fwz = c->fwz_a + bz * std::pow(w_speed, c->fwz_c);
+    const double ea = std::exp(2.3026 * (7.5 * Tdew / (Tdew + 237.3) + (double)0.6609f));
+    A2<double> temp_cell = FD(c, GOM_F_TEMP_CELL), dz_cell = FD(c, GOM_F_DZ_CELL);
+    A1<int32_t> top_el = FI1(c, GOM_F_TOP_LAYER_CELL);
+    for (int i = 1; i <= NC; ++i) {
+        double *phi_sz = c->phi_sz.data() + (size_t)(i - 1) * L;
+        const int tl = top_el(i), b = c->bottom_layer_at_element(i);
+        if (tl == 0) {
+            for (int k = 1; k <= L; ++k) phi_sz[k - 1] = 0.0;
+            continue;
+        }
+        const double Tw = temp_cell(tl, i);
+        const double xw = Tw + (double)273.15f, x2 = xw * xw;
+        const double phi_br = (double)(0.97f * 5.67e-8f) * (x2 * x2);
+        const double es = Tw < 0.0 ? std::exp(2.3026 * (9.5 * Tw / (Tw + 265.5) + (double)0.6609f))
+                                   : std::exp(2.3026 * (7.5 * Tw / (Tw + 237.3) + (double)0.6609f));
+        const double phi_e = fwz * (es - ea);
+        const double phi_c = 0.47 * fwz * (Tw - Ta);
+        const double phi_n = phi_sn + phi_an - phi_br - phi_e - phi_c;
+        const double phi_sw = c->sed_water_exchange * (c->t_sed - temp_cell(b, i));
+        c->phi_sw[i - 1] = phi_sw;
+        double sol_out = (1.0 - c->sol_absorb) * phi_sn * std::exp(-(c->light_extinction * dz_cell(tl, i)));
+        phi_sz[tl - 1] = phi_n - sol_out;
+        for (int k = tl - 1; k >= b; --k) {
+            const double sol_in = sol_out;
+            sol_out = sol_in * std::exp(-(c->light_extinction * dz_cell(k, i)));
+            phi_sz[k - 1] = sol_in - sol_out;
+        }
+        for (int k = b; k <= tl; ++k) {
+            phi_sz[k - 1] = phi_sz[k - 1] + sol_out * c->sed_temp_coeff;
+            phi_sz[k - 1] = phi_sz[k - 1] + phi_sw;
+        }
+    }
+}
+
 int gom_step_all(gom_ctx *c, int32_t *pcg_iters) {
     if (!c) return GOM_E_ARG;
     int e;
@@ -3379,6 +3482,7 @@ int gom_step_all(gom_ctx *c, int32_t *pcg_iters) {
     if ((e = gom_step_velocities(c))) return e;
     if ((e = gom_step_layers(c))) return e;
     if ((e = gom_step_node_velocity(c))) return e;
+    if (c->has_series && c->heat_flag == 1) heat_terms(c);
     if ((e = gom_step_transport(c))) return e;
     if ((e = gom_step_density(c))) return e;
     if ((e = gom_step_turbulence(c))) return e;

@@ -452,3 +452,110 @@ def test_hurricane_method2_equals_host_restatement(oracle_so):
     assert b.status().code == 0
     for name in STATE:
         assert np.array_equal(a.get_field(name), b.get_field(name)), name
+
+
+# ----------------------------------------------------------------------------- heat balance
+def _heat_host(deck, bs, julian_day, temp, dz, top):
+    """heat_term_by_term.f90:27-156 (sol_swr 2) restated with Python floats and the C library's
+    exp / log / pow (as the oracle calls them): (phi_sz (L, NC), phi_sw (NC)) of one step from the
+    temperatures and thicknesses at the step's start and the tops after its layer update."""
+    h = bs.heat
+    f32 = lambda x: float(np.float32(x))
+    rdd = float(np.float32(bs.reference_diff_days) * np.float32(86400.0))
+    u2 = julian_day * 86400.0
+    t, av = np.asarray(h["air_time"]), np.asarray(h["air_values"])
+    v = [0.0] * 5
+    for q in range(1, len(t)):
+        u1, u3 = float(t[q - 1]) - rdd, float(t[q]) - rdd
+        if u1 <= u2 <= u3:
+            v = [(u2 - u1) * (float(av[c, q]) - float(av[c, q - 1])) / (u3 - u1) + float(av[c, q - 1]) for c in range(5)]
+            break
+    ta, tdew, ws, sol, cloud = v
+    c2 = cloud * cloud
+    phi_sn = (1.0 - f32(0.65) * c2) * sol
+    xa = ta + 273.15
+    if ta >= 5.0:
+        x3 = xa * xa * xa
+        phi_ac = f32(5.31e-13) * (x3 * x3)
+    else:
+        x2 = xa * xa
+        phi_ac = f32(5.67e-8) * (x2 * x2) * (1.0 - f32(0.261) * math.exp(-(f32(7.77e-4) * (ta * ta))))
+    phi_an = phi_ac * (1.0 + f32(0.17) * c2) * 0.97
+    z0 = f32(0.001) if ws <= f32(2.3) else f32(0.005)
+    alpha = math.log(h["wind_height"] / z0) / math.log(2.0 / z0)
+    fwz = h["fwz_a"] + h["fwz_b"] / math.pow(alpha, h["fwz_c"]) * math.pow(ws, h["fwz_c"])
+    ea = math.exp(2.3026 * (7.5 * tdew / (tdew + 237.3) + f32(0.6609)))
+    L, nc = deck.n_layers, deck.n_cells
+    bottom = deck.geo["bottom_layer_at_element"]
+    phi_sz = np.zeros((nc, L))
+    phi_sw = np.zeros(nc)
+    for i in range(nc):
+        tl, b = int(top[i]), int(bottom[i])
+        if tl == 0:
+            continue
+        tw = float(temp[tl - 1, i])
+        xw = tw + f32(273.15)
+        x2 = xw * xw
+        phi_br = float(np.float32(np.float32(0.97) * np.float32(5.67e-8))) * (x2 * x2)
+        if tw < 0.0:
+            es = math.exp(2.3026 * (9.5 * tw / (tw + 265.5) + f32(0.6609)))
+        else:
+            es = math.exp(2.3026 * (7.5 * tw / (tw + 237.3) + f32(0.6609)))
+        phi_n = phi_sn + phi_an - phi_br - fwz * (es - ea) - 0.47 * fwz * (tw - ta)
+        sw = h["sed_water_exchange"] * (h["t_sed"] - float(temp[b - 1, i]))
+        phi_sw[i] = sw
+        sol_out = (1.0 - h["sol_absorb"]) * phi_sn * math.exp(-(h["light_extinction"] * float(dz[tl - 1, i])))
+        phi_sz[i, tl - 1] = phi_n - sol_out
+        for k in range(tl - 1, b - 1, -1):
+            sol_in = sol_out
+            sol_out = sol_in * math.exp(-(h["light_extinction"] * float(dz[k - 1, i])))
+            phi_sz[i, k - 1] = sol_in - sol_out
+        for k in range(b, tl + 1):
+            phi_sz[i, k - 1] = phi_sz[i, k - 1] + sol_out * h["sed_temp_coeff"]
+            phi_sz[i, k - 1] = phi_sz[i, k - 1] + sw
+    return phi_sz, phi_sw
+
+
+def test_heat_balance_equals_host_restatement(oracle_so):
+    """heat_term_by_term (sol_swr 2) formed by the context before every transport equals the Python
+    restatement on the same state bit for bit (both on the C library's exp, log and pow)."""
+    from gom_release_gb300.series import with_heat_balance
+
+    deck = estuary(nx=12, ny=5, dx=100.0, n_layers=5, trans_sub_iter=2)
+    deck = replace(deck, params=replace(deck.params, heat_option=1))
+    bs = with_heat_balance(from_synthetic(deck), hours=6, seed=4)
+    hf = HostForcing(deck)
+    c = GomCore(deck, lib_path=oracle_so)
+    prepare(c, initial_state(deck))
+    c.set_forcing(hf.static())
+    c.set_boundary_series(bs)
+    L, nc = deck.n_layers, deck.n_cells
+    jd = 0.0
+    for it in range(1, 7):
+        temp = c.get_field("temp_cell").reshape(nc, L).T.copy()
+        dz = c.get_field("dz_cell").reshape(nc, L).T.copy()
+        c.step_all()
+        jd = jd + deck.params.dt / 86400.0
+        top = c.get_field("top_layer_cell")
+        sz, sw = _heat_host(deck, bs, jd, temp, dz, top)
+        got_sz = c.get_field("phi_sz").reshape(nc, L)
+        wet = top > 0
+        assert np.array_equal(c.get_field("phi_sw")[wet], sw[wet]), it
+        for i in np.nonzero(wet)[0]:
+            b = int(deck.geo["bottom_layer_at_element"][i])
+            assert np.array_equal(got_sz[i, b - 1:top[i]], sz[i, b - 1:top[i]]), (it, i)
+    assert float(np.abs(c.get_field("phi_sz")).max()) > 0.0
+
+
+def test_heat_balance_argument_rules(oracle_so):
+    from gom_release_gb300.series import with_heat_balance
+
+    deck = estuary(nx=8, ny=4, dx=100.0, n_layers=3, trans_sub_iter=1)       # heat_option 2
+    c = GomCore(deck, lib_path=oracle_so)
+    with pytest.raises(GomError):
+        c.set_boundary_series(with_heat_balance(from_synthetic(deck)))
+    deck1 = replace(deck, params=replace(deck.params, heat_option=1))
+    c1 = GomCore(deck1, lib_path=oracle_so)
+    with pytest.raises(GomError):
+        c1.set_boundary_series(with_heat_balance(from_synthetic(deck1), sol_swr=1))
+    c1.set_boundary_series(with_heat_balance(from_synthetic(deck1)))

@@ -271,3 +271,36 @@ def test_hurricane_method2_equals_oracle(oracle_so, gpu_lib):
     assert gpu.status().code == 0 and ref.status().code == 0
     for name in ("eta_cell", "un_face", "salt_cell", "temp_cell"):
         assert _close(gpu.get_field(name), ref.get_field(name)), name
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_heat_balance_equals_oracle(oracle_so, gpu_lib, precision):
+    """heat_term_by_term (sol_swr 2) on the device against the oracle: phi_sz and phi_sw of every
+    step within the last bits of CUDA's exp, log and pow against the C library's (1e-12 of the
+    field's magnitude; FP64 context), and the temperatures after the run; the mixed context reads
+    FP32 temperatures and thicknesses (1e-4)."""
+    import dataclasses
+
+    from gom_release_gb300.series import with_heat_balance
+
+    deck = estuary(nx=30, ny=12, dx=100.0, n_layers=8, trans_sub_iter=3)
+    deck = dataclasses.replace(deck, params=dataclasses.replace(deck.params, heat_option=1))
+    bs = with_heat_balance(from_synthetic(deck), hours=6, seed=6, sed_temp_coeff=0.3)
+    st = initial_state(deck)
+    ref = _ctx(deck, st, lib_path=oracle_so)
+    dg = dataclasses.replace(deck, params=dataclasses.replace(deck.params, precision=precision))
+    gpu = _ctx(dg, st, lib=gpu_lib)
+    static = HostForcing(deck).static()
+    for c in (ref, gpu):
+        c.set_forcing(static)
+        c.set_boundary_series(bs)
+    tol = 1e-12 if precision == 0 else 1e-4
+    for it in range(1, 11):
+        ref.step_all()
+        gpu.step_all()
+        for name in ("phi_sz", "phi_sw"):
+            a, b = gpu.get_field(name), ref.get_field(name)
+            scale = max(float(np.abs(b).max()), 1e-30)
+            assert float(np.abs(a - b).max()) <= tol * scale, (it, name, float(np.abs(a - b).max()) / scale)
+    assert gpu.status().code == 0
+    assert _close(gpu.get_field("temp_cell"), ref.get_field("temp_cell"), rtol=1e-9 if precision == 0 else 1e-4)
