@@ -232,6 +232,12 @@ def read_deck(directory, overrides: dict | None = None) -> DeckData:
     v["is_salt"], v["num_salt_ser"], v["salt_ser_shape"] = float(salt_row[0]), float(salt_row[1]), float(salt_row[2])
     v["is_temp"], v["num_temp_ser"], v["temp_ser_shape"] = float(temp_row[0]), float(temp_row[1]), float(temp_row[2])
     v["heat_option"] = num("C7_3", 0, 0)
+    # cards C7_3 / C7_4: the heat balance of heat_term_by_term.f90
+    for k, val in zip(("heat_option", "sol_swr", "fwz_a", "fwz_b", "fwz_c", "wind_height"), c["C7_3"][0]):
+        v[k] = float(val)
+    for k, val in zip(("light_extinction", "sol_absorb", "sed_water_exchange", "t_sed", "sed_temp_coeff"),
+                      c.get("C7_4", [[]])[0]):
+        v[k] = float(val)
     r20 = c["C20"]
     n_ob = int(r20[0][0])
     v["n_ob"], v["num_harmonic_ser"] = n_ob, float(r20[1][1])
@@ -266,6 +272,14 @@ def read_deck(directory, overrides: dict | None = None) -> DeckData:
             t, val, _ = _series_file(d / f"{kind}_ser{shape}.inp", int(v[key]), shape)
             series[kind] = (t, val)
     nn = len(x)
+    if int(v["heat_option"]) == 1 and (d / "air_ser.inp").exists():
+        # read_air_ser.f90:21-26: count, time conversion and adjustment, then rows of time, air and
+        # dew-point temperature, wind speed, short-wave radiation, cloud (rain and evaporation unused)
+        rec = _records(d / "air_ser.inp")
+        n, conv, adj = int(rec[0][0]), float(rec[0][1]), float(rec[0][2])
+        rows = rec[1:1 + n]
+        t = np.array([(float(r[0]) + adj) * conv for r in rows])
+        series["air"] = ([t] * 5, [np.array([float(r[col]) for r in rows]) for col in range(1, 6)])
     salt_init = _init_file(d / "salt_init.inp", nn, L) if (d / "salt_init.inp").exists() else None
     temp_init = _init_file(d / "temp_init.inp", nn, L) if (d / "temp_init.inp").exists() else None
     return DeckData(name=d.parent.name, x=x, y=y, h=h, tri_or_quad=tq, cells=cells, cards=v, z_level=z, ob=ob,

@@ -94,11 +94,12 @@ class BoundarySeries:
                                                                    "phase")], shift)
 
 
-def from_deck_data(deck) -> BoundarySeries:
+def from_deck_data(deck, heat: bool = False) -> BoundarySeries:
     """The boundary tables of a reference deck (``deck.meta['reference']``, a ``DeckData``):
     ids from cards C20_1 / C22_1, series as the readers store them (times and values already
     adjusted and converted), start time from card C3 (julian.f90), reference_diff_days from
-    calculate_reference_diff_days.f90, spin-up from card C21."""
+    calculate_reference_diff_days.f90, spin-up from card C21.  With ``heat`` (and the deck's
+    heat_option 1, sol_swr 2 and its air series) also the heat balance of cards C7_3 / C7_4."""
     from .gom_inputs import julian_day0, reference_diff_days
 
     data = deck.meta["reference"]
@@ -120,7 +121,18 @@ def from_deck_data(deck) -> BoundarySeries:
         ob_temp_id=ob[:, 6].astype(np.int32),
         qb_q_id=qb[:, 2].astype(np.int32), qb_salt_id=qb[:, 4].astype(np.int32),
         qb_temp_id=qb[:, 5].astype(np.int32), qb_portion=qb[:, 3].astype(np.float64),
-        series=series)
+        series=series, heat=_deck_heat(data) if heat else {})
+
+
+def _deck_heat(data) -> dict:
+    v = data.cards
+    if int(v.get("heat_option", 0)) != 1 or int(v.get("sol_swr", 0)) != 2 or "air" not in data.series:
+        raise ValueError("the deck's heat balance needs heat_option 1, sol_swr 2 and air_ser.inp")
+    ts, vs = data.series["air"]
+    return dict(flag=1, sol_swr=2, fwz_a=v["fwz_a"], fwz_b=v["fwz_b"], fwz_c=v["fwz_c"], wind_height=v["wind_height"],
+                light_extinction=v["light_extinction"], sol_absorb=v["sol_absorb"],
+                sed_water_exchange=v["sed_water_exchange"], t_sed=v["t_sed"], sed_temp_coeff=v["sed_temp_coeff"],
+                air_time=np.asarray(ts[0], np.float64), air_values=np.stack([np.asarray(x, np.float64) for x in vs]))
 
 
 def _constant(value: float):

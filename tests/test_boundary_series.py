@@ -559,3 +559,32 @@ def test_heat_balance_argument_rules(oracle_so):
     with pytest.raises(GomError):
         c1.set_boundary_series(with_heat_balance(from_synthetic(deck1), sol_swr=1))
     c1.set_boundary_series(with_heat_balance(from_synthetic(deck1)))
+
+
+def test_mobile_bay_heat_balance_equals_host_restatement(oracle_so):
+    """The reference's Mobile Bay deck with its own air series and heat cards (heat_option 1,
+    sol_swr 2): the heat terms the context forms equal the Python restatement bit for bit."""
+    data = DeckData.from_npz(FIXTURE)
+    deck = deck_from_data(data)
+    bs = from_deck_data(deck, heat=True)
+    assert bs.heat["air_values"].shape == (5, 961)
+    c = GomCore(deck, lib_path=oracle_so)
+    prepare(c, initial_state(deck))
+    c.set_forcing(SeriesForcing(deck).static())
+    c.set_boundary_series(bs)
+    L, nc = deck.n_layers, deck.n_cells
+    jd = bs.julian_day
+    for it in range(1, 3):
+        temp = c.get_field("temp_cell").reshape(nc, L).T.copy()
+        dz = c.get_field("dz_cell").reshape(nc, L).T.copy()
+        c.step_all()
+        jd = jd + deck.params.dt / 86400.0
+        top = c.get_field("top_layer_cell")
+        sz, sw = _heat_host(deck, bs, jd, temp, dz, top)
+        wet = top > 0
+        assert np.array_equal(c.get_field("phi_sw")[wet], sw[wet]), it
+        got = c.get_field("phi_sz").reshape(nc, L)
+        bottom = deck.geo["bottom_layer_at_element"]
+        for i in np.nonzero(wet)[0]:
+            assert np.array_equal(got[i, bottom[i] - 1:top[i]], sz[i, bottom[i] - 1:top[i]]), (it, i)
+    assert float(np.abs(c.get_field("phi_sz")).max()) > 0.0

@@ -304,3 +304,28 @@ def test_heat_balance_equals_oracle(oracle_so, gpu_lib, precision):
             assert float(np.abs(a - b).max()) <= tol * scale, (it, name, float(np.abs(a - b).max()) / scale)
     assert gpu.status().code == 0
     assert _close(gpu.get_field("temp_cell"), ref.get_field("temp_cell"), rtol=1e-9 if precision == 0 else 1e-4)
+
+
+def test_mobile_bay_heat_balance_equals_oracle(oracle_so, gpu_lib):
+    """The reference's Mobile Bay deck with its boundary series, air series and heat cards all on
+    the device: phi_sz / phi_sw within the last bits of CUDA's transcendental functions of the
+    oracle's every step, the temperatures after ten steps within 1e-9."""
+    deck = deck_from_data(DeckData.from_npz(FIXTURE))
+    st = initial_state(deck)
+    ref = _ctx(deck, st, lib_path=oracle_so)
+    gpu = _ctx(deck, st, lib=gpu_lib)
+    bs = from_deck_data(deck, heat=True)
+    static = SeriesForcing(deck).static()
+    for c in (ref, gpu):
+        c.set_forcing(static)
+        c.set_boundary_series(bs)
+    for it in range(1, 11):
+        ref.step_all()
+        gpu.step_all()
+        for name in ("phi_sz", "phi_sw"):
+            a, b = gpu.get_field(name), ref.get_field(name)
+            scale = max(float(np.abs(b).max()), 1e-30)
+            assert float(np.abs(a - b).max()) <= 1e-12 * scale, (it, name)
+    assert gpu.status().code == 0
+    for name in ("temp_cell", "salt_cell", "eta_cell"):
+        assert _close(gpu.get_field(name), ref.get_field(name)), name
