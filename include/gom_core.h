@@ -409,9 +409,11 @@ int gom_set_storms(struct gom_ctx *ctx, int32_t n_storms, const gom_storm *storm
  * times minus reference_diff_days x 86400); a time outside a series keeps the value that entry
  * had.  An open-boundary cell of type -1 with no interior cell around its nodes records GOM_E_ARG
  * in the step status (the reference stops there).  Single-run contexts only.  The separate
- * gom_step_* entry points do not run it.  gom_set_forcing is then needed only
- * for what the series leave alone (wind stress, Gamma_T, air pressure, heat terms).  Not with
- * gom_set_storms on the same context (GOM_E_ARG). */
+ * gom_step_* entry points do not run it.  Station wind, hurricane frames and the heat balance
+ * (the fields below) are evaluated the same way, the heat terms just before the transport.
+ * gom_set_forcing is then needed only for what the series leave alone (with none of those: wind
+ * stress, Gamma_T, air pressure, heat terms).  Not with gom_set_storms on the same context
+ * (GOM_E_ARG). */
 typedef struct gom_series {
     int32_t n_series;          /* number of series                                          */
     int32_t reserved;
