@@ -144,7 +144,8 @@ class GomBoundarySeries(C.Structure):
         [(n, C.c_int32) for n in ("heat_flag", "sol_swr", "n_air", "reserved_heat")] + \
         [(n, C.c_double) for n in ("fwz_a", "fwz_b", "fwz_c", "wind_height", "light_extinction", "sol_absorb",
                                    "sed_water_exchange", "t_sed", "sed_temp_coeff")] + \
-        [("air_time", _D), ("air_values", _D)]
+        [("air_time", _D), ("air_values", _D), ("year", C.c_int32), ("month", C.c_int32), ("lon", C.c_double),
+         ("lat", C.c_double)]
 
 
 class GomMesh(C.Structure):
@@ -553,7 +554,9 @@ class GomCore:
             light_extinction=float(heat.get("light_extinction", 0.45)), sol_absorb=float(heat.get("sol_absorb", 0.45)),
             sed_water_exchange=float(heat.get("sed_water_exchange", 0.3)), t_sed=float(heat.get("t_sed", 11.5)),
             sed_temp_coeff=float(heat.get("sed_temp_coeff", 0.0)),
-            air_time=dbls(air_t) if n_air else None, air_values=dbls(air_v) if n_air else None, **sets)
+            air_time=dbls(air_t) if n_air else None, air_values=dbls(air_v) if n_air else None,
+            year=int(heat.get("year", 2001)), month=int(heat.get("month", 1)), lon=float(heat.get("lon", 0.0)),
+            lat=float(heat.get("lat", 0.0)), **sets)
         self._check(self.lib.gom_set_boundary_series(self.ctx, C.byref(arg)), "set_boundary_series")
 
     def push_hurricane_frame(self, frame) -> None:

@@ -1352,7 +1352,8 @@ int gom_set_boundary_series(gom_ctx *c, const gom_boundary_series *bs) {
     // short-wave radiation from the air series (sol_swr 2); the series' times non-decreasing
     if (bs->heat_flag != 0 && bs->heat_flag != 1) return GOM_E_ARG;
     if (bs->heat_flag == 1) {
-        if (!c->hp.transport_flag || !c->hp.is_temp || c->hp.heat_option != 1 || bs->sol_swr != 2 || bs->n_air < 0 ||
+        if (!c->hp.transport_flag || !c->hp.is_temp || c->hp.heat_option != 1 || (bs->sol_swr != 1 && bs->sol_swr != 2) ||
+            bs->n_air < 0 || (bs->sol_swr == 1 && (bs->month < 1 || bs->month > 12)) ||
             (bs->n_air > 0 && (!bs->air_time || !bs->air_values)))
             return GOM_E_ARG;
         for (int t = 1; t < bs->n_air; ++t)
@@ -1429,6 +1430,14 @@ int gom_set_boundary_series(gom_ctx *c, const gom_boundary_series *bs) {
         e = series_upload(c, &at, na > 0 ? bs->air_time : nullptr, na);
         if (e == cudaSuccess) e = series_upload(c, &av, na > 0 ? bs->air_values : nullptr, 5 * na);
         if (e == cudaSuccess) e = series_upload(c, &hs, (const double *)nullptr, 8);
+        const int month_state[2] = {bs->month, 0};
+        const int *ms = nullptr;
+        if (e == cudaSuccess) e = series_upload(c, &ms, month_state, 2);
+        S.heat_month = const_cast<int *>(ms);
+        S.sol_swr = bs->sol_swr;
+        S.year = bs->year;
+        S.lon = bs->lon;
+        S.lat = bs->lat;
         S.air_time = at;
         S.air_values = av;
         S.heat_scal = const_cast<double *>(hs);

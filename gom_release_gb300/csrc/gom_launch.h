@@ -167,7 +167,9 @@ struct SeriesDev {
     double *hur_w1n;                       // (NN, 3)
     // heat balance (heat_term_by_term.f90, sol_swr 2): the air series, card C7_3 / C7_4 values and
     // this step's scalar terms [Ta, phi_sn, phi_an, fWz, ea]
-    int heat_flag, n_air;
+    int heat_flag, n_air, sol_swr, year;
+    int *heat_month;                       // julian_to_localtime's state: [month, table set]
+    double lon, lat;
     const double *air_time, *air_values;   // (n_air), (n_air, 5)
     double fwz_a, fwz_b, fwz_c, wind_height, light_extinction, sol_absorb, sed_water_exchange, t_sed,
         sed_temp_coeff;

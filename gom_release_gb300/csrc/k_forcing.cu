@@ -602,6 +602,36 @@ cudaError_t launch_storm_forcing(const Geom &g, const Forcing &f, const Params &
 // short-wave term, the atmospheric long-wave term, the wind function and the air vapour pressure.
 // Default-REAL constants are widened from single precision, as the reference's mixed expressions
 // widen them; integer powers are products (x^4 = (x^2)^2, x^6 = (x^2 x)^2).
+// julian_to_localtime.f90:16-86 with its state: the hour of julian day jday.  The month table is
+// saved between calls and set with the month; in a leap year (other than 1900) only while the
+// month variable is 3 or more (so a run starting in January or February keeps a zero table)
+__device__ int local_hour(int year, int *state, double jday) {
+    const double leap[12] = {0, 32, 60, 91, 121, 152, 182, 213, 244, 274, 305, 335};
+    const double normal[12] = {0, 31, 59, 90, 120, 151, 181, 212, 243, 273, 304, 334};
+    const double leap_top[11] = {31, 60, 91, 121, 152, 182, 213, 244, 274, 305, 335};
+    const double normal_top[11] = {31, 59, 90, 120, 151, 181, 212, 243, 273, 304, 334};
+    int month = state[0];
+    double m;
+    if (year % 4 == 0) {
+        if (year != 1900 && month >= 3) {
+            int k = 0;
+            while (k < 11 && jday > leap_top[k]) ++k;
+            month = k + 1;
+            state[1] = 1;
+        }
+        m = state[1] ? leap[month - 1] : 0.0;
+    } else {
+        int k = 0;
+        while (k < 11 && jday > normal_top[k]) ++k;
+        month = k + 1;
+        m = normal[month - 1];
+    }
+    state[0] = month;
+    const double day_temp = jday - m;
+    const int day = (int)day_temp + 1;
+    return (int)((day_temp + 1 - day) * 24.0);
+}
+
 __global__ void k_heat_scalars(Forcing f, SeriesDev S) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     const double u2 = f.scal[4] * 86400.0;
@@ -618,7 +648,31 @@ __global__ void k_heat_scalars(Forcing f, SeriesDev S) {
     }
     const double Ta = v[0], Tdew = v[1], w_speed = v[2], sol_rad = v[3], cloud = v[4];
     const double c2 = cloud * cloud;
-    const double phi_sn = (1.0 - (double)0.65f * c2) * sol_rad;
+    double phi_sn = 0.0;   // sol_swr 1 with the sun below the horizon: the reference leaves it unset
+    if (S.sol_swr == 1) {
+        // :64-83: the sun's elevation A0 at the local hour, and the clear-sky short-wave from it
+        const int hr = local_hour(S.year, S.heat_month, f.scal[4]);
+        const double pi = 3.141592653589793, deg2rad = pi / 180.0, rad2deg = 180.0 / pi;
+        const double j_day = f.scal[4] + 1;
+        const double tau_d = 2.0 * pi * (double)((int)(j_day + 1) - 1) / 365.0;
+        const double sdec = (double)0.006918f - (double)0.399912f * cos(tau_d) + (double)0.070257f * sin(tau_d) -
+                            (double)0.006758f * cos(2.0 * tau_d) + (double)0.000907f * sin(2.0 * tau_d) -
+                            (double)0.002697f * cos(3.0 * tau_d) + (double)0.001480f * sin(3.0 * tau_d);
+        const double eqt = (double)0.170f * sin(4.0 * pi * (double)((int)j_day - 80) / 373.0) -
+                           (double)0.129f * sin(2.0 * pi * (double)((int)j_day - 8) / 355.0);
+        const double sm = 15.0 * (double)(int)(S.lon / 15.0);
+        const double lha = (double)0.261799f * ((double)hr - (S.lon - sm) * (double)0.0666667f + eqt - 12.0);
+        const double a0 =
+            asin(sin(S.lat * deg2rad) * sin(sdec) + cos(S.lat * deg2rad) * cos(sdec) * cos(lha)) * rad2deg;
+        if (a0 > 0.0) {
+            const double a2 = a0 * a0, a3 = a2 * a0, a4 = a2 * a2;
+            phi_sn = (1.0 - (double)0.65f * c2) * 24.0 *
+                     ((double)2.0444f * a0 + (double)0.1296f * a2 - (double)1.941e-3f * a3 + (double)7.591e-6f * a4) *
+                     (double)0.1314f;
+        }
+    } else {
+        phi_sn = (1.0 - (double)0.65f * c2) * sol_rad;
+    }
     const double xa = Ta + 273.15;
     double phi_ac;
     if (Ta >= 5.0) {

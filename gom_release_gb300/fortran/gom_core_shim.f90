@@ -230,6 +230,10 @@ module gom_core_abi
      real(c_double) :: sed_temp_coeff
      type(c_ptr) :: air_time
      type(c_ptr) :: air_values
+     integer(c_int32_t) :: year
+     integer(c_int32_t) :: month
+     real(c_double) :: lon
+     real(c_double) :: lat
   end type
 
   type, bind(c) :: gom_mesh
@@ -943,8 +947,12 @@ contains
     bs%sed_temp_coeff = sed_temp_coeff
     bs%air_time = c_null_ptr
     bs%air_values = c_null_ptr
+    bs%year = year
+    bs%month = month
+    bs%lon = lon
+    bs%lat = lat
     gom_device_heat = .false.
-    if (transport_flag == 1 .and. is_temp == 1 .and. heat_option == 1 .and. sol_swr == 2) then
+    if (transport_flag == 1 .and. is_temp == 1 .and. heat_option == 1 .and. (sol_swr == 1 .or. sol_swr == 2)) then
        if (allocated(airt)) deallocate(airt, airv)
        allocate(airt(max(max_air_data_num, 1)), airv(5 * max(max_air_data_num, 1)))
        do j = 1, max_air_data_num

@@ -126,10 +126,12 @@ def from_deck_data(deck, heat: bool = False) -> BoundarySeries:
 
 def _deck_heat(data) -> dict:
     v = data.cards
-    if int(v.get("heat_option", 0)) != 1 or int(v.get("sol_swr", 0)) != 2 or "air" not in data.series:
-        raise ValueError("the deck's heat balance needs heat_option 1, sol_swr 2 and air_ser.inp")
+    if int(v.get("heat_option", 0)) != 1 or int(v.get("sol_swr", 0)) not in (1, 2) or "air" not in data.series:
+        raise ValueError("the deck's heat balance needs heat_option 1, sol_swr 1 or 2 and air_ser.inp")
     ts, vs = data.series["air"]
-    return dict(flag=1, sol_swr=2, fwz_a=v["fwz_a"], fwz_b=v["fwz_b"], fwz_c=v["fwz_c"], wind_height=v["wind_height"],
+    return dict(flag=1, sol_swr=int(v["sol_swr"]), year=int(v["start_year"]), month=int(v["start_month"]),
+                lon=float(v["lon"]), lat=float(v["lat"]),
+                fwz_a=v["fwz_a"], fwz_b=v["fwz_b"], fwz_c=v["fwz_c"], wind_height=v["wind_height"],
                 light_extinction=v["light_extinction"], sol_absorb=v["sol_absorb"],
                 sed_water_exchange=v["sed_water_exchange"], t_sed=v["t_sed"], sed_temp_coeff=v["sed_temp_coeff"],
                 air_time=np.asarray(ts[0], np.float64), air_values=np.stack([np.asarray(x, np.float64) for x in vs]))
@@ -265,7 +267,9 @@ def with_heat_balance(bs: BoundarySeries, *, hours: float = 48.0, seed: int = 0,
     """`bs` with a seeded hourly air series (air temperature 15-30 C, dew point 5-10 C below it,
     wind 0-8 m/s, a diurnal short-wave cycle up to 900 W/m2 under seeded cloud cover) from an hour
     before the run's start, and the heat-balance cards of the Mobile Bay deck (C7_3: 9.2, 0.46, 2.0,
-    2 m; C7_4: 0.45, 0.45, 0.3, 11.5 C) with the given sediment share; ``cards`` overrides them."""
+    2 m; C7_4: 0.45, 0.45, 0.3, 11.5 C) with the given sediment share; for sol_swr 1 the year,
+    month and position of a July run at Mobile Bay (2005, 7, 88 W, 30.5 N); ``cards`` overrides
+    them."""
     from dataclasses import replace
 
     rng = np.random.default_rng(seed)
@@ -280,7 +284,7 @@ def with_heat_balance(bs: BoundarySeries, *, hours: float = 48.0, seed: int = 0,
     sol = np.maximum(0.0, 900.0 * np.sin(np.pi * (hour_of_day - 6.0) / 12.0))
     heat = dict(flag=1, sol_swr=2, fwz_a=9.2, fwz_b=0.46, fwz_c=2.0, wind_height=2.0, light_extinction=0.45,
                 sol_absorb=0.45, sed_water_exchange=0.3, t_sed=11.5, sed_temp_coeff=float(sed_temp_coeff),
-                air_time=t, air_values=np.stack([ta, td, ws, sol, cloud]))
+                air_time=t, air_values=np.stack([ta, td, ws, sol, cloud]), year=2005, month=7, lon=-88.0, lat=30.5)
     heat.update(cards)
     return replace(bs, heat=heat)
 

@@ -484,13 +484,15 @@ typedef struct gom_boundary_series {
     int32_t reserved_hurricane;
     double hurricane_track[6];      /* method 2: hurric_x_1, hurric_y_1, hurricane_time_1,
                                        hurric_x_2, hurric_y_2, hurricane_time_2 (julian days)   */
-    /* heat balance (heat_option 1 with temperature transport, heat_term_by_term.f90 with sol_swr
-     * 2): every step, before the transport, the air series of air_ser.inp interpolated at
-     * julian_day, the short-wave, long-wave, back-radiation, evaporation and conduction terms, and
-     * phi_sz (per wet layer) and phi_sw from the top and bottom temperatures and the layer
-     * thicknesses; with heat_flag 0 phi_sz / phi_sw are left as gom_set_forcing set them */
+    /* heat balance (heat_option 1 with temperature transport, heat_term_by_term.f90): every step,
+     * before the transport, the air series of air_ser.inp interpolated at julian_day, the
+     * short-wave term (sol_swr 1: from the sun's elevation at the local hour of
+     * julian_to_localtime.f90; sol_swr 2: from the series), the long-wave, back-radiation,
+     * evaporation and conduction terms, and phi_sz (per wet layer) and phi_sw from the top and
+     * bottom temperatures and the layer thicknesses; with heat_flag 0 phi_sz / phi_sw are left as
+     * gom_set_forcing set them */
     int32_t heat_flag;              /* 1: form phi_sz and phi_sw on the device                  */
-    int32_t sol_swr;                /* 2: short-wave radiation from the air series              */
+    int32_t sol_swr;                /* 1: from the solar elevation, 2: from the air series      */
     int32_t n_air;                  /* samples of air_ser.inp                                   */
     int32_t reserved_heat;
     double fwz_a, fwz_b, fwz_c, wind_height;                               /* card C7_3 */
@@ -498,6 +500,9 @@ typedef struct gom_boundary_series {
     const double *air_time;         /* (n_air) air_ser_time (s, as read_air_ser.f90 stores it)  */
     const double *air_values;       /* (n_air, 5): T_air, T_dew, air_wind_speed,
                                        solar_radiation, cloud                                   */
+    int32_t year;                   /* sol_swr 1: the driver's year (card C3 start year) and     */
+    int32_t month;                  /* its month variable before the next step                   */
+    double lon, lat;                /* card C1 (degrees)                                         */
 } gom_boundary_series;
 int gom_set_boundary_series(struct gom_ctx *ctx, const gom_boundary_series *series);
 

@@ -139,7 +139,8 @@ struct gom_ctx {
     std::vector<int64_t> search_start;
     std::vector<int32_t> search_nodes;
     // heat balance (heat_term_by_term.f90, sol_swr 2): air series and card values
-    int heat_flag = 0;
+    int heat_flag = 0, sol_swr = 2, year = 2001, month = 1, month_table_set = 0;
+    double lon = 0, lat = 0;
     std::vector<double> air_time, air_values;
     double fwz_a = 0, fwz_b = 0, fwz_c = 0, wind_height = 0, light_extinction = 0, sol_absorb = 0,
            sed_water_exchange = 0, t_sed = 0, sed_temp_coeff = 0;
@@ -1088,7 +1089,8 @@ int gom_set_boundary_series(gom_ctx *c, const gom_boundary_series *bs) {
         return GOM_E_ARG;
     if (bs->heat_flag != 0 && bs->heat_flag != 1) return GOM_E_ARG;
     if (bs->heat_flag == 1) {
-        if (!c->p.transport_flag || !c->p.is_temp || c->p.heat_option != 1 || bs->sol_swr != 2 || bs->n_air < 0 ||
+        if (!c->p.transport_flag || !c->p.is_temp || c->p.heat_option != 1 || (bs->sol_swr != 1 && bs->sol_swr != 2) ||
+            bs->n_air < 0 || (bs->sol_swr == 1 && (bs->month < 1 || bs->month > 12)) ||
             (bs->n_air > 0 && (!bs->air_time || !bs->air_values)))
             return GOM_E_ARG;
         for (int t = 1; t < bs->n_air; ++t)
@@ -1189,6 +1191,12 @@ int gom_set_boundary_series(gom_ctx *c, const gom_boundary_series *bs) {
     c->face_u.assign(c->NF, 0.0);
     c->face_v.assign(c->NF, 0.0);
     c->heat_flag = bs->heat_flag;
+    c->sol_swr = bs->sol_swr;
+    c->year = bs->year;
+    c->month = bs->month;
+    c->month_table_set = 0;
+    c->lon = bs->lon;
+    c->lat = bs->lat;
     c->air_time.clear();
     c->air_values.clear();
     if (bs->heat_flag == 1 && bs->n_air > 0) {
@@ -3405,6 +3413,35 @@ int gom_step_swap(gom_ctx *c) {
 // top and bottom temperatures (the top layer after the layer update, the old thicknesses).  Default-
 // REAL constants widened from single precision; integer powers as products (x^4 = (x^2)^2,
 // x^6 = (x^2 x)^2); exp, log and pow of the C library (the GPU's differ in the last bits)
+// julian_to_localtime.f90:16-86 with its state: the hour of julian day jday.  The month table is
+// saved between calls and set with the month; in a leap year (other than 1900) only while the
+// month variable is 3 or more (so a run starting in January or February keeps a zero table)
+static int local_hour(int year, int &month, int &table_set, double jday) {
+    static const double leap[12] = {0, 32, 60, 91, 121, 152, 182, 213, 244, 274, 305, 335};
+    static const double normal[12] = {0, 31, 59, 90, 120, 151, 181, 212, 243, 273, 304, 334};
+    static const double leap_top[11] = {31, 60, 91, 121, 152, 182, 213, 244, 274, 305, 335};
+    static const double normal_top[11] = {31, 59, 90, 120, 151, 181, 212, 243, 273, 304, 334};
+    double m;
+    if (year % 4 == 0) {
+        if (year != 1900 && month >= 3) {
+            int k = 0;
+            while (k < 11 && jday > leap_top[k]) ++k;
+            month = k + 1;
+            table_set = 1;
+        }
+        m = table_set ? leap[month - 1] : 0.0;
+    } else {
+        int k = 0;
+        while (k < 11 && jday > normal_top[k]) ++k;
+        month = k + 1;
+        table_set = 2;
+        m = normal[month - 1];
+    }
+    const double day_temp = jday - m;
+    const int day = (int)day_temp + 1;
+    return (int)((day_temp + 1 - day) * 24.0);
+}
+
 static void heat_terms(gom_ctx *c) {
     const int L = c->L, NC = c->NC, n = (int)c->air_time.size();
     const double u2 = c->jday * 86400.0;
@@ -3421,7 +3458,31 @@ static void heat_terms(gom_ctx *c) {
     }
     const double Ta = v[0], Tdew = v[1], w_speed = v[2], sol_rad = v[3], cloud = v[4];
     const double c2 = cloud * cloud;
-    const double phi_sn = (1.0 - (double)0.65f * c2) * sol_rad;
+    double phi_sn = 0.0;   // sol_swr 1 with the sun below the horizon: the reference leaves it unset
+    if (c->sol_swr == 1) {
+        // :64-83: the sun's elevation A0 at the local hour, and the clear-sky short-wave from it
+        const int hr = local_hour(c->year, c->month, c->month_table_set, c->jday);
+        const double pi = 3.141592653589793, deg2rad = pi / 180.0, rad2deg = 180.0 / pi;
+        const double j_day = c->jday + 1;
+        const double tau_d = 2.0 * pi * (double)((int)(j_day + 1) - 1) / 365.0;
+        const double sdec = (double)0.006918f - (double)0.399912f * std::cos(tau_d) + (double)0.070257f * std::sin(tau_d) -
+                            (double)0.006758f * std::cos(2.0 * tau_d) + (double)0.000907f * std::sin(2.0 * tau_d) -
+                            (double)0.002697f * std::cos(3.0 * tau_d) + (double)0.001480f * std::sin(3.0 * tau_d);
+        const double eqt = (double)0.170f * std::sin(4.0 * pi * (double)((int)j_day - 80) / 373.0) -
+                           (double)0.129f * std::sin(2.0 * pi * (double)((int)j_day - 8) / 355.0);
+        const double sm = 15.0 * (double)(int)(c->lon / 15.0);
+        const double lha = (double)0.261799f * ((double)hr - (c->lon - sm) * (double)0.0666667f + eqt - 12.0);
+        const double a0 = std::asin(std::sin(c->lat * deg2rad) * std::sin(sdec) +
+                                    std::cos(c->lat * deg2rad) * std::cos(sdec) * std::cos(lha)) * rad2deg;
+        if (a0 > 0.0) {
+            const double a2 = a0 * a0, a3 = a2 * a0, a4 = a2 * a2;
+            phi_sn = (1.0 - (double)0.65f * c2) * 24.0 *
+                     ((double)2.0444f * a0 + (double)0.1296f * a2 - (double)1.941e-3f * a3 + (double)7.591e-6f * a4) *
+                     (double)0.1314f;
+        }
+    } else {
+        phi_sn = (1.0 - (double)0.65f * c2) * sol_rad;
+    }
     const double xa = Ta + 273.15;
     double phi_ac;
     if (Ta >= 5.0) {

@@ -455,7 +455,51 @@ def test_hurricane_method2_equals_host_restatement(oracle_so):
 
 
 # ----------------------------------------------------------------------------- heat balance
-def _heat_host(deck, bs, julian_day, temp, dz, top):
+def _local_hour(year, state, jday):
+    """julian_to_localtime.f90:16-86 with its saved month table (state: [month, table set])."""
+    leap = [0, 32, 60, 91, 121, 152, 182, 213, 244, 274, 305, 335]
+    normal = [0, 31, 59, 90, 120, 151, 181, 212, 243, 273, 304, 334]
+    leap_top = [31, 60, 91, 121, 152, 182, 213, 244, 274, 305, 335]
+    normal_top = [31, 59, 90, 120, 151, 181, 212, 243, 273, 304, 334]
+    if year % 4 == 0:
+        if year != 1900 and state[0] >= 3:
+            state[0] = 1 + sum(1 for t in leap_top if jday > t)
+            state[1] = 1
+        m = float(leap[state[0] - 1]) if state[1] else 0.0
+    else:
+        state[0] = 1 + sum(1 for t in normal_top if jday > t)
+        m = float(normal[state[0] - 1])
+    day_temp = jday - m
+    day = int(day_temp) + 1
+    return int((day_temp + 1 - day) * 24.0)
+
+
+def _solar_short_wave(h, julian_day, c2, f32, state):
+    """heat_term_by_term.f90:64-83 (sol_swr 1): the sun's elevation at the local hour; 0 below the
+    horizon (the reference leaves the term unset there)."""
+    hr = _local_hour(h["year"], state, julian_day)
+    pi = 3.141592653589793
+    deg2rad, rad2deg = pi / 180.0, 180.0 / pi
+    j_day = julian_day + 1
+    tau_d = 2.0 * pi * float(int(j_day + 1) - 1) / 365.0
+    sdec = (f32(0.006918) - f32(0.399912) * math.cos(tau_d) + f32(0.070257) * math.sin(tau_d)
+            - f32(0.006758) * math.cos(2.0 * tau_d) + f32(0.000907) * math.sin(2.0 * tau_d)
+            - f32(0.002697) * math.cos(3.0 * tau_d) + f32(0.001480) * math.sin(3.0 * tau_d))
+    eqt = (f32(0.170) * math.sin(4.0 * pi * float(int(j_day) - 80) / 373.0)
+           - f32(0.129) * math.sin(2.0 * pi * float(int(j_day) - 8) / 355.0))
+    sm = 15.0 * float(int(h["lon"] / 15.0))
+    lha = f32(0.261799) * (float(hr) - (h["lon"] - sm) * f32(0.0666667) + eqt - 12.0)
+    a0 = math.asin(math.sin(h["lat"] * deg2rad) * math.sin(sdec)
+                   + math.cos(h["lat"] * deg2rad) * math.cos(sdec) * math.cos(lha)) * rad2deg
+    if not a0 > 0.0:
+        return 0.0
+    a2 = a0 * a0
+    a3, a4 = a2 * a0, a2 * a2
+    poly = f32(2.0444) * a0 + f32(0.1296) * a2 - f32(1.941e-3) * a3 + f32(7.591e-6) * a4
+    return (1.0 - f32(0.65) * c2) * 24.0 * poly * f32(0.1314)
+
+
+def _heat_host(deck, bs, julian_day, temp, dz, top, state=None):
     """heat_term_by_term.f90:27-156 (sol_swr 2) restated with Python floats and the C library's
     exp / log / pow (as the oracle calls them): (phi_sz (L, NC), phi_sw (NC)) of one step from the
     temperatures and thicknesses at the step's start and the tops after its layer update."""
@@ -472,7 +516,10 @@ def _heat_host(deck, bs, julian_day, temp, dz, top):
             break
     ta, tdew, ws, sol, cloud = v
     c2 = cloud * cloud
-    phi_sn = (1.0 - f32(0.65) * c2) * sol
+    if h["sol_swr"] == 1:
+        phi_sn = _solar_short_wave(h, julian_day, c2, f32, state)
+    else:
+        phi_sn = (1.0 - f32(0.65) * c2) * sol
     xa = ta + 273.15
     if ta >= 5.0:
         x3 = xa * xa * xa
@@ -556,8 +603,9 @@ def test_heat_balance_argument_rules(oracle_so):
         c.set_boundary_series(with_heat_balance(from_synthetic(deck)))
     deck1 = replace(deck, params=replace(deck.params, heat_option=1))
     c1 = GomCore(deck1, lib_path=oracle_so)
-    with pytest.raises(GomError):
-        c1.set_boundary_series(with_heat_balance(from_synthetic(deck1), sol_swr=1))
+    for bad in (dict(sol_swr=3), dict(sol_swr=1, month=13)):
+        with pytest.raises(GomError):
+            c1.set_boundary_series(with_heat_balance(from_synthetic(deck1), **bad))
     c1.set_boundary_series(with_heat_balance(from_synthetic(deck1)))
 
 
@@ -588,3 +636,40 @@ def test_mobile_bay_heat_balance_equals_host_restatement(oracle_so):
         for i in np.nonzero(wet)[0]:
             assert np.array_equal(got[i, bottom[i] - 1:top[i]], sz[i, bottom[i] - 1:top[i]]), (it, i)
     assert float(np.abs(c.get_field("phi_sz")).max()) > 0.0
+
+
+@pytest.mark.parametrize("year,month", [(2005, 7), (2004, 7), (2004, 1)])
+def test_heat_balance_solar_elevation_equals_host_restatement(oracle_so, year, month):
+    """sol_swr 1: the short-wave term from the sun's elevation at the local hour of
+    julian_to_localtime (a common year; a leap year from July, with the leap month table; a leap
+    year from January, whose saved table stays zero) equals the Python restatement bit for bit
+    over the hour of sunrise (the local hour turns from 4 to 5 half-way)."""
+    from gom_release_gb300.series import with_heat_balance
+
+    deck = estuary(nx=10, ny=4, dx=100.0, n_layers=4, trans_sub_iter=1)
+    deck = replace(deck, params=replace(deck.params, heat_option=1))
+    bs = with_heat_balance(replace(from_synthetic(deck), julian_day=190.19), hours=3, seed=2, sol_swr=1,
+                           year=year, month=month)
+    c = GomCore(deck, lib_path=oracle_so)
+    prepare(c, initial_state(deck))
+    c.set_forcing(HostForcing(deck).static())
+    c.set_boundary_series(bs)
+    L, nc = deck.n_layers, deck.n_cells
+    state = [month, 0]
+    jd = bs.julian_day
+    seen_day = seen_night = False
+    for it in range(1, 61):
+        temp = c.get_field("temp_cell").reshape(nc, L).T.copy()
+        dz = c.get_field("dz_cell").reshape(nc, L).T.copy()
+        c.step_all()
+        jd = jd + deck.params.dt / 86400.0
+        top = c.get_field("top_layer_cell")
+        sz, sw = _heat_host(deck, bs, jd, temp, dz, top, state)
+        got = c.get_field("phi_sz").reshape(nc, L)
+        bottom = deck.geo["bottom_layer_at_element"]
+        for i in np.nonzero(top > 0)[0]:
+            assert np.array_equal(got[i, bottom[i] - 1:top[i]], sz[i, bottom[i] - 1:top[i]]), (it, i)
+        sun = _solar_short_wave(bs.heat, jd, 0.0, lambda x: float(np.float32(x)), list(state))
+        seen_day = seen_day or sun > 0.0
+        seen_night = seen_night or sun == 0.0
+    assert seen_day and seen_night

@@ -329,3 +329,33 @@ def test_mobile_bay_heat_balance_equals_oracle(oracle_so, gpu_lib):
     assert gpu.status().code == 0
     for name in ("temp_cell", "salt_cell", "eta_cell"):
         assert _close(gpu.get_field(name), ref.get_field(name)), name
+
+
+def test_heat_balance_solar_elevation_equals_oracle(oracle_so, gpu_lib):
+    """sol_swr 1 on the device: the local hour of julian_to_localtime (integer arithmetic, the same
+    on both) and the sun's elevation through CUDA's sin, cos and asin, across the hour of sunrise:
+    phi_sz / phi_sw within 1e-12 of the oracle's every step."""
+    import dataclasses
+
+    from gom_release_gb300.series import with_heat_balance
+
+    deck = estuary(nx=30, ny=12, dx=100.0, n_layers=8, trans_sub_iter=3)
+    deck = dataclasses.replace(deck, params=dataclasses.replace(deck.params, heat_option=1))
+    bs = with_heat_balance(dataclasses.replace(from_synthetic(deck), julian_day=190.19), hours=3, seed=3,
+                           sol_swr=1, year=2004, month=7)
+    st = initial_state(deck)
+    ref = _ctx(deck, st, lib_path=oracle_so)
+    gpu = _ctx(deck, st, lib=gpu_lib)
+    static = HostForcing(deck).static()
+    for c in (ref, gpu):
+        c.set_forcing(static)
+        c.set_boundary_series(bs)
+    for it in range(1, 61):
+        ref.step_all()
+        gpu.step_all()
+        if it % 5 == 0 or 28 <= it <= 32:
+            for name in ("phi_sz", "phi_sw"):
+                a, b = gpu.get_field(name), ref.get_field(name)
+                scale = max(float(np.abs(b).max()), 1e-30)
+                assert float(np.abs(a - b).max()) <= 1e-12 * scale, (it, name)
+    assert gpu.status().code == 0
